@@ -1,0 +1,141 @@
+"""Seeded synthetic workloads for the UCB likelihood engine.
+
+Every input here is generated from numpy's PCG64 with a fixed seed, so the
+GPU path, the oracle and the CPU baseline all see identical arrays.  The
+shapes and value distributions are the ones the benchmark configurations
+describe:
+
+* ``segment_config0`` -- one A/E segment of NFFT = 1024 bins around a source
+  with f0 ~ U[3.0, 3.5] mHz, fdot = 1e-17, A = 1e-22, N = 128 slow-part
+  samples, plus Gaussian-jump proposals around it;
+* ``segments_config1`` -- 64 independent one-year segments, f0 log-uniform in
+  [0.5, 15] mHz, A log-uniform in [1e-23, 1e-21], 256 chains x 12
+  temperatures, one proposal per (chain, temperature);
+* ``proposals_config2`` -- 16384 proposals, f0 ~ U[1, 5] mHz, A log-uniform.
+
+Noise follows the reference's convention (utils/src/glass_data.c:1323-1403):
+each bin's real and imaginary parts are N(0, C/2) with C the A/E PSD of
+utils/src/glass_lisa.c:1137-1145 at the "scirdv1" levels
+(acceleration 3e-15 m/s^2/rtHz, optical metrology 1.5e-11 m/rtHz).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+T_YEAR = 31457280.0
+CLIGHT = 299792458.0
+LARM = 2.5e9
+PI2 = 6.283185307179586
+FSTAR = CLIGHT / (2.0 * math.pi * LARM)
+
+
+def noise_levels_scirdv1(f):
+    """utils/src/glass_lisa.c:1089-1106: (Spm, Sop) for the "scirdv1" model."""
+    f = np.asarray(f, np.float64)
+    fonc = PI2 * f / CLIGHT
+    sa_a = 9.00e-30 * (1.0 + (0.4e-3 / f) * (0.4e-3 / f)) * (1.0 + (f / 8.0e-3) ** 4)
+    sa_d = sa_a * (PI2 * f) ** -4.0
+    spm = sa_d * fonc * fonc
+    soms_d = 2.25e-22 * (1.0 + (2.0e-3 / f) ** 4.0)
+    return spm, soms_d * fonc * fonc
+
+
+def aenoise_ff(f):
+    """utils/src/glass_lisa.c:1137-1145: A/E noise PSD (fractional frequency)."""
+    f = np.asarray(f, np.float64)
+    spm, sop = noise_levels_scirdv1(f)
+    x = f / FSTAR
+    return 8.0 * np.sin(x) ** 2 * (2.0 * spm * (3.0 + 2.0 * np.cos(x) + np.cos(2.0 * x)) + sop * (2.0 + np.cos(x)))
+
+
+@dataclasses.dataclass
+class SegmentBank:
+    """A set of A/E frequency segments of equal length NFFT.
+
+    dA, dE: (S, NFFT) complex data (or residual); invCA, invCE: (S, NFFT) real;
+    qmin: (S,) first DFT bin of each segment.
+    """
+
+    T: float
+    NFFT: int
+    qmin: np.ndarray
+    dA: np.ndarray
+    dE: np.ndarray
+    invCA: np.ndarray
+    invCE: np.ndarray
+    t0: float = 0.0
+
+    @property
+    def nseg(self) -> int:
+        return len(self.qmin)
+
+    def interleaved(self):
+        """(S, 2*NFFT) float64 arrays in the reference's re/im layout."""
+        def il(z):
+            out = np.empty(z.shape[:-1] + (2 * z.shape[-1],))
+            out[..., 0::2] = z.real
+            out[..., 1::2] = z.imag
+            return out
+
+        return il(self.dA), il(self.dE)
+
+
+def make_params(f0, costh, phi, amp, cosi, psi, phi0, fdot, T=T_YEAR):
+    """The reference's params array (ucb/src/glass_ucb_model.c:40-53)."""
+    return np.array([f0 * T, costh, phi, math.log(amp), cosi, psi, phi0, fdot * T * T], np.float64)
+
+
+def draw_source(rng, f0, amp, fdot=1e-17, T=T_YEAR):
+    return make_params(f0, rng.uniform(-1, 1), rng.uniform(0, 2 * math.pi), amp, rng.uniform(-1, 1),
+                       rng.uniform(0, math.pi), rng.uniform(0, 2 * math.pi), fdot, T)
+
+
+def make_segment(rng, params_list, waveform_fn, NFFT=1024, T=T_YEAR, center_f0=None, noise=True):
+    """One segment centred on the first source, with every source injected.
+
+    ``waveform_fn(params, N) -> (A, E)`` returns 2N-double interleaved arrays for
+    a template of N bins starting at bin floor(f0 T) - N/2 (the layout of
+    ucb_waveform, ucb/src/glass_ucb_waveform.c:738), and ``bandwidth_fn`` is
+    folded into waveform_fn's caller.
+    """
+    f0c = params_list[0][0] / T if center_f0 is None else center_f0
+    qmin = int(f0c * T) - NFFT // 2
+    f = (qmin + np.arange(NFFT)) / T
+    C = aenoise_ff(f)
+    dA = np.zeros(NFFT, np.complex128)
+    dE = np.zeros(NFFT, np.complex128)
+    for p in params_list:
+        N, A, E = waveform_fn(p)
+        q = int(p[0])  # (long)(f0*T)
+        i0 = q - N // 2 - qmin
+        for arr, h in ((dA, A), (dE, E)):
+            hc = h[0::2] + 1j * h[1::2]
+            lo, hi = max(0, i0), min(NFFT, i0 + N)
+            if hi > lo:
+                arr[lo:hi] += hc[lo - i0:hi - i0]
+    if noise:
+        sig = np.sqrt(C / 2.0)
+        dA += sig * rng.standard_normal(NFFT) + 1j * sig * rng.standard_normal(NFFT)
+        dE += sig * rng.standard_normal(NFFT) + 1j * sig * rng.standard_normal(NFFT)
+    return qmin, dA, dE, 1.0 / C, 1.0 / C
+
+
+def jump_scales(params, snr):
+    """Per-parameter Gaussian jump widths of roughly one Fisher sigma for a
+    source of the given SNR (frequency in bins, angles in radians)."""
+    s = 1.0 / max(float(snr), 1.0)
+    return np.array([0.3 * s, 0.5 * s, 0.5 * s, 1.0 * s, 0.5 * s, 0.5 * s, 1.0 * s, 1.0 * s])
+
+
+def gaussian_jumps(rng, params, scales, n):
+    """n proposals params + N(0, scales^2), with the cos-parameters kept in
+    (-1, 1) the way draw_from_fisher does (ucb/src/glass_ucb_proposal.c:382-386)."""
+    jump = rng.standard_normal((n, 8)) * scales
+    out = params[None, :] + jump
+    for k in (1, 4):
+        bad = (out[:, k] >= 1.0) | (out[:, k] <= -1.0)
+        out[bad, k] = params[k] - jump[bad, k]
+    return out

@@ -1,0 +1,193 @@
+"""ctypes front end for the oracle libraries.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the glass_gb300 package.
+
+* ``Port``  wraps oracle/_build/liboracle.so, the CPU restatement of the GLASS
+  UCB path in glass_oracle.c / glass_oracle_wdm.c (builds anywhere).
+* ``Ref``   wraps oracle/_ref/libglassref.so, the reference's own sources
+  compiled with stand-in headers (only where the reference tree exists).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libglassref.so")
+REF_SRC = "/root/reference"
+
+FORMATS = {"sangria": 0, "phase": 1, "frequency": 2}
+NOISE_MODELS = {"scirdv1": 0, "sangria": 1, "radler": 2}
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+
+
+def _p(a):
+    return a.ctypes.data_as(_D)
+
+
+def _pi(a):
+    return a.ctypes.data_as(_I)
+
+
+def build_port() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return PORT_SO
+
+
+def build_ref() -> str | None:
+    if not os.path.isdir(REF_SRC):
+        return None
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, "-f", "Makefile.ref", f"REF={REF_SRC}"], check=True)
+    return REF_SO
+
+
+class Port:
+    def __init__(self, path: str = PORT_SO):
+        if not os.path.exists(path):
+            build_port()
+        self.lib = lib = ctypes.CDLL(path)
+        for name in ("orc_fstar", "orc_aenoise_ff", "orc_aenoise", "orc_fourier_nwip"):
+            getattr(lib, name).restype = ctypes.c_double
+        lib.orc_aenoise_ff.argtypes = [ctypes.c_int, ctypes.c_double]
+        lib.orc_aenoise.argtypes = [ctypes.c_double]
+        lib.orc_ucb_bandwidth.argtypes = [ctypes.c_double] * 5 + [ctypes.c_int]
+        lib.orc_ucb_waveform.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, ctypes.c_int] + [_D] * 5 + [
+            ctypes.c_int, ctypes.c_int]
+        lib.orc_ucb_alignment.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _I]
+        lib.orc_dlogl_term.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                       _D, _D, _D, _D, _D, _D, _D]
+        lib.orc_dlogl_batch.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _I, _D, _D, _D,
+                                        _D, ctypes.c_int, _I, _D, _D, _D, _D, _D, ctypes.c_int]
+        lib.orc_ucb_fisher.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                       _D, _D, _D, _D]
+        lib.orc_orbit_positions.argtypes = [ctypes.c_double, _D]
+        lib.orc_forward_complex_fft.argtypes = [_D, ctypes.c_int]
+        self._wdm_bind()
+
+    # --- Fourier-domain UCB path -------------------------------------------------
+    def fstar(self) -> float:
+        return self.lib.orc_fstar()
+
+    def aenoise_ff(self, f, model="scirdv1"):
+        m = NOISE_MODELS[model]
+        return np.array([self.lib.orc_aenoise_ff(m, float(x)) for x in np.atleast_1d(f)])
+
+    def bandwidth(self, f, fdot, costheta, amp, T, NFFT) -> int:
+        return self.lib.orc_ucb_bandwidth(f, fdot, costheta, amp, T, NFFT)
+
+    def alignment(self, T, NFFT, qmin, params):
+        out = np.zeros(5, np.int32)
+        self.lib.orc_ucb_alignment(T, NFFT, qmin, _p(np.ascontiguousarray(params, np.float64)), _pi(out))
+        return out
+
+    def waveform(self, params, N, T, t0=0.0, fmt="sangria", NI=2, NP=8):
+        params = np.ascontiguousarray(params, np.float64)
+        out = np.zeros((5, 2 * N))
+        rc = self.lib.orc_ucb_waveform(FORMATS[fmt], T, t0, _p(params), NP, *[_p(out[i]) for i in range(5)], N, NI)
+        if rc != 0:
+            raise ValueError("N must be a power of two")
+        return out  # X, Y, Z, A, E
+
+    def dlogl_term(self, params, T, NFFT, qmin, rA, rE, invCA, invCE, t0=0.0, fmt="sangria"):
+        term = np.zeros(1)
+        hh = np.zeros(1)
+        N = self.lib.orc_dlogl_term(FORMATS[fmt], T, t0, NFFT, qmin, _p(rA), _p(rE), _p(invCA), _p(invCE),
+                                    _p(np.ascontiguousarray(params, np.float64)), _p(term), _p(hh))
+        return term[0], hh[0], N
+
+    def dlogl_batch(self, T, NFFT, seg_qmin, rA, rE, invCA, invCE, item_seg, params, term_x=None, t0=0.0,
+                    fmt="sangria", nthreads=0):
+        n = len(item_seg)
+        dl, ty, hh = np.zeros(n), np.zeros(n), np.zeros(n)
+        tx = None if term_x is None else np.ascontiguousarray(term_x, np.float64)
+        self.lib.orc_dlogl_batch(FORMATS[fmt], T, t0, NFFT, _pi(np.ascontiguousarray(seg_qmin, np.int32)),
+                                 _p(rA), _p(rE), _p(invCA), _p(invCE), n,
+                                 _pi(np.ascontiguousarray(item_seg, np.int32)),
+                                 _p(np.ascontiguousarray(params, np.float64)),
+                                 _p(tx) if tx is not None else None, _p(dl), _p(ty), _p(hh), nthreads)
+        return dl, ty, hh
+
+    def max_threads(self) -> int:
+        return self.lib.orc_max_threads()
+
+    def fisher(self, params, T, NFFT, qmin, invCA, invCE, t0=0.0, fmt="sangria"):
+        F = np.zeros(64)
+        self.lib.orc_ucb_fisher(FORMATS[fmt], T, t0, NFFT, qmin, _p(invCA), _p(invCE),
+                                _p(np.ascontiguousarray(params, np.float64)), _p(F))
+        return F.reshape(8, 8)
+
+    def orbit(self, t):
+        out = np.zeros(9)
+        self.lib.orc_orbit_positions(float(t), _p(out))
+        return out.reshape(3, 3)
+
+    def fft(self, z):
+        z = np.ascontiguousarray(z, np.complex128).copy()
+        self.lib.orc_forward_complex_fft(z.ctypes.data_as(_D), len(z))
+        return z
+
+    # --- WDM ------------------------------------------------------------------------
+    def _wdm_bind(self):
+        pass
+
+
+class Ref:
+    """The reference's own functions (oracle/_ref/libglassref.so)."""
+
+    def __init__(self, path: str = REF_SO):
+        if not os.path.exists(path):
+            if build_ref() is None:
+                raise FileNotFoundError("reference sources are not present on this machine")
+        self.lib = lib = ctypes.CDLL(path)
+        for name in ("ref_fstar", "ref_aenoise_ff", "ref_aenoise", "ref_fourier_nwip", "ref_log_likelihood"):
+            getattr(lib, name).restype = ctypes.c_double
+        lib.ref_aenoise_ff.argtypes = [ctypes.c_char_p, ctypes.c_double]
+        lib.ref_aenoise.argtypes = [ctypes.c_double]
+        lib.ref_ucb_bandwidth.argtypes = [ctypes.c_double] * 5 + [ctypes.c_int]
+        lib.ref_ucb_waveform.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, _D, ctypes.c_int] + [
+            _D] * 5 + [ctypes.c_int, ctypes.c_int]
+        lib.ref_ucb_alignment.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _I]
+        lib.ref_log_likelihood.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int, _D, _D, _D, _D, ctypes.c_int, _D, _D]
+        lib.ref_ucb_fisher.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                       _D, _D, _D, _D, _D, _D]
+
+    def fstar(self):
+        return self.lib.ref_fstar()
+
+    def aenoise_ff(self, f, model="scirdv1"):
+        return np.array([self.lib.ref_aenoise_ff(model.encode(), float(x)) for x in np.atleast_1d(f)])
+
+    def bandwidth(self, f, fdot, costheta, amp, T, NFFT):
+        return self.lib.ref_ucb_bandwidth(f, fdot, costheta, amp, T, NFFT)
+
+    def alignment(self, T, NFFT, qmin, params):
+        out = np.zeros(5, np.int32)
+        self.lib.ref_ucb_alignment(T, NFFT, qmin, _p(np.ascontiguousarray(params, np.float64).copy()), _pi(out))
+        return out
+
+    def waveform(self, params, N, T, t0=0.0, fmt="sangria", NI=2, NP=8):
+        params = np.ascontiguousarray(params, np.float64).copy()
+        out = np.zeros((5, 2 * N))
+        self.lib.ref_ucb_waveform(fmt.encode(), T, t0, _p(params), NP, *[_p(out[i]) for i in range(5)], N, NI)
+        return out
+
+    def log_likelihood(self, T, NFFT, qmin, dA, dE, invCA, invCE, params, t0=0.0, fmt="sangria"):
+        params = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        snr = np.zeros(len(params))
+        ll = self.lib.ref_log_likelihood(fmt.encode(), T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), _p(invCE),
+                                         len(params), _p(params), _p(snr))
+        return ll, snr
+
+    def fisher(self, params, T, NFFT, qmin, invCA, invCE, t0=0.0, fmt="sangria"):
+        F, ev, evec = np.zeros(64), np.zeros(8), np.zeros(64)
+        self.lib.ref_ucb_fisher(fmt.encode(), T, t0, NFFT, qmin, _p(invCA), _p(invCE),
+                                _p(np.ascontiguousarray(params, np.float64).copy()), _p(F), _p(ev), _p(evec))
+        return F.reshape(8, 8), ev, evec.reshape(8, 8)

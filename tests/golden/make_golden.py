@@ -1,0 +1,149 @@
+"""Generate the golden vectors in tests/golden/ from the reference itself.
+
+Run on a machine that has the reference sources (they are compiled into
+oracle/_ref/libglassref.so by oracle/Makefile.ref; nothing is copied):
+
+    python tests/golden/make_golden.py
+
+Every output value below comes from the reference's own functions:
+ucb_waveform (ucb/src/glass_ucb_waveform.c:738), ucb_bandwidth (:698),
+ucb_alignment (:727), AEnoise_FF (utils/src/glass_lisa.c:1137),
+generate_ucb_model + gaussian_log_likelihood (ucb/src/glass_ucb_model.c:55,
+utils/src/glass_model.c:726), snr (utils/src/glass_math.c:403) and ucb_fisher
+(ucb/src/glass_ucb_waveform.c:364).  Inputs are seeded numpy draws.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, ROOT)
+
+from oracle import Ref  # noqa: E402
+from glass_gb300 import workloads as wl  # noqa: E402
+
+T = wl.T_YEAR
+
+
+def waveforms(ref, rng):
+    cases = []
+    for fmt in ("sangria", "phase", "frequency"):
+        for N in (32, 64, 128, 256, 512, 1024):
+            f0 = 10 ** rng.uniform(np.log10(0.5e-3), np.log10(15e-3))
+            amp = 10 ** rng.uniform(-23, -21)
+            fdot = 10 ** rng.uniform(-18, -15)
+            cases.append((fmt, N, wl.draw_source(rng, f0, amp, fdot)))
+    cases.append(("sangria", 4096, wl.draw_source(rng, 12e-3, 1e-22, 1e-15)))
+    cases.append(("sangria", 2048, wl.draw_source(rng, 0.7e-3, 1e-22, 1e-18)))
+    # t0 != 0 and NI = 1 variants
+    out = {"fmt": [], "N": [], "NI": [], "t0": [], "params": [], "XYZAE": []}
+    for fmt, N, p in cases:
+        for t0, NI in ((0.0, 2),) + (((1.5e6, 2), (0.0, 1)) if N == 128 else ()):
+            h = ref.waveform(p, N, T, t0=t0, fmt=fmt, NI=NI)
+            out["fmt"].append(fmt)
+            out["N"].append(N)
+            out["NI"].append(NI)
+            out["t0"].append(t0)
+            out["params"].append(p)
+            out["XYZAE"].append(h)
+    np.savez_compressed(os.path.join(HERE, "waveforms.npz"), fmt=np.array(out["fmt"]), N=np.array(out["N"]),
+                        NI=np.array(out["NI"]), t0=np.array(out["t0"]), params=np.array(out["params"]),
+                        **{f"h{i}": h for i, h in enumerate(out["XYZAE"])})
+
+
+def bandwidth(ref, rng):
+    n = 3000
+    f = 10 ** rng.uniform(-4.3, -1.3, n)
+    fdot = 10 ** rng.uniform(-20, -12, n)
+    ct = rng.uniform(-1, 1, n)
+    amp = 10 ** rng.uniform(-24, -19.5, n)
+    nfft = 2 ** rng.integers(5, 15, n)
+    bw = np.array([ref.bandwidth(f[i], fdot[i], ct[i], amp[i], T, int(nfft[i])) for i in range(n)], np.int32)
+    # alignment on a config-1 like grid
+    params = np.array([wl.draw_source(rng, 10 ** rng.uniform(np.log10(0.5e-3), np.log10(15e-3)),
+                                      10 ** rng.uniform(-23, -21)) for _ in range(300)])
+    qmin = np.array([int(p[0]) - 512 + int(rng.integers(-600, 600)) for p in params], np.int32)
+    al = np.array([ref.alignment(T, 1024, int(qmin[i]), params[i]) for i in range(len(params))], np.int32)
+    fgrid = np.geomspace(1e-5, 5e-2, 200)
+    S = ref.aenoise_ff(fgrid, "scirdv1")
+    np.savez_compressed(os.path.join(HERE, "bandwidth.npz"), f=f, fdot=fdot, costh=ct, amp=amp, nfft=nfft, bw=bw,
+                        align_params=params, align_qmin=qmin, align=al, noise_f=fgrid, noise_S=S)
+
+
+def likelihood(ref, rng):
+    """Config-0-like segments: the injected source plus noise, and Gaussian
+    jump proposals; logL of each proposal from the reference."""
+    cases = []
+    for k in range(3):
+        f0 = rng.uniform(3.0e-3, 3.5e-3) if k < 2 else rng.uniform(0.5e-3, 15e-3)
+        amp = 1e-22 if k < 2 else 10 ** rng.uniform(-23, -21)
+        inj = wl.draw_source(rng, f0, amp, 1e-17)
+        extra = []
+        if k == 1:  # a second source near the first one, part of the residual
+            extra = [wl.draw_source(rng, f0 + 40 / T, 5e-23, 1e-17)]
+
+        def wf(p):
+            al = ref.alignment(T, 1024, 0, p)
+            h = ref.waveform(p, int(al[0]), T)
+            return int(al[0]), h[3], h[4]
+
+        qmin, dA, dE, iA, iE = wl.make_segment(rng, [inj] + extra, wf, NFFT=1024, T=T)
+        dA_i = np.empty(2048)
+        dA_i[0::2], dA_i[1::2] = dA.real, dA.imag
+        dE_i = np.empty(2048)
+        dE_i[0::2], dE_i[1::2] = dE.real, dE.imag
+        snr0 = ref.log_likelihood(T, 1024, qmin, dA_i, dE_i, iA, iE, inj)[1][0]
+        props = wl.gaussian_jumps(rng, inj, wl.jump_scales(inj, snr0), 12)
+        props = np.vstack([inj[None], props])
+        logL = []
+        snr = []
+        for p in props:
+            ll, s = ref.log_likelihood(T, 1024, qmin, dA_i, dE_i, iA, iE, np.vstack([p[None]] + [e[None] for e in extra]))
+            logL.append(ll)
+            snr.append(s[0])
+        # model with no sources at all: logL of the bare data
+        ll0, _ = ref.log_likelihood(T, 1024, qmin, dA_i, dE_i, iA, iE, np.zeros((0, 8)))
+        cases.append(dict(qmin=qmin, dA=dA_i, dE=dE_i, invCA=iA, invCE=iE, props=props, logL=np.array(logL),
+                          snr=np.array(snr), logL_empty=ll0,
+                          extra=np.array(extra) if extra else np.zeros((0, 8))))
+    flat = {}
+    for k, c in enumerate(cases):
+        for key, v in c.items():
+            flat[f"c{k}_{key}"] = v
+    np.savez_compressed(os.path.join(HERE, "likelihood.npz"), ncase=len(cases), **flat)
+
+
+def fisher(ref, rng):
+    out = {"params": [], "F": [], "qmin": [], "invC": []}
+    for k in range(4):
+        f0 = rng.uniform(1e-3, 5e-3)
+        p = wl.draw_source(rng, f0, 10 ** rng.uniform(-23, -21), 1e-17)
+        qmin = int(p[0]) - 512
+        invC = 1.0 / wl.aenoise_ff((qmin + np.arange(1024)) / T)
+        F, ev, evec = ref.fisher(p, T, 1024, qmin, invC, invC)
+        out["params"].append(p)
+        out["F"].append(F)
+        out["qmin"].append(qmin)
+        out["invC"].append(invC)
+    np.savez_compressed(os.path.join(HERE, "fisher.npz"), **{k: np.array(v) for k, v in out.items()})
+
+
+def main():
+    ref = Ref()
+    rng = np.random.default_rng(20261203)
+    waveforms(ref, rng)
+    bandwidth(ref, rng)
+    likelihood(ref, rng)
+    fisher(ref, rng)
+    for name in sorted(os.listdir(HERE)):
+        if name.endswith(".npz"):
+            print(name, os.path.getsize(os.path.join(HERE, name)))
+
+
+if __name__ == "__main__":
+    main()

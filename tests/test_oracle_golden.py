@@ -1,0 +1,100 @@
+"""The oracle (oracle/glass_oracle.c) against the reference's own outputs.
+
+The golden vectors were produced by the reference code itself
+(tests/golden/make_golden.py); these tests pin the CPU restatement before it
+is trusted as the checker for the CUDA path.
+"""
+import numpy as np
+import pytest
+
+from glass_gb300 import workloads as wl
+
+T = wl.T_YEAR
+REL = 1e-10
+
+
+def test_waveforms_match_reference(port, golden):
+    g = golden("waveforms.npz")
+    for i in range(len(g["N"])):
+        fmt, N, NI, t0 = str(g["fmt"][i]), int(g["N"][i]), int(g["NI"][i]), float(g["t0"][i])
+        ref = g[f"h{i}"]
+        got = port.waveform(g["params"][i], N, T, t0=t0, fmt=fmt, NI=NI)
+        chans = range(5) if (fmt == "sangria" or NI > 1) else range(1)
+        for c in chans:
+            scale = np.abs(ref[c]).max()
+            assert scale > 0
+            err = np.abs(got[c] - ref[c]).max() / scale
+            assert err < REL, (fmt, N, NI, t0, c, err)
+
+
+def test_bandwidth_rule_is_exact(port, golden):
+    g = golden("bandwidth.npz")
+    got = np.array([port.bandwidth(g["f"][i], g["fdot"][i], g["costh"][i], g["amp"][i], T, int(g["nfft"][i]))
+                    for i in range(len(g["f"]))])
+    np.testing.assert_array_equal(got, g["bw"])
+    al = np.array([port.alignment(T, 1024, int(g["align_qmin"][i]), g["align_params"][i])
+                   for i in range(len(g["align_qmin"]))])
+    np.testing.assert_array_equal(al, g["align"])
+
+
+def test_noise_psd(port, golden):
+    g = golden("bandwidth.npz")
+    np.testing.assert_allclose(port.aenoise_ff(g["noise_f"]), g["noise_S"], rtol=1e-14)
+    # the numpy restatement used to build synthetic segments agrees as well
+    np.testing.assert_allclose(wl.aenoise_ff(g["noise_f"]), g["noise_S"], rtol=1e-13)
+
+
+def _residual(port, case):
+    """data minus the extra (non-proposed) sources of the case."""
+    rA, rE = case["dA"].copy(), case["dE"].copy()
+    for p in case["extra"]:
+        al = port.alignment(T, 1024, int(case["qmin"]), p)
+        N, imin = int(al[0]), int(al[3])
+        h = port.waveform(p, N, T)
+        for i in range(N):
+            j = i + imin
+            if 0 <= j < 1024:
+                rA[2 * j:2 * j + 2] -= h[3][2 * i:2 * i + 2]
+                rE[2 * j:2 * j + 2] -= h[4][2 * i:2 * i + 2]
+    return rA, rE
+
+
+def test_delta_loglikelihood_matches_reference(port, golden):
+    g = golden("likelihood.npz")
+    for k in range(int(g["ncase"])):
+        case = {key[len(f"c{k}_"):]: g[key] for key in g.files if key.startswith(f"c{k}_")}
+        rA, rE = _residual(port, case)
+        terms = [port.dlogl_term(p, T, 1024, int(case["qmin"]), rA, rE, case["invCA"], case["invCE"])
+                 for p in case["props"]]
+        logL = case["logL"]
+        for j in range(1, len(logL)):
+            d_ref = logL[j] - logL[0]
+            d_got = terms[j][0] - terms[0][0]
+            tol = REL * max(1.0, abs(logL[j]))
+            assert abs(d_got - d_ref) < tol, (k, j, d_got, d_ref)
+        if len(case["extra"]) == 0:
+            # term is logL(with source) - logL(empty model)
+            for j in range(len(logL)):
+                assert abs(terms[j][0] - (logL[j] - case["logL_empty"])) < REL * max(1.0, abs(logL[j]))
+
+
+def test_fisher_matches_reference(port, golden):
+    g = golden("fisher.npz")
+    for k in range(len(g["params"])):
+        F = port.fisher(g["params"][k], T, 1024, int(g["qmin"][k]), g["invC"][k], g["invC"][k])
+        ref = g["F"][k]
+        scale = np.abs(np.diag(ref))
+        err = np.abs(F - ref) / np.sqrt(np.outer(scale, scale))
+        assert err.max() < 1e-5, err.max()
+
+
+def test_fft_convention(port):
+    """kiss_fft forward convention: X[k] = sum x[n] exp(-2 pi i k n / N); an
+    impulse transforms to all ones (apps/src/fft_wdm_unit_tests.c:473-490)."""
+    rng = np.random.default_rng(1)
+    for N in (32, 256, 4096):
+        z = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        np.testing.assert_allclose(port.fft(z), np.fft.fft(z), rtol=1e-12, atol=1e-12 * np.abs(z).sum())
+        imp = np.zeros(N, complex)
+        imp[0] = 1
+        np.testing.assert_allclose(port.fft(imp), np.ones(N), atol=1e-14)
