@@ -1,0 +1,412 @@
+"""Benchmark of the UCB delta-logL engine on the batched configuration:
+
+64 independent one-year A/E segments of NFFT = 1024 bins (f0 log-uniform in
+[0.5, 15] mHz, amplitude log-uniform in [1e-23, 1e-21], fdot = 1e-17), and
+256 chains x 12 temperatures proposing one source update each, chain c on
+segment c mod 64.  One step = one sampler step = 3072 proposals, each one
+waveform (N from the reference's bandwidth rule, 32..1024) plus delta logL.
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` is the mixed-precision engine's throughput with
+inputs resident on the GPU (CUDA-event timed, L2 flushed between steps);
+`e2e` is the same metric through the host-pointer C entry point
+(glass_gpu_dlogl_batch_host: copies in and out inside the timed region).
+The plain-FP64 path, the mixed-vs-FP64 error and the roofline of the fused
+kernels are reported beside it.  `--impl reference` times the reference
+algorithm on the host cores instead (the CPU restatement in oracle/, OpenMP
+over proposals as the reference runs one chain per thread).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from glass_gb300 import workloads as wl  # noqa: E402
+
+NSEG, NFFT, NCHAIN, NTEMP = 64, 1024, 256, 12
+T = wl.T_YEAR
+L_ARM = 2.5e9
+METRIC = "UCB dlogL evals/s: batched mixed-prec vs plain FP64 on GB300, |err|<1e-3"
+WORKLOAD = "ucb_dlogl_64seg_nfft1024_256chains_x_12temps"
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def flops_per_eval(N):
+    """Algorithmic work of one Fourier delta-logL eval of size N (FP32 + FP64
+    parts, counted as flops): 48N + 264N + 30 N log2 N + 120N."""
+    return 48.0 * N + 264.0 * N + 30.0 * N * math.log2(N) + 120.0 * N
+
+
+def make_workload(rank, steps):
+    """Segments, injections and (steps) batches of proposals, seeded per rank."""
+    import glass_gb300 as gg
+
+    rng = np.random.default_rng(1 + 1000 * rank)
+    inj, Ns = [], []
+
+    def wf(p):
+        f0 = p[0] / T
+        N = 2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, f0, p[7] / T / T, p[1], math.exp(p[3]), T, NFFT)
+        h = gg.ucb_waveform(p, N, T)
+        return N, h[3], h[4]
+
+    qmin, dA, dE, iA, iE = [], [], [], [], []
+    for s in range(NSEG):
+        f0 = 10 ** rng.uniform(math.log10(0.5e-3), math.log10(15e-3))
+        amp = 10 ** rng.uniform(-23, -21)
+        p = wl.draw_source(rng, f0, amp, 1e-17)
+        q, a, e, ia, ie = wl.make_segment(rng, [p], wf, NFFT=NFFT, T=T)
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie), inj.append(p)
+        Ns.append(wf(p)[0])
+    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                          invCA=np.array(iA), invCE=np.array(iE))
+    inj = np.array(inj)
+    items = NCHAIN * NTEMP
+    item_seg = (np.arange(items) // NTEMP % NSEG).astype(np.int32)
+    temps = 1.5 ** (np.arange(items) % NTEMP)
+    return bank, inj, np.array(Ns), item_seg, temps, rng
+
+
+def draw_batches(rng, inj, snr, item_seg, temps, nbatch):
+    scales = np.array([wl.jump_scales(inj[s], snr[s]) for s in range(len(inj))])
+    out = np.empty((nbatch, len(item_seg), 8))
+    for b in range(nbatch):
+        jump = rng.standard_normal((len(item_seg), 8)) * scales[item_seg] * np.sqrt(temps)[:, None]
+        p = inj[item_seg] + jump
+        for k in (1, 4):
+            bad = (p[:, k] >= 1.0) | (p[:, k] <= -1.0)
+            p[bad, k] = inj[item_seg][bad, k] - jump[bad, k]
+        out[b] = p
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(bank, batches, item_seg, term_x, budget_s=10.0):
+    """The reference algorithm (oracle/ CPU restatement) over all host cores on
+    whole steps of the same workload until the time budget is spent."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Port, build_port
+
+    build_port()
+    port = Port()
+    rA, rE = bank.interleaved()
+    rA, rE = np.ascontiguousarray(rA), np.ascontiguousarray(rE)
+    iA, iE = np.ascontiguousarray(bank.invCA), np.ascontiguousarray(bank.invCE)
+    threads = os.cpu_count() or 1
+    done, t0 = 0, time.perf_counter()
+    b = 0
+    while True:
+        port.dlogl_batch(T, NFFT, bank.qmin, rA, rE, iA, iE, item_seg, batches[b % len(batches)], term_x,
+                         nthreads=threads)
+        done += len(item_seg)
+        b += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s:
+            break
+    return {"value": done / el, "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": f"{b} steps x {len(item_seg)} proposals of the same workload ({el:.1f} s, OpenMP over "
+                      f"proposals, {threads} threads)"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    # the reference arm runs the CPU code only: build the workload with the
+    # oracle's own waveform so that no GPU is touched
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Port, build_port
+
+    build_port()
+    port = Port()
+    rng = np.random.default_rng(1)
+    inj = []
+    qmin, dA, dE, iA, iE = [], [], [], [], []
+
+    def wf(p):
+        al = port.alignment(T, NFFT, 0, p)
+        h = port.waveform(p, int(al[0]), T)
+        return int(al[0]), h[3], h[4]
+
+    for s in range(NSEG):
+        f0 = 10 ** rng.uniform(math.log10(0.5e-3), math.log10(15e-3))
+        amp = 10 ** rng.uniform(-23, -21)
+        p = wl.draw_source(rng, f0, amp, 1e-17)
+        q, a, e, ia, ie = wl.make_segment(rng, [p], wf, NFFT=NFFT, T=T)
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie), inj.append(p)
+    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                          invCA=np.array(iA), invCE=np.array(iE))
+    inj = np.array(inj)
+    rA, rE = bank.interleaved()
+    snr = np.array([math.sqrt(max(port.dlogl_term(inj[s], T, NFFT, int(qmin[s]), rA[s], rE[s], iA[s], iE[s])[1],
+                                  1.0)) for s in range(NSEG)])
+    items = NCHAIN * NTEMP
+    item_seg = (np.arange(items) // NTEMP % NSEG).astype(np.int32)
+    temps = 1.5 ** (np.arange(items) % NTEMP)
+    batches = draw_batches(rng, inj, snr, item_seg, temps, 4)
+    rAc, rEc = np.ascontiguousarray(rA), np.ascontiguousarray(rE)
+    threads = os.cpu_count() or 1
+    for w in range(args.warmup):
+        port.dlogl_batch(T, NFFT, bank.qmin, rAc, rEc, iA, iE, item_seg, batches[w % 4], None, nthreads=threads)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        port.dlogl_batch(T, NFFT, bank.qmin, rAc, rEc, iA, iE, item_seg, batches[k % 4], None, nthreads=threads)
+    el = time.perf_counter() - t0
+    v = args.steps * items / el
+    line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "segments": NSEG, "NFFT": NFFT, "proposals_per_step": items,
+                       "N_range": [32, 1024], "precision": "fp64 (reference algorithm on host cores)"},
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full steps of {items} proposals"},
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import glass_gb300 as gg
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nb = args.warmup + args.steps
+
+    bank, inj, Ns, item_seg, temps, rng = make_workload(rank, nb)
+    eng = gg.Engine(local)
+    eng.upload(bank)
+    # current state of every chain: the injection; its term is the x side of delta logL
+    _, t_inj, hh_inj, st = eng.dlogl_host(np.arange(NSEG, dtype=np.int32), inj, precision=gg.PREC_FP64)
+    snr = np.sqrt(np.maximum(hh_inj, 1.0))
+    batches = draw_batches(rng, inj, snr, item_seg, temps, nb)
+    term_x = t_inj[item_seg]
+    items = len(item_seg)
+
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    d_batches = torch.from_numpy(batches).to(dev)
+    d_seg = torch.from_numpy(item_seg).to(dev)
+    d_tx = torch.from_numpy(term_x).to(dev)
+    d_in = torch.empty((items, 8), dtype=torch.float64, device=dev)
+    outs = {p: (torch.empty(items, dtype=torch.float64, device=dev), torch.empty(items, dtype=torch.float64, device=dev),
+                torch.empty(items, dtype=torch.float64, device=dev), torch.empty(items, dtype=torch.int32, device=dev))
+            for p in (gg.PREC_MIXED, gg.PREC_FP64)}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2
+
+    def step(prec, k):
+        d_in.copy_(d_batches[k], non_blocking=True)
+        dl, ty, hh, stt = outs[prec]
+        eng.dlogl_device(d_seg, d_in, dl, ty, hh, stt, term_x=d_tx, precision=prec)
+
+    # graphs: one per precision over the fixed input buffer
+    graphs = {}
+    with torch.cuda.stream(stream):
+        for prec in (gg.PREC_MIXED, gg.PREC_FP64):
+            step(prec, 0)
+    stream.synchronize()
+    launches_per_step = eng.last_launch_count()
+    for prec in (gg.PREC_MIXED, gg.PREC_FP64):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            dl, ty, hh, stt = outs[prec]
+            eng.dlogl_device(d_seg, d_in, dl, ty, hh, stt, term_x=d_tx, precision=prec)
+        graphs[prec] = g
+
+    def timed(prec, record=None):
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with torch.cuda.stream(stream):
+            for w in range(args.warmup):
+                d_in.copy_(d_batches[w])
+                graphs[prec].replay()
+            stream.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                d_in.copy_(d_batches[args.warmup + k], non_blocking=True)
+                graphs[prec].replay()
+                ev[k][1].record(stream)
+                if record is not None:
+                    record.append(outs[prec][0].clone())
+            stream.synchronize()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return sum(a.elapsed_time(b) for a, b in ev) / 1e3  # seconds of device time
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    rec_mixed, rec_fp64 = [], []
+    t_mixed = timed(gg.PREC_MIXED, rec_mixed)
+    t_fp64 = timed(gg.PREC_FP64, rec_fp64)
+    clk = clocks.stop()
+
+    # end to end through the host-pointer C entry point
+    h_seg = np.ascontiguousarray(item_seg)
+    eng.set_stream(None)
+    for w in range(args.warmup):
+        eng.dlogl_host(h_seg, batches[w], term_x, precision=gg.PREC_MIXED)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        eng.dlogl_host(h_seg, batches[args.warmup + k], term_x, precision=gg.PREC_MIXED)
+    t_e2e = time.perf_counter() - t0
+
+    # max over ranks
+    times = np.array([t_mixed, t_fp64, t_e2e])
+    if world > 1:
+        tt = torch.tensor(times, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        times = tt.cpu().numpy()
+    t_mixed, t_fp64, t_e2e = times
+    total = args.steps * items * world
+    v_mixed, v_fp64, v_e2e = total / t_mixed, total / t_fp64, total / t_e2e
+
+    err = torch.stack(rec_mixed) - torch.stack(rec_fp64)
+    abs_err = err.abs().flatten().cpu().numpy()
+
+    # roofline of the fused kernels (FP32 pipe bound): algorithmic flops per step
+    # from the sizes the bandwidth rule picks, over the measured step time
+    Nitem = np.array([2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, p[0] / T, p[7] / T / T, p[1], math.exp(p[3]), T, NFFT)
+                      for p in batches[args.warmup]])
+    flops_step = float(sum(flops_per_eval(int(n)) for n in Nitem))
+    peak32 = gg.probe_fma_tflops(local, fp64=False)
+    peak64 = gg.probe_fma_tflops(local, fp64=True)
+    ach_mixed = flops_step / (t_mixed / args.steps) / 1e12
+    ach_fp64 = flops_step / (t_fp64 / args.steps) / 1e12
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": v_mixed, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64phase", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "segments": NSEG, "NFFT": NFFT, "proposals_per_step": items,
+                       "N_hist": {str(n): int((Nitem == n).sum()) for n in sorted(set(Nitem.tolist()))},
+                       "precision": "mixed", "l2": "flushed (256 MB write) between timed steps",
+                       "graph": "CUDA graph replay per step"},
+            "fp64": {"value": v_fp64, "unit": "evals/s", "ms_per_step": 1e3 * t_fp64 / args.steps,
+                     "mixed_over_fp64": v_mixed / v_fp64},
+            "accuracy": {"max_abs_dlogl_err_vs_fp64": float(abs_err.max()),
+                         "p99_abs_err": float(np.quantile(abs_err, 0.99)),
+                         "evals_compared": int(abs_err.size)},
+            "e2e": {"value": v_e2e, "unit": "evals/s",
+                    "h2d_bytes_per_step": int(items * (8 * 8 + 4 + 8)),
+                    "d2h_bytes_per_step": int(items * (3 * 8 + 4))},
+            "roofline": {"bound": "fp32", "achieved": ach_mixed, "peak": peak32, "unit": "TFLOP/s",
+                         "frac": ach_mixed / peak32, "traffic": None,
+                         "peak_source": "FP32 FMA probe kernel measured in this run "
+                                        "(MEASURED_PEAKS.json has no CUDA-core FP32 figure)",
+                         "kernels": "plan + per-size fused waveform/delta-logL kernels of one step",
+                         "flops_per_step": flops_step,
+                         "fp64_path": {"achieved": ach_fp64, "peak_fp64": peak64,
+                                       "frac_of_fp64_peak": ach_fp64 / peak64}},
+            "gpu_launches": int(launches_per_step * args.steps * 2 + 0),
+            "clocks": clk,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(bank, batches, item_seg, term_x, budget_s=args.cpu_budget)
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

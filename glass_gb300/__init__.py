@@ -1,0 +1,185 @@
+"""GB300 UCB likelihood engine: Python front end of libglass_gb300.so.
+
+The library is a plain C ABI (include/glass_gb300.h).  This module binds it
+with ctypes and mirrors the reference's call pattern for the UCB likelihood
+path: upload the analysis segments once, then evaluate batches of proposals.
+There is no CPU fallback: if the compiled library is missing, importing the
+engine raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libglass_gb300.so")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+FORMATS = {"sangria": 0, "phase": 1, "frequency": 2}
+
+ITEM_NONFINITE = 1
+ITEM_BAD_SEGMENT = 2
+ITEM_OUTSIDE = 4
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_V = ctypes.c_void_p
+
+# Every symbol include/glass_gb300.h declares.
+EXPORTS = (
+    "ucb_waveform", "glass_ucb_waveform", "ucb_bandwidth",
+    "glass_gpu_create", "glass_gpu_destroy", "glass_gpu_set_stream", "glass_gpu_last_error",
+    "glass_gpu_bank_upload", "glass_gpu_bank_set_residual", "glass_gpu_dlogl_batch",
+    "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_probe_fma_tflops",
+)
+
+_lib = None
+
+
+class GlassError(RuntimeError):
+    pass
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load the compiled engine; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise GlassError(f"{path} is missing: build it with `python -m glass_gb300.build`")
+    lib = ctypes.CDLL(path)
+    lib.glass_gpu_last_error.restype = ctypes.c_char_p
+    lib.glass_gpu_create.argtypes = [ctypes.c_int, ctypes.POINTER(_V)]
+    lib.glass_gpu_destroy.argtypes = [_V]
+    lib.glass_gpu_set_stream.argtypes = [_V, _V]
+    lib.glass_gpu_last_launch_count.argtypes = [_V]
+    lib.glass_gpu_bank_upload.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_int, _I, _D, _D, _D, _D]
+    lib.glass_gpu_bank_set_residual.argtypes = [_V, ctypes.c_int, _D, _D]
+    lib.glass_gpu_dlogl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V, _V, _V, _V]
+    lib.glass_gpu_dlogl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D, _D, _D, _I]
+    lib.glass_ucb_waveform.argtypes = [_D, ctypes.c_char_p, ctypes.c_double, ctypes.c_double, _D, ctypes.c_int,
+                                       _D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_int]
+    lib.ucb_bandwidth.argtypes = [ctypes.c_double] * 7 + [ctypes.c_int]
+    lib.ucb_bandwidth.restype = ctypes.c_int
+    lib.glass_gpu_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _D]
+    _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise GlassError(f"glass_gb300 error {rc}: {_lib.glass_gpu_last_error().decode()}")
+
+
+def _pd(a):
+    return a.ctypes.data_as(_D)
+
+
+def _pi(a):
+    return a.ctypes.data_as(_I)
+
+
+def _ptr(x):
+    """Device address of a tensor-like object (anything with data_ptr()), or None."""
+    if x is None:
+        return None
+    return ctypes.c_void_p(int(x.data_ptr()))
+
+
+def ucb_bandwidth(L, fstar, f, fdot, costheta, amp, T, NFFT) -> int:
+    return load_library().ucb_bandwidth(L, fstar, f, fdot, costheta, amp, T, NFFT)
+
+
+def ucb_waveform(params, N, T, t0=0.0, fmt="sangria", NI=2, NP=8, orbit_xyz=None):
+    """Single template through the drop-in ucb_waveform path.
+
+    Returns a (5, 2N) array X, Y, Z, A, E in the reference layout.  With
+    orbit_xyz (N x 3 x 3 positions in metres) the given orbit is used; otherwise
+    the analytic orbit.
+    """
+    lib = load_library()
+    p = np.ascontiguousarray(params, np.float64)
+    out = np.zeros((5, 2 * N))
+    ox = None if orbit_xyz is None else np.ascontiguousarray(orbit_xyz, np.float64)
+    rc = lib.glass_ucb_waveform(_pd(ox) if ox is not None else None, fmt.encode(), T, t0, _pd(p), NP,
+                                *[_pd(out[i]) for i in range(5)], N, NI)
+    _check(rc)
+    return out
+
+
+def probe_fma_tflops(device: int = 0, fp64: bool = False) -> float:
+    """Measured FMA throughput of the FP32 or FP64 pipe (TFLOP/s)."""
+    out = ctypes.c_double()
+    _check(load_library().glass_gpu_probe_fma_tflops(device, int(fp64), ctypes.byref(out)))
+    return out.value
+
+
+class Engine:
+    """A context on one GPU holding a bank of A/E segments."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        self._ctx = _V()
+        _check(self.lib.glass_gpu_create(device, ctypes.byref(self._ctx)))
+        self.nseg = 0
+        self.NFFT = 0
+
+    def close(self):
+        if self._ctx:
+            self.lib.glass_gpu_destroy(self._ctx)
+            self._ctx = _V()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        _check(self.lib.glass_gpu_set_stream(self._ctx, _V(stream_handle) if stream_handle else None))
+
+    def upload(self, bank, fmt: str = "sangria"):
+        """bank: glass_gb300.workloads.SegmentBank (complex data, real invC)."""
+        rA, rE = bank.interleaved()
+        rA = np.ascontiguousarray(rA, np.float64)
+        rE = np.ascontiguousarray(rE, np.float64)
+        iA = np.ascontiguousarray(bank.invCA, np.float64)
+        iE = np.ascontiguousarray(bank.invCE, np.float64)
+        q = np.ascontiguousarray(bank.qmin, np.int32)
+        _check(self.lib.glass_gpu_bank_upload(self._ctx, FORMATS[fmt], bank.T, bank.t0, bank.NFFT, len(q), _pi(q),
+                                              _pd(rA), _pd(rE), _pd(iA), _pd(iE)))
+        self.nseg, self.NFFT = len(q), bank.NFFT
+
+    def set_residual(self, seg: int, rA, rE):
+        rA = np.ascontiguousarray(rA, np.float64)
+        rE = np.ascontiguousarray(rE, np.float64)
+        _check(self.lib.glass_gpu_bank_set_residual(self._ctx, seg, _pd(rA), _pd(rE)))
+
+    def dlogl_host(self, item_seg, params, term_x=None, precision=PREC_FP64):
+        """Host arrays in, host arrays out: (dlogl, term_y, hh, status)."""
+        seg = np.ascontiguousarray(item_seg, np.int32)
+        p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        n = len(seg)
+        assert p.shape[0] == n
+        tx = None if term_x is None else np.ascontiguousarray(term_x, np.float64)
+        dl, ty, hh = np.empty(n), np.empty(n), np.empty(n)
+        st = np.empty(n, np.int32)
+        _check(self.lib.glass_gpu_dlogl_batch_host(self._ctx, precision, n, _pi(seg), _pd(p),
+                                                   _pd(tx) if tx is not None else None, _pd(dl), _pd(ty), _pd(hh),
+                                                   _pi(st)))
+        return dl, ty, hh, st
+
+    def dlogl_device(self, item_seg, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
+                     precision=PREC_MIXED):
+        """Device tensors (int32 item_seg, float64 params [n,8], float64 outputs);
+        asynchronous on the context's stream."""
+        n = int(item_seg.numel())
+        _check(self.lib.glass_gpu_dlogl_batch(self._ctx, precision, n, _ptr(item_seg), _ptr(params), _ptr(term_x),
+                                              _ptr(dlogl), _ptr(term_y), _ptr(hh), _ptr(status)))
+
+    def last_launch_count(self) -> int:
+        return self.lib.glass_gpu_last_launch_count(self._ctx)

@@ -1,0 +1,504 @@
+// C ABI of the GB300 UCB likelihood engine (include/glass_gb300.h).
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/glass_gb300.h"
+#include "ucb_fd.cuh"
+
+using namespace glass;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_err = "no error";
+
+static int set_err(int code, const char *fmt, const char *arg = "") {
+  char buf[512];
+  snprintf(buf, sizeof(buf), fmt, arg);
+  g_err = buf;
+  return code;
+}
+static int cuda_err(cudaError_t e, const char *where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  g_err = m;
+  return GLASS_ERR_CUDA;
+}
+#define GLASS_CUDA(call, where)                 \
+  do {                                          \
+    cudaError_t e_ = (call);                    \
+    if (e_ != cudaSuccess) return cuda_err(e_, where); \
+  } while (0)
+
+extern "C" const char *glass_gpu_last_error(void) { return g_err.c_str(); }
+
+// ----------------------------------------------------------------- context
+struct glass_gpu_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  FdBankDev bank;
+  void *bank_mem = nullptr;
+  std::vector<int> h_qmin;
+  // host copies needed to rebuild one segment's tables
+  std::vector<double> h_invCA, h_invCE;
+  FdTablesDev tab;
+  bool tab_ready = false;
+  double tab_T = 0, tab_t0 = 0;
+  FdWorkDev work;
+  // staging for the host-pointer entry points
+  void *d_stage = nullptr;
+  size_t d_stage_cap = 0;
+  int last_launches = 0;
+};
+
+static int ctx_activate(glass_gpu_ctx *ctx) {
+  GLASS_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_create(int device, glass_gpu_ctx **out) {
+  if (!out) return set_err(GLASS_ERR_ARG, "glass_gpu_create: null output pointer");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess) return cuda_err(e, "cudaGetDeviceCount");
+  if (device < 0 || device >= ndev) return set_err(GLASS_ERR_ARG, "glass_gpu_create: no such device");
+  glass_gpu_ctx *ctx = new glass_gpu_ctx();
+  ctx->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess) {
+    delete ctx;
+    return cuda_err(e, "cudaSetDevice");
+  }
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if ((e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete ctx;
+    return cuda_err(e, "cudaStreamCreate");
+  }
+  ctx->stream = ctx->own;
+  *out = ctx;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
+  if (!ctx) return GLASS_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->bank_mem);
+  cudaFree(ctx->tab.base);
+  cudaFree(ctx->work.items);
+  cudaFree(ctx->work.bin_count);
+  cudaFree(ctx->work.bin_list);
+  cudaFree(ctx->d_stage);
+  cudaStreamDestroy(ctx->own);
+  delete ctx;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_set_stream(glass_gpu_ctx *ctx, void *stream) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_set_stream: null context");
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_last_launch_count(glass_gpu_ctx *ctx) { return ctx ? ctx->last_launches : 0; }
+
+// -------------------------------------------------------------------- bank
+static int format_code(const char *format) {
+  if (!format) return -1;
+  if (strcmp(format, "sangria") == 0) return GLASS_FMT_SANGRIA;
+  if (strcmp(format, "phase") == 0) return GLASS_FMT_PHASE;
+  if (strcmp(format, "frequency") == 0) return GLASS_FMT_FREQUENCY;
+  return -1;
+}
+
+static double fstar_of_orbit() { return kCLIGHT / (2.0 * M_PI * kLARM); }  // utils/src/glass_lisa.c:129
+
+extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, double t0, int NFFT, int nseg,
+                                     const int *qmin, const double *rA, const double *rE, const double *invCA,
+                                     const double *invCE) {
+  if (!ctx || !qmin || !rA || !rE || !invCA || !invCE) return set_err(GLASS_ERR_ARG, "bank_upload: null argument");
+  if (format < 0 || format > 2) return set_err(GLASS_ERR_FORMAT, "bank_upload: unknown format");
+  if (nseg < 1 || NFFT < kMinN || !(T > 0)) return set_err(GLASS_ERR_ARG, "bank_upload: bad sizes");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t nb = (size_t)nseg * NFFT;
+  std::vector<float4> w32(nb), g32(2 * nb);
+  std::vector<double> Q((size_t)nseg * (NFFT + 1));
+  std::vector<double2> w64(2 * nb), g64(4 * nb);
+  const double fstar = fstar_of_orbit();
+  fd_build_bank_tables(format, T, fstar, NFFT, nseg, qmin, rA, rE, invCA, invCE, w32.data(), g32.data(), Q.data(),
+                       w64.data(), g64.data());
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "bank_upload sync");
+  cudaFree(ctx->bank_mem);
+  ctx->bank_mem = nullptr;
+  size_t off_q = sizeof(int) * ((nseg + 63) / 64 * 64);
+  size_t off_w32 = off_q + sizeof(double) * Q.size();
+  off_w32 = (off_w32 + 255) / 256 * 256;
+  size_t off_g32 = off_w32 + sizeof(float4) * w32.size();
+  size_t off_w64 = off_g32 + sizeof(float4) * g32.size();
+  size_t off_g64 = off_w64 + sizeof(double2) * w64.size();
+  size_t total = off_g64 + sizeof(double2) * g64.size();
+  GLASS_CUDA(cudaMalloc(&ctx->bank_mem, total), "cudaMalloc(bank)");
+  char *base = (char *)ctx->bank_mem;
+  FdBankDev &b = ctx->bank;
+  b.nseg = nseg;
+  b.NFFT = NFFT;
+  b.format = format;
+  b.T = T;
+  b.t0 = t0;
+  b.fstar = fstar;
+  b.qmin = (int *)base;
+  b.Q = (double *)(base + off_q);
+  b.w32 = (float4 *)(base + off_w32);
+  b.g32 = (float4 *)(base + off_g32);
+  b.w64 = (double2 *)(base + off_w64);
+  b.g64 = (double2 *)(base + off_g64);
+  GLASS_CUDA(cudaMemcpy(b.qmin, qmin, sizeof(int) * nseg, cudaMemcpyHostToDevice), "upload qmin");
+  GLASS_CUDA(cudaMemcpy(b.Q, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice), "upload Q");
+  GLASS_CUDA(cudaMemcpy(b.w32, w32.data(), sizeof(float4) * w32.size(), cudaMemcpyHostToDevice), "upload w32");
+  GLASS_CUDA(cudaMemcpy(b.g32, g32.data(), sizeof(float4) * g32.size(), cudaMemcpyHostToDevice), "upload g32");
+  GLASS_CUDA(cudaMemcpy(b.w64, w64.data(), sizeof(double2) * w64.size(), cudaMemcpyHostToDevice), "upload w64");
+  GLASS_CUDA(cudaMemcpy(b.g64, g64.data(), sizeof(double2) * g64.size(), cudaMemcpyHostToDevice), "upload g64");
+  ctx->h_qmin.assign(qmin, qmin + nseg);
+  ctx->h_invCA.assign(invCA, invCA + nb);
+  ctx->h_invCE.assign(invCE, invCE + nb);
+  if (!ctx->tab_ready || ctx->tab_T != T || ctx->tab_t0 != t0) {
+    GLASS_CUDA(fd_build_orbit_tables(ctx->tab, T, t0, ctx->stream), "orbit tables");
+    GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "orbit tables sync");
+    ctx->tab_ready = true;
+    ctx->tab_T = T;
+    ctx->tab_t0 = t0;
+  }
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const double *rA, const double *rE) {
+  if (!ctx || !rA || !rE) return set_err(GLASS_ERR_ARG, "bank_set_residual: null argument");
+  FdBankDev &b = ctx->bank;
+  if (!b.nseg) return set_err(GLASS_ERR_STATE, "bank_set_residual: no bank");
+  if (seg < 0 || seg >= b.nseg) return set_err(GLASS_ERR_ARG, "bank_set_residual: segment out of range");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const int NFFT = b.NFFT;
+  std::vector<float4> w32(NFFT), g32(2 * NFFT);
+  std::vector<double> Q(NFFT + 1);
+  std::vector<double2> w64(2 * NFFT), g64(4 * NFFT);
+  fd_build_bank_tables(b.format, b.T, b.fstar, NFFT, 1, &ctx->h_qmin[seg], rA, rE,
+                       ctx->h_invCA.data() + (size_t)seg * NFFT, ctx->h_invCE.data() + (size_t)seg * NFFT,
+                       w32.data(), g32.data(), Q.data(), w64.data(), g64.data());
+  size_t sj = (size_t)seg * NFFT;
+  GLASS_CUDA(cudaMemcpyAsync(b.w32 + sj, w32.data(), sizeof(float4) * NFFT, cudaMemcpyHostToDevice, ctx->stream),
+             "residual w32");
+  GLASS_CUDA(cudaMemcpyAsync(b.Q + (size_t)seg * (NFFT + 1), Q.data(), sizeof(double) * (NFFT + 1),
+                             cudaMemcpyHostToDevice, ctx->stream), "residual Q");
+  GLASS_CUDA(cudaMemcpyAsync(b.w64 + 2 * sj, w64.data(), sizeof(double2) * 2 * NFFT, cudaMemcpyHostToDevice,
+                             ctx->stream), "residual w64");
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "residual sync");
+  return GLASS_OK;
+}
+
+// --------------------------------------------------------------- batched
+static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
+  FdWorkDev &w = ctx->work;
+  if (nitems <= w.cap) return GLASS_OK;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "work sync");
+  cudaFree(w.items);
+  cudaFree(w.bin_count);
+  cudaFree(w.bin_list);
+  w.items = nullptr;
+  w.bin_count = nullptr;
+  w.bin_list = nullptr;
+  int cap = nitems < 1024 ? 1024 : nitems;
+  GLASS_CUDA(cudaMalloc(&w.items, sizeof(ItemConst) * (size_t)cap), "cudaMalloc(items)");
+  GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * kNumBins), "cudaMalloc(bin_count)");
+  GLASS_CUDA(cudaMalloc(&w.bin_list, sizeof(int) * (size_t)kNumBins * cap), "cudaMalloc(bin_list)");
+  w.cap = cap;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
+                                     const double *params, const double *term_x, double *dlogl, double *term_y,
+                                     double *hh, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "dlogl_batch: null context");
+  if (nitems < 0) return set_err(GLASS_ERR_ARG, "dlogl_batch: negative item count");
+  if (nitems == 0) return GLASS_OK;
+  if (!item_seg || !params || !dlogl) return set_err(GLASS_ERR_ARG, "dlogl_batch: null argument");
+  if (precision != GLASS_PREC_FP64 && precision != GLASS_PREC_MIXED)
+    return set_err(GLASS_ERR_ARG, "dlogl_batch: unknown precision");
+  if (!ctx->bank.nseg) return set_err(GLASS_ERR_STATE, "dlogl_batch: no segment bank uploaded");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_work(ctx, nitems))) return rc;
+  int nl = 0;
+  cudaError_t e = fd_dlogl_launch(ctx->bank, ctx->tab, ctx->work, precision, nitems, item_seg, params, term_x, dlogl,
+                                  term_y, hh, status, ctx->num_sms, ctx->stream, &nl);
+  ctx->last_launches = nl;
+  if (e != cudaSuccess) return cuda_err(e, "dlogl_batch launch");
+  return GLASS_OK;
+}
+
+static int ensure_stage(glass_gpu_ctx *ctx, size_t bytes) {
+  if (bytes <= ctx->d_stage_cap) return GLASS_OK;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "stage sync");
+  cudaFree(ctx->d_stage);
+  ctx->d_stage = nullptr;
+  GLASS_CUDA(cudaMalloc(&ctx->d_stage, bytes), "cudaMalloc(stage)");
+  ctx->d_stage_cap = bytes;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
+                                          const double *params, const double *term_x, double *dlogl,
+                                          double *term_y, double *hh, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "dlogl_batch_host: null context");
+  if (nitems < 0) return set_err(GLASS_ERR_ARG, "dlogl_batch_host: negative item count");
+  if (nitems == 0) return GLASS_OK;
+  if (!item_seg || !params || !dlogl) return set_err(GLASS_ERR_ARG, "dlogl_batch_host: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  // layout: params | term_x | dlogl | term_y | hh (doubles) | item_seg | status (ints)
+  size_t nd = (size_t)nitems;
+  size_t bytes = sizeof(double) * nd * 12 + sizeof(int) * nd * 2 + 256;
+  if ((rc = ensure_stage(ctx, bytes))) return rc;
+  double *d_params = (double *)ctx->d_stage;
+  double *d_tx = d_params + 8 * nd;
+  double *d_dl = d_tx + nd;
+  double *d_ty = d_dl + nd;
+  double *d_hh = d_ty + nd;
+  int *d_seg = (int *)(d_hh + nd);
+  int *d_st = d_seg + nd;
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d_params, params, sizeof(double) * 8 * nd, cudaMemcpyHostToDevice, s), "H2D params");
+  GLASS_CUDA(cudaMemcpyAsync(d_seg, item_seg, sizeof(int) * nd, cudaMemcpyHostToDevice, s), "H2D item_seg");
+  if (term_x) GLASS_CUDA(cudaMemcpyAsync(d_tx, term_x, sizeof(double) * nd, cudaMemcpyHostToDevice, s), "H2D term_x");
+  rc = glass_gpu_dlogl_batch(ctx, precision, nitems, d_seg, d_params, term_x ? d_tx : nullptr, d_dl, d_ty, d_hh, d_st);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(dlogl, d_dl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H dlogl");
+  if (term_y) GLASS_CUDA(cudaMemcpyAsync(term_y, d_ty, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H term_y");
+  if (hh) GLASS_CUDA(cudaMemcpyAsync(hh, d_hh, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H hh");
+  if (status) GLASS_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int) * nd, cudaMemcpyDeviceToHost, s), "D2H status");
+  GLASS_CUDA(cudaStreamSynchronize(s), "dlogl_batch_host sync");
+  return GLASS_OK;
+}
+
+// ------------------------------------------------------- drop-in functions
+// Layout of struct Orbit (utils/src/glass_lisa.h:60-109), restated so the
+// drop-in ucb_waveform can read the arm length, transfer frequency and the
+// orbit function the caller initialised.
+struct OrbitLayout {
+  char OrbitFileName[1024];
+  int Norb;
+  double L, fstar, ecc, R, lambda_0, kappa_0;
+  double *t;
+  double **x, **y, **z;
+  void **dx, **dy, **dz;
+  void (*orbit_function)(struct Orbit *, double, double *, double *, double *);
+};
+
+// Analytic orbits (utils/src/glass_lisa.c:77-124) evaluated on the host for the
+// status-returning entry point when the caller passes no positions.
+static void analytic_positions(double t, double *xyz9) {
+  const double sbs[3] = {0.0, 0.866025403784439, -0.866025403784438};
+  const double cbs[3] = {1.0, -0.5, -0.5};
+  double alpha = kPI2 * t / kYEAR;
+  double sa = sin(alpha), ca = cos(alpha);
+  double R = kAU * (kLARM / (2.0 * kSQ3 * kAU));
+  double sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
+  for (int i = 0; i < 3; i++) {
+    xyz9[3 * i + 0] = kAU * ca + R * (saca * sbs[i] - (1. + sa2) * cbs[i]);
+    xyz9[3 * i + 1] = kAU * sa + R * (saca * cbs[i] - (1. + ca2) * sbs[i]);
+    xyz9[3 * i + 2] = -kSQ3 * R * (ca * cbs[i] + sa * sbs[i]);
+  }
+}
+
+// Per-thread resources of the drop-in entry points: the reference calls them
+// from one OpenMP thread per chain, so each thread gets its own stream and
+// staging buffers.
+struct LegacyThread {
+  bool init = false;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  FdTablesDev tab;  // twiddles only
+  OrbitSample64 *h_pos = nullptr, *d_pos = nullptr;
+  double *h_out = nullptr, *d_out = nullptr, *d_params = nullptr, *h_params = nullptr;
+  ~LegacyThread() {
+    if (!init) return;
+    cudaSetDevice(device);
+    cudaStreamSynchronize(stream);
+    cudaFreeHost(h_pos);
+    cudaFreeHost(h_out);
+    cudaFreeHost(h_params);
+    cudaFree(d_pos);
+    cudaFree(d_out);
+    cudaFree(d_params);
+    cudaFree(tab.base);
+    cudaStreamDestroy(stream);
+  }
+};
+static thread_local LegacyThread g_legacy;
+
+static int legacy_init() {
+  LegacyThread &L = g_legacy;
+  if (L.init) {
+    GLASS_CUDA(cudaSetDevice(L.device), "cudaSetDevice");
+    return GLASS_OK;
+  }
+  const char *dev = getenv("GLASS_GPU_DEVICE");
+  L.device = dev ? atoi(dev) : 0;
+  GLASS_CUDA(cudaSetDevice(L.device), "cudaSetDevice");
+  GLASS_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  GLASS_CUDA(fd_build_orbit_tables(L.tab, 31457280.0, 0.0, L.stream), "twiddle tables");
+  GLASS_CUDA(cudaMallocHost(&L.h_pos, sizeof(OrbitSample64) * kMaxN), "cudaMallocHost");
+  GLASS_CUDA(cudaMallocHost(&L.h_out, sizeof(double) * 10 * kMaxN), "cudaMallocHost");
+  GLASS_CUDA(cudaMallocHost(&L.h_params, sizeof(double) * 16), "cudaMallocHost");
+  GLASS_CUDA(cudaMalloc(&L.d_pos, sizeof(OrbitSample64) * kMaxN), "cudaMalloc");
+  GLASS_CUDA(cudaMalloc(&L.d_out, sizeof(double) * 10 * kMaxN), "cudaMalloc");
+  GLASS_CUDA(cudaMalloc(&L.d_params, sizeof(double) * 16), "cudaMalloc");
+  GLASS_CUDA(cudaStreamSynchronize(L.stream), "init sync");
+  L.init = true;
+  return GLASS_OK;
+}
+
+static int is_pow2_in_range(int n) { return n >= kMinN && n <= kMaxN && (n & (n - 1)) == 0; }
+
+static int bin_index(int N) {
+  int b = 0;
+  while ((32 << b) < N) b++;
+  return b;
+}
+
+// Shared body of the two waveform entry points; positions already in g_legacy.h_pos.
+static int legacy_waveform_run(int fmt, double T, const double *params, int NParams, double *X, double *Y, double *Z,
+                               double *A, double *E, int BW, int NI) {
+  LegacyThread &L = g_legacy;
+  for (int k = 0; k < 8; k++) L.h_params[k] = k < NParams ? params[k] : 0.0;
+  cudaStream_t s = L.stream;
+  GLASS_CUDA(cudaMemcpyAsync(L.d_pos, L.h_pos, sizeof(OrbitSample64) * BW, cudaMemcpyHostToDevice, s), "H2D pos");
+  GLASS_CUDA(cudaMemcpyAsync(L.d_params, L.h_params, sizeof(double) * 8, cudaMemcpyHostToDevice, s), "H2D params");
+  GLASS_CUDA(fd_waveform_launch(L.d_pos, L.d_params, NParams, BW, fmt, NI, T, fstar_of_orbit(), L.d_out,
+                                L.tab.tw64[bin_index(BW)], s),
+             "ucb_waveform launch");
+  bool all = (fmt == GLASS_FMT_SANGRIA) || NI > 1;
+  size_t nout = all ? 10 * (size_t)BW : 2 * (size_t)BW;
+  GLASS_CUDA(cudaMemcpyAsync(L.h_out, L.d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, s), "D2H waveform");
+  GLASS_CUDA(cudaStreamSynchronize(s), "ucb_waveform sync");
+  memcpy(X, L.h_out, sizeof(double) * 2 * BW);
+  if (all) {
+    memcpy(Y, L.h_out + 2 * BW, sizeof(double) * 2 * BW);
+    memcpy(Z, L.h_out + 4 * BW, sizeof(double) * 2 * BW);
+    memcpy(A, L.h_out + 6 * BW, sizeof(double) * 2 * BW);
+    memcpy(E, L.h_out + 8 * BW, sizeof(double) * 2 * BW);
+  }
+  return GLASS_OK;
+}
+
+extern "C" int glass_ucb_waveform(const double *orbit_xyz, const char *format, double T, double t0,
+                                  const double *params, int NParams, double *X, double *Y, double *Z, double *A,
+                                  double *E, int BW, int NI) {
+  int fmt = format_code(format);
+  if (fmt < 0) return set_err(GLASS_ERR_FORMAT, "Unsupported data format %s", format ? format : "(null)");
+  if (!is_pow2_in_range(BW)) return set_err(GLASS_ERR_SIZE, "ucb_waveform: BW must be a power of two in [32, 4096]");
+  if (!params || !X || ((fmt == GLASS_FMT_SANGRIA || NI > 1) && (!Y || !Z || !A || !E)))
+    return set_err(GLASS_ERR_ARG, "ucb_waveform: null argument");
+  if (NParams < 7 || NParams > 8) return set_err(GLASS_ERR_ARG, "ucb_waveform: NParams must be 7 or 8");
+  int rc = legacy_init();
+  if (rc) return rc;
+  LegacyThread &L = g_legacy;
+  for (int n = 0; n < BW; n++) {
+    double t = t0 + T * (double)n / (double)BW;  // ucb/src/glass_ucb_waveform.c:843
+    double xyz[9];
+    if (orbit_xyz) {
+      memcpy(xyz, orbit_xyz + 9 * (size_t)n, sizeof(xyz));
+    } else {
+      analytic_positions(t, xyz);
+    }
+    OrbitSample64 &o = L.h_pos[n];
+    for (int i = 0; i < 3; i++) {
+      o.x[i] = xyz[3 * i];
+      o.y[i] = xyz[3 * i + 1];
+      o.z[i] = xyz[3 * i + 2];
+    }
+    o.t = t;
+  }
+  return legacy_waveform_run(fmt, T, params, NParams, X, Y, Z, A, E, BW, NI);
+}
+
+extern "C" void ucb_waveform(struct Orbit *orbit, char *format, double T, double t0, double *params, int NParams,
+                             double *X, double *Y, double *Z, double *A, double *E, int BW, int NI) {
+  int fmt = format_code(format);
+  if (fmt < 0) {
+    fprintf(stderr, "Unsupported data format %s", format ? format : "(null)");  // ucb/src/glass_ucb_waveform.c:973
+    exit(1);
+  }
+  int rc = GLASS_OK;
+  if (!is_pow2_in_range(BW) || NParams < 7 || NParams > 8) {
+    rc = set_err(GLASS_ERR_SIZE, "ucb_waveform: BW must be a power of two in [32, 4096] and NParams 7 or 8");
+  } else if ((rc = legacy_init()) == GLASS_OK) {
+    const OrbitLayout *o = reinterpret_cast<const OrbitLayout *>(orbit);
+    LegacyThread &L = g_legacy;
+    double x[4], y[4], z[4];
+    for (int n = 0; n < BW; n++) {
+      double t = t0 + T * (double)(n) / (double)BW;
+      o->orbit_function(orbit, t, x, y, z);
+      OrbitSample64 &s = L.h_pos[n];
+      for (int i = 0; i < 3; i++) {
+        s.x[i] = x[i + 1];
+        s.y[i] = y[i + 1];
+        s.z[i] = z[i + 1];
+      }
+      s.t = t;
+    }
+    rc = legacy_waveform_run(fmt, T, params, NParams, X, Y, Z, A, E, BW, NI);
+  }
+  if (rc != GLASS_OK) {
+    fprintf(stderr, "ucb_waveform (GB300): %s\n", g_err.c_str());
+    exit(1);
+  }
+}
+
+// ucb/src/glass_ucb_waveform.c:698-725, with AEnoise of utils/src/glass_lisa.c:1188-1198.
+static double aenoise_host(double L, double fstar, double f) {
+  double fonfstar = f / fstar;
+  double sf = sin(fonfstar);
+  double trans = sf * sf;
+  double r = 1.0e-4 / f;
+  double red = 1. + 16.0 * (pow((2.0e-5 / f), 10.0) + r * r);
+  double w = kPI2 * f;
+  double w4 = w * w * w * w;
+  return (16.0 / 3.0) * trans *
+         ((2.0 + cos(fonfstar)) * (kSPS + kSLOC) +
+          2.0 * (3.0 + 2.0 * cos(fonfstar) + cos(2.0 * fonfstar)) * (kSLOC / 2.0 + kSACC / w4 * red)) /
+         ((2.0 * L) * (2.0 * L));
+}
+
+static int pow2_above_host(double v) {
+  if (!(v >= 1.0)) return 1;
+  int e = ilogb(v) + 1;
+  return e > 30 ? (1 << 30) : (1 << e);
+}
+
+extern "C" int ucb_bandwidth(double L, double fstar, double f, double fdot, double costheta, double A, double T,
+                             int N) {
+  const int Nmin = 16;
+  int half = N / 2;
+  int Nmax = 1;
+  while (Nmax * 2 <= half) Nmax *= 2;
+  if (half < 1) Nmax = 0;
+  double sqT = sqrt(T);
+  double sf = sin(f / fstar);
+  double sn = aenoise_host(L, fstar, f);
+  double sintheta = sin(acos(costheta));
+  double bw = 2 * T * ((4. + kPI2 * f * (kAU / kCLIGHT) * sintheta) / kYEAR + fabs(fdot) * T);
+  int DS = pow2_above_host(bw - 1);
+  if (DS > Nmax) DS = Nmax;
+  if (DS < Nmin) DS = Nmin;
+  double SNRm = A * sqT * sf / sqrt(sn);
+  int SS = pow2_above_host(SNRm - 1);
+  if (SS > Nmax) SS = Nmax;
+  if (SS < Nmin) SS = Nmin;
+  return (DS > SS) ? DS : SS;
+}

@@ -1,0 +1,125 @@
+// Shared device/host definitions of the GB300 UCB likelihood engine.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace glass {
+
+// Physical constants, identical to utils/src/glass_constants.h:31-89 and
+// utils/src/glass_lisa.h:31 (the carrier phase multiplies them by ~1e5, so
+// they must be the same doubles as the reference's).
+constexpr double kSQ3 = 1.73205080757;
+constexpr double kPI2 = 6.283185307179586;
+constexpr double kPI = 3.14159265358979323846;
+constexpr double kCLIGHT = 299792458.;
+constexpr double kYEAR = 3.15581497632e7;
+constexpr double kAU = 1.49597870700e11;
+constexpr double kLARM = 2.5e9;
+constexpr double kSPS = 8.321000e-23;
+constexpr double kSACC = 9.000000e-30;
+constexpr double kSLOC = 2.89e-24;
+constexpr double kINVSQ6 = 0.408248290463863;  // utils/src/glass_lisa.c:435
+constexpr double kSQRT1_2 = 0.70710678118654752440;
+
+// Waveform sizes handled by the batched kernels: N = 32 << b, b in [0, 8).
+constexpr int kNumBins = 8;
+constexpr int kMinN = 32;
+constexpr int kMaxN = 4096;
+
+// ---------------------------------------------------------------- df (double-float)
+// Unevaluated sum hi + lo of two floats, ~48 significant bits.  Error-free
+// transformations after Knuth (two-sum) and Dekker/Ogita-Rump-Oishi (two-product
+// with a fused multiply-add).
+struct df {
+  float hi, lo;
+};
+
+__host__ __device__ inline df df_from_double(double x) {
+  float hi = (float)x;
+  float lo = (float)(x - (double)hi);
+  return {hi, lo};
+}
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ df quick_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return {s, e};
+}
+__device__ __forceinline__ df two_prod(float a, float b) {
+  float p = __fmul_rn(a, b);
+  float e = __fmaf_rn(a, b, -p);
+  return {p, e};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  float lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return quick_two_sum(s.hi, lo);
+}
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df df_mul(df a, df b) {
+  df p = two_prod(a.hi, b.hi);
+  float lo = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
+  return quick_two_sum(p.hi, lo);
+}
+// a (double-float) times an exactly representable float b
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+  df p = two_prod(a.hi, b);
+  float lo = __fmaf_rn(a.lo, b, p.lo);
+  return quick_two_sum(p.hi, lo);
+}
+
+// x reduced to [-pi, pi] and rounded to float.
+__device__ __forceinline__ float df_reduce_2pi(df x) {
+  const float inv2pi = 0.15915494309189535f;
+  const float pi2_hi = 6.28318548202514648f;     // float(2 pi)
+  const float pi2_lo = -1.7484555314695172e-07f;  // 2 pi - float(2 pi)
+  float k = rintf(x.hi * inv2pi);
+  df kp = two_prod(k, pi2_hi);
+  df r = df_add(x, df_neg(kp));
+  return __fsub_rn(__fadd_rn(r.hi, r.lo), k * pi2_lo);
+}
+
+// --------------------------------------------------------- per-item constants
+// Everything a waveform needs that does not depend on the sample index,
+// computed once per proposal (FP64) by the plan kernel.
+struct ItemConst {
+  int seg, N, imin, status;
+  // FP64 copy (plain path)
+  double k[3];
+  double ep[6], ec[6];  // symmetric tensors: xx, xy, xz, yy, yz, zz
+  double DPr, DPi, DCr, DCi;  // amplitude-free polarisation factors
+  double f0, fdot, eps, phi0, amp_s;  // eps = f0*T - q ; amp_s = amp/(2N)
+  // FP32 / double-float copy (mixed path)
+  float kf[3];
+  float epf[6], ecf[6];
+  float DPrf, DPif, DCrf, DCif;
+  float fonfs0;   // f0/f*
+  float fdfs;     // fdot*T/f*   : fonfs_i = fonfs0 + fdfs*(u - tau_i/T)
+  float aef;      // (2/3)*fdot*T/f0 : aevol_i = 1 + aef*(u - tau_i/T)
+  float w0c;      // 2 pi f0 / c
+  float p7pi;     // pi*fdot*T^2
+  float amp_sf;   // amp/(2N)
+  df eps2pi;      // 2 pi eps
+  df beta1, beta2;  // 2 pi f0 AU/c * k_x, k_y
+  df phi0d;
+  df p7pid;       // pi*fdot*T^2
+};
+
+// Per-sample orbit tables, one per waveform size.  Positions of the three
+// spacecraft (FP64, metres) and the sample time; and, for the mixed path,
+// u = t/T and the guiding-centre angle cos/sin(2 pi t / YEAR) as double-floats.
+struct OrbitSample64 {
+  double x[3], y[3], z[3], t;
+};
+struct OrbitSampleMix {
+  float u_hi, u_lo, ca_hi, ca_lo;
+  float sa_hi, sa_lo, pad0, pad1;
+};
+
+}  // namespace glass

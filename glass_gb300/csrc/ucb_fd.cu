@@ -1,0 +1,423 @@
+// Fourier-domain UCB waveform and delta-logL kernels for sm_103a.
+//
+// The reference computes one template at a time on the CPU: ucb_waveform
+// (ucb/src/glass_ucb_waveform.c:738-1001) evaluates the slowly varying part of
+// the response of the six LISA arms at N sample times, takes six N-point FFTs,
+// and synthesises the TDI channels bin by bin (utils/src/glass_lisa.c:645-710);
+// gaussian_log_likelihood (utils/src/glass_model.c:726-774) then sums the
+// noise-weighted residual power over the whole segment.
+//
+// Here one group of threads owns one proposal and does all of it in one pass
+// without leaving the SM:
+//   1. slow part: each thread evaluates R of the N samples;
+//   2. the four arm combinations that the A and E channels need are formed in
+//      the time domain (the TDI sums are linear, so FFT(a - b) replaces
+//      FFT(a) - FFT(b)) and written to shared memory;
+//   3. four N-point radix-4/2 Stockham FFTs in shared memory;
+//   4. every output bin is multiplied by a per-segment-bin table that folds the
+//      TDI transfer factors, A/E combination and noise whitening, and the
+//      residual power over the template support is reduced to one number.
+// Only the template support is visited: logL(r - h) - logL(r) differs from
+// zero only there.
+//
+// Two precisions share the code: plain FP64, and a mixed form in which the
+// carrier phase is carried in double-float arithmetic (the guiding-centre
+// Doppler term reaches ~50 rad and needs ~1e-9 relative accuracy) and
+// everything else is FP32.
+#include "ucb_fd_device.cuh"
+
+namespace glass {
+
+cudaError_t fd_launch_size_mixed(int N, const FdArgs &a, int nitems, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_size_fp64(int N, const FdArgs &a, int nitems, int num_sms, cudaStream_t stream);
+
+// ------------------------------------------------------------- plan kernel
+struct PlanArgs {
+  int nitems, nseg, NFFT, cap;
+  double T, fstar, L;
+  const int *item_seg;
+  const double *params;
+  const double *term_x;
+  const int *seg_qmin;
+  ItemConst *items;
+  int *bin_count, *bin_list;
+  double *dlogl, *term_y, *hh;
+  int *status;
+};
+
+__global__ void fd_plan_kernel(PlanArgs a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.nitems) return;
+  double p[8];
+  bool finite = true;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    p[k] = a.params[8 * (size_t)i + k];
+    finite = finite && isfinite(p[k]);
+  }
+  int seg = a.item_seg[i];
+  int st = 0;
+  if (seg < 0 || seg >= a.nseg) st |= 2;
+  if (!finite || fabs(p[1]) > 1.0 || fabs(p[4]) > 1.0) st |= 1;
+  int N = 0;
+  long long q = 0;
+  if (!st) {
+    double T = a.T;
+    double f0 = p[0] / T;
+    N = 2 * bandwidth_dev(a.L, a.fstar, f0, p[7] / (T * T), p[1], exp(p[3]), T, a.NFFT);
+    q = (long long)(f0 * T);
+    if (N < kMinN || N > kMaxN) st |= 1;
+  }
+  double tx = a.term_x ? a.term_x[i] : 0.0;
+  if (st) {
+    double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    a.dlogl[i] = nan;
+    if (a.term_y) a.term_y[i] = nan;
+    if (a.hh) a.hh[i] = nan;
+    if (a.status) a.status[i] = st;
+    return;
+  }
+  int imin = (int)(q - N / 2) - a.seg_qmin[seg];
+  if (imin >= a.NFFT || imin + N <= 0) {
+    // template support entirely outside the segment: logL is unchanged
+    a.dlogl[i] = 0.0 - tx;
+    if (a.term_y) a.term_y[i] = 0.0;
+    if (a.hh) a.hh[i] = 0.0;
+    if (a.status) a.status[i] = 4;
+    return;
+  }
+  ItemConst c;
+  make_item_const(p, 8, a.T, a.fstar, N, c);
+  c.seg = seg;
+  c.N = N;
+  c.imin = imin;
+  c.status = 0;
+  a.items[i] = c;
+  int b = fd_bin_of(N);
+  int pos = atomicAdd(&a.bin_count[b], 1);
+  a.bin_list[(size_t)b * a.cap + pos] = i;
+}
+
+// ------------------------------------------------------------ orbit tables
+// One thread per (size, sample): analytic orbits of utils/src/glass_lisa.c:77-124
+// at t = t0 + T (n-1)/N (ucb/src/glass_ucb_waveform.c:843), and the FFT
+// twiddles exp(-2 pi i k / N).
+__global__ void fd_orbit_table_kernel(FdTablesDev tab, double T, double t0) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  // sizes 32..4096 laid out back to back: offset of size b is 32 (2^b - 1)
+  int b = 0;
+  while (b < kNumBins && gid >= 32 * ((1 << (b + 1)) - 1)) b++;
+  if (b >= kNumBins) return;
+  int N = 32 << b;
+  int n = gid - 32 * ((1 << b) - 1);
+  double t = t0 + T * (double)n / (double)N;
+  double alpha = kPI2 * t / kYEAR;
+  double sa, ca;
+  sincos(alpha, &sa, &ca);
+  double ecc = kLARM / (2.0 * kSQ3 * kAU);
+  double R = kAU * ecc;
+  double sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca, AUca = kAU * ca, AUsa = kAU * sa;
+  const double sbs[3] = {0.0, 0.866025403784439, -0.866025403784438};
+  const double cbs[3] = {1.0, -0.5, -0.5};
+  OrbitSample64 o;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    double sb = sbs[i], cb = cbs[i];
+    o.x[i] = AUca + R * (saca * sb - (1. + sa2) * cb);
+    o.y[i] = AUsa + R * (saca * cb - (1. + ca2) * sb);
+    o.z[i] = -kSQ3 * R * (ca * cb + sa * sb);
+  }
+  o.t = t;
+  tab.pos64[b][n] = o;
+  OrbitSampleMix m;
+  df u = df_from_double(t / T), cd = df_from_double(ca), sd = df_from_double(sa);
+  m.u_hi = u.hi;
+  m.u_lo = u.lo;
+  m.ca_hi = cd.hi;
+  m.ca_lo = cd.lo;
+  m.sa_hi = sd.hi;
+  m.sa_lo = sd.lo;
+  m.pad0 = m.pad1 = 0.f;
+  tab.mix[b][n] = m;
+  double s, cth;
+  sincospi(-2.0 * (double)n / (double)N, &s, &cth);
+  tab.tw64[b][n] = make_double2(cth, s);
+  tab.tw32[b][n] = make_float2((float)cth, (float)s);
+}
+
+cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStream_t stream) {
+  if (!tab.base) {
+    size_t total = 0;
+    for (int b = 0; b < kNumBins; b++) {
+      int N = 32 << b;
+      total += (size_t)N * (sizeof(OrbitSample64) + sizeof(OrbitSampleMix) + sizeof(float2) + sizeof(double2));
+    }
+    cudaError_t e = cudaMalloc(&tab.base, total);
+    if (e != cudaSuccess) return e;
+    char *p = (char *)tab.base;
+    for (int b = 0; b < kNumBins; b++) {
+      int N = 32 << b;
+      tab.pos64[b] = (OrbitSample64 *)p;
+      p += (size_t)N * sizeof(OrbitSample64);
+      tab.mix[b] = (OrbitSampleMix *)p;
+      p += (size_t)N * sizeof(OrbitSampleMix);
+      tab.tw64[b] = (double2 *)p;
+      p += (size_t)N * sizeof(double2);
+      tab.tw32[b] = (float2 *)p;
+      p += (size_t)N * sizeof(float2);
+    }
+  }
+  int total = 32 * ((1 << kNumBins) - 1);
+  fd_orbit_table_kernel<<<(total + 255) / 256, 256, 0, stream>>>(tab, T, t0);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------- host: bank tables
+void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
+                          const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *g32,
+                          double *Q, double2 *w64, double2 *g64) {
+  const double sqT = sqrt(T);
+  for (int s = 0; s < nseg; s++) {
+    double q = 0.0;
+    Q[(size_t)s * (NFFT + 1)] = 0.0;
+    for (int j = 0; j < NFFT; j++) {
+      size_t sj = (size_t)s * NFFT + j;
+      double f = (double)(qmin[s] + j) / T;
+      double x = f / fstar;
+      double c1 = cos(x), s1 = sin(x);
+      double c2 = 2. * c1 * c1 - 1.0, s2 = 2. * s1 * c1;
+      double c3 = 2. * c1 * c2 - c1, s3 = 2. * s1 * c2 + s1;
+      double pref, w2r, w2i, w1r, w1i;
+      if (format == 0) {  // sangria: utils/src/glass_lisa.c:685-700
+        pref = f * (4.0 / fstar * sqT) * s1;
+        w2r = c2; w2i = -s2;
+        w1r = c1; w1i = -s1;
+      } else {  // phase (:480-530) / frequency (:574-630)
+        pref = (format == 1) ? sqT : sqT * 2. * x;
+        w2r = c3 - c1; w2i = -s3 + s1;
+        w1r = c2 - 1.0; w1i = -s2;
+      }
+      double sA = sqrt(invCA[sj]), sE = sqrt(invCE[sj]);
+      double ka = sA * kSQRT1_2 * pref, ke = sE * kINVSQ6 * pref;
+      double GA2r = ka * w2r, GA2i = ka * w2i, GA1r = ka * w1r, GA1i = ka * w1i;
+      double GE2r = ke * w2r, GE2i = ke * w2i, GE1r = ke * w1r, GE1i = ke * w1i;
+      double conj = (format == 1) ? -1.0 : 1.0;  // "phase" conjugates A and E (:545-546)
+      double wAr = rA[2 * sj] * sA, wAi = conj * rA[2 * sj + 1] * sA;
+      double wEr = rE[2 * sj] * sE, wEi = conj * rE[2 * sj + 1] * sE;
+      w64[2 * sj] = make_double2(wAr, wAi);
+      w64[2 * sj + 1] = make_double2(wEr, wEi);
+      g64[4 * sj + 0] = make_double2(GA2r, GA2i);
+      g64[4 * sj + 1] = make_double2(GA1r, GA1i);
+      g64[4 * sj + 2] = make_double2(GE2r, GE2i);
+      g64[4 * sj + 3] = make_double2(GE1r, GE1i);
+      float4 wf = make_float4((float)wAr, (float)wAi, (float)wEr, (float)wEi);
+      w32[sj] = wf;
+      g32[2 * sj] = make_float4((float)GA2r, (float)GA2i, (float)GA1r, (float)GA1i);
+      g32[2 * sj + 1] = make_float4((float)GE2r, (float)GE2i, (float)GE1r, (float)GE1i);
+      q += (double)wf.x * wf.x + (double)wf.y * wf.y + (double)wf.z * wf.z + (double)wf.w * wf.w;
+      Q[(size_t)s * (NFFT + 1) + j + 1] = q;
+    }
+  }
+}
+
+// --------------------------------------------------------------- launchers
+cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int precision,
+                            int nitems, const int *item_seg, const double *params, const double *term_x,
+                            double *dlogl, double *term_y, double *hh, int *status, int num_sms,
+                            cudaStream_t stream, int *nlaunch) {
+  cudaError_t e;
+  int launches = 0;
+  e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kNumBins, stream);
+  if (e != cudaSuccess) return e;
+  PlanArgs pa;
+  pa.nitems = nitems;
+  pa.nseg = bank.nseg;
+  pa.NFFT = bank.NFFT;
+  pa.cap = work.cap;
+  pa.T = bank.T;
+  pa.fstar = bank.fstar;
+  pa.L = kLARM;
+  pa.item_seg = item_seg;
+  pa.params = params;
+  pa.term_x = term_x;
+  pa.seg_qmin = bank.qmin;
+  pa.items = work.items;
+  pa.bin_count = work.bin_count;
+  pa.bin_list = work.bin_list;
+  pa.dlogl = dlogl;
+  pa.term_y = term_y;
+  pa.hh = hh;
+  pa.status = status;
+  fd_plan_kernel<<<(nitems + 127) / 128, 128, 0, stream>>>(pa);
+  launches++;
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+
+  FdArgs a;
+  a.NFFT = bank.NFFT;
+  a.T = bank.T;
+  a.fstar = bank.fstar;
+  a.L = kLARM;
+  a.R = kAU * (kLARM / (2.0 * kSQ3 * kAU));
+  a.items = work.items;
+  a.bin_count = work.bin_count;
+  a.w32 = bank.w32;
+  a.g32 = bank.g32;
+  a.Q = bank.Q;
+  a.w64 = bank.w64;
+  a.g64 = bank.g64;
+  a.term_x = term_x;
+  a.dlogl = dlogl;
+  a.term_y = term_y;
+  a.hh = hh;
+  a.status = status;
+  const bool mix = precision == 1;
+  // every size a segment of NFFT bins can produce: 32 .. NFFT (ucb_bandwidth caps N at NFFT)
+  for (int b = 0; b < kNumBins; b++) {
+    int N = 32 << b;
+    if (N > bank.NFFT) break;
+    a.bin = b;
+    a.bin_list = work.bin_list + (size_t)b * work.cap;
+    a.pos64 = tab.pos64[b];
+    a.mix = tab.mix[b];
+    a.tw = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
+    e = mix ? fd_launch_size_mixed(N, a, nitems, num_sms, stream) : fd_launch_size_fp64(N, a, nitems, num_sms, stream);
+    launches++;
+    if (e != cudaSuccess) return e;
+  }
+  if (nlaunch) *nlaunch = launches;
+  return cudaSuccess;
+}
+
+// ------------------------------------------------------- legacy single waveform
+// One CTA per Michelson channel (X, Y, Z): slow part, the two FFTs the channel
+// needs, and the format's TDI weights per bin.  A and E follow in
+// fd_ae_kernel from the stored X, Y, Z (utils/src/glass_lisa.c:429-441).
+template <int N>
+__global__ void __launch_bounds__(FdCfg<N>::GT) fd_waveform_kernel(const OrbitSample64 *pos, const double *params,
+                                                                    int NP, int format, double T, double fstar,
+                                                                    double L, double *out, const double2 *twg) {
+  constexpr int GT = FdCfg<N>::GT, R = FdCfg<N>::R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *tw = reinterpret_cast<double2 *>(smem_raw);
+  double2 *buf = tw + N;
+  __shared__ ItemConst c;
+  const int lane = threadIdx.x, ch = blockIdx.x;
+  for (int i = lane; i < N; i += GT) tw[i] = twg[i];
+  if (lane == 0) {
+    double p[8];
+    for (int k = 0; k < 8; k++) p[k] = k < NP ? params[k] : 0.0;
+    make_item_const(p, NP, T, fstar, N, c);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int n = lane + GT * r;
+    double2 d[6];
+    slow_sample64(c, pos[n], T, fstar, L, d);
+    // d: 12, 13, 21, 23, 31, 32 ; X: (12-13, 21-31), Y: (23-21, 32-12), Z: (31-32, 13-23)
+    double2 u, v;
+    if (ch == 0) {
+      u = csub(d[0], d[1]);
+      v = csub(d[2], d[4]);
+    } else if (ch == 1) {
+      u = csub(d[3], d[2]);
+      v = csub(d[5], d[0]);
+    } else {
+      u = csub(d[4], d[5]);
+      v = csub(d[1], d[3]);
+    }
+    buf[n] = u;
+    buf[N + n] = v;
+  }
+  __syncthreads();
+  group_fft<N, GT, 2, 1, double2, 64>(buf, tw, lane);  // CTA barrier: the CTA may be a partial warp
+  const double sqT = sqrt(T);
+  const long long q = (long long)(c.f0 * T);
+  double *X = out + (size_t)ch * 2 * N;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int k = lane + GT * r;
+    const int m = (k + N / 2) & (N - 1);
+    double f = (double)(q + m - N / 2) / T;
+    double x = f / fstar;
+    double s1, c1;
+    sincos(x, &s1, &c1);
+    double c2 = 2. * c1 * c1 - 1.0, s2 = 2. * s1 * c1;
+    double2 W2, W1;
+    double pref;
+    if (format == 0) {
+      pref = f * (4.0 / fstar * sqT) * s1;
+      W2 = make_double2(c2, -s2);
+      W1 = make_double2(c1, -s1);
+    } else {
+      double c3 = 2. * c1 * c2 - c1, s3 = 2. * s1 * c2 + s1;
+      pref = (format == 1) ? sqT : sqT * 2. * x;
+      W2 = make_double2(c3 - c1, -s3 + s1);
+      W1 = make_double2(c2 - 1.0, -s2);
+    }
+    double2 h = cadd(cmul(buf[k], W2), cmul(buf[N + k], W1));
+    double sc = c.amp_s * pref;
+    X[2 * m] = h.x * sc;
+    X[2 * m + 1] = h.y * sc;
+  }
+}
+
+__global__ void fd_ae_kernel(double *out, int N, int format) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= 2 * N) return;
+  const double *X = out, *Y = out + 2 * N, *Z = out + 4 * N;
+  double *A = out + 6 * N, *E = out + 8 * N;
+  double a = (Z[m] - X[m]) * kSQRT1_2;
+  double e = (X[m] - 2 * Y[m] + Z[m]) * kINVSQ6;
+  if (format == 1 && (m & 1)) {
+    a = -a;
+    e = -e;
+  }
+  A[m] = a;
+  E[m] = e;
+}
+
+template <int N>
+static cudaError_t launch_waveform(const OrbitSample64 *pos, const double *params, int NP, int format, int nch,
+                                   double T, double fstar, double *out, const double2 *tw, cudaStream_t stream) {
+  size_t smem = sizeof(double2) * 3 * N;
+  static bool init = false;
+  if (!init) {
+    cudaError_t e = cudaFuncSetAttribute(fd_waveform_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    init = true;
+  }
+  fd_waveform_kernel<N><<<nch, FdCfg<N>::GT, smem, stream>>>(pos, params, NP, format, T, fstar, kLARM, out, tw);
+  return cudaGetLastError();
+}
+
+cudaError_t fd_waveform_launch(const OrbitSample64 *pos, const double *params_dev, int NP, int N, int format,
+                                  int NI, double T, double fstar, double *out, const double2 *tw,
+                                  cudaStream_t stream) {
+  int nch = (format != 0 && NI <= 1) ? 1 : 3;
+  cudaError_t e = cudaErrorInvalidValue;
+  switch (N) {
+#define GLASS_WCASE(NN) \
+  case NN:              \
+    e = launch_waveform<NN>(pos, params_dev, NP, format, nch, T, fstar, out, tw, stream); \
+    break;
+    GLASS_WCASE(32)
+    GLASS_WCASE(64)
+    GLASS_WCASE(128)
+    GLASS_WCASE(256)
+    GLASS_WCASE(512)
+    GLASS_WCASE(1024)
+    GLASS_WCASE(2048)
+    GLASS_WCASE(4096)
+#undef GLASS_WCASE
+  }
+  if (e != cudaSuccess) return e;
+  if (nch == 3) {
+    fd_ae_kernel<<<(2 * N + 127) / 128, 128, 0, stream>>>(out, N, format);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+}  // namespace glass

@@ -1,0 +1,59 @@
+// Internal host-side interface of the Fourier-domain UCB kernels (ucb_fd.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "glass_common.cuh"
+
+namespace glass {
+
+// Device-resident inputs shared by every evaluation of a segment bank.
+struct FdBankDev {
+  int nseg = 0, NFFT = 0, format = 0;
+  double T = 0, t0 = 0, fstar = 0;
+  int *qmin = nullptr;         // [nseg]
+  float4 *w32 = nullptr;       // [nseg*NFFT]   whitened residual {A.re, A.im, E.re, E.im}
+  float4 *g32 = nullptr;       // [nseg*NFFT*2] {GA2, GA1}, {GE2, GE1}
+  double *Q = nullptr;         // [nseg*(NFFT+1)] prefix sums of |w32|^2 over both channels
+  double2 *w64 = nullptr;      // [nseg*NFFT*2] {A}, {E}
+  double2 *g64 = nullptr;      // [nseg*NFFT*4] GA2, GA1, GE2, GE1
+};
+
+// Per-size tables (orbit samples and FFT twiddles) for the bank's (T, t0).
+struct FdTablesDev {
+  OrbitSample64 *pos64[kNumBins] = {};
+  OrbitSampleMix *mix[kNumBins] = {};
+  float2 *tw32[kNumBins] = {};
+  double2 *tw64[kNumBins] = {};
+  void *base = nullptr;  // single allocation backing all of the above
+};
+
+// Scratch of one batched evaluation.
+struct FdWorkDev {
+  int cap = 0;
+  ItemConst *items = nullptr;  // [cap]
+  int *bin_count = nullptr;    // [kNumBins]
+  int *bin_list = nullptr;     // [kNumBins*cap]
+};
+
+// Host-side table construction for a bank: G and w tables, prefix sums.
+void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
+                          const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *g32,
+                          double *Q, double2 *w64, double2 *g64);
+
+cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStream_t stream);
+
+// Enqueue plan + per-size kernels.  Returns the number of kernel launches
+// through *nlaunch.
+cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int precision,
+                            int nitems, const int *item_seg, const double *params, const double *term_x,
+                            double *dlogl, double *term_y, double *hh, int *status, int num_sms,
+                            cudaStream_t stream, int *nlaunch);
+
+// Single waveform in the reference's output layout (legacy ucb_waveform).
+// pos: N orbit samples (device), out: 10*N doubles (device) = X,Y,Z,A,E.
+// tw: the N-point FP64 twiddle table (FdTablesDev::tw64 of the size).
+cudaError_t fd_waveform_launch(const OrbitSample64 *pos, const double *params_dev, int NP, int N, int format, int NI,
+                               double T, double fstar, double *out, const double2 *tw, cudaStream_t stream);
+
+
+}  // namespace glass

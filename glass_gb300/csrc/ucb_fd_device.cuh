@@ -1,0 +1,574 @@
+// Device building blocks of the Fourier-domain UCB kernels (included by the
+// ucb_fd*.cu translation units).
+#pragma once
+#include <math.h>
+#include <stdio.h>
+
+#include <type_traits>
+
+#include "ucb_fd.cuh"
+
+namespace glass {
+
+
+template <int N>
+struct FdCfg {
+  static constexpr int R = (N <= 128) ? 4 : 8;  // samples (and bins) per thread
+  static constexpr int GT = N / R;              // threads per proposal
+  static constexpr int CTA = (GT >= 64) ? GT : 128;
+  static constexpr int GPC = CTA / GT;          // proposals per CTA
+  static constexpr int LOG = (N == 32) ? 5 : (N == 64) ? 6 : (N == 128) ? 7 : (N == 256) ? 8
+                           : (N == 512) ? 9 : (N == 1024) ? 10 : (N == 2048) ? 11 : 12;
+};
+
+__host__ __device__ constexpr int fd_bin_of(int N) {
+  return N == 32 ? 0 : N == 64 ? 1 : N == 128 ? 2 : N == 256 ? 3 : N == 512 ? 4 : N == 1024 ? 5 : N == 2048 ? 6 : 7;
+}
+
+// --------------------------------------------------------------- complex helpers
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// multiply by -i
+__device__ __forceinline__ float2 cmi(float2 a) { return make_float2(a.y, -a.x); }
+__device__ __forceinline__ double2 cmi(double2 a) { return make_double2(a.y, -a.x); }
+template <typename C>
+__device__ __forceinline__ C cscale(C a, decltype(a.x) s) {
+  C r;
+  r.x = a.x * s;
+  r.y = a.y * s;
+  return r;
+}
+
+// ------------------------------------------------------------- group barrier
+// Groups of at most 32 threads live inside full warps of a larger CTA and
+// synchronise with __syncwarp; larger groups are the whole CTA.
+template <int GT>
+__device__ __forceinline__ void group_sync() {
+  if constexpr (GT <= 32) {
+    __syncwarp();
+  } else {
+    __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------------------- FFT
+// In-place forward DFT (exp(-2 pi i k n / N), unnormalised) of NSER series of
+// length N held series-major in shared memory, by a group of GT threads.
+// Radix-4 Stockham stages (plus one radix-2 stage when log2 N is odd): stage
+// with sub-transform size p reads x[i + m N/R], applies exp(-2 pi i m k/(pR)),
+// k = i mod p, and writes y[(i-k)R + k + m p].  Every thread holds its
+// butterflies' inputs in registers between the two barriers of a stage, which
+// lets the stage overwrite its own input.  CH series are processed per round to
+// bound register use.
+template <int N, int GT, int NSER, int CH, typename C, int SYNC_GT = GT>
+__device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
+  constexpr int LOG = FdCfg<N>::LOG;
+  constexpr int NR4 = LOG / 2;
+  constexpr int B4 = N / 4 / GT;
+  static_assert(B4 >= 1, "group too large for radix-4 stages");
+  int p = 1;
+#pragma unroll
+  for (int st = 0; st < NR4; ++st) {
+    const int step = N / (4 * p);
+#pragma unroll
+    for (int c0 = 0; c0 < NSER; c0 += CH) {
+      C v[CH][B4][4];
+#pragma unroll
+      for (int s = 0; s < CH; ++s)
+#pragma unroll
+        for (int b = 0; b < B4; ++b) {
+          int i = lane + GT * b;
+#pragma unroll
+          for (int m = 0; m < 4; ++m) v[s][b][m] = buf[(c0 + s) * N + i + m * (N / 4)];
+        }
+      group_sync<SYNC_GT>();
+#pragma unroll
+      for (int s = 0; s < CH; ++s)
+#pragma unroll
+        for (int b = 0; b < B4; ++b) {
+          int i = lane + GT * b;
+          int k = i & (p - 1);
+          C u0 = v[s][b][0];
+          C u1 = cmul(v[s][b][1], tw[k * step]);
+          C u2 = cmul(v[s][b][2], tw[2 * k * step]);
+          C u3 = cmul(v[s][b][3], tw[3 * k * step]);
+          C a = cadd(u0, u2), bb = csub(u0, u2), c = cadd(u1, u3), d = cmi(csub(u1, u3));
+          int j = (i - k) * 4 + k;
+          C *o = buf + (c0 + s) * N + j;
+          o[0] = cadd(a, c);
+          o[p] = cadd(bb, d);
+          o[2 * p] = csub(a, c);
+          o[3 * p] = csub(bb, d);
+        }
+      group_sync<SYNC_GT>();
+    }
+    p *= 4;
+  }
+  if constexpr (LOG & 1) {
+    constexpr int B2 = N / 2 / GT;
+    const int step = N / (2 * p);
+#pragma unroll
+    for (int c0 = 0; c0 < NSER; c0 += CH) {
+      C v[CH][B2][2];
+#pragma unroll
+      for (int s = 0; s < CH; ++s)
+#pragma unroll
+        for (int b = 0; b < B2; ++b) {
+          int i = lane + GT * b;
+          v[s][b][0] = buf[(c0 + s) * N + i];
+          v[s][b][1] = buf[(c0 + s) * N + i + N / 2];
+        }
+      group_sync<SYNC_GT>();
+#pragma unroll
+      for (int s = 0; s < CH; ++s)
+#pragma unroll
+        for (int b = 0; b < B2; ++b) {
+          int i = lane + GT * b;
+          int k = i & (p - 1);
+          C u1 = cmul(v[s][b][1], tw[k * step]);
+          int j = (i - k) * 2 + k;
+          buf[(c0 + s) * N + j] = cadd(v[s][b][0], u1);
+          buf[(c0 + s) * N + j + p] = csub(v[s][b][0], u1);
+        }
+      group_sync<SYNC_GT>();
+    }
+  }
+}
+
+// ------------------------------------------------------- per-proposal constants
+// utils/src/glass_lisa.c:1188-1198 (AEnoise) with rednoise (:1183).
+__device__ double aenoise_dev(double f, double L, double fstar) {
+  double fonfstar = f / fstar;
+  double sf = sin(fonfstar);
+  double trans = sf * sf;
+  double r = 1.0e-4 / f;
+  double red = 1. + 16.0 * (pow((2.0e-5 / f), 10.0) + r * r);
+  double w = kPI2 * f;
+  double w4 = w * w * w * w;
+  return (16.0 / 3.0) * trans *
+         ((2.0 + cos(fonfstar)) * (kSPS + kSLOC) +
+          2.0 * (3.0 + 2.0 * cos(fonfstar) + cos(2.0 * fonfstar)) * (kSLOC / 2.0 + kSACC / w4 * red)) /
+         ((2.0 * L) * (2.0 * L));
+}
+
+// (int)pow(2, (int)log2(v) + 1) of ucb/src/glass_ucb_waveform.c:712,719.  Every
+// v < 8 ends below the clamp Nmin = 16, so only v >= 1 needs the exact form,
+// where (int)log2(v) is the binary exponent of v.
+__device__ __forceinline__ int pow2_above_dev(double v) {
+  if (!(v >= 1.0)) return 1;
+  int e = ilogb(v) + 1;
+  return e > 30 ? (1 << 30) : (1 << e);
+}
+
+// ucb/src/glass_ucb_waveform.c:698-725 (ucb_bandwidth).
+__device__ int bandwidth_dev(double L, double fstar, double f, double fdot, double costheta, double A, double T,
+                             int NFFT) {
+  const int Nmin = 16;
+  int half = NFFT / 2;
+  int Nmax = half >= 1 ? (1 << (31 - __clz(half))) : 0;
+  double sqT = sqrt(T);
+  double sf = sin(f / fstar);
+  double sn = aenoise_dev(f, L, fstar);
+  double sintheta = sin(acos(costheta));
+  double bw = 2 * T * ((4. + kPI2 * f * (kAU / kCLIGHT) * sintheta) / kYEAR + fabs(fdot) * T);
+  int DS = pow2_above_dev(bw - 1);
+  if (DS > Nmax) DS = Nmax;
+  if (DS < Nmin) DS = Nmin;
+  double SNRm = A * sqT * sf / sqrt(sn);  // analytic_snr, ucb/src/glass_ucb_waveform.c:22-25
+  int SS = pow2_above_dev(SNRm - 1);
+  if (SS > Nmax) SS = Nmax;
+  if (SS < Nmin) SS = Nmin;
+  return (DS > SS) ? DS : SS;
+}
+
+// Per-proposal constants (ucb/src/glass_ucb_waveform.c:802-838 and
+// utils/src/glass_lisa.c:1566-1596), amplitude factored out as amp/(2N).
+__device__ void make_item_const(const double *p, int NP, double T, double fstar, int N, ItemConst &c) {
+  double f0 = p[0] / T, costh = p[1], phi = p[2], amp = exp(p[3]), cosi = p[4], psi = p[5], phi0 = p[6];
+  double fdot = NP > 7 ? p[7] / (T * T) : 0.0;
+  double fT = f0 * T;
+  long long q = (long long)fT;
+  c.eps = fT - (double)q;
+  double sinps, cosps;
+  sincos(2. * psi, &sinps, &cosps);
+  double Aplus = (1. + cosi * cosi) * 0.5, Across = -cosi;
+  c.DPr = Aplus * cosps;
+  c.DPi = -Across * sinps;
+  c.DCr = -Aplus * sinps;
+  c.DCi = -Across * cosps;
+  double sinth = sqrt(1.0 - costh * costh);
+  double sinph, cosph;
+  sincos(phi, &sinph, &cosph);
+  double u[3] = {costh * cosph, costh * sinph, -sinth};
+  double v[3] = {sinph, -cosph, 0.};
+  c.k[0] = -sinth * cosph;
+  c.k[1] = -sinth * sinph;
+  c.k[2] = -costh;
+  int idx = 0;
+  for (int i = 0; i < 3; i++)
+    for (int j = i; j < 3; j++, idx++) {
+      c.ep[idx] = v[i] * v[j] - u[i] * u[j];
+      c.ec[idx] = u[i] * v[j] + v[i] * u[j];
+    }
+  c.f0 = f0;
+  c.fdot = fdot;
+  c.phi0 = phi0;
+  c.amp_s = amp / (2.0 * (double)N);
+  // mixed-precision copy
+  for (int i = 0; i < 3; i++) c.kf[i] = (float)c.k[i];
+  for (int i = 0; i < 6; i++) {
+    c.epf[i] = (float)c.ep[i];
+    c.ecf[i] = (float)c.ec[i];
+  }
+  c.DPrf = (float)c.DPr;
+  c.DPif = (float)c.DPi;
+  c.DCrf = (float)c.DCr;
+  c.DCif = (float)c.DCi;
+  c.fonfs0 = (float)(f0 / fstar);
+  c.fdfs = (float)(fdot * T / fstar);
+  c.aef = (float)(0.66666666666666666666 * fdot * T / f0);
+  c.w0c = (float)(kPI2 * f0 / kCLIGHT);
+  c.p7pi = (float)(kPI * fdot * T * T);
+  c.amp_sf = (float)c.amp_s;
+  c.eps2pi = df_from_double(kPI2 * c.eps);
+  double bscale = kPI2 * f0 * (kAU / kCLIGHT);
+  c.beta1 = df_from_double(bscale * c.k[0]);
+  c.beta2 = df_from_double(bscale * c.k[1]);
+  c.phi0d = df_from_double(phi0);
+  c.p7pid = df_from_double(kPI * fdot * T * T);
+}
+
+// ----------------------------------------------------------------- slow part
+// Symmetric 3x3 quadratic form r^T E r, E stored as xx, xy, xz, yy, yz, zz.
+template <typename R>
+__device__ __forceinline__ R quad(const R *e, R x, R y, R z) {
+  return e[0] * x * x + e[3] * y * y + e[5] * z * z + (R)2 * (e[1] * x * y + e[2] * x * z + e[4] * y * z);
+}
+
+// sin(x)/x: Taylor series through x^12 for |x| <= 1 (truncation < 1e-12).
+__device__ __forceinline__ float sinc_f(float x) {
+  float ax = fabsf(x);
+  if (ax > 1.0f) return sinf(x) / x;
+  float x2 = x * x;
+  float s = 1.6059043836821613e-10f;          // 1/13!
+  s = fmaf(s, x2, -2.505210838544172e-08f);   // -1/11!
+  s = fmaf(s, x2, 2.755731922398589e-06f);    // 1/9!
+  s = fmaf(s, x2, -1.984126984126984e-04f);   // -1/7!
+  s = fmaf(s, x2, 8.333333333333333e-03f);    // 1/5!
+  s = fmaf(s, x2, -1.666666666666667e-01f);   // -1/3!
+  return fmaf(s, x2, 1.0f);
+}
+
+// The six arm series d_ij at one sample (order 12, 13, 21, 23, 31, 32),
+// amplitude-free.  FP64 follows ucb/src/glass_ucb_waveform.c:840-922 with the
+// carrier written relative to bin q: 2 pi f0 xi - 2 pi q t / T
+// = 2 pi (f0 T - q) t / T - 2 pi f0 k.x/c.
+__device__ __forceinline__ void slow_sample64(const ItemConst &c, const OrbitSample64 &o, double T, double fstar,
+                                              double L, double2 d[6]) {
+  double r12[3] = {(o.x[1] - o.x[0]) / L, (o.y[1] - o.y[0]) / L, (o.z[1] - o.z[0]) / L};
+  double r13[3] = {(o.x[2] - o.x[0]) / L, (o.y[2] - o.y[0]) / L, (o.z[2] - o.z[0]) / L};
+  double r23[3] = {(o.x[2] - o.x[1]) / L, (o.y[2] - o.y[1]) / L, (o.z[2] - o.z[1]) / L};
+  double dp12 = quad(c.ep, r12[0], r12[1], r12[2]), dc12 = quad(c.ec, r12[0], r12[1], r12[2]);
+  double dp13 = quad(c.ep, r13[0], r13[1], r13[2]), dc13 = quad(c.ec, r13[0], r13[1], r13[2]);
+  double dp23 = quad(c.ep, r23[0], r23[1], r23[2]), dc23 = quad(c.ec, r23[0], r23[1], r23[2]);
+  double kr12 = c.k[0] * r12[0] + c.k[1] * r12[1] + c.k[2] * r12[2];
+  double kr13 = c.k[0] * r13[0] + c.k[1] * r13[1] + c.k[2] * r13[2];
+  double kr23 = c.k[0] * r23[0] + c.k[1] * r23[1] + c.k[2] * r23[2];
+  double t = o.t;
+  double uT = t / T;
+  double fon[3], arg2[3], aev[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    double kdotx = (o.x[i] * c.k[0] + o.y[i] * c.k[1] + o.z[i] * c.k[2]) / kCLIGHT;
+    double xi = t - kdotx;
+    fon[i] = (c.f0 + c.fdot * xi) / fstar;
+    arg2[i] = kPI2 * c.eps * uT - kPI2 * c.f0 * kdotx - c.phi0 + kPI * c.fdot * xi * xi;
+    aev[i] = 1.0 + 0.66666666666666666666 * c.fdot / c.f0 * xi;
+  }
+  // arms: (i, j, dplus, dcross, k.r_ij)
+  const int ai[6] = {0, 0, 1, 1, 2, 2};
+  const double dps[6] = {dp12, dp13, dp12, dp23, dp13, dp23};
+  const double dcs[6] = {dc12, dc13, dc12, dc23, dc13, dc23};
+  const double krs[6] = {kr12, kr13, -kr12, kr23, -kr13, -kr23};
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    int i = ai[a];
+    double arg1 = 0.5 * fon[i] * (1.0 + krs[a]);
+    double sinc = 0.25 * sin(arg1) / arg1;
+    double t1r = aev[i] * (dps[a] * c.DPr + dcs[a] * c.DCr);
+    double t1i = aev[i] * (dps[a] * c.DPi + dcs[a] * c.DCi);
+    double s2, c2;
+    sincos(arg1 - arg2[i], &s2, &c2);
+    d[a] = make_double2(sinc * (t1r * c2 + t1i * s2), sinc * (-t1r * s2 + t1i * c2));
+  }
+}
+
+// Mixed precision: the carrier phase common to the three spacecraft
+// (heterodyne, guiding-centre Doppler, phi0 and the fdot t^2 term) is summed in
+// double-float and reduced mod 2 pi; the per-spacecraft corrections (< 0.5 rad)
+// and everything else are FP32.
+__device__ __forceinline__ void slow_sample_mix(const ItemConst &c, const OrbitSampleMix &o, float Rorb, float invL,
+                                                float AUc, float invT, float2 d[6]) {
+  const float ca = o.ca_hi, sa = o.sa_hi;
+  const float sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
+  float dx[3], dy[3], dz[3];
+  const float sbf[3] = {0.0f, 0.866025403784439f, -0.866025403784438f};
+  const float cbf[3] = {1.0f, -0.5f, -0.5f};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    dx[i] = Rorb * (saca * sbf[i] - (1.f + sa2) * cbf[i]);
+    dy[i] = Rorb * (saca * cbf[i] - (1.f + ca2) * sbf[i]);
+    dz[i] = -1.73205080757f * Rorb * (ca * cbf[i] + sa * sbf[i]);
+  }
+  float r12[3] = {(dx[1] - dx[0]) * invL, (dy[1] - dy[0]) * invL, (dz[1] - dz[0]) * invL};
+  float r13[3] = {(dx[2] - dx[0]) * invL, (dy[2] - dy[0]) * invL, (dz[2] - dz[0]) * invL};
+  float r23[3] = {(dx[2] - dx[1]) * invL, (dy[2] - dy[1]) * invL, (dz[2] - dz[1]) * invL};
+  float dp12 = quad(c.epf, r12[0], r12[1], r12[2]), dc12 = quad(c.ecf, r12[0], r12[1], r12[2]);
+  float dp13 = quad(c.epf, r13[0], r13[1], r13[2]), dc13 = quad(c.ecf, r13[0], r13[1], r13[2]);
+  float dp23 = quad(c.epf, r23[0], r23[1], r23[2]), dc23 = quad(c.ecf, r23[0], r23[1], r23[2]);
+  float kr12 = c.kf[0] * r12[0] + c.kf[1] * r12[1] + c.kf[2] * r12[2];
+  float kr13 = c.kf[0] * r13[0] + c.kf[1] * r13[1] + c.kf[2] * r13[2];
+  float kr23 = c.kf[0] * r23[0] + c.kf[1] * r23[1] + c.kf[2] * r23[2];
+
+  // common carrier phase in double-float
+  df u = {o.u_hi, o.u_lo};
+  df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
+  df ph = df_mul(c.eps2pi, u);
+  ph = df_add(ph, df_neg(df_add(df_mul(c.beta1, cad), df_mul(c.beta2, sad))));
+  ph = df_add(ph, df_neg(c.phi0d));
+  ph = df_add(ph, df_mul(c.p7pid, df_mul(u, u)));
+  const float psi0 = df_reduce_2pi(ph);
+  const float uf = o.u_hi;
+  const float tgc = AUc * (c.kf[0] * ca + c.kf[1] * sa);  // guiding-centre delay (s)
+
+  float fon[3], arg2[3], aev[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    float kdx = c.kf[0] * dx[i] + c.kf[1] * dy[i] + c.kf[2] * dz[i];  // k.(x_i - x_gc), metres
+    float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
+    float tT = taui * invT;
+    float v = uf - tT;  // xi / T
+    fon[i] = fmaf(c.fdfs, v, c.fonfs0);
+    aev[i] = fmaf(c.aef, v, 1.0f);
+    arg2[i] = psi0 - c.w0c * kdx + c.p7pi * tT * (tT - 2.0f * uf);
+  }
+  const int ai[6] = {0, 0, 1, 1, 2, 2};
+  const float dps[6] = {dp12, dp13, dp12, dp23, dp13, dp23};
+  const float dcs[6] = {dc12, dc13, dc12, dc23, dc13, dc23};
+  const float krs[6] = {kr12, kr13, -kr12, kr23, -kr13, -kr23};
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    int i = ai[a];
+    float arg1 = 0.5f * fon[i] * (1.0f + krs[a]);
+    float sinc = 0.25f * sinc_f(arg1);
+    float t1r = aev[i] * (dps[a] * c.DPrf + dcs[a] * c.DCrf);
+    float t1i = aev[i] * (dps[a] * c.DPif + dcs[a] * c.DCif);
+    float s2, c2;
+    sincosf(arg1 - arg2[i], &s2, &c2);
+    d[a] = make_float2(sinc * (t1r * c2 + t1i * s2), sinc * (-t1r * s2 + t1i * c2));
+  }
+}
+
+// Arm combinations whose FFTs give the A and E channels:
+//   A = (Z - X)/sqrt2 needs FFT(a2) (factor of the exp(-2ix)-type weight) and FFT(a1);
+//   E = (X - 2Y + Z)/sqrt6 needs FFT(e2) and FFT(e1).
+// (utils/src/glass_lisa.c:645-710 and :429-441)
+template <typename C>
+__device__ __forceinline__ void ae_combos(const C d[6], C out[4]) {
+  // d: 12, 13, 21, 23, 31, 32
+  const C d12 = d[0], d13 = d[1], d21 = d[2], d23 = d[3], d31 = d[4], d32 = d[5];
+  out[0] = csub(cadd(d31, d13), cadd(d32, d12));                                     // a2
+  out[1] = csub(cadd(d13, d31), cadd(d23, d21));                                     // a1
+  out[2] = cadd(csub(csub(cadd(d12, d31), d13), d32), cscale(csub(d21, d23), 2));    // e2
+  out[3] = cadd(csub(csub(cadd(d13, d21), d23), d31), cscale(csub(d12, d32), 2));    // e1
+}
+
+// ---------------------------------------------------------- main kernel
+struct FdArgs {
+  int NFFT;
+  double T, fstar, L, R;
+  const ItemConst *items;
+  const int *bin_count;
+  const int *bin_list;  // this size's list
+  const OrbitSample64 *pos64;
+  const OrbitSampleMix *mix;
+  const void *tw;
+  const float4 *w32;
+  const float4 *g32;
+  const double *Q;
+  const double2 *w64;
+  const double2 *g64;
+  const double *term_x;
+  double *dlogl, *term_y, *hh;
+  int *status;
+  int bin;
+};
+
+template <int N, bool MIX>
+struct FdSmem {
+  using C = typename std::conditional<MIX, float2, double2>::type;
+  static constexpr int NSER = (!MIX && N == 4096) ? 2 : 4;  // series resident at once
+  static constexpr int PASSES = 4 / NSER;
+  static constexpr int GPC = FdCfg<N>::GPC;
+  static constexpr size_t bytes = sizeof(C) * (size_t)N * (1 + (size_t)GPC * NSER) + sizeof(double) * 2 * 32;
+};
+
+// Sum over the threads of one group (result valid in every lane for GT <= 32,
+// in lane 0 otherwise).
+template <int GT>
+__device__ __forceinline__ double group_sum(double v, double *red, int lane) {
+#pragma unroll
+  for (int off = (GT < 32 ? GT : 32) / 2; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  if constexpr (GT > 32) {
+    __syncthreads();
+    if ((lane & 31) == 0) red[lane >> 5] = v;
+    __syncthreads();
+    if (lane == 0) {
+      double s = 0;
+      for (int w = 0; w < GT / 32; w++) s += red[w];
+      v = s;
+    }
+  }
+  return v;
+}
+
+template <int N, bool MIX>
+__global__ void __launch_bounds__(FdCfg<N>::CTA) fd_dlogl_kernel(FdArgs a) {
+  using Cfg = FdCfg<N>;
+  using S = FdSmem<N, MIX>;
+  using C = typename S::C;
+  constexpr int GT = Cfg::GT, R = Cfg::R, GPC = Cfg::GPC, NSER = S::NSER, PASSES = S::PASSES;
+  constexpr int CH = MIX ? 4 : ((R == 4) ? 2 : 1);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *tw = reinterpret_cast<C *>(smem_raw);
+  C *bufs = tw + N;
+  double *red = reinterpret_cast<double *>(bufs + (size_t)GPC * NSER * N);
+
+  const C *twg = reinterpret_cast<const C *>(a.tw);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
+  __syncthreads();
+
+  const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
+  C *buf = bufs + (size_t)g * NSER * N;
+  const int count = a.bin_count[a.bin];
+  const int NFFT = a.NFFT;
+  const float Rf = (float)a.R, invLf = (float)(1.0 / a.L), AUcf = (float)(kAU / kCLIGHT), invTf = (float)(1.0 / a.T);
+
+  for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC) {
+    const int slot = base + g;
+    const bool valid = slot < count;
+    const int item = a.bin_list[valid ? slot : count - 1];
+    const ItemConst &c = a.items[item];
+    const int seg = c.seg, imin = c.imin;
+
+    double acc = 0.0, hacc = 0.0;
+#pragma unroll 1
+    for (int pass = 0; pass < PASSES; ++pass) {
+      // 1-2. slow part and arm combinations
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int n = lane + GT * r;
+        C dd[6], cmb[4];
+        if constexpr (MIX) {
+          slow_sample_mix(c, a.mix[n], Rf, invLf, AUcf, invTf, dd);
+        } else {
+          slow_sample64(c, a.pos64[n], a.T, a.fstar, a.L, dd);
+        }
+        ae_combos(dd, cmb);
+#pragma unroll
+        for (int s = 0; s < NSER; ++s) buf[s * N + n] = cmb[pass * NSER + s];
+      }
+      group_sync<GT>();
+      // 3. FFTs
+      group_fft<N, GT, NSER, (CH < NSER ? CH : NSER)>(buf, tw, lane);
+      // 4. TDI weights, whitening and residual power over the support
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int k = lane + GT * r;
+        const int m = (k + N / 2) & (N - 1);
+        const int j = imin + m;
+        if (j < 0 || j >= NFFT) continue;
+        const size_t sj = (size_t)seg * NFFT + j;
+        if constexpr (MIX) {
+          const float4 w = a.w32[sj];
+          const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
+          const float s = c.amp_sf;
+          float2 hA = cadd(cmul(buf[0 * N + k], make_float2(gA.x, gA.y)), cmul(buf[1 * N + k], make_float2(gA.z, gA.w)));
+          float2 hE = cadd(cmul(buf[2 * N + k], make_float2(gE.x, gE.y)), cmul(buf[3 * N + k], make_float2(gE.z, gE.w)));
+          hA = cscale(hA, s);
+          hE = cscale(hE, s);
+          float ar = w.x - hA.x, ai = w.y - hA.y, er = w.z - hE.x, ei = w.w - hE.y;
+          acc += (double)(fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei));
+          hacc += (double)(fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y));
+        } else {
+          const double s = c.amp_s;
+          // series (2 ch, 2 ch + 1) of this pass hold the A (chan 0) or E (chan 1) pair
+#pragma unroll
+          for (int ch = 0; ch < NSER / 2; ++ch) {
+            const int chan = pass * (NSER / 2) + ch;
+            const double2 w = a.w64[2 * sj + chan];
+            const double2 g2 = a.g64[4 * sj + 2 * chan], g1 = a.g64[4 * sj + 2 * chan + 1];
+            double2 h = cadd(cmul(buf[(2 * ch) * N + k], g2), cmul(buf[(2 * ch + 1) * N + k], g1));
+            h = cscale(h, s);
+            acc += 2.0 * (w.x * h.x + w.y * h.y) - (h.x * h.x + h.y * h.y);
+            hacc += h.x * h.x + h.y * h.y;
+          }
+        }
+      }
+      group_sync<GT>();
+    }
+    acc = group_sum<GT>(acc, red, lane);
+    hacc = group_sum<GT>(hacc, red + 16, lane);
+    if (valid && lane == 0) {
+      double term;
+      if constexpr (MIX) {
+        int jlo = imin < 0 ? 0 : imin;
+        int jhi = imin + N > NFFT ? NFFT : imin + N;
+        const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
+        term = (Qs[jhi] - Qs[jlo]) - acc;
+      } else {
+        term = acc;
+      }
+      const double tx = a.term_x ? a.term_x[item] : 0.0;
+      a.dlogl[item] = term - tx;
+      if (a.term_y) a.term_y[item] = term;
+      if (a.hh) a.hh[item] = 2.0 * hacc;
+      if (a.status) a.status[item] = isfinite(term) ? 0 : 1;
+    }
+    if constexpr (GT > 32) __syncthreads();
+  }
+}
+
+
+// Launch of one size's kernel with a grid bounded by the SM count times the
+// occupancy of the kernel.
+template <int N, bool MIX>
+static cudaError_t launch_size(const FdArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
+  using Cfg = FdCfg<N>;
+  size_t smem = FdSmem<N, MIX>::bytes;
+  static int occ = -1;
+  if (occ < 0) {
+    cudaError_t e = cudaFuncSetAttribute(fd_dlogl_kernel<N, MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_dlogl_kernel<N, MIX>, Cfg::CTA, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  int need = (nitems_bound + Cfg::GPC - 1) / Cfg::GPC;
+  int grid = occ * num_sms;
+  if (need < grid) grid = need;
+  if (grid < 1) grid = 1;
+  fd_dlogl_kernel<N, MIX><<<grid, Cfg::CTA, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace glass

@@ -1,0 +1,143 @@
+/*
+ * glass_gb300.h -- C ABI of the GB300 UCB likelihood engine.
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-in replacements that keep the reference's own signatures, so the
+ *     GLASS apps (ucb_mcmc, ucb_wavelet_mcmc, global_fit) link against this
+ *     library instead of the reference's object files.  They take host
+ *     pointers, run on the calling thread's own CUDA stream and return when
+ *     the results are back in host memory.
+ *
+ *  2. Batched entry points (glass_gpu_*) that evaluate many proposals per
+ *     call on device-resident data: plain pointers and sizes, an int status,
+ *     no CPU fallback.
+ *
+ * Every function is thread-safe.  Contexts are not shared between threads
+ * unless the caller serialises their use.
+ */
+#ifndef GLASS_GB300_H
+#define GLASS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define GLASS_OK 0
+#define GLASS_ERR_ARG -1      /* null pointer, bad count, bad enum value */
+#define GLASS_ERR_SIZE -2     /* waveform size outside 32..4096 or not a power of two */
+#define GLASS_ERR_CUDA -3     /* a CUDA call failed; see glass_gpu_last_error() */
+#define GLASS_ERR_FORMAT -4   /* unknown TDI format string */
+#define GLASS_ERR_STATE -5    /* no segment bank uploaded yet */
+
+/* per-item status bits written by the batched kernels */
+#define GLASS_ITEM_OK 0
+#define GLASS_ITEM_NONFINITE 1     /* a parameter was NaN/Inf, or a result was */
+#define GLASS_ITEM_BAD_SEGMENT 2   /* segment index out of range */
+#define GLASS_ITEM_OUTSIDE 4       /* template support does not overlap the segment */
+
+/* precision of a batched evaluation */
+#define GLASS_PREC_FP64 0   /* plain FP64 throughout */
+#define GLASS_PREC_MIXED 1  /* FP32 waveform and inner products, FP64/double-float phase */
+
+/* TDI conventions, as the reference's `format` strings */
+#define GLASS_FMT_SANGRIA 0   /* "sangria"   utils/src/glass_lisa.c:645 */
+#define GLASS_FMT_PHASE 1     /* "phase"     utils/src/glass_lisa.c:458 */
+#define GLASS_FMT_FREQUENCY 2 /* "frequency" utils/src/glass_lisa.c:551 */
+
+/* ------------------------------------------------ drop-in (reference ABI) */
+struct Orbit; /* utils/src/glass_lisa.h:60-109; read: L, fstar, orbit_function */
+
+/*
+ * Replaces ucb_waveform (ucb/src/glass_ucb_waveform.h:210,
+ * ucb/src/glass_ucb_waveform.c:738-1001).  Same arguments and outputs:
+ * X,Y,Z,A,E receive 2*BW doubles each (re/im interleaved); for the "phase" and
+ * "frequency" formats with NI == 1 only X is written.  Spacecraft positions
+ * come from orbit->orbit_function, evaluated on the host at the BW sample
+ * times, so analytic and tabulated orbits both work.  BW must be a power of
+ * two in [32, 4096].  As in the reference, an unsupported format string
+ * prints a message and exits the process; so does a device error.
+ */
+void ucb_waveform(struct Orbit *orbit, char *format, double T, double t0, double *params, int NParams, double *X,
+                  double *Y, double *Z, double *A, double *E, int BW, int NI);
+
+/* Status-returning form of ucb_waveform for callers that handle errors. */
+int glass_ucb_waveform(const double *orbit_xyz, const char *format, double T, double t0, const double *params,
+                       int NParams, double *X, double *Y, double *Z, double *A, double *E, int BW, int NI);
+
+/*
+ * Replaces ucb_bandwidth (ucb/src/glass_ucb_waveform.h:185,
+ * ucb/src/glass_ucb_waveform.c:698-725): the number of slow-part samples N/2
+ * the reference picks for a source (a power of two in [16, Nmax]).
+ */
+int ucb_bandwidth(double L, double fstar, double f, double fdot, double costheta, double A, double T, int N);
+
+/* ---------------------------------------------------------- batched API */
+typedef struct glass_gpu_ctx glass_gpu_ctx;
+
+/* Create a context on a CUDA device with its own non-blocking stream. */
+int glass_gpu_create(int device, glass_gpu_ctx **ctx);
+int glass_gpu_destroy(glass_gpu_ctx *ctx);
+/* Run this context's work on a caller-owned cudaStream_t (NULL restores the
+ * context's own stream). */
+int glass_gpu_set_stream(glass_gpu_ctx *ctx, void *stream);
+/* Last error message of this thread (never NULL). */
+const char *glass_gpu_last_error(void);
+
+/*
+ * Upload a bank of `nseg` A/E frequency segments of NFFT bins each -- the
+ * inputs the reference's gaussian_log_likelihood reads
+ * (utils/src/glass_model.c:726-774, Nchannel == 2): for segment s,
+ *   rA, rE   : residual (data minus every source not being proposed),
+ *              2*NFFT doubles at offset s*2*NFFT, re/im interleaved
+ *   invCA/E  : inverse noise PSD, NFFT doubles at offset s*NFFT
+ *   qmin[s]  : first DFT bin of the segment (Data::qmin)
+ * T and t0 are the observation length and the model start time (Model::t0).
+ * Replaces any previous bank.  Host pointers; synchronous.
+ */
+int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, double t0, int NFFT, int nseg, const int *qmin,
+                          const double *rA, const double *rE, const double *invCA, const double *invCE);
+
+/* Replace the residual of one segment (after an accepted move changed the
+ * other sources of its chain).  Host pointers, 2*NFFT doubles each. */
+int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const double *rA, const double *rE);
+
+/*
+ * Batched proposal evaluation: for item i on segment item_seg[i] with
+ * parameters params[8*i .. 8*i+7] (the reference's params array,
+ * ucb/src/glass_ucb_model.c:40-53), compute
+ *   term_y[i] = logL(residual - h_i) - logL(residual)
+ * exactly as generate_ucb_model + gaussian_log_likelihood would
+ * (ucb/src/glass_ucb_model.c:55-103, utils/src/glass_model.c:726-774), with
+ * the template size from ucb_bandwidth and its placement from ucb_alignment
+ * (ucb/src/glass_ucb_waveform.c:698-736), and
+ *   dlogl[i]  = term_y[i] - term_x[i]       (term_x may be NULL: taken as 0)
+ *   hh[i]     = (h_i|h_i) over the segment   (snr^2, utils/src/glass_math.c:403)
+ *   status[i] = GLASS_ITEM_* bits            (may be NULL)
+ * so dlogl is the sampler's delta logL (ucb/src/glass_ucb_sampler.c:155-160)
+ * when term_x holds the current state's term_y.  All pointers are DEVICE
+ * pointers; the call is asynchronous on the context's stream.
+ */
+int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg, const double *params,
+                          const double *term_x, double *dlogl, double *term_y, double *hh, int *status);
+
+/* Same as glass_gpu_dlogl_batch with HOST pointers: copies in, evaluates,
+ * copies out and synchronises. */
+int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
+                               const double *params, const double *term_x, double *dlogl, double *term_y, double *hh,
+                               int *status);
+
+/* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
+int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
+
+/* ---------------------------------------------------------- diagnostics */
+/* Measured fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) of the
+ * device's FP32 (fp64 == 0) or FP64 pipe: the peak that the CUDA-core-bound
+ * kernels of this library are compared against.  No reference counterpart. */
+int glass_gpu_probe_fma_tflops(int device, int fp64, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GLASS_GB300_H */

@@ -1,0 +1,63 @@
+"""The C-ABI library loads and exports every symbol include/glass_gb300.h
+declares; host-only entry points agree with the reference (no GPU needed)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import glass_gb300 as gg
+from glass_gb300 import workloads as wl
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from glass_gb300 import build
+
+    build.build()
+    return gg.load_library()
+
+
+def _declared_functions():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w \*]*?)\b([A-Za-z_]\w*)\s*\([^;{]*\)\s*;", text, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_header_declares_what_the_module_binds():
+    declared = _declared_functions()
+    assert set(declared) == set(gg.EXPORTS), (declared, gg.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in _declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_ucb_bandwidth_matches_reference(lib, golden):
+    g = golden("bandwidth.npz")
+    L, fstar = 2.5e9, wl.FSTAR
+    got = np.array([gg.ucb_bandwidth(L, fstar, g["f"][i], g["fdot"][i], g["costh"][i], g["amp"][i], wl.T_YEAR,
+                                     int(g["nfft"][i])) for i in range(len(g["f"]))])
+    np.testing.assert_array_equal(got, g["bw"])
+
+
+def test_errors_are_reported_without_a_gpu(lib):
+    """Argument checks run before any device call."""
+    p = np.zeros(8)
+    out = np.zeros((5, 2 * 48))
+    rc = lib.glass_ucb_waveform(None, b"sangria", 1.0, 0.0, p.ctypes.data_as(gg._D), 8,
+                                *[out[i].ctypes.data_as(gg._D) for i in range(5)], 48, 2)
+    assert rc == -2  # GLASS_ERR_SIZE: 48 is not a power of two
+    rc = lib.glass_ucb_waveform(None, b"nonsense", 1.0, 0.0, p.ctypes.data_as(gg._D), 8,
+                                *[out[i].ctypes.data_as(gg._D) for i in range(5)], 32, 2)
+    assert rc == -4  # GLASS_ERR_FORMAT
+    assert b"Unsupported" in lib.glass_gpu_last_error()

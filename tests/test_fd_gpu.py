@@ -1,0 +1,226 @@
+"""Parity of the CUDA Fourier-domain path with the reference (golden vectors)
+and with the oracle, through the C ABI.
+
+Tolerances: the plain FP64 path must match to 1e-10 relative (waveforms:
+relative to the channel's largest value; delta logL: relative to
+max(1, |logL|)); the mixed-precision path must stay within |delta logL
+error| < 1e-3 of the FP64 path.
+"""
+import numpy as np
+import pytest
+
+import glass_gb300 as gg
+from glass_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+T = wl.T_YEAR
+REL = 1e-10
+MIXED_ABS = 1e-3
+
+
+@pytest.fixture(scope="module")
+def engine():
+    from glass_gb300 import build
+
+    build.build()
+    eng = gg.Engine(0)
+    yield eng
+    eng.close()
+
+
+def test_drop_in_waveform_matches_reference(golden):
+    g = golden("waveforms.npz")
+    for i in range(len(g["N"])):
+        fmt, N, NI, t0 = str(g["fmt"][i]), int(g["N"][i]), int(g["NI"][i]), float(g["t0"][i])
+        ref = g[f"h{i}"]
+        got = gg.ucb_waveform(g["params"][i], N, T, t0=t0, fmt=fmt, NI=NI)
+        chans = range(5) if (fmt == "sangria" or NI > 1) else range(1)
+        for c in chans:
+            scale = np.abs(ref[c]).max()
+            err = np.abs(got[c] - ref[c]).max() / scale
+            assert err < REL, (fmt, N, NI, t0, c, err)
+        if not (fmt == "sangria" or NI > 1):
+            assert not got[1:].any()  # Y, Z, A, E untouched for NI == 1
+
+
+def test_drop_in_waveform_with_given_orbit(port):
+    """Positions supplied by the caller (the reference's orbit_function) are used as-is."""
+    rng = np.random.default_rng(3)
+    p = wl.draw_source(rng, 4e-3, 1e-22)
+    N = 256
+    pos = np.array([port.orbit(T * n / N) for n in range(N)])
+    a = gg.ucb_waveform(p, N, T, orbit_xyz=pos)
+    b = port.waveform(p, N, T)
+    for c in range(5):
+        assert np.abs(a[c] - b[c]).max() / np.abs(b[c]).max() < REL
+
+
+def _case(g, k):
+    return {key[len(f"c{k}_"):]: g[key] for key in g.files if key.startswith(f"c{k}_")}
+
+
+def _residual(port, case):
+    rA, rE = case["dA"].copy(), case["dE"].copy()
+    for p in case["extra"]:
+        al = port.alignment(T, 1024, int(case["qmin"]), p)
+        N, imin = int(al[0]), int(al[3])
+        h = port.waveform(p, N, T)
+        for i in range(N):
+            j = i + imin
+            if 0 <= j < 1024:
+                rA[2 * j:2 * j + 2] -= h[3][2 * i:2 * i + 2]
+                rE[2 * j:2 * j + 2] -= h[4][2 * i:2 * i + 2]
+    return rA, rE
+
+
+def _bank_from_interleaved(qmin, rA, rE, iA, iE, NFFT=1024, t0=0.0):
+    rA = np.atleast_2d(rA)
+    rE = np.atleast_2d(rE)
+    return wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.atleast_1d(np.asarray(qmin, np.int32)),
+                          dA=rA[:, 0::2] + 1j * rA[:, 1::2], dE=rE[:, 0::2] + 1j * rE[:, 1::2],
+                          invCA=np.atleast_2d(iA), invCE=np.atleast_2d(iE), t0=t0)
+
+
+def test_fp64_delta_logl_matches_reference(engine, port, golden):
+    g = golden("likelihood.npz")
+    for k in range(int(g["ncase"])):
+        case = _case(g, k)
+        rA, rE = _residual(port, case)
+        engine.upload(_bank_from_interleaved(int(case["qmin"]), rA, rE, case["invCA"], case["invCE"]))
+        props = case["props"]
+        dl, ty, hh, st = engine.dlogl_host(np.zeros(len(props), np.int32), props, precision=gg.PREC_FP64)
+        assert (st == 0).all()
+        logL = case["logL"]
+        for j in range(1, len(props)):
+            d_ref = logL[j] - logL[0]
+            assert abs((ty[j] - ty[0]) - d_ref) < REL * max(1.0, abs(logL[j])), (k, j, ty[j] - ty[0], d_ref)
+        if len(case["extra"]) == 0:
+            for j in range(len(props)):
+                assert abs(ty[j] - (logL[j] - case["logL_empty"])) < REL * max(1.0, abs(logL[j]))
+
+
+def _random_bank(rng, nseg, NFFT, port, t0=0.0, log_f=(0.5e-3, 15e-3)):
+    qmin, dA, dE, iA, iE, inj = [], [], [], [], [], []
+
+    def wf(p):
+        al = port.alignment(T, NFFT, 0, p)
+        h = port.waveform(p, int(al[0]), T, t0=t0)
+        return int(al[0]), h[3], h[4]
+
+    for s in range(nseg):
+        f0 = 10 ** rng.uniform(np.log10(log_f[0]), np.log10(log_f[1]))
+        amp = 10 ** rng.uniform(-23, -21)
+        p = wl.draw_source(rng, f0, amp, 1e-17)
+        q, a, e, ia, ie = wl.make_segment(rng, [p], wf, NFFT=NFFT, T=T)
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie), inj.append(p)
+    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                          invCA=np.array(iA), invCE=np.array(iE), t0=t0)
+    return bank, np.array(inj)
+
+
+def _oracle_terms(port, bank, seg, params, fmt="sangria"):
+    rA, rE = bank.interleaved()
+    out = []
+    for s, p in zip(seg, params):
+        t, h, N = port.dlogl_term(p, T, bank.NFFT, int(bank.qmin[s]), rA[s], rE[s], bank.invCA[s], bank.invCE[s],
+                                  t0=bank.t0, fmt=fmt)
+        out.append((t, h, N))
+    return np.array(out)
+
+
+@pytest.mark.parametrize("fmt", ["sangria", "phase", "frequency"])
+def test_fp64_batch_matches_oracle_all_sizes(engine, port, fmt):
+    """Config-1-like bank: f0 log-uniform over 0.5-15 mHz so N spans 32..1024."""
+    rng = np.random.default_rng({"sangria": 11, "phase": 12, "frequency": 13}[fmt])
+    bank, inj = _random_bank(rng, 16, 1024, port)
+    engine.upload(bank, fmt=fmt)
+    seg = rng.integers(0, 16, 96).astype(np.int32)
+    params = np.array([wl.gaussian_jumps(rng, inj[s], wl.jump_scales(inj[s], 20.0), 1)[0] for s in seg])
+    dl, ty, hh, st = engine.dlogl_host(seg, params, precision=gg.PREC_FP64)
+    ref = _oracle_terms(port, bank, seg, params, fmt)
+    assert (st == 0).all()
+    Ns = set(ref[:, 2].astype(int))
+    assert len(Ns) >= 3, Ns
+    err = np.abs(ty - ref[:, 0]) / np.maximum(1.0, np.abs(ref[:, 0]))
+    assert err.max() < REL, err.max()
+    np.testing.assert_allclose(hh, ref[:, 1], rtol=1e-9, atol=1e-12)
+
+
+def test_mixed_precision_error_budget(engine, port):
+    rng = np.random.default_rng(21)
+    bank, inj = _random_bank(rng, 32, 1024, port)
+    engine.upload(bank)
+    seg = np.repeat(np.arange(32, dtype=np.int32), 16)
+    params = np.vstack([wl.gaussian_jumps(rng, inj[s], wl.jump_scales(inj[s], 20.0), 16) for s in range(32)])
+    tx = rng.normal(0, 5, len(seg))
+    d64, t64, h64, s64 = engine.dlogl_host(seg, params, term_x=tx, precision=gg.PREC_FP64)
+    d32, t32, h32, s32 = engine.dlogl_host(seg, params, term_x=tx, precision=gg.PREC_MIXED)
+    assert (s64 == 0).all() and (s32 == 0).all()
+    err = np.abs(d32 - d64)
+    assert err.max() < MIXED_ABS, (err.max(), np.sqrt(h64[np.argmax(err)]))
+    np.testing.assert_allclose(d64, t64 - tx, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(h32, h64, rtol=1e-4)
+
+
+def test_segment_edges_and_status(engine, port):
+    """Templates that straddle either segment edge are clipped like
+    add_ucb_model (ucb/src/glass_ucb_model.c:180-232); templates outside the
+    segment leave logL unchanged; bad inputs are flagged per item."""
+    rng = np.random.default_rng(5)
+    bank, inj = _random_bank(rng, 2, 256, port, log_f=(3e-3, 3.2e-3))
+    engine.upload(bank)
+    p0 = inj[0].copy()
+    cases = []
+    for shift in (-150.0, -120.0, -100.0, 100.0, 120.0, 140.0, 2000.0, -2000.0):
+        p = p0.copy()
+        p[0] += shift
+        cases.append(p)
+    params = np.array(cases)
+    seg = np.zeros(len(params), np.int32)
+    dl, ty, hh, st = engine.dlogl_host(seg, params, precision=gg.PREC_FP64)
+    ref = _oracle_terms(port, bank, seg, params)
+    err = np.abs(ty - ref[:, 0]) / np.maximum(1.0, np.abs(ref[:, 0]))
+    assert err.max() < REL
+    assert st[-1] == gg.ITEM_OUTSIDE and st[-2] == gg.ITEM_OUTSIDE
+    assert ty[-1] == 0.0 and ty[-2] == 0.0
+    # mixed precision clips identically
+    dm, tm, hm, sm = engine.dlogl_host(seg, params, precision=gg.PREC_MIXED)
+    assert np.abs(tm - ty).max() < MIXED_ABS
+    # invalid inputs
+    bad = np.array([p0, p0, p0, p0])
+    bad[0, 3] = np.nan
+    bad[1, 1] = 1.5
+    segb = np.array([0, 0, 7, -1], np.int32)
+    dl, ty, hh, st = engine.dlogl_host(segb, bad, precision=gg.PREC_FP64)
+    assert st[0] & gg.ITEM_NONFINITE and st[1] & gg.ITEM_NONFINITE
+    assert st[2] & gg.ITEM_BAD_SEGMENT and st[3] & gg.ITEM_BAD_SEGMENT
+    assert np.isnan(dl).all()
+    # empty batch is a no-op
+    engine.dlogl_host(np.zeros(0, np.int32), np.zeros((0, 8)))
+
+
+def test_t0_and_residual_update(engine, port):
+    rng = np.random.default_rng(8)
+    bank, inj = _random_bank(rng, 4, 512, port, t0=2.5e6)
+    engine.upload(bank)
+    seg = np.arange(4, dtype=np.int32)
+    dl, ty, hh, st = engine.dlogl_host(seg, inj, precision=gg.PREC_FP64)
+    ref = _oracle_terms(port, bank, seg, inj)
+    assert (np.abs(ty - ref[:, 0]) / np.maximum(1, np.abs(ref[:, 0]))).max() < REL
+    dm, tm, _, _ = engine.dlogl_host(seg, inj, precision=gg.PREC_MIXED)
+    assert np.abs(tm - ty).max() < MIXED_ABS
+    # replace the residual of segment 2 with data minus the injection
+    rA, rE = bank.interleaved()
+    al = port.alignment(T, 512, int(bank.qmin[2]), inj[2])
+    hw = port.waveform(inj[2], int(al[0]), T, t0=bank.t0)
+    rA2, rE2 = rA[2].copy(), rE[2].copy()
+    for i in range(int(al[0])):
+        j = i + int(al[3])
+        if 0 <= j < 512:
+            rA2[2 * j:2 * j + 2] -= hw[3][2 * i:2 * i + 2]
+            rE2[2 * j:2 * j + 2] -= hw[4][2 * i:2 * i + 2]
+    engine.set_residual(2, rA2, rE2)
+    dl2, ty2, hh2, st2 = engine.dlogl_host(np.array([2], np.int32), inj[2:3], precision=gg.PREC_FP64)
+    t_ref, _, _ = port.dlogl_term(inj[2], T, 512, int(bank.qmin[2]), rA2, rE2, bank.invCA[2], bank.invCE[2],
+                                  t0=bank.t0)
+    assert abs(ty2[0] - t_ref) < REL * max(1, abs(t_ref))
