@@ -145,7 +145,7 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
 
 // ------------------------------------------------------- per-proposal constants
 // utils/src/glass_lisa.c:1188-1198 (AEnoise) with rednoise (:1183).
-__device__ double aenoise_dev(double f, double L, double fstar) {
+static __device__ double aenoise_dev(double f, double L, double fstar) {
   double fonfstar = f / fstar;
   double sf = sin(fonfstar);
   double trans = sf * sf;
@@ -169,7 +169,7 @@ __device__ __forceinline__ int pow2_above_dev(double v) {
 }
 
 // ucb/src/glass_ucb_waveform.c:698-725 (ucb_bandwidth).
-__device__ int bandwidth_dev(double L, double fstar, double f, double fdot, double costheta, double A, double T,
+static __device__ int bandwidth_dev(double L, double fstar, double f, double fdot, double costheta, double A, double T,
                              int NFFT) {
   const int Nmin = 16;
   int half = NFFT / 2;
@@ -191,7 +191,7 @@ __device__ int bandwidth_dev(double L, double fstar, double f, double fdot, doub
 
 // Per-proposal constants (ucb/src/glass_ucb_waveform.c:802-838 and
 // utils/src/glass_lisa.c:1566-1596), amplitude factored out as amp/(2N).
-__device__ void make_item_const(const double *p, int NP, double T, double fstar, int N, ItemConst &c) {
+static __device__ void make_item_const(const double *p, int NP, double T, double fstar, int N, ItemConst &c) {
   double f0 = p[0] / T, costh = p[1], phi = p[2], amp = exp(p[3]), cosi = p[4], psi = p[5], phi0 = p[6];
   double fdot = NP > 7 ? p[7] / (T * T) : 0.0;
   double fT = f0 * T;
