@@ -25,6 +25,11 @@ LIB = os.path.join(OUT_DIR, "libglass_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "-I" + os.path.join(ROOT, "include")]
+# The plain-FP64 translation units evaluate the carrier phase the way the
+# reference does (ucb/src/glass_ucb_waveform.c:877, arguments of ~1e6 rad); a
+# fused multiply-add rounds differently from the reference's separate multiply
+# and add by up to ~1e-10 rad there, so contraction is off for them.
+PER_FILE_FLAGS = {"ucb_fd.cu": ["-fmad=false"], "ucb_fd_fp64.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -46,7 +51,8 @@ def _stale(lib: str, deps) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
-    deps = _sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+    deps = (_sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
+            + [os.path.abspath(__file__)])
     if not force and not _stale(LIB, deps):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
@@ -55,7 +61,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
-        cmd = [cc] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [cc] + ARCH + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

@@ -79,6 +79,17 @@ extern "C" int glass_gpu_create(int device, glass_gpu_ctx **out) {
     return cuda_err(e, "cudaStreamCreate");
   }
   ctx->stream = ctx->own;
+  for (int b = 0; b < kNumBins; b++) {
+    if ((e = cudaStreamCreateWithFlags(&ctx->work.side[b], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->work.join[b], cudaEventDisableTiming)) != cudaSuccess) {
+      glass_gpu_destroy(ctx);
+      return cuda_err(e, "stream/event create");
+    }
+  }
+  if ((e = cudaEventCreateWithFlags(&ctx->work.fork, cudaEventDisableTiming)) != cudaSuccess) {
+    glass_gpu_destroy(ctx);
+    return cuda_err(e, "event create");
+  }
   *out = ctx;
   return GLASS_OK;
 }
@@ -93,6 +104,11 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->work.bin_count);
   cudaFree(ctx->work.bin_list);
   cudaFree(ctx->d_stage);
+  for (int b = 0; b < kNumBins; b++) {
+    if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
+    if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
+  }
+  if (ctx->work.fork) cudaEventDestroy(ctx->work.fork);
   cudaStreamDestroy(ctx->own);
   delete ctx;
   return GLASS_OK;

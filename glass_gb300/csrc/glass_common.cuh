@@ -95,6 +95,7 @@ struct ItemConst {
   double ep[6], ec[6];  // symmetric tensors: xx, xy, xz, yy, yz, zz
   double DPr, DPi, DCr, DCi;  // amplitude-free polarisation factors
   double f0, fdot, eps, phi0, amp_s;  // eps = f0*T - q ; amp_s = amp/(2N)
+  double dfq;                         // 2 pi q / T (ucb/src/glass_ucb_waveform.c:818)
   // FP32 / double-float copy (mixed path)
   float kf[3];
   float epf[6], ecf[6];

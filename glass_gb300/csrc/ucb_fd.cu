@@ -271,19 +271,28 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.hh = hh;
   a.status = status;
   const bool mix = precision == 1;
+  e = cudaEventRecord(work.fork, stream);
+  if (e != cudaSuccess) return e;
   // every size a segment of NFFT bins can produce: 32 .. NFFT (ucb_bandwidth caps N at NFFT)
+  int nb = 0;
   for (int b = 0; b < kNumBins; b++) {
     int N = 32 << b;
     if (N > bank.NFFT) break;
+    cudaStream_t sb = work.side[b];
+    if ((e = cudaStreamWaitEvent(sb, work.fork, 0)) != cudaSuccess) return e;
     a.bin = b;
     a.bin_list = work.bin_list + (size_t)b * work.cap;
     a.pos64 = tab.pos64[b];
     a.mix = tab.mix[b];
     a.tw = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
-    e = mix ? fd_launch_size_mixed(N, a, nitems, num_sms, stream) : fd_launch_size_fp64(N, a, nitems, num_sms, stream);
+    e = mix ? fd_launch_size_mixed(N, a, nitems, num_sms, sb) : fd_launch_size_fp64(N, a, nitems, num_sms, sb);
     launches++;
     if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecord(work.join[b], sb)) != cudaSuccess) return e;
+    nb++;
   }
+  for (int b = 0; b < nb; b++)
+    if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;
   if (nlaunch) *nlaunch = launches;
   return cudaSuccess;
 }

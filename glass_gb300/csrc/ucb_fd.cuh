@@ -29,6 +29,11 @@ struct FdTablesDev {
 
 // Scratch of one batched evaluation.
 struct FdWorkDev {
+  // per-size streams forked from the caller's stream after the plan kernel, so
+  // that the size kernels run concurrently (and become parallel branches when
+  // the caller captures a CUDA graph)
+  cudaStream_t side[kNumBins] = {};
+  cudaEvent_t fork = nullptr, join[kNumBins] = {};
   int cap = 0;
   ItemConst *items = nullptr;  // [cap]
   int *bin_count = nullptr;    // [kNumBins]

@@ -197,6 +197,7 @@ static __device__ void make_item_const(const double *p, int NP, double T, double
   double fT = f0 * T;
   long long q = (long long)fT;
   c.eps = fT - (double)q;
+  c.dfq = kPI2 * (((double)q) / T);
   double sinps, cosps;
   sincos(2. * psi, &sinps, &cosps);
   double Aplus = (1. + cosi * cosi) * 0.5, Across = -cosi;
@@ -268,9 +269,11 @@ __device__ __forceinline__ float sinc_f(float x) {
 }
 
 // The six arm series d_ij at one sample (order 12, 13, 21, 23, 31, 32),
-// amplitude-free.  FP64 follows ucb/src/glass_ucb_waveform.c:840-922 with the
-// carrier written relative to bin q: 2 pi f0 xi - 2 pi q t / T
-// = 2 pi (f0 T - q) t / T - 2 pi f0 k.x/c.
+// amplitude-free, in FP64 with the reference's own sequence of operations
+// (ucb/src/glass_ucb_waveform.c:840-922).  The carrier argument arg2 reaches
+// ~1e6 rad, where every rounding step is worth ~1e-10 rad; this translation
+// unit is compiled without multiply-add contraction so that those roundings
+// are the reference's.
 __device__ __forceinline__ void slow_sample64(const ItemConst &c, const OrbitSample64 &o, double T, double fstar,
                                               double L, double2 d[6]) {
   double r12[3] = {(o.x[1] - o.x[0]) / L, (o.y[1] - o.y[0]) / L, (o.z[1] - o.z[0]) / L};
@@ -282,18 +285,19 @@ __device__ __forceinline__ void slow_sample64(const ItemConst &c, const OrbitSam
   double kr12 = c.k[0] * r12[0] + c.k[1] * r12[1] + c.k[2] * r12[2];
   double kr13 = c.k[0] * r13[0] + c.k[1] * r13[1] + c.k[2] * r13[2];
   double kr23 = c.k[0] * r23[0] + c.k[1] * r23[1] + c.k[2] * r23[2];
-  double t = o.t;
-  double uT = t / T;
+  const double t = o.t;
+  const double w0 = kPI2 * c.f0, wd = kPI * c.fdot, ae = 0.66666666666666666666 * c.fdot / c.f0;
   double fon[3], arg2[3], aev[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     double kdotx = (o.x[i] * c.k[0] + o.y[i] * c.k[1] + o.z[i] * c.k[2]) / kCLIGHT;
     double xi = t - kdotx;
     fon[i] = (c.f0 + c.fdot * xi) / fstar;
-    arg2[i] = kPI2 * c.eps * uT - kPI2 * c.f0 * kdotx - c.phi0 + kPI * c.fdot * xi * xi;
-    aev[i] = 1.0 + 0.66666666666666666666 * c.fdot / c.f0 * xi;
+    double a2 = w0 * xi - c.phi0 - c.dfq * t;
+    a2 += wd * xi * xi;
+    arg2[i] = a2;
+    aev[i] = 1.0 + ae * xi;
   }
-  // arms: (i, j, dplus, dcross, k.r_ij)
   const int ai[6] = {0, 0, 1, 1, 2, 2};
   const double dps[6] = {dp12, dp13, dp12, dp23, dp13, dp23};
   const double dcs[6] = {dc12, dc13, dc12, dc23, dc13, dc23};
