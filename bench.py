@@ -350,9 +350,12 @@ def run_ours(args):
     total = args.steps * items * world
     v_mixed, v_fp64, v_e2e = total / t_mixed, total / t_fp64, total / t_e2e
 
-    err = (torch.stack(rec_mixed) - torch.stack(rec_fp64)).cpu().numpy()
+    m64 = torch.stack(rec_fp64).cpu().numpy()
+    err = torch.stack(rec_mixed).cpu().numpy() - m64
     valid = np.isfinite(err)
     abs_err = np.abs(err[valid])
+    dl64 = m64[valid]
+    near = dl64 > -100.0  # proposals whose acceptance is not already decided
 
     # roofline of the fused kernels (FP32 pipe bound): algorithmic flops per step
     # from the sizes the bandwidth rule picks, over the measured step time
@@ -377,6 +380,10 @@ def run_ours(args):
                      "mixed_over_fp64": v_mixed / v_fp64},
             "accuracy": {"max_abs_dlogl_err_vs_fp64": float(abs_err.max()),
                          "p99_abs_err": float(np.quantile(abs_err, 0.99)),
+                         "frac_abs_err_below_1e-3": float((abs_err < 1e-3).mean()),
+                         "max_abs_err_dlogl_gt_-100": float(abs_err[near].max()) if near.any() else None,
+                         "n_dlogl_gt_-100": int(near.sum()),
+                         "max_rel_err": float((abs_err / np.maximum(1.0, np.abs(dl64))).max()),
                          "evals_compared": int(abs_err.size), "invalid_proposals": int((~valid).sum())},
             "e2e": {"value": v_e2e, "unit": "evals/s",
                     "h2d_bytes_per_step": int(items * (8 * 8 + 4 + 8)),

@@ -100,9 +100,11 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->bank_mem);
   cudaFree(ctx->tab.base);
-  cudaFree(ctx->work.items);
+  cudaFree(ctx->work.items64);
+  cudaFree(ctx->work.itemsmix);
   cudaFree(ctx->work.bin_count);
   cudaFree(ctx->work.bin_list);
+  cudaFree(ctx->work.series);
   cudaFree(ctx->d_stage);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
@@ -142,19 +144,20 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   const size_t nb = (size_t)nseg * NFFT;
-  std::vector<float4> w32(nb), g32(2 * nb);
+  std::vector<float4> w32(nb), w32lo(nb), g32(2 * nb);
   std::vector<double> Q((size_t)nseg * (NFFT + 1));
   std::vector<double2> w64(2 * nb), g64(4 * nb);
   const double fstar = fstar_of_orbit();
-  fd_build_bank_tables(format, T, fstar, NFFT, nseg, qmin, rA, rE, invCA, invCE, w32.data(), g32.data(), Q.data(),
-                       w64.data(), g64.data());
+  fd_build_bank_tables(format, T, fstar, NFFT, nseg, qmin, rA, rE, invCA, invCE, w32.data(), w32lo.data(),
+                       g32.data(), Q.data(), w64.data(), g64.data());
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "bank_upload sync");
   cudaFree(ctx->bank_mem);
   ctx->bank_mem = nullptr;
   size_t off_q = sizeof(int) * ((nseg + 63) / 64 * 64);
   size_t off_w32 = off_q + sizeof(double) * Q.size();
   off_w32 = (off_w32 + 255) / 256 * 256;
-  size_t off_g32 = off_w32 + sizeof(float4) * w32.size();
+  size_t off_w32lo = off_w32 + sizeof(float4) * w32.size();
+  size_t off_g32 = off_w32lo + sizeof(float4) * w32lo.size();
   size_t off_w64 = off_g32 + sizeof(float4) * g32.size();
   size_t off_g64 = off_w64 + sizeof(double2) * w64.size();
   size_t total = off_g64 + sizeof(double2) * g64.size();
@@ -170,12 +173,14 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   b.qmin = (int *)base;
   b.Q = (double *)(base + off_q);
   b.w32 = (float4 *)(base + off_w32);
+  b.w32lo = (float4 *)(base + off_w32lo);
   b.g32 = (float4 *)(base + off_g32);
   b.w64 = (double2 *)(base + off_w64);
   b.g64 = (double2 *)(base + off_g64);
   GLASS_CUDA(cudaMemcpy(b.qmin, qmin, sizeof(int) * nseg, cudaMemcpyHostToDevice), "upload qmin");
   GLASS_CUDA(cudaMemcpy(b.Q, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice), "upload Q");
   GLASS_CUDA(cudaMemcpy(b.w32, w32.data(), sizeof(float4) * w32.size(), cudaMemcpyHostToDevice), "upload w32");
+  GLASS_CUDA(cudaMemcpy(b.w32lo, w32lo.data(), sizeof(float4) * w32lo.size(), cudaMemcpyHostToDevice), "upload w32lo");
   GLASS_CUDA(cudaMemcpy(b.g32, g32.data(), sizeof(float4) * g32.size(), cudaMemcpyHostToDevice), "upload g32");
   GLASS_CUDA(cudaMemcpy(b.w64, w64.data(), sizeof(double2) * w64.size(), cudaMemcpyHostToDevice), "upload w64");
   GLASS_CUDA(cudaMemcpy(b.g64, g64.data(), sizeof(double2) * g64.size(), cudaMemcpyHostToDevice), "upload g64");
@@ -200,15 +205,17 @@ extern "C" int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const do
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   const int NFFT = b.NFFT;
-  std::vector<float4> w32(NFFT), g32(2 * NFFT);
+  std::vector<float4> w32(NFFT), w32lo(NFFT), g32(2 * NFFT);
   std::vector<double> Q(NFFT + 1);
   std::vector<double2> w64(2 * NFFT), g64(4 * NFFT);
   fd_build_bank_tables(b.format, b.T, b.fstar, NFFT, 1, &ctx->h_qmin[seg], rA, rE,
                        ctx->h_invCA.data() + (size_t)seg * NFFT, ctx->h_invCE.data() + (size_t)seg * NFFT,
-                       w32.data(), g32.data(), Q.data(), w64.data(), g64.data());
+                       w32.data(), w32lo.data(), g32.data(), Q.data(), w64.data(), g64.data());
   size_t sj = (size_t)seg * NFFT;
   GLASS_CUDA(cudaMemcpyAsync(b.w32 + sj, w32.data(), sizeof(float4) * NFFT, cudaMemcpyHostToDevice, ctx->stream),
              "residual w32");
+  GLASS_CUDA(cudaMemcpyAsync(b.w32lo + sj, w32lo.data(), sizeof(float4) * NFFT, cudaMemcpyHostToDevice, ctx->stream),
+             "residual w32lo");
   GLASS_CUDA(cudaMemcpyAsync(b.Q + (size_t)seg * (NFFT + 1), Q.data(), sizeof(double) * (NFFT + 1),
                              cudaMemcpyHostToDevice, ctx->stream), "residual Q");
   GLASS_CUDA(cudaMemcpyAsync(b.w64 + 2 * sj, w64.data(), sizeof(double2) * 2 * NFFT, cudaMemcpyHostToDevice,
@@ -218,21 +225,36 @@ extern "C" int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const do
 }
 
 // --------------------------------------------------------------- batched
+// Scratch for a batch: per-proposal constants, size lists and the slow-part
+// series (4 complex series of N <= NFFT samples per proposal), sized for the
+// worst case so that a batch never allocates once the context has seen a batch
+// of that size (required for CUDA-graph capture of glass_gpu_dlogl_batch).
 static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   FdWorkDev &w = ctx->work;
-  if (nitems <= w.cap) return GLASS_OK;
+  size_t series = fd_series_bytes(nitems, ctx->bank.NFFT, GLASS_PREC_FP64);
+  if (nitems <= w.cap && series <= w.series_bytes) return GLASS_OK;
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "work sync");
-  cudaFree(w.items);
+  cudaFree(w.items64);
+  cudaFree(w.itemsmix);
   cudaFree(w.bin_count);
   cudaFree(w.bin_list);
-  w.items = nullptr;
+  cudaFree(w.series);
+  w.items64 = nullptr;
+  w.itemsmix = nullptr;
   w.bin_count = nullptr;
   w.bin_list = nullptr;
+  w.series = nullptr;
+  w.cap = 0;
+  w.series_bytes = 0;
   int cap = nitems < 1024 ? 1024 : nitems;
-  GLASS_CUDA(cudaMalloc(&w.items, sizeof(ItemConst) * (size_t)cap), "cudaMalloc(items)");
+  series = fd_series_bytes(cap, ctx->bank.NFFT, GLASS_PREC_FP64);
+  GLASS_CUDA(cudaMalloc(&w.items64, sizeof(ItemF64) * (size_t)cap), "cudaMalloc(items64)");
+  GLASS_CUDA(cudaMalloc(&w.itemsmix, sizeof(ItemMix) * (size_t)cap), "cudaMalloc(itemsmix)");
   GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * kNumBins), "cudaMalloc(bin_count)");
   GLASS_CUDA(cudaMalloc(&w.bin_list, sizeof(int) * (size_t)kNumBins * cap), "cudaMalloc(bin_list)");
+  GLASS_CUDA(cudaMalloc(&w.series, series), "cudaMalloc(series)");
   w.cap = cap;
+  w.series_bytes = series;
   return GLASS_OK;
 }
 

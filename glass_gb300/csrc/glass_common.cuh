@@ -87,29 +87,41 @@ __device__ __forceinline__ float df_reduce_2pi(df x) {
 
 // --------------------------------------------------------- per-item constants
 // Everything a waveform needs that does not depend on the sample index,
-// computed once per proposal (FP64) by the plan kernel.
-struct ItemConst {
-  int seg, N, imin, status;
-  // FP64 copy (plain path)
+// computed once per proposal (FP64) by the plan kernel.  The antenna-pattern
+// products of ucb/src/glass_ucb_waveform.c:896-897 are folded into two
+// symmetric tensors per proposal,
+//   Mr = DPr e+ + DCr ex,   Mi = DPi e+ + DCi ex,
+// so that dplus*DPr + dcross*DCr = r.Mr.r for an arm direction r.  Symmetric
+// tensors are stored as xx, xy, xz, yy, yz, zz.
+
+// Plain-FP64 path.
+struct ItemF64 {
+  int seg, N, imin, pad;
   double k[3];
-  double ep[6], ec[6];  // symmetric tensors: xx, xy, xz, yy, yz, zz
+  double ep[6], ec[6];        // polarisation tensors e+, ex
   double DPr, DPi, DCr, DCi;  // amplitude-free polarisation factors
-  double f0, fdot, eps, phi0, amp_s;  // eps = f0*T - q ; amp_s = amp/(2N)
-  double dfq;                         // 2 pi q / T (ucb/src/glass_ucb_waveform.c:818)
-  // FP32 / double-float copy (mixed path)
-  float kf[3];
-  float epf[6], ecf[6];
-  float DPrf, DPif, DCrf, DCif;
+  double f0, fdot, phi0, dfq;  // dfq = 2 pi q / T (ucb/src/glass_ucb_waveform.c:818)
+  double amp_s;               // amp / (2N)
+};
+
+// Mixed path: FP32 for everything but the carrier phase, which is carried as
+// double-float values.
+struct __align__(16) ItemMix {
+  int seg, N, imin, pad;
+  float k[4];                 // kx, ky, kz, 0
+  float Mr[6], Mi[6];
   float fonfs0;   // f0/f*
-  float fdfs;     // fdot*T/f*   : fonfs_i = fonfs0 + fdfs*(u - tau_i/T)
+  float fdfs;     // fdot*T/f*       : fonfs_i = fonfs0 + fdfs*(u - tau_i/T)
   float aef;      // (2/3)*fdot*T/f0 : aevol_i = 1 + aef*(u - tau_i/T)
   float w0c;      // 2 pi f0 / c
-  float p7pi;     // pi*fdot*T^2
-  float amp_sf;   // amp/(2N)
-  df eps2pi;      // 2 pi eps
+  float p7pi;     // pi*fdot*T^2 (small corrections)
+  float amp_hi, amp_lo;  // amp/(2N) = amp_hi + amp_lo
+  float pad2;
+  df eps2pi;      // 2 pi (f0 T - q)
   df beta1, beta2;  // 2 pi f0 AU/c * k_x, k_y
-  df phi0d;
-  df p7pid;       // pi*fdot*T^2
+  df phi0;
+  df p7pi_d;      // pi*fdot*T^2
+  df pad3;
 };
 
 // Per-sample orbit tables, one per waveform size.  Positions of the three

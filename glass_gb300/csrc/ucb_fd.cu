@@ -1,4 +1,5 @@
-// Fourier-domain UCB waveform and delta-logL kernels for sm_103a.
+// Fourier-domain UCB waveform and delta-logL kernels for sm_103a: plan,
+// tables, orchestration and the drop-in single-waveform path.
 //
 // The reference computes one template at a time on the CPU: ucb_waveform
 // (ucb/src/glass_ucb_waveform.c:738-1001) evaluates the slowly varying part of
@@ -7,44 +8,36 @@
 // gaussian_log_likelihood (utils/src/glass_model.c:726-774) then sums the
 // noise-weighted residual power over the whole segment.
 //
-// Here one group of threads owns one proposal and does all of it in one pass
-// without leaving the SM:
-//   1. slow part: each thread evaluates R of the N samples;
-//   2. the four arm combinations that the A and E channels need are formed in
-//      the time domain (the TDI sums are linear, so FFT(a - b) replaces
-//      FFT(a) - FFT(b)) and written to shared memory;
-//   3. four N-point radix-4/2 Stockham FFTs in shared memory;
-//   4. every output bin is multiplied by a per-segment-bin table that folds the
-//      TDI transfer factors, A/E combination and noise whitening, and the
-//      residual power over the template support is reduced to one number.
-// Only the template support is visited: logL(r - h) - logL(r) differs from
-// zero only there.
+// Here a batch of proposals of mixed sizes N (32..4096) is evaluated in three
+// steps on one stream:
+//   1. plan (one thread per proposal, FP64): the reference's bandwidth rule
+//      gives N, the alignment gives the template's first segment bin, and the
+//      per-proposal constants are prepared; proposals are binned by N;
+//   2. slow part (one thread per (proposal, sample), all sizes in one launch):
+//      the six arm responses, combined in the time domain into the four series
+//      whose FFTs make the A and E channels (the TDI sums are linear, so
+//      FFT(a - b) replaces FFT(a) - FFT(b)); written to an L2-resident scratch;
+//   3. per size, concurrently: four N-point radix-4/2 Stockham FFTs in shared
+//      memory, the per-segment-bin table folding TDI transfer factors, the A/E
+//      combination and noise whitening, and the residual power over the
+//      template support reduced to one number per proposal.
+// Only the template support is visited: logL(r - h) - logL(r) differs from zero
+// only there.
 //
-// Two precisions share the code: plain FP64, and a mixed form in which the
-// carrier phase is carried in double-float arithmetic (the guiding-centre
-// Doppler term reaches ~50 rad and needs ~1e-9 relative accuracy) and
-// everything else is FP32.
+// Two precisions share the structure: plain FP64 (this file and
+// ucb_fd_fp64.cu, compiled without multiply-add contraction), and a mixed form
+// (ucb_fd_mixed.cu) in which the carrier phase is carried in double-float
+// arithmetic and everything else is FP32.
 #include "ucb_fd_device.cuh"
 
 namespace glass {
 
-cudaError_t fd_launch_size_mixed(int N, const FdArgs &a, int nitems, int num_sms, cudaStream_t stream);
-cudaError_t fd_launch_size_fp64(int N, const FdArgs &a, int nitems, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
 
 // ------------------------------------------------------------- plan kernel
-struct PlanArgs {
-  int nitems, nseg, NFFT, cap;
-  double T, fstar, L;
-  const int *item_seg;
-  const double *params;
-  const double *term_x;
-  const int *seg_qmin;
-  ItemConst *items;
-  int *bin_count, *bin_list;
-  double *dlogl, *term_y, *hh;
-  int *status;
-};
-
 __global__ void fd_plan_kernel(PlanArgs a) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.nitems) return;
@@ -86,13 +79,25 @@ __global__ void fd_plan_kernel(PlanArgs a) {
     if (a.status) a.status[i] = 4;
     return;
   }
-  ItemConst c;
-  make_item_const(p, 8, a.T, a.fstar, N, c);
-  c.seg = seg;
-  c.N = N;
-  c.imin = imin;
-  c.status = 0;
-  a.items[i] = c;
+  SourceGeom g;
+  source_geometry(p, 8, a.T, g);
+  if (a.precision == 1) {
+    ItemMix c;
+    make_item_mix(g, N, a.T, a.fstar, c);
+    c.seg = seg;
+    c.N = N;
+    c.imin = imin;
+    c.pad = 0;
+    a.itemsmix[i] = c;
+  } else {
+    ItemF64 c;
+    make_item_f64(g, N, c);
+    c.seg = seg;
+    c.N = N;
+    c.imin = imin;
+    c.pad = 0;
+    a.items64[i] = c;
+  }
   int b = fd_bin_of(N);
   int pos = atomicAdd(&a.bin_count[b], 1);
   a.bin_list[(size_t)b * a.cap + pos] = i;
@@ -174,8 +179,8 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
 
 // ---------------------------------------------------------- host: bank tables
 void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
-                          const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *g32,
-                          double *Q, double2 *w64, double2 *g64) {
+                          const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *w32lo,
+                          float4 *g32, double *Q, double2 *w64, double2 *g64) {
   const double sqT = sqrt(T);
   for (int s = 0; s < nseg; s++) {
     double q = 0.0;
@@ -210,11 +215,16 @@ void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg
       g64[4 * sj + 1] = make_double2(GA1r, GA1i);
       g64[4 * sj + 2] = make_double2(GE2r, GE2i);
       g64[4 * sj + 3] = make_double2(GE1r, GE1i);
+      // The whitened data of a loud source reach |w| ~ 50 in its bins; rounded
+      // to float, their cross term with the template would carry ~1e-3 of
+      // error into delta logL, so the residual is kept as a double-float pair.
       float4 wf = make_float4((float)wAr, (float)wAi, (float)wEr, (float)wEi);
       w32[sj] = wf;
+      w32lo[sj] = make_float4((float)(wAr - (double)wf.x), (float)(wAi - (double)wf.y), (float)(wEr - (double)wf.z),
+                              (float)(wEi - (double)wf.w));
       g32[2 * sj] = make_float4((float)GA2r, (float)GA2i, (float)GA1r, (float)GA1i);
       g32[2 * sj + 1] = make_float4((float)GE2r, (float)GE2i, (float)GE1r, (float)GE1i);
-      q += (double)wf.x * wf.x + (double)wf.y * wf.y + (double)wf.z * wf.z + (double)wf.w * wf.w;
+      q += wAr * wAr + wAi * wAi + wEr * wEr + wEi * wEi;
       Q[(size_t)s * (NFFT + 1) + j + 1] = q;
     }
   }
@@ -227,6 +237,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
                             cudaStream_t stream, int *nlaunch) {
   cudaError_t e;
   int launches = 0;
+  const bool mix = precision == 1;
   e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kNumBins, stream);
   if (e != cudaSuccess) return e;
   PlanArgs pa;
@@ -234,6 +245,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.nseg = bank.nseg;
   pa.NFFT = bank.NFFT;
   pa.cap = work.cap;
+  pa.precision = precision;
   pa.T = bank.T;
   pa.fstar = bank.fstar;
   pa.L = kLARM;
@@ -241,26 +253,47 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.params = params;
   pa.term_x = term_x;
   pa.seg_qmin = bank.qmin;
-  pa.items = work.items;
+  pa.items64 = work.items64;
+  pa.itemsmix = work.itemsmix;
   pa.bin_count = work.bin_count;
   pa.bin_list = work.bin_list;
   pa.dlogl = dlogl;
   pa.term_y = term_y;
   pa.hh = hh;
   pa.status = status;
-  fd_plan_kernel<<<(nitems + 127) / 128, 128, 0, stream>>>(pa);
+  fd_plan_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(pa);
   launches++;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
 
-  FdArgs a;
+  SlowArgs sa;
+  sa.cap = work.cap;
+  sa.NFFT = bank.NFFT;
+  sa.fstar = bank.fstar;
+  sa.L = kLARM;
+  sa.R = kAU * (kLARM / (2.0 * kSQ3 * kAU));
+  sa.T = bank.T;
+  sa.bin_count = work.bin_count;
+  sa.bin_list = work.bin_list;
+  sa.items64 = work.items64;
+  sa.itemsmix = work.itemsmix;
+  for (int b = 0; b < kNumBins; b++) {
+    sa.pos64[b] = tab.pos64[b];
+    sa.mix[b] = tab.mix[b];
+  }
+  sa.series = work.series;
+  e = mix ? fd_launch_slow_mixed(sa, num_sms, stream) : fd_launch_slow_fp64(sa, num_sms, stream);
+  launches++;
+  if (e != cudaSuccess) return e;
+
+  SpecArgs a;
   a.NFFT = bank.NFFT;
-  a.T = bank.T;
-  a.fstar = bank.fstar;
-  a.L = kLARM;
-  a.R = kAU * (kLARM / (2.0 * kSQ3 * kAU));
-  a.items = work.items;
+  a.cap = work.cap;
   a.bin_count = work.bin_count;
+  a.items64 = work.items64;
+  a.itemsmix = work.itemsmix;
+  a.series = work.series;
   a.w32 = bank.w32;
+  a.w32lo = bank.w32lo;
   a.g32 = bank.g32;
   a.Q = bank.Q;
   a.w64 = bank.w64;
@@ -270,7 +303,6 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.term_y = term_y;
   a.hh = hh;
   a.status = status;
-  const bool mix = precision == 1;
   e = cudaEventRecord(work.fork, stream);
   if (e != cudaSuccess) return e;
   // every size a segment of NFFT bins can produce: 32 .. NFFT (ucb_bandwidth caps N at NFFT)
@@ -282,10 +314,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     if ((e = cudaStreamWaitEvent(sb, work.fork, 0)) != cudaSuccess) return e;
     a.bin = b;
     a.bin_list = work.bin_list + (size_t)b * work.cap;
-    a.pos64 = tab.pos64[b];
-    a.mix = tab.mix[b];
     a.tw = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
-    e = mix ? fd_launch_size_mixed(N, a, nitems, num_sms, sb) : fd_launch_size_fp64(N, a, nitems, num_sms, sb);
+    e = mix ? fd_launch_spec_mixed(N, a, nitems, num_sms, sb) : fd_launch_spec_fp64(N, a, nitems, num_sms, sb);
     launches++;
     if (e != cudaSuccess) return e;
     if ((e = cudaEventRecord(work.join[b], sb)) != cudaSuccess) return e;
@@ -297,32 +327,45 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   return cudaSuccess;
 }
 
+size_t fd_series_bytes(int nitems, int NFFT, int precision) {
+  size_t elem = precision == 1 ? sizeof(float2) : sizeof(double2);
+  return (size_t)nitems * (size_t)NFFT * 4 * elem;
+}
+
 // ------------------------------------------------------- legacy single waveform
 // One CTA per Michelson channel (X, Y, Z): slow part, the two FFTs the channel
 // needs, and the format's TDI weights per bin.  A and E follow in
 // fd_ae_kernel from the stored X, Y, Z (utils/src/glass_lisa.c:429-441).
 template <int N>
-__global__ void __launch_bounds__(FdCfg<N>::GT) fd_waveform_kernel(const OrbitSample64 *pos, const double *params,
+struct LegacyCfg {
+  static constexpr int R = (N <= 128) ? 4 : 8;  // samples per thread
+  static constexpr int GT = N / R;              // threads (one CTA per channel)
+};
+
+template <int N>
+__global__ void __launch_bounds__(LegacyCfg<N>::GT) fd_waveform_kernel(const OrbitSample64 *pos, const double *params,
                                                                     int NP, int format, double T, double fstar,
                                                                     double L, double *out, const double2 *twg) {
-  constexpr int GT = FdCfg<N>::GT, R = FdCfg<N>::R;
+  constexpr int GT = LegacyCfg<N>::GT, R = LegacyCfg<N>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2 *tw = reinterpret_cast<double2 *>(smem_raw);
   double2 *buf = tw + N;
-  __shared__ ItemConst c;
+  __shared__ ItemF64 c;
   const int lane = threadIdx.x, ch = blockIdx.x;
   for (int i = lane; i < N; i += GT) tw[i] = twg[i];
   if (lane == 0) {
     double p[8];
     for (int k = 0; k < 8; k++) p[k] = k < NP ? params[k] : 0.0;
-    make_item_const(p, NP, T, fstar, N, c);
+    SourceGeom geo;
+    source_geometry(p, NP, T, geo);
+    make_item_f64(geo, N, c);
   }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int n = lane + GT * r;
     double2 d[6];
-    slow_sample64(c, pos[n], T, fstar, L, d);
+    slow_sample64(c, pos[n], fstar, L, d);
     // d: 12, 13, 21, 23, 31, 32 ; X: (12-13, 21-31), Y: (23-21, 32-12), Z: (31-32, 13-23)
     double2 u, v;
     if (ch == 0) {
@@ -397,7 +440,7 @@ static cudaError_t launch_waveform(const OrbitSample64 *pos, const double *param
     if (e != cudaSuccess) return e;
     init = true;
   }
-  fd_waveform_kernel<N><<<nch, FdCfg<N>::GT, smem, stream>>>(pos, params, NP, format, T, fstar, kLARM, out, tw);
+  fd_waveform_kernel<N><<<nch, LegacyCfg<N>::GT, smem, stream>>>(pos, params, NP, format, T, fstar, kLARM, out, tw);
   return cudaGetLastError();
 }
 

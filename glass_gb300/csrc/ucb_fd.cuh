@@ -11,9 +11,10 @@ struct FdBankDev {
   int nseg = 0, NFFT = 0, format = 0;
   double T = 0, t0 = 0, fstar = 0;
   int *qmin = nullptr;         // [nseg]
-  float4 *w32 = nullptr;       // [nseg*NFFT]   whitened residual {A.re, A.im, E.re, E.im}
+  float4 *w32 = nullptr;       // [nseg*NFFT]   whitened residual {A.re, A.im, E.re, E.im}, rounded to float
+  float4 *w32lo = nullptr;     // [nseg*NFFT]   residual minus its float rounding (double-float pair with w32)
   float4 *g32 = nullptr;       // [nseg*NFFT*2] {GA2, GA1}, {GE2, GE1}
-  double *Q = nullptr;         // [nseg*(NFFT+1)] prefix sums of |w32|^2 over both channels
+  double *Q = nullptr;         // [nseg*(NFFT+1)] prefix sums of |w|^2 over both channels (FP64)
   double2 *w64 = nullptr;      // [nseg*NFFT*2] {A}, {E}
   double2 *g64 = nullptr;      // [nseg*NFFT*4] GA2, GA1, GE2, GE1
 };
@@ -29,21 +30,24 @@ struct FdTablesDev {
 
 // Scratch of one batched evaluation.
 struct FdWorkDev {
-  // per-size streams forked from the caller's stream after the plan kernel, so
-  // that the size kernels run concurrently (and become parallel branches when
-  // the caller captures a CUDA graph)
+  // per-size streams forked from the caller's stream after the slow-part
+  // kernel, so that the per-size spectral kernels run concurrently (and become
+  // parallel branches when the caller captures a CUDA graph)
   cudaStream_t side[kNumBins] = {};
   cudaEvent_t fork = nullptr, join[kNumBins] = {};
-  int cap = 0;
-  ItemConst *items = nullptr;  // [cap]
-  int *bin_count = nullptr;    // [kNumBins]
-  int *bin_list = nullptr;     // [kNumBins*cap]
+  int cap = 0;                  // proposals
+  size_t series_bytes = 0;      // capacity of `series`
+  ItemF64 *items64 = nullptr;   // [cap]
+  ItemMix *itemsmix = nullptr;  // [cap]
+  int *bin_count = nullptr;     // [kNumBins]
+  int *bin_list = nullptr;      // [kNumBins*cap]
+  void *series = nullptr;       // 4 arm-combination series per proposal
 };
 
 // Host-side table construction for a bank: G and w tables, prefix sums.
 void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
-                          const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *g32,
-                          double *Q, double2 *w64, double2 *g64);
+                          const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *w32lo,
+                          float4 *g32, double *Q, double2 *w64, double2 *g64);
 
 cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStream_t stream);
 
@@ -53,6 +57,10 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
                             int nitems, const int *item_seg, const double *params, const double *term_x,
                             double *dlogl, double *term_y, double *hh, int *status, int num_sms,
                             cudaStream_t stream, int *nlaunch);
+
+// Bytes of series scratch a batch of nitems proposals on segments of NFFT bins
+// can need (every N is at most NFFT).
+size_t fd_series_bytes(int nitems, int NFFT, int precision);
 
 // Single waveform in the reference's output layout (legacy ucb_waveform).
 // pos: N orbit samples (device), out: 10*N doubles (device) = X,Y,Z,A,E.

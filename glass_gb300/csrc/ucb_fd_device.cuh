@@ -10,16 +10,7 @@
 
 namespace glass {
 
-
-template <int N>
-struct FdCfg {
-  static constexpr int R = (N <= 128) ? 4 : 8;  // samples (and bins) per thread
-  static constexpr int GT = N / R;              // threads per proposal
-  static constexpr int CTA = (GT >= 64) ? GT : 128;
-  static constexpr int GPC = CTA / GT;          // proposals per CTA
-  static constexpr int LOG = (N == 32) ? 5 : (N == 64) ? 6 : (N == 128) ? 7 : (N == 256) ? 8
-                           : (N == 512) ? 9 : (N == 1024) ? 10 : (N == 2048) ? 11 : 12;
-};
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 __host__ __device__ constexpr int fd_bin_of(int N) {
   return N == 32 ? 0 : N == 64 ? 1 : N == 128 ? 2 : N == 256 ? 3 : N == 512 ? 4 : N == 1024 ? 5 : N == 2048 ? 6 : 7;
@@ -70,7 +61,7 @@ __device__ __forceinline__ void group_sync() {
 // bound register use.
 template <int N, int GT, int NSER, int CH, typename C, int SYNC_GT = GT>
 __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
-  constexpr int LOG = FdCfg<N>::LOG;
+  constexpr int LOG = ilog2c(N);
   constexpr int NR4 = LOG / 2;
   constexpr int B4 = N / 4 / GT;
   static_assert(B4 >= 1, "group too large for radix-4 stages");
@@ -153,9 +144,9 @@ static __device__ double aenoise_dev(double f, double L, double fstar) {
   double red = 1. + 16.0 * (pow((2.0e-5 / f), 10.0) + r * r);
   double w = kPI2 * f;
   double w4 = w * w * w * w;
+  double cf = cos(fonfstar);
   return (16.0 / 3.0) * trans *
-         ((2.0 + cos(fonfstar)) * (kSPS + kSLOC) +
-          2.0 * (3.0 + 2.0 * cos(fonfstar) + cos(2.0 * fonfstar)) * (kSLOC / 2.0 + kSACC / w4 * red)) /
+         ((2.0 + cf) * (kSPS + kSLOC) + 2.0 * (3.0 + 2.0 * cf + cos(2.0 * fonfstar)) * (kSLOC / 2.0 + kSACC / w4 * red)) /
          ((2.0 * L) * (2.0 * L));
 }
 
@@ -169,8 +160,8 @@ __device__ __forceinline__ int pow2_above_dev(double v) {
 }
 
 // ucb/src/glass_ucb_waveform.c:698-725 (ucb_bandwidth).
-static __device__ int bandwidth_dev(double L, double fstar, double f, double fdot, double costheta, double A, double T,
-                             int NFFT) {
+static __device__ int bandwidth_dev(double L, double fstar, double f, double fdot, double costheta, double A,
+                                    double T, int NFFT) {
   const int Nmin = 16;
   int half = NFFT / 2;
   int Nmax = half >= 1 ? (1 << (31 - __clz(half))) : 0;
@@ -189,62 +180,87 @@ static __device__ int bandwidth_dev(double L, double fstar, double f, double fdo
   return (DS > SS) ? DS : SS;
 }
 
-// Per-proposal constants (ucb/src/glass_ucb_waveform.c:802-838 and
-// utils/src/glass_lisa.c:1566-1596), amplitude factored out as amp/(2N).
-static __device__ void make_item_const(const double *p, int NP, double T, double fstar, int N, ItemConst &c) {
-  double f0 = p[0] / T, costh = p[1], phi = p[2], amp = exp(p[3]), cosi = p[4], psi = p[5], phi0 = p[6];
-  double fdot = NP > 7 ? p[7] / (T * T) : 0.0;
+// Source geometry shared by both precisions (ucb/src/glass_ucb_waveform.c:802-838,
+// utils/src/glass_lisa.c:1566-1596).
+struct SourceGeom {
+  double f0, fdot, phi0, amp, eps, dfq;
+  double k[3], ep[6], ec[6];
+  double DPr, DPi, DCr, DCi;
+};
+
+static __device__ void source_geometry(const double *p, int NP, double T, SourceGeom &g) {
+  double f0 = p[0] / T, costh = p[1], phi = p[2], cosi = p[4], psi = p[5];
+  g.f0 = f0;
+  g.amp = exp(p[3]);
+  g.phi0 = p[6];
+  g.fdot = NP > 7 ? p[7] / (T * T) : 0.0;
   double fT = f0 * T;
   long long q = (long long)fT;
-  c.eps = fT - (double)q;
-  c.dfq = kPI2 * (((double)q) / T);
+  g.eps = fT - (double)q;
+  g.dfq = kPI2 * (((double)q) / T);
   double sinps, cosps;
   sincos(2. * psi, &sinps, &cosps);
   double Aplus = (1. + cosi * cosi) * 0.5, Across = -cosi;
-  c.DPr = Aplus * cosps;
-  c.DPi = -Across * sinps;
-  c.DCr = -Aplus * sinps;
-  c.DCi = -Across * cosps;
+  g.DPr = Aplus * cosps;
+  g.DPi = -Across * sinps;
+  g.DCr = -Aplus * sinps;
+  g.DCi = -Across * cosps;
   double sinth = sqrt(1.0 - costh * costh);
   double sinph, cosph;
   sincos(phi, &sinph, &cosph);
   double u[3] = {costh * cosph, costh * sinph, -sinth};
   double v[3] = {sinph, -cosph, 0.};
-  c.k[0] = -sinth * cosph;
-  c.k[1] = -sinth * sinph;
-  c.k[2] = -costh;
+  g.k[0] = -sinth * cosph;
+  g.k[1] = -sinth * sinph;
+  g.k[2] = -costh;
   int idx = 0;
   for (int i = 0; i < 3; i++)
     for (int j = i; j < 3; j++, idx++) {
-      c.ep[idx] = v[i] * v[j] - u[i] * u[j];
-      c.ec[idx] = u[i] * v[j] + v[i] * u[j];
+      g.ep[idx] = v[i] * v[j] - u[i] * u[j];
+      g.ec[idx] = u[i] * v[j] + v[i] * u[j];
     }
-  c.f0 = f0;
-  c.fdot = fdot;
-  c.phi0 = phi0;
-  c.amp_s = amp / (2.0 * (double)N);
-  // mixed-precision copy
-  for (int i = 0; i < 3; i++) c.kf[i] = (float)c.k[i];
+}
+
+static __device__ void make_item_f64(const SourceGeom &g, int N, ItemF64 &c) {
+  for (int i = 0; i < 3; i++) c.k[i] = g.k[i];
   for (int i = 0; i < 6; i++) {
-    c.epf[i] = (float)c.ep[i];
-    c.ecf[i] = (float)c.ec[i];
+    c.ep[i] = g.ep[i];
+    c.ec[i] = g.ec[i];
   }
-  c.DPrf = (float)c.DPr;
-  c.DPif = (float)c.DPi;
-  c.DCrf = (float)c.DCr;
-  c.DCif = (float)c.DCi;
-  c.fonfs0 = (float)(f0 / fstar);
-  c.fdfs = (float)(fdot * T / fstar);
-  c.aef = (float)(0.66666666666666666666 * fdot * T / f0);
-  c.w0c = (float)(kPI2 * f0 / kCLIGHT);
-  c.p7pi = (float)(kPI * fdot * T * T);
-  c.amp_sf = (float)c.amp_s;
-  c.eps2pi = df_from_double(kPI2 * c.eps);
-  double bscale = kPI2 * f0 * (kAU / kCLIGHT);
-  c.beta1 = df_from_double(bscale * c.k[0]);
-  c.beta2 = df_from_double(bscale * c.k[1]);
-  c.phi0d = df_from_double(phi0);
-  c.p7pid = df_from_double(kPI * fdot * T * T);
+  c.DPr = g.DPr;
+  c.DPi = g.DPi;
+  c.DCr = g.DCr;
+  c.DCi = g.DCi;
+  c.f0 = g.f0;
+  c.fdot = g.fdot;
+  c.phi0 = g.phi0;
+  c.dfq = g.dfq;
+  c.amp_s = g.amp / (2.0 * (double)N);
+}
+
+static __device__ void make_item_mix(const SourceGeom &g, int N, double T, double fstar, ItemMix &c) {
+  for (int i = 0; i < 3; i++) c.k[i] = (float)g.k[i];
+  c.k[3] = 0.f;
+  for (int i = 0; i < 6; i++) {
+    c.Mr[i] = (float)(g.DPr * g.ep[i] + g.DCr * g.ec[i]);
+    c.Mi[i] = (float)(g.DPi * g.ep[i] + g.DCi * g.ec[i]);
+  }
+  c.fonfs0 = (float)(g.f0 / fstar);
+  c.fdfs = (float)(g.fdot * T / fstar);
+  c.aef = (float)(0.66666666666666666666 * g.fdot * T / g.f0);
+  c.w0c = (float)(kPI2 * g.f0 / kCLIGHT);
+  c.p7pi = (float)(kPI * g.fdot * T * T);
+  double s = g.amp / (2.0 * (double)N);
+  c.amp_hi = (float)s;
+  c.amp_lo = (float)(s - (double)c.amp_hi);
+  c.pad2 = 0.f;
+  c.eps2pi = df_from_double(kPI2 * g.eps);
+  double bscale = kPI2 * g.f0 * (kAU / kCLIGHT);
+  c.beta1 = df_from_double(bscale * g.k[0]);
+  c.beta2 = df_from_double(bscale * g.k[1]);
+  c.phi0 = df_from_double(g.phi0);
+  c.p7pi_d = df_from_double(kPI * g.fdot * T * T);
+  c.pad3 = {0.f, 0.f};
 }
 
 // ----------------------------------------------------------------- slow part
@@ -256,8 +272,7 @@ __device__ __forceinline__ R quad(const R *e, R x, R y, R z) {
 
 // sin(x)/x: Taylor series through x^12 for |x| <= 1 (truncation < 1e-12).
 __device__ __forceinline__ float sinc_f(float x) {
-  float ax = fabsf(x);
-  if (ax > 1.0f) return sinf(x) / x;
+  if (fabsf(x) > 1.0f) return sinf(x) / x;
   float x2 = x * x;
   float s = 1.6059043836821613e-10f;          // 1/13!
   s = fmaf(s, x2, -2.505210838544172e-08f);   // -1/11!
@@ -271,11 +286,11 @@ __device__ __forceinline__ float sinc_f(float x) {
 // The six arm series d_ij at one sample (order 12, 13, 21, 23, 31, 32),
 // amplitude-free, in FP64 with the reference's own sequence of operations
 // (ucb/src/glass_ucb_waveform.c:840-922).  The carrier argument arg2 reaches
-// ~1e6 rad, where every rounding step is worth ~1e-10 rad; this translation
-// unit is compiled without multiply-add contraction so that those roundings
-// are the reference's.
-__device__ __forceinline__ void slow_sample64(const ItemConst &c, const OrbitSample64 &o, double T, double fstar,
-                                              double L, double2 d[6]) {
+// ~1e6 rad, where every rounding step is worth ~1e-10 rad; the translation
+// units that use this are compiled without multiply-add contraction so that
+// those roundings are the reference's.
+__device__ __forceinline__ void slow_sample64(const ItemF64 &c, const OrbitSample64 &o, double fstar, double L,
+                                              double2 d[6]) {
   double r12[3] = {(o.x[1] - o.x[0]) / L, (o.y[1] - o.y[0]) / L, (o.z[1] - o.z[0]) / L};
   double r13[3] = {(o.x[2] - o.x[0]) / L, (o.y[2] - o.y[0]) / L, (o.z[2] - o.z[0]) / L};
   double r23[3] = {(o.x[2] - o.x[1]) / L, (o.y[2] - o.y[1]) / L, (o.z[2] - o.z[1]) / L};
@@ -316,10 +331,10 @@ __device__ __forceinline__ void slow_sample64(const ItemConst &c, const OrbitSam
 }
 
 // Mixed precision: the carrier phase common to the three spacecraft
-// (heterodyne, guiding-centre Doppler, phi0 and the fdot t^2 term) is summed in
-// double-float and reduced mod 2 pi; the per-spacecraft corrections (< 0.5 rad)
-// and everything else are FP32.
-__device__ __forceinline__ void slow_sample_mix(const ItemConst &c, const OrbitSampleMix &o, float Rorb, float invL,
+// (heterodyne 2 pi (f0 T - q) t/T, guiding-centre Doppler 2 pi f0 k.x_gc/c,
+// phi0 and pi fdot t^2) is summed in double-float and reduced mod 2 pi; the
+// per-spacecraft corrections (< 0.5 rad) and everything else are FP32.
+__device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSampleMix &o, float Rorb, float invL,
                                                 float AUc, float invT, float2 d[6]) {
   const float ca = o.ca_hi, sa = o.sa_hi;
   const float sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
@@ -335,28 +350,28 @@ __device__ __forceinline__ void slow_sample_mix(const ItemConst &c, const OrbitS
   float r12[3] = {(dx[1] - dx[0]) * invL, (dy[1] - dy[0]) * invL, (dz[1] - dz[0]) * invL};
   float r13[3] = {(dx[2] - dx[0]) * invL, (dy[2] - dy[0]) * invL, (dz[2] - dz[0]) * invL};
   float r23[3] = {(dx[2] - dx[1]) * invL, (dy[2] - dy[1]) * invL, (dz[2] - dz[1]) * invL};
-  float dp12 = quad(c.epf, r12[0], r12[1], r12[2]), dc12 = quad(c.ecf, r12[0], r12[1], r12[2]);
-  float dp13 = quad(c.epf, r13[0], r13[1], r13[2]), dc13 = quad(c.ecf, r13[0], r13[1], r13[2]);
-  float dp23 = quad(c.epf, r23[0], r23[1], r23[2]), dc23 = quad(c.ecf, r23[0], r23[1], r23[2]);
-  float kr12 = c.kf[0] * r12[0] + c.kf[1] * r12[1] + c.kf[2] * r12[2];
-  float kr13 = c.kf[0] * r13[0] + c.kf[1] * r13[1] + c.kf[2] * r13[2];
-  float kr23 = c.kf[0] * r23[0] + c.kf[1] * r23[1] + c.kf[2] * r23[2];
+  const float mr12 = quad(c.Mr, r12[0], r12[1], r12[2]), mi12 = quad(c.Mi, r12[0], r12[1], r12[2]);
+  const float mr13 = quad(c.Mr, r13[0], r13[1], r13[2]), mi13 = quad(c.Mi, r13[0], r13[1], r13[2]);
+  const float mr23 = quad(c.Mr, r23[0], r23[1], r23[2]), mi23 = quad(c.Mi, r23[0], r23[1], r23[2]);
+  const float kr12 = c.k[0] * r12[0] + c.k[1] * r12[1] + c.k[2] * r12[2];
+  const float kr13 = c.k[0] * r13[0] + c.k[1] * r13[1] + c.k[2] * r13[2];
+  const float kr23 = c.k[0] * r23[0] + c.k[1] * r23[1] + c.k[2] * r23[2];
 
   // common carrier phase in double-float
-  df u = {o.u_hi, o.u_lo};
-  df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
+  const df u = {o.u_hi, o.u_lo};
+  const df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
   df ph = df_mul(c.eps2pi, u);
   ph = df_add(ph, df_neg(df_add(df_mul(c.beta1, cad), df_mul(c.beta2, sad))));
-  ph = df_add(ph, df_neg(c.phi0d));
-  ph = df_add(ph, df_mul(c.p7pid, df_mul(u, u)));
+  ph = df_add(ph, df_neg(c.phi0));
+  ph = df_add(ph, df_mul(c.p7pi_d, df_mul(u, u)));
   const float psi0 = df_reduce_2pi(ph);
   const float uf = o.u_hi;
-  const float tgc = AUc * (c.kf[0] * ca + c.kf[1] * sa);  // guiding-centre delay (s)
+  const float tgc = AUc * (c.k[0] * ca + c.k[1] * sa);  // guiding-centre delay (s)
 
   float fon[3], arg2[3], aev[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    float kdx = c.kf[0] * dx[i] + c.kf[1] * dy[i] + c.kf[2] * dz[i];  // k.(x_i - x_gc), metres
+    float kdx = c.k[0] * dx[i] + c.k[1] * dy[i] + c.k[2] * dz[i];  // k.(x_i - x_gc), metres
     float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
     float tT = taui * invT;
     float v = uf - tT;  // xi / T
@@ -365,16 +380,16 @@ __device__ __forceinline__ void slow_sample_mix(const ItemConst &c, const OrbitS
     arg2[i] = psi0 - c.w0c * kdx + c.p7pi * tT * (tT - 2.0f * uf);
   }
   const int ai[6] = {0, 0, 1, 1, 2, 2};
-  const float dps[6] = {dp12, dp13, dp12, dp23, dp13, dp23};
-  const float dcs[6] = {dc12, dc13, dc12, dc23, dc13, dc23};
+  const float mrs[6] = {mr12, mr13, mr12, mr23, mr13, mr23};
+  const float mis[6] = {mi12, mi13, mi12, mi23, mi13, mi23};
   const float krs[6] = {kr12, kr13, -kr12, kr23, -kr13, -kr23};
 #pragma unroll
   for (int a = 0; a < 6; a++) {
     int i = ai[a];
     float arg1 = 0.5f * fon[i] * (1.0f + krs[a]);
     float sinc = 0.25f * sinc_f(arg1);
-    float t1r = aev[i] * (dps[a] * c.DPrf + dcs[a] * c.DCrf);
-    float t1i = aev[i] * (dps[a] * c.DPif + dcs[a] * c.DCif);
+    float t1r = aev[i] * mrs[a];
+    float t1i = aev[i] * mis[a];
     float s2, c2;
     sincosf(arg1 - arg2[i], &s2, &c2);
     d[a] = make_float2(sinc * (t1r * c2 + t1i * s2), sinc * (-t1r * s2 + t1i * c2));
@@ -395,17 +410,45 @@ __device__ __forceinline__ void ae_combos(const C d[6], C out[4]) {
   out[3] = cadd(csub(csub(cadd(d13, d21), d23), d31), cscale(csub(d12, d32), 2));    // e1
 }
 
-// ---------------------------------------------------------- main kernel
-struct FdArgs {
-  int NFFT;
-  double T, fstar, L, R;
-  const ItemConst *items;
+// ------------------------------------------------------------- kernel args
+struct PlanArgs {
+  int nitems, nseg, NFFT, cap, precision;
+  double T, fstar, L;
+  const int *item_seg;
+  const double *params;
+  const double *term_x;
+  const int *seg_qmin;
+  ItemF64 *items64;
+  ItemMix *itemsmix;
+  int *bin_count, *bin_list;
+  double *dlogl, *term_y, *hh;
+  int *status;
+};
+
+// Stage 1: slow part of every (proposal, sample) pair, written to scratch as the
+// four arm-combination series of each proposal.
+struct SlowArgs {
+  int cap, NFFT;
+  double fstar, L, R, T;
+  const int *bin_count, *bin_list;
+  const ItemF64 *items64;
+  const ItemMix *itemsmix;
+  const OrbitSample64 *pos64[kNumBins];
+  const OrbitSampleMix *mix[kNumBins];
+  void *series;  // float2 (mixed) or double2 (FP64)
+};
+
+// Stage 2: FFTs, TDI weights, whitening and the residual power, per size.
+struct SpecArgs {
+  int NFFT, cap, bin;
   const int *bin_count;
   const int *bin_list;  // this size's list
-  const OrbitSample64 *pos64;
-  const OrbitSampleMix *mix;
+  const ItemF64 *items64;
+  const ItemMix *itemsmix;
+  const void *series;
   const void *tw;
   const float4 *w32;
+  const float4 *w32lo;
   const float4 *g32;
   const double *Q;
   const double2 *w64;
@@ -413,20 +456,86 @@ struct FdArgs {
   const double *term_x;
   double *dlogl, *term_y, *hh;
   int *status;
-  int bin;
+};
+
+// Position of proposal slot `slot` of size bin b in the scratch series, in
+// samples: sizes are laid out in increasing order, proposals of one size back to
+// back, each holding 4 series of N samples.
+__device__ __forceinline__ void sample_offsets(const int *bin_count, int nbins, long long *start) {
+  long long acc = 0;
+#pragma unroll
+  for (int b = 0; b < kNumBins; b++) {
+    start[b] = acc;
+    if (b < nbins) acc += (long long)bin_count[b] * (32 << b);
+  }
+}
+
+// ------------------------------------------------------- stage 1 (templated)
+// One warp per 32 consecutive samples of one proposal (every N is a multiple
+// of 32), grid-stride over all proposals of every size.
+template <bool MIX>
+__global__ void __launch_bounds__(256) fd_slow_kernel(SlowArgs a) {
+  using C = typename std::conditional<MIX, float2, double2>::type;
+  int nbins = 0;
+  while (nbins < kNumBins && (32 << nbins) <= a.NFFT) nbins++;
+  int cnt[kNumBins];
+  long long cstart[kNumBins + 1];  // chunk offsets per size
+  long long acc = 0;
+#pragma unroll
+  for (int b = 0; b < kNumBins; b++) {
+    cnt[b] = b < nbins ? a.bin_count[b] : 0;
+    cstart[b] = acc;
+    acc += (long long)cnt[b] * (1 << b);  // chunks of 32 samples: N/32 = 2^b
+  }
+  cstart[kNumBins] = acc;
+  const long long nchunks = acc;
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  C *series = reinterpret_cast<C *>(a.series);
+  const float Rf = (float)a.R, invLf = (float)(1.0 / a.L), AUcf = (float)(kAU / kCLIGHT), invTf = (float)(1.0 / a.T);
+#pragma unroll 1
+  for (long long ch = warp; ch < nchunks; ch += nwarps) {
+    int b = 0;
+#pragma unroll
+    for (int bb = 1; bb < kNumBins; bb++)
+      if (ch >= cstart[bb]) b = bb;
+    const int N = 32 << b;
+    const long long local = ch - cstart[b];
+    const int slot = (int)(local >> b);
+    const int n = (int)((local & ((1 << b) - 1)) << 5) + lane;
+    const int item = a.bin_list[(size_t)b * a.cap + slot];
+    C d[6], cmb[4];
+    if constexpr (MIX) {
+      slow_sample_mix(a.itemsmix[item], a.mix[b][n], Rf, invLf, AUcf, invTf, d);
+    } else {
+      slow_sample64(a.items64[item], a.pos64[b][n], a.fstar, a.L, d);
+    }
+    ae_combos(d, cmb);
+    C *out = series + (cstart[b] * 32 + (long long)slot * N) * 4 + n;
+#pragma unroll
+    for (int s = 0; s < 4; s++) out[(size_t)s * N] = cmb[s];
+  }
+}
+
+// ------------------------------------------------------- stage 2 (templated)
+template <int N>
+struct SpecCfg {
+  static constexpr int GT = N / 4;  // one radix-4 butterfly per series per thread
+  static constexpr int CTA = GT >= 64 ? GT : 128;
+  static constexpr int GPC = CTA / GT;
 };
 
 template <int N, bool MIX>
-struct FdSmem {
+struct SpecSmem {
   using C = typename std::conditional<MIX, float2, double2>::type;
   static constexpr int NSER = (!MIX && N == 4096) ? 2 : 4;  // series resident at once
   static constexpr int PASSES = 4 / NSER;
-  static constexpr int GPC = FdCfg<N>::GPC;
-  static constexpr size_t bytes = sizeof(C) * (size_t)N * (1 + (size_t)GPC * NSER) + sizeof(double) * 2 * 32;
+  static constexpr size_t bytes =
+      sizeof(C) * (size_t)N * (1 + (size_t)SpecCfg<N>::GPC * NSER) + sizeof(double) * 3 * 32;
 };
 
-// Sum over the threads of one group (result valid in every lane for GT <= 32,
-// in lane 0 otherwise).
+// Sum over the threads of one group (result valid in lane 0 of the group).
 template <int GT>
 __device__ __forceinline__ double group_sum(double v, double *red, int lane) {
 #pragma unroll
@@ -445,12 +554,13 @@ __device__ __forceinline__ double group_sum(double v, double *red, int lane) {
 }
 
 template <int N, bool MIX>
-__global__ void __launch_bounds__(FdCfg<N>::CTA) fd_dlogl_kernel(FdArgs a) {
-  using Cfg = FdCfg<N>;
-  using S = FdSmem<N, MIX>;
+__global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
+  using Cfg = SpecCfg<N>;
+  using S = SpecSmem<N, MIX>;
   using C = typename S::C;
-  constexpr int GT = Cfg::GT, R = Cfg::R, GPC = Cfg::GPC, NSER = S::NSER, PASSES = S::PASSES;
-  constexpr int CH = MIX ? 4 : ((R == 4) ? 2 : 1);
+  constexpr int GT = Cfg::GT, GPC = Cfg::GPC, NSER = S::NSER, PASSES = S::PASSES;
+  constexpr int CH = MIX ? 4 : 2;
+  constexpr int B = N / GT;  // bins per thread (4)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *bufs = tw + N;
@@ -463,57 +573,61 @@ __global__ void __launch_bounds__(FdCfg<N>::CTA) fd_dlogl_kernel(FdArgs a) {
   const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
   C *buf = bufs + (size_t)g * NSER * N;
   const int count = a.bin_count[a.bin];
+  long long start[kNumBins];
+  int nbins = 0;
+  while (nbins < kNumBins && (32 << nbins) <= a.NFFT) nbins++;
+  sample_offsets(a.bin_count, nbins, start);
+  const C *series = reinterpret_cast<const C *>(a.series) + start[a.bin] * 4;
   const int NFFT = a.NFFT;
-  const float Rf = (float)a.R, invLf = (float)(1.0 / a.L), AUcf = (float)(kAU / kCLIGHT), invTf = (float)(1.0 / a.T);
 
   for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC) {
     const int slot = base + g;
     const bool valid = slot < count;
-    const int item = a.bin_list[valid ? slot : count - 1];
-    const ItemConst &c = a.items[item];
-    const int seg = c.seg, imin = c.imin;
-
+    const int sl = valid ? slot : count - 1;
+    const int item = a.bin_list[sl];
+    int seg, imin;
+    if constexpr (MIX) {
+      seg = a.itemsmix[item].seg;
+      imin = a.itemsmix[item].imin;
+    } else {
+      seg = a.items64[item].seg;
+      imin = a.items64[item].imin;
+    }
+    const C *src = series + (size_t)sl * 4 * N;
+    float facc = 0.f, fh = 0.f, fc = 0.f;  // mixed: per-thread partial sums
     double acc = 0.0, hacc = 0.0;
 #pragma unroll 1
     for (int pass = 0; pass < PASSES; ++pass) {
-      // 1-2. slow part and arm combinations
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int n = lane + GT * r;
-        C dd[6], cmb[4];
-        if constexpr (MIX) {
-          slow_sample_mix(c, a.mix[n], Rf, invLf, AUcf, invTf, dd);
-        } else {
-          slow_sample64(c, a.pos64[n], a.T, a.fstar, a.L, dd);
-        }
-        ae_combos(dd, cmb);
+      for (int s = 0; s < NSER; ++s)
 #pragma unroll
-        for (int s = 0; s < NSER; ++s) buf[s * N + n] = cmb[pass * NSER + s];
-      }
+        for (int r = 0; r < B; ++r) buf[s * N + lane + GT * r] = src[(size_t)(pass * NSER + s) * N + lane + GT * r];
       group_sync<GT>();
-      // 3. FFTs
       group_fft<N, GT, NSER, (CH < NSER ? CH : NSER)>(buf, tw, lane);
-      // 4. TDI weights, whitening and residual power over the support
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
+      for (int r = 0; r < B; ++r) {
         const int k = lane + GT * r;
-        const int m = (k + N / 2) & (N - 1);
+        const int m = (k + N / 2) & (N - 1);  // fftshift: output bin m holds FFT index m + N/2
         const int j = imin + m;
         if (j < 0 || j >= NFFT) continue;
         const size_t sj = (size_t)seg * NFFT + j;
         if constexpr (MIX) {
           const float4 w = a.w32[sj];
           const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
-          const float s = c.amp_sf;
-          float2 hA = cadd(cmul(buf[0 * N + k], make_float2(gA.x, gA.y)), cmul(buf[1 * N + k], make_float2(gA.z, gA.w)));
-          float2 hE = cadd(cmul(buf[2 * N + k], make_float2(gE.x, gE.y)), cmul(buf[3 * N + k], make_float2(gE.z, gE.w)));
-          hA = cscale(hA, s);
-          hE = cscale(hE, s);
-          float ar = w.x - hA.x, ai = w.y - hA.y, er = w.z - hE.x, ei = w.w - hE.y;
-          acc += (double)(fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei));
-          hacc += (double)(fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y));
+          const float sh = a.itemsmix[item].amp_hi;
+          float2 HA = cadd(cmul(buf[0 * N + k], make_float2(gA.x, gA.y)), cmul(buf[1 * N + k], make_float2(gA.z, gA.w)));
+          float2 HE = cadd(cmul(buf[2 * N + k], make_float2(gE.x, gE.y)), cmul(buf[3 * N + k], make_float2(gE.z, gE.w)));
+          // template scaled by amp_hi (O(1) whitened values; the unscaled
+          // product would overflow FP32 when squared)
+          const float2 hA = cscale(HA, sh), hE = cscale(HE, sh);
+          const float4 wl = a.w32lo[sj];
+          const float ar = (w.x - hA.x) + wl.x, ai = (w.y - hA.y) + wl.y;
+          const float er = (w.z - hE.x) + wl.z, ei = (w.w - hE.y) + wl.w;
+          facc += fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei);
+          fh += fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y);
+          fc += fmaf(ar, hA.x, ai * hA.y) + fmaf(er, hE.x, ei * hE.y);
         } else {
-          const double s = c.amp_s;
+          const double s = a.items64[item].amp_s;
           // series (2 ch, 2 ch + 1) of this pass hold the A (chan 0) or E (chan 1) pair
 #pragma unroll
           for (int ch = 0; ch < NSER / 2; ++ch) {
@@ -529,41 +643,53 @@ __global__ void __launch_bounds__(FdCfg<N>::CTA) fd_dlogl_kernel(FdArgs a) {
       }
       group_sync<GT>();
     }
-    acc = group_sum<GT>(acc, red, lane);
-    hacc = group_sum<GT>(hacc, red + 16, lane);
+    double corr = 0.0;
+    if constexpr (MIX) {
+      acc = group_sum<GT>((double)facc, red, lane);
+      hacc = group_sum<GT>((double)fh, red + 32, lane);
+      corr = group_sum<GT>((double)fc, red + 64, lane);
+    } else {
+      acc = group_sum<GT>(acc, red, lane);
+      hacc = group_sum<GT>(hacc, red + 32, lane);
+    }
     if (valid && lane == 0) {
-      double term;
+      double term, hh;
       if constexpr (MIX) {
+        const ItemMix &c = a.itemsmix[item];
         int jlo = imin < 0 ? 0 : imin;
         int jhi = imin + N > NFFT ? NFFT : imin + N;
         const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
-        term = (Qs[jhi] - Qs[jlo]) - acc;
+        // sum |w - s H|^2 with s = amp_hi (1 + rho), rho = amp_lo/amp_hi: with
+        // d = w - amp_hi H, |w - s H|^2 = |d|^2 - 2 rho Re(d* amp_hi H) + O(rho^2)
+        const double rho = (double)c.amp_lo / (double)c.amp_hi;
+        term = (Qs[jhi] - Qs[jlo]) - acc + 2.0 * rho * corr;
+        hh = 2.0 * (1.0 + rho) * (1.0 + rho) * hacc;
       } else {
         term = acc;
+        hh = 2.0 * hacc;
       }
       const double tx = a.term_x ? a.term_x[item] : 0.0;
       a.dlogl[item] = term - tx;
       if (a.term_y) a.term_y[item] = term;
-      if (a.hh) a.hh[item] = 2.0 * hacc;
+      if (a.hh) a.hh[item] = hh;
       if (a.status) a.status[item] = isfinite(term) ? 0 : 1;
     }
     if constexpr (GT > 32) __syncthreads();
   }
 }
 
-
 // Launch of one size's kernel with a grid bounded by the SM count times the
 // occupancy of the kernel.
 template <int N, bool MIX>
-static cudaError_t launch_size(const FdArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
-  using Cfg = FdCfg<N>;
-  size_t smem = FdSmem<N, MIX>::bytes;
+static cudaError_t launch_spec(const SpecArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
+  using Cfg = SpecCfg<N>;
+  size_t smem = SpecSmem<N, MIX>::bytes;
   static int occ = -1;
   if (occ < 0) {
-    cudaError_t e = cudaFuncSetAttribute(fd_dlogl_kernel<N, MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(fd_spec_kernel<N, MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_dlogl_kernel<N, MIX>, Cfg::CTA, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_kernel<N, MIX>, Cfg::CTA, smem);
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
   }
@@ -571,7 +697,19 @@ static cudaError_t launch_size(const FdArgs &a, int nitems_bound, int num_sms, c
   int grid = occ * num_sms;
   if (need < grid) grid = need;
   if (grid < 1) grid = 1;
-  fd_dlogl_kernel<N, MIX><<<grid, Cfg::CTA, smem, stream>>>(a);
+  fd_spec_kernel<N, MIX><<<grid, Cfg::CTA, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+template <bool MIX>
+static cudaError_t launch_slow(const SlowArgs &a, int num_sms, cudaStream_t stream) {
+  static int occ = -1;
+  if (occ < 0) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_slow_kernel<MIX>, 256, 0);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  fd_slow_kernel<MIX><<<occ * num_sms, 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
