@@ -261,7 +261,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.term_y = term_y;
   pa.hh = hh;
   pa.status = status;
-  fd_plan_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(pa);
+  fd_plan_kernel<<<(nitems + 31) / 32, 32, 0, stream>>>(pa);  // FP64-bound: spread over SMs
   launches++;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
 
@@ -270,8 +270,10 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   sa.NFFT = bank.NFFT;
   sa.fstar = bank.fstar;
   sa.L = kLARM;
-  sa.R = kAU * (kLARM / (2.0 * kSQ3 * kAU));
-  sa.T = bank.T;
+  sa.Rf = (float)(kAU * (kLARM / (2.0 * kSQ3 * kAU)));
+  sa.invLf = (float)(1.0 / kLARM);
+  sa.AUcf = (float)(kAU / kCLIGHT);
+  sa.invTf = (float)(1.0 / bank.T);
   sa.bin_count = work.bin_count;
   sa.bin_list = work.bin_list;
   sa.items64 = work.items64;

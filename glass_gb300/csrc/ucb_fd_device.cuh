@@ -429,7 +429,8 @@ struct PlanArgs {
 // four arm-combination series of each proposal.
 struct SlowArgs {
   int cap, NFFT;
-  double fstar, L, R, T;
+  double fstar, L;
+  float Rf, invLf, AUcf, invTf;  // orbit radius, 1/L, AU/c, 1/T for the FP32 path
   const int *bin_count, *bin_list;
   const ItemF64 *items64;
   const ItemMix *itemsmix;
@@ -458,16 +459,15 @@ struct SpecArgs {
   int *status;
 };
 
-// Position of proposal slot `slot` of size bin b in the scratch series, in
-// samples: sizes are laid out in increasing order, proposals of one size back to
-// back, each holding 4 series of N samples.
-__device__ __forceinline__ void sample_offsets(const int *bin_count, int nbins, long long *start) {
+// Start (in samples) of size bin `bin` in the scratch series: sizes are laid
+// out in increasing order, proposals of one size back to back, each holding 4
+// series of N samples.  Computed in registers from the per-size counts.
+__device__ __forceinline__ long long bin_sample_start(const int *bin_count, int NFFT, int bin) {
   long long acc = 0;
 #pragma unroll
-  for (int b = 0; b < kNumBins; b++) {
-    start[b] = acc;
-    if (b < nbins) acc += (long long)bin_count[b] * (32 << b);
-  }
+  for (int b = 0; b < kNumBins; b++)
+    if (b < bin && (32 << b) <= NFFT) acc += (long long)bin_count[b] * (32 << b);
+  return acc;
 }
 
 // ------------------------------------------------------- stage 1 (templated)
@@ -476,43 +476,42 @@ __device__ __forceinline__ void sample_offsets(const int *bin_count, int nbins, 
 template <bool MIX>
 __global__ void __launch_bounds__(256) fd_slow_kernel(SlowArgs a) {
   using C = typename std::conditional<MIX, float2, double2>::type;
-  int nbins = 0;
-  while (nbins < kNumBins && (32 << nbins) <= a.NFFT) nbins++;
-  int cnt[kNumBins];
-  long long cstart[kNumBins + 1];  // chunk offsets per size
-  long long acc = 0;
+  // chunk offsets per size (chunks of 32 samples: N/32 = 2^b per proposal), in registers
+  int cs[kNumBins + 1];
+  int acc = 0;
 #pragma unroll
   for (int b = 0; b < kNumBins; b++) {
-    cnt[b] = b < nbins ? a.bin_count[b] : 0;
-    cstart[b] = acc;
-    acc += (long long)cnt[b] * (1 << b);  // chunks of 32 samples: N/32 = 2^b
+    cs[b] = acc;
+    if ((32 << b) <= a.NFFT) acc += a.bin_count[b] << b;
   }
-  cstart[kNumBins] = acc;
-  const long long nchunks = acc;
+  cs[kNumBins] = acc;
+  const int nchunks = acc;
   const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   C *series = reinterpret_cast<C *>(a.series);
-  const float Rf = (float)a.R, invLf = (float)(1.0 / a.L), AUcf = (float)(kAU / kCLIGHT), invTf = (float)(1.0 / a.T);
 #pragma unroll 1
-  for (long long ch = warp; ch < nchunks; ch += nwarps) {
-    int b = 0;
+  for (int ch = warp; ch < nchunks; ch += nwarps) {
+    int b = 0, cb = 0;
 #pragma unroll
     for (int bb = 1; bb < kNumBins; bb++)
-      if (ch >= cstart[bb]) b = bb;
+      if (ch >= cs[bb]) {
+        b = bb;
+        cb = cs[bb];
+      }
     const int N = 32 << b;
-    const long long local = ch - cstart[b];
-    const int slot = (int)(local >> b);
-    const int n = (int)((local & ((1 << b) - 1)) << 5) + lane;
+    const int local = ch - cb;
+    const int slot = local >> b;
+    const int n = ((local & ((1 << b) - 1)) << 5) + lane;
     const int item = a.bin_list[(size_t)b * a.cap + slot];
     C d[6], cmb[4];
     if constexpr (MIX) {
-      slow_sample_mix(a.itemsmix[item], a.mix[b][n], Rf, invLf, AUcf, invTf, d);
+      slow_sample_mix(a.itemsmix[item], a.mix[b][n], a.Rf, a.invLf, a.AUcf, a.invTf, d);
     } else {
       slow_sample64(a.items64[item], a.pos64[b][n], a.fstar, a.L, d);
     }
     ae_combos(d, cmb);
-    C *out = series + (cstart[b] * 32 + (long long)slot * N) * 4 + n;
+    C *out = series + ((long long)cb * 32 + (long long)slot * N) * 4 + n;
 #pragma unroll
     for (int s = 0; s < 4; s++) out[(size_t)s * N] = cmb[s];
   }
@@ -553,6 +552,29 @@ __device__ __forceinline__ double group_sum(double v, double *red, int lane) {
   return v;
 }
 
+// The same in double-float arithmetic (FP32 operations only: the FP64 pipe of
+// this GPU runs at 1/64 of the FP32 rate).  Result valid in lane 0 of the group.
+template <int GT>
+__device__ __forceinline__ df group_sum_df(float v, float2 *red, int lane) {
+  df s = {v, 0.f};
+#pragma unroll
+  for (int off = (GT < 32 ? GT : 32) / 2; off > 0; off >>= 1) {
+    df o = {__shfl_xor_sync(0xffffffffu, s.hi, off), __shfl_xor_sync(0xffffffffu, s.lo, off)};
+    s = df_add(s, o);
+  }
+  if constexpr (GT > 32) {
+    __syncthreads();
+    if ((lane & 31) == 0) red[lane >> 5] = make_float2(s.hi, s.lo);
+    __syncthreads();
+    if (lane == 0) {
+      df t = {0.f, 0.f};
+      for (int w = 0; w < GT / 32; w++) t = df_add(t, df{red[w].x, red[w].y});
+      s = t;
+    }
+  }
+  return s;
+}
+
 template <int N, bool MIX>
 __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   using Cfg = SpecCfg<N>;
@@ -573,11 +595,7 @@ __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
   C *buf = bufs + (size_t)g * NSER * N;
   const int count = a.bin_count[a.bin];
-  long long start[kNumBins];
-  int nbins = 0;
-  while (nbins < kNumBins && (32 << nbins) <= a.NFFT) nbins++;
-  sample_offsets(a.bin_count, nbins, start);
-  const C *series = reinterpret_cast<const C *>(a.series) + start[a.bin] * 4;
+  const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, a.bin) * 4;
   const int NFFT = a.NFFT;
 
   for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC) {
@@ -645,9 +663,13 @@ __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
     }
     double corr = 0.0;
     if constexpr (MIX) {
-      acc = group_sum<GT>((double)facc, red, lane);
-      hacc = group_sum<GT>((double)fh, red + 32, lane);
-      corr = group_sum<GT>((double)fc, red + 64, lane);
+      float2 *redf = reinterpret_cast<float2 *>(red);
+      df sa = group_sum_df<GT>(facc, redf, lane);
+      df sh = group_sum_df<GT>(fh, redf + 32, lane);
+      df sc = group_sum_df<GT>(fc, redf + 64, lane);
+      acc = (double)sa.hi + (double)sa.lo;
+      hacc = (double)sh.hi + (double)sh.lo;
+      corr = (double)sc.hi + (double)sc.lo;
     } else {
       acc = group_sum<GT>(acc, red, lane);
       hacc = group_sum<GT>(hacc, red + 32, lane);
