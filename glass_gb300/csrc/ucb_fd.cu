@@ -38,69 +38,168 @@ cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_s
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
 
 // ------------------------------------------------------------- plan kernel
-__global__ void fd_plan_kernel(PlanArgs a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.nitems) return;
+// Four lanes per proposal split its FP64 work (the FP64 pipe is slow and the
+// batch holds only a few thousand proposals, so latency, not throughput, sets
+// the time): lane 0 the Doppler-spread half of ucb_bandwidth, lane 1 the
+// SNR-spread half, lane 2 the sky geometry, lane 3 the polarisation factors;
+// lane 0 then assembles the per-proposal constants.
+__device__ __forceinline__ double shfl_d(double v, int src) {
+  return __longlong_as_double(__shfl_sync(0xffffffffu, __double_as_longlong(v), src));
+}
+
+__global__ void __launch_bounds__(128) fd_plan_kernel(PlanArgs a) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = gt >> 2, role = gt & 3;
+  const int lane = threadIdx.x & 31, lead = lane & ~3;
+  const bool in = i < a.nitems;
   double p[8];
   bool finite = true;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    p[k] = a.params[8 * (size_t)i + k];
+    p[k] = in ? a.params[8 * (size_t)i + k] : 0.0;
     finite = finite && isfinite(p[k]);
   }
-  int seg = a.item_seg[i];
+  const int seg = in ? a.item_seg[i] : 0;
   int st = 0;
   if (seg < 0 || seg >= a.nseg) st |= 2;
   if (!finite || fabs(p[1]) > 1.0 || fabs(p[4]) > 1.0) st |= 1;
-  int N = 0;
-  long long q = 0;
-  if (!st) {
-    double T = a.T;
-    double f0 = p[0] / T;
-    N = 2 * bandwidth_dev(a.L, a.fstar, f0, p[7] / (T * T), p[1], exp(p[3]), T, a.NFFT);
-    q = (long long)(f0 * T);
-    if (N < kMinN || N > kMaxN) st |= 1;
+  const double T = a.T;
+  const double f0 = p[0] / T;
+  const bool work = in && !st;
+
+  // ---- role-specific FP64 work (ucb/src/glass_ucb_waveform.c:698-725, :802-838)
+  const int Nmin = 16;
+  const int half = a.NFFT / 2;
+  const int Nmax = half >= 1 ? (1 << (31 - __clz(half))) : 0;
+  int part = Nmin;                 // roles 0/1: DS or SS
+  double g0 = 0, g1 = 0, g2 = 0;   // role 2: k; role 3: DPr, DPi, DCr (DCi in g3)
+  double g3 = 0;
+  double e[12];                    // role 2: ep, ec
+#pragma unroll
+  for (int k = 0; k < 12; k++) e[k] = 0.0;
+  if (work) {
+    if (role == 0) {
+      double sintheta = sin(acos(p[1]));
+      double fdot = p[7] / (T * T);
+      double bw = 2 * T * ((4. + kPI2 * f0 * (kAU / kCLIGHT) * sintheta) / kYEAR + fabs(fdot) * T);
+      part = pow2_above_dev(bw - 1);
+    } else if (role == 1) {
+      double sf = sin(f0 / a.fstar);
+      double sn = aenoise_dev(f0, a.L, a.fstar);
+      double SNRm = exp(p[3]) * sqrt(T) * sf / sqrt(sn);  // analytic_snr
+      part = pow2_above_dev(SNRm - 1);
+    } else if (role == 2) {
+      double costh = p[1];
+      double sinth = sqrt(1.0 - costh * costh);
+      double sinph, cosph;
+      sincos(p[2], &sinph, &cosph);
+      double u[3] = {costh * cosph, costh * sinph, -sinth};
+      double v[3] = {sinph, -cosph, 0.};
+      g0 = -sinth * cosph;
+      g1 = -sinth * sinph;
+      g2 = -costh;
+      int idx = 0;
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = r; c < 3; c++, idx++) {
+          e[idx] = v[r] * v[c] - u[r] * u[c];
+          e[6 + idx] = u[r] * v[c] + v[r] * u[c];
+        }
+    } else {
+      double cosi = p[4];
+      double sinps, cosps;
+      sincos(2. * p[5], &sinps, &cosps);
+      double Aplus = (1. + cosi * cosi) * 0.5, Across = -cosi;
+      g0 = Aplus * cosps;     // DPr
+      g1 = -Across * sinps;   // DPi
+      g2 = -Aplus * sinps;    // DCr
+      g3 = -Across * cosps;   // DCi
+    }
   }
-  double tx = a.term_x ? a.term_x[i] : 0.0;
-  if (st) {
-    double nan = __longlong_as_double(0x7ff8000000000000ULL);
-    a.dlogl[i] = nan;
-    if (a.term_y) a.term_y[i] = nan;
-    if (a.hh) a.hh[i] = nan;
-    if (a.status) a.status[i] = st;
-    return;
+  if (part > Nmax) part = Nmax;
+  if (part < Nmin) part = Nmin;
+  // ---- gather into lane 0 of the quad (every lane takes part in the shuffles)
+  const int ss = __shfl_sync(0xffffffffu, part, lead + 1);
+  double kx = shfl_d(g0, lead + 2), ky = shfl_d(g1, lead + 2), kz = shfl_d(g2, lead + 2);
+  double DPr = shfl_d(g0, lead + 3), DPi = shfl_d(g1, lead + 3), DCr = shfl_d(g2, lead + 3), DCi = shfl_d(g3, lead + 3);
+  double ee[12];
+#pragma unroll
+  for (int k = 0; k < 12; k++) ee[k] = shfl_d(e[k], lead + 2);
+
+  int N = 2 * ((part > ss) ? part : ss);
+  long long q = (long long)(f0 * T);
+  if (work && (N < kMinN || N > kMaxN)) st |= 1;
+  int b = -1;
+  if (role == 0 && in) {
+    const double tx = a.term_x ? a.term_x[i] : 0.0;
+    if (st) {
+      const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+      a.dlogl[i] = nan;
+      if (a.term_y) a.term_y[i] = nan;
+      if (a.hh) a.hh[i] = nan;
+      if (a.status) a.status[i] = st;
+    } else {
+      const int imin = (int)(q - N / 2) - a.seg_qmin[seg];
+      if (imin >= a.NFFT || imin + N <= 0) {
+        // template support entirely outside the segment: logL is unchanged
+        a.dlogl[i] = 0.0 - tx;
+        if (a.term_y) a.term_y[i] = 0.0;
+        if (a.hh) a.hh[i] = 0.0;
+        if (a.status) a.status[i] = 4;
+      } else {
+        SourceGeom g;
+        g.f0 = f0;
+        g.amp = exp(p[3]);
+        g.phi0 = p[6];
+        g.fdot = p[7] / (T * T);
+        double fT = f0 * T;
+        g.eps = fT - (double)q;
+        g.dfq = kPI2 * (((double)q) / T);
+        g.k[0] = kx;
+        g.k[1] = ky;
+        g.k[2] = kz;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+          g.ep[k] = ee[k];
+          g.ec[k] = ee[6 + k];
+        }
+        g.DPr = DPr;
+        g.DPi = DPi;
+        g.DCr = DCr;
+        g.DCi = DCi;
+        if (a.precision == 1) {
+          ItemMix c;
+          make_item_mix(g, N, T, a.fstar, c);
+          c.seg = seg;
+          c.N = N;
+          c.imin = imin;
+          c.pad = 0;
+          a.itemsmix[i] = c;
+        } else {
+          ItemF64 c;
+          make_item_f64(g, N, c);
+          c.seg = seg;
+          c.N = N;
+          c.imin = imin;
+          c.pad = 0;
+          a.items64[i] = c;
+        }
+        b = fd_bin_of(N);
+      }
+    }
   }
-  int imin = (int)(q - N / 2) - a.seg_qmin[seg];
-  if (imin >= a.NFFT || imin + N <= 0) {
-    // template support entirely outside the segment: logL is unchanged
-    a.dlogl[i] = 0.0 - tx;
-    if (a.term_y) a.term_y[i] = 0.0;
-    if (a.hh) a.hh[i] = 0.0;
-    if (a.status) a.status[i] = 4;
-    return;
+  // ---- warp-aggregated binning: one atomic per distinct size per warp
+  const unsigned leaders = __ballot_sync(0xffffffffu, b >= 0);
+  if (b >= 0) {
+    const unsigned same = __match_any_sync(leaders, b);
+    const int first = __ffs(same) - 1;
+    int base = 0;
+    if (lane == first) base = atomicAdd(&a.bin_count[b], __popc(same));
+    base = __shfl_sync(same, base, first);
+    const int pos = base + __popc(same & ((1u << lane) - 1));
+    a.bin_list[(size_t)b * a.cap + pos] = i;
   }
-  SourceGeom g;
-  source_geometry(p, 8, a.T, g);
-  if (a.precision == 1) {
-    ItemMix c;
-    make_item_mix(g, N, a.T, a.fstar, c);
-    c.seg = seg;
-    c.N = N;
-    c.imin = imin;
-    c.pad = 0;
-    a.itemsmix[i] = c;
-  } else {
-    ItemF64 c;
-    make_item_f64(g, N, c);
-    c.seg = seg;
-    c.N = N;
-    c.imin = imin;
-    c.pad = 0;
-    a.items64[i] = c;
-  }
-  int b = fd_bin_of(N);
-  int pos = atomicAdd(&a.bin_count[b], 1);
-  a.bin_list[(size_t)b * a.cap + pos] = i;
 }
 
 // ------------------------------------------------------------ orbit tables
@@ -261,7 +360,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.term_y = term_y;
   pa.hh = hh;
   pa.status = status;
-  fd_plan_kernel<<<(nitems + 31) / 32, 32, 0, stream>>>(pa);  // FP64-bound: spread over SMs
+  fd_plan_kernel<<<(4 * nitems + 127) / 128, 128, 0, stream>>>(pa);
   launches++;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
 
