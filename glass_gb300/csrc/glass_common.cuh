@@ -124,6 +124,22 @@ struct __align__(16) ItemMix {
   df pad3;
 };
 
+// Gradient / Fisher path: the mixed-precision constants plus what the tangent
+// templates need.  The template is h = DP H+ + DC Hx with H+, Hx the responses
+// to unit plus/cross polarisation factors (ucb/src/glass_ucb_waveform.c:822-835);
+// derivatives of DP, DC give the cos(iota) and psi directions.
+struct __align__(16) ItemGrad {
+  ItemMix m;
+  float ep[6], ec[6];                 // polarisation tensors e+, ex
+  float dep_c[6], dec_c[6];           // d/dcos(theta)
+  float dep_p[6], dec_p[6];           // d/dphi
+  float dk_c[4], dk_p[4];             // dk/dcos(theta), dk/dphi
+  float DP[2], DC[2];                 // complex polarisation factors (amplitude-free)
+  float dDP_i[2], dDC_i[2];           // d/dcos(iota)
+  float dDP_s[2], dDC_s[2];           // d/dpsi
+  float f0, fdot, invT, fstar;        // f0 (Hz), fdot (Hz/s), 1/T, f*
+};
+
 // Per-sample orbit tables, one per waveform size.  Positions of the three
 // spacecraft (FP64, metres) and the sample time; and, for the mixed path,
 // u = t/T and the guiding-centre angle cos/sin(2 pi t / YEAR) as double-floats.

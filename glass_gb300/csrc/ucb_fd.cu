@@ -38,51 +38,6 @@ cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_s
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
 
 // ------------------------------------------------------------- plan kernels
-// Outputs of a proposal that is not evaluated (bad input, or a template
-// entirely outside its segment).
-__device__ __forceinline__ void plan_write_skipped(const PlanArgs &a, int i, int st) {
-  const double tx = a.term_x ? a.term_x[i] : 0.0;
-  if (st & 3) {
-    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
-    a.dlogl[i] = nan;
-    if (a.term_y) a.term_y[i] = nan;
-    if (a.hh) a.hh[i] = nan;
-  } else {  // outside: logL is unchanged
-    a.dlogl[i] = 0.0 - tx;
-    if (a.term_y) a.term_y[i] = 0.0;
-    if (a.hh) a.hh[i] = 0.0;
-  }
-  if (a.status) a.status[i] = st;
-}
-
-// Warp-aggregated binning: one atomic per distinct size per warp.
-__device__ __forceinline__ void plan_bin(const PlanArgs &a, int i, int b) {
-  const int lane = threadIdx.x & 31;
-  const unsigned active = __ballot_sync(0xffffffffu, b >= 0);
-  if (b >= 0) {
-    const unsigned same = __match_any_sync(active, b);
-    const int first = __ffs(same) - 1;
-    int base = 0;
-    if (lane == first) base = atomicAdd(&a.bin_count[b], __popc(same));
-    base = __shfl_sync(same, base, first);
-    a.bin_list[(size_t)b * a.cap + base + __popc(same & ((1u << lane) - 1))] = i;
-  }
-}
-
-__device__ __forceinline__ int plan_validate(const PlanArgs &a, int i, double *p, int &seg) {
-  bool finite = true;
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    p[k] = a.params[8 * (size_t)i + k];
-    finite = finite && isfinite(p[k]);
-  }
-  seg = a.item_seg[i];
-  int st = 0;
-  if (seg < 0 || seg >= a.nseg) st |= 2;
-  if (!finite || fabs(p[1]) > 1.0 || fabs(p[4]) > 1.0) st |= 1;
-  return st;
-}
-
 // Plain-FP64 plan: ucb_bandwidth, ucb_alignment and the per-proposal constants
 // entirely in FP64, one thread per proposal.
 __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
@@ -121,134 +76,18 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
   plan_bin(a, i, b);
 }
 
-// (int)pow(2, (int)log2(v) + 1) from an FP32 estimate of v, or -1 when v lies
-// within 1e-4 (relative) of a power of two, where an FP32 estimate could fall
-// on the other side of the boundary than the reference's FP64 value.
-__device__ __forceinline__ int pow2_above_f32(float v) {
-  if (!(v >= 1.0f)) return (v < 0.99f) ? 1 : -1;
-  int e;
-  float m = frexpf(v, &e);  // v = m 2^e, m in [0.5, 1)
-  if (m < 0.50005f || m > 0.99995f) return -1;
-  return e > 30 ? (1 << 30) : (1 << e);  // (int)log2(v) = e - 1
-}
-
-// Mixed-precision plan: FP32 except where a constant sets the carrier phase
-// (f0 T - q, the Doppler amplitude 2 pi f0 AU/c k, phi0, pi fdot T^2), and the
-// bandwidth rule, which is evaluated in FP32 and re-evaluated in FP64 only for
-// values near a power-of-two boundary, so N is always the reference's.
+// Mixed-precision plan (see planmix_item).
 __global__ void __launch_bounds__(64) fd_planmix_kernel(PlanArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int b = -1;
   if (i < a.nitems) {
-    double p[8];
-    int seg;
-    int st = plan_validate(a, i, p, seg);
-    const double T = a.T;
-    const double f0 = p[0] / T;
-    const float Tf = (float)T, f0f = (float)f0, costhf = (float)p[1];
-    const float fdotf = (float)(p[7] / (T * T));
-    const float ampf = expf((float)p[3]);
-    const float sinthf = sqrtf(fmaxf(0.f, 1.f - costhf * costhf));
-    int N = 0;
-    if (!st) {
-      const int Nmin = 16;
-      const int half = a.NFFT / 2;
-      const int Nmax = half >= 1 ? (1 << (31 - __clz(half))) : 0;
-      // Doppler spread (ucb/src/glass_ucb_waveform.c:708-714)
-      float bw = 2.f * Tf * ((4.f + 6.2831853f * f0f * (float)(kAU / kCLIGHT) * sinthf) / (float)kYEAR + fabsf(fdotf) * Tf);
-      int DS = pow2_above_f32(bw - 1.f);
-      if (DS < 0) {
-        double sintheta = sin(acos(p[1]));
-        double fdot = p[7] / (T * T);
-        DS = pow2_above_dev(2 * T * ((4. + kPI2 * f0 * (kAU / kCLIGHT) * sintheta) / kYEAR + fabs(fdot) * T) - 1);
-      }
-      if (DS > Nmax) DS = Nmax;
-      if (DS < Nmin) DS = Nmin;
-      // SNR spread (:717-722) with AEnoise (utils/src/glass_lisa.c:1188-1198)
-      const float x = f0f / (float)a.fstar;
-      float sx, cx;
-      sincosf(x, &sx, &cx);
-      const float c2x = 2.f * cx * cx - 1.f;
-      const float w = 6.2831853f * f0f, w2 = w * w;
-      const float q1 = 2.0e-5f / f0f, q2 = q1 * q1, q4 = q2 * q2, r1 = 1.0e-4f / f0f;
-      const float red = 1.f + 16.f * (q4 * q4 * q2 + r1 * r1);
-      // AEnoise times (2L)^2: AEnoise itself (~1e-42) is below FP32's normal range
-      const float twoL = 2.f * (float)a.L;
-      const float sn4L2 = (16.f / 3.f) * sx * sx *
-                          ((2.f + cx) * (float)(kSPS + kSLOC) +
-                           2.f * (3.f + 2.f * cx + c2x) * ((float)(kSLOC / 2.0) + (float)kSACC / (w2 * w2) * red));
-      const float snrm = ampf * sqrtf(Tf) * sx * twoL / sqrtf(sn4L2);
-      int SS = pow2_above_f32(snrm - 1.f);
-      if (SS < 0) {
-        double sn64 = aenoise_dev(f0, a.L, a.fstar);
-        SS = pow2_above_dev(exp(p[3]) * sqrt(T) * sin(f0 / a.fstar) / sqrt(sn64) - 1);
-      }
-      if (SS > Nmax) SS = Nmax;
-      if (SS < Nmin) SS = Nmin;
-      N = 2 * ((DS > SS) ? DS : SS);
-      if (N < kMinN || N > kMaxN) st |= 1;
-    }
-    const double fT = f0 * T;
-    const long long q = (long long)fT;
-    int imin = 0;
-    if (!st) {
-      imin = (int)(q - N / 2) - a.seg_qmin[seg];
-      if (imin >= a.NFFT || imin + N <= 0) st = 4;
-    }
+    ItemMix c;
+    int st = planmix_item(a, i, 0, c);
     if (st) {
       plan_write_skipped(a, i, st);
     } else {
-      ItemMix c;
-      c.seg = seg;
-      c.N = N;
-      c.imin = imin;
-      c.pad = 0;
-      // sky direction and polarisation tensors (FP32, utils/src/glass_lisa.c:1566-1596)
-      float sph, cph;
-      sincosf((float)p[2], &sph, &cph);
-      const float u[3] = {costhf * cph, costhf * sph, -sinthf};
-      const float v[3] = {sph, -cph, 0.f};
-      c.k[0] = -sinthf * cph;
-      c.k[1] = -sinthf * sph;
-      c.k[2] = -costhf;
-      c.k[3] = 0.f;
-      const float cosi = (float)p[4];
-      float s2p, c2p;
-      sincosf(2.f * (float)p[5], &s2p, &c2p);
-      const float Aplus = (1.f + cosi * cosi) * 0.5f, Across = -cosi;
-      const float DPr = Aplus * c2p, DPi = -Across * s2p, DCr = -Aplus * s2p, DCi = -Across * c2p;
-      int idx = 0;
-#pragma unroll
-      for (int r = 0; r < 3; r++)
-#pragma unroll
-        for (int cc = r; cc < 3; cc++, idx++) {
-          const float ep = v[r] * v[cc] - u[r] * u[cc];
-          const float ec = u[r] * v[cc] + v[r] * u[cc];
-          c.Mr[idx] = DPr * ep + DCr * ec;
-          c.Mi[idx] = DPi * ep + DCi * ec;
-        }
-      c.fonfs0 = f0f / (float)a.fstar;
-      c.fdfs = fdotf * Tf / (float)a.fstar;
-      c.aef = 0.6666667f * fdotf * Tf / f0f;
-      c.w0c = 6.2831853f * f0f / (float)kCLIGHT;
-      c.p7pi = 3.14159265f * (float)p[7];
-      c.amp_hi = ampf / (float)(2 * N);
-      c.amp_lo = 0.f;
-      c.pad2 = 0.f;
-      // carrier-phase constants in FP64, stored as double-floats
-      c.eps2pi = df_from_double(kPI2 * (fT - (double)q));
-      const double costh = p[1];
-      const double sinth = sqrt(1.0 - costh * costh);
-      double sinph, cosph;
-      sincos(p[2], &sinph, &cosph);
-      const double bscale = kPI2 * f0 * (kAU / kCLIGHT);
-      c.beta1 = df_from_double(-bscale * sinth * cosph);
-      c.beta2 = df_from_double(-bscale * sinth * sinph);
-      c.phi0 = df_from_double(p[6]);
-      c.p7pi_d = df_from_double(kPI * p[7]);
-      c.pad3 = {0.f, 0.f};
       a.itemsmix[i] = c;
-      b = fd_bin_of(N);
+      b = fd_bin_of(c.N);
     }
   }
   plan_bin(a, i, b);
