@@ -243,6 +243,72 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_grad_fisher(gg, torch, dev, rank, steps, warmup):
+    """Gradient + Fisher matrix of 16384 proposals (f0 ~ U[1, 5] mHz, N = 256,
+    amplitude log-uniform in [1e-23, 1e-21]) against one mixed delta-logL eval of
+    the same proposals: the cost ratio the adjoint must keep at or below 3."""
+    rng = np.random.default_rng(2 + 1000 * rank)
+    nseg, per = 64, 256
+    qmin, dA, dE, iA, iE, inj = [], [], [], [], [], []
+
+    def wf(p):
+        h = gg.ucb_waveform(p, 256, T)
+        return 256, h[3], h[4]
+
+    for s in range(nseg):
+        p = wl.draw_source(rng, rng.uniform(1e-3, 5e-3), 10 ** rng.uniform(-23, -21), 1e-17)
+        q, a, e, ia, ie = wl.make_segment(rng, [p], wf, NFFT=NFFT, T=T)
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie), inj.append(p)
+    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                          invCA=np.array(iA), invCE=np.array(iE))
+    inj = np.array(inj)
+    eng = gg.Engine(dev.index or 0)
+    eng.upload(bank)
+    eng.set_template_size(256)
+    _, _, hh, _ = eng.dlogl_host(np.arange(nseg, dtype=np.int32), inj, precision=gg.PREC_FP64)
+    seg = np.repeat(np.arange(nseg, dtype=np.int32), per)
+    scales = np.array([wl.jump_scales(inj[s], max(np.sqrt(max(hh[s], 1.0)), 5.0)) for s in range(nseg)])
+    props = inj[seg] + rng.standard_normal((len(seg), 8)) * scales[seg]
+    for k in (1, 4):
+        props[:, k] = np.clip(props[:, k], -0.999, 0.999)
+    n = len(seg)
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    d_seg = torch.from_numpy(seg).to(dev)
+    d_p = torch.from_numpy(props).to(dev)
+    d_ty = torch.empty(n, dtype=torch.float64, device=dev)
+    d_dl = torch.empty(n, dtype=torch.float64, device=dev)
+    d_g = torch.empty((n, 8), dtype=torch.float64, device=dev)
+    d_F = torch.empty((n, 64), dtype=torch.float64, device=dev)
+    d_st = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def run(kind):
+        if kind == "grad":
+            eng.grad_fisher_device(d_seg, d_p, d_ty, d_g, d_F, d_st)
+        else:
+            eng.dlogl_device(d_seg, d_p, d_dl, None, None, None, precision=gg.PREC_MIXED)
+
+    times = {}
+    with torch.cuda.stream(stream):
+        for kind in ("dlogl", "grad"):
+            for _ in range(warmup):
+                run(kind)
+            stream.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            for k in range(steps):
+                ev[k][0].record(stream)
+                run(kind)
+                ev[k][1].record(stream)
+            stream.synchronize()
+            times[kind] = sum(a.elapsed_time(b) for a, b in ev) / steps / 1e3
+    st = d_st.cpu().numpy()
+    eng.close()
+    return {"workload": f"{n} proposals on {nseg} segments, N=256, f0~U[1,5] mHz (mixed precision)",
+            "grad_fisher_per_s": n / times["grad"], "dlogl_per_s": n / times["dlogl"],
+            "ms_grad_fisher": 1e3 * times["grad"], "ms_dlogl": 1e3 * times["dlogl"],
+            "cost_ratio": times["grad"] / times["dlogl"], "ok_items": int((st == 0).sum())}
+
+
 def run_ours(args):
     import torch
 
@@ -367,6 +433,8 @@ def run_ours(args):
     ach_mixed = flops_step / (t_mixed / args.steps) / 1e12
     ach_fp64 = flops_step / (t_fp64 / args.steps) / 1e12
 
+    grad_line = bench_grad_fisher(gg, torch, dev, rank, max(5, args.steps // 20), args.warmup)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": v_mixed, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
@@ -396,6 +464,7 @@ def run_ours(args):
                          "flops_per_step": flops_step,
                          "fp64_path": {"achieved": ach_fp64, "peak_fp64": peak64,
                                        "frac_of_fp64_peak": ach_fp64 / peak64}},
+            "grad_fisher": grad_line,
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk,
         }

@@ -34,6 +34,7 @@ EXPORTS = (
     "glass_gpu_create", "glass_gpu_destroy", "glass_gpu_set_stream", "glass_gpu_last_error",
     "glass_gpu_bank_upload", "glass_gpu_bank_set_residual", "glass_gpu_dlogl_batch",
     "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_probe_fma_tflops",
+    "glass_gpu_grad_fisher_batch", "glass_gpu_grad_fisher_batch_host", "glass_gpu_set_template_size",
 )
 
 _lib = None
@@ -66,6 +67,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ucb_bandwidth.argtypes = [ctypes.c_double] * 7 + [ctypes.c_int]
     lib.ucb_bandwidth.restype = ctypes.c_int
     lib.glass_gpu_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _D]
+    lib.glass_gpu_grad_fisher_batch.argtypes = [_V, ctypes.c_int, _V, _V, ctypes.c_int, _V, _V, _V, _V]
+    lib.glass_gpu_grad_fisher_batch_host.argtypes = [_V, ctypes.c_int, _I, _D, ctypes.c_int, _D, _D, _D, _I]
+    lib.glass_gpu_set_template_size.argtypes = [_V, ctypes.c_int]
     _lib = lib
     return lib
 
@@ -180,6 +184,28 @@ class Engine:
         n = int(item_seg.numel())
         _check(self.lib.glass_gpu_dlogl_batch(self._ctx, precision, n, _ptr(item_seg), _ptr(params), _ptr(term_x),
                                               _ptr(dlogl), _ptr(term_y), _ptr(hh), _ptr(status)))
+
+    def set_template_size(self, n: int = 0):
+        """0: the reference's bandwidth rule; otherwise every proposal uses N = n."""
+        _check(self.lib.glass_gpu_set_template_size(self._ctx, n))
+
+    def grad_fisher_host(self, item_seg, params, fisher_mode=0, fisher=True):
+        """Host arrays: (term_y [n], grad [n, 8], fisher [n, 8, 8] or None, status [n])."""
+        seg = np.ascontiguousarray(item_seg, np.int32)
+        p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        n = len(seg)
+        ty, g = np.empty(n), np.empty((n, 8))
+        F = np.empty((n, 8, 8)) if fisher else None
+        st = np.empty(n, np.int32)
+        _check(self.lib.glass_gpu_grad_fisher_batch_host(self._ctx, n, _pi(seg), _pd(p), fisher_mode,
+                                                         _pd(ty), _pd(g), _pd(F) if F is not None else None,
+                                                         _pi(st)))
+        return ty, g, F, st
+
+    def grad_fisher_device(self, item_seg, params, term_y, grad, fisher=None, status=None, fisher_mode=0):
+        n = int(item_seg.numel())
+        _check(self.lib.glass_gpu_grad_fisher_batch(self._ctx, n, _ptr(item_seg), _ptr(params), fisher_mode,
+                                                    _ptr(term_y), _ptr(grad), _ptr(fisher), _ptr(status)))
 
     def last_launch_count(self) -> int:
         return self.lib.glass_gpu_last_launch_count(self._ctx)

@@ -54,6 +54,7 @@ struct glass_gpu_ctx {
   void *d_stage = nullptr;
   size_t d_stage_cap = 0;
   int last_launches = 0;
+  int n_fixed = 0;  // template size override (0: bandwidth rule)
 };
 
 static int ctx_activate(glass_gpu_ctx *ctx) {
@@ -102,6 +103,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->tab.base);
   cudaFree(ctx->work.items64);
   cudaFree(ctx->work.itemsmix);
+  cudaFree(ctx->work.itemsgrad);
   cudaFree(ctx->work.bin_count);
   cudaFree(ctx->work.bin_list);
   cudaFree(ctx->work.series);
@@ -123,6 +125,15 @@ extern "C" int glass_gpu_set_stream(glass_gpu_ctx *ctx, void *stream) {
 }
 
 extern "C" int glass_gpu_last_launch_count(glass_gpu_ctx *ctx) { return ctx ? ctx->last_launches : 0; }
+
+static int is_pow2_in_range(int n);
+
+extern "C" int glass_gpu_set_template_size(glass_gpu_ctx *ctx, int n) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "set_template_size: null context");
+  if (n != 0 && !is_pow2_in_range(n)) return set_err(GLASS_ERR_SIZE, "set_template_size: n must be 0 or a power of two in [32, 4096]");
+  ctx->n_fixed = n;
+  return GLASS_OK;
+}
 
 // -------------------------------------------------------------------- bank
 static int format_code(const char *format) {
@@ -160,7 +171,8 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   size_t off_g32 = off_w32lo + sizeof(float4) * w32lo.size();
   size_t off_w64 = off_g32 + sizeof(float4) * g32.size();
   size_t off_g64 = off_w64 + sizeof(double2) * w64.size();
-  size_t total = off_g64 + sizeof(double2) * g64.size();
+  size_t off_invc = off_g64 + sizeof(double2) * g64.size();
+  size_t total = off_invc + sizeof(float2) * nb;
   GLASS_CUDA(cudaMalloc(&ctx->bank_mem, total), "cudaMalloc(bank)");
   char *base = (char *)ctx->bank_mem;
   FdBankDev &b = ctx->bank;
@@ -177,6 +189,7 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   b.g32 = (float4 *)(base + off_g32);
   b.w64 = (double2 *)(base + off_w64);
   b.g64 = (double2 *)(base + off_g64);
+  b.invc = (float2 *)(base + off_invc);
   GLASS_CUDA(cudaMemcpy(b.qmin, qmin, sizeof(int) * nseg, cudaMemcpyHostToDevice), "upload qmin");
   GLASS_CUDA(cudaMemcpy(b.Q, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice), "upload Q");
   GLASS_CUDA(cudaMemcpy(b.w32, w32.data(), sizeof(float4) * w32.size(), cudaMemcpyHostToDevice), "upload w32");
@@ -184,6 +197,11 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   GLASS_CUDA(cudaMemcpy(b.g32, g32.data(), sizeof(float4) * g32.size(), cudaMemcpyHostToDevice), "upload g32");
   GLASS_CUDA(cudaMemcpy(b.w64, w64.data(), sizeof(double2) * w64.size(), cudaMemcpyHostToDevice), "upload w64");
   GLASS_CUDA(cudaMemcpy(b.g64, g64.data(), sizeof(double2) * g64.size(), cudaMemcpyHostToDevice), "upload g64");
+  {
+    std::vector<float2> ic(nb);
+    for (size_t j = 0; j < nb; j++) ic[j] = make_float2((float)invCA[j], (float)invCE[j]);
+    GLASS_CUDA(cudaMemcpy(b.invc, ic.data(), sizeof(float2) * nb, cudaMemcpyHostToDevice), "upload invc");
+  }
   ctx->h_qmin.assign(qmin, qmin + nseg);
   ctx->h_invCA.assign(invCA, invCA + nb);
   ctx->h_invCE.assign(invCE, invCE + nb);
@@ -224,6 +242,8 @@ extern "C" int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const do
   return GLASS_OK;
 }
 
+static int is_pow2_in_range(int n) { return n >= kMinN && n <= kMaxN && (n & (n - 1)) == 0; }
+
 // --------------------------------------------------------------- batched
 // Scratch for a batch: per-proposal constants, size lists and the slow-part
 // series (4 complex series of N <= NFFT samples per proposal), sized for the
@@ -232,15 +252,19 @@ extern "C" int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const do
 static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   FdWorkDev &w = ctx->work;
   size_t series = fd_series_bytes(nitems, ctx->bank.NFFT, GLASS_PREC_FP64);
+  size_t gseries = fd_grad_series_bytes(nitems, ctx->bank.NFFT);
+  if (gseries > series) series = gseries;
   if (nitems <= w.cap && series <= w.series_bytes) return GLASS_OK;
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "work sync");
   cudaFree(w.items64);
   cudaFree(w.itemsmix);
+  cudaFree(w.itemsgrad);
   cudaFree(w.bin_count);
   cudaFree(w.bin_list);
   cudaFree(w.series);
   w.items64 = nullptr;
   w.itemsmix = nullptr;
+  w.itemsgrad = nullptr;
   w.bin_count = nullptr;
   w.bin_list = nullptr;
   w.series = nullptr;
@@ -248,8 +272,11 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   w.series_bytes = 0;
   int cap = nitems < 1024 ? 1024 : nitems;
   series = fd_series_bytes(cap, ctx->bank.NFFT, GLASS_PREC_FP64);
+  gseries = fd_grad_series_bytes(cap, ctx->bank.NFFT);
+  if (gseries > series) series = gseries;
   GLASS_CUDA(cudaMalloc(&w.items64, sizeof(ItemF64) * (size_t)cap), "cudaMalloc(items64)");
   GLASS_CUDA(cudaMalloc(&w.itemsmix, sizeof(ItemMix) * (size_t)cap), "cudaMalloc(itemsmix)");
+  GLASS_CUDA(cudaMalloc(&w.itemsgrad, sizeof(ItemGrad) * (size_t)cap), "cudaMalloc(itemsgrad)");
   GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * kNumBins), "cudaMalloc(bin_count)");
   GLASS_CUDA(cudaMalloc(&w.bin_list, sizeof(int) * (size_t)kNumBins * cap), "cudaMalloc(bin_list)");
   GLASS_CUDA(cudaMalloc(&w.series, series), "cudaMalloc(series)");
@@ -272,8 +299,9 @@ extern "C" int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nite
   if (rc) return rc;
   if ((rc = ensure_work(ctx, nitems))) return rc;
   int nl = 0;
+  if (ctx->n_fixed > ctx->bank.NFFT) return set_err(GLASS_ERR_SIZE, "dlogl_batch: template size above NFFT");
   cudaError_t e = fd_dlogl_launch(ctx->bank, ctx->tab, ctx->work, precision, nitems, item_seg, params, term_x, dlogl,
-                                  term_y, hh, status, ctx->num_sms, ctx->stream, &nl);
+                                  term_y, hh, status, ctx->n_fixed, ctx->num_sms, ctx->stream, &nl);
   ctx->last_launches = nl;
   if (e != cudaSuccess) return cuda_err(e, "dlogl_batch launch");
   return GLASS_OK;
@@ -320,6 +348,61 @@ extern "C" int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int
   if (hh) GLASS_CUDA(cudaMemcpyAsync(hh, d_hh, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H hh");
   if (status) GLASS_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int) * nd, cudaMemcpyDeviceToHost, s), "D2H status");
   GLASS_CUDA(cudaStreamSynchronize(s), "dlogl_batch_host sync");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_grad_fisher_batch(glass_gpu_ctx *ctx, int nitems, const int *item_seg,
+                                           const double *params, int fisher_mode, double *term_y, double *grad,
+                                           double *fisher, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "grad_fisher_batch: null context");
+  if (nitems < 0) return set_err(GLASS_ERR_ARG, "grad_fisher_batch: negative item count");
+  if (nitems == 0) return GLASS_OK;
+  if (!item_seg || !params || !term_y || !grad) return set_err(GLASS_ERR_ARG, "grad_fisher_batch: null argument");
+  const int n_fixed = ctx->n_fixed;
+  if (n_fixed > 1024 || n_fixed > ctx->bank.NFFT)
+    return set_err(GLASS_ERR_SIZE, "grad_fisher_batch: template size above min(1024, NFFT)");
+  if (fisher_mode != 0 && fisher_mode != 1) return set_err(GLASS_ERR_ARG, "grad_fisher_batch: unknown fisher_mode");
+  if (!ctx->bank.nseg) return set_err(GLASS_ERR_STATE, "grad_fisher_batch: no segment bank uploaded");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_work(ctx, nitems))) return rc;
+  int nl = 0;
+  cudaError_t e = fd_grad_launch(ctx->bank, ctx->tab, ctx->work, nitems, item_seg, params, n_fixed, fisher_mode,
+                                 term_y, grad, fisher, status, ctx->num_sms, ctx->stream, &nl);
+  ctx->last_launches = nl;
+  if (e != cudaSuccess) return cuda_err(e, "grad_fisher_batch launch");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_grad_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const int *item_seg,
+                                                const double *params, int fisher_mode, double *term_y,
+                                                double *grad, double *fisher, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "grad_fisher_batch_host: null context");
+  if (nitems < 0) return set_err(GLASS_ERR_ARG, "grad_fisher_batch_host: negative item count");
+  if (nitems == 0) return GLASS_OK;
+  if (!item_seg || !params || !term_y || !grad) return set_err(GLASS_ERR_ARG, "grad_fisher_batch_host: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  size_t nd = (size_t)nitems;
+  size_t bytes = sizeof(double) * nd * (8 + 1 + 8 + 64) + sizeof(int) * nd * 2 + 256;
+  if ((rc = ensure_stage(ctx, bytes))) return rc;
+  double *d_params = (double *)ctx->d_stage;
+  double *d_ty = d_params + 8 * nd;
+  double *d_g = d_ty + nd;
+  double *d_f = d_g + 8 * nd;
+  int *d_seg = (int *)(d_f + 64 * nd);
+  int *d_st = d_seg + nd;
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d_params, params, sizeof(double) * 8 * nd, cudaMemcpyHostToDevice, s), "H2D params");
+  GLASS_CUDA(cudaMemcpyAsync(d_seg, item_seg, sizeof(int) * nd, cudaMemcpyHostToDevice, s), "H2D item_seg");
+  rc = glass_gpu_grad_fisher_batch(ctx, nitems, d_seg, d_params, fisher_mode, d_ty, d_g, fisher ? d_f : nullptr,
+                                   d_st);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(term_y, d_ty, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H term_y");
+  GLASS_CUDA(cudaMemcpyAsync(grad, d_g, sizeof(double) * 8 * nd, cudaMemcpyDeviceToHost, s), "D2H grad");
+  if (fisher) GLASS_CUDA(cudaMemcpyAsync(fisher, d_f, sizeof(double) * 64 * nd, cudaMemcpyDeviceToHost, s), "D2H fisher");
+  if (status) GLASS_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int) * nd, cudaMemcpyDeviceToHost, s), "D2H status");
+  GLASS_CUDA(cudaStreamSynchronize(s), "grad_fisher_batch_host sync");
   return GLASS_OK;
 }
 
@@ -401,7 +484,6 @@ static int legacy_init() {
   return GLASS_OK;
 }
 
-static int is_pow2_in_range(int n) { return n >= kMinN && n <= kMaxN && (n & (n - 1)) == 0; }
 
 static int bin_index(int N) {
   int b = 0;

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
     const double T = a.T, f0 = p[0] / T;
     int N = 0;
     if (!st) {
-      N = 2 * bandwidth_dev(a.L, a.fstar, f0, p[7] / (T * T), p[1], exp(p[3]), T, a.NFFT);
+      N = a.n_fixed > 0 ? a.n_fixed : 2 * bandwidth_dev(a.L, a.fstar, f0, p[7] / (T * T), p[1], exp(p[3]), T, a.NFFT);
       if (N < kMinN || N > kMaxN) st |= 1;
     }
     int imin = 0;
@@ -76,21 +76,169 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
   plan_bin(a, i, b);
 }
 
-// Mixed-precision plan (see planmix_item).
-__global__ void __launch_bounds__(64) fd_planmix_kernel(PlanArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int b = -1;
-  if (i < a.nitems) {
-    ItemMix c;
-    int st = planmix_item(a, i, 0, c);
-    if (st) {
-      plan_write_skipped(a, i, st);
+// Mixed-precision plan, warp-specialised: GB300's FP64 pipe issues a warp
+// instruction only every few tens of cycles, so the FP64 work of a proposal is
+// split over four warps that run in parallel on different SM sub-partitions:
+// warp 0 the bandwidth rule (FP32, FP64 only near a size boundary) and
+// placement, warp 1 the sky direction and polarisation tensors, warp 2 the
+// polarisation factors, warp 3 the amplitude and carrier constants.  The
+// antenna tensors Mr, Mi are then assembled in FP64 by all 128 threads.
+// Same results as planmix_item.
+__global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
+  __shared__ double s_ep[32][6], s_ec[32][6], s_dp[32][4], s_k[32][3], s_beta[32][2], s_amp[32];
+  __shared__ int s_st[32], s_N[32], s_imin[32];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int i = blockIdx.x * 32 + l;
+  const bool in = i < a.nitems;
+  double p[8];
+  int seg = 0, st = 1;
+  if (in) st = plan_validate(a, i, p, seg);
+  const double T = a.T;
+  if (in && !st) {
+    const double f0 = p[0] / T;
+    if (w == 0) {
+      int N;
+      if (a.n_fixed > 0) {
+        N = a.n_fixed;
+      } else {
+        const float Tf = (float)T, f0f = (float)f0, costhf = (float)p[1];
+        const float fdotf = (float)(p[7] / (T * T));
+        const float ampf = expf((float)p[3]);
+        const float sinthf = sqrtf(fmaxf(0.f, (1.f - costhf) * (1.f + costhf)));
+        const int Nmin = 16;
+        const int half = a.NFFT / 2;
+        const int Nmax = half >= 1 ? (1 << (31 - __clz(half))) : 0;
+        float bw = 2.f * Tf * ((4.f + 6.2831853f * f0f * (float)(kAU / kCLIGHT) * sinthf) / (float)kYEAR +
+                               fabsf(fdotf) * Tf);
+        int DS = pow2_above_f32(bw - 1.f);
+        if (DS < 0) {
+          double fdot = p[7] / (T * T);
+          DS = pow2_above_dev(2 * T * ((4. + kPI2 * f0 * (kAU / kCLIGHT) * sin(acos(p[1]))) / kYEAR + fabs(fdot) * T) - 1);
+        }
+        if (DS > Nmax) DS = Nmax;
+        if (DS < Nmin) DS = Nmin;
+        const float x = f0f / (float)a.fstar;
+        float sx, cx;
+        sincosf(x, &sx, &cx);
+        const float c2x = 2.f * cx * cx - 1.f;
+        const float wf = 6.2831853f * f0f, w2 = wf * wf;
+        const float q1 = 2.0e-5f / f0f, q2 = q1 * q1, q4 = q2 * q2, r1 = 1.0e-4f / f0f;
+        const float red = 1.f + 16.f * (q4 * q4 * q2 + r1 * r1);
+        const float twoL = 2.f * (float)a.L;
+        const float sn4L2 = (16.f / 3.f) * sx * sx *
+                            ((2.f + cx) * (float)(kSPS + kSLOC) +
+                             2.f * (3.f + 2.f * cx + c2x) * ((float)(kSLOC / 2.0) + (float)kSACC / (w2 * w2) * red));
+        const float snrm = ampf * sqrtf(Tf) * sx * twoL / sqrtf(sn4L2);
+        int SS = pow2_above_f32(snrm - 1.f);
+        if (SS < 0) {
+          double sn64 = aenoise_dev(f0, a.L, a.fstar);
+          SS = pow2_above_dev(exp(p[3]) * sqrt(T) * sin(f0 / a.fstar) / sqrt(sn64) - 1);
+        }
+        if (SS > Nmax) SS = Nmax;
+        if (SS < Nmin) SS = Nmin;
+        N = 2 * ((DS > SS) ? DS : SS);
+      }
+      int stw = 0, imin = 0;
+      if (N < kMinN || N > kMaxN) {
+        stw = 1;
+      } else {
+        imin = (int)((long long)(f0 * T) - N / 2) - a.seg_qmin[seg];
+        if (imin >= a.NFFT || imin + N <= 0) stw = 4;
+      }
+      s_st[l] = stw;
+      s_N[l] = N;
+      s_imin[l] = imin;
+    } else if (w == 1) {
+      const double cth = p[1], sth = sqrt(1.0 - cth * cth);
+      double sph, cph;
+      sincos(p[2], &sph, &cph);
+      const double u[3] = {cth * cph, cth * sph, -sth}, v[3] = {sph, -cph, 0.};
+      s_k[l][0] = -sth * cph;
+      s_k[l][1] = -sth * sph;
+      s_k[l][2] = -cth;
+      int idx = 0;
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = r; c < 3; c++, idx++) {
+          s_ep[l][idx] = v[r] * v[c] - u[r] * u[c];
+          s_ec[l][idx] = u[r] * v[c] + v[r] * u[c];
+        }
+      const double bscale = kPI2 * f0 * (kAU / kCLIGHT);
+      s_beta[l][0] = bscale * (-sth * cph);
+      s_beta[l][1] = bscale * (-sth * sph);
+    } else if (w == 2) {
+      const double cosi = p[4];
+      double sinps, cosps;
+      sincos(2. * p[5], &sinps, &cosps);
+      const double Aplus = (1. + cosi * cosi) * 0.5, Across = -cosi;
+      s_dp[l][0] = Aplus * cosps;
+      s_dp[l][1] = -Across * sinps;
+      s_dp[l][2] = -Aplus * sinps;
+      s_dp[l][3] = -Across * cosps;
     } else {
-      a.itemsmix[i] = c;
-      b = fd_bin_of(c.N);
+      s_amp[l] = exp(p[3]);
+    }
+  } else if (w == 0) {
+    s_st[l] = st;
+    s_N[l] = 0;
+    s_imin[l] = 0;
+  }
+  __syncthreads();
+  const int stt = in ? (st | s_st[l]) : 1;
+  // antenna tensors: warp w assembles elements 3w/2 .. of the 12 (Mr, Mi) x 6
+  if (in && !stt) {
+    ItemMix *c = a.itemsmix + i;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const int e = 3 * w + q;  // 0..11: (tensor element, real/imag)
+      const int el = e >> 1;
+      const double DPx = s_dp[l][(e & 1) ? 1 : 0], DCx = s_dp[l][(e & 1) ? 3 : 2];
+      const float m = (float)(DPx * s_ep[l][el] + DCx * s_ec[l][el]);
+      if (e & 1)
+        c->Mi[el] = m;
+      else
+        c->Mr[el] = m;
     }
   }
-  plan_bin(a, i, b);
+  int b = -1;
+  if (w == 0) {
+    if (in && stt) {
+      plan_write_skipped(a, i, stt);
+    } else if (in) {
+      const int N = s_N[l];
+      const double f0 = p[0] / T;
+      const double fT = f0 * T;
+      const long long q = (long long)fT;
+      ItemMix *c = a.itemsmix + i;
+      c->seg = seg;
+      c->N = N;
+      c->imin = s_imin[l];
+      c->pad = 0;
+      c->k[0] = (float)s_k[l][0];
+      c->k[1] = (float)s_k[l][1];
+      c->k[2] = (float)s_k[l][2];
+      c->k[3] = 0.f;
+      const double fdot = p[7] / (T * T);
+      c->fonfs0 = (float)(f0 / a.fstar);
+      c->fdfs = (float)(fdot * T / a.fstar);
+      c->aef = (float)(0.66666666666666666666 * fdot * T / f0);
+      c->w0c = (float)(kPI2 * f0 / kCLIGHT);
+      c->p7pi = (float)(kPI * fdot * T * T);
+      const double sc = s_amp[l] / (2.0 * (double)N);
+      c->amp_hi = (float)sc;
+      c->amp_lo = (float)(sc - (double)c->amp_hi);
+      c->pad2 = 0.f;
+      c->eps2pi = df_from_double(kPI2 * (fT - (double)q));
+      c->beta1 = df_from_double(s_beta[l][0]);
+      c->beta2 = df_from_double(s_beta[l][1]);
+      c->phi0 = df_from_double(p[6]);
+      c->p7pi_d = df_from_double(kPI * fdot * T * T);
+      c->pad3 = {0.f, 0.f};
+      b = fd_bin_of(N);
+    }
+    plan_bin(a, i, b);
+  }
 }
 
 // ------------------------------------------------------------ orbit tables
@@ -223,7 +371,7 @@ void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg
 // --------------------------------------------------------------- launchers
 cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int precision,
                             int nitems, const int *item_seg, const double *params, const double *term_x,
-                            double *dlogl, double *term_y, double *hh, int *status, int num_sms,
+                            double *dlogl, double *term_y, double *hh, int *status, int n_fixed, int num_sms,
                             cudaStream_t stream, int *nlaunch) {
   cudaError_t e;
   int launches = 0;
@@ -236,6 +384,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.NFFT = bank.NFFT;
   pa.cap = work.cap;
   pa.precision = precision;
+  pa.n_fixed = n_fixed;
   pa.T = bank.T;
   pa.fstar = bank.fstar;
   pa.L = kLARM;
@@ -252,7 +401,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.hh = hh;
   pa.status = status;
   if (mix)
-    fd_planmix_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(pa);
+    fd_planmix_kernel<<<(nitems + 31) / 32, 128, 0, stream>>>(pa);
   else
     fd_plan64_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(pa);
   launches++;

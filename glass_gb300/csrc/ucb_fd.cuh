@@ -17,6 +17,7 @@ struct FdBankDev {
   double *Q = nullptr;         // [nseg*(NFFT+1)] prefix sums of |w|^2 over both channels (FP64)
   double2 *w64 = nullptr;      // [nseg*NFFT*2] {A}, {E}
   double2 *g64 = nullptr;      // [nseg*NFFT*4] GA2, GA1, GE2, GE1
+  float2 *invc = nullptr;      // [nseg*NFFT] invC_A, invC_E (reference-indexed Fisher weights)
 };
 
 // Per-size tables (orbit samples and FFT twiddles) for the bank's (T, t0).
@@ -39,6 +40,7 @@ struct FdWorkDev {
   size_t series_bytes = 0;      // capacity of `series`
   ItemF64 *items64 = nullptr;   // [cap]
   ItemMix *itemsmix = nullptr;  // [cap]
+  ItemGrad *itemsgrad = nullptr;  // [cap]
   int *bin_count = nullptr;     // [kNumBins]
   int *bin_list = nullptr;      // [kNumBins*cap]
   void *series = nullptr;       // 4 arm-combination series per proposal
@@ -55,12 +57,20 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
 // through *nlaunch.
 cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int precision,
                             int nitems, const int *item_seg, const double *params, const double *term_x,
-                            double *dlogl, double *term_y, double *hh, int *status, int num_sms,
+                            double *dlogl, double *term_y, double *hh, int *status, int n_fixed, int num_sms,
                             cudaStream_t stream, int *nlaunch);
 
 // Bytes of series scratch a batch of nitems proposals on segments of NFFT bins
 // can need (every N is at most NFFT).
 size_t fd_series_bytes(int nitems, int NFFT, int precision);
+
+// Gradient of delta logL and Fisher matrix (ucb_grad.cu).  Sizes up to 1024;
+// larger templates get status GLASS_ITEM_NONFINITE.
+size_t fd_grad_series_bytes(int nitems, int NFFT);
+cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int nitems,
+                           const int *item_seg, const double *params, int N_fixed, int fisher_mode, double *term_y,
+                           double *grad, double *fisher, int *status, int num_sms, cudaStream_t stream,
+                           int *nlaunch);
 
 // Single waveform in the reference's output layout (legacy ucb_waveform).
 // pos: N orbit samples (device), out: 10*N doubles (device) = X,Y,Z,A,E.

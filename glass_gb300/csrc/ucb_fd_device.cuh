@@ -442,6 +442,7 @@ __device__ __forceinline__ void ae_combos(const C d[6], C out[4]) {
 // ------------------------------------------------------------- kernel args
 struct PlanArgs {
   int nitems, nseg, NFFT, cap, precision;
+  int n_fixed;  // 0: bandwidth rule
   double T, fstar, L;
   const int *item_seg;
   const double *params;

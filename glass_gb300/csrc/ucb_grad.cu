@@ -1,0 +1,593 @@
+// Gradient of delta logL and Fisher matrix of UCB proposals, by tangent
+// (forward-mode) propagation through the mixed-precision waveform, replacing
+// the reference's finite-difference ucb_fisher (ucb/src/glass_ucb_waveform.c:364-522),
+// which costs eight extra waveforms per source.
+//
+// Structure of the template used here (ucb/src/glass_ucb_waveform.c:822-922):
+// every arm series is  d = S P e^{-i theta}  with S = sinc(arg1) aevol / 4,
+// P = DP dplus + DC dcross (DP, DC complex polarisation factors) and
+// theta = arg1 - arg2.  Hence
+//   * ln A and phi0 act as  dh/dlnA = h,  dh/dphi0 = -i h  (exact);
+//   * cos(iota) and psi enter only through DP, DC: h = DP H+ + DC Hx with H+,
+//     Hx the responses to unit factors, so two basis templates give both;
+//   * f0, fdot and the sky angles need tangent templates
+//       dd = d (d ln S - i d theta) + S dP e^{-i theta}
+//     propagated sample by sample (FP32: a derivative needs relative, not
+//     absolute, phase accuracy).
+// Six templates (H+, Hx, T_f0, T_fdot, T_costheta, T_phi) x four A/E series are
+// FFT'd; per bin the eight derivatives are assembled and
+//   grad_k = (r - h | dh/dp_k),   F_kl = (dh/dp_k | dh/dp_l)
+// accumulated (inner product of utils/src/glass_math.c:362-380).
+#include "ucb_fd_device.cuh"
+
+namespace glass {
+
+constexpr int kGradTemplates = 6;
+constexpr int kGradSeries = 4 * kGradTemplates;
+constexpr int kGradMaxN = 1024;
+
+// sinc'(x) = (x cos x - sin x)/x^2: Taylor series through x^11 for |x| <= 1.
+__device__ __forceinline__ float dsinc_f(float x) {
+  if (fabsf(x) > 1.0f) {
+    float s, c;
+    sincosf(x, &s, &c);
+    return (x * c - s) / (x * x);
+  }
+  const float x2 = x * x;
+  float p = 1.9270852604024e-09f;      // 12/13!
+  p = fmaf(p, x2, -2.505210838544172e-07f);  // -10/11!
+  p = fmaf(p, x2, 2.2045855379188714e-05f);  // 8/9!
+  p = fmaf(p, x2, -1.1904761904761906e-03f); // -6/7!
+  p = fmaf(p, x2, 3.3333333333333333e-02f);  // 4/5!
+  p = fmaf(p, x2, -0.33333333333333333f);    // -2/3!
+  return p * x;
+}
+
+struct GradPlanArgs {
+  PlanArgs base;
+  int N_fixed;
+  ItemGrad *items;
+  double *grad, *fisher;
+};
+
+__global__ void __launch_bounds__(64) fd_plangrad_kernel(GradPlanArgs ga) {
+  const PlanArgs &a = ga.base;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int b = -1;
+  if (i < a.nitems) {
+    ItemMix c;
+    int st = planmix_item(a, i, ga.N_fixed, c);
+    if (st) {
+      plan_write_skipped(a, i, st);
+      const double v = (st & 3) ? __longlong_as_double(0x7ff8000000000000ULL) : 0.0;
+      for (int k = 0; k < 8; k++) ga.grad[8 * (size_t)i + k] = v;
+      if (ga.fisher)
+        for (int k = 0; k < 64; k++) ga.fisher[64 * (size_t)i + k] = v;
+    } else {
+      ItemGrad g;
+      g.m = c;
+      const double *p = a.params + 8 * (size_t)i;
+      const double T = a.T;
+      const double cth = p[1];
+      double sth = sqrt(1.0 - cth * cth);
+      if (sth < 1e-9) sth = 1e-9;  // d/dcos(theta) is singular at the poles
+      double sph, cph;
+      sincos(p[2], &sph, &cph);
+      const double u[3] = {cth * cph, cth * sph, -sth}, v[3] = {sph, -cph, 0.};
+      const double du_c[3] = {cph, sph, cth / sth}, dv_c[3] = {0., 0., 0.};
+      const double du_p[3] = {-cth * sph, cth * cph, 0.}, dv_p[3] = {cph, sph, 0.};
+      g.dk_c[0] = (float)(cth / sth * cph);
+      g.dk_c[1] = (float)(cth / sth * sph);
+      g.dk_c[2] = -1.f;
+      g.dk_c[3] = 0.f;
+      g.dk_p[0] = (float)(sth * sph);
+      g.dk_p[1] = (float)(-sth * cph);
+      g.dk_p[2] = 0.f;
+      g.dk_p[3] = 0.f;
+      int idx = 0;
+      for (int r = 0; r < 3; r++)
+        for (int s = r; s < 3; s++, idx++) {
+          g.ep[idx] = (float)(v[r] * v[s] - u[r] * u[s]);
+          g.ec[idx] = (float)(u[r] * v[s] + v[r] * u[s]);
+          g.dep_c[idx] = (float)(dv_c[r] * v[s] + v[r] * dv_c[s] - du_c[r] * u[s] - u[r] * du_c[s]);
+          g.dec_c[idx] = (float)(du_c[r] * v[s] + u[r] * dv_c[s] + dv_c[r] * u[s] + v[r] * du_c[s]);
+          g.dep_p[idx] = (float)(dv_p[r] * v[s] + v[r] * dv_p[s] - du_p[r] * u[s] - u[r] * du_p[s]);
+          g.dec_p[idx] = (float)(du_p[r] * v[s] + u[r] * dv_p[s] + dv_p[r] * u[s] + v[r] * du_p[s]);
+        }
+      const double ci = p[4];
+      double s2, c2;
+      sincos(2.0 * p[5], &s2, &c2);
+      const double Ap = 0.5 * (1.0 + ci * ci);
+      g.DP[0] = (float)(Ap * c2);
+      g.DP[1] = (float)(ci * s2);
+      g.DC[0] = (float)(-Ap * s2);
+      g.DC[1] = (float)(ci * c2);
+      g.dDP_i[0] = (float)(ci * c2);
+      g.dDP_i[1] = (float)s2;
+      g.dDC_i[0] = (float)(-ci * s2);
+      g.dDC_i[1] = (float)c2;
+      g.dDP_s[0] = (float)(-2.0 * Ap * s2);
+      g.dDP_s[1] = (float)(2.0 * ci * c2);
+      g.dDC_s[0] = (float)(-2.0 * Ap * c2);
+      g.dDC_s[1] = (float)(-2.0 * ci * s2);
+      g.f0 = (float)(p[0] / T);
+      g.fdot = (float)(p[7] / (T * T));
+      g.invT = (float)(1.0 / T);
+      g.fstar = (float)a.fstar;
+      ga.items[i] = g;
+      b = fd_bin_of(c.N);
+    }
+  }
+  plan_bin(a, i, b);
+}
+
+// Combination coefficients of the four A/E series per directed arm
+// (12, 13, 21, 23, 31, 32): a2, a1, e2, e1 (see ae_combos).
+__constant__ float kComboCoef[4][6] = {
+    {-1.f, 1.f, 0.f, 0.f, 1.f, -1.f},  // a2 = d31 - d32 - d12 + d13
+    {0.f, 1.f, -1.f, -1.f, 1.f, 0.f},  // a1 = d13 - d23 - d21 + d31
+    {1.f, -1.f, 2.f, -2.f, 1.f, -1.f}, // e2 = d12 - d13 + 2 d21 - 2 d23 + d31 - d32
+    {2.f, 1.f, 1.f, -1.f, -1.f, -2.f}, // e1 = 2 d12 + d13 + d21 - d23 - d31 - 2 d32
+};
+
+struct GradSlowArgs {
+  int cap, NFFT;
+  float Rf, invLf, AUcf, invTf, AUf;
+  const int *bin_count, *bin_list;
+  const ItemGrad *items;
+  const OrbitSampleMix *mix[kNumBins];
+  float2 *series;  // 24 series of N per proposal, sizes back to back
+};
+
+// One thread per (proposal, sample): the 6 templates' arm values, combined
+// into their 4 A/E series each.
+__global__ void __launch_bounds__(128) fd_gradslow_kernel(GradSlowArgs a) {
+  int cs[kNumBins + 1];
+  int acc = 0;
+#pragma unroll
+  for (int b = 0; b < kNumBins; b++) {
+    cs[b] = acc;
+    if ((32 << b) <= a.NFFT) acc += a.bin_count[b] << b;
+  }
+  cs[kNumBins] = acc;
+  const int nchunks = acc;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+#pragma unroll 1
+  for (int ch = warp; ch < nchunks; ch += nwarps) {
+    int b = 0, cb = 0;
+#pragma unroll
+    for (int bb = 1; bb < kNumBins; bb++)
+      if (ch >= cs[bb]) {
+        b = bb;
+        cb = cs[bb];
+      }
+    const int N = 32 << b;
+    const int local = ch - cb;
+    const int slot = local >> b;
+    const int n = ((local & ((1 << b) - 1)) << 5) + lane;
+    const ItemGrad &g = a.items[a.bin_list[(size_t)b * a.cap + slot]];
+    const ItemMix &c = g.m;
+    const OrbitSampleMix o = a.mix[b][n];
+
+    // ---- geometry (as slow_sample_mix), plus absolute positions for d tau/dk
+    const float ca = o.ca_hi, sa = o.sa_hi;
+    const float sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
+    const float sbf[3] = {0.0f, 0.866025403784439f, -0.866025403784438f};
+    const float cbf[3] = {1.0f, -0.5f, -0.5f};
+    float dx[3], dy[3], dz[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      dx[i] = a.Rf * (saca * sbf[i] - (1.f + sa2) * cbf[i]);
+      dy[i] = a.Rf * (saca * cbf[i] - (1.f + ca2) * sbf[i]);
+      dz[i] = -1.73205080757f * a.Rf * (ca * cbf[i] + sa * sbf[i]);
+    }
+    // carrier phase (double-float) common to the three spacecraft
+    const df u = {o.u_hi, o.u_lo};
+    const df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
+    df ph = df_mul(c.eps2pi, u);
+    ph = df_add(ph, df_neg(df_add(df_mul(c.beta1, cad), df_mul(c.beta2, sad))));
+    ph = df_add(ph, df_neg(c.phi0));
+    ph = df_add(ph, df_mul(c.p7pi_d, df_mul(u, u)));
+    const float psi0 = df_reduce_2pi(ph);
+    const float uf = o.u_hi;
+    const float tgc = a.AUcf * (c.k[0] * ca + c.k[1] * sa);
+    const float gx = a.AUf * ca, gy = a.AUf * sa;  // guiding centre (m)
+    float fon[3], arg2[3], aev[3], vv[3], wxi[3], dtc[3], dtp[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float kdx = c.k[0] * dx[i] + c.k[1] * dy[i] + c.k[2] * dz[i];
+      const float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
+      const float tT = taui * a.invTf;
+      const float v = uf - tT;  // xi / T
+      vv[i] = v;
+      fon[i] = fmaf(c.fdfs, v, c.fonfs0);
+      aev[i] = fmaf(c.aef, v, 1.0f);
+      arg2[i] = psi0 - c.w0c * kdx + c.p7pi * tT * (tT - 2.0f * uf);
+      // d arg2 / d xi and d tau / d(cos theta), d tau / d phi
+      wxi[i] = 6.2831853f * fmaf(g.fdot, v / a.invTf, g.f0);
+      const float X = gx + dx[i], Y = gy + dy[i], Z = dz[i];
+      dtc[i] = (g.dk_c[0] * X + g.dk_c[1] * Y + g.dk_c[2] * Z) * (float)(1.0 / kCLIGHT);
+      dtp[i] = (g.dk_p[0] * X + g.dk_p[1] * Y + g.dk_p[2] * Z) * (float)(1.0 / kCLIGHT);
+    }
+    // unique arms 12, 13, 23
+    float r[3][3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const int i0 = q == 2 ? 1 : 0, i1 = q == 0 ? 1 : 2;
+      r[q][0] = (dx[i1] - dx[i0]) * a.invLf;
+      r[q][1] = (dy[i1] - dy[i0]) * a.invLf;
+      r[q][2] = (dz[i1] - dz[i0]) * a.invLf;
+    }
+    float2 accs[kGradSeries];
+#pragma unroll
+    for (int s = 0; s < kGradSeries; s++) accs[s] = make_float2(0.f, 0.f);
+
+    const float invfsT = a.invTf / g.fstar;
+    const float f0T = g.f0 / a.invTf;  // f0 T
+#pragma unroll
+    for (int arm = 0; arm < 6; arm++) {
+      // directed arm -> (spacecraft i, unique arm q, orientation sign)
+      const int i = arm >> 1;
+      const int q = (arm == 0 || arm == 2) ? 0 : (arm == 1 || arm == 4) ? 1 : 2;
+      const float sg = (arm == 2 || arm == 4 || arm == 5) ? -1.f : 1.f;
+      const float rx = r[q][0], ry = r[q][1], rz = r[q][2];
+      const float dp = quad(g.ep, rx, ry, rz), dc = quad(g.ec, rx, ry, rz);
+      const float kr = sg * (c.k[0] * rx + c.k[1] * ry + c.k[2] * rz);
+      const float dkr_c = sg * (g.dk_c[0] * rx + g.dk_c[1] * ry + g.dk_c[2] * rz);
+      const float dkr_p = sg * (g.dk_p[0] * rx + g.dk_p[1] * ry + g.dk_p[2] * rz);
+      const float arg1 = 0.5f * fon[i] * (1.0f + kr);
+      const float sn = sinc_f(arg1);
+      const float gS = dsinc_f(arg1) / sn;
+      const float S = 0.25f * sn * aev[i];
+      float sth, cth;
+      fast_sincos(arg1 - arg2[i], &sth, &cth);
+      const float2 E = make_float2(cth, -sth);
+      const float2 SE = make_float2(S * E.x, S * E.y);
+      const float2 Pc = make_float2(g.DP[0] * dp + g.DC[0] * dc, g.DP[1] * dp + g.DC[1] * dc);
+      const float2 d = cmul(Pc, SE);
+      const float2 Bp = make_float2(dp * SE.x, dp * SE.y);
+      const float2 Bx = make_float2(dc * SE.x, dc * SE.y);
+      // f0 (params[0] = f0 T)
+      const float dA1_0 = 0.5f * (1.0f + kr) * invfsT;
+      const float dth_0 = dA1_0 - 6.2831853f * vv[i];
+      const float dlS_0 = gS * dA1_0 - c.aef * vv[i] / (f0T * aev[i]);
+      const float2 T0 = cmul(d, make_float2(dlS_0, -dth_0));
+      // fdot (params[7] = fdot T^2)
+      const float dA1_7 = dA1_0 * vv[i];
+      const float dth_7 = dA1_7 - 3.14159265f * vv[i] * vv[i];
+      const float dlS_7 = gS * dA1_7 + 0.6666667f * vv[i] / (f0T * aev[i]);
+      const float2 T7 = cmul(d, make_float2(dlS_7, -dth_7));
+      // cos(theta)
+      const float dA1_c = 0.5f * fon[i] * dkr_c;
+      const float dth_c = dA1_c + wxi[i] * dtc[i];
+      const float dpc = quad(g.dep_c, rx, ry, rz), dcc = quad(g.dec_c, rx, ry, rz);
+      const float2 dPc = make_float2(g.DP[0] * dpc + g.DC[0] * dcc, g.DP[1] * dpc + g.DC[1] * dcc);
+      const float2 Tc = cadd(cmul(d, make_float2(gS * dA1_c, -dth_c)), cmul(dPc, SE));
+      // phi
+      const float dA1_p = 0.5f * fon[i] * dkr_p;
+      const float dth_p = dA1_p + wxi[i] * dtp[i];
+      const float dpp = quad(g.dep_p, rx, ry, rz), dcp = quad(g.dec_p, rx, ry, rz);
+      const float2 dPp = make_float2(g.DP[0] * dpp + g.DC[0] * dcp, g.DP[1] * dpp + g.DC[1] * dcp);
+      const float2 Tp = cadd(cmul(d, make_float2(gS * dA1_p, -dth_p)), cmul(dPp, SE));
+      const float2 vals[kGradTemplates] = {Bp, Bx, T0, T7, Tc, Tp};
+#pragma unroll
+      for (int t = 0; t < kGradTemplates; t++)
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+          const float cf = kComboCoef[s][arm];
+          accs[4 * t + s].x = fmaf(cf, vals[t].x, accs[4 * t + s].x);
+          accs[4 * t + s].y = fmaf(cf, vals[t].y, accs[4 * t + s].y);
+        }
+    }
+    float2 *out = a.series + ((long long)cb * 32 + (long long)slot * N) * kGradSeries + n;
+#pragma unroll
+    for (int s = 0; s < kGradSeries; s++) out[(size_t)s * N] = accs[s];
+  }
+}
+
+struct GradSpecArgs {
+  int NFFT, cap, bin, fisher_mode;
+  const int *bin_count;
+  const int *bin_list;
+  const ItemGrad *items;
+  const float2 *series;
+  const float2 *tw;
+  const float4 *w32, *w32lo, *g32;
+  const float2 *invc;  // invC_A, invC_E per segment bin (reference-indexed Fisher)
+  const double *Q;
+  double *term_y, *grad, *fisher;
+  int *status;
+};
+
+template <int N>
+struct GradCfg {
+  static constexpr int GT = N / 4;
+  static constexpr int CTA = GT >= 64 ? GT : 128;
+  static constexpr int GPC = CTA / GT;
+  static constexpr int NACC = 8 + 36;  // gradient, Fisher upper triangle
+  static constexpr size_t group_floats2 = 16 * (size_t)N;  // 4 N FFT buffer + 12 N whitened values
+  static constexpr size_t bytes = sizeof(float2) * (N + GPC * group_floats2) + sizeof(float2) * 32 * GPC;
+};
+
+template <int N>
+__global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecArgs a) {
+  using Cfg = GradCfg<N>;
+  constexpr int GT = Cfg::GT, GPC = Cfg::GPC, NACC = Cfg::NACC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+  float2 *groups = tw + N;
+  float2 *redall = groups + GPC * Cfg::group_floats2;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw[i];
+  __syncthreads();
+  const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
+  float2 *fbuf = groups + g * Cfg::group_floats2;  // 4 N
+  float2 *wbuf = fbuf + 4 * N;                      // 12 N: [(2 t + ch) N + k]
+  float *part = reinterpret_cast<float *>(fbuf);    // reduction scratch after use
+  float2 *red = redall + 32 * g;
+  const int count = a.bin_count[a.bin];
+  const float2 *series = a.series + bin_sample_start(a.bin_count, a.NFFT, a.bin) * kGradSeries;
+  const int NFFT = a.NFFT;
+
+  for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC) {
+    const int slot = base + g;
+    const bool valid = slot < count;
+    const int sl = valid ? slot : count - 1;
+    const int item = a.bin_list[sl];
+    const ItemGrad &it = a.items[item];
+    const int seg = it.m.seg, imin = it.m.imin;
+    const float2 *src = series + (size_t)sl * kGradSeries * N;
+    // FFT each template's four series and whiten/weight them per bin
+#pragma unroll 1
+    for (int t = 0; t < kGradTemplates; t++) {
+#pragma unroll
+      for (int s = 0; s < 4; s++)
+#pragma unroll
+        for (int r = 0; r < 4; r++) fbuf[s * N + lane + GT * r] = src[(size_t)(4 * t + s) * N + lane + GT * r];
+      group_sync<GT>();
+      group_fft<N, GT, 4, 4>(fbuf, tw, lane);
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        const int k = lane + GT * r;
+        const int m = (k + N / 2) & (N - 1);
+        const int j = imin + m;
+        float2 vA = make_float2(0.f, 0.f), vE = vA;
+        if (j >= 0 && j < NFFT) {
+          const size_t sj = (size_t)seg * NFFT + j;
+          const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
+          vA = cadd(cmul(fbuf[k], make_float2(gA.x, gA.y)), cmul(fbuf[N + k], make_float2(gA.z, gA.w)));
+          vE = cadd(cmul(fbuf[2 * N + k], make_float2(gE.x, gE.y)), cmul(fbuf[3 * N + k], make_float2(gE.z, gE.w)));
+        }
+        wbuf[(2 * t) * N + k] = vA;
+        wbuf[(2 * t + 1) * N + k] = vE;
+      }
+      group_sync<GT>();
+    }
+    // assemble the eight derivatives per bin and accumulate
+    float accg[NACC];
+#pragma unroll
+    for (int q = 0; q < NACC; q++) accg[q] = 0.f;
+    float racc = 0.f;
+    const float s = it.m.amp_hi;
+    const float2 DP = make_float2(it.DP[0], it.DP[1]), DC = make_float2(it.DC[0], it.DC[1]);
+    const float2 dDPi = make_float2(it.dDP_i[0], it.dDP_i[1]), dDCi = make_float2(it.dDC_i[0], it.dDC_i[1]);
+    const float2 dDPs = make_float2(it.dDP_s[0], it.dDP_s[1]), dDCs = make_float2(it.dDC_s[0], it.dDC_s[1]);
+#pragma unroll 1
+    for (int r = 0; r < 4; r++) {
+      const int k = lane + GT * r;
+      const int m = (k + N / 2) & (N - 1);
+      const int j = imin + m;
+      if (j < 0 || j >= NFFT) continue;
+      const size_t sj = (size_t)seg * NFFT + j;
+      const float4 w = a.w32[sj], wl = a.w32lo[sj];
+      float qw[2] = {1.f, 1.f};
+      if (a.fisher_mode == 1) {
+        const float2 ic_t = a.invc[(size_t)seg * NFFT + m], ic_j = a.invc[sj];
+        qw[0] = ic_t.x / ic_j.x;
+        qw[1] = ic_t.y / ic_j.y;
+      }
+#pragma unroll
+      for (int ch = 0; ch < 2; ch++) {
+        const float2 Hp = cscale(wbuf[(0 + ch) * N + k], s), Hx = cscale(wbuf[(2 + ch) * N + k], s);
+        const float2 h = cadd(cmul(DP, Hp), cmul(DC, Hx));
+        float2 D[8];
+        D[0] = cscale(wbuf[(4 + ch) * N + k], s);
+        D[1] = cscale(wbuf[(8 + ch) * N + k], s);
+        D[2] = cscale(wbuf[(10 + ch) * N + k], s);
+        D[3] = h;
+        D[4] = cadd(cmul(dDPi, Hp), cmul(dDCi, Hx));
+        D[5] = cadd(cmul(dDPs, Hp), cmul(dDCs, Hx));
+        D[6] = cmi(h);
+        D[7] = cscale(wbuf[(6 + ch) * N + k], s);
+        const float wr = ch ? w.z : w.x, wi = ch ? w.w : w.y;
+        const float lr = ch ? wl.z : wl.x, li = ch ? wl.w : wl.y;
+        const float rr = (wr - h.x) + lr, ri = (wi - h.y) + li;
+        racc += fmaf(rr, rr, ri * ri);
+#pragma unroll
+        for (int p = 0; p < 8; p++) accg[p] += 2.f * fmaf(rr, D[p].x, ri * D[p].y);
+        int q = 8;
+#pragma unroll
+        for (int p = 0; p < 8; p++)
+#pragma unroll
+          for (int l = p; l < 8; l++, q++) accg[q] += 2.f * qw[ch] * fmaf(D[p].x, D[l].x, D[p].y * D[l].y);
+      }
+    }
+    // reduce over the group: per-thread partials in shared memory (reusing the
+    // FFT and whitened-value buffers once every thread is done with them)
+    group_sync<GT>();
+#pragma unroll
+    for (int q = 0; q < NACC; q++) part[q * GT + lane] = accg[q];
+    const df rs = group_sum_df<GT>(racc, red, lane);
+    group_sync<GT>();
+    for (int q = lane; q < NACC; q += GT) {
+      float sum = 0.f;
+      for (int t = 0; t < GT; t++) sum += part[q * GT + t];
+      part[q * GT] = sum;  // column head
+    }
+    group_sync<GT>();
+    if (valid) {
+      for (int q = lane; q < NACC; q += GT) {
+        const double v = (double)part[q * GT];
+        if (q < 8) {
+          a.grad[8 * (size_t)item + q] = v;
+        } else if (a.fisher) {
+          int qq = q - 8, p = 0;
+          while (qq >= 8 - p) {
+            qq -= 8 - p;
+            p++;
+          }
+          const int l = p + qq;
+          a.fisher[64 * (size_t)item + 8 * p + l] = v;
+          a.fisher[64 * (size_t)item + 8 * l + p] = v;
+        }
+      }
+      if (lane == 0) {
+        const int jlo = imin < 0 ? 0 : imin;
+        const int jhi = imin + N > NFFT ? NFFT : imin + N;
+        const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
+        const double term = (Qs[jhi] - Qs[jlo]) - ((double)rs.hi + (double)rs.lo);
+        a.term_y[item] = term;
+        if (a.status) a.status[item] = isfinite(term) ? 0 : 1;
+      }
+    }
+    group_sync<GT>();
+  }
+}
+
+template <int N>
+static cudaError_t launch_gradspec(const GradSpecArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
+  using Cfg = GradCfg<N>;
+  size_t smem = Cfg::bytes;
+  static int occ = -1;
+  if (occ < 0) {
+    cudaError_t e = cudaFuncSetAttribute(fd_gradspec_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_gradspec_kernel<N>, Cfg::CTA, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  int need = (nitems_bound + Cfg::GPC - 1) / Cfg::GPC;
+  int grid = occ * num_sms;
+  if (need < grid) grid = need;
+  if (grid < 1) grid = 1;
+  fd_gradspec_kernel<N><<<grid, Cfg::CTA, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+size_t fd_grad_series_bytes(int nitems, int NFFT) {
+  int nmax = NFFT < kGradMaxN ? NFFT : kGradMaxN;
+  return (size_t)nitems * (size_t)nmax * kGradSeries * sizeof(float2);
+}
+
+cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int nitems,
+                           const int *item_seg, const double *params, int N_fixed, int fisher_mode, double *term_y,
+                           double *grad, double *fisher, int *status, int num_sms, cudaStream_t stream,
+                           int *nlaunch) {
+  cudaError_t e;
+  int launches = 0;
+  if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kNumBins, stream)) != cudaSuccess) return e;
+  GradPlanArgs ga;
+  PlanArgs &pa = ga.base;
+  pa.nitems = nitems;
+  pa.nseg = bank.nseg;
+  // sizes above kGradMaxN are refused through the bandwidth cap
+  pa.NFFT = bank.NFFT < kGradMaxN ? bank.NFFT : kGradMaxN;
+  pa.cap = work.cap;
+  pa.precision = 1;
+  pa.n_fixed = N_fixed;
+  pa.T = bank.T;
+  pa.fstar = bank.fstar;
+  pa.L = kLARM;
+  pa.item_seg = item_seg;
+  pa.params = params;
+  pa.term_x = nullptr;
+  pa.seg_qmin = bank.qmin;
+  pa.items64 = nullptr;
+  pa.itemsmix = nullptr;
+  pa.bin_count = work.bin_count;
+  pa.bin_list = work.bin_list;
+  pa.dlogl = term_y;
+  pa.term_y = nullptr;
+  pa.hh = nullptr;
+  pa.status = status;
+  ga.N_fixed = N_fixed;
+  ga.items = work.itemsgrad;
+  ga.grad = grad;
+  ga.fisher = fisher;
+  fd_plangrad_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(ga);
+  launches++;
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+
+  GradSlowArgs sa;
+  sa.cap = work.cap;
+  sa.NFFT = pa.NFFT;
+  sa.Rf = (float)(kAU * (kLARM / (2.0 * kSQ3 * kAU)));
+  sa.invLf = (float)(1.0 / kLARM);
+  sa.AUcf = (float)(kAU / kCLIGHT);
+  sa.invTf = (float)(1.0 / bank.T);
+  sa.AUf = (float)kAU;
+  sa.bin_count = work.bin_count;
+  sa.bin_list = work.bin_list;
+  sa.items = work.itemsgrad;
+  for (int b = 0; b < kNumBins; b++) sa.mix[b] = tab.mix[b];
+  sa.series = reinterpret_cast<float2 *>(work.series);
+  {
+    static int occ = -1;
+    if (occ < 0) {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_gradslow_kernel, 128, 0);
+      if (e != cudaSuccess) return e;
+      if (occ < 1) occ = 1;
+    }
+    fd_gradslow_kernel<<<occ * num_sms, 128, 0, stream>>>(sa);
+    launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+
+  GradSpecArgs a;
+  a.NFFT = bank.NFFT;
+  a.cap = work.cap;
+  a.fisher_mode = fisher_mode;
+  a.bin_count = work.bin_count;
+  a.items = work.itemsgrad;
+  a.series = reinterpret_cast<const float2 *>(work.series);
+  a.w32 = bank.w32;
+  a.w32lo = bank.w32lo;
+  a.g32 = bank.g32;
+  a.invc = bank.invc;
+  a.Q = bank.Q;
+  a.term_y = term_y;
+  a.grad = grad;
+  a.fisher = fisher;
+  a.status = status;
+  if ((e = cudaEventRecord(work.fork, stream)) != cudaSuccess) return e;
+  int nb = 0;
+  for (int b = 0; b < kNumBins; b++) {
+    const int N = 32 << b;
+    if (N > pa.NFFT) break;
+    cudaStream_t sb = work.side[b];
+    if ((e = cudaStreamWaitEvent(sb, work.fork, 0)) != cudaSuccess) return e;
+    a.bin = b;
+    a.bin_list = work.bin_list + (size_t)b * work.cap;
+    a.tw = tab.tw32[b];
+    switch (N) {
+      case 32: e = launch_gradspec<32>(a, nitems, num_sms, sb); break;
+      case 64: e = launch_gradspec<64>(a, nitems, num_sms, sb); break;
+      case 128: e = launch_gradspec<128>(a, nitems, num_sms, sb); break;
+      case 256: e = launch_gradspec<256>(a, nitems, num_sms, sb); break;
+      case 512: e = launch_gradspec<512>(a, nitems, num_sms, sb); break;
+      case 1024: e = launch_gradspec<1024>(a, nitems, num_sms, sb); break;
+      default: e = cudaErrorInvalidValue;
+    }
+    launches++;
+    if (e != cudaSuccess) return e;
+    if ((e = cudaEventRecord(work.join[b], sb)) != cudaSuccess) return e;
+    nb++;
+  }
+  for (int b = 0; b < nb; b++)
+    if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;
+  if (nlaunch) *nlaunch = launches;
+  return cudaSuccess;
+}
+
+}  // namespace glass

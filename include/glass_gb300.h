@@ -99,6 +99,12 @@ const char *glass_gpu_last_error(void);
 int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, double t0, int NFFT, int nseg, const int *qmin,
                           const double *rA, const double *rE, const double *invCA, const double *invCE);
 
+/* Template size of the batched evaluations: 0 (the default) takes N from the
+ * reference's bandwidth rule (ucb_alignment, ucb/src/glass_ucb_waveform.c:727),
+ * otherwise every proposal uses this N (a power of two in [32, min(4096,
+ * NFFT)]), as a caller of ucb_waveform chooses BW. */
+int glass_gpu_set_template_size(glass_gpu_ctx *ctx, int n);
+
 /* Replace the residual of one segment (after an accepted move changed the
  * other sources of its chain).  Host pointers, 2*NFFT doubles each. */
 int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const double *rA, const double *rE);
@@ -127,6 +133,31 @@ int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const i
 int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
                                const double *params, const double *term_x, double *dlogl, double *term_y, double *hh,
                                int *status);
+
+/*
+ * Gradient of delta logL and Fisher matrix of a batch of proposals, by tangent
+ * propagation through the mixed-precision waveform; replaces the reference's
+ * finite-difference ucb_fisher (ucb/src/glass_ucb_waveform.c:364-522,
+ * declared at ucb/src/glass_ucb_waveform.h:150), which costs eight extra
+ * waveforms per source.  Coordinates are the params array's
+ * (f0 T, cos theta, phi, ln A, cos iota, psi, phi0, fdot T^2).
+ *   term_y[i]      : as glass_gpu_dlogl_batch
+ *   grad[8 i + k]  : d term_y / d params[k] = (r - h | dh/dp_k)
+ *   fisher[64 i + 8 k + l] : (dh/dp_k | dh/dp_l)   (may be NULL)
+ * The template size follows glass_gpu_set_template_size (at most 1024 here).
+ * fisher_mode 0
+ * weights every template bin with the noise at that bin; 1 reproduces
+ * ucb_fisher's indexing, which weights template bin i with the noise of
+ * segment bin i (ucb/src/glass_ucb_waveform.c:480-485).  Templates larger
+ * than 1024 samples get status GLASS_ITEM_NONFINITE.  Device pointers;
+ * asynchronous.
+ */
+int glass_gpu_grad_fisher_batch(glass_gpu_ctx *ctx, int nitems, const int *item_seg, const double *params,
+                                int fisher_mode, double *term_y, double *grad, double *fisher, int *status);
+
+/* Same with HOST pointers: copies in, evaluates, copies out, synchronises. */
+int glass_gpu_grad_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const int *item_seg, const double *params,
+                                     int fisher_mode, double *term_y, double *grad, double *fisher, int *status);
 
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
