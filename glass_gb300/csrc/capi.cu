@@ -198,8 +198,14 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   GLASS_CUDA(cudaMemcpy(b.w64, w64.data(), sizeof(double2) * w64.size(), cudaMemcpyHostToDevice), "upload w64");
   GLASS_CUDA(cudaMemcpy(b.g64, g64.data(), sizeof(double2) * g64.size(), cudaMemcpyHostToDevice), "upload g64");
   {
+    // invC relative to the segment's first bin (only ratios are used; invC
+    // itself, ~1e41, is beyond FP32 range)
     std::vector<float2> ic(nb);
-    for (size_t j = 0; j < nb; j++) ic[j] = make_float2((float)invCA[j], (float)invCE[j]);
+    for (int sg = 0; sg < nseg; sg++)
+      for (int j = 0; j < NFFT; j++) {
+        size_t sj = (size_t)sg * NFFT + j, s0 = (size_t)sg * NFFT;
+        ic[sj] = make_float2((float)(invCA[sj] / invCA[s0]), (float)(invCE[sj] / invCE[s0]));
+      }
     GLASS_CUDA(cudaMemcpy(b.invc, ic.data(), sizeof(float2) * nb, cudaMemcpyHostToDevice), "upload invc");
   }
   ctx->h_qmin.assign(qmin, qmin + nseg);

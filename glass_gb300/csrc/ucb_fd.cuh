@@ -17,7 +17,8 @@ struct FdBankDev {
   double *Q = nullptr;         // [nseg*(NFFT+1)] prefix sums of |w|^2 over both channels (FP64)
   double2 *w64 = nullptr;      // [nseg*NFFT*2] {A}, {E}
   double2 *g64 = nullptr;      // [nseg*NFFT*4] GA2, GA1, GE2, GE1
-  float2 *invc = nullptr;      // [nseg*NFFT] invC_A, invC_E (reference-indexed Fisher weights)
+  float2 *invc = nullptr;      // [nseg*NFFT] invC_A, invC_E over their value at the segment's bin 0
+                               // (weights of the reference-indexed Fisher matrix)
 };
 
 // Per-size tables (orbit samples and FFT twiddles) for the bank's (T, t0).
