@@ -83,8 +83,10 @@ def test_fisher_matches_reference_ucb_fisher(engine, golden):
         scale = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
         err = np.abs(F[0] - ref) / scale
         assert err.max() < 1e-3, (k, err.max(), np.unravel_index(err.argmax(), err.shape))
-        # zero residual: the gradient of -|h|^2 is -2 (h | dh/dp), i.e. -2 F[:, lnA]
-        np.testing.assert_allclose(grad[0], -F[0][:, 3], rtol=1e-3, atol=1e-3 * np.sqrt(np.diag(F[0])).max())
+        # zero residual: d/dp of -(h|h)/2 is -(h | dh/dp) = -F[:, lnA] with the
+        # Fisher matrix weighted like the gradient (noise at the template's bins)
+        _, grad0, F0, _ = engine.grad_fisher_host(np.zeros(1, np.int32), g["params"][k:k + 1], fisher_mode=0)
+        np.testing.assert_allclose(grad0[0], -F0[0][:, 3], rtol=1e-3, atol=1e-3 * np.sqrt(np.diag(F0[0])).max())
 
 
 def test_fisher_aligned_matches_finite_differences(engine, port):
