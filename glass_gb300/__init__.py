@@ -35,6 +35,7 @@ EXPORTS = (
     "glass_gpu_bank_upload", "glass_gpu_bank_set_residual", "glass_gpu_dlogl_batch",
     "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_probe_fma_tflops",
     "glass_gpu_grad_fisher_batch", "glass_gpu_grad_fisher_batch_host", "glass_gpu_set_template_size",
+    "glass_gpu_dlogl_fp64_noalloc",
 )
 
 _lib = None
@@ -70,6 +71,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_grad_fisher_batch.argtypes = [_V, ctypes.c_int, _V, _V, ctypes.c_int, _V, _V, _V, _V]
     lib.glass_gpu_grad_fisher_batch_host.argtypes = [_V, ctypes.c_int, _I, _D, ctypes.c_int, _D, _D, _D, _I]
     lib.glass_gpu_set_template_size.argtypes = [_V, ctypes.c_int]
+    lib.glass_gpu_dlogl_fp64_noalloc.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                 ctypes.c_int] + [_V] * 5 + [ctypes.c_int] + [_V] * 7
     _lib = lib
     return lib
 
@@ -92,6 +95,17 @@ def _ptr(x):
     if x is None:
         return None
     return ctypes.c_void_p(int(x.data_ptr()))
+
+
+def lib_constants() -> dict:
+    """Integer #defines of include/glass_gb300.h."""
+    import re
+
+    path = os.path.join(os.path.dirname(HERE), "include", "glass_gb300.h")
+    out = {}
+    for m in re.finditer(r"^#define\s+(GLASS_\w+)\s+(-?\d+)\s*(?:/\*.*)?$", open(path).read(), flags=re.M):
+        out[m.group(1)] = int(m.group(2))
+    return out
 
 
 def ucb_bandwidth(L, fstar, f, fdot, costheta, amp, T, NFFT) -> int:

@@ -471,6 +471,11 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   return cudaSuccess;
 }
 
+cudaError_t fd_launch_plan64(const PlanArgs &a, cudaStream_t stream) {
+  fd_plan64_kernel<<<(a.nitems + 63) / 64, 64, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
 size_t fd_series_bytes(int nitems, int NFFT, int precision) {
   size_t elem = precision == 1 ? sizeof(float2) : sizeof(double2);
   return (size_t)nitems * (size_t)NFFT * 4 * elem;

@@ -162,6 +162,35 @@ int glass_gpu_grad_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const int *
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 
+/* ------------------------------------------- batch that allocates nothing */
+/*
+ * No counterpart in the reference.  For callers that cannot allocate GPU
+ * memory once they are running -- a host that allocates everything at start-up
+ * and forbids it later, code running inside someone else's memory pool, or code
+ * that may not call the CUDA allocator at all -- this evaluates a batch exactly
+ * as glass_gpu_dlogl_batch does with GLASS_PREC_FP64, on the caller's stream,
+ * without calling cudaMalloc or any other allocating routine and without a
+ * context.  All pointers are device pointers the caller owns; the segment
+ * inputs have the layout of glass_gpu_bank_upload.
+ *
+ * Intermediate data live in fixed arrays compiled into the library (about
+ * 41 MB of device memory, held by every GPU that loads the library until the
+ * process exits), which bounds the sizes:
+ *   nitems <= GLASS_NOALLOC_MAX_ITEMS, nseg * NFFT <= GLASS_NOALLOC_MAX_BINS,
+ *   nitems * min(NFFT, 4096) <= GLASS_NOALLOC_MAX_SAMPLES;
+ * larger inputs return GLASS_ERR_SIZE.  Every call on a device shares those
+ * arrays, so calls that overlap on the GPU (other streams, other host threads)
+ * race: serialise them.  The first call on a device looks up the arrays'
+ * addresses; make it before any stream capture.  Asynchronous on `stream`.
+ */
+#define GLASS_NOALLOC_MAX_ITEMS 4096
+#define GLASS_NOALLOC_MAX_BINS 65536
+#define GLASS_NOALLOC_MAX_SAMPLES 524288
+int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, double t0, int NFFT, int nseg, const int *qmin,
+                                 const double *rA, const double *rE, const double *invCA, const double *invCE,
+                                 int nitems, const int *item_seg, const double *params, const double *term_x,
+                                 double *dlogl, double *term_y, double *hh, int *status);
+
 /* ---------------------------------------------------------- diagnostics */
 /* Measured fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) of the
  * device's FP32 (fp64 == 0) or FP64 pipe: the peak that the CUDA-core-bound
