@@ -135,7 +135,58 @@ class Port:
 
     # --- WDM ------------------------------------------------------------------------
     def _wdm_bind(self):
-        pass
+        lib = self.lib
+        lib.orc_incomplete_beta.restype = ctypes.c_double
+        lib.orc_incomplete_beta.argtypes = [ctypes.c_double] * 3
+        lib.orc_wdm_window.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _D]
+        for name in ("orc_wdm_forward", "orc_wdm_inverse", "orc_wdm_from_freq", "orc_wdm_to_freq"):
+            getattr(lib, name).argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _D]
+        lib.orc_rfft.argtypes = [_D, _D, ctypes.c_int]
+        lib.orc_irfft.argtypes = [_D, _D, ctypes.c_int]
+        lib.orc_complex_fft.argtypes = [_D, _D, ctypes.c_int, ctypes.c_int]
+        lib.orc_wdm_by_layers.argtypes = [ctypes.c_int] * 4 + [_D, _D]
+
+    def wdm_window(self, NF, NT, A=0.0, nx=6.0, forward=True):
+        out = np.zeros(NT // 2 + 1)
+        self.lib.orc_wdm_window(NF, NT, A, nx, int(forward), _p(out))
+        return out
+
+    def wdm_forward(self, NF, NT, window, time):
+        out = np.zeros(NF * NT)
+        self.lib.orc_wdm_forward(NF, NT, _p(np.ascontiguousarray(window)), _p(np.ascontiguousarray(time)), _p(out))
+        return out
+
+    def wdm_inverse(self, NF, NT, window, wdm):
+        out = np.zeros(NF * NT)
+        self.lib.orc_wdm_inverse(NF, NT, _p(np.ascontiguousarray(window)), _p(np.ascontiguousarray(wdm)), _p(out))
+        return out
+
+    def wdm_to_freq(self, NF, NT, window, wdm):
+        out = np.zeros(NF * NT + 2)
+        self.lib.orc_wdm_to_freq(NF, NT, _p(np.ascontiguousarray(window)), _p(np.ascontiguousarray(wdm)), _p(out))
+        return out
+
+    def wdm_from_freq(self, NF, NT, window, freq):
+        out = np.zeros(NF * NT)
+        self.lib.orc_wdm_from_freq(NF, NT, _p(np.ascontiguousarray(window)), _p(np.ascontiguousarray(freq)), _p(out))
+        return out
+
+    def rfft(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.zeros(len(x) + 2)
+        self.lib.orc_rfft(_p(x), _p(out), len(x))
+        return out
+
+    def irfft(self, f, N):
+        f = np.ascontiguousarray(f, np.float64)
+        out = np.zeros(N)
+        self.lib.orc_irfft(_p(f), _p(out), N)
+        return out
+
+    def wdm_by_layers(self, NF, NT, jmin, Nlayers, window, timedata):
+        t = np.ascontiguousarray(timedata, np.float64).copy()
+        self.lib.orc_wdm_by_layers(NF, NT, jmin, Nlayers, _p(np.ascontiguousarray(window)), _p(t))
+        return t
 
 
 class Ref:
@@ -161,6 +212,40 @@ class Ref:
 
     def fstar(self):
         return self.lib.ref_fstar()
+
+    def _wdm(self):
+        lib = self.lib
+        lib.ref_wdm_window.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _D]
+        lib.ref_wdm_forward.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D]
+        lib.ref_wdm_inverse.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D]
+        lib.ref_wdm_by_layers.argtypes = [ctypes.c_int] * 4 + [_D]
+
+    def wdm_window(self, NF, NT, A=0.0, forward=True):
+        self._wdm()
+        out = np.zeros(NT // 2 + 1)
+        self.lib.ref_wdm_window(NF, NT, A, int(forward), _p(out))
+        return out
+
+    def wdm_forward(self, NF, NT, time):
+        """wavelet_transform_timefreq (in place in the reference) on a copy."""
+        self._wdm()
+        t = np.ascontiguousarray(time, np.float64).copy()
+        out = np.zeros(NF * NT)
+        self.lib.ref_wdm_forward(NF, NT, _p(t), _p(out))
+        return out
+
+    def wdm_inverse(self, NF, NT, wdm):
+        self._wdm()
+        w = np.ascontiguousarray(wdm, np.float64).copy()
+        out = np.zeros(NF * NT)
+        self.lib.ref_wdm_inverse(NF, NT, _p(w), _p(out))
+        return out
+
+    def wdm_by_layers(self, NF, NT, jmin, Nlayers, timedata):
+        self._wdm()
+        t = np.ascontiguousarray(timedata, np.float64).copy()
+        self.lib.ref_wdm_by_layers(NF, NT, jmin, Nlayers, _p(t))
+        return t
 
     def aenoise_ff(self, f, model="scirdv1"):
         return np.array([self.lib.ref_aenoise_ff(model.encode(), float(x)) for x in np.atleast_1d(f)])

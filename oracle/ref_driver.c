@@ -204,3 +204,53 @@ void ref_ucb_fisher(const char *format, double T, double t0, int NFFT, int qmin,
     free_noise(noise);
     free(data);
 }
+
+/* A WDM grid of NF layers x NT pixels with a hand-filled struct Wavelets: the
+ * reference's initialize_wavelet (utils/src/glass_wavelet.c:210) fixes
+ * NF = 1536; the transforms themselves only read NF, NT and the window. */
+static void ref_wdm_grid(struct Wavelets *w, int NF, int NT)
+{
+    memset(w, 0, sizeof(*w));
+    w->NF = NF;
+    w->NT = NT;
+    w->A = 0.0;
+    w->window_freq_forward = malloc(sizeof(double) * (NT / 2 + 1));
+    build_wdm_filter_freq(w->window_freq_forward, NF, NT, 0.0, true);
+}
+
+/* utils/src/glass_wavelet.c:327 */
+void ref_wdm_window(int NF, int NT, double A, int forward, double *out)
+{
+    build_wdm_filter_freq(out, NF, NT, A, forward != 0);
+}
+
+/* utils/src/glass_wavelet.c:293: wavelet_transform_timefreq (time overwritten) */
+void ref_wdm_forward(int NF, int NT, double *time, double *wdm)
+{
+    struct Wavelets w;
+    ref_wdm_grid(&w, NF, NT);
+    wavelet_transform_timefreq(&w, time);
+    memcpy(wdm, time, sizeof(double) * NF * NT);
+    free(w.window_freq_forward);
+}
+
+/* utils/src/glass_wavelet.c:351 + utils/src/glass_math.c:819 */
+void ref_wdm_inverse(int NF, int NT, double *wdm, double *time)
+{
+    struct Wavelets w;
+    ref_wdm_grid(&w, NF, NT);
+    double *freq = malloc(sizeof(double) * (NF * NT + 2));
+    wavelet_transform_inverse_freq(&w, wdm, freq);
+    glass_inverse_real_fft_outplace(freq, time, NF * NT);
+    free(freq);
+    free(w.window_freq_forward);
+}
+
+/* utils/src/glass_wavelet.c:544 with the grid's forward window */
+void ref_wdm_by_layers(int NF, int NT, int jmin, int Nlayers, double *timedata)
+{
+    struct Wavelets w;
+    ref_wdm_grid(&w, NF, NT);
+    wavelet_transform_timefreq_by_layers(&w, jmin, Nlayers, w.window_freq_forward, timedata);
+    free(w.window_freq_forward);
+}

@@ -133,6 +133,28 @@ def fisher(ref, rng):
     np.savez_compressed(os.path.join(HERE, "fisher.npz"), **{k: np.array(v) for k, v in out.items()})
 
 
+def wdm(ref, rng):
+    """WDM windows, forward and inverse transforms on small grids (the window
+    exponent is the reference's fixed 6, A = 0), and the per-layer transform."""
+    out = {}
+    grids = [(32, 64), (48, 64), (16, 256), (1536, 8)]
+    for NF, NT in grids:
+        key = f"{NF}x{NT}"
+        x = rng.standard_normal(NF * NT)
+        out[f"win_{key}"] = ref.wdm_window(NF, NT)
+        out[f"winv_{key}"] = ref.wdm_window(NF, NT, forward=False)
+        out[f"x_{key}"] = x
+        out[f"fwd_{key}"] = ref.wdm_forward(NF, NT, x)
+        w = rng.standard_normal(NF * NT)
+        out[f"w_{key}"] = w
+        out[f"inv_{key}"] = ref.wdm_inverse(NF, NT, w)
+    NF, NT, jmin, NL = 64, 32, 10, 3
+    x = rng.standard_normal(NT * (NL + 1))
+    out["layers_in"] = x
+    out["layers_out"] = ref.wdm_by_layers(NF, NT, jmin, NL, x)
+    np.savez_compressed(os.path.join(HERE, "wdm.npz"), grids=np.array(grids), **out)
+
+
 def main():
     ref = Ref()
     rng = np.random.default_rng(20261203)
@@ -140,6 +162,7 @@ def main():
     bandwidth(ref, rng)
     likelihood(ref, rng)
     fisher(ref, rng)
+    wdm(ref, rng)
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

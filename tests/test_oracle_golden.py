@@ -98,3 +98,40 @@ def test_fft_convention(port):
         imp = np.zeros(N, complex)
         imp[0] = 1
         np.testing.assert_allclose(port.fft(imp), np.ones(N), atol=1e-14)
+
+
+def test_wdm_matches_reference(port, golden):
+    """WDM window, forward (utils/src/glass_wavelet.c:293-303, 410-460) and
+    inverse (:351-405 plus the inverse real FFT) on the reference's outputs."""
+    g = golden("wdm.npz")
+    for NF, NT in g["grids"]:
+        key = f"{NF}x{NT}"
+        win = port.wdm_window(int(NF), int(NT))
+        np.testing.assert_allclose(win, g[f"win_{key}"], rtol=1e-13, atol=1e-15 * np.abs(win).max())
+        np.testing.assert_allclose(port.wdm_window(int(NF), int(NT), forward=False), g[f"winv_{key}"], rtol=1e-13)
+        fwd = port.wdm_forward(int(NF), int(NT), win, g[f"x_{key}"])
+        ref = g[f"fwd_{key}"]
+        assert np.abs(fwd - ref).max() < 1e-10 * np.abs(ref).max()
+        inv = port.wdm_inverse(int(NF), int(NT), win, g[f"w_{key}"])
+        ref = g[f"inv_{key}"]
+        assert np.abs(inv - ref).max() < 1e-10 * np.abs(ref).max()
+    win = port.wdm_window(64, 32)
+    out = port.wdm_by_layers(64, 32, 10, 3, win, g["layers_in"])
+    assert np.abs(out - g["layers_out"]).max() < 1e-10 * np.abs(g["layers_out"]).max()
+
+
+@pytest.mark.parametrize("NF,NT", [(32, 64), (48, 64), (1536, 8)])
+def test_wdm_impulse_known_answers(port, NF, NT):
+    """The reference's own WDM convention checks (apps/src/fft_wdm_unit_tests.c:547-586):
+    WDM(impulse) taken back to the frequency domain is the impulse's FFT (all
+    ones), and the inverse transform recovers the impulse."""
+    ND = NF * NT
+    win = port.wdm_window(NF, NT)
+    imp = np.zeros(ND)
+    imp[0] = 1.0
+    w = port.wdm_forward(NF, NT, win, imp)
+    f = port.wdm_to_freq(NF, NT, win, w)
+    ref = np.zeros(ND + 2)
+    ref[0::2] = 1.0
+    np.testing.assert_allclose(f, ref, rtol=1e-5, atol=1e-10)
+    np.testing.assert_allclose(port.wdm_inverse(NF, NT, win, w), imp, atol=1e-10)
