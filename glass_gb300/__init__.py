@@ -35,7 +35,8 @@ EXPORTS = (
     "glass_gpu_bank_upload", "glass_gpu_bank_set_residual", "glass_gpu_dlogl_batch",
     "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_probe_fma_tflops",
     "glass_gpu_grad_fisher_batch", "glass_gpu_grad_fisher_batch_host", "glass_gpu_set_template_size",
-    "glass_gpu_dlogl_fp64_noalloc",
+    "glass_gpu_dlogl_fp64_noalloc", "glass_wdm_window", "glass_gpu_wdm_forward", "glass_gpu_wdm_inverse",
+    "glass_gpu_wdm_forward_host", "glass_gpu_wdm_inverse_host",
 )
 
 _lib = None
@@ -73,6 +74,12 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_set_template_size.argtypes = [_V, ctypes.c_int]
     lib.glass_gpu_dlogl_fp64_noalloc.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                                  ctypes.c_int] + [_V] * 5 + [ctypes.c_int] + [_V] * 7
+    lib.glass_wdm_window.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _D]
+    wdm_args = [_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double]
+    lib.glass_gpu_wdm_forward.argtypes = wdm_args + [_V, _V]
+    lib.glass_gpu_wdm_inverse.argtypes = wdm_args + [_V, _V]
+    lib.glass_gpu_wdm_forward_host.argtypes = wdm_args + [_D, _D]
+    lib.glass_gpu_wdm_inverse_host.argtypes = wdm_args + [_D, _D]
     _lib = lib
     return lib
 
@@ -134,6 +141,16 @@ def probe_fma_tflops(device: int = 0, fp64: bool = False) -> float:
     out = ctypes.c_double()
     _check(load_library().glass_gpu_probe_fma_tflops(device, int(fp64), ctypes.byref(out)))
     return out.value
+
+
+WDM_NX = 6.0  # the reference's window exponent (WAVELET_FILTER_CONSTANT)
+
+
+def wdm_window(NF: int, NT: int, A: float = 0.0, nx: float = WDM_NX, forward: bool = True) -> np.ndarray:
+    """Meyer window phif[0..NT/2] of the WDM transform (host computation)."""
+    out = np.empty(NT // 2 + 1)
+    _check(load_library().glass_wdm_window(NF, NT, A, nx, int(forward), _pd(out)))
+    return out
 
 
 class Engine:
@@ -220,6 +237,28 @@ class Engine:
         n = int(item_seg.numel())
         _check(self.lib.glass_gpu_grad_fisher_batch(self._ctx, n, _ptr(item_seg), _ptr(params), fisher_mode,
                                                     _ptr(term_y), _ptr(grad), _ptr(fisher), _ptr(status)))
+
+    def wdm_forward_host(self, NF, NT, time, precision=PREC_FP64, A=0.0, nx=WDM_NX):
+        """Time series (NF*NT) -> WDM coefficients (NF*NT, layout n + NT*m)."""
+        x = np.ascontiguousarray(time, np.float64).reshape(-1)
+        assert x.size == NF * NT
+        out = np.empty(NF * NT)
+        _check(self.lib.glass_gpu_wdm_forward_host(self._ctx, precision, NF, NT, A, nx, _pd(x), _pd(out)))
+        return out
+
+    def wdm_inverse_host(self, NF, NT, wdm, precision=PREC_FP64, A=0.0, nx=WDM_NX):
+        w = np.ascontiguousarray(wdm, np.float64).reshape(-1)
+        assert w.size == NF * NT
+        out = np.empty(NF * NT)
+        _check(self.lib.glass_gpu_wdm_inverse_host(self._ctx, precision, NF, NT, A, nx, _pd(w), _pd(out)))
+        return out
+
+    def wdm_forward_device(self, NF, NT, time, wdm, precision=PREC_FP64, A=0.0, nx=WDM_NX):
+        """Device tensors of NF*NT float64; asynchronous on the context's stream."""
+        _check(self.lib.glass_gpu_wdm_forward(self._ctx, precision, NF, NT, A, nx, _ptr(time), _ptr(wdm)))
+
+    def wdm_inverse_device(self, NF, NT, wdm, time, precision=PREC_FP64, A=0.0, nx=WDM_NX):
+        _check(self.lib.glass_gpu_wdm_inverse(self._ctx, precision, NF, NT, A, nx, _ptr(wdm), _ptr(time)))
 
     def last_launch_count(self) -> int:
         return self.lib.glass_gpu_last_launch_count(self._ctx)

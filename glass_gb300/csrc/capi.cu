@@ -10,6 +10,7 @@
 
 #include "../../include/glass_gb300.h"
 #include "ucb_fd.cuh"
+#include "wdm.cuh"
 
 using namespace glass;
 
@@ -55,6 +56,9 @@ struct glass_gpu_ctx {
   size_t d_stage_cap = 0;
   int last_launches = 0;
   int n_fixed = 0;  // template size override (0: bandwidth rule)
+  WdmPlan wdm;      // tables and work buffers of the last WDM grid used
+  void *wdm_stage = nullptr;  // NF NT doubles for the host-pointer WDM calls
+  size_t wdm_stage_cap = 0;
 };
 
 static int ctx_activate(glass_gpu_ctx *ctx) {
@@ -108,6 +112,8 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->work.bin_list);
   cudaFree(ctx->work.series);
   cudaFree(ctx->d_stage);
+  wdm_release(ctx->wdm);
+  cudaFree(ctx->wdm_stage);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
@@ -627,4 +633,85 @@ extern "C" int ucb_bandwidth(double L, double fstar, double f, double fdot, doub
   if (SS > Nmax) SS = Nmax;
   if (SS < Nmin) SS = Nmin;
   return (DS > SS) ? DS : SS;
+}
+
+// ------------------------------------------------------------------ WDM
+extern "C" int glass_wdm_window(int NF, int NT, double A, double nx, int forward, double *phif) {
+  if (!phif || NF < 1 || NT < 2 || NT % 2) return set_err(GLASS_ERR_ARG, "glass_wdm_window: bad grid or null output");
+  if (!(nx > 0) || !(A >= 0)) return set_err(GLASS_ERR_ARG, "glass_wdm_window: need nx > 0 and A >= 0");
+  wdm_window(NF, NT, A, nx, forward != 0, phif);
+  return GLASS_OK;
+}
+
+static int wdm_plan_for(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx) {
+  if (precision != GLASS_PREC_FP64 && precision != GLASS_PREC_MIXED)
+    return set_err(GLASS_ERR_ARG, "WDM: precision must be GLASS_PREC_FP64 or GLASS_PREC_MIXED");
+  if (!(nx > 0) || !(A >= 0) || !(2 * A < M_PI / NF))
+    return set_err(GLASS_ERR_ARG, "WDM: need nx > 0 and 0 <= A < pi / (2 NF)");
+  if (!wdm_grid_supported(NF, NT))
+    return set_err(GLASS_ERR_SIZE,
+                   "WDM: unsupported grid (NT even, 8..4096, NT and NF NT/2 of the form 2^a 3^b, NF NT/2 <= 4096^2)");
+  WdmPlan &P = ctx->wdm;
+  if (P.base && P.precision == precision && P.NF == NF && P.NT == NT && P.A == A && P.nx == nx) return GLASS_OK;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "WDM plan sync");
+  std::vector<double> win(NT / 2 + 1);
+  wdm_window(NF, NT, A, nx, true, win.data());
+  GLASS_CUDA(wdm_prepare(P, precision, NF, NT, win.data(), ctx->stream), "WDM plan");
+  P.A = A;
+  P.nx = nx;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wdm_forward(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                                     const double *time, double *wdm) {
+  if (!ctx || !time || !wdm) return set_err(GLASS_ERR_ARG, "glass_gpu_wdm_forward: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = wdm_plan_for(ctx, precision, NF, NT, A, nx))) return rc;
+  GLASS_CUDA(wdm_forward(ctx->wdm, time, wdm, ctx->stream), "glass_gpu_wdm_forward");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wdm_inverse(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                                     const double *wdm, double *time) {
+  if (!ctx || !time || !wdm) return set_err(GLASS_ERR_ARG, "glass_gpu_wdm_inverse: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = wdm_plan_for(ctx, precision, NF, NT, A, nx))) return rc;
+  GLASS_CUDA(wdm_inverse(ctx->wdm, wdm, time, ctx->stream), "glass_gpu_wdm_inverse");
+  return GLASS_OK;
+}
+
+static int wdm_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx, const double *in,
+                    double *out, bool forward) {
+  if (!ctx || !in || !out) return set_err(GLASS_ERR_ARG, "glass_gpu_wdm_*_host: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = wdm_plan_for(ctx, precision, NF, NT, A, nx))) return rc;
+  const size_t bytes = sizeof(double) * (size_t)NF * NT;
+  if (ctx->wdm_stage_cap < bytes) {
+    GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "WDM stage sync");
+    cudaFree(ctx->wdm_stage);
+    ctx->wdm_stage = nullptr;
+    ctx->wdm_stage_cap = 0;
+    GLASS_CUDA(cudaMalloc(&ctx->wdm_stage, bytes), "cudaMalloc(WDM stage)");
+    ctx->wdm_stage_cap = bytes;
+  }
+  double *d = (double *)ctx->wdm_stage;
+  GLASS_CUDA(cudaMemcpyAsync(d, in, bytes, cudaMemcpyHostToDevice, ctx->stream), "WDM upload");
+  GLASS_CUDA(forward ? wdm_forward(ctx->wdm, d, d, ctx->stream) : wdm_inverse(ctx->wdm, d, d, ctx->stream),
+             "WDM transform");
+  GLASS_CUDA(cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, ctx->stream), "WDM download");
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "WDM sync");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wdm_forward_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                                          const double *time, double *wdm) {
+  return wdm_host(ctx, precision, NF, NT, A, nx, time, wdm, true);
+}
+
+extern "C" int glass_gpu_wdm_inverse_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                                          const double *wdm, double *time) {
+  return wdm_host(ctx, precision, NF, NT, A, nx, wdm, time, false);
 }

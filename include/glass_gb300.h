@@ -191,6 +191,55 @@ int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, double t0, 
                                  int nitems, const int *item_seg, const double *params, const double *term_x,
                                  double *dlogl, double *term_y, double *hh, int *status);
 
+/* ------------------------------------------------------ WDM transforms */
+/*
+ * Wilson-Daubechies-Meyer time-frequency transform on a grid of NF layers x
+ * NT pixels, ND = NF NT samples, coefficient layout wdm[n + NT m] with the DC
+ * (m = 0) and Nyquist (m = NF) layers in the even and odd pixels of row 0.
+ * The window is the Meyer window with flat half-width A and exponent nx; the
+ * reference fixes A = 0 and nx = 6 (WAVELET_FILTER_CONSTANT,
+ * utils/src/glass_wavelet.h:21) and allocates NF = 1536 layers
+ * (utils/src/glass_wavelet.c:210-271).
+ *
+ * glass_wdm_window replaces build_wdm_filter_freq
+ * (utils/src/glass_wavelet.c:327, declared utils/src/glass_wavelet.h:122):
+ * phif[0..NT/2], forward normalisation when forward != 0.  Host only.
+ */
+int glass_wdm_window(int NF, int NT, double A, double nx, int forward, double *phif);
+
+/*
+ * time (ND samples) -> wdm (ND coefficients).  Replaces
+ * wavelet_transform_timefreq (utils/src/glass_wavelet.c:293, declared
+ * utils/src/glass_wavelet.h:100), which is the real FFT
+ * (utils/src/glass_math.c:808) followed by wavelet_transform_freq
+ * (utils/src/glass_wavelet.c:410).  The reference transforms in place; here
+ * time and wdm may be the same buffer or different ones.
+ * precision GLASS_PREC_FP64 computes in FP64 (matches the reference to about
+ * 1e-13 of the largest coefficient); GLASS_PREC_MIXED computes in FP32 (about
+ * 1e-6).  Grid limits: NT even, 8 <= NT <= 4096, NT and ND/2 of the form
+ * 2^a 3^b with ND/2 = M1 M2, M1, M2 <= 4096 (GLASS_ERR_SIZE otherwise).
+ * Device pointers; asynchronous on the context's stream.  The first call on a
+ * grid builds tables (synchronous, allocates); later calls on the same grid
+ * reuse them.
+ */
+int glass_gpu_wdm_forward(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                          const double *time, double *wdm);
+
+/*
+ * wdm -> time.  Replaces wavelet_transform_inverse_freq
+ * (utils/src/glass_wavelet.c:351, declared utils/src/glass_wavelet.h:108)
+ * followed by glass_inverse_real_fft_outplace (utils/src/glass_math.c:819).
+ * Same arguments, precision and limits as glass_gpu_wdm_forward.
+ */
+int glass_gpu_wdm_inverse(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                          const double *wdm, double *time);
+
+/* The same two with HOST pointers: copy in, transform, copy out, synchronise. */
+int glass_gpu_wdm_forward_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                               const double *time, double *wdm);
+int glass_gpu_wdm_inverse_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                               const double *wdm, double *time);
+
 /* ---------------------------------------------------------- diagnostics */
 /* Measured fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) of the
  * device's FP32 (fp64 == 0) or FP64 pipe: the peak that the CUDA-core-bound

@@ -61,3 +61,14 @@ def test_errors_are_reported_without_a_gpu(lib):
                                 *[out[i].ctypes.data_as(gg._D) for i in range(5)], 32, 2)
     assert rc == -4  # GLASS_ERR_FORMAT
     assert b"Unsupported" in lib.glass_gpu_last_error()
+
+
+def test_wdm_window_matches_reference(lib, golden):
+    """glass_wdm_window (host) against build_wdm_filter_freq's own output."""
+    g = golden("wdm.npz")
+    for NF, NT in g["grids"]:
+        key = f"{NF}x{NT}"
+        np.testing.assert_array_equal(gg.wdm_window(int(NF), int(NT)), g[f"win_{key}"])
+        np.testing.assert_array_equal(gg.wdm_window(int(NF), int(NT), forward=False), g[f"winv_{key}"])
+    with pytest.raises(gg.GlassError):
+        gg.wdm_window(32, 63)
