@@ -139,3 +139,18 @@ def gaussian_jumps(rng, params, scales, n):
         bad = (out[:, k] >= 1.0) | (out[:, k] <= -1.0)
         out[bad, k] = params[k] - jump[bad, k]
     return out
+
+
+def wavelet_invC(N, NT, kmin, scale=1.0):
+    """Inverse noise covariance of a wavelet segment of N pixels starting at
+    pixel kmin of a grid with NT pixels per layer: per pixel the inverse of
+    scale^2 * s(i) * [[1, -0.45, -0.45], [-0.45, 1, -0.45], [-0.45, -0.45, 1]]
+    (X, Y, Z noise correlated as in the equal-arm Michelson channels), with
+    s(i) = 1 + 0.2 sin(2 pi i / NT) + 0.1 sin(2 pi k / 97)^2 a slow trend in the
+    time index i = k mod NT.  Returned as [3][3][N] (the reference's
+    invC[i][j][k] layout)."""
+    k = np.arange(N) + kmin
+    s = (1.0 + 0.2 * np.sin(2 * np.pi * (k % NT) / NT) + 0.1 * np.sin(2 * np.pi * k / 97.0) ** 2) * scale**2
+    base = np.full((3, 3), -0.45) + np.eye(3) * 1.45
+    inv = np.linalg.inv(base)
+    return np.ascontiguousarray(inv[:, :, None] / s[None, None, :])

@@ -4,7 +4,8 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU-baseline leg of bench.py, never by the glass_gb300 package.
 
 * ``Port``  wraps oracle/_build/liboracle.so, the CPU restatement of the GLASS
-  UCB path in glass_oracle.c / glass_oracle_wdm.c (builds anywhere).
+  UCB path in glass_oracle.c, glass_oracle_wdm.c and glass_oracle_wavelet.c
+  (builds anywhere).
 * ``Ref``   wraps oracle/_ref/libglassref.so, the reference's own sources
   compiled with stand-in headers (only where the reference tree exists).
 """
@@ -70,6 +71,7 @@ class Port:
         lib.orc_orbit_positions.argtypes = [ctypes.c_double, _D]
         lib.orc_forward_complex_fft.argtypes = [_D, ctypes.c_int]
         self._wdm_bind()
+        self._wavelet_bind()
 
     # --- Fourier-domain UCB path -------------------------------------------------
     def fstar(self) -> float:
@@ -188,6 +190,74 @@ class Port:
         self.lib.orc_wdm_by_layers(NF, NT, jmin, Nlayers, _p(np.ascontiguousarray(window)), _p(t))
         return t
 
+    # --- wavelet-domain UCB path ---------------------------------------------------
+    def _wavelet_bind(self):
+        lib = self.lib
+        lib.orc_orbit_nodes.argtypes = [ctypes.c_double]
+        lib.orc_orbit_grid.argtypes = [ctypes.c_double, ctypes.c_double, _D, _D]
+        lib.orc_wavelet_layers.argtypes = [ctypes.c_double, _D, ctypes.c_double, ctypes.c_double, _I, _I]
+        lib.orc_ucb_waveform_wavelet.argtypes = [ctypes.c_double, ctypes.c_double, _D, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                 ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _I]
+        lib.orc_wavelet_dh_hh.argtypes = [ctypes.c_int, _D, _D, _D, _I, ctypes.c_int, _D, _D]
+        lib.orc_wavelet_delta_logl.argtypes = [ctypes.c_int, _D, _D, _I, ctypes.c_int, _D, _I, ctypes.c_int, _D]
+        lib.orc_wavelet_delta_logl.restype = ctypes.c_double
+        lib.orc_wavelet_logl_full.argtypes = [ctypes.c_int] * 5 + [_D, _D, _I, ctypes.c_int, _D]
+        lib.orc_wavelet_logl_full.restype = ctypes.c_double
+        lib.orc_wavelet_snr.argtypes = [ctypes.c_int, _D, _I, ctypes.c_int, _D]
+        lib.orc_wavelet_snr.restype = ctypes.c_double
+
+    def orbit_grid(self, Tobs, t0=0.0):
+        n = self.lib.orc_orbit_nodes(Tobs)
+        t, pos = np.zeros(n), np.zeros((3, 3, n))
+        self.lib.orc_orbit_grid(Tobs, t0, _p(t), _p(pos))
+        return t, pos
+
+    def wavelet_layers(self, Tobs, params, df, A=0.0):
+        j, n = ctypes.c_int(), ctypes.c_int()
+        self.lib.orc_wavelet_layers(Tobs, _p(np.ascontiguousarray(params, np.float64)), df, A, ctypes.byref(j),
+                                    ctypes.byref(n))
+        return j.value, n.value
+
+    def wavelet_waveform(self, params, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax, A=0.0, nx=6.0):
+        """(list, xyz [3, kmax-kmin], first layer, layer count)."""
+        N = kmax - kmin
+        xyz = np.zeros((3, N))
+        lst = np.zeros(4 * NT, np.int32)
+        n, nl = ctypes.c_int(), ctypes.c_int()
+        j = self.lib.orc_ucb_waveform_wavelet(Tobs, t0, _p(np.ascontiguousarray(params, np.float64)), NF, NT, wdt,
+                                              wdf, A, nx, kmin, kmax, _pi(lst), ctypes.byref(n), _p(xyz[0]),
+                                              _p(xyz[1]), _p(xyz[2]), ctypes.byref(nl))
+        return lst[:n.value].copy(), xyz, j, nl.value
+
+    def wavelet_dh_hh(self, d, h, invC, lst):
+        d = np.ascontiguousarray(d, np.float64)
+        h = np.ascontiguousarray(h, np.float64)
+        ic = np.ascontiguousarray(invC, np.float64)
+        lst = np.ascontiguousarray(lst, np.int32)
+        dh, hh = ctypes.c_double(), ctypes.c_double()
+        self.lib.orc_wavelet_dh_hh(d.shape[-1], _p(d), _p(h), _p(ic), _pi(lst), len(lst), ctypes.byref(dh),
+                                   ctypes.byref(hh))
+        return dh.value, hh.value
+
+    def wavelet_delta_logl(self, d, invC, hx, lx, hy, ly):
+        d, ic = np.ascontiguousarray(d, np.float64), np.ascontiguousarray(invC, np.float64)
+        hx, hy = np.ascontiguousarray(hx, np.float64), np.ascontiguousarray(hy, np.float64)
+        lx, ly = np.ascontiguousarray(lx, np.int32), np.ascontiguousarray(ly, np.int32)
+        return self.lib.orc_wavelet_delta_logl(d.shape[-1], _p(d), _p(hx), _pi(lx), len(lx), _p(hy), _pi(ly),
+                                               len(ly), _p(ic))
+
+    def wavelet_logl_full(self, NT, kmin, imin, imax, d, h, lst, invC):
+        d, h = np.ascontiguousarray(d, np.float64), np.ascontiguousarray(h, np.float64)
+        lst, ic = np.ascontiguousarray(lst, np.int32), np.ascontiguousarray(invC, np.float64)
+        return self.lib.orc_wavelet_logl_full(d.shape[-1], NT, kmin, imin, imax, _p(d), _p(h), _pi(lst), len(lst),
+                                              _p(ic))
+
+    def wavelet_snr(self, h, lst, invC):
+        h, lst, ic = (np.ascontiguousarray(h, np.float64), np.ascontiguousarray(lst, np.int32),
+                      np.ascontiguousarray(invC, np.float64))
+        return self.lib.orc_wavelet_snr(h.shape[-1], _p(h), _pi(lst), len(lst), _p(ic))
+
 
 class Ref:
     """The reference's own functions (oracle/_ref/libglassref.so)."""
@@ -246,6 +316,58 @@ class Ref:
         t = np.ascontiguousarray(timedata, np.float64).copy()
         self.lib.ref_wdm_by_layers(NF, NT, jmin, Nlayers, _p(t))
         return t
+
+    # --- wavelet-domain UCB path ---------------------------------------------------
+    def _wavelet(self):
+        lib = self.lib
+        lib.ref_ucb_waveform_wavelet.argtypes = [ctypes.c_double, ctypes.c_double, _D, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, _I,
+                                                 _D, _D, _D]
+        lib.ref_orbit_grid.argtypes = [ctypes.c_double, ctypes.c_double, _D, _D]
+        lib.ref_wavelet_delta_logl.argtypes = [ctypes.c_int, _D, _D, _D, _I, ctypes.c_int, _D, _I, ctypes.c_int]
+        lib.ref_wavelet_delta_logl.restype = ctypes.c_double
+        lib.ref_wavelet_logl_full.argtypes = [ctypes.c_int] * 5 + [_D, _D, _I, ctypes.c_int, _D]
+        lib.ref_wavelet_logl_full.restype = ctypes.c_double
+        lib.ref_wavelet_snr.argtypes = [ctypes.c_int, _D, _I, ctypes.c_int, _D]
+        lib.ref_wavelet_snr.restype = ctypes.c_double
+
+    def orbit_grid(self, Tobs, t0=0.0):
+        self._wavelet()
+        n = self.lib.ref_orbit_grid(Tobs, t0, None, None)
+        t, pos = np.zeros(n), np.zeros((3, 3, n))
+        self.lib.ref_orbit_grid(Tobs, t0, _p(t), _p(pos))
+        return t, pos
+
+    def wavelet_waveform(self, params, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax):
+        """ucb_waveform_wavelet (A = 0, window exponent 6): (list, xyz [3, kmax-kmin])."""
+        self._wavelet()
+        N = kmax - kmin
+        xyz = np.zeros((3, N))
+        lst = np.zeros(4 * NT, np.int32)
+        n = self.lib.ref_ucb_waveform_wavelet(Tobs, t0, _p(np.ascontiguousarray(params, np.float64).copy()), NF, NT,
+                                              wdt, wdf, kmin, kmax, _pi(lst), _p(xyz[0]), _p(xyz[1]), _p(xyz[2]))
+        return lst[:n].copy(), xyz
+
+    def wavelet_delta_logl(self, d, invC, hx, lx, hy, ly):
+        self._wavelet()
+        d, ic = np.ascontiguousarray(d, np.float64).copy(), np.ascontiguousarray(invC, np.float64).copy()
+        hx, hy = np.ascontiguousarray(hx, np.float64).copy(), np.ascontiguousarray(hy, np.float64).copy()
+        lx, ly = np.ascontiguousarray(lx, np.int32).copy(), np.ascontiguousarray(ly, np.int32).copy()
+        return self.lib.ref_wavelet_delta_logl(d.shape[-1], _p(d), _p(ic), _p(hx), _pi(lx), len(lx), _p(hy),
+                                               _pi(ly), len(ly))
+
+    def wavelet_logl_full(self, NT, kmin, imin, imax, d, h, lst, invC):
+        self._wavelet()
+        d, h = np.ascontiguousarray(d, np.float64).copy(), np.ascontiguousarray(h, np.float64).copy()
+        lst, ic = np.ascontiguousarray(lst, np.int32).copy(), np.ascontiguousarray(invC, np.float64).copy()
+        return self.lib.ref_wavelet_logl_full(d.shape[-1], NT, kmin, imin, imax, _p(d), _p(h), _pi(lst), len(lst),
+                                              _p(ic))
+
+    def wavelet_snr(self, h, lst, invC):
+        self._wavelet()
+        h, lst, ic = (np.ascontiguousarray(h, np.float64).copy(), np.ascontiguousarray(lst, np.int32).copy(),
+                      np.ascontiguousarray(invC, np.float64).copy())
+        return self.lib.ref_wavelet_snr(h.shape[-1], _p(h), _pi(lst), len(lst), _p(ic))
 
     def aenoise_ff(self, f, model="scirdv1"):
         return np.array([self.lib.ref_aenoise_ff(model.encode(), float(x)) for x in np.atleast_1d(f)])

@@ -254,3 +254,153 @@ void ref_wdm_by_layers(int NF, int NT, int jmin, int Nlayers, double *timedata)
     wavelet_transform_timefreq_by_layers(&w, jmin, Nlayers, w.window_freq_forward, timedata);
     free(w.window_freq_forward);
 }
+
+/* ucb/src/glass_ucb_waveform.c:1061 with interpolated analytic orbits
+ * (utils/src/glass_lisa.c:271) and a hand-filled WDM grid (A = 0): X, Y, Z
+ * are indexed by k - kmin and must be zeroed by the caller; returns Nwavelet. */
+int ref_ucb_waveform_wavelet(double Tobs, double t0, double *params, int NF, int NT, double dt, double df,
+                             int kmin, int kmax, int *list, double *X, double *Y, double *Z)
+{
+    struct Orbit *orbit = calloc(1, sizeof(struct Orbit));
+    initialize_interpolated_analytic_orbits(orbit, Tobs, t0);
+    struct Wavelets w;
+    memset(&w, 0, sizeof(w));
+    w.NF = NF;
+    w.NT = NT;
+    w.dt = dt;
+    w.df = df;
+    w.A = 0.0;
+    w.kmin = kmin;
+    w.kmax = kmax;
+    int n = 0;
+    ucb_waveform_wavelet(orbit, &w, Tobs, t0, params, list, &n, X, Y, Z);
+    free_orbit(orbit);
+    return n;
+}
+
+/* orbit node times and positions of initialize_interpolated_analytic_orbits:
+ * t[Norb], pos[(3 s + d) Norb + n]; returns Norb */
+int ref_orbit_grid(double Tobs, double t0, double *t, double *pos)
+{
+    struct Orbit *orbit = calloc(1, sizeof(struct Orbit));
+    initialize_interpolated_analytic_orbits(orbit, Tobs, t0);
+    int n = orbit->Norb;
+    if (t) {
+        for (int k = 0; k < n; k++) {
+            t[k] = orbit->t[k];
+            for (int s = 0; s < 3; s++) {
+                pos[(3 * s + 0) * n + k] = orbit->x[s][k];
+                pos[(3 * s + 1) * n + k] = orbit->y[s][k];
+                pos[(3 * s + 2) * n + k] = orbit->z[s][k];
+            }
+        }
+    }
+    free_orbit(orbit);
+    return n;
+}
+
+static struct Noise *ref_wavelet_noise(int N, double *invC)
+{
+    struct Noise *noise = calloc(1, sizeof(struct Noise));
+    noise->N = N;
+    noise->invC = malloc(sizeof(double **) * 3);
+    for (int i = 0; i < 3; i++) {
+        noise->invC[i] = malloc(sizeof(double *) * 3);
+        for (int j = 0; j < 3; j++) noise->invC[i][j] = invC + (3 * i + j) * N;
+    }
+    return noise;
+}
+
+static void ref_wavelet_noise_free(struct Noise *noise)
+{
+    for (int i = 0; i < 3; i++) free(noise->invC[i]);
+    free(noise->invC);
+    free(noise);
+}
+
+static struct TDI *ref_tdi_view(int N, double *xyz)
+{
+    struct TDI *t = calloc(1, sizeof(struct TDI));
+    t->N = N;
+    t->Nchannel = 3;
+    t->X = xyz;
+    t->Y = xyz + N;
+    t->Z = xyz + 2 * N;
+    return t;
+}
+
+/* utils/src/glass_model.c:624 for one-source models x and y: d, hx, hy are 3
+ * channels of N pixels, invC 9 arrays of N pixels ([i][j][k]) */
+double ref_wavelet_delta_logl(int N, double *d, double *invC, double *hx, int *lx, int nx, double *hy, int *ly,
+                              int ny)
+{
+    struct Data data;
+    memset(&data, 0, sizeof(data));
+    data.N = N;
+    data.tdi = ref_tdi_view(N, d);
+    struct Noise *noise = ref_wavelet_noise(N, invC);
+    struct Model mx, my;
+    memset(&mx, 0, sizeof(mx));
+    memset(&my, 0, sizeof(my));
+    mx.tdi = ref_tdi_view(N, hx);
+    my.tdi = ref_tdi_view(N, hy);
+    mx.noise = my.noise = noise;
+    mx.list = lx;
+    mx.Nlist = nx;
+    my.list = ly;
+    my.Nlist = ny;
+    double r = delta_log_likelihood(&data, &mx, &my);
+    free(data.tdi);
+    free(mx.tdi);
+    free(my.tdi);
+    ref_wavelet_noise_free(noise);
+    return r;
+}
+
+/* utils/src/glass_model.c:805 on a wavelet segment of N pixels starting at
+ * kmin, grid of NT pixels per layer, edge buffer [imin, imax] */
+double ref_wavelet_logl_full(int N, int NT, int kmin, int imin, int imax, double *d, double *h, int *list, int n,
+                             double *invC)
+{
+    struct Wavelets w;
+    memset(&w, 0, sizeof(w));
+    w.NT = NT;
+    w.kmin = kmin;
+    w.imin = imin;
+    w.imax = imax;
+    struct Data data;
+    memset(&data, 0, sizeof(data));
+    data.N = N;
+    data.tdi = ref_tdi_view(N, d);
+    data.wdm = &w;
+    double *res = malloc(sizeof(double) * 3 * N);
+    struct Model m;
+    memset(&m, 0, sizeof(m));
+    m.tdi = ref_tdi_view(N, h);
+    m.residual = ref_tdi_view(N, res);
+    m.noise = ref_wavelet_noise(N, invC);
+    m.list = list;
+    m.Nlist = n;
+    double r = gaussian_log_likelhood_wavelet(&data, &m);
+    free(data.tdi);
+    free(m.tdi);
+    free(m.residual);
+    free(res);
+    ref_wavelet_noise_free(m.noise);
+    return r;
+}
+
+/* utils/src/glass_math.c:428 */
+double ref_wavelet_snr(int N, double *h, int *list, int n, double *invC)
+{
+    struct Source s;
+    memset(&s, 0, sizeof(s));
+    s.tdi = ref_tdi_view(N, h);
+    s.list = list;
+    s.Nlist = n;
+    struct Noise *noise = ref_wavelet_noise(N, invC);
+    double r = snr_wavelet(&s, noise);
+    free(s.tdi);
+    ref_wavelet_noise_free(noise);
+    return r;
+}

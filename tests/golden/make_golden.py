@@ -10,7 +10,12 @@ ucb_waveform (ucb/src/glass_ucb_waveform.c:738), ucb_bandwidth (:698),
 ucb_alignment (:727), AEnoise_FF (utils/src/glass_lisa.c:1137),
 generate_ucb_model + gaussian_log_likelihood (ucb/src/glass_ucb_model.c:55,
 utils/src/glass_model.c:726), snr (utils/src/glass_math.c:403) and ucb_fisher
-(ucb/src/glass_ucb_waveform.c:364).  Inputs are seeded numpy draws.
+(ucb/src/glass_ucb_waveform.c:364), the WDM transforms
+(utils/src/glass_wavelet.c:293, :351, :544, :327), ucb_waveform_wavelet
+(ucb/src/glass_ucb_waveform.c:1061) with initialize_interpolated_analytic_orbits
+(utils/src/glass_lisa.c:271), delta_log_likelihood and
+gaussian_log_likelhood_wavelet (utils/src/glass_model.c:624, :805) and
+snr_wavelet (utils/src/glass_math.c:428).  Inputs are seeded numpy draws.
 """
 from __future__ import annotations
 
@@ -155,6 +160,84 @@ def wdm(ref, rng):
     np.savez_compressed(os.path.join(HERE, "wdm.npz"), grids=np.array(grids), **out)
 
 
+WAVELET_GRIDS = {
+    # name: (NF, NT, pixel duration, Tobs); 15 s samples, 1024 layers x 2048 pixels
+    "nf1024": (1024, 2048, 15.0 * 1024, 2.0**21 * 15.0),
+    # the reference's own grid (initialize_wavelet, utils/src/glass_wavelet.c:210): 5 s samples
+    "nf1536": (1536, 4096, 7680.0, 4096 * 7680.0),
+}
+
+
+def wavelet_segment(rng, params, grid, below=3, above=3, cut=0):
+    from oracle import Port
+
+    NF, NT, wdt, T = WAVELET_GRIDS[grid]
+    j, nl = Port().wavelet_layers(T, params, 1.0 / (2 * wdt))
+    lmin, lmax = j - below + cut, j + nl + above
+    return lmin * NT, lmax * NT
+
+
+def wavelet_waveforms(ref, rng):
+    """ucb_waveform_wavelet: the pixel list and the X, Y, Z values on it."""
+    out = {"grid": [], "params": [], "t0": [], "kmin": [], "kmax": []}
+    cases = []
+    for k in range(8):
+        f0 = 10 ** rng.uniform(np.log10(0.5e-3), np.log10(15e-3))
+        fdot = 10 ** rng.uniform(-18, -16) * (-1 if k == 5 else 1)
+        p = wl.draw_source(rng, f0, 10 ** rng.uniform(-23, -21), fdot)
+        grid = "nf1536" if k in (2, 7) else "nf1024"
+        t0 = 2.5e5 if k in (1, 7) else 0.0
+        cut = 1 if k in (3, 6) else 0  # the segment starts above the signal's first layer
+        cases.append((grid, p, t0, cut))
+    for i, (grid, p, t0, cut) in enumerate(cases):
+        NF, NT, wdt, T = WAVELET_GRIDS[grid]
+        kmin, kmax = wavelet_segment(rng, p, grid, cut=cut)
+        lst, xyz = ref.wavelet_waveform(p, T, t0, NF, NT, wdt, 1.0 / (2 * wdt), kmin, kmax)
+        out["grid"].append(grid)
+        out["params"].append(p)
+        out["t0"].append(t0)
+        out["kmin"].append(kmin)
+        out["kmax"].append(kmax)
+        out[f"list{i}"] = lst
+        out[f"xyz{i}"] = xyz[:, lst]
+    t, pos = ref.orbit_grid(WAVELET_GRIDS["nf1024"][3], 0.0)
+    np.savez_compressed(os.path.join(HERE, "wavelet_waveform.npz"), orbit_t=t, orbit_pos=pos,
+                        **{k: np.array(v) for k, v in out.items()})
+
+
+def wavelet_likelihood(ref, rng):
+    """Sparse-pixel delta logL (delta_log_likelihood), the full-segment logL
+    (gaussian_log_likelhood_wavelet) and snr_wavelet on a segment holding an
+    injected source plus white noise, for Gaussian jumps around it."""
+    grid = "nf1024"
+    NF, NT, wdt, T = WAVELET_GRIDS[grid]
+    wdf = 1.0 / (2 * wdt)
+    out = {}
+    for c in range(2):
+        f0 = rng.uniform(2e-3, 6e-3)
+        inj = wl.draw_source(rng, f0, 10 ** rng.uniform(-21.7, -21.2), 1e-17)
+        kmin, kmax = wavelet_segment(rng, inj, grid, below=2, above=2)
+        N = kmax - kmin
+        lst, h = ref.wavelet_waveform(inj, T, 0.0, NF, NT, wdt, wdf, kmin, kmax)
+        # noise with covariance C per pixel, scaled to the injection
+        scale = 0.5 * np.abs(h).max()
+        invC_s = wl.wavelet_invC(N, NT, kmin, scale)
+        L = np.linalg.cholesky(np.linalg.inv(invC_s.transpose(2, 0, 1)))
+        d = h + np.einsum("kab,kb->ak", L, rng.standard_normal((N, 3)))
+        props = np.vstack([inj[None], wl.gaussian_jumps(rng, inj, wl.jump_scales(inj, 20.0), 9)])
+        dl, full, snr, lists = [], [], [], []
+        for q, p in enumerate(props):
+            ly, hy = ref.wavelet_waveform(p, T, 0.0, NF, NT, wdt, wdf, kmin, kmax)
+            dl.append(ref.wavelet_delta_logl(d, invC_s, h, lst, hy, ly))
+            imin, imax = 100, NT - 100
+            full.append(ref.wavelet_logl_full(NT, kmin, imin, imax, d, hy, ly, invC_s))
+            snr.append(ref.wavelet_snr(hy, ly, invC_s))
+        out.update({f"c{c}_kmin": kmin, f"c{c}_kmax": kmax, f"c{c}_d": d, f"c{c}_scale": scale,
+                    f"c{c}_inj": inj, f"c{c}_props": props, f"c{c}_dlogl": np.array(dl),
+                    f"c{c}_logl_full": np.array(full), f"c{c}_snr": np.array(snr)})
+    np.savez_compressed(os.path.join(HERE, "wavelet_likelihood.npz"), ncase=2, grid=grid, edge=100, **out)
+
+
 def main():
     ref = Ref()
     rng = np.random.default_rng(20261203)
@@ -163,6 +246,8 @@ def main():
     likelihood(ref, rng)
     fisher(ref, rng)
     wdm(ref, rng)
+    wavelet_waveforms(ref, rng)
+    wavelet_likelihood(ref, rng)
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

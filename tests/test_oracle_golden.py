@@ -135,3 +135,47 @@ def test_wdm_impulse_known_answers(port, NF, NT):
     ref[0::2] = 1.0
     np.testing.assert_allclose(f, ref, rtol=1e-5, atol=1e-10)
     np.testing.assert_allclose(port.wdm_inverse(NF, NT, win, w), imp, atol=1e-10)
+
+
+WAVELET_GRIDS = {"nf1024": (1024, 2048, 15.0 * 1024, 2.0**21 * 15.0), "nf1536": (1536, 4096, 7680.0, 4096 * 7680.0)}
+
+
+def test_interpolated_orbit_grid(port, golden):
+    g = golden("wavelet_waveform.npz")
+    t, pos = port.orbit_grid(WAVELET_GRIDS["nf1024"][3], 0.0)
+    np.testing.assert_array_equal(t, g["orbit_t"])
+    np.testing.assert_array_equal(pos, g["orbit_pos"])
+
+
+def test_wavelet_waveform_matches_reference(port, golden):
+    """ucb_waveform_wavelet: same pixel list; values to the FFT's rounding."""
+    g = golden("wavelet_waveform.npz")
+    for i in range(len(g["grid"])):
+        NF, NT, wdt, Tobs = WAVELET_GRIDS[str(g["grid"][i])]
+        lst, xyz, _, _ = port.wavelet_waveform(g["params"][i], Tobs, float(g["t0"][i]), NF, NT, wdt, 1 / (2 * wdt),
+                                               int(g["kmin"][i]), int(g["kmax"][i]))
+        np.testing.assert_array_equal(lst, g[f"list{i}"])
+        ref = g[f"xyz{i}"]
+        assert np.abs(xyz[:, lst] - ref).max() / np.abs(ref).max() < 1e-12, i
+
+
+def test_wavelet_likelihoods_match_reference(port, golden):
+    """delta_log_likelihood, gaussian_log_likelhood_wavelet and snr_wavelet."""
+    g = golden("wavelet_likelihood.npz")
+    NF, NT, wdt, Tobs = WAVELET_GRIDS[str(g["grid"])]
+    edge = int(g["edge"])
+    for c in range(int(g["ncase"])):
+        kmin, kmax = int(g[f"c{c}_kmin"]), int(g[f"c{c}_kmax"])
+        d = g[f"c{c}_d"]
+        invC = wl.wavelet_invC(kmax - kmin, NT, kmin, float(g[f"c{c}_scale"]))
+        lx, hx, _, _ = port.wavelet_waveform(g[f"c{c}_inj"], Tobs, 0.0, NF, NT, wdt, 1 / (2 * wdt), kmin, kmax)
+        for q, p in enumerate(g[f"c{c}_props"]):
+            ly, hy, _, _ = port.wavelet_waveform(p, Tobs, 0.0, NF, NT, wdt, 1 / (2 * wdt), kmin, kmax)
+            dl = port.wavelet_delta_logl(d, invC, hx, lx, hy, ly)
+            ref = g[f"c{c}_dlogl"][q]
+            assert abs(dl - ref) < 1e-10 * max(1.0, abs(ref)), (c, q, dl, ref)
+            full = port.wavelet_logl_full(NT, kmin, edge, NT - edge, d, hy, ly, invC)
+            ref = g[f"c{c}_logl_full"][q]
+            assert abs(full - ref) < 1e-10 * max(1.0, abs(ref)), (c, q)
+            snr = port.wavelet_snr(hy, ly, invC)
+            assert abs(snr - g[f"c{c}_snr"][q]) < 1e-10 * g[f"c{c}_snr"][q]
