@@ -37,6 +37,8 @@ EXPORTS = (
     "glass_gpu_grad_fisher_batch", "glass_gpu_grad_fisher_batch_host", "glass_gpu_set_template_size",
     "glass_gpu_dlogl_fp64_noalloc", "glass_wdm_window", "glass_gpu_wdm_forward", "glass_gpu_wdm_inverse",
     "glass_gpu_wdm_forward_host", "glass_gpu_wdm_inverse_host",
+    "glass_gpu_wavelet_setup", "glass_gpu_wavelet_set_data", "glass_gpu_wavelet_dlogl_batch",
+    "glass_gpu_wavelet_dlogl_batch_host", "glass_gpu_wavelet_waveform_batch", "glass_gpu_wavelet_waveform_batch_host",
 )
 
 _lib = None
@@ -80,6 +82,14 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_wdm_inverse.argtypes = wdm_args + [_V, _V]
     lib.glass_gpu_wdm_forward_host.argtypes = wdm_args + [_D, _D]
     lib.glass_gpu_wdm_inverse_host.argtypes = wdm_args + [_D, _D]
+    lib.glass_gpu_wavelet_setup.argtypes = [_V, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
+    lib.glass_gpu_wavelet_set_data.argtypes = [_V, _D, _D, _D, _D]
+    lib.glass_gpu_wavelet_dlogl_batch.argtypes = [_V, ctypes.c_int] + [_V] * 6
+    lib.glass_gpu_wavelet_dlogl_batch_host.argtypes = [_V, ctypes.c_int, _D, _D, _D, _D, _D, _I]
+    lib.glass_gpu_wavelet_waveform_batch.argtypes = [_V, ctypes.c_int] + [_V] * 4
+    lib.glass_gpu_wavelet_waveform_batch_host.argtypes = [_V, ctypes.c_int, _D, _I, _D, _I]
     _lib = lib
     return lib
 
@@ -259,6 +269,70 @@ class Engine:
 
     def wdm_inverse_device(self, NF, NT, wdm, time, precision=PREC_FP64, A=0.0, nx=WDM_NX):
         _check(self.lib.glass_gpu_wdm_inverse(self._ctx, precision, NF, NT, A, nx, _ptr(wdm), _ptr(time)))
+
+    # --- wavelet-domain UCB path ---------------------------------------------------
+    WV_MAX_LAYERS = 3
+
+    def wavelet_setup(self, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax, A=0.0, nx=WDM_NX, orbit=None):
+        """Segment of pixels [kmin, kmax) of an NF x NT grid (pixel duration wdt,
+        bandwidth wdf).  orbit: (t [n], positions [3, 3, n] metres) or None for
+        the interpolated analytic orbit."""
+        if orbit is None:
+            ot = op = None
+            n = 0
+        else:
+            ot = np.ascontiguousarray(orbit[0], np.float64)
+            op = np.ascontiguousarray(orbit[1], np.float64)
+            n = len(ot)
+        _check(self.lib.glass_gpu_wavelet_setup(self._ctx, Tobs, t0, NF, NT, wdt, wdf, A, nx, kmin, kmax, n,
+                                                _pd(ot) if ot is not None else None,
+                                                _pd(op) if op is not None else None))
+        self.wv = dict(NT=NT, kmin=kmin, kmax=kmax, N=kmax - kmin)
+
+    def wavelet_set_data(self, res, invC):
+        """res: [3, N] residual X, Y, Z; invC: [3, 3, N] inverse covariance."""
+        r = np.ascontiguousarray(res, np.float64)
+        ic = np.ascontiguousarray(invC, np.float64)
+        _check(self.lib.glass_gpu_wavelet_set_data(self._ctx, _pd(r[0]), _pd(r[1]), _pd(r[2]), _pd(ic)))
+
+    def wavelet_waveform_host(self, params):
+        """(info [n, 4] = first layer, layers, first kept layer, kept layers
+        (-1 when the parameters are invalid), xyz [n, 3, 3 NT], status [n])."""
+        p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        n = len(p)
+        NT = self.wv["NT"]
+        info = np.zeros((n, 4), np.int32)
+        xyz = np.zeros((n, 3, self.WV_MAX_LAYERS * NT))
+        st = np.zeros(n, np.int32)
+        _check(self.lib.glass_gpu_wavelet_waveform_batch_host(self._ctx, n, _pd(p), _pi(info), _pd(xyz), _pi(st)))
+        return info, xyz, st
+
+    def wavelet_list(self, info_row):
+        """Pixel list (k - kmin) of one item, in the order of its values."""
+        _, _, jlo, c = (int(v) for v in info_row)
+        NT, kmin = self.wv["NT"], self.wv["kmin"]
+        if c <= 0:
+            return np.zeros(0, np.int32)
+        i = np.repeat(np.arange(NT), c)
+        j = jlo + np.tile(np.arange(c), NT)
+        return (i + j * NT - kmin).astype(np.int32)
+
+    def wavelet_dlogl_host(self, params, term_x=None):
+        """(dlogl, term_y, hh, status) with term = (h|h) - 2 (d|h) over the
+        item's pixels and dlogl = -(term_y - term_x)/2."""
+        p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        n = len(p)
+        tx = None if term_x is None else np.ascontiguousarray(term_x, np.float64)
+        dl, ty, hh = np.empty(n), np.empty(n), np.empty(n)
+        st = np.empty(n, np.int32)
+        _check(self.lib.glass_gpu_wavelet_dlogl_batch_host(self._ctx, n, _pd(p), _pd(tx) if tx is not None else None,
+                                                           _pd(dl), _pd(ty), _pd(hh), _pi(st)))
+        return dl, ty, hh, st
+
+    def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None):
+        n = int(params.shape[0])
+        _check(self.lib.glass_gpu_wavelet_dlogl_batch(self._ctx, n, _ptr(params), _ptr(term_x), _ptr(dlogl),
+                                                      _ptr(term_y), _ptr(hh), _ptr(status)))
 
     def last_launch_count(self) -> int:
         return self.lib.glass_gpu_last_launch_count(self._ctx)

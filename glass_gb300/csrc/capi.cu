@@ -4,12 +4,14 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/glass_gb300.h"
 #include "ucb_fd.cuh"
+#include "ucb_wavelet.cuh"
 #include "wdm.cuh"
 
 using namespace glass;
@@ -59,6 +61,13 @@ struct glass_gpu_ctx {
   WdmPlan wdm;      // tables and work buffers of the last WDM grid used
   void *wdm_stage = nullptr;  // NF NT doubles for the host-pointer WDM calls
   size_t wdm_stage_cap = 0;
+  // wavelet-domain segment: grid tables, data, per-source work
+  WvGridDev wv{};
+  void *wv_grid_mem = nullptr;
+  void *wv_data_mem = nullptr;
+  bool wv_data_ready = false;
+  WvWorkDev wvw;
+  void *wv_work_mem = nullptr;
 };
 
 static int ctx_activate(glass_gpu_ctx *ctx) {
@@ -114,6 +123,9 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->d_stage);
   wdm_release(ctx->wdm);
   cudaFree(ctx->wdm_stage);
+  cudaFree(ctx->wv_grid_mem);
+  cudaFree(ctx->wv_data_mem);
+  cudaFree(ctx->wv_work_mem);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
@@ -714,4 +726,183 @@ extern "C" int glass_gpu_wdm_forward_host(glass_gpu_ctx *ctx, int precision, int
 extern "C" int glass_gpu_wdm_inverse_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
                                           const double *wdm, double *time) {
   return wdm_host(ctx, precision, NF, NT, A, nx, wdm, time, false);
+}
+
+// ------------------------------------------------------------ wavelet-domain UCB path
+static constexpr int kWvChunk = 4096;  // sources per launch sequence (bounds the work memory)
+
+static bool smooth23_even(int x) {
+  if (x < 2 || x % 2) return false;
+  while (x % 3 == 0) x /= 3;
+  return (x & (x - 1)) == 0;
+}
+
+extern "C" int glass_gpu_wavelet_setup(glass_gpu_ctx *ctx, double Tobs, double t0, int NF, int NT, double wdt,
+                                       double wdf, double A, double nx, int kmin, int kmax, int norb,
+                                       const double *orbit_t, const double *orbit_pos) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_setup: null context");
+  if (!(Tobs > 0) || !(wdt > 0) || !(wdf > 0) || !(A >= 0) || !(nx > 0) || NF < 2)
+    return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_setup: need Tobs, wdt, wdf, nx > 0, A >= 0, NF >= 2");
+  if (!smooth23_even(NT) || NT < 8 || NT > kWvMaxNT)
+    return set_err(GLASS_ERR_SIZE, "glass_gpu_wavelet_setup: NT must be even, of the form 2^a 3^b, 8..4096");
+  if (kmin < 0 || kmax <= kmin || kmin % NT || kmax % NT || kmax / NT > NF + 1)
+    return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_setup: need 0 <= kmin < kmax, both whole layers of the grid");
+  WvGridHost h;
+  h.Tobs = Tobs;
+  h.t0 = t0;
+  h.NF = NF;
+  h.NT = NT;
+  h.wdt = wdt;
+  h.wdf = wdf;
+  h.A = A;
+  h.nx = nx;
+  h.kmin = kmin;
+  h.kmax = kmax;
+  if (orbit_t || orbit_pos) {
+    if (!orbit_t || !orbit_pos || norb < 20 || norb > kWvMaxOrb)
+      return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_setup: orbit needs t and positions of 20..2048 nodes");
+    h.orb_t.assign(orbit_t, orbit_t + norb);
+    h.orb_pos.assign(orbit_pos, orbit_pos + (size_t)9 * norb);
+    for (int i = 1; i < norb; i++)
+      if (!(h.orb_t[i] > h.orb_t[i - 1])) return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_setup: orbit times must increase");
+  } else {
+    wv_analytic_orbit(Tobs, t0, h.orb_t, h.orb_pos);
+    if ((int)h.orb_t.size() > kWvMaxOrb) return set_err(GLASS_ERR_SIZE, "glass_gpu_wavelet_setup: observation too long");
+  }
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "wavelet setup sync");
+  cudaFree(ctx->wv_grid_mem);
+  cudaFree(ctx->wv_data_mem);
+  cudaFree(ctx->wv_work_mem);
+  ctx->wv_grid_mem = ctx->wv_data_mem = ctx->wv_work_mem = nullptr;
+  ctx->wv_data_ready = false;
+  ctx->wv = WvGridDev{};
+  ctx->wvw = WvWorkDev{};
+  GLASS_CUDA(wv_build_grid(h, &ctx->wv, &ctx->wv_grid_mem, ctx->stream), "wavelet grid tables");
+  const size_t N = (size_t)(kmax - kmin);
+  GLASS_CUDA(cudaMalloc(&ctx->wv_data_mem, sizeof(double) * 12 * N), "cudaMalloc(wavelet data)");
+  ctx->wv.res = (const double *)ctx->wv_data_mem;
+  ctx->wv.invC = (const double *)ctx->wv_data_mem + 3 * N;
+  const size_t wb = wv_work_bytes(kWvChunk, ctx->wv.norb, NT);
+  GLASS_CUDA(cudaMalloc(&ctx->wv_work_mem, wb), "cudaMalloc(wavelet work)");
+  wv_work_carve(ctx->wvw, ctx->wv_work_mem, kWvChunk, ctx->wv.norb, NT);
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, const double *rY, const double *rZ,
+                                          const double *invC) {
+  if (!ctx || !rX || !rY || !rZ || !invC) return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_set_data: null argument");
+  if (!ctx->wv_grid_mem) return set_err(GLASS_ERR_STATE, "glass_gpu_wavelet_set_data: call glass_gpu_wavelet_setup first");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t N = (size_t)ctx->wv.N;
+  double *d = (double *)ctx->wv_data_mem;
+  GLASS_CUDA(cudaMemcpyAsync(d, rX, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream), "upload rX");
+  GLASS_CUDA(cudaMemcpyAsync(d + N, rY, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream), "upload rY");
+  GLASS_CUDA(cudaMemcpyAsync(d + 2 * N, rZ, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream), "upload rZ");
+  GLASS_CUDA(cudaMemcpyAsync(d + 3 * N, invC, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, ctx->stream),
+             "upload invC");
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "wavelet data sync");
+  ctx->wv_data_ready = true;
+  return GLASS_OK;
+}
+
+static int wv_check(glass_gpu_ctx *ctx, int nitems, const void *params, const char *who, bool need_data) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "%s: null context", who);
+  if (nitems < 0) return set_err(GLASS_ERR_ARG, "%s: negative item count", who);
+  if (nitems > 0 && !params) return set_err(GLASS_ERR_ARG, "%s: null params", who);
+  if (!ctx->wv_grid_mem) return set_err(GLASS_ERR_STATE, "%s: call glass_gpu_wavelet_setup first", who);
+  if (need_data && !ctx->wv_data_ready) return set_err(GLASS_ERR_STATE, "%s: call glass_gpu_wavelet_set_data first", who);
+  return ctx_activate(ctx);
+}
+
+extern "C" int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int nitems, const double *params,
+                                             const double *term_x, double *dlogl, double *term_y, double *hh,
+                                             int *status) {
+  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_dlogl_batch", true);
+  if (rc) return rc;
+  ctx->last_launches = 0;
+  for (int off = 0; off < nitems; off += kWvChunk) {
+    const int n = std::min(kWvChunk, nitems - off);
+    GLASS_CUDA(wv_waveform_launch(ctx->wv, ctx->wvw, n, params + 8 * (size_t)off, status ? status + off : nullptr,
+                                  ctx->stream, &ctx->last_launches),
+               "wavelet waveform launch");
+    GLASS_CUDA(wv_dlogl_launch(ctx->wv, ctx->wvw, n, term_x ? term_x + off : nullptr, dlogl ? dlogl + off : nullptr,
+                               term_y ? term_y + off : nullptr, hh ? hh + off : nullptr,
+                               status ? status + off : nullptr, ctx->stream, &ctx->last_launches),
+               "wavelet dlogl launch");
+  }
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int nitems, const double *params, int *info,
+                                                double *xyz, int *status) {
+  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_waveform_batch", false);
+  if (rc) return rc;
+  ctx->last_launches = 0;
+  const size_t per = (size_t)3 * kWvMaxLayers * ctx->wv.NT;
+  for (int off = 0; off < nitems; off += kWvChunk) {
+    const int n = std::min(kWvChunk, nitems - off);
+    GLASS_CUDA(wv_waveform_launch(ctx->wv, ctx->wvw, n, params + 8 * (size_t)off, status ? status + off : nullptr,
+                                  ctx->stream, &ctx->last_launches),
+               "wavelet waveform launch");
+    GLASS_CUDA(wv_export(ctx->wv, ctx->wvw, n, info ? info + 4 * (size_t)off : nullptr, xyz ? xyz + per * off : nullptr,
+                         ctx->stream),
+               "wavelet export");
+  }
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params,
+                                                  const double *term_x, double *dlogl, double *term_y, double *hh,
+                                                  int *status) {
+  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_dlogl_batch_host", true);
+  if (rc) return rc;
+  if (nitems == 0) return GLASS_OK;
+  const size_t n = (size_t)nitems;
+  const size_t bytes = sizeof(double) * n * 12 + sizeof(int) * n + 256;
+  if ((rc = ensure_stage(ctx, bytes))) return rc;
+  double *dp = (double *)ctx->d_stage, *dtx = dp + 8 * n, *ddl = dtx + n, *dty = ddl + n, *dhh = dty + n;
+  int *dst = (int *)(dhh + n);
+  GLASS_CUDA(cudaMemcpyAsync(dp, params, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, ctx->stream), "upload params");
+  if (term_x)
+    GLASS_CUDA(cudaMemcpyAsync(dtx, term_x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream), "upload term_x");
+  if ((rc = glass_gpu_wavelet_dlogl_batch(ctx, nitems, dp, term_x ? dtx : nullptr, ddl, dty, dhh, dst))) return rc;
+  if (dlogl) GLASS_CUDA(cudaMemcpyAsync(dlogl, ddl, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "dl");
+  if (term_y) GLASS_CUDA(cudaMemcpyAsync(term_y, dty, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "ty");
+  if (hh) GLASS_CUDA(cudaMemcpyAsync(hh, dhh, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "hh");
+  if (status) GLASS_CUDA(cudaMemcpyAsync(status, dst, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream), "st");
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "wavelet dlogl sync");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, int *info,
+                                                     double *xyz, int *status) {
+  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_waveform_batch_host", false);
+  if (rc) return rc;
+  if (nitems == 0) return GLASS_OK;
+  const size_t per = (size_t)3 * kWvMaxLayers * ctx->wv.NT;
+  for (int off = 0; off < nitems; off += kWvChunk) {
+    const size_t n = (size_t)std::min(kWvChunk, nitems - off);
+    const size_t bytes = sizeof(double) * n * (8 + per) + sizeof(int) * n * 5 + 256;
+    if ((rc = ensure_stage(ctx, bytes))) return rc;
+    double *dp = (double *)ctx->d_stage, *dx = dp + 8 * n;
+    int *dinfo = (int *)(dx + per * n), *dst = dinfo + 4 * n;
+    GLASS_CUDA(cudaMemcpyAsync(dp, params + 8 * (size_t)off, sizeof(double) * 8 * n, cudaMemcpyHostToDevice,
+                               ctx->stream),
+               "upload params");
+    if ((rc = glass_gpu_wavelet_waveform_batch(ctx, (int)n, dp, dinfo, dx, dst))) return rc;
+    if (info)
+      GLASS_CUDA(cudaMemcpyAsync(info + 4 * (size_t)off, dinfo, sizeof(int) * 4 * n, cudaMemcpyDeviceToHost,
+                                 ctx->stream),
+                 "info");
+    if (xyz)
+      GLASS_CUDA(cudaMemcpyAsync(xyz + per * off, dx, sizeof(double) * per * n, cudaMemcpyDeviceToHost, ctx->stream),
+                 "xyz");
+    if (status)
+      GLASS_CUDA(cudaMemcpyAsync(status + off, dst, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream), "status");
+    GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "wavelet waveform sync");
+  }
+  return GLASS_OK;
 }

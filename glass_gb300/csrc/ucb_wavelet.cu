@@ -1,0 +1,914 @@
+// Wavelet-domain UCB waveform (ucb/src/glass_ucb_waveform.c:1061-1240) and its
+// sparse-pixel likelihood (utils/src/glass_model.c:624-691) for batches of
+// sources on sm_103a, in FP64 with the reference's order of operations
+// (compiled with -fmad=false), so that results agree with the reference to
+// rounding.
+//
+// Per source the reference builds barycentre amplitude/phase splines on the
+// orbit nodes, runs the LISA response on the ~200 nodes (8 delayed link terms
+// per TDI channel, utils/src/glass_lisa.c:757-1074), turns each channel into
+// amplitude/phase splines, samples the heterodyned signal at NT (nl + 1)
+// points and applies the per-layer WDM transform
+// (utils/src/glass_wavelet.c:544-611).  The GPU version splits that into:
+//  * wv_plan_kernel    one thread per source: layers, geometry, the two
+//                      barycentre splines (Thomas sweeps; the grid's own
+//                      factors are precomputed, only the data sweeps remain);
+//  * wv_resp_kernel    one thread per (source, orbit node): light-time shift
+//                      and the X, Y, Z responses M, Mf;
+//  * wv_tdi_kernel     one thread per (source, channel): amplitude sign flips,
+//                      phase extraction and unwrapping (sequential scans as in
+//                      utils/src/glass_math.c:1034-1052, 1244-1308), and the
+//                      two channel splines;
+//  * wv_layers_kernel  one CTA per (source, channel): the N_ds samples go
+//                      straight into shared memory in digit-reversed order, an
+//                      in-place mixed-radix (3, 4, 2) FFT gives the packed real
+//                      spectrum, and each layer's windowed NT-point inverse FFT
+//                      runs in a second shared buffer (3 NT complex doubles in
+//                      all: 192 KB at NT = 4096, so the reference's own grid fits);
+//  * wv_dlogl_kernel   one CTA per source: the nine XYZ cross terms of (d|h)
+//                      and (h|h) over the source's pixels, gathered from the
+//                      segment's residual and 3x3 inverse covariance.
+// Everything that does not depend on the source (orbit splines, S/C positions
+// at the spline nodes and at the downsampled times, windows, twiddles and the
+// spline systems' factorisations) is built once per grid on the host.
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "glass_common.cuh"
+#include "ucb_wavelet.cuh"
+#include "wdm.cuh"
+
+namespace glass {
+namespace {
+
+constexpr double kVEARTH = 0.00010103671;  // utils/src/glass_constants.h:89
+constexpr double kSQRT2 = 1.41421356237309504880;
+constexpr int kOrbSamplesPerYear = 200;     // utils/src/glass_lisa.h:37
+
+// ------------------------------------------------------------ splines
+// c points at [4][n] coefficients; value at x[j] + d.
+__device__ __forceinline__ double spl_eval(const double *c, int n, int j, double d) {
+  return c[j] + c[n + j] * d + c[2 * n + j] * d * d + c[3 * n + j] * d * d * d;
+}
+
+// even_sampled_search (utils/src/glass_math.c:393-402)
+__device__ __forceinline__ int even_index(const double *x, int n, double v) {
+  const double dx = x[1] - x[0];
+  int j = (int)floor((v - x[0]) / dx);
+  if (j < 0) j = 0;
+  if (j > n - 1) j = n - 1;
+  return j;
+}
+
+// binary_search (utils/src/glass_math.c:443-473): the largest node <= v; values
+// outside the nodes, where the reference reads outside its array, are clamped.
+__device__ __forceinline__ int bin_index(const double *x, int n, double v) {
+  if (!(v > x[0])) return 0;
+  if (v >= x[n - 1]) return v == x[n - 1] ? n - 1 : n - 2;
+  const double dx = (x[n - 1] - x[0]) / (double)(n - 1);
+  int j = (int)((v - x[0]) / dx);
+  j = min(max(j, 0), n - 2);
+  while (j > 0 && x[j] > v) j--;
+  while (j < n - 2 && x[j + 1] <= v) j++;
+  return j;
+}
+
+// Data part of the natural cubic spline solve (utils/src/glass_math.c:101-175)
+// on a grid whose factors fac = {h, l, mu} are precomputed; c[0..n) holds y.
+__device__ void spline_sweeps(double *c, int n, const double *fac) {
+  const double *h = fac, *l = fac + n, *mu = fac + 2 * n;
+  double *c0 = c, *c1 = c + n, *c2 = c + 2 * n, *c3 = c + 3 * n;
+  double zprev = 0.0;
+  c2[0] = 0.0;
+  for (int i = 1; i < n - 1; i++) {
+    const double al = 3.0 * ((c0[i + 1] - c0[i]) / h[i] - (c0[i] - c0[i - 1]) / h[i - 1]);
+    zprev = (al - h[i - 1] * zprev) / l[i];
+    c2[i] = zprev;
+  }
+  c1[n - 1] = 0.0;
+  c2[n - 1] = 0.0;
+  c3[n - 1] = 0.0;
+  for (int i = n - 2; i >= 0; i--) {
+    c2[i] = c2[i] - mu[i] * c2[i + 1];
+    c1[i] = (c0[i + 1] - c0[i]) / h[i] - h[i] * (c2[i + 1] + 2.0 * c2[i]) / 3.0;
+    c3[i] = (c2[i + 1] - c2[i]) / (3.0 * h[i]);
+  }
+}
+
+// ------------------------------------------------------------ plan
+__global__ void wv_plan_kernel(WvGridDev g, int n, const double *params, WvSrc *srcs, double *ssb, int *status) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double *p = params + 8 * (size_t)s;
+  WvSrc S;
+  const double Tobs = g.Tobs;
+  bool ok = true;
+  for (int q = 0; q < 8; q++) ok = ok && isfinite(p[q]);
+  ok = ok && fabs(p[1]) <= 1.0 && fabs(p[4]) <= 1.0 && p[0] > 0.0;
+  S.status = ok ? 0 : 1;
+  S.jmin = S.nl = S.jlo = S.c = 0;
+  if (ok) {
+    // ucb_wavelet_layers
+    const double fstart = p[0] / Tobs;
+    const double fstop = (p[0] / Tobs + p[7] / Tobs / Tobs);
+    double fmin, fmax;
+    if (fstart < fstop) {
+      fmin = fstart * (1.0 - kVEARTH);
+      fmax = fstop * (1.0 + kVEARTH);
+    } else {
+      fmin = fstop * (1.0 - kVEARTH);
+      fmax = fstart * (1.0 + kVEARTH);
+    }
+    const double jr = rint(fmin / g.wdf);
+    if (!(fabs(jr) < 1e9)) {
+      S.status = 1;
+    } else {
+      const int j = (int)jr;
+      const double dfmin = fmin - j * g.wdf, dfmax = fmax - j * g.wdf;
+      int jmin = j, jmax = j;
+      if (dfmin < 0.0 && fabs(dfmin) > g.A / kPI2) jmin = j - 1;
+      if (dfmax > 0.0 && fabs(dfmax) > g.A / kPI2) jmax = j + 1;
+      S.jmin = jmin;
+      S.nl = jmax - jmin + 1;
+      const int jlo = max(jmin, g.lmin), jhi = min(jmin + S.nl, g.lmax);
+      S.jlo = jlo;
+      S.c = max(0, jhi - jlo);
+    }
+  }
+  // geometry (LISA_polarization_tensor, utils/src/glass_lisa.c:1566-1596)
+  const double costh = p[1], phi = p[2], cosi = p[4], psi = p[5];
+  const double sinth = sqrt(1.0 - costh * costh), cosph = cos(phi), sinph = sin(phi);
+  const double u[3] = {costh * cosph, costh * sinph, -sinth};
+  const double v[3] = {sinph, -cosph, 0.};
+  S.k[0] = -sinth * cosph;
+  S.k[1] = -sinth * sinph;
+  S.k[2] = -costh;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      S.ep[3 * i + j] = v[i] * v[j] - u[i] * u[j];
+      S.ec[3 * i + j] = u[i] * v[j] + v[i] * u[j];
+    }
+  S.c2p = cos(2. * psi);
+  S.s2p = sin(2. * psi);
+  S.Ap = 0.5 * (1. + cosi * cosi);
+  S.Ac = -cosi;
+  S.fhet = (S.jmin - 1) * g.wdf;
+  S.pad = 0;
+  srcs[s] = S;
+  if (status) status[s] = S.status;
+  if (S.status) return;
+  // barycentre amplitude and phase on the orbit nodes (ucb_barycenter_waveform,
+  // ucb/src/glass_ucb_waveform.c:330-362), then their splines
+  const int norb = g.norb;
+  double *amp = ssb + (size_t)s * 8 * norb, *ph = amp + 4 * norb;
+  const double f0 = p[0] / Tobs, phi0 = p[6], fdot = p[7] / Tobs / Tobs, fddot = 0.0;
+  const double A0 = exp(p[3]);
+  for (int i = 0; i < norb; i++) {
+    const double t = g.orb_t[i];
+    ph[i] = -phi0 + kPI2 * (f0 * t + 0.5 * fdot * t * t + 1.0 / 6.0 * fddot * t * t * t);
+    amp[i] = A0 * (1.0 + 2.0 / 3.0 * fdot / f0 * t);
+  }
+  spline_sweeps(amp, norb, g.fac_orb);
+  spline_sweeps(ph, norb, g.fac_orb);
+}
+
+// ------------------------------------------------------------ response
+struct Pol {
+  double Ap, Ac, c2p, s2p;
+  const double *amp, *ph;
+  const double *x;
+  int n;
+};
+
+__device__ __forceinline__ void hpc(const Pol &P, double t, double &hp, double &hc, double &hpf, double &hcf) {
+  const int j = even_index(P.x, P.n, t);
+  const double d = t - P.x[j];
+  const double amp = spl_eval(P.amp, P.n, j, d), ph = spl_eval(P.ph, P.n, j, d);
+  double sp, cp;
+  sincos(ph, &sp, &cp);
+  hp = amp * (P.Ap * P.c2p * cp + P.Ac * P.s2p * sp);
+  hc = amp * (P.Ac * P.c2p * sp - P.Ap * P.s2p * cp);
+  hpf = amp * (-P.Ap * P.c2p * sp + P.Ac * P.s2p * cp);
+  hcf = amp * (P.Ac * P.c2p * cp + P.Ap * P.s2p * sp);
+}
+
+// One Michelson channel (vertex a, arms b and c) from eight delayed link
+// terms; LISA_TDI_spline, utils/src/glass_lisa.c:769-887.
+__device__ void tdi_channel(const Pol &P, double tn, int a, int b, int c, const double *App, const double *Apm,
+                            const double *Acp, const double *Acm, const double *kr, const double *L, double &Mo,
+                            double &Mfo) {
+  double m = 0.0, mf = 0.0, hp, hc, hpf, hcf, t;
+  t = tn - kr[a] - 2.0 * L[c] - 2.0 * L[b];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m += hp * Apm[b] + hc * Acm[b];
+  m -= hp * App[c] + hc * Acp[c];
+  mf += hpf * Apm[b] + hcf * Acm[b];
+  mf -= hpf * App[c] + hcf * Acp[c];
+  t = tn - kr[b] - L[c] - 2.0 * L[b];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m -= hp * Apm[c] + hc * Acm[c];
+  m += hp * App[c] + hc * Acp[c];
+  mf -= hpf * Apm[c] + hcf * Acm[c];
+  mf += hpf * App[c] + hcf * Acp[c];
+  t = tn - kr[c] - L[b] - 2.0 * L[c];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m += hp * App[b] + hc * Acp[b];
+  m -= hp * Apm[b] + hc * Acm[b];
+  mf += hpf * App[b] + hcf * Acp[b];
+  mf -= hpf * Apm[b] + hcf * Acm[b];
+  t = tn - kr[a] - 2.0 * L[b];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m -= hp * Apm[b] + hc * Acm[b];
+  m += hp * Apm[c] + hc * Acm[c];
+  mf -= hpf * Apm[b] + hcf * Acm[b];
+  mf += hpf * Apm[c] + hcf * Acm[c];
+  t = tn - kr[a] - 2.0 * L[c];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m += hp * App[c] + hc * Acp[c];
+  m -= hp * App[b] + hc * Acp[b];
+  mf += hpf * App[c] + hcf * Acp[c];
+  mf -= hpf * App[b] + hcf * Acp[b];
+  t = tn - kr[c] - L[b];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m -= hp * App[b] + hc * Acp[b];
+  m += hp * Apm[b] + hc * Acm[b];
+  mf -= hpf * App[b] + hcf * Acp[b];
+  mf += hpf * Apm[b] + hcf * Acm[b];
+  t = tn - kr[b] - L[c];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m += hp * Apm[c] + hc * Acm[c];
+  m -= hp * App[c] + hc * Acp[c];
+  mf += hpf * Apm[c] + hcf * Acm[c];
+  mf -= hpf * App[c] + hcf * Acp[c];
+  t = tn - kr[a];
+  hpc(P, t, hp, hc, hpf, hcf);
+  m -= hp * Apm[c] + hc * Acm[c];
+  m += hp * App[b] + hc * Acp[b];
+  mf -= hpf * Apm[c] + hcf * Acm[c];
+  mf += hpf * App[b] + hcf * Acp[b];
+  Mo = m;
+  Mfo = mf;
+}
+
+// LISA_spline_response (utils/src/glass_lisa.c:920-1074) at one node, plus the
+// S/C-1 phase used as the reference phase (LISA_spacecraft_to_barycenter_time).
+__global__ void wv_resp_kernel(WvGridDev g, int n, const WvSrc *srcs, const double *ssb, double *resp) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int norb = g.norb;
+  if (idx >= (long long)n * norb) return;
+  const int s = (int)(idx / norb), m = (int)(idx - (long long)s * norb);
+  const WvSrc &S = srcs[s];
+  if (S.status) return;
+  const double *amp = ssb + (size_t)s * 8 * norb, *ph = amp + 4 * norb;
+  const double t = g.tssb[m];
+  const double *G = g.geo + 21 * (size_t)m;
+  double x[3][3], nv[3][3], L[3];
+  for (int i = 0; i < 3; i++)
+    for (int d = 0; d < 3; d++) {
+      x[i][d] = G[3 * i + d];
+      nv[i][d] = G[9 + 3 * i + d];
+    }
+  for (int i = 0; i < 3; i++) L[i] = G[18 + i];
+  const double k[3] = {S.k[0], S.k[1], S.k[2]};
+  double kr0 = 0.0;
+  for (int d = 0; d < 3; d++) kr0 += k[d] * x[0][d];
+  const double tsc = t - kr0;
+  double *out = resp + (size_t)s * 7 * norb;
+  {
+    const int j = even_index(g.orb_t, norb, tsc);
+    out[6 * norb + m] = spl_eval(ph, norb, j, tsc - g.orb_t[j]);
+  }
+  double kr[3], kn[3], dp[3], dc[3], App[3], Apm[3], Acp[3], Acm[3];
+  for (int i = 0; i < 3; i++) {
+    kr[i] = 0.0;
+    for (int d = 0; d < 3; d++) kr[i] += k[d] * x[i][d];
+  }
+  for (int i = 0; i < 3; i++) {
+    kn[i] = 0.0;
+    for (int d = 0; d < 3; d++) kn[i] += k[d] * nv[i][d];
+  }
+  for (int i = 0; i < 3; i++) {
+    dp[i] = 0.0;
+    dc[i] = 0.0;
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) {
+        dp[i] += (nv[i][a] * nv[i][b]) * S.ep[3 * a + b];
+        dc[i] += (nv[i][a] * nv[i][b]) * S.ec[3 * a + b];
+      }
+  }
+  for (int i = 0; i < 3; i++) {
+    App[i] = dp[i] / (1.0 + kn[i]);
+    Apm[i] = dp[i] / (1.0 - kn[i]);
+    Acp[i] = dc[i] / (1.0 + kn[i]);
+    Acm[i] = dc[i] / (1.0 - kn[i]);
+  }
+  Pol P{S.Ap, S.Ac, S.c2p, S.s2p, amp, ph, g.orb_t, norb};
+  double M, Mf;
+  tdi_channel(P, t, 0, 1, 2, App, Apm, Acp, Acm, kr, L, M, Mf);
+  out[0 * norb + m] = M;
+  out[3 * norb + m] = Mf;
+  tdi_channel(P, t, 1, 2, 0, App, Apm, Acp, Acm, kr, L, M, Mf);
+  out[1 * norb + m] = M;
+  out[4 * norb + m] = Mf;
+  tdi_channel(P, t, 2, 0, 1, App, Apm, Acp, Acm, kr, L, M, Mf);
+  out[2 * norb + m] = M;
+  out[5 * norb + m] = Mf;
+}
+
+// ------------------------------------------------------------ TDI splines
+// extract_amplitude_and_phase + unwrap_phase (utils/src/glass_math.c:1244-1308,
+// 1034-1052) and the channel's amplitude / phase splines; one thread per
+// (source, channel).  The flip and phase-jump arrays live in the slots of
+// the spline's c1 and c2 coefficients until the sweeps overwrite them.
+__global__ void wv_tdi_kernel(WvGridDev g, int n, const WvSrc *srcs, const double *resp, double *tdi) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 3 * n) return;
+  const int s = idx / 3, ch = idx - 3 * s;
+  if (srcs[s].status) return;
+  const int N = g.norb;
+  const double *M = resp + ((size_t)s * 7 + ch) * N, *Mf = resp + ((size_t)s * 7 + 3 + ch) * N;
+  const double *phR = resp + ((size_t)s * 7 + 6) * N;
+  double *ca = tdi + ((size_t)s * 3 + ch) * 8 * N, *cp = ca + 4 * N;
+  double *As = ca, *flip = ca + N, *pj = ca + 2 * N;
+  for (int i = 0; i < N; i++) As[i] = sqrt(M[i] * M[i] + Mf[i] * Mf[i]);
+  flip[0] = 1.0;
+  pj[0] = 0.0;
+  int i = 1;
+  do {
+    flip[i] = flip[i - 1];
+    pj[i] = pj[i - 1];
+    if ((As[i] < As[i - 1]) && (As[i] < As[i + 1])) {
+      const double d1 = As[i + 1] + As[i - 1] - 2.0 * As[i];
+      const double d2 = -As[i + 1] + As[i - 1] - 2.0 * As[i];
+      const double d3 = -As[i + 1] + As[i - 1] + 2.0 * As[i];
+      if (fabs(d2 / d1) < 0.1) {
+        flip[i + 1] = -1.0 * flip[i];
+        pj[i + 1] = pj[i] + kPI;
+        i++;
+      }
+      if (fabs(d3 / d1) < 0.1) {
+        flip[i] = -1.0 * flip[i - 1];
+        pj[i] = pj[i - 1] + kPI;
+      }
+    }
+    i++;
+  } while (i < N - 1);
+  flip[N - 1] = flip[N - 2];
+  pj[N - 1] = pj[N - 2];
+  for (i = 0; i < N; i++) {
+    As[i] = flip[i] * As[i];
+    const double v = remainder(phR[i], kPI2);
+    cp[i] = -atan2(Mf[i], M[i]) + pj[i] - v;
+  }
+  double v = cp[0];
+  for (i = 0; i < N; i++) {
+    double u = cp[i];
+    const double q = rint(fabs(u - v) / (kPI2));
+    if (q > 0.0) {
+      if (v > u)
+        u += q * kPI2;
+      else
+        u -= q * kPI2;
+    }
+    v = u;
+    cp[i] = u;
+  }
+  spline_sweeps(ca, N, g.fac_ssb);
+  spline_sweeps(cp, N, g.fac_ssb);
+}
+
+// ------------------------------------------------------------ FFTs
+// Radices of an in-place decimation-in-time FFT: 3s, then 4s, then a 2.
+struct RadixPlan {
+  int n;
+  int r[24];
+  int pre[24];  // R_0 ... R_{s-1}
+};
+
+__device__ __forceinline__ void radix_plan(int L, RadixPlan &P) {
+  P.n = 0;
+  int rem = L, pre = 1;
+  while (rem % 3 == 0) {
+    P.r[P.n] = 3;
+    P.pre[P.n++] = pre;
+    pre *= 3;
+    rem /= 3;
+  }
+  while (rem % 4 == 0) {
+    P.r[P.n] = 4;
+    P.pre[P.n++] = pre;
+    pre *= 4;
+    rem /= 4;
+  }
+  while (rem % 2 == 0) {
+    P.r[P.n] = 2;
+    P.pre[P.n++] = pre;
+    pre *= 2;
+    rem /= 2;
+  }
+}
+
+// Input position of element x: its stage digits read in reverse.
+__device__ __forceinline__ int digit_rev(int x, const RadixPlan &P) {
+  int pos = 0;
+  for (int s = P.n - 1; s >= 0; s--) {
+    const int d = x % P.r[s];
+    x /= P.r[s];
+    pos += d * P.pre[s];
+  }
+  return pos;
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// In-place mixed-radix FFT of a[L] held in digit-reversed order; result in
+// natural order.  tw[j * twmul] = e^{-2 pi i j / L}; sign -1 forward, +1
+// inverse (unnormalised).  Whole CTA.
+__device__ void dit_fft(double2 *a, int L, const RadixPlan &P, const double2 *__restrict__ tw, int twmul,
+                        int sign) {
+  int p = 1;
+  for (int st = 0; st < P.n; st++) {
+    const int R = P.r[st], q = p * R, nb = L / R;
+    const int tstep = (L / q) * twmul;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      const int b = t / p, k = t - b * p;
+      double2 *base = a + (size_t)b * q + k;
+      if (R == 4) {
+        double2 v0 = base[0], v1 = base[p], v2 = base[2 * p], v3 = base[3 * p];
+        double2 w1 = tw[k * tstep], w2 = tw[2 * k * tstep], w3 = tw[3 * k * tstep];
+        if (sign > 0) {
+          w1.y = -w1.y;
+          w2.y = -w2.y;
+          w3.y = -w3.y;
+        }
+        v1 = cmul(v1, w1);
+        v2 = cmul(v2, w2);
+        v3 = cmul(v3, w3);
+        const double2 t0 = make_double2(v0.x + v2.x, v0.y + v2.y), t1 = make_double2(v0.x - v2.x, v0.y - v2.y);
+        const double2 t2 = make_double2(v1.x + v3.x, v1.y + v3.y), t3 = make_double2(v1.x - v3.x, v1.y - v3.y);
+        const double2 t3r = sign < 0 ? make_double2(t3.y, -t3.x) : make_double2(-t3.y, t3.x);
+        base[0] = make_double2(t0.x + t2.x, t0.y + t2.y);
+        base[p] = make_double2(t1.x + t3r.x, t1.y + t3r.y);
+        base[2 * p] = make_double2(t0.x - t2.x, t0.y - t2.y);
+        base[3 * p] = make_double2(t1.x - t3r.x, t1.y - t3r.y);
+      } else if (R == 2) {
+        double2 v0 = base[0], v1 = base[p];
+        double2 w1 = tw[k * tstep];
+        if (sign > 0) w1.y = -w1.y;
+        v1 = cmul(v1, w1);
+        base[0] = make_double2(v0.x + v1.x, v0.y + v1.y);
+        base[p] = make_double2(v0.x - v1.x, v0.y - v1.y);
+      } else {
+        double2 v0 = base[0], v1 = base[p], v2 = base[2 * p];
+        double2 w1 = tw[k * tstep], w2 = tw[2 * k * tstep];
+        if (sign > 0) {
+          w1.y = -w1.y;
+          w2.y = -w2.y;
+        }
+        v1 = cmul(v1, w1);
+        v2 = cmul(v2, w2);
+        const double s3 = 0.86602540378443864676 * (double)sign;
+        const double2 sm = make_double2(v1.x + v2.x, v1.y + v2.y), df = make_double2(v1.x - v2.x, v1.y - v2.y);
+        const double2 m1 = make_double2(v0.x - 0.5 * sm.x, v0.y - 0.5 * sm.y);
+        const double2 m2 = make_double2(-s3 * df.y, s3 * df.x);
+        base[0] = make_double2(v0.x + sm.x, v0.y + sm.y);
+        base[p] = make_double2(m1.x + m2.x, m1.y + m2.y);
+        base[2 * p] = make_double2(m1.x - m2.x, m1.y - m2.y);
+      }
+    }
+    __syncthreads();
+    p = q;
+  }
+}
+
+// ------------------------------------------------------------ layers
+constexpr int kLayerThreads = 256;
+
+__global__ void __launch_bounds__(kLayerThreads) wv_layers_kernel(WvGridDev g, int n, const WvSrc *srcs,
+                                                                  const double *ssb, const double *tdi,
+                                                                  double *coef) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  const int s = blockIdx.x / 3, ch = blockIdx.x - 3 * (blockIdx.x / 3);
+  const WvSrc &S = srcs[s];
+  if (S.status || S.c == 0) return;
+  const int nl = S.nl, NT = g.NT, Nds = NT * (nl + 1), M = Nds / 2, norb = g.norb;
+  double2 *zb = reinterpret_cast<double2 *>(sm_raw);
+  double2 *lb = zb + M;
+  RadixPlan PM, PN;
+  radix_plan(M, PM);
+  radix_plan(NT, PN);
+  const double *ph_ssb = ssb + (size_t)s * 8 * norb + 4 * norb;
+  const double *ca = tdi + ((size_t)s * 3 + ch) * 8 * norb, *cp = ca + 4 * norb;
+  const double k0 = S.k[0], k1 = S.k[1], k2 = S.k[2];
+  const double *r0 = g.r0ds[nl];
+  const double dtds = g.wdt / (double)(nl + 1);
+  // heterodyned samples (build_interpolated_waveform), packed two per complex
+  for (int i = threadIdx.x; i < Nds; i += blockDim.x) {
+    const double tds = g.t0 + i * dtds;
+    const double phhet = kPI2 * S.fhet * tds;
+    double kr = 0.0;
+    kr += k0 * r0[3 * i + 0];
+    kr += k1 * r0[3 * i + 1];
+    kr += k2 * r0[3 * i + 2];
+    const double tsc = tds - kr;
+    const int je = even_index(g.orb_t, norb, tsc);
+    const double phds = spl_eval(ph_ssb, norb, je, tsc - g.orb_t[je]);
+    const int jb = bin_index(g.tssb, norb, tds);
+    const double d = tds - g.tssb[jb];
+    const double a = spl_eval(ca, norb, jb, d);
+    double p = spl_eval(cp, norb, jb, d);
+    p += phds;
+    p -= phhet;
+    const double w = a * cos(p);
+    double *slot = reinterpret_cast<double *>(zb + digit_rev(i >> 1, PM));
+    slot[i & 1] = w;
+  }
+  __syncthreads();
+  const double2 *tw = g.tw[nl];
+  dit_fft(zb, M, PM, tw, 2, -1);
+  const double norm = g.norm_sqrtNF / (nl + 1.0);
+  const double *win = g.win[nl];
+  double *out = coef + ((size_t)s * 3 + ch) * (kWvMaxLayers * (size_t)NT);
+  for (int off = 0; off < nl; off++) {
+    const int m = S.jmin + off;
+    const int center = (off + 1) * NT / 2;
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+      const int j = t - NT / 2, idx = center + j;
+      double2 val = make_double2(0.0, 0.0);
+      if (j > -NT / 2 && idx >= 0 && idx <= M) {
+        double wt = win[j < 0 ? -j : j];
+        if (j == 0 && (m == 0 || m == g.NF)) wt /= 2.0;
+        // bin idx of the real spectrum from the packed spectrum
+        const double2 zk = zb[idx % M], zm0 = zb[(M - idx) % M];
+        const double2 zm = make_double2(zm0.x, -zm0.y);
+        const double2 e = tw[idx];
+        const double2 sm = make_double2(zk.x + zm.x, zk.y + zm.y), df = make_double2(zk.x - zm.x, zk.y - zm.y);
+        const double2 ed = cmul(e, df);
+        const double2 X = make_double2(0.5 * (sm.x + ed.y), 0.5 * (sm.y - ed.x));
+        val = make_double2(wt * X.x, wt * X.y);
+      }
+      lb[digit_rev(t, PN)] = val;
+    }
+    __syncthreads();
+    dit_fft(lb, NT, PN, tw, nl + 1, +1);
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+      const double re = lb[t].x / NT, im = lb[t].y / NT;
+      double v;
+      if (m == 0 || m == g.NF) {
+        v = (t % 2 == 0) ? re * kSQRT2 * norm : 0.0;
+      } else {
+        const double sgn = (m % 2 == 0) ? 1.0 : -1.0;
+        v = (((t + m) % 2 == 0) ? re : sgn * im) * norm;
+      }
+      out[(size_t)t * nl + off] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ likelihood
+constexpr int kDloglThreads = 256;
+
+__global__ void __launch_bounds__(kDloglThreads) wv_dlogl_kernel(WvGridDev g, int n, const WvSrc *srcs,
+                                                                 const double *coef, const double *term_x,
+                                                                 double *dlogl, double *term_y, double *hh_out,
+                                                                 int *status) {
+  const int s = blockIdx.x;
+  const WvSrc &S = srcs[s];
+  __shared__ double red[2][kDloglThreads / 32];
+  if (S.status) {
+    if (threadIdx.x == 0) {
+      if (dlogl) dlogl[s] = NAN;
+      if (term_y) term_y[s] = NAN;
+      if (hh_out) hh_out[s] = NAN;
+    }
+    return;
+  }
+  const int NT = g.NT, N = g.N, c = S.c, npix = NT * c;
+  const double *h0 = coef + (size_t)s * 3 * (kWvMaxLayers * (size_t)NT);
+  const double *h1 = h0 + kWvMaxLayers * (size_t)NT, *h2 = h1 + kWvMaxLayers * (size_t)NT;
+  const double *r = g.res, *ic = g.invC;
+  double dh = 0.0, hh = 0.0;
+  for (int q = threadIdx.x; q < npix; q += blockDim.x) {
+    const int i = q / c, j = S.jlo + (q - i * c);
+    const int k = i + j * NT - g.kmin;
+    const double a0 = h0[q], a1 = h1[q], a2 = h2[q];
+    const double d0 = r[k], d1 = r[N + k], d2 = r[2 * N + k];
+    const double c00 = ic[k], c01 = ic[N + k], c02 = ic[2 * N + k];
+    const double c10 = ic[3 * N + k], c11 = ic[4 * N + k], c12 = ic[5 * N + k];
+    const double c20 = ic[6 * N + k], c21 = ic[7 * N + k], c22 = ic[8 * N + k];
+    dh += d0 * a0 * c00 + d1 * a1 * c11 + d2 * a2 * c22 + d0 * a1 * c01 + d0 * a2 * c02 + d1 * a2 * c12 +
+          d1 * a0 * c10 + d2 * a0 * c20 + d2 * a1 * c21;
+    hh += a0 * a0 * c00 + a1 * a1 * c11 + a2 * a2 * c22 + a0 * a1 * c01 + a0 * a2 * c02 + a1 * a2 * c12 +
+          a1 * a0 * c10 + a2 * a0 * c20 + a2 * a1 * c21;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    dh += __shfl_xor_sync(0xffffffffu, dh, o);
+    hh += __shfl_xor_sync(0xffffffffu, hh, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = dh;
+    red[1][threadIdx.x >> 5] = hh;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    dh = 0.0;
+    hh = 0.0;
+    for (int w = 0; w < kDloglThreads / 32; w++) {
+      dh += red[0][w];
+      hh += red[1][w];
+    }
+    const double term = hh - 2.0 * dh;
+    if (term_y) term_y[s] = term;
+    if (hh_out) hh_out[s] = hh;
+    if (dlogl) {
+      const double tx = term_x ? term_x[s] : 0.0;
+      dlogl[s] = -0.5 * term - (-0.5 * tx);
+    }
+    if (status) status[s] = isfinite(term) ? (c == 0 ? 4 : 0) : 1;
+  }
+}
+
+__global__ void wv_info_kernel(int n, const WvSrc *srcs, int *info) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  info[4 * s + 0] = srcs[s].jmin;
+  info[4 * s + 1] = srcs[s].nl;
+  info[4 * s + 2] = srcs[s].jlo;
+  info[4 * s + 3] = srcs[s].status ? -1 : srcs[s].c;
+}
+
+}  // namespace
+
+// ================================================================ host side
+// initialize_interpolated_analytic_orbits (utils/src/glass_lisa.c:271-380) with
+// analytic_orbits (:77-124)
+void wv_analytic_orbit(double Tobs, double t0, std::vector<double> &t, std::vector<double> &pos) {
+  int n = (int)(kOrbSamplesPerYear * Tobs / kYEAR);
+  if (n < 20) n = 20;
+  const double buffer = Tobs / (double)(n - 1);
+  const double cadence = (Tobs + 2.0 * buffer) / (double)(n - 1);
+  const double R = kAU * (kLARM / (2.0 * kSQ3 * kAU));
+  static const double sbs[3] = {0.0, 0.866025403784439, -0.866025403784438};
+  static const double cbs[3] = {1.0, -0.5, -0.5};
+  t.resize(n);
+  pos.resize((size_t)9 * n);
+  for (int k = 0; k < n; k++) {
+    const double tt = t0 + k * cadence - buffer;
+    const double alpha = kPI2 * tt / kYEAR;
+    const double sa = sin(alpha), ca = cos(alpha);
+    const double sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca, AUca = kAU * ca, AUsa = kAU * sa;
+    t[k] = tt;
+    for (int i = 0; i < 3; i++) {
+      const double sb = sbs[i], cb = cbs[i];
+      pos[(size_t)(3 * i + 0) * n + k] = AUca + R * (saca * sb - (1. + sa2) * cb);
+      pos[(size_t)(3 * i + 1) * n + k] = AUsa + R * (saca * cb - (1. + ca2) * sb);
+      pos[(size_t)(3 * i + 2) * n + k] = -kSQ3 * R * (ca * cb + sa * sb);
+    }
+  }
+}
+
+namespace {
+
+// Host copy of the cubic spline (same arithmetic as spline_sweeps plus the
+// grid factors), evaluated with the binary-search lookup.
+struct HostSpline {
+  int n = 0;
+  const double *x = nullptr;
+  std::vector<double> c;  // [4][n]
+};
+
+static void grid_factors(const double *x, int n, double *fac) {
+  double *h = fac, *l = fac + n, *mu = fac + 2 * n;
+  for (int i = 0; i < 3 * n; i++) fac[i] = 0.0;
+  h[0] = x[1] - x[0];
+  for (int i = 1; i < n - 1; i++) h[i] = x[i + 1] - x[i];
+  l[0] = l[n - 1] = 1.0;
+  for (int i = 1; i < n - 1; i++) {
+    l[i] = 2.0 * (x[i + 1] - x[i - 1]) - h[i - 1] * mu[i - 1];
+    mu[i] = h[i] / l[i];
+  }
+}
+
+static void host_spline(HostSpline &sp, const double *x, const double *y, int n, const double *fac) {
+  sp.n = n;
+  sp.x = x;
+  sp.c.assign((size_t)4 * n, 0.0);
+  double *c0 = sp.c.data(), *c1 = c0 + n, *c2 = c0 + 2 * n, *c3 = c0 + 3 * n;
+  const double *h = fac, *l = fac + n, *mu = fac + 2 * n;
+  for (int i = 0; i < n; i++) c0[i] = y[i];
+  double z = 0.0;
+  c2[0] = 0.0;
+  for (int i = 1; i < n - 1; i++) {
+    const double al = 3.0 * ((c0[i + 1] - c0[i]) / h[i] - (c0[i] - c0[i - 1]) / h[i - 1]);
+    z = (al - h[i - 1] * z) / l[i];
+    c2[i] = z;
+  }
+  c1[n - 1] = c2[n - 1] = c3[n - 1] = 0.0;
+  for (int i = n - 2; i >= 0; i--) {
+    c2[i] = c2[i] - mu[i] * c2[i + 1];
+    c1[i] = (c0[i + 1] - c0[i]) / h[i] - h[i] * (c2[i + 1] + 2.0 * c2[i]) / 3.0;
+    c3[i] = (c2[i + 1] - c2[i]) / (3.0 * h[i]);
+  }
+}
+
+static double host_eval(const HostSpline &sp, double v) {
+  const int n = sp.n;
+  const double *x = sp.x;
+  int j;
+  if (!(v > x[0])) {
+    j = 0;
+  } else if (v >= x[n - 1]) {
+    j = v == x[n - 1] ? n - 1 : n - 2;
+  } else {
+    j = (int)(std::upper_bound(x, x + n, v) - x) - 1;
+  }
+  const double d = v - x[j];
+  const double *c = sp.c.data();
+  return c[j] + c[n + j] * d + c[2 * n + j] * d * d + c[3 * n + j] * d * d * d;
+}
+
+static void unit_root(long long j, long long P, double *c, double *s) {
+  long long r = j % P;
+  if (r < 0) r += P;
+  double sg = -1.0;
+  if (2 * r > P) {
+    r = P - r;
+    sg = 1.0;
+  }
+  const double a = 2.0 * M_PI * ((double)r / (double)P);
+  *c = cos(a);
+  *s = sg * sin(a);
+}
+
+}  // namespace
+
+size_t wv_work_bytes(int cap, int norb, int NT) {
+  auto pad = [](size_t b) { return (b + 255) / 256 * 256; };
+  return pad(sizeof(WvSrc) * (size_t)cap) + pad(sizeof(double) * (size_t)cap * 8 * norb) +
+         pad(sizeof(double) * (size_t)cap * 7 * norb) + pad(sizeof(double) * (size_t)cap * 24 * norb) +
+         pad(sizeof(double) * (size_t)cap * 3 * kWvMaxLayers * NT);
+}
+
+void wv_work_carve(WvWorkDev &w, void *base, int cap, int norb, int NT) {
+  auto pad = [](size_t b) { return (b + 255) / 256 * 256; };
+  char *p = (char *)base;
+  w.cap = cap;
+  w.src = (WvSrc *)p;
+  p += pad(sizeof(WvSrc) * (size_t)cap);
+  w.ssb = (double *)p;
+  p += pad(sizeof(double) * (size_t)cap * 8 * norb);
+  w.resp = (double *)p;
+  p += pad(sizeof(double) * (size_t)cap * 7 * norb);
+  w.tdi = (double *)p;
+  p += pad(sizeof(double) * (size_t)cap * 24 * norb);
+  w.coef = (double *)p;
+}
+
+cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStream_t s) {
+  const int norb = (int)h.orb_t.size(), NT = h.NT;
+  if (norb < 20 || norb > kWvMaxOrb || NT < 8 || NT > kWvMaxNT) return cudaErrorInvalidValue;
+  // orbit position splines on the orbit nodes
+  std::vector<double> fac_orb(3 * (size_t)norb), fac_ssb(3 * (size_t)norb), tssb(norb);
+  grid_factors(h.orb_t.data(), norb, fac_orb.data());
+  HostSpline pos[9];
+  for (int q = 0; q < 9; q++) host_spline(pos[q], h.orb_t.data(), h.orb_pos.data() + (size_t)q * norb, norb,
+                                          fac_orb.data());
+  const double dt = h.Tobs / (double)(norb - 1);
+  for (int i = 0; i < norb; i++) tssb[i] = h.t0 + i * dt;
+  grid_factors(tssb.data(), norb, fac_ssb.data());
+  // S/C positions, unit arm vectors and arm lengths at the TDI nodes
+  std::vector<double> geo(21 * (size_t)norb);
+  for (int m = 0; m < norb; m++) {
+    double x[3][3], nv[3][3], L[3];
+    for (int i = 0; i < 3; i++)
+      for (int d = 0; d < 3; d++) x[i][d] = host_eval(pos[3 * i + d], tssb[m]) / kCLIGHT;
+    for (int d = 0; d < 3; d++) {
+      nv[0][d] = x[1][d] - x[2][d];
+      nv[1][d] = x[2][d] - x[0][d];
+      nv[2][d] = x[0][d] - x[1][d];
+    }
+    for (int i = 0; i < 3; i++) {
+      L[i] = 0.0;
+      for (int d = 0; d < 3; d++) L[i] += nv[i][d] * nv[i][d];
+      L[i] = sqrt(L[i]);
+    }
+    for (int i = 0; i < 3; i++)
+      for (int d = 0; d < 3; d++) nv[i][d] /= L[i];
+    double *G = geo.data() + 21 * (size_t)m;
+    for (int i = 0; i < 3; i++)
+      for (int d = 0; d < 3; d++) {
+        G[3 * i + d] = x[i][d];
+        G[9 + 3 * i + d] = nv[i][d];
+      }
+    for (int i = 0; i < 3; i++) G[18 + i] = L[i];
+  }
+  // per layer count: S/C 1 at the downsampled times, window, twiddles
+  std::vector<double> r0[kWvMaxLayers + 1], win[kWvMaxLayers + 1];
+  std::vector<double2> tw[kWvMaxLayers + 1];
+  for (int nl = 1; nl <= kWvMaxLayers; nl++) {
+    const int Nds = NT * (nl + 1);
+    const double dtds = h.wdt / (double)(nl + 1);
+    r0[nl].resize(3 * (size_t)Nds);
+    for (int i = 0; i < Nds; i++) {
+      const double tds = h.t0 + i * dtds;
+      for (int d = 0; d < 3; d++) r0[nl][3 * (size_t)i + d] = host_eval(pos[d], tds) / kCLIGHT;
+    }
+    win[nl].resize(NT / 2 + 1);
+    wdm_window(nl + 1, NT, h.A, h.nx, true, win[nl].data());
+    tw[nl].resize(Nds);
+    for (int k = 0; k < Nds; k++) {
+      double c, sn;
+      unit_root(k, Nds, &c, &sn);
+      tw[nl][k] = make_double2(c, sn);
+    }
+  }
+  // one allocation
+  auto pad = [](size_t b) { return (b + 255) / 256 * 256; };
+  size_t bytes = pad(8 * (size_t)norb) * 2 + pad(8 * geo.size()) + pad(8 * fac_orb.size()) * 2;
+  for (int nl = 1; nl <= kWvMaxLayers; nl++)
+    bytes += pad(8 * r0[nl].size()) + pad(8 * win[nl].size()) + pad(16 * tw[nl].size());
+  char *base = nullptr;
+  cudaError_t e = cudaMalloc((void **)&base, bytes);
+  if (e != cudaSuccess) return e;
+  *mem = base;
+  char *p = base;
+  auto put = [&](const void *src, size_t b) -> const void * {
+    void *dst = p;
+    p += pad(b);
+    e = e != cudaSuccess ? e : cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, s);
+    return dst;
+  };
+  g->orb_t = (const double *)put(h.orb_t.data(), 8 * (size_t)norb);
+  g->tssb = (const double *)put(tssb.data(), 8 * (size_t)norb);
+  g->geo = (const double *)put(geo.data(), 8 * geo.size());
+  g->fac_orb = (const double *)put(fac_orb.data(), 8 * fac_orb.size());
+  g->fac_ssb = (const double *)put(fac_ssb.data(), 8 * fac_ssb.size());
+  g->r0ds[0] = nullptr;
+  g->win[0] = nullptr;
+  g->tw[0] = nullptr;
+  for (int nl = 1; nl <= kWvMaxLayers; nl++) {
+    g->r0ds[nl] = (const double *)put(r0[nl].data(), 8 * r0[nl].size());
+    g->win[nl] = (const double *)put(win[nl].data(), 8 * win[nl].size());
+    g->tw[nl] = (const double2 *)put(tw[nl].data(), 16 * tw[nl].size());
+  }
+  if (e != cudaSuccess) return e;
+  g->NF = h.NF;
+  g->NT = NT;
+  g->norb = norb;
+  g->kmin = h.kmin;
+  g->kmax = h.kmax;
+  g->N = h.kmax - h.kmin;
+  g->lmin = h.kmin / NT;
+  g->lmax = h.kmax / NT;
+  g->Tobs = h.Tobs;
+  g->t0 = h.t0;
+  g->wdt = h.wdt;
+  g->wdf = h.wdf;
+  g->A = h.A;
+  g->norm_sqrtNF = sqrt((double)h.NF);
+  return cudaStreamSynchronize(s);  // host vectors go out of scope
+}
+
+static size_t layers_smem(int NT) { return sizeof(double2) * (size_t)NT * (kWvMaxLayers + 1) / 2 + sizeof(double2) * NT; }
+
+cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *params, int *status,
+                               cudaStream_t s, int *nlaunch) {
+  if (n <= 0) return cudaSuccess;
+  const int norb = g.norb;
+  wv_plan_kernel<<<(n + 127) / 128, 128, 0, s>>>(g, n, params, w.src, w.ssb, status);
+  const long long nr = (long long)n * norb;
+  wv_resp_kernel<<<(unsigned)((nr + 127) / 128), 128, 0, s>>>(g, n, w.src, w.ssb, w.resp);
+  wv_tdi_kernel<<<(3 * n + 127) / 128, 128, 0, s>>>(g, n, w.src, w.resp, w.tdi);
+  const size_t sm = layers_smem(g.NT);
+  cudaError_t e = cudaFuncSetAttribute(wv_layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  wv_layers_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, w.coef);
+  if (nlaunch) *nlaunch += 4;
+  return cudaGetLastError();
+}
+
+cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *term_x, double *dlogl,
+                            double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch) {
+  if (n <= 0) return cudaSuccess;
+  wv_dlogl_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, w.coef, term_x, dlogl, term_y, hh, status);
+  if (nlaunch) *nlaunch += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t wv_export(const WvGridDev &g, const WvWorkDev &w, int n, int *info, double *xyz, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (info) wv_info_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, w.src, info);
+  if (xyz) {
+    cudaError_t e = cudaMemcpyAsync(xyz, w.coef, sizeof(double) * (size_t)n * 3 * kWvMaxLayers * g.NT,
+                                    cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace glass

@@ -1,0 +1,76 @@
+// Wavelet-domain UCB waveform and sparse-pixel likelihood on the device.
+// See ucb_wavelet.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+namespace glass {
+
+constexpr int kWvMaxOrb = 2048;  // orbit nodes (200 per year of observation)
+constexpr int kWvMaxNT = 4096;   // pixels per layer
+constexpr int kWvMaxLayers = 3;  // ucb_wavelet_layers gives 1..3 layers
+
+// Per-source plan record, written by the plan kernel.
+struct WvSrc {
+  double k[3], ep[9], ec[9];
+  double Ap, Ac, c2p, s2p;
+  double fhet;
+  int jmin, nl, jlo, c;  // first layer, layer count, first kept layer, kept layers per pixel time
+  int status, pad;
+};
+
+// Device view of one wavelet segment: grid tables and data.
+struct WvGridDev {
+  int NF, NT, norb, kmin, kmax, N;  // N = kmax - kmin pixels
+  int lmin, lmax;
+  double Tobs, t0, wdt, wdf, A, norm_sqrtNF;
+  const double *orb_t;    // [norb] orbit node times (even grid of the barycentre splines)
+  const double *tssb;     // [norb] t0 + i Tobs/(norb-1) (grid of the TDI splines)
+  const double *geo;      // [norb][21]: S/C positions / c (9), unit arms (9), arm lengths / c (3) at tssb
+  const double *fac_orb;  // [3][norb]: h, l, mu of the spline system on orb_t
+  const double *fac_ssb;  // [3][norb]: same on tssb
+  const double *r0ds[kWvMaxLayers + 1];  // [NT (nl+1)][3] S/C 1 position / c at the downsampled times
+  const double *win[kWvMaxLayers + 1];   // [NT/2 + 1] window of an (nl+1)-layer grid
+  const double2 *tw[kWvMaxLayers + 1];   // [NT (nl+1)] e^{-2 pi i k / (NT (nl+1))}
+  const double *res;      // [3][N] residual X, Y, Z
+  const double *invC;     // [9][N] inverse noise covariance, [i][j][k]
+};
+
+struct WvWorkDev {
+  int cap = 0;
+  WvSrc *src = nullptr;
+  double *ssb = nullptr;   // [cap][2][4][norb] barycentre amplitude / phase splines
+  double *resp = nullptr;  // [cap][7][norb] M (3), Mf (3), phase at S/C 1
+  double *tdi = nullptr;   // [cap][3][2][4][norb] per-channel amplitude / phase splines
+  double *coef = nullptr;  // [cap][3][kWvMaxLayers NT] coefficients, list order first
+};
+
+// Host-side grid description: orbit nodes and positions plus the WDM grid.
+struct WvGridHost {
+  double Tobs = 0, t0 = 0, wdt = 0, wdf = 0, A = 0, nx = 0;
+  int NF = 0, NT = 0, kmin = 0, kmax = 0;
+  std::vector<double> orb_t;    // orbit node times
+  std::vector<double> orb_pos;  // [(3 s + d) norb + n] metres
+};
+
+// Orbit nodes of initialize_interpolated_analytic_orbits for (Tobs, t0).
+void wv_analytic_orbit(double Tobs, double t0, std::vector<double> &t, std::vector<double> &pos);
+
+// Builds the device tables of a grid into one allocation (*mem) and fills
+// the tables part of *g (res / invC are set by wv_set_data).
+cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStream_t s);
+size_t wv_work_bytes(int cap, int norb, int NT);
+void wv_work_carve(WvWorkDev &w, void *base, int cap, int norb, int NT);
+
+// Waveform batch: plan, response, TDI splines, per-layer transforms.
+cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *params, int *status,
+                               cudaStream_t s, int *nlaunch);
+// Sparse likelihood over each source's pixels (after wv_waveform_launch).
+cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *term_x, double *dlogl,
+                            double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch);
+// Per-item layer info and values in list order: info[4 i] = first layer,
+// layer count, first kept layer, kept layers per time; xyz[(3 i + c) (kWvMaxLayers NT) + q].
+cudaError_t wv_export(const WvGridDev &g, const WvWorkDev &w, int n, int *info, double *xyz, cudaStream_t s);
+
+}  // namespace glass

@@ -240,6 +240,66 @@ int glass_gpu_wdm_forward_host(glass_gpu_ctx *ctx, int precision, int NF, int NT
 int glass_gpu_wdm_inverse_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
                                const double *wdm, double *time);
 
+/* ------------------------------------------- wavelet-domain UCB waveform */
+/*
+ * The wavelet-domain UCB waveform (ucb_waveform_wavelet,
+ * ucb/src/glass_ucb_waveform.c:1061, declared
+ * ucb/src/glass_ucb_waveform.h:231) and the sparse-pixel likelihood
+ * delta_log_likelihood (utils/src/glass_model.c:624, declared
+ * utils/src/glass_model.h) for batches of sources, in FP64.
+ *
+ * glass_gpu_wavelet_setup fixes the segment: observation Tobs from t0, a WDM
+ * grid of NF layers x NT pixels of duration wdt and bandwidth wdf (the
+ * reference's struct Wavelets fields dt, df), Meyer window (A, nx; the
+ * reference uses A = 0, nx = 6), and the data pixels [kmin, kmax) (whole
+ * layers, as the reference's kmin/kmax are).  The orbit is given as norb node
+ * times orbit_t and positions orbit_pos[(3 s + d) norb + n] in metres (the
+ * arrays struct Orbit holds, utils/src/glass_lisa.h:60-109), or, with both
+ * NULL, is initialize_interpolated_analytic_orbits (utils/src/glass_lisa.c:271).
+ * Limits: NT even, of the form 2^a 3^b, 8 <= NT <= 4096; 20 <= norb <= 2048.
+ * Host pointers; synchronous; allocates the grid tables and a work area.
+ */
+int glass_gpu_wavelet_setup(glass_gpu_ctx *ctx, double Tobs, double t0, int NF, int NT, double wdt, double wdf,
+                            double A, double nx, int kmin, int kmax, int norb, const double *orbit_t,
+                            const double *orbit_pos);
+
+/* The segment's residual X, Y, Z (N = kmax - kmin pixels each, pixel k - kmin)
+ * and inverse noise covariance invC[(3 i + j) N + k] (the reference's
+ * noise->invC[i][j][k]).  Host pointers; synchronous. */
+int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, const double *rY, const double *rZ,
+                               const double *invC);
+
+/*
+ * For each of nitems parameter vectors params[8 i ..] (the reference's UCB
+ * params array), the wavelet waveform on its pixel list and
+ *   term_y[i] = (h|h) - 2 (r|h)     (nine XYZ cross terms, as delta_log_likelihood)
+ *   hh[i]     = (h|h)               (snr_wavelet squared, utils/src/glass_math.c:428)
+ *   dlogl[i]  = -(term_y[i] - term_x[i]) / 2
+ * so that dlogl is delta_log_likelihood of replacing a source whose term is
+ * term_x[i] (NULL: 0) by this one against the residual r.  status[i]: 0, or
+ * GLASS_ITEM_NONFINITE for invalid parameters (outputs NaN), or
+ * GLASS_ITEM_OUTSIDE when no pixel of the source falls in the segment.
+ * Device pointers (any may be NULL except params); asynchronous.
+ */
+int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int nitems, const double *params, const double *term_x,
+                                  double *dlogl, double *term_y, double *hh, int *status);
+int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, const double *term_x,
+                                       double *dlogl, double *term_y, double *hh, int *status);
+
+/*
+ * The waveforms themselves: info[4 i ..] = first layer, layer count, first
+ * layer inside the segment (jlo), layers inside the segment (c; -1 for invalid
+ * parameters); xyz[(3 i + ch) 3 NT + q] = channel ch (X, Y, Z) at list entry q
+ * < NT c, whose pixel is k - kmin = q / c + (jlo + q % c) NT - kmin.  This is
+ * ucb_waveform_wavelet's wavelet_list / X[list[q]] output in compact form
+ * (including its rule that the q-th listed pixel takes the q-th coefficient
+ * of the per-layer transform).  Device pointers; asynchronous.
+ */
+int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int nitems, const double *params, int *info, double *xyz,
+                                     int *status);
+int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, int *info,
+                                          double *xyz, int *status);
+
 /* ---------------------------------------------------------- diagnostics */
 /* Measured fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) of the
  * device's FP32 (fp64 == 0) or FP64 pipe: the peak that the CUDA-core-bound

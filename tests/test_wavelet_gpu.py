@@ -1,0 +1,144 @@
+"""Parity of the CUDA wavelet-domain UCB waveform and sparse-pixel likelihood
+with the reference (golden vectors) and the oracle, through the C ABI.
+
+FP64 tolerances: waveform values within 1e-10 of the channel's largest value
+(they agree to the FFTs' rounding, ~1e-14), pixel lists identical; delta logL
+within 1e-10 relative to max(1, |delta logL|).
+"""
+import numpy as np
+import pytest
+
+import glass_gb300 as gg
+from glass_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+REL = 1e-10
+GRIDS = {"nf1024": (1024, 2048, 15.0 * 1024, 2.0**21 * 15.0), "nf1536": (1536, 4096, 7680.0, 4096 * 7680.0)}
+SMALL = (64, 256, 15.0 * 64, 2.0**14 * 15.0)  # NF, NT, pixel duration, Tobs
+
+
+@pytest.fixture(scope="module")
+def engine():
+    from glass_gb300 import build
+
+    build.build()
+    eng = gg.Engine(0)
+    yield eng
+    eng.close()
+
+
+def setup_grid(engine, grid, t0, kmin, kmax):
+    NF, NT, wdt, Tobs = grid
+    engine.wavelet_setup(Tobs, t0, NF, NT, wdt, 1 / (2 * wdt), kmin, kmax)
+
+
+def compact(engine, info, xyz):
+    lst = engine.wavelet_list(info)
+    return lst, xyz[:, : len(lst)]
+
+
+def test_waveform_matches_reference(engine, golden):
+    g = golden("wavelet_waveform.npz")
+    for i in range(len(g["grid"])):
+        grid = GRIDS[str(g["grid"][i])]
+        setup_grid(engine, grid, float(g["t0"][i]), int(g["kmin"][i]), int(g["kmax"][i]))
+        info, xyz, st = engine.wavelet_waveform_host(g["params"][i][None])
+        assert st[0] == 0
+        lst, vals = compact(engine, info[0], xyz[0])
+        np.testing.assert_array_equal(lst, g[f"list{i}"])
+        ref = g[f"xyz{i}"]
+        for c in range(3):
+            err = np.abs(vals[c] - ref[c]).max() / np.abs(ref[c]).max()
+            assert err < REL, (i, c, err)
+
+
+def test_sparse_likelihood_matches_reference(engine, golden):
+    """delta_log_likelihood(model with the injection -> model with each proposal)
+    and snr_wavelet, on the data of the golden segment."""
+    g = golden("wavelet_likelihood.npz")
+    NF, NT, wdt, Tobs = GRIDS[str(g["grid"])]
+    for c in range(int(g["ncase"])):
+        kmin, kmax = int(g[f"c{c}_kmin"]), int(g[f"c{c}_kmax"])
+        setup_grid(engine, (NF, NT, wdt, Tobs), 0.0, kmin, kmax)
+        invC = wl.wavelet_invC(kmax - kmin, NT, kmin, float(g[f"c{c}_scale"]))
+        engine.wavelet_set_data(g[f"c{c}_d"], invC)
+        _, tx, _, st = engine.wavelet_dlogl_host(g[f"c{c}_inj"][None])
+        assert st[0] == 0
+        props = g[f"c{c}_props"]
+        dl, ty, hh, st = engine.wavelet_dlogl_host(props, term_x=np.full(len(props), tx[0]))
+        assert (st == 0).all()
+        ref = g[f"c{c}_dlogl"]
+        err = np.abs(dl - ref) / np.maximum(1.0, np.abs(ref))
+        assert err.max() < REL, err
+        np.testing.assert_allclose(np.sqrt(hh), g[f"c{c}_snr"], rtol=REL)
+
+
+def test_batch_matches_oracle_small_grid(engine, port):
+    """Many sources at once (different layer counts, segments that cut the
+    signal, t0 != 0) on a small grid, against the oracle."""
+    NF, NT, wdt, Tobs = SMALL
+    wdf = 1 / (2 * wdt)
+    rng = np.random.default_rng(21)
+    for t0 in (0.0, 3.3e4):
+        lmin, lmax = 10, 40
+        kmin, kmax = lmin * NT, lmax * NT
+        engine.wavelet_setup(Tobs, t0, NF, NT, wdt, wdf, kmin, kmax)
+        n = 40
+        f0 = rng.uniform((lmin - 1) * wdf, (lmax + 1) * wdf, n)
+        params = np.array([wl.draw_source(rng, f, 10 ** rng.uniform(-22, -21), 10 ** rng.uniform(-15, -13), Tobs)
+                           for f in f0])
+        params[::7, 7] *= -1  # frequency decreasing
+        info, xyz, st = engine.wavelet_waveform_host(params)
+        assert (st == 0).all()
+        for i in range(n):
+            lst_o, xyz_o, j, nl = port.wavelet_waveform(params[i], Tobs, t0, NF, NT, wdt, wdf, kmin, kmax)
+            assert (info[i, 0], info[i, 1]) == (j, nl)
+            lst, vals = compact(engine, info[i], xyz[i])
+            np.testing.assert_array_equal(lst, lst_o)
+            if len(lst):
+                ref = xyz_o[:, lst]
+                assert np.abs(vals - ref).max() <= REL * np.abs(ref).max(), i
+
+
+def test_dlogl_matches_oracle_and_edge_cases(engine, port):
+    NF, NT, wdt, Tobs = SMALL
+    wdf = 1 / (2 * wdt)
+    kmin, kmax = 10 * NT, 40 * NT
+    N = kmax - kmin
+    engine.wavelet_setup(Tobs, 0.0, NF, NT, wdt, wdf, kmin, kmax)
+    rng = np.random.default_rng(5)
+    invC = wl.wavelet_invC(N, NT, kmin, 1e-22)
+    d = rng.standard_normal((3, N)) * 1e-22
+    engine.wavelet_set_data(d, invC)
+    f0 = rng.uniform(9 * wdf, 41 * wdf, 30)
+    params = np.array([wl.draw_source(rng, f, 10 ** rng.uniform(-22, -21), 1e-14, Tobs) for f in f0])
+    params[3, 1] = 1.5  # invalid cos(theta)
+    params[4, 0] = np.nan
+    params[5, 0] = 2 * wdf * Tobs  # far below the segment
+    dl, ty, hh, st = engine.wavelet_dlogl_host(params)
+    assert st[3] == 1 and st[4] == 1 and np.isnan(dl[3]) and np.isnan(dl[4])
+    assert st[5] == 4 and ty[5] == 0.0
+    for i in np.where(st == 0)[0]:
+        lst, h, _, _ = port.wavelet_waveform(params[i], Tobs, 0.0, NF, NT, wdt, wdf, kmin, kmax)
+        dh, hh_o = port.wavelet_dh_hh(d, h, invC, lst)
+        term = hh_o - 2 * dh
+        assert abs(ty[i] - term) <= REL * max(1.0, abs(term)), i
+        assert abs(hh[i] - hh_o) <= REL * hh_o
+
+
+def test_given_orbit_arrays_are_used(engine, port):
+    """Orbit node arrays passed by the caller (struct Orbit's t, x, y, z) give
+    the same waveform as the built-in interpolated analytic orbit when they hold
+    the same nodes."""
+    NF, NT, wdt, Tobs = SMALL
+    wdf = 1 / (2 * wdt)
+    kmin, kmax = 10 * NT, 40 * NT
+    t, pos = port.orbit_grid(Tobs, 0.0)
+    rng = np.random.default_rng(9)
+    p = wl.draw_source(rng, 20 * wdf, 1e-21, 1e-14, Tobs)
+    engine.wavelet_setup(Tobs, 0.0, NF, NT, wdt, wdf, kmin, kmax)
+    a = engine.wavelet_waveform_host(p[None])
+    engine.wavelet_setup(Tobs, 0.0, NF, NT, wdt, wdf, kmin, kmax, orbit=(t, pos))
+    b = engine.wavelet_waveform_host(p[None])
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
