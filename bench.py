@@ -309,6 +309,209 @@ def bench_grad_fisher(gg, torch, dev, rank, steps, warmup):
             "cost_ratio": times["grad"] / times["dlogl"], "ok_items": int((st == 0).sum())}
 
 
+WDM_NF, WDM_NT, WDM_NX = 1024, 2048, 4.0  # 2^21 samples of 15 s: a year in 1024 layers x 2048 pixels
+
+
+def wdm_series(gg, rng, n_ucb=100):
+    """2^21 samples at 15 s: Gaussian noise coloured by the A-channel PSD
+    (AEnoise_FF, scirdv1) drawn in the real-FFT domain, plus n_ucb UCB
+    templates (parameters as in the batched configuration) added in the same
+    domain, then an inverse real FFT."""
+    ND = WDM_NF * WDM_NT
+    f = np.arange(ND // 2 + 1) / T
+    S = wl.aenoise_ff(np.maximum(f, f[1]))
+    X = (rng.standard_normal(f.size) + 1j * rng.standard_normal(f.size)) * np.sqrt(S * T / 4)
+    for _ in range(n_ucb):
+        p = wl.draw_source(rng, 10 ** rng.uniform(np.log10(0.5e-3), np.log10(15e-3)),
+                           10 ** rng.uniform(-23, -21), 1e-17)
+        N = 256
+        h = gg.ucb_waveform(p, N, T)[3]
+        q0 = int(p[0]) - N // 2
+        X[q0:q0 + N] += (h[0::2] + 1j * h[1::2]) * math.sqrt(T)
+    X[0] = X[0].real
+    X[-1] = X[-1].real
+    return np.fft.irfft(X, ND) * (ND / T)
+
+
+def bench_wdm(gg, torch, dev, rank, steps, warmup, cpu, peaks):
+    """Forward + inverse WDM of 2^21 FP64 samples (1024 layers x 2048 pixels,
+    window exponent 4), in FP64 and in FP32 arithmetic."""
+    rng = np.random.default_rng(3 + 1000 * rank)
+    NF, NT, ND = WDM_NF, WDM_NT, WDM_NF * WDM_NT
+    x = wdm_series(gg, rng)
+    eng = gg.Engine(dev.index or 0)
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    d_x = torch.from_numpy(x).to(dev)
+    d_w = torch.empty_like(d_x)
+    d_b = torch.empty_like(d_x)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    out = {"workload": "wdm_roundtrip_2^21_fp64_nf1024_nt2048_nx4",
+           "input": "A-channel coloured noise + 100 UCBs (synthetic)", "l2": "flushed (256 MB write) between steps"}
+    for prec, name in ((gg.PREC_FP64, "fp64"), (gg.PREC_MIXED, "fp32")):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                eng.wdm_forward_device(NF, NT, d_x, d_w, precision=prec, nx=WDM_NX)
+                eng.wdm_inverse_device(NF, NT, d_w, d_b, precision=prec, nx=WDM_NX)
+            stream.synchronize()
+            ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+            for k in range(steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                eng.wdm_forward_device(NF, NT, d_x, d_w, precision=prec, nx=WDM_NX)
+                ev[k][1].record(stream)
+                eng.wdm_inverse_device(NF, NT, d_w, d_b, precision=prec, nx=WDM_NX)
+                ev[k][2].record(stream)
+            stream.synchronize()
+        t_f = sum(e[0].elapsed_time(e[1]) for e in ev) / steps / 1e3
+        t_i = sum(e[1].elapsed_time(e[2]) for e in ev) / steps / 1e3
+        back = d_b.cpu().numpy()
+        algo_bytes = 16.0 * ND  # read + write of the FP64 series
+        flops = 2.5 * ND * math.log2(ND) + (NF + 1) * 5.0 * NT * math.log2(NT) + 4.0 * ND
+        out[name] = {"ms_forward": 1e3 * t_f, "ms_inverse": 1e3 * t_i,
+                     "transforms_per_s": 2.0 / (t_f + t_i), "samples_per_s": 2.0 * ND / (t_f + t_i),
+                     "round_trip_max_err_rel": float(np.abs(back - x).max() / np.abs(x).max()),
+                     "roofline": {"bound": "hbm", "achieved": algo_bytes / t_f / 1e9, "peak": peaks["hbm_gbs"],
+                                  "unit": "GB/s", "frac": algo_bytes / t_f / 1e9 / peaks["hbm_gbs"],
+                                  "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+                                  "algorithmic_bytes": algo_bytes, "kernel": "forward transform (3 launches)",
+                                  "traffic": None,
+                                  "flops": flops, "fp64_tflops": flops / t_f / 1e12}}
+    # end to end with host arrays (copies in and out inside the timed region)
+    eng.set_stream(None)
+    for _ in range(warmup):
+        eng.wdm_inverse_host(NF, NT, eng.wdm_forward_host(NF, NT, x, nx=WDM_NX), nx=WDM_NX)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        eng.wdm_inverse_host(NF, NT, eng.wdm_forward_host(NF, NT, x, nx=WDM_NX), nx=WDM_NX)
+    t_e2e = (time.perf_counter() - t0) / steps
+    out["e2e"] = {"value": 2.0 / t_e2e, "unit": "transforms/s", "h2d_bytes_per_step": 2 * 8 * ND,
+                  "d2h_bytes_per_step": 2 * 8 * ND}
+    eng.close()
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import Port, build_port
+
+        build_port()
+        port = Port()
+        win = port.wdm_window(NF, NT, 0.0, WDM_NX)
+        t0 = time.perf_counter()
+        y = port.wdm_forward(NF, NT, win, x)
+        port.wdm_inverse(NF, NT, win, y)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 2.0 / el, "unit": "transforms/s", "cores": 1, "kind": "port",
+                               "sample": "one forward + one inverse of the same 2^21-sample series, 1 thread "
+                                         "(the reference's transform is single-threaded)"}
+    return out
+
+
+WV_NF, WV_NT, WV_LMIN, WV_LMAX, WV_NSRC = 1024, 2048, 10, 470, 4096
+
+
+def wv_flops(nl, c, norb):
+    """Algorithmic flops of one wavelet waveform + sparse delta logL (all FP64
+    here): 40 Norb + 10 N_ds + 900 Norb + 75 N_ds + 3 (2.5 N_ds log2 N_ds +
+    nl 5 NT log2 NT) + 54 Npix, with N_ds = NT (nl + 1), Npix = NT c."""
+    nds = WV_NT * (nl + 1)
+    return (40.0 * norb + 10.0 * nds + 900.0 * norb + 75.0 * nds
+            + 3.0 * (2.5 * nds * math.log2(nds) + nl * 5.0 * WV_NT * math.log2(WV_NT)) + 54.0 * WV_NT * c)
+
+
+def bench_wavelet(gg, torch, dev, rank, steps, warmup, cpu, peak64):
+    """Wavelet-domain UCB waveform + sparse-pixel delta logL for 4096 sources
+    on a 1024 x 2048 grid (layers 10..469 of a year at 15 s), FP64."""
+    rng = np.random.default_rng(4 + 1000 * rank)
+    NF, NT = WV_NF, WV_NT
+    wdt = 15.0 * NF
+    wdf = 1.0 / (2 * wdt)
+    kmin, kmax = WV_LMIN * NT, WV_LMAX * NT
+    N = kmax - kmin
+    eng = gg.Engine(dev.index or 0)
+    eng.wavelet_setup(T, 0.0, NF, NT, wdt, wdf, kmin, kmax, nx=WDM_NX)
+
+    def draw(n):
+        return np.array([wl.draw_source(rng, 10 ** rng.uniform(np.log10(0.5e-3), np.log10(15e-3)),
+                                        10 ** rng.uniform(-23, -21), 1e-17) for _ in range(n)])
+
+    src = draw(WV_NSRC)
+    # data: white noise of the segment's covariance plus 100 injected sources
+    scale = 1e-23
+    invC = wl.wavelet_invC(N, NT, kmin, scale)
+    data = rng.standard_normal((3, N)) * scale
+    info, xyz, st = eng.wavelet_waveform_host(src[:100])
+    for i in range(100):
+        if st[i] == 0:
+            lst = eng.wavelet_list(info[i])
+            data[:, lst] += xyz[i][:, : len(lst)]
+    eng.wavelet_set_data(data, invC)
+    _, tx, hh, _ = eng.wavelet_dlogl_host(src)
+    snr = np.sqrt(np.maximum(hh, 1.0))
+    props = np.array([wl.gaussian_jumps(rng, src[i], wl.jump_scales(src[i], max(snr[i], 5.0)), 1)[0]
+                      for i in range(WV_NSRC)])
+    info, _, _ = eng.wavelet_waveform_host(props, values=False)
+    norb = int(200 * T / 3.15581497632e7)
+    flops = sum(wv_flops(int(r[1]), max(int(r[3]), 0), norb) for r in info if r[3] >= 0)
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    d_p = torch.from_numpy(props).to(dev)
+    d_tx = torch.from_numpy(tx).to(dev)
+    d_dl = torch.empty(WV_NSRC, dtype=torch.float64, device=dev)
+    d_ty = torch.empty_like(d_dl)
+    d_hh = torch.empty_like(d_dl)
+    d_st = torch.empty(WV_NSRC, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            eng.wavelet_dlogl_device(d_p, d_dl, d_ty, d_hh, d_st, term_x=d_tx)
+        stream.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            eng.wavelet_dlogl_device(d_p, d_dl, d_ty, d_hh, d_st, term_x=d_tx)
+            ev[k][1].record(stream)
+        stream.synchronize()
+    launches = eng.last_launch_count()
+    t = sum(a.elapsed_time(b) for a, b in ev) / steps / 1e3
+    stt = d_st.cpu().numpy()
+    eng.set_stream(None)
+    for _ in range(warmup):
+        eng.wavelet_dlogl_host(props, tx)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        eng.wavelet_dlogl_host(props, tx)
+    t_e2e = (time.perf_counter() - t0) / steps
+    out = {"workload": f"ucb_waveform_wavelet + sparse dlogL, {WV_NSRC} sources, NF={NF} NT={NT}, "
+                       f"layers {WV_LMIN}..{WV_LMAX - 1}, f0 log-U[0.5,15] mHz, FP64",
+           "sources_per_s": WV_NSRC / t, "ms_per_batch": 1e3 * t, "ok_items": int((stt == 0).sum()),
+           "outside_items": int((stt == 4).sum()), "launches_per_batch": launches,
+           "roofline": {"bound": "fp64", "achieved": flops / t / 1e12, "peak": peak64, "unit": "TFLOP/s",
+                        "frac": flops / t / 1e12 / peak64, "flops_per_batch": flops,
+                        "peak_source": "FP64 FMA probe kernel measured in this run", "traffic": None},
+           "e2e": {"value": WV_NSRC / t_e2e, "unit": "sources/s", "h2d_bytes_per_step": WV_NSRC * 9 * 8,
+                   "d2h_bytes_per_step": WV_NSRC * (3 * 8 + 4)}}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import Port, build_port
+
+        build_port()
+        port = Port()
+        done, t0 = 0, time.perf_counter()
+        while True:
+            p = props[done % WV_NSRC]
+            lst, h, _, _ = port.wavelet_waveform(p, T, 0.0, NF, NT, wdt, wdf, kmin, kmax, nx=WDM_NX)
+            port.wavelet_dh_hh(data, h, invC, lst)
+            done += 1
+            el = time.perf_counter() - t0
+            if el > 5.0 or done >= 2000:
+                break
+        out["cpu_baseline"] = {"value": done / el, "unit": "sources/s", "cores": 1, "kind": "port",
+                               "sample": f"{done} sources of the same batch, 1 thread (the reference runs one "
+                                         f"source per call in a chain's thread)"}
+    eng.close()
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -434,6 +637,16 @@ def run_ours(args):
     ach_fp64 = flops_step / (t_fp64 / args.steps) / 1e12
 
     grad_line = bench_grad_fisher(gg, torch, dev, rank, max(5, args.steps // 20), args.warmup)
+    peaks = {"hbm_gbs": 6799.3}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks.update(json.load(fh))
+    except OSError:
+        pass
+    cpu_legs = world == 1 and not args.no_cpu_baseline
+    wdm_line = bench_wdm(gg, torch, dev, rank, max(5, args.steps // 20), args.warmup, cpu_legs and rank == 0, peaks)
+    wv_line = bench_wavelet(gg, torch, dev, rank, max(5, args.steps // 30), args.warmup, cpu_legs and rank == 0,
+                            peak64)
 
     if rank == 0:
         line = {
@@ -465,6 +678,8 @@ def run_ours(args):
                          "fp64_path": {"achieved": ach_fp64, "peak_fp64": peak64,
                                        "frac_of_fp64_peak": ach_fp64 / peak64}},
             "grad_fisher": grad_line,
+            "wdm": wdm_line,
+            "wavelet": wv_line,
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk,
         }

@@ -39,6 +39,9 @@ EXPORTS = (
     "glass_gpu_wdm_forward_host", "glass_gpu_wdm_inverse_host",
     "glass_gpu_wavelet_setup", "glass_gpu_wavelet_set_data", "glass_gpu_wavelet_dlogl_batch",
     "glass_gpu_wavelet_dlogl_batch_host", "glass_gpu_wavelet_waveform_batch", "glass_gpu_wavelet_waveform_batch_host",
+    "glass_gpu_wdm_to_freq", "glass_gpu_wdm_from_freq", "build_wdm_filter_freq", "wavelet_transform_timefreq",
+    "wavelet_transform_freq", "wavelet_transform_inverse_freq", "ucb_waveform_wavelet", "ucb_waveform_wavelet_tab",
+    "ucb_waveform_wavelet_slow", "glass_ucb_waveform_wavelet_tab", "glass_ucb_waveform_wavelet_slow",
 )
 
 _lib = None
@@ -82,6 +85,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_wdm_inverse.argtypes = wdm_args + [_V, _V]
     lib.glass_gpu_wdm_forward_host.argtypes = wdm_args + [_D, _D]
     lib.glass_gpu_wdm_inverse_host.argtypes = wdm_args + [_D, _D]
+    lib.glass_gpu_wdm_to_freq.argtypes = wdm_args + [_V, _V]
+    lib.glass_gpu_wdm_from_freq.argtypes = wdm_args + [_V, _V]
+    lib.glass_ucb_waveform_wavelet_tab.argtypes = []
+    lib.glass_ucb_waveform_wavelet_slow.argtypes = []
     lib.glass_gpu_wavelet_setup.argtypes = [_V, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
@@ -295,16 +302,18 @@ class Engine:
         ic = np.ascontiguousarray(invC, np.float64)
         _check(self.lib.glass_gpu_wavelet_set_data(self._ctx, _pd(r[0]), _pd(r[1]), _pd(r[2]), _pd(ic)))
 
-    def wavelet_waveform_host(self, params):
+    def wavelet_waveform_host(self, params, values=True):
         """(info [n, 4] = first layer, layers, first kept layer, kept layers
-        (-1 when the parameters are invalid), xyz [n, 3, 3 NT], status [n])."""
+        (-1 when the parameters are invalid), xyz [n, 3, 3 NT] or None when
+        values is False, status [n])."""
         p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
         n = len(p)
         NT = self.wv["NT"]
         info = np.zeros((n, 4), np.int32)
-        xyz = np.zeros((n, 3, self.WV_MAX_LAYERS * NT))
+        xyz = np.zeros((n, 3, self.WV_MAX_LAYERS * NT)) if values else None
         st = np.zeros(n, np.int32)
-        _check(self.lib.glass_gpu_wavelet_waveform_batch_host(self._ctx, n, _pd(p), _pi(info), _pd(xyz), _pi(st)))
+        _check(self.lib.glass_gpu_wavelet_waveform_batch_host(self._ctx, n, _pd(p), _pi(info),
+                                                              _pd(xyz) if values else None, _pi(st)))
         return info, xyz, st
 
     def wavelet_list(self, info_row):

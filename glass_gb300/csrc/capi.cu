@@ -694,6 +694,26 @@ extern "C" int glass_gpu_wdm_inverse(glass_gpu_ctx *ctx, int precision, int NF, 
   return GLASS_OK;
 }
 
+extern "C" int glass_gpu_wdm_to_freq(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                                     const double *wdm, double *freq) {
+  if (!ctx || !wdm || !freq) return set_err(GLASS_ERR_ARG, "glass_gpu_wdm_to_freq: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = wdm_plan_for(ctx, precision, NF, NT, A, nx))) return rc;
+  GLASS_CUDA(wdm_to_freq(ctx->wdm, wdm, freq, ctx->stream), "glass_gpu_wdm_to_freq");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wdm_from_freq(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                                       const double *freq, double *wdm) {
+  if (!ctx || !wdm || !freq) return set_err(GLASS_ERR_ARG, "glass_gpu_wdm_from_freq: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = wdm_plan_for(ctx, precision, NF, NT, A, nx))) return rc;
+  GLASS_CUDA(wdm_from_freq(ctx->wdm, freq, wdm, ctx->stream), "glass_gpu_wdm_from_freq");
+  return GLASS_OK;
+}
+
 static int wdm_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx, const double *in,
                     double *out, bool forward) {
   if (!ctx || !in || !out) return set_err(GLASS_ERR_ARG, "glass_gpu_wdm_*_host: null argument");
@@ -885,10 +905,11 @@ extern "C" int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nit
   const size_t per = (size_t)3 * kWvMaxLayers * ctx->wv.NT;
   for (int off = 0; off < nitems; off += kWvChunk) {
     const size_t n = (size_t)std::min(kWvChunk, nitems - off);
-    const size_t bytes = sizeof(double) * n * (8 + per) + sizeof(int) * n * 5 + 256;
+    const size_t nx = xyz ? per * n : 0;
+    const size_t bytes = sizeof(double) * (8 * n + nx) + sizeof(int) * n * 5 + 256;
     if ((rc = ensure_stage(ctx, bytes))) return rc;
-    double *dp = (double *)ctx->d_stage, *dx = dp + 8 * n;
-    int *dinfo = (int *)(dx + per * n), *dst = dinfo + 4 * n;
+    double *dp = (double *)ctx->d_stage, *dx = xyz ? dp + 8 * n : nullptr;
+    int *dinfo = (int *)(dp + 8 * n + nx), *dst = dinfo + 4 * n;
     GLASS_CUDA(cudaMemcpyAsync(dp, params + 8 * (size_t)off, sizeof(double) * 8 * n, cudaMemcpyHostToDevice,
                                ctx->stream),
                "upload params");
@@ -905,4 +926,210 @@ extern "C" int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nit
     GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "wavelet waveform sync");
   }
   return GLASS_OK;
+}
+
+// ------------------------------------------------------------ drop-ins for the wavelet headers
+// The reference's struct Wavelets (utils/src/glass_wavelet.h:25-75), restated
+// field for field so that the drop-in entry points can read the grid from a
+// caller's struct: the field order and types are the interface.
+struct WaveletsLayout {
+  int NF, NT;
+  double cadence, dt, df;
+  int frequency_steps, fdot_steps;
+  double d_fdot;
+  int oversample;
+  double Omega, dOmega, domega, inv_root_dOmega, B, A, BW, deltaf;
+  double *fdot, *window, *window_freq_forward;
+  double norm;
+  int N;
+  double T;
+  int kmin, kmax, imin, imax;
+  int *n_table;
+  double **table;
+};
+
+static constexpr double kWaveletFilterConstant = 6.0;  // WAVELET_FILTER_CONSTANT, utils/src/glass_wavelet.h:21
+
+// One context per host thread for the drop-in entry points (the reference's
+// callers run one chain per OpenMP thread).
+struct DropInThread {
+  glass_gpu_ctx *ctx = nullptr;
+  void *d_buf = nullptr;
+  size_t d_cap = 0;
+  // wavelet waveform grid cache key
+  double key[14] = {0};
+  bool wv_ready = false;
+  std::vector<int> info;
+  std::vector<double> xyz;
+  ~DropInThread() {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaFree(d_buf);
+    glass_gpu_destroy(ctx);
+  }
+};
+static thread_local DropInThread g_dropin;
+
+[[noreturn]] static void dropin_fail(const char *who) {
+  fprintf(stderr, "%s: %s\n", who, glass_gpu_last_error());
+  exit(1);
+}
+
+static glass_gpu_ctx *dropin_ctx(const char *who) {
+  DropInThread &D = g_dropin;
+  if (!D.ctx) {
+    const char *dev = getenv("GLASS_GPU_DEVICE");
+    if (glass_gpu_create(dev ? atoi(dev) : 0, &D.ctx) != GLASS_OK) dropin_fail(who);
+  }
+  return D.ctx;
+}
+
+static double *dropin_buf(size_t doubles, const char *who) {
+  DropInThread &D = g_dropin;
+  const size_t bytes = sizeof(double) * doubles;
+  if (bytes > D.d_cap) {
+    cudaFree(D.d_buf);
+    D.d_buf = nullptr;
+    D.d_cap = 0;
+    cudaError_t e = cudaMalloc(&D.d_buf, bytes);
+    if (e != cudaSuccess) {
+      cuda_err(e, "cudaMalloc(drop-in buffer)");
+      dropin_fail(who);
+    }
+    D.d_cap = bytes;
+  }
+  return (double *)D.d_buf;
+}
+
+// build_wdm_filter_freq (utils/src/glass_wavelet.c:327)
+extern "C" void build_wdm_filter_freq(double *phif, int Nf, int Nt, double A, bool forward) {
+  if (glass_wdm_window(Nf, Nt, A, kWaveletFilterConstant, forward ? 1 : 0, phif) != GLASS_OK)
+    dropin_fail("build_wdm_filter_freq");
+}
+
+// wavelet_transform_timefreq (utils/src/glass_wavelet.c:293): in place, FP64
+extern "C" void wavelet_transform_timefreq(struct Wavelets *wdm, double *timedata) {
+  const WaveletsLayout *w = reinterpret_cast<const WaveletsLayout *>(wdm);
+  glass_gpu_ctx *ctx = dropin_ctx("wavelet_transform_timefreq");
+  if (glass_gpu_wdm_forward_host(ctx, GLASS_PREC_FP64, w->NF, w->NT, w->A, kWaveletFilterConstant, timedata,
+                                 timedata) != GLASS_OK)
+    dropin_fail("wavelet_transform_timefreq");
+}
+
+static void dropin_freq(struct Wavelets *wdm, const double *in, double *out, bool to_freq, const char *who) {
+  const WaveletsLayout *w = reinterpret_cast<const WaveletsLayout *>(wdm);
+  glass_gpu_ctx *ctx = dropin_ctx(who);
+  const size_t ND = (size_t)w->NF * w->NT;
+  double *d = dropin_buf(2 * ND + 2, who);
+  double *d_wdm = d, *d_freq = d + ND;
+  const size_t nin = to_freq ? ND : ND + 2, nout = to_freq ? ND + 2 : ND;
+  double *d_in = to_freq ? d_wdm : d_freq, *d_out = to_freq ? d_freq : d_wdm;
+  cudaError_t e = cudaMemcpyAsync(d_in, in, sizeof(double) * nin, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) {
+    cuda_err(e, who);
+    dropin_fail(who);
+  }
+  int rc = to_freq ? glass_gpu_wdm_to_freq(ctx, GLASS_PREC_FP64, w->NF, w->NT, w->A, kWaveletFilterConstant, d_in, d_out)
+                   : glass_gpu_wdm_from_freq(ctx, GLASS_PREC_FP64, w->NF, w->NT, w->A, kWaveletFilterConstant, d_in,
+                                             d_out);
+  if (rc != GLASS_OK) dropin_fail(who);
+  e = cudaMemcpyAsync(out, d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cuda_err(e, who);
+    dropin_fail(who);
+  }
+}
+
+// wavelet_transform_freq (utils/src/glass_wavelet.c:410): ND/2+1 bins -> wdm
+extern "C" void wavelet_transform_freq(struct Wavelets *wdm, double *freqdata, double *wdmdata) {
+  dropin_freq(wdm, freqdata, wdmdata, false, "wavelet_transform_freq");
+}
+
+// wavelet_transform_inverse_freq (utils/src/glass_wavelet.c:351): wdm -> ND/2+1 bins
+extern "C" void wavelet_transform_inverse_freq(struct Wavelets *wdm, double *wdmdata, double *freqdata) {
+  dropin_freq(wdm, wdmdata, freqdata, true, "wavelet_transform_inverse_freq");
+}
+
+// ucb_waveform_wavelet (ucb/src/glass_ucb_waveform.c:1061): one source, host
+// arrays; the orbit nodes are read from the caller's struct Orbit (t, x, y, z).
+extern "C" void ucb_waveform_wavelet(struct Orbit *orbit, struct Wavelets *wdm, double Tobs, double t0,
+                                     double *params, int *wavelet_list, int *Nwavelet, double *X, double *Y,
+                                     double *Z) {
+  static const char *who = "ucb_waveform_wavelet";
+  const WaveletsLayout *w = reinterpret_cast<const WaveletsLayout *>(wdm);
+  const OrbitLayout *o = reinterpret_cast<const OrbitLayout *>(orbit);
+  DropInThread &D = g_dropin;
+  glass_gpu_ctx *ctx = dropin_ctx(who);
+  const int norb = o->Norb;
+  const double key[14] = {Tobs, t0, (double)w->NF, (double)w->NT, w->dt, w->df, w->A, (double)w->kmin,
+                          (double)w->kmax, (double)norb, (double)(uintptr_t)o->t, norb > 0 ? o->t[0] : 0.0,
+                          norb > 0 ? o->t[norb - 1] : 0.0, norb > 0 ? o->x[0][norb - 1] : 0.0};
+  if (!D.wv_ready || memcmp(key, D.key, sizeof(key)) != 0) {
+    if (norb < 20 || norb > kWvMaxOrb) {
+      set_err(GLASS_ERR_ARG, "ucb_waveform_wavelet: orbit needs 20..2048 nodes");
+      dropin_fail(who);
+    }
+    std::vector<double> pos((size_t)9 * norb);
+    for (int sc = 0; sc < 3; sc++)
+      for (int n = 0; n < norb; n++) {
+        pos[(size_t)(3 * sc + 0) * norb + n] = o->x[sc][n];
+        pos[(size_t)(3 * sc + 1) * norb + n] = o->y[sc][n];
+        pos[(size_t)(3 * sc + 2) * norb + n] = o->z[sc][n];
+      }
+    if (glass_gpu_wavelet_setup(ctx, Tobs, t0, w->NF, w->NT, w->dt, w->df, w->A, kWaveletFilterConstant, w->kmin,
+                                w->kmax, norb, o->t, pos.data()) != GLASS_OK)
+      dropin_fail(who);
+    memcpy(D.key, key, sizeof(key));
+    D.wv_ready = true;
+  }
+  const int NT = w->NT;
+  const size_t per = (size_t)3 * kWvMaxLayers * NT;
+  D.info.resize(4);
+  D.xyz.resize(per);
+  int st = 0;
+  if (glass_gpu_wavelet_waveform_batch_host(ctx, 1, params, D.info.data(), D.xyz.data(), &st) != GLASS_OK)
+    dropin_fail(who);
+  const int jlo = D.info[2], c = D.info[3];
+  if (st != 0 || c < 0) {
+    set_err(GLASS_ERR_ARG, "ucb_waveform_wavelet: invalid source parameters");
+    dropin_fail(who);
+  }
+  const int n = NT * c;
+  const double *hx = D.xyz.data(), *hy = hx + kWvMaxLayers * NT, *hz = hy + kWvMaxLayers * NT;
+  for (int q = 0; q < n; q++) {
+    const int k = q / c + (jlo + q % c) * NT - w->kmin;
+    wavelet_list[q] = k;
+    X[k] = hx[q];
+    Y[k] = hy[q];
+    Z[k] = hz[q];
+  }
+  *Nwavelet = n;
+}
+
+// Status-returning forms of the two reference variants that are not built here.
+extern "C" int glass_ucb_waveform_wavelet_tab(void) {
+  return set_err(GLASS_ERR_STATE,
+                 "ucb_waveform_wavelet_tab: not implemented (the reference's lookup-table variant exits as not "
+                 "implemented too); use ucb_waveform_wavelet");
+}
+
+extern "C" int glass_ucb_waveform_wavelet_slow(void) {
+  return set_err(GLASS_ERR_STATE,
+                 "ucb_waveform_wavelet_slow: not built (a debugging variant that writes files); use "
+                 "ucb_waveform_wavelet");
+}
+
+// ucb/src/glass_ucb_waveform.c:1480 and :1243: report and exit, as the
+// reference's lookup-table variant does
+extern "C" void ucb_waveform_wavelet_tab(struct Orbit *, struct Wavelets *, double, double, double *, int *, int *,
+                                         double *, double *, double *) {
+  glass_ucb_waveform_wavelet_tab();
+  dropin_fail("ucb_waveform_wavelet_tab");
+}
+
+extern "C" void ucb_waveform_wavelet_slow(struct Orbit *, struct Wavelets *, double, double, double *, int *, int *,
+                                          double *, double *, double *) {
+  glass_ucb_waveform_wavelet_slow();
+  dropin_fail("ucb_waveform_wavelet_slow");
 }

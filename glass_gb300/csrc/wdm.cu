@@ -227,10 +227,11 @@ __device__ __forceinline__ C real_bin(const C *Z, long long M, long long k, cons
   return mk<C>((R)0.5 * (s.x + ed.y), (R)0.5 * (s.y - ed.x));
 }
 
-// Forward layers: one CTA per layer m in [0, NF].
+// Forward layers: one CTA per layer m in [0, NF].  The spectrum is either X
+// (bins 0..M given) or unpacked on the fly from Z, the FFT of the packed samples.
 template <typename C>
-__global__ void wdm_fwd_layer_kernel(const C *Z, long long M, int NF, int NT, const decltype(C().x) *phif,
-                                     const C *twNT, const C *tlo, const C *thi, int K,
+__global__ void wdm_fwd_layer_kernel(const C *Z, const C *X, long long M, int NF, int NT,
+                                     const decltype(C().x) *phif, const C *twNT, const C *tlo, const C *thi, int K,
                                      decltype(C().x) *wdm) {
   using R = decltype(C().x);
   extern __shared__ __align__(16) unsigned char sm_raw[];
@@ -250,7 +251,7 @@ __global__ void wdm_fwd_layer_kernel(const C *Z, long long M, int NF, int NT, co
     if (ok) {
       R w = phif[j < 0 ? -j : j];
       if (j == 0 && (m == 0 || m == NF)) w *= (R)0.5;
-      v = csc(real_bin(Z, M, (long long)idx, tlo, thi, K), w);
+      v = csc(X ? X[idx] : real_bin(Z, M, (long long)idx, tlo, thi, K), w);
     }
     a[t] = v;
   }
@@ -542,7 +543,7 @@ static cudaError_t forward_t(const WdmPlan &P, const double *time, double *wdm, 
   if ((e = four_step<C>(P, packed, (C *)P.bufB, (C *)P.bufA, -1, (R)1, s)) != cudaSuccess) return e;
   const size_t sm = fft_smem<C>(P.NT, 1);
   if ((e = set_smem((const void *)wdm_fwd_layer_kernel<C>, sm)) != cudaSuccess) return e;
-  wdm_fwd_layer_kernel<C><<<P.NF + 1, 256, sm, s>>>((const C *)P.bufA, P.M, P.NF, P.NT, (const R *)P.win,
+  wdm_fwd_layer_kernel<C><<<P.NF + 1, 256, sm, s>>>((const C *)P.bufA, nullptr, P.M, P.NF, P.NT, (const R *)P.win,
                                                      (const C *)P.twNT, (const C *)P.nlo, (const C *)P.nhi, P.K,
                                                      out);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -550,8 +551,9 @@ static cudaError_t forward_t(const WdmPlan &P, const double *time, double *wdm, 
   return cudaGetLastError();
 }
 
+// WDM -> spectrum: bins 0..M summed into P.bufX by the windowed layer transforms.
 template <typename C>
-static cudaError_t inverse_t(const WdmPlan &P, const double *wdm, double *time, cudaStream_t s) {
+static cudaError_t inverse_layers_t(const WdmPlan &P, const double *wdm, cudaStream_t s) {
   using R = decltype(C().x);
   constexpr bool kF64 = std::is_same<R, double>::value;
   const long long ND = (long long)P.NF * P.NT, M = P.M;
@@ -571,6 +573,16 @@ static cudaError_t inverse_t(const WdmPlan &P, const double *wdm, double *time, 
   for (int parity = 0; parity < 2; parity++)
     wdm_inv_layer_kernel<C><<<(NF - parity) / 2 + 1, 256, sm, s>>>(in, NF, NT, parity, (const R *)P.win,
                                                                     (const C *)P.twNT, (C *)P.bufX);
+  return cudaGetLastError();
+}
+
+template <typename C>
+static cudaError_t inverse_t(const WdmPlan &P, const double *wdm, double *time, cudaStream_t s) {
+  using R = decltype(C().x);
+  constexpr bool kF64 = std::is_same<R, double>::value;
+  const long long ND = (long long)P.NF * P.NT, M = P.M;
+  cudaError_t e;
+  if ((e = inverse_layers_t<C>(P, wdm, s)) != cudaSuccess) return e;
   wdm_pack_kernel<C><<<blocks_for(M), 256, 0, s>>>((const C *)P.bufX, M, (const C *)P.nlo, (const C *)P.nhi, P.K,
                                                    (C *)P.bufA);
   const bool direct = kF64 && (uintptr_t)time % 16 == 0;
@@ -581,6 +593,50 @@ static cudaError_t inverse_t(const WdmPlan &P, const double *wdm, double *time, 
     wdm_uncast_kernel<C><<<blocks_for(ND), 256, 0, s>>>((const R *)P.rbuf, time, ND);
   else if (!direct)
     return cudaMemcpyAsync(time, P.rbuf, sizeof(double) * ND, cudaMemcpyDeviceToDevice, s);
+  return cudaGetLastError();
+}
+
+// wdm -> ND/2 + 1 complex bins (ND + 2 doubles), wavelet_transform_inverse_freq
+template <typename C>
+static cudaError_t to_freq_t(const WdmPlan &P, const double *wdm, double *freq, cudaStream_t s) {
+  using R = decltype(C().x);
+  constexpr bool kF64 = std::is_same<R, double>::value;
+  const long long n = 2 * (P.M + 1);
+  cudaError_t e;
+  if ((e = inverse_layers_t<C>(P, wdm, s)) != cudaSuccess) return e;
+  if (kF64) return cudaMemcpyAsync(freq, P.bufX, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+  wdm_uncast_kernel<C><<<blocks_for(n), 256, 0, s>>>((const R *)P.bufX, freq, n);
+  return cudaGetLastError();
+}
+
+// ND/2 + 1 complex bins -> wdm, wavelet_transform_freq
+template <typename C>
+static cudaError_t from_freq_t(const WdmPlan &P, const double *freq, double *wdm, cudaStream_t s) {
+  using R = decltype(C().x);
+  constexpr bool kF64 = std::is_same<R, double>::value;
+  const long long ND = (long long)P.NF * P.NT, n = 2 * (P.M + 1);
+  cudaError_t e;
+  const C *X;
+  R *out;
+  if (kF64) {
+    if ((uintptr_t)freq % 16) {
+      if ((e = cudaMemcpyAsync(P.bufX, freq, sizeof(double) * n, cudaMemcpyDeviceToDevice, s)) != cudaSuccess) return e;
+      X = (const C *)P.bufX;
+    } else {
+      X = reinterpret_cast<const C *>(freq);
+    }
+    out = reinterpret_cast<R *>(wdm);
+  } else {
+    wdm_cast_kernel<C><<<blocks_for(n), 256, 0, s>>>(freq, (R *)P.bufX, n);
+    X = (const C *)P.bufX;
+    out = (R *)P.rbuf;
+  }
+  const size_t sm = fft_smem<C>(P.NT, 1);
+  if ((e = set_smem((const void *)wdm_fwd_layer_kernel<C>, sm)) != cudaSuccess) return e;
+  wdm_fwd_layer_kernel<C><<<P.NF + 1, 256, sm, s>>>(nullptr, X, P.M, P.NF, P.NT, (const R *)P.win, (const C *)P.twNT,
+                                                     (const C *)P.nlo, (const C *)P.nhi, P.K, out);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (!kF64) wdm_uncast_kernel<C><<<blocks_for(ND), 256, 0, s>>>(out, wdm, ND);
   return cudaGetLastError();
 }
 
@@ -611,6 +667,14 @@ cudaError_t wdm_forward(const WdmPlan &P, const double *time, double *wdm, cudaS
 
 cudaError_t wdm_inverse(const WdmPlan &P, const double *wdm, double *time, cudaStream_t s) {
   return P.precision == 1 ? inverse_t<float2>(P, wdm, time, s) : inverse_t<double2>(P, wdm, time, s);
+}
+
+cudaError_t wdm_to_freq(const WdmPlan &P, const double *wdm, double *freq, cudaStream_t s) {
+  return P.precision == 1 ? to_freq_t<float2>(P, wdm, freq, s) : to_freq_t<double2>(P, wdm, freq, s);
+}
+
+cudaError_t wdm_from_freq(const WdmPlan &P, const double *freq, double *wdm, cudaStream_t s) {
+  return P.precision == 1 ? from_freq_t<float2>(P, freq, wdm, s) : from_freq_t<double2>(P, freq, wdm, s);
 }
 
 // Meyer window of utils/src/glass_wavelet.c:305-349 with the regularised

@@ -35,5 +35,9 @@ void wdm_release(WdmPlan &P);
 cudaError_t wdm_forward(const WdmPlan &P, const double *time, double *wdm, cudaStream_t s);
 // wdm -> time; may be the same buffer.
 cudaError_t wdm_inverse(const WdmPlan &P, const double *wdm, double *time, cudaStream_t s);
+// wdm -> ND/2 + 1 complex bins (ND + 2 doubles, re/im interleaved), and back.
+// Input and output must not overlap.
+cudaError_t wdm_to_freq(const WdmPlan &P, const double *wdm, double *freq, cudaStream_t s);
+cudaError_t wdm_from_freq(const WdmPlan &P, const double *freq, double *wdm, cudaStream_t s);
 
 }  // namespace glass

@@ -19,6 +19,8 @@
 #ifndef GLASS_GB300_H
 #define GLASS_GB300_H
 
+#include <stdbool.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -47,7 +49,9 @@ extern "C" {
 #define GLASS_FMT_FREQUENCY 2 /* "frequency" utils/src/glass_lisa.c:551 */
 
 /* ------------------------------------------------ drop-in (reference ABI) */
-struct Orbit; /* utils/src/glass_lisa.h:60-109; read: L, fstar, orbit_function */
+struct Orbit; /* utils/src/glass_lisa.h:60-109; read: L, fstar, orbit_function (ucb_waveform), Norb, t, x, y, z
+                 (ucb_waveform_wavelet) */
+struct Wavelets; /* utils/src/glass_wavelet.h:25-75; read: NF, NT, dt, df, A, kmin, kmax */
 
 /*
  * Replaces ucb_waveform (ucb/src/glass_ucb_waveform.h:210,
@@ -234,6 +238,18 @@ int glass_gpu_wdm_forward(glass_gpu_ctx *ctx, int precision, int NF, int NT, dou
 int glass_gpu_wdm_inverse(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
                           const double *wdm, double *time);
 
+/*
+ * wdm -> the ND/2 + 1 complex bins (ND + 2 doubles, re/im interleaved) that
+ * wavelet_transform_inverse_freq (utils/src/glass_wavelet.c:351) produces, and
+ * bins -> wdm as wavelet_transform_freq (utils/src/glass_wavelet.c:410) does.
+ * Same precision and grid limits as glass_gpu_wdm_forward; input and output
+ * must not overlap.  Device pointers; asynchronous.
+ */
+int glass_gpu_wdm_to_freq(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx, const double *wdm,
+                          double *freq);
+int glass_gpu_wdm_from_freq(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
+                            const double *freq, double *wdm);
+
 /* The same two with HOST pointers: copy in, transform, copy out, synchronise. */
 int glass_gpu_wdm_forward_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
                                const double *time, double *wdm);
@@ -299,6 +315,42 @@ int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int nitems, const doubl
                                      int *status);
 int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, int *info,
                                           double *xyz, int *status);
+
+/* ------------------------------------ drop-ins for the wavelet headers */
+/*
+ * Same names and signatures as the reference, so that ucb_wavelet_mcmc and
+ * global_fit link against this library instead of glass_wavelet.o /
+ * glass_ucb_waveform.o.  Host arrays; one GPU context per calling thread
+ * (device from GLASS_GPU_DEVICE, default 0), created on first use.  FP64,
+ * window exponent 6 (WAVELET_FILTER_CONSTANT).  Errors print the reason and
+ * exit(1), the reference's way of failing.
+ *
+ * build_wdm_filter_freq          utils/src/glass_wavelet.c:327 (glass_wavelet.h:122)
+ * wavelet_transform_timefreq     utils/src/glass_wavelet.c:293 (glass_wavelet.h:100), in place
+ * wavelet_transform_freq         utils/src/glass_wavelet.c:410 (glass_wavelet.h:105)
+ * wavelet_transform_inverse_freq utils/src/glass_wavelet.c:351 (glass_wavelet.h:108)
+ * ucb_waveform_wavelet           ucb/src/glass_ucb_waveform.c:1061 (glass_ucb_waveform.h:231);
+ *                                the orbit nodes come from the caller's struct Orbit
+ *                                (Norb, t, x, y, z), so interpolated analytic and
+ *                                numeric orbits both work.
+ * ucb_waveform_wavelet_tab / _slow (glass_ucb_waveform.h:237, :239) are not
+ * built: the reference's lookup-table variant itself exits as "not
+ * implemented", and _slow is a debugging variant that writes files.  They
+ * report that and exit(1); glass_ucb_waveform_wavelet_tab/_slow return the
+ * same as GLASS_ERR_STATE for callers that want a status.
+ */
+void build_wdm_filter_freq(double *phif, int Nf, int Nt, double A, bool forward);
+void wavelet_transform_timefreq(struct Wavelets *wdm, double *timedata);
+void wavelet_transform_freq(struct Wavelets *wdm, double *freqdata, double *wdmdata);
+void wavelet_transform_inverse_freq(struct Wavelets *wdm, double *wdmdata, double *freqdata);
+void ucb_waveform_wavelet(struct Orbit *orbit, struct Wavelets *wdm, double Tobs, double t0, double *params,
+                          int *wavelet_list, int *Nwavelet, double *X, double *Y, double *Z);
+void ucb_waveform_wavelet_tab(struct Orbit *orbit, struct Wavelets *wdm, double Tobs, double t0, double *params,
+                              int *wavelet_list, int *Nwavelet, double *X, double *Y, double *Z);
+void ucb_waveform_wavelet_slow(struct Orbit *orbit, struct Wavelets *wdm, double Tobs, double t0, double *params,
+                               int *wavelet_list, int *Nwavelet, double *X, double *Y, double *Z);
+int glass_ucb_waveform_wavelet_tab(void);
+int glass_ucb_waveform_wavelet_slow(void);
 
 /* ---------------------------------------------------------- diagnostics */
 /* Measured fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) of the

@@ -70,8 +70,10 @@ void orc_wdm_window(int Nf, int Nt, double A, double nx, int forward, double *ph
 
 /* Mixed-radix decimation-in-time DFT, X[k] = sum x[n] exp(sign 2 pi i k n/N)
  * (sign -1 forward), recursive over the smallest prime factor; O(p^2) per
- * butterfly, so fine for the small factors WDM grids have. */
-static void orc_dft_rec(const cplx *x, cplx *X, int N, int stride, int sign, cplx *tmp)
+ * butterfly, so fine for the small factors WDM grids have.  The twiddles come
+ * from one table of the top-level roots: a sub-transform of length N/s uses
+ * every s-th root. */
+static void orc_dft_rec(const cplx *x, cplx *X, int N, int stride, const cplx *w, int Ntop, cplx *tmp)
 {
     if (N == 1) {
         X[0] = x[0];
@@ -81,26 +83,80 @@ static void orc_dft_rec(const cplx *x, cplx *X, int N, int stride, int sign, cpl
     while (p * p <= N && N % p) p++;
     if (N % p) p = N;
     int M = N / p;
-    for (int r = 0; r < p; r++) orc_dft_rec(x + r * stride, tmp + r * M, M, stride * p, sign, X);
+    const long long s = Ntop / N;
+    for (int r = 0; r < p; r++) orc_dft_rec(x + r * stride, tmp + r * M, M, stride * p, w, Ntop, X);
     for (int k = 0; k < M; k++)
         for (int q = 0; q < p; q++) {
             cplx acc = 0;
-            for (int r = 0; r < p; r++) {
-                double ang = sign * 2.0 * M_PI * (double)r * (double)(k + q * M) / (double)N;
-                acc += tmp[r * M + k] * (cos(ang) + I * sin(ang));
-            }
+            for (int r = 0; r < p; r++) acc += tmp[r * M + k] * w[((long long)r * (k + q * M) % N) * s];
             X[k + q * M] = acc;
         }
 }
 
+/* Stockham autosort FFT for N = 2^a 3^b (radix-3 stages, then radix 4, then
+ * one radix 2): stage with radix R after sub-length p reads x[i + m N/R]
+ * (i < N/R, k = i mod p), multiplies by w^{m k N/(p R)}, and writes the R-point
+ * DFT to y[(i - k) R + k + q p]. */
+static int orc_smooth23(int N)
+{
+    while (N % 3 == 0) N /= 3;
+    return N > 0 && (N & (N - 1)) == 0;
+}
+
+static void orc_stockham(const cplx *x, cplx *X, int N, int sign)
+{
+    cplx *w = malloc(sizeof(cplx) * N), *a = malloc(sizeof(cplx) * N), *b = malloc(sizeof(cplx) * N);
+    for (int j = 0; j < N; j++) {
+        double ang = sign * 2.0 * M_PI * (double)j / (double)N;
+        w[j] = cos(ang) + I * sin(ang);
+    }
+    memcpy(a, x, sizeof(cplx) * N);
+    int p = 1, rem = N;
+    while (rem > 1) {
+        int R = rem % 3 == 0 ? 3 : rem % 4 == 0 ? 4 : 2;
+        int nb = N / R, step = N / (p * R);
+        cplx wr[4];
+        for (int q = 0; q < R; q++) wr[q] = w[(long long)q * (N / R) % N];
+        for (int i = 0; i < nb; i++) {
+            int k = i % p, j = (i - k) * R + k;
+            cplx v[4];
+            for (int m = 0; m < R; m++) v[m] = a[i + m * nb] * w[(long long)m * k * step % N];
+            for (int q = 0; q < R; q++) {
+                cplx acc = 0;
+                for (int m = 0; m < R; m++) acc += v[m] * wr[(m * q) % R];
+                b[j + q * p] = acc;
+            }
+        }
+        cplx *t = a;
+        a = b;
+        b = t;
+        p *= R;
+        rem /= R;
+    }
+    memcpy(X, a, sizeof(cplx) * N);
+    free(w);
+    free(a);
+    free(b);
+}
+
 static void orc_dft(const cplx *x, cplx *X, int N, int sign)
 {
+    if (orc_smooth23(N)) {
+        orc_stockham(x, X, N, sign);
+        return;
+    }
     cplx *tmp = malloc(sizeof(cplx) * N);
     cplx *xx = malloc(sizeof(cplx) * N);
+    cplx *w = malloc(sizeof(cplx) * N);
+    for (int j = 0; j < N; j++) {
+        double ang = sign * 2.0 * M_PI * (double)j / (double)N;
+        w[j] = cos(ang) + I * sin(ang);
+    }
     memcpy(xx, x, sizeof(cplx) * N);
-    orc_dft_rec(xx, X, N, 1, sign, tmp);
+    orc_dft_rec(xx, X, N, 1, w, N, tmp);
     free(tmp);
     free(xx);
+    free(w);
 }
 
 void orc_complex_fft(const double *in, double *out, int N, int inverse)

@@ -72,3 +72,25 @@ def test_wdm_window_matches_reference(lib, golden):
         np.testing.assert_array_equal(gg.wdm_window(int(NF), int(NT), forward=False), g[f"winv_{key}"])
     with pytest.raises(gg.GlassError):
         gg.wdm_window(32, 63)
+
+
+def test_unbuilt_wavelet_variants_report_a_status(lib):
+    """ucb_waveform_wavelet_tab / _slow are API-only here; their status forms
+    say so without touching a GPU."""
+    c = gg.lib_constants()
+    assert lib.glass_ucb_waveform_wavelet_tab() == c["GLASS_ERR_STATE"]
+    assert b"not implemented" in lib.glass_gpu_last_error()
+    assert lib.glass_ucb_waveform_wavelet_slow() == c["GLASS_ERR_STATE"]
+    assert b"not built" in lib.glass_gpu_last_error()
+
+
+def test_wavelet_setup_argument_checks(lib):
+    """Grid checks of glass_gpu_wavelet_setup run before any device call."""
+    import ctypes
+
+    c = gg.lib_constants()
+    f = lib.glass_gpu_wavelet_setup
+    V = ctypes.c_void_p(1)  # never dereferenced: the checks fail first
+    assert f(V, 1e6, 0.0, 64, 250, 1.0, 0.5, 0.0, 6.0, 0, 250, 0, None, None) == c["GLASS_ERR_SIZE"]
+    assert f(V, 1e6, 0.0, 64, 256, 1.0, 0.5, 0.0, 6.0, 100, 512, 0, None, None) == c["GLASS_ERR_ARG"]
+    assert f(V, -1.0, 0.0, 64, 256, 1.0, 0.5, 0.0, 6.0, 0, 512, 0, None, None) == c["GLASS_ERR_ARG"]
