@@ -78,14 +78,16 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
 
 // Mixed-precision plan, warp-specialised: GB300's FP64 pipe issues a warp
 // instruction only every few tens of cycles, so the FP64 work of a proposal is
-// split over four warps that run in parallel on different SM sub-partitions:
-// warp 0 the bandwidth rule (FP32, FP64 only near a size boundary) and
-// placement, warp 1 the sky direction and polarisation tensors, warp 2 the
-// polarisation factors, warp 3 the amplitude and carrier constants.  The
-// antenna tensors Mr, Mi are then assembled in FP64 by all 128 threads.
-// Same results as planmix_item.
+// split over four warps that run in parallel on different SM sub-partitions,
+// each writing its share of the ItemMix record directly: warp 0 the bandwidth
+// rule (FP32, FP64 only near a size boundary) and placement, warp 1 the sky
+// direction, polarisation tensors and Doppler constants, warp 2 the
+// polarisation factors and the FP32 frequency constants, warp 3 the amplitude
+// and the double-float carrier constants.  The antenna tensors Mr, Mi are then
+// assembled in FP64 by all 128 threads; only the N-dependent fields wait for
+// the barrier.  Same results as planmix_item (the FP32 constants to rounding).
 __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
-  __shared__ double s_ep[32][6], s_ec[32][6], s_dp[32][4], s_k[32][3], s_beta[32][2], s_amp[32];
+  __shared__ double s_ep[32][6], s_ec[32][6], s_dp[32][4], s_amp[32];
   __shared__ int s_st[32], s_N[32], s_imin[32];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   const int i = blockIdx.x * 32 + l;
@@ -94,6 +96,7 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
   int seg = 0, st = 1;
   if (in) st = plan_validate(a, i, p, seg);
   const double T = a.T;
+  ItemMix *c = a.itemsmix + (in ? i : 0);
   if (in && !st) {
     const double f0 = p[0] / T;
     if (w == 0) {
@@ -153,20 +156,22 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       double sph, cph;
       sincos(p[2], &sph, &cph);
       const double u[3] = {cth * cph, cth * sph, -sth}, v[3] = {sph, -cph, 0.};
-      s_k[l][0] = -sth * cph;
-      s_k[l][1] = -sth * sph;
-      s_k[l][2] = -cth;
+      const double kx = -sth * cph, ky = -sth * sph;
+      c->k[0] = (float)kx;
+      c->k[1] = (float)ky;
+      c->k[2] = (float)(-cth);
+      c->k[3] = 0.f;
       int idx = 0;
 #pragma unroll
       for (int r = 0; r < 3; r++)
 #pragma unroll
-        for (int c = r; c < 3; c++, idx++) {
-          s_ep[l][idx] = v[r] * v[c] - u[r] * u[c];
-          s_ec[l][idx] = u[r] * v[c] + v[r] * u[c];
+        for (int q = r; q < 3; q++, idx++) {
+          s_ep[l][idx] = v[r] * v[q] - u[r] * u[q];
+          s_ec[l][idx] = u[r] * v[q] + v[r] * u[q];
         }
       const double bscale = kPI2 * f0 * (kAU / kCLIGHT);
-      s_beta[l][0] = bscale * (-sth * cph);
-      s_beta[l][1] = bscale * (-sth * sph);
+      c->beta1 = df_from_double(bscale * kx);
+      c->beta2 = df_from_double(bscale * ky);
     } else if (w == 2) {
       const double cosi = p[4];
       double sinps, cosps;
@@ -176,8 +181,21 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       s_dp[l][1] = -Across * sinps;
       s_dp[l][2] = -Aplus * sinps;
       s_dp[l][3] = -Across * cosps;
+      const double fdotT = p[7] / T;  // fdot T
+      c->fonfs0 = (float)(f0 / a.fstar);
+      c->fdfs = (float)(fdotT / a.fstar);
+      c->aef = (float)(0.66666666666666666666 * fdotT / f0);
+      c->w0c = (float)(kPI2 * f0 / kCLIGHT);
+      c->p7pi = (float)(kPI * p[7]);
+      c->pad2 = 0.f;
     } else {
       s_amp[l] = exp(p[3]);
+      const double fT = f0 * T;
+      const long long q = (long long)fT;
+      c->eps2pi = df_from_double(kPI2 * (fT - (double)q));
+      c->phi0 = df_from_double(p[6]);
+      c->p7pi_d = df_from_double(kPI * p[7]);
+      c->pad3 = {0.f, 0.f};
     }
   } else if (w == 0) {
     s_st[l] = st;
@@ -188,7 +206,6 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
   const int stt = in ? (st | s_st[l]) : 1;
   // antenna tensors: warp w assembles elements 3w/2 .. of the 12 (Mr, Mi) x 6
   if (in && !stt) {
-    ItemMix *c = a.itemsmix + i;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
       const int e = 3 * w + q;  // 0..11: (tensor element, real/imag)
@@ -207,34 +224,13 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       plan_write_skipped(a, i, stt);
     } else if (in) {
       const int N = s_N[l];
-      const double f0 = p[0] / T;
-      const double fT = f0 * T;
-      const long long q = (long long)fT;
-      ItemMix *c = a.itemsmix + i;
       c->seg = seg;
       c->N = N;
       c->imin = s_imin[l];
       c->pad = 0;
-      c->k[0] = (float)s_k[l][0];
-      c->k[1] = (float)s_k[l][1];
-      c->k[2] = (float)s_k[l][2];
-      c->k[3] = 0.f;
-      const double fdot = p[7] / (T * T);
-      c->fonfs0 = (float)(f0 / a.fstar);
-      c->fdfs = (float)(fdot * T / a.fstar);
-      c->aef = (float)(0.66666666666666666666 * fdot * T / f0);
-      c->w0c = (float)(kPI2 * f0 / kCLIGHT);
-      c->p7pi = (float)(kPI * fdot * T * T);
-      const double sc = s_amp[l] / (2.0 * (double)N);
+      const double sc = scalbn(s_amp[l], -(32 - __clz(N)));  // amp / (2N), N a power of two
       c->amp_hi = (float)sc;
       c->amp_lo = (float)(sc - (double)c->amp_hi);
-      c->pad2 = 0.f;
-      c->eps2pi = df_from_double(kPI2 * (fT - (double)q));
-      c->beta1 = df_from_double(s_beta[l][0]);
-      c->beta2 = df_from_double(s_beta[l][1]);
-      c->phi0 = df_from_double(p[6]);
-      c->p7pi_d = df_from_double(kPI * fdot * T * T);
-      c->pad3 = {0.f, 0.f};
       b = fd_bin_of(N);
     }
     plan_bin(a, i, b);

@@ -130,169 +130,133 @@ __constant__ float kComboCoef[4][6] = {
     {2.f, 1.f, 1.f, -1.f, -1.f, -2.f}, // e1 = 2 d12 + d13 + d21 - d23 - d31 - 2 d32
 };
 
-struct GradSlowArgs {
-  int cap, NFFT;
+struct GradConsts {
   float Rf, invLf, AUcf, invTf, AUf;
-  const int *bin_count, *bin_list;
-  const ItemGrad *items;
-  const OrbitSampleMix *mix[kNumBins];
-  float2 *series;  // 24 series of N per proposal, sizes back to back
 };
 
-// One thread per (proposal, sample): the 6 templates' arm values, combined
-// into their 4 A/E series each.
-__global__ void __launch_bounds__(128) fd_gradslow_kernel(GradSlowArgs a) {
-  int cs[kNumBins + 1];
-  int acc = 0;
+// One sample n of one proposal: the 6 templates' arm values combined into
+// their 4 A/E series each (the slow part of the waveform and its tangents).
+__device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad &g, const OrbitSampleMix &o,
+                                            float2 (&accs)[kGradSeries]) {
+  const ItemMix &c = g.m;
+  // ---- geometry (as slow_sample_mix), plus absolute positions for d tau/dk
+  const float ca = o.ca_hi, sa = o.sa_hi;
+  const float sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
+  const float sbf[3] = {0.0f, 0.866025403784439f, -0.866025403784438f};
+  const float cbf[3] = {1.0f, -0.5f, -0.5f};
+  float dx[3], dy[3], dz[3];
 #pragma unroll
-  for (int b = 0; b < kNumBins; b++) {
-    cs[b] = acc;
-    if ((32 << b) <= a.NFFT) acc += a.bin_count[b] << b;
+  for (int i = 0; i < 3; i++) {
+    dx[i] = K.Rf * (saca * sbf[i] - (1.f + sa2) * cbf[i]);
+    dy[i] = K.Rf * (saca * cbf[i] - (1.f + ca2) * sbf[i]);
+    dz[i] = -1.73205080757f * K.Rf * (ca * cbf[i] + sa * sbf[i]);
   }
-  cs[kNumBins] = acc;
-  const int nchunks = acc;
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-#pragma unroll 1
-  for (int ch = warp; ch < nchunks; ch += nwarps) {
-    int b = 0, cb = 0;
+  // carrier phase (double-float) common to the three spacecraft
+  const df u = {o.u_hi, o.u_lo};
+  const df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
+  df ph = df_mul(c.eps2pi, u);
+  ph = df_add(ph, df_neg(df_add(df_mul(c.beta1, cad), df_mul(c.beta2, sad))));
+  ph = df_add(ph, df_neg(c.phi0));
+  ph = df_add(ph, df_mul(c.p7pi_d, df_mul(u, u)));
+  const float psi0 = df_reduce_2pi(ph);
+  const float uf = o.u_hi;
+  const float tgc = K.AUcf * (c.k[0] * ca + c.k[1] * sa);
+  const float gx = K.AUf * ca, gy = K.AUf * sa;  // guiding centre (m)
+  float fon[3], arg2[3], aev[3], vv[3], wxi[3], dtc[3], dtp[3];
 #pragma unroll
-    for (int bb = 1; bb < kNumBins; bb++)
-      if (ch >= cs[bb]) {
-        b = bb;
-        cb = cs[bb];
+  for (int i = 0; i < 3; i++) {
+    const float kdx = c.k[0] * dx[i] + c.k[1] * dy[i] + c.k[2] * dz[i];
+    const float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
+    const float tT = taui * K.invTf;
+    const float v = uf - tT;  // xi / T
+    vv[i] = v;
+    fon[i] = fmaf(c.fdfs, v, c.fonfs0);
+    aev[i] = fmaf(c.aef, v, 1.0f);
+    arg2[i] = psi0 - c.w0c * kdx + c.p7pi * tT * (tT - 2.0f * uf);
+    // d arg2 / d xi and d tau / d(cos theta), d tau / d phi
+    wxi[i] = 6.2831853f * fmaf(g.fdot, v / K.invTf, g.f0);
+    const float X = gx + dx[i], Y = gy + dy[i], Z = dz[i];
+    dtc[i] = (g.dk_c[0] * X + g.dk_c[1] * Y + g.dk_c[2] * Z) * (float)(1.0 / kCLIGHT);
+    dtp[i] = (g.dk_p[0] * X + g.dk_p[1] * Y + g.dk_p[2] * Z) * (float)(1.0 / kCLIGHT);
+  }
+  // unique arms 12, 13, 23
+  float r[3][3];
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const int i0 = q == 2 ? 1 : 0, i1 = q == 0 ? 1 : 2;
+    r[q][0] = (dx[i1] - dx[i0]) * K.invLf;
+    r[q][1] = (dy[i1] - dy[i0]) * K.invLf;
+    r[q][2] = (dz[i1] - dz[i0]) * K.invLf;
+  }
+#pragma unroll
+  for (int s = 0; s < kGradSeries; s++) accs[s] = make_float2(0.f, 0.f);
+
+  const float invfsT = K.invTf / g.fstar;
+  const float f0T = g.f0 / K.invTf;  // f0 T
+#pragma unroll
+  for (int arm = 0; arm < 6; arm++) {
+    // directed arm -> (spacecraft i, unique arm q, orientation sign)
+    const int i = arm >> 1;
+    const int q = (arm == 0 || arm == 2) ? 0 : (arm == 1 || arm == 4) ? 1 : 2;
+    const float sg = (arm == 2 || arm == 4 || arm == 5) ? -1.f : 1.f;
+    const float rx = r[q][0], ry = r[q][1], rz = r[q][2];
+    const float dp = quad(g.ep, rx, ry, rz), dc = quad(g.ec, rx, ry, rz);
+    const float kr = sg * (c.k[0] * rx + c.k[1] * ry + c.k[2] * rz);
+    const float dkr_c = sg * (g.dk_c[0] * rx + g.dk_c[1] * ry + g.dk_c[2] * rz);
+    const float dkr_p = sg * (g.dk_p[0] * rx + g.dk_p[1] * ry + g.dk_p[2] * rz);
+    const float arg1 = 0.5f * fon[i] * (1.0f + kr);
+    const float sn = sinc_f(arg1);
+    const float gS = dsinc_f(arg1) / sn;
+    const float S = 0.25f * sn * aev[i];
+    float sth, cth;
+    fast_sincos(arg1 - arg2[i], &sth, &cth);
+    const float2 E = make_float2(cth, -sth);
+    const float2 SE = make_float2(S * E.x, S * E.y);
+    const float2 Pc = make_float2(g.DP[0] * dp + g.DC[0] * dc, g.DP[1] * dp + g.DC[1] * dc);
+    const float2 d = cmul(Pc, SE);
+    const float2 Bp = make_float2(dp * SE.x, dp * SE.y);
+    const float2 Bx = make_float2(dc * SE.x, dc * SE.y);
+    // f0 (params[0] = f0 T)
+    const float dA1_0 = 0.5f * (1.0f + kr) * invfsT;
+    const float dth_0 = dA1_0 - 6.2831853f * vv[i];
+    const float dlS_0 = gS * dA1_0 - c.aef * vv[i] / (f0T * aev[i]);
+    const float2 T0 = cmul(d, make_float2(dlS_0, -dth_0));
+    // fdot (params[7] = fdot T^2)
+    const float dA1_7 = dA1_0 * vv[i];
+    const float dth_7 = dA1_7 - 3.14159265f * vv[i] * vv[i];
+    const float dlS_7 = gS * dA1_7 + 0.6666667f * vv[i] / (f0T * aev[i]);
+    const float2 T7 = cmul(d, make_float2(dlS_7, -dth_7));
+    // cos(theta)
+    const float dA1_c = 0.5f * fon[i] * dkr_c;
+    const float dth_c = dA1_c + wxi[i] * dtc[i];
+    const float dpc = quad(g.dep_c, rx, ry, rz), dcc = quad(g.dec_c, rx, ry, rz);
+    const float2 dPc = make_float2(g.DP[0] * dpc + g.DC[0] * dcc, g.DP[1] * dpc + g.DC[1] * dcc);
+    const float2 Tc = cadd(cmul(d, make_float2(gS * dA1_c, -dth_c)), cmul(dPc, SE));
+    // phi
+    const float dA1_p = 0.5f * fon[i] * dkr_p;
+    const float dth_p = dA1_p + wxi[i] * dtp[i];
+    const float dpp = quad(g.dep_p, rx, ry, rz), dcp = quad(g.dec_p, rx, ry, rz);
+    const float2 dPp = make_float2(g.DP[0] * dpp + g.DC[0] * dcp, g.DP[1] * dpp + g.DC[1] * dcp);
+    const float2 Tp = cadd(cmul(d, make_float2(gS * dA1_p, -dth_p)), cmul(dPp, SE));
+    const float2 vals[kGradTemplates] = {Bp, Bx, T0, T7, Tc, Tp};
+#pragma unroll
+    for (int t = 0; t < kGradTemplates; t++)
+#pragma unroll
+      for (int s = 0; s < 4; s++) {
+        const float cf = kComboCoef[s][arm];
+        accs[4 * t + s].x = fmaf(cf, vals[t].x, accs[4 * t + s].x);
+        accs[4 * t + s].y = fmaf(cf, vals[t].y, accs[4 * t + s].y);
       }
-    const int N = 32 << b;
-    const int local = ch - cb;
-    const int slot = local >> b;
-    const int n = ((local & ((1 << b) - 1)) << 5) + lane;
-    const ItemGrad &g = a.items[a.bin_list[(size_t)b * a.cap + slot]];
-    const ItemMix &c = g.m;
-    const OrbitSampleMix o = a.mix[b][n];
-
-    // ---- geometry (as slow_sample_mix), plus absolute positions for d tau/dk
-    const float ca = o.ca_hi, sa = o.sa_hi;
-    const float sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
-    const float sbf[3] = {0.0f, 0.866025403784439f, -0.866025403784438f};
-    const float cbf[3] = {1.0f, -0.5f, -0.5f};
-    float dx[3], dy[3], dz[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      dx[i] = a.Rf * (saca * sbf[i] - (1.f + sa2) * cbf[i]);
-      dy[i] = a.Rf * (saca * cbf[i] - (1.f + ca2) * sbf[i]);
-      dz[i] = -1.73205080757f * a.Rf * (ca * cbf[i] + sa * sbf[i]);
-    }
-    // carrier phase (double-float) common to the three spacecraft
-    const df u = {o.u_hi, o.u_lo};
-    const df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
-    df ph = df_mul(c.eps2pi, u);
-    ph = df_add(ph, df_neg(df_add(df_mul(c.beta1, cad), df_mul(c.beta2, sad))));
-    ph = df_add(ph, df_neg(c.phi0));
-    ph = df_add(ph, df_mul(c.p7pi_d, df_mul(u, u)));
-    const float psi0 = df_reduce_2pi(ph);
-    const float uf = o.u_hi;
-    const float tgc = a.AUcf * (c.k[0] * ca + c.k[1] * sa);
-    const float gx = a.AUf * ca, gy = a.AUf * sa;  // guiding centre (m)
-    float fon[3], arg2[3], aev[3], vv[3], wxi[3], dtc[3], dtp[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const float kdx = c.k[0] * dx[i] + c.k[1] * dy[i] + c.k[2] * dz[i];
-      const float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
-      const float tT = taui * a.invTf;
-      const float v = uf - tT;  // xi / T
-      vv[i] = v;
-      fon[i] = fmaf(c.fdfs, v, c.fonfs0);
-      aev[i] = fmaf(c.aef, v, 1.0f);
-      arg2[i] = psi0 - c.w0c * kdx + c.p7pi * tT * (tT - 2.0f * uf);
-      // d arg2 / d xi and d tau / d(cos theta), d tau / d phi
-      wxi[i] = 6.2831853f * fmaf(g.fdot, v / a.invTf, g.f0);
-      const float X = gx + dx[i], Y = gy + dy[i], Z = dz[i];
-      dtc[i] = (g.dk_c[0] * X + g.dk_c[1] * Y + g.dk_c[2] * Z) * (float)(1.0 / kCLIGHT);
-      dtp[i] = (g.dk_p[0] * X + g.dk_p[1] * Y + g.dk_p[2] * Z) * (float)(1.0 / kCLIGHT);
-    }
-    // unique arms 12, 13, 23
-    float r[3][3];
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      const int i0 = q == 2 ? 1 : 0, i1 = q == 0 ? 1 : 2;
-      r[q][0] = (dx[i1] - dx[i0]) * a.invLf;
-      r[q][1] = (dy[i1] - dy[i0]) * a.invLf;
-      r[q][2] = (dz[i1] - dz[i0]) * a.invLf;
-    }
-    float2 accs[kGradSeries];
-#pragma unroll
-    for (int s = 0; s < kGradSeries; s++) accs[s] = make_float2(0.f, 0.f);
-
-    const float invfsT = a.invTf / g.fstar;
-    const float f0T = g.f0 / a.invTf;  // f0 T
-#pragma unroll
-    for (int arm = 0; arm < 6; arm++) {
-      // directed arm -> (spacecraft i, unique arm q, orientation sign)
-      const int i = arm >> 1;
-      const int q = (arm == 0 || arm == 2) ? 0 : (arm == 1 || arm == 4) ? 1 : 2;
-      const float sg = (arm == 2 || arm == 4 || arm == 5) ? -1.f : 1.f;
-      const float rx = r[q][0], ry = r[q][1], rz = r[q][2];
-      const float dp = quad(g.ep, rx, ry, rz), dc = quad(g.ec, rx, ry, rz);
-      const float kr = sg * (c.k[0] * rx + c.k[1] * ry + c.k[2] * rz);
-      const float dkr_c = sg * (g.dk_c[0] * rx + g.dk_c[1] * ry + g.dk_c[2] * rz);
-      const float dkr_p = sg * (g.dk_p[0] * rx + g.dk_p[1] * ry + g.dk_p[2] * rz);
-      const float arg1 = 0.5f * fon[i] * (1.0f + kr);
-      const float sn = sinc_f(arg1);
-      const float gS = dsinc_f(arg1) / sn;
-      const float S = 0.25f * sn * aev[i];
-      float sth, cth;
-      fast_sincos(arg1 - arg2[i], &sth, &cth);
-      const float2 E = make_float2(cth, -sth);
-      const float2 SE = make_float2(S * E.x, S * E.y);
-      const float2 Pc = make_float2(g.DP[0] * dp + g.DC[0] * dc, g.DP[1] * dp + g.DC[1] * dc);
-      const float2 d = cmul(Pc, SE);
-      const float2 Bp = make_float2(dp * SE.x, dp * SE.y);
-      const float2 Bx = make_float2(dc * SE.x, dc * SE.y);
-      // f0 (params[0] = f0 T)
-      const float dA1_0 = 0.5f * (1.0f + kr) * invfsT;
-      const float dth_0 = dA1_0 - 6.2831853f * vv[i];
-      const float dlS_0 = gS * dA1_0 - c.aef * vv[i] / (f0T * aev[i]);
-      const float2 T0 = cmul(d, make_float2(dlS_0, -dth_0));
-      // fdot (params[7] = fdot T^2)
-      const float dA1_7 = dA1_0 * vv[i];
-      const float dth_7 = dA1_7 - 3.14159265f * vv[i] * vv[i];
-      const float dlS_7 = gS * dA1_7 + 0.6666667f * vv[i] / (f0T * aev[i]);
-      const float2 T7 = cmul(d, make_float2(dlS_7, -dth_7));
-      // cos(theta)
-      const float dA1_c = 0.5f * fon[i] * dkr_c;
-      const float dth_c = dA1_c + wxi[i] * dtc[i];
-      const float dpc = quad(g.dep_c, rx, ry, rz), dcc = quad(g.dec_c, rx, ry, rz);
-      const float2 dPc = make_float2(g.DP[0] * dpc + g.DC[0] * dcc, g.DP[1] * dpc + g.DC[1] * dcc);
-      const float2 Tc = cadd(cmul(d, make_float2(gS * dA1_c, -dth_c)), cmul(dPc, SE));
-      // phi
-      const float dA1_p = 0.5f * fon[i] * dkr_p;
-      const float dth_p = dA1_p + wxi[i] * dtp[i];
-      const float dpp = quad(g.dep_p, rx, ry, rz), dcp = quad(g.dec_p, rx, ry, rz);
-      const float2 dPp = make_float2(g.DP[0] * dpp + g.DC[0] * dcp, g.DP[1] * dpp + g.DC[1] * dcp);
-      const float2 Tp = cadd(cmul(d, make_float2(gS * dA1_p, -dth_p)), cmul(dPp, SE));
-      const float2 vals[kGradTemplates] = {Bp, Bx, T0, T7, Tc, Tp};
-#pragma unroll
-      for (int t = 0; t < kGradTemplates; t++)
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-          const float cf = kComboCoef[s][arm];
-          accs[4 * t + s].x = fmaf(cf, vals[t].x, accs[4 * t + s].x);
-          accs[4 * t + s].y = fmaf(cf, vals[t].y, accs[4 * t + s].y);
-        }
-    }
-    float2 *out = a.series + ((long long)cb * 32 + (long long)slot * N) * kGradSeries + n;
-#pragma unroll
-    for (int s = 0; s < kGradSeries; s++) out[(size_t)s * N] = accs[s];
   }
 }
 
 struct GradSpecArgs {
   int NFFT, cap, bin, fisher_mode;
+  GradConsts K;
   const int *bin_count;
   const int *bin_list;
   const ItemGrad *items;
-  const float2 *series;
+  const OrbitSampleMix *mix;  // this size's orbit table
   const float2 *tw;
   const float4 *w32, *w32lo, *g32;
   const float2 *invc;  // invC_A, invC_E per segment bin (reference-indexed Fisher)
@@ -307,10 +271,16 @@ struct GradCfg {
   static constexpr int CTA = GT >= 64 ? GT : 128;
   static constexpr int GPC = CTA / GT;
   static constexpr int NACC = 8 + 36;  // gradient, Fisher upper triangle
-  static constexpr size_t group_floats2 = 16 * (size_t)N;  // 4 N FFT buffer + 12 N whitened values
+  // 24 series of N per group; after each template's FFT its whitened A and E
+  // spectra overwrite the first 2N of the template's own 4N
+  static constexpr size_t group_floats2 = (size_t)kGradSeries * N;
   static constexpr size_t bytes = sizeof(float2) * (N + GPC * group_floats2) + sizeof(float2) * 32 * GPC;
 };
 
+// One group of N/4 threads per proposal: the 24 series are computed sample by
+// sample straight into shared memory, FFT'd template by template, whitened,
+// and reduced to the gradient and the Fisher matrix.  Nothing of size N
+// leaves the SM.
 template <int N>
 __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecArgs a) {
   using Cfg = GradCfg<N>;
@@ -322,12 +292,10 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw[i];
   __syncthreads();
   const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
-  float2 *fbuf = groups + g * Cfg::group_floats2;  // 4 N
-  float2 *wbuf = fbuf + 4 * N;                      // 12 N: [(2 t + ch) N + k]
-  float *part = reinterpret_cast<float *>(fbuf);    // reduction scratch after use
+  float2 *sbuf = groups + g * Cfg::group_floats2;  // [s N + n], s = 4 t + combo
+  float *part = reinterpret_cast<float *>(sbuf);   // reduction scratch after use
   float2 *red = redall + 32 * g;
   const int count = a.bin_count[a.bin];
-  const float2 *series = a.series + bin_sample_start(a.bin_count, a.NFFT, a.bin) * kGradSeries;
   const int NFFT = a.NFFT;
 
   for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC) {
@@ -337,15 +305,20 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     const int item = a.bin_list[sl];
     const ItemGrad &it = a.items[item];
     const int seg = it.m.seg, imin = it.m.imin;
-    const float2 *src = series + (size_t)sl * kGradSeries * N;
+    // the 24 series, four samples per thread
+#pragma unroll 1
+    for (int r = 0; r < 4; r++) {
+      const int n = lane + GT * r;
+      float2 accs[kGradSeries];
+      grad_sample(a.K, it, a.mix[n], accs);
+#pragma unroll
+      for (int s = 0; s < kGradSeries; s++) sbuf[(size_t)s * N + n] = accs[s];
+    }
+    group_sync<GT>();
     // FFT each template's four series and whiten/weight them per bin
 #pragma unroll 1
     for (int t = 0; t < kGradTemplates; t++) {
-#pragma unroll
-      for (int s = 0; s < 4; s++)
-#pragma unroll
-        for (int r = 0; r < 4; r++) fbuf[s * N + lane + GT * r] = src[(size_t)(4 * t + s) * N + lane + GT * r];
-      group_sync<GT>();
+      float2 *fbuf = sbuf + (size_t)4 * t * N;
       group_fft<N, GT, 4, 4>(fbuf, tw, lane);
 #pragma unroll
       for (int r = 0; r < 4; r++) {
@@ -359,8 +332,9 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
           vA = cadd(cmul(fbuf[k], make_float2(gA.x, gA.y)), cmul(fbuf[N + k], make_float2(gA.z, gA.w)));
           vE = cadd(cmul(fbuf[2 * N + k], make_float2(gE.x, gE.y)), cmul(fbuf[3 * N + k], make_float2(gE.z, gE.w)));
         }
-        wbuf[(2 * t) * N + k] = vA;
-        wbuf[(2 * t + 1) * N + k] = vE;
+        // bin k's four values are read by this thread only: overwrite in place
+        fbuf[k] = vA;
+        fbuf[N + k] = vE;
       }
       group_sync<GT>();
     }
@@ -373,6 +347,8 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     const float2 DP = make_float2(it.DP[0], it.DP[1]), DC = make_float2(it.DC[0], it.DC[1]);
     const float2 dDPi = make_float2(it.dDP_i[0], it.dDP_i[1]), dDCi = make_float2(it.dDC_i[0], it.dDC_i[1]);
     const float2 dDPs = make_float2(it.dDP_s[0], it.dDP_s[1]), dDCs = make_float2(it.dDC_s[0], it.dDC_s[1]);
+    // whitened template t, channel ch (0 A, 1 E) at bin k
+    auto W = [&](int t, int ch, int k) { return sbuf[(size_t)(4 * t + ch) * N + k]; };
 #pragma unroll 1
     for (int r = 0; r < 4; r++) {
       const int k = lane + GT * r;
@@ -389,17 +365,17 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
       }
 #pragma unroll
       for (int ch = 0; ch < 2; ch++) {
-        const float2 Hp = cscale(wbuf[(0 + ch) * N + k], s), Hx = cscale(wbuf[(2 + ch) * N + k], s);
+        const float2 Hp = cscale(W(0, ch, k), s), Hx = cscale(W(1, ch, k), s);
         const float2 h = cadd(cmul(DP, Hp), cmul(DC, Hx));
         float2 D[8];
-        D[0] = cscale(wbuf[(4 + ch) * N + k], s);
-        D[1] = cscale(wbuf[(8 + ch) * N + k], s);
-        D[2] = cscale(wbuf[(10 + ch) * N + k], s);
+        D[0] = cscale(W(2, ch, k), s);
+        D[1] = cscale(W(4, ch, k), s);
+        D[2] = cscale(W(5, ch, k), s);
         D[3] = h;
         D[4] = cadd(cmul(dDPi, Hp), cmul(dDCi, Hx));
         D[5] = cadd(cmul(dDPs, Hp), cmul(dDCs, Hx));
         D[6] = cmi(h);
-        D[7] = cscale(wbuf[(6 + ch) * N + k], s);
+        D[7] = cscale(W(3, ch, k), s);
         const float wr = ch ? w.z : w.x, wi = ch ? w.w : w.y;
         const float lr = ch ? wl.z : wl.x, li = ch ? wl.w : wl.y;
         const float rr = (wr - h.x) + lr, ri = (wi - h.y) + li;
@@ -414,7 +390,7 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
       }
     }
     // reduce over the group: per-thread partials in shared memory (reusing the
-    // FFT and whitened-value buffers once every thread is done with them)
+    // series buffer once every thread is done with it)
     group_sync<GT>();
 #pragma unroll
     for (int q = 0; q < NACC; q++) part[q * GT + lane] = accg[q];
@@ -475,10 +451,7 @@ static cudaError_t launch_gradspec(const GradSpecArgs &a, int nitems_bound, int 
   return cudaGetLastError();
 }
 
-size_t fd_grad_series_bytes(int nitems, int NFFT) {
-  int nmax = NFFT < kGradMaxN ? NFFT : kGradMaxN;
-  return (size_t)nitems * (size_t)nmax * kGradSeries * sizeof(float2);
-}
+size_t fd_grad_series_bytes(int, int) { return 0; }  // the series never leave shared memory
 
 cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int nitems,
                            const int *item_seg, const double *params, int N_fixed, int fisher_mode, double *term_y,
@@ -519,38 +492,17 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
   launches++;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
 
-  GradSlowArgs sa;
-  sa.cap = work.cap;
-  sa.NFFT = pa.NFFT;
-  sa.Rf = (float)(kAU * (kLARM / (2.0 * kSQ3 * kAU)));
-  sa.invLf = (float)(1.0 / kLARM);
-  sa.AUcf = (float)(kAU / kCLIGHT);
-  sa.invTf = (float)(1.0 / bank.T);
-  sa.AUf = (float)kAU;
-  sa.bin_count = work.bin_count;
-  sa.bin_list = work.bin_list;
-  sa.items = work.itemsgrad;
-  for (int b = 0; b < kNumBins; b++) sa.mix[b] = tab.mix[b];
-  sa.series = reinterpret_cast<float2 *>(work.series);
-  {
-    static int occ = -1;
-    if (occ < 0) {
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_gradslow_kernel, 128, 0);
-      if (e != cudaSuccess) return e;
-      if (occ < 1) occ = 1;
-    }
-    fd_gradslow_kernel<<<occ * num_sms, 128, 0, stream>>>(sa);
-    launches++;
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-
   GradSpecArgs a;
   a.NFFT = bank.NFFT;
   a.cap = work.cap;
   a.fisher_mode = fisher_mode;
   a.bin_count = work.bin_count;
   a.items = work.itemsgrad;
-  a.series = reinterpret_cast<const float2 *>(work.series);
+  a.K.Rf = (float)(kAU * (kLARM / (2.0 * kSQ3 * kAU)));
+  a.K.invLf = (float)(1.0 / kLARM);
+  a.K.AUcf = (float)(kAU / kCLIGHT);
+  a.K.invTf = (float)(1.0 / bank.T);
+  a.K.AUf = (float)kAU;
   a.w32 = bank.w32;
   a.w32lo = bank.w32lo;
   a.g32 = bank.g32;
@@ -570,6 +522,7 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
     a.bin = b;
     a.bin_list = work.bin_list + (size_t)b * work.cap;
     a.tw = tab.tw32[b];
+    a.mix = tab.mix[b];
     switch (N) {
       case 32: e = launch_gradspec<32>(a, nitems, num_sms, sb); break;
       case 64: e = launch_gradspec<64>(a, nitems, num_sms, sb); break;
