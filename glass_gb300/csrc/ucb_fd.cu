@@ -36,6 +36,8 @@ cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t st
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_spec_all_fp64(const SpecAllArgs &A, int num_sms, cudaStream_t stream);
 
 // ------------------------------------------------------------- plan kernels
 // Plain-FP64 plan: ucb_bandwidth, ucb_alignment and the per-proposal constants
@@ -86,12 +88,16 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
 // and the double-float carrier constants.  The antenna tensors Mr, Mi are then
 // assembled in FP64 by all 128 threads; only the N-dependent fields wait for
 // the barrier.  Same results as planmix_item (the FP32 constants to rounding).
+// Proposals per CTA: 16 of the 32 lanes of each role warp, so that a batch of
+// a few thousand proposals spreads over every SM (the kernel is latency-bound).
+constexpr int kPlanItems = 16;
+
 __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
   __shared__ double s_ep[32][6], s_ec[32][6], s_dp[32][4], s_amp[32];
   __shared__ int s_st[32], s_N[32], s_imin[32];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  const int i = blockIdx.x * 32 + l;
-  const bool in = i < a.nitems;
+  const int i = blockIdx.x * kPlanItems + l;
+  const bool in = l < kPlanItems && i < a.nitems;
   double p[8];
   int seg = 0, st = 1;
   if (in) st = plan_validate(a, i, p, seg);
@@ -397,7 +403,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.hh = hh;
   pa.status = status;
   if (mix)
-    fd_planmix_kernel<<<(nitems + 31) / 32, 128, 0, stream>>>(pa);
+    fd_planmix_kernel<<<(nitems + kPlanItems - 1) / kPlanItems, 128, 0, stream>>>(pa);
   else
     fd_plan64_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(pa);
   launches++;
@@ -443,25 +449,42 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.term_y = term_y;
   a.hh = hh;
   a.status = status;
-  e = cudaEventRecord(work.fork, stream);
-  if (e != cudaSuccess) return e;
-  // every size a segment of NFFT bins can produce: 32 .. NFFT (ucb_bandwidth caps N at NFFT)
+  // sizes up to 1024 (every size a segment of NFFT bins can produce, up to
+  // NFFT: ucb_bandwidth caps N there) in one launch on the main stream; 2048
+  // and 4096 as their own kernels on side streams running beside it
+  int nall = 0;
+  while (nall < kSpecAllBins && (32 << nall) <= bank.NFFT) nall++;
   int nb = 0;
-  for (int b = 0; b < kNumBins; b++) {
-    int N = 32 << b;
-    if (N > bank.NFFT) break;
-    cudaStream_t sb = work.side[b];
-    if ((e = cudaStreamWaitEvent(sb, work.fork, 0)) != cudaSuccess) return e;
-    a.bin = b;
-    a.bin_list = work.bin_list + (size_t)b * work.cap;
-    a.tw = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
-    e = mix ? fd_launch_spec_mixed(N, a, nitems, num_sms, sb) : fd_launch_spec_fp64(N, a, nitems, num_sms, sb);
+  if (bank.NFFT > 1024) {
+    if ((e = cudaEventRecord(work.fork, stream)) != cudaSuccess) return e;
+    for (int b = kSpecAllBins; b < kNumBins; b++) {
+      int N = 32 << b;
+      if (N > bank.NFFT) break;
+      cudaStream_t sb = work.side[b];
+      if ((e = cudaStreamWaitEvent(sb, work.fork, 0)) != cudaSuccess) return e;
+      a.bin = b;
+      a.bin_list = work.bin_list + (size_t)b * work.cap;
+      a.tw = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
+      e = mix ? fd_launch_spec_mixed(N, a, nitems, num_sms, sb) : fd_launch_spec_fp64(N, a, nitems, num_sms, sb);
+      launches++;
+      if (e != cudaSuccess) return e;
+      if ((e = cudaEventRecord(work.join[b], sb)) != cudaSuccess) return e;
+      nb++;
+    }
+  }
+  if (nall > 0) {
+    SpecAllArgs A;
+    A.a = a;
+    A.a.bin = 0;
+    A.a.bin_list = work.bin_list;
+    A.a.tw = nullptr;
+    A.nbins = nall;
+    for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
+    e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream) : fd_launch_spec_all_fp64(A, num_sms, stream);
     launches++;
     if (e != cudaSuccess) return e;
-    if ((e = cudaEventRecord(work.join[b], sb)) != cudaSuccess) return e;
-    nb++;
   }
-  for (int b = 0; b < nb; b++)
+  for (int b = kSpecAllBins; b < kSpecAllBins + nb; b++)
     if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;
   if (nlaunch) *nlaunch = launches;
   return cudaSuccess;

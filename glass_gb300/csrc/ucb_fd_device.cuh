@@ -741,14 +741,131 @@ __device__ __forceinline__ df group_sum_df(float v, float2 *red, int lane) {
   return s;
 }
 
+// One unit of the spectral stage: GPC proposals of size N, one group of N/4
+// threads each, in a CTA of GPC N/4 threads.  Per proposal: the 4 A/E series
+// (from the slow kernel's scratch) are FFT'd in shared memory, weighted per bin
+// by the segment's TDI/whitening table and reduced to the residual power.
+// reds: 96 doubles of reduction scratch per group.
+template <int N, bool MIX, int GPC>
+__device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list, int count, int base,
+                                          const typename SpecSmem<N, MIX>::C *series,
+                                          const typename SpecSmem<N, MIX>::C *tw,
+                                          typename SpecSmem<N, MIX>::C *bufs, double *reds) {
+  using S = SpecSmem<N, MIX>;
+  using C = typename S::C;
+  constexpr int GT = N / 4, NSER = S::NSER, PASSES = S::PASSES;
+  constexpr int CH = MIX ? 4 : 2;
+  constexpr int B = N / GT;  // bins per thread (4)
+  const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
+  C *buf = bufs + (size_t)g * NSER * N;
+  double *red = reds + 96 * g;
+  const int NFFT = a.NFFT;
+  const int slot = base + g;
+  const bool valid = slot < count;
+  const int sl = valid ? slot : count - 1;
+  const int item = bin_list[sl];
+  int seg, imin;
+  if constexpr (MIX) {
+    seg = a.itemsmix[item].seg;
+    imin = a.itemsmix[item].imin;
+  } else {
+    seg = a.items64[item].seg;
+    imin = a.items64[item].imin;
+  }
+  const C *src = series + (size_t)sl * 4 * N;
+  float facc = 0.f, fh = 0.f, fc = 0.f;  // mixed: per-thread partial sums
+  double acc = 0.0, hacc = 0.0;
+#pragma unroll 1
+  for (int pass = 0; pass < PASSES; ++pass) {
+#pragma unroll
+    for (int s = 0; s < NSER; ++s)
+#pragma unroll
+      for (int r = 0; r < B; ++r) buf[s * N + lane + GT * r] = src[(size_t)(pass * NSER + s) * N + lane + GT * r];
+    group_sync<GT>();
+    group_fft<N, GT, NSER, (CH < NSER ? CH : NSER)>(buf, tw, lane);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      const int k = lane + GT * r;
+      const int m = (k + N / 2) & (N - 1);  // fftshift: output bin m holds FFT index m + N/2
+      const int j = imin + m;
+      if (j < 0 || j >= NFFT) continue;
+      const size_t sj = (size_t)seg * NFFT + j;
+      if constexpr (MIX) {
+        const float4 w = a.w32[sj];
+        const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
+        const float sh = a.itemsmix[item].amp_hi;
+        float2 HA = cadd(cmul(buf[0 * N + k], make_float2(gA.x, gA.y)), cmul(buf[1 * N + k], make_float2(gA.z, gA.w)));
+        float2 HE = cadd(cmul(buf[2 * N + k], make_float2(gE.x, gE.y)), cmul(buf[3 * N + k], make_float2(gE.z, gE.w)));
+        // template scaled by amp_hi (O(1) whitened values; the unscaled
+        // product would overflow FP32 when squared)
+        const float2 hA = cscale(HA, sh), hE = cscale(HE, sh);
+        const float4 wl = a.w32lo[sj];
+        const float ar = (w.x - hA.x) + wl.x, ai = (w.y - hA.y) + wl.y;
+        const float er = (w.z - hE.x) + wl.z, ei = (w.w - hE.y) + wl.w;
+        facc += fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei);
+        fh += fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y);
+        fc += fmaf(ar, hA.x, ai * hA.y) + fmaf(er, hE.x, ei * hE.y);
+      } else {
+        const double s = a.items64[item].amp_s;
+        // series (2 ch, 2 ch + 1) of this pass hold the A (chan 0) or E (chan 1) pair
+#pragma unroll
+        for (int ch = 0; ch < NSER / 2; ++ch) {
+          const int chan = pass * (NSER / 2) + ch;
+          const double2 w = a.w64[2 * sj + chan];
+          const double2 g2 = a.g64[4 * sj + 2 * chan], g1 = a.g64[4 * sj + 2 * chan + 1];
+          double2 h = cadd(cmul(buf[(2 * ch) * N + k], g2), cmul(buf[(2 * ch + 1) * N + k], g1));
+          h = cscale(h, s);
+          acc += 2.0 * (w.x * h.x + w.y * h.y) - (h.x * h.x + h.y * h.y);
+          hacc += h.x * h.x + h.y * h.y;
+        }
+      }
+    }
+    group_sync<GT>();
+  }
+  double corr = 0.0;
+  if constexpr (MIX) {
+    float2 *redf = reinterpret_cast<float2 *>(red);
+    df sa = group_sum_df<GT>(facc, redf, lane);
+    df sh = group_sum_df<GT>(fh, redf + 32, lane);
+    df sc = group_sum_df<GT>(fc, redf + 64, lane);
+    acc = (double)sa.hi + (double)sa.lo;
+    hacc = (double)sh.hi + (double)sh.lo;
+    corr = (double)sc.hi + (double)sc.lo;
+  } else {
+    acc = group_sum<GT>(acc, red, lane);
+    hacc = group_sum<GT>(hacc, red + 32, lane);
+  }
+  if (valid && lane == 0) {
+    double term, hh;
+    if constexpr (MIX) {
+      const ItemMix &c = a.itemsmix[item];
+      int jlo = imin < 0 ? 0 : imin;
+      int jhi = imin + N > NFFT ? NFFT : imin + N;
+      const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
+      // sum |w - s H|^2 with s = amp_hi (1 + rho), rho = amp_lo/amp_hi: with
+      // d = w - amp_hi H, |w - s H|^2 = |d|^2 - 2 rho Re(d* amp_hi H) + O(rho^2)
+      const double rho = (double)c.amp_lo / (double)c.amp_hi;
+      term = (Qs[jhi] - Qs[jlo]) - acc + 2.0 * rho * corr;
+      hh = 2.0 * (1.0 + rho) * (1.0 + rho) * hacc;
+    } else {
+      term = acc;
+      hh = 2.0 * hacc;
+    }
+    const double tx = a.term_x ? a.term_x[item] : 0.0;
+    a.dlogl[item] = term - tx;
+    if (a.term_y) a.term_y[item] = term;
+    if (a.hh) a.hh[item] = hh;
+    if (a.status) a.status[item] = isfinite(term) ? 0 : 1;
+  }
+  if constexpr (GT > 32) __syncthreads();
+}
+
 template <int N, bool MIX>
 __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   using Cfg = SpecCfg<N>;
   using S = SpecSmem<N, MIX>;
   using C = typename S::C;
-  constexpr int GT = Cfg::GT, GPC = Cfg::GPC, NSER = S::NSER, PASSES = S::PASSES;
-  constexpr int CH = MIX ? 4 : 2;
-  constexpr int B = N / GT;  // bins per thread (4)
+  constexpr int GPC = Cfg::GPC, NSER = S::NSER;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *bufs = tw + N;
@@ -757,113 +874,97 @@ __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   const C *twg = reinterpret_cast<const C *>(a.tw);
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
   __syncthreads();
-
-  const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
-  C *buf = bufs + (size_t)g * NSER * N;
   const int count = a.bin_count[a.bin];
   const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, a.bin) * 4;
-  const int NFFT = a.NFFT;
+  for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC)
+    spec_unit<N, MIX, GPC>(a, a.bin_list, count, base, series, tw, bufs, red);
+}
 
-  for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC) {
-    const int slot = base + g;
-    const bool valid = slot < count;
-    const int sl = valid ? slot : count - 1;
-    const int item = a.bin_list[sl];
-    int seg, imin;
-    if constexpr (MIX) {
-      seg = a.itemsmix[item].seg;
-      imin = a.itemsmix[item].imin;
-    } else {
-      seg = a.items64[item].seg;
-      imin = a.items64[item].imin;
-    }
-    const C *src = series + (size_t)sl * 4 * N;
-    float facc = 0.f, fh = 0.f, fc = 0.f;  // mixed: per-thread partial sums
-    double acc = 0.0, hacc = 0.0;
-#pragma unroll 1
-    for (int pass = 0; pass < PASSES; ++pass) {
+// All sizes up to 1024 in one launch: a persistent grid of 256-thread CTAs
+// walks the units (GPC = 1024/N proposals of one size each), largest sizes
+// first so that the long units start early; a CTA reloads the twiddles when
+// it changes size.  Shared memory: twiddles for 1024 points, 4 x 1024 series
+// values and four groups' reduction scratch, whatever the size.
+constexpr int kSpecAllThreads = 256;
+constexpr int kSpecAllBins = 6;  // N = 32 .. 1024
+
+template <bool MIX>
+struct SpecAllSmem {
+  using C = typename std::conditional<MIX, float2, double2>::type;
+  static constexpr size_t bytes = sizeof(C) * (1024 + 4 * 1024) + sizeof(double) * 96 * 4;
+};
+
+struct SpecAllArgs {
+  SpecArgs a;                    // a.bin_list: all sizes' lists, stride cap; a.tw unused
+  const void *tw[kSpecAllBins];  // twiddles per size
+  int nbins;                     // sizes 32 << b for b < nbins
+};
+
+template <bool MIX>
+__global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAllArgs A) {
+  using C = typename SpecAllSmem<MIX>::C;
+  const SpecArgs &a = A.a;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *tw = reinterpret_cast<C *>(smem_raw);
+  C *bufs = tw + 1024;
+  double *reds = reinterpret_cast<double *>(bufs + 4 * 1024);
+  int ustart[kSpecAllBins + 1];  // in largest-first order
+  int total = 0;
 #pragma unroll
-      for (int s = 0; s < NSER; ++s)
-#pragma unroll
-        for (int r = 0; r < B; ++r) buf[s * N + lane + GT * r] = src[(size_t)(pass * NSER + s) * N + lane + GT * r];
-      group_sync<GT>();
-      group_fft<N, GT, NSER, (CH < NSER ? CH : NSER)>(buf, tw, lane);
-#pragma unroll
-      for (int r = 0; r < B; ++r) {
-        const int k = lane + GT * r;
-        const int m = (k + N / 2) & (N - 1);  // fftshift: output bin m holds FFT index m + N/2
-        const int j = imin + m;
-        if (j < 0 || j >= NFFT) continue;
-        const size_t sj = (size_t)seg * NFFT + j;
-        if constexpr (MIX) {
-          const float4 w = a.w32[sj];
-          const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
-          const float sh = a.itemsmix[item].amp_hi;
-          float2 HA = cadd(cmul(buf[0 * N + k], make_float2(gA.x, gA.y)), cmul(buf[1 * N + k], make_float2(gA.z, gA.w)));
-          float2 HE = cadd(cmul(buf[2 * N + k], make_float2(gE.x, gE.y)), cmul(buf[3 * N + k], make_float2(gE.z, gE.w)));
-          // template scaled by amp_hi (O(1) whitened values; the unscaled
-          // product would overflow FP32 when squared)
-          const float2 hA = cscale(HA, sh), hE = cscale(HE, sh);
-          const float4 wl = a.w32lo[sj];
-          const float ar = (w.x - hA.x) + wl.x, ai = (w.y - hA.y) + wl.y;
-          const float er = (w.z - hE.x) + wl.z, ei = (w.w - hE.y) + wl.w;
-          facc += fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei);
-          fh += fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y);
-          fc += fmaf(ar, hA.x, ai * hA.y) + fmaf(er, hE.x, ei * hE.y);
-        } else {
-          const double s = a.items64[item].amp_s;
-          // series (2 ch, 2 ch + 1) of this pass hold the A (chan 0) or E (chan 1) pair
-#pragma unroll
-          for (int ch = 0; ch < NSER / 2; ++ch) {
-            const int chan = pass * (NSER / 2) + ch;
-            const double2 w = a.w64[2 * sj + chan];
-            const double2 g2 = a.g64[4 * sj + 2 * chan], g1 = a.g64[4 * sj + 2 * chan + 1];
-            double2 h = cadd(cmul(buf[(2 * ch) * N + k], g2), cmul(buf[(2 * ch + 1) * N + k], g1));
-            h = cscale(h, s);
-            acc += 2.0 * (w.x * h.x + w.y * h.y) - (h.x * h.x + h.y * h.y);
-            hacc += h.x * h.x + h.y * h.y;
-          }
-        }
-      }
-      group_sync<GT>();
+  for (int q = 0; q < kSpecAllBins; q++) {
+    const int b = kSpecAllBins - 1 - q;
+    ustart[q] = total;
+    if (b < A.nbins) {
+      const int gpc = 32 >> b;
+      total += (a.bin_count[b] + gpc - 1) / gpc;
     }
-    double corr = 0.0;
-    if constexpr (MIX) {
-      float2 *redf = reinterpret_cast<float2 *>(red);
-      df sa = group_sum_df<GT>(facc, redf, lane);
-      df sh = group_sum_df<GT>(fh, redf + 32, lane);
-      df sc = group_sum_df<GT>(fc, redf + 64, lane);
-      acc = (double)sa.hi + (double)sa.lo;
-      hacc = (double)sh.hi + (double)sh.lo;
-      corr = (double)sc.hi + (double)sc.lo;
-    } else {
-      acc = group_sum<GT>(acc, red, lane);
-      hacc = group_sum<GT>(hacc, red + 32, lane);
-    }
-    if (valid && lane == 0) {
-      double term, hh;
-      if constexpr (MIX) {
-        const ItemMix &c = a.itemsmix[item];
-        int jlo = imin < 0 ? 0 : imin;
-        int jhi = imin + N > NFFT ? NFFT : imin + N;
-        const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
-        // sum |w - s H|^2 with s = amp_hi (1 + rho), rho = amp_lo/amp_hi: with
-        // d = w - amp_hi H, |w - s H|^2 = |d|^2 - 2 rho Re(d* amp_hi H) + O(rho^2)
-        const double rho = (double)c.amp_lo / (double)c.amp_hi;
-        term = (Qs[jhi] - Qs[jlo]) - acc + 2.0 * rho * corr;
-        hh = 2.0 * (1.0 + rho) * (1.0 + rho) * hacc;
-      } else {
-        term = acc;
-        hh = 2.0 * hacc;
-      }
-      const double tx = a.term_x ? a.term_x[item] : 0.0;
-      a.dlogl[item] = term - tx;
-      if (a.term_y) a.term_y[item] = term;
-      if (a.hh) a.hh[item] = hh;
-      if (a.status) a.status[item] = isfinite(term) ? 0 : 1;
-    }
-    if constexpr (GT > 32) __syncthreads();
   }
+  ustart[kSpecAllBins] = total;
+  int cur = -1;
+  for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
+    int q = 0;
+#pragma unroll
+    for (int qq = 1; qq < kSpecAllBins; qq++)
+      if (unit >= ustart[qq]) q = qq;
+    const int b = kSpecAllBins - 1 - q;
+    const int N = 32 << b;
+    if (b != cur) {
+      __syncthreads();
+      const C *twg = reinterpret_cast<const C *>(A.tw[b]);
+      for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
+      __syncthreads();
+      cur = b;
+    }
+    const int gpc = 32 >> b;
+    const int base = (unit - ustart[q]) * gpc;
+    const int count = a.bin_count[b];
+    const int *bl = a.bin_list + (size_t)b * a.cap;
+    const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, b) * 4;
+    switch (b) {
+      case 0: spec_unit<32, MIX, 32>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 1: spec_unit<64, MIX, 16>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 2: spec_unit<128, MIX, 8>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 3: spec_unit<256, MIX, 4>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 4: spec_unit<512, MIX, 2>(a, bl, count, base, series, tw, bufs, reds); break;
+      default: spec_unit<1024, MIX, 1>(a, bl, count, base, series, tw, bufs, reds); break;
+    }
+  }
+}
+
+template <bool MIX>
+static cudaError_t launch_spec_all(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
+  const size_t smem = SpecAllSmem<MIX>::bytes;
+  static int occ = -1;
+  if (occ < 0) {
+    cudaError_t e =
+        cudaFuncSetAttribute(fd_spec_all_kernel<MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_all_kernel<MIX>, kSpecAllThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (occ < 1) occ = 1;
+  }
+  fd_spec_all_kernel<MIX><<<occ * num_sms, kSpecAllThreads, smem, stream>>>(A);
+  return cudaGetLastError();
 }
 
 // Launch of one size's kernel with a grid bounded by the SM count times the

@@ -21,4 +21,8 @@ cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sm
   return cudaErrorInvalidValue;
 }
 
+cudaError_t fd_launch_spec_all_fp64(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
+  return launch_spec_all<false>(A, num_sms, stream);
+}
+
 }  // namespace glass

@@ -21,4 +21,8 @@ cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_s
   return cudaErrorInvalidValue;
 }
 
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
+  return launch_spec_all<true>(A, num_sms, stream);
+}
+
 }  // namespace glass
