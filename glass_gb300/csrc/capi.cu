@@ -301,7 +301,9 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   GLASS_CUDA(cudaMalloc(&w.items64, sizeof(ItemF64) * (size_t)cap), "cudaMalloc(items64)");
   GLASS_CUDA(cudaMalloc(&w.itemsmix, sizeof(ItemMix) * (size_t)cap), "cudaMalloc(itemsmix)");
   GLASS_CUDA(cudaMalloc(&w.itemsgrad, sizeof(ItemGrad) * (size_t)cap), "cudaMalloc(itemsgrad)");
-  GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * kNumBins), "cudaMalloc(bin_count)");
+  GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * (kNumBins + 1)), "cudaMalloc(bin_count)");
+  GLASS_CUDA(cudaMemset(w.bin_count, 0, sizeof(int) * (kNumBins + 1)), "cudaMemset(bin_count)");
+  w.counts_zero = true;
   GLASS_CUDA(cudaMalloc(&w.bin_list, sizeof(int) * (size_t)kNumBins * cap), "cudaMalloc(bin_list)");
   GLASS_CUDA(cudaMalloc(&w.series, series), "cudaMalloc(series)");
   w.cap = cap;

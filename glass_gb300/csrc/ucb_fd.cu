@@ -378,8 +378,11 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   cudaError_t e;
   int launches = 0;
   const bool mix = precision == 1;
-  e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kNumBins, stream);
-  if (e != cudaSuccess) return e;
+  if (!work.counts_zero) {
+    e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream);
+    if (e != cudaSuccess) return e;
+  }
+  work.counts_zero = false;  // until this sequence has been enqueued in full
   PlanArgs pa;
   pa.nitems = nitems;
   pa.nseg = bank.nseg;
@@ -479,6 +482,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.a.bin_list = work.bin_list;
     A.a.tw = nullptr;
     A.nbins = nall;
+    A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
     for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
     e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream) : fd_launch_spec_all_fp64(A, num_sms, stream);
     launches++;
@@ -486,6 +490,10 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   }
   for (int b = kSpecAllBins; b < kSpecAllBins + nb; b++)
     if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;
+  if (nb > 0 || nall == 0) {
+    if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream)) != cudaSuccess) return e;
+  }
+  work.counts_zero = true;
   if (nlaunch) *nlaunch = launches;
   return cudaSuccess;
 }

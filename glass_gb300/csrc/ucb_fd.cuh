@@ -42,8 +42,12 @@ struct FdWorkDev {
   ItemF64 *items64 = nullptr;   // [cap]
   ItemMix *itemsmix = nullptr;  // [cap]
   ItemGrad *itemsgrad = nullptr;  // [cap]
-  int *bin_count = nullptr;     // [kNumBins]
+  int *bin_count = nullptr;     // [kNumBins + 1]: per-size counts, then a CTA-done counter
   int *bin_list = nullptr;      // [kNumBins*cap]
+  // every launch sequence leaves the counts at zero (the spectral kernel's last
+  // CTA, or a trailing memset), so the next one needs no leading memset; false
+  // when that is not known (a launch returned an error part-way)
+  bool counts_zero = false;
   void *series = nullptr;       // 4 arm-combination series per proposal
 };
 

@@ -898,6 +898,8 @@ struct SpecAllArgs {
   SpecArgs a;                    // a.bin_list: all sizes' lists, stride cap; a.tw unused
   const void *tw[kSpecAllBins];  // twiddles per size
   int nbins;                     // sizes 32 << b for b < nbins
+  int *zero_counts;              // non-null: the last CTA to finish zeroes the kNumBins
+                                 // counts there and the done counter after them
 };
 
 template <bool MIX>
@@ -947,6 +949,19 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
       case 3: spec_unit<256, MIX, 4>(a, bl, count, base, series, tw, bufs, reds); break;
       case 4: spec_unit<512, MIX, 2>(a, bl, count, base, series, tw, bufs, reds); break;
       default: spec_unit<1024, MIX, 1>(a, bl, count, base, series, tw, bufs, reds); break;
+    }
+  }
+  if (A.zero_counts) {
+    // leave the counts at zero for the next launch sequence: every CTA has
+    // read them for the last time once it gets here
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (atomicAdd(&A.zero_counts[kNumBins], 1) == (int)gridDim.x - 1) {
+#pragma unroll
+        for (int b = 0; b <= kNumBins; b++) A.zero_counts[b] = 0;
+        __threadfence();
+      }
     }
   }
 }

@@ -459,7 +459,9 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
                            int *nlaunch) {
   cudaError_t e;
   int launches = 0;
-  if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kNumBins, stream)) != cudaSuccess) return e;
+  if (!work.counts_zero && (e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream)) != cudaSuccess)
+    return e;
+  work.counts_zero = false;
   GradPlanArgs ga;
   PlanArgs &pa = ga.base;
   pa.nitems = nitems;
@@ -539,6 +541,9 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
   }
   for (int b = 0; b < nb; b++)
     if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;
+  // leave the counts at zero for the next launch sequence
+  if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream)) != cudaSuccess) return e;
+  work.counts_zero = true;
   if (nlaunch) *nlaunch = launches;
   return cudaSuccess;
 }
