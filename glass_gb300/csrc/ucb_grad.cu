@@ -121,17 +121,8 @@ __global__ void __launch_bounds__(64) fd_plangrad_kernel(GradPlanArgs ga) {
   plan_bin(a, i, b);
 }
 
-// Combination coefficients of the four A/E series per directed arm
-// (12, 13, 21, 23, 31, 32): a2, a1, e2, e1 (see ae_combos).
-__constant__ float kComboCoef[4][6] = {
-    {-1.f, 1.f, 0.f, 0.f, 1.f, -1.f},  // a2 = d31 - d32 - d12 + d13
-    {0.f, 1.f, -1.f, -1.f, 1.f, 0.f},  // a1 = d13 - d23 - d21 + d31
-    {1.f, -1.f, 2.f, -2.f, 1.f, -1.f}, // e2 = d12 - d13 + 2 d21 - 2 d23 + d31 - d32
-    {2.f, 1.f, 1.f, -1.f, -1.f, -2.f}, // e1 = 2 d12 + d13 + d21 - d23 - d31 - 2 d32
-};
-
 struct GradConsts {
-  float Rf, invLf, AUcf, invTf, AUf;
+  float Rf, invLf, AUcf, invTf, AUf, Tf;
 };
 
 // One sample n of one proposal: the 6 templates' arm values combined into
@@ -174,39 +165,59 @@ __device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad 
     aev[i] = fmaf(c.aef, v, 1.0f);
     arg2[i] = psi0 - c.w0c * kdx + c.p7pi * tT * (tT - 2.0f * uf);
     // d arg2 / d xi and d tau / d(cos theta), d tau / d phi
-    wxi[i] = 6.2831853f * fmaf(g.fdot, v / K.invTf, g.f0);
+    wxi[i] = 6.2831853f * fmaf(g.fdot, v * K.Tf, g.f0);
     const float X = gx + dx[i], Y = gy + dy[i], Z = dz[i];
     dtc[i] = (g.dk_c[0] * X + g.dk_c[1] * Y + g.dk_c[2] * Z) * (float)(1.0 / kCLIGHT);
     dtp[i] = (g.dk_p[0] * X + g.dk_p[1] * Y + g.dk_p[2] * Z) * (float)(1.0 / kCLIGHT);
   }
-  // unique arms 12, 13, 23
-  float r[3][3];
+  // unique arms 12, 13, 23: the six quadratic forms share the monomials of the
+  // arm's unit vector; the two directions of an arm differ only in k.r's sign
+  float qf[3][6], krq[3], dkcq[3], dkpq[3];
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     const int i0 = q == 2 ? 1 : 0, i1 = q == 0 ? 1 : 2;
-    r[q][0] = (dx[i1] - dx[i0]) * K.invLf;
-    r[q][1] = (dy[i1] - dy[i0]) * K.invLf;
-    r[q][2] = (dz[i1] - dz[i0]) * K.invLf;
+    const float rx = (dx[i1] - dx[i0]) * K.invLf, ry = (dy[i1] - dy[i0]) * K.invLf, rz = (dz[i1] - dz[i0]) * K.invLf;
+    const float m0 = rx * rx, m3 = ry * ry, m5 = rz * rz;
+    const float m1 = 2.f * rx * ry, m2 = 2.f * rx * rz, m4 = 2.f * ry * rz;
+    const float *E[6] = {g.ep, g.ec, g.dep_c, g.dec_c, g.dep_p, g.dec_p};
+#pragma unroll
+    for (int t = 0; t < 6; t++)
+      qf[q][t] = fmaf(E[t][0], m0, fmaf(E[t][3], m3, fmaf(E[t][5], m5, fmaf(E[t][1], m1, fmaf(E[t][2], m2, E[t][4] * m4)))));
+    krq[q] = c.k[0] * rx + c.k[1] * ry + c.k[2] * rz;
+    dkcq[q] = g.dk_c[0] * rx + g.dk_c[1] * ry + g.dk_c[2] * rz;
+    dkpq[q] = g.dk_p[0] * rx + g.dk_p[1] * ry + g.dk_p[2] * rz;
   }
 #pragma unroll
   for (int s = 0; s < kGradSeries; s++) accs[s] = make_float2(0.f, 0.f);
 
-  const float invfsT = K.invTf / g.fstar;
-  const float f0T = g.f0 / K.invTf;  // f0 T
+  // combination coefficients of the four A/E series per directed arm
+  // (12, 13, 21, 23, 31, 32): a2, a1, e2, e1 (as ae_combos); compile-time
+  // constants, so the zero terms vanish
+  constexpr float kC[4][6] = {
+      {-1.f, 1.f, 0.f, 0.f, 1.f, -1.f},   // a2 = d31 - d32 - d12 + d13
+      {0.f, 1.f, -1.f, -1.f, 1.f, 0.f},   // a1 = d13 - d23 - d21 + d31
+      {1.f, -1.f, 2.f, -2.f, 1.f, -1.f},  // e2 = d12 - d13 + 2 d21 - 2 d23 + d31 - d32
+      {2.f, 1.f, 1.f, -1.f, -1.f, -2.f},  // e1 = 2 d12 + d13 + d21 - d23 - d31 - 2 d32
+  };
+  const float invfsT = __fdividef(K.invTf, g.fstar);
+  const float f0T = g.f0 * K.Tf;  // f0 T
+  // 1 / (f0 T aevol_i) per spacecraft, for the amplitude-evolution derivatives
+  float rfa[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) rfa[i] = __frcp_rn(f0T * aev[i]);
 #pragma unroll
   for (int arm = 0; arm < 6; arm++) {
     // directed arm -> (spacecraft i, unique arm q, orientation sign)
     const int i = arm >> 1;
     const int q = (arm == 0 || arm == 2) ? 0 : (arm == 1 || arm == 4) ? 1 : 2;
     const float sg = (arm == 2 || arm == 4 || arm == 5) ? -1.f : 1.f;
-    const float rx = r[q][0], ry = r[q][1], rz = r[q][2];
-    const float dp = quad(g.ep, rx, ry, rz), dc = quad(g.ec, rx, ry, rz);
-    const float kr = sg * (c.k[0] * rx + c.k[1] * ry + c.k[2] * rz);
-    const float dkr_c = sg * (g.dk_c[0] * rx + g.dk_c[1] * ry + g.dk_c[2] * rz);
-    const float dkr_p = sg * (g.dk_p[0] * rx + g.dk_p[1] * ry + g.dk_p[2] * rz);
+    const float dp = qf[q][0], dc = qf[q][1];
+    const float kr = sg * krq[q];
+    const float dkr_c = sg * dkcq[q];
+    const float dkr_p = sg * dkpq[q];
     const float arg1 = 0.5f * fon[i] * (1.0f + kr);
     const float sn = sinc_f(arg1);
-    const float gS = dsinc_f(arg1) / sn;
+    const float gS = __fdividef(dsinc_f(arg1), sn);
     const float S = 0.25f * sn * aev[i];
     float sth, cth;
     fast_sincos(arg1 - arg2[i], &sth, &cth);
@@ -219,23 +230,23 @@ __device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad 
     // f0 (params[0] = f0 T)
     const float dA1_0 = 0.5f * (1.0f + kr) * invfsT;
     const float dth_0 = dA1_0 - 6.2831853f * vv[i];
-    const float dlS_0 = gS * dA1_0 - c.aef * vv[i] / (f0T * aev[i]);
+    const float dlS_0 = gS * dA1_0 - c.aef * vv[i] * rfa[i];
     const float2 T0 = cmul(d, make_float2(dlS_0, -dth_0));
     // fdot (params[7] = fdot T^2)
     const float dA1_7 = dA1_0 * vv[i];
     const float dth_7 = dA1_7 - 3.14159265f * vv[i] * vv[i];
-    const float dlS_7 = gS * dA1_7 + 0.6666667f * vv[i] / (f0T * aev[i]);
+    const float dlS_7 = gS * dA1_7 + 0.6666667f * vv[i] * rfa[i];
     const float2 T7 = cmul(d, make_float2(dlS_7, -dth_7));
     // cos(theta)
     const float dA1_c = 0.5f * fon[i] * dkr_c;
     const float dth_c = dA1_c + wxi[i] * dtc[i];
-    const float dpc = quad(g.dep_c, rx, ry, rz), dcc = quad(g.dec_c, rx, ry, rz);
+    const float dpc = qf[q][2], dcc = qf[q][3];
     const float2 dPc = make_float2(g.DP[0] * dpc + g.DC[0] * dcc, g.DP[1] * dpc + g.DC[1] * dcc);
     const float2 Tc = cadd(cmul(d, make_float2(gS * dA1_c, -dth_c)), cmul(dPc, SE));
     // phi
     const float dA1_p = 0.5f * fon[i] * dkr_p;
     const float dth_p = dA1_p + wxi[i] * dtp[i];
-    const float dpp = quad(g.dep_p, rx, ry, rz), dcp = quad(g.dec_p, rx, ry, rz);
+    const float dpp = qf[q][4], dcp = qf[q][5];
     const float2 dPp = make_float2(g.DP[0] * dpp + g.DC[0] * dcp, g.DP[1] * dpp + g.DC[1] * dcp);
     const float2 Tp = cadd(cmul(d, make_float2(gS * dA1_p, -dth_p)), cmul(dPp, SE));
     const float2 vals[kGradTemplates] = {Bp, Bx, T0, T7, Tc, Tp};
@@ -243,9 +254,17 @@ __device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad 
     for (int t = 0; t < kGradTemplates; t++)
 #pragma unroll
       for (int s = 0; s < 4; s++) {
-        const float cf = kComboCoef[s][arm];
-        accs[4 * t + s].x = fmaf(cf, vals[t].x, accs[4 * t + s].x);
-        accs[4 * t + s].y = fmaf(cf, vals[t].y, accs[4 * t + s].y);
+        const float cf = kC[s][arm];
+        if (cf == 1.f) {
+          accs[4 * t + s].x += vals[t].x;
+          accs[4 * t + s].y += vals[t].y;
+        } else if (cf == -1.f) {
+          accs[4 * t + s].x -= vals[t].x;
+          accs[4 * t + s].y -= vals[t].y;
+        } else if (cf != 0.f) {
+          accs[4 * t + s].x = fmaf(cf, vals[t].x, accs[4 * t + s].x);
+          accs[4 * t + s].y = fmaf(cf, vals[t].y, accs[4 * t + s].y);
+        }
       }
   }
 }
@@ -505,6 +524,7 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
   a.K.AUcf = (float)(kAU / kCLIGHT);
   a.K.invTf = (float)(1.0 / bank.T);
   a.K.AUf = (float)kAU;
+  a.K.Tf = (float)bank.T;
   a.w32 = bank.w32;
   a.w32lo = bank.w32lo;
   a.g32 = bank.g32;
