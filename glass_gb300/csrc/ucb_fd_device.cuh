@@ -69,6 +69,18 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
 #pragma unroll
   for (int st = 0; st < NR4; ++st) {
     const int step = N / (4 * p);
+    // the thread's butterfly twiddles, shared by every series (all 1 in the
+    // first stage)
+    C w[B4][3];
+    if (st > 0) {
+#pragma unroll
+      for (int b = 0; b < B4; ++b) {
+        const int k = (lane + GT * b) & (p - 1);
+        w[b][0] = tw[k * step];
+        w[b][1] = tw[2 * k * step];
+        w[b][2] = tw[3 * k * step];
+      }
+    }
 #pragma unroll
     for (int c0 = 0; c0 < NSER; c0 += CH) {
       C v[CH][B4][4];
@@ -88,9 +100,9 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
           int i = lane + GT * b;
           int k = i & (p - 1);
           C u0 = v[s][b][0];
-          C u1 = cmul(v[s][b][1], tw[k * step]);
-          C u2 = cmul(v[s][b][2], tw[2 * k * step]);
-          C u3 = cmul(v[s][b][3], tw[3 * k * step]);
+          C u1 = st > 0 ? cmul(v[s][b][1], w[b][0]) : v[s][b][1];
+          C u2 = st > 0 ? cmul(v[s][b][2], w[b][1]) : v[s][b][2];
+          C u3 = st > 0 ? cmul(v[s][b][3], w[b][2]) : v[s][b][3];
           C a = cadd(u0, u2), bb = csub(u0, u2), c = cadd(u1, u3), d = cmi(csub(u1, u3));
           int j = (i - k) * 4 + k;
           C *o = buf + (c0 + s) * N + j;
@@ -106,6 +118,9 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
   if constexpr (LOG & 1) {
     constexpr int B2 = N / 2 / GT;
     const int step = N / (2 * p);
+    C w[B2];
+#pragma unroll
+    for (int b = 0; b < B2; ++b) w[b] = tw[((lane + GT * b) & (p - 1)) * step];
 #pragma unroll
     for (int c0 = 0; c0 < NSER; c0 += CH) {
       C v[CH][B2][2];
@@ -124,7 +139,7 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
         for (int b = 0; b < B2; ++b) {
           int i = lane + GT * b;
           int k = i & (p - 1);
-          C u1 = cmul(v[s][b][1], tw[k * step]);
+          C u1 = cmul(v[s][b][1], w[b]);
           int j = (i - k) * 2 + k;
           buf[(c0 + s) * N + j] = cadd(v[s][b][0], u1);
           buf[(c0 + s) * N + j + p] = csub(v[s][b][0], u1);
