@@ -31,7 +31,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 # and add by up to ~1e-10 rad there, so contraction is off for them.
 PER_FILE_FLAGS = {"ucb_fd.cu": ["-fmad=false"], "ucb_fd_fp64.cu": ["-fmad=false"],
                   "wdm.cu": ["-Xcompiler", "-ffp-contract=off"],
-                  "ucb_wavelet.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
+                  "ucb_wavelet.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+                  "capi.cu": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:

@@ -5,12 +5,14 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/glass_gb300.h"
 #include "ucb_fd.cuh"
+#include "ucb_fd_device.cuh"
 #include "ucb_wavelet.cuh"
 #include "wdm.cuh"
 
@@ -470,18 +472,25 @@ struct LegacyThread {
   int device = 0;
   cudaStream_t stream = nullptr;
   FdTablesDev tab;  // twiddles only
-  OrbitSample64 *h_pos = nullptr, *d_pos = nullptr;
-  double *h_out = nullptr, *d_out = nullptr, *d_params = nullptr, *h_params = nullptr;
+  // staging: [ItemF64][OrbitSample64 x kMaxN] in, 10 kMaxN doubles out
+  unsigned char *h_in = nullptr, *d_in = nullptr;
+  double *h_out = nullptr, *d_out = nullptr;
+  double2 *d_d6 = nullptr;
+  // one CUDA graph per (size, format, channel count): copy in, three kernels, copy out
+  std::map<std::pair<int, double>, cudaGraphExec_t> graphs;
+  ItemF64 *h_item() { return reinterpret_cast<ItemF64 *>(h_in); }
+  OrbitSample64 *h_pos() { return reinterpret_cast<OrbitSample64 *>(h_in + kPosOffset); }
+  static constexpr size_t kPosOffset = (sizeof(ItemF64) + 255) / 256 * 256;
   ~LegacyThread() {
     if (!init) return;
     cudaSetDevice(device);
     cudaStreamSynchronize(stream);
-    cudaFreeHost(h_pos);
+    for (auto &g : graphs) cudaGraphExecDestroy(g.second);
+    cudaFreeHost(h_in);
     cudaFreeHost(h_out);
-    cudaFreeHost(h_params);
-    cudaFree(d_pos);
+    cudaFree(d_in);
     cudaFree(d_out);
-    cudaFree(d_params);
+    cudaFree(d_d6);
     cudaFree(tab.base);
     cudaStreamDestroy(stream);
   }
@@ -499,17 +508,16 @@ static int legacy_init() {
   GLASS_CUDA(cudaSetDevice(L.device), "cudaSetDevice");
   GLASS_CUDA(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "cudaStreamCreate");
   GLASS_CUDA(fd_build_orbit_tables(L.tab, 31457280.0, 0.0, L.stream), "twiddle tables");
-  GLASS_CUDA(cudaMallocHost(&L.h_pos, sizeof(OrbitSample64) * kMaxN), "cudaMallocHost");
+  const size_t in_bytes = LegacyThread::kPosOffset + sizeof(OrbitSample64) * kMaxN;
+  GLASS_CUDA(cudaMallocHost(&L.h_in, in_bytes), "cudaMallocHost");
   GLASS_CUDA(cudaMallocHost(&L.h_out, sizeof(double) * 10 * kMaxN), "cudaMallocHost");
-  GLASS_CUDA(cudaMallocHost(&L.h_params, sizeof(double) * 16), "cudaMallocHost");
-  GLASS_CUDA(cudaMalloc(&L.d_pos, sizeof(OrbitSample64) * kMaxN), "cudaMalloc");
+  GLASS_CUDA(cudaMalloc(&L.d_in, in_bytes), "cudaMalloc");
   GLASS_CUDA(cudaMalloc(&L.d_out, sizeof(double) * 10 * kMaxN), "cudaMalloc");
-  GLASS_CUDA(cudaMalloc(&L.d_params, sizeof(double) * 16), "cudaMalloc");
+  GLASS_CUDA(cudaMalloc(&L.d_d6, sizeof(double2) * 6 * kMaxN), "cudaMalloc");
   GLASS_CUDA(cudaStreamSynchronize(L.stream), "init sync");
   L.init = true;
   return GLASS_OK;
 }
-
 
 static int bin_index(int N) {
   int b = 0;
@@ -517,20 +525,55 @@ static int bin_index(int N) {
   return b;
 }
 
-// Shared body of the two waveform entry points; positions already in g_legacy.h_pos.
+// Enqueue one drop-in waveform: inputs staged in h_in, outputs to h_out.
+static cudaError_t legacy_enqueue(LegacyThread &L, int fmt, double T, int BW, int NI, size_t nout) {
+  cudaStream_t s = L.stream;
+  const size_t in_bytes = LegacyThread::kPosOffset + sizeof(OrbitSample64) * BW;
+  cudaError_t e = cudaMemcpyAsync(L.d_in, L.h_in, in_bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  e = fd_waveform_launch(reinterpret_cast<const OrbitSample64 *>(L.d_in + LegacyThread::kPosOffset),
+                         reinterpret_cast<const ItemF64 *>(L.d_in), BW, fmt, NI, T, fstar_of_orbit(), L.d_d6, L.d_out,
+                         L.tab.tw64[bin_index(BW)], s);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(L.h_out, L.d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, s);
+}
+
+// Shared body of the two waveform entry points; positions already in g_legacy.h_pos().
+// The first call for a (size, format, channels) runs directly and records a
+// CUDA graph of the sequence; later calls replay it (one launch instead of six
+// API calls).  T is a kernel argument, so it is part of the key.
 static int legacy_waveform_run(int fmt, double T, const double *params, int NParams, double *X, double *Y, double *Z,
                                double *A, double *E, int BW, int NI) {
   LegacyThread &L = g_legacy;
-  for (int k = 0; k < 8; k++) L.h_params[k] = k < NParams ? params[k] : 0.0;
-  cudaStream_t s = L.stream;
-  GLASS_CUDA(cudaMemcpyAsync(L.d_pos, L.h_pos, sizeof(OrbitSample64) * BW, cudaMemcpyHostToDevice, s), "H2D pos");
-  GLASS_CUDA(cudaMemcpyAsync(L.d_params, L.h_params, sizeof(double) * 8, cudaMemcpyHostToDevice, s), "H2D params");
-  GLASS_CUDA(fd_waveform_launch(L.d_pos, L.d_params, NParams, BW, fmt, NI, T, fstar_of_orbit(), L.d_out,
-                                L.tab.tw64[bin_index(BW)], s),
-             "ucb_waveform launch");
+  double p[8];
+  for (int k = 0; k < 8; k++) p[k] = k < NParams ? params[k] : 0.0;
+  // the source's constants on the host: the same FP64 code the batched
+  // plan kernels run, with the reference's operation order
+  SourceGeom geo;
+  source_geometry(p, NParams, T, geo);
+  make_item_f64(geo, BW, *L.h_item());
   bool all = (fmt == GLASS_FMT_SANGRIA) || NI > 1;
   size_t nout = all ? 10 * (size_t)BW : 2 * (size_t)BW;
-  GLASS_CUDA(cudaMemcpyAsync(L.h_out, L.d_out, sizeof(double) * nout, cudaMemcpyDeviceToHost, s), "D2H waveform");
+  cudaStream_t s = L.stream;
+  const std::pair<int, double> key((bin_index(BW) * 4 + fmt) * 2 + (all ? 1 : 0), T);
+  auto it = L.graphs.find(key);
+  if (it != L.graphs.end()) {
+    GLASS_CUDA(cudaGraphLaunch(it->second, s), "ucb_waveform graph launch");
+  } else {
+    GLASS_CUDA(legacy_enqueue(L, fmt, T, BW, NI, nout), "ucb_waveform launch");
+    if (L.graphs.size() < 256) {
+      // record the sequence for the next calls (the kernels' attributes are set by now)
+      GLASS_CUDA(cudaStreamSynchronize(s), "ucb_waveform sync");
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      GLASS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+      cudaError_t e = legacy_enqueue(L, fmt, T, BW, NI, nout);
+      cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if (e == cudaSuccess && e2 == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess) L.graphs[key] = ge;
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();  // a failed capture leaves the direct path in use
+    }
+  }
   GLASS_CUDA(cudaStreamSynchronize(s), "ucb_waveform sync");
   memcpy(X, L.h_out, sizeof(double) * 2 * BW);
   if (all) {
@@ -562,7 +605,7 @@ extern "C" int glass_ucb_waveform(const double *orbit_xyz, const char *format, d
     } else {
       analytic_positions(t, xyz);
     }
-    OrbitSample64 &o = L.h_pos[n];
+    OrbitSample64 &o = L.h_pos()[n];
     for (int i = 0; i < 3; i++) {
       o.x[i] = xyz[3 * i];
       o.y[i] = xyz[3 * i + 1];
@@ -590,7 +633,7 @@ extern "C" void ucb_waveform(struct Orbit *orbit, char *format, double T, double
     for (int n = 0; n < BW; n++) {
       double t = t0 + T * (double)(n) / (double)BW;
       o->orbit_function(orbit, t, x, y, z);
-      OrbitSample64 &s = L.h_pos[n];
+      OrbitSample64 &s = L.h_pos()[n];
       for (int i = 0; i < 3; i++) {
         s.x[i] = x[i + 1];
         s.y[i] = y[i + 1];

@@ -509,58 +509,52 @@ size_t fd_series_bytes(int nitems, int NFFT, int precision) {
 }
 
 // ------------------------------------------------------- legacy single waveform
-// One CTA per Michelson channel (X, Y, Z): slow part, the two FFTs the channel
-// needs, and the format's TDI weights per bin.  A and E follow in
-// fd_ae_kernel from the stored X, Y, Z (utils/src/glass_lisa.c:429-441).
+// The drop-in ucb_waveform for one source: the per-source constants come from
+// the host (source_geometry / make_item_f64, the same FP64 code); the six arm
+// responses are computed one thread per sample spread over N/32 CTAs (the
+// FP64 pipe of many SMs, not one); then one CTA per Michelson channel (X, Y,
+// Z) FFTs its two series and applies the format's TDI weights per bin.  A and
+// E follow in fd_ae_kernel from the stored X, Y, Z (utils/src/glass_lisa.c:429-441).
+__global__ void fd_single_slow_kernel(const OrbitSample64 *pos, const ItemF64 *item, int N, double fstar, double L,
+                                      double2 *d6) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  double2 d[6];
+  slow_sample64(*item, pos[n], fstar, L, d);
+#pragma unroll
+  for (int a = 0; a < 6; a++) d6[(size_t)a * N + n] = d[a];
+}
+
 template <int N>
 struct LegacyCfg {
-  static constexpr int R = (N <= 128) ? 4 : 8;  // samples per thread
+  static constexpr int R = (N <= 128) ? 4 : 8;  // bins per thread
   static constexpr int GT = N / R;              // threads (one CTA per channel)
 };
 
 template <int N>
-__global__ void __launch_bounds__(LegacyCfg<N>::GT) fd_waveform_kernel(const OrbitSample64 *pos, const double *params,
-                                                                    int NP, int format, double T, double fstar,
-                                                                    double L, double *out, const double2 *twg) {
+__global__ void __launch_bounds__(LegacyCfg<N>::GT) fd_waveform_kernel(const ItemF64 *item, const double2 *d6,
+                                                                    int format, double T, double fstar,
+                                                                    double *out, const double2 *twg) {
   constexpr int GT = LegacyCfg<N>::GT, R = LegacyCfg<N>::R;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2 *tw = reinterpret_cast<double2 *>(smem_raw);
   double2 *buf = tw + N;
-  __shared__ ItemF64 c;
   const int lane = threadIdx.x, ch = blockIdx.x;
   for (int i = lane; i < N; i += GT) tw[i] = twg[i];
-  if (lane == 0) {
-    double p[8];
-    for (int k = 0; k < 8; k++) p[k] = k < NP ? params[k] : 0.0;
-    SourceGeom geo;
-    source_geometry(p, NP, T, geo);
-    make_item_f64(geo, N, c);
-  }
-  __syncthreads();
+  // d: 12, 13, 21, 23, 31, 32 ; X: (12-13, 21-31), Y: (23-21, 32-12), Z: (31-32, 13-23)
+  const int ua = ch == 0 ? 0 : ch == 1 ? 3 : 4, ub = ch == 0 ? 1 : ch == 1 ? 2 : 5;
+  const int va = ch == 0 ? 2 : ch == 1 ? 5 : 1, vb = ch == 0 ? 4 : ch == 1 ? 0 : 3;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int n = lane + GT * r;
-    double2 d[6];
-    slow_sample64(c, pos[n], fstar, L, d);
-    // d: 12, 13, 21, 23, 31, 32 ; X: (12-13, 21-31), Y: (23-21, 32-12), Z: (31-32, 13-23)
-    double2 u, v;
-    if (ch == 0) {
-      u = csub(d[0], d[1]);
-      v = csub(d[2], d[4]);
-    } else if (ch == 1) {
-      u = csub(d[3], d[2]);
-      v = csub(d[5], d[0]);
-    } else {
-      u = csub(d[4], d[5]);
-      v = csub(d[1], d[3]);
-    }
-    buf[n] = u;
-    buf[N + n] = v;
+    buf[n] = csub(d6[(size_t)ua * N + n], d6[(size_t)ub * N + n]);
+    buf[N + n] = csub(d6[(size_t)va * N + n], d6[(size_t)vb * N + n]);
   }
   __syncthreads();
   group_fft<N, GT, 2, 1, double2, 64>(buf, tw, lane);  // CTA barrier: the CTA may be a partial warp
   const double sqT = sqrt(T);
-  const long long q = (long long)(c.f0 * T);
+  const long long q = (long long)(item->f0 * T);
+  const double amp_s = item->amp_s;
   double *X = out + (size_t)ch * 2 * N;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -584,7 +578,7 @@ __global__ void __launch_bounds__(LegacyCfg<N>::GT) fd_waveform_kernel(const Orb
       W1 = make_double2(c2 - 1.0, -s2);
     }
     double2 h = cadd(cmul(buf[k], W2), cmul(buf[N + k], W1));
-    double sc = c.amp_s * pref;
+    double sc = amp_s * pref;
     X[2 * m] = h.x * sc;
     X[2 * m + 1] = h.y * sc;
   }
@@ -606,8 +600,8 @@ __global__ void fd_ae_kernel(double *out, int N, int format) {
 }
 
 template <int N>
-static cudaError_t launch_waveform(const OrbitSample64 *pos, const double *params, int NP, int format, int nch,
-                                   double T, double fstar, double *out, const double2 *tw, cudaStream_t stream) {
+static cudaError_t launch_waveform(const ItemF64 *item, const double2 *d6, int format, int nch, double T, double fstar,
+                                   double *out, const double2 *tw, cudaStream_t stream) {
   size_t smem = sizeof(double2) * 3 * N;
   static bool init = false;
   if (!init) {
@@ -616,19 +610,21 @@ static cudaError_t launch_waveform(const OrbitSample64 *pos, const double *param
     if (e != cudaSuccess) return e;
     init = true;
   }
-  fd_waveform_kernel<N><<<nch, LegacyCfg<N>::GT, smem, stream>>>(pos, params, NP, format, T, fstar, kLARM, out, tw);
+  fd_waveform_kernel<N><<<nch, LegacyCfg<N>::GT, smem, stream>>>(item, d6, format, T, fstar, out, tw);
   return cudaGetLastError();
 }
 
-cudaError_t fd_waveform_launch(const OrbitSample64 *pos, const double *params_dev, int NP, int N, int format,
-                                  int NI, double T, double fstar, double *out, const double2 *tw,
-                                  cudaStream_t stream) {
+cudaError_t fd_waveform_launch(const OrbitSample64 *pos, const ItemF64 *item, int N, int format, int NI, double T,
+                               double fstar, double2 *d6, double *out, const double2 *tw, cudaStream_t stream) {
   int nch = (format != 0 && NI <= 1) ? 1 : 3;
-  cudaError_t e = cudaErrorInvalidValue;
+  fd_single_slow_kernel<<<(N + 31) / 32, 32, 0, stream>>>(pos, item, N, fstar, kLARM, d6);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = cudaErrorInvalidValue;
   switch (N) {
 #define GLASS_WCASE(NN) \
   case NN:              \
-    e = launch_waveform<NN>(pos, params_dev, NP, format, nch, T, fstar, out, tw, stream); \
+    e = launch_waveform<NN>(item, d6, format, nch, T, fstar, out, tw, stream); \
     break;
     GLASS_WCASE(32)
     GLASS_WCASE(64)

@@ -78,10 +78,12 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
                            int *nlaunch);
 
 // Single waveform in the reference's output layout (legacy ucb_waveform).
-// pos: N orbit samples (device), out: 10*N doubles (device) = X,Y,Z,A,E.
-// tw: the N-point FP64 twiddle table (FdTablesDev::tw64 of the size).
-cudaError_t fd_waveform_launch(const OrbitSample64 *pos, const double *params_dev, int NP, int N, int format, int NI,
-                               double T, double fstar, double *out, const double2 *tw, cudaStream_t stream);
+// pos: N orbit samples (device), item: the source's FP64 constants (device,
+// from source_geometry + make_item_f64), d6: 6 N complex scratch, out: 10*N
+// doubles (device) = X,Y,Z,A,E.  tw: the N-point FP64 twiddle table
+// (FdTablesDev::tw64 of the size).
+cudaError_t fd_waveform_launch(const OrbitSample64 *pos, const ItemF64 *item, int N, int format, int NI, double T,
+                               double fstar, double2 *d6, double *out, const double2 *tw, cudaStream_t stream);
 
 
 }  // namespace glass

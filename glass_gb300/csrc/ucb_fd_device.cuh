@@ -203,7 +203,7 @@ struct SourceGeom {
   double DPr, DPi, DCr, DCi;
 };
 
-static __device__ void source_geometry(const double *p, int NP, double T, SourceGeom &g) {
+static __host__ __device__ void source_geometry(const double *p, int NP, double T, SourceGeom &g) {
   double f0 = p[0] / T, costh = p[1], phi = p[2], cosi = p[4], psi = p[5];
   g.f0 = f0;
   g.amp = exp(p[3]);
@@ -236,7 +236,7 @@ static __device__ void source_geometry(const double *p, int NP, double T, Source
     }
 }
 
-static __device__ void make_item_f64(const SourceGeom &g, int N, ItemF64 &c) {
+static __host__ __device__ void make_item_f64(const SourceGeom &g, int N, ItemF64 &c) {
   for (int i = 0; i < 3; i++) c.k[i] = g.k[i];
   for (int i = 0; i < 6; i++) {
     c.ep[i] = g.ep[i];
