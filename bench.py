@@ -419,7 +419,11 @@ def wv_flops(nl, c, norb):
 
 def bench_wavelet(gg, torch, dev, rank, steps, warmup, cpu, peak64):
     """Wavelet-domain UCB waveform + sparse-pixel delta logL for 4096 sources
-    on a 1024 x 2048 grid (layers 10..469 of a year at 15 s), FP64."""
+    on a 1024 x 2048 grid (layers 10..469 of a year at 15 s), in FP64 and in
+    mixed precision (FP64 phase, FP32 elsewhere).  The data are Gaussian noise
+    of the segment's covariance at a level that puts the batch's median SNR at
+    20, plus 100 of the sources injected; each proposal is one Gaussian jump
+    from a source."""
     rng = np.random.default_rng(4 + 1000 * rank)
     NF, NT = WV_NF, WV_NT
     wdt = 15.0 * NF
@@ -434,10 +438,16 @@ def bench_wavelet(gg, torch, dev, rank, steps, warmup, cpu, peak64):
                                         10 ** rng.uniform(-23, -21), 1e-17) for _ in range(n)])
 
     src = draw(WV_NSRC)
-    # data: white noise of the segment's covariance plus 100 injected sources
-    scale = 1e-23
-    invC = wl.wavelet_invC(N, NT, kmin, scale)
-    data = rng.standard_normal((3, N)) * scale
+    # noise level: <h|h> under the unit-level covariance, then the level that
+    # gives a median SNR of 20
+    unit = wl.wavelet_invC(N, NT, kmin, 1.0)
+    eng.wavelet_set_data(np.zeros((3, N)), unit)
+    _, _, hh_unit, st0 = eng.wavelet_dlogl_host(src)
+    scale = float(np.median(np.sqrt(hh_unit[st0 == 0]))) / 20.0
+    invC = unit / scale**2
+    base = np.full((3, 3), -0.45) + np.eye(3) * 1.45
+    var = 1.0 / unit[0, 0] * np.linalg.inv(base)[0, 0]  # per-pixel s(i)
+    data = (np.linalg.cholesky(base) @ rng.standard_normal((3, N))) * (np.sqrt(var) * scale)[None, :]
     info, xyz, st = eng.wavelet_waveform_host(src[:100])
     for i in range(100):
         if st[i] == 0:
@@ -460,36 +470,55 @@ def bench_wavelet(gg, torch, dev, rank, steps, warmup, cpu, peak64):
     d_hh = torch.empty_like(d_dl)
     d_st = torch.empty(WV_NSRC, dtype=torch.int32, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    with torch.cuda.stream(stream):
-        for _ in range(warmup):
-            eng.wavelet_dlogl_device(d_p, d_dl, d_ty, d_hh, d_st, term_x=d_tx)
-        stream.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        for k in range(steps):
-            flush.zero_()
-            ev[k][0].record(stream)
-            eng.wavelet_dlogl_device(d_p, d_dl, d_ty, d_hh, d_st, term_x=d_tx)
-            ev[k][1].record(stream)
-        stream.synchronize()
-    launches = eng.last_launch_count()
-    t = sum(a.elapsed_time(b) for a, b in ev) / steps / 1e3
-    stt = d_st.cpu().numpy()
+
+    def timed(prec):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                eng.wavelet_dlogl_device(d_p, d_dl, d_ty, d_hh, d_st, term_x=d_tx, precision=prec)
+            stream.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            for k in range(steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                eng.wavelet_dlogl_device(d_p, d_dl, d_ty, d_hh, d_st, term_x=d_tx, precision=prec)
+                ev[k][1].record(stream)
+            stream.synchronize()
+        return (sum(a.elapsed_time(b) for a, b in ev) / steps / 1e3, eng.last_launch_count(),
+                d_dl.cpu().numpy().copy(), d_hh.cpu().numpy().copy(), d_st.cpu().numpy().copy())
+
+    t64, launches64, dl64, hh64, stt = timed(gg.PREC_FP64)
+    t32, launches32, dl32, hh32, st32 = timed(gg.PREC_MIXED)
     eng.set_stream(None)
     for _ in range(warmup):
-        eng.wavelet_dlogl_host(props, tx)
+        eng.wavelet_dlogl_host(props, tx, precision=gg.PREC_MIXED)
     t0 = time.perf_counter()
     for _ in range(steps):
-        eng.wavelet_dlogl_host(props, tx)
+        eng.wavelet_dlogl_host(props, tx, precision=gg.PREC_MIXED)
     t_e2e = (time.perf_counter() - t0) / steps
+    ok = (stt == 0) & (st32 == 0)
+    err = np.abs(dl32 - dl64)
+    near = ok & (dl64 > -100.0)
+    psnr = np.sqrt(np.maximum(hh64, 0.0))
+    quiet = near & (psnr < 1000.0)
+    acc = {"near_items": int(near.sum()), "max_abs_err_near": float(err[near].max()) if near.any() else None,
+           "frac_near_below_1e-3": float((err[near] < 1e-3).mean()) if near.any() else None,
+           "max_abs_err_near_snr_lt_1000": float(err[quiet].max()) if quiet.any() else None,
+           "max_rel_err_all": float((err[ok] / np.maximum(1.0, np.abs(dl64[ok]))).max()),
+           "max_rel_err_hh": float((np.abs(hh32 - hh64)[ok] / np.maximum(hh64[ok], 1.0)).max()),
+           "snr_median": float(np.median(psnr[ok])), "snr_max": float(psnr[ok].max())}
     out = {"workload": f"ucb_waveform_wavelet + sparse dlogL, {WV_NSRC} sources, NF={NF} NT={NT}, "
-                       f"layers {WV_LMIN}..{WV_LMAX - 1}, f0 log-U[0.5,15] mHz, FP64",
-           "sources_per_s": WV_NSRC / t, "ms_per_batch": 1e3 * t, "ok_items": int((stt == 0).sum()),
-           "outside_items": int((stt == 4).sum()), "launches_per_batch": launches,
-           "roofline": {"bound": "fp64", "achieved": flops / t / 1e12, "peak": peak64, "unit": "TFLOP/s",
-                        "frac": flops / t / 1e12 / peak64, "flops_per_batch": flops,
+                       f"layers {WV_LMIN}..{WV_LMAX - 1}, f0 log-U[0.5,15] mHz, noise at median SNR 20, "
+                       f"100 sources injected",
+           "sources_per_s": WV_NSRC / t32, "ms_per_batch": 1e3 * t32, "precision": "mixed (FP64 phase)",
+           "fp64": {"sources_per_s": WV_NSRC / t64, "ms_per_batch": 1e3 * t64, "launches_per_batch": launches64},
+           "mixed_over_fp64": t64 / t32, "accuracy_vs_fp64": acc,
+           "ok_items": int((stt == 0).sum()), "outside_items": int((stt == 4).sum()),
+           "launches_per_batch": launches32,
+           "roofline": {"bound": "fp64", "achieved": flops / t64 / 1e12, "peak": peak64, "unit": "TFLOP/s",
+                        "frac": flops / t64 / 1e12 / peak64, "flops_per_batch": flops, "path": "fp64",
                         "peak_source": "FP64 FMA probe kernel measured in this run", "traffic": None},
-           "e2e": {"value": WV_NSRC / t_e2e, "unit": "sources/s", "h2d_bytes_per_step": WV_NSRC * 9 * 8,
-                   "d2h_bytes_per_step": WV_NSRC * (3 * 8 + 4)}}
+           "e2e": {"value": WV_NSRC / t_e2e, "unit": "sources/s", "precision": "mixed",
+                   "h2d_bytes_per_step": WV_NSRC * 9 * 8, "d2h_bytes_per_step": WV_NSRC * (3 * 8 + 4)}}
     if cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         from oracle import Port, build_port

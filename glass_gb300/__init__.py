@@ -93,10 +93,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                                             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                             ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
     lib.glass_gpu_wavelet_set_data.argtypes = [_V, _D, _D, _D, _D]
-    lib.glass_gpu_wavelet_dlogl_batch.argtypes = [_V, ctypes.c_int] + [_V] * 6
-    lib.glass_gpu_wavelet_dlogl_batch_host.argtypes = [_V, ctypes.c_int, _D, _D, _D, _D, _D, _I]
-    lib.glass_gpu_wavelet_waveform_batch.argtypes = [_V, ctypes.c_int] + [_V] * 4
-    lib.glass_gpu_wavelet_waveform_batch_host.argtypes = [_V, ctypes.c_int, _D, _I, _D, _I]
+    lib.glass_gpu_wavelet_dlogl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 6
+    lib.glass_gpu_wavelet_dlogl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _I]
+    lib.glass_gpu_wavelet_waveform_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 4
+    lib.glass_gpu_wavelet_waveform_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _I, _D, _I]
     _lib = lib
     return lib
 
@@ -302,7 +302,7 @@ class Engine:
         ic = np.ascontiguousarray(invC, np.float64)
         _check(self.lib.glass_gpu_wavelet_set_data(self._ctx, _pd(r[0]), _pd(r[1]), _pd(r[2]), _pd(ic)))
 
-    def wavelet_waveform_host(self, params, values=True):
+    def wavelet_waveform_host(self, params, values=True, precision=PREC_FP64):
         """(info [n, 4] = first layer, layers, first kept layer, kept layers
         (-1 when the parameters are invalid), xyz [n, 3, 3 NT] or None when
         values is False, status [n])."""
@@ -312,7 +312,7 @@ class Engine:
         info = np.zeros((n, 4), np.int32)
         xyz = np.zeros((n, 3, self.WV_MAX_LAYERS * NT)) if values else None
         st = np.zeros(n, np.int32)
-        _check(self.lib.glass_gpu_wavelet_waveform_batch_host(self._ctx, n, _pd(p), _pi(info),
+        _check(self.lib.glass_gpu_wavelet_waveform_batch_host(self._ctx, precision, n, _pd(p), _pi(info),
                                                               _pd(xyz) if values else None, _pi(st)))
         return info, xyz, st
 
@@ -326,7 +326,7 @@ class Engine:
         j = jlo + np.tile(np.arange(c), NT)
         return (i + j * NT - kmin).astype(np.int32)
 
-    def wavelet_dlogl_host(self, params, term_x=None):
+    def wavelet_dlogl_host(self, params, term_x=None, precision=PREC_FP64):
         """(dlogl, term_y, hh, status) with term = (h|h) - 2 (d|h) over the
         item's pixels and dlogl = -(term_y - term_x)/2."""
         p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
@@ -334,13 +334,15 @@ class Engine:
         tx = None if term_x is None else np.ascontiguousarray(term_x, np.float64)
         dl, ty, hh = np.empty(n), np.empty(n), np.empty(n)
         st = np.empty(n, np.int32)
-        _check(self.lib.glass_gpu_wavelet_dlogl_batch_host(self._ctx, n, _pd(p), _pd(tx) if tx is not None else None,
+        _check(self.lib.glass_gpu_wavelet_dlogl_batch_host(self._ctx, precision, n, _pd(p),
+                                                           _pd(tx) if tx is not None else None,
                                                            _pd(dl), _pd(ty), _pd(hh), _pi(st)))
         return dl, ty, hh, st
 
-    def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None):
+    def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
+                             precision=PREC_FP64):
         n = int(params.shape[0])
-        _check(self.lib.glass_gpu_wavelet_dlogl_batch(self._ctx, n, _ptr(params), _ptr(term_x), _ptr(dlogl),
+        _check(self.lib.glass_gpu_wavelet_dlogl_batch(self._ctx, precision, n, _ptr(params), _ptr(term_x), _ptr(dlogl),
                                                       _ptr(term_y), _ptr(hh), _ptr(status)))
 
     def last_launch_count(self) -> int:

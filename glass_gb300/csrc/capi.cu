@@ -846,9 +846,20 @@ extern "C" int glass_gpu_wavelet_setup(glass_gpu_ctx *ctx, double Tobs, double t
   ctx->wvw = WvWorkDev{};
   GLASS_CUDA(wv_build_grid(h, &ctx->wv, &ctx->wv_grid_mem, ctx->stream), "wavelet grid tables");
   const size_t N = (size_t)(kmax - kmin);
-  GLASS_CUDA(cudaMalloc(&ctx->wv_data_mem, sizeof(double) * 12 * N), "cudaMalloc(wavelet data)");
-  ctx->wv.res = (const double *)ctx->wv_data_mem;
-  ctx->wv.invC = (const double *)ctx->wv_data_mem + 3 * N;
+  // FP64 residual and invC, per-pixel data terms, then the mixed-precision copies
+  GLASS_CUDA(cudaMalloc(&ctx->wv_data_mem, sizeof(double) * 13 * N + sizeof(float) * 15 * N),
+             "cudaMalloc(wavelet data)");
+  {
+    double *d = (double *)ctx->wv_data_mem;
+    ctx->wv.res = d;
+    ctx->wv.invC = d + 3 * N;
+    ctx->wv.qpix = d + 12 * N;
+    float *f = (float *)(d + 13 * N);
+    ctx->wv.res_hi = f;
+    ctx->wv.res_lo = f + 3 * N;
+    ctx->wv.invC32 = f + 6 * N;
+    ctx->wv.scale = 1.0;
+  }
   const size_t wb = wv_work_bytes(kWvChunk, ctx->wv.norb, NT);
   GLASS_CUDA(cudaMalloc(&ctx->wv_work_mem, wb), "cudaMalloc(wavelet work)");
   wv_work_carve(ctx->wvw, ctx->wv_work_mem, kWvChunk, ctx->wv.norb, NT);
@@ -868,7 +879,25 @@ extern "C" int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, 
   GLASS_CUDA(cudaMemcpyAsync(d + 2 * N, rZ, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream), "upload rZ");
   GLASS_CUDA(cudaMemcpyAsync(d + 3 * N, invC, sizeof(double) * 9 * N, cudaMemcpyHostToDevice, ctx->stream),
              "upload invC");
+  // mixed-precision copies: residual / s (hi + lo), invC s^2, per-pixel r^T invC r
+  std::vector<float> rhi, rlo, ic32;
+  std::vector<double> qp;
+  double scale = 1.0;
+  wv_mixed_data((int)N, ctx->wv.NT, rX, rY, rZ, invC, &scale, rhi, rlo, ic32, qp);
+  GLASS_CUDA(cudaMemcpyAsync((void *)ctx->wv.qpix, qp.data(), sizeof(double) * qp.size(), cudaMemcpyHostToDevice,
+                             ctx->stream),
+             "upload data terms");
+  GLASS_CUDA(cudaMemcpyAsync((void *)ctx->wv.res_hi, rhi.data(), sizeof(float) * rhi.size(), cudaMemcpyHostToDevice,
+                             ctx->stream),
+             "upload residual hi");
+  GLASS_CUDA(cudaMemcpyAsync((void *)ctx->wv.res_lo, rlo.data(), sizeof(float) * rlo.size(), cudaMemcpyHostToDevice,
+                             ctx->stream),
+             "upload residual lo");
+  GLASS_CUDA(cudaMemcpyAsync((void *)ctx->wv.invC32, ic32.data(), sizeof(float) * ic32.size(),
+                             cudaMemcpyHostToDevice, ctx->stream),
+             "upload invC32");
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "wavelet data sync");
+  ctx->wv.scale = scale;
   ctx->wv_data_ready = true;
   return GLASS_OK;
 }
@@ -882,18 +911,27 @@ static int wv_check(glass_gpu_ctx *ctx, int nitems, const void *params, const ch
   return ctx_activate(ctx);
 }
 
-extern "C" int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int nitems, const double *params,
+static int wv_precision_ok(int precision, const char *who) {
+  if (precision != GLASS_PREC_FP64 && precision != GLASS_PREC_MIXED)
+    return set_err(GLASS_ERR_ARG, "%s: precision must be GLASS_PREC_FP64 or GLASS_PREC_MIXED", who);
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
                                              const double *term_x, double *dlogl, double *term_y, double *hh,
                                              int *status) {
-  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_dlogl_batch", true);
+  int rc = wv_precision_ok(precision, "glass_gpu_wavelet_dlogl_batch");
+  if (rc) return rc;
+  rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_dlogl_batch", true);
   if (rc) return rc;
   ctx->last_launches = 0;
   for (int off = 0; off < nitems; off += kWvChunk) {
     const int n = std::min(kWvChunk, nitems - off);
-    GLASS_CUDA(wv_waveform_launch(ctx->wv, ctx->wvw, n, params + 8 * (size_t)off, status ? status + off : nullptr,
-                                  ctx->stream, &ctx->last_launches),
+    GLASS_CUDA(wv_waveform_launch(ctx->wv, ctx->wvw, precision, n, params + 8 * (size_t)off,
+                                  status ? status + off : nullptr, ctx->stream, &ctx->last_launches),
                "wavelet waveform launch");
-    GLASS_CUDA(wv_dlogl_launch(ctx->wv, ctx->wvw, n, term_x ? term_x + off : nullptr, dlogl ? dlogl + off : nullptr,
+    GLASS_CUDA(wv_dlogl_launch(ctx->wv, ctx->wvw, precision, n, term_x ? term_x + off : nullptr,
+                               dlogl ? dlogl + off : nullptr,
                                term_y ? term_y + off : nullptr, hh ? hh + off : nullptr,
                                status ? status + off : nullptr, ctx->stream, &ctx->last_launches),
                "wavelet dlogl launch");
@@ -901,28 +939,35 @@ extern "C" int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int nitems, con
   return GLASS_OK;
 }
 
-extern "C" int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int nitems, const double *params, int *info,
-                                                double *xyz, int *status) {
-  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_waveform_batch", false);
+extern "C" int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
+                                                int *info, double *xyz, int *status) {
+  int rc = wv_precision_ok(precision, "glass_gpu_wavelet_waveform_batch");
   if (rc) return rc;
+  rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_waveform_batch", false);
+  if (rc) return rc;
+  if (precision == GLASS_PREC_MIXED && !ctx->wv_data_ready)
+    return set_err(GLASS_ERR_STATE, "glass_gpu_wavelet_waveform_batch: mixed precision scales by the data's noise level; "
+                                    "call glass_gpu_wavelet_set_data first");
   ctx->last_launches = 0;
   const size_t per = (size_t)3 * kWvMaxLayers * ctx->wv.NT;
   for (int off = 0; off < nitems; off += kWvChunk) {
     const int n = std::min(kWvChunk, nitems - off);
-    GLASS_CUDA(wv_waveform_launch(ctx->wv, ctx->wvw, n, params + 8 * (size_t)off, status ? status + off : nullptr,
-                                  ctx->stream, &ctx->last_launches),
+    GLASS_CUDA(wv_waveform_launch(ctx->wv, ctx->wvw, precision, n, params + 8 * (size_t)off,
+                                  status ? status + off : nullptr, ctx->stream, &ctx->last_launches),
                "wavelet waveform launch");
-    GLASS_CUDA(wv_export(ctx->wv, ctx->wvw, n, info ? info + 4 * (size_t)off : nullptr, xyz ? xyz + per * off : nullptr,
-                         ctx->stream),
+    GLASS_CUDA(wv_export(ctx->wv, ctx->wvw, precision, n, info ? info + 4 * (size_t)off : nullptr,
+                         xyz ? xyz + per * off : nullptr, ctx->stream),
                "wavelet export");
   }
   return GLASS_OK;
 }
 
-extern "C" int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params,
+extern "C" int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
                                                   const double *term_x, double *dlogl, double *term_y, double *hh,
                                                   int *status) {
-  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_dlogl_batch_host", true);
+  int rc = wv_precision_ok(precision, "glass_gpu_wavelet_dlogl_batch_host");
+  if (rc) return rc;
+  rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_dlogl_batch_host", true);
   if (rc) return rc;
   if (nitems == 0) return GLASS_OK;
   const size_t n = (size_t)nitems;
@@ -933,7 +978,8 @@ extern "C" int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int nitems
   GLASS_CUDA(cudaMemcpyAsync(dp, params, sizeof(double) * 8 * n, cudaMemcpyHostToDevice, ctx->stream), "upload params");
   if (term_x)
     GLASS_CUDA(cudaMemcpyAsync(dtx, term_x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream), "upload term_x");
-  if ((rc = glass_gpu_wavelet_dlogl_batch(ctx, nitems, dp, term_x ? dtx : nullptr, ddl, dty, dhh, dst))) return rc;
+  if ((rc = glass_gpu_wavelet_dlogl_batch(ctx, precision, nitems, dp, term_x ? dtx : nullptr, ddl, dty, dhh, dst)))
+    return rc;
   if (dlogl) GLASS_CUDA(cudaMemcpyAsync(dlogl, ddl, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "dl");
   if (term_y) GLASS_CUDA(cudaMemcpyAsync(term_y, dty, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "ty");
   if (hh) GLASS_CUDA(cudaMemcpyAsync(hh, dhh, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream), "hh");
@@ -942,9 +988,11 @@ extern "C" int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int nitems
   return GLASS_OK;
 }
 
-extern "C" int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, int *info,
-                                                     double *xyz, int *status) {
-  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_waveform_batch_host", false);
+extern "C" int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
+                                                     int *info, double *xyz, int *status) {
+  int rc = wv_precision_ok(precision, "glass_gpu_wavelet_waveform_batch_host");
+  if (rc) return rc;
+  rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_waveform_batch_host", false);
   if (rc) return rc;
   if (nitems == 0) return GLASS_OK;
   const size_t per = (size_t)3 * kWvMaxLayers * ctx->wv.NT;
@@ -958,7 +1006,7 @@ extern "C" int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nit
     GLASS_CUDA(cudaMemcpyAsync(dp, params + 8 * (size_t)off, sizeof(double) * 8 * n, cudaMemcpyHostToDevice,
                                ctx->stream),
                "upload params");
-    if ((rc = glass_gpu_wavelet_waveform_batch(ctx, (int)n, dp, dinfo, dx, dst))) return rc;
+    if ((rc = glass_gpu_wavelet_waveform_batch(ctx, precision, (int)n, dp, dinfo, dx, dst))) return rc;
     if (info)
       GLASS_CUDA(cudaMemcpyAsync(info + 4 * (size_t)off, dinfo, sizeof(int) * 4 * n, cudaMemcpyDeviceToHost,
                                  ctx->stream),
@@ -1133,7 +1181,8 @@ extern "C" void ucb_waveform_wavelet(struct Orbit *orbit, struct Wavelets *wdm, 
   D.info.resize(4);
   D.xyz.resize(per);
   int st = 0;
-  if (glass_gpu_wavelet_waveform_batch_host(ctx, 1, params, D.info.data(), D.xyz.data(), &st) != GLASS_OK)
+  if (glass_gpu_wavelet_waveform_batch_host(ctx, GLASS_PREC_FP64, 1, params, D.info.data(), D.xyz.data(), &st) !=
+      GLASS_OK)
     dropin_fail(who);
   const int jlo = D.info[2], c = D.info[3];
   if (st != 0 || c < 0) {

@@ -424,22 +424,33 @@ __device__ __forceinline__ int digit_rev(int x, const RadixPlan &P) {
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename C>
+__device__ __forceinline__ C mkc(decltype(C::x) x, decltype(C::x) y) {
+  C r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
 
 // In-place mixed-radix FFT of a[L] held in digit-reversed order; result in
 // natural order.  tw[j * twmul] = e^{-2 pi i j / L}; sign -1 forward, +1
-// inverse (unnormalised).  Whole CTA.
-__device__ void dit_fft(double2 *a, int L, const RadixPlan &P, const double2 *__restrict__ tw, int twmul,
-                        int sign) {
+// inverse (unnormalised).  Whole CTA.  C = double2 or float2.
+template <typename C>
+__device__ void dit_fft(C *a, int L, const RadixPlan &P, const C *__restrict__ tw, int twmul, int sign) {
+  using R = decltype(C::x);
   int p = 1;
   for (int st = 0; st < P.n; st++) {
-    const int R = P.r[st], q = p * R, nb = L / R;
+    const int Rd = P.r[st], q = p * Rd, nb = L / Rd;
     const int tstep = (L / q) * twmul;
     for (int t = threadIdx.x; t < nb; t += blockDim.x) {
       const int b = t / p, k = t - b * p;
-      double2 *base = a + (size_t)b * q + k;
-      if (R == 4) {
-        double2 v0 = base[0], v1 = base[p], v2 = base[2 * p], v3 = base[3 * p];
-        double2 w1 = tw[k * tstep], w2 = tw[2 * k * tstep], w3 = tw[3 * k * tstep];
+      C *base = a + (size_t)b * q + k;
+      if (Rd == 4) {
+        C v0 = base[0], v1 = base[p], v2 = base[2 * p], v3 = base[3 * p];
+        C w1 = tw[k * tstep], w2 = tw[2 * k * tstep], w3 = tw[3 * k * tstep];
         if (sign > 0) {
           w1.y = -w1.y;
           w2.y = -w2.y;
@@ -448,36 +459,36 @@ __device__ void dit_fft(double2 *a, int L, const RadixPlan &P, const double2 *__
         v1 = cmul(v1, w1);
         v2 = cmul(v2, w2);
         v3 = cmul(v3, w3);
-        const double2 t0 = make_double2(v0.x + v2.x, v0.y + v2.y), t1 = make_double2(v0.x - v2.x, v0.y - v2.y);
-        const double2 t2 = make_double2(v1.x + v3.x, v1.y + v3.y), t3 = make_double2(v1.x - v3.x, v1.y - v3.y);
-        const double2 t3r = sign < 0 ? make_double2(t3.y, -t3.x) : make_double2(-t3.y, t3.x);
-        base[0] = make_double2(t0.x + t2.x, t0.y + t2.y);
-        base[p] = make_double2(t1.x + t3r.x, t1.y + t3r.y);
-        base[2 * p] = make_double2(t0.x - t2.x, t0.y - t2.y);
-        base[3 * p] = make_double2(t1.x - t3r.x, t1.y - t3r.y);
-      } else if (R == 2) {
-        double2 v0 = base[0], v1 = base[p];
-        double2 w1 = tw[k * tstep];
+        const C t0 = mkc<C>(v0.x + v2.x, v0.y + v2.y), t1 = mkc<C>(v0.x - v2.x, v0.y - v2.y);
+        const C t2 = mkc<C>(v1.x + v3.x, v1.y + v3.y), t3 = mkc<C>(v1.x - v3.x, v1.y - v3.y);
+        const C t3r = sign < 0 ? mkc<C>(t3.y, -t3.x) : mkc<C>(-t3.y, t3.x);
+        base[0] = mkc<C>(t0.x + t2.x, t0.y + t2.y);
+        base[p] = mkc<C>(t1.x + t3r.x, t1.y + t3r.y);
+        base[2 * p] = mkc<C>(t0.x - t2.x, t0.y - t2.y);
+        base[3 * p] = mkc<C>(t1.x - t3r.x, t1.y - t3r.y);
+      } else if (Rd == 2) {
+        C v0 = base[0], v1 = base[p];
+        C w1 = tw[k * tstep];
         if (sign > 0) w1.y = -w1.y;
         v1 = cmul(v1, w1);
-        base[0] = make_double2(v0.x + v1.x, v0.y + v1.y);
-        base[p] = make_double2(v0.x - v1.x, v0.y - v1.y);
+        base[0] = mkc<C>(v0.x + v1.x, v0.y + v1.y);
+        base[p] = mkc<C>(v0.x - v1.x, v0.y - v1.y);
       } else {
-        double2 v0 = base[0], v1 = base[p], v2 = base[2 * p];
-        double2 w1 = tw[k * tstep], w2 = tw[2 * k * tstep];
+        C v0 = base[0], v1 = base[p], v2 = base[2 * p];
+        C w1 = tw[k * tstep], w2 = tw[2 * k * tstep];
         if (sign > 0) {
           w1.y = -w1.y;
           w2.y = -w2.y;
         }
         v1 = cmul(v1, w1);
         v2 = cmul(v2, w2);
-        const double s3 = 0.86602540378443864676 * (double)sign;
-        const double2 sm = make_double2(v1.x + v2.x, v1.y + v2.y), df = make_double2(v1.x - v2.x, v1.y - v2.y);
-        const double2 m1 = make_double2(v0.x - 0.5 * sm.x, v0.y - 0.5 * sm.y);
-        const double2 m2 = make_double2(-s3 * df.y, s3 * df.x);
-        base[0] = make_double2(v0.x + sm.x, v0.y + sm.y);
-        base[p] = make_double2(m1.x + m2.x, m1.y + m2.y);
-        base[2 * p] = make_double2(m1.x - m2.x, m1.y - m2.y);
+        const R s3 = (R)0.86602540378443864676 * (R)sign;
+        const C sm = mkc<C>(v1.x + v2.x, v1.y + v2.y), df = mkc<C>(v1.x - v2.x, v1.y - v2.y);
+        const C m1 = mkc<C>(v0.x - (R)0.5 * sm.x, v0.y - (R)0.5 * sm.y);
+        const C m2 = mkc<C>(-s3 * df.y, s3 * df.x);
+        base[0] = mkc<C>(v0.x + sm.x, v0.y + sm.y);
+        base[p] = mkc<C>(m1.x + m2.x, m1.y + m2.y);
+        base[2 * p] = mkc<C>(m1.x - m2.x, m1.y - m2.y);
       }
     }
     __syncthreads();
@@ -631,6 +642,186 @@ __global__ void __launch_bounds__(kDloglThreads) wv_dlogl_kernel(WvGridDev g, in
     }
     if (status) status[s] = isfinite(term) ? (c == 0 ? 4 : 0) : 1;
   }
+}
+
+// ------------------------------------------------------------ mixed precision
+// Spline value in FP32 (Horner) from FP64 coefficients (the channel amplitude,
+// O(1e-22)).
+__device__ __forceinline__ float spl_eval_f(const double *c, int n, int j, float d) {
+  return (float)c[j] + d * ((float)c[n + j] + d * ((float)c[2 * n + j] + d * (float)c[3 * n + j]));
+}
+
+// As wv_layers_kernel with the phase kept in FP64: the carrier (barycentre
+// phase at S/C 1 minus the heterodyne, up to ~1e6 rad) plus the channel's
+// relative phase, reduced mod 2 pi in FP64; the amplitude spline, the cosine,
+// both FFTs and the layer transforms run in FP32.  Coefficients are written
+// divided by the segment's noise scale.
+__global__ void __launch_bounds__(kLayerThreads) wv_layers_mix_kernel(WvGridDev g, int n, const WvSrc *srcs,
+                                                                      const double *ssb, const double *tdi,
+                                                                      float *coef) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  const int s = blockIdx.x / 3, ch = blockIdx.x - 3 * (blockIdx.x / 3);
+  const WvSrc &S = srcs[s];
+  if (S.status || S.c == 0) return;
+  const int nl = S.nl, NT = g.NT, Nds = NT * (nl + 1), M = Nds / 2, norb = g.norb;
+  float2 *zb = reinterpret_cast<float2 *>(sm_raw);
+  float2 *lb = zb + M;
+  RadixPlan PM, PN;
+  radix_plan(M, PM);
+  radix_plan(NT, PN);
+  const double *ph_ssb = ssb + (size_t)s * 8 * norb + 4 * norb;
+  const double *ca = tdi + ((size_t)s * 3 + ch) * 8 * norb, *cp = ca + 4 * norb;
+  const double k0 = S.k[0], k1 = S.k[1], k2 = S.k[2];
+  const double *r0 = g.r0ds[nl];
+  const double dtds = g.wdt / (double)(nl + 1);
+  for (int i = threadIdx.x; i < Nds; i += blockDim.x) {
+    const double tds = g.t0 + i * dtds;
+    const double phhet = kPI2 * S.fhet * tds;
+    const double kr = k0 * r0[3 * i + 0] + k1 * r0[3 * i + 1] + k2 * r0[3 * i + 2];
+    const double tsc = tds - kr;
+    const int je = even_index(g.orb_t, norb, tsc);
+    const int jb = bin_index(g.tssb, norb, tds);
+    const double dd = tds - g.tssb[jb];
+    // the whole phase in FP64 (the channel's relative phase reaches tens of
+    // radians over a year), reduced mod 2 pi before it is rounded to FP32
+    const double ph = spl_eval(cp, norb, jb, dd) + (spl_eval(ph_ssb, norb, je, tsc - g.orb_t[je]) - phhet);
+    const float pr = (float)(ph - kPI2 * rint(ph * (1.0 / kPI2)));
+    const float a = spl_eval_f(ca, norb, jb, (float)dd);
+    float *slot = reinterpret_cast<float *>(zb + digit_rev(i >> 1, PM));
+    slot[i & 1] = a * cosf(pr);
+  }
+  __syncthreads();
+  const float2 *tw = g.tw32[nl];
+  dit_fft(zb, M, PM, tw, 2, -1);
+  const float norm = (float)(g.norm_sqrtNF / (nl + 1.0) / g.scale / NT);
+  const float *win = g.win32[nl];
+  float *out = coef + ((size_t)s * 3 + ch) * (kWvMaxLayers * (size_t)NT);
+  for (int off = 0; off < nl; off++) {
+    const int m = S.jmin + off;
+    const int center = (off + 1) * NT / 2;
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+      const int j = t - NT / 2, idx = center + j;
+      float2 val = make_float2(0.f, 0.f);
+      if (j > -NT / 2 && idx >= 0 && idx <= M) {
+        float wt = win[j < 0 ? -j : j];
+        if (j == 0 && (m == 0 || m == g.NF)) wt *= 0.5f;
+        const float2 zk = zb[idx % M], zm0 = zb[(M - idx) % M];
+        const float2 zm = make_float2(zm0.x, -zm0.y);
+        const float2 e = tw[idx];
+        const float2 sm = make_float2(zk.x + zm.x, zk.y + zm.y), df = make_float2(zk.x - zm.x, zk.y - zm.y);
+        const float2 ed = cmul(e, df);
+        val = make_float2(wt * 0.5f * (sm.x + ed.y), wt * 0.5f * (sm.y - ed.x));
+      }
+      lb[digit_rev(t, PN)] = val;
+    }
+    __syncthreads();
+    dit_fft(lb, NT, PN, tw, nl + 1, +1);
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+      const float re = lb[t].x * norm, im = lb[t].y * norm;
+      float v;
+      if (m == 0 || m == g.NF) {
+        v = (t % 2 == 0) ? re * (float)kSQRT2 : 0.f;
+      } else {
+        v = ((t + m) % 2 == 0) ? re : ((m % 2 == 0) ? im : -im);
+      }
+      out[(size_t)t * nl + off] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// Sparse delta logL, term = sum over the source's pixels of h^T invC h -
+// 2 h^T invC r, in FP32 products (r/s as hi + lo floats, invC s^2, h/s) with
+// double-float sums.  Per pixel the form with the smaller rounding error is
+// used: the residual form e^T invC e - r^T invC r (e = r - h, the FP64 data
+// term subtracted) where the template matches the data, the direct form
+// h^T invC (h - 2 r) where the data is much louder than the template.
+__global__ void __launch_bounds__(kDloglThreads) wv_dlogl_mix_kernel(WvGridDev g, int n, const WvSrc *srcs,
+                                                                     const float *coef, const double *term_x,
+                                                                     double *dlogl, double *term_y, double *hh_out,
+                                                                     int *status) {
+  const int s = blockIdx.x;
+  const WvSrc &S = srcs[s];
+  __shared__ float2 red[2][kDloglThreads / 32];
+  __shared__ double redq[kDloglThreads / 32];
+  if (S.status) {
+    if (threadIdx.x == 0) {
+      if (dlogl) dlogl[s] = NAN;
+      if (term_y) term_y[s] = NAN;
+      if (hh_out) hh_out[s] = NAN;
+    }
+    return;
+  }
+  const int NT = g.NT, N = g.N, c = S.c, npix = NT * c;
+  const float *h0 = coef + (size_t)s * 3 * (kWvMaxLayers * (size_t)NT);
+  const float *h1 = h0 + kWvMaxLayers * (size_t)NT, *h2 = h1 + kWvMaxLayers * (size_t)NT;
+  const float *rh = g.res_hi, *rl = g.res_lo, *ic = g.invC32;
+  df acc = {0.f, 0.f}, hacc = {0.f, 0.f};
+  double qacc = 0.0;
+  for (int q = threadIdx.x; q < npix; q += blockDim.x) {
+    const int i = q / c, j = S.jlo + (q - i * c);
+    const int k = i + j * NT - g.kmin;
+    const float a0 = h0[q], a1 = h1[q], a2 = h2[q];
+    const float r0h = rh[k], r1h = rh[N + k], r2h = rh[2 * N + k];
+    const float r0l = rl[k], r1l = rl[N + k], r2l = rl[2 * N + k];
+    const float c00 = ic[k], c01 = ic[N + k], c02 = ic[2 * N + k];
+    const float c10 = ic[3 * N + k], c11 = ic[4 * N + k], c12 = ic[5 * N + k];
+    const float c20 = ic[6 * N + k], c21 = ic[7 * N + k], c22 = ic[8 * N + k];
+    const float th = a0 * (a0 * c00 + a1 * c01 + a2 * c02) + a1 * (a0 * c10 + a1 * c11 + a2 * c12) +
+                     a2 * (a0 * c20 + a1 * c21 + a2 * c22);
+    const float e0 = (r0h - a0) + r0l, e1 = (r1h - a1) + r1l, e2 = (r2h - a2) + r2l;
+    const float ee = e0 * e0 + e1 * e1 + e2 * e2;
+    const float hn = a0 * a0 + a1 * a1 + a2 * a2, rn = r0h * r0h + r1h * r1h + r2h * r2h;
+    float t;
+    if (ee * ee <= hn * (hn + 4.f * rn)) {
+      // residual form: rounding ~ |e|^2, the data term exact in FP64
+      t = e0 * (e0 * c00 + e1 * c01 + e2 * c02) + e1 * (e0 * c10 + e1 * c11 + e2 * c12) +
+          e2 * (e0 * c20 + e1 * c21 + e2 * c22);
+      qacc += g.qpix[k];
+    } else {
+      // direct form: rounding ~ |h| (|h| + 2 |r|)
+      const float u0 = (a0 - 2.f * r0h) - 2.f * r0l, u1 = (a1 - 2.f * r1h) - 2.f * r1l,
+                  u2 = (a2 - 2.f * r2h) - 2.f * r2l;
+      t = a0 * (c00 * u0 + c01 * u1 + c02 * u2) + a1 * (c10 * u0 + c11 * u1 + c12 * u2) +
+          a2 * (c20 * u0 + c21 * u1 + c22 * u2);
+    }
+    acc = df_add(acc, df{t, 0.f});
+    hacc = df_add(hacc, df{th, 0.f});
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const df ao = {__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
+    const df ho = {__shfl_xor_sync(0xffffffffu, hacc.hi, o), __shfl_xor_sync(0xffffffffu, hacc.lo, o)};
+    acc = df_add(acc, ao);
+    hacc = df_add(hacc, ho);
+    qacc += __shfl_xor_sync(0xffffffffu, qacc, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = make_float2(acc.hi, acc.lo);
+    red[1][threadIdx.x >> 5] = make_float2(hacc.hi, hacc.lo);
+    redq[threadIdx.x >> 5] = qacc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sr = 0.0, sh = 0.0, sq = 0.0;
+    for (int w = 0; w < kDloglThreads / 32; w++) {
+      sr += (double)red[0][w].x + (double)red[0][w].y;
+      sh += (double)red[1][w].x + (double)red[1][w].y;
+      sq += redq[w];
+    }
+    const double term = sr - sq;
+    if (term_y) term_y[s] = term;
+    if (hh_out) hh_out[s] = sh;
+    if (dlogl) {
+      const double tx = term_x ? term_x[s] : 0.0;
+      dlogl[s] = -0.5 * term - (-0.5 * tx);
+    }
+    if (status) status[s] = isfinite(term) ? (c == 0 ? 4 : 0) : 1;
+  }
+}
+
+__global__ void wv_unscale_kernel(const float *in, double *out, long long n, double scale) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)in[i] * scale;
 }
 
 __global__ void wv_info_kernel(int n, const WvSrc *srcs, int *info) {
@@ -810,6 +1001,8 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
   // per layer count: S/C 1 at the downsampled times, window, twiddles
   std::vector<double> r0[kWvMaxLayers + 1], win[kWvMaxLayers + 1];
   std::vector<double2> tw[kWvMaxLayers + 1];
+  std::vector<float> win32[kWvMaxLayers + 1];
+  std::vector<float2> tw32[kWvMaxLayers + 1];
   for (int nl = 1; nl <= kWvMaxLayers; nl++) {
     const int Nds = NT * (nl + 1);
     const double dtds = h.wdt / (double)(nl + 1);
@@ -821,17 +1014,21 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
     win[nl].resize(NT / 2 + 1);
     wdm_window(nl + 1, NT, h.A, h.nx, true, win[nl].data());
     tw[nl].resize(Nds);
+    tw32[nl].resize(Nds);
     for (int k = 0; k < Nds; k++) {
       double c, sn;
       unit_root(k, Nds, &c, &sn);
       tw[nl][k] = make_double2(c, sn);
+      tw32[nl][k] = make_float2((float)c, (float)sn);
     }
+    win32[nl].assign(win[nl].begin(), win[nl].end());
   }
   // one allocation
   auto pad = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t bytes = pad(8 * (size_t)norb) * 2 + pad(8 * geo.size()) + pad(8 * fac_orb.size()) * 2;
   for (int nl = 1; nl <= kWvMaxLayers; nl++)
-    bytes += pad(8 * r0[nl].size()) + pad(8 * win[nl].size()) + pad(16 * tw[nl].size());
+    bytes += pad(8 * r0[nl].size()) + pad(8 * win[nl].size()) + pad(16 * tw[nl].size()) + pad(4 * win32[nl].size()) +
+             pad(8 * tw32[nl].size());
   char *base = nullptr;
   cudaError_t e = cudaMalloc((void **)&base, bytes);
   if (e != cudaSuccess) return e;
@@ -851,10 +1048,14 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
   g->r0ds[0] = nullptr;
   g->win[0] = nullptr;
   g->tw[0] = nullptr;
+  g->win32[0] = nullptr;
+  g->tw32[0] = nullptr;
   for (int nl = 1; nl <= kWvMaxLayers; nl++) {
     g->r0ds[nl] = (const double *)put(r0[nl].data(), 8 * r0[nl].size());
     g->win[nl] = (const double *)put(win[nl].data(), 8 * win[nl].size());
     g->tw[nl] = (const double2 *)put(tw[nl].data(), 16 * tw[nl].size());
+    g->win32[nl] = (const float *)put(win32[nl].data(), 4 * win32[nl].size());
+    g->tw32[nl] = (const float2 *)put(tw32[nl].data(), 8 * tw32[nl].size());
   }
   if (e != cudaSuccess) return e;
   g->NF = h.NF;
@@ -876,39 +1077,87 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
 
 static size_t layers_smem(int NT) { return sizeof(double2) * (size_t)NT * (kWvMaxLayers + 1) / 2 + sizeof(double2) * NT; }
 
-cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *params, int *status,
-                               cudaStream_t s, int *nlaunch) {
+cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *params,
+                               int *status, cudaStream_t s, int *nlaunch) {
   if (n <= 0) return cudaSuccess;
   const int norb = g.norb;
   wv_plan_kernel<<<(n + 127) / 128, 128, 0, s>>>(g, n, params, w.src, w.ssb, status);
   const long long nr = (long long)n * norb;
   wv_resp_kernel<<<(unsigned)((nr + 127) / 128), 128, 0, s>>>(g, n, w.src, w.ssb, w.resp);
   wv_tdi_kernel<<<(3 * n + 127) / 128, 128, 0, s>>>(g, n, w.src, w.resp, w.tdi);
-  const size_t sm = layers_smem(g.NT);
-  cudaError_t e = cudaFuncSetAttribute(wv_layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  wv_layers_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, w.coef);
+  cudaError_t e;
+  if (precision == 1) {
+    const size_t sm = layers_smem(g.NT) / 2;  // float2
+    e = cudaFuncSetAttribute(wv_layers_mix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    wv_layers_mix_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, reinterpret_cast<float *>(w.coef));
+  } else {
+    const size_t sm = layers_smem(g.NT);
+    e = cudaFuncSetAttribute(wv_layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    wv_layers_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, w.coef);
+  }
   if (nlaunch) *nlaunch += 4;
   return cudaGetLastError();
 }
 
-cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *term_x, double *dlogl,
-                            double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch) {
+cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *term_x,
+                            double *dlogl, double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch) {
   if (n <= 0) return cudaSuccess;
-  wv_dlogl_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, w.coef, term_x, dlogl, term_y, hh, status);
+  if (precision == 1)
+    wv_dlogl_mix_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, reinterpret_cast<const float *>(w.coef), term_x,
+                                                    dlogl, term_y, hh, status);
+  else
+    wv_dlogl_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, w.coef, term_x, dlogl, term_y, hh, status);
   if (nlaunch) *nlaunch += 1;
   return cudaGetLastError();
 }
 
-cudaError_t wv_export(const WvGridDev &g, const WvWorkDev &w, int n, int *info, double *xyz, cudaStream_t s) {
+cudaError_t wv_export(const WvGridDev &g, const WvWorkDev &w, int precision, int n, int *info, double *xyz,
+                      cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   if (info) wv_info_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, w.src, info);
   if (xyz) {
-    cudaError_t e = cudaMemcpyAsync(xyz, w.coef, sizeof(double) * (size_t)n * 3 * kWvMaxLayers * g.NT,
-                                    cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return e;
+    const long long cnt = (long long)n * 3 * kWvMaxLayers * g.NT;
+    if (precision == 1) {
+      wv_unscale_kernel<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(reinterpret_cast<const float *>(w.coef), xyz,
+                                                                      cnt, g.scale);
+    } else {
+      cudaError_t e = cudaMemcpyAsync(xyz, w.coef, sizeof(double) * cnt, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaGetLastError();
+}
+
+void wv_mixed_data(int N, int NT, const double *rX, const double *rY, const double *rZ, const double *invC,
+                   double *scale, std::vector<float> &res_hi, std::vector<float> &res_lo, std::vector<float> &invC32,
+                   std::vector<double> &qpix) {
+  (void)NT;
+  // noise scale: root mean square of the X-channel standard deviation
+  double m = 0.0;
+  for (int k = 0; k < N; k++) m += invC[k] > 0.0 ? 1.0 / invC[k] : 0.0;
+  const double s = m > 0.0 ? sqrt(m / N) : 1.0;
+  *scale = s;
+  const double *r[3] = {rX, rY, rZ};
+  res_hi.resize(3 * (size_t)N);
+  res_lo.resize(3 * (size_t)N);
+  invC32.resize(9 * (size_t)N);
+  for (int c = 0; c < 3; c++)
+    for (int k = 0; k < N; k++) {
+      const double v = r[c][k] / s;
+      const float hi = (float)v;
+      res_hi[(size_t)c * N + k] = hi;
+      res_lo[(size_t)c * N + k] = (float)(v - (double)hi);
+    }
+  for (size_t q = 0; q < 9 * (size_t)N; q++) invC32[q] = (float)(invC[q] * s * s);
+  qpix.assign((size_t)N, 0.0);
+  for (int k = 0; k < N; k++) {
+    double acc = 0.0;
+    for (int a = 0; a < 3; a++)
+      for (int b = 0; b < 3; b++) acc += (r[a][k] / s) * (r[b][k] / s) * (invC[(size_t)(3 * a + b) * N + k] * s * s);
+    qpix[k] = acc;
+  }
 }
 
 }  // namespace glass

@@ -35,6 +35,15 @@ struct WvGridDev {
   const double2 *tw[kWvMaxLayers + 1];   // [NT (nl+1)] e^{-2 pi i k / (NT (nl+1))}
   const double *res;      // [3][N] residual X, Y, Z
   const double *invC;     // [9][N] inverse noise covariance, [i][j][k]
+  // mixed precision: FP32 twiddles and windows, the residual divided by the
+  // segment's noise scale s as hi + lo floats, invC s^2 as floats, and per-pixel
+  // r^T invC r (FP64); templates are produced divided by s
+  const float2 *tw32[kWvMaxLayers + 1];
+  const float *win32[kWvMaxLayers + 1];
+  const float *res_hi, *res_lo;  // [3][N]
+  const float *invC32;           // [9][N]
+  const double *qpix;            // [N]
+  double scale;                  // s
 };
 
 struct WvWorkDev {
@@ -64,13 +73,22 @@ size_t wv_work_bytes(int cap, int norb, int NT);
 void wv_work_carve(WvWorkDev &w, void *base, int cap, int norb, int NT);
 
 // Waveform batch: plan, response, TDI splines, per-layer transforms.
-cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *params, int *status,
-                               cudaStream_t s, int *nlaunch);
-// Sparse likelihood over each source's pixels (after wv_waveform_launch).
-cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *term_x, double *dlogl,
-                            double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch);
+// precision 1: samples with an FP64 phase and FP32 amplitude spline, FP32
+// FFTs, FP32 coefficients (divided by g.scale) in w.coef.
+cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *params,
+                               int *status, cudaStream_t s, int *nlaunch);
+// Sparse likelihood over each source's pixels (after wv_waveform_launch with
+// the same precision).
+cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *term_x,
+                            double *dlogl, double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch);
 // Per-item layer info and values in list order: info[4 i] = first layer,
 // layer count, first kept layer, kept layers per time; xyz[(3 i + c) (kWvMaxLayers NT) + q].
-cudaError_t wv_export(const WvGridDev &g, const WvWorkDev &w, int n, int *info, double *xyz, cudaStream_t s);
+cudaError_t wv_export(const WvGridDev &g, const WvWorkDev &w, int precision, int n, int *info, double *xyz,
+                      cudaStream_t s);
+// Host: the mixed-precision data (hi/lo residual, FP32 invC, per-pixel
+// r^T invC r) of a segment from its FP64 residual and invC; sizes as WvGridDev.
+void wv_mixed_data(int N, int NT, const double *rX, const double *rY, const double *rZ, const double *invC,
+                   double *scale, std::vector<float> &res_hi, std::vector<float> &res_lo, std::vector<float> &invC32,
+                   std::vector<double> &qpix);
 
 }  // namespace glass

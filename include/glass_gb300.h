@@ -286,6 +286,17 @@ int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, const doubl
                                const double *invC);
 
 /*
+ * precision GLASS_PREC_FP64: everything in FP64 with the reference's order
+ * of operations (delta logL to 1e-10 of the reference).  GLASS_PREC_MIXED: the
+ * sample phase (carrier at S/C 1 minus the heterodyne, plus the channel's
+ * relative phase) in FP64 and reduced mod 2 pi, the amplitude spline, FFTs and
+ * layer transforms in FP32, the likelihood from FP32 products with
+ * double-float sums, per pixel in the form (residual or direct) with the
+ * smaller rounding error.  Its error against FP64 is set by the FP32 template
+ * (relative ~1e-6): about 1e-6 x |h| x |r - h| summed over the pixels, so it is
+ * below 1e-3 where the residual holds noise and the source's own signal, and
+ * grows where an unsubtracted loud signal shares the source's pixels.
+ *
  * For each of nitems parameter vectors params[8 i ..] (the reference's UCB
  * params array), the wavelet waveform on its pixel list and
  *   term_y[i] = (h|h) - 2 (r|h)     (nine XYZ cross terms, as delta_log_likelihood)
@@ -297,10 +308,10 @@ int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, const doubl
  * GLASS_ITEM_OUTSIDE when no pixel of the source falls in the segment.
  * Device pointers (any may be NULL except params); asynchronous.
  */
-int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int nitems, const double *params, const double *term_x,
-                                  double *dlogl, double *term_y, double *hh, int *status);
-int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, const double *term_x,
-                                       double *dlogl, double *term_y, double *hh, int *status);
+int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
+                                  const double *term_x, double *dlogl, double *term_y, double *hh, int *status);
+int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
+                                       const double *term_x, double *dlogl, double *term_y, double *hh, int *status);
 
 /*
  * The waveforms themselves: info[4 i ..] = first layer, layer count, first
@@ -311,10 +322,10 @@ int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int nitems, const dou
  * (including its rule that the q-th listed pixel takes the q-th coefficient
  * of the per-layer transform).  Device pointers; asynchronous.
  */
-int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int nitems, const double *params, int *info, double *xyz,
-                                     int *status);
-int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, int *info,
-                                          double *xyz, int *status);
+int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int precision, int nitems, const double *params, int *info,
+                                     double *xyz, int *status);
+int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
+                                          int *info, double *xyz, int *status);
 
 /* ------------------------------------ drop-ins for the wavelet headers */
 /*

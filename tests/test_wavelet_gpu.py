@@ -4,6 +4,12 @@ with the reference (golden vectors) and the oracle, through the C ABI.
 FP64 tolerances: waveform values within 1e-10 of the channel's largest value
 (they agree to the FFTs' rounding, ~1e-14), pixel lists identical; delta logL
 within 1e-10 relative to max(1, |delta logL|).
+
+Mixed precision (FP64 phase, FP32 amplitude, FFTs and products, double-float
+sums) against FP64: waveform values within 1e-5 of the channel's largest
+value; delta logL within 1e-3 absolute where |delta logL| is small (proposals
+near the injection in data of noise plus that source), and within 1e-5 of
+|delta logL| elsewhere; <h|h> within 1e-5 relative.
 """
 import numpy as np
 import pytest
@@ -13,6 +19,8 @@ from glass_gb300 import workloads as wl
 
 pytestmark = pytest.mark.gpu
 REL = 1e-10
+MIXED_ABS = 1e-3
+MIXED_REL_FAR = 1e-5
 GRIDS = {"nf1024": (1024, 2048, 15.0 * 1024, 2.0**21 * 15.0), "nf1536": (1536, 4096, 7680.0, 4096 * 7680.0)}
 SMALL = (64, 256, 15.0 * 64, 2.0**14 * 15.0)  # NF, NT, pixel duration, Tobs
 
@@ -142,3 +150,55 @@ def test_given_orbit_arrays_are_used(engine, port):
     b = engine.wavelet_waveform_host(p[None])
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_mixed_waveform_close_to_fp64(engine, golden):
+    g = golden("wavelet_likelihood.npz")
+    NF, NT, wdt, Tobs = GRIDS[str(g["grid"])]
+    kmin, kmax = int(g["c0_kmin"]), int(g["c0_kmax"])
+    setup_grid(engine, (NF, NT, wdt, Tobs), 0.0, kmin, kmax)
+    invC = wl.wavelet_invC(kmax - kmin, NT, kmin, float(g["c0_scale"]))
+    props = g["c0_props"]
+    with pytest.raises(gg.GlassError):  # mixed precision needs the data's noise level
+        engine.wavelet_waveform_host(props, precision=gg.PREC_MIXED)
+    engine.wavelet_set_data(g["c0_d"], invC)
+    i64, x64, s64 = engine.wavelet_waveform_host(props)
+    i32, x32, s32 = engine.wavelet_waveform_host(props, precision=gg.PREC_MIXED)
+    assert (s64 == 0).all() and (s32 == 0).all()
+    np.testing.assert_array_equal(i32, i64)
+    for i in range(len(props)):
+        lst = engine.wavelet_list(i64[i])
+        for c in range(3):
+            ref = x64[i, c, : len(lst)]
+            assert np.abs(x32[i, c, : len(lst)] - ref).max() < 1e-5 * np.abs(ref).max(), (i, c)
+
+
+def test_mixed_dlogl_error_budget(engine, golden):
+    """Golden segments (noise + one injection) with their proposals, plus wider
+    jumps from the injection: near the injection the error is absolute, far
+    from it relative."""
+    g = golden("wavelet_likelihood.npz")
+    NF, NT, wdt, Tobs = GRIDS[str(g["grid"])]
+    rng = np.random.default_rng(17)
+    for c in range(int(g["ncase"])):
+        kmin, kmax = int(g[f"c{c}_kmin"]), int(g[f"c{c}_kmax"])
+        setup_grid(engine, (NF, NT, wdt, Tobs), 0.0, kmin, kmax)
+        invC = wl.wavelet_invC(kmax - kmin, NT, kmin, float(g[f"c{c}_scale"]))
+        engine.wavelet_set_data(g[f"c{c}_d"], invC)
+        inj = g[f"c{c}_inj"]
+        _, tx, hh0, _ = engine.wavelet_dlogl_host(inj[None])
+        scales = wl.jump_scales(inj, float(np.sqrt(hh0[0])))
+        wide = np.array([wl.gaussian_jumps(rng, inj, scales * f, 1)[0] for f in np.geomspace(0.3, 30, 40)])
+        props = np.concatenate([g[f"c{c}_props"], wide])
+        txs = np.full(len(props), tx[0])
+        dl64, _, hh64, s64 = engine.wavelet_dlogl_host(props, term_x=txs)
+        dl32, _, hh32, s32 = engine.wavelet_dlogl_host(props, term_x=txs, precision=gg.PREC_MIXED)
+        np.testing.assert_array_equal(s32, s64)
+        ok = s64 == 0
+        assert ok.sum() >= len(g[f"c{c}_props"])
+        err = np.abs(dl32 - dl64)[ok]
+        ref = np.abs(dl64[ok])
+        near = ref < 100.0
+        assert (err[near] < MIXED_ABS).all(), err[near].max()
+        assert (err[~near] < MIXED_REL_FAR * ref[~near]).all()
+        np.testing.assert_allclose(hh32[ok], hh64[ok], rtol=MIXED_REL_FAR)
