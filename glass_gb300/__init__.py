@@ -33,7 +33,8 @@ EXPORTS = (
     "ucb_waveform", "glass_ucb_waveform", "ucb_bandwidth",
     "glass_gpu_create", "glass_gpu_destroy", "glass_gpu_set_stream", "glass_gpu_last_error",
     "glass_gpu_bank_upload", "glass_gpu_bank_set_residual", "glass_gpu_dlogl_batch",
-    "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_probe_fma_tflops",
+    "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_set_phase_timing",
+    "glass_gpu_last_phase_ms", "glass_gpu_probe_fma_tflops",
     "glass_gpu_grad_fisher_batch", "glass_gpu_grad_fisher_batch_host", "glass_gpu_set_template_size",
     "glass_gpu_dlogl_fp64_noalloc", "glass_wdm_window", "glass_gpu_wdm_forward", "glass_gpu_wdm_inverse",
     "glass_gpu_wdm_forward_host", "glass_gpu_wdm_inverse_host",
@@ -64,6 +65,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_destroy.argtypes = [_V]
     lib.glass_gpu_set_stream.argtypes = [_V, _V]
     lib.glass_gpu_last_launch_count.argtypes = [_V]
+    lib.glass_gpu_set_phase_timing.argtypes = [_V, ctypes.c_int]
+    lib.glass_gpu_last_phase_ms.argtypes = [_V, ctypes.POINTER(ctypes.c_float)]
     lib.glass_gpu_bank_upload.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_int, _I, _D, _D, _D, _D]
     lib.glass_gpu_bank_set_residual.argtypes = [_V, ctypes.c_int, _D, _D]
@@ -347,3 +350,13 @@ class Engine:
 
     def last_launch_count(self) -> int:
         return self.lib.glass_gpu_last_launch_count(self._ctx)
+
+    def set_phase_timing(self, enable: bool):
+        _check(self.lib.glass_gpu_set_phase_timing(self._ctx, int(bool(enable))))
+
+    def last_phase_ms(self):
+        """(plan, slow part, spectral) milliseconds of the last dlogl batch
+        launched with phase timing on."""
+        ms = (ctypes.c_float * 3)()
+        _check(self.lib.glass_gpu_last_phase_ms(self._ctx, ms))
+        return tuple(float(v) for v in ms)

@@ -133,6 +133,8 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
   }
   if (ctx->work.fork) cudaEventDestroy(ctx->work.fork);
+  for (int i = 0; i < 4; i++)
+    if (ctx->work.phase[i]) cudaEventDestroy(ctx->work.phase[i]);
   cudaStreamDestroy(ctx->own);
   delete ctx;
   return GLASS_OK;
@@ -145,6 +147,29 @@ extern "C" int glass_gpu_set_stream(glass_gpu_ctx *ctx, void *stream) {
 }
 
 extern "C" int glass_gpu_last_launch_count(glass_gpu_ctx *ctx) { return ctx ? ctx->last_launches : 0; }
+
+extern "C" int glass_gpu_set_phase_timing(glass_gpu_ctx *ctx, int enable) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_set_phase_timing: null context");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if (enable && !ctx->work.phase[0])
+    for (int i = 0; i < 4; i++) GLASS_CUDA(cudaEventCreate(&ctx->work.phase[i]), "phase event create");
+  ctx->work.phase_timing = enable != 0;
+  ctx->work.phase_recorded = false;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_last_phase_ms(glass_gpu_ctx *ctx, float *ms) {
+  if (!ctx || !ms) return set_err(GLASS_ERR_ARG, "glass_gpu_last_phase_ms: null argument");
+  if (!ctx->work.phase_recorded)
+    return set_err(GLASS_ERR_STATE, "glass_gpu_last_phase_ms: no step was launched with phase timing on");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  GLASS_CUDA(cudaEventSynchronize(ctx->work.phase[3]), "phase event sync");
+  for (int i = 0; i < 3; i++)
+    GLASS_CUDA(cudaEventElapsedTime(&ms[i], ctx->work.phase[i], ctx->work.phase[i + 1]), "phase elapsed time");
+  return GLASS_OK;
+}
 
 static int is_pow2_in_range(int n);
 

@@ -405,12 +405,16 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   pa.term_y = term_y;
   pa.hh = hh;
   pa.status = status;
+  const bool timing = work.phase_timing;
+  work.phase_recorded = false;
+  if (timing && (e = cudaEventRecord(work.phase[0], stream)) != cudaSuccess) return e;
   if (mix)
     fd_planmix_kernel<<<(nitems + kPlanItems - 1) / kPlanItems, 128, 0, stream>>>(pa);
   else
     fd_plan64_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(pa);
   launches++;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (timing && (e = cudaEventRecord(work.phase[1], stream)) != cudaSuccess) return e;
 
   SlowArgs sa;
   sa.cap = work.cap;
@@ -433,6 +437,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   e = mix ? fd_launch_slow_mixed(sa, num_sms, stream) : fd_launch_slow_fp64(sa, num_sms, stream);
   launches++;
   if (e != cudaSuccess) return e;
+  if (timing && (e = cudaEventRecord(work.phase[2], stream)) != cudaSuccess) return e;
 
   SpecArgs a;
   a.NFFT = bank.NFFT;
@@ -494,6 +499,10 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream)) != cudaSuccess) return e;
   }
   work.counts_zero = true;
+  if (timing) {
+    if ((e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
+    work.phase_recorded = true;
+  }
   if (nlaunch) *nlaunch = launches;
   return cudaSuccess;
 }

@@ -49,6 +49,12 @@ struct FdWorkDev {
   // when that is not known (a launch returned an error part-way)
   bool counts_zero = false;
   void *series = nullptr;       // 4 arm-combination series per proposal
+  // optional timing of each phase of a step on the caller's stream: events
+  // before the plan kernel, after it, after the slow-part kernel and after the
+  // spectral kernels (timing events; only when phase_timing is set)
+  bool phase_timing = false;
+  bool phase_recorded = false;
+  cudaEvent_t phase[4] = {};
 };
 
 // Host-side table construction for a bank: G and w tables, prefix sums.

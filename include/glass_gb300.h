@@ -166,6 +166,18 @@ int glass_gpu_grad_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const int *
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 
+/* Per-phase timing of glass_gpu_dlogl_batch (profiling aid; off by default).
+ * With enable != 0 every later call records four timing events on the
+ * context's stream: before the plan kernel, after it, after the slow-part
+ * kernel, and after the spectral (FFT + likelihood) kernels.
+ * glass_gpu_last_phase_ms waits for the last call's events and writes the
+ * three durations in milliseconds to ms[0..2] (plan, slow part, spectral);
+ * GLASS_ERR_STATE when no call was made with timing on.  Events recorded
+ * while the stream is being captured into a CUDA graph become graph nodes:
+ * read the durations after launches made outside capture. */
+int glass_gpu_set_phase_timing(glass_gpu_ctx *ctx, int enable);
+int glass_gpu_last_phase_ms(glass_gpu_ctx *ctx, float *ms);
+
 /* ------------------------------------------- batch that allocates nothing */
 /*
  * No counterpart in the reference.  For callers that cannot allocate GPU

@@ -237,3 +237,25 @@ def test_t0_and_residual_update(engine, port):
     t_ref, _, _ = port.dlogl_term(inj[2], T, 512, int(bank.qmin[2]), rA2, rE2, bank.invCA[2], bank.invCE[2],
                                   t0=bank.t0)
     assert abs(ty2[0] - t_ref) < REL * max(1, abs(t_ref))
+
+
+def test_phase_timing(engine, port):
+    """Per-phase durations of a step: refused before any timed step, three
+    positive durations after one, and the results unchanged by the events."""
+    rng = np.random.default_rng(31)
+    bank, inj = _random_bank(rng, 8, 1024, port)
+    engine.upload(bank)
+    seg = np.repeat(np.arange(8, dtype=np.int32), 32)
+    params = np.vstack([wl.gaussian_jumps(rng, inj[s], wl.jump_scales(inj[s], 20.0), 32) for s in range(8)])
+    ref = engine.dlogl_host(seg, params, precision=gg.PREC_MIXED)
+    with pytest.raises(gg.GlassError):
+        engine.last_phase_ms()
+    engine.set_phase_timing(True)
+    try:
+        got = engine.dlogl_host(seg, params, precision=gg.PREC_MIXED)
+        ms = engine.last_phase_ms()
+    finally:
+        engine.set_phase_timing(False)
+    assert len(ms) == 3 and all(v > 0 for v in ms)
+    for a, b in zip(got, ref):
+        np.testing.assert_array_equal(a, b)
