@@ -651,11 +651,28 @@ __device__ __forceinline__ float spl_eval_f(const double *c, int n, int j, float
   return (float)c[j] + d * ((float)c[n + j] + d * ((float)c[2 * n + j] + d * (float)c[3 * n + j]));
 }
 
-// As wv_layers_kernel with the phase kept in FP64: the carrier (barycentre
-// phase at S/C 1 minus the heterodyne, up to ~1e6 rad) plus the channel's
-// relative phase, reduced mod 2 pi in FP64; the amplitude spline, the cosine,
-// both FFTs and the layer transforms run in FP32.  Coefficients are written
-// divided by the segment's noise scale.
+// Per spline interval j of one (source, channel), the constants the mixed
+// sampler needs, built in FP64 and stored as floats / double-floats:
+//   carrier (barycentre phase spline on the orbit grid x, heterodyne folded in)
+//     pa = (a_j - 2 pi fhet x_j) mod 2 pi, pb = b_j - 2 pi fhet, pc, pd, pt = t0 - x_j
+//   channel relative phase (spline on the TDI grid y): ca, cb, cc, cd, ct = t0 - y_j
+//   channel amplitude (same grid): aa, ab, ac, ad
+struct WvMixInterval {
+  float4 p0;  // pa.hi, pa.lo, pb.hi, pb.lo
+  float4 p1;  // pc, pd, pt.hi, pt.lo
+  float4 c0;  // ca.hi, ca.lo, cb.hi, cb.lo
+  float4 c1;  // cc, cd, ct.hi, ct.lo
+  float4 a;   // amplitude coefficients
+};
+
+// As wv_layers_kernel in mixed precision.  The sample phase — barycentre
+// phase at the light-time-shifted time minus the heterodyne, plus the
+// channel's relative phase — is evaluated in double-float arithmetic from the
+// per-interval constants above (so no FP64 instruction runs per sample), with
+// the linear terms and the light-time projection k.r0 in double-float and the
+// quadratic and cubic terms (< 0.1 rad) in FP32, then reduced mod 2 pi.  The
+// amplitude spline, the cosine, both FFTs and the layer transforms run in
+// FP32.  Coefficients are written divided by the segment's noise scale.
 __global__ void __launch_bounds__(kLayerThreads) wv_layers_mix_kernel(WvGridDev g, int n, const WvSrc *srcs,
                                                                       const double *ssb, const double *tdi,
                                                                       float *coef) {
@@ -666,27 +683,63 @@ __global__ void __launch_bounds__(kLayerThreads) wv_layers_mix_kernel(WvGridDev 
   const int nl = S.nl, NT = g.NT, Nds = NT * (nl + 1), M = Nds / 2, norb = g.norb;
   float2 *zb = reinterpret_cast<float2 *>(sm_raw);
   float2 *lb = zb + M;
+  // interval table: in the layer buffer's place (unused until the samples are in)
+  WvMixInterval *tab = reinterpret_cast<WvMixInterval *>((reinterpret_cast<uintptr_t>(lb) + 15) & ~(uintptr_t)15);
   RadixPlan PM, PN;
   radix_plan(M, PM);
   radix_plan(NT, PN);
   const double *ph_ssb = ssb + (size_t)s * 8 * norb + 4 * norb;
   const double *ca = tdi + ((size_t)s * 3 + ch) * 8 * norb, *cp = ca + 4 * norb;
-  const double k0 = S.k[0], k1 = S.k[1], k2 = S.k[2];
-  const double *r0 = g.r0ds[nl];
-  const double dtds = g.wdt / (double)(nl + 1);
+  const double w_het = kPI2 * S.fhet;
+  for (int j = threadIdx.x; j < norb; j += blockDim.x) {
+    const double x = g.orb_t[j], y = g.tssb[j];
+    double pa = ph_ssb[j] - w_het * x;
+    pa = pa - kPI2 * rint(pa * (1.0 / kPI2));
+    const df dpa = df_from_double(pa), dpb = df_from_double(ph_ssb[norb + j] - w_het);
+    const df dpt = df_from_double(g.t0 - x), dca = df_from_double(cp[j]), dcb = df_from_double(cp[norb + j]);
+    const df dct = df_from_double(g.t0 - y);
+    WvMixInterval I;
+    I.p0 = make_float4(dpa.hi, dpa.lo, dpb.hi, dpb.lo);
+    I.p1 = make_float4((float)ph_ssb[2 * norb + j], (float)ph_ssb[3 * norb + j], dpt.hi, dpt.lo);
+    I.c0 = make_float4(dca.hi, dca.lo, dcb.hi, dcb.lo);
+    I.c1 = make_float4((float)cp[2 * norb + j], (float)cp[3 * norb + j], dct.hi, dct.lo);
+    I.a = make_float4((float)ca[j], (float)ca[norb + j], (float)ca[2 * norb + j], (float)ca[3 * norb + j]);
+    tab[j] = I;
+  }
+  const df k0 = df_from_double(S.k[0]), k1 = df_from_double(S.k[1]), k2 = df_from_double(S.k[2]);
+  const df whet = df_from_double(w_het);
+  const df dtds = df_from_double(g.wdt / (double)(nl + 1));
+  const float dtds_f = dtds.hi;
+  // interval search in FP32: a sample within a few seconds of a node may take
+  // the neighbouring interval, whose cubic agrees there to rounding
+  const float x0 = (float)(g.t0 - g.orb_t[0]), inv_dx = (float)(1.0 / (g.orb_t[1] - g.orb_t[0]));
+  const float y0 = (float)(g.t0 - g.tssb[0]), inv_dy = (float)(1.0 / (g.tssb[1] - g.tssb[0]));
+  const float *r0h = g.r0hi[nl], *r0l = g.r0lo[nl];
+  __syncthreads();
   for (int i = threadIdx.x; i < Nds; i += blockDim.x) {
-    const double tds = g.t0 + i * dtds;
-    const double phhet = kPI2 * S.fhet * tds;
-    const double kr = k0 * r0[3 * i + 0] + k1 * r0[3 * i + 1] + k2 * r0[3 * i + 2];
-    const double tsc = tds - kr;
-    const int je = even_index(g.orb_t, norb, tsc);
-    const int jb = bin_index(g.tssb, norb, tds);
-    const double dd = tds - g.tssb[jb];
-    // the whole phase in FP64 (the channel's relative phase reaches tens of
-    // radians over a year), reduced mod 2 pi before it is rounded to FP32
-    const double ph = spl_eval(cp, norb, jb, dd) + (spl_eval(ph_ssb, norb, je, tsc - g.orb_t[je]) - phhet);
-    const float pr = (float)(ph - kPI2 * rint(ph * (1.0 / kPI2)));
-    const float a = spl_eval_f(ca, norb, jb, (float)dd);
+    const float fi = (float)i;
+    const df idt = df_mul_f(dtds, fi);  // tds - t0
+    df kr = df_mul(k0, df{r0h[3 * i + 0], r0l[3 * i + 0]});
+    kr = df_add(kr, df_mul(k1, df{r0h[3 * i + 1], r0l[3 * i + 1]}));
+    kr = df_add(kr, df_mul(k2, df{r0h[3 * i + 2], r0l[3 * i + 2]}));
+    const float tf = fmaf(fi, dtds_f, 0.f);
+    const int je = min(max((int)floorf((x0 + tf - kr.hi) * inv_dx), 0), norb - 1);
+    const int jb = min(max((int)floorf((y0 + tf) * inv_dy), 0), norb - 2);
+    const WvMixInterval &P = tab[je];
+    const WvMixInterval &C = tab[jb];
+    const float4 p0 = P.p0, p1 = P.p1, c0 = C.c0, c1 = C.c1, am = C.a;
+    // u = tsc - x_je = (t0 - x_je) + (tds - t0) - k.r0;  v = tds - y_jb
+    const df u = df_add(df_add(df{p1.z, p1.w}, idt), df_neg(kr));
+    const df v = df_add(df{c1.z, c1.w}, idt);
+    const float uf = u.hi, vf = v.hi;
+    df ph = df_add(df{p0.x, p0.y}, df_mul(df{p0.z, p0.w}, u));
+    ph = df_add(ph, df_neg(df_mul(whet, kr)));
+    ph = df_add(ph, df{c0.x, c0.y});
+    ph = df_add(ph, df_mul(df{c0.z, c0.w}, v));
+    const float small = fmaf(fmaf(p1.y, uf, p1.x), uf * uf, fmaf(c1.y, vf, c1.x) * (vf * vf));
+    ph = df_add(ph, df{small, 0.f});
+    const float pr = df_reduce_2pi(ph);
+    const float a = fmaf(fmaf(fmaf(am.w, vf, am.z), vf, am.y), vf, am.x);
     float *slot = reinterpret_cast<float *>(zb + digit_rev(i >> 1, PM));
     slot[i & 1] = a * cosf(pr);
   }
@@ -1001,7 +1054,7 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
   // per layer count: S/C 1 at the downsampled times, window, twiddles
   std::vector<double> r0[kWvMaxLayers + 1], win[kWvMaxLayers + 1];
   std::vector<double2> tw[kWvMaxLayers + 1];
-  std::vector<float> win32[kWvMaxLayers + 1];
+  std::vector<float> win32[kWvMaxLayers + 1], r0hi[kWvMaxLayers + 1], r0lo[kWvMaxLayers + 1];
   std::vector<float2> tw32[kWvMaxLayers + 1];
   for (int nl = 1; nl <= kWvMaxLayers; nl++) {
     const int Nds = NT * (nl + 1);
@@ -1022,13 +1075,19 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
       tw32[nl][k] = make_float2((float)c, (float)sn);
     }
     win32[nl].assign(win[nl].begin(), win[nl].end());
+    r0hi[nl].resize(r0[nl].size());
+    r0lo[nl].resize(r0[nl].size());
+    for (size_t q = 0; q < r0[nl].size(); q++) {
+      r0hi[nl][q] = (float)r0[nl][q];
+      r0lo[nl][q] = (float)(r0[nl][q] - (double)r0hi[nl][q]);
+    }
   }
   // one allocation
   auto pad = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t bytes = pad(8 * (size_t)norb) * 2 + pad(8 * geo.size()) + pad(8 * fac_orb.size()) * 2;
   for (int nl = 1; nl <= kWvMaxLayers; nl++)
     bytes += pad(8 * r0[nl].size()) + pad(8 * win[nl].size()) + pad(16 * tw[nl].size()) + pad(4 * win32[nl].size()) +
-             pad(8 * tw32[nl].size());
+             pad(8 * tw32[nl].size()) + 2 * pad(4 * r0hi[nl].size());
   char *base = nullptr;
   cudaError_t e = cudaMalloc((void **)&base, bytes);
   if (e != cudaSuccess) return e;
@@ -1050,12 +1109,15 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
   g->tw[0] = nullptr;
   g->win32[0] = nullptr;
   g->tw32[0] = nullptr;
+  g->r0hi[0] = g->r0lo[0] = nullptr;
   for (int nl = 1; nl <= kWvMaxLayers; nl++) {
     g->r0ds[nl] = (const double *)put(r0[nl].data(), 8 * r0[nl].size());
     g->win[nl] = (const double *)put(win[nl].data(), 8 * win[nl].size());
     g->tw[nl] = (const double2 *)put(tw[nl].data(), 16 * tw[nl].size());
     g->win32[nl] = (const float *)put(win32[nl].data(), 4 * win32[nl].size());
     g->tw32[nl] = (const float2 *)put(tw32[nl].data(), 8 * tw32[nl].size());
+    g->r0hi[nl] = (const float *)put(r0hi[nl].data(), 4 * r0hi[nl].size());
+    g->r0lo[nl] = (const float *)put(r0lo[nl].data(), 4 * r0lo[nl].size());
   }
   if (e != cudaSuccess) return e;
   g->NF = h.NF;
@@ -1087,7 +1149,10 @@ cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int preci
   wv_tdi_kernel<<<(3 * n + 127) / 128, 128, 0, s>>>(g, n, w.src, w.resp, w.tdi);
   cudaError_t e;
   if (precision == 1) {
-    const size_t sm = layers_smem(g.NT) / 2;  // float2
+    // float2 samples and layer buffer; the interval table shares the layer
+    // buffer's place and may be larger than it
+    const size_t sm = sizeof(float2) * (size_t)g.NT * (kWvMaxLayers + 1) / 2 +
+                      std::max(sizeof(float2) * (size_t)g.NT, sizeof(WvMixInterval) * (size_t)norb + 16);
     e = cudaFuncSetAttribute(wv_layers_mix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     wv_layers_mix_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, reinterpret_cast<float *>(w.coef));

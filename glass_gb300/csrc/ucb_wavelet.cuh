@@ -40,6 +40,7 @@ struct WvGridDev {
   // r^T invC r (FP64); templates are produced divided by s
   const float2 *tw32[kWvMaxLayers + 1];
   const float *win32[kWvMaxLayers + 1];
+  const float *r0hi[kWvMaxLayers + 1], *r0lo[kWvMaxLayers + 1];  // r0ds as hi + lo floats
   const float *res_hi, *res_lo;  // [3][N]
   const float *invC32;           // [9][N]
   const double *qpix;            // [N]
