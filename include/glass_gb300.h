@@ -301,7 +301,8 @@ int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, const doubl
  * precision GLASS_PREC_FP64: everything in FP64 with the reference's order
  * of operations (delta logL to 1e-10 of the reference).  GLASS_PREC_MIXED: the
  * sample phase (carrier at S/C 1 minus the heterodyne, plus the channel's
- * relative phase) in FP64 and reduced mod 2 pi, the amplitude spline, FFTs and
+ * relative phase) to FP64 accuracy (FP64 per-interval constants, double-float
+ * per sample) and reduced mod 2 pi, the amplitude spline, FFTs and
  * layer transforms in FP32, the likelihood from FP32 products with
  * double-float sums, per pixel in the form (residual or direct) with the
  * smaller rounding error.  Its error against FP64 is set by the FP32 template
