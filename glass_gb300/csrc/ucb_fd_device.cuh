@@ -58,7 +58,8 @@ __device__ __forceinline__ void group_sync() {
 // k = i mod p, and writes y[(i-k)R + k + m p].  Every thread holds its
 // butterflies' inputs in registers between the two barriers of a stage, which
 // lets the stage overwrite its own input.  CH series are processed per round to
-// bound register use.
+// bound register use; rounds touch disjoint series, so a round's loads need no
+// barrier after the previous round's stores, only one at the end of the stage.
 template <int N, int GT, int NSER, int CH, typename C, int SYNC_GT = GT>
 __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
   constexpr int LOG = ilog2c(N);
@@ -111,8 +112,8 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
           o[2 * p] = csub(a, c);
           o[3 * p] = csub(bb, d);
         }
-      group_sync<SYNC_GT>();
     }
+    group_sync<SYNC_GT>();
     p *= 4;
   }
   if constexpr (LOG & 1) {
@@ -144,8 +145,8 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
           buf[(c0 + s) * N + j] = cadd(v[s][b][0], u1);
           buf[(c0 + s) * N + j + p] = csub(v[s][b][0], u1);
         }
-      group_sync<SYNC_GT>();
     }
+    group_sync<SYNC_GT>();
   }
 }
 

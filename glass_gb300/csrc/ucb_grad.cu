@@ -334,29 +334,9 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
       for (int s = 0; s < kGradSeries; s++) sbuf[(size_t)s * N + n] = accs[s];
     }
     group_sync<GT>();
-    // FFT each template's four series and whiten/weight them per bin
-#pragma unroll 1
-    for (int t = 0; t < kGradTemplates; t++) {
-      float2 *fbuf = sbuf + (size_t)4 * t * N;
-      group_fft<N, GT, 4, 4>(fbuf, tw, lane);
-#pragma unroll
-      for (int r = 0; r < 4; r++) {
-        const int k = lane + GT * r;
-        const int m = (k + N / 2) & (N - 1);
-        const int j = imin + m;
-        float2 vA = make_float2(0.f, 0.f), vE = vA;
-        if (j >= 0 && j < NFFT) {
-          const size_t sj = (size_t)seg * NFFT + j;
-          const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
-          vA = cadd(cmul(fbuf[k], make_float2(gA.x, gA.y)), cmul(fbuf[N + k], make_float2(gA.z, gA.w)));
-          vE = cadd(cmul(fbuf[2 * N + k], make_float2(gE.x, gE.y)), cmul(fbuf[3 * N + k], make_float2(gE.z, gE.w)));
-        }
-        // bin k's four values are read by this thread only: overwrite in place
-        fbuf[k] = vA;
-        fbuf[N + k] = vE;
-      }
-      group_sync<GT>();
-    }
+    // FFT all 24 series (whitening is applied per bin below, with the
+    // segment's TDI/whitening table loaded once per bin for all templates)
+    group_fft<N, GT, kGradSeries, 4>(sbuf, tw, lane);
     // assemble the eight derivatives per bin and accumulate
     float accg[NACC];
 #pragma unroll
@@ -366,8 +346,12 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     const float2 DP = make_float2(it.DP[0], it.DP[1]), DC = make_float2(it.DC[0], it.DC[1]);
     const float2 dDPi = make_float2(it.dDP_i[0], it.dDP_i[1]), dDCi = make_float2(it.dDC_i[0], it.dDC_i[1]);
     const float2 dDPs = make_float2(it.dDP_s[0], it.dDP_s[1]), dDCs = make_float2(it.dDC_s[0], it.dDC_s[1]);
-    // whitened template t, channel ch (0 A, 1 E) at bin k
-    auto W = [&](int t, int ch, int k) { return sbuf[(size_t)(4 * t + ch) * N + k]; };
+    // whitened template t, channel ch (0 A, 1 E) at bin k: the channel's two
+    // arm-combination spectra times the bin's table entries
+    auto W = [&](int t, int ch, int k, float4 gt) {
+      const float2 *f = sbuf + (size_t)(4 * t + 2 * ch) * N + k;
+      return cadd(cmul(f[0], make_float2(gt.x, gt.y)), cmul(f[N], make_float2(gt.z, gt.w)));
+    };
 #pragma unroll 1
     for (int r = 0; r < 4; r++) {
       const int k = lane + GT * r;
@@ -376,6 +360,7 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
       if (j < 0 || j >= NFFT) continue;
       const size_t sj = (size_t)seg * NFFT + j;
       const float4 w = a.w32[sj], wl = a.w32lo[sj];
+      const float4 gAE[2] = {a.g32[2 * sj], a.g32[2 * sj + 1]};
       float qw[2] = {1.f, 1.f};
       if (a.fisher_mode == 1) {
         const float2 ic_t = a.invc[(size_t)seg * NFFT + m], ic_j = a.invc[sj];
@@ -384,17 +369,18 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
       }
 #pragma unroll
       for (int ch = 0; ch < 2; ch++) {
-        const float2 Hp = cscale(W(0, ch, k), s), Hx = cscale(W(1, ch, k), s);
+        const float4 gt = gAE[ch];
+        const float2 Hp = cscale(W(0, ch, k, gt), s), Hx = cscale(W(1, ch, k, gt), s);
         const float2 h = cadd(cmul(DP, Hp), cmul(DC, Hx));
         float2 D[8];
-        D[0] = cscale(W(2, ch, k), s);
-        D[1] = cscale(W(4, ch, k), s);
-        D[2] = cscale(W(5, ch, k), s);
+        D[0] = cscale(W(2, ch, k, gt), s);
+        D[1] = cscale(W(4, ch, k, gt), s);
+        D[2] = cscale(W(5, ch, k, gt), s);
         D[3] = h;
         D[4] = cadd(cmul(dDPi, Hp), cmul(dDCi, Hx));
         D[5] = cadd(cmul(dDPs, Hp), cmul(dDCs, Hx));
         D[6] = cmi(h);
-        D[7] = cscale(W(3, ch, k), s);
+        D[7] = cscale(W(3, ch, k, gt), s);
         const float wr = ch ? w.z : w.x, wi = ch ? w.w : w.y;
         const float lr = ch ? wl.z : wl.x, li = ch ? wl.w : wl.y;
         const float rr = (wr - h.x) + lr, ri = (wi - h.y) + li;
