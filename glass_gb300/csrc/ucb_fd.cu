@@ -120,10 +120,7 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
         float bw = 2.f * Tf * ((4.f + 6.2831853f * f0f * (float)(kAU / kCLIGHT) * sinthf) / (float)kYEAR +
                                fabsf(fdotf) * Tf);
         int DS = pow2_above_f32(bw - 1.f);
-        if (DS < 0) {
-          double fdot = p[7] / (T * T);
-          DS = pow2_above_dev(2 * T * ((4. + kPI2 * f0 * (kAU / kCLIGHT) * sin(acos(p[1]))) / kYEAR + fabs(fdot) * T) - 1);
-        }
+        if (DS < 0) DS = doppler_spread_fp64(T, f0, p[7] / (T * T), p[1]);
         if (DS > Nmax) DS = Nmax;
         if (DS < Nmin) DS = Nmin;
         const float x = f0f / (float)a.fstar;
@@ -139,10 +136,7 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
                              2.f * (3.f + 2.f * cx + c2x) * ((float)(kSLOC / 2.0) + (float)kSACC / (w2 * w2) * red));
         const float snrm = ampf * sqrtf(Tf) * sx * twoL / sqrtf(sn4L2);
         int SS = pow2_above_f32(snrm - 1.f);
-        if (SS < 0) {
-          double sn64 = aenoise_dev(f0, a.L, a.fstar);
-          SS = pow2_above_dev(exp(p[3]) * sqrt(T) * sin(f0 / a.fstar) / sqrt(sn64) - 1);
-        }
+        if (SS < 0) SS = snr_spread_fp64(T, f0, p[3], a.L, a.fstar);
         if (SS > Nmax) SS = Nmax;
         if (SS < Nmin) SS = Nmin;
         N = 2 * ((DS > SS) ? DS : SS);

@@ -175,6 +175,35 @@ __device__ __forceinline__ int pow2_above_dev(double v) {
   return e > 30 ? (1 << 30) : (1 << e);
 }
 
+// FP64 re-evaluation of the two spreads of the bandwidth rule for the mixed
+// plans, taken when the FP32 estimate lies within 1e-4 of a power of two.
+// Same formulas as ucb/src/glass_ucb_waveform.c:708-722 and AEnoise
+// (utils/src/glass_lisa.c:1188-1198), evaluated with one sincos and products:
+// sin(acos(c)) as sqrt((1 - c)(1 + c)), x^10 as ((x^2)^2)^2 x^2, cos 2x as
+// 2 cos^2 x - 1.  These agree with the library forms to a few ulp, so N can
+// differ from the reference's only for a spread within ~1e-15 of a power of
+// two (where the reference's own result depends on its libm).  A lane that
+// takes this path runs a few hundred FP64 instructions; the library forms
+// (acos, sin, pow) cost several times that on the FP64 pipe and made this rare
+// lane the tail of the whole plan launch.
+__device__ __forceinline__ int doppler_spread_fp64(double T, double f0, double fdot, double costheta) {
+  const double sintheta = sqrt((1.0 - costheta) * (1.0 + costheta));
+  return pow2_above_dev(2 * T * ((4. + kPI2 * f0 * (kAU / kCLIGHT) * sintheta) / kYEAR + fabs(fdot) * T) - 1);
+}
+__device__ __forceinline__ int snr_spread_fp64(double T, double f0, double lnA, double L, double fstar) {
+  const double x = f0 / fstar;
+  double sf, cf;
+  sincos(x, &sf, &cf);
+  const double r = 1.0e-4 / f0, q = 2.0e-5 / f0, q2 = q * q, q4 = q2 * q2;
+  const double red = 1. + 16.0 * (q4 * q4 * q2 + r * r);
+  const double w = kPI2 * f0, w2 = w * w;
+  const double c2x = 2.0 * cf * cf - 1.0;
+  const double sn = (16.0 / 3.0) * sf * sf *
+                    ((2.0 + cf) * (kSPS + kSLOC) + 2.0 * (3.0 + 2.0 * cf + c2x) * (kSLOC / 2.0 + kSACC / (w2 * w2) * red)) /
+                    ((2.0 * L) * (2.0 * L));
+  return pow2_above_dev(exp(lnA) * sqrt(T) * sf / sqrt(sn) - 1);
+}
+
 // ucb/src/glass_ucb_waveform.c:698-725 (ucb_bandwidth).
 static __device__ int bandwidth_dev(double L, double fstar, double f, double fdot, double costheta, double A,
                                     double T, int NFFT) {
@@ -553,11 +582,7 @@ __device__ __forceinline__ int planmix_item(const PlanArgs &a, int i, int N_fixe
     // Doppler spread (ucb/src/glass_ucb_waveform.c:708-714)
     float bw = 2.f * Tf * ((4.f + 6.2831853f * f0f * (float)(kAU / kCLIGHT) * sinthf) / (float)kYEAR + fabsf(fdotf) * Tf);
     int DS = pow2_above_f32(bw - 1.f);
-    if (DS < 0) {
-      double sintheta = sin(acos(p[1]));
-      double fdot = p[7] / (T * T);
-      DS = pow2_above_dev(2 * T * ((4. + kPI2 * f0 * (kAU / kCLIGHT) * sintheta) / kYEAR + fabs(fdot) * T) - 1);
-    }
+    if (DS < 0) DS = doppler_spread_fp64(T, f0, p[7] / (T * T), p[1]);
     if (DS > Nmax) DS = Nmax;
     if (DS < Nmin) DS = Nmin;
     // SNR spread (:717-722) with AEnoise (utils/src/glass_lisa.c:1188-1198)
@@ -575,10 +600,7 @@ __device__ __forceinline__ int planmix_item(const PlanArgs &a, int i, int N_fixe
                          2.f * (3.f + 2.f * cx + c2x) * ((float)(kSLOC / 2.0) + (float)kSACC / (w2 * w2) * red));
     const float snrm = ampf * sqrtf(Tf) * sx * twoL / sqrtf(sn4L2);
     int SS = pow2_above_f32(snrm - 1.f);
-    if (SS < 0) {
-      double sn64 = aenoise_dev(f0, a.L, a.fstar);
-      SS = pow2_above_dev(exp(p[3]) * sqrt(T) * sin(f0 / a.fstar) / sqrt(sn64) - 1);
-    }
+    if (SS < 0) SS = snr_spread_fp64(T, f0, p[3], a.L, a.fstar);
     if (SS > Nmax) SS = Nmax;
     if (SS < Nmin) SS = Nmin;
     N = 2 * ((DS > SS) ? DS : SS);
