@@ -860,15 +860,12 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
     }
     group_sync<GT>();
   }
-  double corr = 0.0;
+  df sa, sh, sc;
   if constexpr (MIX) {
     float2 *redf = reinterpret_cast<float2 *>(red);
-    df sa = group_sum_df<GT>(facc, redf, lane);
-    df sh = group_sum_df<GT>(fh, redf + 32, lane);
-    df sc = group_sum_df<GT>(fc, redf + 64, lane);
-    acc = (double)sa.hi + (double)sa.lo;
-    hacc = (double)sh.hi + (double)sh.lo;
-    corr = (double)sc.hi + (double)sc.lo;
+    sa = group_sum_df<GT>(facc, redf, lane);
+    sh = group_sum_df<GT>(fh, redf + 32, lane);
+    sc = group_sum_df<GT>(fc, redf + 64, lane);
   } else {
     acc = group_sum<GT>(acc, red, lane);
     hacc = group_sum<GT>(hacc, red + 32, lane);
@@ -876,15 +873,19 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   if (valid && lane == 0) {
     double term, hh;
     if constexpr (MIX) {
+      // FP64 only for the final sum (GB300's FP64 pipe is slow, and this runs
+      // once per proposal at the end of every unit)
       const ItemMix &c = a.itemsmix[item];
       int jlo = imin < 0 ? 0 : imin;
       int jhi = imin + N > NFFT ? NFFT : imin + N;
       const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
       // sum |w - s H|^2 with s = amp_hi (1 + rho), rho = amp_lo/amp_hi: with
-      // d = w - amp_hi H, |w - s H|^2 = |d|^2 - 2 rho Re(d* amp_hi H) + O(rho^2)
-      const double rho = (double)c.amp_lo / (double)c.amp_hi;
-      term = (Qs[jhi] - Qs[jlo]) - acc + 2.0 * rho * corr;
-      hh = 2.0 * (1.0 + rho) * (1.0 + rho) * hacc;
+      // d = w - amp_hi H, |w - s H|^2 = |d|^2 - 2 rho Re(d* amp_hi H) + O(rho^2);
+      // |rho| < 6e-8, so the correction and (1 + rho)^2 are FP32 to spare
+      const float rho = __fdiv_rn(c.amp_lo, c.amp_hi);
+      const df tail = df_add(df_neg(sa), df{2.f * rho * sc.hi, 0.f});
+      term = ((Qs[jhi] - Qs[jlo]) + (double)tail.hi) + (double)tail.lo;
+      hh = (double)(2.f * (1.f + rho) * (1.f + rho) * (sh.hi + sh.lo));
     } else {
       term = acc;
       hh = 2.0 * hacc;
