@@ -150,6 +150,156 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
   }
 }
 
+// ---------------------------------------------------- register-resident FFT
+// Shared-memory index of point e of a series whose rows of 16 points are
+// padded to 17: the strided accesses of the stages below then fall on
+// distinct banks.
+__host__ __device__ constexpr int pad16(int e) { return e + (e >> 4); }
+
+// v * exp(-2 pi i J / 16) for a compile-time J.
+template <int J>
+__device__ __forceinline__ float2 w16mul(float2 v) {
+  constexpr int j = J & 15;
+  if constexpr (j == 0) {
+    return v;
+  } else if constexpr (j == 4) {
+    return cmi(v);
+  } else if constexpr (j == 8) {
+    return make_float2(-v.x, -v.y);
+  } else if constexpr (j == 12) {
+    return make_float2(-v.y, v.x);
+  } else {
+    // cos and sin of 2 pi j / 16 (multiples of pi/8)
+    constexpr float c8[16] = {1.f, 0.923879532511286756f, 0.707106781186547524f, 0.382683432365089772f, 0.f,
+                              -0.382683432365089772f, -0.707106781186547524f, -0.923879532511286756f, -1.f,
+                              -0.923879532511286756f, -0.707106781186547524f, -0.382683432365089772f, 0.f,
+                              0.382683432365089772f, 0.707106781186547524f, 0.923879532511286756f};
+    constexpr float c = c8[j], sn = c8[(j + 12) & 15];  // sin x = cos(x - pi/2)
+    return make_float2(fmaf(v.x, c, v.y * sn), fmaf(v.y, c, -(v.x * sn)));
+  }
+}
+
+__device__ __forceinline__ void dft4_inplace(float2 &v0, float2 &v1, float2 &v2, float2 &v3) {
+  const float2 a = cadd(v0, v2), b = csub(v0, v2), c = cadd(v1, v3), d = cmi(csub(v1, v3));
+  v0 = cadd(a, c);
+  v1 = cadd(b, d);
+  v2 = csub(a, c);
+  v3 = csub(b, d);
+}
+
+// Forward DFT of R = 2, 4, 8 or 16 points in registers, natural order out.
+// R = R1 R2 is split as m = m1 + R1 m2, k = k2 + R2 k1: R1 DFTs of R2 points,
+// twiddles exp(-2 pi i m1 k2 / R), R2 DFTs of R1 points.
+template <int R>
+__device__ __forceinline__ void dft_reg(float2 *v) {
+  if constexpr (R == 2) {
+    const float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  } else if constexpr (R == 4) {
+    dft4_inplace(v[0], v[1], v[2], v[3]);
+  } else if constexpr (R == 8) {
+    dft4_inplace(v[0], v[2], v[4], v[6]);
+    dft4_inplace(v[1], v[3], v[5], v[7]);
+    v[3] = w16mul<2>(v[3]);
+    v[5] = w16mul<4>(v[5]);
+    v[7] = w16mul<6>(v[7]);
+    float2 o[8];
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      o[k2] = cadd(v[2 * k2], v[2 * k2 + 1]);
+      o[k2 + 4] = csub(v[2 * k2], v[2 * k2 + 1]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = o[q];
+  } else {
+    static_assert(R == 16, "radix");
+#pragma unroll
+    for (int m1 = 0; m1 < 4; ++m1) dft4_inplace(v[m1], v[m1 + 4], v[m1 + 8], v[m1 + 12]);
+    // v[m1 + 4 k2] *= w16^(m1 k2)
+    v[5] = w16mul<1>(v[5]);
+    v[6] = w16mul<2>(v[6]);
+    v[7] = w16mul<3>(v[7]);
+    v[9] = w16mul<2>(v[9]);
+    v[10] = w16mul<4>(v[10]);
+    v[11] = w16mul<6>(v[11]);
+    v[13] = w16mul<3>(v[13]);
+    v[14] = w16mul<6>(v[14]);
+    v[15] = w16mul<9>(v[15]);
+    float2 o[16];
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      float2 a0 = v[4 * k2], a1 = v[4 * k2 + 1], a2 = v[4 * k2 + 2], a3 = v[4 * k2 + 3];
+      dft4_inplace(a0, a1, a2, a3);
+      o[k2] = a0;
+      o[k2 + 4] = a1;
+      o[k2 + 8] = a2;
+      o[k2 + 12] = a3;
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = o[q];
+  }
+}
+
+// One Stockham stage of radix R and sub-transform size P on a padded series
+// y of length N, by the M = N/16 threads of the series (thread t does the
+// 16/R butterflies i = t + M b): reads x[i + m N/R], multiplies by
+// exp(-2 pi i m k / (P R)), k = i mod P, and writes y[(i - k) R + k + q P].
+// tw: exp(-2 pi i j / N) at pad16(j).
+template <int N, int GT, int R, int P>
+__device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, float2 *v) {
+  constexpr int M = N / 16, NB = 16 / R, STRIDE = N / R, TS = N / (P * R);
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int i = t + M * b, k = i & (P - 1);
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      float2 val = y[pad16(i + m * STRIDE)];
+      if (m > 0) val = cmul(val, tw[pad16(m * k * TS)]);
+      v[b * R + m] = val;
+    }
+  }
+  group_sync<GT>();  // every read of the stage before the in-place writes
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    dft_reg<R>(v + b * R);
+    const int i = t + M * b, k = i & (P - 1);
+#pragma unroll
+    for (int q = 0; q < R; ++q) y[pad16((i - k) * R + k + q * P)] = v[b * R + q];
+  }
+  group_sync<GT>();
+}
+
+// Forward DFT (exp(-2 pi i k n / N), unnormalised) of the 4 series of one
+// proposal, N = 16 M with 32 <= N <= 4096, by a group of GT = 4 M threads:
+// series s = lane / M, thread t = lane % M holds 16 points in registers.
+// Stockham stages of radix 16 (a 4 x 4 split in registers) and one final stage
+// of the remaining radix: 2 stages for N <= 256, 3 up to 4096 (the radix-4
+// version, group_fft, needs log4 N).  The first stage reads the series from
+// global memory (src, 4 series of N back to back); every stage writes the
+// padded shared-memory series sbuf (stride pad16(N)), natural order at the end.
+template <int N, int GT>
+__device__ __forceinline__ void fft4_reg(const float2 *src, float2 *sbuf, const float2 *tw, int lane) {
+  constexpr int M = N / 16, SN = pad16(N);
+  static_assert(4 * M == GT && N >= 32 && N <= 4096, "fft4_reg shape");
+  const int s = lane / M, t = lane - (lane / M) * M;
+  const float2 *x = src + (size_t)s * N;
+  float2 *y = sbuf + s * SN;
+  float2 v[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = x[t + m * M];
+  dft_reg<16>(v);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) y[pad16(t * 16 + q)] = v[q];
+  group_sync<GT>();
+  if constexpr (M >= 16) {
+    reg_stage<N, GT, 16, 16>(y, tw, t, v);
+    if constexpr (N / 256 > 1) reg_stage<N, GT, N / 256, 256>(y, tw, t, v);
+  } else {
+    reg_stage<N, GT, M, 16>(y, tw, t, v);
+  }
+}
+
 // ------------------------------------------------------- per-proposal constants
 // utils/src/glass_lisa.c:1188-1198 (AEnoise) with rednoise (:1183).
 static __device__ double aenoise_dev(double f, double L, double fstar) {
@@ -734,8 +884,10 @@ struct SpecSmem {
   using C = typename std::conditional<MIX, float2, double2>::type;
   static constexpr int NSER = (!MIX && N == 4096) ? 2 : 4;  // series resident at once
   static constexpr int PASSES = 4 / NSER;
+  // mixed: twiddles and series in padded rows (pad16)
+  static constexpr int SN = MIX ? pad16(N) : N;
   static constexpr size_t bytes =
-      sizeof(C) * (size_t)N * (1 + (size_t)SpecCfg<N>::GPC * NSER) + sizeof(double) * 3 * 32;
+      sizeof(C) * (size_t)SN * (1 + (size_t)SpecCfg<N>::GPC * NSER) + sizeof(double) * 3 * 32;
 };
 
 // Sum over the threads of one group (result valid in lane 0 of the group).
@@ -795,7 +947,8 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   constexpr int CH = MIX ? 4 : 2;
   constexpr int B = N / GT;  // bins per thread (4)
   const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
-  C *buf = bufs + (size_t)g * NSER * N;
+  constexpr int SN = S::SN;
+  C *buf = bufs + (size_t)g * NSER * SN;
   double *red = reds + 96 * g;
   const int NFFT = a.NFFT;
   const int slot = base + g;
@@ -815,12 +968,16 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   double acc = 0.0, hacc = 0.0;
 #pragma unroll 1
   for (int pass = 0; pass < PASSES; ++pass) {
+    if constexpr (MIX) {
+      fft4_reg<N, GT>(src, buf, tw, lane);
+    } else {
 #pragma unroll
-    for (int s = 0; s < NSER; ++s)
+      for (int s = 0; s < NSER; ++s)
 #pragma unroll
-      for (int r = 0; r < B; ++r) buf[s * N + lane + GT * r] = src[(size_t)(pass * NSER + s) * N + lane + GT * r];
-    group_sync<GT>();
-    group_fft<N, GT, NSER, (CH < NSER ? CH : NSER)>(buf, tw, lane);
+        for (int r = 0; r < B; ++r) buf[s * N + lane + GT * r] = src[(size_t)(pass * NSER + s) * N + lane + GT * r];
+      group_sync<GT>();
+      group_fft<N, GT, NSER, (CH < NSER ? CH : NSER)>(buf, tw, lane);
+    }
 #pragma unroll
     for (int r = 0; r < B; ++r) {
       const int k = lane + GT * r;
@@ -832,8 +989,9 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
         const float4 w = a.w32[sj];
         const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
         const float sh = a.itemsmix[item].amp_hi;
-        float2 HA = cadd(cmul(buf[0 * N + k], make_float2(gA.x, gA.y)), cmul(buf[1 * N + k], make_float2(gA.z, gA.w)));
-        float2 HE = cadd(cmul(buf[2 * N + k], make_float2(gE.x, gE.y)), cmul(buf[3 * N + k], make_float2(gE.z, gE.w)));
+        const int kp = pad16(k);
+        float2 HA = cadd(cmul(buf[0 * SN + kp], make_float2(gA.x, gA.y)), cmul(buf[1 * SN + kp], make_float2(gA.z, gA.w)));
+        float2 HE = cadd(cmul(buf[2 * SN + kp], make_float2(gE.x, gE.y)), cmul(buf[3 * SN + kp], make_float2(gE.z, gE.w)));
         // template scaled by amp_hi (O(1) whitened values; the unscaled
         // product would overflow FP32 when squared)
         const float2 hA = cscale(HA, sh), hE = cscale(HE, sh);
@@ -906,12 +1064,13 @@ __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   using C = typename S::C;
   constexpr int GPC = Cfg::GPC, NSER = S::NSER;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int SN = S::SN;
   C *tw = reinterpret_cast<C *>(smem_raw);
-  C *bufs = tw + N;
-  double *red = reinterpret_cast<double *>(bufs + (size_t)GPC * NSER * N);
+  C *bufs = tw + SN;
+  double *red = reinterpret_cast<double *>(bufs + (size_t)GPC * NSER * SN);
 
   const C *twg = reinterpret_cast<const C *>(a.tw);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[MIX ? pad16(i) : i] = twg[i];
   __syncthreads();
   const int count = a.bin_count[a.bin];
   const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, a.bin) * 4;
@@ -930,7 +1089,8 @@ constexpr int kSpecAllBins = 6;  // N = 32 .. 1024
 template <bool MIX>
 struct SpecAllSmem {
   using C = typename std::conditional<MIX, float2, double2>::type;
-  static constexpr size_t bytes = sizeof(C) * (1024 + 4 * 1024) + sizeof(double) * 96 * 4;
+  static constexpr int SN = MIX ? pad16(1024) : 1024;  // mixed: padded rows
+  static constexpr size_t bytes = sizeof(C) * (SN + 4 * SN) + sizeof(double) * 96 * 4;
 };
 
 struct SpecAllArgs {
@@ -946,9 +1106,10 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
   using C = typename SpecAllSmem<MIX>::C;
   const SpecArgs &a = A.a;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int SN = SpecAllSmem<MIX>::SN;
   C *tw = reinterpret_cast<C *>(smem_raw);
-  C *bufs = tw + 1024;
-  double *reds = reinterpret_cast<double *>(bufs + 4 * 1024);
+  C *bufs = tw + SN;
+  double *reds = reinterpret_cast<double *>(bufs + 4 * SN);
   int ustart[kSpecAllBins + 1];  // in largest-first order
   int total = 0;
 #pragma unroll
@@ -972,7 +1133,7 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
     if (b != cur) {
       __syncthreads();
       const C *twg = reinterpret_cast<const C *>(A.tw[b]);
-      for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = twg[i];
+      for (int i = threadIdx.x; i < N; i += blockDim.x) tw[MIX ? pad16(i) : i] = twg[i];
       __syncthreads();
       cur = b;
     }
