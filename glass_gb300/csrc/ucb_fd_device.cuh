@@ -554,6 +554,39 @@ __device__ __forceinline__ void slow_sample64(const ItemF64 &c, const OrbitSampl
   }
 }
 
+// Carrier phase common to the three spacecraft, reduced mod 2 pi:
+//   eps2pi u - (beta1 cos a + beta2 sin a) - phi0 + p7pi u^2
+// from double-float constants and table values, as one error-free dot
+// product: exact high products (two_prod), their cross terms and every
+// rounding error of the high-part sum (two_sum) collected in one FP32 error
+// term, one reduction at the end (~55 FP32 instructions; the same to FP32
+// rounding of the reduced angle as df_mul/df_add chains, which take ~100).
+__device__ __forceinline__ float carrier_phase_mix(const ItemMix &c, const OrbitSampleMix &o) {
+  const float uh = o.u_hi, ul = o.u_lo;
+  // u^2 as hi + lo
+  const df uu = two_prod(uh, uh);
+  const float uul = fmaf(2.f * uh, ul, uu.lo);
+  // products
+  const df p1 = two_prod(c.eps2pi.hi, uh);
+  float err = fmaf(c.eps2pi.hi, ul, fmaf(c.eps2pi.lo, uh, p1.lo));
+  const df p2 = two_prod(-c.beta1.hi, o.ca_hi);
+  err += fmaf(-c.beta1.hi, o.ca_lo, fmaf(-c.beta1.lo, o.ca_hi, p2.lo));
+  const df p3 = two_prod(-c.beta2.hi, o.sa_hi);
+  err += fmaf(-c.beta2.hi, o.sa_lo, fmaf(-c.beta2.lo, o.sa_hi, p3.lo));
+  const df p4 = two_prod(c.p7pi_d.hi, uu.hi);
+  err += fmaf(c.p7pi_d.hi, uul, fmaf(c.p7pi_d.lo, uu.hi, p4.lo));
+  // high parts, exactly
+  df sum = two_sum(p1.hi, p2.hi);
+  err += sum.lo;
+  sum = two_sum(sum.hi, p3.hi);
+  err += sum.lo;
+  sum = two_sum(sum.hi, p4.hi);
+  err += sum.lo;
+  sum = two_sum(sum.hi, -c.phi0.hi);
+  err += sum.lo - c.phi0.lo;
+  return df_reduce_2pi(quick_two_sum(sum.hi, err));
+}
+
 // Mixed precision: the carrier phase common to the three spacecraft
 // (heterodyne 2 pi (f0 T - q) t/T, guiding-centre Doppler 2 pi f0 k.x_gc/c,
 // phi0 and pi fdot t^2) is summed in double-float and reduced mod 2 pi; the
@@ -581,14 +614,7 @@ __device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSam
   const float kr13 = c.k[0] * r13[0] + c.k[1] * r13[1] + c.k[2] * r13[2];
   const float kr23 = c.k[0] * r23[0] + c.k[1] * r23[1] + c.k[2] * r23[2];
 
-  // common carrier phase in double-float
-  const df u = {o.u_hi, o.u_lo};
-  const df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
-  df ph = df_mul(c.eps2pi, u);
-  ph = df_add(ph, df_neg(df_add(df_mul(c.beta1, cad), df_mul(c.beta2, sad))));
-  ph = df_add(ph, df_neg(c.phi0));
-  ph = df_add(ph, df_mul(c.p7pi_d, df_mul(u, u)));
-  const float psi0 = df_reduce_2pi(ph);
+  const float psi0 = carrier_phase_mix(c, o);
   const float uf = o.u_hi;
   const float tgc = AUc * (c.k[0] * ca + c.k[1] * sa);  // guiding-centre delay (s)
 

@@ -143,13 +143,7 @@ __device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad 
     dz[i] = -1.73205080757f * K.Rf * (ca * cbf[i] + sa * sbf[i]);
   }
   // carrier phase (double-float) common to the three spacecraft
-  const df u = {o.u_hi, o.u_lo};
-  const df cad = {o.ca_hi, o.ca_lo}, sad = {o.sa_hi, o.sa_lo};
-  df ph = df_mul(c.eps2pi, u);
-  ph = df_add(ph, df_neg(df_add(df_mul(c.beta1, cad), df_mul(c.beta2, sad))));
-  ph = df_add(ph, df_neg(c.phi0));
-  ph = df_add(ph, df_mul(c.p7pi_d, df_mul(u, u)));
-  const float psi0 = df_reduce_2pi(ph);
+  const float psi0 = carrier_phase_mix(c, o);
   const float uf = o.u_hi;
   const float tgc = K.AUcf * (c.k[0] * ca + c.k[1] * sa);
   const float gx = K.AUf * ca, gy = K.AUf * sa;  // guiding centre (m)
