@@ -68,9 +68,11 @@ def spec_flops_per_eval(N):
 
 
 # DRAM bytes (read + write) per launch of the Fourier step's kernels, from one
-# ncu capture each of this workload's mixed step (profiles/fd_*_mixed_step.md);
-# None where no capture was made.
-PROFILED_DRAM_BYTES = {"fd_spec_all_kernel<1>": None, "fd_slow_kernel<1>": None}
+# ncu capture each of this workload's mixed step (profiles/fd_*_mixed_step.md).
+# ncu flushes the caches before the launch, so the spectral kernel's figure is
+# its series scratch (4 x N complex floats per proposal, ~29 MB) read from DRAM;
+# in a live step the slow-part kernel has just written it to L2.
+PROFILED_DRAM_BYTES = {"fd_spec_all_kernel<1>": 31018800 + 768, "fd_slow_kernel<1>": 598528}
 
 
 def make_workload(rank, steps):
