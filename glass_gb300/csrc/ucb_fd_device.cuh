@@ -246,8 +246,8 @@ __device__ __forceinline__ void dft_reg(float2 *v) {
 // 16/R butterflies i = t + M b): reads x[i + m N/R], multiplies by
 // exp(-2 pi i m k / (P R)), k = i mod P, and writes y[(i - k) R + k + q P].
 // tw: exp(-2 pi i j / N) at pad16(j).
-template <int N, int GT, int R, int P>
-__device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, float2 *v) {
+template <int N, int R, int P>
+__device__ __forceinline__ void reg_stage_load(const float2 *y, const float2 *tw, int t, float2 *v) {
   constexpr int M = N / 16, NB = 16 / R, STRIDE = N / R, TS = N / (P * R);
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
@@ -255,11 +255,14 @@ __device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, fl
 #pragma unroll
     for (int m = 0; m < R; ++m) {
       float2 val = y[pad16(i + m * STRIDE)];
-      if (m > 0) val = cmul(val, tw[pad16(m * k * TS)]);
+      if (P > 1 && m > 0) val = cmul(val, tw[pad16(m * k * TS)]);
       v[b * R + m] = val;
     }
   }
-  group_sync<GT>();  // every read of the stage before the in-place writes
+}
+template <int N, int R, int P>
+__device__ __forceinline__ void reg_stage_store(float2 *y, int t, float2 *v) {
+  constexpr int M = N / 16, NB = 16 / R;
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
     dft_reg<R>(v + b * R);
@@ -267,7 +270,46 @@ __device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, fl
 #pragma unroll
     for (int q = 0; q < R; ++q) y[pad16((i - k) * R + k + q * P)] = v[b * R + q];
   }
+}
+template <int N, int GT, int R, int P>
+__device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, float2 *v) {
+  reg_stage_load<N, R, P>(y, tw, t, v);
+  group_sync<GT>();  // every read of the stage before the in-place writes
+  reg_stage_store<N, R, P>(y, t, v);
   group_sync<GT>();
+}
+
+// One stage of fft_reg_smem over NSER series in rounds of 4 (one series per
+// M threads): rounds touch disjoint series, so a round's loads need no
+// barrier after the previous round's stores, only one before its own stores.
+template <int N, int GT, int NSER, int R, int P>
+__device__ __forceinline__ void reg_stage_rounds(float2 *sbuf, const float2 *tw, int s, int t, float2 *v) {
+  constexpr int SN = pad16(N);
+#pragma unroll 1
+  for (int r = 0; r < NSER / 4; ++r) {
+    float2 *y = sbuf + (4 * r + s) * SN;
+    reg_stage_load<N, R, P>(y, tw, t, v);
+    group_sync<GT>();
+    reg_stage_store<N, R, P>(y, t, v);
+  }
+  group_sync<GT>();
+}
+
+// As fft4_reg for NSER (a multiple of 4) series already in the padded
+// shared-memory layout (series stride pad16(N)), transformed in place.
+template <int N, int GT, int NSER>
+__device__ __forceinline__ void fft_reg_smem(float2 *sbuf, const float2 *tw, int lane) {
+  constexpr int M = N / 16;
+  static_assert(4 * M == GT && NSER % 4 == 0 && N >= 32 && N <= 4096, "fft_reg_smem shape");
+  const int s = lane / M, t = lane - (lane / M) * M;
+  float2 v[16];
+  reg_stage_rounds<N, GT, NSER, 16, 1>(sbuf, tw, s, t, v);
+  if constexpr (M >= 16) {
+    reg_stage_rounds<N, GT, NSER, 16, 16>(sbuf, tw, s, t, v);
+    if constexpr (N / 256 > 1) reg_stage_rounds<N, GT, NSER, N / 256, 256>(sbuf, tw, s, t, v);
+  } else {
+    reg_stage_rounds<N, GT, NSER, M, 16>(sbuf, tw, s, t, v);
+  }
 }
 
 // Forward DFT (exp(-2 pi i k n / N), unnormalised) of the 4 series of one

@@ -284,10 +284,10 @@ struct GradCfg {
   static constexpr int CTA = GT >= 64 ? GT : 128;
   static constexpr int GPC = CTA / GT;
   static constexpr int NACC = 8 + 36;  // gradient, Fisher upper triangle
-  // 24 series of N per group; after each template's FFT its whitened A and E
-  // spectra overwrite the first 2N of the template's own 4N
-  static constexpr size_t group_floats2 = (size_t)kGradSeries * N;
-  static constexpr size_t bytes = sizeof(float2) * (N + GPC * group_floats2) + sizeof(float2) * 32 * GPC;
+  // 24 series of N per group in padded rows (pad16), twiddles likewise
+  static constexpr int SN = pad16(N);
+  static constexpr size_t group_floats2 = (size_t)kGradSeries * SN;
+  static constexpr size_t bytes = sizeof(float2) * (SN + GPC * group_floats2) + sizeof(float2) * 32 * GPC;
 };
 
 // One group of N/4 threads per proposal: the 24 series are computed sample by
@@ -299,13 +299,14 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
   using Cfg = GradCfg<N>;
   constexpr int GT = Cfg::GT, GPC = Cfg::GPC, NACC = Cfg::NACC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int SN = Cfg::SN;
   float2 *tw = reinterpret_cast<float2 *>(smem_raw);
-  float2 *groups = tw + N;
+  float2 *groups = tw + SN;
   float2 *redall = groups + GPC * Cfg::group_floats2;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw[i];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[pad16(i)] = a.tw[i];
   __syncthreads();
   const int g = threadIdx.x / GT, lane = threadIdx.x % GT;
-  float2 *sbuf = groups + g * Cfg::group_floats2;  // [s N + n], s = 4 t + combo
+  float2 *sbuf = groups + g * Cfg::group_floats2;  // [s SN + pad16(n)], s = 4 t + combo
   float *part = reinterpret_cast<float *>(sbuf);   // reduction scratch after use
   float2 *red = redall + 32 * g;
   const int count = a.bin_count[a.bin];
@@ -325,12 +326,12 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
       float2 accs[kGradSeries];
       grad_sample(a.K, it, a.mix[n], accs);
 #pragma unroll
-      for (int s = 0; s < kGradSeries; s++) sbuf[(size_t)s * N + n] = accs[s];
+      for (int s = 0; s < kGradSeries; s++) sbuf[(size_t)s * SN + pad16(n)] = accs[s];
     }
     group_sync<GT>();
     // FFT all 24 series (whitening is applied per bin below, with the
     // segment's TDI/whitening table loaded once per bin for all templates)
-    group_fft<N, GT, kGradSeries, 4>(sbuf, tw, lane);
+    fft_reg_smem<N, GT, kGradSeries>(sbuf, tw, lane);
     // assemble the eight derivatives per bin and accumulate
     float accg[NACC];
 #pragma unroll
@@ -343,8 +344,8 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     // whitened template t, channel ch (0 A, 1 E) at bin k: the channel's two
     // arm-combination spectra times the bin's table entries
     auto W = [&](int t, int ch, int k, float4 gt) {
-      const float2 *f = sbuf + (size_t)(4 * t + 2 * ch) * N + k;
-      return cadd(cmul(f[0], make_float2(gt.x, gt.y)), cmul(f[N], make_float2(gt.z, gt.w)));
+      const float2 *f = sbuf + (size_t)(4 * t + 2 * ch) * SN + pad16(k);
+      return cadd(cmul(f[0], make_float2(gt.x, gt.y)), cmul(f[SN], make_float2(gt.z, gt.w)));
     };
 #pragma unroll 1
     for (int r = 0; r < 4; r++) {
