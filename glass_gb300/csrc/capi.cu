@@ -58,6 +58,13 @@ struct glass_gpu_ctx {
   // staging for the host-pointer entry points
   void *d_stage = nullptr;
   size_t d_stage_cap = 0;
+  // glass_gpu_dlogl_batch_host: pinned host staging, and the copy-in, kernels,
+  // copy-out sequence recorded as a CUDA graph per (nitems, precision,
+  // term_x given); the graphs hold the staging, work and bank addresses, so
+  // they are dropped whenever one of those is reallocated
+  void *h_stage = nullptr;
+  size_t h_stage_cap = 0;
+  std::map<long long, cudaGraphExec_t> host_graphs;
   int last_launches = 0;
   int n_fixed = 0;  // template size override (0: bandwidth rule)
   WdmPlan wdm;      // tables and work buffers of the last WDM grid used
@@ -71,6 +78,11 @@ struct glass_gpu_ctx {
   WvWorkDev wvw;
   void *wv_work_mem = nullptr;
 };
+
+static void clear_host_graphs(glass_gpu_ctx *ctx) {
+  for (auto &g : ctx->host_graphs) cudaGraphExecDestroy(g.second);
+  ctx->host_graphs.clear();
+}
 
 static int ctx_activate(glass_gpu_ctx *ctx) {
   GLASS_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
@@ -123,6 +135,8 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->work.bin_list);
   cudaFree(ctx->work.series);
   cudaFree(ctx->d_stage);
+  clear_host_graphs(ctx);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   wdm_release(ctx->wdm);
   cudaFree(ctx->wdm_stage);
   cudaFree(ctx->wv_grid_mem);
@@ -176,6 +190,7 @@ static int is_pow2_in_range(int n);
 extern "C" int glass_gpu_set_template_size(glass_gpu_ctx *ctx, int n) {
   if (!ctx) return set_err(GLASS_ERR_ARG, "set_template_size: null context");
   if (n != 0 && !is_pow2_in_range(n)) return set_err(GLASS_ERR_SIZE, "set_template_size: n must be 0 or a power of two in [32, 4096]");
+  if (ctx->n_fixed != n) clear_host_graphs(ctx);  // n is a kernel argument in the graphs
   ctx->n_fixed = n;
   return GLASS_OK;
 }
@@ -207,6 +222,7 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   fd_build_bank_tables(format, T, fstar, NFFT, nseg, qmin, rA, rE, invCA, invCE, w32.data(), w32lo.data(),
                        g32.data(), Q.data(), w64.data(), g64.data());
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "bank_upload sync");
+  clear_host_graphs(ctx);
   cudaFree(ctx->bank_mem);
   ctx->bank_mem = nullptr;
   size_t off_q = sizeof(int) * ((nseg + 63) / 64 * 64);
@@ -307,6 +323,7 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   if (gseries > series) series = gseries;
   if (nitems <= w.cap && series <= w.series_bytes) return GLASS_OK;
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "work sync");
+  clear_host_graphs(ctx);
   cudaFree(w.items64);
   cudaFree(w.itemsmix);
   cudaFree(w.itemsgrad);
@@ -363,10 +380,45 @@ extern "C" int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nite
 static int ensure_stage(glass_gpu_ctx *ctx, size_t bytes) {
   if (bytes <= ctx->d_stage_cap) return GLASS_OK;
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "stage sync");
+  clear_host_graphs(ctx);
   cudaFree(ctx->d_stage);
   ctx->d_stage = nullptr;
   GLASS_CUDA(cudaMalloc(&ctx->d_stage, bytes), "cudaMalloc(stage)");
   ctx->d_stage_cap = bytes;
+  return GLASS_OK;
+}
+
+static int ensure_host_stage(glass_gpu_ctx *ctx, size_t bytes) {
+  if (bytes <= ctx->h_stage_cap) return GLASS_OK;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "host stage sync");
+  clear_host_graphs(ctx);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  ctx->h_stage = nullptr;
+  ctx->h_stage_cap = 0;
+  GLASS_CUDA(cudaMallocHost(&ctx->h_stage, bytes), "cudaMallocHost(stage)");
+  ctx->h_stage_cap = bytes;
+  return GLASS_OK;
+}
+
+// Copy-in, the batch, copy-out on the context's stream; stage layout (device
+// and pinned host alike): inputs params (8n doubles) | term_x (n doubles) |
+// item_seg (n ints), then at out_off the outputs dlogl | term_y | hh (n
+// doubles each) | status (n ints).
+static int dlogl_host_enqueue(glass_gpu_ctx *ctx, int precision, int nitems, bool has_tx, size_t in_bytes,
+                              size_t out_off, size_t out_bytes) {
+  const size_t nd = (size_t)nitems;
+  char *d = (char *)ctx->d_stage;
+  char *h = (char *)ctx->h_stage;
+  double *d_params = (double *)d, *d_tx = d_params + 8 * nd;
+  int *d_seg = (int *)(d_tx + nd);
+  double *d_dl = (double *)(d + out_off), *d_ty = d_dl + nd, *d_hh = d_ty + nd;
+  int *d_st = (int *)(d_hh + nd);
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d, h, in_bytes, cudaMemcpyHostToDevice, s), "H2D batch inputs");
+  int rc = glass_gpu_dlogl_batch(ctx, precision, nitems, d_seg, d_params, has_tx ? d_tx : nullptr, d_dl, d_ty, d_hh,
+                                 d_st);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(h + out_off, d + out_off, out_bytes, cudaMemcpyDeviceToHost, s), "D2H batch outputs");
   return GLASS_OK;
 }
 
@@ -377,30 +429,57 @@ extern "C" int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int
   if (nitems < 0) return set_err(GLASS_ERR_ARG, "dlogl_batch_host: negative item count");
   if (nitems == 0) return GLASS_OK;
   if (!item_seg || !params || !dlogl) return set_err(GLASS_ERR_ARG, "dlogl_batch_host: null argument");
+  if (precision != GLASS_PREC_FP64 && precision != GLASS_PREC_MIXED)
+    return set_err(GLASS_ERR_ARG, "dlogl_batch_host: unknown precision");
+  if (!ctx->bank.nseg) return set_err(GLASS_ERR_STATE, "dlogl_batch_host: no segment bank uploaded");
   int rc = ctx_activate(ctx);
   if (rc) return rc;
-  // layout: params | term_x | dlogl | term_y | hh (doubles) | item_seg | status (ints)
-  size_t nd = (size_t)nitems;
-  size_t bytes = sizeof(double) * nd * 12 + sizeof(int) * nd * 2 + 256;
+  const size_t nd = (size_t)nitems;
+  const bool has_tx = term_x != nullptr;
+  const size_t in_bytes = sizeof(double) * 9 * nd + sizeof(int) * nd;
+  const size_t out_off = (in_bytes + 255) / 256 * 256;
+  const size_t out_bytes = sizeof(double) * 3 * nd + sizeof(int) * nd;
+  const size_t bytes = out_off + out_bytes;
+  // buffers first, so that nothing is reallocated while a graph is recorded
   if ((rc = ensure_stage(ctx, bytes))) return rc;
-  double *d_params = (double *)ctx->d_stage;
-  double *d_tx = d_params + 8 * nd;
-  double *d_dl = d_tx + nd;
-  double *d_ty = d_dl + nd;
-  double *d_hh = d_ty + nd;
-  int *d_seg = (int *)(d_hh + nd);
-  int *d_st = d_seg + nd;
+  if ((rc = ensure_host_stage(ctx, bytes))) return rc;
+  if ((rc = ensure_work(ctx, nitems))) return rc;
+  char *h = (char *)ctx->h_stage;
+  memcpy(h, params, sizeof(double) * 8 * nd);
+  if (has_tx) memcpy(h + sizeof(double) * 8 * nd, term_x, sizeof(double) * nd);
+  memcpy(h + sizeof(double) * 9 * nd, item_seg, sizeof(int) * nd);
   cudaStream_t s = ctx->stream;
-  GLASS_CUDA(cudaMemcpyAsync(d_params, params, sizeof(double) * 8 * nd, cudaMemcpyHostToDevice, s), "H2D params");
-  GLASS_CUDA(cudaMemcpyAsync(d_seg, item_seg, sizeof(int) * nd, cudaMemcpyHostToDevice, s), "H2D item_seg");
-  if (term_x) GLASS_CUDA(cudaMemcpyAsync(d_tx, term_x, sizeof(double) * nd, cudaMemcpyHostToDevice, s), "H2D term_x");
-  rc = glass_gpu_dlogl_batch(ctx, precision, nitems, d_seg, d_params, term_x ? d_tx : nullptr, d_dl, d_ty, d_hh, d_st);
-  if (rc) return rc;
-  GLASS_CUDA(cudaMemcpyAsync(dlogl, d_dl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H dlogl");
-  if (term_y) GLASS_CUDA(cudaMemcpyAsync(term_y, d_ty, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H term_y");
-  if (hh) GLASS_CUDA(cudaMemcpyAsync(hh, d_hh, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H hh");
-  if (status) GLASS_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int) * nd, cudaMemcpyDeviceToHost, s), "D2H status");
+  const long long key = ((long long)nitems << 3) | ((long long)precision << 1) | (has_tx ? 1 : 0);
+  auto it = ctx->host_graphs.find(key);
+  if (it != ctx->host_graphs.end() && !ctx->work.phase_timing) {
+    GLASS_CUDA(cudaGraphLaunch(it->second, s), "dlogl_batch_host graph launch");
+    ctx->last_launches = 3;
+  } else {
+    if ((rc = dlogl_host_enqueue(ctx, precision, nitems, has_tx, in_bytes, out_off, out_bytes))) return rc;
+    GLASS_CUDA(cudaStreamSynchronize(s), "dlogl_batch_host sync");
+    if (!ctx->work.phase_timing && ctx->host_graphs.size() < 64) {
+      // record the sequence for the next calls of this shape (a stream that
+      // cannot be captured keeps the direct path)
+      const int nl = ctx->last_launches;
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int rc2 = dlogl_host_enqueue(ctx, precision, nitems, has_tx, in_bytes, out_off, out_bytes);
+        const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+        if (rc2 == GLASS_OK && e2 == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess)
+          ctx->host_graphs[key] = ge;
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();
+      ctx->last_launches = nl;
+    }
+  }
   GLASS_CUDA(cudaStreamSynchronize(s), "dlogl_batch_host sync");
+  const char *o = h + out_off;
+  memcpy(dlogl, o, sizeof(double) * nd);
+  if (term_y) memcpy(term_y, o + sizeof(double) * nd, sizeof(double) * nd);
+  if (hh) memcpy(hh, o + sizeof(double) * 2 * nd, sizeof(double) * nd);
+  if (status) memcpy(status, o + sizeof(double) * 3 * nd, sizeof(int) * nd);
   return GLASS_OK;
 }
 

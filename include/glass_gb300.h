@@ -133,7 +133,13 @@ int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const i
                           const double *term_x, double *dlogl, double *term_y, double *hh, int *status);
 
 /* Same as glass_gpu_dlogl_batch with HOST pointers: copies in, evaluates,
- * copies out and synchronises. */
+ * copies out and synchronises.  The inputs go through one pinned staging
+ * buffer of the context (one copy each way), and the copy-in, kernels and
+ * copy-out of a batch shape (nitems, precision, term_x given or not) are
+ * recorded as a CUDA graph on the first call and replayed on later calls of
+ * that shape; a new bank, a new template size or larger buffers drop the
+ * recorded graphs.  Not to be called while the context's stream is being
+ * captured. */
 int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
                                const double *params, const double *term_x, double *dlogl, double *term_y, double *hh,
                                int *status);

@@ -258,3 +258,47 @@ def test_phase_timing(engine, port):
     assert len(ms) == 3 and all(v > 0 for v in ms)
     for a, b in zip(got, ref):
         np.testing.assert_array_equal(a, b)
+
+
+def test_host_entry_point_replays_follow_inputs_and_bank(engine, port):
+    """The host-pointer entry point records its copy-in/kernels/copy-out
+    sequence as a CUDA graph per batch shape and replays it: a replay must see
+    the new inputs, and a new bank or template size must not reuse a graph that
+    holds the old one.  Reference: the device-pointer entry point."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(41)
+    bank, inj = _random_bank(rng, 8, 1024, port)
+    engine.upload(bank)
+    seg = np.repeat(np.arange(8, dtype=np.int32), 24)
+    draws = [np.vstack([wl.gaussian_jumps(rng, inj[s], wl.jump_scales(inj[s], 20.0), 24) for s in range(8)])
+             for _ in range(3)]
+    txs = [rng.normal(0, 5, len(seg)) for _ in range(3)]
+
+    def device(params, tx, prec):
+        d = torch.empty(len(seg), dtype=torch.float64, device="cuda")
+        ty, hh = torch.empty_like(d), torch.empty_like(d)
+        st = torch.empty(len(seg), dtype=torch.int32, device="cuda")
+        dseg = torch.from_numpy(seg).cuda()
+        engine.dlogl_device(dseg, torch.from_numpy(params).cuda(), d, ty, hh, st,
+                            term_x=None if tx is None else torch.from_numpy(tx).cuda(), precision=prec)
+        torch.cuda.synchronize()
+        return d.cpu().numpy(), ty.cpu().numpy(), hh.cpu().numpy(), st.cpu().numpy()
+
+    for prec in (gg.PREC_MIXED, gg.PREC_FP64):
+        for k in (0, 1, 2, 1, 0):  # first call records, the others replay
+            got = engine.dlogl_host(seg, draws[k], term_x=txs[k], precision=prec)
+            for a, b in zip(got, device(draws[k], txs[k], prec)):
+                np.testing.assert_array_equal(a, b)
+        got = engine.dlogl_host(seg, draws[2], precision=prec)  # no term_x: another shape
+        np.testing.assert_array_equal(got[0], device(draws[2], None, prec)[0])
+    # a new bank (new device buffers) and a fixed template size
+    bank2, inj2 = _random_bank(rng, 8, 1024, port)
+    engine.upload(bank2)
+    got = engine.dlogl_host(seg, draws[0], term_x=txs[0], precision=gg.PREC_MIXED)
+    np.testing.assert_array_equal(got[0], device(draws[0], txs[0], gg.PREC_MIXED)[0])
+    engine.set_template_size(256)
+    try:
+        got = engine.dlogl_host(seg, draws[0], term_x=txs[0], precision=gg.PREC_MIXED)
+        np.testing.assert_array_equal(got[0], device(draws[0], txs[0], gg.PREC_MIXED)[0])
+    finally:
+        engine.set_template_size(0)
