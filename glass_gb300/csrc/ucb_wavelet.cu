@@ -75,103 +75,157 @@ __device__ __forceinline__ int bin_index(const double *x, int n, double v) {
   return j;
 }
 
-// Data part of the natural cubic spline solve (utils/src/glass_math.c:101-175)
-// on a grid whose factors fac = {h, l, mu} are precomputed; c[0..n) holds y.
-__device__ void spline_sweeps(double *c, int n, const double *fac) {
-  const double *h = fac, *l = fac + n, *mu = fac + 2 * n;
-  double *c0 = c, *c1 = c + n, *c2 = c + 2 * n, *c3 = c + 3 * n;
+// Natural cubic spline solve (utils/src/glass_math.c:101-175) on a grid whose
+// factors fac = {h, l, mu} are precomputed, split for a CTA that handles many
+// value arrays at once: spline_rhs for node i (the forward sweep's right-hand
+// side, independent per node), spline_recurrence for one array on one thread
+// (the two sequential sweeps on z, which holds the right-hand sides on entry
+// and c2 on exit), spline_coeffs for node i (c1, c3).  Every value has the same
+// FP64 expression as in one sequential sweep.
+__device__ __forceinline__ double spline_rhs(const double *y, int i, const double *h) {
+  return 3.0 * ((y[i + 1] - y[i]) / h[i] - (y[i] - y[i - 1]) / h[i - 1]);
+}
+__device__ __forceinline__ void spline_recurrence(double *z, int N, const double *fac) {
+  const double *h = fac, *l = fac + N, *mu = fac + 2 * N;
   double zprev = 0.0;
-  c2[0] = 0.0;
-  for (int i = 1; i < n - 1; i++) {
-    const double al = 3.0 * ((c0[i + 1] - c0[i]) / h[i] - (c0[i] - c0[i - 1]) / h[i - 1]);
-    zprev = (al - h[i - 1] * zprev) / l[i];
-    c2[i] = zprev;
+  z[0] = 0.0;
+  for (int i = 1; i < N - 1; i++) {
+    zprev = (z[i] - h[i - 1] * zprev) / l[i];
+    z[i] = zprev;
   }
-  c1[n - 1] = 0.0;
-  c2[n - 1] = 0.0;
-  c3[n - 1] = 0.0;
-  for (int i = n - 2; i >= 0; i--) {
-    c2[i] = c2[i] - mu[i] * c2[i + 1];
-    c1[i] = (c0[i + 1] - c0[i]) / h[i] - h[i] * (c2[i + 1] + 2.0 * c2[i]) / 3.0;
-    c3[i] = (c2[i + 1] - c2[i]) / (3.0 * h[i]);
+  z[N - 1] = 0.0;
+  for (int i = N - 2; i >= 0; i--) z[i] = z[i] - mu[i] * z[i + 1];
+}
+// c0..c3 ([4][N], out) of node i from the values y and c2 = z
+__device__ __forceinline__ void spline_coeffs(const double *y, const double *z, int i, int N, const double *h,
+                                              double *out) {
+  out[i] = y[i];
+  out[2 * N + i] = z[i];
+  if (i < N - 1) {
+    out[N + i] = (y[i + 1] - y[i]) / h[i] - h[i] * (z[i + 1] + 2.0 * z[i]) / 3.0;
+    out[3 * N + i] = (z[i + 1] - z[i]) / (3.0 * h[i]);
+  } else {
+    out[N + i] = 0.0;
+    out[3 * N + i] = 0.0;
   }
 }
 
 // ------------------------------------------------------------ plan
-__global__ void wv_plan_kernel(WvGridDev g, int n, const double *params, WvSrc *srcs, double *ssb, int *status) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const double *p = params + 8 * (size_t)s;
-  WvSrc S;
-  const double Tobs = g.Tobs;
-  bool ok = true;
-  for (int q = 0; q < 8; q++) ok = ok && isfinite(p[q]);
-  ok = ok && fabs(p[1]) <= 1.0 && fabs(p[4]) <= 1.0 && p[0] > 0.0;
-  S.status = ok ? 0 : 1;
-  S.jmin = S.nl = S.jlo = S.c = 0;
-  if (ok) {
-    // ucb_wavelet_layers
-    const double fstart = p[0] / Tobs;
-    const double fstop = (p[0] / Tobs + p[7] / Tobs / Tobs);
-    double fmin, fmax;
-    if (fstart < fstop) {
-      fmin = fstart * (1.0 - kVEARTH);
-      fmax = fstop * (1.0 + kVEARTH);
-    } else {
-      fmin = fstop * (1.0 - kVEARTH);
-      fmax = fstart * (1.0 + kVEARTH);
-    }
-    const double jr = rint(fmin / g.wdf);
-    if (!(fabs(jr) < 1e9)) {
-      S.status = 1;
-    } else {
-      const int j = (int)jr;
-      const double dfmin = fmin - j * g.wdf, dfmax = fmax - j * g.wdf;
-      int jmin = j, jmax = j;
-      if (dfmin < 0.0 && fabs(dfmin) > g.A / kPI2) jmin = j - 1;
-      if (dfmax > 0.0 && fabs(dfmax) > g.A / kPI2) jmax = j + 1;
-      S.jmin = jmin;
-      S.nl = jmax - jmin + 1;
-      const int jlo = max(jmin, g.lmin), jhi = min(jmin + S.nl, g.lmax);
-      S.jlo = jlo;
-      S.c = max(0, jhi - jlo);
-    }
-  }
-  // geometry (LISA_polarization_tensor, utils/src/glass_lisa.c:1566-1596)
-  const double costh = p[1], phi = p[2], cosi = p[4], psi = p[5];
-  const double sinth = sqrt(1.0 - costh * costh), cosph = cos(phi), sinph = sin(phi);
-  const double u[3] = {costh * cosph, costh * sinph, -sinth};
-  const double v[3] = {sinph, -cosph, 0.};
-  S.k[0] = -sinth * cosph;
-  S.k[1] = -sinth * sinph;
-  S.k[2] = -costh;
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) {
-      S.ep[3 * i + j] = v[i] * v[j] - u[i] * u[j];
-      S.ec[3 * i + j] = u[i] * v[j] + v[i] * u[j];
-    }
-  S.c2p = cos(2. * psi);
-  S.s2p = sin(2. * psi);
-  S.Ap = 0.5 * (1. + cosi * cosi);
-  S.Ac = -cosi;
-  S.fhet = (S.jmin - 1) * g.wdf;
-  S.pad = 0;
-  srcs[s] = S;
-  if (status) status[s] = S.status;
-  if (S.status) return;
-  // barycentre amplitude and phase on the orbit nodes (ucb_barycenter_waveform,
-  // ucb/src/glass_ucb_waveform.c:330-362), then their splines
+// C sources per CTA of 128 threads, 4 norb doubles of shared memory per
+// source: the per-source record on one thread per source, the barycentre
+// amplitude and phase at the orbit nodes and the spline right-hand sides over
+// all threads (node-parallel), the spline recurrences on one thread per array
+// (2 C threads), the coefficients node-parallel.
+template <int C>
+__global__ void __launch_bounds__(128) wv_plan_kernel(WvGridDev g, int n, const double *params, WvSrc *srcs,
+                                                      double *ssb, int *status) {
+  extern __shared__ __align__(16) double psm[];
+  __shared__ int s_ok[C];
+  __shared__ double s_f0[C], s_phi0[C], s_fdot[C], s_A0[C];
+  const int base = blockIdx.x * C;
+  const int nsrc = min(C, n - base);
   const int norb = g.norb;
-  double *amp = ssb + (size_t)s * 8 * norb, *ph = amp + 4 * norb;
-  const double f0 = p[0] / Tobs, phi0 = p[6], fdot = p[7] / Tobs / Tobs, fddot = 0.0;
-  const double A0 = exp(p[3]);
-  for (int i = 0; i < norb; i++) {
-    const double t = g.orb_t[i];
-    ph[i] = -phi0 + kPI2 * (f0 * t + 0.5 * fdot * t * t + 1.0 / 6.0 * fddot * t * t * t);
-    amp[i] = A0 * (1.0 + 2.0 / 3.0 * fdot / f0 * t);
+  const double Tobs = g.Tobs;
+  if ((int)threadIdx.x < nsrc) {
+    const int s = base + threadIdx.x;
+    const double *p = params + 8 * (size_t)s;
+    WvSrc S;
+    bool ok = true;
+    for (int q = 0; q < 8; q++) ok = ok && isfinite(p[q]);
+    ok = ok && fabs(p[1]) <= 1.0 && fabs(p[4]) <= 1.0 && p[0] > 0.0;
+    S.status = ok ? 0 : 1;
+    S.jmin = S.nl = S.jlo = S.c = 0;
+    if (ok) {
+      // ucb_wavelet_layers
+      const double fstart = p[0] / Tobs;
+      const double fstop = (p[0] / Tobs + p[7] / Tobs / Tobs);
+      double fmin, fmax;
+      if (fstart < fstop) {
+        fmin = fstart * (1.0 - kVEARTH);
+        fmax = fstop * (1.0 + kVEARTH);
+      } else {
+        fmin = fstop * (1.0 - kVEARTH);
+        fmax = fstart * (1.0 + kVEARTH);
+      }
+      const double jr = rint(fmin / g.wdf);
+      if (!(fabs(jr) < 1e9)) {
+        S.status = 1;
+      } else {
+        const int j = (int)jr;
+        const double dfmin = fmin - j * g.wdf, dfmax = fmax - j * g.wdf;
+        int jmin = j, jmax = j;
+        if (dfmin < 0.0 && fabs(dfmin) > g.A / kPI2) jmin = j - 1;
+        if (dfmax > 0.0 && fabs(dfmax) > g.A / kPI2) jmax = j + 1;
+        S.jmin = jmin;
+        S.nl = jmax - jmin + 1;
+        const int jlo = max(jmin, g.lmin), jhi = min(jmin + S.nl, g.lmax);
+        S.jlo = jlo;
+        S.c = max(0, jhi - jlo);
+      }
+    }
+    // geometry (LISA_polarization_tensor, utils/src/glass_lisa.c:1566-1596)
+    const double costh = p[1], phi = p[2], cosi = p[4], psi = p[5];
+    const double sinth = sqrt(1.0 - costh * costh), cosph = cos(phi), sinph = sin(phi);
+    const double u[3] = {costh * cosph, costh * sinph, -sinth};
+    const double v[3] = {sinph, -cosph, 0.};
+    S.k[0] = -sinth * cosph;
+    S.k[1] = -sinth * sinph;
+    S.k[2] = -costh;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        S.ep[3 * i + j] = v[i] * v[j] - u[i] * u[j];
+        S.ec[3 * i + j] = u[i] * v[j] + v[i] * u[j];
+      }
+    S.c2p = cos(2. * psi);
+    S.s2p = sin(2. * psi);
+    S.Ap = 0.5 * (1. + cosi * cosi);
+    S.Ac = -cosi;
+    S.fhet = (S.jmin - 1) * g.wdf;
+    S.pad = 0;
+    srcs[s] = S;
+    if (status) status[s] = S.status;
+    s_ok[threadIdx.x] = S.status == 0;
+    s_f0[threadIdx.x] = p[0] / Tobs;
+    s_phi0[threadIdx.x] = p[6];
+    s_fdot[threadIdx.x] = p[7] / Tobs / Tobs;
+    s_A0[threadIdx.x] = S.status == 0 ? exp(p[3]) : 0.0;
   }
-  spline_sweeps(amp, norb, g.fac_orb);
-  spline_sweeps(ph, norb, g.fac_orb);
+  __syncthreads();
+  // barycentre amplitude and phase on the orbit nodes (ucb_barycenter_waveform,
+  // ucb/src/glass_ucb_waveform.c:330-362)
+  for (int q = threadIdx.x; q < nsrc * norb; q += blockDim.x) {
+    const int c = q / norb, i = q - c * norb;
+    if (!s_ok[c]) continue;
+    double *ya = psm + (size_t)c * 4 * norb, *yp = ya + norb;
+    const double f0 = s_f0[c], phi0 = s_phi0[c], fdot = s_fdot[c], fddot = 0.0;
+    const double A0 = s_A0[c];
+    const double t = g.orb_t[i];
+    yp[i] = -phi0 + kPI2 * (f0 * t + 0.5 * fdot * t * t + 1.0 / 6.0 * fddot * t * t * t);
+    ya[i] = A0 * (1.0 + 2.0 / 3.0 * fdot / f0 * t);
+  }
+  __syncthreads();
+  const double *h = g.fac_orb;
+  for (int q = threadIdx.x; q < nsrc * norb; q += blockDim.x) {
+    const int c = q / norb, i = q - c * norb;
+    if (!s_ok[c] || i == 0 || i == norb - 1) continue;
+    double *ya = psm + (size_t)c * 4 * norb, *yp = ya + norb, *za = ya + 2 * norb, *zp = ya + 3 * norb;
+    za[i] = spline_rhs(ya, i, h);
+    zp[i] = spline_rhs(yp, i, h);
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < 2 * nsrc) {
+    const int c = threadIdx.x >> 1;
+    if (s_ok[c]) spline_recurrence(psm + (size_t)c * 4 * norb + (2 + (threadIdx.x & 1)) * norb, norb, g.fac_orb);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nsrc * norb; q += blockDim.x) {
+    const int c = q / norb, i = q - c * norb;
+    if (!s_ok[c]) continue;
+    const double *ya = psm + (size_t)c * 4 * norb, *yp = ya + norb, *za = ya + 2 * norb, *zp = ya + 3 * norb;
+    double *amp = ssb + (size_t)(base + c) * 8 * norb, *ph = amp + 4 * norb;
+    spline_coeffs(ya, za, i, norb, h, amp);
+    spline_coeffs(yp, zp, i, norb, h, ph);
+  }
 }
 
 // ------------------------------------------------------------ response
@@ -322,61 +376,123 @@ __global__ void wv_resp_kernel(WvGridDev g, int n, const WvSrc *srcs, const doub
 // 1034-1052) and the channel's amplitude / phase splines; one thread per
 // (source, channel).  The flip and phase-jump arrays live in the slots of
 // the spline's c1 and c2 coefficients until the sweeps overwrite them.
-__global__ void wv_tdi_kernel(WvGridDev g, int n, const WvSrc *srcs, const double *resp, double *tdi) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= 3 * n) return;
-  const int s = idx / 3, ch = idx - 3 * s;
-  if (srcs[s].status) return;
+// C (source, channel) pairs per CTA of 128 threads, 4 norb doubles of shared
+// memory per pair: the per-node work (|M + i Mf|, atan2, remainder, the spline
+// right-hand sides and coefficients) over all threads (node-parallel); the
+// flip scan, the unwrapping scan and the spline recurrences on one thread per
+// pair (per array for the recurrences).  The flip and phase-jump arrays use
+// the slots of the two right-hand-side arrays until those are formed.  Every
+// value has the same FP64 expression as in one sequential pass.
+template <int C>
+__global__ void __launch_bounds__(128) wv_tdi_kernel(WvGridDev g, int n, const WvSrc *srcs, const double *resp,
+                                                     double *tdi) {
+  extern __shared__ __align__(16) double tsm[];
+  __shared__ int s_ok[C];
+  const int base = blockIdx.x * C;
+  const int nch = min(C, 3 * n - base);
   const int N = g.norb;
-  const double *M = resp + ((size_t)s * 7 + ch) * N, *Mf = resp + ((size_t)s * 7 + 3 + ch) * N;
-  const double *phR = resp + ((size_t)s * 7 + 6) * N;
-  double *ca = tdi + ((size_t)s * 3 + ch) * 8 * N, *cp = ca + 4 * N;
-  double *As = ca, *flip = ca + N, *pj = ca + 2 * N;
-  for (int i = 0; i < N; i++) As[i] = sqrt(M[i] * M[i] + Mf[i] * Mf[i]);
-  flip[0] = 1.0;
-  pj[0] = 0.0;
-  int i = 1;
-  do {
-    flip[i] = flip[i - 1];
-    pj[i] = pj[i - 1];
-    if ((As[i] < As[i - 1]) && (As[i] < As[i + 1])) {
-      const double d1 = As[i + 1] + As[i - 1] - 2.0 * As[i];
-      const double d2 = -As[i + 1] + As[i - 1] - 2.0 * As[i];
-      const double d3 = -As[i + 1] + As[i - 1] + 2.0 * As[i];
-      if (fabs(d2 / d1) < 0.1) {
-        flip[i + 1] = -1.0 * flip[i];
-        pj[i + 1] = pj[i] + kPI;
-        i++;
+  if ((int)threadIdx.x < nch) s_ok[threadIdx.x] = srcs[(base + threadIdx.x) / 3].status == 0;
+  __syncthreads();
+  // per pair c: As (values of the amplitude spline), Q (phase), then za, zp
+  // (flip and pj until the right-hand sides overwrite them)
+#define WV_TDI_PTRS                                                       \
+  const int idx = base + c, s = idx / 3, ch = idx - 3 * (idx / 3);       \
+  double *As = tsm + (size_t)c * 4 * N, *Q = As + N, *za = As + 2 * N, *zp = As + 3 * N; \
+  const double *M = resp + ((size_t)s * 7 + ch) * N, *Mf = resp + ((size_t)s * 7 + 3 + ch) * N; \
+  (void)M;                                                                \
+  (void)Mf;                                                               \
+  (void)Q;                                                                \
+  (void)za;                                                               \
+  (void)zp;
+  for (int q = threadIdx.x; q < nch * N; q += blockDim.x) {
+    const int c = q / N, i = q - c * N;
+    if (!s_ok[c]) continue;
+    WV_TDI_PTRS
+    As[i] = sqrt(M[i] * M[i] + Mf[i] * Mf[i]);
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nch && s_ok[threadIdx.x]) {
+    const int c = threadIdx.x;
+    WV_TDI_PTRS
+    double *flip = za, *pj = zp;
+    flip[0] = 1.0;
+    pj[0] = 0.0;
+    int i = 1;
+    do {
+      flip[i] = flip[i - 1];
+      pj[i] = pj[i - 1];
+      if ((As[i] < As[i - 1]) && (As[i] < As[i + 1])) {
+        const double d1 = As[i + 1] + As[i - 1] - 2.0 * As[i];
+        const double d2 = -As[i + 1] + As[i - 1] - 2.0 * As[i];
+        const double d3 = -As[i + 1] + As[i - 1] + 2.0 * As[i];
+        if (fabs(d2 / d1) < 0.1) {
+          flip[i + 1] = -1.0 * flip[i];
+          pj[i + 1] = pj[i] + kPI;
+          i++;
+        }
+        if (fabs(d3 / d1) < 0.1) {
+          flip[i] = -1.0 * flip[i - 1];
+          pj[i] = pj[i - 1] + kPI;
+        }
       }
-      if (fabs(d3 / d1) < 0.1) {
-        flip[i] = -1.0 * flip[i - 1];
-        pj[i] = pj[i - 1] + kPI;
-      }
-    }
-    i++;
-  } while (i < N - 1);
-  flip[N - 1] = flip[N - 2];
-  pj[N - 1] = pj[N - 2];
-  for (i = 0; i < N; i++) {
-    As[i] = flip[i] * As[i];
+      i++;
+    } while (i < N - 1);
+    flip[N - 1] = flip[N - 2];
+    pj[N - 1] = pj[N - 2];
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nch * N; q += blockDim.x) {
+    const int c = q / N, i = q - c * N;
+    if (!s_ok[c]) continue;
+    WV_TDI_PTRS
+    const double *phR = resp + ((size_t)s * 7 + 6) * N;
+    As[i] = za[i] * As[i];
     const double v = remainder(phR[i], kPI2);
-    cp[i] = -atan2(Mf[i], M[i]) + pj[i] - v;
+    Q[i] = -atan2(Mf[i], M[i]) + zp[i] - v;
   }
-  double v = cp[0];
-  for (i = 0; i < N; i++) {
-    double u = cp[i];
-    const double q = rint(fabs(u - v) / (kPI2));
-    if (q > 0.0) {
-      if (v > u)
-        u += q * kPI2;
-      else
-        u -= q * kPI2;
+  __syncthreads();
+  if ((int)threadIdx.x < nch && s_ok[threadIdx.x]) {
+    const int c = threadIdx.x;
+    WV_TDI_PTRS
+    double v = Q[0];
+    for (int i = 0; i < N; i++) {
+      double u = Q[i];
+      const double qq = rint(fabs(u - v) / (kPI2));
+      if (qq > 0.0) {
+        if (v > u)
+          u += qq * kPI2;
+        else
+          u -= qq * kPI2;
+      }
+      v = u;
+      Q[i] = u;
     }
-    v = u;
-    cp[i] = u;
   }
-  spline_sweeps(ca, N, g.fac_ssb);
-  spline_sweeps(cp, N, g.fac_ssb);
+  __syncthreads();
+  // natural cubic splines of As and Q (utils/src/glass_math.c:101-175)
+  const double *h = g.fac_ssb;
+  for (int q = threadIdx.x; q < nch * N; q += blockDim.x) {
+    const int c = q / N, i = q - c * N;
+    if (!s_ok[c] || i == 0 || i == N - 1) continue;
+    WV_TDI_PTRS
+    za[i] = spline_rhs(As, i, h);
+    zp[i] = spline_rhs(Q, i, h);
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < 2 * nch && s_ok[threadIdx.x >> 1]) {
+    const int c = threadIdx.x >> 1;
+    spline_recurrence(tsm + (size_t)c * 4 * N + (2 + (threadIdx.x & 1)) * N, N, g.fac_ssb);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nch * N; q += blockDim.x) {
+    const int c = q / N, i = q - c * N;
+    if (!s_ok[c]) continue;
+    WV_TDI_PTRS
+    double *ca = tdi + ((size_t)s * 3 + ch) * 8 * N, *cp = ca + 4 * N;
+    spline_coeffs(As, za, i, N, h, ca);
+    spline_coeffs(Q, zp, i, N, h, cp);
+  }
+#undef WV_TDI_PTRS
 }
 
 // ------------------------------------------------------------ FFTs
@@ -918,7 +1034,7 @@ void wv_analytic_orbit(double Tobs, double t0, std::vector<double> &t, std::vect
 
 namespace {
 
-// Host copy of the cubic spline (same arithmetic as spline_sweeps plus the
+// Host copy of the cubic spline (same arithmetic as warp_spline_pair plus the
 // grid factors), evaluated with the binary-search lookup.
 struct HostSpline {
   int n = 0;
@@ -1139,15 +1255,48 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
 
 static size_t layers_smem(int NT) { return sizeof(double2) * (size_t)NT * (kWvMaxLayers + 1) / 2 + sizeof(double2) * NT; }
 
+// Launches a tile kernel with C = 16, 4 or 1 items per CTA of 128 threads,
+// the largest whose shared memory (C x per bytes) fits 200 KB.
+template <typename K16, typename K4, typename K1, typename... Args>
+static cudaError_t wv_launch_tiles(K16 k16, K4 k4, K1 k1, size_t per, int items, cudaStream_t s, Args... args) {
+  const size_t cap = 200 * 1024;
+  cudaError_t e;
+  if (16 * per <= cap) {
+    if ((e = cudaFuncSetAttribute(k16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(16 * per))) != cudaSuccess)
+      return e;
+    k16<<<(items + 15) / 16, 128, 16 * per, s>>>(args...);
+  } else if (4 * per <= cap) {
+    if ((e = cudaFuncSetAttribute(k4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(4 * per))) != cudaSuccess)
+      return e;
+    k4<<<(items + 3) / 4, 128, 4 * per, s>>>(args...);
+  } else {
+    if ((e = cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)per)) != cudaSuccess) return e;
+    k1<<<items, 128, per, s>>>(args...);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *params,
                                int *status, cudaStream_t s, int *nlaunch) {
   if (n <= 0) return cudaSuccess;
   const int norb = g.norb;
-  wv_plan_kernel<<<(n + 127) / 128, 128, 0, s>>>(g, n, params, w.src, w.ssb, status);
+  cudaError_t e;
+  {
+    // 4 norb doubles of shared memory per source; 16 sources per CTA where
+    // they fit, fewer for long observations
+    const size_t per = sizeof(double) * 4 * (size_t)norb;
+    if ((e = wv_launch_tiles(wv_plan_kernel<16>, wv_plan_kernel<4>, wv_plan_kernel<1>, per, n, s, g, n, params, w.src,
+                             w.ssb, status)) != cudaSuccess)
+      return e;
+  }
   const long long nr = (long long)n * norb;
   wv_resp_kernel<<<(unsigned)((nr + 127) / 128), 128, 0, s>>>(g, n, w.src, w.ssb, w.resp);
-  wv_tdi_kernel<<<(3 * n + 127) / 128, 128, 0, s>>>(g, n, w.src, w.resp, w.tdi);
-  cudaError_t e;
+  {
+    const size_t per = sizeof(double) * 4 * (size_t)norb;
+    if ((e = wv_launch_tiles(wv_tdi_kernel<16>, wv_tdi_kernel<4>, wv_tdi_kernel<1>, per, 3 * n, s, g, n, w.src, w.resp,
+                             w.tdi)) != cudaSuccess)
+      return e;
+  }
   if (precision == 1) {
     // float2 samples and layer buffer; the interval table shares the layer
     // buffer's place and may be larger than it
