@@ -150,5 +150,13 @@ struct OrbitSampleMix {
   float u_hi, u_lo, ca_hi, ca_lo;
   float sa_hi, sa_lo, pad0, pad1;
 };
+// Proposal-independent geometry of one sample for the mixed slow part,
+// computed in FP64 and rounded once: the spacecraft offsets from the guiding
+// centre (metres), f[0..9) = x0 y0 z0 x1 y1 z1 x2 y2 z2, and the monomials of
+// the three unit arms 12, 13, 23 for the quadratic forms r^T M r with M stored
+// xx, xy, xz, yy, yz, zz: f[9 + 6 a ..] = x^2, 2xy, 2xz, y^2, 2yz, z^2.
+struct __align__(16) GeoSampleMix {
+  float f[28];
+};
 
 }  // namespace glass

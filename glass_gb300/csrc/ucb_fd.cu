@@ -278,6 +278,32 @@ __global__ void fd_orbit_table_kernel(FdTablesDev tab, double T, double t0) {
   m.sa_lo = sd.lo;
   m.pad0 = m.pad1 = 0.f;
   tab.mix[b][n] = m;
+  // mixed slow-part geometry: offsets from the guiding centre and arm monomials
+  // (absent from tables built for the FP64 path alone)
+  if (tab.geo[b]) {
+    GeoSampleMix gm;
+    double d[3][3];
+    for (int i = 0; i < 3; i++) {
+      d[i][0] = R * (saca * sbs[i] - (1. + sa2) * cbs[i]);
+      d[i][1] = R * (saca * cbs[i] - (1. + ca2) * sbs[i]);
+      d[i][2] = -kSQ3 * R * (ca * cbs[i] + sa * sbs[i]);
+      for (int q = 0; q < 3; q++) gm.f[3 * i + q] = (float)d[i][q];
+    }
+    const int arm[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int a = 0; a < 3; a++) {
+      double r[3];
+      for (int q = 0; q < 3; q++) r[q] = (d[arm[a][1]][q] - d[arm[a][0]][q]) / kLARM;
+      float *mo = gm.f + 9 + 6 * a;
+      mo[0] = (float)(r[0] * r[0]);
+      mo[1] = (float)(2.0 * r[0] * r[1]);
+      mo[2] = (float)(2.0 * r[0] * r[2]);
+      mo[3] = (float)(r[1] * r[1]);
+      mo[4] = (float)(2.0 * r[1] * r[2]);
+      mo[5] = (float)(r[2] * r[2]);
+    }
+    gm.f[27] = 0.f;
+    tab.geo[b][n] = gm;
+  }
   double s, cth;
   sincospi(-2.0 * (double)n / (double)N, &s, &cth);
   tab.tw64[b][n] = make_double2(cth, s);
@@ -289,7 +315,8 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
     size_t total = 0;
     for (int b = 0; b < kNumBins; b++) {
       int N = 32 << b;
-      total += (size_t)N * (sizeof(OrbitSample64) + sizeof(OrbitSampleMix) + sizeof(float2) + sizeof(double2));
+      total += (size_t)N * (sizeof(OrbitSample64) + sizeof(OrbitSampleMix) + sizeof(GeoSampleMix) + sizeof(float2) +
+                            sizeof(double2));
     }
     cudaError_t e = cudaMalloc(&tab.base, total);
     if (e != cudaSuccess) return e;
@@ -300,6 +327,8 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
       p += (size_t)N * sizeof(OrbitSample64);
       tab.mix[b] = (OrbitSampleMix *)p;
       p += (size_t)N * sizeof(OrbitSampleMix);
+      tab.geo[b] = (GeoSampleMix *)p;
+      p += (size_t)N * sizeof(GeoSampleMix);
       tab.tw64[b] = (double2 *)p;
       p += (size_t)N * sizeof(double2);
       tab.tw32[b] = (float2 *)p;
@@ -426,6 +455,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   for (int b = 0; b < kNumBins; b++) {
     sa.pos64[b] = tab.pos64[b];
     sa.mix[b] = tab.mix[b];
+    sa.geo[b] = tab.geo[b];
   }
   sa.series = work.series;
   e = mix ? fd_launch_slow_mixed(sa, num_sms, stream) : fd_launch_slow_fp64(sa, num_sms, stream);

@@ -25,6 +25,7 @@ struct FdBankDev {
 struct FdTablesDev {
   OrbitSample64 *pos64[kNumBins] = {};
   OrbitSampleMix *mix[kNumBins] = {};
+  GeoSampleMix *geo[kNumBins] = {};
   float2 *tw32[kNumBins] = {};
   double2 *tw64[kNumBins] = {};
   void *base = nullptr;  // single allocation backing all of the above

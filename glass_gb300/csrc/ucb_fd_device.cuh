@@ -633,28 +633,33 @@ __device__ __forceinline__ float carrier_phase_mix(const ItemMix &c, const Orbit
 // (heterodyne 2 pi (f0 T - q) t/T, guiding-centre Doppler 2 pi f0 k.x_gc/c,
 // phi0 and pi fdot t^2) is summed in double-float and reduced mod 2 pi; the
 // per-spacecraft corrections (< 0.5 rad) and everything else are FP32.
-__device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSampleMix &o, float Rorb, float invL,
-                                                float AUc, float invT, float2 d[6]) {
+__device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSampleMix &o, const GeoSampleMix &gm,
+                                                float invL, float AUc, float invT, float2 d[6]) {
   const float ca = o.ca_hi, sa = o.sa_hi;
-  const float sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
-  float dx[3], dy[3], dz[3];
-  const float sbf[3] = {0.0f, 0.866025403784439f, -0.866025403784438f};
-  const float cbf[3] = {1.0f, -0.5f, -0.5f};
+  float f[28];
+  {
+    const float4 *g4 = reinterpret_cast<const float4 *>(gm.f);
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    dx[i] = Rorb * (saca * sbf[i] - (1.f + sa2) * cbf[i]);
-    dy[i] = Rorb * (saca * cbf[i] - (1.f + ca2) * sbf[i]);
-    dz[i] = -1.73205080757f * Rorb * (ca * cbf[i] + sa * sbf[i]);
+    for (int q = 0; q < 7; q++) {
+      const float4 v = g4[q];
+      f[4 * q] = v.x;
+      f[4 * q + 1] = v.y;
+      f[4 * q + 2] = v.z;
+      f[4 * q + 3] = v.w;
+    }
   }
-  float r12[3] = {(dx[1] - dx[0]) * invL, (dy[1] - dy[0]) * invL, (dz[1] - dz[0]) * invL};
-  float r13[3] = {(dx[2] - dx[0]) * invL, (dy[2] - dy[0]) * invL, (dz[2] - dz[0]) * invL};
-  float r23[3] = {(dx[2] - dx[1]) * invL, (dy[2] - dy[1]) * invL, (dz[2] - dz[1]) * invL};
-  const float mr12 = quad(c.Mr, r12[0], r12[1], r12[2]), mi12 = quad(c.Mi, r12[0], r12[1], r12[2]);
-  const float mr13 = quad(c.Mr, r13[0], r13[1], r13[2]), mi13 = quad(c.Mi, r13[0], r13[1], r13[2]);
-  const float mr23 = quad(c.Mr, r23[0], r23[1], r23[2]), mi23 = quad(c.Mi, r23[0], r23[1], r23[2]);
-  const float kr12 = c.k[0] * r12[0] + c.k[1] * r12[1] + c.k[2] * r12[2];
-  const float kr13 = c.k[0] * r13[0] + c.k[1] * r13[1] + c.k[2] * r13[2];
-  const float kr23 = c.k[0] * r23[0] + c.k[1] * r23[1] + c.k[2] * r23[2];
+  // k.(x_i - x_gc) per spacecraft (metres); k.r_ij from their differences
+  float kd[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) kd[i] = fmaf(c.k[0], f[3 * i], fmaf(c.k[1], f[3 * i + 1], c.k[2] * f[3 * i + 2]));
+  const float kr12 = (kd[1] - kd[0]) * invL, kr13 = (kd[2] - kd[0]) * invL, kr23 = (kd[2] - kd[1]) * invL;
+  auto quad6 = [&](const float *M, int a) {
+    const float *mo = f + 9 + 6 * a;
+    return fmaf(M[0], mo[0], fmaf(M[1], mo[1], fmaf(M[2], mo[2], fmaf(M[3], mo[3], fmaf(M[4], mo[4], M[5] * mo[5])))));
+  };
+  const float mr12 = quad6(c.Mr, 0), mi12 = quad6(c.Mi, 0);
+  const float mr13 = quad6(c.Mr, 1), mi13 = quad6(c.Mi, 1);
+  const float mr23 = quad6(c.Mr, 2), mi23 = quad6(c.Mi, 2);
 
   const float psi0 = carrier_phase_mix(c, o);
   const float uf = o.u_hi;
@@ -663,7 +668,7 @@ __device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSam
   float fon[3], arg2[3], aev[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    float kdx = c.k[0] * dx[i] + c.k[1] * dy[i] + c.k[2] * dz[i];  // k.(x_i - x_gc), metres
+    const float kdx = kd[i];  // k.(x_i - x_gc), metres
     float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
     float tT = taui * invT;
     float v = uf - tT;  // xi / T
@@ -858,6 +863,7 @@ struct SlowArgs {
   const ItemMix *itemsmix;
   const OrbitSample64 *pos64[kNumBins];
   const OrbitSampleMix *mix[kNumBins];
+  const GeoSampleMix *geo[kNumBins] = {};  // mixed only
   void *series;  // float2 (mixed) or double2 (FP64)
 };
 
@@ -928,7 +934,7 @@ __global__ void __launch_bounds__(256) fd_slow_kernel(SlowArgs a) {
     const int item = a.bin_list[(size_t)b * a.cap + slot];
     C d[6], cmb[4];
     if constexpr (MIX) {
-      slow_sample_mix(a.itemsmix[item], a.mix[b][n], a.Rf, a.invLf, a.AUcf, a.invTf, d);
+      slow_sample_mix(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.invLf, a.AUcf, a.invTf, d);
     } else {
       slow_sample64(a.items64[item], a.pos64[b][n], a.fstar, a.L, d);
     }
