@@ -310,12 +310,13 @@ def run_reference(args):
     temps = 1.5 ** (np.arange(items) % NTEMP)
     batches = draw_batches(rng, inj, snr, item_seg, temps, 4)
     rAc, rEc = np.ascontiguousarray(rA), np.ascontiguousarray(rE)
+    iAc, iEc = np.ascontiguousarray(bank.invCA), np.ascontiguousarray(bank.invCE)
     threads = os.cpu_count() or 1
     for w in range(args.warmup):
-        port.dlogl_batch(T, NFFT, bank.qmin, rAc, rEc, iA, iE, item_seg, batches[w % 4], None, nthreads=threads)
+        port.dlogl_batch(T, NFFT, bank.qmin, rAc, rEc, iAc, iEc, item_seg, batches[w % 4], None, nthreads=threads)
     t0 = time.perf_counter()
     for k in range(args.steps):
-        port.dlogl_batch(T, NFFT, bank.qmin, rAc, rEc, iA, iE, item_seg, batches[k % 4], None, nthreads=threads)
+        port.dlogl_batch(T, NFFT, bank.qmin, rAc, rEc, iAc, iEc, item_seg, batches[k % 4], None, nthreads=threads)
     el = time.perf_counter() - t0
     v = args.steps * items / el
     line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
