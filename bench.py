@@ -49,6 +49,25 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(values, dev):
+    """The slowest rank's timings: every rank passes its own, all get the
+    element-wise maximum (a no-op for one process).  The whole job's rate is
+    then the units all ranks processed over that time (job_rate)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor(np.asarray(values, np.float64), dtype=torch.float64, device=dev)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.cpu().numpy()
+
+
+def job_rate(steps, units_per_step, world, seconds):
+    """Whole-job throughput under weak scaling: every rank does the same
+    per-step work on its own data."""
+    return steps * units_per_step * world / seconds
+
+
 def flops_per_eval(N):
     """Algorithmic work of one Fourier delta-logL eval of size N (FP32 + FP64
     parts, counted as flops): 48N + 264N + 30 N log2 N + 120N."""
@@ -756,14 +775,8 @@ def run_ours(args):
     t_e2e = time.perf_counter() - t0
 
     # max over ranks
-    times = np.array([t_mixed, t_fp64, t_e2e])
-    if world > 1:
-        tt = torch.tensor(times, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        times = tt.cpu().numpy()
-    t_mixed, t_fp64, t_e2e = times
-    total = args.steps * items * world
-    v_mixed, v_fp64, v_e2e = total / t_mixed, total / t_fp64, total / t_e2e
+    t_mixed, t_fp64, t_e2e = max_over_ranks([t_mixed, t_fp64, t_e2e], dev)
+    v_mixed, v_fp64, v_e2e = (job_rate(args.steps, items, world, t) for t in (t_mixed, t_fp64, t_e2e))
 
     m64 = torch.stack(rec_fp64).cpu().numpy()
     err = torch.stack(rec_mixed).cpu().numpy() - m64
