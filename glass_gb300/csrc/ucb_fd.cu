@@ -88,16 +88,16 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
 // and the double-float carrier constants.  The antenna tensors Mr, Mi are then
 // assembled in FP64 by all 128 threads; only the N-dependent fields wait for
 // the barrier.  Same results as planmix_item (the FP32 constants to rounding).
-// Proposals per CTA: 16 of the 32 lanes of each role warp, so that a batch of
-// a few thousand proposals spreads over every SM (the kernel is latency-bound).
-constexpr int kPlanItems = 16;
+// Proposals per CTA: ceil(n / SMs) lanes of each role warp, at least 16, so
+// that a batch of a few thousand proposals is one wave over every SM (the
+// kernel is latency-bound; a second CTA on some SMs doubles their time).
 
 __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
   __shared__ double s_ep[32][6], s_ec[32][6], s_dp[32][4], s_amp[32];
   __shared__ int s_st[32], s_N[32], s_imin[32];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  const int i = blockIdx.x * kPlanItems + l;
-  const bool in = l < kPlanItems && i < a.nitems;
+  const int i = blockIdx.x * a.per_cta + l;
+  const bool in = l < a.per_cta && i < a.nitems;
   double p[8];
   int seg = 0, st = 1;
   if (in) st = plan_validate(a, i, p, seg);
@@ -431,8 +431,12 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   const bool timing = work.phase_timing;
   work.phase_recorded = false;
   if (timing && (e = cudaEventRecord(work.phase[0], stream)) != cudaSuccess) return e;
+  {
+    int per = (nitems + num_sms - 1) / (num_sms > 0 ? num_sms : 1);
+    pa.per_cta = per < 16 ? 16 : (per > 32 ? 32 : per);
+  }
   if (mix)
-    fd_planmix_kernel<<<(nitems + kPlanItems - 1) / kPlanItems, 128, 0, stream>>>(pa);
+    fd_planmix_kernel<<<(nitems + pa.per_cta - 1) / pa.per_cta, 128, 0, stream>>>(pa);
   else
     fd_plan64_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(pa);
   launches++;

@@ -711,6 +711,7 @@ __device__ __forceinline__ void ae_combos(const C d[6], C out[4]) {
 struct PlanArgs {
   int nitems, nseg, NFFT, cap, precision;
   int n_fixed;  // 0: bandwidth rule
+  int per_cta = 16;  // mixed plan: proposals per CTA (16..32 lanes of each role warp)
   double T, fstar, L;
   const int *item_seg;
   const double *params;
