@@ -50,7 +50,7 @@ struct GradPlanArgs {
   double *grad, *fisher;
 };
 
-__global__ void __launch_bounds__(64) fd_plangrad_kernel(GradPlanArgs ga) {
+__global__ void __launch_bounds__(256) fd_plangrad_kernel(GradPlanArgs ga) {
   const PlanArgs &a = ga.base;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int b = -1;
@@ -128,29 +128,42 @@ struct GradConsts {
 // One sample n of one proposal: the 6 templates' arm values combined into
 // their 4 A/E series each (the slow part of the waveform and its tangents).
 __device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad &g, const OrbitSampleMix &o,
-                                            float2 (&accs)[kGradSeries]) {
+                                            const GeoSampleMix &gm, float2 (&accs)[kGradSeries]) {
   const ItemMix &c = g.m;
-  // ---- geometry (as slow_sample_mix), plus absolute positions for d tau/dk
+  // ---- geometry (as slow_sample_mix: offsets and arm monomials from the
+  // per-size table), plus absolute positions for d tau/dk
   const float ca = o.ca_hi, sa = o.sa_hi;
-  const float sa2 = sa * sa, ca2 = ca * ca, saca = sa * ca;
-  const float sbf[3] = {0.0f, 0.866025403784439f, -0.866025403784438f};
-  const float cbf[3] = {1.0f, -0.5f, -0.5f};
+  float f[28];
+  {
+    const float4 *g4 = reinterpret_cast<const float4 *>(gm.f);
+#pragma unroll
+    for (int q = 0; q < 7; q++) {
+      const float4 v = g4[q];
+      f[4 * q] = v.x;
+      f[4 * q + 1] = v.y;
+      f[4 * q + 2] = v.z;
+      f[4 * q + 3] = v.w;
+    }
+  }
   float dx[3], dy[3], dz[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    dx[i] = K.Rf * (saca * sbf[i] - (1.f + sa2) * cbf[i]);
-    dy[i] = K.Rf * (saca * cbf[i] - (1.f + ca2) * sbf[i]);
-    dz[i] = -1.73205080757f * K.Rf * (ca * cbf[i] + sa * sbf[i]);
+    dx[i] = f[3 * i];
+    dy[i] = f[3 * i + 1];
+    dz[i] = f[3 * i + 2];
   }
   // carrier phase (double-float) common to the three spacecraft
   const float psi0 = carrier_phase_mix(c, o);
   const float uf = o.u_hi;
   const float tgc = K.AUcf * (c.k[0] * ca + c.k[1] * sa);
   const float gx = K.AUf * ca, gy = K.AUf * sa;  // guiding centre (m)
-  float fon[3], arg2[3], aev[3], vv[3], wxi[3], dtc[3], dtp[3];
+  float fon[3], arg2[3], aev[3], vv[3], wxi[3], dtc[3], dtp[3], kd[3], kcd[3], kpd[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     const float kdx = c.k[0] * dx[i] + c.k[1] * dy[i] + c.k[2] * dz[i];
+    kd[i] = kdx;
+    kcd[i] = g.dk_c[0] * dx[i] + g.dk_c[1] * dy[i] + g.dk_c[2] * dz[i];
+    kpd[i] = g.dk_p[0] * dx[i] + g.dk_p[1] * dy[i] + g.dk_p[2] * dz[i];
     const float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
     const float tT = taui * K.invTf;
     const float v = uf - tT;  // xi / T
@@ -170,16 +183,14 @@ __device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad 
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     const int i0 = q == 2 ? 1 : 0, i1 = q == 0 ? 1 : 2;
-    const float rx = (dx[i1] - dx[i0]) * K.invLf, ry = (dy[i1] - dy[i0]) * K.invLf, rz = (dz[i1] - dz[i0]) * K.invLf;
-    const float m0 = rx * rx, m3 = ry * ry, m5 = rz * rz;
-    const float m1 = 2.f * rx * ry, m2 = 2.f * rx * rz, m4 = 2.f * ry * rz;
+    const float *m = f + 9 + 6 * q;  // x^2, 2xy, 2xz, y^2, 2yz, z^2 of the unit arm
     const float *E[6] = {g.ep, g.ec, g.dep_c, g.dec_c, g.dep_p, g.dec_p};
 #pragma unroll
     for (int t = 0; t < 6; t++)
-      qf[q][t] = fmaf(E[t][0], m0, fmaf(E[t][3], m3, fmaf(E[t][5], m5, fmaf(E[t][1], m1, fmaf(E[t][2], m2, E[t][4] * m4)))));
-    krq[q] = c.k[0] * rx + c.k[1] * ry + c.k[2] * rz;
-    dkcq[q] = g.dk_c[0] * rx + g.dk_c[1] * ry + g.dk_c[2] * rz;
-    dkpq[q] = g.dk_p[0] * rx + g.dk_p[1] * ry + g.dk_p[2] * rz;
+      qf[q][t] = fmaf(E[t][0], m[0], fmaf(E[t][3], m[3], fmaf(E[t][5], m[5], fmaf(E[t][1], m[1], fmaf(E[t][2], m[2], E[t][4] * m[4])))));
+    krq[q] = (kd[i1] - kd[i0]) * K.invLf;
+    dkcq[q] = (kcd[i1] - kcd[i0]) * K.invLf;
+    dkpq[q] = (kpd[i1] - kpd[i0]) * K.invLf;
   }
 #pragma unroll
   for (int s = 0; s < kGradSeries; s++) accs[s] = make_float2(0.f, 0.f);
@@ -270,6 +281,7 @@ struct GradSpecArgs {
   const int *bin_list;
   const ItemGrad *items;
   const OrbitSampleMix *mix;  // this size's orbit table
+  const GeoSampleMix *geo;    // this size's sample geometry
   const float2 *tw;
   const float4 *w32, *w32lo, *g32;
   const float2 *invc;  // invC_A, invC_E per segment bin (reference-indexed Fisher)
@@ -324,7 +336,7 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     for (int r = 0; r < 4; r++) {
       const int n = lane + GT * r;
       float2 accs[kGradSeries];
-      grad_sample(a.K, it, a.mix[n], accs);
+      grad_sample(a.K, it, a.mix[n], a.geo[n], accs);
 #pragma unroll
       for (int s = 0; s < kGradSeries; s++) sbuf[(size_t)s * SN + pad16(n)] = accs[s];
     }
@@ -391,20 +403,22 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     }
     // reduce over the group: per-thread partials in shared memory (reusing the
     // series buffer once every thread is done with it)
+    // rows of GT + 1 floats: lane q summing row q reads bank (q + t) mod 32
+    constexpr int PS = GT + 1;
     group_sync<GT>();
 #pragma unroll
-    for (int q = 0; q < NACC; q++) part[q * GT + lane] = accg[q];
+    for (int q = 0; q < NACC; q++) part[q * PS + lane] = accg[q];
     const df rs = group_sum_df<GT>(racc, red, lane);
     group_sync<GT>();
     for (int q = lane; q < NACC; q += GT) {
       float sum = 0.f;
-      for (int t = 0; t < GT; t++) sum += part[q * GT + t];
-      part[q * GT] = sum;  // column head
+      for (int t = 0; t < GT; t++) sum += part[q * PS + t];
+      part[q * PS] = sum;  // row head
     }
     group_sync<GT>();
     if (valid) {
       for (int q = lane; q < NACC; q += GT) {
-        const double v = (double)part[q * GT];
+        const double v = (double)part[q * PS];
         if (q < 8) {
           a.grad[8 * (size_t)item + q] = v;
         } else if (a.fisher) {
@@ -490,7 +504,15 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
   ga.items = work.itemsgrad;
   ga.grad = grad;
   ga.fisher = fisher;
-  fd_plangrad_kernel<<<(nitems + 63) / 64, 64, 0, stream>>>(ga);
+  {
+    // one thread per proposal in CTAs of 64..256 threads, as few CTAs as
+    // SMs where the batch allows (the kernel is a latency-bound FP64 chain: a
+    // second CTA on some SMs doubles their time)
+    int per = (nitems + num_sms - 1) / (num_sms > 0 ? num_sms : 1);
+    per = (per + 31) / 32 * 32;
+    per = per < 64 ? 64 : (per > 256 ? 256 : per);
+    fd_plangrad_kernel<<<(nitems + per - 1) / per, per, 0, stream>>>(ga);
+  }
   launches++;
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
 
@@ -526,6 +548,7 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
     a.bin_list = work.bin_list + (size_t)b * work.cap;
     a.tw = tab.tw32[b];
     a.mix = tab.mix[b];
+    a.geo = tab.geo[b];
     switch (N) {
       case 32: e = launch_gradspec<32>(a, nitems, num_sms, sb); break;
       case 64: e = launch_gradspec<64>(a, nitems, num_sms, sb); break;
