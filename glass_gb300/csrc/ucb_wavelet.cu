@@ -75,6 +75,10 @@ __device__ __forceinline__ int bin_index(const double *x, int n, double v) {
   return j;
 }
 
+// The tile kernels below keep 4 arrays of n doubles per chain in shared memory,
+// chains 4 n + 1 doubles apart: the sequential phases have the chains' threads
+// at the same node index, which an unpadded stride would put on one bank.
+
 // Natural cubic spline solve (utils/src/glass_math.c:101-175) on a grid whose
 // factors fac = {h, l, mu} are precomputed, split for a CTA that handles many
 // value arrays at once: spline_rhs for node i (the forward sweep's right-hand
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(128) wv_plan_kernel(WvGridDev g, int n, const 
   for (int q = threadIdx.x; q < nsrc * norb; q += blockDim.x) {
     const int c = q / norb, i = q - c * norb;
     if (!s_ok[c]) continue;
-    double *ya = psm + (size_t)c * 4 * norb, *yp = ya + norb;
+    double *ya = psm + (size_t)c * (4 * norb + 1), *yp = ya + norb;
     const double f0 = s_f0[c], phi0 = s_phi0[c], fdot = s_fdot[c], fddot = 0.0;
     const double A0 = s_A0[c];
     const double t = g.orb_t[i];
@@ -208,20 +212,20 @@ __global__ void __launch_bounds__(128) wv_plan_kernel(WvGridDev g, int n, const 
   for (int q = threadIdx.x; q < nsrc * norb; q += blockDim.x) {
     const int c = q / norb, i = q - c * norb;
     if (!s_ok[c] || i == 0 || i == norb - 1) continue;
-    double *ya = psm + (size_t)c * 4 * norb, *yp = ya + norb, *za = ya + 2 * norb, *zp = ya + 3 * norb;
+    double *ya = psm + (size_t)c * (4 * norb + 1), *yp = ya + norb, *za = ya + 2 * norb, *zp = ya + 3 * norb;
     za[i] = spline_rhs(ya, i, h);
     zp[i] = spline_rhs(yp, i, h);
   }
   __syncthreads();
   if ((int)threadIdx.x < 2 * nsrc) {
     const int c = threadIdx.x >> 1;
-    if (s_ok[c]) spline_recurrence(psm + (size_t)c * 4 * norb + (2 + (threadIdx.x & 1)) * norb, norb, g.fac_orb);
+    if (s_ok[c]) spline_recurrence(psm + (size_t)c * (4 * norb + 1) + (2 + (threadIdx.x & 1)) * norb, norb, g.fac_orb);
   }
   __syncthreads();
   for (int q = threadIdx.x; q < nsrc * norb; q += blockDim.x) {
     const int c = q / norb, i = q - c * norb;
     if (!s_ok[c]) continue;
-    const double *ya = psm + (size_t)c * 4 * norb, *yp = ya + norb, *za = ya + 2 * norb, *zp = ya + 3 * norb;
+    const double *ya = psm + (size_t)c * (4 * norb + 1), *yp = ya + norb, *za = ya + 2 * norb, *zp = ya + 3 * norb;
     double *amp = ssb + (size_t)(base + c) * 8 * norb, *ph = amp + 4 * norb;
     spline_coeffs(ya, za, i, norb, h, amp);
     spline_coeffs(yp, zp, i, norb, h, ph);
@@ -397,7 +401,7 @@ __global__ void __launch_bounds__(128) wv_tdi_kernel(WvGridDev g, int n, const W
   // (flip and pj until the right-hand sides overwrite them)
 #define WV_TDI_PTRS                                                       \
   const int idx = base + c, s = idx / 3, ch = idx - 3 * (idx / 3);       \
-  double *As = tsm + (size_t)c * 4 * N, *Q = As + N, *za = As + 2 * N, *zp = As + 3 * N; \
+  double *As = tsm + (size_t)c * (4 * N + 1), *Q = As + N, *za = As + 2 * N, *zp = As + 3 * N; \
   const double *M = resp + ((size_t)s * 7 + ch) * N, *Mf = resp + ((size_t)s * 7 + 3 + ch) * N; \
   (void)M;                                                                \
   (void)Mf;                                                               \
@@ -481,7 +485,7 @@ __global__ void __launch_bounds__(128) wv_tdi_kernel(WvGridDev g, int n, const W
   __syncthreads();
   if ((int)threadIdx.x < 2 * nch && s_ok[threadIdx.x >> 1]) {
     const int c = threadIdx.x >> 1;
-    spline_recurrence(tsm + (size_t)c * 4 * N + (2 + (threadIdx.x & 1)) * N, N, g.fac_ssb);
+    spline_recurrence(tsm + (size_t)c * (4 * N + 1) + (2 + (threadIdx.x & 1)) * N, N, g.fac_ssb);
   }
   __syncthreads();
   for (int q = threadIdx.x; q < nch * N; q += blockDim.x) {
@@ -1284,7 +1288,7 @@ cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int preci
   {
     // 4 norb doubles of shared memory per source; 16 sources per CTA where
     // they fit, fewer for long observations
-    const size_t per = sizeof(double) * 4 * (size_t)norb;
+    const size_t per = sizeof(double) * (4 * (size_t)norb + 1);
     if ((e = wv_launch_tiles(wv_plan_kernel<16>, wv_plan_kernel<4>, wv_plan_kernel<1>, per, n, s, g, n, params, w.src,
                              w.ssb, status)) != cudaSuccess)
       return e;
@@ -1292,7 +1296,7 @@ cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int preci
   const long long nr = (long long)n * norb;
   wv_resp_kernel<<<(unsigned)((nr + 127) / 128), 128, 0, s>>>(g, n, w.src, w.ssb, w.resp);
   {
-    const size_t per = sizeof(double) * 4 * (size_t)norb;
+    const size_t per = sizeof(double) * (4 * (size_t)norb + 1);
     if ((e = wv_launch_tiles(wv_tdi_kernel<16>, wv_tdi_kernel<4>, wv_tdi_kernel<1>, per, 3 * n, s, g, n, w.src, w.resp,
                              w.tdi)) != cudaSuccess)
       return e;
