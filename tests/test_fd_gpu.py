@@ -302,3 +302,47 @@ def test_host_entry_point_replays_follow_inputs_and_bank(engine, port):
         np.testing.assert_array_equal(got[0], device(draws[0], txs[0], gg.PREC_MIXED)[0])
     finally:
         engine.set_template_size(0)
+
+
+def test_large_templates_on_8192_bin_segments(engine, port):
+    """Config-4 sizes: segments of 8192 bins, so that the bandwidth rule reaches
+    N = 2048 and 4096 for loud sources (the SNR spread sets N).  Those sizes run
+    in the per-size spectral kernels on forked streams beside the persistent
+    kernel; FP64 against the oracle to 1e-10.  Mixed precision against FP64:
+    templates this loud (SNR in the thousands) carry the FP32 template error
+    (relative ~1e-6) times (h|h), so the bound is relative, 1e-5 of
+    max(1, (h|h)) on the term; the 1e-3 absolute bar is the config-1 one."""
+    rng = np.random.default_rng(77)
+    NFFT, nseg = 8192, 3
+    qmin, dA, dE, iA, iE, inj = [], [], [], [], [], []
+
+    def wf(p):
+        al = port.alignment(T, NFFT, 0, p)
+        return int(al[0]), *port.waveform(p, int(al[0]), T)[3:5]
+
+    for s in range(nseg):
+        p = wl.draw_source(rng, 3e-3 + 1e-3 * s, 1e-20, 1e-17)
+        q, a, e, ia, ie = wl.make_segment(rng, [p], wf, NFFT=NFFT, T=T)
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie), inj.append(p)
+    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                          invCA=np.array(iA), invCE=np.array(iE))
+    engine.upload(bank)
+    # loud proposals near the injections, kept where the rule gives N <= 4096
+    # (the engine's largest template; louder ones get N = 8192 on these segments)
+    seg = np.repeat(np.arange(nseg, dtype=np.int32), 16)
+    params = np.vstack([wl.gaussian_jumps(rng, inj[s], wl.jump_scales(inj[s], 200.0), 16) for s in range(nseg)])
+    params[:, 3] = np.log(10 ** rng.uniform(-21.0, -20.0, len(seg)))
+    keep = np.array([port.alignment(T, NFFT, 0, p)[0] <= 4096 for p in params])
+    seg, params = seg[keep], params[keep]
+    ref = _oracle_terms(port, bank, seg, params)
+    Ns = set(ref[:, 2].astype(int))
+    assert {2048, 4096} <= Ns, Ns
+    dl, ty, hh, st = engine.dlogl_host(seg, params, precision=gg.PREC_FP64)
+    assert (st == 0).all()
+    err = np.abs(ty - ref[:, 0]) / np.maximum(1.0, np.abs(ref[:, 0]))
+    assert err.max() < REL, err.max()
+    np.testing.assert_allclose(hh, ref[:, 1], rtol=1e-9)
+    d32, t32, h32, s32 = engine.dlogl_host(seg, params, precision=gg.PREC_MIXED)
+    assert (s32 == 0).all()
+    assert (np.abs(t32 - ty) <= 1e-5 * np.maximum(1.0, hh)).all(), (np.abs(t32 - ty) / np.maximum(1.0, hh)).max()
+    np.testing.assert_allclose(h32, hh, rtol=1e-4)
