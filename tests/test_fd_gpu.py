@@ -346,3 +346,34 @@ def test_large_templates_on_8192_bin_segments(engine, port):
     assert (s32 == 0).all()
     assert (np.abs(t32 - ty) <= 1e-5 * np.maximum(1.0, hh)).all(), (np.abs(t32 - ty) / np.maximum(1.0, hh)).max()
     np.testing.assert_allclose(h32, hh, rtol=1e-4)
+
+
+def test_drop_in_waveform_from_concurrent_threads():
+    """The reference calls ucb_waveform from OpenMP threads, one chain per
+    thread (apps/src/ucb_mcmc.c:230): concurrent calls must each give the
+    result of a sequential call.  Eight host threads, different sources and
+    sizes, compared bit for bit."""
+    import threading
+
+    rng = np.random.default_rng(12)
+    jobs = [(wl.draw_source(rng, 10 ** rng.uniform(-3.3, -2.0), 1e-22), int(32 << (k % 6))) for k in range(48)]
+    want = [gg.ucb_waveform(p, N, T) for p, N in jobs]
+    got = [None] * len(jobs)
+    errors = []
+
+    def worker(w):
+        try:
+            for rep in range(3):
+                for k in range(w, len(jobs), 8):
+                    got[k] = gg.ucb_waveform(jobs[k][0], jobs[k][1], T)
+        except Exception as e:  # reported below; a thread's exception is not a test failure by itself
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(w,)) for w in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for k in range(len(jobs)):
+        np.testing.assert_array_equal(got[k], want[k])
