@@ -43,6 +43,7 @@ EXPORTS = (
     "glass_gpu_wdm_to_freq", "glass_gpu_wdm_from_freq", "build_wdm_filter_freq", "wavelet_transform_timefreq",
     "wavelet_transform_freq", "wavelet_transform_inverse_freq", "ucb_waveform_wavelet", "ucb_waveform_wavelet_tab",
     "ucb_waveform_wavelet_slow", "glass_ucb_waveform_wavelet_tab", "glass_ucb_waveform_wavelet_slow",
+    "glass_gpu_wavelet_fisher_batch", "glass_gpu_wavelet_fisher_batch_host",
 )
 
 _lib = None
@@ -100,6 +101,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_wavelet_dlogl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D, _D, _I]
     lib.glass_gpu_wavelet_waveform_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 4
     lib.glass_gpu_wavelet_waveform_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _I, _D, _I]
+    lib.glass_gpu_wavelet_fisher_batch.argtypes = [_V, ctypes.c_int, _V, ctypes.c_int, ctypes.c_int, _V, _V]
+    lib.glass_gpu_wavelet_fisher_batch_host.argtypes = [_V, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int, _D, _I]
     _lib = lib
     return lib
 
@@ -341,6 +344,17 @@ class Engine:
                                                            _pd(tx) if tx is not None else None,
                                                            _pd(dl), _pd(ty), _pd(hh), _pi(st)))
         return dl, ty, hh, st
+
+    def wavelet_fisher_host(self, params, imin, imax):
+        """(fisher [n, 8, 8], status [n]): ucb_fisher_wavelet for each source,
+        over time pixels imin < t < imax."""
+        p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        n = len(p)
+        F = np.zeros((n, 8, 8))
+        st = np.zeros(n, np.int32)
+        _check(self.lib.glass_gpu_wavelet_fisher_batch_host(self._ctx, n, _pd(p), int(imin), int(imax), _pd(F),
+                                                            _pi(st)))
+        return F, st
 
     def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                              precision=PREC_FP64):

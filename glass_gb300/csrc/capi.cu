@@ -77,6 +77,7 @@ struct glass_gpu_ctx {
   bool wv_data_ready = false;
   WvWorkDev wvw;
   void *wv_work_mem = nullptr;
+  void *wv_fisher_mem = nullptr;  // perturbed parameters of the Fisher batches
 };
 
 static void clear_host_graphs(glass_gpu_ctx *ctx) {
@@ -142,6 +143,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->wv_grid_mem);
   cudaFree(ctx->wv_data_mem);
   cudaFree(ctx->wv_work_mem);
+  cudaFree(ctx->wv_fisher_mem);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
@@ -1040,6 +1042,48 @@ extern "C" int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int precision, 
                                status ? status + off : nullptr, ctx->stream, &ctx->last_launches),
                "wavelet dlogl launch");
   }
+  return GLASS_OK;
+}
+
+static constexpr int kWvFisherChunk = kWvChunk / 16;  // sources per Fisher launch sequence (16 waveforms each)
+
+extern "C" int glass_gpu_wavelet_fisher_batch(glass_gpu_ctx *ctx, int nitems, const double *params, int imin,
+                                              int imax, double *fisher, int *status) {
+  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_fisher_batch", true);
+  if (rc) return rc;
+  if (nitems > 0 && !fisher) return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_fisher_batch: null fisher");
+  if (!ctx->wv_fisher_mem)
+    GLASS_CUDA(cudaMalloc(&ctx->wv_fisher_mem, sizeof(double) * 8 * 16 * (size_t)kWvFisherChunk),
+               "cudaMalloc(fisher parameters)");
+  ctx->last_launches = 0;
+  for (int off = 0; off < nitems; off += kWvFisherChunk) {
+    const int n = std::min(kWvFisherChunk, nitems - off);
+    GLASS_CUDA(wv_fisher_launch(ctx->wv, ctx->wvw, n, params + 8 * (size_t)off, (double *)ctx->wv_fisher_mem, imin,
+                                imax, fisher + 64 * (size_t)off, status ? status + off : nullptr, ctx->stream,
+                                &ctx->last_launches),
+               "wavelet fisher launch");
+  }
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wavelet_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, int imin,
+                                                   int imax, double *fisher, int *status) {
+  int rc = wv_check(ctx, nitems, params, "glass_gpu_wavelet_fisher_batch_host", true);
+  if (rc) return rc;
+  if (nitems == 0) return GLASS_OK;
+  if (!fisher) return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_fisher_batch_host: null fisher");
+  const size_t nd = (size_t)nitems;
+  const size_t bytes = sizeof(double) * 72 * nd + sizeof(int) * nd + 256;
+  if ((rc = ensure_stage(ctx, bytes))) return rc;
+  double *dp = (double *)ctx->d_stage, *df = dp + 8 * nd;
+  int *dst = (int *)(df + 64 * nd);
+  GLASS_CUDA(cudaMemcpyAsync(dp, params, sizeof(double) * 8 * nd, cudaMemcpyHostToDevice, ctx->stream), "H2D params");
+  if ((rc = glass_gpu_wavelet_fisher_batch(ctx, nitems, dp, imin, imax, df, dst))) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(fisher, df, sizeof(double) * 64 * nd, cudaMemcpyDeviceToHost, ctx->stream),
+             "D2H fisher");
+  if (status)
+    GLASS_CUDA(cudaMemcpyAsync(status, dst, sizeof(int) * nd, cudaMemcpyDeviceToHost, ctx->stream), "D2H status");
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "wavelet fisher sync");
   return GLASS_OK;
 }
 

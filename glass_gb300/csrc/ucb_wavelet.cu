@@ -1259,6 +1259,124 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
 
 static size_t layers_smem(int NT) { return sizeof(double2) * (size_t)NT * (kWvMaxLayers + 1) / 2 + sizeof(double2) * NT; }
 
+// ------------------------------------------------------------ Fisher matrix
+// ucb_fisher_wavelet (ucb/src/glass_ucb_waveform.c:524-640) for a batch of
+// sources: central differences with step 1e-6 (each parameter +-5e-7, the
+// cosine parameters clamped to [-1, 1]) of 16 FP64 wavelet waveforms per
+// source, on the pixels of each + waveform's list whose time index t has
+// imin < t < imax, and the Fisher matrix as the nine XYZ cross terms of invC
+// per pixel (wavelet_nwip, utils/src/glass_math.c:382-391).
+constexpr double kFisherEps = 1.0e-6;
+
+// Row 16 s + 2 i (+) and 16 s + 2 i + 1 (-) of the perturbed parameters.
+__global__ void wv_fisher_params_kernel(int n, const double *params, double *pp) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 16 * n) return;
+  const int s = idx >> 4, r = idx & 15, i = r >> 1;
+  double *o = pp + 8 * (size_t)idx;
+  for (int k = 0; k < 8; k++) o[k] = params[8 * (size_t)s + k];
+  if ((r & 1) == 0) {
+    o[i] += kFisherEps / 2.;
+    if ((i == 1 || i == 4) && o[i] > 1.0) o[i] = 1.0;
+  } else {
+    o[i] -= kFisherEps / 2.;
+    if ((i == 1 || i == 4) && o[i] < -1.0) o[i] = -1.0;
+  }
+}
+
+constexpr int kFisherThreads = 256;
+
+__global__ void __launch_bounds__(kFisherThreads) wv_fisher_kernel(WvGridDev g, int n, const WvSrc *srcs,
+                                                                   const double *coef, int imin, int imax,
+                                                                   double *fisher, int *status) {
+  const int s = blockIdx.x;
+  const WvSrc *S = srcs + 16 * (size_t)s;
+  __shared__ double red[kFisherThreads / 32][36];
+  int st = 0;
+  for (int r = 0; r < 16; r++) st |= S[r].status;
+  if (st) {
+    if (threadIdx.x < 64 && fisher) fisher[64 * (size_t)s + threadIdx.x] = NAN;
+    if (threadIdx.x == 0 && status) status[s] = st;
+    return;
+  }
+  const int NT = g.NT, N = g.N;
+  const size_t LNT = (size_t)kWvMaxLayers * NT;
+  // union of the + waveforms' kept layers
+  int jl = 1 << 30, jh = -(1 << 30);
+  for (int i = 0; i < 8; i++)
+    if (S[2 * i].c > 0) {
+      jl = min(jl, S[2 * i].jlo);
+      jh = max(jh, S[2 * i].jlo + S[2 * i].c);
+    }
+  const int nj = jh > jl ? jh - jl : 0;
+  const double inv = 1. / (kFisherEps);
+  double acc[36];
+#pragma unroll
+  for (int q = 0; q < 36; q++) acc[q] = 0.0;
+  for (int q = threadIdx.x; q < NT * nj; q += blockDim.x) {
+    const int t = q / nj, j = jl + (q - t * nj);
+    const int k = t + j * NT - g.kmin;
+    if (!(t > imin && t < imax) || k < 0 || k >= N) continue;
+    double dh[8][3];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const WvSrc &P = S[2 * i], &M = S[2 * i + 1];
+      dh[i][0] = dh[i][1] = dh[i][2] = 0.0;
+      if (P.c > 0 && j >= P.jlo && j < P.jlo + P.c) {
+        const double *cp = coef + (16 * (size_t)s + 2 * i) * 3 * LNT + t * P.c + (j - P.jlo);
+        double m0 = 0.0, m1 = 0.0, m2 = 0.0;
+        if (M.c > 0 && j >= M.jlo && j < M.jlo + M.c) {
+          const double *cm = coef + (16 * (size_t)s + 2 * i + 1) * 3 * LNT + t * M.c + (j - M.jlo);
+          m0 = cm[0];
+          m1 = cm[LNT];
+          m2 = cm[2 * LNT];
+        }
+        dh[i][0] = (cp[0] - m0) * inv;
+        dh[i][1] = (cp[LNT] - m1) * inv;
+        dh[i][2] = (cp[2 * LNT] - m2) * inv;
+      }
+    }
+    double c[9];
+#pragma unroll
+    for (int ab = 0; ab < 9; ab++) c[ab] = g.invC[(size_t)ab * N + k];
+    int idx = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+      for (int jj = i; jj < 8; jj++, idx++) {
+        double v = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) v += dh[i][a] * dh[jj][b] * c[3 * a + b];
+        acc[idx] += v;
+      }
+  }
+  // CTA reduction of the 36 sums
+#pragma unroll
+  for (int q = 0; q < 36; q++)
+    for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+  if ((threadIdx.x & 31) == 0)
+    for (int q = 0; q < 36; q++) red[threadIdx.x >> 5][q] = acc[q];
+  __syncthreads();
+  if (threadIdx.x < 36) {
+    double v = 0.0;
+    for (int w = 0; w < kFisherThreads / 32; w++) v += red[w][threadIdx.x];
+    if (v != v) v = 10.0;  // the reference's sentinel for a NaN element
+    int i = 0, r = threadIdx.x;
+    while (r >= 8 - i) {
+      r -= 8 - i;
+      i++;
+    }
+    const int jj = i + r;
+    if (fisher) {
+      fisher[64 * (size_t)s + 8 * i + jj] = v;
+      fisher[64 * (size_t)s + 8 * jj + i] = v;
+    }
+  }
+  if (threadIdx.x == 0 && status) status[s] = 0;
+}
+
 // Launches a tile kernel with C = 16, 4 or 1 items per CTA of 128 threads,
 // the largest whose shared memory (C x per bytes) fits 200 KB.
 template <typename K16, typename K4, typename K1, typename... Args>
@@ -1316,6 +1434,18 @@ cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int preci
     wv_layers_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, w.coef);
   }
   if (nlaunch) *nlaunch += 4;
+  return cudaGetLastError();
+}
+
+cudaError_t wv_fisher_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *params, double *pp,
+                             int imin, int imax, double *fisher, int *status, cudaStream_t s, int *nlaunch) {
+  if (n <= 0) return cudaSuccess;
+  if (16 * n > w.cap) return cudaErrorInvalidValue;
+  wv_fisher_params_kernel<<<(16 * n + 127) / 128, 128, 0, s>>>(n, params, pp);
+  cudaError_t e = wv_waveform_launch(g, w, 0, 16 * n, pp, nullptr, s, nlaunch);
+  if (e != cudaSuccess) return e;
+  wv_fisher_kernel<<<n, kFisherThreads, 0, s>>>(g, n, w.src, w.coef, imin, imax, fisher, status);
+  if (nlaunch) *nlaunch += 2;
   return cudaGetLastError();
 }
 

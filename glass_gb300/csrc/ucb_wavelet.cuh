@@ -82,6 +82,10 @@ cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int preci
 // the same precision).
 cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *term_x,
                             double *dlogl, double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch);
+// Fisher matrices of n sources (ucb_fisher_wavelet) in FP64: pp is scratch for
+// 16 n perturbed parameter vectors; needs 16 n <= w.cap; fisher[64 s + 8 i + j].
+cudaError_t wv_fisher_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *params, double *pp,
+                             int imin, int imax, double *fisher, int *status, cudaStream_t s, int *nlaunch);
 // Per-item layer info and values in list order: info[4 i] = first layer,
 // layer count, first kept layer, kept layers per time; xyz[(3 i + c) (kWvMaxLayers NT) + q].
 cudaError_t wv_export(const WvGridDev &g, const WvWorkDev &w, int precision, int n, int *info, double *xyz,

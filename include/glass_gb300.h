@@ -346,6 +346,27 @@ int glass_gpu_wavelet_waveform_batch(glass_gpu_ctx *ctx, int precision, int nite
 int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
                                           int *info, double *xyz, int *status);
 
+/*
+ * Wavelet-domain Fisher matrices, batched: ucb_fisher_wavelet
+ * (ucb/src/glass_ucb_waveform.c:524-640) for nitems sources params[8 i ..]
+ * against the noise of glass_gpu_wavelet_set_data.  Central differences with
+ * the reference's step (each parameter +-5e-7, the cosine parameters clamped
+ * to [-1, 1], divided by 1e-6) of FP64 wavelet waveforms, on the pixels of
+ * each + waveform's list whose time index t has imin < t < imax (the
+ * reference's wdm->imin, wdm->imax), and the nine XYZ cross terms of invC per
+ * pixel (wavelet_nwip).  fisher[64 i + 8 k + l] = (dh/dp_k | dh/dp_l); a NaN
+ * element becomes 10, as in the reference; status[i] (may be NULL) is 0, or
+ * the status of an invalid perturbed parameter set (fisher then NaN).  The
+ * eigen-decomposition the reference does next (matrix_eigenstuff) stays with
+ * the caller.  Device pointers; asynchronous on the context's stream.  The
+ * reference's own ucb_fisher_wavelet also runs unchanged on the drop-in
+ * ucb_waveform_wavelet below, one source at a time.
+ */
+int glass_gpu_wavelet_fisher_batch(glass_gpu_ctx *ctx, int nitems, const double *params, int imin, int imax,
+                                   double *fisher, int *status);
+int glass_gpu_wavelet_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const double *params, int imin, int imax,
+                                        double *fisher, int *status);
+
 /* ------------------------------------ drop-ins for the wavelet headers */
 /*
  * Same names and signatures as the reference, so that ucb_wavelet_mcmc and

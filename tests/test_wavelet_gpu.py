@@ -202,3 +202,53 @@ def test_mixed_dlogl_error_budget(engine, golden):
         assert (err[near] < MIXED_ABS).all(), err[near].max()
         assert (err[~near] < MIXED_REL_FAR * ref[~near]).all()
         np.testing.assert_allclose(hh32[ok], hh64[ok], rtol=MIXED_REL_FAR)
+
+
+def _fisher_oracle(port, p, grid, t0, kmin, kmax, invC, imin, imax):
+    """ucb_fisher_wavelet (ucb/src/glass_ucb_waveform.c:524-640) restated on
+    the oracle's wavelet waveforms: central differences of step 1e-6 on the +
+    waveform's pixels with imin < t < imax, nine XYZ cross terms of invC."""
+    NF, NT, wdt, Tobs = grid
+    wdf = 1 / (2 * wdt)
+    N = kmax - kmin
+    eps = 1e-6
+    dh = np.zeros((8, 3, N))
+    for i in range(8):
+        pp, pm = p.copy(), p.copy()
+        pp[i] += eps / 2
+        pm[i] -= eps / 2
+        if i in (1, 4):
+            pp[i] = min(pp[i], 1.0)
+            pm[i] = max(pm[i], -1.0)
+        lp, xp, _, _ = port.wavelet_waveform(pp, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax)
+        _, xm, _, _ = port.wavelet_waveform(pm, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax)
+        for k in lp:
+            t = (k + kmin) % NT
+            if imin < t < imax and 0 <= k < N:
+                dh[i][:, k] = (xp[:, k] - xm[:, k]) * (1.0 / eps)
+    return np.einsum("iak,abk,jbk->ij", dh, invC, dh)
+
+
+def test_fisher_batch_matches_restated_reference(engine, port):
+    NF, NT, wdt, Tobs = SMALL
+    wdf = 1 / (2 * wdt)
+    kmin, kmax = 10 * NT, 40 * NT
+    N = kmax - kmin
+    imin, imax = 4, NT - 4
+    engine.wavelet_setup(Tobs, 0.0, NF, NT, wdt, wdf, kmin, kmax)
+    rng = np.random.default_rng(33)
+    invC = wl.wavelet_invC(N, NT, kmin, 1e-22)
+    engine.wavelet_set_data(np.zeros((3, N)), invC)
+    params = np.array([wl.draw_source(rng, f, 10 ** rng.uniform(-22, -21), 1e-14, Tobs)
+                       for f in rng.uniform(12 * wdf, 38 * wdf, 5)])
+    params[2, 1] = 1.0 - 2e-7  # the + step of cos(theta) is clamped at 1
+    params[3, 4] = -1.0 + 1e-7  # the - step of cos(iota) is clamped at -1
+    bad = params[0].copy()
+    bad[4] = 1.5
+    F, st = engine.wavelet_fisher_host(np.vstack([params, bad[None]]), imin, imax)
+    assert (st[:-1] == 0).all() and st[-1] != 0 and np.isnan(F[-1]).all()
+    for s in range(len(params)):
+        ref = _fisher_oracle(port, params[s], SMALL, 0.0, kmin, kmax, invC, imin, imax)
+        scale = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+        np.testing.assert_array_equal(F[s], F[s].T)
+        assert (np.abs(F[s] - ref) <= 1e-6 * scale + 1e-300).all(), (s, (np.abs(F[s] - ref) / scale).max())
