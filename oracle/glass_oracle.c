@@ -519,3 +519,237 @@ void orc_ucb_fisher(int format, double T, double t0, int NFFT, int qmin, const d
         }
     free(h0); free(dA); free(dE); free(hp);
 }
+
+/* ------------------------------------------------------------ F-statistic */
+
+/* Inverse of a 4x4 matrix in place by Gauss-Jordan elimination with partial
+ * pivoting (the textbook algorithm; the reference calls LAPACKE dgetrf/dgetri,
+ * utils/src/glass_math.c:501-523, which gives the same inverse to rounding for
+ * the well-conditioned filter matrices of the F-statistic).  Returns -1 for a
+ * singular matrix. */
+int orc_invert4(double *m)
+{
+    double a[4][8];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            a[i][j] = m[4 * i + j];
+            a[i][4 + j] = (i == j) ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 4; c++) {
+        int p = c;
+        for (int r = c + 1; r < 4; r++)
+            if (fabs(a[r][c]) > fabs(a[p][c])) p = r;
+        if (a[p][c] == 0.0) return -1;
+        if (p != c)
+            for (int j = 0; j < 8; j++) { double t = a[c][j]; a[c][j] = a[p][j]; a[p][j] = t; }
+        double inv = 1.0 / a[c][c];
+        for (int j = 0; j < 8; j++) a[c][j] *= inv;
+        for (int r = 0; r < 4; r++) {
+            if (r == c) continue;
+            double f = a[r][c];
+            if (f == 0.0) continue;
+            for (int j = 0; j < 8; j++) a[r][j] -= f * a[c][j];
+        }
+    }
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) m[4 * i + j] = a[i][4 + j];
+    return 0;
+}
+
+static int orc_sgn(double v) { return (v > 0) - (v < 0); }
+
+/*
+ * Maximum-likelihood amplitude, inclination, polarisation and phase from the
+ * filter coefficients a (ucb/src/glass_ucb_fstatistic.c:552-570, the A/E
+ * half of get_F_params).  out: A, iota, psi, phase.
+ */
+void orc_fstat_params(const double *a, double *out)
+{
+    double a1p4 = a[0] + a[3], a2m3 = a[1] - a[2], a1m4 = a[0] - a[3], a2p3 = a[1] + a[2];
+    double Ap = sqrt(a1p4 * a1p4 + a2m3 * a2m3) + sqrt(a1m4 * a1m4 + a2p3 * a2p3);
+    double Ac = sqrt(a1p4 * a1p4 + a2m3 * a2m3) - sqrt(a1m4 * a1m4 + a2p3 * a2p3);
+    double psi = atan2(Ap * a[3] - Ac * a[0], -(Ac * a[1] + Ap * a[2]));
+    psi *= 0.5;
+    double c = (double)orc_sgn(sin(2.0 * psi));
+    out[0] = 0.5 * (Ap + sqrt(Ap * Ap - Ac * Ac));
+    out[1] = acos(-Ac / (Ap + sqrt(Ap * Ap - Ac * Ac)));
+    out[2] = psi;
+    out[3] = atan2(c * (Ap * a[3] - Ac * a[0]), -c * (Ac * a[2] + Ap * a[1]));
+}
+
+/*
+ * ucb/src/glass_ucb_fstatistic.c:646-703 (get_Fstat_logL), A/E channels, on
+ * one segment of NFFT bins starting at bin qmin:
+ *  - four filters (:231-348): ucb_waveform with amplitude 2, inclination pi/2
+ *    and (psi, phase) = (0, 0), (pi/4, pi), (0, 3pi/2), (pi/4, pi/2), all of
+ *    BW = ucb_bandwidth(f0, fdot, cos theta, A = 1e-22) samples;
+ *  - N^i = 4 sum (d.A^i + d.E^i)/C_A and M^ij = 4 sum (A^i.A^j)/C_A +
+ *    4 sum (E^i.E^j)/C_A over the filter bins i whose segment bin
+ *    k = q - qmin + i - BW/2 satisfies 0 < k < NFFT (:350-516; the A-channel
+ *    noise weights both channels, and bin 0 is left out, as there);
+ *  - logL = N^T M^-1 N / 2 (:599-622), a = M^-1 N (:624-644) and the
+ *    maximum-likelihood parameters (:525-597).
+ * dA, dE: 2 NFFT doubles (re/im); C_A = 1/invCA.
+ * out: logL_AE, A, iota, psi, phase.  Returns BW, or -1.
+ */
+int orc_fstat_logl(int format, double T, double t0, int NFFT, int qmin, const double *dA, const double *dE,
+                   const double *invCA, double f0, double fdot, double theta, double phi, double *out)
+{
+    static const double psi_f[4] = {0.0, M_PI_4, 0.0, M_PI_4};
+    static const double phase_f[4] = {0.0, M_PI, 3.0 * M_PI_2, M_PI_2};
+    long q = (long)(f0 * T);
+    int BW = orc_ucb_bandwidth(f0, fdot, cos(theta), 1.e-22, T, NFFT);
+    size_t len = 2 * (size_t)BW;
+    double *buf = calloc(4 * 5 * len, sizeof(double));
+    double *Af[4], *Ef[4];
+    for (int f = 0; f < 4; f++) {
+        double p[8];
+        p[0] = f0 * T;
+        p[1] = cos(theta);
+        p[2] = phi;
+        p[3] = log(2.0);
+        p[4] = cos(M_PI_2);
+        p[5] = psi_f[f];
+        p[6] = phase_f[f];
+        p[7] = fdot * (T * T);
+        double *h = buf + (size_t)f * 5 * len;
+        if (orc_ucb_waveform(format, T, t0, p, 8, h, h + len, h + 2 * len, h + 3 * len, h + 4 * len, BW, 2)) {
+            free(buf);
+            return -1;
+        }
+        Af[f] = h + 3 * len;
+        Ef[f] = h + 4 * len;
+    }
+    long qq = q - (long)qmin;
+    double Nv[4] = {0, 0, 0, 0}, M[16] = {0};
+    for (int i = 0; i < BW; i++) {
+        long k = qq + i - BW / 2;
+        if (!(k > 0 && k < NFFT)) continue;
+        double C = 1.0 / invCA[k];
+        int re = 2 * i, im = re + 1;
+        for (int f = 0; f < 4; f++)
+            Nv[f] += (dA[2 * k] * Af[f][re] + dA[2 * k + 1] * Af[f][im] + dE[2 * k] * Ef[f][re] +
+                      dE[2 * k + 1] * Ef[f][im]) / C;
+        for (int f = 0; f < 4; f++)
+            for (int g = f; g < 4; g++)
+                M[4 * f + g] += 4.0 * (Af[f][re] * Af[g][re] + Af[f][im] * Af[g][im]) / C +
+                                4.0 * (Ef[f][re] * Ef[g][re] + Ef[f][im] * Ef[g][im]) / C;
+    }
+    for (int f = 0; f < 4; f++) Nv[f] *= 4.0;
+    for (int f = 0; f < 4; f++)
+        for (int g = f + 1; g < 4; g++) M[4 * g + f] = M[4 * f + g];
+    free(buf);
+    /* No filter bin inside the segment leaves M = 0; LAPACK's dgetrf/dgetri
+     * then leave it as it is (its LU factors are zero and dgetri stops at the
+     * zero pivot), so logL = 0 and a = 0. */
+    int any = 0;
+    for (int c = 0; c < 16; c++) any |= (M[c] != 0.0);
+    if (any && orc_invert4(M)) return -1;
+    const double *m = M;
+    out[0] = 0.5 * (m[0] * Nv[0] * Nv[0] + 2 * m[1] * Nv[0] * Nv[1] + 2 * m[2] * Nv[0] * Nv[2] +
+                    2 * m[3] * Nv[0] * Nv[3] + m[5] * Nv[1] * Nv[1] + 2 * m[6] * Nv[1] * Nv[2] +
+                    2 * m[7] * Nv[1] * Nv[3] + m[10] * Nv[2] * Nv[2] + 2 * m[11] * Nv[2] * Nv[3] +
+                    m[15] * Nv[3] * Nv[3]);
+    double a[4];
+    for (int i = 0; i < 4; i++)
+        a[i] = m[4 * i] * Nv[0] + m[4 * i + 1] * Nv[1] + m[4 * i + 2] * Nv[2] + m[4 * i + 3] * Nv[3];
+    orc_fstat_params(a, out + 1);
+    return BW;
+}
+
+/* Batched form: cells[4 c] = f0, fdot, theta, phi on segment cell_seg[c];
+ * out[5 c ..] as orc_fstat_logl (OpenMP over cells). */
+void orc_fstat_batch(int format, double T, double t0, int NFFT, const int *seg_qmin, const double *dA,
+                     const double *dE, const double *invCA, int ncells, const int *cell_seg, const double *cells,
+                     double *out, int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 8)
+#endif
+    for (int c = 0; c < ncells; c++) {
+        int s = cell_seg[c];
+        const double *x = cells + 4 * (size_t)c;
+        if (orc_fstat_logl(format, T, t0, NFFT, seg_qmin[s], dA + (size_t)s * 2 * NFFT, dE + (size_t)s * 2 * NFFT,
+                           invCA + (size_t)s * NFFT, x[0], x[1], x[2], x[3], out + 5 * (size_t)c) < 0)
+            for (int k = 0; k < 5; k++) out[5 * (size_t)c + k] = NAN;
+    }
+}
+
+/* ucb/src/glass_ucb_waveform.c:307-314 (ucb_fdot) */
+double orc_ucb_fdot(double Mc, double f0)
+{
+    double M = Mc * 4.92569043916e-6; /* TSUN, utils/src/glass_constants.h:60 */
+    return 19.2 * pow(pow(M_PI, 8) * pow(M, 5) * pow(f0, 11), 1. / 3.);
+}
+
+/* Lowest frequency of a segment starting at bin qmin, as the reference holds
+ * it (utils/src/glass_data.c:2065: fmin = floor(fmin T)/T, and qmin =
+ * (int)(fmin T) at :1078): qmin/T, raised by an ulp where needed so that
+ * (int)(fmin T) gives qmin back. */
+double orc_segment_fmin(int qmin, double T)
+{
+    double fmin = (double)qmin / T;
+    while ((int)(fmin * T) < qmin) fmin = nextafter(fmin, INFINITY);
+    return fmin;
+}
+
+/*
+ * ucb/src/glass_ucb_proposal.c:1085-1182 (build_fstatistic_proposal) on one
+ * segment, with the grid of setup_fstatistic_proposal (:927-943): n_f cells
+ * of one bin in frequency, n_theta in cos(theta) and n_phi in phi, each
+ * evaluated at its centre with fdot = 0 and, where that gives logL > 1, along
+ * a scan of ten chirp masses up to the first logL < 1; the density is the
+ * square of the largest logL, normalised so that its mean is 1.
+ * tensor: n_f n_theta n_phi doubles, [i][j][k]; info = {n_f, norm, maxp}.
+ */
+void orc_fstat_proposal(int format, double T, double t0, int NFFT, int qmin, const double *dA, const double *dE,
+                        const double *invCA, int n_theta, int n_phi, double *tensor, double *info, int nthreads)
+{
+    double fmin = orc_segment_fmin(qmin, T);
+    double fmax = fmin + NFFT / T;
+    int n_f = (int)((fmax - fmin) * T);
+    double d_f = (int)((fmax - fmin) * T) / (double)n_f / T;
+    double d_theta = 2. / (double)n_theta;
+    double d_phi = ORC_PI2 / (double)n_phi;
+    int n_fdot = 10;
+    double d_fdot = (1.1 - 0.1) / n_fdot;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for collapse(2) schedule(dynamic, 4)
+#endif
+    for (int i = 0; i < n_f; i++)
+        for (int j = 0; j < n_theta; j++) {
+            double f = fmin + i * d_f;
+            f += d_f / 2;
+            for (int k = 0; k < n_phi; k++) {
+                double theta = acos((-1. + (double)j * d_theta + d_theta / 2));
+                double phi = (double)k * d_phi + d_phi / 2;
+                double o[5];
+                orc_fstat_logl(format, T, t0, NFFT, qmin, dA, dE, invCA, f, 0, theta, phi, o);
+                double logL_AE = o[0], logLmax = logL_AE;
+                if (logL_AE > 1) {
+                    for (int n = 0; n < n_fdot; n++) {
+                        double fdot = orc_ucb_fdot(0.1 + n * d_fdot, f);
+                        orc_fstat_logl(format, T, t0, NFFT, qmin, dA, dE, invCA, f, fdot, theta, phi, o);
+                        logL_AE = o[0];
+                        if (logL_AE > logLmax) logLmax = logL_AE;
+                        if (logL_AE < 1) break;
+                    }
+                }
+                tensor[((size_t)i * n_theta + j) * n_phi + k] = logLmax * logLmax;
+            }
+        }
+    double norm = 0.0;
+    size_t n = (size_t)n_f * n_theta * n_phi;
+    for (size_t c = 0; c < n; c++) norm += tensor[c];
+    norm = (n_f * n_theta * n_phi) / norm;
+    double maxp = -1.e60;
+    for (size_t c = 0; c < n; c++) {
+        tensor[c] *= norm;
+        if (tensor[c] > maxp) maxp = tensor[c];
+    }
+    info[0] = n_f;
+    info[1] = norm;
+    info[2] = maxp;
+}

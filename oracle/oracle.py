@@ -72,6 +72,7 @@ class Port:
         lib.orc_forward_complex_fft.argtypes = [_D, ctypes.c_int]
         self._wdm_bind()
         self._wavelet_bind()
+        self._fstat_bind()
 
     # --- Fourier-domain UCB path -------------------------------------------------
     def fstar(self) -> float:
@@ -124,6 +125,65 @@ class Port:
         self.lib.orc_ucb_fisher(FORMATS[fmt], T, t0, NFFT, qmin, _p(invCA), _p(invCE),
                                 _p(np.ascontiguousarray(params, np.float64)), _p(F))
         return F.reshape(8, 8)
+
+    # --- F-statistic (ucb/src/glass_ucb_fstatistic.c, ucb/src/glass_ucb_proposal.c) ---
+    def _fstat_bind(self):
+        lib = self.lib
+        lib.orc_fstat_logl.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                       _D, _D, _D] + [ctypes.c_double] * 4 + [_D]
+        lib.orc_fstat_batch.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _I, _D, _D, _D,
+                                        ctypes.c_int, _I, _D, _D, ctypes.c_int]
+        lib.orc_fstat_proposal.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int, _D, _D, _D, ctypes.c_int, ctypes.c_int, _D, _D, ctypes.c_int]
+        lib.orc_ucb_fdot.restype = ctypes.c_double
+        lib.orc_ucb_fdot.argtypes = [ctypes.c_double, ctypes.c_double]
+        lib.orc_segment_fmin.restype = ctypes.c_double
+        lib.orc_segment_fmin.argtypes = [ctypes.c_int, ctypes.c_double]
+        lib.orc_invert4.argtypes = [_D]
+        lib.orc_fstat_params.argtypes = [_D, _D]
+
+    def fstat_logl(self, T, NFFT, qmin, dA, dE, invCA, f0, fdot, theta, phi, t0=0.0, fmt="sangria"):
+        """(logL_AE, A, iota, psi, phase), BW of get_Fstat_logL's A/E half."""
+        out = np.zeros(5)
+        bw = self.lib.orc_fstat_logl(FORMATS[fmt], T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), f0, fdot, theta,
+                                     phi, _p(out))
+        return out, bw
+
+    def fstat_batch(self, T, NFFT, seg_qmin, dA, dE, invCA, cell_seg, cells, t0=0.0, fmt="sangria", nthreads=0):
+        cells = np.ascontiguousarray(cells, np.float64).reshape(-1, 4)
+        out = np.zeros((len(cells), 5))
+        self.lib.orc_fstat_batch(FORMATS[fmt], T, t0, NFFT, _pi(np.ascontiguousarray(seg_qmin, np.int32)),
+                                 _p(np.ascontiguousarray(dA, np.float64)), _p(np.ascontiguousarray(dE, np.float64)),
+                                 _p(np.ascontiguousarray(invCA, np.float64)), len(cells),
+                                 _pi(np.ascontiguousarray(cell_seg, np.int32)), _p(cells), _p(out), nthreads)
+        return out
+
+    def fstat_proposal(self, T, NFFT, qmin, dA, dE, invCA, n_theta, n_phi, t0=0.0, fmt="sangria", nthreads=0):
+        """build_fstatistic_proposal on one segment: (tensor[n_f, n_theta, n_phi], norm, maxp)."""
+        fmin = self.segment_fmin(qmin, T)
+        n_f = int((fmin + NFFT / T - fmin) * T)
+        tensor = np.zeros((n_f, n_theta, n_phi))
+        info = np.zeros(3)
+        self.lib.orc_fstat_proposal(FORMATS[fmt], T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), n_theta, n_phi,
+                                    _p(tensor), _p(info), nthreads)
+        return tensor, info[1], info[2]
+
+    def ucb_fdot(self, Mc, f0):
+        return self.lib.orc_ucb_fdot(Mc, f0)
+
+    def segment_fmin(self, qmin, T):
+        return self.lib.orc_segment_fmin(qmin, T)
+
+    def invert4(self, M):
+        m = np.ascontiguousarray(M, np.float64).reshape(16).copy()
+        if self.lib.orc_invert4(_p(m)) != 0:
+            raise np.linalg.LinAlgError("singular")
+        return m.reshape(4, 4)
+
+    def fstat_params(self, a):
+        out = np.zeros(4)
+        self.lib.orc_fstat_params(_p(np.ascontiguousarray(a, np.float64)), _p(out))
+        return out
 
     def orbit(self, t):
         out = np.zeros(9)
@@ -398,3 +458,25 @@ class Ref:
         self.lib.ref_ucb_fisher(fmt.encode(), T, t0, NFFT, qmin, _p(invCA), _p(invCE),
                                 _p(np.ascontiguousarray(params, np.float64).copy()), _p(F), _p(ev), _p(evec))
         return F.reshape(8, 8), ev, evec.reshape(8, 8)
+
+    def fstat_logl(self, T, NFFT, qmin, dA, dE, invCA, cells, t0=0.0, fmt="sangria"):
+        """get_Fstat_logL per cell (f0, fdot, theta, phi): rows of logL_X, logL_AE, A, iota, psi, phase."""
+        lib = self.lib
+        lib.ref_fstat_logl.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                       _D, _D, _D, ctypes.c_int, _D, _D]
+        cells = np.ascontiguousarray(cells, np.float64).reshape(-1, 4)
+        out = np.zeros((len(cells), 6))
+        lib.ref_fstat_logl(fmt.encode(), T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), len(cells), _p(cells), _p(out))
+        return out
+
+    def fstat_proposal(self, T, NFFT, qmin, dA, dE, invCA, n_theta, n_phi, t0=0.0, fmt="sangria"):
+        """build_fstatistic_proposal: (tensor[n_f, n_theta, n_phi], norm, maxp)."""
+        lib = self.lib
+        lib.ref_fstat_proposal.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int, _D, _D, _D, ctypes.c_int, ctypes.c_int, _D, _D]
+        tensor = np.zeros(NFFT * n_theta * n_phi + 64 * n_theta * n_phi)
+        info = np.zeros(3)
+        lib.ref_fstat_proposal(fmt.encode(), T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), n_theta, n_phi,
+                               _p(tensor), _p(info))
+        n_f = int(info[0])
+        return tensor[:n_f * n_theta * n_phi].reshape(n_f, n_theta, n_phi), info[1], info[2]

@@ -404,3 +404,109 @@ double ref_wavelet_snr(int N, double *h, int *list, int n, double *invC)
     ref_wavelet_noise_free(noise);
     return r;
 }
+
+/* A one-segment struct Data for the F-statistic (ucb/src/glass_ucb_fstatistic.c
+ * reads T, t0, NFFT, fmin, format, dft->X/A/E and noise->C[0][0]); the X
+ * channel of the data is zero.  fmin is qmin/T, raised by an ulp where needed
+ * so that (int)(fmin T) == qmin as in utils/src/glass_data.c:1078. */
+static struct Data *fstat_data(const char *format, double T, double t0, int NFFT, int qmin, const double *dA,
+                               const double *dE, const double *invCA)
+{
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->NFFT = NFFT;
+    data->N = 2 * NFFT;
+    data->Nchannel = 2;
+    data->Nlayer = 1;
+    data->T = T;
+    data->sqT = sqrt(T);
+    data->t0 = t0;
+    data->fmin = (double)qmin / T;
+    while ((int)(data->fmin * T) < qmin) data->fmin = nextafter(data->fmin, INFINITY);
+    data->fmax = data->fmin + NFFT / T;
+    data->qmin = (int)(data->fmin * T);
+    data->qmax = data->qmin + NFFT;
+    strcpy(data->format, format);
+    strcpy(data->basis, "fourier");
+    data->dft = malloc(sizeof(struct TDI));
+    alloc_tdi(data->dft, data->N, 3);
+    memcpy(data->dft->A, dA, sizeof(double) * data->N);
+    memcpy(data->dft->E, dE, sizeof(double) * data->N);
+    data->noise = malloc(sizeof(struct Noise));
+    alloc_noise(data->noise, NFFT, 1, 2);
+    for (int n = 0; n < NFFT; n++) {
+        data->noise->invC[0][0][n] = invCA[n];
+        data->noise->C[0][0][n] = 1.0 / invCA[n];
+        data->noise->invC[1][1][n] = invCA[n];
+        data->noise->C[1][1][n] = 1.0 / invCA[n];
+    }
+    return data;
+}
+
+static void fstat_data_free(struct Data *data)
+{
+    free_tdi(data->dft);
+    free_noise(data->noise);
+    free(data);
+}
+
+/* ucb/src/glass_ucb_fstatistic.c:646 (get_Fstat_logL) for n cells
+ * (f0, fdot, theta, phi); out[6 c ..] = logL_X, logL_AE, Fparams[0..3]. */
+void ref_fstat_logl(const char *format, double T, double t0, int NFFT, int qmin, const double *dA, const double *dE,
+                    const double *invCA, int n, const double *cells, double *out)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct Data *data = fstat_data(format, T, t0, NFFT, qmin, dA, dE, invCA);
+    for (int c = 0; c < n; c++) {
+        const double *x = cells + 4 * c;
+        double *o = out + 6 * c;
+        get_Fstat_logL(&orbit, data, x[0], x[1], x[2], x[3], &o[0], &o[1], o + 2);
+    }
+    fstat_data_free(data);
+}
+
+/* ucb/src/glass_ucb_proposal.c:1085 (build_fstatistic_proposal) with the grid
+ * of setup_fstatistic_proposal (:927-971) at n_theta x n_phi sky cells.
+ * tensor: n_f n_theta n_phi doubles; info = {n_f, norm, maxp}. */
+void ref_fstat_proposal(const char *format, double T, double t0, int NFFT, int qmin, const double *dA,
+                        const double *dE, const double *invCA, int n_theta, int n_phi, double *tensor, double *info)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct Data *data = fstat_data(format, T, t0, NFFT, qmin, dA, dE, invCA);
+    struct Flags flags;
+    memset(&flags, 0, sizeof(flags));
+    flags.quiet = 1;
+    flags.threads = 1;
+    int n_f = (int)((data->fmax - data->fmin) * data->T);
+    struct Proposal proposal;
+    memset(&proposal, 0, sizeof(proposal));
+    proposal.matrix = malloc(3 * sizeof(double *));
+    for (int i = 0; i < 3; i++) proposal.matrix[i] = calloc(2, sizeof(double));
+    proposal.matrix[0][0] = (double)n_f;
+    proposal.matrix[0][1] = (int)((data->fmax - data->fmin) * data->T) / (double)n_f / data->T;
+    proposal.matrix[1][0] = (double)n_theta;
+    proposal.matrix[1][1] = 2. / (double)n_theta;
+    proposal.matrix[2][0] = (double)n_phi;
+    proposal.matrix[2][1] = PI2 / (double)n_phi;
+    proposal.tensor = malloc(n_f * sizeof(double **));
+    for (int i = 0; i < n_f; i++) {
+        proposal.tensor[i] = malloc(n_theta * sizeof(double *));
+        for (int j = 0; j < n_theta; j++) proposal.tensor[i][j] = calloc(n_phi, sizeof(double));
+    }
+    build_fstatistic_proposal(&orbit, data, &flags, &proposal);
+    for (int i = 0; i < n_f; i++) {
+        for (int j = 0; j < n_theta; j++) {
+            for (int k = 0; k < n_phi; k++) tensor[((size_t)i * n_theta + j) * n_phi + k] = proposal.tensor[i][j][k];
+            free(proposal.tensor[i][j]);
+        }
+        free(proposal.tensor[i]);
+    }
+    free(proposal.tensor);
+    info[0] = n_f;
+    info[1] = proposal.norm;
+    info[2] = proposal.maxp;
+    for (int i = 0; i < 3; i++) free(proposal.matrix[i]);
+    free(proposal.matrix);
+    fstat_data_free(data);
+}

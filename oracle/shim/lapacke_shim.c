@@ -67,9 +67,13 @@ int LAPACKE_dgeev(int layout, char jobvl, char jobvr, int n, double *a, int lda,
     return 0;
 }
 
+/* LAPACK semantics: a zero pivot is recorded in the return value (the first
+ * one, 1-based) and the factorisation carries on without scaling that column,
+ * so ipiv is always filled. */
 int LAPACKE_dgetrf(int layout, int mrows, int n, double *a, int lda, int *ipiv)
 {
     (void)layout;
+    int info = 0;
     int kmax = mrows < n ? mrows : n;
     for (int k = 0; k < kmax; k++) {
         int piv = k;
@@ -80,18 +84,25 @@ int LAPACKE_dgetrf(int layout, int mrows, int n, double *a, int lda, int *ipiv)
             for (int j = 0; j < n; j++) {
                 double t = a[k * lda + j]; a[k * lda + j] = a[piv * lda + j]; a[piv * lda + j] = t;
             }
-        if (a[k * lda + k] == 0.0) return k + 1;
+        if (a[k * lda + k] == 0.0) {
+            if (!info) info = k + 1;
+            continue;
+        }
         for (int i = k + 1; i < mrows; i++) {
             a[i * lda + k] /= a[k * lda + k];
             for (int j = k + 1; j < n; j++) a[i * lda + j] -= a[i * lda + k] * a[k * lda + j];
         }
     }
-    return 0;
+    return info;
 }
 
+/* LAPACK semantics: a singular U (a zero on its diagonal) returns that index
+ * and leaves a unchanged. */
 int LAPACKE_dgetri(int layout, int n, double *a, int lda, const int *ipiv)
 {
     (void)layout;
+    for (int i = 0; i < n; i++)
+        if (a[i * lda + i] == 0.0) return i + 1;
     double *inv = calloc((size_t)n * n, sizeof(double));
     for (int col = 0; col < n; col++) {
         double *x = inv + (size_t)col * n; /* column stored contiguously */

@@ -15,12 +15,22 @@ utils/src/glass_model.c:726), snr (utils/src/glass_math.c:403) and ucb_fisher
 (ucb/src/glass_ucb_waveform.c:1061) with initialize_interpolated_analytic_orbits
 (utils/src/glass_lisa.c:271), delta_log_likelihood and
 gaussian_log_likelhood_wavelet (utils/src/glass_model.c:624, :805) and
-snr_wavelet (utils/src/glass_math.c:428).  Inputs are seeded numpy draws.
+snr_wavelet (utils/src/glass_math.c:428), get_Fstat_logL
+(ucb/src/glass_ucb_fstatistic.c:646) and build_fstatistic_proposal
+(ucb/src/glass_ucb_proposal.c:1085).  Inputs are seeded numpy draws.
+
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py fstat      # only the named ones
 """
 from __future__ import annotations
 
 import os
 import sys
+
+# one OpenMP thread for the reference: build_fstatistic_proposal opens a
+# parallel region per frequency, and nested regions with the default team
+# size make it several hundred times slower
+os.environ.setdefault("OMP_NUM_THREADS", "1")
 
 import numpy as np
 
@@ -238,8 +248,63 @@ def wavelet_likelihood(ref, rng):
     np.savez_compressed(os.path.join(HERE, "wavelet_likelihood.npz"), ncase=2, grid=grid, edge=100, **out)
 
 
-def main():
+def _fstat_segment(ref, rng, f0, amp, fdot, NFFT, fmt="sangria"):
+    inj = wl.draw_source(rng, f0, amp, fdot)
+
+    def wf(p):
+        al = ref.alignment(T, NFFT, 0, p)
+        h = ref.waveform(p, int(al[0]), T, fmt=fmt)
+        return int(al[0]), h[3], h[4]
+
+    qmin, dA, dE, iA, _ = wl.make_segment(rng, [inj], wf, NFFT=NFFT, T=T)
+    il = np.empty((2, 2 * NFFT))
+    il[0, 0::2], il[0, 1::2] = dA.real, dA.imag
+    il[1, 0::2], il[1, 1::2] = dE.real, dE.imag
+    return inj, qmin, il[0].copy(), il[1].copy(), iA
+
+
+def fstat(ref, rng):
+    """get_Fstat_logL on cells scattered over (and a little beyond) segments
+    holding one injected source, and build_fstatistic_proposal on a short
+    segment.  Cells whose filters miss the segment entirely are included: the
+    reference returns logL = 0 there."""
+    out = {}
+    cases = [("sangria", 3.2e-3, 3e-22, 1e-17, 160), ("sangria", 0.8e-3, 2e-22, 1e-18, 120),
+             ("sangria", 12e-3, 1e-22, 1e-15, 120), ("phase", 2.5e-3, 2e-22, 1e-17, 40),
+             ("frequency", 6e-3, 2e-22, 1e-16, 40)]
+    for c, (fmt, f0, amp, fdot, n) in enumerate(cases):
+        inj, qmin, dA, dE, iA = _fstat_segment(ref, rng, f0, amp, fdot, 1024, fmt)
+        f = (qmin + rng.uniform(-24, 1048, n)) / T
+        fd = np.where(rng.random(n) < 0.5, 0.0, 10 ** rng.uniform(-18, -13, n))
+        th = np.arccos(rng.uniform(-1, 1, n))
+        ph = rng.uniform(0, 2 * np.pi, n)
+        cells = np.stack([f, fd, th, ph], 1)
+        # a few cells at the source and next to it
+        src = np.array([inj[0] / T, inj[7] / T ** 2, np.arccos(inj[1]), inj[2]])
+        near = src + np.array([[0, 0, 0, 0], [0.5 / T, 0, 0.05, -0.1], [-1.0 / T, 0, -0.1, 0.2], [0.0, 0, 0.3, 0.0]])
+        cells = np.vstack([near, cells])
+        out[f"c{c}_fmt"] = fmt
+        out[f"c{c}_qmin"] = qmin
+        out[f"c{c}_dA"], out[f"c{c}_dE"], out[f"c{c}_invCA"] = dA, dE, iA
+        out[f"c{c}_cells"] = cells
+        out[f"c{c}_out"] = ref.fstat_logl(T, 1024, qmin, dA, dE, iA, cells, fmt=fmt)
+    # the proposal grid of one short segment
+    inj, qmin, dA, dE, iA = _fstat_segment(ref, rng, 4e-3, 4e-22, 1e-17, 64)
+    tensor, norm, maxp = ref.fstat_proposal(T, 64, qmin, dA, dE, iA, 4, 5)
+    out.update(p_qmin=qmin, p_dA=dA, p_dE=dE, p_invCA=iA, p_n_theta=4, p_n_phi=5, p_tensor=tensor, p_norm=norm,
+               p_maxp=maxp)
+    np.savez_compressed(os.path.join(HERE, "fstat.npz"), ncase=len(cases), **out)
+
+
+OWN_SEEDS = {"fstat": 20261204}
+
+
+def main(names=()):
     ref = Ref()
+    if names:  # fixtures with a seed of their own can be regenerated alone
+        for name in names:
+            globals()[name](ref, np.random.default_rng(OWN_SEEDS[name]))
+        return
     rng = np.random.default_rng(20261203)
     waveforms(ref, rng)
     bandwidth(ref, rng)
@@ -248,10 +313,11 @@ def main():
     wdm(ref, rng)
     wavelet_waveforms(ref, rng)
     wavelet_likelihood(ref, rng)
+    fstat(ref, np.random.default_rng(OWN_SEEDS["fstat"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -179,3 +179,63 @@ def test_wavelet_likelihoods_match_reference(port, golden):
             assert abs(full - ref) < 1e-10 * max(1.0, abs(ref)), (c, q)
             snr = port.wavelet_snr(hy, ly, invC)
             assert abs(snr - g[f"c{c}_snr"][q]) < 1e-10 * g[f"c{c}_snr"][q]
+
+
+# ------------------------------------------------------------- F-statistic
+def _fstat_case(g, c):
+    return (str(g[f"c{c}_fmt"]), int(g[f"c{c}_qmin"]), g[f"c{c}_dA"], g[f"c{c}_dE"], g[f"c{c}_invCA"],
+            g[f"c{c}_cells"], g[f"c{c}_out"])
+
+
+def assert_fstat_close(got, ref, rel=1e-11, ang=1e-10):
+    """got, ref: rows of (logL_AE, A, iota, psi, phase).  logL and A to a
+    relative tolerance, the angles to an absolute one; NaN where the
+    reference has NaN (no filter bin inside the segment)."""
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(ref))
+    ok = ~np.isnan(ref)
+    for k in (0, 1):
+        m = ok[:, k]
+        scale = np.maximum(np.abs(ref[m, k]), np.abs(ref[m, k]).max() * 1e-6 if m.any() else 0)
+        scale = np.where(scale > 0, scale, 1.0)
+        err = np.abs(got[m, k] - ref[m, k]) / scale
+        assert err.max(initial=0) < rel, (k, err.max())
+    for k in (2, 3, 4):
+        m = ok[:, k]
+        d = np.abs(got[m, k] - ref[m, k])
+        if k == 4:  # phase is defined mod 2 pi
+            d = np.minimum(d, 2 * np.pi - d)
+        assert d.max(initial=0) < ang, (k, d.max())
+
+
+def test_fstat_matches_reference(port, golden):
+    """get_Fstat_logL (ucb/src/glass_ucb_fstatistic.c:646): logL_AE and the
+    maximum-likelihood A, iota, psi, phase, in all three TDI formats, with
+    template sizes from 16 to 512 and cells beyond both segment edges."""
+    g = golden("fstat.npz")
+    sizes = set()
+    for c in range(int(g["ncase"])):
+        fmt, qmin, dA, dE, iA, cells, ref = _fstat_case(g, c)
+        got = port.fstat_batch(T, 1024, [qmin], dA, dE, iA, np.zeros(len(cells), np.int32), cells, fmt=fmt)
+        assert_fstat_close(got, ref[:, 1:])
+        sizes |= {port.bandwidth(x[0], x[1], np.cos(x[2]), 1e-22, T, 1024) for x in cells}
+    assert {16, 32, 64, 128, 256, 512} <= sizes
+
+
+def test_fstat_proposal_matches_reference(port, golden):
+    """build_fstatistic_proposal (ucb/src/glass_ucb_proposal.c:1085): the
+    normalised density over a 63 x 4 x 5 grid, its norm and maximum."""
+    g = golden("fstat.npz")
+    tensor, norm, maxp = port.fstat_proposal(T, 64, int(g["p_qmin"]), g["p_dA"], g["p_dE"], g["p_invCA"],
+                                             int(g["p_n_theta"]), int(g["p_n_phi"]))
+    assert tensor.shape == g["p_tensor"].shape
+    np.testing.assert_allclose(tensor, g["p_tensor"], rtol=1e-11)
+    assert abs(norm - float(g["p_norm"])) < 1e-11 * abs(float(g["p_norm"]))
+    assert abs(maxp - float(g["p_maxp"])) < 1e-11 * abs(float(g["p_maxp"]))
+
+
+def test_invert4_against_numpy(port):
+    rng = np.random.default_rng(4)
+    for _ in range(50):
+        a = rng.standard_normal((4, 4))
+        m = a @ a.T + 0.1 * np.eye(4)
+        np.testing.assert_allclose(port.invert4(m), np.linalg.inv(m), rtol=1e-9, atol=1e-12)
