@@ -44,6 +44,7 @@ EXPORTS = (
     "wavelet_transform_freq", "wavelet_transform_inverse_freq", "ucb_waveform_wavelet", "ucb_waveform_wavelet_tab",
     "ucb_waveform_wavelet_slow", "glass_ucb_waveform_wavelet_tab", "glass_ucb_waveform_wavelet_slow",
     "glass_gpu_wavelet_fisher_batch", "glass_gpu_wavelet_fisher_batch_host",
+    "glass_gpu_fstat_batch", "glass_gpu_fstat_batch_host", "glass_gpu_fstat_proposal_host",
 )
 
 _lib = None
@@ -103,6 +104,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_wavelet_waveform_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _I, _D, _I]
     lib.glass_gpu_wavelet_fisher_batch.argtypes = [_V, ctypes.c_int, _V, ctypes.c_int, ctypes.c_int, _V, _V]
     lib.glass_gpu_wavelet_fisher_batch_host.argtypes = [_V, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int, _D, _I]
+    lib.glass_gpu_fstat_batch.argtypes = [_V, ctypes.c_int, _V, _V, _V, _V, _V]
+    lib.glass_gpu_fstat_batch_host.argtypes = [_V, ctypes.c_int, _I, _D, _D, _D, _I]
+    lib.glass_gpu_fstat_proposal_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
     _lib = lib
     return lib
 
@@ -355,6 +359,34 @@ class Engine:
         _check(self.lib.glass_gpu_wavelet_fisher_batch_host(self._ctx, n, _pd(p), int(imin), int(imax), _pd(F),
                                                             _pi(st)))
         return F, st
+
+    def fstat_host(self, cell_seg, cells):
+        """F-statistic of cells (f0, fdot, theta, phi) on the bank's segments:
+        (logL_AE [n], fparams [n, 4] = A, iota, psi, phase, status [n])."""
+        seg = np.ascontiguousarray(cell_seg, np.int32)
+        c = np.ascontiguousarray(cells, np.float64).reshape(-1, 4)
+        n = len(seg)
+        assert c.shape[0] == n
+        ll, fp, st = np.empty(n), np.empty((n, 4)), np.empty(n, np.int32)
+        _check(self.lib.glass_gpu_fstat_batch_host(self._ctx, n, _pi(seg), _pd(c), _pd(ll), _pd(fp), _pi(st)))
+        return ll, fp, st
+
+    def fstat_device(self, cell_seg, cells, logl, fparams=None, status=None):
+        """Device tensors (int32 cell_seg, float64 cells [n, 4], float64 outputs);
+        asynchronous on the context's stream."""
+        n = int(cell_seg.numel())
+        _check(self.lib.glass_gpu_fstat_batch(self._ctx, n, _ptr(cell_seg), _ptr(cells), _ptr(logl), _ptr(fparams),
+                                              _ptr(status)))
+
+    def fstat_proposal_host(self, seg, n_theta=20, n_phi=20):
+        """build_fstatistic_proposal on one segment: (tensor [n_f, n_theta, n_phi],
+        norm, maxp, number of cells that ran the chirp-mass scan)."""
+        tensor = np.empty(self.NFFT * n_theta * n_phi)
+        info = np.zeros(4)
+        _check(self.lib.glass_gpu_fstat_proposal_host(self._ctx, int(seg), int(n_theta), int(n_phi), _pd(tensor),
+                                                      _pd(info)))
+        n_f = int(info[0])
+        return tensor[:n_f * n_theta * n_phi].reshape(n_f, n_theta, n_phi), info[1], info[2], int(info[3])
 
     def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                              precision=PREC_FP64):

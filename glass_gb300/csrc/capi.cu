@@ -78,6 +78,7 @@ struct glass_gpu_ctx {
   WvWorkDev wvw;
   void *wv_work_mem = nullptr;
   void *wv_fisher_mem = nullptr;  // perturbed parameters of the Fisher batches
+  FsWorkDev fsw;  // F-statistic scratch
 };
 
 static void clear_host_graphs(glass_gpu_ctx *ctx) {
@@ -144,6 +145,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->wv_data_mem);
   cudaFree(ctx->wv_work_mem);
   cudaFree(ctx->wv_fisher_mem);
+  fs_work_free(ctx->fsw);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
@@ -235,7 +237,8 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   size_t off_w64 = off_g32 + sizeof(float4) * g32.size();
   size_t off_g64 = off_w64 + sizeof(double2) * w64.size();
   size_t off_invc = off_g64 + sizeof(double2) * g64.size();
-  size_t total = off_invc + sizeof(float2) * nb;
+  size_t off_rho = (off_invc + sizeof(float2) * nb + 255) / 256 * 256;
+  size_t total = off_rho + sizeof(double) * nb;
   GLASS_CUDA(cudaMalloc(&ctx->bank_mem, total), "cudaMalloc(bank)");
   char *base = (char *)ctx->bank_mem;
   FdBankDev &b = ctx->bank;
@@ -253,6 +256,7 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   b.w64 = (double2 *)(base + off_w64);
   b.g64 = (double2 *)(base + off_g64);
   b.invc = (float2 *)(base + off_invc);
+  b.rho = (double *)(base + off_rho);
   GLASS_CUDA(cudaMemcpy(b.qmin, qmin, sizeof(int) * nseg, cudaMemcpyHostToDevice), "upload qmin");
   GLASS_CUDA(cudaMemcpy(b.Q, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice), "upload Q");
   GLASS_CUDA(cudaMemcpy(b.w32, w32.data(), sizeof(float4) * w32.size(), cudaMemcpyHostToDevice), "upload w32");
@@ -270,6 +274,9 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
         ic[sj] = make_float2((float)(invCA[sj] / invCA[s0]), (float)(invCE[sj] / invCE[s0]));
       }
     GLASS_CUDA(cudaMemcpy(b.invc, ic.data(), sizeof(float2) * nb, cudaMemcpyHostToDevice), "upload invc");
+    std::vector<double> rho(nb);
+    for (size_t sj = 0; sj < nb; sj++) rho[sj] = invCA[sj] / invCE[sj];
+    GLASS_CUDA(cudaMemcpy(b.rho, rho.data(), sizeof(double) * nb, cudaMemcpyHostToDevice), "upload rho");
   }
   ctx->h_qmin.assign(qmin, qmin + nseg);
   ctx->h_invCA.assign(invCA, invCA + nb);
@@ -537,6 +544,183 @@ extern "C" int glass_gpu_grad_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, 
   if (fisher) GLASS_CUDA(cudaMemcpyAsync(fisher, d_f, sizeof(double) * 64 * nd, cudaMemcpyDeviceToHost, s), "D2H fisher");
   if (status) GLASS_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int) * nd, cudaMemcpyDeviceToHost, s), "D2H status");
   GLASS_CUDA(cudaStreamSynchronize(s), "grad_fisher_batch_host sync");
+  return GLASS_OK;
+}
+
+// ------------------------------------------------------------ F-statistic
+// Scratch of the F-statistic batches: cells per launch sequence bounded so
+// that the filter series (16 N complex doubles per cell at the segment's
+// largest filter size) stay within kFsSeriesBudget.
+static constexpr size_t kFsSeriesBudget = (size_t)2 << 30;
+
+static int ensure_fs_work(glass_gpu_ctx *ctx, int ncells) {
+  int maxN = fs_max_size(ctx->bank.NFFT);
+  if (maxN > kMaxN) maxN = kMaxN;
+  const size_t per_cell = (size_t)16 * maxN * sizeof(double2);
+  size_t chunk = kFsSeriesBudget / per_cell;
+  if (chunk < 256) chunk = 256;
+  size_t want = 256;
+  while (want < (size_t)ncells && want < chunk) want *= 2;
+  if (want > chunk) want = chunk;
+  FsWorkDev &w = ctx->fsw;
+  if (w.mem && (size_t)w.cap >= want && w.series_bytes >= (size_t)w.cap * per_cell) return GLASS_OK;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "fstat work sync");
+  GLASS_CUDA(fs_work_alloc(w, (int)want, ctx->bank.NFFT), "cudaMalloc(fstat work)");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_fstat_batch(glass_gpu_ctx *ctx, int ncells, const int *cell_seg, const double *cells,
+                                     double *logl, double *fparams, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "fstat_batch: null context");
+  if (ncells < 0) return set_err(GLASS_ERR_ARG, "fstat_batch: negative cell count");
+  if (ncells == 0) return GLASS_OK;
+  if (!cell_seg || !cells || !logl) return set_err(GLASS_ERR_ARG, "fstat_batch: null argument");
+  if (!ctx->bank.nseg) return set_err(GLASS_ERR_STATE, "fstat_batch: no segment bank uploaded");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_fs_work(ctx, ncells))) return rc;
+  int nl = 0;
+  cudaError_t e = fs_launch(ctx->bank, ctx->tab, ctx->bank.rho, ctx->fsw, ncells, cell_seg, 0, cells, logl, fparams,
+                            status, ctx->num_sms, ctx->stream, &nl);
+  ctx->last_launches = nl;
+  if (e != cudaSuccess) return cuda_err(e, "fstat_batch launch");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_fstat_batch_host(glass_gpu_ctx *ctx, int ncells, const int *cell_seg, const double *cells,
+                                          double *logl, double *fparams, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "fstat_batch_host: null context");
+  if (ncells < 0) return set_err(GLASS_ERR_ARG, "fstat_batch_host: negative cell count");
+  if (ncells == 0) return GLASS_OK;
+  if (!cell_seg || !cells || !logl) return set_err(GLASS_ERR_ARG, "fstat_batch_host: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t nd = (size_t)ncells;
+  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (4 + 1 + 4) + sizeof(int) * nd * 2 + 256))) return rc;
+  double *d_cells = (double *)ctx->d_stage;
+  double *d_logl = d_cells + 4 * nd;
+  double *d_fp = d_logl + nd;
+  int *d_seg = (int *)(d_fp + 4 * nd);
+  int *d_st = d_seg + nd;
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d_cells, cells, sizeof(double) * 4 * nd, cudaMemcpyHostToDevice, s), "H2D cells");
+  GLASS_CUDA(cudaMemcpyAsync(d_seg, cell_seg, sizeof(int) * nd, cudaMemcpyHostToDevice, s), "H2D cell_seg");
+  rc = glass_gpu_fstat_batch(ctx, ncells, d_seg, d_cells, d_logl, fparams ? d_fp : nullptr, d_st);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(logl, d_logl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
+  if (fparams)
+    GLASS_CUDA(cudaMemcpyAsync(fparams, d_fp, sizeof(double) * 4 * nd, cudaMemcpyDeviceToHost, s), "D2H fparams");
+  if (status) GLASS_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int) * nd, cudaMemcpyDeviceToHost, s), "D2H status");
+  GLASS_CUDA(cudaStreamSynchronize(s), "fstat_batch_host sync");
+  return GLASS_OK;
+}
+
+// ucb/src/glass_ucb_waveform.c:307-314 (ucb_fdot)
+static double host_ucb_fdot(double Mc, double f0) {
+  double M = Mc * 4.92569043916e-6;  // TSUN, utils/src/glass_constants.h:60
+  return 19.2 * pow(pow(M_PI, 8) * pow(M, 5) * pow(f0, 11), 1. / 3.);
+}
+
+extern "C" int glass_gpu_fstat_proposal_host(glass_gpu_ctx *ctx, int seg, int n_theta, int n_phi, double *tensor,
+                                             double *info) {
+  if (!ctx || !tensor || !info) return set_err(GLASS_ERR_ARG, "fstat_proposal_host: null argument");
+  const FdBankDev &b = ctx->bank;
+  if (!b.nseg) return set_err(GLASS_ERR_STATE, "fstat_proposal_host: no segment bank uploaded");
+  if (seg < 0 || seg >= b.nseg) return set_err(GLASS_ERR_ARG, "fstat_proposal_host: segment out of range");
+  if (n_theta < 1 || n_phi < 1) return set_err(GLASS_ERR_ARG, "fstat_proposal_host: empty sky grid");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  // the segment's frequency range as the reference holds it
+  // (utils/src/glass_data.c:1077-1078, 2065-2066) and the grid of
+  // setup_fstatistic_proposal (ucb/src/glass_ucb_proposal.c:927-943)
+  const double T = b.T;
+  const int qmin = ctx->h_qmin[seg];
+  double fmin = (double)qmin / T;
+  while ((int)(fmin * T) < qmin) fmin = nextafter(fmin, INFINITY);
+  const double fmax = fmin + b.NFFT / T;
+  FsGrid G;
+  G.n_f = (int)((fmax - fmin) * T);
+  G.n_theta = n_theta;
+  G.n_phi = n_phi;
+  G.fmin = fmin;
+  G.d_f = (int)((fmax - fmin) * T) / (double)G.n_f / T;
+  G.d_theta = 2. / (double)n_theta;
+  G.d_phi = kPI2 / (double)n_phi;
+  if (G.n_f < 1) return set_err(GLASS_ERR_ARG, "fstat_proposal_host: empty frequency grid");
+  const long long nll = (long long)G.n_f * n_theta * n_phi;
+  if (nll > (1LL << 28)) return set_err(GLASS_ERR_ARG, "fstat_proposal_host: grid too large");
+  const int n = (int)nll;
+  // chirp-mass scan values per frequency row (:1099-1100, :1142)
+  std::vector<double> fdot_tab((size_t)G.n_f * kFsScan);
+  const double dMc = (1.1 - 0.1) / kFsScan;
+  for (int i = 0; i < G.n_f; i++) {
+    double f = fmin + i * G.d_f;
+    f += G.d_f / 2;
+    for (int s = 0; s < kFsScan; s++) fdot_tab[(size_t)i * kFsScan + s] = host_ucb_fdot(0.1 + s * dMc, f);
+  }
+  if ((rc = ensure_fs_work(ctx, n))) return rc;
+  cudaStream_t st = ctx->stream;
+  // scratch: grid cells, logL at fdot = 0, scan bookkeeping, density
+  char *mem = nullptr;
+  const size_t n_d = (size_t)n;
+  size_t off_logl0 = sizeof(double) * 4 * n_d;
+  size_t off_tensor = off_logl0 + sizeof(double) * n_d;
+  size_t off_fdot = off_tensor + sizeof(double) * n_d;
+  size_t off_pos = off_fdot + sizeof(double) * fdot_tab.size();
+  size_t off_active = off_pos + sizeof(int) * n_d;
+  size_t off_count = off_active + sizeof(int) * n_d;
+  size_t total = off_count + 256;
+  GLASS_CUDA(cudaMalloc(&mem, total), "cudaMalloc(fstat grid)");
+  struct Free {
+    char *&p;
+    ~Free() { cudaFree(p); }
+  } guard{mem};
+  double *d_cells = (double *)mem, *d_logl0 = (double *)(mem + off_logl0), *d_tensor = (double *)(mem + off_tensor);
+  double *d_fdot = (double *)(mem + off_fdot);
+  int *d_pos = (int *)(mem + off_pos), *d_active = (int *)(mem + off_active), *d_count = (int *)(mem + off_count);
+  GLASS_CUDA(cudaMemcpyAsync(d_fdot, fdot_tab.data(), sizeof(double) * fdot_tab.size(), cudaMemcpyHostToDevice, st),
+             "H2D fdot table");
+  GLASS_CUDA(fs_grid_cells(G, 0, n, d_cells, st), "fstat grid cells");
+  int nl = 0, nl2 = 0;
+  GLASS_CUDA(fs_launch(b, ctx->tab, b.rho, ctx->fsw, n, nullptr, seg, d_cells, d_logl0, nullptr, nullptr,
+                       ctx->num_sms, st, &nl), "fstat grid launch");
+  GLASS_CUDA(cudaMemsetAsync(d_count, 0, sizeof(int), st), "fstat scan count");
+  GLASS_CUDA(fs_scan_mark(d_logl0, n, d_count, d_active, d_pos, st), "fstat scan mark");
+  int nact = 0;
+  GLASS_CUDA(cudaMemcpyAsync(&nact, d_count, sizeof(int), cudaMemcpyDeviceToHost, st), "D2H scan count");
+  GLASS_CUDA(cudaStreamSynchronize(st), "fstat scan sync");
+  double *d_scan = nullptr;
+  char *smem = nullptr;
+  struct Free2 {
+    char *&p;
+    ~Free2() { cudaFree(p); }
+  } guard2{smem};
+  if (nact > 0) {
+    const size_t ns = (size_t)nact * kFsScan;
+    GLASS_CUDA(cudaMalloc(&smem, sizeof(double) * 5 * ns), "cudaMalloc(fstat scan)");
+    double *d_scells = (double *)smem;
+    d_scan = d_scells + 4 * ns;
+    GLASS_CUDA(fs_scan_cells(G, d_active, 0, (int)ns, d_fdot, d_scells, st), "fstat scan cells");
+    GLASS_CUDA(fs_launch(b, ctx->tab, b.rho, ctx->fsw, (int)ns, nullptr, seg, d_scells, d_scan, nullptr, nullptr,
+                         ctx->num_sms, st, &nl2), "fstat scan launch");
+  }
+  GLASS_CUDA(fs_finalize(d_logl0, d_pos, d_scan, n, d_tensor, st), "fstat finalize");
+  ctx->last_launches = nl + nl2 + 4 + (nact > 0 ? 1 : 0);
+  GLASS_CUDA(cudaMemcpyAsync(tensor, d_tensor, sizeof(double) * n_d, cudaMemcpyDeviceToHost, st), "D2H tensor");
+  GLASS_CUDA(cudaStreamSynchronize(st), "fstat proposal sync");
+  // normalisation and maximum in the reference's order (:1154-1181)
+  double norm = 0.0;
+  for (size_t c = 0; c < n_d; c++) norm += tensor[c];
+  norm = (G.n_f * n_theta * n_phi) / norm;
+  double maxp = -1.e60;
+  for (size_t c = 0; c < n_d; c++) {
+    tensor[c] *= norm;
+    if (tensor[c] > maxp) maxp = tensor[c];
+  }
+  info[0] = G.n_f;
+  info[1] = norm;
+  info[2] = maxp;
+  info[3] = nact;
   return GLASS_OK;
 }
 

@@ -9,6 +9,7 @@ namespace glass {
 // Device-resident inputs shared by every evaluation of a segment bank.
 struct FdBankDev {
   int nseg = 0, NFFT = 0, format = 0;
+  double *rho = nullptr;       // [nseg*NFFT] invC_A / invC_E (F-statistic weights of the E channel)
   double T = 0, t0 = 0, fstar = 0;
   int *qmin = nullptr;         // [nseg]
   float4 *w32 = nullptr;       // [nseg*NFFT]   whitened residual {A.re, A.im, E.re, E.im}, rounded to float
@@ -83,6 +84,42 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
                            const int *item_seg, const double *params, int N_fixed, int fisher_mode, double *term_y,
                            double *grad, double *fisher, int *status, int num_sms, cudaStream_t stream,
                            int *nlaunch);
+
+// F-statistic of sky/frequency cells (ucb_fstat.cu).  Scratch for up to `cap`
+// cells per launch sequence, sized for the largest filter of the segment size.
+struct FsWorkDev {
+  int cap = 0;
+  void *mem = nullptr;
+  void *cells = nullptr;     // [cap] per-cell constants
+  int *bin_count = nullptr;  // [16]
+  int *bin_list = nullptr;   // [9*cap]
+  void *series = nullptr;    // 16 series of N complex doubles per cell
+  size_t series_bytes = 0;
+};
+size_t fs_cell_bytes();
+int fs_max_size(int NFFT);
+cudaError_t fs_work_alloc(FsWorkDev &w, int cap, int NFFT);
+void fs_work_free(FsWorkDev &w);
+// cells[4 c] = f0, fdot, theta, phi; outputs as glass_gpu_fstat_batch.  Runs
+// the cells in chunks of w.cap.
+// cell_seg may be null: every cell on segment seg_const.
+cudaError_t fs_launch(const FdBankDev &bank, const FdTablesDev &tab, const double *rho, FsWorkDev &w, int ncells,
+                      const int *cell_seg, int seg_const, const double *cells, double *logl, double *fparams,
+                      int *status, int num_sms, cudaStream_t stream, int *nlaunch);
+
+// The frequency x sky grid of build_fstatistic_proposal
+// (ucb/src/glass_ucb_proposal.c:927-943, 1085-1182) and its chirp-mass scan.
+constexpr int kFsScan = 10;  // chirp masses 0.1, 0.2, ... 1.0 (:1099-1100)
+struct FsGrid {
+  int n_f, n_theta, n_phi;
+  double fmin, d_f, d_theta, d_phi;
+};
+cudaError_t fs_grid_cells(const FsGrid &G, int g0, int n, double *cells, cudaStream_t stream);
+cudaError_t fs_scan_mark(const double *logl0, int n, int *count, int *active, int *pos, cudaStream_t stream);
+cudaError_t fs_scan_cells(const FsGrid &G, const int *active, int c0, int n, const double *fdot_tab, double *cells,
+                          cudaStream_t stream);
+cudaError_t fs_finalize(const double *logl0, const int *pos, const double *scan, int n, double *tensor,
+                        cudaStream_t stream);
 
 // Single waveform in the reference's output layout (legacy ucb_waveform).
 // pos: N orbit samples (device), item: the source's FP64 constants (device,

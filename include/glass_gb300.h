@@ -169,6 +169,51 @@ int glass_gpu_grad_fisher_batch(glass_gpu_ctx *ctx, int nitems, const int *item_
 int glass_gpu_grad_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const int *item_seg, const double *params,
                                      int fisher_mode, double *term_y, double *grad, double *fisher, int *status);
 
+/*
+ * F-statistic of sky/frequency cells on the bank's segments; replaces
+ * get_Fstat_logL (ucb/src/glass_ucb_fstatistic.c:646-703, declared at
+ * ucb/src/glass_ucb_fstatistic.h:79), A/E channels.  Cell c is
+ *   cells[4 c ..] = f0 (Hz), fdot (Hz/s), theta (colatitude, rad), phi (rad)
+ * on segment cell_seg[c]; its four filters have the reference's size
+ * ucb_bandwidth(f0, fdot, cos theta, A = 1e-22) and parameters (:241-344).
+ *   logl[c]         = logL_AE = N^T M^-1 N / 2 (:599-622)
+ *   fparams[4 c ..] = A, iota, psi, phase, the maximum-likelihood values
+ *                     (:525-597, :697-700); may be NULL
+ *   status[c]       = GLASS_ITEM_* bits (may be NULL): GLASS_ITEM_OUTSIDE when
+ *                     no filter bin lies inside the segment (logL = 0, as the
+ *                     reference gives when LAPACK meets the zero matrix),
+ *                     GLASS_ITEM_NONFINITE for non-finite input, f0 <= 0,
+ *                     filters above 4096 samples (segments over 8192 bins) or
+ *                     a singular M.
+ * As in the reference, N^i and M^ij run over the segment bins 0 < k < NFFT and
+ * weight both channels with the A channel's noise.  logL_X (the X channel) is
+ * not computed: the bank holds A and E.  FP64 throughout.  Device pointers;
+ * asynchronous on the context's stream.
+ */
+int glass_gpu_fstat_batch(glass_gpu_ctx *ctx, int ncells, const int *cell_seg, const double *cells, double *logl,
+                          double *fparams, int *status);
+
+/* Same with HOST pointers: copies in, evaluates, copies out, synchronises. */
+int glass_gpu_fstat_batch_host(glass_gpu_ctx *ctx, int ncells, const int *cell_seg, const double *cells, double *logl,
+                               double *fparams, int *status);
+
+/*
+ * The F-statistic proposal density of segment seg; replaces
+ * build_fstatistic_proposal (ucb/src/glass_ucb_proposal.c:1085-1182, declared
+ * at ucb/src/glass_ucb_proposal.h:244) on the grid of
+ * setup_fstatistic_proposal (:927-943): n_f cells of one bin in frequency
+ * (n_f = (int)((fmax - fmin) T), NFFT or NFFT - 1), n_theta in cos(theta),
+ * n_phi in phi (the reference uses 20 x 20).  Each cell is evaluated at its
+ * centre with fdot = 0 and, where that gives logL > 1, along the chirp-mass
+ * scan Mc = 0.1, 0.2, ... up to its first logL < 1; the density is the square
+ * of the largest logL, normalised to mean 1.
+ *   tensor: HOST, at least NFFT n_theta n_phi doubles; receives [i][j][k]
+ *   info:   HOST, 4 doubles: n_f, norm, maxp (proposal->norm, ->maxp) and the
+ *           number of cells that ran the scan
+ * Synchronous.
+ */
+int glass_gpu_fstat_proposal_host(glass_gpu_ctx *ctx, int seg, int n_theta, int n_phi, double *tensor, double *info);
+
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 
