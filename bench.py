@@ -671,6 +671,118 @@ def bench_wavelet(gg, torch, dev, rank, steps, warmup, cpu, peak64):
     eng.close()
     return out
 
+FS_NTHETA, FS_NPHI = 20, 20  # sky grid of setup_fstatistic_proposal (ucb/src/glass_ucb_proposal.c:929-930)
+
+
+def fstat_flops_per_cell(N):
+    """Algorithmic work of one F-statistic cell with filters of N samples:
+    four filter waveforms (flops_per_eval each, as the reference computes four
+    ucb_waveform calls), the 4 + 10 inner products over N bins in both
+    channels (112 N) and the 4x4 solve (200)."""
+    return 4.0 * flops_per_eval(N) + 112.0 * N + 200.0
+
+
+def bench_fstat(gg, torch, dev, rank, steps, warmup, cpu, peak64):
+    """F-statistic proposal of one 1024-bin, 1-year segment at 3.2 mHz holding
+    one source (A = 3e-22) in Gaussian noise: the 1023 x 20 x 20 grid of
+    build_fstatistic_proposal.  Device figure: the grid's fdot = 0 batch with
+    the cells resident in HBM; end to end: the whole proposal through
+    glass_gpu_fstat_proposal_host (grid, chirp-mass scan of the cells with
+    logL > 1, density back in host memory)."""
+    rng = np.random.default_rng(7 + 1000 * rank)
+    NF1 = 1024
+    inj = wl.draw_source(rng, 3.2e-3, 3e-22, 1e-17)
+    f = (int(inj[0]) - NF1 // 2 + np.arange(NF1)) / T
+    C = wl.aenoise_ff(f)
+    sig = np.sqrt(C / 2.0)
+    eng = gg.Engine(dev.index or 0)
+    N0 = 2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, inj[0] / T, inj[7] / T**2, inj[1], math.exp(inj[3]), T, NF1)
+    h = gg.ucb_waveform(inj, N0, T)
+    qmin = int(inj[0]) - NF1 // 2
+    dA = sig * rng.standard_normal(NF1) + 1j * sig * rng.standard_normal(NF1)
+    dE = sig * rng.standard_normal(NF1) + 1j * sig * rng.standard_normal(NF1)
+    i0 = int(inj[0]) - N0 // 2 - qmin
+    dA[i0:i0 + N0] += h[3][0::2] + 1j * h[3][1::2]
+    dE[i0:i0 + N0] += h[4][0::2] + 1j * h[4][1::2]
+    bank = wl.SegmentBank(T=T, NFFT=NF1, qmin=np.array([qmin], np.int32), dA=dA[None], dE=dE[None],
+                          invCA=(1.0 / C)[None], invCE=(1.0 / C)[None])
+    eng.upload(bank)
+    # the grid's fdot = 0 cells (ucb/src/glass_ucb_proposal.c:1119-1134)
+    fmin = qmin / T
+    n_f = int((fmin + NF1 / T - fmin) * T)
+    d_f = n_f / float(n_f) / T
+    g = np.arange(n_f * FS_NTHETA * FS_NPHI)
+    i, j, k = g // (FS_NTHETA * FS_NPHI), (g // FS_NPHI) % FS_NTHETA, g % FS_NPHI
+    dth, dph = 2.0 / FS_NTHETA, 2 * math.pi / FS_NPHI
+    cells = np.stack([fmin + i * d_f + d_f / 2, np.zeros(g.size), np.arccos(-1.0 + j * dth + dth / 2),
+                      k * dph + dph / 2], 1)
+    n = len(cells)
+    Ns = np.array([gg.ucb_bandwidth(L_ARM, wl.FSTAR, c[0], 0.0, math.cos(c[2]), 1e-22, T, NF1) for c in cells[::397]])
+    flops_cell = float(np.mean([fstat_flops_per_cell(int(x)) for x in Ns]))
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    d_c = torch.from_numpy(cells).to(dev)
+    d_s = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_l = torch.empty(n, dtype=torch.float64, device=dev)
+    d_fp = torch.empty((n, 4), dtype=torch.float64, device=dev)
+    d_st = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            eng.fstat_device(d_s, d_c, d_l, d_fp, d_st)
+        stream.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for s_ in range(steps):
+            flush.zero_()
+            ev[s_][0].record(stream)
+            eng.fstat_device(d_s, d_c, d_l, d_fp, d_st)
+            ev[s_][1].record(stream)
+        stream.synchronize()
+    t_dev = sum(a.elapsed_time(b) for a, b in ev) / steps / 1e3
+    launches = eng.last_launch_count()
+    st = d_st.cpu().numpy()
+    eng.set_stream(None)
+    eng.fstat_proposal_host(0, FS_NTHETA, FS_NPHI)
+    t0 = time.perf_counter()
+    reps = max(2, steps // 2)
+    for _ in range(reps):
+        tensor, norm, maxp, nscan = eng.fstat_proposal_host(0, FS_NTHETA, FS_NPHI)
+    t_e2e = (time.perf_counter() - t0) / reps
+    cells_e2e = n + 10 * nscan
+    out = {"workload": f"F-statistic proposal grid (build_fstatistic_proposal): 1024-bin 1-year segment at "
+                       f"3.2 mHz, one source A=3e-22 in noise, {n_f} x {FS_NTHETA} x {FS_NPHI} cells, filters of "
+                       f"N={sorted(set(Ns.tolist()))} samples, FP64",
+           "cells_per_s": n / t_dev, "ms_per_grid": 1e3 * t_dev, "cells": n, "ok_cells": int((st == 0).sum()),
+           "launches_per_grid": launches,
+           "roofline": {"bound": "fp64", "achieved": flops_cell * n / t_dev / 1e12, "peak": peak64,
+                        "unit": "TFLOP/s", "frac": flops_cell * n / t_dev / 1e12 / peak64,
+                        "flops_per_cell": flops_cell, "peak_source": "FP64 FMA probe kernel measured in this run",
+                        "traffic": None},
+           "e2e": {"value": cells_e2e / t_e2e, "unit": "cells/s", "ms_per_proposal": 1e3 * t_e2e,
+                   "scan_cells": 10 * nscan, "norm": norm, "maxp": maxp,
+                   "h2d_bytes_per_step": n_f * 10 * 8, "d2h_bytes_per_step": n * 8 + 4}}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import Port, build_port
+
+        build_port()
+        port = Port()
+        nth = os.cpu_count() or 1
+        rA, rE = bank.interleaved()
+        sub = np.random.default_rng(3).choice(n, 4000, replace=False)
+        done, t0 = 0, time.perf_counter()
+        while True:
+            port.fstat_batch(T, NF1, bank.qmin, rA, rE, bank.invCA, np.zeros(400, np.int32),
+                             cells[sub[done % 4000:done % 4000 + 400]], nthreads=nth)
+            done += 400
+            el = time.perf_counter() - t0
+            if el > 5.0 or done >= 40000:
+                break
+        out["cpu_baseline"] = {"value": done / el, "unit": "cells/s", "cores": nth, "kind": "port",
+                               "sample": f"{done} grid cells at fdot = 0, OpenMP over cells"}
+    eng.close()
+    return out
+
 
 def run_ours(args):
     import torch
@@ -842,6 +954,8 @@ def run_ours(args):
     wdm_line = bench_wdm(gg, torch, dev, rank, max(5, args.steps // 20), args.warmup, cpu_legs and rank == 0, peaks)
     wv_line = bench_wavelet(gg, torch, dev, rank, max(5, args.steps // 30), args.warmup, cpu_legs and rank == 0,
                             peak64)
+    fs_line = bench_fstat(gg, torch, dev, rank, max(3, args.steps // 100), args.warmup, cpu_legs and rank == 0,
+                          peak64)
 
     if rank == 0:
         line = {
@@ -868,6 +982,7 @@ def run_ours(args):
             "grad_fisher": grad_line,
             "wdm": wdm_line,
             "wavelet": wv_line,
+            "fstat": fs_line,
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk,
         }

@@ -41,6 +41,11 @@ constexpr int kFsSeries = 16;  // 4 filters x (A2, A1, E2, E1)
 // inclination pi/2, and these polarisations and phases.
 __constant__ double kFsPsi[4] = {0.0, M_PI_4, 0.0, M_PI_4};
 __constant__ double kFsPhase[4] = {0.0, M_PI, 3.0 * M_PI_2, M_PI_2};
+// each phase as a quadrant k (phase = k pi/2 to the rounding of the double),
+// and k pi/2 as a double-double hi + lo
+__constant__ int kFsQuadrant[4] = {0, 2, 3, 1};
+__constant__ double kFsKPio2Hi[4] = {0.0, 1.5707963267948966, 3.141592653589793, 4.71238898038469};
+__constant__ double kFsKPio2Lo[4] = {0.0, 6.123233995736766e-17, 1.2246467991473532e-16, 1.8369701987210297e-16};
 
 struct FsCell {
   ItemF64 it;        // the cell's geometry, f0, fdot, q, amp/(2N), segment, N, imin
@@ -312,6 +317,14 @@ __global__ void __launch_bounds__(256) fs_slow_kernel(FsSlowArgs a) {
     }
     const int Nn = N;
     double2 *out = a.series + fs_bin_start(a.bin_count, b) + (long long)slot * kFsSeries * Nn + n;
+    // Filter 0 (phase 0) takes sincos of its arguments x0 = arg1 - arg2.  The
+    // other filters' arguments xf, rounded exactly as the reference rounds
+    // them, differ from x0 by their phase k pi/2 plus ~1e-10 (the rounding of
+    // w0 xi - phi0 at |w0 xi| ~ 1e6): sincos(xf) is sincos(x0) turned by the
+    // quadrant k and by eps = xf - x0 - k pi/2, taken exactly (two-sum, and
+    // k pi/2 as a double-double); |eps| < 1e-9, so cos eps = 1 and sin eps =
+    // eps to double precision.
+    double s0[6], c0[6], x0[6];
 #pragma unroll 1
     for (int f = 0; f < 4; f++) {
       double arg2[3];
@@ -322,19 +335,37 @@ __global__ void __launch_bounds__(256) fs_slow_kernel(FsSlowArgs a) {
         arg2[i] = a2;
       }
       const double DPr = c.DP[f][0], DPi = c.DP[f][1], DCr = c.DP[f][2], DCi = c.DP[f][3];
+      const int k = kFsQuadrant[f];
+      const double khi = kFsKPio2Hi[k], klo = kFsKPio2Lo[k];
       double2 d[6], cmb[4];
 #pragma unroll
       for (int q = 0; q < 6; q++) {
         const int i = ai[q];
         const double t1r = aev[i] * (dps[q] * DPr + dcs[q] * DCr);
         const double t1i = aev[i] * (dps[q] * DPi + dcs[q] * DCi);
+        const double x = arg1[q] - arg2[i];
         double s2, c2;
-        sincos(arg1[q] - arg2[i], &s2, &c2);
+        if (f == 0) {
+          sincos(x, &s2, &c2);
+          s0[q] = s2;
+          c0[q] = c2;
+          x0[q] = x;
+        } else {
+          const double dh = x - x0[q];
+          const double bb = dh - x;
+          const double dl = (x - (dh - bb)) + (-x0[q] - bb);
+          const double eps = ((dh - khi) + dl) - klo;
+          const double rs = (k & 1) ? c0[q] : s0[q];
+          const double rc = (k & 1) ? -s0[q] : c0[q];
+          const double qs = (k & 2) ? -rs : rs, qc = (k & 2) ? -rc : rc;
+          s2 = qs + qc * eps;
+          c2 = qc - qs * eps;
+        }
         d[q] = make_double2(sinc[q] * (t1r * c2 + t1i * s2), sinc[q] * (-t1r * s2 + t1i * c2));
       }
       ae_combos(d, cmb);
 #pragma unroll
-      for (int k = 0; k < 4; k++) out[(size_t)(4 * f + k) * Nn] = cmb[k];
+      for (int kk = 0; kk < 4; kk++) out[(size_t)(4 * f + kk) * Nn] = cmb[kk];
     }
   }
 }
