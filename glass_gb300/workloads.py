@@ -154,3 +154,36 @@ def wavelet_invC(N, NT, kmin, scale=1.0):
     base = np.full((3, 3), -0.45) + np.eye(3) * 1.45
     inv = np.linalg.inv(base)
     return np.ascontiguousarray(inv[:, :, None] / s[None, None, :])
+
+
+# Noise-model defaults of the noise module (noise/src/glass_noise_model.c:1378-1458):
+# link levels and the galactic foreground for a one-year observation.
+NOISE_SACC0 = 5.76e-30
+NOISE_SOMS0 = 1.28e-22
+
+
+def default_noise_params(T=T_YEAR):
+    """(inst [12], sgal [5]) at the noise module's starting point."""
+    inst = np.array([NOISE_SACC0] * 6 + [NOISE_SOMS0] * 6)
+    f1 = 10.0 ** (-2.235e-1 * math.log10(T / 3.15581497632e7) - 2.7040844)
+    fk = 10.0 ** (-3.60976122e-1 * math.log10(T / 3.15581497632e7) - 2.37822436)
+    sgal = np.array([math.log(1.2826e-44), math.log(f1), 1.629667, math.log(fk), math.log(4.810781e-4)])
+    return inst, sgal
+
+
+def xyz_from_covariance(rng, C6):
+    """Complex XYZ bins with E[x x^H] = C for real symmetric per-bin C given as
+    [N, 6] = xx, yy, zz, xy, xz, yz; returned interleaved (3, 2N)."""
+    N = len(C6)
+    C = np.empty((N, 3, 3))
+    C[:, 0, 0], C[:, 1, 1], C[:, 2, 2] = C6[:, 0], C6[:, 1], C6[:, 2]
+    C[:, 0, 1] = C[:, 1, 0] = C6[:, 3]
+    C[:, 0, 2] = C[:, 2, 0] = C6[:, 4]
+    C[:, 1, 2] = C[:, 2, 1] = C6[:, 5]
+    L = np.linalg.cholesky(C)
+    g = (rng.standard_normal((N, 3)) + 1j * rng.standard_normal((N, 3))) * math.sqrt(0.5)
+    x = np.einsum("nij,nj->ni", L, g)
+    out = np.empty((3, 2 * N))
+    out[:, 0::2] = x.real.T
+    out[:, 1::2] = x.imag.T
+    return out

@@ -185,6 +185,32 @@ class Port:
         self.lib.orc_fstat_params(_p(np.ascontiguousarray(a, np.float64)), _p(out))
         return out
 
+    # --- noise-model likelihood (noise/src/glass_noise_model.c) -------------------
+    def noise_logl(self, T, fmin, X, Y, Z, inst, sgal=None, nthreads=0):
+        """my_noise_log_likelihood of each noise model: inst [n, 12] (sacc[6],
+        soms[6]), sgal [n, 5] or None; X, Y, Z interleaved (2 NFFT)."""
+        lib = self.lib
+        lib.orc_noise_logl_batch.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _D, _D, _D,
+                                             ctypes.c_int, _D, _D, _D, ctypes.c_int]
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        out = np.zeros(len(inst))
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        lib.orc_noise_logl_batch(T, fmin, len(X) // 2, _p(X), _p(Y), _p(Z), len(inst), _p(inst),
+                                 _p(sg) if sg is not None else None, _p(out), nthreads)
+        return out
+
+    def noise_covariance(self, T, fmin, N, inst, sgal=None):
+        """[N, 6] covariance entries xx, yy, zz, xy, xz, yz of one noise model."""
+        lib = self.lib
+        lib.orc_noise_covariance.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _D, _D, _D, _D]
+        inst = np.ascontiguousarray(inst, np.float64).reshape(12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(5)
+        out = np.zeros((N, 6))
+        lib.orc_noise_covariance(T, fmin, N, _p(inst[:6].copy()), _p(inst[6:].copy()),
+                                 _p(sg) if sg is not None else None, _p(out))
+        return out
+
     def orbit(self, t):
         out = np.zeros(9)
         self.lib.orc_orbit_positions(float(t), _p(out))
@@ -480,3 +506,17 @@ class Ref:
                                _p(tensor), _p(info))
         n_f = int(info[0])
         return tensor[:n_f * n_theta * n_phi].reshape(n_f, n_theta, n_phi), info[1], info[2]
+
+    def noise_logl(self, T, fmin, X, Y, Z, inst, sgal=None):
+        """The reference's instrument (+ foreground) covariance, inverse and
+        my_noise_log_likelihood for each noise model."""
+        lib = self.lib
+        lib.ref_noise_logl.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _D, _D, _D, ctypes.c_int,
+                                       _D, _D, _D]
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        out = np.zeros(len(inst))
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        lib.ref_noise_logl(T, fmin, len(X) // 2, _p(X), _p(Y), _p(Z), len(inst), _p(inst),
+                           _p(sg) if sg is not None else None, _p(out))
+        return out

@@ -12,6 +12,7 @@
  */
 #include "glass_utils.h"
 #include "glass_ucb.h"
+#include "glass_noise.h"
 
 static void setup_orbit(struct Orbit *orbit)
 {
@@ -509,4 +510,66 @@ void ref_fstat_proposal(const char *format, double T, double t0, int NFFT, int q
     for (int i = 0; i < 3; i++) free(proposal.matrix[i]);
     free(proposal.matrix);
     fstat_data_free(data);
+}
+
+/* The noise module's XYZ likelihood for n noise models on the grid
+ * f = fmin + k/T, k < NFFT (noise/src/glass_noise_model.c:1378-1403 for the
+ * grid): generate_instrument_noise_model (:389), optionally
+ * generate_galactic_foreground_model (:612) added by
+ * generate_full_covariance_matrix (:894), invert_noise_covariance_matrix
+ * (utils/src/glass_math.c:240) and my_noise_log_likelihood
+ * (noise/src/glass_noise_model.c:1243), as noise_instrument_model_mcmc
+ * combines them (noise/src/glass_noise_sampler.c:555-572).
+ * inst[12 p ..] = sacc[6], soms[6]; sgal[5 p ..] or NULL. */
+void ref_noise_logl(double T, double fmin, int NFFT, const double *X, const double *Y, const double *Z, int n,
+                    const double *inst, const double *sgal, double *logl)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->NFFT = NFFT;
+    data->N = 2 * NFFT;
+    data->Nchannel = 3;
+    data->Nlayer = 1;
+    data->T = T;
+    data->fmin = fmin;
+    strcpy(data->basis, "fourier");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, 3);
+    memcpy(data->tdi->X, X, sizeof(double) * data->N);
+    memcpy(data->tdi->Y, Y, sizeof(double) * data->N);
+    memcpy(data->tdi->Z, Z, sizeof(double) * data->N);
+    struct InstrumentModel inst_model;
+    memset(&inst_model, 0, sizeof(inst_model));
+    alloc_instrument_model(&inst_model, NFFT, 1, 3);
+    for (int k = 0; k < NFFT; k++) inst_model.psd->f[k] = data->fmin + (double)k / data->T;
+    struct ForegroundModel gal;
+    memset(&gal, 0, sizeof(gal));
+    alloc_foreground_model(&gal, NFFT, 1, 3);
+    for (int k = 0; k < NFFT; k++) gal.psd->f[k] = data->fmin + (double)k / data->T;
+    struct Noise *psd = malloc(sizeof(struct Noise));
+    alloc_noise(psd, NFFT, 1, 3);
+    for (int p = 0; p < n; p++) {
+        for (int l = 0; l < 6; l++) {
+            inst_model.sacc[l] = inst[12 * p + l];
+            inst_model.soms[l] = inst[12 * p + 6 + l];
+        }
+        generate_instrument_noise_model(&orbit, &inst_model);
+        copy_Cij(inst_model.psd->C, psd->C, psd->Nchannel, psd->N);
+        if (sgal) {
+            for (int q = 0; q < 5; q++) gal.sgal[q] = sgal[5 * p + q];
+            generate_galactic_foreground_model(&gal);
+            generate_full_covariance_matrix(psd, gal.psd, 3);
+        }
+        invert_noise_covariance_matrix(psd);
+        logl[p] = my_noise_log_likelihood(data, psd);
+    }
+    free_noise(psd);
+    free_noise(inst_model.psd);
+    free(inst_model.sacc);
+    free(inst_model.soms);
+    free_noise(gal.psd);
+    free(gal.sgal);
+    free_tdi(data->tdi);
+    free(data);
 }

@@ -17,13 +17,18 @@ utils/src/glass_model.c:726), snr (utils/src/glass_math.c:403) and ucb_fisher
 gaussian_log_likelhood_wavelet (utils/src/glass_model.c:624, :805) and
 snr_wavelet (utils/src/glass_math.c:428), get_Fstat_logL
 (ucb/src/glass_ucb_fstatistic.c:646) and build_fstatistic_proposal
-(ucb/src/glass_ucb_proposal.c:1085).  Inputs are seeded numpy draws.
+(ucb/src/glass_ucb_proposal.c:1085), and the noise module's
+generate_instrument_noise_model, generate_galactic_foreground_model,
+invert_noise_covariance_matrix and my_noise_log_likelihood
+(noise/src/glass_noise_model.c:389, :612, utils/src/glass_math.c:240,
+noise/src/glass_noise_model.c:1243).  Inputs are seeded numpy draws.
 
     python tests/golden/make_golden.py            # every fixture
-    python tests/golden/make_golden.py fstat      # only the named ones
+    python tests/golden/make_golden.py fstat noise   # only the named ones
 """
 from __future__ import annotations
 
+import math
 import os
 import sys
 
@@ -296,7 +301,34 @@ def fstat(ref, rng):
     np.savez_compressed(os.path.join(HERE, "fstat.npz"), ncase=len(cases), **out)
 
 
-OWN_SEEDS = {"fstat": 20261204}
+def noise(ref, rng):
+    """The noise module's XYZ likelihood (instrument covariance, optionally
+    plus the galactic foreground, inverse, my_noise_log_likelihood) for noise
+    models around the starting point, on 1024-bin grids at 0.1 mHz, at 2 mHz
+    (where the foreground dominates), across the acceleration-noise cutoff
+    (10 mHz) and across the foreground's high-frequency cutoff (~20 mHz); data
+    drawn from the starting point's covariance."""
+    from oracle import Port
+
+    port = Port()
+    NF = 1024
+    inst0, sgal0 = wl.default_noise_params(T)
+    out = {}
+    starts = [int(1e-4 * T), int(2e-3 * T), int(1e-2 * T) - 500, int(10 * math.exp(sgal0[1]) * T) - 500]
+    for c, q in enumerate(starts):
+        fmin = q / T
+        X, Y, Z = wl.xyz_from_covariance(rng, port.noise_covariance(T, fmin, NF, inst0, sgal0))
+        inst = inst0 * np.exp(rng.uniform(-0.3, 0.3, (12, 12)))
+        sgal = sgal0 + rng.uniform(-0.2, 0.2, (12, 5))
+        out[f"c{c}_qmin"] = q
+        out[f"c{c}_X"], out[f"c{c}_Y"], out[f"c{c}_Z"] = X, Y, Z
+        out[f"c{c}_inst"], out[f"c{c}_sgal"] = inst, sgal
+        out[f"c{c}_logl_inst"] = ref.noise_logl(T, fmin, X, Y, Z, inst)
+        out[f"c{c}_logl_gal"] = ref.noise_logl(T, fmin, X, Y, Z, inst, sgal)
+    np.savez_compressed(os.path.join(HERE, "noise.npz"), ncase=len(starts), NFFT=NF, **out)
+
+
+OWN_SEEDS = {"fstat": 20261204, "noise": 20261205}
 
 
 def main(names=()):
@@ -314,6 +346,7 @@ def main(names=()):
     wavelet_waveforms(ref, rng)
     wavelet_likelihood(ref, rng)
     fstat(ref, np.random.default_rng(OWN_SEEDS["fstat"]))
+    noise(ref, np.random.default_rng(OWN_SEEDS["noise"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -239,3 +239,18 @@ def test_invert4_against_numpy(port):
         a = rng.standard_normal((4, 4))
         m = a @ a.T + 0.1 * np.eye(4)
         np.testing.assert_allclose(port.invert4(m), np.linalg.inv(m), rtol=1e-9, atol=1e-12)
+
+
+# ---------------------------------------------------------- noise likelihood
+def test_noise_likelihood_matches_reference(port, golden):
+    """The noise module's XYZ likelihood (noise/src/glass_noise_model.c:389,
+    :612, :1243; utils/src/glass_math.c:240): instrument only and with the
+    galactic foreground, in four frequency bands."""
+    g = golden("noise.npz")
+    for c in range(int(g["ncase"])):
+        fmin = int(g[f"c{c}_qmin"]) / T
+        X, Y, Z = g[f"c{c}_X"], g[f"c{c}_Y"], g[f"c{c}_Z"]
+        got = port.noise_logl(T, fmin, X, Y, Z, g[f"c{c}_inst"])
+        np.testing.assert_allclose(got, g[f"c{c}_logl_inst"], rtol=1e-13)
+        got = port.noise_logl(T, fmin, X, Y, Z, g[f"c{c}_inst"], g[f"c{c}_sgal"])
+        np.testing.assert_allclose(got, g[f"c{c}_logl_gal"], rtol=1e-13)
