@@ -784,6 +784,95 @@ def bench_fstat(gg, torch, dev, rank, steps, warmup, cpu, peak64):
     return out
 
 
+NOISE_NF, NOISE_NPROP = 15360, 1024  # apps/src/noise_likelihood_benchmarks.c:25 grid; one batch of models
+
+
+def noise_flops_per_bin(foreground):
+    """Algorithmic work of one noise model on one bin, transcendentals counted
+    as 20 flops: instrument covariance (60), foreground (20 + exp, pow, tanh:
+    80), inverse and log-determinant (4 divisions, 3 logs, 1/det and the six
+    cofactors: 140), likelihood terms (25)."""
+    return 60.0 + (100.0 if foreground else 0.0) + 140.0 + 25.0
+
+
+def bench_noise(gg, torch, dev, rank, steps, warmup, cpu, peak64):
+    """Noise-model likelihood of the noise module's sampler on the reference
+    benchmark's grid: 15360 XYZ bins from 0.1 mHz of one year, data drawn from
+    the starting model's covariance, a batch of 1024 noise models (instrument
+    levels and galactic foreground around the starting point), FP64."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Port, build_port
+
+    build_port()
+    port = Port()
+    rng = np.random.default_rng(9 + 1000 * rank)
+    q = int(1e-4 * T)
+    inst0, sgal0 = wl.default_noise_params(T)
+    X, Y, Z = wl.xyz_from_covariance(rng, port.noise_covariance(T, q / T, NOISE_NF, inst0, sgal0))
+    inst = inst0 * np.exp(rng.uniform(-0.3, 0.3, (NOISE_NPROP, 12)))
+    sgal = sgal0 + rng.uniform(-0.2, 0.2, (NOISE_NPROP, 5))
+    eng = gg.Engine(dev.index or 0)
+    eng.noise_setup(T, q, X, Y, Z)
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    d_i = torch.from_numpy(inst).to(dev)
+    d_g = torch.from_numpy(sgal).to(dev)
+    d_l = torch.empty(NOISE_NPROP, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    out = {}
+    for name, g in (("instrument+foreground", d_g), ("instrument", None)):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                eng.noise_logl_device(d_i, d_l, g)
+            stream.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            for k in range(steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                eng.noise_logl_device(d_i, d_l, g)
+                ev[k][1].record(stream)
+            stream.synchronize()
+        t = sum(a.elapsed_time(b) for a, b in ev) / steps / 1e3
+        fl = noise_flops_per_bin(g is not None) * NOISE_NF * NOISE_NPROP
+        out[name] = {"models_per_s": NOISE_NPROP / t, "ms_per_batch": 1e3 * t,
+                     "roofline": {"bound": "fp64", "achieved": fl / t / 1e12, "peak": peak64, "unit": "TFLOP/s",
+                                  "frac": fl / t / 1e12 / peak64, "flops_per_model_bin": fl / NOISE_NF / NOISE_NPROP,
+                                  "peak_source": "FP64 FMA probe kernel measured in this run", "traffic": None}}
+    launches = eng.last_launch_count()
+    eng.set_stream(None)
+    for _ in range(warmup):
+        eng.noise_logl_host(inst, sgal)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        host = eng.noise_logl_host(inst, sgal)
+    t_e2e = (time.perf_counter() - t0) / steps
+    res = {"workload": f"noise-model logL (instrument + galactic foreground, XYZ), {NOISE_NF} bins from 0.1 mHz, "
+                       f"{NOISE_NPROP} models per batch, FP64",
+           "models_per_s": out["instrument+foreground"]["models_per_s"],
+           "ms_per_batch": out["instrument+foreground"]["ms_per_batch"],
+           "roofline": out["instrument+foreground"]["roofline"],
+           "instrument_only": out["instrument"], "launches_per_batch": launches,
+           "e2e": {"value": NOISE_NPROP / t_e2e, "unit": "models/s", "h2d_bytes_per_step": NOISE_NPROP * 17 * 8,
+                   "d2h_bytes_per_step": NOISE_NPROP * 8}}
+    if cpu:
+        nth = os.cpu_count() or 1
+        done, t0 = 0, time.perf_counter()
+        while True:
+            k = done % NOISE_NPROP
+            ref = port.noise_logl(T, q / T, X, Y, Z, inst[k:k + 64], sgal[k:k + 64], nthreads=nth)
+            done += 64
+            el = time.perf_counter() - t0
+            if el > 5.0 or done >= NOISE_NPROP:
+                break
+        res["cpu_baseline"] = {"value": done / el, "unit": "models/s", "cores": nth, "kind": "port",
+                               "sample": f"{done} models of the same batch, OpenMP over models"}
+        res["max_rel_err_vs_oracle"] = float(np.max(np.abs(host[:64] - port.noise_logl(T, q / T, X, Y, Z, inst[:64],
+                                                                                         sgal[:64], nthreads=nth))
+                                                    / np.abs(host[:64])))
+    eng.close()
+    return res
+
+
 def run_ours(args):
     import torch
 
@@ -956,6 +1045,8 @@ def run_ours(args):
                             peak64)
     fs_line = bench_fstat(gg, torch, dev, rank, max(3, args.steps // 100), args.warmup, cpu_legs and rank == 0,
                           peak64)
+    noise_line = bench_noise(gg, torch, dev, rank, max(5, args.steps // 30), args.warmup, cpu_legs and rank == 0,
+                             peak64)
 
     if rank == 0:
         line = {
@@ -983,6 +1074,7 @@ def run_ours(args):
             "wdm": wdm_line,
             "wavelet": wv_line,
             "fstat": fs_line,
+            "noise": noise_line,
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk,
         }

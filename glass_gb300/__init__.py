@@ -45,6 +45,7 @@ EXPORTS = (
     "ucb_waveform_wavelet_slow", "glass_ucb_waveform_wavelet_tab", "glass_ucb_waveform_wavelet_slow",
     "glass_gpu_wavelet_fisher_batch", "glass_gpu_wavelet_fisher_batch_host",
     "glass_gpu_fstat_batch", "glass_gpu_fstat_batch_host", "glass_gpu_fstat_proposal_host",
+    "glass_gpu_noise_setup", "glass_gpu_noise_logl_batch", "glass_gpu_noise_logl_batch_host",
 )
 
 _lib = None
@@ -107,6 +108,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_fstat_batch.argtypes = [_V, ctypes.c_int, _V, _V, _V, _V, _V]
     lib.glass_gpu_fstat_batch_host.argtypes = [_V, ctypes.c_int, _I, _D, _D, _D, _I]
     lib.glass_gpu_fstat_proposal_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D]
+    lib.glass_gpu_noise_setup.argtypes = [_V, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _D, _D]
+    lib.glass_gpu_noise_logl_batch.argtypes = [_V, ctypes.c_int, _V, _V, _V]
+    lib.glass_gpu_noise_logl_batch_host.argtypes = [_V, ctypes.c_int, _D, _D, _D]
     _lib = lib
     return lib
 
@@ -387,6 +391,25 @@ class Engine:
                                                       _pd(info)))
         n_f = int(info[0])
         return tensor[:n_f * n_theta * n_phi].reshape(n_f, n_theta, n_phi), info[1], info[2], int(info[3])
+
+    def noise_setup(self, T, qmin, X, Y, Z):
+        """XYZ data (interleaved, 2 NFFT each) on the bins qmin/T + n/T."""
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        _check(self.lib.glass_gpu_noise_setup(self._ctx, float(T), int(qmin), len(X) // 2, _pd(X), _pd(Y), _pd(Z)))
+
+    def noise_logl_host(self, inst, sgal=None):
+        """my_noise_log_likelihood of each noise model: inst [n, 12], sgal [n, 5] or None."""
+        i = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        g = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        out = np.empty(len(i))
+        _check(self.lib.glass_gpu_noise_logl_batch_host(self._ctx, len(i), _pd(i), _pd(g) if g is not None else None,
+                                                        _pd(out)))
+        return out
+
+    def noise_logl_device(self, inst, logl, sgal=None):
+        """Device tensors: inst [n, 12], sgal [n, 5] or None, logl [n]; asynchronous."""
+        n = int(inst.shape[0])
+        _check(self.lib.glass_gpu_noise_logl_batch(self._ctx, n, _ptr(inst), _ptr(sgal), _ptr(logl)))
 
     def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                              precision=PREC_FP64):

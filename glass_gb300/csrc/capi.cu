@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/glass_gb300.h"
+#include "noise.cuh"
 #include "ucb_fd.cuh"
 #include "ucb_fd_device.cuh"
 #include "ucb_wavelet.cuh"
@@ -79,6 +80,7 @@ struct glass_gpu_ctx {
   void *wv_work_mem = nullptr;
   void *wv_fisher_mem = nullptr;  // perturbed parameters of the Fisher batches
   FsWorkDev fsw;  // F-statistic scratch
+  NoiseDev noise;  // noise-model likelihood: per-bin table and chunk sums
 };
 
 static void clear_host_graphs(glass_gpu_ctx *ctx) {
@@ -146,6 +148,8 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->wv_work_mem);
   cudaFree(ctx->wv_fisher_mem);
   fs_work_free(ctx->fsw);
+  cudaFree(ctx->noise.tab);
+  cudaFree(ctx->noise.partial);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
@@ -721,6 +725,79 @@ extern "C" int glass_gpu_fstat_proposal_host(glass_gpu_ctx *ctx, int seg, int n_
   info[1] = norm;
   info[2] = maxp;
   info[3] = nact;
+  return GLASS_OK;
+}
+
+// ------------------------------------------------------- noise likelihood
+extern "C" int glass_gpu_noise_setup(glass_gpu_ctx *ctx, double T, int qmin, int NFFT, const double *X,
+                                     const double *Y, const double *Z) {
+  if (!ctx || !X || !Y || !Z) return set_err(GLASS_ERR_ARG, "noise_setup: null argument");
+  if (!(T > 0) || NFFT < 1 || qmin < 1) return set_err(GLASS_ERR_ARG, "noise_setup: bad grid (T > 0, NFFT >= 1, qmin >= 1)");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const double fmin = (double)qmin / T;  // floor(fmin T)/T (utils/src/glass_data.c:2065)
+  std::vector<double> tab((size_t)kNoiseTabRows * NFFT);
+  noise_build_table(T, fmin, NFFT, X, Y, Z, tab.data());
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "noise_setup sync");
+  NoiseDev &nd = ctx->noise;
+  cudaFree(nd.tab);
+  nd.tab = nullptr;
+  GLASS_CUDA(cudaMalloc(&nd.tab, sizeof(double) * tab.size()), "cudaMalloc(noise table)");
+  GLASS_CUDA(cudaMemcpy(nd.tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice), "upload noise table");
+  nd.N = NFFT;
+  nd.T = T;
+  nd.fmin = fmin;
+  cudaFree(nd.partial);
+  nd.partial = nullptr;
+  nd.partial_models = 0;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                          double *logl) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_logl_batch: null context");
+  if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_logl_batch: negative model count");
+  if (nprop == 0) return GLASS_OK;
+  if (!inst || !logl) return set_err(GLASS_ERR_ARG, "noise_logl_batch: null argument");
+  NoiseDev &nd = ctx->noise;
+  if (!nd.tab) return set_err(GLASS_ERR_STATE, "noise_logl_batch: no data set (glass_gpu_noise_setup)");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if (nprop > nd.partial_models) {
+    int want = nd.partial_models > 0 ? nd.partial_models : 64;
+    while (want < nprop) want *= 2;
+    GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "noise partial sync");
+    cudaFree(nd.partial);
+    nd.partial = nullptr;
+    nd.partial_models = 0;
+    GLASS_CUDA(cudaMalloc(&nd.partial, sizeof(double) * (size_t)want * noise_chunks(nd.N)), "cudaMalloc(noise partial)");
+    nd.partial_models = want;
+  }
+  int nl = 0;
+  cudaError_t e = noise_logl_launch(nd, nprop, inst, sgal, logl, ctx->stream, &nl);
+  ctx->last_launches = nl;
+  if (e != cudaSuccess) return cuda_err(e, "noise_logl_batch launch");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                               double *logl) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_logl_batch_host: null context");
+  if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_logl_batch_host: negative model count");
+  if (nprop == 0) return GLASS_OK;
+  if (!inst || !logl) return set_err(GLASS_ERR_ARG, "noise_logl_batch_host: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t nd = (size_t)nprop;
+  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (12 + 5 + 1) + 256))) return rc;
+  double *d_inst = (double *)ctx->d_stage, *d_sgal = d_inst + 12 * nd, *d_logl = d_sgal + 5 * nd;
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d_inst, inst, sizeof(double) * 12 * nd, cudaMemcpyHostToDevice, s), "H2D inst");
+  if (sgal) GLASS_CUDA(cudaMemcpyAsync(d_sgal, sgal, sizeof(double) * 5 * nd, cudaMemcpyHostToDevice, s), "H2D sgal");
+  rc = glass_gpu_noise_logl_batch(ctx, nprop, d_inst, sgal ? d_sgal : nullptr, d_logl);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(logl, d_logl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
+  GLASS_CUDA(cudaStreamSynchronize(s), "noise_logl_batch_host sync");
   return GLASS_OK;
 }
 

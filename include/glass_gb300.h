@@ -214,6 +214,27 @@ int glass_gpu_fstat_batch_host(glass_gpu_ctx *ctx, int ncells, const int *cell_s
  */
 int glass_gpu_fstat_proposal_host(glass_gpu_ctx *ctx, int seg, int n_theta, int n_phi, double *tensor, double *info);
 
+/*
+ * Noise-model likelihood of XYZ frequency-domain data (the noise module's
+ * sampler, noise/src/glass_noise_sampler.c:395-752).  glass_gpu_noise_setup
+ * takes the data (X, Y, Z: 2 NFFT doubles each, re/im) on the bins
+ * f = qmin/T + n/T, n < NFFT.  glass_gpu_noise_logl_batch then gives, for each
+ * noise model p,
+ *   logl[p] = my_noise_log_likelihood (noise/src/glass_noise_model.c:1243)
+ * of the covariance generate_instrument_noise_model (:389, three channels)
+ * builds from inst[12 p ..] = sacc[6], soms[6] (the reference's link order
+ * 12, 21, 23, 32, 13, 31), plus, when sgal is not NULL, the galactic foreground
+ * generate_galactic_foreground_model (:612) builds from sgal[5 p ..] =
+ * ln A, ln f1, alpha, ln fk, ln f2, inverted as invert_noise_covariance_matrix
+ * does (utils/src/glass_math.c:240).  FP64.  Device pointers; asynchronous.
+ * The _host form takes host pointers and synchronises.
+ */
+int glass_gpu_noise_setup(glass_gpu_ctx *ctx, double T, int qmin, int NFFT, const double *X, const double *Y,
+                          const double *Z);
+int glass_gpu_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal, double *logl);
+int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                    double *logl);
+
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 
