@@ -187,3 +187,27 @@ def xyz_from_covariance(rng, C6):
     out[:, 0::2] = x.real.T
     out[:, 1::2] = x.imag.T
     return out
+
+
+def wavelet_noise_data(rng, C6_layers, NT):
+    """Real wavelet coefficients X, Y, Z (pixel i of layer j at i + j NT) drawn
+    per layer with covariance C6_layers [Nlayer, 6] (xx, yy, zz, xy, xz, yz)."""
+    Nl = len(C6_layers)
+    C = np.empty((Nl, 3, 3))
+    C[:, 0, 0], C[:, 1, 1], C[:, 2, 2] = C6_layers[:, 0], C6_layers[:, 1], C6_layers[:, 2]
+    C[:, 0, 1] = C[:, 1, 0] = C6_layers[:, 3]
+    C[:, 0, 2] = C[:, 2, 0] = C6_layers[:, 4]
+    C[:, 1, 2] = C[:, 2, 1] = C6_layers[:, 5]
+    L = np.linalg.cholesky(C)
+    x = np.einsum("jab,jbi->aji", L, rng.standard_normal((Nl, 3, NT)))
+    return x.reshape(3, Nl * NT)
+
+
+def galaxy_modulation_like(Ncoarse, phase=0.0):
+    """A smooth modulation cache (6, Ncoarse) with the structure of
+    galaxy_modulation_cache_for_Q's output (XX, YY, ZZ, XY, XZ, YZ): yearly
+    variation of the three auto terms, cross terms -0.45 sqrt(auto auto), so
+    that the modulated foreground stays a covariance."""
+    q = np.arange(Ncoarse)
+    a = [1.0 + 0.3 * np.cos(2 * np.pi * q / Ncoarse + phase + 2.1 * k) for k in range(3)]
+    return np.stack(a + [-0.45 * np.sqrt(a[0] * a[1]), -0.45 * np.sqrt(a[0] * a[2]), -0.45 * np.sqrt(a[1] * a[2])])

@@ -197,3 +197,149 @@ void orc_noise_covariance(double T, double fmin, int N, const double *sacc, cons
         o[0] = C[0][0]; o[1] = C[1][1]; o[2] = C[2][2]; o[3] = C[0][1]; o[4] = C[0][2]; o[5] = C[1][2];
     }
 }
+
+/* ------------------------------------------------------ wavelet domain */
+
+/* invert_noise_covariance_matrix's three-channel branch
+ * (utils/src/glass_math.c:259-286): inverse entries ixx, iyy, izz, ixy, ixz,
+ * iyz and the log-determinant. */
+static void orc_invert3(const double *c6, double *i6, double *logdet)
+{
+    double cxx = c6[0], cyy = c6[1], czz = c6[2], cxy = c6[3], cxz = c6[4], cyz = c6[5];
+    double d1 = cxx;
+    double d2 = cyy - cxy * cxy / d1;
+    double tt = cyz - cxy * cxz / d1;
+    double d3 = (czz - cxz * cxz / d1) - (tt * tt) / d2;
+    double ld = log(d1) + log(d2) + log(d3);
+#define ORC_SLD(num) copysign(exp(log(fabs(num)) - ld), (num))
+    i6[0] = ORC_SLD(cyy * czz - cyz * cyz);
+    i6[1] = ORC_SLD(czz * cxx - cxz * cxz);
+    i6[2] = ORC_SLD(cxx * cyy - cxy * cxy);
+    i6[3] = ORC_SLD(cxz * cyz - czz * cxy);
+    i6[4] = ORC_SLD(cxy * cyz - cxz * cyy);
+    i6[5] = ORC_SLD(cxy * cxz - cxx * cyz);
+#undef ORC_SLD
+    *logdet = ld;
+}
+
+/*
+ * The noise module's coarse-grained wavelet-domain likelihood for one noise
+ * model (noise/src/glass_noise_model.c:1211-1241), on layers lmin ..
+ * lmin + Nlayer - 1 of an NF x NT grid (layer width df) coarsened by Q in
+ * time:
+ *  - instrument variance per layer: the Fourier model at the layer centre
+ *    (lmin + k) df over ND = NF NT (generate_instrument_noise_model_wavelet,
+ *    :561-610);
+ *  - mode 1 (stationary foreground): the foreground at the layer centre with
+ *    the off-diagonals' -1/2 undone, over ND (generate_galactic_foreground_
+ *    model_wavelet :656-722), added as generate_full_stationary_covariance_
+ *    matrix_coarse does (:983-1029: diagonal +, off-diagonal - 1/2);
+ *  - mode 2 (modulated foreground): the same foreground times the modulation
+ *    of coarse cell q, mod[6 Ncoarse] = XX, YY, ZZ, XY, XZ, YZ, entry by entry
+ *    (generate_full_dynamic_covariance_matrix_coarse :923-981);
+ *  - mode 0: instrument only;
+ *  - inverse per pixel, and the per-pixel Wishart sum with the cells'
+ *    sample (cross-)covariances P[6][Nlayer Ncoarse] (coarse_grain_wavelet_data
+ *    :1057-1102, cell k = q + j Ncoarse), minus 3/2 Nlayer NT log 2 pi.
+ * inst: sacc[6], soms[6]; sgal: 5 (unused in mode 0).
+ */
+double orc_noise_wavelet_logl(int NF, int NT, double df, int lmin, int Nlayer, int Q, const double *P, int mode,
+                              const double *mod, const double *inst, const double *sgal)
+{
+    const int Ncoarse = NT / Q;
+    const double inv_ND = 1.0 / (double)(NF * NT);
+    const double log2pi = log(2 * M_PI);
+    double Amp = 0, f1 = 0, alpha = 0, fk = 0, f2 = 0;
+    if (mode) {
+        Amp = exp(sgal[0]);
+        f1 = exp(sgal[1]);
+        alpha = sgal[2];
+        fk = exp(sgal[3]);
+        f2 = exp(sgal[4]);
+    }
+    const size_t Npix = (size_t)Nlayer * Ncoarse;
+    const double *Pxx = P, *Pyy = P + Npix, *Pzz = P + 2 * Npix, *Pxy = P + 3 * Npix, *Pxz = P + 4 * Npix,
+                 *Pyz = P + 5 * Npix;
+    const double Qd = (double)Q;
+    double logL = 0.0;
+    for (int j = 0; j < Nlayer; j++) {
+        const double f = (double)(lmin + j) * df;
+        double Ci[3][3], Cg[3][3];
+        orc_noise_cov_bin(f, inst, inst + 6, 0, 0, 0, 0, 0, 0, Ci);
+        double inst6[6] = {Ci[0][0] * inv_ND, Ci[1][1] * inv_ND, Ci[2][2] * inv_ND,
+                           Ci[0][1] * inv_ND, Ci[0][2] * inv_ND, Ci[1][2] * inv_ND};
+        double conf6[6] = {0, 0, 0, 0, 0, 0};
+        if (mode) {
+            /* the foreground of generate_galactic_foreground_model alone */
+            double fs = ORC_CLIGHT / (ORC_PI2 * ORC_LARM);
+            double xg = f / fs;
+            double t = 4. * xg * xg * sin(xg) * sin(xg);
+            double Sgal = (f > f1 * 10) ? 0.0 : orc_galaxy_foreground(f, Amp, f1, alpha, fk, f2);
+            memset(Cg, 0, sizeof(Cg));
+            double dg = t * Sgal / 4.0, og = -0.5 * t * Sgal / 4.0;
+            if (lmin + j == 0) dg = og = 0.0;
+            og *= -2.0;
+            conf6[0] = conf6[1] = conf6[2] = dg * inv_ND;
+            conf6[3] = conf6[4] = conf6[5] = og * inv_ND;
+        }
+        for (int q = 0; q < Ncoarse; q++) {
+            double c6[6], i6[6], ld;
+            for (int e = 0; e < 6; e++) c6[e] = inst6[e];
+            if (mode == 1) {
+                c6[0] += conf6[0]; c6[1] += conf6[1]; c6[2] += conf6[2];
+                c6[3] -= conf6[3] / 2.; c6[4] -= conf6[4] / 2.; c6[5] -= conf6[5] / 2.;
+            } else if (mode == 2) {
+                for (int e = 0; e < 6; e++) c6[e] += conf6[e] * mod[(size_t)e * Ncoarse + q];
+            }
+            orc_invert3(c6, i6, &ld);
+            size_t k = (size_t)q + (size_t)j * Ncoarse;
+            double s = 0.0;
+            s -= 0.5 * Qd * i6[0] * Pxx[k];
+            s -= 0.5 * Qd * i6[1] * Pyy[k];
+            s -= 0.5 * Qd * i6[2] * Pzz[k];
+            s -= Qd * i6[3] * Pxy[k];
+            s -= Qd * i6[4] * Pxz[k];
+            s -= Qd * i6[5] * Pyz[k];
+            s -= 0.5 * Qd * ld;
+            logL += s;
+        }
+    }
+    logL -= 0.5 * 3 * (Nlayer * NT) * log2pi;
+    return logL;
+}
+
+/* The cells' sample (cross-)covariances of wavelet data on Nlayer layers
+ * (coarse_grain_wavelet_data, noise/src/glass_noise_model.c:1057-1102):
+ * X, Y, Z hold pixel i of layer j at i + j NT; P as above. */
+void orc_noise_coarse_stats(int NT, int Nlayer, int Q, const double *X, const double *Y, const double *Z, double *P)
+{
+    const int Ncoarse = NT / Q;
+    const size_t Npix = (size_t)Nlayer * Ncoarse;
+    double invQ = 1.0 / (double)Q;
+    for (int j = 0; j < Nlayer; j++)
+        for (int q = 0; q < Ncoarse; q++) {
+            double sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
+            for (int i = q * Q; i < (q + 1) * Q; i++) {
+                size_t k = (size_t)i + (size_t)j * NT;
+                double wx = X[k], wy = Y[k], wz = Z[k];
+                sxx += wx * wx; syy += wy * wy; szz += wz * wz;
+                sxy += wx * wy; sxz += wx * wz; syz += wy * wz;
+            }
+            size_t kc = (size_t)q + (size_t)j * Ncoarse;
+            P[kc] = sxx * invQ; P[Npix + kc] = syy * invQ; P[2 * Npix + kc] = szz * invQ;
+            P[3 * Npix + kc] = sxy * invQ; P[4 * Npix + kc] = sxz * invQ; P[5 * Npix + kc] = syz * invQ;
+        }
+}
+
+void orc_noise_wavelet_logl_batch(int NF, int NT, double df, int lmin, int Nlayer, int Q, const double *P, int mode,
+                                  const double *mod, int nprop, const double *inst, const double *sgal, double *logl,
+                                  int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int p = 0; p < nprop; p++)
+        logl[p] = orc_noise_wavelet_logl(NF, NT, df, lmin, Nlayer, Q, P, mode, mod, inst + 12 * (size_t)p,
+                                         sgal ? sgal + 5 * (size_t)p : NULL);
+}

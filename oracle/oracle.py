@@ -211,6 +211,34 @@ class Port:
                                  _p(sg) if sg is not None else None, _p(out))
         return out
 
+    def noise_wavelet_logl(self, NF, NT, df, lmin, P, Q, inst, sgal=None, mode=0, mod=None, nthreads=0):
+        """my_noise_log_likelihood_wavelet_coarse of each noise model: P [6, Nlayer, NT/Q]
+        cell statistics, mode 0 instrument / 1 stationary foreground / 2 modulated
+        (mod [6, NT/Q])."""
+        lib = self.lib
+        lib.orc_noise_wavelet_logl_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                     ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, _D, ctypes.c_int,
+                                                     _D, _D, _D, ctypes.c_int]
+        P = np.ascontiguousarray(P, np.float64)
+        Nlayer = P.shape[1]
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        md = None if mod is None else np.ascontiguousarray(mod, np.float64)
+        out = np.zeros(len(inst))
+        lib.orc_noise_wavelet_logl_batch(NF, NT, df, lmin, Nlayer, Q, _p(P), mode, _p(md) if md is not None else None,
+                                         len(inst), _p(inst), _p(sg) if sg is not None else None, _p(out), nthreads)
+        return out
+
+    def noise_coarse_stats(self, NT, Q, X, Y, Z):
+        """[6, Nlayer, NT/Q] cell statistics of wavelet data [Nlayer NT] (coarse_grain_wavelet_data)."""
+        lib = self.lib
+        lib.orc_noise_coarse_stats.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]
+        Nlayer = len(X) // NT
+        P = np.zeros((6, Nlayer, NT // Q))
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        lib.orc_noise_coarse_stats(NT, Nlayer, Q, _p(X), _p(Y), _p(Z), _p(P))
+        return P
+
     def orbit(self, t):
         out = np.zeros(9)
         self.lib.orc_orbit_positions(float(t), _p(out))
@@ -520,3 +548,22 @@ class Ref:
         lib.ref_noise_logl(T, fmin, len(X) // 2, _p(X), _p(Y), _p(Z), len(inst), _p(inst),
                            _p(sg) if sg is not None else None, _p(out))
         return out
+
+    def noise_wavelet_logl(self, NF, NT, dt, df, lmin, Q, X, Y, Z, inst, sgal=None, mode=0, mod=None):
+        """The reference's coarse-grained wavelet noise likelihood for each model,
+        and the cell statistics it used: (logl [n], P [6, Nlayer, NT/Q])."""
+        lib = self.lib
+        lib.ref_noise_wavelet_logl.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_int, _D,
+                                               ctypes.c_int, _D, _D, _D, _D]
+        Nlayer = len(X) // NT
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        md = None if mod is None else np.ascontiguousarray(mod, np.float64)
+        out = np.zeros(len(inst))
+        P = np.zeros((6, Nlayer, NT // Q))
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        lib.ref_noise_wavelet_logl(NF, NT, dt, df, lmin, Nlayer, Q, _p(X), _p(Y), _p(Z), mode,
+                                   _p(md) if md is not None else None, len(inst), _p(inst),
+                                   _p(sg) if sg is not None else None, _p(out), _p(P))
+        return out, P

@@ -573,3 +573,104 @@ void ref_noise_logl(double T, double fmin, int NFFT, const double *X, const doub
     free_tdi(data->tdi);
     free(data);
 }
+
+/* The noise module's coarse-grained wavelet likelihood for n noise models on
+ * layers lmin .. lmin + Nlayer - 1 of an NF x NT grid (pixel dt, layer df):
+ * coarse_grain_wavelet_data (noise/src/glass_noise_model.c:1057) of the
+ * wavelet data X, Y, Z (pixel i of layer j at i + j NT), then per model
+ * generate_instrument_noise_model_wavelet (:561), for mode 1/2
+ * generate_galactic_foreground_model_wavelet (:656), the stationary (:983,
+ * modes 0/1) or modulated (:923, mode 2) coarse covariance,
+ * invert_noise_covariance_matrix and my_noise_log_likelihood_wavelet_coarse
+ * (:1211).  The modulation cache (6 x NT/Q: XX, YY, ZZ, XY, XZ, YZ) is given,
+ * as galaxy_modulation_cache_for_Q (utils/src/glass_galaxy.c:773) would have
+ * filled it. */
+void ref_noise_wavelet_logl(int NF, int NT, double dt, double df, int lmin, int Nlayer, int Q, const double *X,
+                            const double *Y, const double *Z, int mode, const double *mod, int n, const double *inst,
+                            const double *sgal, double *logl, double *P_out)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct Wavelets wdm;
+    memset(&wdm, 0, sizeof(wdm));
+    wdm.NF = NF;
+    wdm.NT = NT;
+    wdm.dt = dt;
+    wdm.df = df;
+    wdm.kmin = lmin * NT;
+    wdm.kmax = (lmin + Nlayer) * NT;
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->wdm = &wdm;
+    data->Nchannel = 3;
+    data->Nlayer = Nlayer;
+    data->lmin = lmin;
+    data->lmax = lmin + Nlayer;
+    data->N = Nlayer * NT;
+    data->NFFT = data->N / 2;
+    data->T = NT * dt;
+    strcpy(data->basis, "wavelet");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, 3);
+    memcpy(data->tdi->X, X, sizeof(double) * data->N);
+    memcpy(data->tdi->Y, Y, sizeof(double) * data->N);
+    memcpy(data->tdi->Z, Z, sizeof(double) * data->N);
+    struct CoarseStats stats;
+    alloc_coarse_stats(&stats, Nlayer, Q, NT);
+    coarse_grain_wavelet_data(data, &stats);
+    const int Ncoarse = NT / Q;
+    const size_t Npix = (size_t)Nlayer * Ncoarse;
+    if (P_out) {
+        memcpy(P_out, stats.Pxx, sizeof(double) * Npix);
+        memcpy(P_out + Npix, stats.Pyy, sizeof(double) * Npix);
+        memcpy(P_out + 2 * Npix, stats.Pzz, sizeof(double) * Npix);
+        memcpy(P_out + 3 * Npix, stats.Pxy, sizeof(double) * Npix);
+        memcpy(P_out + 4 * Npix, stats.Pxz, sizeof(double) * Npix);
+        memcpy(P_out + 5 * Npix, stats.Pyz, sizeof(double) * Npix);
+    }
+    struct InstrumentModel im;
+    memset(&im, 0, sizeof(im));
+    alloc_instrument_model(&im, Nlayer, Nlayer, 3);
+    for (int k = 0; k < Nlayer; k++) im.psd->f[k] = (lmin + k) * df;
+    struct ForegroundModel conf;
+    memset(&conf, 0, sizeof(conf));
+    alloc_foreground_model(&conf, Nlayer, Nlayer, 3);
+    for (int k = 0; k < Nlayer; k++) conf.psd->f[k] = (lmin + k) * df;
+    conf.Tobs = data->T;
+    struct GalaxyModulation gm;
+    memset(&gm, 0, sizeof(gm));
+    gm.Q_cached = Q;
+    gm.Nt_cached = Ncoarse;
+    gm.Nt_alloc = Ncoarse;
+    if (mod) {
+        gm.cache_XX = (double *)mod;
+        gm.cache_YY = (double *)mod + Ncoarse;
+        gm.cache_ZZ = (double *)mod + 2 * Ncoarse;
+        gm.cache_XY = (double *)mod + 3 * Ncoarse;
+        gm.cache_XZ = (double *)mod + 4 * Ncoarse;
+        gm.cache_YZ = (double *)mod + 5 * Ncoarse;
+    }
+    conf.modulation = &gm;
+    struct Noise *coarse = malloc(sizeof(struct Noise));
+    alloc_noise(coarse, (int)Npix, Nlayer, 3);
+    for (int p = 0; p < n; p++) {
+        for (int l = 0; l < 6; l++) {
+            im.sacc[l] = inst[12 * p + l];
+            im.soms[l] = inst[12 * p + 6 + l];
+        }
+        generate_instrument_noise_model_wavelet(&wdm, &orbit, &im);
+        if (mode) {
+            for (int q = 0; q < 5; q++) conf.sgal[q] = sgal[5 * p + q];
+            generate_galactic_foreground_model_wavelet(&wdm, &conf);
+        }
+        if (mode == 2)
+            generate_full_dynamic_covariance_matrix_coarse(&wdm, Q, &im, &conf, NULL, coarse);
+        else
+            generate_full_stationary_covariance_matrix_coarse(&wdm, Q, &im, mode ? &conf : NULL, NULL, coarse);
+        invert_noise_covariance_matrix(coarse);
+        logl[p] = my_noise_log_likelihood_wavelet_coarse(data, coarse, &stats);
+    }
+    free_noise(coarse);
+    free_coarse_stats(&stats);
+    free_tdi(data->tdi);
+    free(data);
+}

@@ -21,7 +21,8 @@ snr_wavelet (utils/src/glass_math.c:428), get_Fstat_logL
 generate_instrument_noise_model, generate_galactic_foreground_model,
 invert_noise_covariance_matrix and my_noise_log_likelihood
 (noise/src/glass_noise_model.c:389, :612, utils/src/glass_math.c:240,
-noise/src/glass_noise_model.c:1243).  Inputs are seeded numpy draws.
+noise/src/glass_noise_model.c:1243) with their wavelet-domain, coarse-grained
+forms (:561, :656, :923, :983, :1057, :1211).  Inputs are seeded numpy draws.
 
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py fstat noise   # only the named ones
@@ -328,7 +329,41 @@ def noise(ref, rng):
     np.savez_compressed(os.path.join(HERE, "noise.npz"), ncase=len(starts), NFFT=NF, **out)
 
 
-OWN_SEEDS = {"fstat": 20261204, "noise": 20261205}
+def noise_wavelet(ref, rng):
+    """The noise module's coarse-grained wavelet-domain likelihood: instrument
+    only, with the stationary foreground and with the modulated foreground
+    (a smooth modulation cache of galaxy_modulation_cache_for_Q's shape), at
+    Q = 1 (full resolution) and Q = 8, on 16 layers of a 1024 x 256 grid at
+    0.3 mHz and across the 10 mHz acceleration cutoff; data drawn per layer
+    from the starting model's covariance."""
+    from oracle import Port
+
+    port = Port()
+    NF, NT = 1024, 256
+    dt = 15.0 * NF
+    df = 1.0 / (2 * dt)
+    Nl = 16
+    inst0, sgal0 = wl.default_noise_params(T)
+    out = {}
+    c = 0
+    for band, lmin in enumerate((10, 300)):
+        C6 = np.array([port.noise_covariance(T, (lmin + j) * df, 1, inst0, sgal0)[0] for j in range(Nl)]) / (NF * NT)
+        X, Y, Z = wl.wavelet_noise_data(rng, C6, NT)
+        out[f"b{band}_X"], out[f"b{band}_Y"], out[f"b{band}_Z"] = X, Y, Z
+        inst = inst0 * np.exp(rng.uniform(-0.3, 0.3, (8, 12)))
+        sgal = sgal0 + rng.uniform(-0.2, 0.2, (8, 5))
+        for Q in (1, 8):
+            mod = wl.galaxy_modulation_like(NT // Q, phase=0.3 * c)
+            out[f"c{c}_lmin"], out[f"c{c}_Q"], out[f"c{c}_band"] = lmin, Q, band
+            out[f"c{c}_inst"], out[f"c{c}_sgal"], out[f"c{c}_mod"] = inst, sgal, mod
+            for mode in (0, 1, 2):
+                out[f"c{c}_logl{mode}"], P = ref.noise_wavelet_logl(NF, NT, dt, df, lmin, Q, X, Y, Z, inst, sgal, mode,
+                                                                    mod if mode == 2 else None)
+            c += 1
+    np.savez_compressed(os.path.join(HERE, "noise_wavelet.npz"), ncase=c, NF=NF, NT=NT, dt=dt, df=df, **out)
+
+
+OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206}
 
 
 def main(names=()):
@@ -347,6 +382,7 @@ def main(names=()):
     wavelet_likelihood(ref, rng)
     fstat(ref, np.random.default_rng(OWN_SEEDS["fstat"]))
     noise(ref, np.random.default_rng(OWN_SEEDS["noise"]))
+    noise_wavelet(ref, np.random.default_rng(OWN_SEEDS["noise_wavelet"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -254,3 +254,19 @@ def test_noise_likelihood_matches_reference(port, golden):
         np.testing.assert_allclose(got, g[f"c{c}_logl_inst"], rtol=1e-13)
         got = port.noise_logl(T, fmin, X, Y, Z, g[f"c{c}_inst"], g[f"c{c}_sgal"])
         np.testing.assert_allclose(got, g[f"c{c}_logl_gal"], rtol=1e-13)
+
+
+def test_noise_wavelet_likelihood_matches_reference(port, golden):
+    """my_noise_log_likelihood_wavelet_coarse (noise/src/glass_noise_model.c:1211)
+    after the wavelet-domain instrument/foreground models and the stationary or
+    modulated coarse covariance, at Q = 1 and 8, in two bands; and the cell
+    statistics of coarse_grain_wavelet_data (:1057)."""
+    g = golden("noise_wavelet.npz")
+    NF, NT, df = int(g["NF"]), int(g["NT"]), float(g["df"])
+    for c in range(int(g["ncase"])):
+        Q, lmin, b = int(g[f"c{c}_Q"]), int(g[f"c{c}_lmin"]), int(g[f"c{c}_band"])
+        P = port.noise_coarse_stats(NT, Q, g[f"b{b}_X"], g[f"b{b}_Y"], g[f"b{b}_Z"])
+        for mode in (0, 1, 2):
+            got = port.noise_wavelet_logl(NF, NT, df, lmin, P, Q, g[f"c{c}_inst"], g[f"c{c}_sgal"], mode,
+                                          g[f"c{c}_mod"] if mode == 2 else None)
+            np.testing.assert_allclose(got, g[f"c{c}_logl{mode}"], rtol=1e-13)
