@@ -854,8 +854,45 @@ def bench_noise(gg, torch, dev, rank, steps, warmup, cpu, peak64):
            "instrument_only": out["instrument"], "launches_per_batch": launches,
            "e2e": {"value": NOISE_NPROP / t_e2e, "unit": "models/s", "h2d_bytes_per_step": NOISE_NPROP * 17 * 8,
                    "d2h_bytes_per_step": NOISE_NPROP * 8}}
+    # wavelet domain: layers 10..469 of the 1024 x 2048 grid, Q = 16, the three covariances
+    NF, NT, lmin, Nl, Q = 1024, 2048, 10, 460, 16
+    df = 1.0 / (2 * 15.0 * NF)
+    C6 = np.array([port.noise_covariance(T, (lmin + j) * df, 1, inst0, sgal0)[0] for j in range(Nl)]) / (NF * NT)
+    Xw, Yw, Zw = wl.wavelet_noise_data(rng, C6, NT)
+    mod = wl.galaxy_modulation_like(NT // Q)
+    eng.noise_wavelet_setup(NF, NT, df, lmin, Q, Xw, Yw, Zw, mod)
+    eng.set_stream(stream.cuda_stream)
+    wv = {}
+    for mode, name in ((2, "modulated_foreground"), (1, "stationary_foreground"), (0, "instrument")):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                eng.noise_wavelet_logl_device(d_i, d_l, d_g, mode)
+            stream.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            for k in range(steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                eng.noise_wavelet_logl_device(d_i, d_l, d_g, mode)
+                ev[k][1].record(stream)
+            stream.synchronize()
+        t = sum(a.elapsed_time(b) for a, b in ev) / steps / 1e3
+        wv[name] = {"models_per_s": NOISE_NPROP / t, "ms_per_batch": 1e3 * t}
+    eng.set_stream(None)
+    res["wavelet"] = {"workload": f"my_noise_log_likelihood_wavelet_coarse, layers {lmin}..{lmin + Nl - 1} of "
+                                  f"{NF} x {NT}, Q = {Q} ({Nl * NT // Q} cells), {NOISE_NPROP} models per batch, FP64",
+                      **wv}
     if cpu:
         nth = os.cpu_count() or 1
+        Pw = port.noise_coarse_stats(NT, Q, Xw, Yw, Zw)
+        done, t0 = 0, time.perf_counter()
+        while True:
+            port.noise_wavelet_logl(NF, NT, df, lmin, Pw, Q, inst[:64], sgal[:64], 2, mod, nthreads=nth)
+            done += 64
+            el = time.perf_counter() - t0
+            if el > 3.0 or done >= NOISE_NPROP:
+                break
+        res["wavelet"]["cpu_baseline"] = {"value": done / el, "unit": "models/s", "cores": nth, "kind": "port",
+                                          "sample": f"{done} models, modulated foreground, OpenMP over models"}
         done, t0 = 0, time.perf_counter()
         while True:
             k = done % NOISE_NPROP

@@ -46,6 +46,7 @@ EXPORTS = (
     "glass_gpu_wavelet_fisher_batch", "glass_gpu_wavelet_fisher_batch_host",
     "glass_gpu_fstat_batch", "glass_gpu_fstat_batch_host", "glass_gpu_fstat_proposal_host",
     "glass_gpu_noise_setup", "glass_gpu_noise_logl_batch", "glass_gpu_noise_logl_batch_host",
+    "glass_gpu_noise_wavelet_setup", "glass_gpu_noise_wavelet_logl_batch", "glass_gpu_noise_wavelet_logl_batch_host",
 )
 
 _lib = None
@@ -111,6 +112,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_noise_setup.argtypes = [_V, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D, _D, _D]
     lib.glass_gpu_noise_logl_batch.argtypes = [_V, ctypes.c_int, _V, _V, _V]
     lib.glass_gpu_noise_logl_batch_host.argtypes = [_V, ctypes.c_int, _D, _D, _D]
+    lib.glass_gpu_noise_wavelet_setup.argtypes = [_V, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                  ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]
+    lib.glass_gpu_noise_wavelet_logl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V]
+    lib.glass_gpu_noise_wavelet_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D]
     _lib = lib
     return lib
 
@@ -410,6 +415,27 @@ class Engine:
         """Device tensors: inst [n, 12], sgal [n, 5] or None, logl [n]; asynchronous."""
         n = int(inst.shape[0])
         _check(self.lib.glass_gpu_noise_logl_batch(self._ctx, n, _ptr(inst), _ptr(sgal), _ptr(logl)))
+
+    def noise_wavelet_setup(self, NF, NT, df, lmin, Q, X, Y, Z, mod=None):
+        """Wavelet data (pixel i of layer j at i + j NT) on layers lmin.., cells of Q
+        pixels, and the foreground modulation [6, NT/Q] (or None)."""
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        md = None if mod is None else np.ascontiguousarray(mod, np.float64)
+        _check(self.lib.glass_gpu_noise_wavelet_setup(self._ctx, int(NF), int(NT), float(df), int(lmin),
+                                                      len(X) // int(NT), int(Q), _pd(X), _pd(Y), _pd(Z),
+                                                      _pd(md) if md is not None else None))
+
+    def noise_wavelet_logl_host(self, inst, sgal=None, mode=0):
+        i = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        g = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        out = np.empty(len(i))
+        _check(self.lib.glass_gpu_noise_wavelet_logl_batch_host(self._ctx, int(mode), len(i), _pd(i),
+                                                                _pd(g) if g is not None else None, _pd(out)))
+        return out
+
+    def noise_wavelet_logl_device(self, inst, logl, sgal=None, mode=0):
+        n = int(inst.shape[0])
+        _check(self.lib.glass_gpu_noise_wavelet_logl_batch(self._ctx, int(mode), n, _ptr(inst), _ptr(sgal), _ptr(logl)))
 
     def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                              precision=PREC_FP64):

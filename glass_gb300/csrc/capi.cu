@@ -81,6 +81,7 @@ struct glass_gpu_ctx {
   void *wv_fisher_mem = nullptr;  // perturbed parameters of the Fisher batches
   FsWorkDev fsw;  // F-statistic scratch
   NoiseDev noise;  // noise-model likelihood: per-bin table and chunk sums
+  NoiseWvDev noise_wv;  // the same in the wavelet domain
 };
 
 static void clear_host_graphs(glass_gpu_ctx *ctx) {
@@ -150,6 +151,8 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   fs_work_free(ctx->fsw);
   cudaFree(ctx->noise.tab);
   cudaFree(ctx->noise.partial);
+  cudaFree(ctx->noise_wv.mem);
+  cudaFree(ctx->noise_wv.partial);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
@@ -798,6 +801,93 @@ extern "C" int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, co
   if (rc) return rc;
   GLASS_CUDA(cudaMemcpyAsync(logl, d_logl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
   GLASS_CUDA(cudaStreamSynchronize(s), "noise_logl_batch_host sync");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_wavelet_setup(glass_gpu_ctx *ctx, int NF, int NT, double df, int lmin, int Nlayer,
+                                             int Q, const double *X, const double *Y, const double *Z,
+                                             const double *mod) {
+  if (!ctx || !X || !Y || !Z) return set_err(GLASS_ERR_ARG, "noise_wavelet_setup: null argument");
+  if (NF < 1 || NT < 1 || Nlayer < 1 || lmin < 0 || !(df > 0) || Q < 1 || Q > NT)
+    return set_err(GLASS_ERR_ARG, "noise_wavelet_setup: bad grid (NF, NT, Nlayer >= 1, lmin >= 0, df > 0, 1 <= Q <= NT)");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const int Nc = NT / Q;
+  const size_t Npix = (size_t)Nlayer * Nc;
+  std::vector<double> tab((size_t)kNoiseTabRows * Nlayer), P(6 * Npix);
+  noise_wv_build(NT, df, lmin, Nlayer, Q, X, Y, Z, tab.data(), P.data());
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "noise_wavelet_setup sync");
+  NoiseWvDev &w = ctx->noise_wv;
+  cudaFree(w.mem);
+  cudaFree(w.partial);
+  w = NoiseWvDev{};
+  const size_t bytes = sizeof(double) * (tab.size() + P.size() + 6 * (size_t)Nc);
+  GLASS_CUDA(cudaMalloc(&w.mem, bytes), "cudaMalloc(noise wavelet)");
+  w.tab = (double *)w.mem;
+  w.P = w.tab + tab.size();
+  w.mod = w.P + P.size();
+  GLASS_CUDA(cudaMemcpy(w.tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice), "upload noise wv table");
+  GLASS_CUDA(cudaMemcpy(w.P, P.data(), sizeof(double) * P.size(), cudaMemcpyHostToDevice), "upload noise wv stats");
+  if (mod)
+    GLASS_CUDA(cudaMemcpy(w.mod, mod, sizeof(double) * 6 * Nc, cudaMemcpyHostToDevice), "upload modulation");
+  w.NF = NF;
+  w.NT = NT;
+  w.lmin = lmin;
+  w.Nlayer = Nlayer;
+  w.Q = Q;
+  w.Ncoarse = Nc;
+  w.df = df;
+  w.has_mod = mod != nullptr;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                                  const double *sgal, double *logl) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch: null context");
+  if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch: negative model count");
+  if (mode < 0 || mode > 2) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch: mode is 0, 1 or 2");
+  if (nprop == 0) return GLASS_OK;
+  if (!inst || !logl || (mode && !sgal)) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch: null argument");
+  NoiseWvDev &w = ctx->noise_wv;
+  if (!w.mem) return set_err(GLASS_ERR_STATE, "noise_wavelet_logl_batch: no data set (glass_gpu_noise_wavelet_setup)");
+  if (mode == 2 && !w.has_mod) return set_err(GLASS_ERR_STATE, "noise_wavelet_logl_batch: mode 2 needs the modulation");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if (mode == 2 && nprop > w.partial_models) {
+    int want = w.partial_models > 0 ? w.partial_models : 64;
+    while (want < nprop) want *= 2;
+    GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "noise wv partial sync");
+    cudaFree(w.partial);
+    w.partial = nullptr;
+    w.partial_models = 0;
+    GLASS_CUDA(cudaMalloc(&w.partial, sizeof(double) * (size_t)want * noise_wv_chunks(w)), "cudaMalloc(noise wv partial)");
+    w.partial_models = want;
+  }
+  int nl = 0;
+  cudaError_t e = noise_wv_logl_launch(w, mode, nprop, inst, sgal, logl, ctx->stream, &nl);
+  ctx->last_launches = nl;
+  if (e != cudaSuccess) return cuda_err(e, "noise_wavelet_logl_batch launch");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                                       const double *sgal, double *logl) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch_host: null context");
+  if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch_host: negative model count");
+  if (nprop == 0) return GLASS_OK;
+  if (!inst || !logl) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch_host: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t nd = (size_t)nprop;
+  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (12 + 5 + 1) + 256))) return rc;
+  double *d_inst = (double *)ctx->d_stage, *d_sgal = d_inst + 12 * nd, *d_logl = d_sgal + 5 * nd;
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d_inst, inst, sizeof(double) * 12 * nd, cudaMemcpyHostToDevice, s), "H2D inst");
+  if (sgal) GLASS_CUDA(cudaMemcpyAsync(d_sgal, sgal, sizeof(double) * 5 * nd, cudaMemcpyHostToDevice, s), "H2D sgal");
+  rc = glass_gpu_noise_wavelet_logl_batch(ctx, mode, nprop, d_inst, sgal ? d_sgal : nullptr, d_logl);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(logl, d_logl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
+  GLASS_CUDA(cudaStreamSynchronize(s), "noise_wavelet_logl_batch_host sync");
   return GLASS_OK;
 }
 

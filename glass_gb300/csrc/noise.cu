@@ -39,6 +39,80 @@ struct NoiseArgs {
   double *partial;     // [nprop][nchunks]
 };
 
+// Instrument covariance of one bin at link levels in[12] (sacc[6], soms[6]),
+// from the bin's cos(f/f*), -8 sin^2(f/f*) and transfer functions
+// (noise/src/glass_noise_model.c:445-546; acc_tf is 0 at f >= 10 mHz, where the
+// reference leaves out the acceleration terms: adding exact zeros changes
+// nothing), normalised by 4.
+__device__ __forceinline__ void noise_inst_cov(double cosx, double tdi, double acc_tf, double oms_tf,
+                                               const double *in, double &cxx, double &cyy, double &czz, double &cxy,
+                                               double &cxz, double &cyz) {
+  const double A12 = in[0] * acc_tf, A21 = in[1] * acc_tf, A23 = in[2] * acc_tf;
+  const double A32 = in[3] * acc_tf, A13 = in[4] * acc_tf, A31 = in[5] * acc_tf;
+  const double O12 = in[6] * oms_tf, O21 = in[7] * oms_tf, O23 = in[8] * oms_tf;
+  const double O32 = in[9] * oms_tf, O13 = in[10] * oms_tf, O31 = in[11] * oms_tf;
+  double c00 = (O12 + O21 + O13 + O31) * .25;
+  double c11 = (O23 + O32 + O21 + O12) * .25;
+  double c22 = (O31 + O13 + O32 + O23) * .25;
+  double c01 = (O12 + O21) * .5;
+  double c02 = (O13 + O31) * .5;
+  double c12 = (O32 + O23) * .5;
+  c00 += ((A12 + A13) + ((A21 + A31)) * cosx * cosx);
+  c11 += ((A23 + A21) + ((A32 + A12)) * cosx * cosx);
+  c22 += ((A31 + A32) + ((A13 + A23)) * cosx * cosx);
+  c01 += 2. * (A12 + A21);
+  c02 += 2. * (A13 + A31);
+  c12 += 2. * (A32 + A23);
+  c00 *= -2. * tdi;
+  c11 *= -2. * tdi;
+  c22 *= -2. * tdi;
+  c01 *= tdi * cosx;
+  c02 *= tdi * cosx;
+  c12 *= tdi * cosx;
+  cxx = c00 / 4.0;
+  cyy = c11 / 4.0;
+  czz = c22 / 4.0;
+  cxy = c01 / 4.0;
+  cxz = c02 / 4.0;
+  cyz = c12 / 4.0;
+}
+
+// The galactic foreground's PSD at f (utils/src/glass_galaxy.c:40-44), zero
+// above 10 f1 as in noise/src/glass_noise_model.c:627-631; fp73 = f^(-7/3).
+__device__ __forceinline__ double noise_sgal(double f, double fp73, double Amp, double f1, double alpha, double fk,
+                                             double f2) {
+  return (f > f1 * 10) ? 0.0 : Amp * fp73 * exp(-pow(f / f1, alpha)) * 0.5 * (1. + tanh((fk - f) / f2));
+}
+
+// Inverse and log-determinant of a symmetric 3x3 covariance by the
+// reference's elimination (utils/src/glass_math.c:261-274), the entries as
+// cofactor / det: iv = xx, yy, zz, xy, xz, yz.
+__device__ __forceinline__ void noise_inv3(double cxx, double cyy, double czz, double cxy, double cxz, double cyz,
+                                           double *iv, double &logdetC) {
+  const double d1 = cxx;
+  const double d2 = cyy - cxy * cxy / d1;
+  const double tt = cyz - cxy * cxz / d1;
+  const double d3 = (czz - cxz * cxz / d1) - (tt * tt) / d2;
+  logdetC = log(d1) + log(d2) + log(d3);
+  const double idet = 1.0 / (d1 * d2 * d3);
+  iv[0] = (cyy * czz - cyz * cyz) * idet;
+  iv[1] = (czz * cxx - cxz * cxz) * idet;
+  iv[2] = (cxx * cyy - cxy * cxy) * idet;
+  iv[3] = (cxz * cyz - czz * cxy) * idet;
+  iv[4] = (cxy * cyz - cxz * cyy) * idet;
+  iv[5] = (cxy * cxz - cxx * cyz) * idet;
+}
+
+__device__ __forceinline__ void noise_gal_params(const double *sg, double &Amp, double &f1, double &alpha,
+                                                 double &fk, double &f2) {
+  // map_array_to_foreground_params (noise/src/glass_noise_model.c:67-74)
+  Amp = exp(sg[0]);
+  f1 = exp(sg[1]);
+  alpha = sg[2];
+  fk = exp(sg[3]);
+  f2 = exp(sg[4]);
+}
+
 __device__ __forceinline__ double block_sum(double v, double *red) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
@@ -57,18 +131,9 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_logl_kernel(NoiseArgs a) 
   __shared__ double red[kNoiseThreads / 32];
   const int chunk = blockIdx.x, p = blockIdx.y;
   const double *in = a.inst + 12 * (size_t)p;
-  const double s12 = in[0], s21 = in[1], s23 = in[2], s32 = in[3], s13 = in[4], s31 = in[5];
-  const double o12 = in[6], o21 = in[7], o23 = in[8], o32 = in[9], o13 = in[10], o31 = in[11];
   const bool gal = a.sgal != nullptr;
   double Amp = 0, f1 = 0, alpha = 0, fk = 0, f2 = 0;
-  if (gal) {  // map_array_to_foreground_params (noise/src/glass_noise_model.c:67-74)
-    const double *sg = a.sgal + 5 * (size_t)p;
-    Amp = exp(sg[0]);
-    f1 = exp(sg[1]);
-    alpha = sg[2];
-    fk = exp(sg[3]);
-    f2 = exp(sg[4]);
-  }
+  if (gal) noise_gal_params(a.sgal + 5 * (size_t)p, Amp, f1, alpha, fk, f2);
   const int N = a.N;
   const double *F = a.tab + (size_t)kTabF * N, *COSX = a.tab + (size_t)kTabCosx * N;
   const double *TDI = a.tab + (size_t)kTabTdi * N, *ACC = a.tab + (size_t)kTabAcc * N;
@@ -85,42 +150,11 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_logl_kernel(NoiseArgs a) 
     const double f = F[n];
     double cxx = 0.0, cyy = 0.0, czz = 0.0, cxy = 0.0, cxz = 0.0, cyz = 0.0;
     if (f != 0.0) {
-      const double cosx = COSX[n], tdi = TDI[n], acc_tf = ACC[n], oms_tf = OMS[n];
-      // acc_tf is 0 at f >= 10 mHz, where the reference leaves out the
-      // acceleration terms: adding exact zeros changes nothing
-      const double A12 = s12 * acc_tf, A21 = s21 * acc_tf, A23 = s23 * acc_tf;
-      const double A32 = s32 * acc_tf, A13 = s13 * acc_tf, A31 = s31 * acc_tf;
-      const double O12 = o12 * oms_tf, O21 = o21 * oms_tf, O23 = o23 * oms_tf;
-      const double O32 = o32 * oms_tf, O13 = o13 * oms_tf, O31 = o31 * oms_tf;
-      double c00 = (O12 + O21 + O13 + O31) * .25;
-      double c11 = (O23 + O32 + O21 + O12) * .25;
-      double c22 = (O31 + O13 + O32 + O23) * .25;
-      double c01 = (O12 + O21) * .5;
-      double c02 = (O13 + O31) * .5;
-      double c12 = (O32 + O23) * .5;
-      c00 += ((A12 + A13) + ((A21 + A31)) * cosx * cosx);
-      c11 += ((A23 + A21) + ((A32 + A12)) * cosx * cosx);
-      c22 += ((A31 + A32) + ((A13 + A23)) * cosx * cosx);
-      c01 += 2. * (A12 + A21);
-      c02 += 2. * (A13 + A31);
-      c12 += 2. * (A32 + A23);
-      c00 *= -2. * tdi;
-      c11 *= -2. * tdi;
-      c22 *= -2. * tdi;
-      c01 *= tdi * cosx;
-      c02 *= tdi * cosx;
-      c12 *= tdi * cosx;
-      cxx = c00 / 4.0;
-      cyy = c11 / 4.0;
-      czz = c22 / 4.0;
-      cxy = c01 / 4.0;
-      cxz = c02 / 4.0;
-      cyz = c12 / 4.0;
+      noise_inst_cov(COSX[n], TDI[n], ACC[n], OMS[n], in, cxx, cyy, czz, cxy, cxz, cyz);
       if (gal) {
         // utils/src/glass_galaxy.c:40-44, skipped above 10 f1 as the reference does
         const double t = TG[n];
-        const double Sgal =
-            (f > f1 * 10) ? 0.0 : Amp * P73[n] * exp(-pow(f / f1, alpha)) * 0.5 * (1. + tanh((fk - f) / f2));
+        const double Sgal = noise_sgal(f, P73[n], Amp, f1, alpha, fk, f2);
         const double d = t * Sgal / 4.0, o = -0.5 * t * Sgal / 4.0;
         cxx += d;
         cyy += d;
@@ -130,25 +164,15 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_logl_kernel(NoiseArgs a) 
         cyz += o;
       }
     }
-    const double d1 = cxx;
-    const double d2 = cyy - cxy * cxy / d1;
-    const double tt = cyz - cxy * cxz / d1;
-    const double d3 = (czz - cxz * cxz / d1) - (tt * tt) / d2;
-    const double logdetC = log(d1) + log(d2) + log(d3);
-    const double idet = 1.0 / (d1 * d2 * d3);
-    const double ixx = (cyy * czz - cyz * cyz) * idet;
-    const double iyy = (czz * cxx - cxz * cxz) * idet;
-    const double izz = (cxx * cyy - cxy * cxy) * idet;
-    const double ixy = (cxz * cyz - czz * cxy) * idet;
-    const double ixz = (cxy * cyz - cxz * cyy) * idet;
-    const double iyz = (cxy * cxz - cxx * cyz) * idet;
+    double iv[6], logdetC;
+    noise_inv3(cxx, cyy, czz, cxy, cxz, cyz, iv, logdetC);
     double l = 0.0;
-    l -= 0.5 * XX[n] * ixx * 2;
-    l -= 0.5 * YY[n] * iyy * 2;
-    l -= 0.5 * ZZ[n] * izz * 2;
-    l -= XY[n] * ixy * 2;
-    l -= XZ[n] * ixz * 2;
-    l -= YZ[n] * iyz * 2;
+    l -= 0.5 * XX[n] * iv[0] * 2;
+    l -= 0.5 * YY[n] * iv[1] * 2;
+    l -= 0.5 * ZZ[n] * iv[2] * 2;
+    l -= XY[n] * iv[3] * 2;
+    l -= XZ[n] * iv[4] * 2;
+    l -= YZ[n] * iv[5] * 2;
     l -= logdetC;
     acc += l;
   }
@@ -163,6 +187,137 @@ __global__ void noise_finish_kernel(const double *partial, int nchunks, int npro
   double s = 0.0;
   for (int c = 0; c < nchunks; c++) s += partial[(size_t)p * nchunks + c];
   logl[p] = s - cst;
+}
+
+
+// ------------------------------------------------------- wavelet domain
+struct NoiseWvArgs {
+  int Nlayer, Ncoarse, Q, LJ, nchunks, mode;
+  double inv_ND;
+  const double *tab, *P, *mod;
+  const double *inst, *sgal;
+  double *out;  // logl (modes 0/1) or partial (mode 2)
+};
+
+// Instrument (and foreground) variance of one layer in the wavelet domain:
+// the Fourier model at the layer centre over ND (generate_instrument_noise_
+// model_wavelet :561-610, generate_galactic_foreground_model_wavelet :656-722,
+// whose off-diagonals have the isotropic -1/2 undone).  inst6, conf6: xx, yy,
+// zz, xy, xz, yz.
+__device__ __forceinline__ void noise_wv_layer(const NoiseWvArgs &a, int j, const double *in, bool gal, double Amp,
+                                               double f1, double alpha, double fk, double f2, double *inst6,
+                                               double *conf6) {
+  const int NL = a.Nlayer;
+  const double f = a.tab[(size_t)kTabF * NL + j];
+  double cxx = 0, cyy = 0, czz = 0, cxy = 0, cxz = 0, cyz = 0;
+  if (f != 0.0)
+    noise_inst_cov(a.tab[(size_t)kTabCosx * NL + j], a.tab[(size_t)kTabTdi * NL + j], a.tab[(size_t)kTabAcc * NL + j],
+                   a.tab[(size_t)kTabOms * NL + j], in, cxx, cyy, czz, cxy, cxz, cyz);
+  inst6[0] = cxx * a.inv_ND;
+  inst6[1] = cyy * a.inv_ND;
+  inst6[2] = czz * a.inv_ND;
+  inst6[3] = cxy * a.inv_ND;
+  inst6[4] = cxz * a.inv_ND;
+  inst6[5] = cyz * a.inv_ND;
+  double dg = 0.0, og = 0.0;
+  if (gal && f != 0.0) {
+    const double t = a.tab[(size_t)kTabTgal * NL + j];
+    const double Sgal = noise_sgal(f, a.tab[(size_t)kTabFp73 * NL + j], Amp, f1, alpha, fk, f2);
+    dg = t * Sgal / 4.0;
+    og = -0.5 * t * Sgal / 4.0;
+    og *= -2.0;
+  }
+  conf6[0] = conf6[1] = conf6[2] = dg * a.inv_ND;
+  conf6[3] = conf6[4] = conf6[5] = og * a.inv_ND;
+}
+
+// Modes 0/1: the covariance is the same for every cell of a layer, so a
+// layer's cells contribute -Q/2 (ixx Sxx + ... + 2 ixy Sxy ...) - Q/2 Ncoarse
+// log det with S the layer's sums of the cell statistics.  One CTA per model.
+__global__ void __launch_bounds__(kNoiseThreads) noise_wv_stationary_kernel(NoiseWvArgs a) {
+  __shared__ double red[kNoiseThreads / 32];
+  const int p = blockIdx.x;
+  const double *in = a.inst + 12 * (size_t)p;
+  const bool gal = a.mode == 1;
+  double Amp = 0, f1 = 0, alpha = 0, fk = 0, f2 = 0;
+  if (gal) noise_gal_params(a.sgal + 5 * (size_t)p, Amp, f1, alpha, fk, f2);
+  const int NL = a.Nlayer;
+  const double Qd = (double)a.Q;
+  double acc = 0.0;
+  for (int j = threadIdx.x; j < NL; j += blockDim.x) {
+    double c6[6], g6[6];
+    noise_wv_layer(a, j, in, gal, Amp, f1, alpha, fk, f2, c6, g6);
+    if (gal) {  // generate_full_stationary_covariance_matrix_coarse (:1003-1010)
+      c6[0] += g6[0];
+      c6[1] += g6[1];
+      c6[2] += g6[2];
+      c6[3] -= g6[3] / 2.;
+      c6[4] -= g6[4] / 2.;
+      c6[5] -= g6[5] / 2.;
+    }
+    double iv[6], ld;
+    noise_inv3(c6[0], c6[1], c6[2], c6[3], c6[4], c6[5], iv, ld);
+    double s = 0.0;
+    s -= 0.5 * Qd * iv[0] * a.tab[(size_t)kTabXX * NL + j];
+    s -= 0.5 * Qd * iv[1] * a.tab[(size_t)kTabYY * NL + j];
+    s -= 0.5 * Qd * iv[2] * a.tab[(size_t)kTabZZ * NL + j];
+    s -= Qd * iv[3] * a.tab[(size_t)kTabXY * NL + j];
+    s -= Qd * iv[4] * a.tab[(size_t)kTabXZ * NL + j];
+    s -= Qd * iv[5] * a.tab[(size_t)kTabYZ * NL + j];
+    s -= 0.5 * Qd * ld * (double)a.Ncoarse;
+    acc += s;
+  }
+  const double s = block_sum(acc, red);
+  if (threadIdx.x == 0) a.out[p] = s;
+}
+
+// Mode 2: the foreground modulated per cell (generate_full_dynamic_covariance_
+// matrix_coarse :923-981).  One CTA per (chunk of LJ layers, model); the
+// chunk's layer covariances go to shared memory, then every cell is inverted
+// and summed with its statistics (my_noise_log_likelihood_wavelet_coarse
+// :1211-1241).
+constexpr int kNoiseWvMaxLJ = 64;
+__global__ void __launch_bounds__(kNoiseThreads) noise_wv_dynamic_kernel(NoiseWvArgs a) {
+  __shared__ double red[kNoiseThreads / 32];
+  __shared__ double lay[kNoiseWvMaxLJ][12];
+  const int chunk = blockIdx.x, p = blockIdx.y;
+  const double *in = a.inst + 12 * (size_t)p;
+  double Amp, f1, alpha, fk, f2;
+  noise_gal_params(a.sgal + 5 * (size_t)p, Amp, f1, alpha, fk, f2);
+  const int j0 = chunk * a.LJ;
+  const int nl = min(a.LJ, a.Nlayer - j0);
+  for (int t = threadIdx.x; t < nl; t += blockDim.x)
+    noise_wv_layer(a, j0 + t, in, true, Amp, f1, alpha, fk, f2, &lay[t][0], &lay[t][6]);
+  __syncthreads();
+  const int Nc = a.Ncoarse;
+  const size_t Npix = (size_t)a.Nlayer * Nc;
+  const double Qd = (double)a.Q;
+  double acc = 0.0;
+  for (int idx = threadIdx.x; idx < nl * Nc; idx += blockDim.x) {
+    const int jj = idx / Nc, q = idx - jj * Nc;
+    double c6[6];
+#pragma unroll
+    for (int e = 0; e < 6; e++) c6[e] = lay[jj][e] + lay[jj][6 + e] * a.mod[(size_t)e * Nc + q];
+    double iv[6], ld;
+    noise_inv3(c6[0], c6[1], c6[2], c6[3], c6[4], c6[5], iv, ld);
+    const size_t k = (size_t)(j0 + jj) * Nc + q;
+    double s = 0.0;
+    s -= 0.5 * Qd * iv[0] * a.P[k];
+    s -= 0.5 * Qd * iv[1] * a.P[Npix + k];
+    s -= 0.5 * Qd * iv[2] * a.P[2 * Npix + k];
+    s -= Qd * iv[3] * a.P[3 * Npix + k];
+    s -= Qd * iv[4] * a.P[4 * Npix + k];
+    s -= Qd * iv[5] * a.P[5 * Npix + k];
+    s -= 0.5 * Qd * ld;
+    acc += s;
+  }
+  const double s = block_sum(acc, red);
+  if (threadIdx.x == 0) a.out[(size_t)p * a.nchunks + chunk] = s;
+}
+
+__global__ void noise_wv_const_kernel(double *logl, int nprop, double cst) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < nprop) logl[p] -= cst;
 }
 
 }  // namespace
@@ -206,6 +361,124 @@ void noise_build_table(double T, double fmin, int N, const double *X, const doub
     *col[kTabXZ] = rex * rez + imx * imz;
     *col[kTabYZ] = rey * rez + imy * imz;
   }
+}
+
+static void noise_freq_rows(double f, double *tab, int N, int n) {
+  const double fstar = kCLIGHT / (2.0 * M_PI * kLARM);
+  const double acc_units = 2.81837551648e-19;  // 1/(2 pi c)^2
+  const double oms_units = 4.39256635604e-16;  // (2 pi / c)^2
+  const double acc_fmax = 0.01;
+  double *col[kNoiseTabRows];
+  for (int r = 0; r < kNoiseTabRows; r++) col[r] = tab + (size_t)r * N + n;
+  *col[kTabF] = f;
+  if (f != 0.0) {
+    const double x = f / fstar, f2 = f * f;
+    const double sx = sin(x);
+    *col[kTabCosx] = cos(x);
+    *col[kTabTdi] = -8.0 * (sx * sx);
+    *col[kTabAcc] = (f < acc_fmax) ? acc_units / f2 * (1.0 + pow(0.4e-3 / f, 2)) * (1.0 + pow(f / 8.0e-3, 4)) : 0.0;
+    *col[kTabOms] = oms_units * f2 * (1.0 + pow(2.0e-3 / f, 4));
+    const double xg = f / (kCLIGHT / (kPI2 * kLARM));
+    *col[kTabTgal] = 4. * xg * xg * sin(xg) * sin(xg);
+    *col[kTabFp73] = pow(f, -7. / 3.);
+  } else {
+    *col[kTabCosx] = *col[kTabTdi] = *col[kTabAcc] = *col[kTabOms] = *col[kTabTgal] = *col[kTabFp73] = 0.0;
+  }
+}
+
+void noise_wv_build(int NT, double df, int lmin, int Nlayer, int Q, const double *X, const double *Y, const double *Z,
+                    double *tab, double *P) {
+  const int Nc = NT / Q;
+  const size_t Npix = (size_t)Nlayer * Nc;
+  const double invQ = 1.0 / (double)Q;
+  for (int j = 0; j < Nlayer; j++) {
+    noise_freq_rows((double)(lmin + j) * df, tab, Nlayer, j);
+    double S[6] = {0, 0, 0, 0, 0, 0};
+    for (int q = 0; q < Nc; q++) {
+      double sxx = 0, syy = 0, szz = 0, sxy = 0, sxz = 0, syz = 0;
+      for (int i = q * Q; i < (q + 1) * Q; i++) {
+        const size_t k = (size_t)i + (size_t)j * NT;
+        const double wx = X[k], wy = Y[k], wz = Z[k];
+        sxx += wx * wx;
+        syy += wy * wy;
+        szz += wz * wz;
+        sxy += wx * wy;
+        sxz += wx * wz;
+        syz += wy * wz;
+      }
+      const size_t kc = (size_t)q + (size_t)j * Nc;
+      const double v[6] = {sxx * invQ, syy * invQ, szz * invQ, sxy * invQ, sxz * invQ, syz * invQ};
+      for (int e = 0; e < 6; e++) {
+        P[(size_t)e * Npix + kc] = v[e];
+        S[e] += v[e];
+      }
+    }
+    for (int e = 0; e < 6; e++) tab[(size_t)(kTabXX + e) * Nlayer + j] = S[e];
+  }
+}
+
+static int noise_wv_lj(const NoiseWvDev &w) {
+  int lj = 4096 / (w.Ncoarse > 0 ? w.Ncoarse : 1);
+  if (lj < 1) lj = 1;
+  if (lj > kNoiseWvMaxLJ) lj = kNoiseWvMaxLJ;
+  return lj;
+}
+
+int noise_wv_chunks(const NoiseWvDev &w) {
+  const int lj = noise_wv_lj(w);
+  return (w.Nlayer + lj - 1) / lj;
+}
+
+cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const double *inst, const double *sgal,
+                                 double *logl, cudaStream_t stream, int *nlaunch) {
+  NoiseWvArgs a;
+  a.Nlayer = w.Nlayer;
+  a.Ncoarse = w.Ncoarse;
+  a.Q = w.Q;
+  a.LJ = noise_wv_lj(w);
+  a.nchunks = noise_wv_chunks(w);
+  a.mode = mode;
+  a.inv_ND = 1.0 / (double)((long long)w.NF * w.NT);
+  a.tab = w.tab;
+  a.P = w.P;
+  a.mod = w.mod;
+  a.inst = inst;
+  a.sgal = sgal;
+  int launches = 0;
+  cudaError_t e;
+  if (mode != 2) {
+    for (int p0 = 0; p0 < nprop; p0 += 65535 * 16) {
+      const int np = nprop - p0 < 65535 * 16 ? nprop - p0 : 65535 * 16;
+      NoiseWvArgs s = a;
+      s.inst = inst + 12 * (size_t)p0;
+      s.sgal = sgal ? sgal + 5 * (size_t)p0 : nullptr;
+      s.out = logl + p0;
+      noise_wv_stationary_kernel<<<np, kNoiseThreads, 0, stream>>>(s);
+      launches++;
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+  } else {
+    for (int p0 = 0; p0 < nprop; p0 += 65535) {
+      const int np = nprop - p0 < 65535 ? nprop - p0 : 65535;
+      NoiseWvArgs s = a;
+      s.inst = inst + 12 * (size_t)p0;
+      s.sgal = sgal + 5 * (size_t)p0;
+      s.out = w.partial + (size_t)p0 * a.nchunks;
+      noise_wv_dynamic_kernel<<<dim3(a.nchunks, np), kNoiseThreads, 0, stream>>>(s);
+      launches++;
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+  }
+  // my_noise_log_likelihood_wavelet_coarse's constant over the full pixel count (:1238-1240)
+  const double cst = 0.5 * 3 * ((double)w.Nlayer * w.NT) * log(2 * M_PI);
+  if (mode == 2) {
+    noise_finish_kernel<<<(nprop + 255) / 256, 256, 0, stream>>>(w.partial, a.nchunks, nprop, cst, logl);
+  } else {
+    noise_wv_const_kernel<<<(nprop + 255) / 256, 256, 0, stream>>>(logl, nprop, cst);
+  }
+  launches++;
+  if (nlaunch) *nlaunch = launches;
+  return cudaGetLastError();
 }
 
 int noise_chunks(int N) { return (N + kNoiseChunk - 1) / kNoiseChunk; }

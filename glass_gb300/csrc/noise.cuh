@@ -22,6 +22,32 @@ struct NoiseDev {
 };
 
 void noise_build_table(double T, double fmin, int N, const double *X, const double *Y, const double *Z, double *tab);
+
+// Wavelet-domain form (coarse-grained): layers lmin .. lmin + Nlayer - 1 of an
+// NF x NT grid of layer width df, cells of Q pixels in time.
+struct NoiseWvDev {
+  int NF = 0, NT = 0, lmin = 0, Nlayer = 0, Q = 0, Ncoarse = 0;
+  double df = 0;
+  bool has_mod = false;
+  double *tab = nullptr;      // kNoiseTabRows x Nlayer: layer-centre factors, then per-layer sums of P over q
+  double *P = nullptr;        // 6 x Nlayer Ncoarse cell statistics (xx, yy, zz, xy, xz, yz)
+  double *mod = nullptr;      // 6 x Ncoarse modulation of the foreground (or unused)
+  double *partial = nullptr;  // per-model chunk sums
+  int partial_models = 0;
+  void *mem = nullptr;        // backs tab, P, mod
+};
+
+// Layer-centre factors (rows kTabF .. kTabFp73) at f = (lmin + j) df, the cell
+// statistics P (coarse_grain_wavelet_data, noise/src/glass_noise_model.c:1057)
+// of X, Y, Z (pixel i of layer j at i + j NT) and their per-layer sums (rows
+// kTabXX .. kTabYZ).
+void noise_wv_build(int NT, double df, int lmin, int Nlayer, int Q, const double *X, const double *Y, const double *Z,
+                    double *tab, double *P);
+int noise_wv_chunks(const NoiseWvDev &w);
+// mode 0 instrument, 1 stationary foreground, 2 modulated foreground;
+// w.partial must hold nprop x noise_wv_chunks(w) (mode 2).
+cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const double *inst, const double *sgal,
+                                 double *logl, cudaStream_t stream, int *nlaunch);
 int noise_chunks(int N);
 // logl[p] for noise models inst[12 p ..] (sacc[6], soms[6]) and sgal[5 p ..]
 // (or null: instrument only); nd.partial must hold nprop x noise_chunks(N).

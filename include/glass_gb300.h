@@ -235,6 +235,33 @@ int glass_gpu_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, const double *inst
 int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
                                     double *logl);
 
+/*
+ * The same likelihood in the wavelet domain, coarse-grained
+ * (my_noise_log_likelihood_wavelet_coarse, noise/src/glass_noise_model.c:1211;
+ * Q = 1 is the full-resolution my_noise_log_likelihood_wavelet, :1182).
+ * glass_gpu_noise_wavelet_setup takes the wavelet data on layers lmin ..
+ * lmin + Nlayer - 1 of an NF x NT grid with layer width df (X, Y, Z: pixel i
+ * of layer j at i + j NT, Nlayer NT doubles each), forms the cells' sample
+ * covariances over Q pixels (coarse_grain_wavelet_data, :1057), and keeps the
+ * foreground modulation mod[6 (NT/Q)] = XX, YY, ZZ, XY, XZ, YZ per cell (the
+ * cache galaxy_modulation_cache_for_Q fills, utils/src/glass_galaxy.c:773; may
+ * be NULL when mode 2 is not used).  glass_gpu_noise_wavelet_logl_batch gives
+ * logl[p] for the covariance of
+ *   mode 0: the instrument (generate_instrument_noise_model_wavelet, :561),
+ *   mode 1: plus the stationary foreground
+ *           (generate_full_stationary_covariance_matrix_coarse, :983),
+ *   mode 2: plus the modulated foreground
+ *           (generate_full_dynamic_covariance_matrix_coarse, :923),
+ * with inst, sgal as glass_gpu_noise_logl_batch (sgal unused in mode 0).
+ * FP64.  Device pointers; asynchronous.  _host: host pointers, synchronous.
+ */
+int glass_gpu_noise_wavelet_setup(glass_gpu_ctx *ctx, int NF, int NT, double df, int lmin, int Nlayer, int Q,
+                                  const double *X, const double *Y, const double *Z, const double *mod);
+int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst, const double *sgal,
+                                       double *logl);
+int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                            const double *sgal, double *logl);
+
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 

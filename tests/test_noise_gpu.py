@@ -93,3 +93,56 @@ def test_noise_logl_device_entry_and_large_batches(engine, port):
 def test_noise_errors(engine):
     with pytest.raises(gg.GlassError):
         engine.noise_setup(T, 0, np.zeros(8), np.zeros(8), np.zeros(8))
+
+
+# ------------------------------------------------------------ wavelet domain
+def test_noise_wavelet_logl_matches_reference(engine, golden):
+    """my_noise_log_likelihood_wavelet_coarse with the instrument, stationary and
+    modulated foreground covariances, Q = 1 and 8, two bands."""
+    g = golden("noise_wavelet.npz")
+    NF, NT, df = int(g["NF"]), int(g["NT"]), float(g["df"])
+    for c in range(int(g["ncase"])):
+        Q, lmin, b = int(g[f"c{c}_Q"]), int(g[f"c{c}_lmin"]), int(g[f"c{c}_band"])
+        engine.noise_wavelet_setup(NF, NT, df, lmin, Q, g[f"b{b}_X"], g[f"b{b}_Y"], g[f"b{b}_Z"], g[f"c{c}_mod"])
+        for mode in (0, 1, 2):
+            got = engine.noise_wavelet_logl_host(g[f"c{c}_inst"], g[f"c{c}_sgal"], mode)
+            ref = g[f"c{c}_logl{mode}"]
+            np.testing.assert_allclose(got, ref, rtol=REL)
+            np.testing.assert_allclose(got - got[0], ref - ref[0], atol=REL * abs(ref[0]))
+
+
+def test_noise_wavelet_full_grid_against_oracle(engine, port):
+    """460 layers of the 1024 x 2048 grid (0.33 .. 15.3 mHz), Q = 16, all modes,
+    40 models, and device pointers."""
+    import torch
+
+    rng = np.random.default_rng(23)
+    NF, NT, lmin, Nl, Q = 1024, 2048, 10, 460, 16
+    df = 1.0 / (2 * 15.0 * NF)
+    inst0, sgal0 = wl.default_noise_params(T)
+    C6 = np.array([port.noise_covariance(T, (lmin + j) * df, 1, inst0, sgal0)[0] for j in range(Nl)]) / (NF * NT)
+    X, Y, Z = wl.wavelet_noise_data(rng, C6, NT)
+    mod = wl.galaxy_modulation_like(NT // Q)
+    engine.noise_wavelet_setup(NF, NT, df, lmin, Q, X, Y, Z, mod)
+    P = port.noise_coarse_stats(NT, Q, X, Y, Z)
+    inst = inst0 * np.exp(rng.uniform(-0.3, 0.3, (40, 12)))
+    sgal = sgal0 + rng.uniform(-0.2, 0.2, (40, 5))
+    for mode in (0, 1, 2):
+        got = engine.noise_wavelet_logl_host(inst, sgal, mode)
+        ref = port.noise_wavelet_logl(NF, NT, df, lmin, P, Q, inst, sgal, mode, mod if mode == 2 else None)
+        np.testing.assert_allclose(got, ref, rtol=REL)
+        np.testing.assert_allclose(got - got[0], ref - ref[0], atol=REL * abs(ref[0]))
+        di, dg = torch.tensor(inst, device="cuda"), torch.tensor(sgal, device="cuda")
+        dl = torch.empty(40, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        engine.noise_wavelet_logl_device(di, dl, dg, mode)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(dl.cpu().numpy(), got)
+
+
+def test_noise_wavelet_errors(engine):
+    with pytest.raises(gg.GlassError):
+        engine.noise_wavelet_setup(1024, 256, 1e-5, 10, 512, np.zeros(256), np.zeros(256), np.zeros(256))
+    engine.noise_wavelet_setup(1024, 256, 1e-5, 10, 8, np.ones(256), np.ones(256), np.ones(256))
+    with pytest.raises(gg.GlassError):  # the modulated foreground needs the modulation
+        engine.noise_wavelet_logl_host(np.ones((1, 12)), np.ones((1, 5)), mode=2)
