@@ -279,15 +279,15 @@ __device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, fl
   group_sync<GT>();
 }
 
-// One stage of fft_reg_smem over NSER series in rounds of 4 (one series per
-// M threads): rounds touch disjoint series, so a round's loads need no
+// One stage of fft_reg_smem over NSER series in rounds of GT/M (one series
+// per M threads): rounds touch disjoint series, so a round's loads need no
 // barrier after the previous round's stores, only one before its own stores.
 template <int N, int GT, int NSER, int R, int P>
 __device__ __forceinline__ void reg_stage_rounds(float2 *sbuf, const float2 *tw, int s, int t, float2 *v) {
-  constexpr int SN = pad16(N);
+  constexpr int SN = pad16(N), SPR = GT / (N / 16);
 #pragma unroll 1
-  for (int r = 0; r < NSER / 4; ++r) {
-    float2 *y = sbuf + (4 * r + s) * SN;
+  for (int r = 0; r < NSER / SPR; ++r) {
+    float2 *y = sbuf + (SPR * r + s) * SN;
     reg_stage_load<N, R, P>(y, tw, t, v);
     group_sync<GT>();
     reg_stage_store<N, R, P>(y, t, v);
@@ -295,12 +295,13 @@ __device__ __forceinline__ void reg_stage_rounds(float2 *sbuf, const float2 *tw,
   group_sync<GT>();
 }
 
-// As fft4_reg for NSER (a multiple of 4) series already in the padded
-// shared-memory layout (series stride pad16(N)), transformed in place.
+// As fft4_reg for NSER series already in the padded shared-memory layout
+// (series stride pad16(N)), transformed in place by GT threads: GT/M series
+// at a time (a multiple of 4 dividing NSER).
 template <int N, int GT, int NSER>
 __device__ __forceinline__ void fft_reg_smem(float2 *sbuf, const float2 *tw, int lane) {
   constexpr int M = N / 16;
-  static_assert(4 * M == GT && NSER % 4 == 0 && N >= 32 && N <= 4096, "fft_reg_smem shape");
+  static_assert(GT % (4 * M) == 0 && NSER % (GT / M) == 0 && N >= 32 && N <= 4096, "fft_reg_smem shape");
   const int s = lane / M, t = lane - (lane / M) * M;
   float2 v[16];
   reg_stage_rounds<N, GT, NSER, 16, 1>(sbuf, tw, s, t, v);

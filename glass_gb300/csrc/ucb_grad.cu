@@ -292,7 +292,11 @@ struct GradSpecArgs {
 
 template <int N>
 struct GradCfg {
-  static constexpr int GT = N / 4;
+  // N = 256: two samples and two bins per thread, at most 168 registers (three
+  // 128-thread groups per SM instead of four 64-thread ones, which the 205
+  // registers of the four-sample form allowed); other sizes four per thread
+  static constexpr int GT = N == 256 ? N / 2 : N / 4;
+  static constexpr int MINB = N == 256 ? 3 : 1;
   static constexpr int CTA = GT >= 64 ? GT : 128;
   static constexpr int GPC = CTA / GT;
   static constexpr int NACC = 8 + 36;  // gradient, Fisher upper triangle
@@ -307,7 +311,7 @@ struct GradCfg {
 // and reduced to the gradient and the Fisher matrix.  Nothing of size N
 // leaves the SM.
 template <int N>
-__global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecArgs a) {
+__global__ void __launch_bounds__(GradCfg<N>::CTA, GradCfg<N>::MINB) fd_gradspec_kernel(GradSpecArgs a) {
   using Cfg = GradCfg<N>;
   constexpr int GT = Cfg::GT, GPC = Cfg::GPC, NACC = Cfg::NACC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -331,9 +335,9 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     const int item = a.bin_list[sl];
     const ItemGrad &it = a.items[item];
     const int seg = it.m.seg, imin = it.m.imin;
-    // the 24 series, four samples per thread
+    // the 24 series, N/GT samples per thread
 #pragma unroll 1
-    for (int r = 0; r < 4; r++) {
+    for (int r = 0; r < N / GT; r++) {
       const int n = lane + GT * r;
       float2 accs[kGradSeries];
       grad_sample(a.K, it, a.mix[n], a.geo[n], accs);
@@ -360,7 +364,7 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
       return cadd(cmul(f[0], make_float2(gt.x, gt.y)), cmul(f[SN], make_float2(gt.z, gt.w)));
     };
 #pragma unroll 1
-    for (int r = 0; r < 4; r++) {
+    for (int r = 0; r < N / GT; r++) {
       const int k = lane + GT * r;
       const int m = (k + N / 2) & (N - 1);
       const int j = imin + m;
@@ -392,13 +396,15 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
         const float lr = ch ? wl.z : wl.x, li = ch ? wl.w : wl.y;
         const float rr = (wr - h.x) + lr, ri = (wi - h.y) + li;
         racc += fmaf(rr, rr, ri * ri);
+        // half of every sum (the factor 2 of (a|b) = 2 sum Re(a b*) is applied
+        // once at the end, where it is exact)
 #pragma unroll
-        for (int p = 0; p < 8; p++) accg[p] += 2.f * fmaf(rr, D[p].x, ri * D[p].y);
+        for (int p = 0; p < 8; p++) accg[p] = fmaf(rr, D[p].x, fmaf(ri, D[p].y, accg[p]));
         int q = 8;
 #pragma unroll
         for (int p = 0; p < 8; p++)
 #pragma unroll
-          for (int l = p; l < 8; l++, q++) accg[q] += 2.f * qw[ch] * fmaf(D[p].x, D[l].x, D[p].y * D[l].y);
+          for (int l = p; l < 8; l++, q++) accg[q] = fmaf(qw[ch], fmaf(D[p].x, D[l].x, D[p].y * D[l].y), accg[q]);
       }
     }
     // reduce over the group: per-thread partials in shared memory (reusing the
@@ -418,7 +424,7 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA) fd_gradspec_kernel(GradSpecAr
     group_sync<GT>();
     if (valid) {
       for (int q = lane; q < NACC; q += GT) {
-        const double v = (double)part[q * PS];
+        const double v = 2.0 * (double)part[q * PS];
         if (q < 8) {
           a.grad[8 * (size_t)item + q] = v;
         } else if (a.fisher) {
