@@ -47,6 +47,7 @@ EXPORTS = (
     "glass_gpu_fstat_batch", "glass_gpu_fstat_batch_host", "glass_gpu_fstat_proposal_host",
     "glass_gpu_noise_setup", "glass_gpu_noise_logl_batch", "glass_gpu_noise_logl_batch_host",
     "glass_gpu_noise_wavelet_setup", "glass_gpu_noise_wavelet_logl_batch", "glass_gpu_noise_wavelet_logl_batch_host",
+    "glass_gpu_dlogl_batch_channels", "glass_gpu_noise_eta_batch", "glass_gpu_noise_eta_batch_host",
 )
 
 _lib = None
@@ -116,6 +117,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                                                   ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]
     lib.glass_gpu_noise_wavelet_logl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V]
     lib.glass_gpu_noise_wavelet_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D]
+    lib.glass_gpu_dlogl_batch_channels.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 8
+    lib.glass_gpu_noise_eta_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 6
+    lib.glass_gpu_noise_eta_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D, _D, _I]
     _lib = lib
     return lib
 
@@ -436,6 +440,26 @@ class Engine:
     def noise_wavelet_logl_device(self, inst, logl, sgal=None, mode=0):
         n = int(inst.shape[0])
         _check(self.lib.glass_gpu_noise_wavelet_logl_batch(self._ctx, int(mode), n, _ptr(inst), _ptr(sgal), _ptr(logl)))
+
+    def dlogl_channels_device(self, item_seg, params, dlogl, term_ch, term_y=None, hh=None, status=None, term_x=None,
+                              precision=PREC_MIXED):
+        """glass_gpu_dlogl_batch with per-channel terms term_ch [n, 2] (device tensors)."""
+        n = int(item_seg.numel())
+        _check(self.lib.glass_gpu_dlogl_batch_channels(self._ctx, precision, n, _ptr(item_seg), _ptr(params),
+                                                       _ptr(term_x), _ptr(dlogl), _ptr(term_y), _ptr(hh),
+                                                       _ptr(status), _ptr(term_ch)))
+
+    def noise_eta_host(self, item_seg, params, eta_x, eta_y, precision=PREC_MIXED):
+        """(logL + logLnorm)(eta_y) - (logL + logLnorm)(eta_x) per chain, and status."""
+        seg = np.ascontiguousarray(item_seg, np.int32)
+        p = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        ex = np.ascontiguousarray(eta_x, np.float64).reshape(-1, 2)
+        ey = np.ascontiguousarray(eta_y, np.float64).reshape(-1, 2)
+        n = len(seg)
+        out, st = np.empty(n), np.empty(n, np.int32)
+        _check(self.lib.glass_gpu_noise_eta_batch_host(self._ctx, precision, n, _pi(seg), _pd(p), _pd(ex), _pd(ey),
+                                                       _pd(out), _pi(st)))
+        return out, st
 
     def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                              precision=PREC_FP64):

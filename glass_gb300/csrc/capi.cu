@@ -82,6 +82,8 @@ struct glass_gpu_ctx {
   FsWorkDev fsw;  // F-statistic scratch
   NoiseDev noise;  // noise-model likelihood: per-bin table and chunk sums
   NoiseWvDev noise_wv;  // the same in the wavelet domain
+  double *eta_scratch = nullptr;  // glass_gpu_noise_eta_batch: 5 doubles per chain
+  size_t eta_cap = 0;
 };
 
 static void clear_host_graphs(glass_gpu_ctx *ctx) {
@@ -153,6 +155,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->noise.partial);
   cudaFree(ctx->noise_wv.mem);
   cudaFree(ctx->noise_wv.partial);
+  cudaFree(ctx->eta_scratch);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
@@ -227,11 +230,11 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   if (rc) return rc;
   const size_t nb = (size_t)nseg * NFFT;
   std::vector<float4> w32(nb), w32lo(nb), g32(2 * nb);
-  std::vector<double> Q((size_t)nseg * (NFFT + 1));
+  std::vector<double> Q((size_t)nseg * (NFFT + 1)), QA((size_t)nseg * (NFFT + 1));
   std::vector<double2> w64(2 * nb), g64(4 * nb);
   const double fstar = fstar_of_orbit();
   fd_build_bank_tables(format, T, fstar, NFFT, nseg, qmin, rA, rE, invCA, invCE, w32.data(), w32lo.data(),
-                       g32.data(), Q.data(), w64.data(), g64.data());
+                       g32.data(), Q.data(), w64.data(), g64.data(), QA.data());
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "bank_upload sync");
   clear_host_graphs(ctx);
   cudaFree(ctx->bank_mem);
@@ -245,7 +248,8 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   size_t off_g64 = off_w64 + sizeof(double2) * w64.size();
   size_t off_invc = off_g64 + sizeof(double2) * g64.size();
   size_t off_rho = (off_invc + sizeof(float2) * nb + 255) / 256 * 256;
-  size_t total = off_rho + sizeof(double) * nb;
+  size_t off_qa = off_rho + sizeof(double) * nb;
+  size_t total = off_qa + sizeof(double) * QA.size();
   GLASS_CUDA(cudaMalloc(&ctx->bank_mem, total), "cudaMalloc(bank)");
   char *base = (char *)ctx->bank_mem;
   FdBankDev &b = ctx->bank;
@@ -264,8 +268,10 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   b.g64 = (double2 *)(base + off_g64);
   b.invc = (float2 *)(base + off_invc);
   b.rho = (double *)(base + off_rho);
+  b.QA = (double *)(base + off_qa);
   GLASS_CUDA(cudaMemcpy(b.qmin, qmin, sizeof(int) * nseg, cudaMemcpyHostToDevice), "upload qmin");
   GLASS_CUDA(cudaMemcpy(b.Q, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice), "upload Q");
+  GLASS_CUDA(cudaMemcpy(b.QA, QA.data(), sizeof(double) * QA.size(), cudaMemcpyHostToDevice), "upload QA");
   GLASS_CUDA(cudaMemcpy(b.w32, w32.data(), sizeof(float4) * w32.size(), cudaMemcpyHostToDevice), "upload w32");
   GLASS_CUDA(cudaMemcpy(b.w32lo, w32lo.data(), sizeof(float4) * w32lo.size(), cudaMemcpyHostToDevice), "upload w32lo");
   GLASS_CUDA(cudaMemcpy(b.g32, g32.data(), sizeof(float4) * g32.size(), cudaMemcpyHostToDevice), "upload g32");
@@ -307,11 +313,11 @@ extern "C" int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const do
   if (rc) return rc;
   const int NFFT = b.NFFT;
   std::vector<float4> w32(NFFT), w32lo(NFFT), g32(2 * NFFT);
-  std::vector<double> Q(NFFT + 1);
+  std::vector<double> Q(NFFT + 1), QA(NFFT + 1);
   std::vector<double2> w64(2 * NFFT), g64(4 * NFFT);
   fd_build_bank_tables(b.format, b.T, b.fstar, NFFT, 1, &ctx->h_qmin[seg], rA, rE,
                        ctx->h_invCA.data() + (size_t)seg * NFFT, ctx->h_invCE.data() + (size_t)seg * NFFT,
-                       w32.data(), w32lo.data(), g32.data(), Q.data(), w64.data(), g64.data());
+                       w32.data(), w32lo.data(), g32.data(), Q.data(), w64.data(), g64.data(), QA.data());
   size_t sj = (size_t)seg * NFFT;
   GLASS_CUDA(cudaMemcpyAsync(b.w32 + sj, w32.data(), sizeof(float4) * NFFT, cudaMemcpyHostToDevice, ctx->stream),
              "residual w32");
@@ -319,6 +325,8 @@ extern "C" int glass_gpu_bank_set_residual(glass_gpu_ctx *ctx, int seg, const do
              "residual w32lo");
   GLASS_CUDA(cudaMemcpyAsync(b.Q + (size_t)seg * (NFFT + 1), Q.data(), sizeof(double) * (NFFT + 1),
                              cudaMemcpyHostToDevice, ctx->stream), "residual Q");
+  GLASS_CUDA(cudaMemcpyAsync(b.QA + (size_t)seg * (NFFT + 1), QA.data(), sizeof(double) * (NFFT + 1),
+                             cudaMemcpyHostToDevice, ctx->stream), "residual QA");
   GLASS_CUDA(cudaMemcpyAsync(b.w64 + 2 * sj, w64.data(), sizeof(double2) * 2 * NFFT, cudaMemcpyHostToDevice,
                              ctx->stream), "residual w64");
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "residual sync");
@@ -390,6 +398,28 @@ extern "C" int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nite
                                   term_y, hh, status, ctx->n_fixed, ctx->num_sms, ctx->stream, &nl);
   ctx->last_launches = nl;
   if (e != cudaSuccess) return cuda_err(e, "dlogl_batch launch");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_dlogl_batch_channels(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
+                                              const double *params, const double *term_x, double *dlogl,
+                                              double *term_y, double *hh, int *status, double *term_ch) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "dlogl_batch_channels: null context");
+  if (nitems < 0) return set_err(GLASS_ERR_ARG, "dlogl_batch_channels: negative item count");
+  if (nitems == 0) return GLASS_OK;
+  if (!item_seg || !params || !dlogl || !term_ch) return set_err(GLASS_ERR_ARG, "dlogl_batch_channels: null argument");
+  if (precision != GLASS_PREC_FP64 && precision != GLASS_PREC_MIXED)
+    return set_err(GLASS_ERR_ARG, "dlogl_batch_channels: unknown precision");
+  if (!ctx->bank.nseg) return set_err(GLASS_ERR_STATE, "dlogl_batch_channels: no segment bank uploaded");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_work(ctx, nitems))) return rc;
+  if (ctx->n_fixed > ctx->bank.NFFT) return set_err(GLASS_ERR_SIZE, "dlogl_batch_channels: template size above NFFT");
+  int nl = 0;
+  cudaError_t e = fd_dlogl_launch(ctx->bank, ctx->tab, ctx->work, precision, nitems, item_seg, params, term_x, dlogl,
+                                  term_y, hh, status, ctx->n_fixed, ctx->num_sms, ctx->stream, &nl, term_ch);
+  ctx->last_launches = nl;
+  if (e != cudaSuccess) return cuda_err(e, "dlogl_batch_channels launch");
   return GLASS_OK;
 }
 
@@ -728,6 +758,97 @@ extern "C" int glass_gpu_fstat_proposal_host(glass_gpu_ctx *ctx, int seg, int n_
   info[1] = norm;
   info[2] = maxp;
   info[3] = nact;
+  return GLASS_OK;
+}
+
+// --------------------------------------------- the UCB sampler's noise step
+// noise_model_mcmc (ucb/src/glass_ucb_sampler.c:29-73) scales each channel's
+// noise by eta (generate_noise_model, ucb/src/glass_ucb_model.c:336-346) and
+// compares (logL + logLnorm) at eta_y with eta_x for the chain's unchanged
+// residual r = d - h: logL = -sum |r|^2 / (C eta') per channel
+// (gaussian_log_likelihood, utils/src/glass_model.c:726-774, with
+// eta' = sqrt(eta eta) as :342 forms it) and logLnorm = -sum log(C eta')
+// (:788-803).  With S_c = sum |r_c|^2 / C_c over the segment (the bank's
+// residual power Q minus the chain template's per-channel term):
+//   d = -S_A (1/eta'_yA - 1/eta'_xA) - S_E (1/eta'_yE - 1/eta'_xE)
+//       - NFFT (log eta'_yA - log eta'_xA + log eta'_yE - log eta'_xE).
+__global__ void noise_eta_kernel(int n, const int *item_seg, const double *term_ch, const double *Q, const double *QA,
+                                 int NFFT, int nseg, const double *eta_x, const double *eta_y, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int seg = item_seg[i];
+  if (seg < 0 || seg >= nseg) {
+    out[i] = __longlong_as_double(0x7ff8000000000000ULL);
+    return;
+  }
+  const size_t e = (size_t)seg * (NFFT + 1) + NFFT;
+  const double qa = QA[e], qe = Q[e] - QA[e];
+  const double SA = qa - term_ch[2 * (size_t)i], SE = qe - term_ch[2 * (size_t)i + 1];
+  const double xa = sqrt(eta_x[2 * i] * eta_x[2 * i]), xe = sqrt(eta_x[2 * i + 1] * eta_x[2 * i + 1]);
+  const double ya = sqrt(eta_y[2 * i] * eta_y[2 * i]), ye = sqrt(eta_y[2 * i + 1] * eta_y[2 * i + 1]);
+  const double dl = -(SA / ya - SA / xa) - (SE / ye - SE / xe);
+  const double dn = -(double)NFFT * ((log(ya) - log(xa)) + (log(ye) - log(xe)));
+  out[i] = dl + dn;
+}
+
+extern "C" int glass_gpu_noise_eta_batch(glass_gpu_ctx *ctx, int precision, int n, const int *item_seg,
+                                         const double *params, const double *eta_x, const double *eta_y,
+                                         double *dlogl_noise, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_eta_batch: null context");
+  if (n < 0) return set_err(GLASS_ERR_ARG, "noise_eta_batch: negative chain count");
+  if (n == 0) return GLASS_OK;
+  if (!item_seg || !params || !eta_x || !eta_y || !dlogl_noise) return set_err(GLASS_ERR_ARG, "noise_eta_batch: null argument");
+  if (!ctx->bank.nseg) return set_err(GLASS_ERR_STATE, "noise_eta_batch: no segment bank uploaded");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  // scratch: dlogl, term_y, hh, term_ch (2 per chain)
+  const size_t nd = (size_t)n;
+  if (ctx->eta_cap < nd) {
+    GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "noise eta scratch sync");
+    cudaFree(ctx->eta_scratch);
+    ctx->eta_scratch = nullptr;
+    ctx->eta_cap = 0;
+    GLASS_CUDA(cudaMalloc(&ctx->eta_scratch, sizeof(double) * nd * 5), "cudaMalloc(noise eta scratch)");
+    ctx->eta_cap = nd;
+  }
+  double *scratch = ctx->eta_scratch;
+  rc = glass_gpu_dlogl_batch_channels(ctx, precision, n, item_seg, params, nullptr, scratch, scratch + nd,
+                                      scratch + 2 * nd, status, scratch + 3 * nd);
+  if (rc == GLASS_OK) {
+    noise_eta_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, item_seg, scratch + 3 * nd, ctx->bank.Q,
+                                                                ctx->bank.QA, ctx->bank.NFFT, ctx->bank.nseg, eta_x,
+                                                                eta_y, dlogl_noise);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_err(e, "noise_eta_kernel");
+    else ctx->last_launches += 1;
+  }
+  return rc;
+}
+
+extern "C" int glass_gpu_noise_eta_batch_host(glass_gpu_ctx *ctx, int precision, int n, const int *item_seg,
+                                              const double *params, const double *eta_x, const double *eta_y,
+                                              double *dlogl_noise, int *status) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_eta_batch_host: null context");
+  if (n < 0) return set_err(GLASS_ERR_ARG, "noise_eta_batch_host: negative chain count");
+  if (n == 0) return GLASS_OK;
+  if (!item_seg || !params || !eta_x || !eta_y || !dlogl_noise)
+    return set_err(GLASS_ERR_ARG, "noise_eta_batch_host: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t nd = (size_t)n;
+  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (8 + 2 + 2 + 1) + sizeof(int) * nd * 2 + 256))) return rc;
+  double *d_params = (double *)ctx->d_stage, *d_ex = d_params + 8 * nd, *d_ey = d_ex + 2 * nd, *d_out = d_ey + 2 * nd;
+  int *d_seg = (int *)(d_out + nd), *d_st = d_seg + nd;
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d_params, params, sizeof(double) * 8 * nd, cudaMemcpyHostToDevice, s), "H2D params");
+  GLASS_CUDA(cudaMemcpyAsync(d_ex, eta_x, sizeof(double) * 2 * nd, cudaMemcpyHostToDevice, s), "H2D eta_x");
+  GLASS_CUDA(cudaMemcpyAsync(d_ey, eta_y, sizeof(double) * 2 * nd, cudaMemcpyHostToDevice, s), "H2D eta_y");
+  GLASS_CUDA(cudaMemcpyAsync(d_seg, item_seg, sizeof(int) * nd, cudaMemcpyHostToDevice, s), "H2D item_seg");
+  rc = glass_gpu_noise_eta_batch(ctx, precision, n, d_seg, d_params, d_ex, d_ey, d_out, d_st);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(dlogl_noise, d_out, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H dlogl_noise");
+  if (status) GLASS_CUDA(cudaMemcpyAsync(status, d_st, sizeof(int) * nd, cudaMemcpyDeviceToHost, s), "D2H status");
+  GLASS_CUDA(cudaStreamSynchronize(s), "noise_eta_batch_host sync");
   return GLASS_OK;
 }
 

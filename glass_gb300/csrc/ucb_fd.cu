@@ -34,10 +34,10 @@ namespace glass {
 
 cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
-cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
-cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
-cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream);
-cudaError_t fd_launch_spec_all_fp64(const SpecAllArgs &A, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
+cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
+cudaError_t fd_launch_spec_all_fp64(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
 
 // ------------------------------------------------------------- plan kernels
 // Plain-FP64 plan: ucb_bandwidth, ucb_alignment and the per-proposal constants
@@ -343,11 +343,12 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
 // ---------------------------------------------------------- host: bank tables
 void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
                           const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *w32lo,
-                          float4 *g32, double *Q, double2 *w64, double2 *g64) {
+                          float4 *g32, double *Q, double2 *w64, double2 *g64, double *QA) {
   const double sqT = sqrt(T);
   for (int s = 0; s < nseg; s++) {
-    double q = 0.0;
+    double q = 0.0, qa = 0.0;
     Q[(size_t)s * (NFFT + 1)] = 0.0;
+    if (QA) QA[(size_t)s * (NFFT + 1)] = 0.0;
     for (int j = 0; j < NFFT; j++) {
       size_t sj = (size_t)s * NFFT + j;
       double f = (double)(qmin[s] + j) / T;
@@ -389,6 +390,10 @@ void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg
       g32[2 * sj + 1] = make_float4((float)GE2r, (float)GE2i, (float)GE1r, (float)GE1i);
       q += wAr * wAr + wAi * wAi + wEr * wEr + wEi * wEi;
       Q[(size_t)s * (NFFT + 1) + j + 1] = q;
+      if (QA) {
+        qa += wAr * wAr + wAi * wAi;
+        QA[(size_t)s * (NFFT + 1) + j + 1] = qa;
+      }
     }
   }
 }
@@ -397,7 +402,7 @@ void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg
 cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int precision,
                             int nitems, const int *item_seg, const double *params, const double *term_x,
                             double *dlogl, double *term_y, double *hh, int *status, int n_fixed, int num_sms,
-                            cudaStream_t stream, int *nlaunch) {
+                            cudaStream_t stream, int *nlaunch, double *term_ch) {
   cudaError_t e;
   int launches = 0;
   const bool mix = precision == 1;
@@ -485,6 +490,9 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.term_y = term_y;
   a.hh = hh;
   a.status = status;
+  a.term_ch = term_ch;
+  a.QA = bank.QA;
+  const bool perch = term_ch != nullptr;
   // sizes up to 1024 (every size a segment of NFFT bins can produce, up to
   // NFFT: ucb_bandwidth caps N there) in one launch on the main stream; 2048
   // and 4096 as their own kernels on side streams running beside it
@@ -501,7 +509,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
       a.bin = b;
       a.bin_list = work.bin_list + (size_t)b * work.cap;
       a.tw = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
-      e = mix ? fd_launch_spec_mixed(N, a, nitems, num_sms, sb) : fd_launch_spec_fp64(N, a, nitems, num_sms, sb);
+      e = mix ? fd_launch_spec_mixed(N, a, nitems, num_sms, sb, perch)
+              : fd_launch_spec_fp64(N, a, nitems, num_sms, sb, perch);
       launches++;
       if (e != cudaSuccess) return e;
       if ((e = cudaEventRecord(work.join[b], sb)) != cudaSuccess) return e;
@@ -517,7 +526,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.nbins = nall;
     A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
     for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
-    e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream) : fd_launch_spec_all_fp64(A, num_sms, stream);
+    e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch) : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
     launches++;
     if (e != cudaSuccess) return e;
   }

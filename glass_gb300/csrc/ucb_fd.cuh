@@ -16,6 +16,7 @@ struct FdBankDev {
   float4 *w32lo = nullptr;     // [nseg*NFFT]   residual minus its float rounding (double-float pair with w32)
   float4 *g32 = nullptr;       // [nseg*NFFT*2] {GA2, GA1}, {GE2, GE1}
   double *Q = nullptr;         // [nseg*(NFFT+1)] prefix sums of |w|^2 over both channels (FP64)
+  double *QA = nullptr;        // [nseg*(NFFT+1)] the same for the A channel alone
   double2 *w64 = nullptr;      // [nseg*NFFT*2] {A}, {E}
   double2 *g64 = nullptr;      // [nseg*NFFT*4] GA2, GA1, GE2, GE1
   float2 *invc = nullptr;      // [nseg*NFFT] invC_A, invC_E over their value at the segment's bin 0
@@ -62,7 +63,7 @@ struct FdWorkDev {
 // Host-side table construction for a bank: G and w tables, prefix sums.
 void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
                           const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *w32lo,
-                          float4 *g32, double *Q, double2 *w64, double2 *g64);
+                          float4 *g32, double *Q, double2 *w64, double2 *g64, double *QA = nullptr);
 
 cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStream_t stream);
 
@@ -71,7 +72,7 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
 cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWorkDev &work, int precision,
                             int nitems, const int *item_seg, const double *params, const double *term_x,
                             double *dlogl, double *term_y, double *hh, int *status, int n_fixed, int num_sms,
-                            cudaStream_t stream, int *nlaunch);
+                            cudaStream_t stream, int *nlaunch, double *term_ch = nullptr);
 
 // Bytes of series scratch a batch of nitems proposals on segments of NFFT bins
 // can need (every N is at most NFFT).

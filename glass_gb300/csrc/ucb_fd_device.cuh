@@ -887,6 +887,10 @@ struct SpecArgs {
   const double *term_x;
   double *dlogl, *term_y, *hh;
   int *status;
+  // per-channel form (the PERCH kernels): term_ch[2 i + c] is channel c's
+  // share of term_y (c = 0 A, 1 E); QA the A channel's part of Q
+  double *term_ch = nullptr;
+  const double *QA = nullptr;
 };
 
 // Start (in samples) of size bin `bin` in the scratch series: sizes are laid
@@ -1012,7 +1016,7 @@ __device__ __forceinline__ df group_sum_df(float v, float2 *red, int lane) {
 // (from the slow kernel's scratch) are FFT'd in shared memory, weighted per bin
 // by the segment's TDI/whitening table and reduced to the residual power.
 // reds: 96 doubles of reduction scratch per group.
-template <int N, bool MIX, int GPC>
+template <int N, bool MIX, int GPC, bool PERCH = false>
 __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list, int count, int base,
                                           const typename SpecSmem<N, MIX>::C *series,
                                           const typename SpecSmem<N, MIX>::C *tw,
@@ -1042,6 +1046,8 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   const C *src = series + (size_t)sl * 4 * N;
   float facc = 0.f, fh = 0.f, fc = 0.f;  // mixed: per-thread partial sums
   double acc = 0.0, hacc = 0.0;
+  float faccE = 0.f, fcE = 0.f;  // PERCH: the E channel's shares (facc, fc then hold A's)
+  double accE = 0.0;
 #pragma unroll 1
   for (int pass = 0; pass < PASSES; ++pass) {
     if constexpr (MIX) {
@@ -1074,9 +1080,16 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
         const float4 wl = a.w32lo[sj];
         const float ar = (w.x - hA.x) + wl.x, ai = (w.y - hA.y) + wl.y;
         const float er = (w.z - hE.x) + wl.z, ei = (w.w - hE.y) + wl.w;
-        facc += fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei);
+        if constexpr (PERCH) {
+          facc += fmaf(ar, ar, ai * ai);
+          faccE += fmaf(er, er, ei * ei);
+          fc += fmaf(ar, hA.x, ai * hA.y);
+          fcE += fmaf(er, hE.x, ei * hE.y);
+        } else {
+          facc += fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei);
+          fc += fmaf(ar, hA.x, ai * hA.y) + fmaf(er, hE.x, ei * hE.y);
+        }
         fh += fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y);
-        fc += fmaf(ar, hA.x, ai * hA.y) + fmaf(er, hE.x, ei * hE.y);
       } else {
         const double s = a.items64[item].amp_s;
         // series (2 ch, 2 ch + 1) of this pass hold the A (chan 0) or E (chan 1) pair
@@ -1087,22 +1100,30 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
           const double2 g2 = a.g64[4 * sj + 2 * chan], g1 = a.g64[4 * sj + 2 * chan + 1];
           double2 h = cadd(cmul(buf[(2 * ch) * N + k], g2), cmul(buf[(2 * ch + 1) * N + k], g1));
           h = cscale(h, s);
-          acc += 2.0 * (w.x * h.x + w.y * h.y) - (h.x * h.x + h.y * h.y);
+          if (PERCH && chan == 1)
+            accE += 2.0 * (w.x * h.x + w.y * h.y) - (h.x * h.x + h.y * h.y);
+          else
+            acc += 2.0 * (w.x * h.x + w.y * h.y) - (h.x * h.x + h.y * h.y);
           hacc += h.x * h.x + h.y * h.y;
         }
       }
     }
     group_sync<GT>();
   }
-  df sa, sh, sc;
+  df sa, sh, sc, saE, scE;
   if constexpr (MIX) {
     float2 *redf = reinterpret_cast<float2 *>(red);
     sa = group_sum_df<GT>(facc, redf, lane);
     sh = group_sum_df<GT>(fh, redf + 32, lane);
     sc = group_sum_df<GT>(fc, redf + 64, lane);
+    if constexpr (PERCH) {
+      saE = group_sum_df<GT>(faccE, redf, lane);
+      scE = group_sum_df<GT>(fcE, redf + 32, lane);
+    }
   } else {
     acc = group_sum<GT>(acc, red, lane);
     hacc = group_sum<GT>(hacc, red + 32, lane);
+    if constexpr (PERCH) accE = group_sum<GT>(accE, red + 64, lane);
   }
   if (valid && lane == 0) {
     double term, hh;
@@ -1118,10 +1139,27 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       // |rho| < 6e-8, so the correction and (1 + rho)^2 are FP32 to spare
       const float rho = __fdiv_rn(c.amp_lo, c.amp_hi);
       const df tail = df_add(df_neg(sa), df{2.f * rho * sc.hi, 0.f});
-      term = ((Qs[jhi] - Qs[jlo]) + (double)tail.hi) + (double)tail.lo;
+      if constexpr (PERCH) {
+        const double *QAs = a.QA + (size_t)seg * (NFFT + 1);
+        const df tailE = df_add(df_neg(saE), df{2.f * rho * scE.hi, 0.f});
+        const double qa = QAs[jhi] - QAs[jlo];
+        const double tA = (qa + (double)tail.hi) + (double)tail.lo;
+        const double tE = (((Qs[jhi] - Qs[jlo]) - qa) + (double)tailE.hi) + (double)tailE.lo;
+        a.term_ch[2 * (size_t)item] = tA;
+        a.term_ch[2 * (size_t)item + 1] = tE;
+        term = tA + tE;
+      } else {
+        term = ((Qs[jhi] - Qs[jlo]) + (double)tail.hi) + (double)tail.lo;
+      }
       hh = (double)(2.f * (1.f + rho) * (1.f + rho) * (sh.hi + sh.lo));
     } else {
-      term = acc;
+      if constexpr (PERCH) {
+        a.term_ch[2 * (size_t)item] = acc;
+        a.term_ch[2 * (size_t)item + 1] = accE;
+        term = acc + accE;
+      } else {
+        term = acc;
+      }
       hh = 2.0 * hacc;
     }
     const double tx = a.term_x ? a.term_x[item] : 0.0;
@@ -1133,7 +1171,7 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   if constexpr (GT > 32) __syncthreads();
 }
 
-template <int N, bool MIX>
+template <int N, bool MIX, bool PERCH = false>
 __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   using Cfg = SpecCfg<N>;
   using S = SpecSmem<N, MIX>;
@@ -1151,7 +1189,7 @@ __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   const int count = a.bin_count[a.bin];
   const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, a.bin) * 4;
   for (int base = blockIdx.x * GPC; base < count; base += gridDim.x * GPC)
-    spec_unit<N, MIX, GPC>(a, a.bin_list, count, base, series, tw, bufs, red);
+    spec_unit<N, MIX, GPC, PERCH>(a, a.bin_list, count, base, series, tw, bufs, red);
 }
 
 // All sizes up to 1024 in one launch: a persistent grid of 256-thread CTAs
@@ -1177,7 +1215,7 @@ struct SpecAllArgs {
                                  // counts there and the done counter after them
 };
 
-template <bool MIX>
+template <bool MIX, bool PERCH = false>
 __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAllArgs A) {
   using C = typename SpecAllSmem<MIX>::C;
   const SpecArgs &a = A.a;
@@ -1219,12 +1257,12 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
     const int *bl = a.bin_list + (size_t)b * a.cap;
     const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, b) * 4;
     switch (b) {
-      case 0: spec_unit<32, MIX, 32>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 1: spec_unit<64, MIX, 16>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 2: spec_unit<128, MIX, 8>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 3: spec_unit<256, MIX, 4>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 4: spec_unit<512, MIX, 2>(a, bl, count, base, series, tw, bufs, reds); break;
-      default: spec_unit<1024, MIX, 1>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 0: spec_unit<32, MIX, 32, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 1: spec_unit<64, MIX, 16, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 2: spec_unit<128, MIX, 8, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 3: spec_unit<256, MIX, 4, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 4: spec_unit<512, MIX, 2, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      default: spec_unit<1024, MIX, 1, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
     }
   }
   if (A.zero_counts) {
@@ -1242,34 +1280,34 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
   }
 }
 
-template <bool MIX>
+template <bool MIX, bool PERCH = false>
 static cudaError_t launch_spec_all(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
   const size_t smem = SpecAllSmem<MIX>::bytes;
   static int occ = -1;
   if (occ < 0) {
-    cudaError_t e =
-        cudaFuncSetAttribute(fd_spec_all_kernel<MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(fd_spec_all_kernel<MIX, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_all_kernel<MIX>, kSpecAllThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_all_kernel<MIX, PERCH>, kSpecAllThreads, smem);
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
   }
-  fd_spec_all_kernel<MIX><<<occ * num_sms, kSpecAllThreads, smem, stream>>>(A);
+  fd_spec_all_kernel<MIX, PERCH><<<occ * num_sms, kSpecAllThreads, smem, stream>>>(A);
   return cudaGetLastError();
 }
 
 // Launch of one size's kernel with a grid bounded by the SM count times the
 // occupancy of the kernel.
-template <int N, bool MIX>
+template <int N, bool MIX, bool PERCH = false>
 static cudaError_t launch_spec(const SpecArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
   using Cfg = SpecCfg<N>;
   size_t smem = SpecSmem<N, MIX>::bytes;
   static int occ = -1;
   if (occ < 0) {
-    cudaError_t e = cudaFuncSetAttribute(fd_spec_kernel<N, MIX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(fd_spec_kernel<N, MIX, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_kernel<N, MIX>, Cfg::CTA, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_kernel<N, MIX, PERCH>, Cfg::CTA, smem);
     if (e != cudaSuccess) return e;
     if (occ < 1) occ = 1;
   }
@@ -1277,7 +1315,7 @@ static cudaError_t launch_spec(const SpecArgs &a, int nitems_bound, int num_sms,
   int grid = occ * num_sms;
   if (need < grid) grid = need;
   if (grid < 1) grid = 1;
-  fd_spec_kernel<N, MIX><<<grid, Cfg::CTA, smem, stream>>>(a);
+  fd_spec_kernel<N, MIX, PERCH><<<grid, Cfg::CTA, smem, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -7,7 +7,15 @@ cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t st
   return launch_slow<true>(a, num_sms, stream);
 }
 
-cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream) {
+cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream,
+                                bool perch) {
+  if (perch) {
+    switch (N) {
+      case 2048: return launch_spec<2048, true, true>(a, nitems, num_sms, stream);
+      case 4096: return launch_spec<4096, true, true>(a, nitems, num_sms, stream);
+    }
+    return cudaErrorInvalidValue;
+  }
   switch (N) {
     case 32: return launch_spec<32, true>(a, nitems, num_sms, stream);
     case 64: return launch_spec<64, true>(a, nitems, num_sms, stream);
@@ -21,7 +29,8 @@ cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_s
   return cudaErrorInvalidValue;
 }
 
-cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch) {
+  if (perch) return launch_spec_all<true, true>(A, num_sms, stream);
   return launch_spec_all<true>(A, num_sms, stream);
 }
 

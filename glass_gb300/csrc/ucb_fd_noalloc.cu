@@ -25,7 +25,7 @@
 namespace glass {
 
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
-cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_plan64(const PlanArgs &a, cudaStream_t stream);
 
 namespace {
@@ -233,7 +233,7 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
     a.bin = b;
     a.bin_list = na->bin_list + (size_t)b * kNaMaxItems;
     a.tw = tab.tw64[b];
-    if (fd_launch_spec_fp64(N, a, nitems, na->num_sms, s) != cudaSuccess) return GLASS_ERR_CUDA;
+    if (fd_launch_spec_fp64(N, a, nitems, na->num_sms, s, false) != cudaSuccess) return GLASS_ERR_CUDA;
   }
   return GLASS_OK;
 }

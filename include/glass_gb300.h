@@ -262,6 +262,31 @@ int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, int nprop, 
 int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
                                             const double *sgal, double *logl);
 
+/* glass_gpu_dlogl_batch with each channel's share of term_y as well:
+ * term_ch[2 i] (A) + term_ch[2 i + 1] (E) = term_y[i].  Device pointers. */
+int glass_gpu_dlogl_batch_channels(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
+                                   const double *params, const double *term_x, double *dlogl, double *term_y,
+                                   double *hh, int *status, double *term_ch);
+
+/*
+ * The UCB sampler's noise step (noise_model_mcmc, ucb/src/glass_ucb_sampler.c:29-73,
+ * Fourier basis, A/E): for chain i whose model on segment item_seg[i] is the
+ * bank's residual minus the template of params[8 i ..], the change of
+ * logL + logLnorm when each channel's noise level moves from eta_x[2 i + c] to
+ * eta_y[2 i + c] (c = 0 A, 1 E) with the residual unchanged
+ * (generate_noise_model, ucb/src/glass_ucb_model.c:336; gaussian_log_likelihood
+ * and gaussian_log_likelihood_model_norm, utils/src/glass_model.c:726, :788):
+ *   dlogl_noise[i] = (logL + logLnorm)(eta_y) - (logL + logLnorm)(eta_x).
+ * The sampler divides by the temperature and adds the prior as before.  The
+ * template's per-channel power comes from the batched path in `precision`.
+ * Device pointers, asynchronous; the _host form synchronises.
+ */
+int glass_gpu_noise_eta_batch(glass_gpu_ctx *ctx, int precision, int n, const int *item_seg, const double *params,
+                              const double *eta_x, const double *eta_y, double *dlogl_noise, int *status);
+int glass_gpu_noise_eta_batch_host(glass_gpu_ctx *ctx, int precision, int n, const int *item_seg,
+                                   const double *params, const double *eta_x, const double *eta_y,
+                                   double *dlogl_noise, int *status);
+
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 

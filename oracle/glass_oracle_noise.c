@@ -343,3 +343,37 @@ void orc_noise_wavelet_logl_batch(int NF, int NT, double df, int lmin, int Nlaye
         logl[p] = orc_noise_wavelet_logl(NF, NT, df, lmin, Nlayer, Q, P, mode, mod, inst + 12 * (size_t)p,
                                          sgal ? sgal + 5 * (size_t)p : NULL);
 }
+
+/* ------------------------------------------------ the UCB sampler's noise step */
+
+/*
+ * noise_model_mcmc's likelihood change (ucb/src/glass_ucb_sampler.c:29-73,
+ * Fourier, two channels) for a chain whose residual is r = data - model:
+ * each channel's covariance C = 1/invC scaled by sqrt(eta eta)
+ * (generate_noise_model, ucb/src/glass_ucb_model.c:336-346), inverted and its
+ * log-determinant taken (utils/src/glass_math.c:253-257), then
+ * logL = -fourier_nwip(r, r, invC')/2 per channel (gaussian_log_likelihood,
+ * utils/src/glass_model.c:726-774) and logLnorm = -sum logdetC
+ * (:788-803).  Returns (logL + logLnorm)(eta_y) - (logL + logLnorm)(eta_x).
+ * rA, rE: 2 NFFT doubles.
+ */
+double orc_noise_eta_delta(int NFFT, const double *rA, const double *rE, const double *invCA, const double *invCE,
+                           const double *eta_x, const double *eta_y)
+{
+    double tot[2];
+    for (int w = 0; w < 2; w++) {
+        const double *eta = w ? eta_y : eta_x;
+        double ca = 0.0, ce = 0.0, norm = 0.0;
+        for (int n = 0; n < NFFT; n++) {
+            double CA = (1.0 / invCA[n]) * sqrt(eta[0] * eta[0]);
+            double CE = (1.0 / invCE[n]) * sqrt(eta[1] * eta[1]);
+            norm -= log(CA) + log(CE);
+            double iA = 1. / CA, iE = 1. / CE;
+            ca += (rA[2 * n] * rA[2 * n] + rA[2 * n + 1] * rA[2 * n + 1]) * iA;
+            ce += (rE[2 * n] * rE[2 * n] + rE[2 * n + 1] * rE[2 * n + 1]) * iE;
+        }
+        double chi2 = 2.0 * ca + 2.0 * ce;
+        tot[w] = -0.5 * chi2 + norm;
+    }
+    return tot[1] - tot[0];
+}

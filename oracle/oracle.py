@@ -239,6 +239,16 @@ class Port:
         lib.orc_noise_coarse_stats(NT, Nlayer, Q, _p(X), _p(Y), _p(Z), _p(P))
         return P
 
+    def noise_eta_delta(self, rA, rE, invCA, invCE, eta_x, eta_y):
+        """noise_model_mcmc's (logL + logLnorm)(eta_y) - (.)(eta_x) for one residual."""
+        lib = self.lib
+        lib.orc_noise_eta_delta.restype = ctypes.c_double
+        lib.orc_noise_eta_delta.argtypes = [ctypes.c_int, _D, _D, _D, _D, _D, _D]
+        rA, rE, invCA, invCE = (np.ascontiguousarray(a, np.float64) for a in (rA, rE, invCA, invCE))
+        ex = np.ascontiguousarray(eta_x, np.float64)
+        ey = np.ascontiguousarray(eta_y, np.float64)
+        return lib.orc_noise_eta_delta(len(invCA), _p(rA), _p(rE), _p(invCA), _p(invCE), _p(ex), _p(ey))
+
     def orbit(self, t):
         out = np.zeros(9)
         self.lib.orc_orbit_positions(float(t), _p(out))
@@ -567,3 +577,15 @@ class Ref:
                                    _p(md) if md is not None else None, len(inst), _p(inst),
                                    _p(sg) if sg is not None else None, _p(out), _p(P))
         return out, P
+
+    def noise_eta(self, T, NFFT, qmin, dA, dE, invCA, invCE, params, eta, t0=0.0, fmt="sangria"):
+        """noise_model_mcmc's likelihood change per chain: eta [n, 4] = xA, xE, yA, yE."""
+        lib = self.lib
+        lib.ref_noise_eta.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                      _D, _D, _D, _D, ctypes.c_int, _D, _D, _D]
+        params = np.ascontiguousarray(params, np.float64).reshape(-1, 8)
+        eta = np.ascontiguousarray(eta, np.float64).reshape(-1, 4)
+        out = np.zeros(len(params))
+        lib.ref_noise_eta(fmt.encode(), T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), _p(invCE), len(params),
+                          _p(params), _p(eta), _p(out))
+        return out

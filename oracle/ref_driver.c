@@ -674,3 +674,71 @@ void ref_noise_wavelet_logl(int NF, int NT, double dt, double df, int lmin, int 
     free_tdi(data->tdi);
     free(data);
 }
+
+/* noise_model_mcmc's likelihood change (ucb/src/glass_ucb_sampler.c:29-73)
+ * for n chains with one source each (params[8 c ..]) on one A/E segment:
+ * generate_ucb_model, then for eta_x and eta_y (eta[4 c ..] = xA, xE, yA, yE)
+ * generate_noise_model, gaussian_log_likelihood and
+ * gaussian_log_likelihood_model_norm; out[c] = (logL + norm)(y) - (logL + norm)(x). */
+void ref_noise_eta(const char *format, double T, double t0, int NFFT, int qmin, const double *dA, const double *dE,
+                   const double *invCA, const double *invCE, int n, const double *params, const double *eta,
+                   double *out)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->NFFT = NFFT;
+    data->N = 2 * NFFT;
+    data->Nchannel = 2;
+    data->Nlayer = 1;
+    data->T = T;
+    data->sqT = sqrt(T);
+    data->t0 = t0;
+    data->qmin = qmin;
+    data->qmax = qmin + NFFT;
+    data->fmin = qmin / T;
+    data->fmax = (qmin + NFFT) / T;
+    strcpy(data->format, format);
+    strcpy(data->basis, "fourier");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, data->Nchannel);
+    memcpy(data->tdi->A, dA, sizeof(double) * data->N);
+    memcpy(data->tdi->E, dE, sizeof(double) * data->N);
+    data->noise = malloc(sizeof(struct Noise));
+    alloc_noise(data->noise, NFFT, 1, 2);
+    for (int k = 0; k < NFFT; k++) {
+        data->noise->C[0][0][k] = 1.0 / invCA[k];
+        data->noise->C[1][1][k] = 1.0 / invCE[k];
+        data->noise->C[0][1][k] = data->noise->C[1][0][k] = 0.0;
+        data->noise->invC[0][0][k] = invCA[k];
+        data->noise->invC[1][1][k] = invCE[k];
+    }
+    struct Model *model = calloc(1, sizeof(struct Model));
+    alloc_model(data, model, UCB_MODEL_NP, 1);
+    model->Nlive = 1;
+    model->t0 = t0;
+    for (int c = 0; c < n; c++) {
+        for (int p = 0; p < UCB_MODEL_NP; p++) model->source[0]->params[p] = params[c * UCB_MODEL_NP + p];
+        for (int k = 0; k < NFFT; k++) {
+            model->noise->invC[0][0][k] = invCA[k];
+            model->noise->invC[1][1][k] = invCE[k];
+            model->noise->C[0][0][k] = 1.0 / invCA[k];
+            model->noise->C[1][1][k] = 1.0 / invCE[k];
+        }
+        generate_ucb_model(&orbit, data, model, -1);
+        double tot[2];
+        for (int w = 0; w < 2; w++) {
+            model->noise->eta[0] = eta[4 * c + 2 * w];
+            model->noise->eta[1] = eta[4 * c + 2 * w + 1];
+            generate_noise_model(data, model);
+            double logL = gaussian_log_likelihood(data, model);
+            double norm = gaussian_log_likelihood_model_norm(data, model);
+            tot[w] = logL + norm;
+        }
+        out[c] = tot[1] - tot[0];
+    }
+    free_model(model);
+    free_noise(data->noise);
+    free_tdi(data->tdi);
+    free(data);
+}

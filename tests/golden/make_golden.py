@@ -22,7 +22,9 @@ generate_instrument_noise_model, generate_galactic_foreground_model,
 invert_noise_covariance_matrix and my_noise_log_likelihood
 (noise/src/glass_noise_model.c:389, :612, utils/src/glass_math.c:240,
 noise/src/glass_noise_model.c:1243) with their wavelet-domain, coarse-grained
-forms (:561, :656, :923, :983, :1057, :1211).  Inputs are seeded numpy draws.
+forms (:561, :656, :923, :983, :1057, :1211), and the UCB sampler's noise
+step (noise_model_mcmc, ucb/src/glass_ucb_sampler.c:29).  Inputs are seeded
+numpy draws.
 
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py fstat noise   # only the named ones
@@ -363,7 +365,38 @@ def noise_wavelet(ref, rng):
     np.savez_compressed(os.path.join(HERE, "noise_wavelet.npz"), ncase=c, NF=NF, NT=NT, dt=dt, df=df, **out)
 
 
-OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206}
+def noise_eta(ref, rng):
+    """noise_model_mcmc's likelihood change (ucb/src/glass_ucb_sampler.c:29-73)
+    for chains with one source on a config-0-like segment: small eta jumps as
+    the sampler draws them (0.001) and larger ones."""
+    out = {}
+    for c in range(2):
+        f0 = rng.uniform(3.0e-3, 3.5e-3)
+        inj = wl.draw_source(rng, f0, 2e-22, 1e-17)
+
+        def wf(p):
+            al = ref.alignment(T, 1024, 0, p)
+            h = ref.waveform(p, int(al[0]), T)
+            return int(al[0]), h[3], h[4]
+
+        qmin, dA, dE, iA, iE = wl.make_segment(rng, [inj], wf, NFFT=1024, T=T)
+        iE = iE * rng.uniform(0.9, 1.1)  # the two channels' noise need not be equal
+        il = np.empty((2, 2048))
+        il[0, 0::2], il[0, 1::2] = dA.real, dA.imag
+        il[1, 0::2], il[1, 1::2] = dE.real, dE.imag
+        props = np.vstack([inj[None], wl.gaussian_jumps(rng, inj, wl.jump_scales(inj, 20.0), 15)])
+        ex = rng.uniform(0.8, 1.25, (16, 2))
+        ey = np.where(np.arange(16)[:, None] < 8, ex + 0.001 * rng.standard_normal((16, 2)),
+                      ex * rng.uniform(0.5, 2.0, (16, 2)))
+        eta = np.column_stack([ex, ey])
+        out[f"c{c}_qmin"] = qmin
+        out[f"c{c}_dA"], out[f"c{c}_dE"], out[f"c{c}_invCA"], out[f"c{c}_invCE"] = il[0], il[1], iA, iE
+        out[f"c{c}_params"], out[f"c{c}_eta"] = props, eta
+        out[f"c{c}_delta"] = ref.noise_eta(T, 1024, qmin, il[0].copy(), il[1].copy(), iA, iE, props, eta)
+    np.savez_compressed(os.path.join(HERE, "noise_eta.npz"), ncase=2, **out)
+
+
+OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207}
 
 
 def main(names=()):
@@ -383,6 +416,7 @@ def main(names=()):
     fstat(ref, np.random.default_rng(OWN_SEEDS["fstat"]))
     noise(ref, np.random.default_rng(OWN_SEEDS["noise"]))
     noise_wavelet(ref, np.random.default_rng(OWN_SEEDS["noise_wavelet"]))
+    noise_eta(ref, np.random.default_rng(OWN_SEEDS["noise_eta"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -119,7 +119,7 @@ def test_fstat_every_size_on_a_multi_segment_bank(engine, port):
     cells, segs = [], []
     for s in range(2):
         q = int(bank.qmin[s])
-        for fdot in (0.0, 1e-16, 1e-14, 3e-13, 1e-12, 3e-12, 1e-11):
+        for fdot in (0.0, 1e-16, 1e-14, 5e-14, 1e-13, 2e-13, 3e-13, 1e-12, 3e-12, 1e-11):
             for _ in range(3):
                 cells.append([(q + rng.uniform(0, NFFT)) / T, fdot, np.arccos(rng.uniform(-1, 1)),
                               rng.uniform(0, 2 * np.pi)])

@@ -146,3 +146,61 @@ def test_noise_wavelet_errors(engine):
     engine.noise_wavelet_setup(1024, 256, 1e-5, 10, 8, np.ones(256), np.ones(256), np.ones(256))
     with pytest.raises(gg.GlassError):  # the modulated foreground needs the modulation
         engine.noise_wavelet_logl_host(np.ones((1, 12)), np.ones((1, 5)), mode=2)
+
+
+# ------------------------------------------------- the UCB sampler's noise step
+def _eta_bank(g, c):
+    dA, dE = g[f"c{c}_dA"], g[f"c{c}_dE"]
+    return wl.SegmentBank(T=T, NFFT=1024, qmin=np.array([int(g[f"c{c}_qmin"])], np.int32),
+                          dA=(dA[0::2] + 1j * dA[1::2])[None], dE=(dE[0::2] + 1j * dE[1::2])[None],
+                          invCA=g[f"c{c}_invCA"][None].copy(), invCE=g[f"c{c}_invCE"][None].copy())
+
+
+def test_noise_step_matches_reference(engine, golden):
+    """glass_gpu_noise_eta_batch against noise_model_mcmc's own likelihood change:
+    FP64 to 1e-8, mixed precision (FP32 templates) to 2e-3."""
+    g = golden("noise_eta.npz")
+    for c in range(int(g["ncase"])):
+        engine.upload(_eta_bank(g, c))
+        p, e, ref = g[f"c{c}_params"], g[f"c{c}_eta"], g[f"c{c}_delta"]
+        seg = np.zeros(len(p), np.int32)
+        for prec, tol in ((gg.PREC_FP64, 1e-8), (gg.PREC_MIXED, 2e-3)):
+            got, st = engine.noise_eta_host(seg, p, e[:, :2], e[:, 2:], precision=prec)
+            assert (st == 0).all()
+            np.testing.assert_allclose(got, ref, atol=tol)
+
+
+def test_dlogl_channels_split_term_y(engine, golden, port):
+    """term_ch sums to term_y, and each channel matches the oracle's per-channel
+    sums over the template's bins."""
+    import torch
+
+    g = golden("noise_eta.npz")
+    engine.upload(_eta_bank(g, 0))
+    p = g["c0_params"]
+    q = int(g["c0_qmin"])
+    n = len(p)
+    for prec, tol in ((gg.PREC_FP64, 1e-9), (gg.PREC_MIXED, 1e-3)):
+        dseg = torch.zeros(n, dtype=torch.int32, device="cuda")
+        dp = torch.tensor(p, device="cuda")
+        dl, ty = torch.empty(n, dtype=torch.float64, device="cuda"), torch.empty(n, dtype=torch.float64, device="cuda")
+        tch = torch.empty((n, 2), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        engine.dlogl_channels_device(dseg, dp, dl, tch, term_y=ty, precision=prec)
+        torch.cuda.synchronize()
+        tch, ty = tch.cpu().numpy(), ty.cpu().numpy()
+        np.testing.assert_allclose(tch.sum(1), ty, rtol=1e-12, atol=1e-9)
+        for i in range(n):
+            dA, dE = g["c0_dA"], g["c0_dE"]
+            al = port.alignment(T, 1024, q, p[i])
+            N, i0 = int(al[0]), int(al[3])
+            h = port.waveform(p[i], N, T)
+            ref = [0.0, 0.0]
+            for ch, (d, hc, ic) in enumerate(((dA, h[3], g["c0_invCA"]), (dE, h[4], g["c0_invCE"]))):
+                for k in range(N):
+                    j = i0 + k
+                    if 0 <= j < 1024:
+                        r = d[2 * j:2 * j + 2]
+                        hh = hc[2 * k:2 * k + 2]
+                        ref[ch] -= (((r - hh) ** 2).sum() - (r ** 2).sum()) * ic[j]
+            np.testing.assert_allclose(tch[i], ref, atol=tol)

@@ -270,3 +270,27 @@ def test_noise_wavelet_likelihood_matches_reference(port, golden):
             got = port.noise_wavelet_logl(NF, NT, df, lmin, P, Q, g[f"c{c}_inst"], g[f"c{c}_sgal"], mode,
                                           g[f"c{c}_mod"] if mode == 2 else None)
             np.testing.assert_allclose(got, g[f"c{c}_logl{mode}"], rtol=1e-13)
+
+
+def _residual_minus_template(port, q, dA, dE, p, NFFT=1024):
+    al = port.alignment(T, NFFT, q, p)
+    N, i0 = int(al[0]), int(al[3])
+    h = port.waveform(p, N, T)
+    rA, rE = dA.copy(), dE.copy()
+    for k in range(N):
+        j = i0 + k
+        if 0 <= j < NFFT:
+            rA[2 * j:2 * j + 2] -= h[3][2 * k:2 * k + 2]
+            rE[2 * j:2 * j + 2] -= h[4][2 * k:2 * k + 2]
+    return rA, rE
+
+
+def test_noise_step_matches_reference(port, golden):
+    """noise_model_mcmc's likelihood change (ucb/src/glass_ucb_sampler.c:29-73)."""
+    g = golden("noise_eta.npz")
+    for c in range(int(g["ncase"])):
+        q = int(g[f"c{c}_qmin"])
+        for p, e, ref in zip(g[f"c{c}_params"], g[f"c{c}_eta"], g[f"c{c}_delta"]):
+            rA, rE = _residual_minus_template(port, q, g[f"c{c}_dA"], g[f"c{c}_dE"], p)
+            got = port.noise_eta_delta(rA, rE, g[f"c{c}_invCA"], g[f"c{c}_invCE"], e[:2], e[2:])
+            assert abs(got - ref) < 1e-9, (c, got, ref)
