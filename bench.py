@@ -910,6 +910,48 @@ def bench_noise(gg, torch, dev, rank, steps, warmup, cpu, peak64):
     return res
 
 
+def bench_sampler(gg, torch, dev, steps, warmup):
+    """The on-device sampler step's tail for the headline workload's chains:
+    ucb_mcmc's accept/reject for 3072 chains and ptmcmc for 256 ladders of 12
+    temperatures, on device-resident state (CUDA events)."""
+    rng = np.random.default_rng(5)
+    n, NC = NSEG * 48, 12
+    nens = n // NC
+    eng = gg.Engine(dev.index or 0)
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    t = lambda a, dt=torch.float64: torch.tensor(a, dtype=dt, device=dev)
+    T = t(np.tile(1.3 ** np.arange(NC), nens))
+    dl, lpx, lpy = t(rng.normal(-2, 3, n)), t(rng.normal(-5, 1, n)), t(rng.normal(-5, 1, n))
+    qxy, qyx, snr = t(rng.normal(0, 1, n)), t(rng.normal(0, 1, n)), t(rng.uniform(0, 20, n))
+    logL, px, py = t(rng.normal(1000, 10, n)), t(rng.normal(0, 1, (n, 8))), t(rng.normal(0, 1, (n, 8)))
+    seed = t(rng.integers(1, 2**31, n), torch.int32)
+    acc = torch.empty(n, dtype=torch.int32, device=dev)
+    temps = t(1.3 ** np.arange(NC))
+    idx = t(np.tile(np.arange(NC), (nens, 1)), torch.int32)
+    pacc = torch.zeros((nens, NC), dtype=torch.float64, device=dev)
+    L = logL.view(nens, NC)
+    out = {}
+    for name, fn in (("mh_accept", lambda: eng.mh_accept_device(T, dl, lpx, lpy, qxy, qyx, seed, logL, px, py,
+                                                                accepted=acc, snr=snr)),
+                     ("ptmcmc", lambda: eng.ptmcmc_device(temps, L, idx, seed.view(nens, NC), pacc))):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                fn()
+            stream.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(steps):
+                fn()
+            b.record(stream)
+            stream.synchronize()
+        out[name + "_us"] = 1e3 * a.elapsed_time(b) / steps
+    eng.set_stream(None)
+    eng.close()
+    return {"workload": f"{n} chains: ucb_mcmc accept/reject tail; {nens} ladders x {NC} temperatures: ptmcmc; "
+                        f"reference rand_r streams", **out}
+
+
 def run_ours(args):
     import torch
 
@@ -1084,6 +1126,7 @@ def run_ours(args):
                           peak64)
     noise_line = bench_noise(gg, torch, dev, rank, max(5, args.steps // 30), args.warmup, cpu_legs and rank == 0,
                              peak64)
+    sampler_line = bench_sampler(gg, torch, dev, max(20, args.steps // 3), args.warmup)
 
     if rank == 0:
         line = {
@@ -1112,6 +1155,7 @@ def run_ours(args):
             "wavelet": wv_line,
             "fstat": fs_line,
             "noise": noise_line,
+            "sampler": sampler_line,
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk,
         }

@@ -48,6 +48,7 @@ EXPORTS = (
     "glass_gpu_noise_setup", "glass_gpu_noise_logl_batch", "glass_gpu_noise_logl_batch_host",
     "glass_gpu_noise_wavelet_setup", "glass_gpu_noise_wavelet_logl_batch", "glass_gpu_noise_wavelet_logl_batch_host",
     "glass_gpu_dlogl_batch_channels", "glass_gpu_noise_eta_batch", "glass_gpu_noise_eta_batch_host",
+    "glass_gpu_rand_r_fill", "glass_gpu_mh_accept", "glass_gpu_ptmcmc",
 )
 
 _lib = None
@@ -120,6 +121,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_dlogl_batch_channels.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 8
     lib.glass_gpu_noise_eta_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 6
     lib.glass_gpu_noise_eta_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D, _D, _I]
+    lib.glass_gpu_rand_r_fill.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V]
+    lib.glass_gpu_mh_accept.argtypes = [_V, ctypes.c_int] + [_V] * 12
+    lib.glass_gpu_ptmcmc.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 6
     _lib = lib
     return lib
 
@@ -460,6 +464,23 @@ class Engine:
         _check(self.lib.glass_gpu_noise_eta_batch_host(self._ctx, precision, n, _pi(seg), _pd(p), _pd(ex), _pd(ey),
                                                        _pd(out), _pi(st)))
         return out, st
+
+    def rand_r_fill_device(self, seed, out):
+        """seed: int32 tensor [n] (unsigned bit pattern), out: int32 [n, count]."""
+        n, count = int(out.shape[0]), int(out.shape[1])
+        _check(self.lib.glass_gpu_rand_r_fill(self._ctx, n, count, _ptr(seed), _ptr(out)))
+
+    def mh_accept_device(self, temperature, dlogl, logPx, logPy, logQxy, logQyx, seed, logL_x, params_x, params_y,
+                         accepted=None, snr=None):
+        n = int(dlogl.numel())
+        _check(self.lib.glass_gpu_mh_accept(self._ctx, n, _ptr(temperature), _ptr(dlogl), _ptr(logPx), _ptr(logPy),
+                                            _ptr(logQxy), _ptr(logQyx), _ptr(snr), _ptr(seed), _ptr(logL_x),
+                                            _ptr(params_x), _ptr(params_y), _ptr(accepted)))
+
+    def ptmcmc_device(self, temperature, logL, index, seed, acceptance, logLnorm=None):
+        nens, NC = int(index.shape[0]), int(index.shape[1])
+        _check(self.lib.glass_gpu_ptmcmc(self._ctx, nens, NC, _ptr(temperature), _ptr(logL), _ptr(logLnorm),
+                                         _ptr(index), _ptr(seed), _ptr(acceptance)))
 
     def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                              precision=PREC_FP64):

@@ -12,6 +12,7 @@
 
 #include "../../include/glass_gb300.h"
 #include "noise.cuh"
+#include "sampler.cuh"
 #include "ucb_fd.cuh"
 #include "ucb_fd_device.cuh"
 #include "ucb_wavelet.cuh"
@@ -1009,6 +1010,45 @@ extern "C" int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int m
   if (rc) return rc;
   GLASS_CUDA(cudaMemcpyAsync(logl, d_logl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
   GLASS_CUDA(cudaStreamSynchronize(s), "noise_wavelet_logl_batch_host sync");
+  return GLASS_OK;
+}
+
+// ------------------------------------------------------ on-device sampler
+extern "C" int glass_gpu_rand_r_fill(glass_gpu_ctx *ctx, int n, int count, unsigned int *seed, int *out) {
+  if (!ctx || !seed || !out || n < 0 || count < 0) return set_err(GLASS_ERR_ARG, "rand_r_fill: bad argument");
+  if (n == 0 || count == 0) return GLASS_OK;
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  GLASS_CUDA(rand_r_fill_launch(n, count, seed, out, ctx->stream), "rand_r_fill");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_mh_accept(glass_gpu_ctx *ctx, int n, const double *temperature, const double *dlogl,
+                                   const double *logPx, const double *logPy, const double *logQxy,
+                                   const double *logQyx, const double *snr, unsigned int *seed, double *logL_x,
+                                   double *params_x, const double *params_y, int *accepted) {
+  if (!ctx || n < 0) return set_err(GLASS_ERR_ARG, "mh_accept: bad argument");
+  if (n == 0) return GLASS_OK;
+  if (!temperature || !dlogl || !logPx || !logPy || !logQxy || !logQyx || !seed || !logL_x || !params_x || !params_y)
+    return set_err(GLASS_ERR_ARG, "mh_accept: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  MhArgs a{n, temperature, dlogl, logPx, logPy, logQxy, logQyx, snr, logL_x, params_x, params_y, seed, accepted};
+  GLASS_CUDA(mh_accept_launch(a, ctx->stream), "mh_accept");
+  ctx->last_launches = 1;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_ptmcmc(glass_gpu_ctx *ctx, int nens, int NC, const double *temperature, const double *logL,
+                                const double *logLnorm, int *index, unsigned int *seed, double *acceptance) {
+  if (!ctx || nens < 0 || NC < 1) return set_err(GLASS_ERR_ARG, "ptmcmc: bad argument");
+  if (nens == 0) return GLASS_OK;
+  if (!temperature || !logL || !index || !seed || !acceptance) return set_err(GLASS_ERR_ARG, "ptmcmc: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  PtArgs a{nens, NC, temperature, logL, logLnorm, index, seed, acceptance};
+  GLASS_CUDA(ptmcmc_launch(a, ctx->stream), "ptmcmc");
+  ctx->last_launches = 1;
   return GLASS_OK;
 }
 

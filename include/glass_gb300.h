@@ -287,6 +287,37 @@ int glass_gpu_noise_eta_batch_host(glass_gpu_ctx *ctx, int precision, int n, con
                                    const double *params, const double *eta_x, const double *eta_y,
                                    double *dlogl_noise, int *status);
 
+/* ------------------------------------------------ on-device sampler */
+/*
+ * The reference draws a chain's random numbers from the C library's rand_r on
+ * that chain's seed (rand_r_U_0_1 = rand_r / RAND_MAX, utils/src/glass_utils.c:19;
+ * chain->r[ic]).  These kernels advance the same seeds with the same
+ * algorithm, so the decisions are the reference's; the seeds, like every other
+ * argument, are DEVICE arrays updated in place.  Asynchronous.
+ *
+ * glass_gpu_rand_r_fill: out[i count + k] = the next count rand_r values of
+ * seed[i] (a check of the stream).
+ *
+ * glass_gpu_mh_accept: the accept/reject tail of ucb_mcmc
+ * (ucb/src/glass_ucb_sampler.c:141-172) for n chains: where logPy[i] is
+ * finite, snr[i] < 5 (snr may be NULL) rejects as the reference does, logH =
+ * dlogl[i]/temperature[i] + logPy - logPx + logQxy - logQyx, one draw
+ * loga = log U(0,1), and acceptance when logH is finite and > loga; no draw
+ * where logPy is -inf.  On acceptance params_x[8 i ..] = params_y[8 i ..] and
+ * logL_x[i] += dlogl[i].  accepted[i] = 1/0 (may be NULL).
+ *
+ * glass_gpu_ptmcmc: ptmcmc (utils/src/glass_sampler.c:19-63) on nens ladders
+ * of NC chains: ladder e's chain c at e NC + c of logL, logLnorm (may be
+ * NULL), index (the ladder's permutation of 0..NC-1), seed and acceptance;
+ * temperature[NC] shared.
+ */
+int glass_gpu_rand_r_fill(glass_gpu_ctx *ctx, int n, int count, unsigned int *seed, int *out);
+int glass_gpu_mh_accept(glass_gpu_ctx *ctx, int n, const double *temperature, const double *dlogl, const double *logPx,
+                        const double *logPy, const double *logQxy, const double *logQyx, const double *snr,
+                        unsigned int *seed, double *logL_x, double *params_x, const double *params_y, int *accepted);
+int glass_gpu_ptmcmc(glass_gpu_ctx *ctx, int nens, int NC, const double *temperature, const double *logL,
+                     const double *logLnorm, int *index, unsigned int *seed, double *acceptance);
+
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 

@@ -249,6 +249,41 @@ class Port:
         ey = np.ascontiguousarray(eta_y, np.float64)
         return lib.orc_noise_eta_delta(len(invCA), _p(rA), _p(rE), _p(invCA), _p(invCE), _p(ex), _p(ey))
 
+    # --- sampler (utils/src/glass_sampler.c, ucb/src/glass_ucb_sampler.c) ---------
+    def rand_r_seq(self, seeds, count):
+        """[n, count] successive rand_r values from each seed; returns (values, new seeds)."""
+        lib = self.lib
+        lib.orc_rand_r_seq.argtypes = [ctypes.POINTER(ctypes.c_uint), ctypes.c_int, _I]
+        seeds = np.array(seeds, dtype=np.uint32).copy()
+        out = np.zeros((len(seeds), count), np.int32)
+        for i in range(len(seeds)):
+            s = ctypes.c_uint(int(seeds[i]))
+            lib.orc_rand_r_seq(ctypes.byref(s), count, out[i].ctypes.data_as(_I))
+            seeds[i] = s.value
+        return out, seeds
+
+    def ptmcmc(self, temperature, logL, index, seed, acceptance, logLnorm=None):
+        """In place on index [nens, NC] (int32), seed (uint32), acceptance (float64)."""
+        lib = self.lib
+        lib.orc_ptmcmc.argtypes = [ctypes.c_int, ctypes.c_int, _D, _D, _D, _I, ctypes.POINTER(ctypes.c_uint), _D]
+        nens, NC = index.shape
+        lib.orc_ptmcmc(nens, NC, _p(np.ascontiguousarray(temperature, np.float64)),
+                       _p(np.ascontiguousarray(logL, np.float64)),
+                       _p(np.ascontiguousarray(logLnorm, np.float64)) if logLnorm is not None else None,
+                       index.ctypes.data_as(_I), seed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), _p(acceptance))
+
+    def mh_accept(self, T, logL_x, dlogl, logPx, logPy, logQxy, logQyx, seed, params_x, params_y, snr=None):
+        """In place on logL_x, seed (uint32), params_x [n, 8]; returns accepted [n]."""
+        lib = self.lib
+        lib.orc_mh_accept.argtypes = [ctypes.c_int] + [_D] * 8 + [ctypes.POINTER(ctypes.c_uint), _D, _D, _I]
+        n = len(dlogl)
+        acc = np.zeros(n, np.int32)
+        c = lambda a: _p(np.ascontiguousarray(a, np.float64))
+        lib.orc_mh_accept(n, c(T), _p(logL_x), c(dlogl), c(logPx), c(logPy), c(logQxy), c(logQyx),
+                          c(snr) if snr is not None else None, seed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)),
+                          _p(params_x), c(params_y), acc.ctypes.data_as(_I))
+        return acc
+
     def orbit(self, t):
         out = np.zeros(9)
         self.lib.orc_orbit_positions(float(t), _p(out))
@@ -589,3 +624,12 @@ class Ref:
         lib.ref_noise_eta(fmt.encode(), T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), _p(invCE), len(params),
                           _p(params), _p(eta), _p(out))
         return out
+
+    def ptmcmc(self, temperature, logL, index, seed, acceptance, logLnorm=None):
+        """The reference's ptmcmc on one ladder, in place."""
+        lib = self.lib
+        lib.ref_ptmcmc.argtypes = [ctypes.c_int, _D, _D, _D, _I, ctypes.POINTER(ctypes.c_uint), _D]
+        NC = len(index)
+        lib.ref_ptmcmc(NC, _p(np.ascontiguousarray(temperature, np.float64)), _p(np.ascontiguousarray(logL, np.float64)),
+                       _p(np.ascontiguousarray(logLnorm, np.float64)) if logLnorm is not None else None,
+                       index.ctypes.data_as(_I), seed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), _p(acceptance))

@@ -742,3 +742,29 @@ void ref_noise_eta(const char *format, double T, double t0, int NFFT, int qmin, 
     free_tdi(data->tdi);
     free(data);
 }
+
+/* ptmcmc (utils/src/glass_sampler.c:19) on one ladder of NC chains whose
+ * models hold logL and logLnorm; index, seed and acceptance are updated. */
+void ref_ptmcmc(int NC, const double *temperature, const double *logL, const double *logLnorm, int *index,
+                unsigned int *seed, double *acceptance)
+{
+    struct Chain chain;
+    memset(&chain, 0, sizeof(chain));
+    chain.NC = NC;
+    chain.index = index;
+    chain.temperature = (double *)temperature;
+    chain.acceptance = acceptance;
+    chain.r = seed;
+    struct Model **model = malloc(sizeof(struct Model *) * NC);
+    struct Model *m = calloc(NC, sizeof(struct Model));
+    for (int c = 0; c < NC; c++) {
+        m[c].logL = logL[c];
+        m[c].logLnorm = logLnorm ? logLnorm[c] : 0.0;
+        model[c] = &m[c];
+    }
+    struct Flags flags;
+    memset(&flags, 0, sizeof(flags));
+    ptmcmc(model, &chain, &flags);
+    free(m);
+    free(model);
+}

@@ -23,8 +23,9 @@ invert_noise_covariance_matrix and my_noise_log_likelihood
 (noise/src/glass_noise_model.c:389, :612, utils/src/glass_math.c:240,
 noise/src/glass_noise_model.c:1243) with their wavelet-domain, coarse-grained
 forms (:561, :656, :923, :983, :1057, :1211), and the UCB sampler's noise
-step (noise_model_mcmc, ucb/src/glass_ucb_sampler.c:29).  Inputs are seeded
-numpy draws.
+step (noise_model_mcmc, ucb/src/glass_ucb_sampler.c:29), and the
+parallel-tempering exchange ptmcmc (utils/src/glass_sampler.c:19).  Inputs are
+seeded numpy draws.
 
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py fstat noise   # only the named ones
@@ -396,7 +397,34 @@ def noise_eta(ref, rng):
     np.savez_compressed(os.path.join(HERE, "noise_eta.npz"), ncase=2, **out)
 
 
-OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207}
+def sampler(ref, rng):
+    """ptmcmc (utils/src/glass_sampler.c:19) of 16 ladders of 12 chains with a
+    geometric temperature ladder, 40 successive exchange sweeps each on fixed
+    log-likelihoods: the permutation, acceptance and seeds after the first
+    sweep and after the last."""
+    NC, nens, sweeps = 12, 16, 40
+    temperature = 1.3 ** np.arange(NC)
+    logL = rng.normal(1000.0, 20.0, (nens, NC))
+    logLn = rng.normal(-50.0, 5.0, (nens, NC))
+    seed0 = rng.integers(1, 2**31, (nens, NC)).astype(np.uint32)
+    idx1, acc1, s1 = [], [], []
+    idxN, accN, sN = [], [], []
+    for e in range(nens):
+        index = np.arange(NC, dtype=np.int32)
+        seed = seed0[e].copy()
+        acc = np.zeros(NC)
+        for k in range(sweeps):
+            ref.ptmcmc(temperature, logL[e], index, seed, acc, logLn[e])
+            if k == 0:
+                idx1.append(index.copy()), acc1.append(acc.copy()), s1.append(seed.copy())
+        idxN.append(index), accN.append(acc), sN.append(seed)
+    np.savez_compressed(os.path.join(HERE, "sampler.npz"), NC=NC, sweeps=sweeps, temperature=temperature, logL=logL,
+                        logLnorm=logLn, seed0=seed0, index1=np.array(idx1), acc1=np.array(acc1),
+                        seed1=np.array(s1), indexN=np.array(idxN), accN=np.array(accN), seedN=np.array(sN))
+
+
+OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
+             "sampler": 20261208}
 
 
 def main(names=()):
@@ -417,6 +445,7 @@ def main(names=()):
     noise(ref, np.random.default_rng(OWN_SEEDS["noise"]))
     noise_wavelet(ref, np.random.default_rng(OWN_SEEDS["noise_wavelet"]))
     noise_eta(ref, np.random.default_rng(OWN_SEEDS["noise_eta"]))
+    sampler(ref, np.random.default_rng(OWN_SEEDS["sampler"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -294,3 +294,26 @@ def test_noise_step_matches_reference(port, golden):
             rA, rE = _residual_minus_template(port, q, g[f"c{c}_dA"], g[f"c{c}_dE"], p)
             got = port.noise_eta_delta(rA, rE, g[f"c{c}_invCA"], g[f"c{c}_invCE"], e[:2], e[2:])
             assert abs(got - ref) < 1e-9, (c, got, ref)
+
+
+# ------------------------------------------------------------------ sampler
+def _ptmcmc_run(port, g, sweeps):
+    NC = int(g["NC"])
+    nens = len(g["seed0"])
+    index = np.tile(np.arange(NC, dtype=np.int32), (nens, 1))
+    seed = g["seed0"].astype(np.uint32).copy()
+    acc = np.zeros((nens, NC))
+    for _ in range(sweeps):
+        port.ptmcmc(g["temperature"], g["logL"], index, seed, acc, g["logLnorm"])
+    return index, seed, acc
+
+
+def test_ptmcmc_matches_reference(port, golden):
+    """ptmcmc (utils/src/glass_sampler.c:19-63): permutation, acceptance and the
+    chains' seeds after one and after 40 sweeps, exactly."""
+    g = golden("sampler.npz")
+    for sweeps, tag in ((1, "1"), (int(g["sweeps"]), "N")):
+        index, seed, acc = _ptmcmc_run(port, g, sweeps)
+        np.testing.assert_array_equal(index, g["index" + tag])
+        np.testing.assert_array_equal(seed, g["seed" + tag])
+        np.testing.assert_array_equal(acc, g["acc" + tag])

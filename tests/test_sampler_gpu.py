@@ -1,0 +1,105 @@
+"""The on-device sampler kernels against the C library's rand_r, the
+reference's ptmcmc (golden vectors) and the oracle's restatement of
+ucb_mcmc's accept/reject tail, bit for bit: same seeds in, same decisions,
+states and seeds out."""
+import numpy as np
+import pytest
+
+import glass_gb300 as gg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def engine():
+    from glass_gb300 import build
+
+    build.build()
+    eng = gg.Engine(0)
+    yield eng
+    eng.close()
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, np.uint32).view(np.int32)
+
+
+def test_rand_r_stream_matches_c_library(engine, port):
+    import torch
+
+    rng = np.random.default_rng(31)
+    seeds = np.concatenate([[0, 1, 12345, 2**31 - 1, 2**32 - 1], rng.integers(0, 2**32, 995, dtype=np.uint64)])
+    seeds = seeds.astype(np.uint32)
+    ref, ref_next = port.rand_r_seq(seeds, 64)
+    ds = torch.tensor(_u32(seeds), device="cuda")
+    out = torch.empty((len(seeds), 64), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    engine.rand_r_fill_device(ds, out)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+    np.testing.assert_array_equal(ds.cpu().numpy().view(np.uint32), ref_next)
+
+
+def test_ptmcmc_matches_reference(engine, golden):
+    import torch
+
+    g = golden("sampler.npz")
+    NC = int(g["NC"])
+    nens = len(g["seed0"])
+    dT = torch.tensor(g["temperature"], device="cuda")
+    dL = torch.tensor(g["logL"], device="cuda")
+    dLn = torch.tensor(g["logLnorm"], device="cuda")
+    didx = torch.tensor(np.tile(np.arange(NC, dtype=np.int32), (nens, 1)), device="cuda")
+    dseed = torch.tensor(_u32(g["seed0"]), device="cuda")
+    dacc = torch.zeros((nens, NC), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    for k in range(int(g["sweeps"])):
+        engine.ptmcmc_device(dT, dL, didx, dseed, dacc, logLnorm=dLn)
+        if k == 0:
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(didx.cpu().numpy(), g["index1"])
+            np.testing.assert_array_equal(dseed.cpu().numpy().view(np.uint32), g["seed1"])
+            np.testing.assert_array_equal(dacc.cpu().numpy(), g["acc1"])
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(didx.cpu().numpy(), g["indexN"])
+    np.testing.assert_array_equal(dseed.cpu().numpy().view(np.uint32), g["seedN"])
+    np.testing.assert_array_equal(dacc.cpu().numpy(), g["accN"])
+
+
+def test_mh_accept_matches_restated_reference(engine, port):
+    """ucb_mcmc's tail (ucb/src/glass_ucb_sampler.c:141-172): infinite priors
+    (no draw), SNR below 5 (a draw, then rejection), non-finite logH, and
+    ordinary proposals at a range of temperatures; 20 successive steps."""
+    import torch
+
+    rng = np.random.default_rng(32)
+    n = 4096
+    T = 1.3 ** rng.integers(0, 12, n)
+    logL = rng.normal(1000, 10, n)
+    px = rng.normal(0, 1, (n, 8))
+    seed = rng.integers(1, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    d = {k: torch.tensor(v, device="cuda") for k, v in (("T", T), ("logL", logL.copy()), ("px", px.copy()))}
+    dseed = torch.tensor(_u32(seed), device="cuda")
+    for step in range(20):
+        dlogl = rng.normal(-2, 3, n)
+        dlogl[rng.random(n) < 0.01] = np.nan
+        logPx = rng.normal(-5, 1, n)
+        logPy = rng.normal(-5, 1, n)
+        logPy[rng.random(n) < 0.1] = -np.inf
+        logQxy, logQyx = rng.normal(0, 1, n), rng.normal(0, 1, n)
+        snr = rng.uniform(0, 20, n)
+        py = rng.normal(0, 1, (n, 8))
+        acc_ref = port.mh_accept(T, logL, dlogl, logPx, logPy, logQxy, logQyx, seed, px, py, snr=snr)
+        dd = {k: torch.tensor(v, device="cuda") for k, v in (("dl", dlogl), ("lpx", logPx), ("lpy", logPy),
+                                                            ("qxy", logQxy), ("qyx", logQyx), ("snr", snr),
+                                                            ("py", py))}
+        dacc = torch.empty(n, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        engine.mh_accept_device(d["T"], dd["dl"], dd["lpx"], dd["lpy"], dd["qxy"], dd["qyx"], dseed, d["logL"],
+                                d["px"], dd["py"], accepted=dacc, snr=dd["snr"])
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(dacc.cpu().numpy(), acc_ref)
+        np.testing.assert_array_equal(dseed.cpu().numpy().view(np.uint32), seed)
+        np.testing.assert_array_equal(d["logL"].cpu().numpy(), logL)
+        np.testing.assert_array_equal(d["px"].cpu().numpy(), px)
+    assert 0.05 < acc_ref.mean() < 0.9
