@@ -91,7 +91,7 @@ def spec_flops_per_eval(N):
 # ncu flushes the caches before the launch, so the spectral kernel's figure is
 # its series scratch (4 x N complex floats per proposal, ~29 MB) read from DRAM;
 # in a live step the slow-part kernel has just written it to L2.
-PROFILED_DRAM_BYTES = {"fd_spec_all_kernel<1>": 31018800 + 768, "fd_slow_kernel<1>": 598528}
+PROFILED_DRAM_BYTES = {"fd_spec_all_kernel<1, 0>": 31018800 + 768, "fd_slow_kernel<1>": 598528}
 
 
 def make_workload(rank, steps):
@@ -1094,7 +1094,7 @@ def run_ours(args):
 
     # dominant kernel of the mixed step: the longer of the slow-part and the
     # spectral kernel; its algorithmic flops per launch over its mean duration
-    kern = {"fd_slow_kernel<1>": (phase_ms[1], flops_slow), "fd_spec_all_kernel<1>": (phase_ms[2], flops_spec)}
+    kern = {"fd_slow_kernel<1>": (phase_ms[1], flops_slow), "fd_spec_all_kernel<1, 0>": (phase_ms[2], flops_spec)}
     dom = max(kern, key=lambda k: kern[k][0])
     ms_dom, fl_dom = kern[dom]
     ach_dom = fl_dom / (ms_dom * 1e-3) / 1e12
@@ -1104,7 +1104,7 @@ def run_ours(args):
                 "peak_source": "FP32 FMA probe kernel measured in this run "
                                "(MEASURED_PEAKS.json has no CUDA-core FP32 figure)",
                 "phase_ms": {"fd_planmix_kernel": phase_ms[0], "fd_slow_kernel<1>": phase_ms[1],
-                             "fd_spec_all_kernel<1>": phase_ms[2]},
+                             "fd_spec_all_kernel<1, 0>": phase_ms[2]},
                 "timing": "CUDA timing events between the step's launches on its stream, "
                           f"{len(phase)} steps outside graph capture, L2 flushed before each",
                 "step": {"achieved": ach_mixed, "frac": ach_mixed / peak32, "flops_per_step": flops_step},
