@@ -1058,20 +1058,50 @@ def run_ours(args):
     eng.set_phase_timing(False)
     phase_ms = np.mean(np.array(phase), axis=0)
 
-    # end to end through the host-pointer C entry point
+    # end to end through the host-pointer C entry point, with the caller's
+    # proposal and result buffers kept between calls (one per step, filled
+    # before the timed region, as the sampler fills its own)
     h_seg = np.ascontiguousarray(item_seg)
     eng.set_stream(None)
+    hbs = []
+    for k in range(args.warmup + args.steps):
+        hb = eng.host_batch(items)
+        hb.item_seg[:] = h_seg
+        hb.params[:] = batches[k]
+        hb.term_x[:] = term_x
+        hbs.append(hb)
+
+    def time_host_batches():
+        for w in range(args.warmup):
+            hbs[w].run(gg.PREC_MIXED)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            hbs[args.warmup + k].run(gg.PREC_MIXED)
+        return time.perf_counter() - t0
+
+    t_e2e = time_host_batches()
+    host_in_place = eng.host_access()[1]
+    # the same through pinned staging copies, where the default path is the
+    # in-place one (the device reading and writing the host arrays)
+    t_stage = t_e2e
+    if host_in_place:
+        eng.set_host_access(0)
+        t_stage = time_host_batches()
+        eng.set_host_access(-1)
+    # and through the Python wrapper, which converts its arguments on every call
     for w in range(args.warmup):
         eng.dlogl_host(h_seg, batches[w], term_x, precision=gg.PREC_MIXED)
-    torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(args.steps):
         eng.dlogl_host(h_seg, batches[args.warmup + k], term_x, precision=gg.PREC_MIXED)
-    t_e2e = time.perf_counter() - t0
+    t_wrap = time.perf_counter() - t0
+    del hbs
 
     # max over ranks
-    t_mixed, t_fp64, t_e2e = max_over_ranks([t_mixed, t_fp64, t_e2e], dev)
-    v_mixed, v_fp64, v_e2e = (job_rate(args.steps, items, world, t) for t in (t_mixed, t_fp64, t_e2e))
+    t_mixed, t_fp64, t_e2e, t_stage, t_wrap = max_over_ranks([t_mixed, t_fp64, t_e2e, t_stage, t_wrap], dev)
+    v_mixed, v_fp64, v_e2e, v_stage, v_wrap = (job_rate(args.steps, items, world, t)
+                                               for t in (t_mixed, t_fp64, t_e2e, t_stage, t_wrap))
 
     m64 = torch.stack(rec_fp64).cpu().numpy()
     err = torch.stack(rec_mixed).cpu().numpy() - m64
@@ -1148,7 +1178,12 @@ def run_ours(args):
                          "evals_compared": int(abs_err.size), "invalid_proposals": int((~valid).sum())},
             "e2e": {"value": v_e2e, "unit": "evals/s",
                     "h2d_bytes_per_step": int(items * (8 * 8 + 4 + 8)),
-                    "d2h_bytes_per_step": int(items * (3 * 8 + 4))},
+                    "d2h_bytes_per_step": int(items * (3 * 8 + 4)),
+                    "host_access": ("in place: gather/scatter kernels read and write the pageable host arrays "
+                                    "through the host page tables" if host_in_place else "pinned staging copies"),
+                    "pinned_staging_value": v_stage,
+                    "api": "glass_gpu_dlogl_batch_host on host buffers kept between calls (HostBatch.run)",
+                    "python_wrapper_value": v_wrap},
             "roofline": roofline,
             "grad_fisher": grad_line,
             "wdm": wdm_line,

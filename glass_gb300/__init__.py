@@ -34,6 +34,7 @@ EXPORTS = (
     "glass_gpu_create", "glass_gpu_destroy", "glass_gpu_set_stream", "glass_gpu_last_error",
     "glass_gpu_bank_upload", "glass_gpu_bank_set_residual", "glass_gpu_dlogl_batch",
     "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_set_phase_timing",
+    "glass_gpu_set_host_access", "glass_gpu_get_host_access",
     "glass_gpu_last_phase_ms", "glass_gpu_probe_fma_tflops",
     "glass_gpu_grad_fisher_batch", "glass_gpu_grad_fisher_batch_host", "glass_gpu_set_template_size",
     "glass_gpu_dlogl_fp64_noalloc", "glass_wdm_window", "glass_gpu_wdm_forward", "glass_gpu_wdm_inverse",
@@ -72,6 +73,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_set_stream.argtypes = [_V, _V]
     lib.glass_gpu_last_launch_count.argtypes = [_V]
     lib.glass_gpu_set_phase_timing.argtypes = [_V, ctypes.c_int]
+    lib.glass_gpu_set_host_access.argtypes = [_V, ctypes.c_int]
+    lib.glass_gpu_get_host_access.argtypes = [_V, _I, _I]
     lib.glass_gpu_last_phase_ms.argtypes = [_V, ctypes.POINTER(ctypes.c_float)]
     lib.glass_gpu_bank_upload.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_int, _I, _D, _D, _D, _D]
@@ -251,6 +254,10 @@ class Engine:
                                                    _pd(tx) if tx is not None else None, _pd(dl), _pd(ty), _pd(hh),
                                                    _pi(st)))
         return dl, ty, hh, st
+
+    def host_batch(self, n: int, with_term_x: bool = True) -> "HostBatch":
+        """Host arrays for batches of n proposals, kept between calls (see HostBatch)."""
+        return HostBatch(self, n, with_term_x)
 
     def dlogl_device(self, item_seg, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                      precision=PREC_MIXED):
@@ -491,6 +498,17 @@ class Engine:
     def last_launch_count(self) -> int:
         return self.lib.glass_gpu_last_launch_count(self._ctx)
 
+    def set_host_access(self, mode: int = -1):
+        """How dlogl_host moves data: 1 in place (the device reads and writes
+        the host arrays), 0 pinned staging copies, -1 in place where supported."""
+        _check(self.lib.glass_gpu_set_host_access(self._ctx, int(mode)))
+
+    def host_access(self):
+        """(supported, direct): in-place host access possible / in use."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        _check(self.lib.glass_gpu_get_host_access(self._ctx, ctypes.byref(a), ctypes.byref(b)))
+        return bool(a.value), bool(b.value)
+
     def set_phase_timing(self, enable: bool):
         _check(self.lib.glass_gpu_set_phase_timing(self._ctx, int(bool(enable))))
 
@@ -500,3 +518,27 @@ class Engine:
         ms = (ctypes.c_float * 3)()
         _check(self.lib.glass_gpu_last_phase_ms(self._ctx, ms))
         return tuple(float(v) for v in ms)
+
+
+class HostBatch:
+    """The host arrays of one batch of n proposals for
+    glass_gpu_dlogl_batch_host, with their C pointers resolved once: the way a
+    C caller keeps its proposal and result buffers from one sampler step to the
+    next.  Fill item_seg, params (n x 8) and term_x, call run(), read dlogl,
+    term_y, hh and status."""
+
+    def __init__(self, engine: Engine, n: int, with_term_x: bool = True):
+        self.engine = engine
+        self.n = int(n)
+        self.item_seg = np.zeros(self.n, np.int32)
+        self.params = np.zeros((self.n, 8))
+        self.term_x = np.zeros(self.n) if with_term_x else None
+        self.dlogl, self.term_y, self.hh = np.empty(self.n), np.empty(self.n), np.empty(self.n)
+        self.status = np.empty(self.n, np.int32)
+        self._fn = engine.lib.glass_gpu_dlogl_batch_host
+        self._args = (_pi(self.item_seg), _pd(self.params), _pd(self.term_x) if with_term_x else None,
+                      _pd(self.dlogl), _pd(self.term_y), _pd(self.hh), _pi(self.status))
+
+    def run(self, precision: int = PREC_MIXED):
+        """Evaluate the batch (synchronous); results in dlogl, term_y, hh, status."""
+        _check(self._fn(self.engine._ctx, precision, self.n, *self._args))

@@ -43,6 +43,15 @@ static int cuda_err(cudaError_t e, const char *where) {
 extern "C" const char *glass_gpu_last_error(void) { return g_err.c_str(); }
 
 // ----------------------------------------------------------------- context
+// Host pointers of one glass_gpu_dlogl_batch_host call (direct host access).
+struct HostIo {
+  const double *params;
+  const double *term_x;
+  const int *item_seg;
+  double *dlogl, *term_y, *hh;
+  int *status;
+};
+
 struct glass_gpu_ctx {
   int device = 0;
   int num_sms = 0;
@@ -66,6 +75,14 @@ struct glass_gpu_ctx {
   // they are dropped whenever one of those is reallocated
   void *h_stage = nullptr;
   size_t h_stage_cap = 0;
+  // Direct host access: where the device reads the caller's pageable memory
+  // through the host's page tables (ATS over a coherent CPU-GPU link), a
+  // gather kernel reads the inputs and a scatter kernel writes the outputs in
+  // place of the staging copies; the call's host pointers sit in a pinned
+  // block that the two kernels read, so one graph serves every call of a shape
+  bool host_direct_ok = false;  // device attributes allow it
+  bool host_direct = false;     // in use
+  HostIo *h_io = nullptr;
   std::map<long long, cudaGraphExec_t> host_graphs;
   int last_launches = 0;
   int n_fixed = 0;  // template size override (0: bandwidth rule)
@@ -110,6 +127,15 @@ extern "C" int glass_gpu_create(int device, glass_gpu_ctx **out) {
     return cuda_err(e, "cudaSetDevice");
   }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  {
+    int pageable = 0, host_tables = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+    cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device);
+    // only with the host's own page tables: without them (HMM) a device access
+    // migrates the caller's pages instead of reading them in place
+    ctx->host_direct_ok = pageable && host_tables;
+    ctx->host_direct = ctx->host_direct_ok;
+  }
   if ((e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking)) != cudaSuccess) {
     delete ctx;
     return cuda_err(e, "cudaStreamCreate");
@@ -145,6 +171,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->d_stage);
   clear_host_graphs(ctx);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  if (ctx->h_io) cudaFreeHost(ctx->h_io);
   wdm_release(ctx->wdm);
   cudaFree(ctx->wdm_stage);
   cudaFree(ctx->wv_grid_mem);
@@ -176,6 +203,22 @@ extern "C" int glass_gpu_set_stream(glass_gpu_ctx *ctx, void *stream) {
 }
 
 extern "C" int glass_gpu_last_launch_count(glass_gpu_ctx *ctx) { return ctx ? ctx->last_launches : 0; }
+
+extern "C" int glass_gpu_set_host_access(glass_gpu_ctx *ctx, int mode) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_set_host_access: null context");
+  if (mode < -1 || mode > 1) return set_err(GLASS_ERR_ARG, "glass_gpu_set_host_access: mode is -1, 0 or 1");
+  if (mode == 1 && !ctx->host_direct_ok)
+    return set_err(GLASS_ERR_STATE, "glass_gpu_set_host_access: the device cannot read pageable host memory in place");
+  ctx->host_direct = mode == 1 || (mode == -1 && ctx->host_direct_ok);
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_get_host_access(glass_gpu_ctx *ctx, int *supported, int *direct) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_get_host_access: null context");
+  if (supported) *supported = ctx->host_direct_ok ? 1 : 0;
+  if (direct) *direct = ctx->host_direct ? 1 : 0;
+  return GLASS_OK;
+}
 
 extern "C" int glass_gpu_set_phase_timing(glass_gpu_ctx *ctx, int enable) {
   if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_set_phase_timing: null context");
@@ -451,6 +494,88 @@ static int ensure_host_stage(glass_gpu_ctx *ctx, size_t bytes) {
 // and pinned host alike): inputs params (8n doubles) | term_x (n doubles) |
 // item_seg (n ints), then at out_off the outputs dlogl | term_y | hh (n
 // doubles each) | status (n ints).
+// Direct host access.  The pointer block is re-read on every launch: the
+// first threads of each gather CTA load it (ld.global.cv) into shared memory
+// and CTA 0 leaves a device copy for the scatter kernel; the caller's arrays
+// are read the same way, since both change between replays of one graph, and
+// the outputs are written through (st.global.wt).
+__device__ __forceinline__ void host_io_load_block(const HostIo *io, HostIo *s, HostIo *d_io) {
+  const unsigned long long *w = reinterpret_cast<const unsigned long long *>(io);
+  unsigned long long *sw = reinterpret_cast<unsigned long long *>(s);
+  constexpr int kWords = sizeof(HostIo) / sizeof(unsigned long long);
+  if (threadIdx.x < kWords) {
+    const unsigned long long v = __ldcv(w + threadIdx.x);
+    sw[threadIdx.x] = v;
+    if (blockIdx.x == 0) reinterpret_cast<unsigned long long *>(d_io)[threadIdx.x] = v;
+  }
+  __syncthreads();
+}
+
+// params (8n doubles), term_x (n, when given), item_seg (n ints) into the
+// device stage
+__global__ void host_gather_kernel(const HostIo *io, HostIo *d_io, int n, double *d_params, double *d_tx,
+                                   int *d_seg) {
+  __shared__ HostIo h;
+  host_io_load_block(io, &h, d_io);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if ((reinterpret_cast<unsigned long long>(h.params) & 15) == 0) {
+    const double2 *src = reinterpret_cast<const double2 *>(h.params);
+    double2 *dst = reinterpret_cast<double2 *>(d_params);
+    for (long long i = t; i < 4LL * n; i += stride) dst[i] = __ldcv(src + i);
+  } else {
+    for (long long i = t; i < 8LL * n; i += stride) d_params[i] = __ldcv(h.params + i);
+  }
+  if (h.term_x)
+    for (long long i = t; i < n; i += stride) d_tx[i] = __ldcv(h.term_x + i);
+  for (long long i = t; i < n; i += stride) d_seg[i] = __ldcv(h.item_seg + i);
+}
+
+// dlogl, term_y, hh (n doubles each) and status (n ints) to the caller's
+// arrays; the three optional ones are skipped when NULL
+__global__ void host_scatter_kernel(const HostIo *d_io, int n, const double *d_dl, const double *d_ty,
+                                    const double *d_hh, const int *d_st) {
+  const HostIo h = *d_io;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long i = t; i < n; i += stride) __stwt(h.dlogl + i, d_dl[i]);
+  if (h.term_y)
+    for (long long i = t; i < n; i += stride) __stwt(h.term_y + i, d_ty[i]);
+  if (h.hh)
+    for (long long i = t; i < n; i += stride) __stwt(h.hh + i, d_hh[i]);
+  if (h.status)
+    for (long long i = t; i < n; i += stride) __stwt(h.status + i, d_st[i]);
+}
+
+static int host_copy_grid(const glass_gpu_ctx *ctx, long long elems) {
+  const long long b = (elems + 255) / 256;
+  return (int)std::max(1LL, std::min(b, 4LL * ctx->num_sms));
+}
+
+// gather, the batch, scatter on the context's stream (same stage layout as
+// dlogl_host_enqueue below)
+static int dlogl_direct_enqueue(glass_gpu_ctx *ctx, int precision, int nitems, bool has_tx, size_t out_off) {
+  const size_t nd = (size_t)nitems;
+  char *d = (char *)ctx->d_stage;
+  double *d_params = (double *)d, *d_tx = d_params + 8 * nd;
+  int *d_seg = (int *)(d_tx + nd);
+  double *d_dl = (double *)(d + out_off), *d_ty = d_dl + nd, *d_hh = d_ty + nd;
+  int *d_st = (int *)(d_hh + nd);
+  cudaStream_t s = ctx->stream;
+  // the device copy of the pointer block sits after the outputs
+  HostIo *d_io = (HostIo *)(d + out_off + ((sizeof(double) * 3 * nd + sizeof(int) * nd + 15) / 16) * 16);
+  host_gather_kernel<<<host_copy_grid(ctx, 4LL * nitems), 256, 0, s>>>(ctx->h_io, d_io, nitems, d_params, d_tx,
+                                                                       d_seg);
+  GLASS_CUDA(cudaGetLastError(), "host_gather_kernel launch");
+  int rc = glass_gpu_dlogl_batch(ctx, precision, nitems, d_seg, d_params, has_tx ? d_tx : nullptr, d_dl, d_ty, d_hh,
+                                 d_st);
+  if (rc) return rc;
+  host_scatter_kernel<<<host_copy_grid(ctx, nitems), 256, 0, s>>>(d_io, nitems, d_dl, d_ty, d_hh, d_st);
+  GLASS_CUDA(cudaGetLastError(), "host_scatter_kernel launch");
+  ctx->last_launches += 2;
+  return GLASS_OK;
+}
+
 static int dlogl_host_enqueue(glass_gpu_ctx *ctx, int precision, int nitems, bool has_tx, size_t in_bytes,
                               size_t out_off, size_t out_bytes) {
   const size_t nd = (size_t)nitems;
@@ -487,6 +612,47 @@ extern "C" int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int
   const size_t out_off = (in_bytes + 255) / 256 * 256;
   const size_t out_bytes = sizeof(double) * 3 * nd + sizeof(int) * nd;
   const size_t bytes = out_off + out_bytes;
+  cudaStream_t s = ctx->stream;
+  if (ctx->host_direct) {
+    // + the device copy of the pointer block
+    if ((rc = ensure_stage(ctx, out_off + (out_bytes + 15) / 16 * 16 + sizeof(HostIo)))) return rc;
+    if ((rc = ensure_work(ctx, nitems))) return rc;
+    if (!ctx->h_io) GLASS_CUDA(cudaMallocHost(&ctx->h_io, sizeof(HostIo)), "cudaMallocHost(host io)");
+    // the previous call synchronised, so no kernel reads the block now
+    HostIo *io = ctx->h_io;
+    io->params = params;
+    io->term_x = term_x;
+    io->item_seg = item_seg;
+    io->dlogl = dlogl;
+    io->term_y = term_y;
+    io->hh = hh;
+    io->status = status;
+    const long long key = ((long long)nitems << 4) | (1LL << 3) | ((long long)precision << 1) | (has_tx ? 1 : 0);
+    auto it = ctx->host_graphs.find(key);
+    if (it != ctx->host_graphs.end() && !ctx->work.phase_timing) {
+      GLASS_CUDA(cudaGraphLaunch(it->second, s), "dlogl_batch_host graph launch");
+      ctx->last_launches = 5;
+    } else {
+      if ((rc = dlogl_direct_enqueue(ctx, precision, nitems, has_tx, out_off))) return rc;
+      GLASS_CUDA(cudaStreamSynchronize(s), "dlogl_batch_host sync");
+      if (!ctx->work.phase_timing && ctx->host_graphs.size() < 64) {
+        const int nl = ctx->last_launches;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          const int rc2 = dlogl_direct_enqueue(ctx, precision, nitems, has_tx, out_off);
+          const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+          if (rc2 == GLASS_OK && e2 == cudaSuccess && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess)
+            ctx->host_graphs[key] = ge;
+          if (g) cudaGraphDestroy(g);
+        }
+        cudaGetLastError();
+        ctx->last_launches = nl;
+      }
+    }
+    GLASS_CUDA(cudaStreamSynchronize(s), "dlogl_batch_host sync");
+    return GLASS_OK;
+  }
   // buffers first, so that nothing is reallocated while a graph is recorded
   if ((rc = ensure_stage(ctx, bytes))) return rc;
   if ((rc = ensure_host_stage(ctx, bytes))) return rc;
@@ -495,8 +661,7 @@ extern "C" int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int
   memcpy(h, params, sizeof(double) * 8 * nd);
   if (has_tx) memcpy(h + sizeof(double) * 8 * nd, term_x, sizeof(double) * nd);
   memcpy(h + sizeof(double) * 9 * nd, item_seg, sizeof(int) * nd);
-  cudaStream_t s = ctx->stream;
-  const long long key = ((long long)nitems << 3) | ((long long)precision << 1) | (has_tx ? 1 : 0);
+  const long long key = ((long long)nitems << 4) | ((long long)precision << 1) | (has_tx ? 1 : 0);
   auto it = ctx->host_graphs.find(key);
   if (it != ctx->host_graphs.end() && !ctx->work.phase_timing) {
     GLASS_CUDA(cudaGraphLaunch(it->second, s), "dlogl_batch_host graph launch");

@@ -133,16 +133,30 @@ int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const i
                           const double *term_x, double *dlogl, double *term_y, double *hh, int *status);
 
 /* Same as glass_gpu_dlogl_batch with HOST pointers: copies in, evaluates,
- * copies out and synchronises.  The inputs go through one pinned staging
- * buffer of the context (one copy each way), and the copy-in, kernels and
- * copy-out of a batch shape (nitems, precision, term_x given or not) are
- * recorded as a CUDA graph on the first call and replayed on later calls of
- * that shape; a new bank, a new template size or larger buffers drop the
- * recorded graphs.  Not to be called while the context's stream is being
- * captured. */
+ * copies out and synchronises.  Two ways to move the data (see
+ * glass_gpu_set_host_access): by default, where the device reads pageable
+ * host memory in place through the host's page tables (a coherent CPU-GPU
+ * link), a gather kernel reads the caller's arrays and a scatter kernel
+ * writes the results into them; otherwise the inputs go through one pinned
+ * staging buffer of the context (one copy each way).  Either sequence for a
+ * batch shape (nitems, precision, term_x given or not) is recorded as a CUDA
+ * graph on the first call and replayed on later calls of that shape; a new
+ * bank, a new template size or larger buffers drop the recorded graphs.  Not
+ * to be called while the context's stream is being captured. */
 int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
                                const double *params, const double *term_x, double *dlogl, double *term_y, double *hh,
                                int *status);
+
+/* How glass_gpu_dlogl_batch_host moves host data: mode 1 reads and writes the
+ * caller's arrays from the device in place (GLASS_ERR_STATE where the device
+ * cannot: cudaDevAttrPageableMemoryAccess and
+ * cudaDevAttrPageableMemoryAccessUsesHostPageTables both required), 0 copies
+ * through pinned staging, -1 (the default) picks 1 where supported.  The
+ * results are identical either way. */
+int glass_gpu_set_host_access(glass_gpu_ctx *ctx, int mode);
+/* supported: the device can access pageable host memory in place; direct: the
+ * in-place path is in use (either may be NULL). */
+int glass_gpu_get_host_access(glass_gpu_ctx *ctx, int *supported, int *direct);
 
 /*
  * Gradient of delta logL and Fisher matrix of a batch of proposals, by tangent

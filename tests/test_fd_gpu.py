@@ -377,3 +377,63 @@ def test_drop_in_waveform_from_concurrent_threads():
     assert not errors, errors
     for k in range(len(jobs)):
         np.testing.assert_array_equal(got[k], want[k])
+
+
+def test_host_access_paths_agree(engine, port):
+    """glass_gpu_dlogl_batch_host gives the same bits through pinned staging
+    and, where the device reads pageable host memory in place, through the
+    gather/scatter kernels; graph replays pick up new host arrays of the same
+    shape; NULL optional outputs are left out."""
+    rng = np.random.default_rng(31)
+    bank, inj = _random_bank(rng, 8, 1024, port)
+    engine.upload(bank)
+    n = 700
+    seg = rng.integers(0, 8, n).astype(np.int32)
+    draws = [np.array([wl.gaussian_jumps(rng, inj[s], wl.jump_scales(inj[s], 20.0), 1)[0] for s in seg])
+             for _ in range(3)]
+    tx = rng.normal(0, 5, n)
+    supported, direct = engine.host_access()
+    assert direct == supported  # the default picks the in-place path where it exists
+    modes = [0] + ([1] if supported else [])
+    if not supported:
+        with pytest.raises(gg.GlassError):
+            engine.set_host_access(1)
+    with pytest.raises(gg.GlassError):
+        engine.set_host_access(2)
+    res = {}
+    try:
+        for m in modes:
+            engine.set_host_access(m)
+            assert engine.host_access()[1] == (m == 1)
+            for prec in (gg.PREC_FP64, gg.PREC_MIXED):
+                for t in (None, tx):
+                    for k, p in enumerate(draws):  # first call records, later calls replay
+                        res[(m, prec, t is None, k)] = engine.dlogl_host(seg, p.copy(), term_x=t, precision=prec)
+            # optional outputs left NULL
+            dl = np.full(n, np.nan)
+            p = draws[0].copy()
+            gg._check(engine.lib.glass_gpu_dlogl_batch_host(engine._ctx, gg.PREC_MIXED, n, gg._pi(seg), gg._pd(p),
+                                                            None, gg._pd(dl), None, None, None))
+            np.testing.assert_array_equal(dl, res[(m, gg.PREC_MIXED, True, 0)][0])
+    finally:
+        engine.set_host_access(-1)
+    for (m, prec, notx, k), r in res.items():
+        ref = res[(0, prec, notx, k)]
+        for a, b in zip(r, ref):
+            np.testing.assert_array_equal(a, b)
+        assert (r[3] == 0).all()
+    # the draws differ, so a replay that kept old inputs would show
+    for m in modes:
+        assert not np.array_equal(res[(m, gg.PREC_FP64, True, 0)][1], res[(m, gg.PREC_FP64, True, 1)][1])
+    # and the device entry point agrees
+    import torch
+
+    p = draws[2]
+    d_out = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    d_st = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_seg, d_p, d_tx = (torch.tensor(a, device="cuda") for a in (seg, p, tx))
+    torch.cuda.synchronize()
+    engine.dlogl_device(d_seg, d_p, d_out[0], d_out[1], d_out[2], d_st, term_x=d_tx, precision=gg.PREC_MIXED)
+    torch.cuda.synchronize()
+    for a, b in zip(d_out, res[(modes[-1], gg.PREC_MIXED, False, 2)][:3]):
+        np.testing.assert_array_equal(a.cpu().numpy(), b)
