@@ -911,9 +911,11 @@ def bench_noise(gg, torch, dev, rank, steps, warmup, cpu, peak64):
 
 
 def bench_sampler(gg, torch, dev, steps, warmup):
-    """The on-device sampler step's tail for the headline workload's chains:
-    ucb_mcmc's accept/reject for 3072 chains and ptmcmc for 256 ladders of 12
-    temperatures, on device-resident state (CUDA events)."""
+    """The on-device sampler step for the headline workload's chains:
+    draw_from_fisher and ucb_mcmc's accept/reject for 3072 chains and ptmcmc
+    for 256 ladders of 12 temperatures, on device-resident state (CUDA events)."""
+    from glass_gb300 import workloads as gg_workloads
+
     rng = np.random.default_rng(5)
     n, NC = NSEG * 48, 12
     nens = n // NC
@@ -931,10 +933,16 @@ def bench_sampler(gg, torch, dev, steps, warmup):
     idx = t(np.tile(np.arange(NC), (nens, 1)), torch.int32)
     pacc = torch.zeros((nens, NC), dtype=torch.float64, device=dev)
     L = logL.view(nens, NC)
+    fx, fev, fel, fseed = gg_workloads.fisher_draw_inputs(rng, n=n)
+    fx, fev, fel = t(fx), t(fev), t(fel)
+    fseed = t(fseed.view(np.int32), torch.int32)
+    fy, fq = torch.empty((n, 8), dtype=torch.float64, device=dev), torch.empty(n, dtype=torch.float64, device=dev)
+    fst = torch.empty(n, dtype=torch.int32, device=dev)
     out = {}
     for name, fn in (("mh_accept", lambda: eng.mh_accept_device(T, dl, lpx, lpy, qxy, qyx, seed, logL, px, py,
                                                                 accepted=acc, snr=snr)),
-                     ("ptmcmc", lambda: eng.ptmcmc_device(temps, L, idx, seed.view(nens, NC), pacc))):
+                     ("ptmcmc", lambda: eng.ptmcmc_device(temps, L, idx, seed.view(nens, NC), pacc)),
+                     ("fisher_draw", lambda: eng.fisher_draw_device(fx, fev, fel, fseed, fy, fq, fst))):
         with torch.cuda.stream(stream):
             for _ in range(warmup):
                 fn()
@@ -948,8 +956,8 @@ def bench_sampler(gg, torch, dev, steps, warmup):
         out[name + "_us"] = 1e3 * a.elapsed_time(b) / steps
     eng.set_stream(None)
     eng.close()
-    return {"workload": f"{n} chains: ucb_mcmc accept/reject tail; {nens} ladders x {NC} temperatures: ptmcmc; "
-                        f"reference rand_r streams", **out}
+    return {"workload": f"{n} chains: ucb_mcmc accept/reject tail and draw_from_fisher; {nens} ladders x {NC} "
+                        f"temperatures: ptmcmc; reference rand_r streams", **out}
 
 
 def run_ours(args):

@@ -23,6 +23,8 @@ FORMATS = {"sangria": 0, "phase": 1, "frequency": 2}
 ITEM_NONFINITE = 1
 ITEM_BAD_SEGMENT = 2
 ITEM_OUTSIDE = 4
+# glass_gpu_fisher_draw status codes
+DRAW_OK, DRAW_NAN, DRAW_RNG_LIMIT = 0, 1, 2
 
 _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int)
@@ -49,7 +51,7 @@ EXPORTS = (
     "glass_gpu_noise_setup", "glass_gpu_noise_logl_batch", "glass_gpu_noise_logl_batch_host",
     "glass_gpu_noise_wavelet_setup", "glass_gpu_noise_wavelet_logl_batch", "glass_gpu_noise_wavelet_logl_batch_host",
     "glass_gpu_dlogl_batch_channels", "glass_gpu_noise_eta_batch", "glass_gpu_noise_eta_batch_host",
-    "glass_gpu_rand_r_fill", "glass_gpu_mh_accept", "glass_gpu_ptmcmc",
+    "glass_gpu_rand_r_fill", "glass_gpu_mh_accept", "glass_gpu_fisher_draw", "glass_gpu_ptmcmc",
 )
 
 _lib = None
@@ -73,6 +75,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_set_stream.argtypes = [_V, _V]
     lib.glass_gpu_last_launch_count.argtypes = [_V]
     lib.glass_gpu_set_phase_timing.argtypes = [_V, ctypes.c_int]
+    lib.glass_gpu_fisher_draw.argtypes = [_V, ctypes.c_int] + [_V] * 7
     lib.glass_gpu_set_host_access.argtypes = [_V, ctypes.c_int]
     lib.glass_gpu_get_host_access.argtypes = [_V, _I, _I]
     lib.glass_gpu_last_phase_ms.argtypes = [_V, ctypes.POINTER(ctypes.c_float)]
@@ -488,6 +491,14 @@ class Engine:
         nens, NC = int(index.shape[0]), int(index.shape[1])
         _check(self.lib.glass_gpu_ptmcmc(self._ctx, nens, NC, _ptr(temperature), _ptr(logL), _ptr(logLnorm),
                                          _ptr(index), _ptr(seed), _ptr(acceptance)))
+
+    def fisher_draw_device(self, params_x, evec, evalue, seed, params_y, logQ=None, status=None):
+        """draw_from_fisher for n chains (device tensors: params_x/params_y [n, 8],
+        evec [n, 8, 8] with evec[i, j, k] = fisher_evectr[j][k], evalue [n, 8],
+        seed uint32/int32 [n] advanced in place)."""
+        n = int(params_x.shape[0])
+        _check(self.lib.glass_gpu_fisher_draw(self._ctx, n, _ptr(params_x), _ptr(evec), _ptr(evalue), _ptr(seed),
+                                              _ptr(params_y), _ptr(logQ), _ptr(status)))
 
     def wavelet_dlogl_device(self, params, dlogl, term_y=None, hh=None, status=None, term_x=None,
                              precision=PREC_FP64):

@@ -33,7 +33,7 @@ PER_FILE_FLAGS = {"ucb_fd.cu": ["-fmad=false"], "ucb_fd_fp64.cu": ["-fmad=false"
                   "wdm.cu": ["-Xcompiler", "-ffp-contract=off"],
                   "ucb_wavelet.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
                   "ucb_fstat.cu": ["-fmad=false"], "noise.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
-                  "capi.cu": ["-Xcompiler", "-ffp-contract=off"]}
+                  "capi.cu": ["-Xcompiler", "-ffp-contract=off"], "sampler.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:

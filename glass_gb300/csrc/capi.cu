@@ -1217,6 +1217,20 @@ extern "C" int glass_gpu_ptmcmc(glass_gpu_ctx *ctx, int nens, int NC, const doub
   return GLASS_OK;
 }
 
+extern "C" int glass_gpu_fisher_draw(glass_gpu_ctx *ctx, int n, const double *params_x, const double *evec,
+                                     const double *evalue, unsigned int *seed, double *params_y, double *logQ,
+                                     int *status) {
+  if (!ctx || n < 0) return set_err(GLASS_ERR_ARG, "fisher_draw: bad argument");
+  if (n == 0) return GLASS_OK;
+  if (!params_x || !evec || !evalue || !seed || !params_y) return set_err(GLASS_ERR_ARG, "fisher_draw: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  FisherDrawArgs a{n, params_x, evec, evalue, seed, params_y, logQ, status};
+  GLASS_CUDA(fisher_draw_launch(a, ctx->stream), "fisher_draw");
+  ctx->last_launches = 1;
+  return GLASS_OK;
+}
+
 // ------------------------------------------------------- drop-in functions
 // Layout of struct Orbit (utils/src/glass_lisa.h:60-109), restated so the
 // drop-in ucb_waveform can read the arm length, transfer frequency and the

@@ -47,6 +47,73 @@ __global__ void rand_r_fill_kernel(int n, int count, unsigned int *seed, int *ou
   seed[i] = s;
 }
 
+// rand_r_N_0_1 (utils/src/glass_utils.c:24-35): Marsaglia's polar method on
+// rand_r_U_0_1 pairs.  The rejection loop is bounded: a run of 4096 rejections
+// has probability (1 - pi/4)^4096, and then the chain reports
+// GLASS_DRAW_RNG_LIMIT instead of looping on.
+__device__ __forceinline__ bool glass_n01(unsigned int *seed, double *z) {
+  for (int it = 0; it < 4096; it++) {
+    const double u = 2 * glass_u01(seed) - 1;
+    const double v = 2 * glass_u01(seed) - 1;
+    const double s = u * u + v * v;
+    if (!(s >= 1 || s == 0)) {
+      *z = u * sqrt(-2 * log(s) / s);
+      return true;
+    }
+  }
+  *z = 0.0;
+  return false;
+}
+
+// draw_from_fisher (ucb/src/glass_ucb_proposal.c:348-391), one thread per
+// chain: eight N(0,1) amplitudes over sqrt(eigenvalue), one eigenvector picked
+// by a ninth draw, the jump along it, the NaN and |cos| >= 1 repairs.
+__global__ void fisher_draw_kernel(FisherDrawArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double *x = a.params_x + 8 * (size_t)i;
+  const double *ev = a.evec + 64 * (size_t)i;
+  const double *el = a.evalue + 8 * (size_t)i;
+  double *y = a.params_y + 8 * (size_t)i;
+  unsigned int s = a.seed[i];
+  int st = GLASS_DRAW_OK;
+  double amps[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    double z;
+    if (!glass_n01(&s, &z)) st = GLASS_DRAW_RNG_LIMIT;
+    amps[k] = z / sqrt(el[k]);
+  }
+  // (int)(U * 8) is 8 when rand_r returns RAND_MAX (U = 1), where the
+  // reference reads one column past the matrix; the last column is taken here
+  int c = (int)(glass_u01(&s) * 8.0);
+  if (c > 7) c = 7;
+  double jump[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    jump[j] = 0.0;
+    jump[j] += amps[c] * ev[8 * j + c];
+    if (jump[j] != jump[j]) jump[j] = 0.01 * x[j];
+  }
+  double p[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) p[j] = x[j] + jump[j];
+  if (p[1] >= 1.) p[1] = x[1] - jump[1];
+  if (p[1] <= -1.) p[1] = x[1] - jump[1];
+  if (p[4] >= 1.) p[4] = x[4] - jump[4];
+  if (p[4] <= -1.) p[4] = x[4] - jump[4];
+  double logQ = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    y[j] = p[j];
+    if (p[j] != p[j]) logQ = -INFINITY;
+  }
+  if (logQ < 0.0 && st == GLASS_DRAW_OK) st = GLASS_DRAW_NAN;
+  a.seed[i] = s;
+  if (a.logQ) a.logQ[i] = logQ;
+  if (a.status) a.status[i] = st;
+}
+
 // ucb/src/glass_ucb_sampler.c:141-172, one thread per chain.
 __global__ void mh_accept_kernel(MhArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,6 +183,13 @@ cudaError_t rand_r_fill_launch(int n, int count, unsigned int *seed, int *out, c
 
 cudaError_t mh_accept_launch(const MhArgs &a, cudaStream_t stream) {
   mh_accept_kernel<<<(a.n + 255) / 256, 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t fisher_draw_launch(const FisherDrawArgs &a, cudaStream_t stream) {
+  // one warp per CTA: the kernel is bound by the FP64 pipe of the SMs it
+  // occupies, so the chains are spread over as many SMs as possible
+  fisher_draw_kernel<<<(a.n + 31) / 32, 32, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -211,3 +211,31 @@ def galaxy_modulation_like(Ncoarse, phase=0.0):
     q = np.arange(Ncoarse)
     a = [1.0 + 0.3 * np.cos(2 * np.pi * q / Ncoarse + phase + 2.1 * k) for k in range(3)]
     return np.stack(a + [-0.45 * np.sqrt(a[0] * a[1]), -0.45 * np.sqrt(a[0] * a[2]), -0.45 * np.sqrt(a[1] * a[2])])
+
+
+def fisher_draw_inputs(rng, n=64):
+    """Chains for draw_from_fisher: UCB parameter arrays (f0 T, cos theta, phi,
+    ln A, cos iota, psi, phi0, fdot T^2), Fisher eigenvectors from random
+    orthogonal matrices and eigenvalues from 1e2 to 1e12; the last chains are
+    edge cases: cosines near +-1 with wide jumps (reflections), a zero and a
+    negative eigenvalue (infinite and NaN amplitudes), a NaN parameter."""
+    T = 31457280.0
+    x = np.column_stack([rng.uniform(1e-3, 1e-2, n) * T, rng.uniform(-1, 1, n), rng.uniform(0, 2 * np.pi, n),
+                         np.log(10 ** rng.uniform(-23, -21, n)), rng.uniform(-1, 1, n), rng.uniform(0, np.pi, n),
+                         rng.uniform(0, 2 * np.pi, n), rng.normal(0, 1, n)])
+    evec = np.zeros((n, 8, 8))
+    evalue = np.zeros((n, 8))
+    for i in range(n):
+        q, r = np.linalg.qr(rng.normal(size=(8, 8)))
+        evec[i] = q * np.sign(np.diag(r))
+        evalue[i] = 10 ** rng.uniform(2, 12, 8)
+    for i in range(n - 8, n - 4):  # cosines at the edge, jumps of order 1
+        x[i, 1] = 0.9999 if i % 2 else -0.9999
+        x[i, 4] = -0.9998 if i % 2 else 0.9998
+        evalue[i] = 1.0
+    evalue[n - 4, 3] = 0.0
+    evalue[n - 3, 5] = -1.0
+    evalue[n - 3, 2] = 0.0
+    x[n - 2, 6] = np.nan
+    seed = rng.integers(1, 2**31, n).astype(np.uint32)
+    return x, evec, evalue, seed

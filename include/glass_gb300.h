@@ -324,13 +324,31 @@ int glass_gpu_noise_eta_batch_host(glass_gpu_ctx *ctx, int precision, int n, con
  * of NC chains: ladder e's chain c at e NC + c of logL, logLnorm (may be
  * NULL), index (the ladder's permutation of 0..NC-1), seed and acceptance;
  * temperature[NC] shared.
+ *
+ * glass_gpu_fisher_draw: draw_from_fisher (ucb/src/glass_ucb_proposal.c:348-391)
+ * for n chains: from params_x[8 i ..], the eigenvectors evec[64 i + 8 j + k]
+ * (= source->fisher_evectr[j][k]) and eigenvalues evalue[8 i ..], eight
+ * rand_r_N_0_1 amplitudes (utils/src/glass_utils.c:24-35) over sqrt(eigenvalue)
+ * and one rand_r_U_0_1 choice of the eigenvector, the jump along it, a NaN jump
+ * component replaced by 0.01 params_x, params_y = params_x + jump with the two
+ * cosines reflected back where they reach +-1.  logQ[i] (may be NULL) is 0, or
+ * -inf where a drawn parameter is NaN (the reference's return value);
+ * status[i] (may be NULL) a GLASS_DRAW_* code.  The seeds advance exactly as
+ * the reference's; the parameters agree with the C library's to within the
+ * last bits of its log.  Where the choice draw is RAND_MAX the reference reads
+ * one column past the matrix; the last column is used here.
  */
+#define GLASS_DRAW_OK 0
+#define GLASS_DRAW_NAN 1        /* a drawn parameter is NaN: logQ = -inf */
+#define GLASS_DRAW_RNG_LIMIT 2  /* 4096 rejections in a row in the polar method (probability ~1e-2700) */
 int glass_gpu_rand_r_fill(glass_gpu_ctx *ctx, int n, int count, unsigned int *seed, int *out);
 int glass_gpu_mh_accept(glass_gpu_ctx *ctx, int n, const double *temperature, const double *dlogl, const double *logPx,
                         const double *logPy, const double *logQxy, const double *logQyx, const double *snr,
                         unsigned int *seed, double *logL_x, double *params_x, const double *params_y, int *accepted);
 int glass_gpu_ptmcmc(glass_gpu_ctx *ctx, int nens, int NC, const double *temperature, const double *logL,
                      const double *logLnorm, int *index, unsigned int *seed, double *acceptance);
+int glass_gpu_fisher_draw(glass_gpu_ctx *ctx, int n, const double *params_x, const double *evec, const double *evalue,
+                          unsigned int *seed, double *params_y, double *logQ, int *status);
 
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);

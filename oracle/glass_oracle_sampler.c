@@ -87,3 +87,51 @@ void orc_mh_accept(int n, const double *T, double *logL_x, const double *dlogl, 
         }
     }
 }
+
+/* rand_r_N_0_1 (utils/src/glass_utils.c:24-35): Marsaglia's polar method. */
+static double orc_n01(unsigned int *seed)
+{
+    double u, v, s;
+    do {
+        u = 2 * orc_u01(seed) - 1;
+        v = 2 * orc_u01(seed) - 1;
+        s = u * u + v * v;
+    } while (s >= 1 || s == 0);
+    return u * sqrt(-2 * log(s) / s);
+}
+
+/*
+ * draw_from_fisher (ucb/src/glass_ucb_proposal.c:348-391) for n chains: chain
+ * i's parameters x = params_x[8 i ..], eigenvectors evec[64 i + 8 j + k] =
+ * fisher_evectr[j][k], eigenvalues evalue[8 i ..].  Eight N(0,1) amplitudes
+ * over sqrt(eigenvalue), one uniform picks the eigenvector c, jump_j = amp_c
+ * evec[j][c] (0.01 x_j where that is NaN), y = x + jump with cos(theta) and
+ * cos(iota) reflected (x - jump) where they reach +-1; logQ = 0, or -inf where
+ * a parameter of y is NaN.  c is clamped to 7 when the uniform is exactly 1.
+ */
+void orc_fisher_draw(int n, const double *params_x, const double *evec, const double *evalue, unsigned int *seed,
+                     double *params_y, double *logQ)
+{
+    for (int i = 0; i < n; i++) {
+        const double *x = params_x + 8 * (size_t)i, *ev = evec + 64 * (size_t)i, *el = evalue + 8 * (size_t)i;
+        double *y = params_y + 8 * (size_t)i;
+        double amps[8], jump[8];
+        for (int k = 0; k < 8; k++) {
+            amps[k] = orc_n01(&seed[i]) / sqrt(el[k]);
+            jump[k] = 0.0;
+        }
+        int c = (int)(orc_u01(&seed[i]) * 8.0);
+        if (c > 7) c = 7;
+        for (int j = 0; j < 8; j++) jump[j] += amps[c] * ev[8 * j + c];
+        for (int j = 0; j < 8; j++)
+            if (jump[j] != jump[j]) jump[j] = 0.01 * x[j];
+        for (int j = 0; j < 8; j++) y[j] = x[j] + jump[j];
+        if (y[1] >= 1.) y[1] = x[1] - jump[1];
+        if (y[1] <= -1.) y[1] = x[1] - jump[1];
+        if (y[4] >= 1.) y[4] = x[4] - jump[4];
+        if (y[4] <= -1.) y[4] = x[4] - jump[4];
+        logQ[i] = 0.0;
+        for (int j = 0; j < 8; j++)
+            if (y[j] != y[j]) logQ[i] = -INFINITY;
+    }
+}

@@ -284,6 +284,21 @@ class Port:
                           _p(params_x), c(params_y), acc.ctypes.data_as(_I))
         return acc
 
+    def fisher_draw(self, params_x, evec, evalue, seed):
+        """draw_from_fisher for n chains: params_x [n, 8], evec [n, 8, 8]
+        (evec[i, j, k] = fisher_evectr[j][k]), evalue [n, 8]; seed (uint32 [n])
+        advanced in place; returns (params_y [n, 8], logQ [n])."""
+        lib = self.lib
+        lib.orc_fisher_draw.argtypes = [ctypes.c_int, _D, _D, _D, ctypes.POINTER(ctypes.c_uint), _D, _D]
+        x = np.ascontiguousarray(params_x, np.float64).reshape(-1, 8)
+        n = len(x)
+        y = np.zeros((n, 8))
+        logQ = np.zeros(n)
+        lib.orc_fisher_draw(n, _p(x), _p(np.ascontiguousarray(evec, np.float64)),
+                            _p(np.ascontiguousarray(evalue, np.float64)),
+                            seed.ctypes.data_as(ctypes.POINTER(ctypes.c_uint)), _p(y), _p(logQ))
+        return y, logQ
+
     def orbit(self, t):
         out = np.zeros(9)
         self.lib.orc_orbit_positions(float(t), _p(out))
@@ -624,6 +639,23 @@ class Ref:
         lib.ref_noise_eta(fmt.encode(), T, t0, NFFT, qmin, _p(dA), _p(dE), _p(invCA), _p(invCE), len(params),
                           _p(params), _p(eta), _p(out))
         return out
+
+    def fisher_draw(self, params_x, evec, evalue, seed):
+        """The reference's draw_from_fisher chain by chain (same layout as the
+        port's); seed advanced in place; returns (params_y, logQ)."""
+        lib = self.lib
+        lib.ref_fisher_draw.restype = ctypes.c_double
+        lib.ref_fisher_draw.argtypes = [_D, _D, _D, ctypes.POINTER(ctypes.c_uint), _D]
+        x = np.ascontiguousarray(params_x, np.float64).reshape(-1, 8)
+        ev = np.ascontiguousarray(evec, np.float64).reshape(-1, 64)
+        el = np.ascontiguousarray(evalue, np.float64).reshape(-1, 8)
+        y = np.zeros_like(x)
+        logQ = np.zeros(len(x))
+        for i in range(len(x)):
+            s = ctypes.c_uint(int(seed[i]))
+            logQ[i] = lib.ref_fisher_draw(_p(x[i]), _p(ev[i]), _p(el[i]), ctypes.byref(s), _p(y[i]))
+            seed[i] = s.value
+        return y, logQ
 
     def ptmcmc(self, temperature, logL, index, seed, acceptance, logLnorm=None):
         """The reference's ptmcmc on one ladder, in place."""

@@ -768,3 +768,25 @@ void ref_ptmcmc(int NC, const double *temperature, const double *logL, const dou
     free(m);
     free(model);
 }
+
+/* The reference's draw_from_fisher (ucb/src/glass_ucb_proposal.c:348-391) on
+ * one source: x[8], evec[64] (row j = fisher_evectr[j]), evalue[8]; returns
+ * its value (0 or -inf) and writes the drawn parameters to y[8]. */
+double ref_fisher_draw(const double *x, const double *evec, const double *evalue, unsigned int *seed, double *y)
+{
+    struct Source s;
+    memset(&s, 0, sizeof(s));
+    double params[8], val[8], rows[8][8];
+    double *rowp[8];
+    memcpy(params, x, sizeof(params));
+    memcpy(val, evalue, sizeof(val));
+    for (int j = 0; j < 8; j++) {
+        memcpy(rows[j], evec + 8 * j, sizeof(rows[j]));
+        rowp[j] = rows[j];
+    }
+    s.NP = 8;
+    s.params = params;
+    s.fisher_evalue = val;
+    s.fisher_evectr = rowp;
+    return draw_from_fisher(NULL, NULL, &s, NULL, y, seed);
+}

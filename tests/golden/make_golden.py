@@ -423,8 +423,22 @@ def sampler(ref, rng):
                         seed1=np.array(s1), indexN=np.array(idxN), accN=np.array(accN), seedN=np.array(sN))
 
 
+def fisher_draw(ref, rng):
+    """draw_from_fisher (ucb/src/glass_ucb_proposal.c:348) of 64 chains, four
+    successive draws each from the same state: the drawn parameters, the
+    return values and the seeds after every draw."""
+    x, evec, evalue, seed0 = wl.fisher_draw_inputs(rng)
+    seed = seed0.copy()
+    ys, qs, ss = [], [], []
+    for k in range(4):
+        y, q = ref.fisher_draw(x, evec, evalue, seed)
+        ys.append(y), qs.append(q), ss.append(seed.copy())
+    np.savez_compressed(os.path.join(HERE, "fisher_draw.npz"), x=x, evec=evec, evalue=evalue, seed0=seed0,
+                        y=np.array(ys), logQ=np.array(qs), seeds=np.array(ss))
+
+
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
-             "sampler": 20261208}
+             "sampler": 20261208, "fisher_draw": 20261209}
 
 
 def main(names=()):
@@ -446,6 +460,7 @@ def main(names=()):
     noise_wavelet(ref, np.random.default_rng(OWN_SEEDS["noise_wavelet"]))
     noise_eta(ref, np.random.default_rng(OWN_SEEDS["noise_eta"]))
     sampler(ref, np.random.default_rng(OWN_SEEDS["sampler"]))
+    fisher_draw(ref, np.random.default_rng(OWN_SEEDS["fisher_draw"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -317,3 +317,17 @@ def test_ptmcmc_matches_reference(port, golden):
         np.testing.assert_array_equal(index, g["index" + tag])
         np.testing.assert_array_equal(seed, g["seed" + tag])
         np.testing.assert_array_equal(acc, g["acc" + tag])
+
+
+def test_fisher_draw_matches_reference(port, golden):
+    """draw_from_fisher (ucb/src/glass_ucb_proposal.c:348-391): four successive
+    draws per chain, including reflections at cos = +-1, zero and negative
+    eigenvalues and a NaN parameter: seeds and return values exactly, the
+    drawn parameters to the last bits of the C library's log."""
+    g = golden("fisher_draw.npz")
+    seed = g["seed0"].copy()
+    for k in range(4):
+        y, logQ = port.fisher_draw(g["x"], g["evec"], g["evalue"], seed)
+        np.testing.assert_array_equal(seed, g["seeds"][k])
+        np.testing.assert_array_equal(logQ, g["logQ"][k])
+        np.testing.assert_allclose(y, g["y"][k], rtol=1e-14, atol=0)

@@ -103,3 +103,49 @@ def test_mh_accept_matches_restated_reference(engine, port):
         np.testing.assert_array_equal(d["logL"].cpu().numpy(), logL)
         np.testing.assert_array_equal(d["px"].cpu().numpy(), px)
     assert 0.05 < acc_ref.mean() < 0.9
+
+
+def _fisher_draw_device(engine, x, evec, evalue, seed, draws):
+    import torch
+
+    dx, dev, del_ = (torch.tensor(np.ascontiguousarray(a, np.float64), device="cuda") for a in (x, evec, evalue))
+    ds = torch.tensor(_u32(seed), device="cuda")
+    n = len(x)
+    dy = torch.empty((n, 8), dtype=torch.float64, device="cuda")
+    dq = torch.empty(n, dtype=torch.float64, device="cuda")
+    dst = torch.empty(n, dtype=torch.int32, device="cuda")
+    out = []
+    torch.cuda.synchronize()
+    for _ in range(draws):
+        engine.fisher_draw_device(dx, dev, del_, ds, dy, dq, dst)
+        torch.cuda.synchronize()
+        out.append((dy.cpu().numpy().copy(), dq.cpu().numpy().copy(), dst.cpu().numpy().copy(),
+                    ds.cpu().numpy().view(np.uint32).copy()))
+    return out
+
+
+def test_fisher_draw_matches_reference(engine, golden):
+    """draw_from_fisher on the device against the reference's own draws
+    (golden vectors): seeds and return values exactly, parameters to 1e-14
+    relative (the device's log against the C library's)."""
+    g = golden("fisher_draw.npz")
+    res = _fisher_draw_device(engine, g["x"], g["evec"], g["evalue"], g["seed0"], 4)
+    for k, (y, q, st, s) in enumerate(res):
+        np.testing.assert_array_equal(s, g["seeds"][k])
+        np.testing.assert_array_equal(q, g["logQ"][k])
+        np.testing.assert_allclose(y, g["y"][k], rtol=1e-14, atol=0)
+        np.testing.assert_array_equal(st, np.where(np.isinf(q), gg.DRAW_NAN, gg.DRAW_OK))
+
+
+def test_fisher_draw_many_chains(engine, port):
+    """3072 chains, eight successive draws, against the oracle's restatement."""
+    from glass_gb300 import workloads as wl
+
+    x, evec, evalue, seed = wl.fisher_draw_inputs(np.random.default_rng(33), n=3072)
+    res = _fisher_draw_device(engine, x, evec, evalue, seed, 8)
+    s = seed.copy()
+    for y, q, st, sd in res:
+        yr, qr = port.fisher_draw(x, evec, evalue, s)
+        np.testing.assert_array_equal(sd, s)
+        np.testing.assert_array_equal(q, qr)
+        np.testing.assert_allclose(y, yr, rtol=1e-14, atol=0)
