@@ -65,12 +65,11 @@ __device__ __forceinline__ bool glass_n01(unsigned int *seed, double *z) {
   return false;
 }
 
-// draw_from_fisher (ucb/src/glass_ucb_proposal.c:348-391), one thread per
-// chain: eight N(0,1) amplitudes over sqrt(eigenvalue), one eigenvector picked
-// by a ninth draw, the jump along it, the NaN and |cos| >= 1 repairs.
-__global__ void fisher_draw_kernel(FisherDrawArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+// draw_from_fisher (ucb/src/glass_ucb_proposal.c:348-391) for chain i by one
+// thread, in the reference's order: eight N(0,1) amplitudes over
+// sqrt(eigenvalue), one eigenvector picked by a ninth draw, the jump along
+// it, the NaN and |cos| >= 1 repairs.
+__device__ void fisher_draw_serial(const FisherDrawArgs &a, int i) {
   const double *x = a.params_x + 8 * (size_t)i;
   const double *ev = a.evec + 64 * (size_t)i;
   const double *el = a.evalue + 8 * (size_t)i;
@@ -112,6 +111,107 @@ __global__ void fisher_draw_kernel(FisherDrawArgs a) {
   a.seed[i] = s;
   if (a.logQ) a.logQ[i] = logQ;
   if (a.status) a.status[i] = st;
+}
+
+
+// rand_r's linear congruence advanced k steps at once: next = A next + C.
+__device__ __forceinline__ void lcg_jump(int k, unsigned int &A, unsigned int &C) {
+  A = 1u;
+  C = 0u;
+  for (int j = 0; j < k; j++) {
+    A *= 1103515245u;
+    C = C * 1103515245u + 12345u;
+  }
+}
+
+// The same draw with eight lanes per chain.  The polar method's pairs are
+// independent given the stream, so the lanes generate the chain's next 48
+// rand_r values at once (lane l takes values l, l + 8, ..., each rand_r being
+// three steps of the congruence, reached by jumps), test the 24 pairs, and
+// the k-th accepted pair gives lane k its amplitude: the FP64 log and sqrt of
+// the eight amplitudes run side by side instead of one after another.  The
+// ninth draw is the value after the eighth accepted pair, and the seed ends
+// where it ends for the reference.  When the 48 values hold fewer than eight
+// accepted pairs and the choice (probability about 1e-8), the chain's first
+// lane redoes the draw in the reference's order.
+__global__ void __launch_bounds__(128) fisher_draw_kernel(FisherDrawArgs a) {
+  constexpr int V = 48;  // values per chain and pass: 24 pairs
+  __shared__ int val[16][V];
+  __shared__ unsigned int post[16][V];  // the seed after each value
+  const int gi = threadIdx.x >> 3, sub = threadIdx.x & 7;
+  const int i = blockIdx.x * 16 + gi;
+  if (i >= a.n) return;  // all eight lanes of a chain leave together
+  const unsigned int gmask = 0xffu << (threadIdx.x & 24);
+  const unsigned int s0 = a.seed[i];
+  {
+    unsigned int A, C, A8, C8;
+    lcg_jump(3 * sub, A, C);
+    lcg_jump(24, A8, C8);
+    unsigned int st = A * s0 + C;  // the state before value sub
+    for (int q = 0; q < V / 8; q++) {
+      unsigned int t = st;
+      val[gi][sub + 8 * q] = glass_rand_r(&t);
+      post[gi][sub + 8 * q] = t;
+      st = A8 * st + C8;
+    }
+  }
+  __syncwarp(gmask);
+  // pair p accepted: s in (0, 1)
+  unsigned int accmask = 0;
+  for (int p = sub; p < V / 2; p += 8) {
+    const double u = 2 * ((double)val[gi][2 * p] / 2147483647.0) - 1;
+    const double v = 2 * ((double)val[gi][2 * p + 1] / 2147483647.0) - 1;
+    const double s = u * u + v * v;
+    if (!(s >= 1 || s == 0)) accmask |= 1u << p;
+  }
+  // OR over the chain's lanes
+  for (int o = 4; o > 0; o >>= 1) accmask |= __shfl_xor_sync(gmask, accmask, o, 8);
+  // pair of the k-th accepted (k = sub), and of the eighth
+  int pk = -1, p7 = -1;
+  {
+    unsigned int m = accmask;
+    for (int k = 0; k < 8 && m; k++) {
+      const int p = __ffs(m) - 1;
+      m &= m - 1;
+      if (k == sub) pk = p;
+      if (k == 7) p7 = p;
+    }
+  }
+  const bool fast = p7 >= 0 && 2 * p7 + 2 < V;
+  if (!fast) {
+    if (sub == 0) fisher_draw_serial(a, i);
+    return;
+  }
+  const double *x = a.params_x + 8 * (size_t)i;
+  double amp;
+  {
+    const double u = 2 * ((double)val[gi][2 * pk] / 2147483647.0) - 1;
+    const double v = 2 * ((double)val[gi][2 * pk + 1] / 2147483647.0) - 1;
+    const double s = u * u + v * v;
+    const double z = u * sqrt(-2 * log(s) / s);
+    amp = z / sqrt(a.evalue[8 * (size_t)i + sub]);
+  }
+  int c = (int)(((double)val[gi][2 * p7 + 2] / 2147483647.0) * 8.0);
+  if (c > 7) c = 7;
+  const double ampc = __shfl_sync(gmask, amp, c, 8);
+  // lane j: component j of the jump and of the drawn parameters
+  const int j = sub;
+  const double xj = x[j];
+  double jump = 0.0;
+  jump += ampc * a.evec[64 * (size_t)i + 8 * j + c];
+  if (jump != jump) jump = 0.01 * xj;
+  double y = xj + jump;
+  if (j == 1 || j == 4) {
+    if (y >= 1.) y = xj - jump;
+    if (y <= -1.) y = xj - jump;
+  }
+  a.params_y[8 * (size_t)i + j] = y;
+  const bool nan_any = __any_sync(gmask, y != y);
+  if (sub == 0) {
+    a.seed[i] = post[gi][2 * p7 + 2];
+    if (a.logQ) a.logQ[i] = nan_any ? -INFINITY : 0.0;
+    if (a.status) a.status[i] = nan_any ? GLASS_DRAW_NAN : GLASS_DRAW_OK;
+  }
 }
 
 // ucb/src/glass_ucb_sampler.c:141-172, one thread per chain.
@@ -182,19 +282,20 @@ cudaError_t rand_r_fill_launch(int n, int count, unsigned int *seed, int *out, c
 }
 
 cudaError_t mh_accept_launch(const MhArgs &a, cudaStream_t stream) {
-  mh_accept_kernel<<<(a.n + 255) / 256, 256, 0, stream>>>(a);
+  // one warp per CTA, like the exchanges below: the chains' FP64 log calls
+  // are spread over as many SMs as there are warps
+  mh_accept_kernel<<<(a.n + 31) / 32, 32, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t fisher_draw_launch(const FisherDrawArgs &a, cudaStream_t stream) {
-  // one warp per CTA: the kernel is bound by the FP64 pipe of the SMs it
-  // occupies, so the chains are spread over as many SMs as possible
-  fisher_draw_kernel<<<(a.n + 31) / 32, 32, 0, stream>>>(a);
+  // eight lanes per chain, sixteen chains per CTA
+  fisher_draw_kernel<<<(a.n + 15) / 16, 128, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
 cudaError_t ptmcmc_launch(const PtArgs &a, cudaStream_t stream) {
-  ptmcmc_kernel<<<(a.nens + 127) / 128, 128, 0, stream>>>(a);
+  ptmcmc_kernel<<<(a.nens + 31) / 32, 32, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -138,10 +138,24 @@ def test_fisher_draw_matches_reference(engine, golden):
 
 
 def test_fisher_draw_many_chains(engine, port):
-    """3072 chains, eight successive draws, against the oracle's restatement."""
+    """3072 chains, eight successive draws, against the oracle's restatement.
+    The first six seeds start draws that need more than the 48 rand_r values
+    the kernel's lanes generate at once (fewer than eight accepted polar pairs
+    in them, or the eighth in the last pair), so those chains take the
+    one-lane path; the test checks that they do need more."""
     from glass_gb300 import workloads as wl
 
     x, evec, evalue, seed = wl.fisher_draw_inputs(np.random.default_rng(33), n=3072)
+    long_seeds = np.array([620013, 1277705, 2079646, 1627781, 2377129, 3502334], np.uint32)
+    seed[:6] = long_seeds
+    for k in range(6):  # values one draw consumes from each of these seeds
+        s1 = seed[k:k + 1].copy()
+        port.fisher_draw(x[k:k + 1], evec[k:k + 1], evalue[k:k + 1], s1)
+        st, used = seed[k:k + 1].copy(), 0
+        while st[0] != s1[0]:
+            _, st = port.rand_r_seq(st, 1)
+            used += 1
+        assert used > 48, (k, used)
     res = _fisher_draw_device(engine, x, evec, evalue, seed, 8)
     s = seed.copy()
     for y, q, st, sd in res:
