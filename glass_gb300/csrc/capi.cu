@@ -512,39 +512,50 @@ __device__ __forceinline__ void host_io_load_block(const HostIo *io, HostIo *s, 
 }
 
 // params (8n doubles), term_x (n, when given), item_seg (n ints) into the
-// device stage
+// device stage: one element per thread over a flat index (16-byte pairs of
+// params where the caller's array allows), so that each thread waits for one
+// host-memory round trip, not one per array
 __global__ void host_gather_kernel(const HostIo *io, HostIo *d_io, int n, double *d_params, double *d_tx,
                                    int *d_seg) {
   __shared__ HostIo h;
   host_io_load_block(io, &h, d_io);
+  const bool v2 = (reinterpret_cast<unsigned long long>(h.params) & 15) == 0;
+  const long long np = v2 ? 4LL * n : 8LL * n;  // params elements
+  const long long tot = np + 2LL * n;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if ((reinterpret_cast<unsigned long long>(h.params) & 15) == 0) {
-    const double2 *src = reinterpret_cast<const double2 *>(h.params);
-    double2 *dst = reinterpret_cast<double2 *>(d_params);
-    for (long long i = t; i < 4LL * n; i += stride) dst[i] = __ldcv(src + i);
-  } else {
-    for (long long i = t; i < 8LL * n; i += stride) d_params[i] = __ldcv(h.params + i);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot; i += stride) {
+    if (i < np) {
+      if (v2)
+        reinterpret_cast<double2 *>(d_params)[i] = __ldcv(reinterpret_cast<const double2 *>(h.params) + i);
+      else
+        d_params[i] = __ldcv(h.params + i);
+    } else if (i < np + n) {
+      if (h.term_x) d_tx[i - np] = __ldcv(h.term_x + (i - np));
+    } else {
+      d_seg[i - np - n] = __ldcv(h.item_seg + (i - np - n));
+    }
   }
-  if (h.term_x)
-    for (long long i = t; i < n; i += stride) d_tx[i] = __ldcv(h.term_x + i);
-  for (long long i = t; i < n; i += stride) d_seg[i] = __ldcv(h.item_seg + i);
 }
 
 // dlogl, term_y, hh (n doubles each) and status (n ints) to the caller's
-// arrays; the three optional ones are skipped when NULL
+// arrays, one element per thread; the three optional ones are skipped when NULL
 __global__ void host_scatter_kernel(const HostIo *d_io, int n, const double *d_dl, const double *d_ty,
                                     const double *d_hh, const int *d_st) {
   const HostIo h = *d_io;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  for (long long i = t; i < n; i += stride) __stwt(h.dlogl + i, d_dl[i]);
-  if (h.term_y)
-    for (long long i = t; i < n; i += stride) __stwt(h.term_y + i, d_ty[i]);
-  if (h.hh)
-    for (long long i = t; i < n; i += stride) __stwt(h.hh + i, d_hh[i]);
-  if (h.status)
-    for (long long i = t; i < n; i += stride) __stwt(h.status + i, d_st[i]);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < 4LL * n; i += stride) {
+    const int q = (int)(i / n);
+    const long long j = i - (long long)q * n;
+    if (q == 0) {
+      __stwt(h.dlogl + j, d_dl[j]);
+    } else if (q == 1) {
+      if (h.term_y) __stwt(h.term_y + j, d_ty[j]);
+    } else if (q == 2) {
+      if (h.hh) __stwt(h.hh + j, d_hh[j]);
+    } else if (h.status) {
+      __stwt(h.status + j, d_st[j]);
+    }
+  }
 }
 
 static int host_copy_grid(const glass_gpu_ctx *ctx, long long elems) {
@@ -564,13 +575,13 @@ static int dlogl_direct_enqueue(glass_gpu_ctx *ctx, int precision, int nitems, b
   cudaStream_t s = ctx->stream;
   // the device copy of the pointer block sits after the outputs
   HostIo *d_io = (HostIo *)(d + out_off + ((sizeof(double) * 3 * nd + sizeof(int) * nd + 15) / 16) * 16);
-  host_gather_kernel<<<host_copy_grid(ctx, 4LL * nitems), 256, 0, s>>>(ctx->h_io, d_io, nitems, d_params, d_tx,
+  host_gather_kernel<<<host_copy_grid(ctx, 6LL * nitems), 256, 0, s>>>(ctx->h_io, d_io, nitems, d_params, d_tx,
                                                                        d_seg);
   GLASS_CUDA(cudaGetLastError(), "host_gather_kernel launch");
   int rc = glass_gpu_dlogl_batch(ctx, precision, nitems, d_seg, d_params, has_tx ? d_tx : nullptr, d_dl, d_ty, d_hh,
                                  d_st);
   if (rc) return rc;
-  host_scatter_kernel<<<host_copy_grid(ctx, nitems), 256, 0, s>>>(d_io, nitems, d_dl, d_ty, d_hh, d_st);
+  host_scatter_kernel<<<host_copy_grid(ctx, 4LL * nitems), 256, 0, s>>>(d_io, nitems, d_dl, d_ty, d_hh, d_st);
   GLASS_CUDA(cudaGetLastError(), "host_scatter_kernel launch");
   ctx->last_launches += 2;
   return GLASS_OK;
