@@ -52,6 +52,7 @@ EXPORTS = (
     "glass_gpu_noise_wavelet_setup", "glass_gpu_noise_wavelet_logl_batch", "glass_gpu_noise_wavelet_logl_batch_host",
     "glass_gpu_dlogl_batch_channels", "glass_gpu_noise_eta_batch", "glass_gpu_noise_eta_batch_host",
     "glass_gpu_rand_r_fill", "glass_gpu_mh_accept", "glass_gpu_fisher_draw", "glass_gpu_ptmcmc",
+    "glass_gpu_set_mixed_tolerance", "glass_gpu_set_mixed_tolerance_scale", "glass_gpu_mixed_reevaluated",
 )
 
 _lib = None
@@ -79,6 +80,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_set_host_access.argtypes = [_V, ctypes.c_int]
     lib.glass_gpu_get_host_access.argtypes = [_V, _I, _I]
     lib.glass_gpu_last_phase_ms.argtypes = [_V, ctypes.POINTER(ctypes.c_float)]
+    lib.glass_gpu_set_mixed_tolerance.argtypes = [_V, ctypes.c_double]
+    lib.glass_gpu_set_mixed_tolerance_scale.argtypes = [_V, ctypes.c_int, _D]
+    lib.glass_gpu_mixed_reevaluated.argtypes = [_V, _V]
     lib.glass_gpu_bank_upload.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_int, _I, _D, _D, _D, _D]
     lib.glass_gpu_bank_set_residual.argtypes = [_V, ctypes.c_int, _D, _D]
@@ -524,11 +528,33 @@ class Engine:
         _check(self.lib.glass_gpu_set_phase_timing(self._ctx, int(bool(enable))))
 
     def last_phase_ms(self):
-        """(plan, slow part, spectral) milliseconds of the last dlogl batch
-        launched with phase timing on."""
-        ms = (ctypes.c_float * 3)()
+        """(plan, slow part, spectral, re-evaluation) milliseconds of the last
+        dlogl batch launched with phase timing on."""
+        ms = (ctypes.c_float * 4)()
         _check(self.lib.glass_gpu_last_phase_ms(self._ctx, ms))
         return tuple(float(v) for v in ms)
+
+    def set_mixed_tolerance(self, tol: float = 1e-3):
+        """Mixed precision: proposals whose estimated delta-logL error exceeds
+        tol are evaluated again in higher precision within the same batch
+        (tol <= 0: off)."""
+        _check(self.lib.glass_gpu_set_mixed_tolerance(self._ctx, float(tol)))
+
+    def set_mixed_tolerance_scale(self, scale=None):
+        """Per-proposal tolerance tol * scale[i] (e.g. the chains'
+        temperatures); None: tol for all."""
+        if scale is None:
+            _check(self.lib.glass_gpu_set_mixed_tolerance_scale(self._ctx, 0, None))
+        else:
+            sc = np.ascontiguousarray(scale, np.float64)
+            _check(self.lib.glass_gpu_set_mixed_tolerance_scale(self._ctx, int(sc.size), _pd(sc)))
+
+    def mixed_reevaluated(self):
+        """(double-float, FP64-series) counts of re-evaluated proposals so far
+        (synchronises the stream)."""
+        n = (ctypes.c_ulonglong * 2)()
+        _check(self.lib.glass_gpu_mixed_reevaluated(self._ctx, n))
+        return int(n[0]), int(n[1])
 
 
 class HostBatch:

@@ -29,7 +29,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 # reference does (ucb/src/glass_ucb_waveform.c:877, arguments of ~1e6 rad); a
 # fused multiply-add rounds differently from the reference's separate multiply
 # and add by up to ~1e-10 rad there, so contraction is off for them.
-PER_FILE_FLAGS = {"ucb_fd.cu": ["-fmad=false"], "ucb_fd_fp64.cu": ["-fmad=false"],
+PER_FILE_FLAGS = {"ucb_fd.cu": ["-fmad=false"], "ucb_fd_fp64.cu": ["-fmad=false"], "ucb_fd_noalloc.cu": ["-fmad=false"],
                   "wdm.cu": ["-Xcompiler", "-ffp-contract=off"],
                   "ucb_wavelet.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
                   "ucb_fstat.cu": ["-fmad=false"], "noise.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],

@@ -42,6 +42,26 @@ static int cuda_err(cudaError_t e, const char *where) {
 
 extern "C" const char *glass_gpu_last_error(void) { return g_err.c_str(); }
 
+namespace glass {
+// Error reporting for the entry points defined in other translation units.
+int report_error(int code, const char *msg) { return set_err(code, "%s", msg); }
+int report_cuda_error(cudaError_t e, const char *where) { return cuda_err(e, where); }
+}  // namespace glass
+
+// Error model of the mixed-precision delta logL, in the whitened sums the
+// spectral kernel has at hand (hw = |h|^2 and rr = |r - h|^2 over the template
+// support, so that (h|h) = 2 hw):
+//   |error| <= kMixedErrK1 sqrt(hw rr) + kMixedErrK2 (hw + rr).
+// An FP32 FFT leaves up to ~1e-7 of relative error on the few bins that hold
+// a narrowband template's power; the largest ratio measured on the
+// 64-segment benchmark workload was 7.9e-8.
+static constexpr double kMixedErrK1 = 1.0e-7;
+static constexpr double kMixedErrK2 = 0.0;
+// The same after the double-float re-evaluation of FP32 series: what is left
+// is the rounding of the series values (measured up to 7.9e-9).
+static constexpr double kHpErrK1 = 2.0e-8;
+static constexpr double kMixedTolDefault = 1e-3;
+
 // ----------------------------------------------------------------- context
 // Host pointers of one glass_gpu_dlogl_batch_host call (direct host access).
 struct HostIo {
@@ -86,6 +106,9 @@ struct glass_gpu_ctx {
   std::map<long long, cudaGraphExec_t> host_graphs;
   int last_launches = 0;
   int n_fixed = 0;  // template size override (0: bandwidth rule)
+  // mixed precision: proposals whose estimated delta-logL error exceeds this
+  // are evaluated again in higher precision (<= 0: never)
+  double mixed_tol = kMixedTolDefault;
   WdmPlan wdm;      // tables and work buffers of the last WDM grid used
   void *wdm_stage = nullptr;  // NF NT doubles for the host-pointer WDM calls
   size_t wdm_stage_cap = 0;
@@ -168,6 +191,11 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->work.bin_count);
   cudaFree(ctx->work.bin_list);
   cudaFree(ctx->work.series);
+  cudaFree(ctx->work.fb_list);
+  cudaFree(ctx->work.fb_off);
+  cudaFree(ctx->work.fb2_list);
+  cudaFree(ctx->work.fb_total);
+  cudaFree(ctx->work.fb_inv_scale);
   cudaFree(ctx->d_stage);
   clear_host_graphs(ctx);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
@@ -189,7 +217,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
     if (ctx->work.join[b]) cudaEventDestroy(ctx->work.join[b]);
   }
   if (ctx->work.fork) cudaEventDestroy(ctx->work.fork);
-  for (int i = 0; i < 4; i++)
+  for (int i = 0; i < 5; i++)
     if (ctx->work.phase[i]) cudaEventDestroy(ctx->work.phase[i]);
   cudaStreamDestroy(ctx->own);
   delete ctx;
@@ -225,7 +253,7 @@ extern "C" int glass_gpu_set_phase_timing(glass_gpu_ctx *ctx, int enable) {
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   if (enable && !ctx->work.phase[0])
-    for (int i = 0; i < 4; i++) GLASS_CUDA(cudaEventCreate(&ctx->work.phase[i]), "phase event create");
+    for (int i = 0; i < 5; i++) GLASS_CUDA(cudaEventCreate(&ctx->work.phase[i]), "phase event create");
   ctx->work.phase_timing = enable != 0;
   ctx->work.phase_recorded = false;
   return GLASS_OK;
@@ -237,9 +265,66 @@ extern "C" int glass_gpu_last_phase_ms(glass_gpu_ctx *ctx, float *ms) {
     return set_err(GLASS_ERR_STATE, "glass_gpu_last_phase_ms: no step was launched with phase timing on");
   int rc = ctx_activate(ctx);
   if (rc) return rc;
-  GLASS_CUDA(cudaEventSynchronize(ctx->work.phase[3]), "phase event sync");
-  for (int i = 0; i < 3; i++)
+  GLASS_CUDA(cudaEventSynchronize(ctx->work.phase[4]), "phase event sync");
+  for (int i = 0; i < 4; i++)
     GLASS_CUDA(cudaEventElapsedTime(&ms[i], ctx->work.phase[i], ctx->work.phase[i + 1]), "phase elapsed time");
+  return GLASS_OK;
+}
+
+static void apply_mixed_tol(glass_gpu_ctx *ctx) {
+  const double t = ctx->mixed_tol;
+  ctx->work.fb_e1 = t > 0 ? (float)(kMixedErrK1 / t) : 0.f;
+  ctx->work.fb_e2 = t > 0 ? (float)(kMixedErrK2 / t) : 0.f;
+  ctx->work.hp_e1 = t > 0 ? (float)(kHpErrK1 / t) : 0.f;
+}
+
+extern "C" int glass_gpu_set_mixed_tolerance(glass_gpu_ctx *ctx, double tol) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_set_mixed_tolerance: null context");
+  if (!(tol == tol)) return set_err(GLASS_ERR_ARG, "glass_gpu_set_mixed_tolerance: NaN tolerance");
+  if (tol != ctx->mixed_tol) clear_host_graphs(ctx);  // the estimate's scale is a kernel argument in the graphs
+  ctx->mixed_tol = tol;
+  apply_mixed_tol(ctx);
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_set_mixed_tolerance_scale(glass_gpu_ctx *ctx, int n, const double *scale) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "glass_gpu_set_mixed_tolerance_scale: null context");
+  if (n < 0 || (n > 0 && !scale)) return set_err(GLASS_ERR_ARG, "glass_gpu_set_mixed_tolerance_scale: bad array");
+  std::vector<float> inv((size_t)n);
+  for (int i = 0; i < n; i++) {
+    if (!(scale[i] > 0) || !isfinite(scale[i]))
+      return set_err(GLASS_ERR_ARG, "glass_gpu_set_mixed_tolerance_scale: scales must be finite and positive");
+    inv[i] = (float)(1.0 / scale[i]);
+  }
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  FdWorkDev &w = ctx->work;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "tolerance scale sync");
+  if (n > w.fb_nscale_cap) {
+    clear_host_graphs(ctx);  // the graphs hold the array's address
+    cudaFree(w.fb_inv_scale);
+    w.fb_inv_scale = nullptr;
+    w.fb_nscale_cap = 0;
+    GLASS_CUDA(cudaMalloc(&w.fb_inv_scale, sizeof(float) * (size_t)n), "cudaMalloc(tolerance scale)");
+    w.fb_nscale_cap = n;
+  }
+  if (n > 0)
+    GLASS_CUDA(cudaMemcpy(w.fb_inv_scale, inv.data(), sizeof(float) * (size_t)n, cudaMemcpyHostToDevice),
+               "upload tolerance scale");
+  if (n != w.fb_nscale) clear_host_graphs(ctx);  // the count is a kernel argument in the graphs
+  w.fb_nscale = n;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_mixed_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count) {
+  if (!ctx || !count) return set_err(GLASS_ERR_ARG, "glass_gpu_mixed_reevaluated: null argument");
+  count[0] = count[1] = 0;
+  if (!ctx->work.fb_total) return GLASS_OK;
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(count, ctx->work.fb_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             ctx->stream), "read re-evaluation count");
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "read re-evaluation count");
   return GLASS_OK;
 }
 
@@ -273,12 +358,12 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   const size_t nb = (size_t)nseg * NFFT;
-  std::vector<float4> w32(nb), w32lo(nb), g32(2 * nb);
+  std::vector<float4> w32(nb), w32lo(nb), g32(2 * nb), g32lo(2 * nb);
   std::vector<double> Q((size_t)nseg * (NFFT + 1)), QA((size_t)nseg * (NFFT + 1));
   std::vector<double2> w64(2 * nb), g64(4 * nb);
   const double fstar = fstar_of_orbit();
   fd_build_bank_tables(format, T, fstar, NFFT, nseg, qmin, rA, rE, invCA, invCE, w32.data(), w32lo.data(),
-                       g32.data(), Q.data(), w64.data(), g64.data(), QA.data());
+                       g32.data(), Q.data(), w64.data(), g64.data(), QA.data(), g32lo.data());
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "bank_upload sync");
   clear_host_graphs(ctx);
   cudaFree(ctx->bank_mem);
@@ -293,7 +378,8 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   size_t off_invc = off_g64 + sizeof(double2) * g64.size();
   size_t off_rho = (off_invc + sizeof(float2) * nb + 255) / 256 * 256;
   size_t off_qa = off_rho + sizeof(double) * nb;
-  size_t total = off_qa + sizeof(double) * QA.size();
+  size_t off_g32lo = (off_qa + sizeof(double) * QA.size() + 255) / 256 * 256;
+  size_t total = off_g32lo + sizeof(float4) * g32lo.size();
   GLASS_CUDA(cudaMalloc(&ctx->bank_mem, total), "cudaMalloc(bank)");
   char *base = (char *)ctx->bank_mem;
   FdBankDev &b = ctx->bank;
@@ -313,12 +399,15 @@ extern "C" int glass_gpu_bank_upload(glass_gpu_ctx *ctx, int format, double T, d
   b.invc = (float2 *)(base + off_invc);
   b.rho = (double *)(base + off_rho);
   b.QA = (double *)(base + off_qa);
+  b.g32lo = (float4 *)(base + off_g32lo);
   GLASS_CUDA(cudaMemcpy(b.qmin, qmin, sizeof(int) * nseg, cudaMemcpyHostToDevice), "upload qmin");
   GLASS_CUDA(cudaMemcpy(b.Q, Q.data(), sizeof(double) * Q.size(), cudaMemcpyHostToDevice), "upload Q");
   GLASS_CUDA(cudaMemcpy(b.QA, QA.data(), sizeof(double) * QA.size(), cudaMemcpyHostToDevice), "upload QA");
   GLASS_CUDA(cudaMemcpy(b.w32, w32.data(), sizeof(float4) * w32.size(), cudaMemcpyHostToDevice), "upload w32");
   GLASS_CUDA(cudaMemcpy(b.w32lo, w32lo.data(), sizeof(float4) * w32lo.size(), cudaMemcpyHostToDevice), "upload w32lo");
   GLASS_CUDA(cudaMemcpy(b.g32, g32.data(), sizeof(float4) * g32.size(), cudaMemcpyHostToDevice), "upload g32");
+  GLASS_CUDA(cudaMemcpy(b.g32lo, g32lo.data(), sizeof(float4) * g32lo.size(), cudaMemcpyHostToDevice),
+             "upload g32lo");
   GLASS_CUDA(cudaMemcpy(b.w64, w64.data(), sizeof(double2) * w64.size(), cudaMemcpyHostToDevice), "upload w64");
   GLASS_CUDA(cudaMemcpy(b.g64, g64.data(), sizeof(double2) * g64.size(), cudaMemcpyHostToDevice), "upload g64");
   {
@@ -398,6 +487,14 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   cudaFree(w.bin_count);
   cudaFree(w.bin_list);
   cudaFree(w.series);
+  cudaFree(w.fb_list);
+  cudaFree(w.fb_off);
+  cudaFree(w.fb2_list);
+  w.fb_list = nullptr;
+  w.fb_off = nullptr;
+  w.fb2_list = nullptr;
+  w.fb_count = nullptr;
+  w.fb2_count = nullptr;
   w.items64 = nullptr;
   w.itemsmix = nullptr;
   w.itemsgrad = nullptr;
@@ -413,8 +510,18 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   GLASS_CUDA(cudaMalloc(&w.items64, sizeof(ItemF64) * (size_t)cap), "cudaMalloc(items64)");
   GLASS_CUDA(cudaMalloc(&w.itemsmix, sizeof(ItemMix) * (size_t)cap), "cudaMalloc(itemsmix)");
   GLASS_CUDA(cudaMalloc(&w.itemsgrad, sizeof(ItemGrad) * (size_t)cap), "cudaMalloc(itemsgrad)");
-  GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * (kNumBins + 1)), "cudaMalloc(bin_count)");
-  GLASS_CUDA(cudaMemset(w.bin_count, 0, sizeof(int) * (kNumBins + 1)), "cudaMemset(bin_count)");
+  GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * (kNumBins + 6)), "cudaMalloc(bin_count)");
+  GLASS_CUDA(cudaMemset(w.bin_count, 0, sizeof(int) * (kNumBins + 6)), "cudaMemset(bin_count)");
+  w.fb_count = w.bin_count + kNumBins + 1;
+  w.fb2_count = w.bin_count + kNumBins + 2;
+  GLASS_CUDA(cudaMalloc(&w.fb_list, sizeof(int) * (size_t)cap), "cudaMalloc(fb_list)");
+  GLASS_CUDA(cudaMalloc(&w.fb_off, sizeof(long long) * (size_t)cap), "cudaMalloc(fb_off)");
+  GLASS_CUDA(cudaMalloc(&w.fb2_list, sizeof(int) * (size_t)cap), "cudaMalloc(fb2_list)");
+  if (!w.fb_total) {
+    GLASS_CUDA(cudaMalloc(&w.fb_total, 2 * sizeof(unsigned long long)), "cudaMalloc(fb_total)");
+    GLASS_CUDA(cudaMemset(w.fb_total, 0, 2 * sizeof(unsigned long long)), "cudaMemset(fb_total)");
+  }
+  apply_mixed_tol(ctx);
   w.counts_zero = true;
   GLASS_CUDA(cudaMalloc(&w.bin_list, sizeof(int) * (size_t)kNumBins * cap), "cudaMalloc(bin_list)");
   GLASS_CUDA(cudaMalloc(&w.series, series), "cudaMalloc(series)");

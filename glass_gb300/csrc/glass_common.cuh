@@ -3,7 +3,40 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 namespace glass {
+
+// ------------------------------------------------------ per-device launch set-up
+// A kernel's dynamic shared-memory limit (cudaFuncSetAttribute) and the
+// occupancy derived from it belong to the current device, and the entry points
+// are called from several host threads: the set-up runs once per device, under
+// a lock, and later launches on that device read the stored occupancy.
+constexpr int kMaxDevices = 64;
+struct LaunchSetup {
+  std::mutex m;
+  int occ[kMaxDevices] = {};  // 0: not yet set up on that device
+};
+// init(int *occ) sets the attributes and writes the occupancy (CTAs per SM).
+template <typename Init>
+inline cudaError_t launch_setup(LaunchSetup &s, Init init, int *occ) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  int v = __atomic_load_n(&s.occ[dev], __ATOMIC_ACQUIRE);
+  if (v <= 0) {
+    std::lock_guard<std::mutex> g(s.m);
+    v = s.occ[dev];
+    if (v <= 0) {
+      if ((e = init(&v)) != cudaSuccess) return e;
+      if (v < 1) v = 1;
+      __atomic_store_n(&s.occ[dev], v, __ATOMIC_RELEASE);
+    }
+  }
+  *occ = v;
+  return cudaSuccess;
+}
 
 // Physical constants, identical to utils/src/glass_constants.h:31-89 and
 // utils/src/glass_lisa.h:31 (the carrier phase multiplies them by ~1e5, so
@@ -85,6 +118,18 @@ __device__ __forceinline__ float df_reduce_2pi(df x) {
   return __fsub_rn(__fadd_rn(r.hi, r.lo), k * pi2_lo);
 }
 
+// The same, kept as a double-float (hi in about [-pi, pi]): 2 pi is carried
+// to ~1e-15 relative (hi + lo floats), so k 2 pi for the few k of a phase of
+// tens of radians adds ~1e-14 rad.
+__device__ __forceinline__ df df_reduce_2pi_df(df x) {
+  const float inv2pi = 0.15915494309189535f;
+  const float pi2_hi = 6.28318548202514648f;
+  const float pi2_lo = -1.7484555314695172e-07f;
+  const float k = rintf(x.hi * inv2pi);
+  const df r = df_add(x, df_neg(two_prod(k, pi2_hi)));
+  return df_add(r, df_neg(two_prod(k, pi2_lo)));
+}
+
 // --------------------------------------------------------- per-item constants
 // Everything a waveform needs that does not depend on the sample index,
 // computed once per proposal (FP64) by the plan kernel.  The antenna-pattern
@@ -110,18 +155,29 @@ struct __align__(16) ItemMix {
   int seg, N, imin, pad;
   float k[4];                 // kx, ky, kz, 0
   float Mr[6], Mi[6];
+  // Mr, Mi minus their float rounding: the antenna factors multiply every
+  // sample of the template, so their rounding (3e-8 rms) would be a relative
+  // error common to the whole template, i.e. of (h|h), which delta logL
+  // carries times (h|h) for a loud template far from the data
+  float Mrl[6], Mil[6];
   float fonfs0;   // f0/f*
   float fdfs;     // fdot*T/f*       : fonfs_i = fonfs0 + fdfs*(u - tau_i/T)
   float aef;      // (2/3)*fdot*T/f0 : aevol_i = 1 + aef*(u - tau_i/T)
   float w0c;      // 2 pi f0 / c
   float p7pi;     // pi*fdot*T^2 (small corrections)
-  float amp_hi, amp_lo;  // amp/(2N) = amp_hi + amp_lo
-  float pad2;
+  float amp_hi, amp_lo;  // amp/(2N) = amp_hi + amp_lo (gradient path)
+  // amp/(2N) = m 2^e with m in [1, 2): amp_p2 = 2^e, exactly, and Mr, Mi (hi
+  // and lo) hold m (DP e+ + DC ex), so the likelihood kernels scale the
+  // template by a power of two, which rounds nothing
+  float amp_p2;
+  // k, w0c, fonfs0 minus their float rounding: they set the phase differences
+  // between the arms, and so the size of the A/E combinations; a rounding
+  // common to the template is a coherent phase and amplitude error
+  float kl[3], w0cl, fonfs0l;
   df eps2pi;      // 2 pi (f0 T - q)
   df beta1, beta2;  // 2 pi f0 AU/c * k_x, k_y
   df phi0;
   df p7pi_d;      // pi*fdot*T^2
-  df pad3;
 };
 
 // Gradient / Fisher path: the mixed-precision constants plus what the tangent

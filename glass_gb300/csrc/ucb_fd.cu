@@ -34,6 +34,7 @@ namespace glass {
 
 cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_slow_fp64_wide(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
@@ -76,6 +77,37 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
     }
   }
   plan_bin(a, i, b);
+}
+
+// FP64 constants of the proposals listed for an FP64 slow part
+// (list[0 .. *count)), binned by size: the size and placement are the mixed
+// plan's (the same bandwidth rule), so only the source geometry is evaluated
+// in FP64 here.  Grid-stride with warp-uniform trips, as plan_bin needs
+// whole warps.
+__global__ void __launch_bounds__(64) fd_item64_list_kernel(PlanArgs a, const int *list, const int *count) {
+  const int n = *count;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int k = base + threadIdx.x;
+    int b = -1, i = 0;
+    if (k < n) {
+      i = list[k];
+      const ItemMix &m = a.itemsmix[i];
+      double p[8];
+      for (int q = 0; q < 8; q++) p[q] = a.params[8 * (size_t)i + q];
+      SourceGeom g;
+      source_geometry(p, 8, a.T, g);
+      ItemF64 c;
+      make_item_f64(g, m.N, c);
+      c.seg = m.seg;
+      c.N = m.N;
+      c.imin = m.imin;
+      c.pad = 0;
+      a.items64[i] = c;
+      b = fd_bin_of(m.N);
+    }
+    plan_bin(a, i, b);
+  }
 }
 
 // Mixed-precision plan, warp-specialised: GB300's FP64 pipe issues a warp
@@ -161,6 +193,9 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       c->k[1] = (float)ky;
       c->k[2] = (float)(-cth);
       c->k[3] = 0.f;
+      c->kl[0] = (float)(kx - (double)c->k[0]);
+      c->kl[1] = (float)(ky - (double)c->k[1]);
+      c->kl[2] = (float)(-cth - (double)c->k[2]);
       int idx = 0;
 #pragma unroll
       for (int r = 0; r < 3; r++)
@@ -183,11 +218,12 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       s_dp[l][3] = -Across * cosps;
       const double fdotT = p[7] / T;  // fdot T
       c->fonfs0 = (float)(f0 / a.fstar);
+      c->fonfs0l = (float)(f0 / a.fstar - (double)c->fonfs0);
       c->fdfs = (float)(fdotT / a.fstar);
       c->aef = (float)(0.66666666666666666666 * fdotT / f0);
       c->w0c = (float)(kPI2 * f0 / kCLIGHT);
+      c->w0cl = (float)(kPI2 * f0 / kCLIGHT - (double)c->w0c);
       c->p7pi = (float)(kPI * p[7]);
-      c->pad2 = 0.f;
     } else {
       s_amp[l] = exp(p[3]);
       const double fT = f0 * T;
@@ -195,7 +231,6 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       c->eps2pi = df_from_double(kPI2 * (fT - (double)q));
       c->phi0 = df_from_double(p[6]);
       c->p7pi_d = df_from_double(kPI * p[7]);
-      c->pad3 = {0.f, 0.f};
     }
   } else if (w == 0) {
     s_st[l] = st;
@@ -204,6 +239,15 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
   }
   __syncthreads();
   const int stt = in ? (st | s_st[l]) : 1;
+  // amp/(2N) = m 2^e, m in [1, 2): the power of two scales the template
+  // exactly in the likelihood kernels, m goes into the antenna tensors
+  double msc = 1.0;
+  if (in && !stt) {
+    const double sc = scalbn(s_amp[l], -(32 - __clz(s_N[l])));  // amp / (2N), N a power of two
+    const int ex = ilogb(sc);
+    msc = scalbn(sc, -ex);
+    if (w == 0) c->amp_p2 = (float)scalbn(1.0, ex);
+  }
   // antenna tensors: warp w assembles elements 3w/2 .. of the 12 (Mr, Mi) x 6
   if (in && !stt) {
 #pragma unroll
@@ -211,11 +255,15 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       const int e = 3 * w + q;  // 0..11: (tensor element, real/imag)
       const int el = e >> 1;
       const double DPx = s_dp[l][(e & 1) ? 1 : 0], DCx = s_dp[l][(e & 1) ? 3 : 2];
-      const float m = (float)(DPx * s_ep[l][el] + DCx * s_ec[l][el]);
-      if (e & 1)
+      const double md = msc * (DPx * s_ep[l][el] + DCx * s_ec[l][el]);
+      const float m = (float)md, ml = (float)(md - (double)m);
+      if (e & 1) {
         c->Mi[el] = m;
-      else
+        c->Mil[el] = ml;
+      } else {
         c->Mr[el] = m;
+        c->Mrl[el] = ml;
+      }
     }
   }
   int b = -1;
@@ -308,6 +356,10 @@ __global__ void fd_orbit_table_kernel(FdTablesDev tab, double T, double t0) {
   sincospi(-2.0 * (double)n / (double)N, &s, &cth);
   tab.tw64[b][n] = make_double2(cth, s);
   tab.tw32[b][n] = make_float2((float)cth, (float)s);
+  if (tab.tw32x[b]) {
+    const float ch = (float)cth, sh = (float)s;
+    tab.tw32x[b][n] = make_float4(ch, sh, (float)(cth - (double)ch), (float)(s - (double)sh));
+  }
 }
 
 cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStream_t stream) {
@@ -316,7 +368,7 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
     for (int b = 0; b < kNumBins; b++) {
       int N = 32 << b;
       total += (size_t)N * (sizeof(OrbitSample64) + sizeof(OrbitSampleMix) + sizeof(GeoSampleMix) + sizeof(float2) +
-                            sizeof(double2));
+                            sizeof(double2) + sizeof(float4));
     }
     cudaError_t e = cudaMalloc(&tab.base, total);
     if (e != cudaSuccess) return e;
@@ -333,6 +385,8 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
       p += (size_t)N * sizeof(double2);
       tab.tw32[b] = (float2 *)p;
       p += (size_t)N * sizeof(float2);
+      tab.tw32x[b] = (float4 *)p;
+      p += (size_t)N * sizeof(float4);
     }
   }
   int total = 32 * ((1 << kNumBins) - 1);
@@ -343,7 +397,7 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
 // ---------------------------------------------------------- host: bank tables
 void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
                           const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *w32lo,
-                          float4 *g32, double *Q, double2 *w64, double2 *g64, double *QA) {
+                          float4 *g32, double *Q, double2 *w64, double2 *g64, double *QA, float4 *g32lo) {
   const double sqT = sqrt(T);
   for (int s = 0; s < nseg; s++) {
     double q = 0.0, qa = 0.0;
@@ -386,8 +440,18 @@ void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg
       w32[sj] = wf;
       w32lo[sj] = make_float4((float)(wAr - (double)wf.x), (float)(wAi - (double)wf.y), (float)(wEr - (double)wf.z),
                               (float)(wEi - (double)wf.w));
-      g32[2 * sj] = make_float4((float)GA2r, (float)GA2i, (float)GA1r, (float)GA1i);
-      g32[2 * sj + 1] = make_float4((float)GE2r, (float)GE2i, (float)GE1r, (float)GE1i);
+      const float4 ga = make_float4((float)GA2r, (float)GA2i, (float)GA1r, (float)GA1i);
+      const float4 ge = make_float4((float)GE2r, (float)GE2i, (float)GE1r, (float)GE1i);
+      g32[2 * sj] = ga;
+      g32[2 * sj + 1] = ge;
+      // a template's power sits in a few bins, so the rounding of these
+      // entries would not average out over its support: kept as hi + lo
+      if (g32lo) {
+        g32lo[2 * sj] = make_float4((float)(GA2r - (double)ga.x), (float)(GA2i - (double)ga.y),
+                                    (float)(GA1r - (double)ga.z), (float)(GA1i - (double)ga.w));
+        g32lo[2 * sj + 1] = make_float4((float)(GE2r - (double)ge.x), (float)(GE2i - (double)ge.y),
+                                        (float)(GE1r - (double)ge.z), (float)(GE1i - (double)ge.w));
+      }
       q += wAr * wAr + wAi * wAi + wEr * wEr + wEi * wEi;
       Q[(size_t)s * (NFFT + 1) + j + 1] = q;
       if (QA) {
@@ -407,9 +471,10 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   int launches = 0;
   const bool mix = precision == 1;
   if (!work.counts_zero) {
-    e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream);
+    e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 6), stream);
     if (e != cudaSuccess) return e;
   }
+  const bool fallback = mix && (work.fb_e1 > 0.f || work.fb_e2 > 0.f);
   work.counts_zero = false;  // until this sequence has been enqueued in full
   PlanArgs pa;
   pa.nitems = nitems;
@@ -482,6 +547,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.w32 = bank.w32;
   a.w32lo = bank.w32lo;
   a.g32 = bank.g32;
+  a.g32lo = bank.g32lo;
   a.Q = bank.Q;
   a.w64 = bank.w64;
   a.g64 = bank.g64;
@@ -492,7 +558,36 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.status = status;
   a.term_ch = term_ch;
   a.QA = bank.QA;
+  if (fallback) {
+    a.fb_count = work.fb_count;
+    a.fb_list = work.fb_list;
+    a.fb_off = work.fb_off;
+    a.fb_total = work.fb_total;
+    a.fb_e1 = work.fb_e1;
+    a.fb_e2 = work.fb_e2;
+    a.fb2_count = work.fb2_count;
+    a.fb2_list = work.fb2_list;
+    a.hp_e1 = work.hp_e1;
+    a.fb_inv_scale = work.fb_inv_scale;
+    a.fb_nscale = work.fb_nscale;
+  }
   const bool perch = term_ch != nullptr;
+  // Inside a CUDA-graph capture, the FP64-series re-evaluation (three
+  // launches, idle in most batches) sits behind a conditional node that the
+  // last kernel before it sets when something is listed; outside capture, or
+  // where the graph API refuses, it is launched unconditionally.
+  bool cond = false;
+  cudaGraphConditionalHandle cond_h = 0;
+  cudaGraph_t cap_graph = nullptr;
+  if (fallback) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamGetCaptureInfo(stream, &cs, nullptr, &cap_graph) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusActive &&
+        cudaGraphConditionalHandleCreate(&cond_h, cap_graph, 0, cudaGraphCondAssignDefault) == cudaSuccess)
+      cond = true;
+    (void)cudaGetLastError();
+  }
+  const bool big = bank.NFFT > 1024;  // sizes 2048, 4096 in their own kernels
   // sizes up to 1024 (every size a segment of NFFT bins can produce, up to
   // NFFT: ucb_bandwidth caps N there) in one launch on the main stream; 2048
   // and 4096 as their own kernels on side streams running beside it
@@ -508,7 +603,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
       if ((e = cudaStreamWaitEvent(sb, work.fork, 0)) != cudaSuccess) return e;
       a.bin = b;
       a.bin_list = work.bin_list + (size_t)b * work.cap;
-      a.tw = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
+      a.tw = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
       e = mix ? fd_launch_spec_mixed(N, a, nitems, num_sms, sb, perch)
               : fd_launch_spec_fp64(N, a, nitems, num_sms, sb, perch);
       launches++;
@@ -525,7 +620,11 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.a.tw = nullptr;
     A.nbins = nall;
     A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
-    for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32[b] : (const void *)tab.tw64[b];
+    A.sched = work.bin_count + kNumBins + 4;
+    A.has_cond = cond && !big;
+    A.cond = cond_h;
+    A.cond_count = work.fb2_count;
+    for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
     e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch) : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
     launches++;
     if (e != cudaSuccess) return e;
@@ -535,9 +634,113 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   if (nb > 0 || nall == 0) {
     if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream)) != cudaSuccess) return e;
   }
+  if (timing && (e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
+
+  // Re-evaluation of flagged mixed proposals.  Sizes up to 1024 were
+  // re-evaluated in double-float by the persistent spectral kernel itself;
+  // the listed ones of sizes 2048 and 4096 get the same from the standalone
+  // kernel.  Proposals still above the tolerance get FP64 series (FP64
+  // constants, FP64 slow part) that the standalone kernel transforms in
+  // double-float.  Results are written over the mixed ones; counts and lists
+  // live on the device, and each kernel leaves its counters at zero.
+  if (fallback) {
+    int nmax = kMaxN;
+    while (nmax > bank.NFFT) nmax >>= 1;
+    HpArgs h;
+    h.NFFT = bank.NFFT;
+    h.cap = work.cap;
+    h.nmax = nmax;
+    h.list = work.fb_list;
+    h.count = work.fb_count;
+    h.off = work.fb_off;
+    h.series32 = reinterpret_cast<const float2 *>(work.series);
+    h.itemsmix = work.itemsmix;
+    h.zero_at = work.fb_count;
+    h.nzero = 1;
+    h.done = work.bin_count + kNumBins + 3;
+    h.w32 = bank.w32;
+    h.w32lo = bank.w32lo;
+    h.g32 = bank.g32;
+    h.g32lo = bank.g32lo;
+    h.Q = bank.Q;
+    h.QA = bank.QA;
+    for (int b = 0; b < kNumBins; b++) h.tw32x[b] = tab.tw32x[b];
+    h.term_x = term_x;
+    h.dlogl = dlogl;
+    h.term_y = term_y;
+    h.hh = hh;
+    h.term_ch = term_ch;
+    h.status = status;
+    h.next_count = work.fb2_count;
+    h.next_list = work.fb2_list;
+    h.next_total = work.fb_total + 1;
+    h.next_e1 = work.hp_e1;
+    h.inv_scale = work.fb_inv_scale;
+    h.nscale = work.fb_nscale;
+    if (big) {
+      h.has_cond = cond;
+      h.cond = cond_h;
+      e = fd_launch_hp(h, false, perch, num_sms, stream);
+      launches++;
+      if (e != cudaSuccess) return e;
+    }
+    // the FP64-series tier, behind the conditional node when capturing
+    cudaStream_t ts = stream;
+    cudaGraphNode_t cnode = nullptr;
+    if (cond) {
+      const cudaGraphNode_t *deps = nullptr;
+      size_t nd = 0;
+      cudaStreamCaptureStatus cs;
+      cudaGraphNodeParams np = {};
+      np.type = cudaGraphNodeTypeConditional;
+      np.conditional.handle = cond_h;
+      np.conditional.type = cudaGraphCondTypeIf;
+      np.conditional.size = 1;
+      if ((e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd)) != cudaSuccess) return e;
+      if ((e = cudaGraphAddNode(&cnode, cap_graph, deps, nullptr, nd, &np)) != cudaSuccess) return e;
+      ts = work.side[0];
+      if ((e = cudaStreamBeginCaptureToGraph(ts, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeRelaxed)) != cudaSuccess)
+        return e;
+    }
+    PlanArgs pb = pa;
+    pb.precision = 0;
+    fd_item64_list_kernel<<<num_sms, 64, 0, ts>>>(pb, work.fb2_list, work.fb2_count);
+    launches++;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = fd_launch_slow_fp64_wide(sa, num_sms, ts);
+    launches++;
+    if (e != cudaSuccess) return e;
+    HpArgs h2 = h;
+    h2.has_cond = false;
+    h2.list = nullptr;
+    h2.count = nullptr;
+    h2.off = nullptr;
+    h2.series32 = nullptr;
+    h2.itemsmix = nullptr;
+    h2.series64 = reinterpret_cast<const double2 *>(work.series);
+    h2.bin_count = work.bin_count;
+    h2.bin_list = work.bin_list;
+    h2.items64 = work.items64;
+    h2.zero_at = work.bin_count;  // the size counts, the done counter, fb_count and fb2_count
+    h2.nzero = kNumBins + 3;
+    h2.next_count = nullptr;
+    h2.next_list = nullptr;
+    h2.next_total = nullptr;
+    e = fd_launch_hp(h2, true, perch, num_sms, ts);
+    launches++;
+    if (e != cudaSuccess) return e;
+    if (cond) {
+      cudaGraph_t body = nullptr;
+      if ((e = cudaStreamEndCapture(ts, &body)) != cudaSuccess) return e;
+      if ((e = cudaStreamUpdateCaptureDependencies(stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+          cudaSuccess)
+        return e;
+    }
+  }
   work.counts_zero = true;
   if (timing) {
-    if ((e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(work.phase[4], stream)) != cudaSuccess) return e;
     work.phase_recorded = true;
   }
   if (nlaunch) *nlaunch = launches;
@@ -649,13 +852,13 @@ template <int N>
 static cudaError_t launch_waveform(const ItemF64 *item, const double2 *d6, int format, int nch, double T, double fstar,
                                    double *out, const double2 *tw, cudaStream_t stream) {
   size_t smem = sizeof(double2) * 3 * N;
-  static bool init = false;
-  if (!init) {
-    cudaError_t e = cudaFuncSetAttribute(fd_waveform_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    init = true;
-  }
+  static LaunchSetup setup;
+  int occ = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    *o = 1;
+    return cudaFuncSetAttribute(fd_waveform_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }, &occ);
+  if (e != cudaSuccess) return e;
   fd_waveform_kernel<N><<<nch, LegacyCfg<N>::GT, smem, stream>>>(item, d6, format, T, fstar, out, tw);
   return cudaGetLastError();
 }

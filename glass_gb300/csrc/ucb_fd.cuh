@@ -15,6 +15,7 @@ struct FdBankDev {
   float4 *w32 = nullptr;       // [nseg*NFFT]   whitened residual {A.re, A.im, E.re, E.im}, rounded to float
   float4 *w32lo = nullptr;     // [nseg*NFFT]   residual minus its float rounding (double-float pair with w32)
   float4 *g32 = nullptr;       // [nseg*NFFT*2] {GA2, GA1}, {GE2, GE1}
+  float4 *g32lo = nullptr;     // [nseg*NFFT*2] the same minus their float rounding
   double *Q = nullptr;         // [nseg*(NFFT+1)] prefix sums of |w|^2 over both channels (FP64)
   double *QA = nullptr;        // [nseg*(NFFT+1)] the same for the A channel alone
   double2 *w64 = nullptr;      // [nseg*NFFT*2] {A}, {E}
@@ -29,6 +30,7 @@ struct FdTablesDev {
   OrbitSampleMix *mix[kNumBins] = {};
   GeoSampleMix *geo[kNumBins] = {};
   float2 *tw32[kNumBins] = {};
+  float4 *tw32x[kNumBins] = {};  // the same twiddles as hi + lo floats (mixed likelihood)
   double2 *tw64[kNumBins] = {};
   void *base = nullptr;  // single allocation backing all of the above
 };
@@ -45,25 +47,46 @@ struct FdWorkDev {
   ItemF64 *items64 = nullptr;   // [cap]
   ItemMix *itemsmix = nullptr;  // [cap]
   ItemGrad *itemsgrad = nullptr;  // [cap]
-  int *bin_count = nullptr;     // [kNumBins + 1]: per-size counts, then a CTA-done counter
+  // [kNumBins + 6]: per-size counts, a done counter (unused by the persistent
+  // spectral kernel), fb_count, fb2_count, the re-evaluation kernel's
+  // CTA-done counter, and the persistent spectral kernel's next-unit and
+  // CTA-done counters
+  int *bin_count = nullptr;
   int *bin_list = nullptr;      // [kNumBins*cap]
+  // Mixed precision: proposals whose error estimate exceeds the tolerance are
+  // re-evaluated with the spectral stage in double-float (in place by the
+  // persistent spectral kernel; sizes 2048 and 4096 listed in fb_list with
+  // their series offsets for the standalone kernel); those still above it
+  // (fb2_list) get FP64 series that the standalone kernel transforms, all in
+  // the same launch sequence (fb_e1 = fb_e2 = 0: no re-evaluation)
+  float fb_e1 = 0.f, fb_e2 = 0.f, hp_e1 = 0.f;
+  int *fb_list = nullptr;                  // [cap]
+  long long *fb_off = nullptr;             // [cap]
+  int *fb2_list = nullptr;                 // [cap]
+  int *fb_count = nullptr;                 // bin_count + kNumBins + 1
+  int *fb2_count = nullptr;                // bin_count + kNumBins + 2
+  unsigned long long *fb_total = nullptr;  // [2]: re-evaluated in double-float, from FP64 series
+  float *fb_inv_scale = nullptr;           // [fb_nscale]: 1 / per-proposal tolerance scale (null: 1)
+  int fb_nscale = 0, fb_nscale_cap = 0;
   // every launch sequence leaves the counts at zero (the spectral kernel's last
   // CTA, or a trailing memset), so the next one needs no leading memset; false
   // when that is not known (a launch returned an error part-way)
   bool counts_zero = false;
   void *series = nullptr;       // 4 arm-combination series per proposal
   // optional timing of each phase of a step on the caller's stream: events
-  // before the plan kernel, after it, after the slow-part kernel and after the
-  // spectral kernels (timing events; only when phase_timing is set)
+  // before the plan kernel, after it, after the slow-part kernel, after the
+  // spectral kernels and after the re-evaluations that follow them (timing
+  // events; only when phase_timing is set)
   bool phase_timing = false;
   bool phase_recorded = false;
-  cudaEvent_t phase[4] = {};
+  cudaEvent_t phase[5] = {};
 };
 
 // Host-side table construction for a bank: G and w tables, prefix sums.
 void fd_build_bank_tables(int format, double T, double fstar, int NFFT, int nseg, const int *qmin, const double *rA,
                           const double *rE, const double *invCA, const double *invCE, float4 *w32, float4 *w32lo,
-                          float4 *g32, double *Q, double2 *w64, double2 *g64, double *QA = nullptr);
+                          float4 *g32, double *Q, double2 *w64, double2 *g64, double *QA = nullptr,
+                          float4 *g32lo = nullptr);
 
 cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStream_t stream);
 

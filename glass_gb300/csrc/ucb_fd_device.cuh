@@ -157,6 +157,14 @@ __device__ __forceinline__ void group_fft(C *buf, const C *tw, int lane) {
 __host__ __device__ constexpr int pad16(int e) { return e + (e >> 4); }
 
 // v * exp(-2 pi i J / 16) for a compile-time J.
+//
+// The rotations must not change |v| on average: a template's power sits in a
+// few output bins, so a gain error common to every use of a constant becomes
+// a relative error of (h|h), which delta logL carries times (h|h) (1e-7 of a
+// template power of 1e6 is 0.1).  Rounded to floats, cos and sin of pi/8 give
+// |w|^2 - 1 = -5.7e-8 and those of pi/4 -3.4e-8: a gain of -2.3e-8 in every
+// 16-point pass.  So each constant is a hi + lo pair of floats and a product
+// takes two fused multiply-adds per term; only the two main products round.
 template <int J>
 __device__ __forceinline__ float2 w16mul(float2 v) {
   constexpr int j = J & 15;
@@ -169,13 +177,17 @@ __device__ __forceinline__ float2 w16mul(float2 v) {
   } else if constexpr (j == 12) {
     return make_float2(-v.y, v.x);
   } else {
-    // cos and sin of 2 pi j / 16 (multiples of pi/8)
-    constexpr float c8[16] = {1.f, 0.923879532511286756f, 0.707106781186547524f, 0.382683432365089772f, 0.f,
-                              -0.382683432365089772f, -0.707106781186547524f, -0.923879532511286756f, -1.f,
-                              -0.923879532511286756f, -0.707106781186547524f, -0.382683432365089772f, 0.f,
-                              0.382683432365089772f, 0.707106781186547524f, 0.923879532511286756f};
-    constexpr float c = c8[j], sn = c8[(j + 12) & 15];  // sin x = cos(x - pi/2)
-    return make_float2(fmaf(v.x, c, v.y * sn), fmaf(v.y, c, -(v.x * sn)));
+    // cos(k pi/8) = hi + lo: 1, cos(pi/8), sqrt(1/2), sin(pi/8), 0, ...
+    constexpr float Ch = 0.9238795042037964f, Cl = 2.830748968563057e-08f;
+    constexpr float Kh = 0.7071067690849304f, Kl = 1.2101617485882343e-08f;
+    constexpr float Sh = 0.3826834261417389f, Sl = 6.2233507236442165e-09f;
+    constexpr float hi[16] = {1.f, Ch, Kh, Sh, 0.f, -Sh, -Kh, -Ch, -1.f, -Ch, -Kh, -Sh, 0.f, Sh, Kh, Ch};
+    constexpr float lo[16] = {0.f, Cl, Kl, Sl, 0.f, -Sl, -Kl, -Cl, 0.f, -Cl, -Kl, -Sl, 0.f, Sl, Kl, Cl};
+    constexpr int js = (j + 12) & 15;  // sin x = cos(x - pi/2)
+    constexpr float c = hi[j], cl = lo[j], s = hi[js], sl = lo[js];
+    // (x c + y s, y c - x s)
+    return make_float2(fmaf(v.x, c, fmaf(v.y, s, fmaf(v.x, cl, v.y * sl))),
+                       fmaf(v.y, c, fmaf(-v.x, s, fmaf(v.y, cl, -(v.x * sl)))));
   }
 }
 
@@ -241,13 +253,23 @@ __device__ __forceinline__ void dft_reg(float2 *v) {
   }
 }
 
+// Twiddle products of the register FFT: a float2 twiddle, or a float4
+// holding a twiddle as hi + lo floats (x, y: hi; z, w: lo), whose product
+// rounds only at its two main terms.  In a loud narrowband template the few
+// twiddles on its bins' paths set an error common to the template.
+__device__ __forceinline__ float2 twmul(float2 v, float2 t) { return cmul(v, t); }
+__device__ __forceinline__ float2 twmul(float2 v, float4 t) {
+  return make_float2(fmaf(v.x, t.x, fmaf(-v.y, t.y, fmaf(v.x, t.z, -(v.y * t.w)))),
+                     fmaf(v.x, t.y, fmaf(v.y, t.x, fmaf(v.x, t.w, v.y * t.z))));
+}
+
 // One Stockham stage of radix R and sub-transform size P on a padded series
 // y of length N, by the M = N/16 threads of the series (thread t does the
 // 16/R butterflies i = t + M b): reads x[i + m N/R], multiplies by
 // exp(-2 pi i m k / (P R)), k = i mod P, and writes y[(i - k) R + k + q P].
-// tw: exp(-2 pi i j / N) at pad16(j).
-template <int N, int R, int P>
-__device__ __forceinline__ void reg_stage_load(const float2 *y, const float2 *tw, int t, float2 *v) {
+// tw: exp(-2 pi i j / N) at pad16(j) (float2, or float4 as hi + lo).
+template <int N, int R, int P, typename TW>
+__device__ __forceinline__ void reg_stage_load(const float2 *y, const TW *tw, int t, float2 *v) {
   constexpr int M = N / 16, NB = 16 / R, STRIDE = N / R, TS = N / (P * R);
 #pragma unroll
   for (int b = 0; b < NB; ++b) {
@@ -255,7 +277,7 @@ __device__ __forceinline__ void reg_stage_load(const float2 *y, const float2 *tw
 #pragma unroll
     for (int m = 0; m < R; ++m) {
       float2 val = y[pad16(i + m * STRIDE)];
-      if (P > 1 && m > 0) val = cmul(val, tw[pad16(m * k * TS)]);
+      if (P > 1 && m > 0) val = twmul(val, tw[pad16(m * k * TS)]);
       v[b * R + m] = val;
     }
   }
@@ -271,8 +293,8 @@ __device__ __forceinline__ void reg_stage_store(float2 *y, int t, float2 *v) {
     for (int q = 0; q < R; ++q) y[pad16((i - k) * R + k + q * P)] = v[b * R + q];
   }
 }
-template <int N, int GT, int R, int P>
-__device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, float2 *v) {
+template <int N, int GT, int R, int P, typename TW>
+__device__ __forceinline__ void reg_stage(float2 *y, const TW *tw, int t, float2 *v) {
   reg_stage_load<N, R, P>(y, tw, t, v);
   group_sync<GT>();  // every read of the stage before the in-place writes
   reg_stage_store<N, R, P>(y, t, v);
@@ -282,8 +304,8 @@ __device__ __forceinline__ void reg_stage(float2 *y, const float2 *tw, int t, fl
 // One stage of fft_reg_smem over NSER series in rounds of GT/M (one series
 // per M threads): rounds touch disjoint series, so a round's loads need no
 // barrier after the previous round's stores, only one before its own stores.
-template <int N, int GT, int NSER, int R, int P>
-__device__ __forceinline__ void reg_stage_rounds(float2 *sbuf, const float2 *tw, int s, int t, float2 *v) {
+template <int N, int GT, int NSER, int R, int P, typename TW>
+__device__ __forceinline__ void reg_stage_rounds(float2 *sbuf, const TW *tw, int s, int t, float2 *v) {
   constexpr int SN = pad16(N), SPR = GT / (N / 16);
 #pragma unroll 1
   for (int r = 0; r < NSER / SPR; ++r) {
@@ -298,8 +320,8 @@ __device__ __forceinline__ void reg_stage_rounds(float2 *sbuf, const float2 *tw,
 // As fft4_reg for NSER series already in the padded shared-memory layout
 // (series stride pad16(N)), transformed in place by GT threads: GT/M series
 // at a time (a multiple of 4 dividing NSER).
-template <int N, int GT, int NSER>
-__device__ __forceinline__ void fft_reg_smem(float2 *sbuf, const float2 *tw, int lane) {
+template <int N, int GT, int NSER, typename TW>
+__device__ __forceinline__ void fft_reg_smem(float2 *sbuf, const TW *tw, int lane) {
   constexpr int M = N / 16;
   static_assert(GT % (4 * M) == 0 && NSER % (GT / M) == 0 && N >= 32 && N <= 4096, "fft_reg_smem shape");
   const int s = lane / M, t = lane - (lane / M) * M;
@@ -321,8 +343,8 @@ __device__ __forceinline__ void fft_reg_smem(float2 *sbuf, const float2 *tw, int
 // version, group_fft, needs log4 N).  The first stage reads the series from
 // global memory (src, 4 series of N back to back); every stage writes the
 // padded shared-memory series sbuf (stride pad16(N)), natural order at the end.
-template <int N, int GT>
-__device__ __forceinline__ void fft4_reg(const float2 *src, float2 *sbuf, const float2 *tw, int lane) {
+template <int N, int GT, typename TW>
+__device__ __forceinline__ void fft4_reg(const float2 *src, float2 *sbuf, const TW *tw, int lane) {
   constexpr int M = N / 16, SN = pad16(N);
   static_assert(4 * M == GT && N >= 32 && N <= 4096, "fft4_reg shape");
   const int s = lane / M, t = lane - (lane / M) * M;
@@ -477,28 +499,37 @@ static __host__ __device__ void make_item_f64(const SourceGeom &g, int N, ItemF6
 }
 
 static __device__ void make_item_mix(const SourceGeom &g, int N, double T, double fstar, ItemMix &c) {
-  for (int i = 0; i < 3; i++) c.k[i] = (float)g.k[i];
+  for (int i = 0; i < 3; i++) {
+    c.k[i] = (float)g.k[i];
+    c.kl[i] = (float)(g.k[i] - (double)c.k[i]);
+  }
   c.k[3] = 0.f;
+  const double s = g.amp / (2.0 * (double)N);
+  const int e = ilogb(s);
+  const double m = scalbn(s, -e);  // in [1, 2)
+  c.amp_p2 = (float)scalbn(1.0, e);
   for (int i = 0; i < 6; i++) {
-    c.Mr[i] = (float)(g.DPr * g.ep[i] + g.DCr * g.ec[i]);
-    c.Mi[i] = (float)(g.DPi * g.ep[i] + g.DCi * g.ec[i]);
+    const double mr = m * (g.DPr * g.ep[i] + g.DCr * g.ec[i]), mi = m * (g.DPi * g.ep[i] + g.DCi * g.ec[i]);
+    c.Mr[i] = (float)mr;
+    c.Mi[i] = (float)mi;
+    c.Mrl[i] = (float)(mr - (double)c.Mr[i]);
+    c.Mil[i] = (float)(mi - (double)c.Mi[i]);
   }
   c.fonfs0 = (float)(g.f0 / fstar);
+  c.fonfs0l = (float)(g.f0 / fstar - (double)c.fonfs0);
   c.fdfs = (float)(g.fdot * T / fstar);
   c.aef = (float)(0.66666666666666666666 * g.fdot * T / g.f0);
   c.w0c = (float)(kPI2 * g.f0 / kCLIGHT);
+  c.w0cl = (float)(kPI2 * g.f0 / kCLIGHT - (double)c.w0c);
   c.p7pi = (float)(kPI * g.fdot * T * T);
-  double s = g.amp / (2.0 * (double)N);
   c.amp_hi = (float)s;
   c.amp_lo = (float)(s - (double)c.amp_hi);
-  c.pad2 = 0.f;
   c.eps2pi = df_from_double(kPI2 * g.eps);
   double bscale = kPI2 * g.f0 * (kAU / kCLIGHT);
   c.beta1 = df_from_double(bscale * g.k[0]);
   c.beta2 = df_from_double(bscale * g.k[1]);
   c.phi0 = df_from_double(g.phi0);
   c.p7pi_d = df_from_double(kPI * g.fdot * T * T);
-  c.pad3 = {0.f, 0.f};
 }
 
 // ----------------------------------------------------------------- slow part
@@ -523,24 +554,29 @@ __device__ __forceinline__ float sinc_f(float x) {
 
 // sin and cos of an FP32 argument of a few radians, FMA-only: Cody-Waite
 // reduction by pi/2 (two-part constant, exact first product under FMA) to
-// r in [-pi/4, pi/4], then sin r = r + r^3 P(r^2) and cos r = 1 + r^2 Q(r^2)
-// with coefficients fitted for this library by least squares on Chebyshev
-// nodes (maximum error 4e-8 for sin and 7e-8 for cos on the interval, i.e.
-// FP32 rounding level).  Valid for |x| < ~1e3.
+// r in [-pi/4, pi/4], then sin r = r + r^3 P(r^2) (degree 11) and
+// cos r = 1 + r^2 Q(r^2) (degree 12), coefficients fitted for this library by
+// least squares in 40-digit arithmetic and rounded to float: the polynomial
+// error (a few 1e-10) is far below the final rounding, so what is left is
+// the rounding of the result.  (A polynomial error at the FP32 rounding level
+// is a smooth function of the phase: a template-wide error, not noise.)
+// Valid for |x| < ~1e3.
 __device__ __forceinline__ void fast_sincos(float x, float *s, float *c) {
   const float q = rintf(x * 0.63661977236758134f);  // 2/pi
   float r = fmaf(-q, 1.57079637050628662f, x);      // float(pi/2)
   r = fmaf(-q, -4.37113900018624283e-08f, r);       // pi/2 - float(pi/2)
   const float z = r * r;
-  float ps = 2.7505225261847954e-06f;
-  ps = fmaf(ps, z, -1.9841050379909575e-04f);
-  ps = fmaf(ps, z, 8.33333283662796e-03f);
-  ps = fmaf(ps, z, -0.1666666716337204f);
+  float ps = -2.4744322334957435e-08f;
+  ps = fmaf(ps, z, 2.755507975968258e-06f);
+  ps = fmaf(ps, z, -1.9841262250796924e-04f);
+  ps = fmaf(ps, z, 8.333333321634624e-03f);
+  ps = fmaf(ps, z, -0.16666666666603547f);
   const float sr = fmaf(r * z, ps, r);
-  float pc = -2.723719489949872e-07f;
-  pc = fmaf(pc, z, 2.4799863240332343e-05f);
-  pc = fmaf(pc, z, -1.3888884568586946e-03f);
-  pc = fmaf(pc, z, 4.16666679084301e-02f);
+  float pc = 2.0646641311441812e-09f;
+  pc = fmaf(pc, z, -2.7555547982977536e-07f);
+  pc = fmaf(pc, z, 2.4801580851006652e-05f);
+  pc = fmaf(pc, z, -1.3888888877952254e-03f);
+  pc = fmaf(pc, z, 4.1666666666599225e-02f);
   pc = fmaf(pc, z, -0.5f);
   const float cr = fmaf(z, pc, 1.0f);
   const int qi = ((int)q) & 3;
@@ -604,7 +640,7 @@ __device__ __forceinline__ void slow_sample64(const ItemF64 &c, const OrbitSampl
 // rounding error of the high-part sum (two_sum) collected in one FP32 error
 // term, one reduction at the end (~55 FP32 instructions; the same to FP32
 // rounding of the reduced angle as df_mul/df_add chains, which take ~100).
-__device__ __forceinline__ float carrier_phase_mix(const ItemMix &c, const OrbitSampleMix &o) {
+__device__ __forceinline__ df carrier_phase_mix(const ItemMix &c, const OrbitSampleMix &o) {
   const float uh = o.u_hi, ul = o.u_lo;
   // u^2 as hi + lo
   const df uu = two_prod(uh, uh);
@@ -627,7 +663,7 @@ __device__ __forceinline__ float carrier_phase_mix(const ItemMix &c, const Orbit
   err += sum.lo;
   sum = two_sum(sum.hi, -c.phi0.hi);
   err += sum.lo - c.phi0.lo;
-  return df_reduce_2pi(quick_two_sum(sum.hi, err));
+  return df_reduce_2pi_df(quick_two_sum(sum.hi, err));
 }
 
 // Mixed precision: the carrier phase common to the three spacecraft
@@ -652,30 +688,41 @@ __device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSam
   // k.(x_i - x_gc) per spacecraft (metres); k.r_ij from their differences
   float kd[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++) kd[i] = fmaf(c.k[0], f[3 * i], fmaf(c.k[1], f[3 * i + 1], c.k[2] * f[3 * i + 2]));
+  for (int i = 0; i < 3; i++)
+    kd[i] = fmaf(c.k[0], f[3 * i], fmaf(c.k[1], f[3 * i + 1], fmaf(c.k[2], f[3 * i + 2],
+            fmaf(c.kl[0], f[3 * i], fmaf(c.kl[1], f[3 * i + 1], c.kl[2] * f[3 * i + 2])))));
   const float kr12 = (kd[1] - kd[0]) * invL, kr13 = (kd[2] - kd[0]) * invL, kr23 = (kd[2] - kd[1]) * invL;
-  auto quad6 = [&](const float *M, int a) {
+  // r^T M r with M = hi + lo: the lo part's sum first, so that only the
+  // products of the hi part round at full size
+  auto quad6 = [&](const float *M, const float *Ml, int a) {
     const float *mo = f + 9 + 6 * a;
-    return fmaf(M[0], mo[0], fmaf(M[1], mo[1], fmaf(M[2], mo[2], fmaf(M[3], mo[3], fmaf(M[4], mo[4], M[5] * mo[5])))));
+    const float l = fmaf(Ml[0], mo[0], fmaf(Ml[1], mo[1], fmaf(Ml[2], mo[2], fmaf(Ml[3], mo[3], fmaf(Ml[4], mo[4], Ml[5] * mo[5])))));
+    return fmaf(M[0], mo[0], fmaf(M[1], mo[1], fmaf(M[2], mo[2], fmaf(M[3], mo[3], fmaf(M[4], mo[4], fmaf(M[5], mo[5], l))))));
   };
-  const float mr12 = quad6(c.Mr, 0), mi12 = quad6(c.Mi, 0);
-  const float mr13 = quad6(c.Mr, 1), mi13 = quad6(c.Mi, 1);
-  const float mr23 = quad6(c.Mr, 2), mi23 = quad6(c.Mi, 2);
+  const float mr12 = quad6(c.Mr, c.Mrl, 0), mi12 = quad6(c.Mi, c.Mil, 0);
+  const float mr13 = quad6(c.Mr, c.Mrl, 1), mi13 = quad6(c.Mi, c.Mil, 1);
+  const float mr23 = quad6(c.Mr, c.Mrl, 2), mi23 = quad6(c.Mi, c.Mil, 2);
 
-  const float psi0 = carrier_phase_mix(c, o);
+  // The phase of each arm is carried as hi + lo until the rotation: rounded
+  // to float it would carry ~2e-7 rad of noise per sample from three
+  // roundings, which the first-order correction of the sine and cosine
+  // below removes.
+  const df psi0 = carrier_phase_mix(c, o);
   const float uf = o.u_hi;
   const float tgc = AUc * (c.k[0] * ca + c.k[1] * sa);  // guiding-centre delay (s)
 
-  float fon[3], arg2[3], aev[3];
+  float fon[3], aev[3];
+  df arg2[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     const float kdx = kd[i];  // k.(x_i - x_gc), metres
     float taui = tgc + kdx * (float)(1.0 / kCLIGHT);
     float tT = taui * invT;
     float v = uf - tT;  // xi / T
-    fon[i] = fmaf(c.fdfs, v, c.fonfs0);
+    fon[i] = c.fonfs0 + fmaf(c.fdfs, v, c.fonfs0l);
     aev[i] = fmaf(c.aef, v, 1.0f);
-    arg2[i] = psi0 - c.w0c * kdx + c.p7pi * tT * (tT - 2.0f * uf);
+    const df wk = two_prod(c.w0c, kdx);
+    arg2[i] = df_add(psi0, df{-wk.hi, fmaf(c.p7pi * tT, tT - 2.0f * uf, -fmaf(c.w0cl, kdx, wk.lo))});
   }
   const int ai[6] = {0, 0, 1, 1, 2, 2};
   const float mrs[6] = {mr12, mr13, mr12, mr23, mr13, mr23};
@@ -688,9 +735,12 @@ __device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSam
     float sinc = 0.25f * sinc_f(arg1);
     float t1r = aev[i] * mrs[a];
     float t1i = aev[i] * mis[a];
+    const df th = two_sum(arg1, -arg2[i].hi);
+    const float tl = th.lo - arg2[i].lo;
     float s2, c2;
-    fast_sincos(arg1 - arg2[i], &s2, &c2);
-    d[a] = make_float2(sinc * (t1r * c2 + t1i * s2), sinc * (-t1r * s2 + t1i * c2));
+    fast_sincos(th.hi, &s2, &c2);
+    const float s2c = fmaf(tl, c2, s2), c2c = fmaf(-tl, s2, c2);  // sin, cos of th.hi + tl
+    d[a] = make_float2(sinc * (t1r * c2c + t1i * s2c), sinc * (-t1r * s2c + t1i * c2c));
   }
 }
 
@@ -881,6 +931,7 @@ struct SpecArgs {
   const float4 *w32;
   const float4 *w32lo;
   const float4 *g32;
+  const float4 *g32lo = nullptr;
   const double *Q;
   const double2 *w64;
   const double2 *g64;
@@ -891,7 +942,71 @@ struct SpecArgs {
   // share of term_y (c = 0 A, 1 E); QA the A channel's part of Q
   double *term_ch = nullptr;
   const double *QA = nullptr;
+  // mixed precision: a proposal whose error estimate
+  //   (fb_e1 sqrt(hw rr) + fb_e2 (hw + rr)) / scale_i
+  // (hw = |h|^2, rr = |r - h|^2, whitened sums over the template support)
+  // exceeds 1 is re-evaluated in double-float: in place by the persistent
+  // kernel, or listed in fb_list (count in *fb_count, series offsets in
+  // fb_off) by the per-size kernels; fb_total[0] counts them.  No list: no
+  // estimate.
+  int *fb_count = nullptr, *fb_list = nullptr;
+  long long *fb_off = nullptr;
+  unsigned long long *fb_total = nullptr;  // [2]: re-evaluated in double-float, from FP64 series
+  float fb_e1 = 0.f, fb_e2 = 0.f;
+  // proposals still above the tolerance after the double-float re-evaluation
+  // (estimate hp_e1 sqrt(hw rr) / scale_i) go to fb2_list for FP64 series
+  int *fb2_count = nullptr, *fb2_list = nullptr;
+  float hp_e1 = 0.f;
+  // per-proposal tolerance scale: 1/scale_i for i < fb_nscale (null: 1)
+  const float *fb_inv_scale = nullptr;
+  int fb_nscale = 0;
 };
+
+// The estimate's factor for proposal i (1 / its tolerance scale).
+__device__ __forceinline__ float fb_scale_of(const float *inv_scale, int n, int i) {
+  return (inv_scale && i < n) ? inv_scale[i] : 1.f;
+}
+
+// Double-float spectral re-evaluation (ucb_fd_hp.cu) of listed mixed proposals
+// (list mode) or of the FP64 series of binned proposals (bin mode).
+struct HpArgs {
+  int NFFT, cap;
+  int nmax;  // largest template size the bank allows (shared memory is sized for it)
+  // list mode (mixed series): items list[0 .. *count), series offsets off[] (float2 elements)
+  const int *list = nullptr;
+  const int *count = nullptr;
+  const long long *off = nullptr;
+  const float2 *series32 = nullptr;
+  const ItemMix *itemsmix = nullptr;
+  // bin mode (FP64 series from the FP64 slow part, laid out by the size counts)
+  const double2 *series64 = nullptr;
+  const int *bin_count = nullptr;
+  const int *bin_list = nullptr;
+  const ItemF64 *items64 = nullptr;
+  // zeroing at the end: the last CTA zeroes nzero ints at zero_at
+  int *zero_at = nullptr;
+  int nzero = 0;
+  int *done = nullptr;  // CTA-done counter (zeroed by the last CTA)
+  // segment tables, as hi + lo floats: whitened residual {A, E}, TDI/whitening
+  // weights {G2, G1} per channel, and twiddles of each size
+  const float4 *w32, *w32lo, *g32, *g32lo;
+  const double *Q, *QA;
+  const float4 *tw32x[kNumBins];
+  // outputs
+  const double *term_x;
+  double *dlogl, *term_y, *hh, *term_ch;
+  int *status;
+  // next tier (list mode): items whose estimate e1 sqrt(hw rr) / scale_i exceeds 1
+  int *next_count = nullptr, *next_list = nullptr;
+  unsigned long long *next_total = nullptr;
+  float next_e1 = 0.f;
+  bool has_cond = false;  // set the conditional node's value to (*next_count > 0) at the end
+  cudaGraphConditionalHandle cond = 0;
+  const float *inv_scale = nullptr;
+  int nscale = 0;
+};
+size_t fd_hp_smem_bytes(int nmax);
+cudaError_t fd_launch_hp(const HpArgs &a, bool bin_mode, bool perch, int num_sms, cudaStream_t stream);
 
 // Start (in samples) of size bin `bin` in the scratch series: sizes are laid
 // out in increasing order, proposals of one size back to back, each holding 4
@@ -907,8 +1022,8 @@ __device__ __forceinline__ long long bin_sample_start(const int *bin_count, int 
 // ------------------------------------------------------- stage 1 (templated)
 // One warp per 32 consecutive samples of one proposal (every N is a multiple
 // of 32), grid-stride over all proposals of every size.
-template <bool MIX>
-__global__ void __launch_bounds__(256) fd_slow_kernel(SlowArgs a) {
+template <bool MIX, int BLOCK = 256>
+__global__ void __launch_bounds__(BLOCK) fd_slow_kernel(SlowArgs a) {
   using C = typename std::conditional<MIX, float2, double2>::type;
   // chunk offsets per size (chunks of 32 samples: N/32 = 2^b per proposal), in registers
   int cs[kNumBins + 1];
@@ -962,12 +1077,14 @@ struct SpecCfg {
 template <int N, bool MIX>
 struct SpecSmem {
   using C = typename std::conditional<MIX, float2, double2>::type;
+  // twiddles: FP64, or hi + lo floats for the mixed register FFT
+  using TW = typename std::conditional<MIX, float4, double2>::type;
   static constexpr int NSER = (!MIX && N == 4096) ? 2 : 4;  // series resident at once
   static constexpr int PASSES = 4 / NSER;
   // mixed: twiddles and series in padded rows (pad16)
   static constexpr int SN = MIX ? pad16(N) : N;
   static constexpr size_t bytes =
-      sizeof(C) * (size_t)SN * (1 + (size_t)SpecCfg<N>::GPC * NSER) + sizeof(double) * 3 * 32;
+      sizeof(TW) * (size_t)SN + sizeof(C) * (size_t)SN * (size_t)SpecCfg<N>::GPC * NSER + sizeof(double) * 3 * 32;
 };
 
 // Sum over the threads of one group (result valid in lane 0 of the group).
@@ -1011,16 +1128,64 @@ __device__ __forceinline__ df group_sum_df(float v, float2 *red, int lane) {
   return s;
 }
 
+// The same for a double-float value per thread.
+template <int GT>
+__device__ __forceinline__ df group_sum_df(df s, float2 *red, int lane) {
+#pragma unroll
+  for (int off = (GT < 32 ? GT : 32) / 2; off > 0; off >>= 1) {
+    df o = {__shfl_xor_sync(0xffffffffu, s.hi, off), __shfl_xor_sync(0xffffffffu, s.lo, off)};
+    s = df_add(s, o);
+  }
+  if constexpr (GT > 32) {
+    __syncthreads();
+    if ((lane & 31) == 0) red[lane >> 5] = make_float2(s.hi, s.lo);
+    __syncthreads();
+    if (lane == 0) {
+      df t = {0.f, 0.f};
+      for (int w = 0; w < GT / 32; w++) t = df_add(t, df{red[w].x, red[w].y});
+      s = t;
+    }
+  }
+  return s;
+}
+
+// Adds (w_hi + w_lo - h)^2 to the compensated sum (S, E): the residual's
+// rounding error and the square's are carried exactly (two_sum, two_prod)
+// and every addition's error collects in E (cascaded summation), so the sum
+// has no rounding of the order of its terms.  A loud template far from the
+// data puts |r|^2 ~ 1e6 into a few bins; rounded there, the sum would carry
+// an error of ~1e-8 of itself into delta logL.
+__device__ __forceinline__ void acc_resid_sq(float whi, float wlo, float h, float &S, float &E) {
+  const df r = two_sum(whi, -h);
+  const float rl = r.lo + wlo;
+  const df p = two_prod(r.hi, r.hi);
+  const df t = two_sum(S, p.hi);
+  S = t.hi;
+  E += t.lo + fmaf(2.f * r.hi, rl, p.lo);
+}
+
+// a b + c, complex, with fused multiply-adds
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, c.y)));
+}
+
+}  // namespace glass
+#include "ucb_fd_hp.cuh"
+namespace glass {
+
 // One unit of the spectral stage: GPC proposals of size N, one group of N/4
 // threads each, in a CTA of GPC N/4 threads.  Per proposal: the 4 A/E series
 // (from the slow kernel's scratch) are FFT'd in shared memory, weighted per bin
 // by the segment's TDI/whitening table and reduced to the residual power.
 // reds: 96 doubles of reduction scratch per group.
+// flags (shared memory, one per group; null: list the flagged proposals in
+// fb_list instead): set for a mixed proposal whose error estimate exceeds
+// the tolerance, which the caller then re-evaluates in place.
 template <int N, bool MIX, int GPC, bool PERCH = false>
 __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list, int count, int base,
                                           const typename SpecSmem<N, MIX>::C *series,
-                                          const typename SpecSmem<N, MIX>::C *tw,
-                                          typename SpecSmem<N, MIX>::C *bufs, double *reds) {
+                                          const typename SpecSmem<N, MIX>::TW *tw,
+                                          typename SpecSmem<N, MIX>::C *bufs, double *reds, int *flags = nullptr) {
   using S = SpecSmem<N, MIX>;
   using C = typename S::C;
   constexpr int GT = N / 4, NSER = S::NSER, PASSES = S::PASSES;
@@ -1044,9 +1209,10 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
     imin = a.items64[item].imin;
   }
   const C *src = series + (size_t)sl * 4 * N;
-  float facc = 0.f, fh = 0.f, fc = 0.f;  // mixed: per-thread partial sums
+  // mixed: per-thread compensated sums of |r - h|^2 (A in (rS, eS), E in
+  // (rE, eE): two independent chains) and a float sum of |h|^2
+  float rS = 0.f, rE = 0.f, eS = 0.f, eE = 0.f, fh = 0.f;
   double acc = 0.0, hacc = 0.0;
-  float faccE = 0.f, fcE = 0.f;  // PERCH: the E channel's shares (facc, fc then hold A's)
   double accE = 0.0;
 #pragma unroll 1
   for (int pass = 0; pass < PASSES; ++pass) {
@@ -1068,27 +1234,26 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       if (j < 0 || j >= NFFT) continue;
       const size_t sj = (size_t)seg * NFFT + j;
       if constexpr (MIX) {
-        const float4 w = a.w32[sj];
+        const float4 w = a.w32[sj], wl = a.w32lo[sj];
         const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
-        const float sh = a.itemsmix[item].amp_hi;
+        const float4 gAl = a.g32lo[2 * sj], gEl = a.g32lo[2 * sj + 1];
+        const float p2 = a.itemsmix[item].amp_p2;
         const int kp = pad16(k);
-        float2 HA = cadd(cmul(buf[0 * SN + kp], make_float2(gA.x, gA.y)), cmul(buf[1 * SN + kp], make_float2(gA.z, gA.w)));
-        float2 HE = cadd(cmul(buf[2 * SN + kp], make_float2(gE.x, gE.y)), cmul(buf[3 * SN + kp], make_float2(gE.z, gE.w)));
-        // template scaled by amp_hi (O(1) whitened values; the unscaled
-        // product would overflow FP32 when squared)
-        const float2 hA = cscale(HA, sh), hE = cscale(HE, sh);
-        const float4 wl = a.w32lo[sj];
-        const float ar = (w.x - hA.x) + wl.x, ai = (w.y - hA.y) + wl.y;
-        const float er = (w.z - hE.x) + wl.z, ei = (w.w - hE.y) + wl.w;
-        if constexpr (PERCH) {
-          facc += fmaf(ar, ar, ai * ai);
-          faccE += fmaf(er, er, ei * ei);
-          fc += fmaf(ar, hA.x, ai * hA.y);
-          fcE += fmaf(er, hE.x, ei * hE.y);
-        } else {
-          facc += fmaf(ar, ar, ai * ai) + fmaf(er, er, ei * ei);
-          fc += fmaf(ar, hA.x, ai * hA.y) + fmaf(er, hE.x, ei * hE.y);
-        }
+        const float2 b0 = buf[0 * SN + kp], b1 = buf[1 * SN + kp], b2 = buf[2 * SN + kp], b3 = buf[3 * SN + kp];
+        // the bin's table entries as hi + lo (the lo products first), then
+        // the amplitude's power of two, which is exact: O(1) whitened values
+        // (unscaled, their squares would overflow FP32)
+        const float2 HA = cfma(b0, make_float2(gA.x, gA.y),
+                               cfma(b1, make_float2(gA.z, gA.w),
+                                    cfma(b0, make_float2(gAl.x, gAl.y), cmul(b1, make_float2(gAl.z, gAl.w)))));
+        const float2 HE = cfma(b2, make_float2(gE.x, gE.y),
+                               cfma(b3, make_float2(gE.z, gE.w),
+                                    cfma(b2, make_float2(gEl.x, gEl.y), cmul(b3, make_float2(gEl.z, gEl.w)))));
+        const float2 hA = cscale(HA, p2), hE = cscale(HE, p2);
+        acc_resid_sq(w.x, wl.x, hA.x, rS, eS);
+        acc_resid_sq(w.y, wl.y, hA.y, rS, eS);
+        acc_resid_sq(w.z, wl.z, hE.x, rE, eE);
+        acc_resid_sq(w.w, wl.w, hE.y, rE, eE);
         fh += fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y);
       } else {
         const double s = a.items64[item].amp_s;
@@ -1110,16 +1275,16 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
     }
     group_sync<GT>();
   }
-  df sa, sh, sc, saE, scE;
+  df sa, sh, saE;
   if constexpr (MIX) {
     float2 *redf = reinterpret_cast<float2 *>(red);
-    sa = group_sum_df<GT>(facc, redf, lane);
-    sh = group_sum_df<GT>(fh, redf + 32, lane);
-    sc = group_sum_df<GT>(fc, redf + 64, lane);
     if constexpr (PERCH) {
-      saE = group_sum_df<GT>(faccE, redf, lane);
-      scE = group_sum_df<GT>(fcE, redf + 32, lane);
+      sa = group_sum_df<GT>(quick_two_sum(rS, eS), redf, lane);
+      saE = group_sum_df<GT>(quick_two_sum(rE, eE), redf + 64, lane);
+    } else {
+      sa = group_sum_df<GT>(df_add(quick_two_sum(rS, eS), quick_two_sum(rE, eE)), redf, lane);
     }
+    sh = group_sum_df<GT>(fh, redf + 32, lane);
   } else {
     acc = group_sum<GT>(acc, red, lane);
     hacc = group_sum<GT>(hacc, red + 32, lane);
@@ -1130,28 +1295,39 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
     if constexpr (MIX) {
       // FP64 only for the final sum (GB300's FP64 pipe is slow, and this runs
       // once per proposal at the end of every unit)
-      const ItemMix &c = a.itemsmix[item];
       int jlo = imin < 0 ? 0 : imin;
       int jhi = imin + N > NFFT ? NFFT : imin + N;
       const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
-      // sum |w - s H|^2 with s = amp_hi (1 + rho), rho = amp_lo/amp_hi: with
-      // d = w - amp_hi H, |w - s H|^2 = |d|^2 - 2 rho Re(d* amp_hi H) + O(rho^2);
-      // |rho| < 6e-8, so the correction and (1 + rho)^2 are FP32 to spare
-      const float rho = __fdiv_rn(c.amp_lo, c.amp_hi);
-      const df tail = df_add(df_neg(sa), df{2.f * rho * sc.hi, 0.f});
+      float rr;  // |r - h|^2 over the support, both channels
       if constexpr (PERCH) {
         const double *QAs = a.QA + (size_t)seg * (NFFT + 1);
-        const df tailE = df_add(df_neg(saE), df{2.f * rho * scE.hi, 0.f});
         const double qa = QAs[jhi] - QAs[jlo];
-        const double tA = (qa + (double)tail.hi) + (double)tail.lo;
-        const double tE = (((Qs[jhi] - Qs[jlo]) - qa) + (double)tailE.hi) + (double)tailE.lo;
+        const double tA = (qa - (double)sa.hi) - (double)sa.lo;
+        const double tE = (((Qs[jhi] - Qs[jlo]) - qa) - (double)saE.hi) - (double)saE.lo;
         a.term_ch[2 * (size_t)item] = tA;
         a.term_ch[2 * (size_t)item + 1] = tE;
         term = tA + tE;
+        rr = sa.hi + saE.hi;
       } else {
-        term = ((Qs[jhi] - Qs[jlo]) + (double)tail.hi) + (double)tail.lo;
+        term = ((Qs[jhi] - Qs[jlo]) - (double)sa.hi) - (double)sa.lo;
+        rr = sa.hi;
       }
-      hh = (double)(2.f * (1.f + rho) * (1.f + rho) * (sh.hi + sh.lo));
+      const float hw = sh.hi + sh.lo;
+      hh = 2.0 * (double)hw;
+      if (a.fb_list) {
+        const float est = fmaf(a.fb_e1, sqrtf(hw * rr), a.fb_e2 * (hw + rr)) *
+                          fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
+        if (!(est <= 1.f)) {  // also a non-finite estimate
+          atomicAdd(a.fb_total, 1ull);
+          if (flags) {
+            flags[g] = 1;
+          } else {
+            const int q = atomicAdd(a.fb_count, 1);
+            a.fb_list[q] = item;
+            a.fb_off[q] = (long long)(src - reinterpret_cast<const C *>(a.series));
+          }
+        }
+      }
     } else {
       if constexpr (PERCH) {
         a.term_ch[2 * (size_t)item] = acc;
@@ -1176,14 +1352,15 @@ __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
   using Cfg = SpecCfg<N>;
   using S = SpecSmem<N, MIX>;
   using C = typename S::C;
+  using TW = typename S::TW;
   constexpr int GPC = Cfg::GPC, NSER = S::NSER;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int SN = S::SN;
-  C *tw = reinterpret_cast<C *>(smem_raw);
-  C *bufs = tw + SN;
+  TW *tw = reinterpret_cast<TW *>(smem_raw);
+  C *bufs = reinterpret_cast<C *>(tw + SN);
   double *red = reinterpret_cast<double *>(bufs + (size_t)GPC * NSER * SN);
 
-  const C *twg = reinterpret_cast<const C *>(a.tw);
+  const TW *twg = reinterpret_cast<const TW *>(a.tw);
   for (int i = threadIdx.x; i < N; i += blockDim.x) tw[MIX ? pad16(i) : i] = twg[i];
   __syncthreads();
   const int count = a.bin_count[a.bin];
@@ -1203,8 +1380,9 @@ constexpr int kSpecAllBins = 6;  // N = 32 .. 1024
 template <bool MIX>
 struct SpecAllSmem {
   using C = typename std::conditional<MIX, float2, double2>::type;
+  using TW = typename std::conditional<MIX, float4, double2>::type;
   static constexpr int SN = MIX ? pad16(1024) : 1024;  // mixed: padded rows
-  static constexpr size_t bytes = sizeof(C) * (SN + 4 * SN) + sizeof(double) * 96 * 4;
+  static constexpr size_t bytes = sizeof(TW) * SN + sizeof(C) * 4 * SN + sizeof(double) * 96 * 4;
 };
 
 struct SpecAllArgs {
@@ -1212,18 +1390,37 @@ struct SpecAllArgs {
   const void *tw[kSpecAllBins];  // twiddles per size
   int nbins;                     // sizes 32 << b for b < nbins
   int *zero_counts;              // non-null: the last CTA to finish zeroes the kNumBins
-                                 // counts there and the done counter after them
+                                 // counts there, the done counter after them and
+                                 // zero_extra more ints after that
+  int zero_extra = 0;
+  // [2]: the next-unit counter (units after the first grid's worth are handed
+  // out dynamically when proposals are re-evaluated in place) and the
+  // CTA-done counter; the last CTA zeroes both
+  int *sched = nullptr;
+  // when the launch is being captured into a CUDA graph: the handle of the
+  // conditional node around the FP64-series re-evaluation, which the last CTA
+  // sets to (*cond_count > 0)
+  bool has_cond = false;
+  cudaGraphConditionalHandle cond = 0;
+  const int *cond_count = nullptr;
 };
 
 template <bool MIX, bool PERCH = false>
 __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAllArgs A) {
   using C = typename SpecAllSmem<MIX>::C;
+  using TW = typename SpecAllSmem<MIX>::TW;
   const SpecArgs &a = A.a;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int SN = SpecAllSmem<MIX>::SN;
-  C *tw = reinterpret_cast<C *>(smem_raw);
-  C *bufs = tw + SN;
+  TW *tw = reinterpret_cast<TW *>(smem_raw);
+  C *bufs = reinterpret_cast<C *>(tw + SN);
   double *reds = reinterpret_cast<double *>(bufs + 4 * SN);
+  __shared__ int s_flag[32], s_next;
+  // mixed precision with a tolerance: a flagged proposal is evaluated again
+  // by this CTA (double-float spectral stage, in the shared memory of the
+  // twiddles and series: 3 N double-float values <= 48 KB), while the other
+  // CTAs take the remaining units, which are then handed out dynamically
+  const bool inplace = MIX && a.fb_list != nullptr;
   int ustart[kSpecAllBins + 1];  // in largest-first order
   int total = 0;
 #pragma unroll
@@ -1237,7 +1434,8 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
   }
   ustart[kSpecAllBins] = total;
   int cur = -1;
-  for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
+  int unit = blockIdx.x;
+  while (unit < total) {
     int q = 0;
 #pragma unroll
     for (int qq = 1; qq < kSpecAllBins; qq++)
@@ -1246,7 +1444,7 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
     const int N = 32 << b;
     if (b != cur) {
       __syncthreads();
-      const C *twg = reinterpret_cast<const C *>(A.tw[b]);
+      const TW *twg = reinterpret_cast<const TW *>(A.tw[b]);
       for (int i = threadIdx.x; i < N; i += blockDim.x) tw[MIX ? pad16(i) : i] = twg[i];
       __syncthreads();
       cur = b;
@@ -1256,26 +1454,72 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
     const int count = a.bin_count[b];
     const int *bl = a.bin_list + (size_t)b * a.cap;
     const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, b) * 4;
+    int *fl = nullptr;
+    if (inplace) {
+      if (threadIdx.x < 32) s_flag[threadIdx.x] = 0;
+      __syncthreads();
+      fl = s_flag;
+    }
     switch (b) {
-      case 0: spec_unit<32, MIX, 32, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 1: spec_unit<64, MIX, 16, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 2: spec_unit<128, MIX, 8, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 3: spec_unit<256, MIX, 4, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 4: spec_unit<512, MIX, 2, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
-      default: spec_unit<1024, MIX, 1, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 0: spec_unit<32, MIX, 32, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
+      case 1: spec_unit<64, MIX, 16, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
+      case 2: spec_unit<128, MIX, 8, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
+      case 3: spec_unit<256, MIX, 4, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
+      case 4: spec_unit<512, MIX, 2, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
+      default: spec_unit<1024, MIX, 1, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
+    }
+    if constexpr (MIX) {
+      if (inplace) {
+        __syncthreads();
+        for (int g = 0; g < gpc; g++) {
+          if (!s_flag[g]) continue;  // the same in every thread
+          const int slot = base + g;
+          const int item = bl[slot];
+          const ItemMix &c = a.itemsmix[item];
+          const HpTab t{a.NFFT, a.w32, a.w32lo, a.g32, a.g32lo};
+          df sums[3];
+          hp_item_sums(series + (size_t)slot * 4 * N, N, c.seg, c.imin, df{c.amp_p2, 0.f}, true,
+                       reinterpret_cast<const float4 *>(A.tw[b]), t, reinterpret_cast<dc *>(smem_raw),
+                       reinterpret_cast<float2 *>(reds), sums);
+          if (threadIdx.x == 0) {
+            hp_write(item, N, c.seg, c.imin, a.NFFT, sums, a.Q, a.QA, PERCH, a.term_x, a.dlogl, a.term_y, a.hh,
+                     a.term_ch, a.status);
+            const float est = a.hp_e1 * sqrtf(sums[2].hi * (sums[0].hi + sums[1].hi)) *
+                              fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
+            if (!(est <= 1.f)) {
+              a.fb2_list[atomicAdd(a.fb2_count, 1)] = item;
+              atomicAdd(a.fb_total + 1, 1ull);
+            }
+          }
+          __syncthreads();
+          cur = -1;  // the twiddles' shared memory was used
+        }
+      }
+    }
+    if (inplace) {
+      if (threadIdx.x == 0) s_next = (int)gridDim.x + atomicAdd(&A.sched[0], 1);
+      __syncthreads();
+      unit = s_next;
+      __syncthreads();
+    } else {
+      unit += gridDim.x;
     }
   }
-  if (A.zero_counts) {
-    // leave the counts at zero for the next launch sequence: every CTA has
-    // read them for the last time once it gets here
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      if (atomicAdd(&A.zero_counts[kNumBins], 1) == (int)gridDim.x - 1) {
+  // the last CTA to finish resets the scheduling counters and, when asked,
+  // leaves the size counts at zero for the next launch sequence: every CTA
+  // has read them for the last time once it gets here
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&A.sched[1], 1) == (int)gridDim.x - 1) {
+      A.sched[0] = 0;
+      A.sched[1] = 0;
+      if (A.zero_counts) {
 #pragma unroll
-        for (int b = 0; b <= kNumBins; b++) A.zero_counts[b] = 0;
-        __threadfence();
+        for (int b = 0; b <= kNumBins + A.zero_extra; b++) A.zero_counts[b] = 0;
       }
+      __threadfence();
+      if (A.has_cond) cudaGraphSetConditional(A.cond, *(volatile const int *)A.cond_count > 0 ? 1u : 0u);
     }
   }
 }
@@ -1283,15 +1527,15 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
 template <bool MIX, bool PERCH = false>
 static cudaError_t launch_spec_all(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
   const size_t smem = SpecAllSmem<MIX>::bytes;
-  static int occ = -1;
-  if (occ < 0) {
-    cudaError_t e = cudaFuncSetAttribute(fd_spec_all_kernel<MIX, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  static LaunchSetup setup;
+  int occ = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    cudaError_t r = cudaFuncSetAttribute(fd_spec_all_kernel<MIX, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_all_kernel<MIX, PERCH>, kSpecAllThreads, smem);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-  }
+    if (r != cudaSuccess) return r;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_spec_all_kernel<MIX, PERCH>, kSpecAllThreads, smem);
+  }, &occ);
+  if (e != cudaSuccess) return e;
   fd_spec_all_kernel<MIX, PERCH><<<occ * num_sms, kSpecAllThreads, smem, stream>>>(A);
   return cudaGetLastError();
 }
@@ -1302,15 +1546,15 @@ template <int N, bool MIX, bool PERCH = false>
 static cudaError_t launch_spec(const SpecArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
   using Cfg = SpecCfg<N>;
   size_t smem = SpecSmem<N, MIX>::bytes;
-  static int occ = -1;
-  if (occ < 0) {
-    cudaError_t e = cudaFuncSetAttribute(fd_spec_kernel<N, MIX, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  static LaunchSetup setup;
+  int occ = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    cudaError_t r = cudaFuncSetAttribute(fd_spec_kernel<N, MIX, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_spec_kernel<N, MIX, PERCH>, Cfg::CTA, smem);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-  }
+    if (r != cudaSuccess) return r;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_spec_kernel<N, MIX, PERCH>, Cfg::CTA, smem);
+  }, &occ);
+  if (e != cudaSuccess) return e;
   int need = (nitems_bound + Cfg::GPC - 1) / Cfg::GPC;
   int grid = occ * num_sms;
   if (need < grid) grid = need;
@@ -1321,13 +1565,23 @@ static cudaError_t launch_spec(const SpecArgs &a, int nitems_bound, int num_sms,
 
 template <bool MIX>
 static cudaError_t launch_slow(const SlowArgs &a, int num_sms, cudaStream_t stream) {
-  static int occ = -1;
-  if (occ < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_slow_kernel<MIX>, 256, 0);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-  }
+  static LaunchSetup setup;
+  int occ = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_slow_kernel<MIX>, 256, 0);
+  }, &occ);
+  if (e != cudaSuccess) return e;
   fd_slow_kernel<MIX><<<occ * num_sms, 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// The slow part of a few proposals (the FP64 re-evaluation of flagged mixed
+// ones): one warp per CTA, so that the chunks of 32 samples spread over the
+// SMs instead of filling the first few (an FP64 sample costs ~700 FP64
+// instructions and the FP64 pipe of an SM issues a warp's in 16 cycles).
+template <bool MIX>
+static cudaError_t launch_slow_wide(const SlowArgs &a, int num_sms, cudaStream_t stream) {
+  fd_slow_kernel<MIX, 32><<<4 * num_sms, 32, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -7,6 +7,10 @@ cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t str
   return launch_slow<false>(a, num_sms, stream);
 }
 
+cudaError_t fd_launch_slow_fp64_wide(const SlowArgs &a, int num_sms, cudaStream_t stream) {
+  return launch_slow_wide<false>(a, num_sms, stream);
+}
+
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream,
                                 bool perch) {
   if (perch) {

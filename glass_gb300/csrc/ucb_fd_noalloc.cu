@@ -27,6 +27,8 @@ namespace glass {
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_plan64(const PlanArgs &a, cudaStream_t stream);
+int report_error(int code, const char *msg);
+int report_cuda_error(cudaError_t e, const char *where);
 
 namespace {
 
@@ -132,18 +134,24 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
                                             const double *invCA, const double *invCE, int nitems,
                                             const int *item_seg, const double *params, const double *term_x,
                                             double *dlogl, double *term_y, double *hh, int *status) {
-  if (nitems < 0 || nseg < 1 || NFFT < kMinN || !(T > 0)) return GLASS_ERR_ARG;
-  if (format < 0 || format > 2) return GLASS_ERR_FORMAT;
+  if (nitems < 0 || nseg < 1 || NFFT < kMinN || !(T > 0))
+    return report_error(GLASS_ERR_ARG, "dlogl_fp64_noalloc: negative item count, no segment, NFFT below 32 or T <= 0");
+  if (format < 0 || format > 2) return report_error(GLASS_ERR_FORMAT, "dlogl_fp64_noalloc: unknown format");
   if (nitems == 0) return GLASS_OK;
-  if (!qmin || !rA || !rE || !invCA || !invCE || !item_seg || !params || !dlogl) return GLASS_ERR_ARG;
-  if (nitems > kNaMaxItems || (long long)nseg * NFFT > kNaMaxBins ||
-      (long long)nitems * (NFFT < kMaxN ? NFFT : kMaxN) > kNaMaxSamples)
-    return GLASS_ERR_SIZE;
+  if (!qmin || !rA || !rE || !invCA || !invCE || !item_seg || !params || !dlogl)
+    return report_error(GLASS_ERR_ARG, "dlogl_fp64_noalloc: null argument");
+  if (nitems > kNaMaxItems)
+    return report_error(GLASS_ERR_SIZE, "dlogl_fp64_noalloc: more than GLASS_NOALLOC_MAX_ITEMS proposals");
+  if ((long long)nseg * NFFT > kNaMaxBins)
+    return report_error(GLASS_ERR_SIZE, "dlogl_fp64_noalloc: nseg * NFFT above GLASS_NOALLOC_MAX_BINS");
+  if ((long long)nitems * (NFFT < kMaxN ? NFFT : kMaxN) > kNaMaxSamples)
+    return report_error(GLASS_ERR_SIZE, "dlogl_fp64_noalloc: nitems * min(NFFT, 4096) above GLASS_NOALLOC_MAX_SAMPLES");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return GLASS_ERR_CUDA;
+  if (e != cudaSuccess) return report_cuda_error(e, "dlogl_fp64_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kNaMaxDevices) return report_error(GLASS_ERR_CUDA, "dlogl_fp64_noalloc: device index above 63");
   NaAddrs *na = nullptr;
-  if (na_setup(dev, na) != cudaSuccess) return GLASS_ERR_CUDA;
+  if ((e = na_setup(dev, na)) != cudaSuccess) return report_cuda_error(e, "dlogl_fp64_noalloc: array addresses");
   cudaStream_t s = (cudaStream_t)stream;
   const double fstar = kCLIGHT / (2.0 * kPI * kLARM);
 
@@ -161,8 +169,11 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
     tab.tw32[b] = na->tw32 + off;
     off += (size_t)32 << b;
   }
-  if (fd_build_orbit_tables(tab, T, t0, s) != cudaSuccess) return GLASS_ERR_CUDA;
-  if (cudaMemsetAsync(na->bin_count, 0, sizeof(int) * kNumBins, s) != cudaSuccess) return GLASS_ERR_CUDA;
+  if ((e = cudaGetLastError()) != cudaSuccess) return report_cuda_error(e, "dlogl_fp64_noalloc: bank tables");
+  if ((e = fd_build_orbit_tables(tab, T, t0, s)) != cudaSuccess)
+    return report_cuda_error(e, "dlogl_fp64_noalloc: orbit tables");
+  if ((e = cudaMemsetAsync(na->bin_count, 0, sizeof(int) * kNumBins, s)) != cudaSuccess)
+    return report_cuda_error(e, "dlogl_fp64_noalloc: count reset");
 
   // plan, slow part, per-size spectral kernels (the FP64 path's own kernels)
   PlanArgs pa;
@@ -187,7 +198,7 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
   pa.term_y = term_y;
   pa.hh = hh;
   pa.status = status;
-  if (fd_launch_plan64(pa, s) != cudaSuccess) return GLASS_ERR_CUDA;
+  if ((e = fd_launch_plan64(pa, s)) != cudaSuccess) return report_cuda_error(e, "dlogl_fp64_noalloc: plan");
 
   SlowArgs sa;
   sa.cap = kNaMaxItems;
@@ -207,7 +218,8 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
     sa.mix[b] = tab.mix[b];
   }
   sa.series = na->series;
-  if (fd_launch_slow_fp64(sa, na->num_sms, s) != cudaSuccess) return GLASS_ERR_CUDA;
+  if ((e = fd_launch_slow_fp64(sa, na->num_sms, s)) != cudaSuccess)
+    return report_cuda_error(e, "dlogl_fp64_noalloc: slow part");
 
   SpecArgs a;
   a.NFFT = NFFT;
@@ -233,7 +245,8 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
     a.bin = b;
     a.bin_list = na->bin_list + (size_t)b * kNaMaxItems;
     a.tw = tab.tw64[b];
-    if (fd_launch_spec_fp64(N, a, nitems, na->num_sms, s, false) != cudaSuccess) return GLASS_ERR_CUDA;
+    if ((e = fd_launch_spec_fp64(N, a, nitems, na->num_sms, s, false)) != cudaSuccess)
+      return report_cuda_error(e, "dlogl_fp64_noalloc: spectral kernels");
   }
   return GLASS_OK;
 }

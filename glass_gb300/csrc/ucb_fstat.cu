@@ -501,15 +501,14 @@ __global__ void __launch_bounds__(FsCfg<N>::CTA) fs_spec_kernel(FsSpecArgs a) {
 template <int N>
 cudaError_t fs_launch_spec(const FsSpecArgs &a, int ncells, int num_sms, cudaStream_t stream) {
   using Cfg = FsCfg<N>;
-  static int occ = -1;
-  if (occ < 0) {
-    cudaError_t e =
-        cudaFuncSetAttribute(fs_spec_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::smem);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs_spec_kernel<N>, Cfg::CTA, Cfg::smem);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-  }
+  static LaunchSetup setup;
+  int occ = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    cudaError_t r = cudaFuncSetAttribute(fs_spec_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg::smem);
+    if (r != cudaSuccess) return r;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fs_spec_kernel<N>, Cfg::CTA, Cfg::smem);
+  }, &occ);
+  if (e != cudaSuccess) return e;
   int need = (ncells + Cfg::GPC - 1) / Cfg::GPC;
   int grid = occ * num_sms;
   if (need < grid) grid = need;
@@ -678,12 +677,12 @@ cudaError_t fs_launch(const FdBankDev &bank, const FdTablesDev &tab, const doubl
     for (int b = 0; b < kNumBins; b++) sa.pos64[b] = tab.pos64[b];
     sa.series = (double2 *)w.series;
     {
-      static int occ = -1;
-      if (occ < 0) {
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fs_slow_kernel, 256, 0)) != cudaSuccess)
-          return e;
-        if (occ < 1) occ = 1;
-      }
+      static LaunchSetup setup;
+      int occ = 0;
+      if ((e = launch_setup(setup, [&](int *o) {
+             return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fs_slow_kernel, 256, 0);
+           }, &occ)) != cudaSuccess)
+        return e;
       fs_slow_kernel<<<occ * num_sms, 256, 0, stream>>>(sa);
       launches++;
       if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -153,7 +153,7 @@ __device__ __forceinline__ void grad_sample(const GradConsts &K, const ItemGrad 
     dz[i] = f[3 * i + 2];
   }
   // carrier phase (double-float) common to the three spacecraft
-  const float psi0 = carrier_phase_mix(c, o);
+  const float psi0 = carrier_phase_mix(c, o).hi;
   const float uf = o.u_hi;
   const float tgc = K.AUcf * (c.k[0] * ca + c.k[1] * sa);
   const float gx = K.AUf * ca, gy = K.AUf * sa;  // guiding centre (m)
@@ -455,14 +455,14 @@ template <int N>
 static cudaError_t launch_gradspec(const GradSpecArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
   using Cfg = GradCfg<N>;
   size_t smem = Cfg::bytes;
-  static int occ = -1;
-  if (occ < 0) {
-    cudaError_t e = cudaFuncSetAttribute(fd_gradspec_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fd_gradspec_kernel<N>, Cfg::CTA, smem);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) occ = 1;
-  }
+  static LaunchSetup setup;
+  int occ = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    cudaError_t r = cudaFuncSetAttribute(fd_gradspec_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (r != cudaSuccess) return r;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_gradspec_kernel<N>, Cfg::CTA, smem);
+  }, &occ);
+  if (e != cudaSuccess) return e;
   int need = (nitems_bound + Cfg::GPC - 1) / Cfg::GPC;
   int grid = occ * num_sms;
   if (need < grid) grid = need;

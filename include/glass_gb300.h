@@ -354,27 +354,61 @@ int glass_gpu_fisher_draw(glass_gpu_ctx *ctx, int n, const double *params_x, con
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 
 /* Per-phase timing of glass_gpu_dlogl_batch (profiling aid; off by default).
- * With enable != 0 every later call records four timing events on the
+ * With enable != 0 every later call records five timing events on the
  * context's stream: before the plan kernel, after it, after the slow-part
- * kernel, and after the spectral (FFT + likelihood) kernels.
- * glass_gpu_last_phase_ms waits for the last call's events and writes the
- * three durations in milliseconds to ms[0..2] (plan, slow part, spectral);
- * GLASS_ERR_STATE when no call was made with timing on.  Events recorded
- * while the stream is being captured into a CUDA graph become graph nodes:
- * read the durations after launches made outside capture. */
+ * kernel, after the spectral (FFT + likelihood) kernels and after the
+ * re-evaluations that follow them (see glass_gpu_set_mixed_tolerance; empty
+ * in FP64 or with the tolerance off).  glass_gpu_last_phase_ms waits for the
+ * last call's events and writes the four durations in milliseconds to
+ * ms[0..3] (plan, slow part, spectral, re-evaluation); GLASS_ERR_STATE when no
+ * call was made with timing on.  Events recorded while the stream is being
+ * captured into a CUDA graph become graph nodes: read the durations after
+ * launches made outside capture. */
 int glass_gpu_set_phase_timing(glass_gpu_ctx *ctx, int enable);
 int glass_gpu_last_phase_ms(glass_gpu_ctx *ctx, float *ms);
+
+/*
+ * Accuracy of GLASS_PREC_MIXED.  No counterpart in the reference, which is
+ * FP64 throughout.  An FP32 FFT leaves a relative error of up to ~1e-7 on the
+ * few bins that hold a narrowband template's power, so delta logL carries an
+ * error up to ~1e-7 sqrt(H R), H = (h|h)/2 and R = |r - h|^2 the whitened
+ * powers over the template support: below 1e-3 except for loud templates
+ * (near the data of an SNR ~ 300 source, or far from the data with a power of
+ * 1e6, as a jump of a weak source's amplitude by e^6 gives).  The spectral
+ * kernel estimates each proposal's error from the sums it already has and,
+ * for those above `tol`, evaluates the spectral stage again in double-float
+ * arithmetic (in the same kernel, for sizes up to 1024); proposals still
+ * above `tol` get FP64 series transformed the same way.  Results are written
+ * over the mixed ones, in the same launch sequence (and CUDA graph).
+ * tol <= 0 turns the re-evaluation off (pure mixed precision); the default is
+ * 1e-3.  Changing it drops the context's recorded host-path graphs.
+ */
+int glass_gpu_set_mixed_tolerance(glass_gpu_ctx *ctx, double tol);
+/* Per-proposal tolerance: proposal i < n of every later batch uses
+ * tol * scale[i] (HOST array, copied; scales finite and positive; n = 0
+ * restores tol for all).  A parallel-tempering sampler passes its ladder
+ * (scale[i] = the temperature of batch slot i): the error of the Hastings
+ * ratio's likelihood part, delta logL / T, is then at most tol for every
+ * proposal, and only the cold chains' proposals need delta logL itself to
+ * tol.  Synchronises the context's stream. */
+int glass_gpu_set_mixed_tolerance_scale(glass_gpu_ctx *ctx, int n, const double *scale);
+/* Numbers of proposals re-evaluated since the context's work buffers were
+ * allocated: count[0] in double-float from their mixed series, count[1] (a
+ * subset of those) from FP64 series.  Synchronises the context's stream. */
+int glass_gpu_mixed_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count);
 
 /* ------------------------------------------- batch that allocates nothing */
 /*
  * No counterpart in the reference.  For callers that cannot allocate GPU
  * memory once they are running -- a host that allocates everything at start-up
  * and forbids it later, code running inside someone else's memory pool, or code
- * that may not call the CUDA allocator at all -- this evaluates a batch exactly
- * as glass_gpu_dlogl_batch does with GLASS_PREC_FP64, on the caller's stream,
- * without calling cudaMalloc or any other allocating routine and without a
- * context.  All pointers are device pointers the caller owns; the segment
- * inputs have the layout of glass_gpu_bank_upload.
+ * that may not call the CUDA allocator at all -- this evaluates a batch with
+ * the kernels glass_gpu_dlogl_batch runs for GLASS_PREC_FP64, on the caller's
+ * stream, without calling cudaMalloc or any other allocating routine and
+ * without a context.  The segment tables are built on the device here (on the
+ * host there), so the two agree to about 1e-13 relative, not bit for bit.
+ * All pointers are device pointers the caller owns; the segment inputs have
+ * the layout of glass_gpu_bank_upload.
  *
  * Intermediate data live in fixed arrays compiled into the library (about
  * 41 MB of device memory, held by every GPU that loads the library until the

@@ -239,8 +239,9 @@ def test_t0_and_residual_update(engine, port):
 
 
 def test_phase_timing(engine, port):
-    """Per-phase durations of a step: refused before any timed step, three
-    positive durations after one, and the results unchanged by the events."""
+    """Per-phase durations of a step: refused before any timed step, four
+    durations after one (plan, slow part and spectral positive; the
+    re-evaluation non-negative), and the results unchanged by the events."""
     rng = np.random.default_rng(31)
     bank, inj = _random_bank(rng, 8, 1024, port)
     engine.upload(bank)
@@ -255,7 +256,7 @@ def test_phase_timing(engine, port):
         ms = engine.last_phase_ms()
     finally:
         engine.set_phase_timing(False)
-    assert len(ms) == 3 and all(v > 0 for v in ms)
+    assert len(ms) == 4 and all(v > 0 for v in ms[:3]) and ms[3] >= 0
     for a, b in zip(got, ref):
         np.testing.assert_array_equal(a, b)
 

@@ -91,4 +91,5 @@ def test_noalloc_batch_matches_the_allocating_entry_point(port):
                                            ptr(d_rA), ptr(d_rE), ptr(d_iA), ptr(d_iE), gg.lib_constants()["GLASS_NOALLOC_MAX_ITEMS"] + 1,
                                            ptr(d_seg), ptr(d_p), None, ptr(d_dl), None, None, None)
     assert big == -2
+    assert b"GLASS_NOALLOC_MAX_ITEMS" in lib.glass_gpu_last_error()  # the refusal says why
     eng.close()
