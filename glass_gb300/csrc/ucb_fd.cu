@@ -473,6 +473,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   if (!work.counts_zero) {
     e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 6), stream);
     if (e != cudaSuccess) return e;
+    if (work.hp_arrive && (e = cudaMemsetAsync(work.hp_arrive, 0, sizeof(int) * (size_t)work.cap, stream)) != cudaSuccess)
+      return e;
   }
   const bool fallback = mix && (work.fb_e1 > 0.f || work.fb_e2 > 0.f);
   work.counts_zero = false;  // until this sequence has been enqueued in full
@@ -565,9 +567,6 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     a.fb_total = work.fb_total;
     a.fb_e1 = work.fb_e1;
     a.fb_e2 = work.fb_e2;
-    a.fb2_count = work.fb2_count;
-    a.fb2_list = work.fb2_list;
-    a.hp_e1 = work.hp_e1;
     a.fb_inv_scale = work.fb_inv_scale;
     a.fb_nscale = work.fb_nscale;
   }
@@ -587,7 +586,6 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
       cond = true;
     (void)cudaGetLastError();
   }
-  const bool big = bank.NFFT > 1024;  // sizes 2048, 4096 in their own kernels
   // sizes up to 1024 (every size a segment of NFFT bins can produce, up to
   // NFFT: ucb_bandwidth caps N there) in one launch on the main stream; 2048
   // and 4096 as their own kernels on side streams running beside it
@@ -620,10 +618,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.a.tw = nullptr;
     A.nbins = nall;
     A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
-    A.sched = work.bin_count + kNumBins + 4;
-    A.has_cond = cond && !big;
-    A.cond = cond_h;
-    A.cond_count = work.fb2_count;
+    A.done = work.bin_count + kNumBins;
     for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
     e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch) : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
     launches++;
@@ -636,13 +631,12 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   }
   if (timing && (e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
 
-  // Re-evaluation of flagged mixed proposals.  Sizes up to 1024 were
-  // re-evaluated in double-float by the persistent spectral kernel itself;
-  // the listed ones of sizes 2048 and 4096 get the same from the standalone
-  // kernel.  Proposals still above the tolerance get FP64 series (FP64
-  // constants, FP64 slow part) that the standalone kernel transforms in
-  // double-float.  Results are written over the mixed ones; counts and lists
-  // live on the device, and each kernel leaves its counters at zero.
+  // Re-evaluation of flagged mixed proposals: the listed ones get a
+  // double-float spectral stage on their FP32 series; proposals still above
+  // the tolerance get FP64 series (FP64 constants, FP64 slow part) that the
+  // same kernel transforms in double-float.  Results are written over the
+  // mixed ones; counts and lists live on the device, and each kernel leaves
+  // its counters at zero.
   if (fallback) {
     int nmax = kMaxN;
     while (nmax > bank.NFFT) nmax >>= 1;
@@ -677,13 +671,13 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     h.next_e1 = work.hp_e1;
     h.inv_scale = work.fb_inv_scale;
     h.nscale = work.fb_nscale;
-    if (big) {
-      h.has_cond = cond;
-      h.cond = cond_h;
-      e = fd_launch_hp(h, false, perch, num_sms, stream);
-      launches++;
-      if (e != cudaSuccess) return e;
-    }
+    h.part = work.hp_part;
+    h.arrive = work.hp_arrive;
+    h.has_cond = cond;
+    h.cond = cond_h;
+    e = fd_launch_hp(h, false, perch, num_sms, stream);
+    launches++;
+    if (e != cudaSuccess) return e;
     // the FP64-series tier, behind the conditional node when capturing
     cudaStream_t ts = stream;
     cudaGraphNode_t cnode = nullptr;

@@ -47,22 +47,22 @@ struct FdWorkDev {
   ItemF64 *items64 = nullptr;   // [cap]
   ItemMix *itemsmix = nullptr;  // [cap]
   ItemGrad *itemsgrad = nullptr;  // [cap]
-  // [kNumBins + 6]: per-size counts, a done counter (unused by the persistent
-  // spectral kernel), fb_count, fb2_count, the re-evaluation kernel's
-  // CTA-done counter, and the persistent spectral kernel's next-unit and
-  // CTA-done counters
+  // [kNumBins + 6]: per-size counts, the persistent spectral kernel's
+  // CTA-done counter, fb_count, fb2_count, the re-evaluation kernel's
+  // CTA-done counter and two spare ints
   int *bin_count = nullptr;
   int *bin_list = nullptr;      // [kNumBins*cap]
   // Mixed precision: proposals whose error estimate exceeds the tolerance are
-  // re-evaluated with the spectral stage in double-float (in place by the
-  // persistent spectral kernel; sizes 2048 and 4096 listed in fb_list with
-  // their series offsets for the standalone kernel); those still above it
-  // (fb2_list) get FP64 series that the standalone kernel transforms, all in
-  // the same launch sequence (fb_e1 = fb_e2 = 0: no re-evaluation)
+  // listed in fb_list with their series offsets and re-evaluated with the
+  // spectral stage in double-float; those still above it (fb2_list) get FP64
+  // series that the same kernel transforms, all in the same launch sequence
+  // (fb_e1 = fb_e2 = 0: no re-evaluation)
   float fb_e1 = 0.f, fb_e2 = 0.f, hp_e1 = 0.f;
   int *fb_list = nullptr;                  // [cap]
   long long *fb_off = nullptr;             // [cap]
   int *fb2_list = nullptr;                 // [cap]
+  float4 *hp_part = nullptr;               // [2 cap]: per-channel sums of the re-evaluation
+  int *hp_arrive = nullptr;                // [cap]: channels done per entry (zero between launches)
   int *fb_count = nullptr;                 // bin_count + kNumBins + 1
   int *fb2_count = nullptr;                // bin_count + kNumBins + 2
   unsigned long long *fb_total = nullptr;  // [2]: re-evaluated in double-float, from FP64 series

@@ -945,18 +945,13 @@ struct SpecArgs {
   // mixed precision: a proposal whose error estimate
   //   (fb_e1 sqrt(hw rr) + fb_e2 (hw + rr)) / scale_i
   // (hw = |h|^2, rr = |r - h|^2, whitened sums over the template support)
-  // exceeds 1 is re-evaluated in double-float: in place by the persistent
-  // kernel, or listed in fb_list (count in *fb_count, series offsets in
-  // fb_off) by the per-size kernels; fb_total[0] counts them.  No list: no
-  // estimate.
+  // exceeds 1 is listed in fb_list (count in *fb_count, series offsets in
+  // fb_off) for the double-float re-evaluation; fb_total[0] counts them.  No
+  // list: no estimate.
   int *fb_count = nullptr, *fb_list = nullptr;
   long long *fb_off = nullptr;
-  unsigned long long *fb_total = nullptr;  // [2]: re-evaluated in double-float, from FP64 series
+  unsigned long long *fb_total = nullptr;
   float fb_e1 = 0.f, fb_e2 = 0.f;
-  // proposals still above the tolerance after the double-float re-evaluation
-  // (estimate hp_e1 sqrt(hw rr) / scale_i) go to fb2_list for FP64 series
-  int *fb2_count = nullptr, *fb2_list = nullptr;
-  float hp_e1 = 0.f;
   // per-proposal tolerance scale: 1/scale_i for i < fb_nscale (null: 1)
   const float *fb_inv_scale = nullptr;
   int fb_nscale = 0;
@@ -996,6 +991,10 @@ struct HpArgs {
   const double *term_x;
   double *dlogl, *term_y, *hh, *term_ch;
   int *status;
+  // per entry: each channel's sums {rr hi, rr lo, hw hi, hw lo} and the
+  // count of channels done (zero between launches)
+  float4 *part = nullptr;
+  int *arrive = nullptr;
   // next tier (list mode): items whose estimate e1 sqrt(hw rr) / scale_i exceeds 1
   int *next_count = nullptr, *next_list = nullptr;
   unsigned long long *next_total = nullptr;
@@ -1005,7 +1004,6 @@ struct HpArgs {
   const float *inv_scale = nullptr;
   int nscale = 0;
 };
-size_t fd_hp_smem_bytes(int nmax);
 cudaError_t fd_launch_hp(const HpArgs &a, bool bin_mode, bool perch, int num_sms, cudaStream_t stream);
 
 // Start (in samples) of size bin `bin` in the scratch series: sizes are laid
@@ -1178,14 +1176,11 @@ namespace glass {
 // (from the slow kernel's scratch) are FFT'd in shared memory, weighted per bin
 // by the segment's TDI/whitening table and reduced to the residual power.
 // reds: 96 doubles of reduction scratch per group.
-// flags (shared memory, one per group; null: list the flagged proposals in
-// fb_list instead): set for a mixed proposal whose error estimate exceeds
-// the tolerance, which the caller then re-evaluates in place.
 template <int N, bool MIX, int GPC, bool PERCH = false>
 __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list, int count, int base,
                                           const typename SpecSmem<N, MIX>::C *series,
                                           const typename SpecSmem<N, MIX>::TW *tw,
-                                          typename SpecSmem<N, MIX>::C *bufs, double *reds, int *flags = nullptr) {
+                                          typename SpecSmem<N, MIX>::C *bufs, double *reds) {
   using S = SpecSmem<N, MIX>;
   using C = typename S::C;
   constexpr int GT = N / 4, NSER = S::NSER, PASSES = S::PASSES;
@@ -1319,13 +1314,9 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
                           fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
         if (!(est <= 1.f)) {  // also a non-finite estimate
           atomicAdd(a.fb_total, 1ull);
-          if (flags) {
-            flags[g] = 1;
-          } else {
-            const int q = atomicAdd(a.fb_count, 1);
-            a.fb_list[q] = item;
-            a.fb_off[q] = (long long)(src - reinterpret_cast<const C *>(a.series));
-          }
+          const int q = atomicAdd(a.fb_count, 1);
+          a.fb_list[q] = item;
+          a.fb_off[q] = (long long)(src - reinterpret_cast<const C *>(a.series));
         }
       }
     } else {
@@ -1389,20 +1380,8 @@ struct SpecAllArgs {
   SpecArgs a;                    // a.bin_list: all sizes' lists, stride cap; a.tw unused
   const void *tw[kSpecAllBins];  // twiddles per size
   int nbins;                     // sizes 32 << b for b < nbins
-  int *zero_counts;              // non-null: the last CTA to finish zeroes the kNumBins
-                                 // counts there, the done counter after them and
-                                 // zero_extra more ints after that
-  int zero_extra = 0;
-  // [2]: the next-unit counter (units after the first grid's worth are handed
-  // out dynamically when proposals are re-evaluated in place) and the
-  // CTA-done counter; the last CTA zeroes both
-  int *sched = nullptr;
-  // when the launch is being captured into a CUDA graph: the handle of the
-  // conditional node around the FP64-series re-evaluation, which the last CTA
-  // sets to (*cond_count > 0)
-  bool has_cond = false;
-  cudaGraphConditionalHandle cond = 0;
-  const int *cond_count = nullptr;
+  int *zero_counts;              // non-null: the last CTA to finish zeroes the kNumBins counts there
+  int *done = nullptr;           // CTA-done counter (zero between launches)
 };
 
 template <bool MIX, bool PERCH = false>
@@ -1415,12 +1394,6 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
   TW *tw = reinterpret_cast<TW *>(smem_raw);
   C *bufs = reinterpret_cast<C *>(tw + SN);
   double *reds = reinterpret_cast<double *>(bufs + 4 * SN);
-  __shared__ int s_flag[32], s_next;
-  // mixed precision with a tolerance: a flagged proposal is evaluated again
-  // by this CTA (double-float spectral stage, in the shared memory of the
-  // twiddles and series: 3 N double-float values <= 48 KB), while the other
-  // CTAs take the remaining units, which are then handed out dynamically
-  const bool inplace = MIX && a.fb_list != nullptr;
   int ustart[kSpecAllBins + 1];  // in largest-first order
   int total = 0;
 #pragma unroll
@@ -1434,8 +1407,7 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
   }
   ustart[kSpecAllBins] = total;
   int cur = -1;
-  int unit = blockIdx.x;
-  while (unit < total) {
+  for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
     int q = 0;
 #pragma unroll
     for (int qq = 1; qq < kSpecAllBins; qq++)
@@ -1454,72 +1426,27 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
     const int count = a.bin_count[b];
     const int *bl = a.bin_list + (size_t)b * a.cap;
     const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, b) * 4;
-    int *fl = nullptr;
-    if (inplace) {
-      if (threadIdx.x < 32) s_flag[threadIdx.x] = 0;
-      __syncthreads();
-      fl = s_flag;
-    }
     switch (b) {
-      case 0: spec_unit<32, MIX, 32, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
-      case 1: spec_unit<64, MIX, 16, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
-      case 2: spec_unit<128, MIX, 8, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
-      case 3: spec_unit<256, MIX, 4, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
-      case 4: spec_unit<512, MIX, 2, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
-      default: spec_unit<1024, MIX, 1, PERCH>(a, bl, count, base, series, tw, bufs, reds, fl); break;
-    }
-    if constexpr (MIX) {
-      if (inplace) {
-        __syncthreads();
-        for (int g = 0; g < gpc; g++) {
-          if (!s_flag[g]) continue;  // the same in every thread
-          const int slot = base + g;
-          const int item = bl[slot];
-          const ItemMix &c = a.itemsmix[item];
-          const HpTab t{a.NFFT, a.w32, a.w32lo, a.g32, a.g32lo};
-          df sums[3];
-          hp_item_sums(series + (size_t)slot * 4 * N, N, c.seg, c.imin, df{c.amp_p2, 0.f}, true,
-                       reinterpret_cast<const float4 *>(A.tw[b]), t, reinterpret_cast<dc *>(smem_raw),
-                       reinterpret_cast<float2 *>(reds), sums);
-          if (threadIdx.x == 0) {
-            hp_write(item, N, c.seg, c.imin, a.NFFT, sums, a.Q, a.QA, PERCH, a.term_x, a.dlogl, a.term_y, a.hh,
-                     a.term_ch, a.status);
-            const float est = a.hp_e1 * sqrtf(sums[2].hi * (sums[0].hi + sums[1].hi)) *
-                              fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
-            if (!(est <= 1.f)) {
-              a.fb2_list[atomicAdd(a.fb2_count, 1)] = item;
-              atomicAdd(a.fb_total + 1, 1ull);
-            }
-          }
-          __syncthreads();
-          cur = -1;  // the twiddles' shared memory was used
-        }
-      }
-    }
-    if (inplace) {
-      if (threadIdx.x == 0) s_next = (int)gridDim.x + atomicAdd(&A.sched[0], 1);
-      __syncthreads();
-      unit = s_next;
-      __syncthreads();
-    } else {
-      unit += gridDim.x;
+      case 0: spec_unit<32, MIX, 32, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 1: spec_unit<64, MIX, 16, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 2: spec_unit<128, MIX, 8, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 3: spec_unit<256, MIX, 4, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 4: spec_unit<512, MIX, 2, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      default: spec_unit<1024, MIX, 1, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
     }
   }
-  // the last CTA to finish resets the scheduling counters and, when asked,
-  // leaves the size counts at zero for the next launch sequence: every CTA
-  // has read them for the last time once it gets here
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(&A.sched[1], 1) == (int)gridDim.x - 1) {
-      A.sched[0] = 0;
-      A.sched[1] = 0;
-      if (A.zero_counts) {
-#pragma unroll
-        for (int b = 0; b <= kNumBins + A.zero_extra; b++) A.zero_counts[b] = 0;
-      }
+  // the last CTA to finish leaves the size counts at zero for the next
+  // launch sequence (every CTA has read them for the last time once it gets
+  // here) and resets its done counter
+  if (A.zero_counts) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
       __threadfence();
-      if (A.has_cond) cudaGraphSetConditional(A.cond, *(volatile const int *)A.cond_count > 0 ? 1u : 0u);
+      if (atomicAdd(A.done, 1) == (int)gridDim.x - 1) {
+#pragma unroll
+        for (int b = 0; b < kNumBins; b++) A.zero_counts[b] = 0;
+        *A.done = 0;
+      }
     }
   }
 }

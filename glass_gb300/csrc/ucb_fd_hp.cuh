@@ -1,7 +1,6 @@
-// Double-float (pairs of floats) complex arithmetic and the CTA-wide
-// re-evaluation of one proposal's spectral stage, shared by the persistent
-// mixed spectral kernel (which re-evaluates the proposals it flags in place)
-// and the standalone kernel of ucb_fd_hp.cu.
+// Double-float (pairs of floats) complex arithmetic, the CTA-wide Stockham
+// FFT and reduction, and the result write of the double-float re-evaluation
+// of mixed proposals (ucb_fd_hp.cu).
 #pragma once
 #include "glass_common.cuh"
 
@@ -87,78 +86,6 @@ static __device__ df hp_block_sum(df v, float2 *red) {
   if (threadIdx.x == 0)
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = df_add(t, df{red[w].x, red[w].y});
   return t;
-}
-
-// Segment tables of the re-evaluation, as hi + lo floats.
-struct HpTab {
-  int NFFT;
-  const float4 *w32, *w32lo, *g32, *g32lo;  // whitened residual {A, E}; {G2, G1} per channel
-};
-
-// Residual powers of one proposal, by every thread of the CTA (sums valid in
-// thread 0): the four arm-combination series at src (4 series of N, float2
-// from the mixed slow part or double2 from the FP64 one) through double-float
-// FFTs, the bins' TDI/whitening weights, the template scale (amp: an exact
-// power of two for mixed series, whose mantissa they carry, or amp/(2N)), and
-// the whitened residual: out[0], out[1] = sum |r - h|^2 of A, E; out[2] =
-// sum |h|^2.  buf: 3 N double-float complex values of shared memory; red: 32
-// float2; tw: the size's twiddles as hi + lo floats.  Not inlined: its
-// registers then do not count against the mixed spectral kernel's main path,
-// which calls it only for flagged proposals.
-template <typename SIN>
-__device__ __noinline__ void hp_item_sums(const SIN *src, int N, int seg, int imin, df amp, bool amp_pow2,
-                                          const float4 *tw, const HpTab &t, dc *buf, float2 *red, df out[3]) {
-  dc *B[3] = {buf, buf + N, buf + 2 * N};
-  const int NFFT = t.NFFT;
-  df rr[2] = {{0.f, 0.f}, {0.f, 0.f}}, hw = {0.f, 0.f};
-#pragma unroll 1
-  for (int ch = 0; ch < 2; ch++) {
-    // the channel's two series (A: a2, a1; E: e2, e1): the first in B[0]
-    // (ping-pong with B[1]), the second in the two buffers not holding the
-    // first one's spectrum
-    dc *res[2];
-#pragma unroll 1
-    for (int s = 0; s < 2; s++) {
-      dc *x = B[0], *y = B[1];
-      if (s == 1) {
-        x = res[0] == B[0] ? B[1] : B[0];
-        y = B[2];
-      }
-      const SIN *ser = src + (size_t)(2 * ch + s) * N;
-      for (int n = threadIdx.x; n < N; n += blockDim.x) {
-        const SIN v = ser[n];
-        if constexpr (sizeof(SIN) == sizeof(double2)) {
-          x[n] = {df_from_double(v.x), df_from_double(v.y)};
-        } else {
-          x[n] = {{v.x, 0.f}, {v.y, 0.f}};
-        }
-      }
-      __syncthreads();
-      res[s] = hp_fft(x, y, N, tw);
-    }
-    // per bin: h = amp (S2 G2 + S1 G1), r = w - h
-    for (int k = threadIdx.x; k < N; k += blockDim.x) {
-      const int m = (k + N / 2) & (N - 1);  // fftshift
-      const int j = imin + m;
-      if (j < 0 || j >= NFFT) continue;
-      const size_t sj = (size_t)seg * NFFT + j;
-      const float4 gh = t.g32[2 * sj + ch], gl = t.g32lo[2 * sj + ch];
-      const dc g2 = dc_from(make_float2(gh.x, gh.y), make_float2(gl.x, gl.y));
-      const dc g1 = dc_from(make_float2(gh.z, gh.w), make_float2(gl.z, gl.w));
-      dc h = dc_add(dc_mul(res[0][k], g2), dc_mul(res[1][k], g1));
-      h = amp_pow2 ? dc_scale2(h, amp.hi) : dc_scale(h, amp);
-      const float4 wh = t.w32[sj], wl = t.w32lo[sj];
-      const dc w = ch == 0 ? dc_from(make_float2(wh.x, wh.y), make_float2(wl.x, wl.y))
-                           : dc_from(make_float2(wh.z, wh.w), make_float2(wl.z, wl.w));
-      const dc r = dc_sub(w, h);
-      rr[ch] = df_add(rr[ch], df_sq_sum(r));
-      hw = df_add(hw, df_sq_sum(h));
-    }
-    __syncthreads();
-  }
-  out[0] = hp_block_sum(rr[0], red);
-  out[1] = hp_block_sum(rr[1], red);
-  out[2] = hp_block_sum(hw, red);
 }
 
 // Writes a re-evaluated proposal's results (thread 0), as the spectral
