@@ -473,8 +473,6 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   if (!work.counts_zero) {
     e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 6), stream);
     if (e != cudaSuccess) return e;
-    if (work.hp_arrive && (e = cudaMemsetAsync(work.hp_arrive, 0, sizeof(int) * (size_t)work.cap, stream)) != cudaSuccess)
-      return e;
   }
   const bool fallback = mix && (work.fb_e1 > 0.f || work.fb_e2 > 0.f);
   work.counts_zero = false;  // until this sequence has been enqueued in full
@@ -671,8 +669,6 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     h.next_e1 = work.hp_e1;
     h.inv_scale = work.fb_inv_scale;
     h.nscale = work.fb_nscale;
-    h.part = work.hp_part;
-    h.arrive = work.hp_arrive;
     h.has_cond = cond;
     h.cond = cond_h;
     e = fd_launch_hp(h, false, perch, num_sms, stream);

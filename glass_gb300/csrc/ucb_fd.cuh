@@ -61,8 +61,6 @@ struct FdWorkDev {
   int *fb_list = nullptr;                  // [cap]
   long long *fb_off = nullptr;             // [cap]
   int *fb2_list = nullptr;                 // [cap]
-  float4 *hp_part = nullptr;               // [2 cap]: per-channel sums of the re-evaluation
-  int *hp_arrive = nullptr;                // [cap]: channels done per entry (zero between launches)
   int *fb_count = nullptr;                 // bin_count + kNumBins + 1
   int *fb2_count = nullptr;                // bin_count + kNumBins + 2
   unsigned long long *fb_total = nullptr;  // [2]: re-evaluated in double-float, from FP64 series

@@ -991,10 +991,6 @@ struct HpArgs {
   const double *term_x;
   double *dlogl, *term_y, *hh, *term_ch;
   int *status;
-  // per entry: each channel's sums {rr hi, rr lo, hw hi, hw lo} and the
-  // count of channels done (zero between launches)
-  float4 *part = nullptr;
-  int *arrive = nullptr;
   // next tier (list mode): items whose estimate e1 sqrt(hw rr) / scale_i exceeds 1
   int *next_count = nullptr, *next_list = nullptr;
   unsigned long long *next_total = nullptr;

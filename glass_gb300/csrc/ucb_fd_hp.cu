@@ -8,24 +8,26 @@
 // far from the data with (h|h) ~ 1e6.  The mixed spectral kernels list those
 // proposals with their series offsets, and their spectral stage is evaluated
 // again in double-float arithmetic (pairs of floats, ~48 bits, on the FP32
-// pipe, which on GB300 runs 64 times the FP64 rate) by one wide kernel: one
-// CTA per (proposal, TDI channel) transforms the channel's two series in
-// shared memory (radix-4 Stockham, twiddles as hi + lo floats), forms per bin
-// the whitened template and residual from hi + lo tables and sums the
-// residual power and the template power; the second CTA of a proposal to
-// finish adds the other channel's sums and writes the results over the mixed
-// ones.  A proposal's latency is two FFTs by one CTA, and the re-evaluation
-// of a few hundred proposals takes about one wave.
+// pipe, which on GB300 runs 64 times the FP64 rate) by one wide kernel whose
+// thread-block clusters of 4 CTAs each take one proposal: CTA r transforms
+// series r in its shared memory (radix-4 Stockham, twiddles as hi + lo floats
+// in shared memory), then CTAs 2c and 2c + 1 form channel c's whitened
+// template per bin from their own spectrum and their partner's (read through
+// distributed shared memory), each over half of the bins, and sum the
+// residual power and the template power; CTA 0 gathers the four partial sums
+// and writes the results over the mixed ones.  A proposal's latency is one
+// FFT, and a few hundred proposals take about one wave.
 //   list mode reads the mixed series (the error left is their FP32 rounding,
-//     ~1e-8 of the same scale); proposals still above the tolerance are
+//     ~2e-8 of the same scale); proposals still above the tolerance are
 //     listed for FP64 series from the FP64 slow part,
 //   bin mode reads those FP64 series through the size counts.
+#include <cooperative_groups.h>
+
 #include "ucb_fd_device.cuh"
 
 namespace glass {
 
 constexpr int kHpThreads = 256;
-constexpr int kHpSmemTwMax = 2048;  // larger sizes read their twiddles through L1
 
 // The proposal of entry k: item index, size, segment, placement, series
 // offset (elements of the series scratch) and template scale.
@@ -100,50 +102,42 @@ __device__ __forceinline__ void hp_load(const HpArgs &a, long long off, int N, d
 
 template <bool BIN, bool PERCH>
 __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ float2 red[32];
-  __shared__ int s_last;
+  __shared__ float4 s_part;  // this CTA's {rr hi, rr lo, hw hi, hw lo}
   const int NM = a.nmax, NFFT = a.NFFT;
-  dc *xb = reinterpret_cast<dc *>(smem_raw), *yb = xb + NM, *hb = yb + NM;
-  float4 *tws = reinterpret_cast<float4 *>(hb + NM);
+  dc *xb = reinterpret_cast<dc *>(smem_raw), *yb = xb + NM;
+  float4 *tws = reinterpret_cast<float4 *>(yb + NM);
+  const int r = (int)cluster.block_rank(), ch = r >> 1;
+  const int ncl = (int)(gridDim.x >> 2);
   int cs[kNumBins + 1];
-  const int total = 2 * hp_entries<BIN>(a, cs);
+  const int total = hp_entries<BIN>(a, cs);
   int cur = -1;
-  for (int u = blockIdx.x; u < total; u += gridDim.x) {
-    const int k = u >> 1, ch = u & 1;
+  for (int k = (int)(blockIdx.x >> 2); k < total; k += ncl) {
     const HpEntry e = hp_entry<BIN>(a, k, cs);
     const int N = e.N;
-    const float4 *tw = a.tw32x[e.bin];
-    __syncthreads();  // the previous unit is done with the buffers
-    if (N <= kHpSmemTwMax) {
-      if (e.bin != cur)
-        for (int n = threadIdx.x; n < N; n += blockDim.x) tws[n] = tw[n];
+    if (e.bin != cur) {
+      const float4 *tw = a.tw32x[e.bin];
+      for (int n = threadIdx.x; n < N; n += blockDim.x) tws[n] = tw[n];
       cur = e.bin;
-      tw = tws;
     }
-    // series 2 ch: its spectrum times the channel's G2 weight, kept in hb
-    hp_load<BIN>(a, e.off + (long long)(2 * ch) * N, N, xb);
+    hp_load<BIN>(a, e.off + (long long)r * N, N, xb);
     __syncthreads();
-    const dc *S = hp_fft(xb, yb, N, tw);
-    for (int q = threadIdx.x; q < N; q += blockDim.x) {
-      const int j = e.imin + ((q + N / 2) & (N - 1));  // fftshift
-      if (j < 0 || j >= NFFT) continue;
-      const size_t sj = 2 * ((size_t)e.seg * NFFT + j) + ch;
-      const float4 gh = a.g32[sj], gl = a.g32lo[sj];
-      hb[q] = dc_mul(S[q], dc_from(make_float2(gh.x, gh.y), make_float2(gl.x, gl.y)));
-    }
-    __syncthreads();
-    // series 2 ch + 1 times G1, plus the above: the channel's whitened template
-    hp_load<BIN>(a, e.off + (long long)(2 * ch + 1) * N, N, xb);
-    __syncthreads();
-    S = hp_fft(xb, yb, N, tw);
+    dc *S = hp_fft(xb, yb, N, tws);
+    cluster.sync();  // every spectrum of the proposal is complete
+    const dc *Sp = cluster.map_shared_rank(S, (unsigned)(r ^ 1));
+    const dc *S0 = (r & 1) ? Sp : S, *S1 = (r & 1) ? S : Sp;  // the channel's series 2c, 2c + 1
     df rr = {0.f, 0.f}, hw = {0.f, 0.f};
-    for (int q = threadIdx.x; q < N; q += blockDim.x) {
-      const int j = e.imin + ((q + N / 2) & (N - 1));
+    const int half = N >> 1, q0 = (r & 1) * half;
+    for (int q = q0 + threadIdx.x; q < q0 + half; q += blockDim.x) {
+      const int j = e.imin + ((q + half) & (N - 1));  // fftshift
       if (j < 0 || j >= NFFT) continue;
       const size_t sj = (size_t)e.seg * NFFT + j;
       const float4 gh = a.g32[2 * sj + ch], gl = a.g32lo[2 * sj + ch];
-      dc h = dc_add(hb[q], dc_mul(S[q], dc_from(make_float2(gh.z, gh.w), make_float2(gl.z, gl.w))));
+      dc h = dc_add(dc_mul(S0[q], dc_from(make_float2(gh.x, gh.y), make_float2(gl.x, gl.y))),
+                    dc_mul(S1[q], dc_from(make_float2(gh.z, gh.w), make_float2(gl.z, gl.w))));
       h = e.pow2 ? dc_scale2(h, e.amp.hi) : dc_scale(h, e.amp);
       const float4 wh = a.w32[sj], wl = a.w32lo[sj];
       const dc w = ch == 0 ? dc_from(make_float2(wh.x, wh.y), make_float2(wl.x, wl.y))
@@ -153,23 +147,15 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
     }
     rr = hp_block_sum(rr, red);
     hw = hp_block_sum(hw, red);
-    // the channel's sums to the entry's slot; the second CTA to arrive adds
-    // both channels and writes the proposal's results
-    if (threadIdx.x == 0) {
-      a.part[2 * (size_t)k + ch] = make_float4(rr.hi, rr.lo, hw.hi, hw.lo);
-      __threadfence();
-      s_last = atomicAdd(a.arrive + k, 1) == 1;
-    }
-    __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-      __threadfence();
-      const float4 o = __ldcg(a.part + 2 * (size_t)k + (ch ^ 1));  // L2: written by the other CTA
-      const df ro = {o.x, o.y}, ho = {o.z, o.w};
-      df s[3];
-      s[ch] = rr;
-      s[ch ^ 1] = ro;
-      s[2] = df_add(hw, ho);
-      a.arrive[k] = 0;
+    if (threadIdx.x == 0) s_part = make_float4(rr.hi, rr.lo, hw.hi, hw.lo);
+    cluster.sync();  // partial sums are published; the partner is done with S
+    if (r == 0 && threadIdx.x == 0) {
+      df s[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      for (int q = 0; q < 4; q++) {
+        const float4 o = *cluster.map_shared_rank(&s_part, (unsigned)q);
+        s[q >> 1] = df_add(s[q >> 1], df{o.x, o.y});
+        s[2] = df_add(s[2], df{o.z, o.w});
+      }
       hp_write(e.item, N, e.seg, e.imin, NFFT, s, a.Q, a.QA, PERCH, a.term_x, a.dlogl, a.term_y, a.hh, a.term_ch,
                a.status);
       if (!BIN && a.next_list) {
@@ -181,10 +167,10 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
         }
       }
     }
+    cluster.sync();  // s_part is read before the next proposal overwrites it
   }
   // the last CTA leaves the counters it was given at zero and sets the
   // conditional node that follows (when captured)
-  __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     if (atomicAdd(a.done, 1) == (int)gridDim.x - 1) {
@@ -197,24 +183,36 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
   }
 }
 
-static size_t hp_smem_bytes(int nmax) {
-  return (size_t)nmax * 3 * sizeof(dc) + (size_t)(nmax < kHpSmemTwMax ? nmax : kHpSmemTwMax) * sizeof(float4);
-}
+static size_t hp_smem_bytes(int nmax) { return (size_t)nmax * (2 * sizeof(dc) + sizeof(float4)); }
 
 template <bool BIN, bool PERCH>
 static cudaError_t launch_hp(const HpArgs &a, int num_sms, cudaStream_t stream) {
   const size_t smem = hp_smem_bytes(a.nmax);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 4;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kHpThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   static LaunchSetup setup[kNumBins];
-  int occ = 0;
+  int ncl = 0;
   cudaError_t e = launch_setup(setup[fd_bin_of(a.nmax)], [&](int *o) {
     cudaError_t r = cudaFuncSetAttribute(fd_hp_kernel<BIN, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hp_smem_bytes(kMaxN));
     if (r != cudaSuccess) return r;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_hp_kernel<BIN, PERCH>, kHpThreads, smem);
-  }, &occ);
+    cudaLaunchConfig_t q = cfg;
+    q.gridDim = dim3(4 * num_sms);
+    return cudaOccupancyMaxActiveClusters(o, fd_hp_kernel<BIN, PERCH>, &q);
+  }, &ncl);
   if (e != cudaSuccess) return e;
-  fd_hp_kernel<BIN, PERCH><<<occ * num_sms, kHpThreads, smem, stream>>>(a);
-  return cudaGetLastError();
+  if (ncl < 1) ncl = 1;
+  cfg.gridDim = dim3(4 * ncl);
+  return cudaLaunchKernelEx(&cfg, fd_hp_kernel<BIN, PERCH>, a);
 }
 
 cudaError_t fd_launch_hp(const HpArgs &a, bool bin_mode, bool perch, int num_sms, cudaStream_t stream) {

@@ -32,7 +32,7 @@ __device__ __forceinline__ dc dc_scale(dc a, df s) { return {df_mul(a.re, s), df
 // writes y[(i - k) 4 + k + m p]) and a final radix-2 stage when log2 N is
 // odd.  tw[j] = exp(-2 pi i j / N) as hi + lo floats.  Returns the buffer
 // holding the result.
-static __device__ dc *hp_fft(dc *x, dc *y, int N, const float4 *tw) {
+__device__ __forceinline__ dc *hp_fft(dc *x, dc *y, int N, const float4 *tw) {
   int p = 1;
   for (; 4 * p <= N; p <<= 2) {
     const int step = N / (4 * p), q = N / 4;
