@@ -192,6 +192,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->work.bin_count);
   cudaFree(ctx->work.bin_list);
   cudaFree(ctx->work.series);
+  cudaFree(ctx->work.series2);
   cudaFree(ctx->work.fb_list);
   cudaFree(ctx->work.fb_off);
   cudaFree(ctx->work.fb2_list);
@@ -488,6 +489,7 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   cudaFree(w.bin_count);
   cudaFree(w.bin_list);
   cudaFree(w.series);
+  cudaFree(w.series2);
   cudaFree(w.fb_list);
   cudaFree(w.fb_off);
   cudaFree(w.fb2_list);
@@ -502,6 +504,7 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   w.bin_count = nullptr;
   w.bin_list = nullptr;
   w.series = nullptr;
+  w.series2 = nullptr;
   w.cap = 0;
   w.series_bytes = 0;
   int cap = nitems < 1024 ? 1024 : nitems;
@@ -513,8 +516,8 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   GLASS_CUDA(cudaMalloc(&w.itemsgrad, sizeof(ItemGrad) * (size_t)cap), "cudaMalloc(itemsgrad)");
   GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * (kNumBins + 6)), "cudaMalloc(bin_count)");
   GLASS_CUDA(cudaMemset(w.bin_count, 0, sizeof(int) * (kNumBins + 6)), "cudaMemset(bin_count)");
-  w.fb_count = w.bin_count + kNumBins + 1;
-  w.fb2_count = w.bin_count + kNumBins + 2;
+  w.fb_count = w.bin_count + kNumBins + 2;
+  w.fb2_count = w.bin_count + kNumBins;
   GLASS_CUDA(cudaMalloc(&w.fb_list, sizeof(int) * (size_t)cap), "cudaMalloc(fb_list)");
   GLASS_CUDA(cudaMalloc(&w.fb_off, sizeof(long long) * (size_t)cap), "cudaMalloc(fb_off)");
   GLASS_CUDA(cudaMalloc(&w.fb2_list, sizeof(int) * (size_t)cap), "cudaMalloc(fb2_list)");
@@ -526,6 +529,7 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   w.counts_zero = true;
   GLASS_CUDA(cudaMalloc(&w.bin_list, sizeof(int) * (size_t)kNumBins * cap), "cudaMalloc(bin_list)");
   GLASS_CUDA(cudaMalloc(&w.series, series), "cudaMalloc(series)");
+  GLASS_CUDA(cudaMalloc(&w.series2, series), "cudaMalloc(series2)");
   w.cap = cap;
   w.series_bytes = series;
   return GLASS_OK;

@@ -84,6 +84,11 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
 // plan's (the same bandwidth rule), so only the source geometry is evaluated
 // in FP64 here.  Grid-stride with warp-uniform trips, as plan_bin needs
 // whole warps.
+// Sets a CUDA-graph conditional node's value to (*count > 0).
+__global__ void fd_cond_kernel(const int *count, cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0) cudaGraphSetConditional(h, *(volatile const int *)count > 0 ? 1u : 0u);
+}
+
 __global__ void __launch_bounds__(64) fd_item64_list_kernel(PlanArgs a, const int *list, const int *count) {
   const int n = *count;
   const int stride = gridDim.x * blockDim.x;
@@ -474,7 +479,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 6), stream);
     if (e != cudaSuccess) return e;
   }
-  const bool fallback = mix && (work.fb_e1 > 0.f || work.fb_e2 > 0.f);
+  const bool fallback = mix && (work.fb_e1 > 0.f || work.fb_e2 > 0.f) && work.series2 != nullptr;
   work.counts_zero = false;  // until this sequence has been enqueued in full
   PlanArgs pa;
   pa.nitems = nitems;
@@ -565,13 +570,16 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     a.fb_total = work.fb_total;
     a.fb_e1 = work.fb_e1;
     a.fb_e2 = work.fb_e2;
+    a.hp_e1 = work.hp_e1;
+    a.fb2_count = work.fb2_count;
+    a.fb2_list = work.fb2_list;
     a.fb_inv_scale = work.fb_inv_scale;
     a.fb_nscale = work.fb_nscale;
   }
   const bool perch = term_ch != nullptr;
   // Inside a CUDA-graph capture, the FP64-series re-evaluation (three
-  // launches, idle in most batches) sits behind a conditional node that the
-  // last kernel before it sets when something is listed; outside capture, or
+  // launches, idle in most batches) sits behind a conditional node that a
+  // one-thread kernel sets when something is listed; outside capture, or
   // where the graph API refuses, it is launched unconditionally.
   bool cond = false;
   cudaGraphConditionalHandle cond_h = 0;
@@ -616,7 +624,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.a.tw = nullptr;
     A.nbins = nall;
     A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
-    A.done = work.bin_count + kNumBins;
+    A.done = work.bin_count + kNumBins + 1;
     for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
     e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch) : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
     launches++;
@@ -629,12 +637,12 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   }
   if (timing && (e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
 
-  // Re-evaluation of flagged mixed proposals: the listed ones get a
-  // double-float spectral stage on their FP32 series; proposals still above
-  // the tolerance get FP64 series (FP64 constants, FP64 slow part) that the
-  // same kernel transforms in double-float.  Results are written over the
-  // mixed ones; counts and lists live on the device, and each kernel leaves
-  // its counters at zero.
+  // Re-evaluation of flagged mixed proposals, in two concurrent branches:
+  // the double-float spectral stage on the FP32 series of fb_list (main
+  // stream), and FP64 series (FP64 constants, FP64 slow part, in series2)
+  // transformed by the same kernel for fb2_list (side stream).  Results are
+  // written over the mixed ones; counts and lists live on the device, and
+  // each branch leaves its counters at zero.
   if (fallback) {
     int nmax = kMaxN;
     while (nmax > bank.NFFT) nmax >>= 1;
@@ -642,14 +650,6 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     h.NFFT = bank.NFFT;
     h.cap = work.cap;
     h.nmax = nmax;
-    h.list = work.fb_list;
-    h.count = work.fb_count;
-    h.off = work.fb_off;
-    h.series32 = reinterpret_cast<const float2 *>(work.series);
-    h.itemsmix = work.itemsmix;
-    h.zero_at = work.fb_count;
-    h.nzero = 1;
-    h.done = work.bin_count + kNumBins + 3;
     h.w32 = bank.w32;
     h.w32lo = bank.w32lo;
     h.g32 = bank.g32;
@@ -663,21 +663,17 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     h.hh = hh;
     h.term_ch = term_ch;
     h.status = status;
-    h.next_count = work.fb2_count;
-    h.next_list = work.fb2_list;
-    h.next_total = work.fb_total + 1;
-    h.next_e1 = work.hp_e1;
-    h.inv_scale = work.fb_inv_scale;
-    h.nscale = work.fb_nscale;
-    h.has_cond = cond;
-    h.cond = cond_h;
-    e = fd_launch_hp(h, false, perch, num_sms, stream);
-    launches++;
-    if (e != cudaSuccess) return e;
-    // the FP64-series tier, behind the conditional node when capturing
-    cudaStream_t ts = stream;
+
+    // FP64-series branch on its own stream
+    cudaStream_t s2 = work.side[1];
+    if ((e = cudaEventRecord(work.join[0], stream)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(s2, work.join[0], 0)) != cudaSuccess) return e;
+    cudaStream_t ts = s2;
     cudaGraphNode_t cnode = nullptr;
     if (cond) {
+      fd_cond_kernel<<<1, 32, 0, s2>>>(work.fb2_count, cond_h);
+      launches++;
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
       const cudaGraphNode_t *deps = nullptr;
       size_t nd = 0;
       cudaStreamCaptureStatus cs;
@@ -686,7 +682,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
       np.conditional.handle = cond_h;
       np.conditional.type = cudaGraphCondTypeIf;
       np.conditional.size = 1;
-      if ((e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd)) != cudaSuccess) return e;
+      if ((e = cudaStreamGetCaptureInfo(s2, &cs, nullptr, nullptr, &deps, nullptr, &nd)) != cudaSuccess) return e;
       if ((e = cudaGraphAddNode(&cnode, cap_graph, deps, nullptr, nd, &np)) != cudaSuccess) return e;
       ts = work.side[0];
       if ((e = cudaStreamBeginCaptureToGraph(ts, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
@@ -698,35 +694,44 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     fd_item64_list_kernel<<<num_sms, 64, 0, ts>>>(pb, work.fb2_list, work.fb2_count);
     launches++;
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    e = fd_launch_slow_fp64_wide(sa, num_sms, ts);
+    SlowArgs s64 = sa;
+    s64.series = work.series2;
+    e = fd_launch_slow_fp64_wide(s64, num_sms, ts);
     launches++;
     if (e != cudaSuccess) return e;
     HpArgs h2 = h;
-    h2.has_cond = false;
-    h2.list = nullptr;
-    h2.count = nullptr;
-    h2.off = nullptr;
-    h2.series32 = nullptr;
-    h2.itemsmix = nullptr;
-    h2.series64 = reinterpret_cast<const double2 *>(work.series);
+    h2.series64 = reinterpret_cast<const double2 *>(work.series2);
     h2.bin_count = work.bin_count;
     h2.bin_list = work.bin_list;
     h2.items64 = work.items64;
-    h2.zero_at = work.bin_count;  // the size counts, the done counter, fb_count and fb2_count
-    h2.nzero = kNumBins + 3;
-    h2.next_count = nullptr;
-    h2.next_list = nullptr;
-    h2.next_total = nullptr;
+    h2.zero_at = work.bin_count;  // the size counts and fb2_count
+    h2.nzero = kNumBins + 1;
+    h2.done = work.bin_count + kNumBins + 4;
     e = fd_launch_hp(h2, true, perch, num_sms, ts);
     launches++;
     if (e != cudaSuccess) return e;
     if (cond) {
       cudaGraph_t body = nullptr;
       if ((e = cudaStreamEndCapture(ts, &body)) != cudaSuccess) return e;
-      if ((e = cudaStreamUpdateCaptureDependencies(stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+      if ((e = cudaStreamUpdateCaptureDependencies(s2, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
           cudaSuccess)
         return e;
     }
+    if ((e = cudaEventRecord(work.join[1], s2)) != cudaSuccess) return e;
+
+    // double-float branch on the caller's stream
+    h.list = work.fb_list;
+    h.count = work.fb_count;
+    h.off = work.fb_off;
+    h.series32 = reinterpret_cast<const float2 *>(work.series);
+    h.itemsmix = work.itemsmix;
+    h.zero_at = work.fb_count;
+    h.nzero = 1;
+    h.done = work.bin_count + kNumBins + 3;
+    e = fd_launch_hp(h, false, perch, num_sms, stream);
+    launches++;
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(stream, work.join[1], 0)) != cudaSuccess) return e;
   }
   work.counts_zero = true;
   if (timing) {

@@ -47,22 +47,24 @@ struct FdWorkDev {
   ItemF64 *items64 = nullptr;   // [cap]
   ItemMix *itemsmix = nullptr;  // [cap]
   ItemGrad *itemsgrad = nullptr;  // [cap]
-  // [kNumBins + 6]: per-size counts, the persistent spectral kernel's
-  // CTA-done counter, fb_count, fb2_count, the re-evaluation kernel's
-  // CTA-done counter and two spare ints
+  // [kNumBins + 6]: per-size counts, fb2_count, the persistent spectral
+  // kernel's CTA-done counter, fb_count, the CTA-done counters of the two
+  // re-evaluation launches and a spare int
   int *bin_count = nullptr;
   int *bin_list = nullptr;      // [kNumBins*cap]
   // Mixed precision: proposals whose error estimate exceeds the tolerance are
   // listed in fb_list with their series offsets and re-evaluated with the
-  // spectral stage in double-float; those still above it (fb2_list) get FP64
-  // series that the same kernel transforms, all in the same launch sequence
-  // (fb_e1 = fb_e2 = 0: no re-evaluation)
+  // spectral stage in double-float; those whose bound after that would still
+  // exceed it (fb2_list) get FP64 series (in series2) that the same kernel
+  // transforms, concurrently, in the same launch sequence (fb_e1 = fb_e2 = 0:
+  // no re-evaluation)
   float fb_e1 = 0.f, fb_e2 = 0.f, hp_e1 = 0.f;
   int *fb_list = nullptr;                  // [cap]
   long long *fb_off = nullptr;             // [cap]
   int *fb2_list = nullptr;                 // [cap]
-  int *fb_count = nullptr;                 // bin_count + kNumBins + 1
-  int *fb2_count = nullptr;                // bin_count + kNumBins + 2
+  int *fb_count = nullptr;                 // bin_count + kNumBins + 2
+  int *fb2_count = nullptr;                // bin_count + kNumBins
+  void *series2 = nullptr;                 // [series_bytes]: FP64 series of fb2_list
   unsigned long long *fb_total = nullptr;  // [2]: re-evaluated in double-float, from FP64 series
   float *fb_inv_scale = nullptr;           // [fb_nscale]: 1 / per-proposal tolerance scale (null: 1)
   int fb_nscale = 0, fb_nscale_cap = 0;

@@ -945,13 +945,16 @@ struct SpecArgs {
   // mixed precision: a proposal whose error estimate
   //   (fb_e1 sqrt(hw rr) + fb_e2 (hw + rr)) / scale_i
   // (hw = |h|^2, rr = |r - h|^2, whitened sums over the template support)
-  // exceeds 1 is listed in fb_list (count in *fb_count, series offsets in
-  // fb_off) for the double-float re-evaluation; fb_total[0] counts them.  No
-  // list: no estimate.
+  // exceeds 1 is listed for re-evaluation: in fb_list (count in *fb_count,
+  // series offsets in fb_off) for the double-float spectral stage on its FP32
+  // series, or, when the error left after that (estimate hp_e1 sqrt(hw rr) /
+  // scale_i) would still exceed 1, in fb2_list for FP64 series; fb_total[0]
+  // and [1] count them.  No list: no estimate.
   int *fb_count = nullptr, *fb_list = nullptr;
   long long *fb_off = nullptr;
+  int *fb2_count = nullptr, *fb2_list = nullptr;
   unsigned long long *fb_total = nullptr;
-  float fb_e1 = 0.f, fb_e2 = 0.f;
+  float fb_e1 = 0.f, fb_e2 = 0.f, hp_e1 = 0.f;
   // per-proposal tolerance scale: 1/scale_i for i < fb_nscale (null: 1)
   const float *fb_inv_scale = nullptr;
   int fb_nscale = 0;
@@ -991,14 +994,6 @@ struct HpArgs {
   const double *term_x;
   double *dlogl, *term_y, *hh, *term_ch;
   int *status;
-  // next tier (list mode): items whose estimate e1 sqrt(hw rr) / scale_i exceeds 1
-  int *next_count = nullptr, *next_list = nullptr;
-  unsigned long long *next_total = nullptr;
-  float next_e1 = 0.f;
-  bool has_cond = false;  // set the conditional node's value to (*next_count > 0) at the end
-  cudaGraphConditionalHandle cond = 0;
-  const float *inv_scale = nullptr;
-  int nscale = 0;
 };
 cudaError_t fd_launch_hp(const HpArgs &a, bool bin_mode, bool perch, int num_sms, cudaStream_t stream);
 
@@ -1306,13 +1301,18 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       const float hw = sh.hi + sh.lo;
       hh = 2.0 * (double)hw;
       if (a.fb_list) {
-        const float est = fmaf(a.fb_e1, sqrtf(hw * rr), a.fb_e2 * (hw + rr)) *
-                          fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
+        const float sq = sqrtf(hw * rr), sc = fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
+        const float est = fmaf(a.fb_e1, sq, a.fb_e2 * (hw + rr)) * sc;
         if (!(est <= 1.f)) {  // also a non-finite estimate
-          atomicAdd(a.fb_total, 1ull);
-          const int q = atomicAdd(a.fb_count, 1);
-          a.fb_list[q] = item;
-          a.fb_off[q] = (long long)(src - reinterpret_cast<const C *>(a.series));
+          if (!(a.hp_e1 * sq * sc <= 1.f)) {
+            atomicAdd(a.fb_total + 1, 1ull);
+            a.fb2_list[atomicAdd(a.fb2_count, 1)] = item;
+          } else {
+            atomicAdd(a.fb_total, 1ull);
+            const int q = atomicAdd(a.fb_count, 1);
+            a.fb_list[q] = item;
+            a.fb_off[q] = (long long)(src - reinterpret_cast<const C *>(a.series));
+          }
         }
       }
     } else {

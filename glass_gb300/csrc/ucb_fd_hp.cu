@@ -18,9 +18,11 @@
 // and writes the results over the mixed ones.  A proposal's latency is one
 // FFT, and a few hundred proposals take about one wave.
 //   list mode reads the mixed series (the error left is their FP32 rounding,
-//     ~2e-8 of the same scale); proposals still above the tolerance are
-//     listed for FP64 series from the FP64 slow part,
-//   bin mode reads those FP64 series through the size counts.
+//     up to ~2e-8 of the same scale),
+//   bin mode reads FP64 series from the FP64 slow part through the size
+//     counts, for the proposals whose bound after list mode would still
+//     exceed the tolerance (listed as such by the spectral kernels, and
+//     evaluated concurrently with list mode).
 #include <cooperative_groups.h>
 
 #include "ucb_fd_device.cuh"
@@ -158,27 +160,15 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
       }
       hp_write(e.item, N, e.seg, e.imin, NFFT, s, a.Q, a.QA, PERCH, a.term_x, a.dlogl, a.term_y, a.hh, a.term_ch,
                a.status);
-      if (!BIN && a.next_list) {
-        const float est =
-            a.next_e1 * sqrtf(s[2].hi * (s[0].hi + s[1].hi)) * fb_scale_of(a.inv_scale, a.nscale, e.item);
-        if (!(est <= 1.f)) {
-          a.next_list[atomicAdd(a.next_count, 1)] = e.item;
-          atomicAdd(a.next_total, 1ull);
-        }
-      }
     }
     cluster.sync();  // s_part is read before the next proposal overwrites it
   }
-  // the last CTA leaves the counters it was given at zero and sets the
-  // conditional node that follows (when captured)
+  // the last CTA leaves the counters it was given at zero
   if (threadIdx.x == 0) {
     __threadfence();
     if (atomicAdd(a.done, 1) == (int)gridDim.x - 1) {
-      const int nx = a.next_count ? *(volatile const int *)a.next_count : 0;
       for (int q = 0; q < a.nzero; q++) a.zero_at[q] = 0;
       *a.done = 0;
-      __threadfence();
-      if (a.has_cond) cudaGraphSetConditional(a.cond, nx > 0 ? 1u : 0u);
     }
   }
 }
