@@ -25,11 +25,14 @@ LIB = os.path.join(OUT_DIR, "libglass_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "-I" + os.path.join(ROOT, "include")]
-# The plain-FP64 translation units evaluate the carrier phase the way the
-# reference does (ucb/src/glass_ucb_waveform.c:877, arguments of ~1e6 rad); a
-# fused multiply-add rounds differently from the reference's separate multiply
-# and add by up to ~1e-10 rad there, so contraction is off for them.
-PER_FILE_FLAGS = {"ucb_fd.cu": ["-fmad=false"], "ucb_fd_fp64.cu": ["-fmad=false"], "ucb_fd_noalloc.cu": ["-fmad=false"],
+# The FP64 likelihood evaluates the delay and the carrier phase the way the
+# reference does (ucb/src/glass_ucb_waveform.c:858-877, arguments of ~1e6 rad,
+# where a fused multiply-add would round differently by up to ~1e-10 rad) with
+# explicit round-to-nearest operations, so its translation units contract
+# freely.  The no-allocation entry point, the F-statistic, the wavelet-domain
+# waveform and the noise and sampler units keep contraction off: their
+# results follow the reference's operation order throughout.
+PER_FILE_FLAGS = {"ucb_fd_noalloc.cu": ["-fmad=false"],
                   "wdm.cu": ["-Xcompiler", "-ffp-contract=off"],
                   "ucb_wavelet.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
                   "ucb_fstat.cu": ["-fmad=false"], "noise.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],

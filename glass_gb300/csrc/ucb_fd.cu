@@ -25,7 +25,8 @@
 // only there.
 //
 // Two precisions share the structure: plain FP64 (this file and
-// ucb_fd_fp64.cu, compiled without multiply-add contraction), and a mixed form
+// ucb_fd_fp64.cu; the delay and carrier phase round each operation on its
+// own, as the reference's C does), and a mixed form
 // (ucb_fd_mixed.cu) in which the carrier phase is carried in double-float
 // arithmetic and everything else is FP32.
 #include "ucb_fd_device.cuh"
@@ -79,16 +80,16 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
   plan_bin(a, i, b);
 }
 
-// FP64 constants of the proposals listed for an FP64 slow part
-// (list[0 .. *count)), binned by size: the size and placement are the mixed
-// plan's (the same bandwidth rule), so only the source geometry is evaluated
-// in FP64 here.  Grid-stride with warp-uniform trips, as plan_bin needs
-// whole warps.
 // Sets a CUDA-graph conditional node's value to (*count > 0).
 __global__ void fd_cond_kernel(const int *count, cudaGraphConditionalHandle h) {
   if (threadIdx.x == 0) cudaGraphSetConditional(h, *(volatile const int *)count > 0 ? 1u : 0u);
 }
 
+// FP64 constants of the proposals listed for an FP64 slow part
+// (list[0 .. *count)), binned by size: the size and placement are the mixed
+// plan's (the same bandwidth rule), so only the source geometry is evaluated
+// in FP64 here.  Grid-stride with warp-uniform trips, as plan_bin needs
+// whole warps.
 __global__ void __launch_bounds__(64) fd_item64_list_kernel(PlanArgs a, const int *list, const int *count) {
   const int n = *count;
   const int stride = gridDim.x * blockDim.x;

@@ -586,12 +586,37 @@ __device__ __forceinline__ void fast_sincos(float x, float *s, float *c) {
   *c = ((qi + 1) & 2) ? -cc : cc;
 }
 
+// Delay of spacecraft i's sample, xi = t - k.x_i / c, and the carrier
+// argument w0 xi - phi0 - dfq t + wd xi^2 (ucb/src/glass_ucb_waveform.c:858-870),
+// every operation rounded on its own.
+__device__ __forceinline__ double slow_xi64(const ItemF64 &c, const OrbitSample64 &o, int i) {
+  const double kx = __dadd_rn(__dadd_rn(__dmul_rn(o.x[i], c.k[0]), __dmul_rn(o.y[i], c.k[1])), __dmul_rn(o.z[i], c.k[2]));
+  return __dsub_rn(o.t, __ddiv_rn(kx, kCLIGHT));
+}
+__device__ __forceinline__ double slow_arg2_64(const ItemF64 &c, double t, double w0, double wd, double xi) {
+  const double a2 = __dsub_rn(__dsub_rn(__dmul_rn(w0, xi), c.phi0), __dmul_rn(c.dfq, t));
+  return __dadd_rn(a2, __dmul_rn(__dmul_rn(wd, xi), xi));
+}
+// One arm from its spacecraft's terms and its own projections
+// (ucb/src/glass_ucb_waveform.c:880-922).
+__device__ __forceinline__ double2 slow_arm64(const ItemF64 &c, double fon, double aev, double arg2, double dp,
+                                              double dcr, double kr) {
+  const double arg1 = 0.5 * fon * (1.0 + kr);
+  const double sinc = 0.25 * sin(arg1) / arg1;
+  const double t1r = aev * (dp * c.DPr + dcr * c.DCr);
+  const double t1i = aev * (dp * c.DPi + dcr * c.DCi);
+  double s2, c2;
+  sincos(__dsub_rn(arg1, arg2), &s2, &c2);
+  return make_double2(sinc * (t1r * c2 + t1i * s2), sinc * (-t1r * s2 + t1i * c2));
+}
+
 // The six arm series d_ij at one sample (order 12, 13, 21, 23, 31, 32),
 // amplitude-free, in FP64 with the reference's own sequence of operations
 // (ucb/src/glass_ucb_waveform.c:840-922).  The carrier argument arg2 reaches
-// ~1e6 rad, where every rounding step is worth ~1e-10 rad; the translation
-// units that use this are compiled without multiply-add contraction so that
-// those roundings are the reference's.
+// ~1e6 rad, where every rounding step is worth ~1e-10 rad: the delay xi and
+// the carrier phase round every product and sum separately (explicit
+// round-to-nearest operations, which multiply-add contraction leaves alone),
+// as the reference's C does; everything else may contract.
 __device__ __forceinline__ void slow_sample64(const ItemF64 &c, const OrbitSample64 &o, double fstar, double L,
                                               double2 d[6]) {
   double r12[3] = {(o.x[1] - o.x[0]) / L, (o.y[1] - o.y[0]) / L, (o.z[1] - o.z[0]) / L};
@@ -608,12 +633,9 @@ __device__ __forceinline__ void slow_sample64(const ItemF64 &c, const OrbitSampl
   double fon[3], arg2[3], aev[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    double kdotx = (o.x[i] * c.k[0] + o.y[i] * c.k[1] + o.z[i] * c.k[2]) / kCLIGHT;
-    double xi = t - kdotx;
+    const double xi = slow_xi64(c, o, i);
     fon[i] = (c.f0 + c.fdot * xi) / fstar;
-    double a2 = w0 * xi - c.phi0 - c.dfq * t;
-    a2 += wd * xi * xi;
-    arg2[i] = a2;
+    arg2[i] = slow_arg2_64(c, t, w0, wd, xi);
     aev[i] = 1.0 + ae * xi;
   }
   const int ai[6] = {0, 0, 1, 1, 2, 2};
@@ -623,14 +645,33 @@ __device__ __forceinline__ void slow_sample64(const ItemF64 &c, const OrbitSampl
 #pragma unroll
   for (int a = 0; a < 6; a++) {
     int i = ai[a];
-    double arg1 = 0.5 * fon[i] * (1.0 + krs[a]);
-    double sinc = 0.25 * sin(arg1) / arg1;
-    double t1r = aev[i] * (dps[a] * c.DPr + dcs[a] * c.DCr);
-    double t1i = aev[i] * (dps[a] * c.DPi + dcs[a] * c.DCi);
-    double s2, c2;
-    sincos(arg1 - arg2[i], &s2, &c2);
-    d[a] = make_double2(sinc * (t1r * c2 + t1i * s2), sinc * (-t1r * s2 + t1i * c2));
+    d[a] = slow_arm64(c, fon[i], aev[i], arg2[i], dps[a], dcs[a], krs[a]);
   }
+}
+
+// The two arms of spacecraft i (12, 13 | 21, 23 | 31, 32) with the same
+// operations as slow_sample64, for a slow part that spreads the arms of a
+// sample over three warps.
+__device__ __forceinline__ void slow_arms64(const ItemF64 &c, const OrbitSample64 &o, double fstar, double L, int i,
+                                            double2 d[2]) {
+  // arm vectors: spacecraft 0 needs r12, r13; 1 needs r12 (as r21 = -r12), r23; 2 needs r13, r23
+  const int pb = i == 2 ? 2 : 1;  // first vector r_{0 pb}: r12 (i = 0, 1) or r13 (i = 2)
+  const int qa = i == 0 ? 0 : 1;  // second vector r_{qa 2}: r13 (i = 0) or r23 (i = 1, 2)
+  const int pa = 0, qb = 2;
+  const double u[3] = {(o.x[pb] - o.x[pa]) / L, (o.y[pb] - o.y[pa]) / L, (o.z[pb] - o.z[pa]) / L};
+  const double v[3] = {(o.x[qb] - o.x[qa]) / L, (o.y[qb] - o.y[qa]) / L, (o.z[qb] - o.z[qa]) / L};
+  const double dpu = quad(c.ep, u[0], u[1], u[2]), dcu = quad(c.ec, u[0], u[1], u[2]);
+  const double dpv = quad(c.ep, v[0], v[1], v[2]), dcv = quad(c.ec, v[0], v[1], v[2]);
+  const double kru = c.k[0] * u[0] + c.k[1] * u[1] + c.k[2] * u[2];
+  const double krv = c.k[0] * v[0] + c.k[1] * v[1] + c.k[2] * v[2];
+  const double w0 = kPI2 * c.f0, wd = kPI * c.fdot, ae = 0.66666666666666666666 * c.fdot / c.f0;
+  const double xi = slow_xi64(c, o, i);
+  const double fon = (c.f0 + c.fdot * xi) / fstar;
+  const double arg2 = slow_arg2_64(c, o.t, w0, wd, xi);
+  const double aev = 1.0 + ae * xi;
+  // arm order: i = 0: 12 (u), 13 (v); i = 1: 21 (-u), 23 (v); i = 2: 31 (-u), 32 (-v)
+  d[0] = slow_arm64(c, fon, aev, arg2, dpu, dcu, i == 0 ? kru : -kru);
+  d[1] = slow_arm64(c, fon, aev, arg2, dpv, dcv, i == 2 ? -krv : krv);
 }
 
 // Carrier phase common to the three spacecraft, reduced mod 2 pi:
@@ -1502,10 +1543,5 @@ static cudaError_t launch_slow(const SlowArgs &a, int num_sms, cudaStream_t stre
 // ones): one warp per CTA, so that the chunks of 32 samples spread over the
 // SMs instead of filling the first few (an FP64 sample costs ~700 FP64
 // instructions and the FP64 pipe of an SM issues a warp's in 16 cycles).
-template <bool MIX>
-static cudaError_t launch_slow_wide(const SlowArgs &a, int num_sms, cudaStream_t stream) {
-  fd_slow_kernel<MIX, 32><<<4 * num_sms, 32, 0, stream>>>(a);
-  return cudaGetLastError();
-}
 
 }  // namespace glass
