@@ -826,8 +826,8 @@ extern "C" int glass_gpu_grad_fisher_batch(glass_gpu_ctx *ctx, int nitems, const
   if (nitems == 0) return GLASS_OK;
   if (!item_seg || !params || !term_y || !grad) return set_err(GLASS_ERR_ARG, "grad_fisher_batch: null argument");
   const int n_fixed = ctx->n_fixed;
-  if (n_fixed > 1024 || n_fixed > ctx->bank.NFFT)
-    return set_err(GLASS_ERR_SIZE, "grad_fisher_batch: template size above min(1024, NFFT)");
+  if (n_fixed > kMaxN || n_fixed > ctx->bank.NFFT)
+    return set_err(GLASS_ERR_SIZE, "grad_fisher_batch: template size above min(4096, NFFT)");
   if (fisher_mode != 0 && fisher_mode != 1) return set_err(GLASS_ERR_ARG, "grad_fisher_batch: unknown fisher_mode");
   if (!ctx->bank.nseg) return set_err(GLASS_ERR_STATE, "grad_fisher_batch: no segment bank uploaded");
   int rc = ctx_activate(ctx);

@@ -18,13 +18,14 @@
 // FFT'd; per bin the eight derivatives are assembled and
 //   grad_k = (r - h | dh/dp_k),   F_kl = (dh/dp_k | dh/dp_l)
 // accumulated (inner product of utils/src/glass_math.c:362-380).
+#include <cooperative_groups.h>
+
 #include "ucb_fd_device.cuh"
 
 namespace glass {
 
 constexpr int kGradTemplates = 6;
 constexpr int kGradSeries = 4 * kGradTemplates;
-constexpr int kGradMaxN = 1024;
 
 // sinc'(x) = (x cos x - sin x)/x^2: Taylor series through x^11 for |x| <= 1.
 __device__ __forceinline__ float dsinc_f(float x) {
@@ -451,6 +452,252 @@ __global__ void __launch_bounds__(GradCfg<N>::CTA, GradCfg<N>::MINB) fd_gradspec
   }
 }
 
+// Sizes 2048 and 4096: the 24 series of a proposal (384 KB at N = 4096 with
+// a work buffer) do not fit one SM, so a cluster of 8 CTAs takes each
+// proposal and keeps them in its distributed shared memory: CTA r computes
+// samples [r N/8, (r+1) N/8) of all 24 series (the per-sample work shares its
+// geometry across the series) and stores each value in the CTA that owns the
+// series (3 per CTA); each CTA transforms its three series; CTA r then
+// assembles the derivatives over bins [r N/8, (r+1) N/8), reading the 24
+// spectra of a bin from the CTAs that hold them, and CTA 0 sums the eight
+// CTAs' partial sums.
+constexpr int kGradCluster = 8;
+constexpr int kGradBigThreads = 256;
+
+template <int N>
+struct GradBigCfg {
+  static constexpr int SPC = kGradSeries / kGradCluster;  // series per CTA
+  static constexpr size_t bytes = sizeof(float2) * (size_t)N * (SPC + 2);  // series, work buffer, twiddles
+};
+
+// Stockham FFT of N complex floats by the CTA, out of place between x and y:
+// radix-4 stages (butterfly i < N/4, k = i mod p, reads x[i + m N/4], writes
+// y[(i - k) 4 + k + m p] after the twiddles exp(-2 pi i m k / (4p))) and a
+// radix-2 stage when log2 N is odd.  tw[j] = exp(-2 pi i j / N).  Sizes
+// 2048 and 4096 take an even number of passes: the result is back in x.
+template <int N>
+__device__ __forceinline__ void cta_fft_f32(float2 *x, float2 *y, const float2 *tw) {
+  constexpr int L2 = N == 4096 ? 12 : 11;
+  static_assert((N == 2048 || N == 4096) && (L2 / 2 + L2 % 2) % 2 == 0, "even number of passes");
+  int p = 1;
+#pragma unroll 1
+  for (; 4 * p <= N; p <<= 2) {
+    const int step = N / (4 * p), q = N / 4;
+    for (int i = threadIdx.x; i < q; i += blockDim.x) {
+      const int k = i & (p - 1);
+      float2 u0 = x[i], u1 = x[i + q], u2 = x[i + 2 * q], u3 = x[i + 3 * q];
+      if (p > 1) {
+        u1 = cmul(u1, tw[k * step]);
+        u2 = cmul(u2, tw[2 * k * step]);
+        u3 = cmul(u3, tw[3 * k * step]);
+      }
+      const float2 a = cadd(u0, u2), b = csub(u0, u2), c = cadd(u1, u3), d = cmi(csub(u1, u3));
+      const int j = (i - k) * 4 + k;
+      y[j] = cadd(a, c);
+      y[j + p] = cadd(b, d);
+      y[j + 2 * p] = csub(a, c);
+      y[j + 3 * p] = csub(b, d);
+    }
+    __syncthreads();
+    float2 *t = x;
+    x = y;
+    y = t;
+  }
+  if (p < N) {  // log2 N odd: p = N/2
+    for (int i = threadIdx.x; i < N / 2; i += blockDim.x) {
+      const int k = i & (p - 1);
+      const float2 a = x[i], b = cmul(x[i + N / 2], tw[k]);
+      const int j = (i - k) * 2 + k;
+      y[j] = cadd(a, b);
+      y[j + p] = csub(a, b);
+    }
+    __syncthreads();
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(kGradBigThreads, 1) fd_gradspec_big_kernel(GradSpecArgs a) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  constexpr int SPC = GradBigCfg<N>::SPC, CL = kGradCluster, NB = N / CL, NACC = 8 + 36;
+  constexpr int NW = kGradBigThreads / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *ser = reinterpret_cast<float2 *>(smem_raw);  // [SPC][N]: this CTA's series, then spectra
+  float2 *work = ser + SPC * N;
+  float2 *tw = work + N;
+  __shared__ float s_warp[NW][NACC];
+  __shared__ float2 s_warp_rr[NW];
+  __shared__ float s_tot[NACC];
+  __shared__ float2 s_rr;
+  const int r = (int)cluster.block_rank(), lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = a.tw[i];
+  float2 *sers[CL];
+#pragma unroll
+  for (int q = 0; q < CL; q++) sers[q] = cluster.map_shared_rank(ser, q);
+  const int count = a.bin_count[a.bin];
+  const int NFFT = a.NFFT;
+  for (int slot = (int)(blockIdx.x / CL); slot < count; slot += (int)(gridDim.x / CL)) {
+    const int item = a.bin_list[slot];
+    const ItemGrad &it = a.items[item];
+    const int seg = it.m.seg, imin = it.m.imin;
+    // 1. this CTA's samples of the 24 series, to the CTAs that own them
+    for (int n = r * NB + threadIdx.x; n < (r + 1) * NB; n += blockDim.x) {
+      float2 accs[kGradSeries];
+      grad_sample(a.K, it, a.mix[n], a.geo[n], accs);
+#pragma unroll
+      for (int sidx = 0; sidx < kGradSeries; sidx++) sers[sidx / SPC][(sidx % SPC) * N + n] = accs[sidx];
+    }
+    cluster.sync();
+    // 2. this CTA's three series
+#pragma unroll 1
+    for (int sidx = 0; sidx < SPC; sidx++) cta_fft_f32<N>(ser + sidx * N, work, tw);
+    cluster.sync();
+    // 3. derivatives over this CTA's bins (as fd_gradspec_kernel)
+    float accg[NACC];
+#pragma unroll
+    for (int q = 0; q < NACC; q++) accg[q] = 0.f;
+    float racc = 0.f;
+    const float sc = it.m.amp_hi;
+    const float2 DP = make_float2(it.DP[0], it.DP[1]), DC = make_float2(it.DC[0], it.DC[1]);
+    const float2 dDPi = make_float2(it.dDP_i[0], it.dDP_i[1]), dDCi = make_float2(it.dDC_i[0], it.dDC_i[1]);
+    const float2 dDPs = make_float2(it.dDP_s[0], it.dDP_s[1]), dDCs = make_float2(it.dDC_s[0], it.dDC_s[1]);
+    auto W = [&](int t, int ch, int k, float4 gt) {
+      const int s0 = 4 * t + 2 * ch, s1 = s0 + 1;
+      const float2 f0 = sers[s0 / SPC][(s0 % SPC) * N + k], f1 = sers[s1 / SPC][(s1 % SPC) * N + k];
+      return cadd(cmul(f0, make_float2(gt.x, gt.y)), cmul(f1, make_float2(gt.z, gt.w)));
+    };
+#pragma unroll 1
+    for (int k = r * NB + threadIdx.x; k < (r + 1) * NB; k += blockDim.x) {
+      const int m = (k + N / 2) & (N - 1);
+      const int j = imin + m;
+      if (j < 0 || j >= NFFT) continue;
+      const size_t sj = (size_t)seg * NFFT + j;
+      const float4 w = a.w32[sj], wl = a.w32lo[sj];
+      const float4 gAE[2] = {a.g32[2 * sj], a.g32[2 * sj + 1]};
+      float qw[2] = {1.f, 1.f};
+      if (a.fisher_mode == 1) {
+        const float2 ic_t = a.invc[(size_t)seg * NFFT + m], ic_j = a.invc[sj];
+        qw[0] = ic_t.x / ic_j.x;
+        qw[1] = ic_t.y / ic_j.y;
+      }
+#pragma unroll
+      for (int ch = 0; ch < 2; ch++) {
+        const float4 gt = gAE[ch];
+        const float2 Hp = cscale(W(0, ch, k, gt), sc), Hx = cscale(W(1, ch, k, gt), sc);
+        const float2 h = cadd(cmul(DP, Hp), cmul(DC, Hx));
+        float2 D[8];
+        D[0] = cscale(W(2, ch, k, gt), sc);
+        D[1] = cscale(W(4, ch, k, gt), sc);
+        D[2] = cscale(W(5, ch, k, gt), sc);
+        D[3] = h;
+        D[4] = cadd(cmul(dDPi, Hp), cmul(dDCi, Hx));
+        D[5] = cadd(cmul(dDPs, Hp), cmul(dDCs, Hx));
+        D[6] = cmi(h);
+        D[7] = cscale(W(3, ch, k, gt), sc);
+        const float wr = ch ? w.z : w.x, wi = ch ? w.w : w.y;
+        const float lr = ch ? wl.z : wl.x, li = ch ? wl.w : wl.y;
+        const float rr = (wr - h.x) + lr, ri = (wi - h.y) + li;
+        racc += fmaf(rr, rr, ri * ri);
+#pragma unroll
+        for (int p = 0; p < 8; p++) accg[p] = fmaf(rr, D[p].x, fmaf(ri, D[p].y, accg[p]));
+        int q = 8;
+#pragma unroll
+        for (int p = 0; p < 8; p++)
+#pragma unroll
+          for (int l = p; l < 8; l++, q++) accg[q] = fmaf(qw[ch], fmaf(D[p].x, D[l].x, D[p].y * D[l].y), accg[q]);
+      }
+    }
+    // 4. sums over the CTA (the residual power in double-float), then over the cluster
+    df rs = {racc, 0.f};
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+      for (int q = 0; q < NACC; q++) accg[q] += __shfl_xor_sync(0xffffffffu, accg[q], off);
+      rs = df_add(rs, df{__shfl_xor_sync(0xffffffffu, rs.hi, off), __shfl_xor_sync(0xffffffffu, rs.lo, off)});
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NACC; q++) s_warp[wid][q] = accg[q];
+      s_warp_rr[wid] = make_float2(rs.hi, rs.lo);
+    }
+    __syncthreads();
+    if (threadIdx.x < NACC) {
+      float v = 0.f;
+      for (int w2 = 0; w2 < NW; w2++) v += s_warp[w2][threadIdx.x];
+      s_tot[threadIdx.x] = v;
+    } else if (threadIdx.x == NACC) {
+      df t = {0.f, 0.f};
+      for (int w2 = 0; w2 < NW; w2++) t = df_add(t, df{s_warp_rr[w2].x, s_warp_rr[w2].y});
+      s_rr = make_float2(t.hi, t.lo);
+    }
+    cluster.sync();  // every CTA's sums are published; the spectra are no longer read
+    if (r == 0) {
+      if (threadIdx.x < NACC) {
+        const int q = threadIdx.x;
+        float v = 0.f;
+        for (int c = 0; c < CL; c++) v += *cluster.map_shared_rank(&s_tot[q], c);
+        const double dv = 2.0 * (double)v;
+        if (q < 8) {
+          a.grad[8 * (size_t)item + q] = dv;
+        } else if (a.fisher) {
+          int qq = q - 8, p = 0;
+          while (qq >= 8 - p) {
+            qq -= 8 - p;
+            p++;
+          }
+          const int l = p + qq;
+          a.fisher[64 * (size_t)item + 8 * p + l] = dv;
+          a.fisher[64 * (size_t)item + 8 * l + p] = dv;
+        }
+      } else if (threadIdx.x == NACC) {
+        df t = {0.f, 0.f};
+        for (int c = 0; c < CL; c++) {
+          const float2 o = *cluster.map_shared_rank(&s_rr, c);
+          t = df_add(t, df{o.x, o.y});
+        }
+        const int jlo = imin < 0 ? 0 : imin;
+        const int jhi = imin + N > NFFT ? NFFT : imin + N;
+        const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
+        const double term = (Qs[jhi] - Qs[jlo]) - ((double)t.hi + (double)t.lo);
+        a.term_y[item] = term;
+        if (a.status) a.status[item] = isfinite(term) ? 0 : 1;
+      }
+    }
+    cluster.sync();  // CTA 0 has read the sums before the next proposal overwrites them
+  }
+}
+
+template <int N>
+static cudaError_t launch_gradspec_big(const GradSpecArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
+  const size_t smem = GradBigCfg<N>::bytes;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kGradCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kGradBigThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  static LaunchSetup setup;
+  int ncl = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    cudaError_t r = cudaFuncSetAttribute(fd_gradspec_big_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (r != cudaSuccess) return r;
+    cudaLaunchConfig_t q = cfg;
+    q.gridDim = dim3(kGradCluster * num_sms);
+    return cudaOccupancyMaxActiveClusters(o, fd_gradspec_big_kernel<N>, &q);
+  }, &ncl);
+  if (e != cudaSuccess) return e;
+  if (ncl < 1) ncl = 1;
+  if (ncl > nitems_bound) ncl = nitems_bound > 0 ? nitems_bound : 1;
+  cfg.gridDim = dim3(kGradCluster * ncl);
+  return cudaLaunchKernelEx(&cfg, fd_gradspec_big_kernel<N>, a);
+}
+
 template <int N>
 static cudaError_t launch_gradspec(const GradSpecArgs &a, int nitems_bound, int num_sms, cudaStream_t stream) {
   using Cfg = GradCfg<N>;
@@ -486,8 +733,7 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
   PlanArgs &pa = ga.base;
   pa.nitems = nitems;
   pa.nseg = bank.nseg;
-  // sizes above kGradMaxN are refused through the bandwidth cap
-  pa.NFFT = bank.NFFT < kGradMaxN ? bank.NFFT : kGradMaxN;
+  pa.NFFT = bank.NFFT;
   pa.cap = work.cap;
   pa.precision = 1;
   pa.n_fixed = N_fixed;
@@ -562,12 +808,18 @@ cudaError_t fd_grad_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWork
       case 256: e = launch_gradspec<256>(a, nitems, num_sms, sb); break;
       case 512: e = launch_gradspec<512>(a, nitems, num_sms, sb); break;
       case 1024: e = launch_gradspec<1024>(a, nitems, num_sms, sb); break;
-      default: e = cudaErrorInvalidValue;
+      case 2048: e = launch_gradspec_big<2048>(a, nitems, num_sms, sb); break;
+      default: e = launch_gradspec_big<4096>(a, nitems, num_sms, sb); break;
     }
     launches++;
-    if (e != cudaSuccess) return e;
-    if ((e = cudaEventRecord(work.join[b], sb)) != cudaSuccess) return e;
+    // the branch is joined to the caller's stream even when its launch failed
+    const cudaError_t ej = cudaEventRecord(work.join[b], sb);
     nb++;
+    if (e == cudaSuccess) e = ej;
+    if (e != cudaSuccess) {
+      for (int q = 0; q < nb; q++) cudaStreamWaitEvent(stream, work.join[q], 0);
+      return e;
+    }
   }
   for (int b = 0; b < nb; b++)
     if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;

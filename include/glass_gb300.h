@@ -168,12 +168,11 @@ int glass_gpu_get_host_access(glass_gpu_ctx *ctx, int *supported, int *direct);
  *   term_y[i]      : as glass_gpu_dlogl_batch
  *   grad[8 i + k]  : d term_y / d params[k] = (r - h | dh/dp_k)
  *   fisher[64 i + 8 k + l] : (dh/dp_k | dh/dp_l)   (may be NULL)
- * The template size follows glass_gpu_set_template_size (at most 1024 here).
- * fisher_mode 0
+ * The template size follows glass_gpu_set_template_size (32 to 4096; sizes
+ * 2048 and 4096 are evaluated by clusters of 8 CTAs).  fisher_mode 0
  * weights every template bin with the noise at that bin; 1 reproduces
  * ucb_fisher's indexing, which weights template bin i with the noise of
- * segment bin i (ucb/src/glass_ucb_waveform.c:480-485).  Templates larger
- * than 1024 samples get status GLASS_ITEM_NONFINITE.  Device pointers;
+ * segment bin i (ucb/src/glass_ucb_waveform.c:480-485).  Device pointers;
  * asynchronous.
  */
 int glass_gpu_grad_fisher_batch(glass_gpu_ctx *ctx, int nitems, const int *item_seg, const double *params,

@@ -157,6 +157,29 @@ def fisher(ref, rng):
     np.savez_compressed(os.path.join(HERE, "fisher.npz"), **{k: np.array(v) for k, v in out.items()})
 
 
+def fisher_big(ref, rng):
+    """ucb_fisher on 8192-bin segments with templates of 2048 and 4096
+    samples (two each): loud sources at 5-20 mHz, redrawn until the
+    reference's own alignment gives the wanted size."""
+    NFFT = 8192
+    out = {"params": [], "F": [], "qmin": [], "invC": [], "N": []}
+    for want in (2048, 2048, 4096, 4096):
+        while True:
+            p = wl.draw_source(rng, rng.uniform(5e-3, 2e-2), 10 ** rng.uniform(-21, -20), 1e-17)
+            qmin = int(p[0]) - NFFT // 2
+            N = int(ref.alignment(T, NFFT, qmin, p)[0])
+            if N == want:
+                break
+        invC = 1.0 / wl.aenoise_ff((qmin + np.arange(NFFT)) / T)
+        F, ev, evec = ref.fisher(p, T, NFFT, qmin, invC, invC)
+        out["params"].append(p)
+        out["F"].append(F)
+        out["qmin"].append(qmin)
+        out["invC"].append(invC)
+        out["N"].append(N)
+    np.savez_compressed(os.path.join(HERE, "fisher_big.npz"), **{k: np.array(v) for k, v in out.items()})
+
+
 def wdm(ref, rng):
     """WDM windows, forward and inverse transforms on small grids (the window
     exponent is the reference's fixed 6, A = 0), and the per-layer transform."""
@@ -438,7 +461,7 @@ def fisher_draw(ref, rng):
 
 
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
-             "sampler": 20261208, "fisher_draw": 20261209}
+             "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210}
 
 
 def main(names=()):
@@ -461,6 +484,7 @@ def main(names=()):
     noise_eta(ref, np.random.default_rng(OWN_SEEDS["noise_eta"]))
     sampler(ref, np.random.default_rng(OWN_SEEDS["sampler"]))
     fisher_draw(ref, np.random.default_rng(OWN_SEEDS["fisher_draw"]))
+    fisher_big(ref, np.random.default_rng(OWN_SEEDS["fisher_big"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -23,7 +23,7 @@ def engine():
     eng.close()
 
 
-def _bank(rng, port, nseg=8, NFFT=1024, f=(1e-3, 5e-3)):
+def _bank(rng, port, nseg=8, NFFT=1024, f=(1e-3, 5e-3), amp=(-22.5, -21.3)):
     qmin, dA, dE, iA, iE, inj = [], [], [], [], [], []
 
     def wf(p):
@@ -32,7 +32,7 @@ def _bank(rng, port, nseg=8, NFFT=1024, f=(1e-3, 5e-3)):
         return int(al[0]), h[3], h[4]
 
     for s in range(nseg):
-        p = wl.draw_source(rng, rng.uniform(*f), 10 ** rng.uniform(-22.5, -21.3), 1e-17)
+        p = wl.draw_source(rng, rng.uniform(*f), 10 ** rng.uniform(*amp), 1e-17)
         p[1] = np.clip(p[1], -0.9, 0.9)
         p[4] = np.clip(p[4], -0.9, 0.9)
         q, a, e, ia, ie = wl.make_segment(rng, [p], wf, NFFT=NFFT, T=T)
@@ -87,6 +87,60 @@ def test_fisher_matches_reference_ucb_fisher(engine, golden):
         # Fisher matrix weighted like the gradient (noise at the template's bins)
         _, grad0, F0, _ = engine.grad_fisher_host(np.zeros(1, np.int32), g["params"][k:k + 1], fisher_mode=0)
         np.testing.assert_allclose(grad0[0], -F0[0][:, 3], rtol=1e-3, atol=1e-3 * np.sqrt(np.diag(F0[0])).max())
+
+
+def test_fisher_big_templates_match_reference_ucb_fisher(engine, golden):
+    """Templates of 2048 and 4096 samples on 8192-bin segments (the cluster
+    kernels) against the reference's ucb_fisher."""
+    g = golden("fisher_big.npz")
+    NFFT = g["invC"].shape[1]
+    for k in range(len(g["params"])):
+        invC = g["invC"][k]
+        zero = np.zeros((1, NFFT), complex)
+        bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array([g["qmin"][k]], np.int32), dA=zero, dE=zero,
+                              invCA=invC[None], invCE=invC[None])
+        engine.upload(bank)
+        ty, grad, F, st = engine.grad_fisher_host(np.zeros(1, np.int32), g["params"][k:k + 1], fisher_mode=1)
+        assert st[0] == 0
+        ref = g["F"][k]
+        scale = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+        err = np.abs(F[0] - ref) / scale
+        assert err.max() < 1e-3, (int(g["N"][k]), err.max(), np.unravel_index(err.argmax(), err.shape))
+        _, grad0, F0, _ = engine.grad_fisher_host(np.zeros(1, np.int32), g["params"][k:k + 1], fisher_mode=0)
+        np.testing.assert_allclose(grad0[0], -F0[0][:, 3], rtol=1e-3, atol=1e-3 * np.sqrt(np.diag(F0[0])).max())
+
+
+def test_gradient_big_templates_match_central_differences(engine, port):
+    """Proposals of 2048 and 4096 samples on an 8192-bin bank, mixed with
+    small ones in the same batch: every size's gradient against central
+    differences of the FP64 path."""
+    rng = np.random.default_rng(33)
+    bank, inj = _bank(rng, port, nseg=6, NFFT=8192, f=(5e-3, 2e-2), amp=(-21.0, -20.0))
+    engine.upload(bank)
+    seg = np.repeat(np.arange(len(inj), dtype=np.int32), 2)
+    props = np.array([wl.gaussian_jumps(rng, inj[s], wl.jump_scales(inj[s], 300.0), 1)[0] for s in seg])
+    small = inj[:2].copy()
+    small[:, 3] -= 4.0  # quieter copies: small templates on the same segments
+    seg = np.concatenate([seg, np.arange(2, dtype=np.int32)])
+    props = np.vstack([props, small])
+    ty, g, F, st = engine.grad_fisher_host(seg, props)
+    assert (st == 0).all(), st
+    Ns = {int(port.alignment(T, 8192, int(bank.qmin[s]), p)[0]) for s, p in zip(seg, props)}
+    assert {2048, 4096} <= Ns, Ns
+    _, t64, _, _ = engine.dlogl_host(seg, props, precision=gg.PREC_FP64)
+    assert (np.abs(ty - t64) / np.maximum(1.0, np.abs(t64))).max() < 1e-6
+    eps = 1e-6
+    fd = np.zeros_like(g)
+    for k in range(8):
+        pp, pm = props.copy(), props.copy()
+        pp[:, k] += eps
+        pm[:, k] -= eps
+        _, tp, _, _ = engine.dlogl_host(seg, pp, precision=gg.PREC_FP64)
+        _, tm, _, _ = engine.dlogl_host(seg, pm, precision=gg.PREC_FP64)
+        fd[:, k] = (tp - tm) / (2 * eps)
+    sig = np.sqrt(np.maximum(np.einsum("nkk->nk", F), 1e-30))
+    err = np.abs(g - fd) / (sig + np.abs(fd))
+    assert err.max() < 2e-3, err.max(axis=0)
 
 
 def test_fisher_aligned_matches_finite_differences(engine, port):
