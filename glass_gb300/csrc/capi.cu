@@ -53,9 +53,10 @@ int report_cuda_error(cudaError_t e, const char *where) { return cuda_err(e, whe
 // support, so that (h|h) = 2 hw):
 //   |error| <= kMixedErrK1 sqrt(hw rr) + kMixedErrK2 (hw + rr).
 // An FP32 FFT leaves up to ~1e-7 of relative error on the few bins that hold
-// a narrowband template's power; the largest ratio measured on the
-// 64-segment benchmark workload was 7.9e-8.
-static constexpr double kMixedErrK1 = 1.0e-7;
+// a narrowband template's power; the largest ratios measured were 7.9e-8 on
+// the 64-segment benchmark workload and 1.15e-7 on loud templates far from
+// the data (amplitude x30), so the bound takes twice the typical maximum.
+static constexpr double kMixedErrK1 = 2.0e-7;
 static constexpr double kMixedErrK2 = 0.0;
 // The same after the double-float re-evaluation of FP32 series: what is left
 // is the rounding of the series values (measured up to 2.1e-8 on proposals
