@@ -60,8 +60,8 @@ static constexpr double kMixedErrK1 = 2.0e-7;
 static constexpr double kMixedErrK2 = 0.0;
 // The same after the double-float re-evaluation of FP32 series: what is left
 // is the rounding of the series values (measured up to 2.1e-8 on proposals
-// far from the data).
-static constexpr double kHpErrK1 = 4.0e-8;
+// far from the data, 6.9e-8 on loud ones near it).
+static constexpr double kHpErrK1 = 1.2e-7;
 static constexpr double kMixedTolDefault = 1e-3;
 
 // ----------------------------------------------------------------- context
