@@ -549,12 +549,12 @@ class Engine:
             sc = np.ascontiguousarray(scale, np.float64)
             _check(self.lib.glass_gpu_set_mixed_tolerance_scale(self._ctx, int(sc.size), _pd(sc)))
 
-    def mixed_reevaluated(self):
-        """(double-float, FP64-series) counts of re-evaluated proposals so far
+    def mixed_reevaluated(self) -> int:
+        """Number of proposals re-evaluated in double-float so far
         (synchronises the stream)."""
-        n = (ctypes.c_ulonglong * 2)()
-        _check(self.lib.glass_gpu_mixed_reevaluated(self._ctx, n))
-        return int(n[0]), int(n[1])
+        n = ctypes.c_ulonglong(0)
+        _check(self.lib.glass_gpu_mixed_reevaluated(self._ctx, ctypes.byref(n)))
+        return int(n.value)
 
 
 class HostBatch:

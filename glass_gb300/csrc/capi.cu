@@ -58,10 +58,6 @@ int report_cuda_error(cudaError_t e, const char *where) { return cuda_err(e, whe
 // the data (amplitude x30), so the bound takes twice the typical maximum.
 static constexpr double kMixedErrK1 = 2.0e-7;
 static constexpr double kMixedErrK2 = 0.0;
-// The same after the double-float re-evaluation of FP32 series: what is left
-// is the rounding of the series values (measured up to 2.1e-8 on proposals
-// far from the data, 6.9e-8 on loud ones near it).
-static constexpr double kHpErrK1 = 1.2e-7;
 static constexpr double kMixedTolDefault = 1e-3;
 
 // ----------------------------------------------------------------- context
@@ -195,8 +191,6 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->work.series);
   cudaFree(ctx->work.series2);
   cudaFree(ctx->work.fb_list);
-  cudaFree(ctx->work.fb_off);
-  cudaFree(ctx->work.fb2_list);
   cudaFree(ctx->work.fb_total);
   cudaFree(ctx->work.fb_inv_scale);
   cudaFree(ctx->d_stage);
@@ -278,7 +272,6 @@ static void apply_mixed_tol(glass_gpu_ctx *ctx) {
   const double t = ctx->mixed_tol;
   ctx->work.fb_e1 = t > 0 ? (float)(kMixedErrK1 / t) : 0.f;
   ctx->work.fb_e2 = t > 0 ? (float)(kMixedErrK2 / t) : 0.f;
-  ctx->work.hp_e1 = t > 0 ? (float)(kHpErrK1 / t) : 0.f;
 }
 
 extern "C" int glass_gpu_set_mixed_tolerance(glass_gpu_ctx *ctx, double tol) {
@@ -321,11 +314,11 @@ extern "C" int glass_gpu_set_mixed_tolerance_scale(glass_gpu_ctx *ctx, int n, co
 
 extern "C" int glass_gpu_mixed_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count) {
   if (!ctx || !count) return set_err(GLASS_ERR_ARG, "glass_gpu_mixed_reevaluated: null argument");
-  count[0] = count[1] = 0;
+  *count = 0;
   if (!ctx->work.fb_total) return GLASS_OK;
   int rc = ctx_activate(ctx);
   if (rc) return rc;
-  GLASS_CUDA(cudaMemcpyAsync(count, ctx->work.fb_total, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+  GLASS_CUDA(cudaMemcpyAsync(count, ctx->work.fb_total, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              ctx->stream), "read re-evaluation count");
   GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "read re-evaluation count");
   return GLASS_OK;
@@ -492,13 +485,8 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   cudaFree(w.series);
   cudaFree(w.series2);
   cudaFree(w.fb_list);
-  cudaFree(w.fb_off);
-  cudaFree(w.fb2_list);
   w.fb_list = nullptr;
-  w.fb_off = nullptr;
-  w.fb2_list = nullptr;
   w.fb_count = nullptr;
-  w.fb2_count = nullptr;
   w.items64 = nullptr;
   w.itemsmix = nullptr;
   w.itemsgrad = nullptr;
@@ -517,14 +505,11 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   GLASS_CUDA(cudaMalloc(&w.itemsgrad, sizeof(ItemGrad) * (size_t)cap), "cudaMalloc(itemsgrad)");
   GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * (kNumBins + 6)), "cudaMalloc(bin_count)");
   GLASS_CUDA(cudaMemset(w.bin_count, 0, sizeof(int) * (kNumBins + 6)), "cudaMemset(bin_count)");
-  w.fb_count = w.bin_count + kNumBins + 2;
-  w.fb2_count = w.bin_count + kNumBins;
+  w.fb_count = w.bin_count + kNumBins;
   GLASS_CUDA(cudaMalloc(&w.fb_list, sizeof(int) * (size_t)cap), "cudaMalloc(fb_list)");
-  GLASS_CUDA(cudaMalloc(&w.fb_off, sizeof(long long) * (size_t)cap), "cudaMalloc(fb_off)");
-  GLASS_CUDA(cudaMalloc(&w.fb2_list, sizeof(int) * (size_t)cap), "cudaMalloc(fb2_list)");
   if (!w.fb_total) {
-    GLASS_CUDA(cudaMalloc(&w.fb_total, 2 * sizeof(unsigned long long)), "cudaMalloc(fb_total)");
-    GLASS_CUDA(cudaMemset(w.fb_total, 0, 2 * sizeof(unsigned long long)), "cudaMemset(fb_total)");
+    GLASS_CUDA(cudaMalloc(&w.fb_total, sizeof(unsigned long long)), "cudaMalloc(fb_total)");
+    GLASS_CUDA(cudaMemset(w.fb_total, 0, sizeof(unsigned long long)), "cudaMemset(fb_total)");
   }
   apply_mixed_tol(ctx);
   w.counts_zero = true;

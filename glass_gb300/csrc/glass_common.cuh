@@ -174,6 +174,7 @@ struct __align__(16) ItemMix {
   // between the arms, and so the size of the A/E combinations; a rounding
   // common to the template is a coherent phase and amplitude error
   float kl[3], w0cl, fonfs0l;
+  float fdfsl, aefl;  // fdfs, aef minus their float rounding (double-float slow part)
   df eps2pi;      // 2 pi (f0 T - q)
   df beta1, beta2;  // 2 pi f0 AU/c * k_x, k_y
   df phi0;

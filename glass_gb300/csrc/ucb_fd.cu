@@ -35,7 +35,6 @@ namespace glass {
 
 cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
-cudaError_t fd_launch_slow_fp64_wide(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
@@ -83,37 +82,6 @@ __global__ void __launch_bounds__(64) fd_plan64_kernel(PlanArgs a) {
 // Sets a CUDA-graph conditional node's value to (*count > 0).
 __global__ void fd_cond_kernel(const int *count, cudaGraphConditionalHandle h) {
   if (threadIdx.x == 0) cudaGraphSetConditional(h, *(volatile const int *)count > 0 ? 1u : 0u);
-}
-
-// FP64 constants of the proposals listed for an FP64 slow part
-// (list[0 .. *count)), binned by size: the size and placement are the mixed
-// plan's (the same bandwidth rule), so only the source geometry is evaluated
-// in FP64 here.  Grid-stride with warp-uniform trips, as plan_bin needs
-// whole warps.
-__global__ void __launch_bounds__(64) fd_item64_list_kernel(PlanArgs a, const int *list, const int *count) {
-  const int n = *count;
-  const int stride = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const int k = base + threadIdx.x;
-    int b = -1, i = 0;
-    if (k < n) {
-      i = list[k];
-      const ItemMix &m = a.itemsmix[i];
-      double p[8];
-      for (int q = 0; q < 8; q++) p[q] = a.params[8 * (size_t)i + q];
-      SourceGeom g;
-      source_geometry(p, 8, a.T, g);
-      ItemF64 c;
-      make_item_f64(g, m.N, c);
-      c.seg = m.seg;
-      c.N = m.N;
-      c.imin = m.imin;
-      c.pad = 0;
-      a.items64[i] = c;
-      b = fd_bin_of(m.N);
-    }
-    plan_bin(a, i, b);
-  }
 }
 
 // Mixed-precision plan, warp-specialised: GB300's FP64 pipe issues a warp
@@ -226,7 +194,9 @@ __global__ void __launch_bounds__(128) fd_planmix_kernel(PlanArgs a) {
       c->fonfs0 = (float)(f0 / a.fstar);
       c->fonfs0l = (float)(f0 / a.fstar - (double)c->fonfs0);
       c->fdfs = (float)(fdotT / a.fstar);
+      c->fdfsl = (float)(fdotT / a.fstar - (double)c->fdfs);
       c->aef = (float)(0.66666666666666666666 * fdotT / f0);
+      c->aefl = (float)(0.66666666666666666666 * fdotT / f0 - (double)c->aef);
       c->w0c = (float)(kPI2 * f0 / kCLIGHT);
       c->w0cl = (float)(kPI2 * f0 / kCLIGHT - (double)c->w0c);
       c->p7pi = (float)(kPI * p[7]);
@@ -335,28 +305,34 @@ __global__ void fd_orbit_table_kernel(FdTablesDev tab, double T, double t0) {
   // mixed slow-part geometry: offsets from the guiding centre and arm monomials
   // (absent from tables built for the FP64 path alone)
   if (tab.geo[b]) {
-    GeoSampleMix gm;
+    double v[28];
     double d[3][3];
     for (int i = 0; i < 3; i++) {
       d[i][0] = R * (saca * sbs[i] - (1. + sa2) * cbs[i]);
       d[i][1] = R * (saca * cbs[i] - (1. + ca2) * sbs[i]);
       d[i][2] = -kSQ3 * R * (ca * cbs[i] + sa * sbs[i]);
-      for (int q = 0; q < 3; q++) gm.f[3 * i + q] = (float)d[i][q];
+      for (int q = 0; q < 3; q++) v[3 * i + q] = d[i][q];
     }
     const int arm[3][2] = {{0, 1}, {0, 2}, {1, 2}};
     for (int a = 0; a < 3; a++) {
       double r[3];
       for (int q = 0; q < 3; q++) r[q] = (d[arm[a][1]][q] - d[arm[a][0]][q]) / kLARM;
-      float *mo = gm.f + 9 + 6 * a;
-      mo[0] = (float)(r[0] * r[0]);
-      mo[1] = (float)(2.0 * r[0] * r[1]);
-      mo[2] = (float)(2.0 * r[0] * r[2]);
-      mo[3] = (float)(r[1] * r[1]);
-      mo[4] = (float)(2.0 * r[1] * r[2]);
-      mo[5] = (float)(r[2] * r[2]);
+      double *mo = v + 9 + 6 * a;
+      mo[0] = r[0] * r[0];
+      mo[1] = 2.0 * r[0] * r[1];
+      mo[2] = 2.0 * r[0] * r[2];
+      mo[3] = r[1] * r[1];
+      mo[4] = 2.0 * r[1] * r[2];
+      mo[5] = r[2] * r[2];
     }
-    gm.f[27] = 0.f;
+    v[27] = 0.0;
+    GeoSampleMix gm, gl;
+    for (int q = 0; q < 28; q++) {
+      gm.f[q] = (float)v[q];
+      gl.f[q] = (float)(v[q] - (double)gm.f[q]);
+    }
     tab.geo[b][n] = gm;
+    if (tab.geolo[b]) tab.geolo[b][n] = gl;
   }
   double s, cth;
   sincospi(-2.0 * (double)n / (double)N, &s, &cth);
@@ -373,8 +349,8 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
     size_t total = 0;
     for (int b = 0; b < kNumBins; b++) {
       int N = 32 << b;
-      total += (size_t)N * (sizeof(OrbitSample64) + sizeof(OrbitSampleMix) + sizeof(GeoSampleMix) + sizeof(float2) +
-                            sizeof(double2) + sizeof(float4));
+      total += (size_t)N * (sizeof(OrbitSample64) + sizeof(OrbitSampleMix) + 2 * sizeof(GeoSampleMix) +
+                            sizeof(float2) + sizeof(double2) + sizeof(float4));
     }
     cudaError_t e = cudaMalloc(&tab.base, total);
     if (e != cudaSuccess) return e;
@@ -386,6 +362,8 @@ cudaError_t fd_build_orbit_tables(FdTablesDev &tab, double T, double t0, cudaStr
       tab.mix[b] = (OrbitSampleMix *)p;
       p += (size_t)N * sizeof(OrbitSampleMix);
       tab.geo[b] = (GeoSampleMix *)p;
+      p += (size_t)N * sizeof(GeoSampleMix);
+      tab.geolo[b] = (GeoSampleMix *)p;
       p += (size_t)N * sizeof(GeoSampleMix);
       tab.tw64[b] = (double2 *)p;
       p += (size_t)N * sizeof(double2);
@@ -567,19 +545,15 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   if (fallback) {
     a.fb_count = work.fb_count;
     a.fb_list = work.fb_list;
-    a.fb_off = work.fb_off;
     a.fb_total = work.fb_total;
     a.fb_e1 = work.fb_e1;
     a.fb_e2 = work.fb_e2;
-    a.hp_e1 = work.hp_e1;
-    a.fb2_count = work.fb2_count;
-    a.fb2_list = work.fb2_list;
     a.fb_inv_scale = work.fb_inv_scale;
     a.fb_nscale = work.fb_nscale;
   }
   const bool perch = term_ch != nullptr;
-  // Inside a CUDA-graph capture, the FP64-series re-evaluation (three
-  // launches, idle in most batches) sits behind a conditional node that a
+  // Inside a CUDA-graph capture, the re-evaluation (three launches, idle in
+  // batches with nothing listed) sits behind a conditional node that a
   // one-thread kernel sets when something is listed; outside capture, or
   // where the graph API refuses, it is launched unconditionally.
   bool cond = false;
@@ -625,7 +599,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.a.tw = nullptr;
     A.nbins = nall;
     A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
-    A.done = work.bin_count + kNumBins + 1;
+    A.done = work.bin_count + kNumBins + 1;  // fb_count is at kNumBins
     for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
     e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch) : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
     launches++;
@@ -638,19 +612,30 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   }
   if (timing && (e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
 
-  // Re-evaluation of flagged mixed proposals, in two concurrent branches:
-  // the double-float spectral stage on the FP32 series of fb_list (main
-  // stream), and FP64 series (FP64 constants, FP64 slow part, in series2)
-  // transformed by the same kernel for fb2_list (side stream).  Results are
-  // written over the mixed ones; counts and lists live on the device, and
-  // each branch leaves its counters at zero.
+  // Re-evaluation of the listed mixed proposals in double-float: series
+  // (into series2), spectral stage, results written over the mixed ones; the
+  // size counts and fb_count end at zero.
   if (fallback) {
     int nmax = kMaxN;
     while (nmax > bank.NFFT) nmax >>= 1;
+    SlowArgs sh = sa;
+    sh.series = work.series2;
+    for (int b = 0; b < kNumBins; b++) sh.geolo[b] = tab.geolo[b];
+    sh.invLd = df_from_double(1.0 / kLARM);
+    sh.AUcd = df_from_double(kAU / kCLIGHT);
+    sh.invTd = df_from_double(1.0 / bank.T);
+    sh.invcd = df_from_double(1.0 / kCLIGHT);
     HpArgs h;
     h.NFFT = bank.NFFT;
     h.cap = work.cap;
     h.nmax = nmax;
+    h.bin_count = work.bin_count;
+    h.bin_list = work.bin_list;
+    h.itemsmix = work.itemsmix;
+    h.series = reinterpret_cast<const float4 *>(work.series2);
+    h.zero_at = work.bin_count;  // the size counts and fb_count
+    h.nzero = kNumBins + 1;
+    h.done = work.bin_count + kNumBins + 2;
     h.w32 = bank.w32;
     h.w32lo = bank.w32lo;
     h.g32 = bank.g32;
@@ -664,15 +649,10 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     h.hh = hh;
     h.term_ch = term_ch;
     h.status = status;
-
-    // FP64-series branch on its own stream
-    cudaStream_t s2 = work.side[1];
-    if ((e = cudaEventRecord(work.join[0], stream)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(s2, work.join[0], 0)) != cudaSuccess) return e;
-    cudaStream_t ts = s2;
+    cudaStream_t ts = stream;
     cudaGraphNode_t cnode = nullptr;
     if (cond) {
-      fd_cond_kernel<<<1, 32, 0, s2>>>(work.fb2_count, cond_h);
+      fd_cond_kernel<<<1, 32, 0, stream>>>(work.fb_count, cond_h);
       launches++;
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
       const cudaGraphNode_t *deps = nullptr;
@@ -683,7 +663,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
       np.conditional.handle = cond_h;
       np.conditional.type = cudaGraphCondTypeIf;
       np.conditional.size = 1;
-      if ((e = cudaStreamGetCaptureInfo(s2, &cs, nullptr, nullptr, &deps, nullptr, &nd)) != cudaSuccess) return e;
+      if ((e = cudaStreamGetCaptureInfo(stream, &cs, nullptr, nullptr, &deps, nullptr, &nd)) != cudaSuccess) return e;
       if ((e = cudaGraphAddNode(&cnode, cap_graph, deps, nullptr, nd, &np)) != cudaSuccess) return e;
       ts = work.side[0];
       if ((e = cudaStreamBeginCaptureToGraph(ts, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
@@ -691,48 +671,15 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
         return e;
     }
     PlanArgs pb = pa;
-    pb.precision = 0;
-    fd_item64_list_kernel<<<num_sms, 64, 0, ts>>>(pb, work.fb2_list, work.fb2_count);
-    launches++;
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    SlowArgs s64 = sa;
-    s64.series = work.series2;
-    e = fd_launch_slow_fp64_wide(s64, num_sms, ts);
-    launches++;
-    if (e != cudaSuccess) return e;
-    HpArgs h2 = h;
-    h2.series64 = reinterpret_cast<const double2 *>(work.series2);
-    h2.bin_count = work.bin_count;
-    h2.bin_list = work.bin_list;
-    h2.items64 = work.items64;
-    h2.zero_at = work.bin_count;  // the size counts and fb2_count
-    h2.nzero = kNumBins + 1;
-    h2.done = work.bin_count + kNumBins + 4;
-    e = fd_launch_hp(h2, true, perch, num_sms, ts);
-    launches++;
+    e = fd_launch_reeval(pb, work.fb_list, work.fb_count, sh, h, perch, num_sms, ts, &launches);
     if (e != cudaSuccess) return e;
     if (cond) {
       cudaGraph_t body = nullptr;
       if ((e = cudaStreamEndCapture(ts, &body)) != cudaSuccess) return e;
-      if ((e = cudaStreamUpdateCaptureDependencies(s2, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+      if ((e = cudaStreamUpdateCaptureDependencies(stream, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
           cudaSuccess)
         return e;
     }
-    if ((e = cudaEventRecord(work.join[1], s2)) != cudaSuccess) return e;
-
-    // double-float branch on the caller's stream
-    h.list = work.fb_list;
-    h.count = work.fb_count;
-    h.off = work.fb_off;
-    h.series32 = reinterpret_cast<const float2 *>(work.series);
-    h.itemsmix = work.itemsmix;
-    h.zero_at = work.fb_count;
-    h.nzero = 1;
-    h.done = work.bin_count + kNumBins + 3;
-    e = fd_launch_hp(h, false, perch, num_sms, stream);
-    launches++;
-    if (e != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(stream, work.join[1], 0)) != cudaSuccess) return e;
   }
   work.counts_zero = true;
   if (timing) {

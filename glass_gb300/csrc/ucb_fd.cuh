@@ -29,6 +29,7 @@ struct FdTablesDev {
   OrbitSample64 *pos64[kNumBins] = {};
   OrbitSampleMix *mix[kNumBins] = {};
   GeoSampleMix *geo[kNumBins] = {};
+  GeoSampleMix *geolo[kNumBins] = {};  // the same minus its float rounding (double-float slow part)
   float2 *tw32[kNumBins] = {};
   float4 *tw32x[kNumBins] = {};  // the same twiddles as hi + lo floats (mixed likelihood)
   double2 *tw64[kNumBins] = {};
@@ -47,25 +48,20 @@ struct FdWorkDev {
   ItemF64 *items64 = nullptr;   // [cap]
   ItemMix *itemsmix = nullptr;  // [cap]
   ItemGrad *itemsgrad = nullptr;  // [cap]
-  // [kNumBins + 6]: per-size counts, fb2_count, the persistent spectral
-  // kernel's CTA-done counter, fb_count, the CTA-done counters of the two
-  // re-evaluation launches and a spare int
+  // [kNumBins + 6]: per-size counts, fb_count, the CTA-done counters of the
+  // persistent spectral kernel and of the re-evaluation kernel, and three
+  // spare ints
   int *bin_count = nullptr;
   int *bin_list = nullptr;      // [kNumBins*cap]
   // Mixed precision: proposals whose error estimate exceeds the tolerance are
-  // listed in fb_list with their series offsets and re-evaluated with the
-  // spectral stage in double-float; those whose bound after that would still
-  // exceed it (fb2_list) get FP64 series (in series2) that the same kernel
-  // transforms, concurrently, in the same launch sequence (fb_e1 = fb_e2 = 0:
-  // no re-evaluation)
-  float fb_e1 = 0.f, fb_e2 = 0.f, hp_e1 = 0.f;
+  // listed in fb_list and evaluated again in double-float (series in
+  // series2), in the same launch sequence (fb_e1 = fb_e2 = 0: no
+  // re-evaluation)
+  float fb_e1 = 0.f, fb_e2 = 0.f;
   int *fb_list = nullptr;                  // [cap]
-  long long *fb_off = nullptr;             // [cap]
-  int *fb2_list = nullptr;                 // [cap]
-  int *fb_count = nullptr;                 // bin_count + kNumBins + 2
-  int *fb2_count = nullptr;                // bin_count + kNumBins
-  void *series2 = nullptr;                 // [series_bytes]: FP64 series of fb2_list
-  unsigned long long *fb_total = nullptr;  // [2]: re-evaluated in double-float, from FP64 series
+  int *fb_count = nullptr;                 // bin_count + kNumBins
+  void *series2 = nullptr;                 // [series_bytes]: double-float series of fb_list
+  unsigned long long *fb_total = nullptr;  // proposals re-evaluated
   float *fb_inv_scale = nullptr;           // [fb_nscale]: 1 / per-proposal tolerance scale (null: 1)
   int fb_nscale = 0, fb_nscale_cap = 0;
   // every launch sequence leaves the counts at zero (the spectral kernel's last

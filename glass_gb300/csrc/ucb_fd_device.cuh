@@ -518,7 +518,9 @@ static __device__ void make_item_mix(const SourceGeom &g, int N, double T, doubl
   c.fonfs0 = (float)(g.f0 / fstar);
   c.fonfs0l = (float)(g.f0 / fstar - (double)c.fonfs0);
   c.fdfs = (float)(g.fdot * T / fstar);
+  c.fdfsl = (float)(g.fdot * T / fstar - (double)c.fdfs);
   c.aef = (float)(0.66666666666666666666 * g.fdot * T / g.f0);
+  c.aefl = (float)(0.66666666666666666666 * g.fdot * T / g.f0 - (double)c.aef);
   c.w0c = (float)(kPI2 * g.f0 / kCLIGHT);
   c.w0cl = (float)(kPI2 * g.f0 / kCLIGHT - (double)c.w0c);
   c.p7pi = (float)(kPI * g.fdot * T * T);
@@ -958,6 +960,10 @@ struct SlowArgs {
   const OrbitSampleMix *mix[kNumBins];
   const GeoSampleMix *geo[kNumBins] = {};  // mixed only
   void *series;  // float2 (mixed) or double2 (FP64)
+  // double-float slow part of the re-evaluation: the geometry's low parts
+  // and 1/L, AU/c, 1/T, 1/c as hi + lo floats; series as float4
+  const GeoSampleMix *geolo[kNumBins] = {};
+  df invLd, AUcd, invTd, invcd;
 };
 
 // Stage 2: FFTs, TDI weights, whitening and the residual power, per size.
@@ -986,16 +992,11 @@ struct SpecArgs {
   // mixed precision: a proposal whose error estimate
   //   (fb_e1 sqrt(hw rr) + fb_e2 (hw + rr)) / scale_i
   // (hw = |h|^2, rr = |r - h|^2, whitened sums over the template support)
-  // exceeds 1 is listed for re-evaluation: in fb_list (count in *fb_count,
-  // series offsets in fb_off) for the double-float spectral stage on its FP32
-  // series, or, when the error left after that (estimate hp_e1 sqrt(hw rr) /
-  // scale_i) would still exceed 1, in fb2_list for FP64 series; fb_total[0]
-  // and [1] count them.  No list: no estimate.
+  // exceeds 1 is listed in fb_list (count in *fb_count) for the
+  // double-float re-evaluation; fb_total counts them.  No list: no estimate.
   int *fb_count = nullptr, *fb_list = nullptr;
-  long long *fb_off = nullptr;
-  int *fb2_count = nullptr, *fb2_list = nullptr;
   unsigned long long *fb_total = nullptr;
-  float fb_e1 = 0.f, fb_e2 = 0.f, hp_e1 = 0.f;
+  float fb_e1 = 0.f, fb_e2 = 0.f;
   // per-proposal tolerance scale: 1/scale_i for i < fb_nscale (null: 1)
   const float *fb_inv_scale = nullptr;
   int fb_nscale = 0;
@@ -1006,22 +1007,15 @@ __device__ __forceinline__ float fb_scale_of(const float *inv_scale, int n, int 
   return (inv_scale && i < n) ? inv_scale[i] : 1.f;
 }
 
-// Double-float spectral re-evaluation (ucb_fd_hp.cu) of listed mixed proposals
-// (list mode) or of the FP64 series of binned proposals (bin mode).
+// Double-float re-evaluation (ucb_fd_hp.cu) of listed mixed proposals: their
+// series in double-float, laid out by the size counts, and the spectral stage
+// in double-float.
 struct HpArgs {
   int NFFT, cap;
   int nmax;  // largest template size the bank allows (shared memory is sized for it)
-  // list mode (mixed series): items list[0 .. *count), series offsets off[] (float2 elements)
-  const int *list = nullptr;
-  const int *count = nullptr;
-  const long long *off = nullptr;
-  const float2 *series32 = nullptr;
+  const int *bin_count = nullptr, *bin_list = nullptr;
   const ItemMix *itemsmix = nullptr;
-  // bin mode (FP64 series from the FP64 slow part, laid out by the size counts)
-  const double2 *series64 = nullptr;
-  const int *bin_count = nullptr;
-  const int *bin_list = nullptr;
-  const ItemF64 *items64 = nullptr;
+  const float4 *series = nullptr;  // (hi re, hi im, lo re, lo im) per sample
   // zeroing at the end: the last CTA zeroes nzero ints at zero_at
   int *zero_at = nullptr;
   int nzero = 0;
@@ -1036,7 +1030,11 @@ struct HpArgs {
   double *dlogl, *term_y, *hh, *term_ch;
   int *status;
 };
-cudaError_t fd_launch_hp(const HpArgs &a, bool bin_mode, bool perch, int num_sms, cudaStream_t stream);
+// Bins the listed proposals, computes their series in double-float and
+// evaluates their spectral stage in double-float, writing over the mixed
+// results; the counts end at zero.
+cudaError_t fd_launch_reeval(const PlanArgs &pa, const int *list, const int *count, const SlowArgs &sa,
+                             const HpArgs &h, bool perch, int num_sms, cudaStream_t stream, int *nlaunch);
 
 // Start (in samples) of size bin `bin` in the scratch series: sizes are laid
 // out in increasing order, proposals of one size back to back, each holding 4
@@ -1342,18 +1340,11 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       const float hw = sh.hi + sh.lo;
       hh = 2.0 * (double)hw;
       if (a.fb_list) {
-        const float sq = sqrtf(hw * rr), sc = fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
-        const float est = fmaf(a.fb_e1, sq, a.fb_e2 * (hw + rr)) * sc;
+        const float est = fmaf(a.fb_e1, sqrtf(hw * rr), a.fb_e2 * (hw + rr)) *
+                          fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
         if (!(est <= 1.f)) {  // also a non-finite estimate
-          if (!(a.hp_e1 * sq * sc <= 1.f)) {
-            atomicAdd(a.fb_total + 1, 1ull);
-            a.fb2_list[atomicAdd(a.fb2_count, 1)] = item;
-          } else {
-            atomicAdd(a.fb_total, 1ull);
-            const int q = atomicAdd(a.fb_count, 1);
-            a.fb_list[q] = item;
-            a.fb_off[q] = (long long)(src - reinterpret_cast<const C *>(a.series));
-          }
+          atomicAdd(a.fb_total, 1ull);
+          a.fb_list[atomicAdd(a.fb_count, 1)] = item;
         }
       }
     } else {

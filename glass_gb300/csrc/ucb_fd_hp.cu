@@ -1,28 +1,29 @@
 // Double-float re-evaluation of mixed-precision proposals.
 //
-// The mixed path's template is an FP32 FFT of FP32 series; an FP32 FFT leaves
-// a relative error of up to ~1e-7 on the few bins that hold a narrowband
+// The mixed path's template is an FP32 FFT of FP32 series; both leave
+// relative errors of order 1e-7 on the few bins that hold a narrowband
 // template's power, so its delta logL carries an error of up to ~1e-7 x
 // sqrt((h|h)/2 |r - h|^2) (whitened sums over the template support): below
 // 1e-3 except for loud templates, near the data of a source with SNR ~ 300 or
 // far from the data with (h|h) ~ 1e6.  The mixed spectral kernels list those
-// proposals with their series offsets, and their spectral stage is evaluated
-// again in double-float arithmetic (pairs of floats, ~48 bits, on the FP32
-// pipe, which on GB300 runs 64 times the FP64 rate) by one wide kernel whose
-// thread-block clusters of 4 CTAs each take one proposal: CTA r transforms
-// series r in its shared memory (radix-4 Stockham, twiddles as hi + lo floats
-// in shared memory), then CTAs 2c and 2c + 1 form channel c's whitened
-// template per bin from their own spectrum and their partner's (read through
-// distributed shared memory), each over half of the bins, and sum the
-// residual power and the template power; CTA 0 gathers the four partial sums
-// and writes the results over the mixed ones.  A proposal's latency is one
-// FFT, and a few hundred proposals take about one wave.
-//   list mode reads the mixed series (the error left is their FP32 rounding,
-//     up to ~2e-8 of the same scale),
-//   bin mode reads FP64 series from the FP64 slow part through the size
-//     counts, for the proposals whose bound after list mode would still
-//     exceed the tolerance (listed as such by the spectral kernels, and
-//     evaluated concurrently with list mode).
+// proposals, and they are evaluated again with every step in double-float
+// arithmetic (pairs of floats, ~48 bits, on the FP32 pipe, which on GB300
+// runs 64 times the FP64 rate), in three launches:
+//   fd_hp_bin_kernel:  the listed proposals binned by size;
+//   fd_slow_hp_kernel: their four A/E arm-combination series in
+//     double-float, one warp per 32 samples: the mixed slow part's formulation
+//     (carrier phase heterodyned to the segment and reduced mod 2 pi, so that
+//     its absolute error stays ~1e-12 rad) with every product and sum in
+//     double-float, double-float sine, cosine and sinc, and the per-sample
+//     geometry and per-proposal constants as hi + lo floats;
+//   fd_hp_kernel:      thread-block clusters of 4 CTAs, one proposal each:
+//     CTA r transforms series r in its shared memory (radix-4 Stockham,
+//     twiddles as hi + lo floats), then CTAs 2c and 2c + 1 form channel c's
+//     whitened template per bin from their own spectrum and their partner's
+//     (read through distributed shared memory), each over half of the bins,
+//     and sum the residual power and the template power; CTA 0 gathers the
+//     four partial sums and writes the results over the mixed ones.
+// What is left is of order 1e-12 of the same scale.
 #include <cooperative_groups.h>
 
 #include "ucb_fd_device.cuh"
@@ -31,78 +32,161 @@ namespace glass {
 
 constexpr int kHpThreads = 256;
 
-// The proposal of entry k: item index, size, segment, placement, series
-// offset (elements of the series scratch) and template scale.
+// ------------------------------------------------------------------ binning
+// The listed proposals (list[0 .. *count)) binned by their mixed plan's size.
+// Grid-stride with warp-uniform trips, as plan_bin needs whole warps.
+__global__ void __launch_bounds__(64) fd_hp_bin_kernel(PlanArgs a, const int *list, const int *count) {
+  const int n = *count;
+  const int stride = gridDim.x * blockDim.x;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const int k = base + threadIdx.x;
+    int b = -1, i = 0;
+    if (k < n) {
+      i = list[k];
+      b = fd_bin_of(a.itemsmix[i].N);
+    }
+    plan_bin(a, i, b);
+  }
+}
+
+// -------------------------------------------------------- slow part, df
+// The six arm series at one sample, as slow_sample_mix computes them, in
+// double-float throughout.
+__device__ __forceinline__ void slow_sample_hp(const ItemMix &c, const OrbitSampleMix &o, const GeoSampleMix &gm,
+                                               const GeoSampleMix &gl, const SlowArgs &K, dc d[6]) {
+  df f[27];
+#pragma unroll
+  for (int q = 0; q < 27; q++) f[q] = df{gm.f[q], gl.f[q]};
+  const df k0 = {c.k[0], c.kl[0]}, k1 = {c.k[1], c.kl[1]}, k2 = {c.k[2], c.kl[2]};
+  // k.(x_i - x_gc) per spacecraft (metres); k.r_ij from their differences
+  df kd[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    kd[i] = df_add(df_add(df_mul(k0, f[3 * i]), df_mul(k1, f[3 * i + 1])), df_mul(k2, f[3 * i + 2]));
+  const df kr12 = df_mul(df_add(kd[1], df_neg(kd[0])), K.invLd);
+  const df kr13 = df_mul(df_add(kd[2], df_neg(kd[0])), K.invLd);
+  const df kr23 = df_mul(df_add(kd[2], df_neg(kd[1])), K.invLd);
+  // r^T M r of the three arms, M = m (DP e+ + DC ex) as hi + lo
+  auto quad6 = [&](const float *M, const float *Ml, int a) {
+    const df *mo = f + 9 + 6 * a;
+    df acc = df_mul(df{M[0], Ml[0]}, mo[0]);
+#pragma unroll
+    for (int q = 1; q < 6; q++) acc = df_add(acc, df_mul(df{M[q], Ml[q]}, mo[q]));
+    return acc;
+  };
+  const df mr12 = quad6(c.Mr, c.Mrl, 0), mi12 = quad6(c.Mi, c.Mil, 0);
+  const df mr13 = quad6(c.Mr, c.Mrl, 1), mi13 = quad6(c.Mi, c.Mil, 1);
+  const df mr23 = quad6(c.Mr, c.Mrl, 2), mi23 = quad6(c.Mi, c.Mil, 2);
+
+  const df psi0 = carrier_phase_mix(c, o);
+  const df u = {o.u_hi, o.u_lo}, ca = {o.ca_hi, o.ca_lo}, sa = {o.sa_hi, o.sa_lo};
+  const df tgc = df_mul(K.AUcd, df_add(df_mul(k0, ca), df_mul(k1, sa)));  // guiding-centre delay (s)
+  const df fonfs0 = {c.fonfs0, c.fonfs0l}, fdfs = {c.fdfs, c.fdfsl}, aef = {c.aef, c.aefl};
+  const df w0c = {c.w0c, c.w0cl};
+  const df u2 = df{2.f * u.hi, 2.f * u.lo};
+  df fon[3], aev[3], arg2[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const df tT = df_mul(df_add(tgc, df_mul(kd[i], K.invcd)), K.invTd);  // tau_i / T
+    const df v = df_add(u, df_neg(tT));                                 // xi / T
+    fon[i] = df_add(fonfs0, df_mul(fdfs, v));
+    aev[i] = df_add(df{1.f, 0.f}, df_mul(aef, v));
+    arg2[i] = df_add(df_add(psi0, df_neg(df_mul(w0c, kd[i]))),
+                     df_mul(c.p7pi_d, df_mul(tT, df_add(tT, df_neg(u2)))));
+  }
+  const int ai[6] = {0, 0, 1, 1, 2, 2};
+  const df mrs[6] = {mr12, mr13, mr12, mr23, mr13, mr23};
+  const df mis[6] = {mi12, mi13, mi12, mi23, mi13, mi23};
+  const df krs[6] = {kr12, kr13, df_neg(kr12), kr23, df_neg(kr13), df_neg(kr23)};
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    const int i = ai[a];
+    const df h1 = df_add(df{1.f, 0.f}, krs[a]);
+    const df arg1 = df_mul(df{0.5f * fon[i].hi, 0.5f * fon[i].lo}, h1);
+    const df sc = df_sinc(arg1);
+    const df sinc = {0.25f * sc.hi, 0.25f * sc.lo};
+    const df t1r = df_mul(aev[i], mrs[a]), t1i = df_mul(aev[i], mis[a]);
+    df s2, c2;
+    df_sincos(df_add(arg1, df_neg(arg2[i])), &s2, &c2);
+    const df re = df_add(df_mul(t1r, c2), df_mul(t1i, s2));
+    const df im = df_add(df_mul(t1i, c2), df_neg(df_mul(t1r, s2)));
+    d[a] = {df_mul(sinc, re), df_mul(sinc, im)};
+  }
+}
+
+// One warp per 32 consecutive samples of one binned proposal, grid-stride
+// over all of them; the four arm combinations of ae_combos in double-float.
+__global__ void __launch_bounds__(64) fd_slow_hp_kernel(SlowArgs a) {
+  int cs[kNumBins + 1];
+  int acc = 0;
+#pragma unroll
+  for (int b = 0; b < kNumBins; b++) {
+    cs[b] = acc;
+    if ((32 << b) <= a.NFFT) acc += a.bin_count[b] << b;
+  }
+  cs[kNumBins] = acc;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  float4 *series = reinterpret_cast<float4 *>(a.series);
+#pragma unroll 1
+  for (int ch = warp; ch < acc; ch += nwarps) {
+    int b = 0, cb = 0;
+#pragma unroll
+    for (int bb = 1; bb < kNumBins; bb++)
+      if (ch >= cs[bb]) {
+        b = bb;
+        cb = cs[bb];
+      }
+    const int N = 32 << b;
+    const int local = ch - cb;
+    const int slot = local >> b;
+    const int n = ((local & ((1 << b) - 1)) << 5) + lane;
+    const int item = a.bin_list[(size_t)b * a.cap + slot];
+    dc d[6];
+    slow_sample_hp(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.geolo[b][n], a, d);
+    // d: 12, 13, 21, 23, 31, 32
+    const dc a2 = dc_sub(dc_add(d[4], d[1]), dc_add(d[5], d[0]));
+    const dc a1 = dc_sub(dc_add(d[1], d[4]), dc_add(d[3], d[2]));
+    const dc t2 = dc_sub(d[2], d[3]), t1 = dc_sub(d[0], d[5]);
+    const dc e2 = dc_add(dc_sub(dc_sub(dc_add(d[0], d[4]), d[1]), d[5]), dc_add(t2, t2));
+    const dc e1 = dc_add(dc_sub(dc_sub(dc_add(d[1], d[2]), d[3]), d[4]), dc_add(t1, t1));
+    const dc cmb[4] = {a2, a1, e2, e1};
+    float4 *out = series + ((long long)cb * 32 + (long long)slot * N) * 4 + n;
+#pragma unroll
+    for (int s = 0; s < 4; s++)
+      out[(size_t)s * N] = make_float4(cmb[s].re.hi, cmb[s].im.hi, cmb[s].re.lo, cmb[s].im.lo);
+  }
+}
+
+// ------------------------------------------------------- spectral stage, df
+// The proposal of entry k (in size order): item, size, segment, placement,
+// size bin and series offset (float4 elements).
 struct HpEntry {
   int item, N, seg, imin, bin;
   long long off;
-  df amp;
-  bool pow2;
+  float amp_p2;
 };
 
-template <bool BIN>
 __device__ __forceinline__ HpEntry hp_entry(const HpArgs &a, int k, const int *cs) {
-  HpEntry e;
-  if constexpr (BIN) {
-    int bin = 0;
+  int bin = 0;
 #pragma unroll
-    for (int b = 1; b < kNumBins; b++)
-      if (k >= cs[b]) bin = b;
-    const int slot = k - cs[bin];
-    e.item = a.bin_list[(size_t)bin * a.cap + slot];
-    const ItemF64 &c = a.items64[e.item];
-    e.N = c.N;
-    e.seg = c.seg;
-    e.imin = c.imin;
-    e.bin = bin;
-    e.off = (bin_sample_start(a.bin_count, a.NFFT, bin) + (long long)slot * c.N) * 4;
-    e.amp = df_from_double(c.amp_s);
-    e.pow2 = false;
-  } else {
-    e.item = a.list[k];
-    const ItemMix &c = a.itemsmix[e.item];
-    e.N = c.N;
-    e.seg = c.seg;
-    e.imin = c.imin;
-    e.bin = fd_bin_of(c.N);
-    e.off = a.off[k];
-    e.amp = df{c.amp_p2, 0.f};
-    e.pow2 = true;
-  }
+  for (int b = 1; b < kNumBins; b++)
+    if (k >= cs[b]) bin = b;
+  const int slot = k - cs[bin];
+  HpEntry e;
+  e.item = a.bin_list[(size_t)bin * a.cap + slot];
+  const ItemMix &c = a.itemsmix[e.item];
+  e.N = c.N;
+  e.seg = c.seg;
+  e.imin = c.imin;
+  e.bin = bin;
+  e.off = (bin_sample_start(a.bin_count, a.NFFT, bin) + (long long)slot * c.N) * 4;
+  e.amp_p2 = c.amp_p2;
   return e;
 }
 
-template <bool BIN>
-__device__ __forceinline__ int hp_entries(const HpArgs &a, int *cs) {
-  int total = 0;
-  if constexpr (BIN) {
-#pragma unroll
-    for (int b = 0; b < kNumBins; b++) {
-      cs[b] = total;
-      if ((32 << b) <= a.NFFT) total += a.bin_count[b];
-    }
-    cs[kNumBins] = total;
-  } else {
-    total = *a.count;
-  }
-  return total;
-}
-
-// One series of the entry, as double-floats, into x.
-template <bool BIN>
-__device__ __forceinline__ void hp_load(const HpArgs &a, long long off, int N, dc *x) {
-  for (int n = threadIdx.x; n < N; n += blockDim.x) {
-    if constexpr (BIN) {
-      const double2 v = a.series64[off + n];
-      x[n] = {df_from_double(v.x), df_from_double(v.y)};
-    } else {
-      const float2 v = a.series32[off + n];
-      x[n] = {{v.x, 0.f}, {v.y, 0.f}};
-    }
-  }
-}
-
-template <bool BIN, bool PERCH>
+template <bool PERCH>
 __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
@@ -115,17 +199,24 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
   const int r = (int)cluster.block_rank(), ch = r >> 1;
   const int ncl = (int)(gridDim.x >> 2);
   int cs[kNumBins + 1];
-  const int total = hp_entries<BIN>(a, cs);
+  int total = 0;
+#pragma unroll
+  for (int b = 0; b < kNumBins; b++) {
+    cs[b] = total;
+    if ((32 << b) <= NFFT) total += a.bin_count[b];
+  }
+  cs[kNumBins] = total;
   int cur = -1;
   for (int k = (int)(blockIdx.x >> 2); k < total; k += ncl) {
-    const HpEntry e = hp_entry<BIN>(a, k, cs);
+    const HpEntry e = hp_entry(a, k, cs);
     const int N = e.N;
     if (e.bin != cur) {
       const float4 *tw = a.tw32x[e.bin];
       for (int n = threadIdx.x; n < N; n += blockDim.x) tws[n] = tw[n];
       cur = e.bin;
     }
-    hp_load<BIN>(a, e.off + (long long)r * N, N, xb);
+    const float4 *src = a.series + e.off + (long long)r * N;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) xb[n] = dc_from(src[n]);
     __syncthreads();
     dc *S = hp_fft(xb, yb, N, tws);
     cluster.sync();  // every spectrum of the proposal is complete
@@ -140,7 +231,7 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
       const float4 gh = a.g32[2 * sj + ch], gl = a.g32lo[2 * sj + ch];
       dc h = dc_add(dc_mul(S0[q], dc_from(make_float2(gh.x, gh.y), make_float2(gl.x, gl.y))),
                     dc_mul(S1[q], dc_from(make_float2(gh.z, gh.w), make_float2(gl.z, gl.w))));
-      h = e.pow2 ? dc_scale2(h, e.amp.hi) : dc_scale(h, e.amp);
+      h = dc_scale2(h, e.amp_p2);
       const float4 wh = a.w32[sj], wl = a.w32lo[sj];
       const dc w = ch == 0 ? dc_from(make_float2(wh.x, wh.y), make_float2(wl.x, wl.y))
                            : dc_from(make_float2(wh.z, wh.w), make_float2(wl.z, wl.w));
@@ -175,7 +266,7 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
 
 static size_t hp_smem_bytes(int nmax) { return (size_t)nmax * (2 * sizeof(dc) + sizeof(float4)); }
 
-template <bool BIN, bool PERCH>
+template <bool PERCH>
 static cudaError_t launch_hp(const HpArgs &a, int num_sms, cudaStream_t stream) {
   const size_t smem = hp_smem_bytes(a.nmax);
   cudaLaunchConfig_t cfg = {};
@@ -192,22 +283,29 @@ static cudaError_t launch_hp(const HpArgs &a, int num_sms, cudaStream_t stream) 
   static LaunchSetup setup[kNumBins];
   int ncl = 0;
   cudaError_t e = launch_setup(setup[fd_bin_of(a.nmax)], [&](int *o) {
-    cudaError_t r = cudaFuncSetAttribute(fd_hp_kernel<BIN, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t r = cudaFuncSetAttribute(fd_hp_kernel<PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hp_smem_bytes(kMaxN));
     if (r != cudaSuccess) return r;
     cudaLaunchConfig_t q = cfg;
     q.gridDim = dim3(4 * num_sms);
-    return cudaOccupancyMaxActiveClusters(o, fd_hp_kernel<BIN, PERCH>, &q);
+    return cudaOccupancyMaxActiveClusters(o, fd_hp_kernel<PERCH>, &q);
   }, &ncl);
   if (e != cudaSuccess) return e;
   if (ncl < 1) ncl = 1;
   cfg.gridDim = dim3(4 * ncl);
-  return cudaLaunchKernelEx(&cfg, fd_hp_kernel<BIN, PERCH>, a);
+  return cudaLaunchKernelEx(&cfg, fd_hp_kernel<PERCH>, a);
 }
 
-cudaError_t fd_launch_hp(const HpArgs &a, bool bin_mode, bool perch, int num_sms, cudaStream_t stream) {
-  if (bin_mode) return perch ? launch_hp<true, true>(a, num_sms, stream) : launch_hp<true, false>(a, num_sms, stream);
-  return perch ? launch_hp<false, true>(a, num_sms, stream) : launch_hp<false, false>(a, num_sms, stream);
+cudaError_t fd_launch_reeval(const PlanArgs &pa, const int *list, const int *count, const SlowArgs &sa,
+                             const HpArgs &h, bool perch, int num_sms, cudaStream_t stream, int *nlaunch) {
+  fd_hp_bin_kernel<<<num_sms, 64, 0, stream>>>(pa, list, count);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  fd_slow_hp_kernel<<<4 * num_sms, 64, 0, stream>>>(sa);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  e = perch ? launch_hp<true>(h, num_sms, stream) : launch_hp<false>(h, num_sms, stream);
+  if (nlaunch) *nlaunch += 3;
+  return e;
 }
 
 }  // namespace glass

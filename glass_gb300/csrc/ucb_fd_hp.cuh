@@ -1,6 +1,7 @@
-// Double-float (pairs of floats) complex arithmetic, the CTA-wide Stockham
-// FFT and reduction, and the result write of the double-float re-evaluation
-// of mixed proposals (ucb_fd_hp.cu).
+// Double-float (pairs of floats) arithmetic: complex operations, division,
+// sine, cosine and sinc, the CTA-wide Stockham FFT and reduction, and the
+// result write of the double-float re-evaluation of mixed proposals
+// (ucb_fd_hp.cu).
 #pragma once
 #include "glass_common.cuh"
 
@@ -25,6 +26,82 @@ __device__ __forceinline__ dc dc_scale2(dc a, float p2) {
   return {{a.re.hi * p2, a.re.lo * p2}, {a.im.hi * p2, a.im.lo * p2}};
 }
 __device__ __forceinline__ dc dc_scale(dc a, df s) { return {df_mul(a.re, s), df_mul(a.im, s)}; }
+
+// Double-float division (one Newton correction of the float quotient).
+__device__ __forceinline__ df df_div(df a, df b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const df r = df_add(a, df_neg(df_mul_f(b, q1)));
+  return quick_two_sum(q1, __fdiv_rn(r.hi, b.hi));
+}
+
+// Inverse factorials 1/n! as hi + lo floats, n = 0..19 (the Taylor
+// coefficients of sin and cos).
+__device__ __forceinline__ df inv_fact(int n) {
+  switch (n) {
+    case 0: case 1: return {1.f, 0.f};
+    case 2: return {0.5f, 0.f};
+    case 3: return {0.1666666716337204f, -4.967053879312289e-09f};
+    case 4: return {0.0416666679084301f, -1.2417634698280722e-09f};
+    case 5: return {0.008333333767950535f, -4.34617203337595e-10f};
+    case 6: return {0.0013888889225199819f, -3.3631094437103215e-11f};
+    case 7: return {0.00019841270113829523f, -2.725596874933456e-12f};
+    case 8: return {2.4801587642286904e-05f, -3.40699609366682e-13f};
+    case 9: return {2.7557318844628753e-06f, 3.793571224297229e-14f};
+    case 10: return {2.755731998149713e-07f, -7.575112209051195e-15f};
+    case 11: return {2.5052107943679403e-08f, 4.4176230446483665e-16f};
+    case 12: return {2.0876755879584152e-09f, 1.1082839147459852e-16f};
+    case 13: return {1.6059044372074283e-10f, -5.352526511562726e-18f};
+    case 14: return {1.147074536050896e-11f, 2.372207689231238e-19f};
+    case 15: return {7.647163609812713e-13f, 1.2200710471178288e-20f};
+    case 16: return {4.7794772561329454e-14f, 7.62544404448643e-22f};
+    case 17: return {2.8114573589663704e-15f, -1.0462084739763658e-22f};
+    case 18: return {1.5619206814541513e-16f, 1.5404471465941993e-24f};
+    default: return {8.220635078476521e-18f, 1.681478096855898e-25f};
+  }
+}
+
+// sum_k (-1)^k x2^k / (2k + first)!, k = 0..terms-1, by Horner in
+// double-float (first = 1: sin(x)/x; first = 0: cos x).
+template <int FIRST, int TERMS>
+__device__ __forceinline__ df df_alt_series(df x2) {
+  df p = inv_fact(2 * (TERMS - 1) + FIRST);
+  if ((TERMS - 1) & 1) p = df_neg(p);
+#pragma unroll
+  for (int k = TERMS - 2; k >= 0; k--) {
+    df c = inv_fact(2 * k + FIRST);
+    if (k & 1) c = df_neg(c);
+    p = df_add(df_mul(p, x2), c);
+  }
+  return p;
+}
+
+// sin and cos of a double-float angle of at most a few tens of radians:
+// reduction by pi/2 (three-part constant, exact products of the quadrant
+// count), then the Taylor series of sin (through r^17) and cos (through
+// r^16) on r in [-pi/4, pi/4] (truncation below 1e-16).
+__device__ __forceinline__ void df_sincos(df x, df *s, df *c) {
+  const float q = rintf(x.hi * 0.63661977236758134f);
+  df r = df_add(x, df_neg(two_prod(q, 1.5707963705062866f)));
+  r = df_add(r, df_neg(two_prod(q, -4.371138828673793e-08f)));
+  r = df_add(r, df{q * 1.7151245100058819e-15f, 0.f});
+  const df r2 = df_mul(r, r);
+  const df sr = df_mul(r, df_alt_series<1, 9>(r2));
+  const df cr = df_alt_series<0, 9>(r2);
+  const int qi = ((int)q) & 3;
+  const df ss = (qi & 1) ? cr : sr;
+  const df cc = (qi & 1) ? sr : cr;
+  *s = (qi & 2) ? df_neg(ss) : ss;
+  *c = ((qi + 1) & 2) ? df_neg(cc) : cc;
+}
+
+// sin(x)/x in double-float: Taylor series through x^18 for |x| <= 1
+// (truncation below 1e-17), sin x / x beyond.
+__device__ __forceinline__ df df_sinc(df x) {
+  if (fabsf(x.hi) <= 1.f) return df_alt_series<1, 10>(df_mul(x, x));
+  df s, c;
+  df_sincos(x, &s, &c);
+  return df_div(s, x);
+}
 
 // Stockham FFT of one series of N double-floats by the CTA, ping-ponging
 // between x and y: radix-4 stages (sub-transform size p: butterfly i < N/4,

@@ -391,10 +391,8 @@ int glass_gpu_set_mixed_tolerance(glass_gpu_ctx *ctx, double tol);
  * proposal, and only the cold chains' proposals need delta logL itself to
  * tol.  Synchronises the context's stream. */
 int glass_gpu_set_mixed_tolerance_scale(glass_gpu_ctx *ctx, int n, const double *scale);
-/* Numbers of proposals re-evaluated since the context's work buffers were
- * allocated: count[0] with a double-float spectral stage on their mixed
- * series, count[1] (disjoint from those) with FP64 series.  Synchronises the
- * context's stream. */
+/* Number of proposals re-evaluated in double-float since the context's work
+ * buffers were allocated.  Synchronises the context's stream. */
 int glass_gpu_mixed_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count);
 
 /* ------------------------------------------- batch that allocates nothing */

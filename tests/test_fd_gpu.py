@@ -194,11 +194,11 @@ def _loud_batch(rng, inj, nseg):
 
 
 def test_mixed_tolerance_tiers(engine, port):
-    """Default tolerance: every proposal within 1e-3 of FP64, with both
-    re-evaluation tiers used on loud templates; per-proposal scale (the
-    temperature): |error| / T within 1e-3 with fewer re-evaluations; zero
-    tolerance: no re-evaluation.  A CUDA-graph replay (conditional node
-    around the FP64-series tier) reproduces the direct launch exactly."""
+    """Default tolerance: every proposal within 1e-3 of FP64, with the
+    double-float re-evaluation used on loud templates; per-proposal scale
+    (the temperature): |error| / T within 1e-3 with fewer re-evaluations;
+    zero tolerance: no re-evaluation.  A CUDA-graph replay (conditional node
+    around the re-evaluation) reproduces the direct launch exactly."""
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(77)
     bank, inj = _random_bank(rng, 16, 1024, port, amp=(1e-22, 1e-21))
@@ -208,22 +208,22 @@ def test_mixed_tolerance_tiers(engine, port):
     d64 = engine.dlogl_host(seg, params, term_x=tx, precision=gg.PREC_FP64)[0]
     try:
         engine.set_mixed_tolerance(1e-3)
-        n0 = np.array(engine.mixed_reevaluated())
+        n0 = engine.mixed_reevaluated()
         dm = engine.dlogl_host(seg, params, term_x=tx, precision=gg.PREC_MIXED)[0]
-        n1 = np.array(engine.mixed_reevaluated())
+        n1 = engine.mixed_reevaluated()
         assert_mixed_close(dm, d64)
-        assert (n1 - n0 > 0).all(), n1 - n0
+        assert n1 > n0
         # per-proposal scale
         engine.set_mixed_tolerance_scale(temps)
         dt = engine.dlogl_host(seg, params, term_x=tx, precision=gg.PREC_MIXED)[0]
-        n2 = np.array(engine.mixed_reevaluated())
+        n2 = engine.mixed_reevaluated()
         assert_mixed_close(dt, d64, scale=temps)
-        assert (n2 - n1).sum() < (n1 - n0).sum()
+        assert 0 < n2 - n1 < n1 - n0
         engine.set_mixed_tolerance_scale(None)
         # raw mixed
         engine.set_mixed_tolerance(0.0)
         dr = engine.dlogl_host(seg, params, term_x=tx, precision=gg.PREC_MIXED)[0]
-        assert (np.array(engine.mixed_reevaluated()) == n2).all()
+        assert engine.mixed_reevaluated() == n2
         assert np.abs(dr - d64).max() > np.abs(dm - d64).max()
         # graph replay of the default tolerance
         engine.set_mixed_tolerance(1e-3)
