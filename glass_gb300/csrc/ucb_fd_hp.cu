@@ -11,10 +11,11 @@
 // runs 64 times the FP64 rate), in three launches:
 //   fd_hp_bin_kernel:  the listed proposals binned by size;
 //   fd_slow_hp_kernel: their four A/E arm-combination series in
-//     double-float, one warp per 32 samples: the mixed slow part's formulation
+//     double-float, three warps per 32 samples: the mixed slow part's formulation
 //     (carrier phase heterodyned to the segment and reduced mod 2 pi, so that
 //     its absolute error stays ~1e-12 rad) with every product and sum in
-//     double-float, double-float sine, cosine and sinc, and the per-sample
+//     double-float, double-float sine, cosine (table of k pi/32 plus short
+//     Taylor series) and sinc, and the per-sample
 //     geometry and per-proposal constants as hi + lo floats;
 //   fd_hp_kernel:      thread-block clusters of 4 CTAs, one proposal each:
 //     CTA r transforms series r in its shared memory (radix-4 Stockham,
@@ -50,73 +51,74 @@ __global__ void __launch_bounds__(64) fd_hp_bin_kernel(PlanArgs a, const int *li
 }
 
 // -------------------------------------------------------- slow part, df
-// The six arm series at one sample, as slow_sample_mix computes them, in
-// double-float throughout.
-__device__ __forceinline__ void slow_sample_hp(const ItemMix &c, const OrbitSampleMix &o, const GeoSampleMix &gm,
-                                               const GeoSampleMix &gl, const SlowArgs &K, dc d[6]) {
-  df f[27];
-#pragma unroll
-  for (int q = 0; q < 27; q++) f[q] = df{gm.f[q], gl.f[q]};
+// The two arms of spacecraft i (12, 13 | 21, 23 | 31, 32) at one sample, as
+// slow_sample_mix computes them, in double-float throughout.  tab: the
+// sine/cosine table of df_sincos_tab.
+__device__ __forceinline__ void slow_arms_hp(const ItemMix &c, const OrbitSampleMix &o, const GeoSampleMix &gm,
+                                             const GeoSampleMix &gl, const SlowArgs &K, const float4 *tab, int i,
+                                             dc d[2]) {
   const df k0 = {c.k[0], c.kl[0]}, k1 = {c.k[1], c.kl[1]}, k2 = {c.k[2], c.kl[2]};
-  // k.(x_i - x_gc) per spacecraft (metres); k.r_ij from their differences
+  // k.(x_j - x_gc) for the three spacecraft (metres)
   df kd[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++)
-    kd[i] = df_add(df_add(df_mul(k0, f[3 * i]), df_mul(k1, f[3 * i + 1])), df_mul(k2, f[3 * i + 2]));
-  const df kr12 = df_mul(df_add(kd[1], df_neg(kd[0])), K.invLd);
-  const df kr13 = df_mul(df_add(kd[2], df_neg(kd[0])), K.invLd);
-  const df kr23 = df_mul(df_add(kd[2], df_neg(kd[1])), K.invLd);
-  // r^T M r of the three arms, M = m (DP e+ + DC ex) as hi + lo
-  auto quad6 = [&](const float *M, const float *Ml, int a) {
-    const df *mo = f + 9 + 6 * a;
-    df acc = df_mul(df{M[0], Ml[0]}, mo[0]);
-#pragma unroll
-    for (int q = 1; q < 6; q++) acc = df_add(acc, df_mul(df{M[q], Ml[q]}, mo[q]));
-    return acc;
-  };
-  const df mr12 = quad6(c.Mr, c.Mrl, 0), mi12 = quad6(c.Mi, c.Mil, 0);
-  const df mr13 = quad6(c.Mr, c.Mrl, 1), mi13 = quad6(c.Mi, c.Mil, 1);
-  const df mr23 = quad6(c.Mr, c.Mrl, 2), mi23 = quad6(c.Mi, c.Mil, 2);
-
+  for (int j = 0; j < 3; j++)
+    kd[j] = df_add(df_add(df_mul(k0, df{gm.f[3 * j], gl.f[3 * j]}), df_mul(k1, df{gm.f[3 * j + 1], gl.f[3 * j + 1]})),
+                   df_mul(k2, df{gm.f[3 * j + 2], gl.f[3 * j + 2]}));
+  // this spacecraft's two arms as unique arms (0: 12, 1: 13, 2: 23) with the
+  // orientation signs of k.r: 12 +0, 13 +1 | 21 -0, 23 +2 | 31 -1, 32 -2
+  const int ua[2] = {i == 2 ? 1 : 0, i == 0 ? 1 : 2};
+  const bool neg[2] = {i != 0, i == 2};
+  const int ends[3][2] = {{0, 1}, {0, 2}, {1, 2}};
   const df psi0 = carrier_phase_mix(c, o);
   const df u = {o.u_hi, o.u_lo}, ca = {o.ca_hi, o.ca_lo}, sa = {o.sa_hi, o.sa_lo};
   const df tgc = df_mul(K.AUcd, df_add(df_mul(k0, ca), df_mul(k1, sa)));  // guiding-centre delay (s)
-  const df fonfs0 = {c.fonfs0, c.fonfs0l}, fdfs = {c.fdfs, c.fdfsl}, aef = {c.aef, c.aefl};
-  const df w0c = {c.w0c, c.w0cl};
-  const df u2 = df{2.f * u.hi, 2.f * u.lo};
-  df fon[3], aev[3], arg2[3];
+  const df tT = df_mul(df_add(tgc, df_mul(kd[i], K.invcd)), K.invTd);    // tau_i / T
+  const df v = df_add(u, df_neg(tT));                                    // xi / T
+  const df fon = df_add(df{c.fonfs0, c.fonfs0l}, df_mul(df{c.fdfs, c.fdfsl}, v));
+  const df aev = df_add(df{1.f, 0.f}, df_mul(df{c.aef, c.aefl}, v));
+  const df arg2 = df_add(df_add(psi0, df_neg(df_mul(df{c.w0c, c.w0cl}, kd[i]))),
+                         df_mul(c.p7pi_d, df_mul(tT, df_add(tT, df{-2.f * u.hi, -2.f * u.lo}))));
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    const df tT = df_mul(df_add(tgc, df_mul(kd[i], K.invcd)), K.invTd);  // tau_i / T
-    const df v = df_add(u, df_neg(tT));                                 // xi / T
-    fon[i] = df_add(fonfs0, df_mul(fdfs, v));
-    aev[i] = df_add(df{1.f, 0.f}, df_mul(aef, v));
-    arg2[i] = df_add(df_add(psi0, df_neg(df_mul(w0c, kd[i]))),
-                     df_mul(c.p7pi_d, df_mul(tT, df_add(tT, df_neg(u2)))));
-  }
-  const int ai[6] = {0, 0, 1, 1, 2, 2};
-  const df mrs[6] = {mr12, mr13, mr12, mr23, mr13, mr23};
-  const df mis[6] = {mi12, mi13, mi12, mi23, mi13, mi23};
-  const df krs[6] = {kr12, kr13, df_neg(kr12), kr23, df_neg(kr13), df_neg(kr23)};
+  for (int q = 0; q < 2; q++) {
+    const int a = ua[q];
+    df kr = df_mul(df_add(kd[ends[a][1]], df_neg(kd[ends[a][0]])), K.invLd);
+    if (neg[q]) kr = df_neg(kr);
+    // r^T M r with M = m (DP e+ + DC ex) as hi + lo
+    df mr = {0.f, 0.f}, mi = {0.f, 0.f};
 #pragma unroll
-  for (int a = 0; a < 6; a++) {
-    const int i = ai[a];
-    const df h1 = df_add(df{1.f, 0.f}, krs[a]);
-    const df arg1 = df_mul(df{0.5f * fon[i].hi, 0.5f * fon[i].lo}, h1);
-    const df sc = df_sinc(arg1);
+    for (int t = 0; t < 6; t++) {
+      const df mo = {gm.f[9 + 6 * a + t], gl.f[9 + 6 * a + t]};
+      mr = df_add(mr, df_mul(df{c.Mr[t], c.Mrl[t]}, mo));
+      mi = df_add(mi, df_mul(df{c.Mi[t], c.Mil[t]}, mo));
+    }
+    const df h1 = df_add(df{1.f, 0.f}, kr);
+    const df arg1 = df_mul(df{0.5f * fon.hi, 0.5f * fon.lo}, h1);
+    const df sc = df_sinc(arg1, tab);
     const df sinc = {0.25f * sc.hi, 0.25f * sc.lo};
-    const df t1r = df_mul(aev[i], mrs[a]), t1i = df_mul(aev[i], mis[a]);
+    const df t1r = df_mul(aev, mr), t1i = df_mul(aev, mi);
     df s2, c2;
-    df_sincos(df_add(arg1, df_neg(arg2[i])), &s2, &c2);
+    df_sincos_tab(df_add(arg1, df_neg(arg2)), tab, &s2, &c2);
     const df re = df_add(df_mul(t1r, c2), df_mul(t1i, s2));
     const df im = df_add(df_mul(t1i, c2), df_neg(df_mul(t1r, s2)));
-    d[a] = {df_mul(sinc, re), df_mul(sinc, im)};
+    d[q] = {df_mul(sinc, re), df_mul(sinc, im)};
   }
 }
 
-// One warp per 32 consecutive samples of one binned proposal, grid-stride
-// over all of them; the four arm combinations of ae_combos in double-float.
-__global__ void __launch_bounds__(64) fd_slow_hp_kernel(SlowArgs a) {
+// One CTA of three warps per 32 consecutive samples of one binned proposal,
+// grid-stride over all of them: warp i computes the arms of spacecraft i (a
+// third of the dependent chain of a sample each, on separate SM
+// sub-partitions); warps 0 and 1 then form the A and E arm combinations of
+// ae_combos in double-float.
+__global__ void __launch_bounds__(96) fd_slow_hp_kernel(SlowArgs a) {
+  __shared__ dc s_d[6][32];
+  __shared__ float4 s_tab[64];
+  if (threadIdx.x < 64) {
+    double sn, cs;
+    sincospi((double)threadIdx.x / 32.0, &sn, &cs);
+    const df s = df_from_double(sn), c = df_from_double(cs);
+    s_tab[threadIdx.x] = make_float4(s.hi, s.lo, c.hi, c.lo);
+  }
+  __syncthreads();
   int cs[kNumBins + 1];
   int acc = 0;
 #pragma unroll
@@ -125,12 +127,10 @@ __global__ void __launch_bounds__(64) fd_slow_hp_kernel(SlowArgs a) {
     if ((32 << b) <= a.NFFT) acc += a.bin_count[b] << b;
   }
   cs[kNumBins] = acc;
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31, sc = threadIdx.x >> 5;
   float4 *series = reinterpret_cast<float4 *>(a.series);
 #pragma unroll 1
-  for (int ch = warp; ch < acc; ch += nwarps) {
+  for (int ch = blockIdx.x; ch < acc; ch += gridDim.x) {
     int b = 0, cb = 0;
 #pragma unroll
     for (int bb = 1; bb < kNumBins; bb++)
@@ -143,19 +143,30 @@ __global__ void __launch_bounds__(64) fd_slow_hp_kernel(SlowArgs a) {
     const int slot = local >> b;
     const int n = ((local & ((1 << b) - 1)) << 5) + lane;
     const int item = a.bin_list[(size_t)b * a.cap + slot];
-    dc d[6];
-    slow_sample_hp(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.geolo[b][n], a, d);
-    // d: 12, 13, 21, 23, 31, 32
-    const dc a2 = dc_sub(dc_add(d[4], d[1]), dc_add(d[5], d[0]));
-    const dc a1 = dc_sub(dc_add(d[1], d[4]), dc_add(d[3], d[2]));
-    const dc t2 = dc_sub(d[2], d[3]), t1 = dc_sub(d[0], d[5]);
-    const dc e2 = dc_add(dc_sub(dc_sub(dc_add(d[0], d[4]), d[1]), d[5]), dc_add(t2, t2));
-    const dc e1 = dc_add(dc_sub(dc_sub(dc_add(d[1], d[2]), d[3]), d[4]), dc_add(t1, t1));
-    const dc cmb[4] = {a2, a1, e2, e1};
-    float4 *out = series + ((long long)cb * 32 + (long long)slot * N) * 4 + n;
+    dc d2[2];
+    slow_arms_hp(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.geolo[b][n], a, s_tab, sc, d2);
+    s_d[2 * sc][lane] = d2[0];
+    s_d[2 * sc + 1][lane] = d2[1];
+    __syncthreads();
+    if (sc < 2) {
+      dc d[6];
 #pragma unroll
-    for (int s = 0; s < 4; s++)
-      out[(size_t)s * N] = make_float4(cmb[s].re.hi, cmb[s].im.hi, cmb[s].re.lo, cmb[s].im.lo);
+      for (int q = 0; q < 6; q++) d[q] = s_d[q][lane];
+      // d: 12, 13, 21, 23, 31, 32
+      dc c0, c1;
+      if (sc == 0) {
+        c0 = dc_sub(dc_add(d[4], d[1]), dc_add(d[5], d[0]));  // a2
+        c1 = dc_sub(dc_add(d[1], d[4]), dc_add(d[3], d[2]));  // a1
+      } else {
+        const dc t2 = dc_sub(d[2], d[3]), t1 = dc_sub(d[0], d[5]);
+        c0 = dc_add(dc_sub(dc_sub(dc_add(d[0], d[4]), d[1]), d[5]), dc_add(t2, t2));  // e2
+        c1 = dc_add(dc_sub(dc_sub(dc_add(d[1], d[2]), d[3]), d[4]), dc_add(t1, t1));  // e1
+      }
+      float4 *out = series + ((long long)cb * 32 + (long long)slot * N) * 4 + (size_t)(2 * sc) * N + n;
+      out[0] = make_float4(c0.re.hi, c0.im.hi, c0.re.lo, c0.im.lo);
+      out[N] = make_float4(c1.re.hi, c1.im.hi, c1.re.lo, c1.im.lo);
+    }
+    __syncthreads();
   }
 }
 
@@ -301,7 +312,13 @@ cudaError_t fd_launch_reeval(const PlanArgs &pa, const int *list, const int *cou
   fd_hp_bin_kernel<<<num_sms, 64, 0, stream>>>(pa, list, count);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  fd_slow_hp_kernel<<<4 * num_sms, 64, 0, stream>>>(sa);
+  static LaunchSetup slow_setup;
+  int occ = 0;
+  e = launch_setup(slow_setup, [&](int *o) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_slow_hp_kernel, 96, 0);
+  }, &occ);
+  if (e != cudaSuccess) return e;
+  fd_slow_hp_kernel<<<(occ > 0 ? occ : 1) * num_sms, 96, 0, stream>>>(sa);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   e = perch ? launch_hp<true>(h, num_sms, stream) : launch_hp<false>(h, num_sms, stream);
   if (nlaunch) *nlaunch += 3;

@@ -94,12 +94,33 @@ __device__ __forceinline__ void df_sincos(df x, df *s, df *c) {
   *c = ((qi + 1) & 2) ? df_neg(cc) : cc;
 }
 
-// sin(x)/x in double-float: Taylor series through x^18 for |x| <= 1
-// (truncation below 1e-17), sin x / x beyond.
-__device__ __forceinline__ df df_sinc(df x) {
-  if (fabsf(x.hi) <= 1.f) return df_alt_series<1, 10>(df_mul(x, x));
+// sin and cos of a double-float angle with a table: tab[k] = (sin, cos) of
+// k pi/32 as hi + lo floats (float4: sin hi, sin lo, cos hi, cos lo), k mod
+// 64; x = k pi/32 + d with |d| <= pi/64 (three-part pi/32), whose sine
+// (through d^7) and cosine (through d^8) have truncation errors below 1e-15;
+// then the angle-sum formulas.
+__device__ __forceinline__ void df_sincos_tab(df x, const float4 *tab, df *s, df *c) {
+  const float q = rintf(x.hi * 10.185916357881302f);  // 32/pi
+  df d = df_add(x, df_neg(two_prod(q, 0.09817477315664291f)));
+  d = df_add(d, df_neg(two_prod(q, -2.7319617679211206e-09f)));
+  d = df_add(d, df{q * 1.0719528187536762e-16f, 0.f});
+  const df d2 = df_mul(d, d);
+  const df sd = df_mul(d, df_alt_series<1, 4>(d2));
+  const df cd = df_alt_series<0, 5>(d2);
+  const float4 t = tab[((int)q) & 63];
+  const df sk = {t.x, t.y}, ck = {t.z, t.w};
+  *s = df_add(df_mul(sk, cd), df_mul(ck, sd));
+  *c = df_add(df_mul(ck, cd), df_neg(df_mul(sk, sd)));
+}
+
+// sin(x)/x in double-float: Taylor series through x^12 for |x| <= 1/2 and
+// through x^18 for |x| <= 1 (truncation below 1e-17), sin x / x beyond.
+__device__ __forceinline__ df df_sinc(df x, const float4 *tab) {
+  const float ax = fabsf(x.hi);
+  if (ax <= 0.5f) return df_alt_series<1, 7>(df_mul(x, x));
+  if (ax <= 1.f) return df_alt_series<1, 10>(df_mul(x, x));
   df s, c;
-  df_sincos(x, &s, &c);
+  df_sincos_tab(x, tab, &s, &c);
   return df_div(s, x);
 }
 
