@@ -37,7 +37,7 @@ cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t st
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
-cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch, bool fused);
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_spec_all_fp64(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
 
 // ------------------------------------------------------------- plan kernels
@@ -516,14 +516,9 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     sa.geo[b] = tab.geo[b];
   }
   sa.series = work.series;
-  // mixed precision: the series of sizes up to 1024 are computed by the
-  // spectral kernel itself (in shared memory); the slow-part kernel runs for
-  // 2048 and 4096 only, beside it on a side stream (below)
-  if (!mix) {
-    e = fd_launch_slow_fp64(sa, num_sms, stream);
-    launches++;
-    if (e != cudaSuccess) return e;
-  }
+  e = mix ? fd_launch_slow_mixed(sa, num_sms, stream) : fd_launch_slow_fp64(sa, num_sms, stream);
+  launches++;
+  if (e != cudaSuccess) return e;
   if (timing && (e = cudaEventRecord(work.phase[2], stream)) != cudaSuccess) return e;
 
   SpecArgs a;
@@ -538,13 +533,6 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.g32 = bank.g32;
   a.g32lo = bank.g32lo;
   a.Q = bank.Q;
-  for (int b = 0; b < kNumBins; b++) {
-    a.omix[b] = tab.mix[b];
-    a.ogeo[b] = tab.geo[b];
-  }
-  a.invLf = sa.invLf;
-  a.AUcf = sa.AUcf;
-  a.invTf = sa.invTf;
   a.w64 = bank.w64;
   a.g64 = bank.g64;
   a.term_x = term_x;
@@ -581,28 +569,17 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   }
   // sizes up to 1024 (every size a segment of NFFT bins can produce, up to
   // NFFT: ucb_bandwidth caps N there) in one launch on the main stream; 2048
-  // and 4096 as their own kernels on side streams running beside it (mixed:
-  // after their slow part, on the first of those streams)
+  // and 4096 as their own kernels on side streams running beside it
   int nall = 0;
   while (nall < kSpecAllBins && (32 << nall) <= bank.NFFT) nall++;
   int nb = 0;
   if (bank.NFFT > 1024) {
     if ((e = cudaEventRecord(work.fork, stream)) != cudaSuccess) return e;
-    if (mix) {
-      cudaStream_t s0 = work.side[kSpecAllBins];
-      if ((e = cudaStreamWaitEvent(s0, work.fork, 0)) != cudaSuccess) return e;
-      SlowArgs sb = sa;
-      sb.bin_lo = kSpecAllBins;
-      e = fd_launch_slow_mixed(sb, num_sms, s0);
-      launches++;
-      if (e != cudaSuccess) return e;
-      if ((e = cudaEventRecord(work.join[0], s0)) != cudaSuccess) return e;
-    }
     for (int b = kSpecAllBins; b < kNumBins; b++) {
       int N = 32 << b;
       if (N > bank.NFFT) break;
       cudaStream_t sb = work.side[b];
-      if ((e = cudaStreamWaitEvent(sb, mix ? work.join[0] : work.fork, 0)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(sb, work.fork, 0)) != cudaSuccess) return e;
       a.bin = b;
       a.bin_list = work.bin_list + (size_t)b * work.cap;
       a.tw = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
@@ -624,15 +601,14 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
     A.done = work.bin_count + kNumBins + 1;  // fb_count is at kNumBins
     for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
-    e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch, true)
-            : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
+    e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch) : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
     launches++;
     if (e != cudaSuccess) return e;
   }
   for (int b = kSpecAllBins; b < kSpecAllBins + nb; b++)
     if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;
-  if (nb > 0 || nall == 0) {  // the size counts only: fb_count follows them
-    if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kNumBins, stream)) != cudaSuccess) return e;
+  if (nb > 0 || nall == 0) {
+    if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream)) != cudaSuccess) return e;
   }
   if (timing && (e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
 

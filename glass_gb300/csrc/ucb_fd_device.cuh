@@ -960,7 +960,6 @@ struct SlowArgs {
   const OrbitSampleMix *mix[kNumBins];
   const GeoSampleMix *geo[kNumBins] = {};  // mixed only
   void *series;  // float2 (mixed) or double2 (FP64)
-  int bin_lo = 0;  // sizes below 32 << bin_lo are skipped (their series are computed in the spectral kernel)
   // double-float slow part of the re-evaluation: the geometry's low parts
   // and 1/L, AU/c, 1/T, 1/c as hi + lo floats; series as float4
   const GeoSampleMix *geolo[kNumBins] = {};
@@ -975,12 +974,6 @@ struct SpecArgs {
   const ItemF64 *items64;
   const ItemMix *itemsmix;
   const void *series;
-  // fused mixed kernel: the slow part's per-size orbit tables and FP32
-  // constants (1/L, AU/c, 1/T), from which each group computes its
-  // proposal's series in shared memory instead of reading `series`
-  const OrbitSampleMix *omix[kNumBins] = {};
-  const GeoSampleMix *ogeo[kNumBins] = {};
-  float invLf = 0.f, AUcf = 0.f, invTf = 0.f;
   const void *tw;
   const float4 *w32;
   const float4 *w32lo;
@@ -1070,16 +1063,12 @@ __global__ void __launch_bounds__(BLOCK) fd_slow_kernel(SlowArgs a) {
   }
   cs[kNumBins] = acc;
   const int nchunks = acc;
-  int first = 0;
-#pragma unroll
-  for (int b = 0; b < kNumBins; b++)
-    if (b == a.bin_lo) first = cs[b];
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   C *series = reinterpret_cast<C *>(a.series);
 #pragma unroll 1
-  for (int ch = first + warp; ch < nchunks; ch += nwarps) {
+  for (int ch = warp; ch < nchunks; ch += nwarps) {
     int b = 0, cb = 0;
 #pragma unroll
     for (int bb = 1; bb < kNumBins; bb++)
@@ -1217,7 +1206,7 @@ namespace glass {
 // (from the slow kernel's scratch) are FFT'd in shared memory, weighted per bin
 // by the segment's TDI/whitening table and reduced to the residual power.
 // reds: 96 doubles of reduction scratch per group.
-template <int N, bool MIX, int GPC, bool PERCH = false, bool FUSED = false>
+template <int N, bool MIX, int GPC, bool PERCH = false>
 __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list, int count, int base,
                                           const typename SpecSmem<N, MIX>::C *series,
                                           const typename SpecSmem<N, MIX>::TW *tw,
@@ -1252,23 +1241,7 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   double accE = 0.0;
 #pragma unroll 1
   for (int pass = 0; pass < PASSES; ++pass) {
-    if constexpr (MIX && FUSED) {
-      // the slow part for samples lane + GT r of this proposal, straight into
-      // the padded shared-memory rows that the FFT reads
-      const ItemMix &ci = a.itemsmix[item];
-      constexpr int b = fd_bin_of(N);
-#pragma unroll 1
-      for (int r = 0; r < B; ++r) {
-        const int n = lane + GT * r;
-        float2 d6[6], cmb[4];
-        slow_sample_mix(ci, a.omix[b][n], a.ogeo[b][n], a.invLf, a.AUcf, a.invTf, d6);
-        ae_combos(d6, cmb);
-#pragma unroll
-        for (int s4 = 0; s4 < 4; ++s4) buf[s4 * SN + pad16(n)] = cmb[s4];
-      }
-      group_sync<GT>();
-      fft_reg_smem<N, GT, 4>(buf, tw, lane);
-    } else if constexpr (MIX) {
+    if constexpr (MIX) {
       fft4_reg<N, GT>(src, buf, tw, lane);
     } else {
 #pragma unroll
@@ -1439,8 +1412,8 @@ struct SpecAllArgs {
   int *done = nullptr;           // CTA-done counter (zero between launches)
 };
 
-template <bool MIX, bool PERCH = false, bool FUSED = false>
-__global__ void __launch_bounds__(kSpecAllThreads, FUSED ? 2 : 4) fd_spec_all_kernel(SpecAllArgs A) {
+template <bool MIX, bool PERCH = false>
+__global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAllArgs A) {
   using C = typename SpecAllSmem<MIX>::C;
   using TW = typename SpecAllSmem<MIX>::TW;
   const SpecArgs &a = A.a;
@@ -1482,12 +1455,12 @@ __global__ void __launch_bounds__(kSpecAllThreads, FUSED ? 2 : 4) fd_spec_all_ke
     const int *bl = a.bin_list + (size_t)b * a.cap;
     const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, b) * 4;
     switch (b) {
-      case 0: spec_unit<32, MIX, 32, PERCH, FUSED>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 1: spec_unit<64, MIX, 16, PERCH, FUSED>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 2: spec_unit<128, MIX, 8, PERCH, FUSED>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 3: spec_unit<256, MIX, 4, PERCH, FUSED>(a, bl, count, base, series, tw, bufs, reds); break;
-      case 4: spec_unit<512, MIX, 2, PERCH, FUSED>(a, bl, count, base, series, tw, bufs, reds); break;
-      default: spec_unit<1024, MIX, 1, PERCH, FUSED>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 0: spec_unit<32, MIX, 32, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 1: spec_unit<64, MIX, 16, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 2: spec_unit<128, MIX, 8, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 3: spec_unit<256, MIX, 4, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      case 4: spec_unit<512, MIX, 2, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
+      default: spec_unit<1024, MIX, 1, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
     }
   }
   // the last CTA to finish leaves the size counts at zero for the next
@@ -1506,20 +1479,19 @@ __global__ void __launch_bounds__(kSpecAllThreads, FUSED ? 2 : 4) fd_spec_all_ke
   }
 }
 
-template <bool MIX, bool PERCH = false, bool FUSED = false>
+template <bool MIX, bool PERCH = false>
 static cudaError_t launch_spec_all(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
   const size_t smem = SpecAllSmem<MIX>::bytes;
   static LaunchSetup setup;
   int occ = 0;
   cudaError_t e = launch_setup(setup, [&](int *o) {
-    cudaError_t r = cudaFuncSetAttribute(fd_spec_all_kernel<MIX, PERCH, FUSED>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t r = cudaFuncSetAttribute(fd_spec_all_kernel<MIX, PERCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (r != cudaSuccess) return r;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_spec_all_kernel<MIX, PERCH, FUSED>, kSpecAllThreads,
-                                                         smem);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_spec_all_kernel<MIX, PERCH>, kSpecAllThreads, smem);
   }, &occ);
   if (e != cudaSuccess) return e;
-  fd_spec_all_kernel<MIX, PERCH, FUSED><<<occ * num_sms, kSpecAllThreads, smem, stream>>>(A);
+  fd_spec_all_kernel<MIX, PERCH><<<occ * num_sms, kSpecAllThreads, smem, stream>>>(A);
   return cudaGetLastError();
 }
 

@@ -29,9 +29,7 @@ cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_s
   return cudaErrorInvalidValue;
 }
 
-cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch, bool fused) {
-  if (fused) return perch ? launch_spec_all<true, true, true>(A, num_sms, stream)
-                          : launch_spec_all<true, false, true>(A, num_sms, stream);
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch) {
   if (perch) return launch_spec_all<true, true>(A, num_sms, stream);
   return launch_spec_all<true>(A, num_sms, stream);
 }
