@@ -607,8 +607,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   }
   for (int b = kSpecAllBins; b < kSpecAllBins + nb; b++)
     if ((e = cudaStreamWaitEvent(stream, work.join[b], 0)) != cudaSuccess) return e;
-  if (nb > 0 || nall == 0) {
-    if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 1), stream)) != cudaSuccess) return e;
+  if (nb > 0 || nall == 0) {  // the size counts only: fb_count follows them
+    if ((e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kNumBins, stream)) != cudaSuccess) return e;
   }
   if (timing && (e = cudaEventRecord(work.phase[3], stream)) != cudaSuccess) return e;
 
