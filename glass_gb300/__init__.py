@@ -53,6 +53,10 @@ EXPORTS = (
     "glass_gpu_dlogl_batch_channels", "glass_gpu_noise_eta_batch", "glass_gpu_noise_eta_batch_host",
     "glass_gpu_rand_r_fill", "glass_gpu_mh_accept", "glass_gpu_fisher_draw", "glass_gpu_ptmcmc",
     "glass_gpu_set_mixed_tolerance", "glass_gpu_set_mixed_tolerance_scale", "glass_gpu_mixed_reevaluated",
+    "glass_gpu_wdm_by_layers_host", "wavelet_transform_timefreq_by_layers",
+    "analytic_orbits", "initialize_analytic_orbit", "map_array_to_ucb_params", "ucb_alignment", "add_ucb_model",
+    "remove_ucb_model", "generate_ucb_model", "update_ucb_model", "fourier_nwip", "snr", "gaussian_log_likelihood",
+    "matrix_eigenstuff", "ucb_fisher",
 )
 
 _lib = None

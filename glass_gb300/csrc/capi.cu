@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/glass_gb300.h"
+#include "dropin.h"
 #include "noise.cuh"
 #include "sampler.cuh"
 #include "ucb_fd.cuh"
@@ -1699,6 +1700,40 @@ extern "C" int glass_gpu_wdm_inverse_host(glass_gpu_ctx *ctx, int precision, int
   return wdm_host(ctx, precision, NF, NT, A, nx, wdm, time, false);
 }
 
+extern "C" int glass_gpu_wdm_by_layers_host(glass_gpu_ctx *ctx, int NF, int NT, int jmin, int nlayers,
+                                            const double *window, double *timedata) {
+  if (!ctx || !window || !timedata) return set_err(GLASS_ERR_ARG, "glass_gpu_wdm_by_layers_host: null argument");
+  const long long N = (long long)NT * (nlayers + 1);
+  int r = (int)(N / 2);
+  while (r > 1 && r % 3 == 0) r /= 3;
+  while (r > 1 && r % 2 == 0) r /= 2;
+  if (NT < 4 || (NT & (NT - 1)) || nlayers < 1 || r != 1 || N % 2)
+    return set_err(GLASS_ERR_SIZE, "glass_gpu_wdm_by_layers_host: NT a power of two, NT (Nlayers + 1) / 2 of the "
+                                   "form 2^a 3^b");
+  if ((size_t)(N / 2 + NT) * sizeof(double2) > 227 * 1024)
+    return set_err(GLASS_ERR_SIZE, "glass_gpu_wdm_by_layers_host: NT (Nlayers + 3) / 2 complex values must fit "
+                                   "227 KB of shared memory");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  std::vector<double2> tw((size_t)N);
+  wdm_unit_roots((int)N, tw.data());
+  const size_t nwin = (size_t)NT / 2 + 1;
+  const size_t bytes = sizeof(double2) * N + sizeof(double) * (N + nwin);
+  void *mem = nullptr;
+  GLASS_CUDA(cudaMallocAsync(&mem, bytes, ctx->stream), "cudaMallocAsync(by_layers)");
+  double2 *d_tw = (double2 *)mem;
+  double *d_data = (double *)(d_tw + N), *d_win = d_data + N;
+  cudaError_t e = cudaMemcpyAsync(d_tw, tw.data(), sizeof(double2) * N, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_data, timedata, sizeof(double) * N, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_win, window, sizeof(double) * nwin, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = wdm_by_layers_launch(NF, NT, jmin, nlayers, d_win, d_tw, d_data, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(timedata, d_data, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaFreeAsync(mem, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  GLASS_CUDA(e, "wdm_by_layers");
+  return GLASS_OK;
+}
+
 // ------------------------------------------------------------ wavelet-domain UCB path
 static constexpr int kWvChunk = 4096;  // sources per launch sequence (bounds the work memory)
 
@@ -2011,12 +2046,12 @@ struct DropInThread {
 };
 static thread_local DropInThread g_dropin;
 
-[[noreturn]] static void dropin_fail(const char *who) {
+[[noreturn]] void dropin_fail(const char *who) {
   fprintf(stderr, "%s: %s\n", who, glass_gpu_last_error());
   exit(1);
 }
 
-static glass_gpu_ctx *dropin_ctx(const char *who) {
+glass_gpu_ctx *dropin_ctx(const char *who) {
   DropInThread &D = g_dropin;
   if (!D.ctx) {
     const char *dev = getenv("GLASS_GPU_DEVICE");
@@ -2055,6 +2090,16 @@ extern "C" void wavelet_transform_timefreq(struct Wavelets *wdm, double *timedat
   if (glass_gpu_wdm_forward_host(ctx, GLASS_PREC_FP64, w->NF, w->NT, w->A, kWaveletFilterConstant, timedata,
                                  timedata) != GLASS_OK)
     dropin_fail("wavelet_transform_timefreq");
+}
+
+// wavelet_transform_timefreq_by_layers (utils/src/glass_wavelet.c:544): in
+// place on the caller's NT (Nlayers + 1) samples, FP64
+extern "C" void wavelet_transform_timefreq_by_layers(struct Wavelets *wdm, int jmin, int Nlayers, double *window,
+                                                     double *timedata) {
+  const WaveletsLayout *w = reinterpret_cast<const WaveletsLayout *>(wdm);
+  glass_gpu_ctx *ctx = dropin_ctx("wavelet_transform_timefreq_by_layers");
+  if (glass_gpu_wdm_by_layers_host(ctx, w->NF, w->NT, jmin, Nlayers, window, timedata) != GLASS_OK)
+    dropin_fail("wavelet_transform_timefreq_by_layers");
 }
 
 static void dropin_freq(struct Wavelets *wdm, const double *in, double *out, bool to_freq, const char *who) {

@@ -41,6 +41,7 @@
 #include "wdm.cuh"
 
 namespace glass {
+
 namespace {
 
 constexpr double kVEARTH = 0.00010103671;  // utils/src/glass_constants.h:89
@@ -701,6 +702,68 @@ __global__ void __launch_bounds__(kLayerThreads) wv_layers_kernel(WvGridDev g, i
   }
 }
 
+// wavelet_transform_timefreq_by_layers (utils/src/glass_wavelet.c:544-610)
+// on a caller's series: the real FFT of its N = NT (nl + 1) samples (packed
+// two per complex, mixed radix), then per layer the windowed band around its
+// centre, an NT-point inverse FFT and the layer's pixels, as the waveform
+// kernel above does for its own samples.  One CTA; the output replaces the
+// input (zero beyond NT nl).
+__global__ void __launch_bounds__(kLayerThreads) wdm_by_layers_kernel(int NF, int NT, int jmin, int nl,
+                                                                      const double *win, const double2 *tw,
+                                                                      double *data) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  const int Nds = NT * (nl + 1), M = Nds / 2;
+  double2 *zb = reinterpret_cast<double2 *>(sm_raw);
+  double2 *lb = zb + M;
+  RadixPlan PM, PN;
+  radix_plan(M, PM);
+  radix_plan(NT, PN);
+  for (int i = threadIdx.x; i < Nds; i += blockDim.x) {
+    double *slot = reinterpret_cast<double *>(zb + digit_rev(i >> 1, PM));
+    slot[i & 1] = data[i];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < Nds; i += blockDim.x) data[i] = 0.0;
+  dit_fft(zb, M, PM, tw, 2, -1);
+  const double norm = sqrt((double)NF) / (nl + 1.0);
+  for (int off = 0; off < nl; off++) {
+    const int m = jmin + off;
+    const int center = (off + 1) * NT / 2;
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+      const int j = t - NT / 2, idx = center + j;
+      double2 val = make_double2(0.0, 0.0);
+      if (j > -NT / 2 && idx >= 0 && idx <= M) {
+        double wt = win[j < 0 ? -j : j];
+        if (j == 0 && (m == 0 || m == NF)) wt /= 2.0;
+        const double2 zk = zb[idx % M], zm0 = zb[(M - idx) % M];
+        const double2 zm = make_double2(zm0.x, -zm0.y);
+        const double2 e = tw[idx];
+        const double2 sm = make_double2(zk.x + zm.x, zk.y + zm.y), df = make_double2(zk.x - zm.x, zk.y - zm.y);
+        const double2 ed = cmul(e, df);
+        const double2 X = make_double2(0.5 * (sm.x + ed.y), 0.5 * (sm.y - ed.x));
+        val = make_double2(wt * X.x, wt * X.y);
+      }
+      lb[digit_rev(t, PN)] = val;
+    }
+    __syncthreads();
+    dit_fft(lb, NT, PN, tw, nl + 1, +1);
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+      const double re = lb[t].x / NT, im = lb[t].y / NT;
+      double v;
+      if (m == 0 || m == NF) {
+        if (t % 2) continue;  // odd pixels stay zero
+        v = re * kSQRT2 * norm;
+      } else {
+        const double sgn = (m % 2 == 0) ? 1.0 : -1.0;
+        v = (((t + m) % 2 == 0) ? re : sgn * im) * norm;
+      }
+      data[(size_t)t * nl + off] = v;
+    }
+    __syncthreads();
+  }
+}
+
+
 // ------------------------------------------------------------ likelihood
 constexpr int kDloglThreads = 256;
 
@@ -1110,6 +1173,24 @@ static void unit_root(long long j, long long P, double *c, double *s) {
 }
 
 }  // namespace
+
+cudaError_t wdm_by_layers_launch(int NF, int NT, int jmin, int nl, const double *d_win, const double2 *d_tw,
+                                 double *d_data, cudaStream_t s) {
+  const size_t sm = sizeof(double2) * ((size_t)NT * (nl + 1) / 2 + NT);
+  cudaError_t e = cudaFuncSetAttribute(wdm_by_layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  wdm_by_layers_kernel<<<1, kLayerThreads, sm, s>>>(NF, NT, jmin, nl, d_win, d_tw, d_data);
+  return cudaGetLastError();
+}
+
+void wdm_unit_roots(int P, double2 *out) {
+  for (int k = 0; k < P; k++) {
+    double c, sn;
+    unit_root(k, P, &c, &sn);
+    out[k] = make_double2(c, sn);
+  }
+}
+
 
 size_t wv_work_bytes(int cap, int norb, int NT) {
   auto pad = [](size_t b) { return (b + 255) / 256 * 256; };

@@ -73,6 +73,14 @@ cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStr
 size_t wv_work_bytes(int cap, int norb, int NT);
 void wv_work_carve(WvWorkDev &w, void *base, int cap, int norb, int NT);
 
+// wavelet_transform_timefreq_by_layers on a device series of NT (nl + 1)
+// samples, in place (one CTA): nl layers from jmin, window win[NT/2 + 1],
+// tw[k] = e^{-2 pi i k / (NT (nl + 1))}; NT (nl + 1) must have no prime factor
+// above 3.
+cudaError_t wdm_by_layers_launch(int NF, int NT, int jmin, int nl, const double *d_win, const double2 *d_tw,
+                                 double *d_data, cudaStream_t s);
+void wdm_unit_roots(int P, double2 *out);
+
 // Waveform batch: plan, response, TDI splines, per-layer transforms.
 // precision 1: samples with an FP64 phase and FP32 amplitude spline, FP32
 // FFTs, FP32 coefficients (divided by g.scale) in w.coef.

@@ -77,6 +77,53 @@ int glass_ucb_waveform(const double *orbit_xyz, const char *format, double T, do
  */
 int ucb_bandwidth(double L, double fstar, double f, double fdot, double costheta, double A, double T, int N);
 
+/* ----------------------------- drop-ins for the model and likelihood headers */
+struct Data;   /* utils/src/glass_data.h:50-97; read: N, NFFT, Nchannel, T, t0, qmin, tdi, format */
+struct Source; /* utils/src/glass_model.h:81-121; read/written: params, tdi, f0 .. phiref, dfdt, BW, qmin,
+                  qmax, imin, imax, fisher_matrix, fisher_evectr, fisher_evalue */
+struct Model;  /* utils/src/glass_model.h:25-60; read: Nlive, source, noise, tdi, residual, t0 */
+struct Noise;  /* utils/src/glass_data.h:337-360; read: invC */
+/*
+ * Same names, signatures and results as the reference (the structures'
+ * layouts are the interface), so that ucb_mcmc links against this library:
+ *   analytic_orbits, initialize_analytic_orbit  utils/src/glass_lisa.c:77, :125
+ *   map_array_to_ucb_params  ucb/src/glass_ucb_model.c:25 (glass_ucb_model.h)
+ *   ucb_alignment            ucb/src/glass_ucb_waveform.c:727 (glass_ucb_waveform.h:170)
+ *   add_ucb_model, remove_ucb_model  ucb/src/glass_ucb_model.c:192, :149
+ *   generate_ucb_model       ucb/src/glass_ucb_model.c:55 (glass_ucb_model.h:36)
+ *   update_ucb_model         ucb/src/glass_ucb_model.c:271 (glass_ucb_model.h:45)
+ *   fourier_nwip, snr        utils/src/glass_math.c:362, :403
+ *   gaussian_log_likelihood  utils/src/glass_model.c:726
+ *   matrix_eigenstuff        utils/src/glass_math.c:475
+ *   ucb_fisher               ucb/src/glass_ucb_waveform.c:364 (glass_ucb_waveform.h:150)
+ * Waveforms come from the GPU ucb_waveform above.  ucb_fisher takes its
+ * Fisher matrix for A/E data from the adjoint kernels (glass_gpu_grad_fisher
+ * _batch with the reference's noise indexing, fisher_mode 1; the segment's
+ * noise is uploaded to the thread's context when it changes), and for X or
+ * XYZ data from forward differences of the GPU waveform as the reference
+ * does.  The sums over a segment's bins run on the caller's host arrays in
+ * the reference's order of operations (bit-identical): a GPU launch per call
+ * would cost more than the arithmetic.  matrix_eigenstuff: symmetric input
+ * (the reference passes Fisher matrices to LAPACK's general solver);
+ * eigenvector j is column j, unit length, pairs sorted by decreasing
+ * eigenvalue with each vector's largest component positive (LAPACK's order
+ * and signs are not reproduced).  Errors print the reason and exit(1).
+ */
+void analytic_orbits(struct Orbit *orbit, double t, double *x, double *y, double *z);
+void initialize_analytic_orbit(struct Orbit *orbit);
+void map_array_to_ucb_params(struct Source *source, double *params, double T);
+void ucb_alignment(struct Orbit *orbit, struct Data *data, struct Source *source);
+void add_ucb_model(struct Data *data, struct Model *model, struct Source *source);
+void remove_ucb_model(struct Data *data, struct Model *model, struct Source *source);
+void generate_ucb_model(struct Orbit *orbit, struct Data *data, struct Model *model, int source_id);
+void update_ucb_model(struct Orbit *orbit, struct Data *data, struct Model *model_x, struct Model *model_y,
+                      int source_id);
+double fourier_nwip(const double *a, const double *b, const double *invC, int N);
+double snr(struct Source *source, struct Noise *noise);
+double gaussian_log_likelihood(struct Data *data, struct Model *model);
+void matrix_eigenstuff(double **matrix, double **evectors, double *evalues, int N);
+void ucb_fisher(struct Orbit *orbit, struct Data *data, struct Source *source, struct Noise *noise);
+
 /* ---------------------------------------------------------- batched API */
 typedef struct glass_gpu_ctx glass_gpu_ctx;
 
@@ -487,6 +534,17 @@ int glass_gpu_wdm_forward_host(glass_gpu_ctx *ctx, int precision, int NF, int NT
 int glass_gpu_wdm_inverse_host(glass_gpu_ctx *ctx, int precision, int NF, int NT, double A, double nx,
                                const double *wdm, double *time);
 
+/*
+ * wavelet_transform_timefreq_by_layers (utils/src/glass_wavelet.c:544-610,
+ * glass_wavelet.h:119) on a HOST series of NT (nlayers + 1) samples, in place:
+ * the real FFT of the series, then for each of the nlayers layers from jmin
+ * the band around its centre weighted by window[0 .. NT/2] and an NT-point
+ * inverse FFT, written to timedata[n nlayers + layer] (the rest zero).  FP64,
+ * one CTA; NT a power of two and NT (nlayers + 1) / 2 of the form 2^a 3^b.
+ */
+int glass_gpu_wdm_by_layers_host(glass_gpu_ctx *ctx, int NF, int NT, int jmin, int nlayers, const double *window,
+                                 double *timedata);
+
 /* ------------------------------------------- wavelet-domain UCB waveform */
 /*
  * The wavelet-domain UCB waveform (ucb_waveform_wavelet,
@@ -593,6 +651,7 @@ int glass_gpu_wavelet_fisher_batch_host(glass_gpu_ctx *ctx, int nitems, const do
  * wavelet_transform_timefreq     utils/src/glass_wavelet.c:293 (glass_wavelet.h:100), in place
  * wavelet_transform_freq         utils/src/glass_wavelet.c:410 (glass_wavelet.h:105)
  * wavelet_transform_inverse_freq utils/src/glass_wavelet.c:351 (glass_wavelet.h:108)
+ * wavelet_transform_timefreq_by_layers utils/src/glass_wavelet.c:544 (glass_wavelet.h:119), in place
  * ucb_waveform_wavelet           ucb/src/glass_ucb_waveform.c:1061 (glass_ucb_waveform.h:231);
  *                                the orbit nodes come from the caller's struct Orbit
  *                                (Norb, t, x, y, z), so interpolated analytic and
@@ -607,6 +666,8 @@ void build_wdm_filter_freq(double *phif, int Nf, int Nt, double A, bool forward)
 void wavelet_transform_timefreq(struct Wavelets *wdm, double *timedata);
 void wavelet_transform_freq(struct Wavelets *wdm, double *freqdata, double *wdmdata);
 void wavelet_transform_inverse_freq(struct Wavelets *wdm, double *wdmdata, double *freqdata);
+void wavelet_transform_timefreq_by_layers(struct Wavelets *wdm, int jmin, int Nlayers, double *window,
+                                          double *timedata);
 void ucb_waveform_wavelet(struct Orbit *orbit, struct Wavelets *wdm, double Tobs, double t0, double *params,
                           int *wavelet_list, int *Nwavelet, double *X, double *Y, double *Z);
 void ucb_waveform_wavelet_tab(struct Orbit *orbit, struct Wavelets *wdm, double Tobs, double t0, double *params,
