@@ -37,7 +37,7 @@ EXPORTS = (
     "glass_gpu_bank_upload", "glass_gpu_bank_set_residual", "glass_gpu_dlogl_batch",
     "glass_gpu_dlogl_batch_host", "glass_gpu_last_launch_count", "glass_gpu_set_phase_timing",
     "glass_gpu_set_host_access", "glass_gpu_get_host_access",
-    "glass_gpu_last_phase_ms", "glass_gpu_probe_fma_tflops",
+    "glass_gpu_last_phase_ms",
     "glass_gpu_grad_fisher_batch", "glass_gpu_grad_fisher_batch_host", "glass_gpu_set_template_size",
     "glass_gpu_dlogl_fp64_noalloc", "glass_wdm_window", "glass_gpu_wdm_forward", "glass_gpu_wdm_inverse",
     "glass_gpu_wdm_forward_host", "glass_gpu_wdm_inverse_host",
@@ -96,7 +96,6 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                                        _D, _D, _D, _D, _D, ctypes.c_int, ctypes.c_int]
     lib.ucb_bandwidth.argtypes = [ctypes.c_double] * 7 + [ctypes.c_int]
     lib.ucb_bandwidth.restype = ctypes.c_int
-    lib.glass_gpu_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _D]
     lib.glass_gpu_grad_fisher_batch.argtypes = [_V, ctypes.c_int, _V, _V, ctypes.c_int, _V, _V, _V, _V]
     lib.glass_gpu_grad_fisher_batch_host.argtypes = [_V, ctypes.c_int, _I, _D, ctypes.c_int, _D, _D, _D, _I]
     lib.glass_gpu_set_template_size.argtypes = [_V, ctypes.c_int]
@@ -194,10 +193,21 @@ def ucb_waveform(params, N, T, t0=0.0, fmt="sangria", NI=2, NP=8, orbit_xyz=None
     return out
 
 
+PROBE_PATH = os.path.join(HERE, "lib", "libglass_probe.so")
+
+
 def probe_fma_tflops(device: int = 0, fp64: bool = False) -> float:
-    """Measured FMA throughput of the FP32 or FP64 pipe (TFLOP/s)."""
+    """Measured FMA throughput of the FP32 or FP64 pipe (TFLOP/s), from the
+    benchmark's probe library (lib/libglass_probe.so, not part of the
+    engine)."""
+    if not os.path.exists(PROBE_PATH):
+        raise GlassError(f"{PROBE_PATH} is not built (python -m glass_gb300.build)")
+    lib = ctypes.CDLL(PROBE_PATH)
+    lib.glass_gpu_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     out = ctypes.c_double()
-    _check(load_library().glass_gpu_probe_fma_tflops(device, int(fp64), ctypes.byref(out)))
+    rc = lib.glass_gpu_probe_fma_tflops(device, int(fp64), ctypes.byref(out))
+    if rc != 0:
+        raise GlassError(f"FMA probe failed ({rc})")
     return out.value
 
 

@@ -21,6 +21,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libglass_gb300.so")
+# the benchmark's FMA-throughput probe: a separate library, not the engine
+PROBE_SRC = os.path.join(HERE, "probe", "fma_probe.cu")
+PROBE_LIB = os.path.join(OUT_DIR, "libglass_probe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
@@ -61,6 +64,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     deps = (_sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
             + [os.path.abspath(__file__)])
     if not force and not _stale(LIB, deps):
+        build_probe()
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(OBJ_DIR, exist_ok=True)
@@ -84,7 +88,19 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_probe(force)
     return LIB
+
+
+def build_probe(force: bool = False) -> str:
+    if not force and not _stale(PROBE_LIB, [PROBE_SRC, os.path.abspath(__file__)]):
+        return PROBE_LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    cmd = [nvcc()] + ARCH + NVCC_FLAGS + ["-shared", PROBE_SRC, "-o", PROBE_LIB, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {PROBE_SRC}:\n{r.stdout}\n{r.stderr}")
+    return PROBE_LIB
 
 
 if __name__ == "__main__":

@@ -1,9 +1,12 @@
 // Measured FMA throughput of the GPU's FP32 and FP64 pipes, so that rooflines
 // of the CUDA-core-bound kernels are reported against this machine's own peak
-// rather than a datasheet figure.
+// rather than a datasheet figure.  A measuring aid for the benchmark, built
+// into its own library (lib/libglass_probe.so), not into the engine.
 #include <cuda_runtime.h>
 
-#include "../../include/glass_gb300.h"
+#define GLASS_OK 0
+#define GLASS_ERR_ARG -1
+#define GLASS_ERR_CUDA -3
 
 namespace {
 

@@ -677,11 +677,6 @@ void ucb_waveform_wavelet_slow(struct Orbit *orbit, struct Wavelets *wdm, double
 int glass_ucb_waveform_wavelet_tab(void);
 int glass_ucb_waveform_wavelet_slow(void);
 
-/* ---------------------------------------------------------- diagnostics */
-/* Measured fused-multiply-add throughput (TFLOP/s, 2 flops per FMA) of the
- * device's FP32 (fp64 == 0) or FP64 pipe: the peak that the CUDA-core-bound
- * kernels of this library are compared against.  No reference counterpart. */
-int glass_gpu_probe_fma_tflops(int device, int fp64, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libglassref.so")
-REF_SRC = "/root/reference"
+# the reference source tree (development machine only): $GLASS_REFERENCE_SRC
+REF_SRC = os.environ.get("GLASS_REFERENCE_SRC", "/root/reference")
 
 FORMATS = {"sangria": 0, "phase": 1, "frequency": 2}
 NOISE_MODELS = {"scirdv1": 0, "sangria": 1, "radler": 2}
