@@ -95,11 +95,10 @@ PROFILED_DRAM_BYTES = {"fd_spec_all_kernel<1, 0>": 31018800 + 768, "fd_slow_kern
 
 
 def make_workload(rank, steps):
-    """Segments, injections and (steps) batches of proposals, seeded per rank."""
+    """Segments, injections and the chains' layout, seeded per rank."""
     import glass_gb300 as gg
 
     rng = np.random.default_rng(1 + 1000 * rank)
-    inj, Ns = [], []
 
     def wf(p):
         f0 = p[0] / T
@@ -107,41 +106,12 @@ def make_workload(rank, steps):
         h = gg.ucb_waveform(p, N, T)
         return N, h[3], h[4]
 
-    qmin, dA, dE, iA, iE = [], [], [], [], []
-    for s in range(NSEG):
-        f0 = 10 ** rng.uniform(math.log10(0.5e-3), math.log10(15e-3))
-        amp = 10 ** rng.uniform(-23, -21)
-        p = wl.draw_source(rng, f0, amp, 1e-17)
-        q, a, e, ia, ie = wl.make_segment(rng, [p], wf, NFFT=NFFT, T=T)
-        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie), inj.append(p)
-        Ns.append(wf(p)[0])
-    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
-                          invCA=np.array(iA), invCE=np.array(iE))
-    inj = np.array(inj)
-    items = NCHAIN * NTEMP
-    item_seg = (np.arange(items) // NTEMP % NSEG).astype(np.int32)
-    temps = 1.5 ** (np.arange(items) % NTEMP)
-    return bank, inj, np.array(Ns), item_seg, temps, rng
+    bank, inj, Ns, item_seg, temps = wl.tempered_bank(rng, wf, NSEG, NFFT, NCHAIN, NTEMP)
+    return bank, inj, Ns, item_seg, temps, rng
 
 
 def draw_batches(rng, inj, snr, item_seg, temps, nbatch):
-    """Gaussian jumps around each chain's state, widened by sqrt(temperature);
-    cos-parameters reflected back inside (-1, 1) as draw_from_fisher does
-    (ucb/src/glass_ucb_proposal.c:382-386), and left unchanged when even the
-    reflection falls outside."""
-    scales = np.array([wl.jump_scales(inj[s], max(snr[s], 5.0)) for s in range(len(inj))])
-    out = np.empty((nbatch, len(item_seg), 8))
-    x = inj[item_seg]
-    for b in range(nbatch):
-        jump = rng.standard_normal((len(item_seg), 8)) * scales[item_seg] * np.sqrt(temps)[:, None]
-        p = x + jump
-        for k in (1, 4):
-            bad = (p[:, k] >= 1.0) | (p[:, k] <= -1.0)
-            p[bad, k] = x[bad, k] - jump[bad, k]
-            bad = (p[:, k] >= 1.0) | (p[:, k] <= -1.0)
-            p[bad, k] = x[bad, k]
-        out[b] = p
-    return out
+    return wl.tempered_proposals(rng, inj, snr, item_seg, temps, nbatch)
 
 
 class NvmlClockPoller:

@@ -53,7 +53,8 @@ EXPORTS = (
     "glass_gpu_dlogl_batch_channels", "glass_gpu_noise_eta_batch", "glass_gpu_noise_eta_batch_host",
     "glass_gpu_rand_r_fill", "glass_gpu_mh_accept", "glass_gpu_fisher_draw", "glass_gpu_ptmcmc",
     "glass_gpu_set_mixed_tolerance", "glass_gpu_set_mixed_tolerance_scale", "glass_gpu_mixed_reevaluated",
-    "glass_gpu_wdm_by_layers_host", "wavelet_transform_timefreq_by_layers",
+    "glass_gpu_wdm_by_layers_host", "wavelet_transform_timefreq_by_layers", "glass_gpu_set_tuning",
+    "glass_gpu_get_tuning",
     "analytic_orbits", "initialize_analytic_orbit", "map_array_to_ucb_params", "ucb_alignment", "add_ucb_model",
     "remove_ucb_model", "generate_ucb_model", "update_ucb_model", "fourier_nwip", "snr", "gaussian_log_likelihood",
     "matrix_eigenstuff", "ucb_fisher",
@@ -87,6 +88,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_set_mixed_tolerance.argtypes = [_V, ctypes.c_double]
     lib.glass_gpu_set_mixed_tolerance_scale.argtypes = [_V, ctypes.c_int, _D]
     lib.glass_gpu_mixed_reevaluated.argtypes = [_V, _V]
+    lib.glass_gpu_set_tuning.argtypes = [_V, ctypes.c_char_p, ctypes.c_int]
+    lib.glass_gpu_get_tuning.argtypes = [_V, ctypes.c_char_p, _V]
     lib.glass_gpu_bank_upload.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_int, _I, _D, _D, _D, _D]
     lib.glass_gpu_bank_set_residual.argtypes = [_V, ctypes.c_int, _D, _D]
@@ -562,6 +565,22 @@ class Engine:
         else:
             sc = np.ascontiguousarray(scale, np.float64)
             _check(self.lib.glass_gpu_set_mixed_tolerance_scale(self._ctx, int(sc.size), _pd(sc)))
+
+    def set_tuning(self, key: str, value: int):
+        """One launch-shape parameter of the mixed path (glass_gpu_set_tuning)."""
+        _check(self.lib.glass_gpu_set_tuning(self._ctx, key.encode(), int(value)))
+
+    def get_tuning(self, key: str) -> int:
+        v = ctypes.c_int(0)
+        _check(self.lib.glass_gpu_get_tuning(self._ctx, key.encode(), ctypes.byref(v)))
+        return v.value
+
+    def apply_tuning(self, path: str | None = None) -> dict:
+        """Applies the autotuner's table (glass_gb300/tuning.json by default)
+        for this GPU model, if it has an entry; returns what was applied."""
+        from . import tune
+
+        return tune.apply(self, path)
 
     def mixed_reevaluated(self) -> int:
         """Number of proposals re-evaluated in double-float so far

@@ -313,6 +313,46 @@ extern "C" int glass_gpu_set_mixed_tolerance_scale(glass_gpu_ctx *ctx, int n, co
   return GLASS_OK;
 }
 
+// Launch-shape parameters of the mixed path by name (the autotuner's knobs).
+static int *tuning_slot(glass_gpu_ctx *ctx, const char *key, int *lo, int *hi) {
+  FdWorkDev::Tuning &t = ctx->work.tune;
+  struct Knob {
+    const char *name;
+    int *slot, lo, hi;
+  } knobs[] = {{"slow_block", &t.slow_block, 128, 512},
+               {"slow_ctas_per_sm", &t.slow_ctas_per_sm, 0, 16},
+               {"spec_ctas_per_sm", &t.spec_ctas_per_sm, 0, 8},
+               {"plan_per_cta", &t.plan_per_cta, 0, 32}};
+  for (const Knob &k : knobs)
+    if (!strcmp(key, k.name)) {
+      *lo = k.lo;
+      *hi = k.hi;
+      return k.slot;
+    }
+  return nullptr;
+}
+
+extern "C" int glass_gpu_set_tuning(glass_gpu_ctx *ctx, const char *key, int value) {
+  if (!ctx || !key) return set_err(GLASS_ERR_ARG, "glass_gpu_set_tuning: null argument");
+  int lo = 0, hi = 0;
+  int *slot = tuning_slot(ctx, key, &lo, &hi);
+  if (!slot) return set_err(GLASS_ERR_ARG, "glass_gpu_set_tuning: unknown parameter %s", key);
+  if (value < lo || value > hi || (!strcmp(key, "slow_block") && value != 128 && value != 256 && value != 512))
+    return set_err(GLASS_ERR_ARG, "glass_gpu_set_tuning: value out of range for %s", key);
+  if (*slot != value) clear_host_graphs(ctx);  // launch shapes are baked into recorded graphs
+  *slot = value;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_get_tuning(glass_gpu_ctx *ctx, const char *key, int *value) {
+  if (!ctx || !key || !value) return set_err(GLASS_ERR_ARG, "glass_gpu_get_tuning: null argument");
+  int lo = 0, hi = 0;
+  int *slot = tuning_slot(ctx, key, &lo, &hi);
+  if (!slot) return set_err(GLASS_ERR_ARG, "glass_gpu_get_tuning: unknown parameter %s", key);
+  *value = *slot;
+  return GLASS_OK;
+}
+
 extern "C" int glass_gpu_mixed_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count) {
   if (!ctx || !count) return set_err(GLASS_ERR_ARG, "glass_gpu_mixed_reevaluated: null argument");
   *count = 0;

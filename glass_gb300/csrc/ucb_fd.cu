@@ -33,11 +33,11 @@
 
 namespace glass {
 
-cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream);
+cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream, int block, int cap);
 cudaError_t fd_launch_slow_fp64(const SlowArgs &a, int num_sms, cudaStream_t stream);
 cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
 cudaError_t fd_launch_spec_fp64(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream, bool perch);
-cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch, int cap);
 cudaError_t fd_launch_spec_all_fp64(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch);
 
 // ------------------------------------------------------------- plan kernels
@@ -488,6 +488,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   {
     int per = (nitems + num_sms - 1) / (num_sms > 0 ? num_sms : 1);
     pa.per_cta = per < 16 ? 16 : (per > 32 ? 32 : per);
+    if (work.tune.plan_per_cta >= 8 && work.tune.plan_per_cta <= 32) pa.per_cta = work.tune.plan_per_cta;
   }
   if (mix)
     fd_planmix_kernel<<<(nitems + pa.per_cta - 1) / pa.per_cta, 128, 0, stream>>>(pa);
@@ -516,7 +517,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     sa.geo[b] = tab.geo[b];
   }
   sa.series = work.series;
-  e = mix ? fd_launch_slow_mixed(sa, num_sms, stream) : fd_launch_slow_fp64(sa, num_sms, stream);
+  e = mix ? fd_launch_slow_mixed(sa, num_sms, stream, work.tune.slow_block, work.tune.slow_ctas_per_sm)
+          : fd_launch_slow_fp64(sa, num_sms, stream);
   launches++;
   if (e != cudaSuccess) return e;
   if (timing && (e = cudaEventRecord(work.phase[2], stream)) != cudaSuccess) return e;
@@ -601,7 +603,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     A.zero_counts = nb == 0 ? work.bin_count : nullptr;  // side kernels would still be reading them
     A.done = work.bin_count + kNumBins + 1;  // fb_count is at kNumBins
     for (int b = 0; b < kSpecAllBins; b++) A.tw[b] = mix ? (const void *)tab.tw32x[b] : (const void *)tab.tw64[b];
-    e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch) : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
+    e = mix ? fd_launch_spec_all_mixed(A, num_sms, stream, perch, work.tune.spec_ctas_per_sm)
+            : fd_launch_spec_all_fp64(A, num_sms, stream, perch);
     launches++;
     if (e != cudaSuccess) return e;
   }

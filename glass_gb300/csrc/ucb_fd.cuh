@@ -68,6 +68,14 @@ struct FdWorkDev {
   // CTA, or a trailing memset), so the next one needs no leading memset; false
   // when that is not known (a launch returned an error part-way)
   bool counts_zero = false;
+  // launch shapes of the mixed path, chosen by the autotuner
+  // (glass_gb300/tune.py, glass_gpu_set_tuning); 0: the built-in choice
+  struct Tuning {
+    int slow_block = 256;         // slow-part threads per CTA (128, 256, 512)
+    int slow_ctas_per_sm = 0;     // cap on resident slow-part CTAs per SM
+    int spec_ctas_per_sm = 0;     // cap on persistent spectral CTAs per SM
+    int plan_per_cta = 0;         // proposals per plan CTA (8 .. 32)
+  } tune;
   void *series = nullptr;       // 4 arm-combination series per proposal
   // optional timing of each phase of a step on the caller's stream: events
   // before the plan kernel, after it, after the slow-part kernel, after the

@@ -1480,7 +1480,7 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
 }
 
 template <bool MIX, bool PERCH = false>
-static cudaError_t launch_spec_all(const SpecAllArgs &A, int num_sms, cudaStream_t stream) {
+static cudaError_t launch_spec_all(const SpecAllArgs &A, int num_sms, cudaStream_t stream, int cap = 0) {
   const size_t smem = SpecAllSmem<MIX>::bytes;
   static LaunchSetup setup;
   int occ = 0;
@@ -1491,6 +1491,7 @@ static cudaError_t launch_spec_all(const SpecAllArgs &A, int num_sms, cudaStream
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_spec_all_kernel<MIX, PERCH>, kSpecAllThreads, smem);
   }, &occ);
   if (e != cudaSuccess) return e;
+  if (cap > 0 && cap < occ) occ = cap;
   fd_spec_all_kernel<MIX, PERCH><<<occ * num_sms, kSpecAllThreads, smem, stream>>>(A);
   return cudaGetLastError();
 }
@@ -1518,15 +1519,16 @@ static cudaError_t launch_spec(const SpecArgs &a, int nitems_bound, int num_sms,
   return cudaGetLastError();
 }
 
-template <bool MIX>
-static cudaError_t launch_slow(const SlowArgs &a, int num_sms, cudaStream_t stream) {
+template <bool MIX, int BLOCK = 256>
+static cudaError_t launch_slow(const SlowArgs &a, int num_sms, cudaStream_t stream, int cap = 0) {
   static LaunchSetup setup;
   int occ = 0;
   cudaError_t e = launch_setup(setup, [&](int *o) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_slow_kernel<MIX>, 256, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_slow_kernel<MIX, BLOCK>, BLOCK, 0);
   }, &occ);
   if (e != cudaSuccess) return e;
-  fd_slow_kernel<MIX><<<occ * num_sms, 256, 0, stream>>>(a);
+  if (cap > 0 && cap < occ) occ = cap;
+  fd_slow_kernel<MIX, BLOCK><<<occ * num_sms, BLOCK, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -3,8 +3,12 @@
 
 namespace glass {
 
-cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream) {
-  return launch_slow<true>(a, num_sms, stream);
+cudaError_t fd_launch_slow_mixed(const SlowArgs &a, int num_sms, cudaStream_t stream, int block, int cap) {
+  switch (block) {
+    case 128: return launch_slow<true, 128>(a, num_sms, stream, cap);
+    case 512: return launch_slow<true, 512>(a, num_sms, stream, cap);
+    default: return launch_slow<true, 256>(a, num_sms, stream, cap);
+  }
 }
 
 cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_sms, cudaStream_t stream,
@@ -29,9 +33,9 @@ cudaError_t fd_launch_spec_mixed(int N, const SpecArgs &a, int nitems, int num_s
   return cudaErrorInvalidValue;
 }
 
-cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch) {
-  if (perch) return launch_spec_all<true, true>(A, num_sms, stream);
-  return launch_spec_all<true>(A, num_sms, stream);
+cudaError_t fd_launch_spec_all_mixed(const SpecAllArgs &A, int num_sms, cudaStream_t stream, bool perch, int cap) {
+  if (perch) return launch_spec_all<true, true>(A, num_sms, stream, cap);
+  return launch_spec_all<true>(A, num_sms, stream, cap);
 }
 
 }  // namespace glass

@@ -141,6 +141,51 @@ def gaussian_jumps(rng, params, scales, n):
     return out
 
 
+def tempered_bank(rng, waveform_fn, nseg=64, NFFT=1024, nchain=256, ntemp=12, f_range=(0.5e-3, 15e-3),
+                  log10_amp_range=(-23.0, -21.0), T=T_YEAR):
+    """A parallel-tempering likelihood workload: nseg independent segments of
+    NFFT bins, each the injection of one source (f0 log-uniform over f_range,
+    log10 amplitude uniform over log10_amp_range) in Gaussian A/E noise; nchain x
+    ntemp proposals per batch, chain c of segment c mod nseg at temperature
+    1.5^(i mod ntemp).  waveform_fn(params) -> (N, A, E) places a template.
+    Returns bank, injections, template sizes, item_seg and temperatures."""
+    inj, Ns = [], []
+    qmin, dA, dE, iA, iE = [], [], [], [], []
+    for s in range(nseg):
+        f0 = 10 ** rng.uniform(math.log10(f_range[0]), math.log10(f_range[1]))
+        amp = 10 ** rng.uniform(log10_amp_range[0], log10_amp_range[1])
+        p = draw_source(rng, f0, amp, 1e-17, T=T)
+        q, a, e, ia, ie = make_segment(rng, [p], waveform_fn, NFFT=NFFT, T=T)
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie), inj.append(p)
+        Ns.append(waveform_fn(p)[0])
+    bank = SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                       invCA=np.array(iA), invCE=np.array(iE))
+    items = nchain * ntemp
+    item_seg = (np.arange(items) // ntemp % nseg).astype(np.int32)
+    temps = 1.5 ** (np.arange(items) % ntemp)
+    return bank, np.array(inj), np.array(Ns), item_seg, temps
+
+
+def tempered_proposals(rng, inj, snr, item_seg, temps, nbatch):
+    """nbatch batches of Gaussian jumps around each chain's state, widened by
+    sqrt(temperature); cos-parameters reflected back inside (-1, 1) as
+    draw_from_fisher does (ucb/src/glass_ucb_proposal.c:382-386), and left
+    unchanged when even the reflection falls outside."""
+    scales = np.array([jump_scales(inj[s], max(snr[s], 5.0)) for s in range(len(inj))])
+    out = np.empty((nbatch, len(item_seg), 8))
+    x = inj[item_seg]
+    for b in range(nbatch):
+        jump = rng.standard_normal((len(item_seg), 8)) * scales[item_seg] * np.sqrt(temps)[:, None]
+        p = x + jump
+        for k in (1, 4):
+            bad = (p[:, k] >= 1.0) | (p[:, k] <= -1.0)
+            p[bad, k] = x[bad, k] - jump[bad, k]
+            bad = (p[:, k] >= 1.0) | (p[:, k] <= -1.0)
+            p[bad, k] = x[bad, k]
+        out[b] = p
+    return out
+
+
 def wavelet_invC(N, NT, kmin, scale=1.0):
     """Inverse noise covariance of a wavelet segment of N pixels starting at
     pixel kmin of a grid with NT pixels per layer: per pixel the inverse of

@@ -438,6 +438,20 @@ int glass_gpu_set_mixed_tolerance(glass_gpu_ctx *ctx, double tol);
  * proposal, and only the cold chains' proposals need delta logL itself to
  * tol.  Synchronises the context's stream. */
 int glass_gpu_set_mixed_tolerance_scale(glass_gpu_ctx *ctx, int n, const double *scale);
+/*
+ * Launch shapes of the mixed-precision path, by name; the autotuner
+ * (glass_gb300/tune.py) sweeps them on the target workload and records the
+ * fastest per GPU model.  0 selects the built-in choice.
+ *   "slow_block"        slow-part kernel threads per CTA: 128, 256 (default), 512
+ *   "slow_ctas_per_sm"  cap on its resident CTAs per SM (0: occupancy limit)
+ *   "spec_ctas_per_sm"  cap on the persistent spectral kernel's CTAs per SM
+ *   "plan_per_cta"      proposals per plan CTA, 8..32 (0: ceil(n / SMs) in 16..32)
+ * Changing a value drops the context's recorded host-path graphs; graphs the
+ * caller captured keep the shapes they were captured with.
+ */
+int glass_gpu_set_tuning(glass_gpu_ctx *ctx, const char *key, int value);
+int glass_gpu_get_tuning(glass_gpu_ctx *ctx, const char *key, int *value);
+
 /* Number of proposals re-evaluated in double-float since the context's work
  * buffers were allocated.  Synchronises the context's stream. */
 int glass_gpu_mixed_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count);

@@ -94,3 +94,30 @@ def test_wavelet_setup_argument_checks(lib):
     assert f(V, 1e6, 0.0, 64, 250, 1.0, 0.5, 0.0, 6.0, 0, 250, 0, None, None) == c["GLASS_ERR_SIZE"]
     assert f(V, 1e6, 0.0, 64, 256, 1.0, 0.5, 0.0, 6.0, 100, 512, 0, None, None) == c["GLASS_ERR_ARG"]
     assert f(V, -1.0, 0.0, 64, 256, 1.0, 0.5, 0.0, 6.0, 0, 512, 0, None, None) == c["GLASS_ERR_ARG"]
+
+
+def test_tuning_table_applies_the_entry_of_this_gpu(tmp_path, monkeypatch):
+    """glass_gb300.tune.apply sets the recorded knobs of the GPU model it runs
+    on, and nothing for a model the table does not know."""
+    import json
+
+    from glass_gb300 import tune
+
+    table = {"GB300 test": {"knobs": {"slow_block": 128, "spec_ctas_per_sm": 2}}}
+    path = tmp_path / "tuning.json"
+    path.write_text(json.dumps(table))
+
+    class FakeEngine:
+        def __init__(self):
+            self.set = {}
+
+        def set_tuning(self, k, v):
+            self.set[k] = v
+
+    monkeypatch.setattr(tune, "gpu_name", lambda device=0: "GB300 test")
+    eng = FakeEngine()
+    assert tune.apply(eng, str(path)) == {"slow_block": 128, "spec_ctas_per_sm": 2}
+    assert eng.set == {"slow_block": 128, "spec_ctas_per_sm": 2}
+    monkeypatch.setattr(tune, "gpu_name", lambda device=0: "other")
+    eng = FakeEngine()
+    assert tune.apply(eng, str(path)) == {} and eng.set == {}
