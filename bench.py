@@ -965,6 +965,7 @@ def run_ours(args):
 
     bank, inj, Ns, item_seg, temps, rng = make_workload(rank, nb)
     eng = gg.Engine(local)
+    tuning = eng.apply_tuning()  # the autotuner's launch shapes for this GPU model, if recorded
     eng.upload(bank)
     # current state of every chain: the injection; its term is the x side of delta logL
     _, t_inj, hh_inj, st = eng.dlogl_host(np.arange(NSEG, dtype=np.int32), inj, precision=gg.PREC_FP64)
@@ -1196,7 +1197,8 @@ def run_ours(args):
                       "precision": "mixed (FP32, double-float carrier phase), proposals over the 1e-3 error "
                                    "bound re-evaluated in double-float in the same graph",
                       "l2": "flushed (256 MB write) between timed steps",
-                      "graph": "one CUDA graph per step, replayed on that step's proposals in HBM"},
+                      "graph": "one CUDA graph per step, replayed on that step's proposals in HBM",
+                      "tuning": tuning or "built-in launch shapes"},
             "fp64": {"value": v_fp64, "unit": "evals/s", "ms_per_step": 1e3 * t_fp64 / args.steps,
                      "mixed_over_fp64": v_mixed / v_fp64},
             "accuracy": dict(acc["flat"], reevaluated_per_step=reeval_flat,
