@@ -949,6 +949,283 @@ def bench_sampler(gg, torch, dev, steps, warmup):
                         f"temperatures: ptmcmc; reference rand_r streams", **out}
 
 
+def bench_config0(gg, rank, budget_s=3.0, cap=10000, cpu=True):
+    """One source in a 1-year segment of 1024 A/E bins around f0 ~ U[3.0, 3.5]
+    mHz (A = 1e-22, fdot = 1e-17), 1 chain at 1 temperature: 1e4 seed-fixed
+    Gaussian-jump proposals evaluated one after the other, each one waveform
+    plus delta logL in FP64, through (a) the reference's own per-proposal calls
+    on this library's drop-ins (update_ucb_model + gaussian_log_likelihood on
+    the reference's structs, as an unchanged ucb_mcmc makes them), (b) the
+    batched engine called with one proposal (glass_gpu_dlogl_batch_host), and
+    (c) the reference algorithm on one host thread (the oracle port).  Each
+    path runs up to 1e4 proposals or budget_s seconds."""
+    import ctypes
+
+    from glass_gb300 import refstructs as rs
+
+    rng = np.random.default_rng(31 + 1000 * rank)
+    f0 = rng.uniform(3.0e-3, 3.5e-3)
+    p0 = wl.draw_source(rng, f0, 1e-22, 1e-17)
+
+    def wf(p):
+        N = 2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, p[0] / T, p[7] / T / T, p[1], math.exp(p[3]), T, 1024)
+        h = gg.ucb_waveform(p, N, T)
+        return N, h[3], h[4]
+
+    qmin, dA, dE, iA, iE = wl.make_segment(rng, [p0], wf, NFFT=1024, T=T)
+    bank = wl.SegmentBank(T=T, NFFT=1024, qmin=np.array([qmin], np.int32), dA=dA[None], dE=dE[None],
+                          invCA=iA[None], invCE=iE[None])
+    rA, rE = bank.interleaved()
+    N0 = wf(p0)[0]
+    props = wl.gaussian_jumps(rng, p0, wl.jump_scales(p0, 50.0), cap)
+    out = {"workload": "1 source, 1024-bin segment, f0~U[3,3.5] mHz, A=1e-22, 1 chain x 1 temperature, "
+                       "sequential Gaussian-jump proposals, FP64", "template_size": int(N0)}
+
+    def timed(fn):
+        n, t0 = 0, time.perf_counter()
+        while n < cap:
+            fn(props[n])
+            n += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
+        el = time.perf_counter() - t0
+        return n / el, n, el
+
+    # (a) the reference's calls on the drop-ins
+    L = rs.bind_dropins(gg.load_library())
+    keep = rs.Keep()
+    orbit = rs.Orbit()
+    L.initialize_analytic_orbit(ctypes.byref(orbit))
+    noise = rs.make_noise(keep, iA, iE)
+    data = rs.make_data(keep, 1024, int(qmin), rA[0], rE[0], noise)
+    mx, _ = rs.make_model(keep, [p0], 1024, noise)
+    my, _ = rs.make_model(keep, [p0], 1024, noise)
+    for m in (mx, my):
+        L.generate_ucb_model(ctypes.byref(orbit), ctypes.byref(data), ctypes.byref(m), -1)
+    sx, sy = mx.source[0].contents, my.source[0].contents
+    ll_x = L.gaussian_log_likelihood(ctypes.byref(data), ctypes.byref(mx))
+    dl_dropin = []
+    view = lambda ptr: np.ctypeslib.as_array(ptr, (2048,))  # noqa: E731
+    copies = [(view(my.tdi.contents.A), view(mx.tdi.contents.A)), (view(my.tdi.contents.E), view(mx.tdi.contents.E)),
+              (view(sy.tdi.contents.A), view(sx.tdi.contents.A)), (view(sy.tdi.contents.E), view(sx.tdi.contents.E))]
+
+    def dropin(p):
+        for q in range(8):
+            sy.params[q] = p[q]
+        L.update_ucb_model(ctypes.byref(orbit), ctypes.byref(data), ctypes.byref(mx), ctypes.byref(my), 0)
+        dl_dropin.append(L.gaussian_log_likelihood(ctypes.byref(data), ctypes.byref(my)) - ll_x)
+        # rejected: the proposed state becomes the current one again, as the
+        # sampler's copy_model does (ucb/src/glass_ucb_model.c)
+        for dst, src in copies:
+            dst[:] = src
+        for q in range(8):
+            sy.params[q] = p0[q]
+        for k in ("BW", "qmin", "qmax", "imin", "imax"):
+            setattr(sy, k, getattr(sx, k))
+
+    for w in range(5):
+        dropin(props[w])
+    dl_dropin.clear()
+    v, n, el = timed(dropin)
+    out["dropin_update_model_likelihood"] = {"value": v, "unit": "proposals/s", "proposals": n,
+                                             "api": "update_ucb_model + gaussian_log_likelihood (reference structs), "
+                                                    "then the current model copied back (rejection)",
+                                             "gpu_waveforms_per_proposal": 1}
+    # (b) the batched engine, one proposal per call
+    eng = gg.Engine(0)
+    eng.upload(bank)
+    hb = eng.host_batch(1)
+    hb.item_seg[0] = 0
+    _, t0x, _, _ = eng.dlogl_host(np.zeros(1, np.int32), p0[None], precision=gg.PREC_FP64)
+    hb.term_x[0] = t0x[0]
+    dl_engine = []
+
+    def engine_one(p):
+        hb.params[0] = p
+        hb.run(gg.PREC_FP64)
+        dl_engine.append(hb.dlogl[0])
+
+    for w in range(5):
+        engine_one(props[w])
+    dl_engine.clear()
+    v, n_e, el = timed(engine_one)
+    out["engine_one_per_call"] = {"value": v, "unit": "proposals/s", "proposals": n_e,
+                                  "api": "glass_gpu_dlogl_batch_host, 1 proposal, FP64"}
+    del hb
+    eng.close()
+    # agreement of the two GPU paths on the same proposals
+    k = min(len(dl_dropin), len(dl_engine))
+    if k:
+        d = np.abs(np.array(dl_dropin[:k]) - np.array(dl_engine[:k]))
+        out["dropin_vs_engine_max_abs_diff"] = float(d.max())
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import Port, build_port
+
+        build_port()
+        port = Port()
+        tx = port.dlogl_term(p0, T, 1024, int(qmin), rA[0], rE[0], iA, iE)[0]
+
+        def port_one(p):
+            port.dlogl_term(p, T, 1024, int(qmin), rA[0], rE[0], iA, iE)
+
+        v, n, el = timed(port_one)
+        out["cpu_port_1_thread"] = {"value": v, "unit": "proposals/s", "proposals": n, "cores": 1,
+                                    "cpu_model": cpu_model(), "kind": "port"}
+        out["dropin_over_cpu"] = out["dropin_update_model_likelihood"]["value"] / v
+        out["engine_over_cpu"] = out["engine_one_per_call"]["value"] / v
+        del tx
+    return out
+
+
+def bench_config4(gg, torch, dev, rank, steps=1000, grad_steps=50, warmup=3):
+    """Global-fit-scale batch: 1e4 sources of a synthetic Galactic population
+    (f0 log-uniform over 0.1-10 mHz, fdot from the GR chirp with chirp mass
+    ~U[0.2, 0.8] Msun, amplitude from the chirp mass, f0 and a distance
+    ~U[1, 15] kpc, isotropic sky and orientation) in 512 segments of 8192 A/E
+    bins (sizes 32..4096 from the bandwidth rule), Gaussian noise; 64 chains
+    x 16 temperatures own the sources (about 10 each).  One step proposes one
+    RJMCMC move per source: an update (Gaussian jump widened by sqrt(T)) or,
+    for one source in five, a birth (a prior draw in the segment, nothing
+    there yet).  The batched mixed-precision delta logL at the default 1e-3
+    tolerance is replayed through CUDA graphs (8 batches in turn) for `steps`
+    steps (1e7 evaluations at the default), and the adjoint gradient + Fisher
+    matrix of the same proposals for `grad_steps` steps."""
+    rng = np.random.default_rng(4 + 1000 * rank)
+    nsrc, nseg, NFFT, nchain, ntemp = 10000, 512, 8192, 64, 16
+    MSUN_S, KPC_M = 4.925491025543576e-06, 3.0856775814913673e19
+    f = 10 ** rng.uniform(math.log10(1e-4), math.log10(1e-2), nsrc)
+    mc = rng.uniform(0.2, 0.8, nsrc) * MSUN_S
+    dist = rng.uniform(1.0, 15.0, nsrc) * KPC_M
+    amp = 2.0 * mc ** (5.0 / 3.0) * (math.pi * f) ** (2.0 / 3.0) * wl.CLIGHT / dist
+    fdot = 96.0 / 5.0 * math.pi ** (8.0 / 3.0) * mc ** (5.0 / 3.0) * f ** (11.0 / 3.0)
+    src = np.array([wl.make_params(f[i], rng.uniform(-1, 1), rng.uniform(0, 2 * math.pi), amp[i],
+                                   rng.uniform(-1, 1), rng.uniform(0, math.pi), rng.uniform(0, 2 * math.pi), fdot[i])
+                    for i in range(nsrc)])
+    # segments centred on log-spaced frequencies; each source in the nearest
+    centres = np.exp(np.linspace(math.log(1.3e-4), math.log(9.7e-3), nseg))
+    centres = np.maximum(centres, (NFFT // 2 + 16) / T)  # every segment starts above 0 Hz
+    seg_of = np.clip(np.searchsorted((centres[1:] + centres[:-1]) / 2, f), 0, nseg - 1).astype(np.int32)
+
+    def wf(p):
+        N = 2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, p[0] / T, p[7] / T / T, p[1], math.exp(p[3]), T, NFFT)
+        N = min(N, 4096)
+        h = gg.ucb_waveform(p, N, T)
+        return N, h[3], h[4]
+
+    qmin, dA, dE, iA, iE = [], [], [], [], []
+    for s in range(nseg):
+        members = [src[i] for i in np.nonzero(seg_of == s)[0]]
+        q, a, e, ia, ie = wl.make_segment(rng, members, wf, NFFT=NFFT, T=T, center_f0=centres[s])
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie)
+    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                          invCA=np.array(iA), invCE=np.array(iE))
+    eng = gg.Engine(0)
+    eng.upload(bank)
+    _, t_src, hh_src, st_src = eng.dlogl_host(seg_of, src, precision=gg.PREC_FP64)
+    snr = np.sqrt(np.maximum(hh_src, 1.0))
+    temps = 1.5 ** (np.arange(nsrc) % (nchain * ntemp) % ntemp)
+    nb = 8
+    batches, tx = np.empty((nb, nsrc, 8)), np.empty((nb, nsrc))
+    for b in range(nb):
+        birth = rng.uniform(size=nsrc) < 0.2
+        scales = np.array([wl.jump_scales(src[i], max(snr[i], 5.0)) for i in range(nsrc)])
+        jump = rng.standard_normal((nsrc, 8)) * scales * np.sqrt(temps)[:, None]
+        p = src + jump
+        for k in (1, 4):
+            bad = np.abs(p[:, k]) >= 1.0
+            p[bad, k] = src[bad, k]
+        # births: a prior draw inside the segment
+        qs = bank.qmin[seg_of] + rng.uniform(0.1, 0.9, nsrc) * NFFT
+        bp = np.array([wl.make_params(qs[i] / T, rng.uniform(-1, 1), rng.uniform(0, 2 * math.pi),
+                                      10 ** rng.uniform(-23, -21), rng.uniform(-1, 1), rng.uniform(0, math.pi),
+                                      rng.uniform(0, 2 * math.pi), 0.0) for i in range(nsrc)])
+        p[birth] = bp[birth]
+        batches[b] = p
+        tx[b] = np.where(birth, 0.0, t_src)
+    items = nsrc
+    d_seg = torch.from_numpy(seg_of).to(dev)
+    d_b = torch.from_numpy(batches).to(dev)
+    d_tx = torch.from_numpy(tx).to(dev)
+    dl, ty, hh = (torch.empty(items, dtype=torch.float64, device=dev) for _ in range(3))
+    st = torch.empty(items, dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    eng.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        eng.dlogl_device(d_seg, d_b[0], dl, ty, hh, st, term_x=d_tx[0], precision=gg.PREC_MIXED)
+    stream.synchronize()
+    graphs = []
+    for b in range(nb):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            eng.dlogl_device(d_seg, d_b[b], dl, ty, hh, st, term_x=d_tx[b], precision=gg.PREC_MIXED)
+        graphs.append(g)
+    n0 = eng.mixed_reevaluated()
+    with torch.cuda.stream(stream):
+        for w in range(warmup):
+            graphs[w % nb].replay()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(steps):
+            graphs[k % nb].replay()
+        e1.record(stream)
+    stream.synchronize()
+    t_dl = e0.elapsed_time(e1) / 1e3
+    reeval = (eng.mixed_reevaluated() - n0) / (steps + warmup)
+    # accuracy of one batch against the FP64 path
+    with torch.cuda.stream(stream):
+        graphs[0].replay()
+    stream.synchronize()
+    mixed = dl.cpu().numpy()
+    ref = eng.dlogl_host(seg_of, batches[0], tx[0], precision=gg.PREC_FP64)[0]
+    stat = st.cpu().numpy()
+    ok = (stat == 0) & np.isfinite(ref)
+    err = np.abs(mixed[ok] - ref[ok])
+    # gradient + Fisher of the same proposals
+    tyg = torch.empty(items, dtype=torch.float64, device=dev)
+    grad = torch.empty((items, 8), dtype=torch.float64, device=dev)
+    fis = torch.empty((items, 8, 8), dtype=torch.float64, device=dev)
+    stg = torch.empty(items, dtype=torch.int32, device=dev)
+    with torch.cuda.stream(stream):
+        eng.grad_fisher_device(d_seg, d_b[0], tyg, grad, fis, stg)
+    stream.synchronize()
+    ggraphs = []
+    for b in range(nb):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            eng.grad_fisher_device(d_seg, d_b[b], tyg, grad, fis, stg)
+        ggraphs.append(g)
+    with torch.cuda.stream(stream):
+        for w in range(warmup):
+            ggraphs[w % nb].replay()
+        e0.record(stream)
+        for k in range(grad_steps):
+            ggraphs[k % nb].replay()
+        e1.record(stream)
+    stream.synchronize()
+    t_gr = e0.elapsed_time(e1) / 1e3
+    eng.set_stream(None)
+    Ns = []
+    for p, s in zip(batches[0], seg_of):
+        Ns.append(2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, p[0] / T, p[7] / T / T, p[1], math.exp(p[3]), T, NFFT))
+    Ns = np.array(Ns)
+    eng.close()
+    v_dl = steps * items / t_dl
+    v_gr = grad_steps * items / t_gr
+    return {"workload": "1e4 Galactic sources in 512 segments x 8192 bins, 64 chains x 16 temperatures, "
+                        "update (80%) and birth (20%) proposals, one per source per step",
+            "evals": steps * items, "value": v_dl, "unit": "evals/s", "ms_per_step": 1e3 * t_dl / steps,
+            "reevaluated_per_step": reeval,
+            "N_hist": {str(int(n)): int((Ns == n).sum()) for n in sorted(set(Ns.tolist()))},
+            "grad_fisher": {"value": v_gr, "unit": "evals/s", "ms_per_step": 1e3 * t_gr / grad_steps,
+                            "cost_ratio": (t_gr / grad_steps) / (t_dl / steps),
+                            "ok_items": int((stg.cpu().numpy() == 0).sum())},
+            "accuracy": {"max_abs_dlogl_err_vs_fp64": float(err.max()), "frac_below_1e-3": float((err < 1e-3).mean()),
+                         "evals_compared": int(err.size), "invalid": int((~ok).sum())},
+            "graph": "8 step graphs replayed in turn", "precision": "mixed, 1e-3 tolerance"}
+
+
 def run_ours(args):
     import torch
 
@@ -1186,6 +1463,8 @@ def run_ours(args):
     noise_line = bench_noise(gg, torch, dev, rank, max(5, args.steps // 30), args.warmup, cpu_legs and rank == 0,
                              peak64)
     sampler_line = bench_sampler(gg, torch, dev, max(20, args.steps // 3), args.warmup)
+    c0_line = bench_config0(gg, rank, cpu=cpu_legs and rank == 0)
+    c4_line = bench_config4(gg, torch, dev, rank, steps=max(100, 3 * args.steps), warmup=args.warmup)
 
     if rank == 0:
         line = {
@@ -1225,6 +1504,8 @@ def run_ours(args):
             "fstat": fs_line,
             "noise": noise_line,
             "sampler": sampler_line,
+            "config0_sequential": c0_line,
+            "config4_global_fit": c4_line,
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk,
         }

@@ -19,160 +19,15 @@ from glass_gb300 import workloads as wl
 pytestmark = pytest.mark.gpu
 T = wl.T_YEAR
 REL = 1e-10
-c_int, c_double = ctypes.c_int, ctypes.c_double
-_D = ctypes.POINTER(c_double)
-_DD = ctypes.POINTER(_D)
-_DDD = ctypes.POINTER(_DD)
-
-
-class TDI(ctypes.Structure):
-    """utils/src/glass_lisa.h:116-140"""
-    _fields_ = [("X", _D), ("Y", _D), ("Z", _D), ("A", _D), ("E", _D), ("T", _D), ("Nchannel", c_int), ("N", c_int),
-                ("delta", c_double)]
-
-
-class Noise(ctypes.Structure):
-    """utils/src/glass_data.h:337-360"""
-    _fields_ = [("N", c_int), ("kmin", c_int), ("Nchannel", c_int), ("Nlayer", c_int), ("eta", _D), ("f", _D),
-                ("C", _DDD), ("invC", _DDD), ("logdetC", _D), ("transfer", _D)]
-
-
-class Data(ctypes.Structure):
-    """utils/src/glass_data.h:50-97 (through the format string)"""
-    _fields_ = [("N", c_int), ("NFFT", c_int), ("Nchannel", c_int), ("Nlayer", c_int), ("logN", c_double),
-                ("cseed", ctypes.c_uint), ("nseed", ctypes.c_uint), ("iseed", ctypes.c_uint), ("T", c_double),
-                ("sqT", c_double), ("t0", c_double), ("wdm", ctypes.c_void_p), ("qmin", c_int), ("qmax", c_int),
-                ("qpad", c_int), ("lmin", c_int), ("lmax", c_int), ("fmin", c_double), ("fmax", c_double),
-                ("sine_f_on_fstar", c_double), ("tdi", ctypes.POINTER(TDI)), ("raw", ctypes.POINTER(TDI)),
-                ("dft", ctypes.POINTER(TDI)), ("dwt", ctypes.POINTER(TDI)), ("noise", ctypes.POINTER(Noise)),
-                ("format", ctypes.c_char * 16)]
-
-
-class Source(ctypes.Structure):
-    """utils/src/glass_model.h:81-121"""
-    _fields_ = ([("NP", c_int), ("params", _D), ("tdi", ctypes.POINTER(TDI))]
-                + [(k, c_double) for k in ("f0", "dfdt", "d2fdt2", "amp", "psi", "cosi", "phiref", "phi", "costheta",
-                                           "dL", "tref", "m1", "m2", "Mchirp", "Mtotal", "chi1", "chi2")]
-                + [(k, c_int) for k in ("BW", "qmin", "qmax", "imin", "imax")]
-                + [("fisher_matrix", _DD), ("fisher_evectr", _DD), ("fisher_evalue", _D),
-                   ("fisher_update_flag", c_int), ("list", ctypes.POINTER(c_int)), ("Nlist", c_int)])
-
-
-class Model(ctypes.Structure):
-    """utils/src/glass_model.h:25-60"""
-    _fields_ = [("NP", c_int), ("Nmax", c_int), ("Neff", c_int), ("Nlive", c_int),
-                ("source", ctypes.POINTER(ctypes.POINTER(Source))), ("noise", ctypes.POINTER(Noise)),
-                ("calibration", ctypes.c_void_p), ("tdi", ctypes.POINTER(TDI)), ("residual", ctypes.POINTER(TDI)),
-                ("t0", c_double), ("prior", _DD), ("logPriorVolume", _D), ("logL", c_double),
-                ("logLnorm", c_double), ("list", ctypes.POINTER(c_int)), ("Nlist", c_int),
-                ("log_likelihood", ctypes.c_void_p), ("generate_signal_model", ctypes.c_void_p)]
-
-
-class Orbit(ctypes.Structure):
-    """utils/src/glass_lisa.h:60-109"""
-    _fields_ = [("OrbitFileName", ctypes.c_char * 1024), ("Norb", c_int), ("L", c_double), ("fstar", c_double),
-                ("ecc", c_double), ("R", c_double), ("lambda_0", c_double), ("kappa_0", c_double), ("t", _D),
-                ("x", _DD), ("y", _DD), ("z", _DD), ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p),
-                ("dz", ctypes.c_void_p), ("orbit_function", ctypes.c_void_p)]
-
-
-class Keep:
-    """Holds the numpy arrays behind a struct's pointers."""
-
-    def __init__(self):
-        self.refs = []
-
-    def arr(self, a):
-        a = np.ascontiguousarray(a, np.float64)
-        self.refs.append(a)
-        return a.ctypes.data_as(_D)
-
-    def ptrs(self, rows):
-        p = (_D * len(rows))(*[self.arr(r) for r in rows])
-        self.refs.append(p)
-        return ctypes.cast(p, _DD)
-
-
-def make_tdi(keep, N, nch, A=None, E=None):
-    t = TDI()
-    t.X, t.Y, t.Z, t.T = (keep.arr(np.zeros(N)) for _ in range(4))
-    t.A = keep.arr(np.zeros(N) if A is None else A)
-    t.E = keep.arr(np.zeros(N) if E is None else E)
-    t.Nchannel, t.N = nch, N
-    keep.refs.append(t)
-    return t
-
-
-def make_noise(keep, invCA, invCE):
-    n = Noise()
-    n.N, n.Nchannel = len(invCA), 2
-    rows = [[invCA, np.zeros_like(invCA)], [np.zeros_like(invCA), invCE]]
-    outer = (_DD * 2)(*[keep.ptrs(r) for r in rows])
-    keep.refs.append(outer)
-    n.invC = ctypes.cast(outer, _DDD)
-    n.C = n.invC
-    keep.refs.append(n)
-    return n
-
-
-def make_data(keep, NFFT, qmin, dA, dE, noise, fmt=b"sangria"):
-    d = Data()
-    d.N, d.NFFT, d.Nchannel, d.Nlayer = 2 * NFFT, NFFT, 2, 1
-    d.T, d.sqT, d.t0 = T, np.sqrt(T), 0.0
-    d.qmin, d.qmax = qmin, qmin + NFFT
-    d.tdi = ctypes.pointer(make_tdi(keep, 2 * NFFT, 2, dA, dE))
-    d.noise = ctypes.pointer(noise)
-    d.format = fmt
-    keep.refs.append(d)
-    return d
-
-
-def make_source(keep, params, N, nch=2):
-    s = Source()
-    s.NP = 8
-    s.params = keep.arr(np.array(params, np.float64))
-    s.tdi = ctypes.pointer(make_tdi(keep, N, nch))
-    s.fisher_matrix = keep.ptrs(np.zeros((8, 8)))
-    s.fisher_evectr = keep.ptrs(np.zeros((8, 8)))
-    s.fisher_evalue = keep.arr(np.zeros(8))
-    keep.refs.append(s)
-    return s
-
-
-def make_model(keep, params_list, NFFT, noise):
-    m = Model()
-    srcs = [make_source(keep, p, 2 * NFFT) for p in params_list]
-    arr = (ctypes.POINTER(Source) * max(1, len(srcs)))(*[ctypes.pointer(s) for s in srcs])
-    keep.refs.append(arr)
-    m.NP, m.Nmax, m.Nlive = 8, len(srcs), len(srcs)
-    m.source = ctypes.cast(arr, ctypes.POINTER(ctypes.POINTER(Source)))
-    m.noise = ctypes.pointer(noise)
-    m.tdi = ctypes.pointer(make_tdi(keep, 2 * NFFT, 2))
-    m.residual = ctypes.pointer(make_tdi(keep, 2 * NFFT, 2))
-    keep.refs.append(m)
-    return m, srcs
-
+from glass_gb300.refstructs import (Keep, Orbit, _D, bind_dropins, make_data, make_model, make_noise,
+                                    make_source)
 
 @pytest.fixture(scope="module")
 def lib():
     from glass_gb300 import build
 
     build.build()
-    L = gg.load_library()
-    P = ctypes.POINTER
-    L.initialize_analytic_orbit.argtypes = [P(Orbit)]
-    L.generate_ucb_model.argtypes = [P(Orbit), P(Data), P(Model), c_int]
-    L.update_ucb_model.argtypes = [P(Orbit), P(Data), P(Model), P(Model), c_int]
-    L.gaussian_log_likelihood.argtypes = [P(Data), P(Model)]
-    L.gaussian_log_likelihood.restype = c_double
-    L.snr.argtypes = [P(Source), P(Noise)]
-    L.snr.restype = c_double
-    L.fourier_nwip.argtypes = [_D, _D, _D, c_int]
-    L.fourier_nwip.restype = c_double
-    L.ucb_alignment.argtypes = [P(Orbit), P(Data), P(Source)]
-    L.ucb_fisher.argtypes = [P(Orbit), P(Data), P(Source), P(Noise)]
-    L.matrix_eigenstuff.argtypes = [_DD, _DD, _D, c_int]
-    L.wavelet_transform_timefreq_by_layers.argtypes = [ctypes.c_void_p, c_int, c_int, _D, _D]
+    L = bind_dropins(gg.load_library())
     return L
 
 
