@@ -189,7 +189,14 @@ int glass_gpu_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems, const i
  * batch shape (nitems, precision, term_x given or not) is recorded as a CUDA
  * graph on the first call and replayed on later calls of that shape; a new
  * bank, a new template size or larger buffers drop the recorded graphs.  Not
- * to be called while the context's stream is being captured. */
+ * to be called while the context's stream is being captured.
+ * In the in-place mode the GPU itself reads item_seg, params and term_x and
+ * writes dlogl, term_y, hh and status: every array must be valid, mapped
+ * memory of this process for nitems elements until the call returns.  A bad
+ * pointer is then a GPU memory fault, not a host crash, and it leaves the
+ * context (and every later call on it) in an error state; callers who want a
+ * host-side fault for bad pointers select the staging copies with
+ * glass_gpu_set_host_access(ctx, 0). */
 int glass_gpu_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,
                                const double *params, const double *term_x, double *dlogl, double *term_y, double *hh,
                                int *status);
