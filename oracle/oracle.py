@@ -415,6 +415,18 @@ class Port:
                                    ctypes.byref(hh))
         return dh.value, hh.value
 
+    def fisher_wavelet(self, params, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax, imin, imax, invC):
+        """ucb_fisher_wavelet on one source: (F 8x8, regularised flag)."""
+        lib = self.lib
+        lib.ref_ucb_fisher_wavelet.argtypes = [ctypes.c_double, ctypes.c_double, _D, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_double, ctypes.c_double] + [ctypes.c_int] * 4 + [_D, _D]
+        lib.ref_ucb_fisher_wavelet.restype = ctypes.c_int
+        F = np.zeros(64)
+        reg = lib.ref_ucb_fisher_wavelet(Tobs, t0, _p(np.ascontiguousarray(params, np.float64).copy()), NF, NT,
+                                         wdt, wdf, kmin, kmax, imin, imax,
+                                         _p(np.ascontiguousarray(invC, np.float64).reshape(-1)), _p(F))
+        return F.reshape(8, 8), bool(reg)
+
     def wavelet_delta_logl(self, d, invC, hx, lx, hy, ly):
         d, ic = np.ascontiguousarray(d, np.float64), np.ascontiguousarray(invC, np.float64)
         hx, hy = np.ascontiguousarray(hx, np.float64), np.ascontiguousarray(hy, np.float64)
@@ -522,6 +534,18 @@ class Ref:
         n = self.lib.ref_ucb_waveform_wavelet(Tobs, t0, _p(np.ascontiguousarray(params, np.float64).copy()), NF, NT,
                                               wdt, wdf, kmin, kmax, _pi(lst), _p(xyz[0]), _p(xyz[1]), _p(xyz[2]))
         return lst[:n].copy(), xyz
+
+    def fisher_wavelet(self, params, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax, imin, imax, invC):
+        """ucb_fisher_wavelet on one source: (F 8x8, regularised flag)."""
+        lib = self.lib
+        lib.ref_ucb_fisher_wavelet.argtypes = [ctypes.c_double, ctypes.c_double, _D, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_double, ctypes.c_double] + [ctypes.c_int] * 4 + [_D, _D]
+        lib.ref_ucb_fisher_wavelet.restype = ctypes.c_int
+        F = np.zeros(64)
+        reg = lib.ref_ucb_fisher_wavelet(Tobs, t0, _p(np.ascontiguousarray(params, np.float64).copy()), NF, NT,
+                                         wdt, wdf, kmin, kmax, imin, imax,
+                                         _p(np.ascontiguousarray(invC, np.float64).reshape(-1)), _p(F))
+        return F.reshape(8, 8), bool(reg)
 
     def wavelet_delta_logl(self, d, invC, hx, lx, hy, ly):
         self._wavelet()

@@ -279,6 +279,61 @@ int ref_ucb_waveform_wavelet(double Tobs, double t0, double *params, int NF, int
     return n;
 }
 
+/*
+ * ucb_fisher_wavelet (ucb/src/glass_ucb_waveform.c:524) on one source of a
+ * hand-filled wavelet grid (A = 0) with interpolated analytic orbits:
+ * invC[(3 i + j) N + k] the per-pixel inverse noise covariance of the N =
+ * kmax - kmin pixels, F[64] row-major.  Returns 0, or 1 when the reference
+ * regularised the matrix (an eigenvalue <= 0).
+ */
+int ref_ucb_fisher_wavelet(double Tobs, double t0, double *params, int NF, int NT, double dt, double df,
+                           int kmin, int kmax, int imin, int imax, const double *invC, double *F)
+{
+    struct Orbit *orbit = calloc(1, sizeof(struct Orbit));
+    initialize_interpolated_analytic_orbits(orbit, Tobs, t0);
+    struct Wavelets w;
+    memset(&w, 0, sizeof(w));
+    w.NF = NF;
+    w.NT = NT;
+    w.dt = dt;
+    w.df = df;
+    w.A = 0.0;
+    w.kmin = kmin;
+    w.kmax = kmax;
+    w.imin = imin;
+    w.imax = imax;
+    const int N = kmax - kmin;
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->N = N;
+    data->Nchannel = 3;
+    data->T = Tobs;
+    data->t0 = t0;
+    data->wdm = &w;
+    struct Noise *noise = malloc(sizeof(struct Noise));
+    alloc_noise(noise, N, 1, 3);
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < N; k++) {
+                noise->invC[i][j][k] = invC[(3 * i + j) * N + k];
+                noise->C[i][j][k] = i == j ? 1.0 / invC[(3 * i + j) * N + k] : 0.0;
+            }
+    struct Source *source = malloc(sizeof(struct Source));
+    alloc_source(source, N, UCB_MODEL_NP, 3);
+    for (int p = 0; p < UCB_MODEL_NP; p++) source->params[p] = params[p];
+    map_array_to_ucb_params(source, source->params, Tobs);
+    ucb_fisher_wavelet(orbit, data, source, noise);
+    int reg = 0;
+    for (int i = 0; i < UCB_MODEL_NP; i++) {
+        if (!(source->fisher_evalue[i] > 0)) reg = 1;
+        for (int j = 0; j < UCB_MODEL_NP; j++) F[i * UCB_MODEL_NP + j] = source->fisher_matrix[i][j];
+    }
+    free_source(source);
+    free_noise(noise);
+    free(data);
+    free_orbit(orbit);
+    return reg;
+}
+
 /* orbit node times and positions of initialize_interpolated_analytic_orbits:
  * t[Norb], pos[(3 s + d) Norb + n]; returns Norb */
 int ref_orbit_grid(double Tobs, double t0, double *t, double *pos)

@@ -180,6 +180,28 @@ def fisher_big(ref, rng):
     np.savez_compressed(os.path.join(HERE, "fisher_big.npz"), **{k: np.array(v) for k, v in out.items()})
 
 
+def fisher_wavelet(ref, rng):
+    """ucb_fisher_wavelet (ucb/src/glass_ucb_waveform.c:524) on the 64 x 256
+    test grid of tests/test_wavelet_gpu.py (pixels of layers 10..39, time
+    indices 4..251 counted), five sources of that band with a positive
+    definite matrix (the reference regularises others)."""
+    NF, NT, wdt, Tobs = 64, 256, 15.0 * 64, 2.0**14 * 15.0
+    wdf = 1 / (2 * wdt)
+    kmin, kmax = 10 * NT, 40 * NT
+    imin, imax = 4, NT - 4
+    invC = wl.wavelet_invC(kmax - kmin, NT, kmin, 1e-22)
+    out = {"params": [], "F": []}
+    while len(out["F"]) < 5:
+        p = wl.draw_source(rng, rng.uniform(12 * wdf, 38 * wdf), 10 ** rng.uniform(-22, -21), 1e-14, Tobs)
+        F, reg = ref.fisher_wavelet(p, Tobs, 0.0, NF, NT, wdt, wdf, kmin, kmax, imin, imax, invC)
+        if reg:
+            continue
+        out["params"].append(p)
+        out["F"].append(F)
+    np.savez_compressed(os.path.join(HERE, "fisher_wavelet.npz"), grid=np.array([NF, NT, wdt, Tobs]),
+                        kmin=kmin, kmax=kmax, imin=imin, imax=imax, **{k: np.array(v) for k, v in out.items()})
+
+
 def wdm(ref, rng):
     """WDM windows, forward and inverse transforms on small grids (the window
     exponent is the reference's fixed 6, A = 0), and the per-layer transform."""
@@ -461,7 +483,8 @@ def fisher_draw(ref, rng):
 
 
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
-             "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210}
+             "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210,
+             "fisher_wavelet": 20261211}
 
 
 def main(names=()):
@@ -485,6 +508,7 @@ def main(names=()):
     sampler(ref, np.random.default_rng(OWN_SEEDS["sampler"]))
     fisher_draw(ref, np.random.default_rng(OWN_SEEDS["fisher_draw"]))
     fisher_big(ref, np.random.default_rng(OWN_SEEDS["fisher_big"]))
+    fisher_wavelet(ref, np.random.default_rng(OWN_SEEDS["fisher_wavelet"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -252,3 +252,23 @@ def test_fisher_batch_matches_restated_reference(engine, port):
         scale = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
         np.testing.assert_array_equal(F[s], F[s].T)
         assert (np.abs(F[s] - ref) <= 1e-6 * scale + 1e-300).all(), (s, (np.abs(F[s] - ref) / scale).max())
+
+
+def test_fisher_batch_matches_reference_ucb_fisher_wavelet(engine, golden):
+    """The reference's own ucb_fisher_wavelet (central differences of its
+    wavelet waveform, ucb/src/glass_ucb_waveform.c:524-640) on the same grid:
+    golden matrices from its sources (tests/golden/fisher_wavelet.npz)."""
+    g = golden("fisher_wavelet.npz")
+    NF, NT, wdt, Tobs = (float(x) for x in g["grid"])
+    NF, NT = int(NF), int(NT)
+    kmin, kmax, imin, imax = int(g["kmin"]), int(g["kmax"]), int(g["imin"]), int(g["imax"])
+    engine.wavelet_setup(Tobs, 0.0, NF, NT, wdt, 1 / (2 * wdt), kmin, kmax)
+    invC = wl.wavelet_invC(kmax - kmin, NT, kmin, 1e-22)
+    engine.wavelet_set_data(np.zeros((3, kmax - kmin)), invC)
+    F, st = engine.wavelet_fisher_host(g["params"], imin, imax)
+    assert (st == 0).all()
+    for s in range(len(g["params"])):
+        ref = g["F"][s]
+        scale = np.sqrt(np.outer(np.diag(ref), np.diag(ref)))
+        err = np.abs(F[s] - ref) / scale
+        assert err.max() < 1e-6, (s, err.max(), np.unravel_index(err.argmax(), err.shape))
