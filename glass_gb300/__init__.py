@@ -54,7 +54,7 @@ EXPORTS = (
     "glass_gpu_rand_r_fill", "glass_gpu_mh_accept", "glass_gpu_fisher_draw", "glass_gpu_ptmcmc",
     "glass_gpu_set_mixed_tolerance", "glass_gpu_set_mixed_tolerance_scale", "glass_gpu_mixed_reevaluated",
     "glass_gpu_wdm_by_layers_host", "wavelet_transform_timefreq_by_layers", "glass_gpu_set_tuning",
-    "glass_gpu_get_tuning",
+    "glass_gpu_get_tuning", "glass_gpu_sym_eigen8", "glass_gpu_prior_draw", "glass_gpu_ucb_prior",
     "analytic_orbits", "initialize_analytic_orbit", "map_array_to_ucb_params", "ucb_alignment", "add_ucb_model",
     "remove_ucb_model", "generate_ucb_model", "update_ucb_model", "fourier_nwip", "snr", "gaussian_log_likelihood",
     "matrix_eigenstuff", "ucb_fisher",
@@ -89,6 +89,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_set_mixed_tolerance_scale.argtypes = [_V, ctypes.c_int, _D]
     lib.glass_gpu_mixed_reevaluated.argtypes = [_V, _V]
     lib.glass_gpu_set_tuning.argtypes = [_V, ctypes.c_char_p, ctypes.c_int]
+    lib.glass_gpu_sym_eigen8.argtypes = [_V, ctypes.c_int, _V, _V, _V]
+    lib.glass_gpu_prior_draw.argtypes = [_V, ctypes.c_int, _V, ctypes.c_int, _V, _V, _V, _V]
+    lib.glass_gpu_ucb_prior.argtypes = [_V, ctypes.c_int, _V, _V, ctypes.c_int, _V, _V, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int, _V]
     lib.glass_gpu_get_tuning.argtypes = [_V, ctypes.c_char_p, _V]
     lib.glass_gpu_bank_upload.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                           ctypes.c_int, _I, _D, _D, _D, _D]
@@ -512,6 +516,24 @@ class Engine:
         nens, NC = int(index.shape[0]), int(index.shape[1])
         _check(self.lib.glass_gpu_ptmcmc(self._ctx, nens, NC, _ptr(temperature), _ptr(logL), _ptr(logLnorm),
                                          _ptr(index), _ptr(seed), _ptr(acceptance)))
+
+    def sym_eigen8_device(self, matrix, evec, evalue):
+        """Eigen-decomposition of n symmetric 8x8 matrices (glass_gpu_sym_eigen8)."""
+        n = int(matrix.numel() // 64)
+        _check(self.lib.glass_gpu_sym_eigen8(self._ctx, n, _ptr(matrix), _ptr(evec), _ptr(evalue)))
+
+    def prior_draw_device(self, prior, logPV, seed, params, logQ, per_chain=False):
+        """draw_from_uniform_prior for n chains (glass_gpu_prior_draw)."""
+        n = int(seed.numel())
+        _check(self.lib.glass_gpu_prior_draw(self._ctx, n, _ptr(prior), int(per_chain), _ptr(logPV), _ptr(seed),
+                                             _ptr(params), _ptr(logQ)))
+
+    def ucb_prior_device(self, params, prior, logPV, logP, per_chain=False, skyhist=None, dcostheta=0.0, dphi=0.0,
+                         nphi=0):
+        """evaluate_ucb_prior for n chains (glass_gpu_ucb_prior); params wrapped in place."""
+        n = int(params.numel() // 8)
+        _check(self.lib.glass_gpu_ucb_prior(self._ctx, n, _ptr(params), _ptr(prior), int(per_chain), _ptr(logPV),
+                                            _ptr(skyhist), float(dcostheta), float(dphi), int(nphi), _ptr(logP)))
 
     def fisher_draw_device(self, params_x, evec, evalue, seed, params_y, logQ=None, status=None):
         """draw_from_fisher for n chains (device tensors: params_x/params_y [n, 8],

@@ -1381,6 +1381,59 @@ extern "C" int glass_gpu_fisher_draw(glass_gpu_ctx *ctx, int n, const double *pa
   return GLASS_OK;
 }
 
+extern "C" int glass_gpu_sym_eigen8(glass_gpu_ctx *ctx, int n, const double *matrix, double *evec, double *evalue) {
+  if (!ctx || n < 0) return set_err(GLASS_ERR_ARG, "sym_eigen8: bad argument");
+  if (n == 0) return GLASS_OK;
+  if (!matrix || !evec || !evalue) return set_err(GLASS_ERR_ARG, "sym_eigen8: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  GLASS_CUDA(sym_eigen8_launch(n, matrix, evec, evalue, ctx->stream), "sym_eigen8");
+  ctx->last_launches = 1;
+  return GLASS_OK;
+}
+
+static int prior_args(const char *who, glass_gpu_ctx *ctx, int n, const double *prior, int prior_stride,
+                      const double *logPV, double *params, double *out, PriorArgs &a) {
+  if (!ctx || n < 0 || (prior_stride != 0 && prior_stride != 1)) return set_err(GLASS_ERR_ARG, "%s: bad argument", who);
+  if (n > 0 && (!prior || !logPV || !params || !out)) return set_err(GLASS_ERR_ARG, "%s: null argument", who);
+  a = PriorArgs{};
+  a.n = n;
+  a.prior = prior;
+  a.logPV = logPV;
+  a.stride = prior_stride;
+  a.params = params;
+  a.out = out;
+  return ctx_activate(ctx);
+}
+
+extern "C" int glass_gpu_prior_draw(glass_gpu_ctx *ctx, int n, const double *prior, int prior_stride,
+                                    const double *logPV, unsigned int *seed, double *params, double *logQ) {
+  PriorArgs a;
+  int rc = prior_args("prior_draw", ctx, n, prior, prior_stride, logPV, params, logQ, a);
+  if (rc || n == 0) return rc;
+  if (!seed) return set_err(GLASS_ERR_ARG, "prior_draw: null seed");
+  a.seed = seed;
+  GLASS_CUDA(prior_draw_launch(a, ctx->stream), "prior_draw");
+  ctx->last_launches = 1;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_ucb_prior(glass_gpu_ctx *ctx, int n, double *params, const double *prior, int prior_stride,
+                                   const double *logPV, const double *skyhist, double dcostheta, double dphi, int nphi,
+                                   double *logP) {
+  PriorArgs a;
+  int rc = prior_args("ucb_prior", ctx, n, prior, prior_stride, logPV, params, logP, a);
+  if (rc || n == 0) return rc;
+  if (skyhist && !(dcostheta > 0 && dphi > 0 && nphi > 0)) return set_err(GLASS_ERR_ARG, "ucb_prior: bad sky grid");
+  a.skyhist = skyhist;
+  a.dcostheta = dcostheta;
+  a.dphi = dphi;
+  a.nphi = nphi;
+  GLASS_CUDA(ucb_prior_launch(a, ctx->stream), "ucb_prior");
+  ctx->last_launches = 1;
+  return GLASS_OK;
+}
+
 // ------------------------------------------------------- drop-in functions
 // Layout of struct Orbit (utils/src/glass_lisa.h:60-109), restated so the
 // drop-in ucb_waveform can read the arm length, transfer frequency and the

@@ -274,7 +274,188 @@ __global__ void ptmcmc_kernel(PtArgs a) {
   }
 }
 
+// Eigen-decomposition of one symmetric 8x8 matrix per thread (the Fisher
+// matrix of a chain, for draw_from_fisher without a trip to the host), as
+// the drop-in matrix_eigenstuff does it: cyclic Jacobi rotations until every
+// off-diagonal entry is negligible against its two diagonal entries (every
+// eigenvalue to full relative accuracy), pairs sorted by decreasing
+// eigenvalue, each unit eigenvector's largest component positive.
+// evec[64 i + 8 j + k] = component j of eigenvector k (fisher_evectr[j][k]).
+__global__ void __launch_bounds__(32) sym_eigen8_kernel(int n, const double *matrix, double *evec, double *evalue) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double a[8][8], v[8][8];
+  const double *m = matrix + 64 * (size_t)i;
+  for (int r = 0; r < 8; r++)
+    for (int c = 0; c < 8; c++) {
+      a[r][c] = 0.5 * (m[8 * r + c] + m[8 * c + r]);
+      v[r][c] = r == c ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 64; sweep++) {
+    int rotations = 0;
+    for (int p = 0; p < 8; p++)
+      for (int q = p + 1; q < 8; q++) {
+        const double apq = a[p][q], app = a[p][p], aqq = a[q][q];
+        if (!(fabs(apq) > 1e-18 * sqrt(fabs(app * aqq))) || !(fabs(apq) > 1e-300)) continue;
+        rotations++;
+        const double theta = (aqq - app) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < 8; k++) {
+          const double akp = a[k][p], akq = a[k][q];
+          a[k][p] = c * akp - s * akq;
+          a[k][q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 8; k++) {
+          const double apk = a[p][k], aqk = a[q][k];
+          a[p][k] = c * apk - s * aqk;
+          a[q][k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < 8; k++) {
+          const double vkp = v[k][p], vkq = v[k][q];
+          v[k][p] = c * vkp - s * vkq;
+          v[k][q] = s * vkp + c * vkq;
+        }
+      }
+    if (rotations == 0) break;
+  }
+  int ord[8];
+  for (int j = 0; j < 8; j++) ord[j] = j;
+  for (int x = 1; x < 8; x++)
+    for (int j = x; j > 0 && a[ord[j]][ord[j]] > a[ord[j - 1]][ord[j - 1]]; j--) {
+      const int t = ord[j];
+      ord[j] = ord[j - 1];
+      ord[j - 1] = t;
+    }
+  double *ev = evec + 64 * (size_t)i;
+  for (int j = 0; j < 8; j++) {
+    const int c = ord[j];
+    evalue[8 * (size_t)i + j] = a[c][c];
+    int big = 0;
+    for (int r = 1; r < 8; r++)
+      if (fabs(v[r][c]) > fabs(v[big][c])) big = r;
+    const double sg = v[big][c] < 0.0 ? -1.0 : 1.0;
+    for (int r = 0; r < 8; r++) ev[8 * r + j] = sg * v[r][c];
+  }
+}
+
+// draw_from_uniform_prior (utils/src/glass_sampler.c:96-107), one thread per
+// chain: the eight parameters from rand_r_U_0_1 in order, logQ = -sum of the
+// log prior volumes.
+__global__ void prior_draw_kernel(PriorArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double *pr = a.prior + 16 * (size_t)i * a.stride;
+  const double *lv = a.logPV + 8 * (size_t)i * a.stride;
+  unsigned int s = a.seed[i];
+  double logQ = 0.0;
+  for (int k = 0; k < 8; k++) {
+    a.params[8 * (size_t)i + k] = pr[2 * k] + glass_u01(&s) * (pr[2 * k + 1] - pr[2 * k]);
+    logQ -= lv[k];
+  }
+  a.seed[i] = s;
+  a.out[i] = logQ;
+}
+
+// evaluate_ucb_prior (ucb/src/glass_ucb_prior.c:536-556) on the blind-search
+// path (no catalogue prior): check_range (:400-438, which wraps longitude,
+// polarisation and phase in place), the sky-location prior (:590-639,
+// uniform or the galaxy histogram) and evaluate_uniform_priors (:560-588).
+__global__ void ucb_prior_kernel(PriorArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double *pr = a.prior + 16 * (size_t)i * a.stride;
+  const double *lv = a.logPV + 8 * (size_t)i * a.stride;
+  double *p = a.params + 8 * (size_t)i;
+  const double twopi = 6.283185307179586;
+  auto lo = [&](int k) { return pr[2 * k]; };
+  auto hi = [&](int k) { return pr[2 * k + 1]; };
+  // check_range
+  bool bad = false;
+  for (int k = 0; k < 8; k++)
+    if (p[k] != p[k]) bad = true;
+  if (!bad && (p[0] < lo(0) || p[0] > hi(0))) bad = true;
+  if (!bad && (p[1] < lo(1) || p[1] > hi(1))) bad = true;
+  if (!bad && (p[2] < lo(2) || p[2] >= hi(2))) {
+    p[2] = atan2(sin(p[2]), cos(p[2]));
+    if (p[2] < 0.0) p[2] += twopi;
+  }
+  if (!bad && (p[3] < lo(3) || p[3] > hi(3))) bad = true;
+  if (!bad && (p[4] < lo(4) || p[4] > hi(4))) bad = true;
+  if (!bad) {
+    for (int it = 0; it < 64 && p[5] < lo(5); it++) p[5] += M_PI;
+    for (int it = 0; it < 64 && p[5] > hi(5); it++) p[5] -= M_PI;
+    for (int it = 0; it < 64 && p[6] < lo(6); it++) p[6] += twopi;
+    for (int it = 0; it < 64 && p[6] > hi(6); it++) p[6] -= twopi;
+    if (p[7] < lo(7) || p[7] > hi(7)) bad = true;
+  }
+  if (bad) {
+    a.out[i] = -INFINITY;
+    return;
+  }
+  double logP = 0.0;
+  // sky location
+  if (a.skyhist) {
+    if (p[1] < lo(1) || p[1] > hi(1)) {
+      a.out[i] = -INFINITY;
+      return;
+    }
+    if (lo(2) > 0.0 || hi(2) < twopi) {
+      if (p[2] < lo(2) || p[2] > hi(2)) {
+        a.out[i] = -INFINITY;
+        return;
+      }
+    } else {
+      for (int it = 0; it < 64 && p[2] < 0; it++) p[2] += twopi;
+      for (int it = 0; it < 64 && p[2] > twopi; it++) p[2] -= twopi;
+    }
+    const int ci = (int)floor((p[1] - lo(1)) / a.dcostheta);
+    const int cj = (int)floor((p[2] - lo(2)) / a.dphi);
+    logP += a.skyhist[ci * a.nphi + cj];
+  } else {
+    if (p[1] < lo(1) || p[1] > hi(1)) {
+      a.out[i] = -INFINITY;
+      return;
+    }
+    logP -= lv[1];
+    if (lo(2) > 0.0 || hi(2) < twopi) {
+      if (p[2] < lo(2) || p[2] > hi(2)) {
+        a.out[i] = -INFINITY;
+        return;
+      }
+    } else if (p[2] < lo(2) || p[2] >= hi(2)) {
+      p[2] = atan2(sin(p[2]), cos(p[2]));
+      if (p[2] < 0.0) p[2] += twopi;
+    }
+    logP -= lv[2];
+  }
+  // evaluate_uniform_priors (its own range check passes: params are in range now)
+  logP -= log(hi(0) - lo(0));
+  logP -= lv[3];
+  logP -= lv[4];
+  logP -= lv[5];
+  logP -= lv[6];
+  logP -= lv[7];
+  a.out[i] = logP;
+}
+
 }  // namespace
+
+cudaError_t sym_eigen8_launch(int n, const double *matrix, double *evec, double *evalue, cudaStream_t stream) {
+  // one warp per CTA: the chains' FP64 rotations spread over the SMs
+  sym_eigen8_kernel<<<(n + 31) / 32, 32, 0, stream>>>(n, matrix, evec, evalue);
+  return cudaGetLastError();
+}
+
+cudaError_t prior_draw_launch(const PriorArgs &a, cudaStream_t stream) {
+  prior_draw_kernel<<<(a.n + 31) / 32, 32, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t ucb_prior_launch(const PriorArgs &a, cudaStream_t stream) {
+  ucb_prior_kernel<<<(a.n + 31) / 32, 32, 0, stream>>>(a);
+  return cudaGetLastError();
+}
 
 cudaError_t rand_r_fill_launch(int n, int count, unsigned int *seed, int *out, cudaStream_t stream) {
   rand_r_fill_kernel<<<(n + 127) / 128, 128, 0, stream>>>(n, count, seed, out);

@@ -403,6 +403,40 @@ int glass_gpu_ptmcmc(glass_gpu_ctx *ctx, int nens, int NC, const double *tempera
 int glass_gpu_fisher_draw(glass_gpu_ctx *ctx, int n, const double *params_x, const double *evec, const double *evalue,
                           unsigned int *seed, double *params_y, double *logQ, int *status);
 
+/*
+ * glass_gpu_sym_eigen8: the eigen-decomposition matrix_eigenstuff
+ * (utils/src/glass_math.c:475-499) gives a chain's Fisher matrix, for n
+ * symmetric 8x8 matrices (matrix[64 i + 8 r + c]), so that
+ * glass_gpu_grad_fisher_batch -> glass_gpu_sym_eigen8 -> glass_gpu_fisher_draw
+ * runs without the host: evec[64 i + 8 j + k] = component j of eigenvector k,
+ * evalue[8 i + k]; cyclic Jacobi rotations in FP64 (every eigenvalue to full
+ * relative accuracy), pairs sorted by decreasing eigenvalue, each vector's
+ * largest component positive (the drop-in matrix_eigenstuff's convention;
+ * LAPACK's order and signs are not reproduced).
+ *
+ * glass_gpu_prior_draw: draw_from_uniform_prior (utils/src/glass_sampler.c:96-107)
+ * for n chains: params[8 i + k] = prior[2 k] + rand_r_U_0_1 (prior[2 k + 1] -
+ * prior[2 k]) in order k = 0..7, logQ[i] = -sum logPV[k]; prior[16 c ..] the
+ * model's bounds and logPV[8 c ..] its log prior volumes, c = i prior_stride
+ * (0: one model for all chains, 1: one per chain).  Seeds advance as the
+ * reference's.
+ *
+ * glass_gpu_ucb_prior: evaluate_ucb_prior (ucb/src/glass_ucb_prior.c:536-556)
+ * without the catalogue (GMM) prior: check_range (:400-438: NaN or a bound
+ * violated gives -inf; longitude, polarisation and phase are wrapped into
+ * range IN PLACE in params, as the reference does), the sky-location prior
+ * (:590-639: skyhist[i nphi + j] over cells dcostheta x dphi from the lower
+ * bounds when skyhist is given, else uniform) and evaluate_uniform_priors
+ * (:560-588).  The wrapping loops stop after 64 turns (the reference's do not).
+ * All pointers DEVICE pointers; asynchronous.
+ */
+int glass_gpu_sym_eigen8(glass_gpu_ctx *ctx, int n, const double *matrix, double *evec, double *evalue);
+int glass_gpu_prior_draw(glass_gpu_ctx *ctx, int n, const double *prior, int prior_stride, const double *logPV,
+                         unsigned int *seed, double *params, double *logQ);
+int glass_gpu_ucb_prior(glass_gpu_ctx *ctx, int n, double *params, const double *prior, int prior_stride,
+                        const double *logPV, const double *skyhist, double dcostheta, double dphi, int nphi,
+                        double *logP);
+
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 

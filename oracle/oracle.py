@@ -415,6 +415,29 @@ class Port:
                                    ctypes.byref(hh))
         return dh.value, hh.value
 
+    def draw_uniform_prior(self, prior16, logPV8, seed):
+        """draw_from_uniform_prior: (params, logQ, seed after)."""
+        lib = self.lib
+        lib.ref_draw_uniform_prior.argtypes = [_D, _D, ctypes.POINTER(ctypes.c_uint), _D]
+        lib.ref_draw_uniform_prior.restype = ctypes.c_double
+        s = ctypes.c_uint(int(seed))
+        p = np.zeros(8)
+        q = lib.ref_draw_uniform_prior(_p(np.ascontiguousarray(prior16, np.float64)),
+                                       _p(np.ascontiguousarray(logPV8, np.float64)), ctypes.byref(s), _p(p))
+        return p, q, s.value
+
+    def ucb_prior(self, params, prior16, logPV8, skyhist=None, dcostheta=0.0, dphi=0.0, nphi=0):
+        """evaluate_ucb_prior (no catalogue prior): (logP, params after wrapping)."""
+        lib = self.lib
+        lib.ref_ucb_prior.argtypes = [_D, _D, _D, ctypes.c_int, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        lib.ref_ucb_prior.restype = ctypes.c_double
+        p = np.ascontiguousarray(params, np.float64).copy()
+        sh = None if skyhist is None else np.ascontiguousarray(skyhist, np.float64)
+        lp = lib.ref_ucb_prior(_p(p), _p(np.ascontiguousarray(prior16, np.float64)),
+                               _p(np.ascontiguousarray(logPV8, np.float64)), int(sh is not None),
+                               _p(sh) if sh is not None else None, dcostheta, dphi, nphi)
+        return lp, p
+
     def fisher_wavelet(self, params, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax, imin, imax, invC):
         """ucb_fisher_wavelet on one source: (F 8x8, regularised flag)."""
         lib = self.lib
@@ -534,6 +557,29 @@ class Ref:
         n = self.lib.ref_ucb_waveform_wavelet(Tobs, t0, _p(np.ascontiguousarray(params, np.float64).copy()), NF, NT,
                                               wdt, wdf, kmin, kmax, _pi(lst), _p(xyz[0]), _p(xyz[1]), _p(xyz[2]))
         return lst[:n].copy(), xyz
+
+    def draw_uniform_prior(self, prior16, logPV8, seed):
+        """draw_from_uniform_prior: (params, logQ, seed after)."""
+        lib = self.lib
+        lib.ref_draw_uniform_prior.argtypes = [_D, _D, ctypes.POINTER(ctypes.c_uint), _D]
+        lib.ref_draw_uniform_prior.restype = ctypes.c_double
+        s = ctypes.c_uint(int(seed))
+        p = np.zeros(8)
+        q = lib.ref_draw_uniform_prior(_p(np.ascontiguousarray(prior16, np.float64)),
+                                       _p(np.ascontiguousarray(logPV8, np.float64)), ctypes.byref(s), _p(p))
+        return p, q, s.value
+
+    def ucb_prior(self, params, prior16, logPV8, skyhist=None, dcostheta=0.0, dphi=0.0, nphi=0):
+        """evaluate_ucb_prior (no catalogue prior): (logP, params after wrapping)."""
+        lib = self.lib
+        lib.ref_ucb_prior.argtypes = [_D, _D, _D, ctypes.c_int, _D, ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        lib.ref_ucb_prior.restype = ctypes.c_double
+        p = np.ascontiguousarray(params, np.float64).copy()
+        sh = None if skyhist is None else np.ascontiguousarray(skyhist, np.float64)
+        lp = lib.ref_ucb_prior(_p(p), _p(np.ascontiguousarray(prior16, np.float64)),
+                               _p(np.ascontiguousarray(logPV8, np.float64)), int(sh is not None),
+                               _p(sh) if sh is not None else None, dcostheta, dphi, nphi)
+        return lp, p
 
     def fisher_wavelet(self, params, Tobs, t0, NF, NT, wdt, wdf, kmin, kmax, imin, imax, invC):
         """ucb_fisher_wavelet on one source: (F 8x8, regularised flag)."""

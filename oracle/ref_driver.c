@@ -845,3 +845,43 @@ double ref_fisher_draw(const double *x, const double *evec, const double *evalue
     s.fisher_evectr = rowp;
     return draw_from_fisher(NULL, NULL, &s, NULL, y, seed);
 }
+
+
+/* draw_from_uniform_prior (utils/src/glass_sampler.c:96) with UCB_MODEL_NP
+ * parameters: prior16[2 k + {0, 1}] the bounds, logPV8 the log volumes;
+ * returns logQ, advances *seed. */
+double ref_draw_uniform_prior(const double *prior16, const double *logPV8, unsigned int *seed, double *params)
+{
+    struct Model m;
+    memset(&m, 0, sizeof(m));
+    double *rows[UCB_MODEL_NP];
+    for (int k = 0; k < UCB_MODEL_NP; k++) rows[k] = (double *)prior16 + 2 * k;
+    m.NP = UCB_MODEL_NP;
+    m.prior = rows;
+    m.logPriorVolume = (double *)logPV8;
+    return draw_from_uniform_prior(NULL, &m, NULL, NULL, params, seed);
+}
+
+/* evaluate_ucb_prior (ucb/src/glass_ucb_prior.c:536) without the catalogue
+ * prior; galaxy != 0 uses skyhist[i nphi + j].  params may be wrapped in place. */
+double ref_ucb_prior(double *params, const double *prior16, const double *logPV8, int galaxy, double *skyhist,
+                     double dcostheta, double dphi, int nphi)
+{
+    struct Flags flags;
+    memset(&flags, 0, sizeof(flags));
+    flags.galaxyPrior = galaxy;
+    struct Model m;
+    memset(&m, 0, sizeof(m));
+    double *rows[UCB_MODEL_NP];
+    for (int k = 0; k < UCB_MODEL_NP; k++) rows[k] = (double *)prior16 + 2 * k;
+    m.NP = UCB_MODEL_NP;
+    m.prior = rows;
+    m.logPriorVolume = (double *)logPV8;
+    struct Prior pr;
+    memset(&pr, 0, sizeof(pr));
+    pr.skyhist = skyhist;
+    pr.dcostheta = dcostheta;
+    pr.dphi = dphi;
+    pr.nphi = nphi;
+    return evaluate_ucb_prior(&flags, NULL, &m, &pr, params);
+}

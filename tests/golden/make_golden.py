@@ -202,6 +202,47 @@ def fisher_wavelet(ref, rng):
                         kmin=kmin, kmax=kmax, imin=imin, imax=imax, **{k: np.array(v) for k, v in out.items()})
 
 
+def priors(ref, rng):
+    """draw_from_uniform_prior (utils/src/glass_sampler.c:96) for 64 chains,
+    three draws each, and evaluate_ucb_prior (ucb/src/glass_ucb_prior.c:536)
+    on 200 parameter sets (in range, out of range, NaN, wrapped longitude,
+    polarisation and phase) with the uniform sky and with a sky histogram."""
+    T = wl.T_YEAR
+    q0 = 1000.0
+    prior = np.array([[q0, q0 + 512.0], [-1.0, 1.0], [0.0, 2 * np.pi], [np.log(1e-24), np.log(1e-20)],
+                      [-1.0, 1.0], [0.0, np.pi], [0.0, 2 * np.pi], [-10.0, 10.0]])
+    logPV = np.log(prior[:, 1] - prior[:, 0])
+    seeds0 = rng.integers(1, 2**31, 64).astype(np.uint32)
+    draws, logQ, seeds = [], [], []
+    s = seeds0.copy()
+    for k in range(3):
+        row_p, row_q = [], []
+        for c in range(64):
+            p, q, s[c] = ref.draw_uniform_prior(prior.reshape(-1), logPV, int(s[c]))
+            row_p.append(p)
+            row_q.append(q)
+        draws.append(row_p), logQ.append(row_q), seeds.append(s.copy())
+    params = np.column_stack([rng.uniform(q0 - 20, q0 + 532, 200), rng.uniform(-1.1, 1.1, 200),
+                              rng.uniform(-7, 14, 200), rng.uniform(np.log(1e-25), np.log(1e-19), 200),
+                              rng.uniform(-1.05, 1.05, 200), rng.uniform(-4, 7, 200), rng.uniform(-8, 15, 200),
+                              rng.uniform(-11, 11, 200)])
+    params[5, 3] = np.nan
+    nphi, ncos = 16, 8
+    skyhist = np.log(rng.uniform(0.5, 2.0, ncos * nphi) / (4 * np.pi))
+    lp_u, p_u, lp_g, p_g = [], [], [], []
+    for p in params:
+        a, b = ref.ucb_prior(p, prior.reshape(-1), logPV)
+        lp_u.append(a), p_u.append(b)
+        a, b = ref.ucb_prior(p, prior.reshape(-1), logPV, skyhist, 2.0 / ncos, 2 * np.pi / nphi, nphi)
+        lp_g.append(a), p_g.append(b)
+    np.savez_compressed(os.path.join(HERE, "priors.npz"), prior=prior, logPV=logPV, seeds0=seeds0,
+                        draws=np.array(draws), logQ=np.array(logQ), seeds=np.array(seeds), params=params,
+                        logP_uniform=np.array(lp_u), params_uniform=np.array(p_u), skyhist=skyhist, nphi=nphi,
+                        dcostheta=2.0 / ncos, dphi=2 * np.pi / nphi, logP_galaxy=np.array(lp_g),
+                        params_galaxy=np.array(p_g))
+    del T
+
+
 def wdm(ref, rng):
     """WDM windows, forward and inverse transforms on small grids (the window
     exponent is the reference's fixed 6, A = 0), and the per-layer transform."""
@@ -484,7 +525,7 @@ def fisher_draw(ref, rng):
 
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
              "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210,
-             "fisher_wavelet": 20261211}
+             "fisher_wavelet": 20261211, "priors": 20261212}
 
 
 def main(names=()):
@@ -509,6 +550,7 @@ def main(names=()):
     fisher_draw(ref, np.random.default_rng(OWN_SEEDS["fisher_draw"]))
     fisher_big(ref, np.random.default_rng(OWN_SEEDS["fisher_big"]))
     fisher_wavelet(ref, np.random.default_rng(OWN_SEEDS["fisher_wavelet"]))
+    priors(ref, np.random.default_rng(OWN_SEEDS["priors"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

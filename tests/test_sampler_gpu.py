@@ -163,3 +163,111 @@ def test_fisher_draw_many_chains(engine, port):
         np.testing.assert_array_equal(sd, s)
         np.testing.assert_array_equal(q, qr)
         np.testing.assert_allclose(y, yr, rtol=1e-14, atol=0)
+
+
+def test_prior_draw_matches_reference(engine, golden):
+    """draw_from_uniform_prior: three successive draws of 64 chains, bit for
+    bit (parameters, logQ and the seeds after each draw)."""
+    import torch
+
+    g = golden("priors.npz")
+    prior = torch.tensor(g["prior"].reshape(-1), device="cuda")
+    logPV = torch.tensor(g["logPV"], device="cuda")
+    seed = torch.tensor(_u32(g["seeds0"]), device="cuda")
+    params = torch.empty((64, 8), dtype=torch.float64, device="cuda")
+    logQ = torch.empty(64, dtype=torch.float64, device="cuda")
+    for k in range(3):
+        engine.prior_draw_device(prior, logPV, seed, params, logQ)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(params.cpu().numpy(), g["draws"][k])
+        np.testing.assert_array_equal(logQ.cpu().numpy(), g["logQ"][k])
+        np.testing.assert_array_equal(seed.cpu().numpy().view(np.uint32), g["seeds"][k])
+
+
+def test_ucb_prior_matches_reference(engine, golden):
+    """evaluate_ucb_prior on 200 parameter sets, uniform and galaxy sky:
+    the same -inf decisions, log priors and wrapped parameters."""
+    import torch
+
+    g = golden("priors.npz")
+    prior = torch.tensor(g["prior"].reshape(-1), device="cuda")
+    logPV = torch.tensor(g["logPV"], device="cuda")
+    sky = torch.tensor(g["skyhist"], device="cuda")
+    for key, kw in (("uniform", {}), ("galaxy", dict(skyhist=sky, dcostheta=float(g["dcostheta"]),
+                                                        dphi=float(g["dphi"]), nphi=int(g["nphi"])))):
+        p = torch.tensor(g["params"], device="cuda")
+        lp = torch.empty(len(g["params"]), dtype=torch.float64, device="cuda")
+        engine.ucb_prior_device(p, prior, logPV, lp, **kw)
+        torch.cuda.synchronize()
+        ref = g[f"logP_{key}"]
+        got = lp.cpu().numpy()
+        np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
+        fin = np.isfinite(ref)
+        np.testing.assert_allclose(got[fin], ref[fin], rtol=1e-14, atol=0)
+        # the reference wraps longitude, polarisation and phase in place
+        np.testing.assert_allclose(p.cpu().numpy()[fin], g[f"params_{key}"][fin], rtol=1e-13, atol=1e-13)
+
+
+def test_device_fisher_jump_pipeline(engine, port, golden):
+    """gradient/Fisher kernel -> device eigen-decomposition -> draw_from_fisher
+    with no host round trip: the decomposition reconstructs each Fisher matrix
+    (sorted eigenvalues, unit vectors), agrees with the drop-in
+    matrix_eigenstuff, and the jumps drawn from it equal those drawn from the
+    host decomposition."""
+    import ctypes
+
+    import torch
+
+    from glass_gb300 import workloads as wl
+    from glass_gb300.refstructs import Keep, bind_dropins
+
+    g = golden("fisher.npz")
+    T = wl.T_YEAR
+    invC = g["invC"][0]
+    zero = np.zeros((1, 1024), complex)
+    engine.upload(wl.SegmentBank(T=T, NFFT=1024, qmin=np.array([g["qmin"][0]], np.int32), dA=zero, dE=zero,
+                                 invCA=invC[None], invCE=invC[None]))
+    rng = np.random.default_rng(12)
+    base = g["params"][0]
+    props = base + rng.standard_normal((96, 8)) * wl.jump_scales(base, 30.0)
+    props[:, 1] = np.clip(props[:, 1], -0.99, 0.99)
+    props[:, 4] = np.clip(props[:, 4], -0.99, 0.99)
+    n = len(props)
+    d_seg = torch.zeros(n, dtype=torch.int32, device="cuda")
+    d_p = torch.tensor(props, device="cuda")
+    ty = torch.empty(n, dtype=torch.float64, device="cuda")
+    grad = torch.empty((n, 8), dtype=torch.float64, device="cuda")
+    F = torch.empty((n, 8, 8), dtype=torch.float64, device="cuda")
+    st = torch.empty(n, dtype=torch.int32, device="cuda")
+    evec = torch.empty((n, 8, 8), dtype=torch.float64, device="cuda")
+    eval_ = torch.empty((n, 8), dtype=torch.float64, device="cuda")
+    seeds0 = rng.integers(1, 2**31, n).astype(np.uint32)
+    seed = torch.tensor(_u32(seeds0), device="cuda")
+    y = torch.empty((n, 8), dtype=torch.float64, device="cuda")
+    engine.grad_fisher_device(d_seg, d_p, ty, grad, F, st)
+    engine.sym_eigen8_device(F, evec, eval_)
+    engine.fisher_draw_device(d_p, evec, eval_, seed, y)
+    torch.cuda.synchronize()
+    Fh, V, lam = F.cpu().numpy(), evec.cpu().numpy(), eval_.cpu().numpy()
+    assert (st.cpu().numpy() == 0).all()
+    L = bind_dropins(gg.load_library())
+    Vh, lh = np.zeros_like(V), np.zeros_like(lam)
+    for i in range(n):
+        assert (np.diff(lam[i]) <= 0).all()
+        np.testing.assert_allclose(np.linalg.norm(V[i], axis=0), 1.0, rtol=1e-12)
+        np.testing.assert_allclose(V[i] @ np.diag(lam[i]) @ V[i].T, Fh[i], rtol=0, atol=1e-10 * np.abs(Fh[i]).max())
+        # the drop-in on the host: the same convention
+        keep = Keep()
+        vp = keep.ptrs(np.zeros((8, 8)))
+        L.matrix_eigenstuff(keep.ptrs(Fh[i]), vp, lh[i].ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 8)
+        Vh[i] = np.array([[vp[r][c] for c in range(8)] for r in range(8)])
+    np.testing.assert_allclose(lh, lam, rtol=1e-9, atol=0)
+    # the same draw from the host decomposition: the same chains' choices and seeds,
+    # jumps equal to the decompositions' agreement
+    seed2 = torch.tensor(_u32(seeds0), device="cuda")
+    y2 = torch.empty_like(y)
+    engine.fisher_draw_device(d_p, torch.tensor(Vh, device="cuda"), torch.tensor(lh, device="cuda"), seed2, y2)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(seed.cpu().numpy(), seed2.cpu().numpy())
+    jump, jump2 = y.cpu().numpy() - props, y2.cpu().numpy() - props
+    np.testing.assert_allclose(jump, jump2, rtol=1e-6, atol=1e-9 * np.abs(jump).max())
