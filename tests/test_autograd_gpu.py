@@ -98,7 +98,7 @@ def test_autograd_function_matches_central_differences(engine, port):
     assert err.max() < 2e-3, err.max(axis=0)
     # forward value: the FP64 term to the mixed path's accuracy
     t64 = engine.dlogl_host(seg, props, precision=gg.PREC_FP64)[1]
-    assert abs(float(y) - float((t64 / Tn).sum())) < 1e-3 * len(seg)
+    assert abs(float(y.detach()) - float((t64 / Tn).sum())) < 1e-3 * len(seg)
 
 
 def test_fisher_is_the_gauss_newton_hessian_of_the_term(engine, port):
