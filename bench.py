@@ -1517,6 +1517,39 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile_step(args):
+    """The headline workload's mixed step launched eagerly (no graph) `steps`
+    times in one tolerance mode, for a profiler's launch list and kernel
+    captures (python bench.py --profile-step flat --steps 5)."""
+    import torch
+
+    import glass_gb300 as gg
+
+    dev = torch.device("cuda", 0)
+    nb = max(1, args.steps)
+    bank, inj, Ns, item_seg, temps, rng = make_workload(0, nb)
+    eng = gg.Engine(0)
+    eng.upload(bank)
+    _, t_inj, hh_inj, _ = eng.dlogl_host(np.arange(NSEG, dtype=np.int32), inj, precision=gg.PREC_FP64)
+    batches = draw_batches(rng, inj, np.sqrt(np.maximum(hh_inj, 1.0)), item_seg, temps, nb)
+    tol, scale = {"flat": (1e-3, None), "tempered": (1e-3, temps), "raw": (0.0, None)}[args.profile_step]
+    eng.set_mixed_tolerance(tol)
+    eng.set_mixed_tolerance_scale(scale)
+    n = len(item_seg)
+    d_seg = torch.from_numpy(item_seg).to(dev)
+    d_b = torch.from_numpy(batches).to(dev)
+    d_tx = torch.from_numpy(t_inj[item_seg]).to(dev)
+    outs = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(3)]
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+    n0 = eng.mixed_reevaluated()
+    for k in range(nb):
+        eng.dlogl_device(d_seg, d_b[k], *outs, st, term_x=d_tx, precision=gg.PREC_MIXED)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_step": args.profile_step, "steps": nb, "proposals_per_step": n,
+                      "reevaluated_per_step": (eng.mixed_reevaluated() - n0) / nb}), flush=True)
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1525,11 +1558,15 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--profile-step", choices=["flat", "tempered", "raw"], default=None,
+                    help="only the headline step, launched eagerly, for a profiler")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.profile_step:
+        run_profile_step(args)
     else:
         run_ours(args)
 
