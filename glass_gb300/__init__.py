@@ -57,7 +57,9 @@ EXPORTS = (
     "glass_gpu_get_tuning", "glass_gpu_sym_eigen8", "glass_gpu_prior_draw", "glass_gpu_ucb_prior",
     "analytic_orbits", "initialize_analytic_orbit", "map_array_to_ucb_params", "ucb_alignment", "add_ucb_model",
     "remove_ucb_model", "generate_ucb_model", "update_ucb_model", "fourier_nwip", "snr", "gaussian_log_likelihood",
-    "matrix_eigenstuff", "ucb_fisher",
+    "matrix_eigenstuff", "ucb_fisher", "wavelet_nwip", "snr_wavelet", "delta_log_likelihood", "ucb_fisher_wavelet",
+    "glass_gpu_noise_sgwb_setup", "glass_gpu_noise_logl_batch_sgwb", "glass_gpu_noise_logl_batch_sgwb_host",
+    "glass_gpu_noise_wavelet_logl_batch_sgwb", "glass_gpu_noise_wavelet_logl_batch_sgwb_host",
 )
 
 _lib = None
@@ -138,6 +140,11 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                                                   ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]
     lib.glass_gpu_noise_wavelet_logl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V]
     lib.glass_gpu_noise_wavelet_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D]
+    lib.glass_gpu_noise_sgwb_setup.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D]
+    lib.glass_gpu_noise_logl_batch_sgwb.argtypes = [_V, ctypes.c_int, _V, _V, _V, _V]
+    lib.glass_gpu_noise_logl_batch_sgwb_host.argtypes = [_V, ctypes.c_int, _D, _D, _D, _D]
+    lib.glass_gpu_noise_wavelet_logl_batch_sgwb.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V]
+    lib.glass_gpu_noise_wavelet_logl_batch_sgwb_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D, _D]
     lib.glass_gpu_dlogl_batch_channels.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 8
     lib.glass_gpu_noise_eta_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 6
     lib.glass_gpu_noise_eta_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D, _D, _I]
@@ -445,19 +452,30 @@ class Engine:
         X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
         _check(self.lib.glass_gpu_noise_setup(self._ctx, float(T), int(qmin), len(X) // 2, _pd(X), _pd(Y), _pd(Z)))
 
-    def noise_logl_host(self, inst, sgal=None):
-        """my_noise_log_likelihood of each noise model: inst [n, 12], sgal [n, 5] or None."""
+    def noise_sgwb_setup(self, sgwb_type, resp=None):
+        """The SGWB template (0 power law, 1 lognormal, 2 phase transition; -1
+        none) and the response table rows [n, 7] = f, XX, YY, ZZ, XY, XZ, YZ."""
+        r = None if resp is None else np.ascontiguousarray(resp, np.float64).reshape(-1, 7)
+        _check(self.lib.glass_gpu_noise_sgwb_setup(self._ctx, int(sgwb_type), 0 if r is None else len(r),
+                                                   _pd(r) if r is not None else None))
+
+    def noise_logl_host(self, inst, sgal=None, sgwb=None):
+        """my_noise_log_likelihood of each noise model: inst [n, 12], sgal [n, 5]
+        or None, sgwb [n, 4] (the template's parameters first) or None."""
         i = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
         g = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        b = None if sgwb is None else np.ascontiguousarray(sgwb, np.float64).reshape(-1, 4)
         out = np.empty(len(i))
-        _check(self.lib.glass_gpu_noise_logl_batch_host(self._ctx, len(i), _pd(i), _pd(g) if g is not None else None,
-                                                        _pd(out)))
+        _check(self.lib.glass_gpu_noise_logl_batch_sgwb_host(self._ctx, len(i), _pd(i),
+                                                             _pd(g) if g is not None else None,
+                                                             _pd(b) if b is not None else None, _pd(out)))
         return out
 
-    def noise_logl_device(self, inst, logl, sgal=None):
-        """Device tensors: inst [n, 12], sgal [n, 5] or None, logl [n]; asynchronous."""
+    def noise_logl_device(self, inst, logl, sgal=None, sgwb=None):
+        """Device tensors: inst [n, 12], sgal [n, 5] or None, sgwb [n, 4] or
+        None, logl [n]; asynchronous."""
         n = int(inst.shape[0])
-        _check(self.lib.glass_gpu_noise_logl_batch(self._ctx, n, _ptr(inst), _ptr(sgal), _ptr(logl)))
+        _check(self.lib.glass_gpu_noise_logl_batch_sgwb(self._ctx, n, _ptr(inst), _ptr(sgal), _ptr(sgwb), _ptr(logl)))
 
     def noise_wavelet_setup(self, NF, NT, df, lmin, Q, X, Y, Z, mod=None):
         """Wavelet data (pixel i of layer j at i + j NT) on layers lmin.., cells of Q
@@ -468,17 +486,20 @@ class Engine:
                                                       len(X) // int(NT), int(Q), _pd(X), _pd(Y), _pd(Z),
                                                       _pd(md) if md is not None else None))
 
-    def noise_wavelet_logl_host(self, inst, sgal=None, mode=0):
+    def noise_wavelet_logl_host(self, inst, sgal=None, mode=0, sgwb=None):
         i = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
         g = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        b = None if sgwb is None else np.ascontiguousarray(sgwb, np.float64).reshape(-1, 4)
         out = np.empty(len(i))
-        _check(self.lib.glass_gpu_noise_wavelet_logl_batch_host(self._ctx, int(mode), len(i), _pd(i),
-                                                                _pd(g) if g is not None else None, _pd(out)))
+        _check(self.lib.glass_gpu_noise_wavelet_logl_batch_sgwb_host(self._ctx, int(mode), len(i), _pd(i),
+                                                                     _pd(g) if g is not None else None,
+                                                                     _pd(b) if b is not None else None, _pd(out)))
         return out
 
-    def noise_wavelet_logl_device(self, inst, logl, sgal=None, mode=0):
+    def noise_wavelet_logl_device(self, inst, logl, sgal=None, mode=0, sgwb=None):
         n = int(inst.shape[0])
-        _check(self.lib.glass_gpu_noise_wavelet_logl_batch(self._ctx, int(mode), n, _ptr(inst), _ptr(sgal), _ptr(logl)))
+        _check(self.lib.glass_gpu_noise_wavelet_logl_batch_sgwb(self._ctx, int(mode), n, _ptr(inst), _ptr(sgal),
+                                                                _ptr(sgwb), _ptr(logl)))
 
     def dlogl_channels_device(self, item_seg, params, dlogl, term_ch, term_y=None, hh=None, status=None, term_x=None,
                               precision=PREC_MIXED):

@@ -34,12 +34,16 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 # explicit round-to-nearest operations, so its translation units contract
 # freely.  The no-allocation entry point, the F-statistic, the wavelet-domain
 # waveform and the noise and sampler units keep contraction off: their
-# results follow the reference's operation order throughout.
+# results follow the reference's operation order throughout.  So do the host
+# sums of the struct-based drop-ins (dropin_model.cu), which are bit-identical
+# to the reference's x86 build only without contraction (gcc on aarch64
+# contracts a * b + c by default).
 PER_FILE_FLAGS = {"ucb_fd_noalloc.cu": ["-fmad=false"],
                   "wdm.cu": ["-Xcompiler", "-ffp-contract=off"],
                   "ucb_wavelet.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
                   "ucb_fstat.cu": ["-fmad=false"], "noise.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
-                  "capi.cu": ["-Xcompiler", "-ffp-contract=off"], "sampler.cu": ["-fmad=false"]}
+                  "capi.cu": ["-Xcompiler", "-ffp-contract=off"], "sampler.cu": ["-fmad=false"],
+                  "dropin_model.cu": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:

@@ -122,6 +122,8 @@ struct glass_gpu_ctx {
   FsWorkDev fsw;  // F-statistic scratch
   NoiseDev noise;  // noise-model likelihood: per-bin table and chunk sums
   NoiseWvDev noise_wv;  // the same in the wavelet domain
+  int sgwb_type = -1;             // SGWB template of glass_gpu_noise_sgwb_setup (-1: none)
+  std::vector<double> sgwb_resp;  // its response table rows (f, XX, YY, ZZ, XY, XZ, YZ)
   double *eta_scratch = nullptr;  // glass_gpu_noise_eta_batch: 5 doubles per chain
   size_t eta_cap = 0;
 };
@@ -206,8 +208,10 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->wv_fisher_mem);
   fs_work_free(ctx->fsw);
   cudaFree(ctx->noise.tab);
+  cudaFree(ctx->noise.rsg);
   cudaFree(ctx->noise.partial);
   cudaFree(ctx->noise_wv.mem);
+  cudaFree(ctx->noise_wv.rsg);
   cudaFree(ctx->noise_wv.partial);
   cudaFree(ctx->eta_scratch);
   for (int b = 0; b < kNumBins; b++) {
@@ -1169,6 +1173,56 @@ extern "C" int glass_gpu_noise_eta_batch_host(glass_gpu_ctx *ctx, int precision,
 }
 
 // ------------------------------------------------------- noise likelihood
+// The SGWB response rows of the context's grids (Fourier bins, wavelet layer
+// centres) from its response table; freed when no template is set.
+static int sgwb_build_rows(glass_gpu_ctx *ctx) {
+  struct Grid {
+    double **rsg;
+    std::vector<double> f;
+  };
+  std::vector<Grid> grids;
+  if (ctx->noise.tab) {
+    Grid g{&ctx->noise.rsg, std::vector<double>(ctx->noise.N)};
+    for (int n = 0; n < ctx->noise.N; n++) g.f[n] = ctx->noise.fmin + (double)n / ctx->noise.T;
+    grids.push_back(std::move(g));
+  }
+  if (ctx->noise_wv.mem) {
+    Grid g{&ctx->noise_wv.rsg, std::vector<double>(ctx->noise_wv.Nlayer)};
+    for (int j = 0; j < ctx->noise_wv.Nlayer; j++) g.f[j] = (double)(ctx->noise_wv.lmin + j) * ctx->noise_wv.df;
+    grids.push_back(std::move(g));
+  }
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "sgwb rows sync");
+  for (Grid &g : grids) {
+    cudaFree(*g.rsg);
+    *g.rsg = nullptr;
+    if (ctx->sgwb_type < 0) continue;
+    const int N = (int)g.f.size();
+    std::vector<double> R((size_t)6 * N);
+    if (noise_sgwb_rows((int)(ctx->sgwb_resp.size() / 7), ctx->sgwb_resp.data(), N, g.f.data(), R.data()))
+      return set_err(GLASS_ERR_ARG, "noise_sgwb_setup: response table needs 10..3000 rows with f, XX, YY, ZZ > 0");
+    GLASS_CUDA(cudaMalloc(g.rsg, sizeof(double) * R.size()), "cudaMalloc(sgwb response)");
+    GLASS_CUDA(cudaMemcpy(*g.rsg, R.data(), sizeof(double) * R.size(), cudaMemcpyHostToDevice), "upload sgwb response");
+  }
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_sgwb_setup(glass_gpu_ctx *ctx, int type, int nresp, const double *resp) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_sgwb_setup: null context");
+  if (type < -1 || type >= kSgwbTypes) return set_err(GLASS_ERR_ARG, "noise_sgwb_setup: template is -1, 0, 1 or 2");
+  if (type >= 0 && (!resp || nresp < 10 || nresp > 3000))
+    return set_err(GLASS_ERR_ARG, "noise_sgwb_setup: response table needs 10..3000 rows");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  ctx->sgwb_type = type;
+  if (type >= 0)
+    ctx->sgwb_resp.assign(resp, resp + 7 * (size_t)nresp);
+  else
+    ctx->sgwb_resp.clear();
+  rc = sgwb_build_rows(ctx);
+  if (rc) ctx->sgwb_type = -1;
+  return rc;
+}
+
 extern "C" int glass_gpu_noise_setup(glass_gpu_ctx *ctx, double T, int qmin, int NFFT, const double *X,
                                      const double *Y, const double *Z) {
   if (!ctx || !X || !Y || !Z) return set_err(GLASS_ERR_ARG, "noise_setup: null argument");
@@ -1190,17 +1244,19 @@ extern "C" int glass_gpu_noise_setup(glass_gpu_ctx *ctx, double T, int qmin, int
   cudaFree(nd.partial);
   nd.partial = nullptr;
   nd.partial_models = 0;
-  return GLASS_OK;
+  return sgwb_build_rows(ctx);
 }
 
-extern "C" int glass_gpu_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
-                                          double *logl) {
+extern "C" int glass_gpu_noise_logl_batch_sgwb(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                               const double *sgwb, double *logl) {
   if (!ctx) return set_err(GLASS_ERR_ARG, "noise_logl_batch: null context");
   if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_logl_batch: negative model count");
   if (nprop == 0) return GLASS_OK;
   if (!inst || !logl) return set_err(GLASS_ERR_ARG, "noise_logl_batch: null argument");
   NoiseDev &nd = ctx->noise;
   if (!nd.tab) return set_err(GLASS_ERR_STATE, "noise_logl_batch: no data set (glass_gpu_noise_setup)");
+  if (sgwb && (ctx->sgwb_type < 0 || !nd.rsg))
+    return set_err(GLASS_ERR_STATE, "noise_logl_batch: no SGWB template set (glass_gpu_noise_sgwb_setup)");
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   if (nprop > nd.partial_models) {
@@ -1214,14 +1270,19 @@ extern "C" int glass_gpu_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, const d
     nd.partial_models = want;
   }
   int nl = 0;
-  cudaError_t e = noise_logl_launch(nd, nprop, inst, sgal, logl, ctx->stream, &nl);
+  cudaError_t e = noise_logl_launch(nd, nprop, inst, sgal, ctx->sgwb_type, sgwb, logl, ctx->stream, &nl);
   ctx->last_launches = nl;
   if (e != cudaSuccess) return cuda_err(e, "noise_logl_batch launch");
   return GLASS_OK;
 }
 
-extern "C" int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
-                                               double *logl) {
+extern "C" int glass_gpu_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                          double *logl) {
+  return glass_gpu_noise_logl_batch_sgwb(ctx, nprop, inst, sgal, nullptr, logl);
+}
+
+extern "C" int glass_gpu_noise_logl_batch_sgwb_host(glass_gpu_ctx *ctx, int nprop, const double *inst,
+                                                    const double *sgal, const double *sgwb, double *logl) {
   if (!ctx) return set_err(GLASS_ERR_ARG, "noise_logl_batch_host: null context");
   if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_logl_batch_host: negative model count");
   if (nprop == 0) return GLASS_OK;
@@ -1229,16 +1290,23 @@ extern "C" int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, co
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   const size_t nd = (size_t)nprop;
-  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (12 + 5 + 1) + 256))) return rc;
-  double *d_inst = (double *)ctx->d_stage, *d_sgal = d_inst + 12 * nd, *d_logl = d_sgal + 5 * nd;
+  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (12 + 5 + 4 + 1) + 256))) return rc;
+  double *d_inst = (double *)ctx->d_stage, *d_sgal = d_inst + 12 * nd, *d_sgwb = d_sgal + 5 * nd,
+         *d_logl = d_sgwb + 4 * nd;
   cudaStream_t s = ctx->stream;
   GLASS_CUDA(cudaMemcpyAsync(d_inst, inst, sizeof(double) * 12 * nd, cudaMemcpyHostToDevice, s), "H2D inst");
   if (sgal) GLASS_CUDA(cudaMemcpyAsync(d_sgal, sgal, sizeof(double) * 5 * nd, cudaMemcpyHostToDevice, s), "H2D sgal");
-  rc = glass_gpu_noise_logl_batch(ctx, nprop, d_inst, sgal ? d_sgal : nullptr, d_logl);
+  if (sgwb) GLASS_CUDA(cudaMemcpyAsync(d_sgwb, sgwb, sizeof(double) * 4 * nd, cudaMemcpyHostToDevice, s), "H2D sgwb");
+  rc = glass_gpu_noise_logl_batch_sgwb(ctx, nprop, d_inst, sgal ? d_sgal : nullptr, sgwb ? d_sgwb : nullptr, d_logl);
   if (rc) return rc;
   GLASS_CUDA(cudaMemcpyAsync(logl, d_logl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
   GLASS_CUDA(cudaStreamSynchronize(s), "noise_logl_batch_host sync");
   return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                               double *logl) {
+  return glass_gpu_noise_logl_batch_sgwb_host(ctx, nprop, inst, sgal, nullptr, logl);
 }
 
 extern "C" int glass_gpu_noise_wavelet_setup(glass_gpu_ctx *ctx, int NF, int NT, double df, int lmin, int Nlayer,
@@ -1257,6 +1325,7 @@ extern "C" int glass_gpu_noise_wavelet_setup(glass_gpu_ctx *ctx, int NF, int NT,
   NoiseWvDev &w = ctx->noise_wv;
   cudaFree(w.mem);
   cudaFree(w.partial);
+  cudaFree(w.rsg);
   w = NoiseWvDev{};
   const size_t bytes = sizeof(double) * (tab.size() + P.size() + 6 * (size_t)Nc);
   GLASS_CUDA(cudaMalloc(&w.mem, bytes), "cudaMalloc(noise wavelet)");
@@ -1275,11 +1344,11 @@ extern "C" int glass_gpu_noise_wavelet_setup(glass_gpu_ctx *ctx, int NF, int NT,
   w.Ncoarse = Nc;
   w.df = df;
   w.has_mod = mod != nullptr;
-  return GLASS_OK;
+  return sgwb_build_rows(ctx);
 }
 
-extern "C" int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
-                                                  const double *sgal, double *logl) {
+extern "C" int glass_gpu_noise_wavelet_logl_batch_sgwb(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                                       const double *sgal, const double *sgwb, double *logl) {
   if (!ctx) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch: null context");
   if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch: negative model count");
   if (mode < 0 || mode > 2) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch: mode is 0, 1 or 2");
@@ -1288,6 +1357,8 @@ extern "C" int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, 
   NoiseWvDev &w = ctx->noise_wv;
   if (!w.mem) return set_err(GLASS_ERR_STATE, "noise_wavelet_logl_batch: no data set (glass_gpu_noise_wavelet_setup)");
   if (mode == 2 && !w.has_mod) return set_err(GLASS_ERR_STATE, "noise_wavelet_logl_batch: mode 2 needs the modulation");
+  if (sgwb && (ctx->sgwb_type < 0 || !w.rsg))
+    return set_err(GLASS_ERR_STATE, "noise_wavelet_logl_batch: no SGWB template set (glass_gpu_noise_sgwb_setup)");
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   if (mode == 2 && nprop > w.partial_models) {
@@ -1301,14 +1372,20 @@ extern "C" int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, 
     w.partial_models = want;
   }
   int nl = 0;
-  cudaError_t e = noise_wv_logl_launch(w, mode, nprop, inst, sgal, logl, ctx->stream, &nl);
+  cudaError_t e = noise_wv_logl_launch(w, mode, nprop, inst, sgal, ctx->sgwb_type, sgwb, logl, ctx->stream, &nl);
   ctx->last_launches = nl;
   if (e != cudaSuccess) return cuda_err(e, "noise_wavelet_logl_batch launch");
   return GLASS_OK;
 }
 
-extern "C" int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
-                                                       const double *sgal, double *logl) {
+extern "C" int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                                  const double *sgal, double *logl) {
+  return glass_gpu_noise_wavelet_logl_batch_sgwb(ctx, mode, nprop, inst, sgal, nullptr, logl);
+}
+
+extern "C" int glass_gpu_noise_wavelet_logl_batch_sgwb_host(glass_gpu_ctx *ctx, int mode, int nprop,
+                                                            const double *inst, const double *sgal,
+                                                            const double *sgwb, double *logl) {
   if (!ctx) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch_host: null context");
   if (nprop < 0) return set_err(GLASS_ERR_ARG, "noise_wavelet_logl_batch_host: negative model count");
   if (nprop == 0) return GLASS_OK;
@@ -1316,16 +1393,24 @@ extern "C" int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int m
   int rc = ctx_activate(ctx);
   if (rc) return rc;
   const size_t nd = (size_t)nprop;
-  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (12 + 5 + 1) + 256))) return rc;
-  double *d_inst = (double *)ctx->d_stage, *d_sgal = d_inst + 12 * nd, *d_logl = d_sgal + 5 * nd;
+  if ((rc = ensure_stage(ctx, sizeof(double) * nd * (12 + 5 + 4 + 1) + 256))) return rc;
+  double *d_inst = (double *)ctx->d_stage, *d_sgal = d_inst + 12 * nd, *d_sgwb = d_sgal + 5 * nd,
+         *d_logl = d_sgwb + 4 * nd;
   cudaStream_t s = ctx->stream;
   GLASS_CUDA(cudaMemcpyAsync(d_inst, inst, sizeof(double) * 12 * nd, cudaMemcpyHostToDevice, s), "H2D inst");
   if (sgal) GLASS_CUDA(cudaMemcpyAsync(d_sgal, sgal, sizeof(double) * 5 * nd, cudaMemcpyHostToDevice, s), "H2D sgal");
-  rc = glass_gpu_noise_wavelet_logl_batch(ctx, mode, nprop, d_inst, sgal ? d_sgal : nullptr, d_logl);
+  if (sgwb) GLASS_CUDA(cudaMemcpyAsync(d_sgwb, sgwb, sizeof(double) * 4 * nd, cudaMemcpyHostToDevice, s), "H2D sgwb");
+  rc = glass_gpu_noise_wavelet_logl_batch_sgwb(ctx, mode, nprop, d_inst, sgal ? d_sgal : nullptr,
+                                               sgwb ? d_sgwb : nullptr, d_logl);
   if (rc) return rc;
   GLASS_CUDA(cudaMemcpyAsync(logl, d_logl, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
   GLASS_CUDA(cudaStreamSynchronize(s), "noise_wavelet_logl_batch_host sync");
   return GLASS_OK;
+}
+
+extern "C" int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                                       const double *sgal, double *logl) {
+  return glass_gpu_noise_wavelet_logl_batch_sgwb_host(ctx, mode, nprop, inst, sgal, nullptr, logl);
 }
 
 // ------------------------------------------------------ on-device sampler
@@ -2098,25 +2183,6 @@ extern "C" int glass_gpu_wavelet_waveform_batch_host(glass_gpu_ctx *ctx, int pre
 }
 
 // ------------------------------------------------------------ drop-ins for the wavelet headers
-// The reference's struct Wavelets (utils/src/glass_wavelet.h:25-75), restated
-// field for field so that the drop-in entry points can read the grid from a
-// caller's struct: the field order and types are the interface.
-struct WaveletsLayout {
-  int NF, NT;
-  double cadence, dt, df;
-  int frequency_steps, fdot_steps;
-  double d_fdot;
-  int oversample;
-  double Omega, dOmega, domega, inv_root_dOmega, B, A, BW, deltaf;
-  double *fdot, *window, *window_freq_forward;
-  double norm;
-  int N;
-  double T;
-  int kmin, kmax, imin, imax;
-  int *n_table;
-  double **table;
-};
-
 static constexpr double kWaveletFilterConstant = 6.0;  // WAVELET_FILTER_CONSTANT, utils/src/glass_wavelet.h:21
 
 // One context per host thread for the drop-in entry points (the reference's
@@ -2237,31 +2303,8 @@ extern "C" void ucb_waveform_wavelet(struct Orbit *orbit, struct Wavelets *wdm, 
                                      double *Z) {
   static const char *who = "ucb_waveform_wavelet";
   const WaveletsLayout *w = reinterpret_cast<const WaveletsLayout *>(wdm);
-  const OrbitLayout *o = reinterpret_cast<const OrbitLayout *>(orbit);
   DropInThread &D = g_dropin;
-  glass_gpu_ctx *ctx = dropin_ctx(who);
-  const int norb = o->Norb;
-  const double key[14] = {Tobs, t0, (double)w->NF, (double)w->NT, w->dt, w->df, w->A, (double)w->kmin,
-                          (double)w->kmax, (double)norb, (double)(uintptr_t)o->t, norb > 0 ? o->t[0] : 0.0,
-                          norb > 0 ? o->t[norb - 1] : 0.0, norb > 0 ? o->x[0][norb - 1] : 0.0};
-  if (!D.wv_ready || memcmp(key, D.key, sizeof(key)) != 0) {
-    if (norb < 20 || norb > kWvMaxOrb) {
-      set_err(GLASS_ERR_ARG, "ucb_waveform_wavelet: orbit needs 20..2048 nodes");
-      dropin_fail(who);
-    }
-    std::vector<double> pos((size_t)9 * norb);
-    for (int sc = 0; sc < 3; sc++)
-      for (int n = 0; n < norb; n++) {
-        pos[(size_t)(3 * sc + 0) * norb + n] = o->x[sc][n];
-        pos[(size_t)(3 * sc + 1) * norb + n] = o->y[sc][n];
-        pos[(size_t)(3 * sc + 2) * norb + n] = o->z[sc][n];
-      }
-    if (glass_gpu_wavelet_setup(ctx, Tobs, t0, w->NF, w->NT, w->dt, w->df, w->A, kWaveletFilterConstant, w->kmin,
-                                w->kmax, norb, o->t, pos.data()) != GLASS_OK)
-      dropin_fail(who);
-    memcpy(D.key, key, sizeof(key));
-    D.wv_ready = true;
-  }
+  glass_gpu_ctx *ctx = dropin_wavelet_grid(orbit, wdm, Tobs, t0, who);
   const int NT = w->NT;
   const size_t per = (size_t)3 * kWvMaxLayers * NT;
   D.info.resize(4);
@@ -2285,6 +2328,39 @@ extern "C" void ucb_waveform_wavelet(struct Orbit *orbit, struct Wavelets *wdm, 
     Z[k] = hz[q];
   }
   *Nwavelet = n;
+}
+
+// The calling thread's context with its wavelet grid set up for this WDM
+// grid, segment and orbit (kept while they stay the same).
+glass_gpu_ctx *dropin_wavelet_grid(struct Orbit *orbit, struct Wavelets *wdm, double Tobs, double t0,
+                                   const char *who) {
+  const WaveletsLayout *w = reinterpret_cast<const WaveletsLayout *>(wdm);
+  const OrbitLayout *o = reinterpret_cast<const OrbitLayout *>(orbit);
+  DropInThread &D = g_dropin;
+  glass_gpu_ctx *ctx = dropin_ctx(who);
+  const int norb = o->Norb;
+  const double key[14] = {Tobs, t0, (double)w->NF, (double)w->NT, w->dt, w->df, w->A, (double)w->kmin,
+                          (double)w->kmax, (double)norb, (double)(uintptr_t)o->t, norb > 0 ? o->t[0] : 0.0,
+                          norb > 0 ? o->t[norb - 1] : 0.0, norb > 0 ? o->x[0][norb - 1] : 0.0};
+  if (!D.wv_ready || memcmp(key, D.key, sizeof(key)) != 0) {
+    if (norb < 20 || norb > kWvMaxOrb) {
+      set_err(GLASS_ERR_ARG, "%s: orbit needs 20..2048 nodes", who);
+      dropin_fail(who);
+    }
+    std::vector<double> pos((size_t)9 * norb);
+    for (int sc = 0; sc < 3; sc++)
+      for (int n = 0; n < norb; n++) {
+        pos[(size_t)(3 * sc + 0) * norb + n] = o->x[sc][n];
+        pos[(size_t)(3 * sc + 1) * norb + n] = o->y[sc][n];
+        pos[(size_t)(3 * sc + 2) * norb + n] = o->z[sc][n];
+      }
+    if (glass_gpu_wavelet_setup(ctx, Tobs, t0, w->NF, w->NT, w->dt, w->df, w->A, kWaveletFilterConstant, w->kmin,
+                                w->kmax, norb, o->t, pos.data()) != GLASS_OK)
+      dropin_fail(who);
+    memcpy(D.key, key, sizeof(key));
+    D.wv_ready = true;
+  }
+  return ctx;
 }
 
 // Status-returning forms of the two reference variants that are not built here.

@@ -15,12 +15,19 @@
 //   gaussian_log_likelihood   utils/src/glass_model.c:726-774
 //   matrix_eigenstuff         utils/src/glass_math.c:475-499
 //   ucb_fisher                ucb/src/glass_ucb_waveform.c:364-522
+//   wavelet_nwip              utils/src/glass_math.c:382-391
+//   snr_wavelet               utils/src/glass_math.c:428-438
+//   delta_log_likelihood      utils/src/glass_model.c:624-687
+//   ucb_fisher_wavelet        ucb/src/glass_ucb_waveform.c:524-696
 //
 // The waveforms come from this library's GPU ucb_waveform; ucb_fisher's
 // Fisher matrix for A/E data from the GPU adjoint kernels (the reference's
 // eight finite-difference waveforms are not needed; its indexing of the noise
 // by template bin is kept, fisher_mode 1), for X or XYZ data from forward
-// differences of the GPU waveform as the reference takes them.  The sums over
+// differences of the GPU waveform as the reference takes them;
+// ucb_fisher_wavelet's from the batched wavelet Fisher kernels
+// (glass_gpu_wavelet_fisher_batch, the reference's central differences on the
+// GPU waveform).  The sums over
 // a segment's bins (fourier_nwip, snr, gaussian_log_likelihood, the model
 // updates) work on the caller's host arrays, in the reference's order of
 // operations (bit-identical): one GPU launch per call would cost more than the
@@ -529,6 +536,128 @@ void ucb_fisher(struct Orbit *orbit, struct Data *data, struct Source *source, s
       s->fisher_matrix[i][j] = s->fisher_matrix[j][i] = f;
     }
   matrix_eigenstuff(s->fisher_matrix, s->fisher_evectr, s->fisher_evalue, kUcbNP);
+}
+
+double wavelet_nwip(const double *a, const double *b, const double *invC, const int *list, int N) {
+  double arg = 0.0;
+  for (int n = 0; n < N; n++) {
+    const int k = list[n];
+    arg += a[k] * b[k] * invC[k];
+  }
+  return arg;
+}
+
+double snr_wavelet(struct Source *source, struct Noise *noise) {
+  const SourceLayout *s = reinterpret_cast<const SourceLayout *>(source);
+  double ***ic = reinterpret_cast<const NoiseLayout *>(noise)->invC;
+  const TDILayout *t = s->tdi;
+  const int *l = s->list, n = s->Nlist;
+  double snr2 = 0.0;
+  snr2 += wavelet_nwip(t->X, t->X, ic[0][0], l, n);
+  snr2 += wavelet_nwip(t->Y, t->Y, ic[1][1], l, n);
+  snr2 += wavelet_nwip(t->Z, t->Z, ic[2][2], l, n);
+  snr2 += wavelet_nwip(t->X, t->Y, ic[0][1], l, n) * 2;
+  snr2 += wavelet_nwip(t->X, t->Z, ic[0][2], l, n) * 2;
+  snr2 += wavelet_nwip(t->Y, t->Z, ic[1][2], l, n) * 2;
+  return sqrt(snr2);
+}
+
+}  // extern "C"
+
+namespace {
+// The nine XYZ cross terms of (a|h) over a pixel list, in the reference's
+// order: XX, YY, ZZ, XY, XZ, YZ, YX, ZX, ZY (utils/src/glass_model.c:641-683).
+double xyz_nwip9(const TDILayout *a, const TDILayout *h, double ***ic, const int *l, int n) {
+  double r = 0.0;
+  r += wavelet_nwip(a->X, h->X, ic[0][0], l, n);
+  r += wavelet_nwip(a->Y, h->Y, ic[1][1], l, n);
+  r += wavelet_nwip(a->Z, h->Z, ic[2][2], l, n);
+  r += wavelet_nwip(a->X, h->Y, ic[0][1], l, n);
+  r += wavelet_nwip(a->X, h->Z, ic[0][2], l, n);
+  r += wavelet_nwip(a->Y, h->Z, ic[1][2], l, n);
+  r += wavelet_nwip(a->Y, h->X, ic[1][0], l, n);
+  r += wavelet_nwip(a->Z, h->X, ic[2][0], l, n);
+  r += wavelet_nwip(a->Z, h->Y, ic[2][1], l, n);
+  return r;
+}
+}  // namespace
+
+extern "C" {
+
+// The sparse-pixel likelihood difference of two wavelet-domain models: each
+// model's (d|h) and (h|h) over its own pixel list with its own noise; the
+// (d|d) terms cancel.
+double delta_log_likelihood(struct Data *data, struct Model *model_x, struct Model *model_y) {
+  const DataLayout *d = reinterpret_cast<const DataLayout *>(data);
+  const ModelLayout *mx = reinterpret_cast<const ModelLayout *>(model_x);
+  const ModelLayout *my = reinterpret_cast<const ModelLayout *>(model_y);
+  double ***icx = mx->noise->invC, ***icy = my->noise->invC;
+  const double dh_x = xyz_nwip9(d->tdi, mx->tdi, icx, mx->list, mx->Nlist);
+  const double hh_x = xyz_nwip9(mx->tdi, mx->tdi, icx, mx->list, mx->Nlist);
+  const double dh_y = xyz_nwip9(d->tdi, my->tdi, icy, my->list, my->Nlist);
+  const double hh_y = xyz_nwip9(my->tdi, my->tdi, icy, my->list, my->Nlist);
+  const double logLx = -0.5 * (hh_x - 2.0 * dh_x);
+  const double logLy = -0.5 * (hh_y - 2.0 * dh_y);
+  return logLy - logLx;
+}
+
+// The wavelet-domain Fisher matrix of one source: the batched GPU kernels
+// (central differences of the FP64 wavelet waveform with the reference's step
+// and clamping, the nine XYZ cross terms per pixel inside the time window
+// imin < t < imax), then the eigen-decomposition, and the reference's
+// regularisation when an eigenvalue is not positive: 0.1 added to the
+// diagonal and the decomposition redone; still not positive: report, exit.
+void ucb_fisher_wavelet(struct Orbit *orbit, struct Data *data, struct Source *source, struct Noise *noise) {
+  static const char *who = "ucb_fisher_wavelet";
+  const DataLayout *d = reinterpret_cast<const DataLayout *>(data);
+  SourceLayout *s = reinterpret_cast<SourceLayout *>(source);
+  const NoiseLayout *nz = reinterpret_cast<const NoiseLayout *>(noise);
+  struct Wavelets *wdm = reinterpret_cast<struct Wavelets *>(d->wdm);
+  const WaveletsLayout *w = reinterpret_cast<const WaveletsLayout *>(d->wdm);
+  const int N = w->kmax - w->kmin;
+  if (N != d->N) {
+    fprintf(stderr, "%s: data->N (%d) is not the grid's kmax - kmin (%d)\n", who, d->N, N);
+    exit(1);
+  }
+  glass_gpu_ctx *ctx = dropin_wavelet_grid(orbit, wdm, d->T, d->t0, who);
+  // the noise the Fisher matrix is weighted with, as invC[(3 i + j) N + k]
+  thread_local std::vector<double> resid, icv;
+  resid.assign((size_t)3 * N, 0.0);
+  icv.resize((size_t)9 * N);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) memcpy(&icv[(size_t)(3 * i + j) * N], nz->invC[i][j], sizeof(double) * (size_t)N);
+  if (glass_gpu_wavelet_set_data(ctx, resid.data(), resid.data() + N, resid.data() + 2 * N, icv.data()) != GLASS_OK)
+    dropin_fail(who);
+  double F[kUcbNP * kUcbNP];
+  int st = 0;
+  if (glass_gpu_wavelet_fisher_batch_host(ctx, 1, s->params, w->imin, w->imax, F, &st) != GLASS_OK)
+    dropin_fail(who);
+  if (st != 0) {
+    fprintf(stderr, "%s: invalid perturbed parameters (status %d)\n", who, st);
+    exit(1);
+  }
+  for (int i = 0; i < kUcbNP; i++)
+    for (int j = 0; j < kUcbNP; j++) s->fisher_matrix[i][j] = F[i * kUcbNP + j];
+  matrix_eigenstuff(s->fisher_matrix, s->fisher_evectr, s->fisher_evalue, kUcbNP);
+  bool bad = false;
+  for (int i = 0; i < kUcbNP; i++) {
+    const double e = s->fisher_evalue[i];
+    if (e <= 0 || e != e) {
+      fprintf(stderr, "WARNING: bad eigenvalue in ucb_fisher_wavelet (GB300): fisher_evalue[%i] = %lg\n", i, e);
+      bad = true;
+    }
+  }
+  if (!bad) return;
+  fprintf(stderr, "WARNING: try regularization FIM and re-inverting\n");
+  for (int i = 0; i < kUcbNP; i++) s->fisher_matrix[i][i] += 1.0e-1;
+  matrix_eigenstuff(s->fisher_matrix, s->fisher_evectr, s->fisher_evalue, kUcbNP);
+  for (int i = 0; i < kUcbNP; i++) {
+    const double e = s->fisher_evalue[i];
+    if (e <= 0 || e != e) {
+      fprintf(stderr, "ERROR: bad eigenvalue in ucb_fisher_wavelet (GB300): fisher_evalue[%i] = %lg\n", i, e);
+      exit(1);
+    }
+  }
 }
 
 }  // extern "C"

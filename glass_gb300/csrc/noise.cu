@@ -3,7 +3,10 @@
 // optionally plus the galactic foreground (:612-654, added as
 // generate_full_covariance_matrix does, :894-907), the 3x3 inverse and
 // log-determinant (utils/src/glass_math.c:240-289) and my_noise_log_likelihood
-// (noise/src/glass_noise_model.c:1243-1273), for a batch of noise models.
+// (noise/src/glass_noise_model.c:1243-1273), for a batch of noise models,
+// optionally with a stochastic background (SGWB) of one of the reference's
+// three spectral templates times the instrument's response
+// (generate_sgwb_model, :778-842; the wavelet form :843-892).
 //
 // The reference regenerates the whole covariance, inverts it and sums the
 // likelihood for every proposed noise model (noise_instrument_model_mcmc and
@@ -18,6 +21,10 @@
 // FP64, compiled without multiply-add contraction.  The inverse's entries are
 // the cofactors times 1/det instead of the reference's
 // exp(log|cofactor| - log det) (the same numbers to a few ulp).
+
+#include <math.h>
+
+#include <vector>
 
 #include "../../include/glass_gb300.h"
 #include "glass_common.cuh"
@@ -36,6 +43,9 @@ struct NoiseArgs {
   const double *tab;  // kNoiseTabRows rows of N
   const double *inst;  // [nprop][12]
   const double *sgal;  // [nprop][5] or null
+  int sg_type;         // SGWB template
+  const double *sgwb;  // [nprop][4] or null
+  const double *rsg;   // SGWB response, 6 rows of N
   double *partial;     // [nprop][nchunks]
 };
 
@@ -82,6 +92,66 @@ __device__ __forceinline__ void noise_inst_cov(double cosx, double tdi, double a
 __device__ __forceinline__ double noise_sgal(double f, double fp73, double Amp, double f1, double alpha, double fk,
                                              double f2) {
   return (f > f1 * 10) ? 0.0 : Amp * fp73 * exp(-pow(f / f1, alpha)) * 0.5 * (1. + tanh((fk - f) / f2));
+}
+
+// ------------------------------------------------------------------ SGWB
+// Cosmological constants of the templates (utils/src/glass_constants.h:81-86):
+// H0 = 70 km/s/Mpc in 1/s, the f^-3 prefactor 3 H0^2 / (4 pi^2) that turns
+// an energy-density spectrum into a strain PSD, and the radiation-era
+// transfer factor of the lognormal template.
+constexpr double kSgH0 = 70 * 3.24078e-20;
+constexpr double kSgHscale = 3 * kSgH0 * kSgH0 / (4 * M_PI * M_PI);
+constexpr double kSgCgOr0 = 1.6e-5 / (0.7 * 0.7);
+
+// erfc by Abramowitz & Stegun 7.1.26 (|error| < 1.5e-7), the rational
+// approximation the reference's glass_erfc uses (utils/src/glass_math.c:1310),
+// evaluated on |x| and reflected (erfc(-x) = 2 - erfc(x)).
+__device__ __forceinline__ double sgwb_erfc(double x) {
+  const double ax = fabs(x);
+  const double t = 1.0 / (1.0 + 0.3275911 * ax);
+  const double poly = ((((1.061405429 * t - 1.453152027) * t + 1.421413741) * t - 0.284496736) * t + 0.254829592) * t;
+  const double y = poly * exp(-ax * ax);
+  return x < 0.0 ? 2.0 - y : y;
+}
+
+// The background's strain PSD at f > 0 (noise/src/glass_noise_model.c:725-776):
+//  powerlaw          p = log10 A, alpha: A (f / 25 Hz)^alpha
+//  lognormal         p = log10 A, log10 f*, log10 Delta: the wide-Delta
+//                    lognormal-peak spectrum of Pi & Sasaki (JCAP 2020,
+//                    eq. 3.29), its asymptote 0.783e-3 A^2 for Delta >= 9
+//  phase transition  p = rb, b, log10 Ap, log10 fp: Ap times the broken power
+//                    law in s = f / fp with slopes 9 and b
+// each times Hscale / f^3.
+__device__ double sgwb_psd(int type, double f, const double *p) {
+  const double pre = kSgHscale / (f * f * f);
+  if (type == kSgwbPowerlaw) {
+    const double A = pow(10.0, p[0]);
+    return pre * A * pow(f / 25.0, p[1]);
+  }
+  if (type == kSgwbLognormal) {
+    const double A = pow(10.0, p[0]), fst = pow(10.0, p[1]), D = pow(10.0, p[2]);
+    const double scale = pre * kSgCgOr0 * A * A;
+    if (!(D < 9.0)) return scale * 0.783 / 1e3;
+    const double ft = f / fst, lft = log(ft), D2 = D * D;
+    const double rpi = sqrt(M_PI);
+    const double h32 = 0.5 * log(1.5);
+    const double lK = lft + 1.5 * D2;
+    const double u = lK + h32;
+    const double t1 = 4.0 / 5.0 / rpi * ft * ft * ft * exp(9.0 * D2 / 4.0) / D *
+                      ((lK * lK + 0.5 * D2) * sgwb_erfc(u / D) - D / rpi * exp(-u * u / D2) * (lK - h32));
+    const double v = lft + D2 - 0.5 * log(4.0 / 3.0);
+    const double t2 = 0.0659 / D2 * ft * ft * exp(D2) * exp(-v * v / D2);
+    const double t3 = (1.0 / 3.0) * sqrt(2.0) / rpi * pow(ft, -4) * exp(8.0 * D2) / D * exp(-lft * lft / (2.0 * D2)) *
+                      sgwb_erfc((4.0 * D2 - lft + log(4.0)) / (D * sqrt(2.0)));
+    return scale * (t1 + t2 + t3);
+  }
+  // phase transition
+  const double rb = p[0], b = p[1], Ap = pow(10.0, p[2]), fp = pow(10.0, p[3]);
+  const double rb4 = rb * rb * rb * rb;
+  const double m = (9 * rb4 + b) / (rb4 + 1);
+  const double sr = f / fp, s4 = sr * sr * sr * sr, s9 = s4 * s4 * sr;
+  const double M = s9 * pow((1 + rb4) / (rb4 + s4), (9 - b) / 4) * pow((b + 4) / (b + 4 - m + m * sr * sr), (b + 4) / 2);
+  return Ap * M * pre;
 }
 
 // Inverse and log-determinant of a symmetric 3x3 covariance by the
@@ -134,6 +204,7 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_logl_kernel(NoiseArgs a) 
   const bool gal = a.sgal != nullptr;
   double Amp = 0, f1 = 0, alpha = 0, fk = 0, f2 = 0;
   if (gal) noise_gal_params(a.sgal + 5 * (size_t)p, Amp, f1, alpha, fk, f2);
+  const double *sgp = a.sgwb ? a.sgwb + 4 * (size_t)p : nullptr;
   const int N = a.N;
   const double *F = a.tab + (size_t)kTabF * N, *COSX = a.tab + (size_t)kTabCosx * N;
   const double *TDI = a.tab + (size_t)kTabTdi * N, *ACC = a.tab + (size_t)kTabAcc * N;
@@ -162,6 +233,18 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_logl_kernel(NoiseArgs a) 
         cxy += o;
         cxz += o;
         cyz += o;
+      }
+      if (sgp) {
+        // added last, as the instrument sampler combines the three
+        // (noise/src/glass_noise_sampler.c:559-568)
+        const double S = sgwb_psd(a.sg_type, f, sgp);
+        const double *R = a.rsg;
+        cxx += R[n] * S;
+        cyy += R[(size_t)N + n] * S;
+        czz += R[2 * (size_t)N + n] * S;
+        cxy += R[3 * (size_t)N + n] * S;
+        cxz += R[4 * (size_t)N + n] * S;
+        cyz += R[5 * (size_t)N + n] * S;
       }
     }
     double iv[6], logdetC;
@@ -196,8 +279,21 @@ struct NoiseWvArgs {
   double inv_ND;
   const double *tab, *P, *mod;
   const double *inst, *sgal;
+  int sg_type;
+  const double *sgwb, *rsg;  // [nprop][4] or null; 6 rows of Nlayer
   double *out;  // logl (modes 0/1) or partial (mode 2)
 };
+
+// The background's variance in layer j (generate_sgwb_model_wavelet
+// :843-892: the Fourier model at the layer centre over ND, zero in the DC
+// layer): sg6 = xx, yy, zz, xy, xz, yz.
+__device__ __forceinline__ void noise_wv_sgwb(const NoiseWvArgs &a, int j, const double *sgp, double *sg6) {
+  const int NL = a.Nlayer;
+  const double f = a.tab[(size_t)kTabF * NL + j];
+  const double S = f != 0.0 ? sgwb_psd(a.sg_type, f, sgp) : 0.0;
+#pragma unroll
+  for (int e = 0; e < 6; e++) sg6[e] = f != 0.0 ? a.rsg[(size_t)e * NL + j] * S * a.inv_ND : 0.0;
+}
 
 // Instrument (and foreground) variance of one layer in the wavelet domain:
 // the Fourier model at the layer centre over ND (generate_instrument_noise_
@@ -243,6 +339,7 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_wv_stationary_kernel(Nois
   if (gal) noise_gal_params(a.sgal + 5 * (size_t)p, Amp, f1, alpha, fk, f2);
   const int NL = a.Nlayer;
   const double Qd = (double)a.Q;
+  const double *sgp = a.sgwb ? a.sgwb + 4 * (size_t)p : nullptr;
   double acc = 0.0;
   for (int j = threadIdx.x; j < NL; j += blockDim.x) {
     double c6[6], g6[6];
@@ -254,6 +351,12 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_wv_stationary_kernel(Nois
       c6[3] -= g6[3] / 2.;
       c6[4] -= g6[4] / 2.;
       c6[5] -= g6[5] / 2.;
+    }
+    if (sgp) {  // added last (:1012-1019)
+      double s6[6];
+      noise_wv_sgwb(a, j, sgp, s6);
+#pragma unroll
+      for (int e = 0; e < 6; e++) c6[e] += s6[e];
     }
     double iv[6], ld;
     noise_inv3(c6[0], c6[1], c6[2], c6[3], c6[4], c6[5], iv, ld);
@@ -279,15 +382,21 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_wv_stationary_kernel(Nois
 constexpr int kNoiseWvMaxLJ = 64;
 __global__ void __launch_bounds__(kNoiseThreads) noise_wv_dynamic_kernel(NoiseWvArgs a) {
   __shared__ double red[kNoiseThreads / 32];
-  __shared__ double lay[kNoiseWvMaxLJ][12];
+  __shared__ double lay[kNoiseWvMaxLJ][18];
   const int chunk = blockIdx.x, p = blockIdx.y;
   const double *in = a.inst + 12 * (size_t)p;
   double Amp, f1, alpha, fk, f2;
   noise_gal_params(a.sgal + 5 * (size_t)p, Amp, f1, alpha, fk, f2);
+  const double *sgp = a.sgwb ? a.sgwb + 4 * (size_t)p : nullptr;
   const int j0 = chunk * a.LJ;
   const int nl = min(a.LJ, a.Nlayer - j0);
-  for (int t = threadIdx.x; t < nl; t += blockDim.x)
+  for (int t = threadIdx.x; t < nl; t += blockDim.x) {
     noise_wv_layer(a, j0 + t, in, true, Amp, f1, alpha, fk, f2, &lay[t][0], &lay[t][6]);
+    if (sgp)
+      noise_wv_sgwb(a, j0 + t, sgp, &lay[t][12]);
+    else
+      for (int e = 12; e < 18; e++) lay[t][e] = 0.0;
+  }
   __syncthreads();
   const int Nc = a.Ncoarse;
   const size_t Npix = (size_t)a.Nlayer * Nc;
@@ -298,6 +407,10 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_wv_dynamic_kernel(NoiseWv
     double c6[6];
 #pragma unroll
     for (int e = 0; e < 6; e++) c6[e] = lay[jj][e] + lay[jj][6 + e] * a.mod[(size_t)e * Nc + q];
+    if (sgp) {  // the stationary background last (:964-971)
+#pragma unroll
+      for (int e = 0; e < 6; e++) c6[e] += lay[jj][12 + e];
+    }
     double iv[6], ld;
     noise_inv3(c6[0], c6[1], c6[2], c6[3], c6[4], c6[5], iv, ld);
     const size_t k = (size_t)(j0 + jj) * Nc + q;
@@ -417,6 +530,81 @@ void noise_wv_build(int NT, double df, int lmin, int Nlayer, int Q, const double
   }
 }
 
+// Natural cubic spline through (x[i], y[i]) in the coefficient form
+// y0 + y1 d + y2 d^2 + y3 d^3 on interval i (the tridiagonal solve of
+// spline_coefficients, utils/src/glass_math.c:98-178), evaluated with the
+// even-spacing lookup of even_sampled_search (:393-402: floor of the offset
+// over x[1] - x[0], clamped to [0, n - 1]; the last node's polynomial is the
+// constant y[n - 1]).
+namespace {
+struct SgSpline {
+  std::vector<double> x, c0, c1, c2, c3;
+  void fit(const std::vector<double> &xs, const std::vector<double> &ys) {
+    const int n = (int)xs.size();
+    x = xs;
+    c0.assign(n, 0.0);
+    c1.assign(n, 0.0);
+    c2.assign(n, 0.0);
+    c3.assign(n, 0.0);
+    std::vector<double> h(n, 0.0), rhs(n, 0.0), diag(n, 1.0), up(n, 0.0), z(n, 0.0);
+    h[0] = xs[1] - xs[0];
+    for (int i = 1; i < n - 1; i++) {
+      h[i] = xs[i + 1] - xs[i];
+      rhs[i] = 3.0 * ((ys[i + 1] - ys[i]) / h[i] - (ys[i] - ys[i - 1]) / h[i - 1]);
+    }
+    for (int i = 1; i < n - 1; i++) {  // forward elimination, natural ends
+      diag[i] = 2.0 * (xs[i + 1] - xs[i - 1]) - h[i - 1] * up[i - 1];
+      up[i] = h[i] / diag[i];
+      z[i] = (rhs[i] - h[i - 1] * z[i - 1]) / diag[i];
+    }
+    c0[n - 1] = ys[n - 1];
+    for (int i = n - 2; i >= 0; i--) {  // back substitution
+      c0[i] = ys[i];
+      c2[i] = z[i] - up[i] * c2[i + 1];
+      c1[i] = (c0[i + 1] - c0[i]) / h[i] - h[i] * (c2[i + 1] + 2.0 * c2[i]) / 3.0;
+      c3[i] = (c2[i + 1] - c2[i]) / (3.0 * h[i]);
+    }
+  }
+  double at(double v) const {
+    const int n = (int)x.size();
+    int j = (int)floor((v - x[0]) / (x[1] - x[0]));
+    if (j < 0) j = 0;
+    if (j > n - 1) j = n - 1;
+    const double d = v - x[j];
+    return c0[j] + c1[j] * d + c2[j] * d * d + c3[j] * d * d * d;
+  }
+};
+}  // namespace
+
+int noise_sgwb_rows(int nresp, const double *resp, int N, const double *f, double *R6) {
+  // alloc_pop_sgwb_response (noise/src/glass_noise_model.c:134-189): 10 to
+  // 3000 rows; log of f and of the auto-responses, asinh of the
+  // cross-responses over 1e-7
+  if (nresp < 10 || nresp > 3000) return -1;
+  const double ascale = 1e-7;
+  std::vector<double> lf(nresp), col[6];
+  for (int e = 0; e < 6; e++) col[e].resize(nresp);
+  for (int i = 0; i < nresp; i++) {
+    const double *r = resp + 7 * (size_t)i;
+    if (!(r[0] > 0) || !(r[1] > 0) || !(r[2] > 0) || !(r[3] > 0)) return -1;
+    lf[i] = log(r[0]);
+    for (int e = 0; e < 3; e++) col[e][i] = log(r[1 + e]);
+    for (int e = 3; e < 6; e++) col[e][i] = asinh(r[1 + e] / ascale);
+  }
+  SgSpline sp[6];
+  for (int e = 0; e < 6; e++) sp[e].fit(lf, col[e]);
+  for (int n = 0; n < N; n++) {
+    if (f[n] == 0.0) {
+      for (int e = 0; e < 6; e++) R6[(size_t)e * N + n] = 0.0;
+      continue;
+    }
+    const double l = log(f[n]);  // generate_sgwb_model (:808-820)
+    for (int e = 0; e < 3; e++) R6[(size_t)e * N + n] = exp(sp[e].at(l));
+    for (int e = 3; e < 6; e++) R6[(size_t)e * N + n] = ascale * sinh(sp[e].at(l));
+  }
+  return 0;
+}
+
 static int noise_wv_lj(const NoiseWvDev &w) {
   int lj = 4096 / (w.Ncoarse > 0 ? w.Ncoarse : 1);
   if (lj < 1) lj = 1;
@@ -430,7 +618,7 @@ int noise_wv_chunks(const NoiseWvDev &w) {
 }
 
 cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const double *inst, const double *sgal,
-                                 double *logl, cudaStream_t stream, int *nlaunch) {
+                                 int sg_type, const double *sgwb, double *logl, cudaStream_t stream, int *nlaunch) {
   NoiseWvArgs a;
   a.Nlayer = w.Nlayer;
   a.Ncoarse = w.Ncoarse;
@@ -444,6 +632,9 @@ cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const
   a.mod = w.mod;
   a.inst = inst;
   a.sgal = sgal;
+  a.sg_type = sg_type;
+  a.sgwb = sgwb;
+  a.rsg = w.rsg;
   int launches = 0;
   cudaError_t e;
   if (mode != 2) {
@@ -452,6 +643,7 @@ cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const
       NoiseWvArgs s = a;
       s.inst = inst + 12 * (size_t)p0;
       s.sgal = sgal ? sgal + 5 * (size_t)p0 : nullptr;
+      s.sgwb = sgwb ? sgwb + 4 * (size_t)p0 : nullptr;
       s.out = logl + p0;
       noise_wv_stationary_kernel<<<np, kNoiseThreads, 0, stream>>>(s);
       launches++;
@@ -463,6 +655,7 @@ cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const
       NoiseWvArgs s = a;
       s.inst = inst + 12 * (size_t)p0;
       s.sgal = sgal + 5 * (size_t)p0;
+      s.sgwb = sgwb ? sgwb + 4 * (size_t)p0 : nullptr;
       s.out = w.partial + (size_t)p0 * a.nchunks;
       noise_wv_dynamic_kernel<<<dim3(a.nchunks, np), kNoiseThreads, 0, stream>>>(s);
       launches++;
@@ -483,8 +676,8 @@ cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const
 
 int noise_chunks(int N) { return (N + kNoiseChunk - 1) / kNoiseChunk; }
 
-cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst, const double *sgal, double *logl,
-                              cudaStream_t stream, int *nlaunch) {
+cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst, const double *sgal, int sg_type,
+                              const double *sgwb, double *logl, cudaStream_t stream, int *nlaunch) {
   NoiseArgs a;
   a.N = nd.N;
   a.nchunks = noise_chunks(nd.N);
@@ -492,6 +685,9 @@ cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst,
   a.tab = nd.tab;
   a.inst = inst;
   a.sgal = sgal;
+  a.sg_type = sg_type;
+  a.sgwb = sgwb;
+  a.rsg = nd.rsg;
   a.partial = nd.partial;
   int launches = 0;
   // models in slices of at most 65535 (the grid's y extent)
@@ -501,6 +697,7 @@ cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst,
     s.nprop = np;
     s.inst = inst + 12 * (size_t)p0;
     s.sgal = sgal ? sgal + 5 * (size_t)p0 : nullptr;
+    s.sgwb = sgwb ? sgwb + 4 * (size_t)p0 : nullptr;
     s.partial = nd.partial + (size_t)p0 * a.nchunks;
     noise_logl_kernel<<<dim3(a.nchunks, np), kNoiseThreads, 0, stream>>>(s);
     launches++;

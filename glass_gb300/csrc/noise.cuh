@@ -17,6 +17,7 @@ struct NoiseDev {
   int N = 0;
   double T = 0, fmin = 0;
   double *tab = nullptr;      // kNoiseTabRows x N
+  double *rsg = nullptr;      // 6 x N: the SGWB response (xx, yy, zz, xy, xz, yz) per bin, or null
   double *partial = nullptr;  // per-model chunk sums
   int partial_models = 0;     // models the partial buffer holds
 };
@@ -32,6 +33,7 @@ struct NoiseWvDev {
   double *tab = nullptr;      // kNoiseTabRows x Nlayer: layer-centre factors, then per-layer sums of P over q
   double *P = nullptr;        // 6 x Nlayer Ncoarse cell statistics (xx, yy, zz, xy, xz, yz)
   double *mod = nullptr;      // 6 x Ncoarse modulation of the foreground (or unused)
+  double *rsg = nullptr;      // 6 x Nlayer: the SGWB response at the layer centres, or null
   double *partial = nullptr;  // per-model chunk sums
   int partial_models = 0;
   void *mem = nullptr;        // backs tab, P, mod
@@ -44,14 +46,26 @@ struct NoiseWvDev {
 void noise_wv_build(int NT, double df, int lmin, int Nlayer, int Q, const double *X, const double *Y, const double *Z,
                     double *tab, double *P);
 int noise_wv_chunks(const NoiseWvDev &w);
-// mode 0 instrument, 1 stationary foreground, 2 modulated foreground;
+// mode 0 instrument, 1 stationary foreground, 2 modulated foreground; plus,
+// with sgwb (4 per model, template sg_type), the stochastic background;
 // w.partial must hold nprop x noise_wv_chunks(w) (mode 2).
 cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const double *inst, const double *sgal,
-                                 double *logl, cudaStream_t stream, int *nlaunch);
+                                 int sg_type, const double *sgwb, double *logl, cudaStream_t stream, int *nlaunch);
+
+// SGWB templates (SGWB_t, noise/src/glass_noise_model.h:99-108) and their
+// parameter counts
+enum { kSgwbPowerlaw = 0, kSgwbLognormal = 1, kSgwbPhaseTransition = 2, kSgwbTypes = 3 };
+constexpr int kSgwbParams[kSgwbTypes] = {2, 3, 4};
+// The instrument's SGWB response at frequencies f[N] from the table rows
+// resp[7 i ..] = f, XX, YY, ZZ, XY, XZ, YZ (i < nresp): R6[e N + n], e = xx,
+// yy, zz, xy, xz, yz (0 at f = 0).  Returns 0, or -1 for a table the
+// reference would refuse or cannot take a log of.
+int noise_sgwb_rows(int nresp, const double *resp, int N, const double *f, double *R6);
 int noise_chunks(int N);
 // logl[p] for noise models inst[12 p ..] (sacc[6], soms[6]) and sgal[5 p ..]
-// (or null: instrument only); nd.partial must hold nprop x noise_chunks(N).
-cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst, const double *sgal, double *logl,
-                              cudaStream_t stream, int *nlaunch);
+// (or null: instrument only), plus, with sgwb[4 p ..] (or null), the SGWB of
+// template sg_type; nd.partial must hold nprop x noise_chunks(N).
+cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst, const double *sgal, int sg_type,
+                              const double *sgwb, double *logl, cudaStream_t stream, int *nlaunch);
 
 }  // namespace glass

@@ -68,6 +68,17 @@ class Orbit(ctypes.Structure):
                 ("dz", ctypes.c_void_p), ("orbit_function", ctypes.c_void_p)]
 
 
+class Wavelets(ctypes.Structure):
+    """utils/src/glass_wavelet.h:25-75"""
+    _fields_ = [("NF", c_int), ("NT", c_int), ("cadence", c_double), ("dt", c_double), ("df", c_double),
+                ("frequency_steps", c_int), ("fdot_steps", c_int), ("d_fdot", c_double), ("oversample", c_int),
+                ("Omega", c_double), ("dOmega", c_double), ("domega", c_double), ("inv_root_dOmega", c_double),
+                ("B", c_double), ("A", c_double), ("BW", c_double), ("deltaf", c_double), ("fdot", _D),
+                ("window", _D), ("window_freq_forward", _D), ("norm", c_double), ("N", c_int), ("T", c_double),
+                ("kmin", c_int), ("kmax", c_int), ("imin", c_int), ("imax", c_int), ("n_table", ctypes.c_void_p),
+                ("table", ctypes.c_void_p)]
+
+
 class Keep:
     """Holds the numpy arrays behind a struct's pointers."""
 
@@ -147,6 +158,62 @@ def make_model(keep, params_list, NFFT, noise):
 
 
 
+def make_orbit_nodes(keep, t, pos):
+    """struct Orbit holding node times t and positions pos[sc, dim, node]."""
+    o = Orbit()
+    o.Norb = len(t)
+    o.t = keep.arr(t)
+    for name, d in (("x", 0), ("y", 1), ("z", 2)):
+        setattr(o, name, keep.ptrs([pos[sc, d] for sc in range(3)]))
+    keep.refs.append(o)
+    return o
+
+
+def make_wavelets(keep, NF, NT, wdt, kmin, kmax, imin=0, imax=0):
+    w = Wavelets()
+    w.NF, w.NT, w.dt, w.df, w.A = NF, NT, wdt, 1 / (2 * wdt), 0.0
+    w.kmin, w.kmax, w.imin, w.imax = kmin, kmax, imin, imax
+    keep.refs.append(w)
+    return w
+
+
+def make_noise_xyz(keep, invC):
+    """struct Noise with the 3 x 3 inverse covariance invC[i, j, k] per pixel."""
+    n = Noise()
+    n.N, n.Nchannel = invC.shape[2], 3
+    outer = (_DD * 3)(*[keep.ptrs([invC[i, j] for j in range(3)]) for i in range(3)])
+    keep.refs.append(outer)
+    n.invC = ctypes.cast(outer, _DDD)
+    n.C = n.invC
+    keep.refs.append(n)
+    return n
+
+
+def make_wavelet_tdi(keep, xyz):
+    """struct TDI of the X, Y, Z pixel arrays xyz[3, N]."""
+    t = TDI()
+    N = xyz.shape[1]
+    t.X, t.Y, t.Z = (keep.arr(xyz[c]) for c in range(3))
+    t.A, t.E, t.T = (keep.arr(np.zeros(N)) for _ in range(3))
+    t.Nchannel, t.N = 3, N
+    keep.refs.append(t)
+    return t
+
+
+def make_wavelet_model(keep, xyz, pixels, noise):
+    """struct Model of one wavelet-domain template: its pixel arrays, its
+    pixel list and the noise it is weighted with."""
+    m = Model()
+    m.tdi = ctypes.pointer(make_wavelet_tdi(keep, xyz))
+    lst = np.ascontiguousarray(pixels, np.int32)
+    keep.refs.append(lst)
+    m.list = lst.ctypes.data_as(ctypes.POINTER(c_int))
+    m.Nlist = len(lst)
+    m.noise = ctypes.pointer(noise)
+    keep.refs.append(m)
+    return m
+
+
 def bind_dropins(L):
     """argtypes/restypes of the struct-based drop-ins on a loaded library."""
     P = ctypes.POINTER
@@ -163,4 +230,11 @@ def bind_dropins(L):
     L.ucb_fisher.argtypes = [P(Orbit), P(Data), P(Source), P(Noise)]
     L.matrix_eigenstuff.argtypes = [_DD, _DD, _D, c_int]
     L.wavelet_transform_timefreq_by_layers.argtypes = [ctypes.c_void_p, c_int, c_int, _D, _D]
+    L.wavelet_nwip.argtypes = [_D, _D, _D, P(c_int), c_int]
+    L.wavelet_nwip.restype = c_double
+    L.snr_wavelet.argtypes = [P(Source), P(Noise)]
+    L.snr_wavelet.restype = c_double
+    L.delta_log_likelihood.argtypes = [P(Data), P(Model), P(Model)]
+    L.delta_log_likelihood.restype = c_double
+    L.ucb_fisher_wavelet.argtypes = [P(Orbit), P(Data), P(Source), P(Noise)]
     return L

@@ -216,6 +216,59 @@ def default_noise_params(T=T_YEAR):
     return inst, sgal
 
 
+def sgwb_response_table(n=1000, fmin=1e-5, fmax=1.0):
+    """A synthetic instrument response to an isotropic stochastic background
+    in the layout of the noise module's response file (rows f, XX, YY, ZZ, XY,
+    XZ, YZ; f log-evenly spaced): a smooth equal-arm-like shape, x^6 at low
+    frequency (x = f / f*) with transfer-function ripples above f*, slightly
+    unequal channels, cross-responses near -1/2 of the auto-responses at low
+    frequency that change sign above f*.  Stands in for the response file the
+    reference reads, which is data, not part of this library."""
+    f = np.exp(np.linspace(math.log(fmin), math.log(fmax), n))
+    x = f / FSTAR
+    auto = 27.0 * np.sin(x) ** 2 * x ** 4 / (1.0 + 0.6 * x ** 2) + 1e-30 * x ** 2
+    rows = np.empty((n, 7))
+    rows[:, 0] = f
+    rows[:, 1] = auto
+    rows[:, 2] = auto * (1.0 + 1e-3 * np.sin(x))
+    rows[:, 3] = auto * (1.0 - 1e-3 * np.sin(2 * x))
+    cross = -0.5 * auto * np.cos(x) / (1.0 + 0.05 * x ** 2)
+    rows[:, 4] = cross
+    rows[:, 5] = cross * (1.0 + 2e-3 * np.cos(x))
+    rows[:, 6] = cross * (1.0 - 2e-3 * np.sin(x))
+    return rows
+
+
+def default_sgwb_params(sgwb_type):
+    """The noise module's starting point per SGWB template
+    (default_sgwb_injection, noise/src/glass_noise_model.c:1459-1486)."""
+    return {0: np.array([-8.45, 2.0 / 3.0]), 1: np.array([-2.5, math.log(2e-3) / math.log(10.0), 0.0]),
+            2: np.array([1.0, 1.0, -18.0, -2.5])}[int(sgwb_type)]
+
+
+def sgwb_params_draw(rng, sgwb_type, n):
+    """n parameter sets [n, 4] of an SGWB template around its starting point,
+    the amplitude raised so that the background rivals the instrument noise
+    near 2 mHz (power law x30, lognormal x3 in A, phase transition x1e9);
+    phase transitions kept where their spectrum is finite at every
+    frequency (rb^4 (5 - b) < 4, i.e. b + 4 > m)."""
+    t = int(sgwb_type)
+    p0 = default_sgwb_params(t)
+    lift = {0: 1.5, 1: 0.5, 2: 9.0}[t]
+    out = np.zeros((n, 4))
+    for k in range(n):
+        while True:
+            p = p0 + rng.uniform(-0.3, 0.3, len(p0))
+            p[0 if t < 2 else 2] += lift
+            if t == 2:
+                p[1] = rng.uniform(1.5, 3.0)
+                if p[0] ** 4 * (5.0 - p[1]) >= 3.6:
+                    continue
+            break
+        out[k, :len(p0)] = p
+    return out
+
+
 def xyz_from_covariance(rng, C6):
     """Complex XYZ bins with E[x x^H] = C for real symmetric per-bin C given as
     [N, 6] = xx, yy, zz, xy, xz, yz; returned interleaved (3, 2N)."""

@@ -96,12 +96,23 @@ struct Noise;  /* utils/src/glass_data.h:337-360; read: invC */
  *   gaussian_log_likelihood  utils/src/glass_model.c:726
  *   matrix_eigenstuff        utils/src/glass_math.c:475
  *   ucb_fisher               ucb/src/glass_ucb_waveform.c:364 (glass_ucb_waveform.h:150)
+ *   wavelet_nwip, snr_wavelet  utils/src/glass_math.c:382, :428 (glass_math.h:261)
+ *   delta_log_likelihood     utils/src/glass_model.c:624 (glass_model.h:211), wavelet basis
+ *   ucb_fisher_wavelet       ucb/src/glass_ucb_waveform.c:524 (glass_ucb_waveform.h:156)
  * Waveforms come from the GPU ucb_waveform above.  ucb_fisher takes its
  * Fisher matrix for A/E data from the adjoint kernels (glass_gpu_grad_fisher
  * _batch with the reference's noise indexing, fisher_mode 1; the segment's
  * noise is uploaded to the thread's context when it changes), and for X or
  * XYZ data from forward differences of the GPU waveform as the reference
- * does.  The sums over a segment's bins run on the caller's host arrays in
+ * does.  ucb_fisher_wavelet takes its Fisher matrix from the batched
+ * wavelet Fisher kernels (glass_gpu_wavelet_fisher_batch: the reference's
+ * central differences of the FP64 wavelet waveform) on the grid of
+ * data->wdm, the segment of data (T, t0; data->N must be kmax - kmin) and the
+ * nodes of the caller's orbit, weighted with noise->invC; then the
+ * eigen-decomposition and, where an eigenvalue is not positive, the
+ * reference's regularisation (0.1 added to the diagonal, decomposition
+ * redone; still not positive: report and exit(1)).  The sums over a
+ * segment's bins or a pixel list run on the caller's host arrays in
  * the reference's order of operations (bit-identical): a GPU launch per call
  * would cost more than the arithmetic.  matrix_eigenstuff: symmetric input
  * (the reference passes Fisher matrices to LAPACK's general solver);
@@ -123,6 +134,10 @@ double snr(struct Source *source, struct Noise *noise);
 double gaussian_log_likelihood(struct Data *data, struct Model *model);
 void matrix_eigenstuff(double **matrix, double **evectors, double *evalues, int N);
 void ucb_fisher(struct Orbit *orbit, struct Data *data, struct Source *source, struct Noise *noise);
+double wavelet_nwip(const double *a, const double *b, const double *invC, const int *list, int N);
+double snr_wavelet(struct Source *source, struct Noise *noise);
+double delta_log_likelihood(struct Data *data, struct Model *model_x, struct Model *model_y);
+void ucb_fisher_wavelet(struct Orbit *orbit, struct Data *data, struct Source *source, struct Noise *noise);
 
 /* ---------------------------------------------------------- batched API */
 typedef struct glass_gpu_ctx glass_gpu_ctx;
@@ -303,6 +318,40 @@ int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double 
                                     double *logl);
 
 /*
+ * A stochastic gravitational-wave background (SGWB) added to the noise
+ * covariance of both likelihoods above (the noise module's SGWBModel:
+ * generate_sgwb_model, noise/src/glass_noise_model.c:778, in the Fourier
+ * domain; generate_sgwb_model_wavelet, :843, at the layer centres over ND in
+ * the wavelet domain).  glass_gpu_noise_sgwb_setup sets the spectral template
+ * (SGWB_t, noise/src/glass_noise_model.h:99):
+ *   0 power law         p = log10 A, alpha
+ *   1 lognormal         p = log10 A, log10 fstar [Hz], log10 Delta
+ *   2 phase transition  p = rb, b, log10 Ap, log10 fp [Hz]
+ * (-1 removes it) and the instrument's response to an isotropic background as
+ * the rows resp[7 i ..] = f, XX, YY, ZZ, XY, XZ, YZ, i < nresp (10 .. 3000;
+ * the content of the reference's response file, read by
+ * alloc_pop_sgwb_response, :134; f log-evenly spaced, f and the auto-responses
+ * positive).  The response enters as the reference builds it: cubic splines
+ * over log f of log XX, log YY, log ZZ and asinh(XY / 1e-7), ... evaluated at
+ * every bin (or layer centre) of the grids set up, now and by later
+ * glass_gpu_noise_setup / glass_gpu_noise_wavelet_setup calls.  Host
+ * pointers; synchronous.
+ *
+ * The _sgwb batch forms take sgwb[4 p ..] (the template's first 2, 3 or 4
+ * parameters; the rest ignored), or NULL for no background, and add
+ * C_ij += R_ij(f) S(f) after the instrument and foreground, as
+ * noise_instrument_model_mcmc (noise/src/glass_noise_sampler.c:559-568) and
+ * the coarse wavelet covariances (:923, :983) combine them.  FP64.  Device
+ * pointers, asynchronous; _host forms: host pointers, synchronous.  The
+ * forms without _sgwb are these with sgwb = NULL.
+ */
+int glass_gpu_noise_sgwb_setup(glass_gpu_ctx *ctx, int type, int nresp, const double *resp);
+int glass_gpu_noise_logl_batch_sgwb(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                    const double *sgwb, double *logl);
+int glass_gpu_noise_logl_batch_sgwb_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
+                                         const double *sgwb, double *logl);
+
+/*
  * The same likelihood in the wavelet domain, coarse-grained
  * (my_noise_log_likelihood_wavelet_coarse, noise/src/glass_noise_model.c:1211;
  * Q = 1 is the full-resolution my_noise_log_likelihood_wavelet, :1182).
@@ -328,6 +377,10 @@ int glass_gpu_noise_wavelet_logl_batch(glass_gpu_ctx *ctx, int mode, int nprop, 
                                        double *logl);
 int glass_gpu_noise_wavelet_logl_batch_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
                                             const double *sgal, double *logl);
+int glass_gpu_noise_wavelet_logl_batch_sgwb(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                            const double *sgal, const double *sgwb, double *logl);
+int glass_gpu_noise_wavelet_logl_batch_sgwb_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
+                                                 const double *sgal, const double *sgwb, double *logl);
 
 /* glass_gpu_dlogl_batch with each channel's share of term_y as well:
  * term_ch[2 i] (A) + term_ch[2 i + 1] (E) = term_y[i].  Device pointers. */

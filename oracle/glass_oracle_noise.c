@@ -99,6 +99,120 @@ static void orc_noise_cov_bin(double f, const double *sacc, const double *soms, 
     }
 }
 
+/* ------------------------------------------------------------------ SGWB */
+/* utils/src/glass_constants.h:81-86 */
+#define ORC_H0 (70 * 3.24078e-20)
+#define ORC_HSCALE (3 * ORC_H0 * ORC_H0 / (4 * M_PI * M_PI))
+#define ORC_CGOR0 (1.6e-5 / (0.7 * 0.7))
+
+/* glass_erfc (utils/src/glass_math.c:1310-1320): Abramowitz & Stegun 7.1.26 */
+static double orc_erfc(double x)
+{
+    double ax = fabs(x);
+    double t = 1.0 / (1.0 + 0.3275911 * ax);
+    double poly = ((((1.061405429 * t - 1.453152027) * t + 1.421413741) * t - 0.284496736) * t + 0.254829592) * t;
+    double y = poly * exp(-ax * ax);
+    return (x < 0.0) ? (2.0 - y) : y;
+}
+
+/* sgwb_powerlaw, sgwb_lognormal, sgwb_phase_transition
+ * (noise/src/glass_noise_model.c:725-776), in their operation order */
+double orc_sgwb_psd(int type, double f, const double *p)
+{
+    double prefactor = ORC_HSCALE / (f * f * f);
+    if (type == 0) {
+        double A = pow(10.0, p[0]);
+        return prefactor * A * pow(f / 25.0, p[1]);
+    }
+    if (type == 1) {
+        double A = pow(10.0, p[0]), fst = pow(10.0, p[1]), D = pow(10.0, p[2]);
+        double ft = f / fst;
+        if (D < 9.0) {
+            double logft = log(ft);
+            double logK = logft + 1.5 * D * D;
+            double sqrtpi = sqrt(M_PI);
+            double half_log32 = 0.5 * log(1.5);
+            double D2 = D * D;
+            double t1 = 4.0 / 5.0 / sqrtpi * ft * ft * ft * exp(9.0 * D2 / 4.0) / D *
+                        ((logK * logK + 0.5 * D2) * orc_erfc((logK + half_log32) / D) -
+                         D / sqrtpi * exp(-(logK + half_log32) * (logK + half_log32) / D2) * (logK - half_log32));
+            double t2 = 0.0659 / D2 * ft * ft * exp(D2) *
+                        exp(-(logft + D2 - 0.5 * log(4.0 / 3.0)) * (logft + D2 - 0.5 * log(4.0 / 3.0)) / D2);
+            double t3 = (1.0 / 3.0) * sqrt(2.0) / sqrtpi * pow(ft, -4) * exp(8.0 * D2) / D *
+                        exp(-logft * logft / (2.0 * D2)) * orc_erfc((4.0 * D2 - logft + log(4.0)) / (D * sqrt(2.0)));
+            return prefactor * ORC_CGOR0 * A * A * (t1 + t2 + t3);
+        }
+        return prefactor * ORC_CGOR0 * A * A * 0.783 / 1e3;
+    }
+    double rb = p[0], b = p[1], Ap = pow(10.0, p[2]), fp = pow(10.0, p[3]);
+    double rb4 = rb * rb * rb * rb;
+    double m = (9 * rb4 + b) / (rb4 + 1);
+    double sv = f / fp;
+    double s4 = sv * sv * sv * sv;
+    double s9 = s4 * s4 * sv;
+    double M = s9 * pow((1 + rb4) / (rb4 + s4), (9 - b) / 4) * pow((b + 4) / (b + 4 - m + m * sv * sv), (b + 4) / 2);
+    return Ap * M * prefactor;
+}
+
+/* The response R6[e N + n] (xx, yy, zz, xy, xz, yz) at f[n]: natural cubic
+ * splines over log f of log XX, log YY, log ZZ and asinh(XY / 1e-7), ...
+ * (alloc_pop_sgwb_response, noise/src/glass_noise_model.c:134-189), evaluated
+ * as generate_sgwb_model does (:808-820); 0 at f = 0.  resp[7 i ..] = f, XX,
+ * YY, ZZ, XY, XZ, YZ. */
+void orc_sgwb_response(int nresp, const double *resp, int N, const double *f, double *R6)
+{
+    const double ascale = 1e-7;
+    double *x = malloc(sizeof(double) * nresp), *y = malloc(sizeof(double) * nresp);
+    double *h = calloc(nresp, sizeof(double)), *al = calloc(nresp, sizeof(double));
+    double *l = calloc(nresp, sizeof(double)), *z = calloc(nresp, sizeof(double)), *mu = calloc(nresp, sizeof(double));
+    double *c0 = malloc(sizeof(double) * nresp), *c1 = malloc(sizeof(double) * nresp);
+    double *c2 = malloc(sizeof(double) * nresp), *c3 = malloc(sizeof(double) * nresp);
+    for (int i = 0; i < nresp; i++) x[i] = log(resp[7 * i]);
+    for (int e = 0; e < 6; e++) {
+        for (int i = 0; i < nresp; i++) {
+            double v = resp[7 * i + 1 + e];
+            y[i] = e < 3 ? log(v) : asinh(v / ascale);
+        }
+        /* spline_coefficients (utils/src/glass_math.c:98-178) */
+        h[0] = x[1] - x[0];
+        for (int i = 1; i < nresp - 1; i++) {
+            h[i] = x[i + 1] - x[i];
+            al[i] = 3.0 * ((y[i + 1] - y[i]) / h[i] - (y[i] - y[i - 1]) / h[i - 1]);
+        }
+        l[0] = l[nresp - 1] = 1.0;
+        mu[0] = z[0] = 0.0;
+        for (int i = 1; i < nresp - 1; i++) {
+            l[i] = 2.0 * (x[i + 1] - x[i - 1]) - h[i - 1] * mu[i - 1];
+            mu[i] = h[i] / l[i];
+            z[i] = (al[i] - h[i - 1] * z[i - 1]) / l[i];
+        }
+        c0[nresp - 1] = y[nresp - 1];
+        c1[nresp - 1] = c2[nresp - 1] = c3[nresp - 1] = 0.0;
+        for (int i = nresp - 2; i >= 0; i--) {
+            c0[i] = y[i];
+            c2[i] = z[i] - mu[i] * c2[i + 1];
+            c1[i] = (c0[i + 1] - c0[i]) / h[i] - h[i] * (c2[i + 1] + 2.0 * c2[i]) / 3.0;
+            c3[i] = (c2[i + 1] - c2[i]) / (3.0 * h[i]);
+        }
+        for (int n = 0; n < N; n++) {
+            if (f[n] == 0.0) {
+                R6[(size_t)e * N + n] = 0.0;
+                continue;
+            }
+            double v = log(f[n]);
+            /* even_sampled_search (utils/src/glass_math.c:393-402) */
+            int j = (int)floor((v - x[0]) / (x[1] - x[0]));
+            if (j < 0) j = 0;
+            if (j > nresp - 1) j = nresp - 1;
+            double d = v - x[j];
+            double s = c0[j] + c1[j] * d + c2[j] * d * d + c3[j] * d * d * d;
+            R6[(size_t)e * N + n] = e < 3 ? exp(s) : ascale * sinh(s);
+        }
+    }
+    free(x); free(y); free(h); free(al); free(l); free(z); free(mu);
+    free(c0); free(c1); free(c2); free(c3);
+}
+
 /*
  * One noise model on the XYZ frequency grid f_n = fmin + n/T, n < N:
  *  - instrument covariance (noise/src/glass_noise_model.c:389-546, three
@@ -112,8 +226,23 @@ static void orc_noise_cov_bin(double f, const double *sacc, const double *soms, 
  *  - my_noise_log_likelihood (noise/src/glass_noise_model.c:1243-1273).
  * X, Y, Z: 2N doubles each (re/im).  Returns logL.
  */
+double orc_noise_logl_sgwb(double T, double fmin, int N, const double *X, const double *Y, const double *Z,
+                           const double *sacc, const double *soms, const double *sgal, int sg_type,
+                           const double *sgwb, const double *R6);
+
 double orc_noise_logl(double T, double fmin, int N, const double *X, const double *Y, const double *Z,
                       const double *sacc, const double *soms, const double *sgal)
+{
+    return orc_noise_logl_sgwb(T, fmin, N, X, Y, Z, sacc, soms, sgal, -1, NULL, NULL);
+}
+
+/* orc_noise_logl with, when sgwb is given, the background of template
+ * sg_type added last (noise_instrument_model_mcmc's order,
+ * noise/src/glass_noise_sampler.c:559-568): C += R(f) S(f), the response
+ * R6 (6 rows of N, orc_sgwb_response) at the grid's bins. */
+double orc_noise_logl_sgwb(double T, double fmin, int N, const double *X, const double *Y, const double *Z,
+                           const double *sacc, const double *soms, const double *sgal, int sg_type,
+                           const double *sgwb, const double *R6)
 {
     double Amp = 0, f1 = 0, alpha = 0, fk = 0, f2 = 0;
     if (sgal) {
@@ -130,6 +259,15 @@ double orc_noise_logl(double T, double fmin, int N, const double *X, const doubl
         double C[3][3];
         orc_noise_cov_bin(f, sacc, soms, sgal != NULL, Amp, f1, alpha, fk, f2, C);
         double cxx = C[0][0], cyy = C[1][1], czz = C[2][2], cxy = C[0][1], cxz = C[0][2], cyz = C[1][2];
+        if (sgwb && f != 0.0) {
+            double S = orc_sgwb_psd(sg_type, f, sgwb);
+            cxx += R6[n] * S;
+            cyy += R6[(size_t)N + n] * S;
+            czz += R6[2 * (size_t)N + n] * S;
+            cxy += R6[3 * (size_t)N + n] * S;
+            cxz += R6[4 * (size_t)N + n] * S;
+            cyz += R6[5 * (size_t)N + n] * S;
+        }
         double d1 = cxx;
         double d2 = cyy - cxy * cxy / d1;
         double tt = cyz - cxy * cxz / d1;
@@ -162,6 +300,25 @@ double orc_noise_logl(double T, double fmin, int N, const double *X, const doubl
     }
     logL -= 3 * N * log2pi;
     return logL;
+}
+
+/* Batched form with the background: sgwb[4 p ..] of template sg_type. */
+void orc_noise_logl_sgwb_batch(double T, double fmin, int N, const double *X, const double *Y, const double *Z,
+                               int nprop, const double *inst, const double *sgal, int sg_type, const double *sgwb,
+                               int nresp, const double *resp, double *logl, int nthreads)
+{
+    double *f = malloc(sizeof(double) * N), *R6 = malloc(sizeof(double) * 6 * (size_t)N);
+    for (int n = 0; n < N; n++) f[n] = fmin + (double)n / T;
+    orc_sgwb_response(nresp, resp, N, f, R6);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int p = 0; p < nprop; p++)
+        logl[p] = orc_noise_logl_sgwb(T, fmin, N, X, Y, Z, inst + 12 * (size_t)p, inst + 12 * (size_t)p + 6,
+                                      sgal ? sgal + 5 * (size_t)p : NULL, sg_type, sgwb + 4 * (size_t)p, R6);
+    free(f);
+    free(R6);
 }
 
 /* Batched form: inst[12 p ..] = sacc[6], soms[6]; sgal[5 p ..] or NULL. */
@@ -243,8 +400,24 @@ static void orc_invert3(const double *c6, double *i6, double *logdet)
  *    :1057-1102, cell k = q + j Ncoarse), minus 3/2 Nlayer NT log 2 pi.
  * inst: sacc[6], soms[6]; sgal: 5 (unused in mode 0).
  */
+double orc_noise_wavelet_logl_sgwb(int NF, int NT, double df, int lmin, int Nlayer, int Q, const double *P, int mode,
+                                   const double *mod, const double *inst, const double *sgal, int sg_type,
+                                   const double *sgwb, const double *R6);
+
 double orc_noise_wavelet_logl(int NF, int NT, double df, int lmin, int Nlayer, int Q, const double *P, int mode,
                               const double *mod, const double *inst, const double *sgal)
+{
+    return orc_noise_wavelet_logl_sgwb(NF, NT, df, lmin, Nlayer, Q, P, mode, mod, inst, sgal, -1, NULL, NULL);
+}
+
+/* With the background (generate_sgwb_model_wavelet,
+ * noise/src/glass_noise_model.c:843-892: the Fourier model at the layer
+ * centre over ND, zero in the DC layer) added last to every cell's
+ * covariance (:964-971, :1012-1019); R6: 6 rows of Nlayer at the layer
+ * centres. */
+double orc_noise_wavelet_logl_sgwb(int NF, int NT, double df, int lmin, int Nlayer, int Q, const double *P, int mode,
+                                   const double *mod, const double *inst, const double *sgal, int sg_type,
+                                   const double *sgwb, const double *R6)
 {
     const int Ncoarse = NT / Q;
     const double inv_ND = 1.0 / (double)(NF * NT);
@@ -282,6 +455,11 @@ double orc_noise_wavelet_logl(int NF, int NT, double df, int lmin, int Nlayer, i
             conf6[0] = conf6[1] = conf6[2] = dg * inv_ND;
             conf6[3] = conf6[4] = conf6[5] = og * inv_ND;
         }
+        double sg6[6] = {0, 0, 0, 0, 0, 0};
+        if (sgwb && lmin + j != 0) {
+            double S = orc_sgwb_psd(sg_type, f, sgwb);
+            for (int e = 0; e < 6; e++) sg6[e] = R6[(size_t)e * Nlayer + j] * S * inv_ND;
+        }
         for (int q = 0; q < Ncoarse; q++) {
             double c6[6], i6[6], ld;
             for (int e = 0; e < 6; e++) c6[e] = inst6[e];
@@ -291,6 +469,8 @@ double orc_noise_wavelet_logl(int NF, int NT, double df, int lmin, int Nlayer, i
             } else if (mode == 2) {
                 for (int e = 0; e < 6; e++) c6[e] += conf6[e] * mod[(size_t)e * Ncoarse + q];
             }
+            if (sgwb)
+                for (int e = 0; e < 6; e++) c6[e] += sg6[e];
             orc_invert3(c6, i6, &ld);
             size_t k = (size_t)q + (size_t)j * Ncoarse;
             double s = 0.0;
@@ -329,6 +509,25 @@ void orc_noise_coarse_stats(int NT, int Nlayer, int Q, const double *X, const do
             P[kc] = sxx * invQ; P[Npix + kc] = syy * invQ; P[2 * Npix + kc] = szz * invQ;
             P[3 * Npix + kc] = sxy * invQ; P[4 * Npix + kc] = sxz * invQ; P[5 * Npix + kc] = syz * invQ;
         }
+}
+
+void orc_noise_wavelet_logl_sgwb_batch(int NF, int NT, double df, int lmin, int Nlayer, int Q, const double *P,
+                                       int mode, const double *mod, int nprop, const double *inst,
+                                       const double *sgal, int sg_type, const double *sgwb, int nresp,
+                                       const double *resp, double *logl, int nthreads)
+{
+    double *f = malloc(sizeof(double) * Nlayer), *R6 = malloc(sizeof(double) * 6 * (size_t)Nlayer);
+    for (int j = 0; j < Nlayer; j++) f[j] = (double)(lmin + j) * df;
+    orc_sgwb_response(nresp, resp, Nlayer, f, R6);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int p = 0; p < nprop; p++)
+        logl[p] = orc_noise_wavelet_logl_sgwb(NF, NT, df, lmin, Nlayer, Q, P, mode, mod, inst + 12 * (size_t)p,
+                                              sgal ? sgal + 5 * (size_t)p : NULL, sg_type, sgwb + 4 * (size_t)p, R6);
+    free(f);
+    free(R6);
 }
 
 void orc_noise_wavelet_logl_batch(int NF, int NT, double df, int lmin, int Nlayer, int Q, const double *P, int mode,

@@ -230,6 +230,64 @@ class Port:
                                          len(inst), _p(inst), _p(sg) if sg is not None else None, _p(out), nthreads)
         return out
 
+    def sgwb_psd(self, sgwb_type, f, params):
+        """The background's strain PSD of template sgwb_type at f > 0."""
+        lib = self.lib
+        lib.orc_sgwb_psd.argtypes = [ctypes.c_int, ctypes.c_double, _D]
+        lib.orc_sgwb_psd.restype = ctypes.c_double
+        p = np.zeros(4)
+        p[:len(params)] = params
+        return lib.orc_sgwb_psd(int(sgwb_type), float(f), _p(p))
+
+    def sgwb_response(self, resp, f):
+        """[6, len(f)] response xx, yy, zz, xy, xz, yz at f from the table rows resp [n, 7]."""
+        lib = self.lib
+        lib.orc_sgwb_response.argtypes = [ctypes.c_int, _D, ctypes.c_int, _D, _D]
+        r = np.ascontiguousarray(resp, np.float64).reshape(-1, 7)
+        f = np.ascontiguousarray(f, np.float64)
+        out = np.zeros((6, len(f)))
+        lib.orc_sgwb_response(len(r), _p(r), len(f), _p(f), _p(out))
+        return out
+
+    def noise_logl_sgwb(self, T, fmin, X, Y, Z, inst, sgal, sgwb_type, sgwb, resp, nthreads=0):
+        """noise_logl with the background of template sgwb_type (sgwb [n, 4]) added last."""
+        lib = self.lib
+        lib.orc_noise_logl_sgwb_batch.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _D, _D, _D,
+                                                  ctypes.c_int, _D, _D, ctypes.c_int, _D, ctypes.c_int, _D, _D,
+                                                  ctypes.c_int]
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        b = np.ascontiguousarray(sgwb, np.float64).reshape(-1, 4)
+        r = np.ascontiguousarray(resp, np.float64).reshape(-1, 7)
+        out = np.zeros(len(inst))
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        lib.orc_noise_logl_sgwb_batch(T, fmin, len(X) // 2, _p(X), _p(Y), _p(Z), len(inst), _p(inst),
+                                      _p(sg) if sg is not None else None, int(sgwb_type), _p(b), len(r), _p(r),
+                                      _p(out), nthreads)
+        return out
+
+    def noise_wavelet_logl_sgwb(self, NF, NT, df, lmin, P, Q, inst, sgal, mode, mod, sgwb_type, sgwb, resp,
+                                nthreads=0):
+        """noise_wavelet_logl with the background added last to every cell."""
+        lib = self.lib
+        lib.orc_noise_wavelet_logl_sgwb_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                          ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, _D,
+                                                          ctypes.c_int, _D, _D, ctypes.c_int, _D, ctypes.c_int, _D,
+                                                          _D, ctypes.c_int]
+        P = np.ascontiguousarray(P, np.float64)
+        Nlayer = P.shape[1]
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        md = None if mod is None else np.ascontiguousarray(mod, np.float64)
+        b = np.ascontiguousarray(sgwb, np.float64).reshape(-1, 4)
+        r = np.ascontiguousarray(resp, np.float64).reshape(-1, 7)
+        out = np.zeros(len(inst))
+        lib.orc_noise_wavelet_logl_sgwb_batch(NF, NT, df, lmin, Nlayer, Q, _p(P), mode,
+                                              _p(md) if md is not None else None, len(inst), _p(inst),
+                                              _p(sg) if sg is not None else None, int(sgwb_type), _p(b), len(r),
+                                              _p(r), _p(out), nthreads)
+        return out
+
     def noise_coarse_stats(self, NT, Q, X, Y, Z):
         """[6, Nlayer, NT/Q] cell statistics of wavelet data [Nlayer NT] (coarse_grain_wavelet_data)."""
         lib = self.lib
@@ -698,6 +756,56 @@ class Ref:
                                    _p(md) if md is not None else None, len(inst), _p(inst),
                                    _p(sg) if sg is not None else None, _p(out), _p(P))
         return out, P
+
+    def sgwb_model(self, sgwb_type, params, resp, f):
+        """The reference's generate_sgwb_model on frequencies f: [len(f), 6]
+        covariance xx, yy, zz, xy, xz, yz (response from the table rows resp)."""
+        lib = self.lib
+        lib.ref_sgwb_model.argtypes = [ctypes.c_int, _D, ctypes.c_int, _D, ctypes.c_int, _D, _D]
+        p = np.zeros(4)
+        p[:len(params)] = params
+        r = np.ascontiguousarray(resp, np.float64).reshape(-1, 7)
+        f = np.ascontiguousarray(f, np.float64)
+        out = np.zeros((len(f), 6))
+        lib.ref_sgwb_model(int(sgwb_type), _p(p), len(r), _p(r), len(f), _p(f), _p(out))
+        return out
+
+    def noise_logl_sgwb(self, T, fmin, X, Y, Z, inst, sgal, sgwb_type, sgwb, resp):
+        """The reference's likelihood with the background added last."""
+        lib = self.lib
+        lib.ref_noise_logl_sgwb.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int, _D, _D, _D, ctypes.c_int,
+                                            _D, _D, ctypes.c_int, _D, ctypes.c_int, _D, _D]
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        b = np.ascontiguousarray(sgwb, np.float64).reshape(-1, 4)
+        r = np.ascontiguousarray(resp, np.float64).reshape(-1, 7)
+        out = np.zeros(len(inst))
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        lib.ref_noise_logl_sgwb(T, fmin, len(X) // 2, _p(X), _p(Y), _p(Z), len(inst), _p(inst),
+                                _p(sg) if sg is not None else None, int(sgwb_type), _p(b), len(r), _p(r), _p(out))
+        return out
+
+    def noise_wavelet_logl_sgwb(self, NF, NT, dt, df, lmin, Q, X, Y, Z, inst, sgal, mode, mod, sgwb_type, sgwb,
+                                resp):
+        """The reference's coarse wavelet likelihood with the background."""
+        lib = self.lib
+        lib.ref_noise_wavelet_logl_sgwb.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                    ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, _D, _D,
+                                                    ctypes.c_int, _D, ctypes.c_int, _D, _D, ctypes.c_int, _D,
+                                                    ctypes.c_int, _D, _D]
+        Nlayer = len(X) // NT
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        md = None if mod is None else np.ascontiguousarray(mod, np.float64)
+        b = np.ascontiguousarray(sgwb, np.float64).reshape(-1, 4)
+        r = np.ascontiguousarray(resp, np.float64).reshape(-1, 7)
+        out = np.zeros(len(inst))
+        X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
+        lib.ref_noise_wavelet_logl_sgwb(NF, NT, dt, df, lmin, Nlayer, Q, _p(X), _p(Y), _p(Z), mode,
+                                        _p(md) if md is not None else None, len(inst), _p(inst),
+                                        _p(sg) if sg is not None else None, int(sgwb_type), _p(b), len(r), _p(r),
+                                        _p(out))
+        return out
 
     def noise_eta(self, T, NFFT, qmin, dA, dE, invCA, invCE, params, eta, t0=0.0, fmt="sangria"):
         """noise_model_mcmc's likelihood change per chain: eta [n, 4] = xA, xE, yA, yE."""

@@ -730,6 +730,222 @@ void ref_noise_wavelet_logl(int NF, int NT, double dt, double df, int lmin, int 
     free(data);
 }
 
+/* ------------------------------------------------------------ SGWB */
+/* The reference reads the instrument's SGWB response from a table file
+ * (alloc_pop_sgwb_response, noise/src/glass_noise_model.c:134-189: the row
+ * count, then rows f, XX, YY, ZZ, XY, XZ, YZ).  The rows resp[7 i ..] are
+ * written to a temporary file in that format and read back by it, so the
+ * splines are the reference's own. */
+extern struct SGWBResponse *global_SGWBResponse;
+
+static struct SGWBResponse *ref_sgwb_response(int nresp, const double *resp)
+{
+    char name[] = "/tmp/glass_sgwb_respXXXXXX";
+    int fd = mkstemp(name);
+    if (fd < 0) return NULL;
+    FILE *fp = fdopen(fd, "w");
+    fprintf(fp, "%d\n", nresp);
+    for (int i = 0; i < nresp; i++) {
+        const double *r = resp + 7 * (size_t)i;
+        fprintf(fp, "%.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", r[0], r[1], r[2], r[3], r[4], r[5], r[6]);
+    }
+    fclose(fp);
+    struct SGWBResponse *R = calloc(1, sizeof(struct SGWBResponse));
+    alloc_pop_sgwb_response(R, name);
+    unlink(name);
+    /* generate_sgwb_model_wavelet's grid model shares the response */
+    global_SGWBResponse = R;
+    return R;
+}
+
+static void ref_sgwb_init(struct SGWBModel *m, int type, struct SGWBResponse *R, int N)
+{
+    memset(m, 0, sizeof(*m));
+    m->SGWB_type = (SGWB_t)type;
+    m->Nparams = SGWB_TEMPLATE_NPARAMS[type];
+    m->params = calloc(4, sizeof(double));
+    m->psd = malloc(sizeof(struct Noise));
+    alloc_noise(m->psd, N, 1, 3);
+    m->R = R;
+    m->grid_cache = NULL;
+}
+
+/* generate_sgwb_model (noise/src/glass_noise_model.c:778-842) on the
+ * frequencies f[N]: C6[6 n ..] = xx, yy, zz, xy, xz, yz. */
+void ref_sgwb_model(int type, const double *params, int nresp, const double *resp, int N, const double *f, double *C6)
+{
+    struct SGWBResponse *R = ref_sgwb_response(nresp, resp);
+    struct SGWBModel m;
+    ref_sgwb_init(&m, type, R, N);
+    for (int q = 0; q < m.Nparams; q++) m.params[q] = params[q];
+    for (int n = 0; n < N; n++) m.psd->f[n] = f[n];
+    generate_sgwb_model(&m);
+    for (int n = 0; n < N; n++) {
+        double *o = C6 + 6 * (size_t)n;
+        o[0] = m.psd->C[0][0][n]; o[1] = m.psd->C[1][1][n]; o[2] = m.psd->C[2][2][n];
+        o[3] = m.psd->C[0][1][n]; o[4] = m.psd->C[0][2][n]; o[5] = m.psd->C[1][2][n];
+    }
+    free_noise(m.psd);
+    free(m.params);
+}
+
+/* ref_noise_logl with the SGWB of template `type` (parameters sgwb[4 p ..],
+ * the template's first 2, 3 or 4) added last, in the order
+ * noise_instrument_model_mcmc combines the three
+ * (noise/src/glass_noise_sampler.c:559-570). */
+void ref_noise_logl_sgwb(double T, double fmin, int NFFT, const double *X, const double *Y, const double *Z, int n,
+                         const double *inst, const double *sgal, int type, const double *sgwb, int nresp,
+                         const double *resp, double *logl)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct SGWBResponse *R = ref_sgwb_response(nresp, resp);
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->NFFT = NFFT;
+    data->N = 2 * NFFT;
+    data->Nchannel = 3;
+    data->Nlayer = 1;
+    data->T = T;
+    data->fmin = fmin;
+    strcpy(data->basis, "fourier");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, 3);
+    memcpy(data->tdi->X, X, sizeof(double) * data->N);
+    memcpy(data->tdi->Y, Y, sizeof(double) * data->N);
+    memcpy(data->tdi->Z, Z, sizeof(double) * data->N);
+    struct InstrumentModel inst_model;
+    memset(&inst_model, 0, sizeof(inst_model));
+    alloc_instrument_model(&inst_model, NFFT, 1, 3);
+    struct ForegroundModel gal;
+    memset(&gal, 0, sizeof(gal));
+    alloc_foreground_model(&gal, NFFT, 1, 3);
+    struct SGWBModel sg;
+    ref_sgwb_init(&sg, type, R, NFFT);
+    for (int k = 0; k < NFFT; k++)
+        inst_model.psd->f[k] = gal.psd->f[k] = sg.psd->f[k] = data->fmin + (double)k / data->T;
+    struct Noise *psd = malloc(sizeof(struct Noise));
+    alloc_noise(psd, NFFT, 1, 3);
+    for (int p = 0; p < n; p++) {
+        for (int l = 0; l < 6; l++) {
+            inst_model.sacc[l] = inst[12 * p + l];
+            inst_model.soms[l] = inst[12 * p + 6 + l];
+        }
+        generate_instrument_noise_model(&orbit, &inst_model);
+        copy_Cij(inst_model.psd->C, psd->C, psd->Nchannel, psd->N);
+        if (sgal) {
+            for (int q = 0; q < 5; q++) gal.sgal[q] = sgal[5 * p + q];
+            generate_galactic_foreground_model(&gal);
+            generate_full_covariance_matrix(psd, gal.psd, 3);
+        }
+        for (int q = 0; q < sg.Nparams; q++) sg.params[q] = sgwb[4 * p + q];
+        generate_sgwb_model(&sg);
+        generate_full_covariance_matrix(psd, sg.psd, 3);
+        invert_noise_covariance_matrix(psd);
+        logl[p] = my_noise_log_likelihood(data, psd);
+    }
+    free_noise(psd);
+    free_noise(inst_model.psd);
+    free(inst_model.sacc);
+    free(inst_model.soms);
+    free_noise(gal.psd);
+    free(gal.sgal);
+    free_noise(sg.psd);
+    free(sg.params);
+    free_tdi(data->tdi);
+    free(data);
+}
+
+/* ref_noise_wavelet_logl with the SGWB of template `type` (sgwb[4 p ..]):
+ * generate_sgwb_model_wavelet (noise/src/glass_noise_model.c:843-892) on the
+ * layer centres, passed to the coarse covariance builders (:923, :983),
+ * which add it last. */
+void ref_noise_wavelet_logl_sgwb(int NF, int NT, double dt, double df, int lmin, int Nlayer, int Q, const double *X,
+                                 const double *Y, const double *Z, int mode, const double *mod, int n,
+                                 const double *inst, const double *sgal, int type, const double *sgwb, int nresp,
+                                 const double *resp, double *logl)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct SGWBResponse *R = ref_sgwb_response(nresp, resp);
+    struct Wavelets wdm;
+    memset(&wdm, 0, sizeof(wdm));
+    wdm.NF = NF;
+    wdm.NT = NT;
+    wdm.dt = dt;
+    wdm.df = df;
+    wdm.kmin = lmin * NT;
+    wdm.kmax = (lmin + Nlayer) * NT;
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->wdm = &wdm;
+    data->Nchannel = 3;
+    data->Nlayer = Nlayer;
+    data->lmin = lmin;
+    data->lmax = lmin + Nlayer;
+    data->N = Nlayer * NT;
+    data->NFFT = data->N / 2;
+    data->T = NT * dt;
+    strcpy(data->basis, "wavelet");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, 3);
+    memcpy(data->tdi->X, X, sizeof(double) * data->N);
+    memcpy(data->tdi->Y, Y, sizeof(double) * data->N);
+    memcpy(data->tdi->Z, Z, sizeof(double) * data->N);
+    struct CoarseStats stats;
+    alloc_coarse_stats(&stats, Nlayer, Q, NT);
+    coarse_grain_wavelet_data(data, &stats);
+    const int Ncoarse = NT / Q;
+    const size_t Npix = (size_t)Nlayer * Ncoarse;
+    struct InstrumentModel im;
+    memset(&im, 0, sizeof(im));
+    alloc_instrument_model(&im, Nlayer, Nlayer, 3);
+    struct ForegroundModel conf;
+    memset(&conf, 0, sizeof(conf));
+    alloc_foreground_model(&conf, Nlayer, Nlayer, 3);
+    struct SGWBModel sg;
+    ref_sgwb_init(&sg, type, R, Nlayer);
+    for (int k = 0; k < Nlayer; k++) im.psd->f[k] = conf.psd->f[k] = sg.psd->f[k] = (lmin + k) * df;
+    conf.Tobs = sg.Tobs = data->T;
+    struct GalaxyModulation gm;
+    memset(&gm, 0, sizeof(gm));
+    gm.Q_cached = Q;
+    gm.Nt_cached = Ncoarse;
+    gm.Nt_alloc = Ncoarse;
+    if (mod) {
+        gm.cache_XX = (double *)mod;
+        gm.cache_YY = (double *)mod + Ncoarse;
+        gm.cache_ZZ = (double *)mod + 2 * Ncoarse;
+        gm.cache_XY = (double *)mod + 3 * Ncoarse;
+        gm.cache_XZ = (double *)mod + 4 * Ncoarse;
+        gm.cache_YZ = (double *)mod + 5 * Ncoarse;
+    }
+    conf.modulation = &gm;
+    struct Noise *coarse = malloc(sizeof(struct Noise));
+    alloc_noise(coarse, (int)Npix, Nlayer, 3);
+    for (int p = 0; p < n; p++) {
+        for (int l = 0; l < 6; l++) {
+            im.sacc[l] = inst[12 * p + l];
+            im.soms[l] = inst[12 * p + 6 + l];
+        }
+        generate_instrument_noise_model_wavelet(&wdm, &orbit, &im);
+        if (mode) {
+            for (int q = 0; q < 5; q++) conf.sgal[q] = sgal[5 * p + q];
+            generate_galactic_foreground_model_wavelet(&wdm, &conf);
+        }
+        for (int q = 0; q < sg.Nparams; q++) sg.params[q] = sgwb[4 * p + q];
+        generate_sgwb_model_wavelet(&wdm, &sg);
+        if (mode == 2)
+            generate_full_dynamic_covariance_matrix_coarse(&wdm, Q, &im, &conf, &sg, coarse);
+        else
+            generate_full_stationary_covariance_matrix_coarse(&wdm, Q, &im, mode ? &conf : NULL, &sg, coarse);
+        invert_noise_covariance_matrix(coarse);
+        logl[p] = my_noise_log_likelihood_wavelet_coarse(data, coarse, &stats);
+    }
+    free_noise(coarse);
+    free_coarse_stats(&stats);
+    free_tdi(data->tdi);
+    free(data);
+}
+
 /* noise_model_mcmc's likelihood change (ucb/src/glass_ucb_sampler.c:29-73)
  * for n chains with one source each (params[8 c ..]) on one A/E segment:
  * generate_ucb_model, then for eta_x and eta_y (eta[4 c ..] = xA, xE, yA, yE)

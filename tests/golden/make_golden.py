@@ -452,6 +452,73 @@ def noise_wavelet(ref, rng):
     np.savez_compressed(os.path.join(HERE, "noise_wavelet.npz"), ncase=c, NF=NF, NT=NT, dt=dt, df=df, **out)
 
 
+def sgwb(ref, rng):
+    """The noise module's stochastic background (generate_sgwb_model, all three
+    templates) with the synthetic response table of
+    glass_gb300.workloads.sgwb_response_table (the reference reads its table
+    from a file in the same layout): the covariance on a frequency grid; the
+    XYZ likelihood with instrument + foreground + background for models around
+    the starting point on 1024-bin grids at 0.1 and 2 mHz; the coarse wavelet
+    likelihood (modes 0, 1, 2 with the background) at Q = 1 and 8."""
+    from oracle import Port
+
+    port = Port()
+    resp = wl.sgwb_response_table()
+    inst0, sgal0 = wl.default_noise_params(T)
+    out = {"resp": resp}
+    fgrid = np.exp(np.linspace(math.log(5e-5), math.log(0.05), 97))
+    for t in range(3):
+        params = wl.sgwb_params_draw(rng, t, 4)
+        if t == 1:
+            params[3, 2] = 0.98  # Delta = 10^0.98 >= 9: the asymptotic branch
+        if t == 2:
+            # b + 4 < m: the template's base goes negative at low frequency and
+            # the reference gives NaN there
+            params[0] = (1.2, 0.5, -18.0, -2.5)
+        out[f"t{t}_params"] = params
+        npar = len(wl.default_sgwb_params(t))
+        out[f"t{t}_C"] = np.array([ref.sgwb_model(t, params[k, :npar], resp, fgrid) for k in range(4)])
+    out["fgrid"] = fgrid
+    # Fourier likelihood
+    NF = 1024
+    for c, q in enumerate((int(2e-3 * T), int(8e-3 * T))):
+        fmin = q / T
+        X, Y, Z = wl.xyz_from_covariance(rng, port.noise_covariance(T, fmin, NF, inst0, sgal0))
+        out[f"c{c}_qmin"] = q
+        out[f"c{c}_X"], out[f"c{c}_Y"], out[f"c{c}_Z"] = X, Y, Z
+        inst = inst0 * np.exp(rng.uniform(-0.3, 0.3, (6, 12)))
+        sgal = sgal0 + rng.uniform(-0.2, 0.2, (6, 5))
+        out[f"c{c}_inst"], out[f"c{c}_sgal"] = inst, sgal
+        for t in range(3):
+            sg = wl.sgwb_params_draw(rng, t, 6)
+            out[f"c{c}_t{t}_sgwb"] = sg
+            out[f"c{c}_t{t}_logl"] = ref.noise_logl_sgwb(T, fmin, X, Y, Z, inst, sgal, t, sg, resp)
+            out[f"c{c}_t{t}_logl_inst"] = ref.noise_logl_sgwb(T, fmin, X, Y, Z, inst, None, t, sg, resp)
+    # wavelet likelihood
+    NFw, NT = 1024, 256
+    dt = 15.0 * NFw
+    df = 1.0 / (2 * dt)
+    Nl, lmin = 16, 60
+    C6 = np.array([port.noise_covariance(T, (lmin + j) * df, 1, inst0, sgal0)[0] for j in range(Nl)]) / (NFw * NT)
+    X, Y, Z = wl.wavelet_noise_data(rng, C6, NT)
+    out["w_X"], out["w_Y"], out["w_Z"] = X, Y, Z
+    inst = inst0 * np.exp(rng.uniform(-0.3, 0.3, (4, 12)))
+    sgal = sgal0 + rng.uniform(-0.2, 0.2, (4, 5))
+    out["w_inst"], out["w_sgal"] = inst, sgal
+    for Q in (1, 8):
+        mod = wl.galaxy_modulation_like(NT // Q, phase=0.2)
+        out[f"w_Q{Q}_mod"] = mod
+        for t in range(3):
+            sg = wl.sgwb_params_draw(rng, t, 4)
+            out[f"w_Q{Q}_t{t}_sgwb"] = sg
+            for mode in (0, 1, 2):
+                out[f"w_Q{Q}_t{t}_logl{mode}"] = ref.noise_wavelet_logl_sgwb(NFw, NT, dt, df, lmin, Q, X, Y, Z, inst,
+                                                                            sgal, mode, mod if mode == 2 else None,
+                                                                            t, sg, resp)
+    np.savez_compressed(os.path.join(HERE, "sgwb.npz"), NFFT=NF, NF=NFw, NT=NT, dt=dt, df=df, lmin=lmin, Nl=Nl,
+                        **out)
+
+
 def noise_eta(ref, rng):
     """noise_model_mcmc's likelihood change (ucb/src/glass_ucb_sampler.c:29-73)
     for chains with one source on a config-0-like segment: small eta jumps as
@@ -525,7 +592,7 @@ def fisher_draw(ref, rng):
 
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
              "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210,
-             "fisher_wavelet": 20261211, "priors": 20261212}
+             "fisher_wavelet": 20261211, "priors": 20261212, "sgwb": 20261213}
 
 
 def main(names=()):
@@ -551,6 +618,7 @@ def main(names=()):
     fisher_big(ref, np.random.default_rng(OWN_SEEDS["fisher_big"]))
     fisher_wavelet(ref, np.random.default_rng(OWN_SEEDS["fisher_wavelet"]))
     priors(ref, np.random.default_rng(OWN_SEEDS["priors"]))
+    sgwb(ref, np.random.default_rng(OWN_SEEDS["sgwb"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

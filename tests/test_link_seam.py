@@ -33,7 +33,8 @@ def test_reference_calls_bind_to_the_drop_ins():
                 "map_array_to_ucb_params", "ucb_alignment", "add_ucb_model", "remove_ucb_model", "generate_ucb_model",
                 "fourier_nwip", "snr", "gaussian_log_likelihood", "matrix_eigenstuff", "ucb_fisher",
                 "wavelet_transform_timefreq_by_layers", "wavelet_transform_timefreq", "build_wdm_filter_freq",
-                "wavelet_transform_freq", "ucb_waveform_wavelet"):
+                "wavelet_transform_freq", "wavelet_transform_inverse_freq", "ucb_waveform_wavelet", "wavelet_nwip",
+                "snr_wavelet", "delta_log_likelihood", "ucb_fisher_wavelet"):
         lines = [ln for ln in log.splitlines() if "libglassref.so" in ln.split(" to ")[0] and f"`{sym}'" in ln]
         assert lines, sym
         assert all("libglass_gb300.so" in ln.split(" to ")[1] for ln in lines), lines
