@@ -990,10 +990,12 @@ struct SpecArgs {
   double *term_ch = nullptr;
   const double *QA = nullptr;
   // mixed precision: a proposal whose error estimate
-  //   (fb_e1 sqrt(hw rr) + fb_e2 (hw + rr)) / scale_i
-  // (hw = |h|^2, rr = |r - h|^2, whitened sums over the template support)
-  // exceeds 1 is listed in fb_list (count in *fb_count) for the
-  // double-float re-evaluation; fb_total counts them.  No list: no estimate.
+  //   (fb_e1 sqrt(hw_full rr / N) + fb_e2 |(h|r - h)|) / scale_i
+  // (hw = |h|^2, rr = |r - h|^2, whitened sums over the template support;
+  // hw_full = hw scaled by the template's raw power over all its N bins
+  // against the power inside the segment) exceeds 1 is listed in fb_list
+  // (count in *fb_count) for the double-float re-evaluation; fb_total counts
+  // them.  No list: no estimate.
   int *fb_count = nullptr, *fb_list = nullptr;
   unsigned long long *fb_total = nullptr;
   float fb_e1 = 0.f, fb_e2 = 0.f;
@@ -1156,6 +1158,40 @@ __device__ __forceinline__ df group_sum_df(float v, float2 *red, int lane) {
   return s;
 }
 
+// Four float sums at once (FP32: the mixed path's error estimate).  red: 4
+// floats per warp of the group; result valid in lane 0.
+template <int GT>
+__device__ __forceinline__ float4 group_sum4(float4 v, float *red, int lane) {
+#pragma unroll
+  for (int off = (GT < 32 ? GT : 32) / 2; off > 0; off >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+    v.z += __shfl_xor_sync(0xffffffffu, v.z, off);
+    v.w += __shfl_xor_sync(0xffffffffu, v.w, off);
+  }
+  if constexpr (GT > 32) {
+    __syncthreads();
+    if ((lane & 31) == 0) {
+      float *o = red + 4 * (lane >> 5);
+      o[0] = v.x;
+      o[1] = v.y;
+      o[2] = v.z;
+      o[3] = v.w;
+    }
+    __syncthreads();
+    if (lane == 0) {
+      v = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int w = 0; w < GT / 32; w++) {
+        v.x += red[4 * w];
+        v.y += red[4 * w + 1];
+        v.z += red[4 * w + 2];
+        v.w += red[4 * w + 3];
+      }
+    }
+  }
+  return v;
+}
+
 // The same for a double-float value per thread.
 template <int GT>
 __device__ __forceinline__ df group_sum_df(df s, float2 *red, int lane) {
@@ -1234,9 +1270,17 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
     imin = a.items64[item].imin;
   }
   const C *src = series + (size_t)sl * 4 * N;
+  // the error estimate's sums: only with a re-evaluation list; the raw
+  // spectral power only for a template the segment edge clips
+  const bool est_on = MIX && a.fb_list != nullptr;
+  const bool clipped = imin < 0 || imin + N > NFFT;
   // mixed: per-thread compensated sums of |r - h|^2 (A in (rS, eS), E in
-  // (rE, eE): two independent chains) and a float sum of |h|^2
+  // (rE, eE): two independent chains) and a float sum of |h|^2; for the error
+  // estimate, Re and Im of (h|r - h) over the support (x, y) and the
+  // template's raw spectral power inside the segment (z) and over all its
+  // bins (w)
   float rS = 0.f, rE = 0.f, eS = 0.f, eE = 0.f, fh = 0.f;
+  float4 ev = make_float4(0.f, 0.f, 0.f, 0.f);
   double acc = 0.0, hacc = 0.0;
   double accE = 0.0;
 #pragma unroll 1
@@ -1256,15 +1300,22 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       const int k = lane + GT * r;
       const int m = (k + N / 2) & (N - 1);  // fftshift: output bin m holds FFT index m + N/2
       const int j = imin + m;
-      if (j < 0 || j >= NFFT) continue;
-      const size_t sj = (size_t)seg * NFFT + j;
       if constexpr (MIX) {
+        const int kp = pad16(k);
+        const float2 b0 = buf[0 * SN + kp], b1 = buf[1 * SN + kp], b2 = buf[2 * SN + kp], b3 = buf[3 * SN + kp];
+        const bool inside = j >= 0 && j < NFFT;
+        if (est_on && clipped) {
+          const float pw = fmaf(b0.x, b0.x, fmaf(b0.y, b0.y, fmaf(b1.x, b1.x, fmaf(b1.y, b1.y,
+                           fmaf(b2.x, b2.x, fmaf(b2.y, b2.y, fmaf(b3.x, b3.x, b3.y * b3.y)))))));
+          ev.w += pw;
+          if (inside) ev.z += pw;
+        }
+        if (!inside) continue;
+        const size_t sj = (size_t)seg * NFFT + j;
         const float4 w = a.w32[sj], wl = a.w32lo[sj];
         const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
         const float4 gAl = a.g32lo[2 * sj], gEl = a.g32lo[2 * sj + 1];
         const float p2 = a.itemsmix[item].amp_p2;
-        const int kp = pad16(k);
-        const float2 b0 = buf[0 * SN + kp], b1 = buf[1 * SN + kp], b2 = buf[2 * SN + kp], b3 = buf[3 * SN + kp];
         // the bin's table entries as hi + lo (the lo products first), then
         // the amplitude's power of two, which is exact: O(1) whitened values
         // (unscaled, their squares would overflow FP32)
@@ -1280,7 +1331,14 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
         acc_resid_sq(w.z, wl.z, hE.x, rE, eE);
         acc_resid_sq(w.w, wl.w, hE.y, rE, eE);
         fh += fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y);
+        if (est_on) {
+          const float dAx = w.x - hA.x, dAy = w.y - hA.y, dEx = w.z - hE.x, dEy = w.w - hE.y;
+          ev.x += fmaf(hA.x, dAx, fmaf(hA.y, dAy, fmaf(hE.x, dEx, hE.y * dEy)));
+          ev.y += fmaf(hA.x, dAy, fmaf(-hA.y, dAx, fmaf(hE.x, dEy, -hE.y * dEx)));
+        }
       } else {
+        if (j < 0 || j >= NFFT) continue;
+        const size_t sj = (size_t)seg * NFFT + j;
         const double s = a.items64[item].amp_s;
         // series (2 ch, 2 ch + 1) of this pass hold the A (chan 0) or E (chan 1) pair
 #pragma unroll
@@ -1310,6 +1368,7 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       sa = group_sum_df<GT>(df_add(quick_two_sum(rS, eS), quick_two_sum(rE, eE)), redf, lane);
     }
     sh = group_sum_df<GT>(fh, redf + 32, lane);
+    if (est_on) ev = group_sum4<GT>(ev, reinterpret_cast<float *>(red), lane);
   } else {
     acc = group_sum<GT>(acc, red, lane);
     hacc = group_sum<GT>(hacc, red + 32, lane);
@@ -1340,7 +1399,14 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       const float hw = sh.hi + sh.lo;
       hh = 2.0 * (double)hw;
       if (a.fb_list) {
-        const float est = fmaf(a.fb_e1, sqrtf(hw * rr), a.fb_e2 * (hw + rr)) *
+        // the FP32 template's rounding: spread evenly over its N bins (a
+        // random part ~ sqrt(hw_full rr / N), hw_full the power of the whole
+        // template when the segment edge clips it, from the raw spectra's
+        // power ratio) plus a systematic part along h (~ |(h|r - h)|, from
+        // the FP32 per-proposal constants)
+        const float hf = clipped && ev.z > 0.f ? hw * (ev.w / ev.z) : hw;
+        const float he = sqrtf(fmaf(ev.x, ev.x, ev.y * ev.y));
+        const float est = fmaf(a.fb_e1, sqrtf(hf * rr * (1.f / (float)N)), a.fb_e2 * he) *
                           fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
         if (!(est <= 1.f)) {  // also a non-finite estimate
           atomicAdd(a.fb_total, 1ull);

@@ -509,17 +509,20 @@ int glass_gpu_last_phase_ms(glass_gpu_ctx *ctx, float *ms);
 
 /*
  * Accuracy of GLASS_PREC_MIXED.  No counterpart in the reference, which is
- * FP64 throughout.  An FP32 FFT leaves a relative error of up to ~1e-7 on the
- * few bins that hold a narrowband template's power, so delta logL carries an
- * error up to ~1e-7 sqrt(H R), H = (h|h)/2 and R = |r - h|^2 the whitened
- * powers over the template support: below 1e-3 except for loud templates
- * (near the data of an SNR ~ 300 source, or far from the data with a power of
- * 1e6, as a jump of a weak source's amplitude by e^6 gives).  The spectral
- * kernel estimates each proposal's error from the sums it already has and,
- * for those above `tol`, evaluates the spectral stage again in double-float
- * arithmetic (in the same kernel, for sizes up to 1024); proposals still
- * above `tol` get FP64 series transformed the same way.  Results are written
- * over the mixed ones, in the same launch sequence (and CUDA graph).
+ * FP64 throughout.  The FP32 template's rounding error enters delta logL
+ * through the template's inner product with the residual r - h: a part
+ * spread over the template's N bins, up to ~6e-7 sqrt(H R / N), and a part
+ * along the template (the FP32 per-proposal constants), up to ~1.5e-7
+ * |(h|r - h)|/2, H = (h|h)/2 and R = |r - h|^2 the whitened powers over the
+ * template support (H of the whole template when the segment edge clips it).
+ * That is below 1e-3 except for loud templates (near the data of an SNR ~ 300
+ * source, or far from the data with a power of 1e6, as a jump of a weak
+ * source's amplitude by e^6 gives).  The spectral kernel estimates each
+ * proposal's error from sums it already has (with the constants 9e-7 and
+ * 2e-7) and lists those above `tol`; the listed proposals are evaluated again
+ * in double-float arithmetic (slow part, FFTs and sums; error ~1e-12) and the
+ * results written over the mixed ones, in the same launch sequence (and CUDA
+ * graph: a conditional node skips the re-evaluation when nothing is listed).
  * tol <= 0 turns the re-evaluation off (pure mixed precision); the default is
  * 1e-3.  Changing it drops the context's recorded host-path graphs.
  */
