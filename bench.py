@@ -1089,66 +1089,23 @@ def bench_config0(gg, rank, budget_s=3.0, cap=10000, cpu=True):
 
 
 def config4_workload(gg, rng, nb=8):
-    """The global-fit population and its proposals: 1e4 sources of a
-    synthetic Galactic population (f0 log-uniform over 0.1-10 mHz, fdot from
-    the GR chirp with chirp mass ~U[0.2, 0.8] Msun, amplitude from the chirp
-    mass, f0 and a distance ~U[1, 15] kpc, isotropic sky and orientation) in
-    512 segments of 8192 A/E bins (sizes 32..4096 from the bandwidth rule),
-    Gaussian noise; 64 chains x 16 temperatures own the sources (about 10
-    each).  nb batches of one RJMCMC move per source: an update (Gaussian jump
-    widened by sqrt(T)) or, for one source in five, a birth (a prior draw in
-    the segment, nothing there yet).  Returns (bank, engine with the bank
-    uploaded, seg_of, batches [nb, nsrc, 8], term_x [nb, nsrc])."""
-    nsrc, nseg, NFFT, nchain, ntemp = 10000, 512, 8192, 64, 16
-    MSUN_S, KPC_M = 4.925491025543576e-06, 3.0856775814913673e19
-    f = 10 ** rng.uniform(math.log10(1e-4), math.log10(1e-2), nsrc)
-    mc = rng.uniform(0.2, 0.8, nsrc) * MSUN_S
-    dist = rng.uniform(1.0, 15.0, nsrc) * KPC_M
-    amp = 2.0 * mc ** (5.0 / 3.0) * (math.pi * f) ** (2.0 / 3.0) * wl.CLIGHT / dist
-    fdot = 96.0 / 5.0 * math.pi ** (8.0 / 3.0) * mc ** (5.0 / 3.0) * f ** (11.0 / 3.0)
-    src = np.array([wl.make_params(f[i], rng.uniform(-1, 1), rng.uniform(0, 2 * math.pi), amp[i],
-                                   rng.uniform(-1, 1), rng.uniform(0, math.pi), rng.uniform(0, 2 * math.pi), fdot[i])
-                    for i in range(nsrc)])
-    # segments centred on log-spaced frequencies; each source in the nearest
-    centres = np.exp(np.linspace(math.log(1.3e-4), math.log(9.7e-3), nseg))
-    centres = np.maximum(centres, (NFFT // 2 + 16) / T)  # every segment starts above 0 Hz
-    seg_of = np.clip(np.searchsorted((centres[1:] + centres[:-1]) / 2, f), 0, nseg - 1).astype(np.int32)
+    """The global-fit population (workloads.global_fit_bank: 1e4 Galactic
+    sources in 512 segments of 8192 A/E bins) and nb batches of one RJMCMC
+    move per source (workloads.global_fit_proposals).  Returns (bank, engine
+    with the bank uploaded, seg_of, batches [nb, nsrc, 8], term_x [nb, nsrc])."""
 
     def wf(p):
-        N = 2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, p[0] / T, p[7] / T / T, p[1], math.exp(p[3]), T, NFFT)
+        N = 2 * gg.ucb_bandwidth(L_ARM, wl.FSTAR, p[0] / T, p[7] / T / T, p[1], math.exp(p[3]), T, 8192)
         N = min(N, 4096)
         h = gg.ucb_waveform(p, N, T)
         return N, h[3], h[4]
 
-    qmin, dA, dE, iA, iE = [], [], [], [], []
-    for s in range(nseg):
-        members = [src[i] for i in np.nonzero(seg_of == s)[0]]
-        q, a, e, ia, ie = wl.make_segment(rng, members, wf, NFFT=NFFT, T=T, center_f0=centres[s])
-        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie)
-    bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
-                          invCA=np.array(iA), invCE=np.array(iE))
+    bank, src, seg_of = wl.global_fit_bank(rng, wf)
     eng = gg.Engine(0)
     eng.upload(bank)
-    _, t_src, hh_src, st_src = eng.dlogl_host(seg_of, src, precision=gg.PREC_FP64)
-    snr = np.sqrt(np.maximum(hh_src, 1.0))
-    temps = 1.5 ** (np.arange(nsrc) % (nchain * ntemp) % ntemp)
-    batches, tx = np.empty((nb, nsrc, 8)), np.empty((nb, nsrc))
-    for b in range(nb):
-        birth = rng.uniform(size=nsrc) < 0.2
-        scales = np.array([wl.jump_scales(src[i], max(snr[i], 5.0)) for i in range(nsrc)])
-        jump = rng.standard_normal((nsrc, 8)) * scales * np.sqrt(temps)[:, None]
-        p = src + jump
-        for k in (1, 4):
-            bad = np.abs(p[:, k]) >= 1.0
-            p[bad, k] = src[bad, k]
-        # births: a prior draw inside the segment
-        qs = bank.qmin[seg_of] + rng.uniform(0.1, 0.9, nsrc) * NFFT
-        bp = np.array([wl.make_params(qs[i] / T, rng.uniform(-1, 1), rng.uniform(0, 2 * math.pi),
-                                      10 ** rng.uniform(-23, -21), rng.uniform(-1, 1), rng.uniform(0, math.pi),
-                                      rng.uniform(0, 2 * math.pi), 0.0) for i in range(nsrc)])
-        p[birth] = bp[birth]
-        batches[b] = p
-        tx[b] = np.where(birth, 0.0, t_src)
+    _, t_src, hh_src, _ = eng.dlogl_host(seg_of, src, precision=gg.PREC_FP64)
+    batches, birth = wl.global_fit_proposals(rng, bank, src, seg_of, np.sqrt(np.maximum(hh_src, 1.0)), nb)
+    tx = np.where(birth, 0.0, t_src[None, :])
     return bank, eng, seg_of, batches, tx
 
 

@@ -186,6 +186,64 @@ def tempered_proposals(rng, inj, snr, item_seg, temps, nbatch):
     return out
 
 
+def global_fit_bank(rng, waveform_fn, nsrc=10000, nseg=512, NFFT=8192, T=T_YEAR):
+    """A global-fit-scale population: nsrc sources of a synthetic Galactic
+    population (f0 log-uniform over 0.1-10 mHz, fdot from the GR chirp with
+    chirp mass ~U[0.2, 0.8] Msun, amplitude from the chirp mass, f0 and a
+    distance ~U[1, 15] kpc, isotropic sky and orientation) injected into nseg
+    segments of NFFT A/E bins centred on log-spaced frequencies (each source
+    in the nearest), with Gaussian noise.  Returns (bank, sources [nsrc, 8],
+    segment of each source)."""
+    MSUN_S, KPC_M = 4.925491025543576e-06, 3.0856775814913673e19
+    f = 10 ** rng.uniform(math.log10(1e-4), math.log10(1e-2), nsrc)
+    mc = rng.uniform(0.2, 0.8, nsrc) * MSUN_S
+    dist = rng.uniform(1.0, 15.0, nsrc) * KPC_M
+    amp = 2.0 * mc ** (5.0 / 3.0) * (math.pi * f) ** (2.0 / 3.0) * CLIGHT / dist
+    fdot = 96.0 / 5.0 * math.pi ** (8.0 / 3.0) * mc ** (5.0 / 3.0) * f ** (11.0 / 3.0)
+    src = np.array([make_params(f[i], rng.uniform(-1, 1), rng.uniform(0, 2 * math.pi), amp[i], rng.uniform(-1, 1),
+                                rng.uniform(0, math.pi), rng.uniform(0, 2 * math.pi), fdot[i], T)
+                    for i in range(nsrc)])
+    centres = np.exp(np.linspace(math.log(1.3e-4), math.log(9.7e-3), nseg))
+    centres = np.maximum(centres, (NFFT // 2 + 16) / T)  # every segment starts above 0 Hz
+    seg_of = np.clip(np.searchsorted((centres[1:] + centres[:-1]) / 2, f), 0, nseg - 1).astype(np.int32)
+    qmin, dA, dE, iA, iE = [], [], [], [], []
+    for s in range(nseg):
+        members = [src[i] for i in np.nonzero(seg_of == s)[0]]
+        q, a, e, ia, ie = make_segment(rng, members, waveform_fn, NFFT=NFFT, T=T, center_f0=centres[s])
+        qmin.append(q), dA.append(a), dE.append(e), iA.append(ia), iE.append(ie)
+    bank = SegmentBank(T=T, NFFT=NFFT, qmin=np.array(qmin, np.int32), dA=np.array(dA), dE=np.array(dE),
+                       invCA=np.array(iA), invCE=np.array(iE))
+    return bank, src, seg_of
+
+
+def global_fit_proposals(rng, bank, src, seg_of, snr, nb, nchain=64, ntemp=16, T=T_YEAR):
+    """nb batches of one RJMCMC move per source of global_fit_bank, the
+    sources owned by nchain x ntemp chains (temperature 1.5^(i mod ntemp)):
+    an update (Gaussian jump of about a Fisher sigma at the source's SNR,
+    widened by sqrt(T)) or, for one source in five, a birth (a prior draw in
+    the source's segment, nothing there yet).  Returns (batches [nb, nsrc, 8],
+    birth mask [nb, nsrc])."""
+    nsrc = len(src)
+    temps = 1.5 ** (np.arange(nsrc) % (nchain * ntemp) % ntemp)
+    batches, births = np.empty((nb, nsrc, 8)), np.empty((nb, nsrc), bool)
+    for b in range(nb):
+        birth = rng.uniform(size=nsrc) < 0.2
+        scales = np.array([jump_scales(src[i], max(snr[i], 5.0)) for i in range(nsrc)])
+        jump = rng.standard_normal((nsrc, 8)) * scales * np.sqrt(temps)[:, None]
+        p = src + jump
+        for k in (1, 4):
+            bad = np.abs(p[:, k]) >= 1.0
+            p[bad, k] = src[bad, k]
+        qs = bank.qmin[seg_of] + rng.uniform(0.1, 0.9, nsrc) * bank.NFFT
+        bp = np.array([make_params(qs[i] / T, rng.uniform(-1, 1), rng.uniform(0, 2 * math.pi),
+                                   10 ** rng.uniform(-23, -21), rng.uniform(-1, 1), rng.uniform(0, math.pi),
+                                   rng.uniform(0, 2 * math.pi), 0.0, T) for i in range(nsrc)])
+        p[birth] = bp[birth]
+        batches[b] = p
+        births[b] = birth
+    return batches, births
+
+
 def wavelet_invC(N, NT, kmin, scale=1.0):
     """Inverse noise covariance of a wavelet segment of N pixels starting at
     pixel kmin of a grid with NT pixels per layer: per pixel the inverse of
