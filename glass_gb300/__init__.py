@@ -14,7 +14,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libglass_gb300.so")
+# The engine library; GLASS_GB300_LIB selects another build of it (the test
+# suite's checked build, lib/libglass_gb300_checks.so).
+LIB_PATH = os.environ.get("GLASS_GB300_LIB") or os.path.join(HERE, "lib", "libglass_gb300.so")
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -60,6 +62,7 @@ EXPORTS = (
     "matrix_eigenstuff", "ucb_fisher", "wavelet_nwip", "snr_wavelet", "delta_log_likelihood", "ucb_fisher_wavelet",
     "glass_gpu_noise_sgwb_setup", "glass_gpu_noise_logl_batch_sgwb", "glass_gpu_noise_logl_batch_sgwb_host",
     "glass_gpu_noise_wavelet_logl_batch_sgwb", "glass_gpu_noise_wavelet_logl_batch_sgwb_host",
+    "glass_gpu_checked_build", "glass_gpu_check_status",
 )
 
 _lib = None
@@ -141,6 +144,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_noise_wavelet_logl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V]
     lib.glass_gpu_noise_wavelet_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D]
     lib.glass_gpu_noise_sgwb_setup.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D]
+    lib.glass_gpu_check_status.argtypes = [_V, ctypes.POINTER(ctypes.c_uint)]
     lib.glass_gpu_noise_logl_batch_sgwb.argtypes = [_V, ctypes.c_int, _V, _V, _V, _V]
     lib.glass_gpu_noise_logl_batch_sgwb_host.argtypes = [_V, ctypes.c_int, _D, _D, _D, _D]
     lib.glass_gpu_noise_wavelet_logl_batch_sgwb.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V]

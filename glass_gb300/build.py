@@ -21,6 +21,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libglass_gb300.so")
+OBJ_DIR_CHECKS = os.path.join(HERE, "_build_checks")
+LIB_CHECKS = os.path.join(OUT_DIR, "libglass_gb300_checks.so")
 # the benchmark's FMA-throughput probe: a separate library, not the engine
 PROBE_SRC = os.path.join(HERE, "probe", "fma_probe.cu")
 PROBE_LIB = os.path.join(OUT_DIR, "libglass_probe.so")
@@ -64,19 +66,27 @@ def _stale(lib: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-    deps = (_sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(ROOT, "include", "*.h"))
-            + [os.path.abspath(__file__)])
-    if not force and not _stale(LIB, deps):
-        build_probe()
-        return LIB
+def build(verbose: bool = False, force: bool = False, checks: bool = False) -> str:
+    """Compile the engine (lib/libglass_gb300.so); with checks=True the
+    checked build instead (lib/libglass_gb300_checks.so, -DGLASS_GPU_CHECKS:
+    the kernels check their indexed accesses, see glass_gpu_check_status)."""
+    lib = LIB_CHECKS if checks else LIB
+    obj_dir = OBJ_DIR_CHECKS if checks else OBJ_DIR
+    extra = ["-DGLASS_GPU_CHECKS"] if checks else []
+    deps = (_sources() + glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))
+            + glob.glob(os.path.join(ROOT, "include", "*.h")) + [os.path.abspath(__file__)])
+    if not force and not _stale(lib, deps):
+        if not checks:
+            build_probe()
+        return lib
     os.makedirs(OUT_DIR, exist_ok=True)
-    os.makedirs(OBJ_DIR, exist_ok=True)
+    os.makedirs(obj_dir, exist_ok=True)
     cc = nvcc()
 
     def compile_one(src):
-        obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
-        cmd = [cc] + ARCH + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj]
+        obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
+        cmd = ([cc] + ARCH + NVCC_FLAGS + extra + PER_FILE_FLAGS.get(os.path.basename(src), [])
+               + ["-c", src, "-o", obj])
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
@@ -86,14 +96,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=min(8, len(_sources()))) as ex:
         objs = list(ex.map(compile_one, _sources()))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [cc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    build_probe(force)
-    return LIB
+    os.replace(tmp, lib)
+    if not checks:
+        build_probe(force)
+    return lib
 
 
 def build_probe(force: bool = False) -> str:
@@ -108,4 +119,4 @@ def build_probe(force: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, checks="--checks" in sys.argv))

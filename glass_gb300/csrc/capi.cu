@@ -44,6 +44,23 @@ static int cuda_err(cudaError_t e, const char *where) {
 extern "C" const char *glass_gpu_last_error(void) { return g_err.c_str(); }
 
 namespace glass {
+// The checked build's per-translation-unit check words (glass_common.cuh).
+static std::vector<unsigned (*)()> &check_readers() {
+  static std::vector<unsigned (*)()> r;
+  return r;
+}
+static std::mutex g_check_mutex;
+void register_check_reader(unsigned (*read_reset)()) {
+  std::lock_guard<std::mutex> g(g_check_mutex);
+  check_readers().push_back(read_reset);
+}
+unsigned check_status_all() {
+  std::lock_guard<std::mutex> g(g_check_mutex);
+  unsigned w = 0;
+  for (auto f : check_readers()) w |= f();
+  return w;
+}
+
 // Error reporting for the entry points defined in other translation units.
 int report_error(int code, const char *msg) { return set_err(code, "%s", msg); }
 int report_cuda_error(cudaError_t e, const char *where) { return cuda_err(e, where); }
@@ -342,6 +359,19 @@ static int *tuning_slot(glass_gpu_ctx *ctx, const char *key, int *lo, int *hi) {
       return k.slot;
     }
   return nullptr;
+}
+
+// The checked build's failed-check sites since the last call (0 in a build
+// without checks, which returns 0 from glass_gpu_checked_build).
+extern "C" int glass_gpu_checked_build(void) { return kCheckedBuild ? 1 : 0; }
+
+extern "C" int glass_gpu_check_status(glass_gpu_ctx *ctx, unsigned int *word) {
+  if (!ctx || !word) return set_err(GLASS_ERR_ARG, "check_status: null argument");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "check_status sync");
+  *word = check_status_all();
+  return GLASS_OK;
 }
 
 extern "C" int glass_gpu_set_tuning(glass_gpu_ctx *ctx, const char *key, int value) {

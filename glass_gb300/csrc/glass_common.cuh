@@ -7,6 +7,46 @@
 
 namespace glass {
 
+// ------------------------------------------------------------ checked build
+// With -DGLASS_GPU_CHECKS (the checked library, libglass_gb300_checks.so,
+// which the test suite runs in place of compute-sanitizer) the kernels check
+// their indexed accesses against the extents of the buffers they index: a
+// failed check sets its site's bit in the translation unit's check word and
+// skips the access, so the kernel runs to its end and the host reads the
+// word (glass_gpu_check_status).  Without the flag every check is the
+// constant true and compiles away.
+enum : unsigned {
+  kChkBankRead = 1u << 0,     // a segment bin outside the bank
+  kChkSeriesRead = 1u << 1,   // a series element outside the scratch
+  kChkSeriesWrite = 1u << 2,  // the same, written
+  kChkItem = 1u << 3,         // a proposal index outside the batch
+  kChkBinList = 1u << 4,      // a size-list slot outside its capacity
+  kChkReevalList = 1u << 5,   // a re-evaluation list slot outside its capacity
+  kChkOutput = 1u << 6,       // an output element outside its array
+};
+// Every translation unit of the checked build registers a reader of its
+// check word (returns the word and clears it); check_status_all ORs them.
+void register_check_reader(unsigned (*read_reset)());
+unsigned check_status_all();
+#ifdef GLASS_GPU_CHECKS
+constexpr bool kCheckedBuild = true;
+static __device__ unsigned int g_check_word;
+__device__ __forceinline__ bool chk(bool ok, unsigned site) {
+  if (!ok) atomicOr(&g_check_word, site);
+  return ok;
+}
+static unsigned check_read_reset() {
+  unsigned v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_check_word, sizeof(v)) != cudaSuccess) v = ~0u;
+  (void)cudaMemcpyToSymbol(g_check_word, &z, sizeof(z));
+  return v;
+}
+[[maybe_unused]] static const bool g_check_registered = (register_check_reader(&check_read_reset), true);
+#else
+constexpr bool kCheckedBuild = false;
+__device__ __forceinline__ constexpr bool chk(bool, unsigned) { return true; }
+#endif
+
 // ------------------------------------------------------ per-device launch set-up
 // A kernel's dynamic shared-memory limit (cudaFuncSetAttribute) and the
 // occupancy derived from it belong to the current device, and the entry points

@@ -517,6 +517,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     sa.geo[b] = tab.geo[b];
   }
   sa.series = work.series;
+  sa.nitems = nitems;
+  sa.series_len = (long long)(work.series_bytes / (mix ? sizeof(float2) : sizeof(double2)));
   e = mix ? fd_launch_slow_mixed(sa, num_sms, stream, work.tune.slow_block, work.tune.slow_ctas_per_sm)
           : fd_launch_slow_fp64(sa, num_sms, stream);
   launches++;
@@ -530,6 +532,9 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.items64 = work.items64;
   a.itemsmix = work.itemsmix;
   a.series = work.series;
+  a.nitems = nitems;
+  a.nseg = bank.nseg;
+  a.series_len = sa.series_len;
   a.w32 = bank.w32;
   a.w32lo = bank.w32lo;
   a.g32 = bank.g32;
@@ -623,6 +628,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     while (nmax > bank.NFFT) nmax >>= 1;
     SlowArgs sh = sa;
     sh.series = work.series2;
+    sh.series_len = (long long)(work.series_bytes / sizeof(float4));
     for (int b = 0; b < kNumBins; b++) sh.geolo[b] = tab.geolo[b];
     sh.invLd = df_from_double(1.0 / kLARM);
     sh.AUcd = df_from_double(kAU / kCLIGHT);
@@ -631,6 +637,9 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     HpArgs h;
     h.NFFT = bank.NFFT;
     h.cap = work.cap;
+    h.nitems = nitems;
+    h.nseg = bank.nseg;
+    h.series_len = sh.series_len;
     h.nmax = nmax;
     h.bin_count = work.bin_count;
     h.bin_list = work.bin_list;

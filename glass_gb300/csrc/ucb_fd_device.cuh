@@ -845,7 +845,8 @@ __device__ __forceinline__ void plan_bin(const PlanArgs &a, int i, int b) {
     int base = 0;
     if (lane == first) base = atomicAdd(&a.bin_count[b], __popc(same));
     base = __shfl_sync(same, base, first);
-    a.bin_list[(size_t)b * a.cap + base + __popc(same & ((1u << lane) - 1))] = i;
+    const int slot = base + __popc(same & ((1u << lane) - 1));
+    if (chk(slot < a.cap && b < kNumBins, kChkBinList)) a.bin_list[(size_t)b * a.cap + slot] = i;
   }
 }
 
@@ -964,11 +965,17 @@ struct SlowArgs {
   // and 1/L, AU/c, 1/T, 1/c as hi + lo floats; series as float4
   const GeoSampleMix *geolo[kNumBins] = {};
   df invLd, AUcd, invTd, invcd;
+  // extents for the checked build: proposals, and series elements
+  int nitems = 0;
+  long long series_len = 0;
 };
 
 // Stage 2: FFTs, TDI weights, whitening and the residual power, per size.
 struct SpecArgs {
   int NFFT, cap, bin;
+  // extents for the checked build: proposals, segments, series elements
+  int nitems = 0, nseg = 0;
+  long long series_len = 0;
   const int *bin_count;
   const int *bin_list;  // this size's list
   const ItemF64 *items64;
@@ -1014,6 +1021,9 @@ __device__ __forceinline__ float fb_scale_of(const float *inv_scale, int n, int 
 // in double-float.
 struct HpArgs {
   int NFFT, cap;
+  // extents for the checked build: proposals, segments, series elements
+  int nitems = 0, nseg = 0;
+  long long series_len = 0;
   int nmax;  // largest template size the bank allows (shared memory is sized for it)
   const int *bin_count = nullptr, *bin_list = nullptr;
   const ItemMix *itemsmix = nullptr;
@@ -1082,7 +1092,9 @@ __global__ void __launch_bounds__(BLOCK) fd_slow_kernel(SlowArgs a) {
     const int local = ch - cb;
     const int slot = local >> b;
     const int n = ((local & ((1 << b) - 1)) << 5) + lane;
+    if (!chk(slot < a.cap, kChkBinList)) continue;
     const int item = a.bin_list[(size_t)b * a.cap + slot];
+    if (!chk(item >= 0 && item < a.nitems, kChkItem)) continue;
     C d[6], cmb[4];
     if constexpr (MIX) {
       slow_sample_mix(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.invLf, a.AUcf, a.invTf, d);
@@ -1090,7 +1102,9 @@ __global__ void __launch_bounds__(BLOCK) fd_slow_kernel(SlowArgs a) {
       slow_sample64(a.items64[item], a.pos64[b][n], a.fstar, a.L, d);
     }
     ae_combos(d, cmb);
-    C *out = series + ((long long)cb * 32 + (long long)slot * N) * 4 + n;
+    const long long o0 = ((long long)cb * 32 + (long long)slot * N) * 4 + n;
+    if (!chk(o0 >= 0 && o0 + 3LL * N < a.series_len, kChkSeriesWrite)) continue;
+    C *out = series + o0;
 #pragma unroll
     for (int s = 0; s < 4; s++) out[(size_t)s * N] = cmb[s];
   }
@@ -1260,16 +1274,29 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   const int slot = base + g;
   const bool valid = slot < count;
   const int sl = valid ? slot : count - 1;
-  const int item = bin_list[sl];
-  int seg, imin;
+  // checked build: an index outside its buffer is recorded, the group reads
+  // from the buffers' starts instead (it still runs its FFT and barriers) and
+  // the proposal's results are not written
+  const bool lok = chk(sl >= 0 && sl < a.cap, kChkBinList);
+  const int item = lok ? bin_list[sl] : 0;
+  const bool iok = chk(item >= 0 && item < a.nitems, kChkItem);
+  int seg = 0, imin = 0;
   if constexpr (MIX) {
-    seg = a.itemsmix[item].seg;
-    imin = a.itemsmix[item].imin;
+    if (iok) {
+      seg = a.itemsmix[item].seg;
+      imin = a.itemsmix[item].imin;
+    }
   } else {
-    seg = a.items64[item].seg;
-    imin = a.items64[item].imin;
+    if (iok) {
+      seg = a.items64[item].seg;
+      imin = a.items64[item].imin;
+    }
   }
-  const C *src = series + (size_t)sl * 4 * N;
+  const bool sok = chk(seg >= 0 && seg < a.nseg, kChkBankRead);
+  const bool rok = chk((long long)(sl + 1) * 4 * N <= a.series_len, kChkSeriesRead);
+  const bool inb = lok && iok && sok && rok;
+  if (!inb) seg = 0;
+  const C *src = series + (inb ? (size_t)sl * 4 * N : 0);
   // the error estimate's sums: only with a re-evaluation list; the raw
   // spectral power only for a template the segment edge clips
   const bool est_on = MIX && a.fb_list != nullptr;
@@ -1374,7 +1401,7 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
     hacc = group_sum<GT>(hacc, red + 32, lane);
     if constexpr (PERCH) accE = group_sum<GT>(accE, red + 64, lane);
   }
-  if (valid && lane == 0) {
+  if (valid && inb && lane == 0) {
     double term, hh;
     if constexpr (MIX) {
       // FP64 only for the final sum (GB300's FP64 pipe is slow, and this runs
@@ -1410,7 +1437,8 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
                           fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
         if (!(est <= 1.f)) {  // also a non-finite estimate
           atomicAdd(a.fb_total, 1ull);
-          a.fb_list[atomicAdd(a.fb_count, 1)] = item;
+          const int k = atomicAdd(a.fb_count, 1);
+          if (chk(k < a.nitems, kChkReevalList)) a.fb_list[k] = item;
         }
       }
     } else {

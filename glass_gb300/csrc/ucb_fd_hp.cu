@@ -42,9 +42,9 @@ __global__ void __launch_bounds__(64) fd_hp_bin_kernel(PlanArgs a, const int *li
   for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const int k = base + threadIdx.x;
     int b = -1, i = 0;
-    if (k < n) {
+    if (k < n && chk(k < a.nitems, kChkReevalList)) {
       i = list[k];
-      b = fd_bin_of(a.itemsmix[i].N);
+      if (chk(i >= 0 && i < a.nitems, kChkItem)) b = fd_bin_of(a.itemsmix[i].N);
     }
     plan_bin(a, i, b);
   }
@@ -142,13 +142,21 @@ __global__ void __launch_bounds__(96) fd_slow_hp_kernel(SlowArgs a) {
     const int local = ch - cb;
     const int slot = local >> b;
     const int n = ((local & ((1 << b) - 1)) << 5) + lane;
-    const int item = a.bin_list[(size_t)b * a.cap + slot];
+    // checked build: an index outside its buffer is recorded and the chunk
+    // computed from proposal 0 without being written (the CTA keeps its
+    // barriers)
+    const bool lok = chk(slot < a.cap, kChkReevalList);
+    int item = lok ? a.bin_list[(size_t)b * a.cap + slot] : 0;
+    const bool iok = chk(item >= 0 && item < a.nitems, kChkItem);
+    if (!iok) item = 0;
+    const long long o0 = ((long long)cb * 32 + (long long)slot * N) * 4 + n;
+    const bool wok = lok && iok && chk(o0 >= 0 && o0 + 3LL * N < a.series_len, kChkSeriesWrite);
     dc d2[2];
     slow_arms_hp(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.geolo[b][n], a, s_tab, sc, d2);
     s_d[2 * sc][lane] = d2[0];
     s_d[2 * sc + 1][lane] = d2[1];
     __syncthreads();
-    if (sc < 2) {
+    if (sc < 2 && wok) {
       dc d[6];
 #pragma unroll
       for (int q = 0; q < 6; q++) d[q] = s_d[q][lane];
@@ -177,6 +185,7 @@ struct HpEntry {
   int item, N, seg, imin, bin;
   long long off;
   float amp_p2;
+  bool ok;  // checked build: every index in bounds (else read safely, not written)
 };
 
 __device__ __forceinline__ HpEntry hp_entry(const HpArgs &a, int k, const int *cs) {
@@ -186,14 +195,24 @@ __device__ __forceinline__ HpEntry hp_entry(const HpArgs &a, int k, const int *c
     if (k >= cs[b]) bin = b;
   const int slot = k - cs[bin];
   HpEntry e;
-  e.item = a.bin_list[(size_t)bin * a.cap + slot];
-  const ItemMix &c = a.itemsmix[e.item];
+  e.ok = chk(slot < a.cap, kChkReevalList);
+  e.item = e.ok ? a.bin_list[(size_t)bin * a.cap + slot] : 0;
+  e.ok = e.ok && chk(e.item >= 0 && e.item < a.nitems, kChkItem);
+  const ItemMix &c = a.itemsmix[e.ok ? e.item : 0];
   e.N = c.N;
   e.seg = c.seg;
   e.imin = c.imin;
   e.bin = bin;
   e.off = (bin_sample_start(a.bin_count, a.NFFT, bin) + (long long)slot * c.N) * 4;
   e.amp_p2 = c.amp_p2;
+  e.ok = e.ok && chk(e.seg >= 0 && e.seg < a.nseg, kChkBankRead) &&
+         chk(e.N >= 32 && e.N <= a.nmax && e.off >= 0 && e.off + 4LL * e.N <= a.series_len, kChkSeriesRead);
+  if (!e.ok) {
+    e.N = 32;
+    e.bin = 0;
+    e.seg = 0;
+    e.off = 0;
+  }
   return e;
 }
 
@@ -253,7 +272,7 @@ __global__ void __launch_bounds__(kHpThreads) fd_hp_kernel(HpArgs a) {
     hw = hp_block_sum(hw, red);
     if (threadIdx.x == 0) s_part = make_float4(rr.hi, rr.lo, hw.hi, hw.lo);
     cluster.sync();  // partial sums are published; the partner is done with S
-    if (r == 0 && threadIdx.x == 0) {
+    if (r == 0 && threadIdx.x == 0 && e.ok) {
       df s[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
       for (int q = 0; q < 4; q++) {
         const float4 o = *cluster.map_shared_rank(&s_part, (unsigned)q);

@@ -218,6 +218,8 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
     sa.mix[b] = tab.mix[b];
   }
   sa.series = na->series;
+  sa.nitems = nitems;
+  sa.series_len = 4 * kNaMaxSamples;
   if ((e = fd_launch_slow_fp64(sa, na->num_sms, s)) != cudaSuccess)
     return report_cuda_error(e, "dlogl_fp64_noalloc: slow part");
 
@@ -228,6 +230,9 @@ extern "C" int glass_gpu_dlogl_fp64_noalloc(void *stream, int format, double T, 
   a.items64 = na->items;
   a.itemsmix = nullptr;
   a.series = na->series;
+  a.nitems = nitems;
+  a.nseg = nseg;
+  a.series_len = 4 * kNaMaxSamples;
   a.w32 = nullptr;
   a.w32lo = nullptr;
   a.g32 = nullptr;

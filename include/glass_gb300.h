@@ -152,6 +152,21 @@ int glass_gpu_set_stream(glass_gpu_ctx *ctx, void *stream);
 const char *glass_gpu_last_error(void);
 
 /*
+ * The checked build (libglass_gb300_checks.so: python -m glass_gb300.build
+ * --checks; the stand-in for compute-sanitizer) checks the kernels' indexed
+ * accesses (bank bins, series scratch, proposal indices, size lists, the
+ * re-evaluation list, outputs) against the buffers' extents; a failed check
+ * records its site and skips the access.  glass_gpu_checked_build() is 1 in
+ * that library and 0 in the product one; glass_gpu_check_status synchronises
+ * the context's stream and returns in *word the sites that failed since the
+ * last call (bits: 1 bank read, 2 series read, 4 series write, 8 proposal
+ * index, 16 size list, 32 re-evaluation list, 64 output; 0 in the product
+ * library).
+ */
+int glass_gpu_checked_build(void);
+int glass_gpu_check_status(glass_gpu_ctx *ctx, unsigned int *word);
+
+/*
  * Upload a bank of `nseg` A/E frequency segments of NFFT bins each -- the
  * inputs the reference's gaussian_log_likelihood reads
  * (utils/src/glass_model.c:726-774, Nchannel == 2): for segment s,
