@@ -176,6 +176,10 @@ extern "C" int glass_gpu_create(int device, glass_gpu_ctx **out) {
     return cuda_err(e, "cudaSetDevice");
   }
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if ((e = fd_hp_tables_init()) != cudaSuccess) {
+    delete ctx;
+    return cuda_err(e, "re-evaluation tables");
+  }
   {
     int pageable = 0, host_tables = 0;
     cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
@@ -218,7 +222,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->work.bin_list);
   cudaFree(ctx->work.series);
   cudaFree(ctx->work.series2);
-  cudaFree(ctx->work.fb_list);
+  cudaFree(ctx->work.hp_list);
   cudaFree(ctx->work.fb_total);
   cudaFree(ctx->work.fb_inv_scale);
   cudaFree(ctx->d_stage);
@@ -567,8 +571,9 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   cudaFree(w.bin_list);
   cudaFree(w.series);
   cudaFree(w.series2);
-  cudaFree(w.fb_list);
-  w.fb_list = nullptr;
+  cudaFree(w.hp_list);
+  w.hp_list = nullptr;
+  w.hp_count = nullptr;
   w.fb_count = nullptr;
   w.items64 = nullptr;
   w.itemsmix = nullptr;
@@ -586,10 +591,11 @@ static int ensure_work(glass_gpu_ctx *ctx, int nitems) {
   GLASS_CUDA(cudaMalloc(&w.items64, sizeof(ItemF64) * (size_t)cap), "cudaMalloc(items64)");
   GLASS_CUDA(cudaMalloc(&w.itemsmix, sizeof(ItemMix) * (size_t)cap), "cudaMalloc(itemsmix)");
   GLASS_CUDA(cudaMalloc(&w.itemsgrad, sizeof(ItemGrad) * (size_t)cap), "cudaMalloc(itemsgrad)");
-  GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * (kNumBins + 6)), "cudaMalloc(bin_count)");
-  GLASS_CUDA(cudaMemset(w.bin_count, 0, sizeof(int) * (kNumBins + 6)), "cudaMemset(bin_count)");
+  GLASS_CUDA(cudaMalloc(&w.bin_count, sizeof(int) * kFdCounts), "cudaMalloc(bin_count)");
+  GLASS_CUDA(cudaMemset(w.bin_count, 0, sizeof(int) * kFdCounts), "cudaMemset(bin_count)");
   w.fb_count = w.bin_count + kNumBins;
-  GLASS_CUDA(cudaMalloc(&w.fb_list, sizeof(int) * (size_t)cap), "cudaMalloc(fb_list)");
+  w.hp_count = w.bin_count + kNumBins + 6;
+  GLASS_CUDA(cudaMalloc(&w.hp_list, sizeof(int) * (size_t)kNumBins * cap), "cudaMalloc(hp_list)");
   if (!w.fb_total) {
     GLASS_CUDA(cudaMalloc(&w.fb_total, sizeof(unsigned long long)), "cudaMalloc(fb_total)");
     GLASS_CUDA(cudaMemset(w.fb_total, 0, sizeof(unsigned long long)), "cudaMemset(fb_total)");

@@ -455,7 +455,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   int launches = 0;
   const bool mix = precision == 1;
   if (!work.counts_zero) {
-    e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * (kNumBins + 6), stream);
+    e = cudaMemsetAsync(work.bin_count, 0, sizeof(int) * kFdCounts, stream);
     if (e != cudaSuccess) return e;
   }
   const bool fallback = mix && (work.fb_e1 > 0.f || work.fb_e2 > 0.f) && work.series2 != nullptr;
@@ -551,7 +551,8 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
   a.QA = bank.QA;
   if (fallback) {
     a.fb_count = work.fb_count;
-    a.fb_list = work.fb_list;
+    a.hp_count = work.hp_count;
+    a.hp_list = work.hp_list;
     a.fb_total = work.fb_total;
     a.fb_e1 = work.fb_e1;
     a.fb_e2 = work.fb_e2;
@@ -622,11 +623,13 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
 
   // Re-evaluation of the listed mixed proposals in double-float: series
   // (into series2), spectral stage, results written over the mixed ones; the
-  // size counts and fb_count end at zero.
+  // re-evaluation's counts and fb_count end at zero.
   if (fallback) {
     int nmax = kMaxN;
     while (nmax > bank.NFFT) nmax >>= 1;
     SlowArgs sh = sa;
+    sh.bin_count = work.hp_count;
+    sh.bin_list = work.hp_list;
     sh.series = work.series2;
     sh.series_len = (long long)(work.series_bytes / sizeof(float4));
     for (int b = 0; b < kNumBins; b++) sh.geolo[b] = tab.geolo[b];
@@ -641,12 +644,12 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
     h.nseg = bank.nseg;
     h.series_len = sh.series_len;
     h.nmax = nmax;
-    h.bin_count = work.bin_count;
-    h.bin_list = work.bin_list;
+    h.bin_count = work.hp_count;
+    h.bin_list = work.hp_list;
     h.itemsmix = work.itemsmix;
     h.series = reinterpret_cast<const float4 *>(work.series2);
-    h.zero_at = work.bin_count;  // the size counts and fb_count
-    h.nzero = kNumBins + 1;
+    h.zero_at = work.fb_count;  // fb_count, the done counters, the spares and hp_count
+    h.nzero = kFdCounts - kNumBins;
     h.done = work.bin_count + kNumBins + 2;
     h.w32 = bank.w32;
     h.w32lo = bank.w32lo;
@@ -682,8 +685,7 @@ cudaError_t fd_dlogl_launch(const FdBankDev &bank, const FdTablesDev &tab, FdWor
                                              cudaStreamCaptureModeRelaxed)) != cudaSuccess)
         return e;
     }
-    PlanArgs pb = pa;
-    e = fd_launch_reeval(pb, work.fb_list, work.fb_count, sh, h, perch, num_sms, ts, &launches);
+    e = fd_launch_reeval(sh, h, perch, num_sms, ts, &launches);
     if (e != cudaSuccess) return e;
     if (cond) {
       cudaGraph_t body = nullptr;

@@ -37,6 +37,9 @@ struct FdTablesDev {
 };
 
 // Scratch of one batched evaluation.
+// ints in FdWorkDev::bin_count (see there)
+constexpr int kFdCounts = 2 * kNumBins + 6;
+
 struct FdWorkDev {
   // per-size streams forked from the caller's stream after the slow-part
   // kernel, so that the per-size spectral kernels run concurrently (and become
@@ -48,19 +51,20 @@ struct FdWorkDev {
   ItemF64 *items64 = nullptr;   // [cap]
   ItemMix *itemsmix = nullptr;  // [cap]
   ItemGrad *itemsgrad = nullptr;  // [cap]
-  // [kNumBins + 6]: per-size counts, fb_count, the CTA-done counters of the
-  // persistent spectral kernel and of the re-evaluation kernel, and three
-  // spare ints
+  // [kFdCounts]: per-size counts, fb_count, the CTA-done counters of the
+  // persistent spectral kernel and of the re-evaluation kernel, three spare
+  // ints, and the re-evaluation's per-size counts (hp_count)
   int *bin_count = nullptr;
   int *bin_list = nullptr;      // [kNumBins*cap]
   // Mixed precision: proposals whose error estimate exceeds the tolerance are
-  // listed in fb_list and evaluated again in double-float (series in
-  // series2), in the same launch sequence (fb_e1 = fb_e2 = 0: no
-  // re-evaluation)
+  // listed by size in hp_list (counts in hp_count, their total in fb_count)
+  // and evaluated again in double-float (series in series2), in the same
+  // launch sequence (fb_e1 = fb_e2 = 0: no re-evaluation)
   float fb_e1 = 0.f, fb_e2 = 0.f;
-  int *fb_list = nullptr;                  // [cap]
+  int *hp_list = nullptr;                  // [kNumBins*cap]
+  int *hp_count = nullptr;                 // bin_count + kNumBins + 6
   int *fb_count = nullptr;                 // bin_count + kNumBins
-  void *series2 = nullptr;                 // [series_bytes]: double-float series of fb_list
+  void *series2 = nullptr;                 // [series_bytes]: double-float series of the listed proposals
   unsigned long long *fb_total = nullptr;  // proposals re-evaluated
   float *fb_inv_scale = nullptr;           // [fb_nscale]: 1 / per-proposal tolerance scale (null: 1)
   int fb_nscale = 0, fb_nscale_cap = 0;

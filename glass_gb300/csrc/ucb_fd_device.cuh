@@ -1000,10 +1000,11 @@ struct SpecArgs {
   //   (fb_e1 sqrt(hw_full rr / N) + fb_e2 |(h|r - h)|) / scale_i
   // (hw = |h|^2, rr = |r - h|^2, whitened sums over the template support;
   // hw_full = hw scaled by the template's raw power over all its N bins
-  // against the power inside the segment) exceeds 1 is listed in fb_list
-  // (count in *fb_count) for the double-float re-evaluation; fb_total counts
-  // them.  No list: no estimate.
-  int *fb_count = nullptr, *fb_list = nullptr;
+  // against the power inside the segment) exceeds 1 is listed for the
+  // double-float re-evaluation in its size's list, hp_list[bin cap ..]
+  // (count hp_count[bin]), the total in *fb_count; fb_total counts them over
+  // the context's life.  No list: no estimate.
+  int *fb_count = nullptr, *hp_count = nullptr, *hp_list = nullptr;
   unsigned long long *fb_total = nullptr;
   float fb_e1 = 0.f, fb_e2 = 0.f;
   // per-proposal tolerance scale: 1/scale_i for i < fb_nscale (null: 1)
@@ -1042,11 +1043,13 @@ struct HpArgs {
   double *dlogl, *term_y, *hh, *term_ch;
   int *status;
 };
-// Bins the listed proposals, computes their series in double-float and
-// evaluates their spectral stage in double-float, writing over the mixed
-// results; the counts end at zero.
-cudaError_t fd_launch_reeval(const PlanArgs &pa, const int *list, const int *count, const SlowArgs &sa,
-                             const HpArgs &h, bool perch, int num_sms, cudaStream_t stream, int *nlaunch);
+// Computes the listed proposals' series in double-float and evaluates their
+// spectral stage in double-float, writing over the mixed results; the
+// re-evaluation's counts end at zero.
+cudaError_t fd_launch_reeval(const SlowArgs &sa, const HpArgs &h, bool perch, int num_sms, cudaStream_t stream,
+                             int *nlaunch);
+// The re-evaluation's constant tables on the current device (once per device).
+cudaError_t fd_hp_tables_init();
 
 // Start (in samples) of size bin `bin` in the scratch series: sizes are laid
 // out in increasing order, proposals of one size back to back, each holding 4
@@ -1299,7 +1302,7 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
   const C *src = series + (inb ? (size_t)sl * 4 * N : 0);
   // the error estimate's sums: only with a re-evaluation list; the raw
   // spectral power only for a template the segment edge clips
-  const bool est_on = MIX && a.fb_list != nullptr;
+  const bool est_on = MIX && a.hp_list != nullptr;
   const bool clipped = imin < 0 || imin + N > NFFT;
   // mixed: per-thread compensated sums of |r - h|^2 (A in (rS, eS), E in
   // (rE, eE): two independent chains) and a float sum of |h|^2; for the error
@@ -1425,7 +1428,7 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
       }
       const float hw = sh.hi + sh.lo;
       hh = 2.0 * (double)hw;
-      if (a.fb_list) {
+      if (a.hp_list) {
         // the FP32 template's rounding: spread evenly over its N bins (a
         // random part ~ sqrt(hw_full rr / N), hw_full the power of the whole
         // template when the segment edge clips it, from the raw spectra's
@@ -1437,8 +1440,10 @@ __device__ __forceinline__ void spec_unit(const SpecArgs &a, const int *bin_list
                           fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
         if (!(est <= 1.f)) {  // also a non-finite estimate
           atomicAdd(a.fb_total, 1ull);
-          const int k = atomicAdd(a.fb_count, 1);
-          if (chk(k < a.nitems, kChkReevalList)) a.fb_list[k] = item;
+          atomicAdd(a.fb_count, 1);
+          constexpr int bin = fd_bin_of(N);
+          const int k = atomicAdd(&a.hp_count[bin], 1);
+          if (chk(k < a.cap, kChkReevalList)) a.hp_list[(size_t)bin * a.cap + k] = item;
         }
       }
     } else {

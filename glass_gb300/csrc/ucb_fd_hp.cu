@@ -1,15 +1,14 @@
 // Double-float re-evaluation of mixed-precision proposals.
 //
-// The mixed path's template is an FP32 FFT of FP32 series; both leave
-// relative errors of order 1e-7 on the few bins that hold a narrowband
-// template's power, so its delta logL carries an error of up to ~1e-7 x
-// sqrt((h|h)/2 |r - h|^2) (whitened sums over the template support): below
-// 1e-3 except for loud templates, near the data of a source with SNR ~ 300 or
-// far from the data with (h|h) ~ 1e6.  The mixed spectral kernels list those
-// proposals, and they are evaluated again with every step in double-float
-// arithmetic (pairs of floats, ~48 bits, on the FP32 pipe, which on GB300
-// runs 64 times the FP64 rate), in three launches:
-//   fd_hp_bin_kernel:  the listed proposals binned by size;
+// The mixed path's template is an FP32 FFT of FP32 series from FP32
+// per-proposal constants; its delta logL carries an error of up to
+// ~6e-7 sqrt(hw rr / N) + 1.5e-7 |(h|r - h)| (whitened sums over the template
+// support): below 1e-3 except for loud templates, near the data of a source
+// with SNR ~ 300 or far from the data with (h|h) ~ 1e6.  The mixed spectral
+// kernels estimate it and list those
+// proposals by size, and they are evaluated again with every step in
+// double-float arithmetic (pairs of floats, ~48 bits, on the FP32 pipe, which
+// on GB300 runs 64 times the FP64 rate), in two launches:
 //   fd_slow_hp_kernel: their four A/E arm-combination series in
 //     double-float, three warps per 32 samples: the mixed slow part's formulation
 //     (carrier phase heterodyned to the segment and reduced mod 2 pi, so that
@@ -25,6 +24,8 @@
 //     and sum the residual power and the template power; CTA 0 gathers the
 //     four partial sums and writes the results over the mixed ones.
 // What is left is of order 1e-12 of the same scale.
+#include <math.h>
+
 #include <cooperative_groups.h>
 
 #include "ucb_fd_device.cuh"
@@ -32,23 +33,6 @@
 namespace glass {
 
 constexpr int kHpThreads = 256;
-
-// ------------------------------------------------------------------ binning
-// The listed proposals (list[0 .. *count)) binned by their mixed plan's size.
-// Grid-stride with warp-uniform trips, as plan_bin needs whole warps.
-__global__ void __launch_bounds__(64) fd_hp_bin_kernel(PlanArgs a, const int *list, const int *count) {
-  const int n = *count;
-  const int stride = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
-    const int k = base + threadIdx.x;
-    int b = -1, i = 0;
-    if (k < n && chk(k < a.nitems, kChkReevalList)) {
-      i = list[k];
-      if (chk(i >= 0 && i < a.nitems, kChkItem)) b = fd_bin_of(a.itemsmix[i].N);
-    }
-    plan_bin(a, i, b);
-  }
-}
 
 // -------------------------------------------------------- slow part, df
 // The two arms of spacecraft i (12, 13 | 21, 23 | 31, 32) at one sample, as
@@ -109,15 +93,14 @@ __device__ __forceinline__ void slow_arms_hp(const ItemMix &c, const OrbitSample
 // third of the dependent chain of a sample each, on separate SM
 // sub-partitions); warps 0 and 1 then form the A and E arm combinations of
 // ae_combos in double-float.
+// sin(k pi / 32), cos(k pi / 32) as hi + lo floats {s.hi, s.lo, c.hi, c.lo},
+// k < 64: built once per device on the host (hp_sincos_table).
+static __device__ float4 g_hp_sincos[64];
+
 __global__ void __launch_bounds__(96) fd_slow_hp_kernel(SlowArgs a) {
   __shared__ dc s_d[6][32];
   __shared__ float4 s_tab[64];
-  if (threadIdx.x < 64) {
-    double sn, cs;
-    sincospi((double)threadIdx.x / 32.0, &sn, &cs);
-    const df s = df_from_double(sn), c = df_from_double(cs);
-    s_tab[threadIdx.x] = make_float4(s.hi, s.lo, c.hi, c.lo);
-  }
+  if (threadIdx.x < 64) s_tab[threadIdx.x] = g_hp_sincos[threadIdx.x];
   __syncthreads();
   int cs[kNumBins + 1];
   int acc = 0;
@@ -326,11 +309,28 @@ static cudaError_t launch_hp(const HpArgs &a, int num_sms, cudaStream_t stream) 
   return cudaLaunchKernelEx(&cfg, fd_hp_kernel<PERCH>, a);
 }
 
-cudaError_t fd_launch_reeval(const PlanArgs &pa, const int *list, const int *count, const SlowArgs &sa,
-                             const HpArgs &h, bool perch, int num_sms, cudaStream_t stream, int *nlaunch) {
-  fd_hp_bin_kernel<<<num_sms, 64, 0, stream>>>(pa, list, count);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+// The double-float sine/cosine table of the current device, from
+// extended-precision host values; once per device, when a context is created
+// (a synchronous copy, never inside a stream capture).
+cudaError_t fd_hp_tables_init() {
+  static LaunchSetup setup;
+  int done = 0;
+  return launch_setup(setup, [&](int *o) {
+    float4 t[64];
+    for (int k = 0; k < 64; k++) {
+      const long double x = (long double)k * (3.14159265358979323846264338327950288L / 32.0L);
+      const long double sv = sinl(x), cv = cosl(x);
+      const float sh = (float)sv, ch = (float)cv;
+      t[k] = make_float4(sh, (float)(sv - (long double)sh), ch, (float)(cv - (long double)ch));
+    }
+    *o = 1;
+    return cudaMemcpyToSymbol(g_hp_sincos, t, sizeof(t));
+  }, &done);
+}
+
+cudaError_t fd_launch_reeval(const SlowArgs &sa, const HpArgs &h, bool perch, int num_sms, cudaStream_t stream,
+                             int *nlaunch) {
+  cudaError_t e;
   static LaunchSetup slow_setup;
   int occ = 0;
   e = launch_setup(slow_setup, [&](int *o) {
@@ -340,7 +340,7 @@ cudaError_t fd_launch_reeval(const PlanArgs &pa, const int *list, const int *cou
   fd_slow_hp_kernel<<<(occ > 0 ? occ : 1) * num_sms, 96, 0, stream>>>(sa);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   e = perch ? launch_hp<true>(h, num_sms, stream) : launch_hp<false>(h, num_sms, stream);
-  if (nlaunch) *nlaunch += 3;
+  if (nlaunch) *nlaunch += 2;
   return e;
 }
 
