@@ -542,6 +542,21 @@ __device__ __forceinline__ R quad(const R *e, R x, R y, R z) {
 }
 
 // sin(x)/x: Taylor series through x^12 for |x| <= 1 (truncation < 1e-12).
+// sinc(x) - 1, so that a product with sinc(x) ~ 1 need not round it near 1
+// (as 1 + small it would round to the same float over many samples of a
+// slowly varying argument: a relative error common to the whole template).
+__device__ __forceinline__ float sinc_m1_f(float x) {
+  if (fabsf(x) > 1.0f) return sinf(x) / x - 1.0f;
+  float x2 = x * x;
+  float s = 1.6059043836821613e-10f;          // 1/13!
+  s = fmaf(s, x2, -2.505210838544172e-08f);   // -1/11!
+  s = fmaf(s, x2, 2.755731922398589e-06f);    // 1/9!
+  s = fmaf(s, x2, -1.984126984126984e-04f);   // -1/7!
+  s = fmaf(s, x2, 8.333333333333333e-03f);    // 1/5!
+  s = fmaf(s, x2, -1.666666666666667e-01f);   // -1/3!
+  return s * x2;
+}
+
 __device__ __forceinline__ float sinc_f(float x) {
   if (fabsf(x) > 1.0f) return sinf(x) / x;
   float x2 = x * x;
@@ -754,7 +769,10 @@ __device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSam
   const float uf = o.u_hi;
   const float tgc = AUc * (c.k[0] * ca + c.k[1] * sa);  // guiding-centre delay (s)
 
-  float fon[3], aev[3];
+  // aev_i = 1 + aef v is kept as aef v: for a slowly chirping source it is
+  // below one float ulp of 1, and rounded it would be the same float over
+  // many samples (a relative error common to the template)
+  float fon[3], aevm1[3];
   df arg2[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -763,7 +781,7 @@ __device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSam
     float tT = taui * invT;
     float v = uf - tT;  // xi / T
     fon[i] = c.fonfs0 + fmaf(c.fdfs, v, c.fonfs0l);
-    aev[i] = fmaf(c.aef, v, 1.0f);
+    aevm1[i] = c.aef * v;
     const df wk = two_prod(c.w0c, kdx);
     arg2[i] = df_add(psi0, df{-wk.hi, fmaf(c.p7pi * tT, tT - 2.0f * uf, -fmaf(c.w0cl, kdx, wk.lo))});
   }
@@ -774,16 +792,17 @@ __device__ __forceinline__ void slow_sample_mix(const ItemMix &c, const OrbitSam
 #pragma unroll
   for (int a = 0; a < 6; a++) {
     int i = ai[a];
-    float arg1 = 0.5f * fon[i] * (1.0f + krs[a]);
-    float sinc = 0.25f * sinc_f(arg1);
-    float t1r = aev[i] * mrs[a];
-    float t1i = aev[i] * mis[a];
+    const float arg1 = 0.5f * fon[i] * (1.0f + krs[a]);
+    const float sm1 = sinc_m1_f(arg1);  // sinc - 1
+    const float t1r = fmaf(aevm1[i], mrs[a], mrs[a]);
+    const float t1i = fmaf(aevm1[i], mis[a], mis[a]);
     const df th = two_sum(arg1, -arg2[i].hi);
     const float tl = th.lo - arg2[i].lo;
     float s2, c2;
     fast_sincos(th.hi, &s2, &c2);
     const float s2c = fmaf(tl, c2, s2), c2c = fmaf(-tl, s2, c2);  // sin, cos of th.hi + tl
-    d[a] = make_float2(sinc * (t1r * c2c + t1i * s2c), sinc * (-t1r * s2c + t1i * c2c));
+    const float pr = t1r * c2c + t1i * s2c, pi = -t1r * s2c + t1i * c2c;
+    d[a] = make_float2(0.25f * fmaf(sm1, pr, pr), 0.25f * fmaf(sm1, pi, pi));
   }
 }
 
