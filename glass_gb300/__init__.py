@@ -63,6 +63,7 @@ EXPORTS = (
     "glass_gpu_noise_sgwb_setup", "glass_gpu_noise_logl_batch_sgwb", "glass_gpu_noise_logl_batch_sgwb_host",
     "glass_gpu_noise_wavelet_logl_batch_sgwb", "glass_gpu_noise_wavelet_logl_batch_sgwb_host",
     "glass_gpu_checked_build", "glass_gpu_check_status",
+    "glass_gpu_spline_noise_setup", "glass_gpu_spline_noise_logl_batch", "glass_gpu_spline_noise_logl_batch_host",
 )
 
 _lib = None
@@ -145,6 +146,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_noise_wavelet_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D]
     lib.glass_gpu_noise_sgwb_setup.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D]
     lib.glass_gpu_check_status.argtypes = [_V, ctypes.POINTER(ctypes.c_uint)]
+    lib.glass_gpu_spline_noise_setup.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D,
+                                                 _D, _D]
+    lib.glass_gpu_spline_noise_logl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V]
+    lib.glass_gpu_spline_noise_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D]
     lib.glass_gpu_noise_logl_batch_sgwb.argtypes = [_V, ctypes.c_int, _V, _V, _V, _V]
     lib.glass_gpu_noise_logl_batch_sgwb_host.argtypes = [_V, ctypes.c_int, _D, _D, _D, _D]
     lib.glass_gpu_noise_wavelet_logl_batch_sgwb.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V]
@@ -480,6 +485,32 @@ class Engine:
         None, logl [n]; asynchronous."""
         n = int(inst.shape[0])
         _check(self.lib.glass_gpu_noise_logl_batch_sgwb(self._ctx, n, _ptr(inst), _ptr(sgal), _ptr(sgwb), _ptr(logl)))
+
+    def spline_noise_setup(self, T, qmin, transfer, d0, d1=None):
+        """The spline noise model's data: transfer [NFFT] and one (d0) or two
+        (d0, d1) channels, interleaved (2 NFFT each), on the bins qmin/T + n/T."""
+        tr = np.ascontiguousarray(transfer, np.float64)
+        a = np.ascontiguousarray(d0, np.float64)
+        b = None if d1 is None else np.ascontiguousarray(d1, np.float64)
+        _check(self.lib.glass_gpu_spline_noise_setup(self._ctx, 1 if b is None else 2, float(T), int(qmin), len(tr),
+                                                     _pd(tr), _pd(a), _pd(b) if b is not None else None))
+
+    def spline_noise_logl_host(self, nknots, knot_f, knot_C):
+        """noise_log_likelihood per model: nknots [n], knot_f [n, kmax],
+        knot_C [n, nchannel, kmax]."""
+        k = np.ascontiguousarray(nknots, np.int32)
+        f = np.ascontiguousarray(knot_f, np.float64)
+        c = np.ascontiguousarray(knot_C, np.float64)
+        out = np.empty(len(k))
+        _check(self.lib.glass_gpu_spline_noise_logl_batch_host(self._ctx, len(k), f.shape[1], _pi(k), _pd(f), _pd(c),
+                                                               _pd(out)))
+        return out
+
+    def spline_noise_logl_device(self, nknots, knot_f, knot_C, logl):
+        """Device tensors as spline_noise_logl_host's arrays; asynchronous."""
+        n = int(nknots.numel())
+        _check(self.lib.glass_gpu_spline_noise_logl_batch(self._ctx, n, int(knot_f.shape[1]), _ptr(nknots),
+                                                          _ptr(knot_f), _ptr(knot_C), _ptr(logl)))
 
     def noise_wavelet_setup(self, NF, NT, df, lmin, Q, X, Y, Z, mod=None):
         """Wavelet data (pixel i of layer j at i + j NT) on layers lmin.., cells of Q

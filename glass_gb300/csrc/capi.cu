@@ -147,6 +147,7 @@ struct glass_gpu_ctx {
   FsWorkDev fsw;  // F-statistic scratch
   NoiseDev noise;  // noise-model likelihood: per-bin table and chunk sums
   NoiseWvDev noise_wv;  // the same in the wavelet domain
+  SplineNoiseDev spline_noise;    // the one- and two-channel spline noise model
   int sgwb_type = -1;             // SGWB template of glass_gpu_noise_sgwb_setup (-1: none)
   std::vector<double> sgwb_resp;  // its response table rows (f, XX, YY, ZZ, XY, XZ, YZ)
   double *eta_scratch = nullptr;  // glass_gpu_noise_eta_batch: 5 doubles per chain
@@ -242,6 +243,7 @@ extern "C" int glass_gpu_destroy(glass_gpu_ctx *ctx) {
   cudaFree(ctx->noise_wv.mem);
   cudaFree(ctx->noise_wv.rsg);
   cudaFree(ctx->noise_wv.partial);
+  cudaFree(ctx->spline_noise.tab);
   cudaFree(ctx->eta_scratch);
   for (int b = 0; b < kNumBins; b++) {
     if (ctx->work.side[b]) cudaStreamDestroy(ctx->work.side[b]);
@@ -1351,6 +1353,96 @@ extern "C" int glass_gpu_noise_logl_batch_sgwb_host(glass_gpu_ctx *ctx, int npro
 extern "C" int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
                                                double *logl) {
   return glass_gpu_noise_logl_batch_sgwb_host(ctx, nprop, inst, sgal, nullptr, logl);
+}
+
+// ------------------------------------------------------ spline noise model
+extern "C" int glass_gpu_spline_noise_setup(glass_gpu_ctx *ctx, int nchannel, double T, int qmin, int NFFT,
+                                            const double *transfer, const double *d0, const double *d1) {
+  if (!ctx || !transfer || !d0 || (nchannel == 2 && !d1))
+    return set_err(GLASS_ERR_ARG, "spline_noise_setup: null argument");
+  if (nchannel < 1 || nchannel > 2) return set_err(GLASS_ERR_ARG, "spline_noise_setup: one or two channels");
+  if (!(T > 0) || NFFT < 1 || qmin < 0) return set_err(GLASS_ERR_ARG, "spline_noise_setup: bad grid");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t N = (size_t)NFFT;
+  std::vector<double> tab((2 + nchannel) * N);
+  const double fmin = (double)qmin / T;
+  for (size_t n = 0; n < N; n++) {
+    tab[n] = fmin + (double)n / T;  // the model's grid (noise/src/glass_noise_model.c:1349)
+    tab[N + n] = transfer[n];
+    for (int c = 0; c < nchannel; c++) {
+      const double *d = c == 0 ? d0 : d1;
+      tab[(2 + c) * N + n] = d[2 * n] * d[2 * n] + d[2 * n + 1] * d[2 * n + 1];
+    }
+  }
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "spline_noise_setup sync");
+  SplineNoiseDev &sd = ctx->spline_noise;
+  cudaFree(sd.tab);
+  sd.tab = nullptr;
+  GLASS_CUDA(cudaMalloc(&sd.tab, sizeof(double) * tab.size()), "cudaMalloc(spline noise table)");
+  GLASS_CUDA(cudaMemcpy(sd.tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice),
+             "upload spline noise table");
+  sd.nch = nchannel;
+  sd.N = NFFT;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_spline_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, int kmax, const int *nknots,
+                                                 const double *knot_f, const double *knot_C, double *logl) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch: null context");
+  if (nprop < 0) return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch: negative model count");
+  if (nprop == 0) return GLASS_OK;
+  if (!nknots || !knot_f || !knot_C || !logl) return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch: null argument");
+  if (kmax < 2 || kmax > kSplineMaxKnots)
+    return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch: kmax must be 2 .. %s", std::to_string(kSplineMaxKnots).c_str());
+  if (!ctx->spline_noise.tab) return set_err(GLASS_ERR_STATE, "spline_noise_logl_batch: no data (glass_gpu_spline_noise_setup)");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  int nl = 0;
+  cudaError_t e = spline_noise_launch(ctx->spline_noise, nprop, kmax, nknots, knot_f, knot_C, logl, ctx->stream, &nl);
+  ctx->last_launches = nl;
+  if (e != cudaSuccess) return cuda_err(e, "spline_noise_logl_batch launch");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_spline_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, int kmax, const int *nknots,
+                                                      const double *knot_f, const double *knot_C, double *logl) {
+  if (!ctx) return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch_host: null context");
+  if (nprop < 0) return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch_host: negative model count");
+  if (nprop == 0) return GLASS_OK;
+  if (!nknots || !knot_f || !knot_C || !logl)
+    return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch_host: null argument");
+  if (kmax < 2 || kmax > kSplineMaxKnots)
+    return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch_host: kmax must be 2 .. %s",
+                   std::to_string(kSplineMaxKnots).c_str());
+  if (!ctx->spline_noise.tab)
+    return set_err(GLASS_ERR_STATE, "spline_noise_logl_batch_host: no data (glass_gpu_spline_noise_setup)");
+  const int nch = ctx->spline_noise.nch;
+  for (int p = 0; p < nprop; p++) {  // knot counts in range, frequencies increasing
+    if (nknots[p] < 2 || nknots[p] > kmax)
+      return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch_host: model %s has a knot count outside 2 .. kmax",
+                     std::to_string(p).c_str());
+    for (int k = 1; k < nknots[p]; k++)
+      if (!(knot_f[(size_t)p * kmax + k] > knot_f[(size_t)p * kmax + k - 1]))
+        return set_err(GLASS_ERR_ARG, "spline_noise_logl_batch_host: model %s's knot frequencies do not increase",
+                       std::to_string(p).c_str());
+  }
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const size_t nd = (size_t)nprop, km = (size_t)kmax;
+  const size_t bytes = sizeof(double) * nd * (km * (1 + nch) + 1) + sizeof(int) * nd;
+  if ((rc = ensure_stage(ctx, bytes))) return rc;
+  double *d_f = (double *)ctx->d_stage, *d_C = d_f + nd * km, *d_l = d_C + nd * km * nch;
+  int *d_n = (int *)(d_l + nd);
+  cudaStream_t s = ctx->stream;
+  GLASS_CUDA(cudaMemcpyAsync(d_f, knot_f, sizeof(double) * nd * km, cudaMemcpyHostToDevice, s), "H2D knot_f");
+  GLASS_CUDA(cudaMemcpyAsync(d_C, knot_C, sizeof(double) * nd * km * nch, cudaMemcpyHostToDevice, s), "H2D knot_C");
+  GLASS_CUDA(cudaMemcpyAsync(d_n, nknots, sizeof(int) * nd, cudaMemcpyHostToDevice, s), "H2D nknots");
+  rc = glass_gpu_spline_noise_logl_batch(ctx, nprop, kmax, d_n, d_f, d_C, d_l);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(logl, d_l, sizeof(double) * nd, cudaMemcpyDeviceToHost, s), "D2H logl");
+  GLASS_CUDA(cudaStreamSynchronize(s), "spline_noise_logl_batch_host sync");
+  return GLASS_OK;
 }
 
 extern "C" int glass_gpu_noise_wavelet_setup(glass_gpu_ctx *ctx, int NF, int NT, double df, int lmin, int Nlayer,

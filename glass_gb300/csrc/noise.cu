@@ -433,6 +433,94 @@ __global__ void noise_wv_const_kernel(double *logl, int nprop, double cst) {
   if (p < nprop) logl[p] -= cst;
 }
 
+// ------------------------------------------------ spline noise model
+// One CTA per model (noise_spline_model_mcmc / _rjmcmc,
+// noise/src/glass_noise_sampler.c:133, :232): one thread per channel solves
+// the natural cubic spline through the model's control points
+// (spline_coefficients, utils/src/glass_math.c:98-178: the tridiagonal
+// system's forward elimination and back substitution, sequential), then all
+// threads evaluate it over the bins with the binary-search lookup (the largest
+// knot <= f: binary_search, :443-473, on distinct knots), add the transfer
+// floor (generate_spline_noise_model, noise/src/glass_noise_model.c:366-387),
+// and sum noise_log_likelihood's terms (:1104-1134): -|d|^2 / C per channel
+// and -log C.
+struct SplineNoiseArgs {
+  int nch, N, kmax;
+  const double *tab;  // f, transfer, P0[, P1]
+  const int *nknots;
+  const double *knot_f, *knot_C;
+  double *logl;
+};
+
+__device__ __forceinline__ int spline_knot_below(int K, const double *x, double v) {
+  if (v <= x[0]) return 0;
+  if (v >= x[K - 1]) return K - 1;
+  int lo = 0, hi = K - 1;  // x[lo] <= v < x[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (x[mid] <= v)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kNoiseThreads) spline_noise_kernel(SplineNoiseArgs a) {
+  extern __shared__ double sm[];
+  __shared__ double red[kNoiseThreads / 32];
+  const int p = blockIdx.x, K = a.nknots[p], KM = a.kmax;
+  if (K < 2 || K > KM) {  // the whole CTA leaves before any barrier
+    if (threadIdx.x == 0) a.logl[p] = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
+  // x[KM], then per channel c0, c1, c2, c3, mu, z (each KM)
+  double *x = sm;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) x[k] = a.knot_f[(size_t)p * KM + k];
+  __syncthreads();
+  if (threadIdx.x < a.nch) {
+    const int c = threadIdx.x;
+    double *c0 = sm + KM * (1 + 6 * c), *c1 = c0 + KM, *c2 = c1 + KM, *c3 = c2 + KM, *mu = c3 + KM, *z = mu + KM;
+    const double *y = a.knot_C + ((size_t)p * a.nch + c) * KM;
+    mu[0] = z[0] = 0.0;
+    for (int i = 1; i < K - 1; i++) {
+      const double hm = x[i] - x[i - 1], hi = x[i + 1] - x[i];
+      const double al = 3.0 * ((y[i + 1] - y[i]) / hi - (y[i] - y[i - 1]) / hm);
+      const double l = 2.0 * (x[i + 1] - x[i - 1]) - hm * mu[i - 1];
+      mu[i] = hi / l;
+      z[i] = (al - hm * z[i - 1]) / l;
+    }
+    c0[K - 1] = y[K - 1];
+    c1[K - 1] = c2[K - 1] = c3[K - 1] = 0.0;
+    for (int i = K - 2; i >= 0; i--) {
+      const double h = x[i + 1] - x[i];
+      c0[i] = y[i];
+      c2[i] = z[i] - mu[i] * c2[i + 1];
+      c1[i] = (c0[i + 1] - c0[i]) / h - h * (c2[i + 1] + 2.0 * c2[i]) / 3.0;
+      c3[i] = (c2[i + 1] - c2[i]) / (3.0 * h);
+    }
+  }
+  __syncthreads();
+  const int N = a.N;
+  const double *F = a.tab, *TR = a.tab + N;
+  double acc = 0.0;
+  for (int n = threadIdx.x; n < N; n += blockDim.x) {
+    const double f = F[n];
+    const int j = spline_knot_below(K, x, f);
+    const double d = f - x[j];
+    double ld = 0.0;
+    for (int c = 0; c < a.nch; c++) {
+      const double *c0 = sm + KM * (1 + 6 * c), *c1 = c0 + KM, *c2 = c1 + KM, *c3 = c2 + KM;
+      const double C = (c0[j] + c1[j] * d + c2[j] * d * d + c3[j] * d * d * d) + TR[n];
+      acc -= 0.5 * (2.0 * (a.tab[(size_t)(2 + c) * N + n] * (1. / C)));
+      ld += log(C);
+    }
+    acc -= ld;
+  }
+  const double s = block_sum(acc, red);
+  if (threadIdx.x == 0) a.logl[p] = s;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------- host
@@ -675,6 +763,32 @@ cudaError_t noise_wv_logl_launch(const NoiseWvDev &w, int mode, int nprop, const
 }
 
 int noise_chunks(int N) { return (N + kNoiseChunk - 1) / kNoiseChunk; }
+
+static size_t spline_smem(int nch, int kmax) { return sizeof(double) * (size_t)kmax * (1 + 6 * nch); }
+
+cudaError_t spline_noise_launch(const SplineNoiseDev &s, int nprop, int kmax, const int *nknots, const double *knot_f,
+                                const double *knot_C, double *logl, cudaStream_t stream, int *nlaunch) {
+  static LaunchSetup setup;
+  int dummy = 0;
+  cudaError_t e = launch_setup(setup, [&](int *o) {
+    *o = 1;
+    return cudaFuncSetAttribute(spline_noise_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)spline_smem(2, kSplineMaxKnots));
+  }, &dummy);
+  if (e != cudaSuccess) return e;
+  SplineNoiseArgs a;
+  a.nch = s.nch;
+  a.N = s.N;
+  a.kmax = kmax;
+  a.tab = s.tab;
+  a.nknots = nknots;
+  a.knot_f = knot_f;
+  a.knot_C = knot_C;
+  a.logl = logl;
+  spline_noise_kernel<<<nprop, kNoiseThreads, spline_smem(s.nch, kmax), stream>>>(a);
+  if (nlaunch) *nlaunch = 1;
+  return cudaGetLastError();
+}
 
 cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst, const double *sgal, int sg_type,
                               const double *sgwb, double *logl, cudaStream_t stream, int *nlaunch) {

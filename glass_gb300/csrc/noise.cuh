@@ -61,6 +61,18 @@ constexpr int kSgwbParams[kSgwbTypes] = {2, 3, 4};
 // yy, zz, xy, xz, yz (0 at f = 0).  Returns 0, or -1 for a table the
 // reference would refuse or cannot take a log of.
 int noise_sgwb_rows(int nresp, const double *resp, int N, const double *f, double *R6);
+
+// The spline noise model (one or two channels): the bins' frequencies, the
+// transfer floor and each channel's data power |d|^2, all N doubles.
+constexpr int kSplineMaxKnots = 512;
+struct SplineNoiseDev {
+  int nch = 0, N = 0;
+  double *tab = nullptr;  // f, transfer, P0[, P1]: (2 + nch) x N
+};
+// logl[p] for nprop spline models: nknots[p] control points knot_f[p kmax ..],
+// knot_C[(p nch + c) kmax ..] (device pointers)
+cudaError_t spline_noise_launch(const SplineNoiseDev &s, int nprop, int kmax, const int *nknots, const double *knot_f,
+                                const double *knot_C, double *logl, cudaStream_t stream, int *nlaunch);
 int noise_chunks(int N);
 // logl[p] for noise models inst[12 p ..] (sacc[6], soms[6]) and sgal[5 p ..]
 // (or null: instrument only), plus, with sgwb[4 p ..] (or null), the SGWB of

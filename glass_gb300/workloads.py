@@ -327,6 +327,60 @@ def sgwb_params_draw(rng, sgwb_type, n):
     return out
 
 
+def spline_noise_data(rng, T, qmin, NFFT, nch, excess=1.0):
+    """Data for the spline noise model on bins qmin/T + n/T: the A/E noise
+    PSD as the transfer function (initialize_spline_model,
+    noise/src/glass_noise_model.c:1346-1355, with the A/E form for one channel
+    too) and, per channel, complex bins with E|d|^2 = transfer (1 + excess
+    bump), a smooth excess (a Gaussian in log f centred in the band, as a
+    foreground would add) that the spline has to fit.  Returns (transfer
+    [NFFT], d [nch, 2 NFFT], the excess spectrum [nch, NFFT] over transfer)."""
+    f = (qmin + np.arange(NFFT)) / T
+    tr = aenoise_ff(f)
+    lf = np.log(f)
+    mid, wid = 0.5 * (lf[0] + lf[-1]), max(0.25 * (lf[-1] - lf[0]), 1e-12)
+    d = np.empty((nch, 2 * NFFT))
+    ex = np.empty((nch, NFFT))
+    for c in range(nch):
+        ex[c] = tr * excess * (1.0 + 0.2 * c) * np.exp(-0.5 * ((lf - mid) / wid) ** 2)
+        sd = np.sqrt(0.5 * (tr + ex[c]))
+        d[c, 0::2] = rng.standard_normal(NFFT) * sd
+        d[c, 1::2] = rng.standard_normal(NFFT) * sd
+    return tr, d, ex
+
+
+def spline_noise_models(rng, T, qmin, NFFT, excess, n, kmax, kmin=2, first_full=True):
+    """n spline noise models [knots in the layout the batched likelihood
+    takes]: nknots [n], knot_f [n, kmax], knot_C [n, nch, kmax].  The first
+    (first_full) has kmax knots log-evenly spaced over fmin .. fmax with the
+    first moved down half a bin (initialize_spline_model,
+    noise/src/glass_noise_model.c:1357-1372); the others a knot count drawn
+    from kmin .. kmax (the trans-dimensional sampler's range) with the end
+    knots kept and the interior knots on an even grid moved by up to 0.3 of
+    its spacing.  Control values: the excess (excess [nch, NFFT], linearly
+    interpolated) times 1 + U(-0.1, 0.1)."""
+    nch = len(excess)
+    fmin, fmax = qmin / T, (qmin + NFFT) / T
+    f = (qmin + np.arange(NFFT)) / T
+    nk = np.zeros(n, np.int32)
+    kf = np.zeros((n, kmax))
+    kC = np.zeros((n, nch, kmax))
+    for p in range(n):
+        if p == 0 and first_full:
+            K = kmax
+            x = np.exp(np.linspace(math.log(fmin), math.log(fmax), K))
+        else:
+            K = int(rng.integers(kmin, kmax + 1))
+            x = np.linspace(fmin, fmax, K)
+            x[1:-1] += rng.uniform(-0.3, 0.3, K - 2) * (fmax - fmin) / (K - 1)
+        x[0] -= 0.5 / T
+        nk[p] = K
+        kf[p, :K] = x
+        for c in range(nch):
+            kC[p, c, :K] = np.interp(x, f, excess[c]) * (1.0 + rng.uniform(-0.1, 0.1, K))
+    return nk, kf, kC
+
+
 def xyz_from_covariance(rng, C6):
     """Complex XYZ bins with E[x x^H] = C for real symmetric per-bin C given as
     [N, 6] = xx, yy, zz, xy, xz, yz; returned interleaved (3, 2N)."""

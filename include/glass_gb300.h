@@ -397,6 +397,31 @@ int glass_gpu_noise_wavelet_logl_batch_sgwb(glass_gpu_ctx *ctx, int mode, int np
 int glass_gpu_noise_wavelet_logl_batch_sgwb_host(glass_gpu_ctx *ctx, int mode, int nprop, const double *inst,
                                                  const double *sgal, const double *sgwb, double *logl);
 
+/*
+ * The noise module's one- and two-channel spline noise model
+ * (noise_spline_model_mcmc / _rjmcmc, noise/src/glass_noise_sampler.c:213-393):
+ * each model's noise spectrum per channel is the natural cubic spline through
+ * its control points (CubicSplineGLASS with the binary-search lookup,
+ * utils/src/glass_math.c:855-868) at f_n = qmin/T + n/T plus the transfer
+ * function (generate_spline_noise_model, noise/src/glass_noise_model.c:366-387),
+ * and logl[p] is noise_log_likelihood (:1104-1134) of the data for it:
+ *   -sum_c sum_n |d_c[n]|^2 / C_c[n]  -  sum_n sum_c log C_c[n].
+ * glass_gpu_spline_noise_setup keeps the grid, transfer[NFFT] and the data's
+ * power |d_c|^2 (d0, d1: 2 NFFT interleaved doubles; d1 used when nchannel
+ * is 2).  glass_gpu_spline_noise_logl_batch: model p has nknots[p] control
+ * points (2 .. kmax, frequencies strictly increasing) at knot_f[p kmax + k],
+ * values knot_C[(p nchannel + c) kmax + k]; kmax <= 512.  One launch, one CTA
+ * per model.  FP64.  Device pointers, asynchronous (a knot count outside
+ * 2 .. kmax gives NaN).  _host: host pointers, synchronous, and the knot
+ * counts and orders are checked (GLASS_ERR_ARG).
+ */
+int glass_gpu_spline_noise_setup(glass_gpu_ctx *ctx, int nchannel, double T, int qmin, int NFFT,
+                                 const double *transfer, const double *d0, const double *d1);
+int glass_gpu_spline_noise_logl_batch(glass_gpu_ctx *ctx, int nprop, int kmax, const int *nknots,
+                                      const double *knot_f, const double *knot_C, double *logl);
+int glass_gpu_spline_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, int kmax, const int *nknots,
+                                           const double *knot_f, const double *knot_C, double *logl);
+
 /* glass_gpu_dlogl_batch with each channel's share of term_y as well:
  * term_ch[2 i] (A) + term_ch[2 i + 1] (E) = term_y[i].  Device pointers. */
 int glass_gpu_dlogl_batch_channels(glass_gpu_ctx *ctx, int precision, int nitems, const int *item_seg,

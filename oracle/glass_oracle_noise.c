@@ -99,6 +99,110 @@ static void orc_noise_cov_bin(double f, const double *sacc, const double *soms, 
     }
 }
 
+/* ------------------------------------------------------- natural splines */
+/* spline_coefficients (utils/src/glass_math.c:98-178): natural cubic spline
+ * through (x[i], y[i]), i < n, coefficients c0..c3 of interval i. */
+static void orc_nat_spline(int n, const double *x, const double *y, double *c0, double *c1, double *c2, double *c3)
+{
+    double *h = calloc(n, sizeof(double)), *al = calloc(n, sizeof(double));
+    double *l = calloc(n, sizeof(double)), *z = calloc(n, sizeof(double)), *mu = calloc(n, sizeof(double));
+    h[0] = x[1] - x[0];
+    for (int i = 1; i < n - 1; i++) {
+        h[i] = x[i + 1] - x[i];
+        al[i] = 3.0 * ((y[i + 1] - y[i]) / h[i] - (y[i] - y[i - 1]) / h[i - 1]);
+    }
+    l[0] = l[n - 1] = 1.0;
+    for (int i = 1; i < n - 1; i++) {
+        l[i] = 2.0 * (x[i + 1] - x[i - 1]) - h[i - 1] * mu[i - 1];
+        mu[i] = h[i] / l[i];
+        z[i] = (al[i] - h[i - 1] * z[i - 1]) / l[i];
+    }
+    c0[n - 1] = y[n - 1];
+    c1[n - 1] = c2[n - 1] = c3[n - 1] = 0.0;
+    for (int i = n - 2; i >= 0; i--) {
+        c0[i] = y[i];
+        c2[i] = z[i] - mu[i] * c2[i + 1];
+        c1[i] = (c0[i + 1] - c0[i]) / h[i] - h[i] * (c2[i + 1] + 2.0 * c2[i]) / 3.0;
+        c3[i] = (c2[i + 1] - c2[i]) / (3.0 * h[i]);
+    }
+    free(h); free(al); free(l); free(z); free(mu);
+}
+
+/* binary_search (utils/src/glass_math.c:443-473) on distinct knots: the
+ * largest i with x[i] <= v (0 below the first knot, where the reference's
+ * lookup is undefined). */
+static int orc_knot_below(int n, const double *x, double v)
+{
+    int lo = 0, hi = n - 1;
+    if (v <= x[0]) return 0;
+    if (v >= x[n - 1]) return n - 1;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) / 2;
+        if (x[mid] <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+/* ----------------------------------------------------- spline noise model */
+/* The noise module's one- and two-channel spline noise model for one model:
+ * per channel c the natural cubic spline through the control points
+ * (kf[k], kC[c K + k]), k < K, evaluated at f = fmin + n/T with the
+ * binary-search lookup (CubicSplineGLASS, utils/src/glass_math.c:855-868),
+ * plus transfer[n] (generate_spline_noise_model,
+ * noise/src/glass_noise_model.c:366-387), inverted per channel
+ * (invert_noise_covariance_matrix's one- and two-channel branches,
+ * utils/src/glass_math.c:248-258), and noise_log_likelihood
+ * (noise/src/glass_noise_model.c:1104-1134): -1/2 fourier_nwip per channel
+ * minus the log-determinants.  d0, d1: 2 NFFT doubles (X; or A, E). */
+double orc_spline_noise_logl(int nch, int NFFT, double T, double fmin, const double *d0, const double *d1,
+                             const double *transfer, int K, const double *kf, const double *kC)
+{
+    double *c0 = malloc(sizeof(double) * K), *c1 = malloc(sizeof(double) * K);
+    double *c2 = malloc(sizeof(double) * K), *c3 = malloc(sizeof(double) * K);
+    double *C = malloc(sizeof(double) * (size_t)nch * NFFT);
+    for (int c = 0; c < nch; c++) {
+        orc_nat_spline(K, kf, kC + (size_t)c * K, c0, c1, c2, c3);
+        for (int n = 0; n < NFFT; n++) {
+            double f = fmin + (double)n / T;
+            int j = orc_knot_below(K, kf, f);
+            double d = f - kf[j];
+            C[(size_t)c * NFFT + n] = (c0[j] + c1[j] * d + c2[j] * d * d + c3[j] * d * d * d) + transfer[n];
+        }
+    }
+    double logL = 0.0;
+    for (int c = 0; c < nch; c++) {
+        const double *dd = c == 0 ? d0 : d1;
+        double arg = 0.0;
+        for (int n = 0; n < NFFT; n++) {
+            double product = dd[2 * n] * dd[2 * n] + dd[2 * n + 1] * dd[2 * n + 1];
+            arg += product * (1. / C[(size_t)c * NFFT + n]);
+        }
+        logL += -0.5 * (2.0 * arg);
+    }
+    for (int n = 0; n < NFFT; n++) {
+        double ld = log(C[n]);
+        if (nch == 2) ld += log(C[(size_t)NFFT + n]);
+        logL -= ld;
+    }
+    free(c0); free(c1); free(c2); free(c3); free(C);
+    return logL;
+}
+
+/* Batched: knots kf[p kmax + k], kC[(p nch + c) kmax + k], k < nknots[p]. */
+void orc_spline_noise_logl_batch(int nch, int NFFT, double T, double fmin, const double *d0, const double *d1,
+                                 const double *transfer, int nprop, int kmax, const int *nknots, const double *kf,
+                                 const double *kC, double *logl)
+{
+    double *cc = malloc(sizeof(double) * (size_t)nch * kmax);
+    for (int p = 0; p < nprop; p++) {
+        int K = nknots[p];
+        for (int c = 0; c < nch; c++)
+            memcpy(cc + (size_t)c * K, kC + ((size_t)p * nch + c) * kmax, sizeof(double) * K);
+        logl[p] = orc_spline_noise_logl(nch, NFFT, T, fmin, d0, d1, transfer, K, kf + (size_t)p * kmax, cc);
+    }
+    free(cc);
+}
+
 /* ------------------------------------------------------------------ SGWB */
 /* utils/src/glass_constants.h:81-86 */
 #define ORC_H0 (70 * 3.24078e-20)

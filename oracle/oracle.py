@@ -288,6 +288,23 @@ class Port:
                                               _p(r), _p(out), nthreads)
         return out
 
+    def spline_noise_logl(self, T, fmin, d, transfer, nknots, knot_f, knot_C):
+        """The spline noise model's noise_log_likelihood for each model: d [nch, 2 NFFT]
+        (X; or A, E), knot_f [n, kmax], knot_C [n, nch, kmax], nknots [n]."""
+        lib = self.lib
+        lib.orc_spline_noise_logl_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                    _D, _D, _D, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D]
+        d = np.ascontiguousarray(d, np.float64)
+        nch, NFFT = d.shape[0], d.shape[1] // 2
+        kf = np.ascontiguousarray(knot_f, np.float64)
+        kC = np.ascontiguousarray(knot_C, np.float64)
+        nk = np.ascontiguousarray(nknots, np.int32)
+        out = np.zeros(len(nk))
+        lib.orc_spline_noise_logl_batch(nch, NFFT, T, fmin, _p(d[0]), _p(d[nch - 1]),
+                                        _p(np.ascontiguousarray(transfer, np.float64)), len(nk), kf.shape[1], _pi(nk),
+                                        _p(kf), _p(kC), _p(out))
+        return out
+
     def noise_coarse_stats(self, NT, Q, X, Y, Z):
         """[6, Nlayer, NT/Q] cell statistics of wavelet data [Nlayer NT] (coarse_grain_wavelet_data)."""
         lib = self.lib
@@ -805,6 +822,22 @@ class Ref:
                                         _p(md) if md is not None else None, len(inst), _p(inst),
                                         _p(sg) if sg is not None else None, int(sgwb_type), _p(b), len(r), _p(r),
                                         _p(out))
+        return out
+
+    def spline_noise_logl(self, T, fmin, d, transfer, nknots, knot_f, knot_C):
+        """The reference's generate_spline_noise_model + noise_log_likelihood."""
+        lib = self.lib
+        lib.ref_spline_noise_logl.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, _D, _D,
+                                              _D, ctypes.c_int, ctypes.c_int, _I, _D, _D, _D]
+        d = np.ascontiguousarray(d, np.float64)
+        nch, NFFT = d.shape[0], d.shape[1] // 2
+        kf = np.ascontiguousarray(knot_f, np.float64)
+        kC = np.ascontiguousarray(knot_C, np.float64)
+        nk = np.ascontiguousarray(nknots, np.int32)
+        out = np.zeros(len(nk))
+        lib.ref_spline_noise_logl(nch, NFFT, T, fmin, _p(d[0]), _p(d[nch - 1]),
+                                  _p(np.ascontiguousarray(transfer, np.float64)), len(nk), kf.shape[1],
+                                  nk.ctypes.data_as(_I), _p(kf), _p(kC), _p(out))
         return out
 
     def noise_eta(self, T, NFFT, qmin, dA, dE, invCA, invCE, params, eta, t0=0.0, fmt="sangria"):

@@ -946,6 +946,55 @@ void ref_noise_wavelet_logl_sgwb(int NF, int NT, double dt, double df, int lmin,
     free(data);
 }
 
+/* The noise module's spline noise model (the one- and two-channel model of
+ * noise_spline_model_mcmc / _rjmcmc, noise/src/glass_noise_sampler.c:133,
+ * :232) for n models: control points knot_f[p kmax + k],
+ * knot_C[(p nch + c) kmax + k] (k < nknots[p]) of each channel c, the
+ * transfer floor transfer[NFFT] on the bins f = fmin + k/T;
+ * generate_spline_noise_model (noise/src/glass_noise_model.c:366) and
+ * noise_log_likelihood (:1104) on the data d0 (X, or A) and d1 (E), 2 NFFT
+ * doubles each. */
+void ref_spline_noise_logl(int nch, int NFFT, double T, double fmin, const double *d0, const double *d1,
+                           const double *transfer, int n, int kmax, const int *nknots, const double *knot_f,
+                           const double *knot_C, double *logl)
+{
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->NFFT = NFFT;
+    data->N = 2 * NFFT;
+    data->Nchannel = nch;
+    data->Nlayer = 1;
+    data->T = T;
+    data->fmin = fmin;
+    strcpy(data->basis, "fourier");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, nch);
+    if (nch == 1) {
+        memcpy(data->tdi->X, d0, sizeof(double) * data->N);
+    } else {
+        memcpy(data->tdi->A, d0, sizeof(double) * data->N);
+        memcpy(data->tdi->E, d1, sizeof(double) * data->N);
+    }
+    for (int p = 0; p < n; p++) {
+        struct SplineModel model;
+        memset(&model, 0, sizeof(model));
+        alloc_spline_model(&model, NFFT, 1, nch, nknots[p]);
+        for (int k = 0; k < NFFT; k++) {
+            model.psd->f[k] = fmin + (double)k / T;
+            model.psd->transfer[k] = transfer[k];
+        }
+        for (int k = 0; k < nknots[p]; k++) {
+            model.spline->f[k] = knot_f[(size_t)p * kmax + k];
+            for (int c = 0; c < nch; c++) model.spline->C[c][c][k] = knot_C[((size_t)p * nch + c) * kmax + k];
+        }
+        generate_spline_noise_model(&model);
+        logl[p] = noise_log_likelihood(data, model.psd);
+        free_noise(model.psd);
+        free_noise(model.spline);
+    }
+    free_tdi(data->tdi);
+    free(data);
+}
+
 /* noise_model_mcmc's likelihood change (ucb/src/glass_ucb_sampler.c:29-73)
  * for n chains with one source each (params[8 c ..]) on one A/E segment:
  * generate_ucb_model, then for eta_x and eta_y (eta[4 c ..] = xA, xE, yA, yE)

@@ -590,9 +590,35 @@ def fisher_draw(ref, rng):
                         y=np.array(ys), logQ=np.array(qs), seeds=np.array(ss))
 
 
+def spline_noise(ref, rng):
+    """The noise module's spline noise model (generate_spline_noise_model +
+    noise_log_likelihood, one and two channels): models around a synthetic
+    excess over the A/E noise PSD, at 2 mHz on 1000 bins (one channel, 24
+    knots at most, 2-knot models among them), 4 mHz on 1024 bins (two
+    channels, 24 knots), and 512 knots on 2048 bins (two channels, the
+    kernel's largest knot count)."""
+    out = {}
+    for name, q, NFFT, nch, n, kmax, kmin in (("one", int(2e-3 * T), 1000, 1, 10, 24, 2),
+                                             ("two", int(4e-3 * T), 1024, 2, 10, 24, 2),
+                                             ("max", int(3e-3 * T), 2048, 2, 2, 512, 512)):
+        tr, d, ex = wl.spline_noise_data(rng, T, q, NFFT, nch, excess=2.0)
+        nk, kf, kC = wl.spline_noise_models(rng, T, q, NFFT, ex, n, kmax, kmin)
+        if name == "one":
+            nk[1] = 2  # the smallest model: a straight line
+            kf[1, :] = 0.0
+            kf[1, 0], kf[1, 1] = q / T - 0.5 / T, (q + NFFT) / T
+            kC[1, :, 2:] = 0.0
+        out[f"{name}_qmin"] = q
+        out[f"{name}_transfer"], out[f"{name}_d"] = tr, d
+        out[f"{name}_nknots"], out[f"{name}_knot_f"], out[f"{name}_knot_C"] = nk, kf, kC
+        out[f"{name}_logl"] = ref.spline_noise_logl(T, q / T, d, tr, nk, kf, kC)
+    np.savez_compressed(os.path.join(HERE, "spline_noise.npz"), **out)
+
+
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
              "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210,
-             "fisher_wavelet": 20261211, "priors": 20261212, "sgwb": 20261213}
+             "fisher_wavelet": 20261211, "priors": 20261212, "sgwb": 20261213,
+             "spline_noise": 20261214}
 
 
 def main(names=()):
@@ -619,6 +645,7 @@ def main(names=()):
     fisher_wavelet(ref, np.random.default_rng(OWN_SEEDS["fisher_wavelet"]))
     priors(ref, np.random.default_rng(OWN_SEEDS["priors"]))
     sgwb(ref, np.random.default_rng(OWN_SEEDS["sgwb"]))
+    spline_noise(ref, np.random.default_rng(OWN_SEEDS["spline_noise"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))
