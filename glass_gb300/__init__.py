@@ -64,6 +64,7 @@ EXPORTS = (
     "glass_gpu_noise_wavelet_logl_batch_sgwb", "glass_gpu_noise_wavelet_logl_batch_sgwb_host",
     "glass_gpu_checked_build", "glass_gpu_check_status",
     "glass_gpu_spline_noise_setup", "glass_gpu_spline_noise_logl_batch", "glass_gpu_spline_noise_logl_batch_host",
+    "glass_gpu_noise_setup_channels",
 )
 
 _lib = None
@@ -146,6 +147,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_noise_wavelet_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D]
     lib.glass_gpu_noise_sgwb_setup.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D]
     lib.glass_gpu_check_status.argtypes = [_V, ctypes.POINTER(ctypes.c_uint)]
+    lib.glass_gpu_noise_setup_channels.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D,
+                                                   _D, _D]
     lib.glass_gpu_spline_noise_setup.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D,
                                                  _D, _D]
     lib.glass_gpu_spline_noise_logl_batch.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V]
@@ -460,6 +463,13 @@ class Engine:
         """XYZ data (interleaved, 2 NFFT each) on the bins qmin/T + n/T."""
         X, Y, Z = (np.ascontiguousarray(a, np.float64) for a in (X, Y, Z))
         _check(self.lib.glass_gpu_noise_setup(self._ctx, float(T), int(qmin), len(X) // 2, _pd(X), _pd(Y), _pd(Z)))
+
+    def noise_setup_channels(self, T, qmin, d0, d1=None, d2=None):
+        """One channel (d0 = X), two (d0, d1 = A, E) or three (X, Y, Z),
+        interleaved (2 NFFT each), on the bins qmin/T + n/T."""
+        ds = [np.ascontiguousarray(a, np.float64) for a in (d0, d1, d2) if a is not None]
+        ptr = [_pd(a) for a in ds] + [None] * (3 - len(ds))
+        _check(self.lib.glass_gpu_noise_setup_channels(self._ctx, len(ds), float(T), int(qmin), len(ds[0]) // 2, *ptr))
 
     def noise_sgwb_setup(self, sgwb_type, resp=None):
         """The SGWB template (0 power law, 1 lognormal, 2 phase transition; -1

@@ -1284,6 +1284,38 @@ extern "C" int glass_gpu_noise_setup(glass_gpu_ctx *ctx, double T, int qmin, int
   nd.tab = nullptr;
   GLASS_CUDA(cudaMalloc(&nd.tab, sizeof(double) * tab.size()), "cudaMalloc(noise table)");
   GLASS_CUDA(cudaMemcpy(nd.tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice), "upload noise table");
+  nd.nch = 3;
+  nd.N = NFFT;
+  nd.T = T;
+  nd.fmin = fmin;
+  cudaFree(nd.partial);
+  nd.partial = nullptr;
+  nd.partial_models = 0;
+  return sgwb_build_rows(ctx);
+}
+
+extern "C" int glass_gpu_noise_setup_channels(glass_gpu_ctx *ctx, int nchannel, double T, int qmin, int NFFT,
+                                              const double *d0, const double *d1, const double *d2) {
+  if (nchannel == 3) return glass_gpu_noise_setup(ctx, T, qmin, NFFT, d0, d1, d2);
+  if (!ctx) return set_err(GLASS_ERR_ARG, "noise_setup_channels: null context");
+  if (nchannel != 1 && nchannel != 2) return set_err(GLASS_ERR_ARG, "noise_setup_channels: one, two or three channels");
+  if (!d0 || (nchannel == 2 && !d1)) return set_err(GLASS_ERR_ARG, "noise_setup_channels: null argument");
+  // qmin >= 1: at f = 0 the reference's one- and two-channel branch writes
+  // covariance entries of three channels
+  if (!(T > 0) || NFFT < 1 || qmin < 1)
+    return set_err(GLASS_ERR_ARG, "noise_setup_channels: bad grid (T > 0, NFFT >= 1, qmin >= 1)");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  const double fmin = (double)qmin / T;
+  std::vector<double> tab((size_t)kNoiseTabRows * NFFT);
+  noise_build_table_ch(T, fmin, NFFT, nchannel, d0, d1, tab.data());
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "noise_setup_channels sync");
+  NoiseDev &nd = ctx->noise;
+  cudaFree(nd.tab);
+  nd.tab = nullptr;
+  GLASS_CUDA(cudaMalloc(&nd.tab, sizeof(double) * tab.size()), "cudaMalloc(noise table)");
+  GLASS_CUDA(cudaMemcpy(nd.tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice), "upload noise table");
+  nd.nch = nchannel;
   nd.N = NFFT;
   nd.T = T;
   nd.fmin = fmin;
@@ -1301,6 +1333,8 @@ extern "C" int glass_gpu_noise_logl_batch_sgwb(glass_gpu_ctx *ctx, int nprop, co
   if (!inst || !logl) return set_err(GLASS_ERR_ARG, "noise_logl_batch: null argument");
   NoiseDev &nd = ctx->noise;
   if (!nd.tab) return set_err(GLASS_ERR_STATE, "noise_logl_batch: no data set (glass_gpu_noise_setup)");
+  if (sgwb && nd.nch != 3)  // generate_sgwb_model stops for Nchannel 1 or 2
+    return set_err(GLASS_ERR_ARG, "noise_logl_batch: the SGWB covariance needs three channels");
   if (sgwb && (ctx->sgwb_type < 0 || !nd.rsg))
     return set_err(GLASS_ERR_STATE, "noise_logl_batch: no SGWB template set (glass_gpu_noise_sgwb_setup)");
   int rc = ctx_activate(ctx);

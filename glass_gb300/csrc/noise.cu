@@ -263,6 +263,60 @@ __global__ void __launch_bounds__(kNoiseThreads) noise_logl_kernel(NoiseArgs a) 
   if (threadIdx.x == 0) a.partial[(size_t)p * a.nchunks + chunk] = s;
 }
 
+// The one- and two-channel forms: the instrument covariance of
+// generate_instrument_noise_model's case 1 (Michelson X, XYZnoise_FF) and
+// case 2 (A and E, AEnoise_FF; utils/src/glass_lisa.c:1121-1145) on the link
+// levels sacc12 = in[0], soms12 = in[6] (noise/src/glass_noise_model.c:450-461),
+// normalised by 4, plus the foreground's case 1 (Sgal / 4) or case 2
+// (1.5 t Sgal / 4, :635-641), the diagonal inverse and log-determinant
+// (utils/src/glass_math.c:248-258) and noise_log_likelihood's sum
+// (noise/src/glass_noise_model.c:1104-1134).  sin^2(f/f*) is the table's
+// -8 sin^2 times -1/8 (exact).
+__global__ void __launch_bounds__(kNoiseThreads) noise_ch12_kernel(NoiseArgs a, int nch) {
+  __shared__ double red[kNoiseThreads / 32];
+  const int chunk = blockIdx.x, p = blockIdx.y;
+  const double *in = a.inst + 12 * (size_t)p;
+  const bool gal = a.sgal != nullptr;
+  double Amp = 0, f1 = 0, alpha = 0, fk = 0, f2 = 0;
+  if (gal) noise_gal_params(a.sgal + 5 * (size_t)p, Amp, f1, alpha, fk, f2);
+  const double sacc12 = in[0], soms12 = in[6];
+  const int N = a.N;
+  const double *F = a.tab + (size_t)kTabF * N, *COSX = a.tab + (size_t)kTabCosx * N;
+  const double *TDI = a.tab + (size_t)kTabTdi * N, *ACC = a.tab + (size_t)kTabAcc * N;
+  const double *OMS = a.tab + (size_t)kTabOms * N, *TG = a.tab + (size_t)kTabTgal * N;
+  const double *P73 = a.tab + (size_t)kTabFp73 * N, *C2X = a.tab + (size_t)kTabCos2x * N;
+  const double *P0 = a.tab + (size_t)kTabP0 * N, *P1 = a.tab + (size_t)kTabP1 * N;
+  double acc = 0.0;
+#pragma unroll 1
+  for (int r = 0; r < kNoiseBinsPerThread; r++) {
+    const int n = chunk * kNoiseChunk + r * kNoiseThreads + threadIdx.x;
+    if (n >= N) break;
+    const double f = F[n];
+    double c = 0.0;
+    if (f != 0.0) {
+      const double cosx = COSX[n], sx2 = TDI[n] * -0.125;
+      const double Spm = sacc12 * ACC[n], Sop = soms12 * OMS[n];
+      c = (nch == 1) ? 16. * sx2 * (2. * (1.0 + cosx * cosx) * Spm + Sop)
+                     : 8. * sx2 * (2. * Spm * (3. + 2. * cosx + C2X[n]) + Sop * (2. + cosx));
+      c = c / 4.0;
+      if (gal) {
+        const double Sgal = noise_sgal(f, P73[n], Amp, f1, alpha, fk, f2);
+        c += (nch == 1 ? Sgal : 1.5 * TG[n] * Sgal) / 4.0;
+      }
+    }
+    const double ic = 1. / c;
+    double l = -0.5 * (2.0 * (P0[n] * ic));
+    double ld = log(c);
+    if (nch == 2) {
+      l -= 0.5 * (2.0 * (P1[n] * ic));
+      ld += log(c);
+    }
+    acc += l - ld;
+  }
+  const double s = block_sum(acc, red);
+  if (threadIdx.x == 0) a.partial[(size_t)p * a.nchunks + chunk] = s;
+}
+
 // Per model: the chunks' sums in order, and the constant -3 N log(2 pi).
 __global__ void noise_finish_kernel(const double *partial, int nchunks, int nprop, double cst, double *logl) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -587,6 +641,18 @@ static void noise_freq_rows(double f, double *tab, int N, int n) {
   }
 }
 
+void noise_build_table_ch(double T, double fmin, int N, int nch, const double *d0, const double *d1, double *tab) {
+  const double fstar = kCLIGHT / (2.0 * M_PI * kLARM);
+  for (int n = 0; n < N; n++) {
+    const double f = fmin + (double)n / T;
+    noise_freq_rows(f, tab, N, n);
+    tab[(size_t)kTabCos2x * N + n] = cos(2. * (f / fstar));  // AEnoise_FF's cos 2x
+    tab[(size_t)kTabP0 * N + n] = d0[2 * n] * d0[2 * n] + d0[2 * n + 1] * d0[2 * n + 1];
+    tab[(size_t)kTabP1 * N + n] = nch == 2 ? d1[2 * n] * d1[2 * n] + d1[2 * n + 1] * d1[2 * n + 1] : 0.0;
+    for (int r = kTabXY; r <= kTabYZ; r++) tab[(size_t)r * N + n] = 0.0;
+  }
+}
+
 void noise_wv_build(int NT, double df, int lmin, int Nlayer, int Q, const double *X, const double *Y, const double *Z,
                     double *tab, double *P) {
   const int Nc = NT / Q;
@@ -813,12 +879,15 @@ cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst,
     s.sgal = sgal ? sgal + 5 * (size_t)p0 : nullptr;
     s.sgwb = sgwb ? sgwb + 4 * (size_t)p0 : nullptr;
     s.partial = nd.partial + (size_t)p0 * a.nchunks;
-    noise_logl_kernel<<<dim3(a.nchunks, np), kNoiseThreads, 0, stream>>>(s);
+    if (nd.nch == 3)
+      noise_logl_kernel<<<dim3(a.nchunks, np), kNoiseThreads, 0, stream>>>(s);
+    else
+      noise_ch12_kernel<<<dim3(a.nchunks, np), kNoiseThreads, 0, stream>>>(s, nd.nch);
     launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  const double cst = 3 * nd.N * log(2 * M_PI);
+  const double cst = nd.nch == 3 ? 3 * nd.N * log(2 * M_PI) : 0.0;
   noise_finish_kernel<<<(nprop + 255) / 256, 256, 0, stream>>>(nd.partial, a.nchunks, nprop, cst, logl);
   launches++;
   if (nlaunch) *nlaunch = launches;

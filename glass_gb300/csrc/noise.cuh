@@ -12,8 +12,12 @@ enum {
   kTabF = 0, kTabCosx, kTabTdi, kTabAcc, kTabOms, kTabTgal, kTabFp73,
   kTabXX, kTabYY, kTabZZ, kTabXY, kTabXZ, kTabYZ, kNoiseTabRows
 };
+// One- and two-channel data (Michelson X; or A and E) keep the data's power
+// |X|^2 (or |A|^2, |E|^2) and cos(2 f/f*) in the rows of XX, YY and ZZ.
+enum { kTabP0 = kTabXX, kTabP1 = kTabYY, kTabCos2x = kTabZZ };
 
 struct NoiseDev {
+  int nch = 3;  // 3: X, Y, Z; 1: X; 2: A, E
   int N = 0;
   double T = 0, fmin = 0;
   double *tab = nullptr;      // kNoiseTabRows x N
@@ -23,6 +27,8 @@ struct NoiseDev {
 };
 
 void noise_build_table(double T, double fmin, int N, const double *X, const double *Y, const double *Z, double *tab);
+// The same table for one channel (d0 = X) or two (d0, d1 = A, E).
+void noise_build_table_ch(double T, double fmin, int N, int nch, const double *d0, const double *d1, double *tab);
 
 // Wavelet-domain form (coarse-grained): layers lmin .. lmin + Nlayer - 1 of an
 // NF x NT grid of layer width df, cells of Q pixels in time.
@@ -76,7 +82,9 @@ cudaError_t spline_noise_launch(const SplineNoiseDev &s, int nprop, int kmax, co
 int noise_chunks(int N);
 // logl[p] for noise models inst[12 p ..] (sacc[6], soms[6]) and sgal[5 p ..]
 // (or null: instrument only), plus, with sgwb[4 p ..] (or null), the SGWB of
-// template sg_type; nd.partial must hold nprop x noise_chunks(N).
+// template sg_type (three channels only); nd.partial must hold nprop x
+// noise_chunks(N).  Three channels: my_noise_log_likelihood; one or two:
+// noise_log_likelihood (no 2 pi constant), link levels sacc[0], soms[0].
 cudaError_t noise_logl_launch(const NoiseDev &nd, int nprop, const double *inst, const double *sgal, int sg_type,
                               const double *sgwb, double *logl, cudaStream_t stream, int *nlaunch);
 

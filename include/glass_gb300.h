@@ -361,6 +361,23 @@ int glass_gpu_noise_logl_batch_host(glass_gpu_ctx *ctx, int nprop, const double 
  * forms without _sgwb are these with sgwb = NULL.
  */
 int glass_gpu_noise_sgwb_setup(glass_gpu_ctx *ctx, int type, int nresp, const double *resp);
+
+/*
+ * One- and two-channel data for the same batched likelihood:
+ * nchannel 1 (d0 = Michelson X) or 2 (d0, d1 = A, E), 2 NFFT interleaved
+ * doubles each, on the bins qmin/T + n/T (qmin >= 1); nchannel 3 is
+ * glass_gpu_noise_setup(d0, d1, d2).  With one or two channels
+ * glass_gpu_noise_logl_batch[_host] gives noise_log_likelihood
+ * (noise/src/glass_noise_model.c:1104-1134) of the covariance of
+ * generate_instrument_noise_model's case 1 / case 2 (:450-461: XYZnoise_FF or
+ * AEnoise_FF of the link levels sacc[0], soms[0]; the other ten link levels
+ * are not read) plus, with sgal, the foreground's case 1 / case 2 (:635-641),
+ * diagonal inverse (utils/src/glass_math.c:248-258); no 2 pi constant.  The
+ * SGWB covariance is three-channel only (GLASS_ERR_ARG otherwise, where
+ * generate_sgwb_model stops).
+ */
+int glass_gpu_noise_setup_channels(glass_gpu_ctx *ctx, int nchannel, double T, int qmin, int NFFT, const double *d0,
+                                   const double *d1, const double *d2);
 int glass_gpu_noise_logl_batch_sgwb(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,
                                     const double *sgwb, double *logl);
 int glass_gpu_noise_logl_batch_sgwb_host(glass_gpu_ctx *ctx, int nprop, const double *inst, const double *sgal,

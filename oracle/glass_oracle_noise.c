@@ -99,6 +99,69 @@ static void orc_noise_cov_bin(double f, const double *sacc, const double *soms, 
     }
 }
 
+/* ------------------------------------------- one- and two-channel forms */
+/* The instrument covariance of generate_instrument_noise_model's case 1
+ * (Michelson X: XYZnoise_FF) and case 2 (A, E: AEnoise_FF;
+ * utils/src/glass_lisa.c:1121-1145) with the link levels sacc12, soms12
+ * (noise/src/glass_noise_model.c:450-461), normalised by 4; plus the
+ * foreground's case 1 / case 2 (:635-641) added as
+ * generate_full_covariance_matrix does; the diagonal inverse
+ * (invert_noise_covariance_matrix, utils/src/glass_math.c:248-258) and
+ * noise_log_likelihood (noise/src/glass_noise_model.c:1104-1134).  d0 = X
+ * (one channel) or A, d1 = E; 2 N doubles each; f = fmin + n/T > 0. */
+double orc_noise_logl_ch(int nch, double T, double fmin, int N, const double *d0, const double *d1,
+                         const double *sacc, const double *soms, const double *sgal)
+{
+    const double fstar = ORC_CLIGHT / (2.0 * M_PI * ORC_LARM);
+    const double acc_units = 2.81837551648e-19;
+    const double oms_units = 4.39256635604e-16;
+    const double acc_fmax = 0.01;
+    double Amp = 0, f1 = 0, alpha = 0, fk = 0, f2g = 0;
+    if (sgal) {
+        Amp = exp(sgal[0]); f1 = exp(sgal[1]); alpha = sgal[2]; fk = exp(sgal[3]); f2g = exp(sgal[4]);
+    }
+    double *C = malloc(sizeof(double) * (size_t)N);
+    for (int n = 0; n < N; n++) {
+        double f = fmin + (double)n / T;
+        double x = f / fstar, f2 = f * f;
+        double acc_tf = (f < acc_fmax) ? acc_units / f2 * (1.0 + pow(0.4e-3 / f, 2)) * (1.0 + pow(f / 8.0e-3, 4)) : 0.0;
+        double oms_tf = oms_units * f2 * (1.0 + pow(2.0e-3 / f, 4));
+        double Spm = sacc[0] * acc_tf, Sop = soms[0] * oms_tf;
+        double cosx = cos(x), c;
+        if (nch == 1)
+            c = 16. * orc_noise_transfer_function(x) * (2. * (1.0 + cosx * cosx) * Spm + Sop);
+        else
+            c = 8. * orc_noise_transfer_function(x) * (2. * Spm * (3. + 2. * cosx + cos(2. * x)) + Sop * (2. + cosx));
+        c /= 4.0;
+        if (sgal) {
+            double fs = ORC_CLIGHT / (ORC_PI2 * ORC_LARM);
+            double xg = f / fs;
+            double t = 4. * xg * xg * sin(xg) * sin(xg);
+            double Sgal = (f > f1 * 10) ? 0.0 : orc_galaxy_foreground(f, Amp, f1, alpha, fk, f2g);
+            c += (nch == 1 ? Sgal : 1.5 * t * Sgal) / 4.0;
+        }
+        C[n] = c;
+    }
+    double logL = 0.0;
+    for (int ch = 0; ch < nch; ch++) {
+        const double *d = ch == 0 ? d0 : d1;
+        double arg = 0.0;
+        for (int n = 0; n < N; n++) arg += (d[2 * n] * d[2 * n] + d[2 * n + 1] * d[2 * n + 1]) * (1. / C[n]);
+        logL += -0.5 * (2.0 * arg);
+    }
+    for (int n = 0; n < N; n++) logL -= (nch == 2) ? log(C[n]) + log(C[n]) : log(C[n]);
+    free(C);
+    return logL;
+}
+
+void orc_noise_logl_ch_batch(int nch, double T, double fmin, int N, const double *d0, const double *d1, int nprop,
+                             const double *inst, const double *sgal, double *logl)
+{
+    for (int p = 0; p < nprop; p++)
+        logl[p] = orc_noise_logl_ch(nch, T, fmin, N, d0, d1, inst + 12 * (size_t)p, inst + 12 * (size_t)p + 6,
+                                    sgal ? sgal + 5 * (size_t)p : NULL);
+}
+
 /* ------------------------------------------------------- natural splines */
 /* spline_coefficients (utils/src/glass_math.c:98-178): natural cubic spline
  * through (x[i], y[i]), i < n, coefficients c0..c3 of interval i. */

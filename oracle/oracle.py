@@ -288,6 +288,21 @@ class Port:
                                               _p(r), _p(out), nthreads)
         return out
 
+    def noise_logl_channels(self, T, fmin, d, inst, sgal=None):
+        """noise_log_likelihood of the one-channel (d [1, 2 NFFT] = X) or
+        two-channel (d [2, 2 NFFT] = A, E) instrument (+ foreground) model for
+        each row of inst [n, 12] (sacc[0], soms[0] used), sgal [n, 5] or None."""
+        lib = self.lib
+        lib.orc_noise_logl_ch_batch.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _D, _D,
+                                                ctypes.c_int, _D, _D, _D]
+        d = np.ascontiguousarray(d, np.float64)
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        out = np.zeros(len(inst))
+        lib.orc_noise_logl_ch_batch(d.shape[0], T, fmin, d.shape[1] // 2, _p(d[0]), _p(d[-1]), len(inst), _p(inst),
+                                    _p(sg) if sg is not None else None, _p(out))
+        return out
+
     def spline_noise_logl(self, T, fmin, d, transfer, nknots, knot_f, knot_C):
         """The spline noise model's noise_log_likelihood for each model: d [nch, 2 NFFT]
         (X; or A, E), knot_f [n, kmax], knot_C [n, nch, kmax], nknots [n]."""
@@ -822,6 +837,20 @@ class Ref:
                                         _p(md) if md is not None else None, len(inst), _p(inst),
                                         _p(sg) if sg is not None else None, int(sgwb_type), _p(b), len(r), _p(r),
                                         _p(out))
+        return out
+
+    def noise_logl_channels(self, T, fmin, d, inst, sgal=None):
+        """The reference's one- or two-channel instrument (+ foreground)
+        covariance, inverse and noise_log_likelihood for each noise model."""
+        lib = self.lib
+        lib.ref_noise_logl_channels.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _D, _D,
+                                                ctypes.c_int, _D, _D, _D]
+        d = np.ascontiguousarray(d, np.float64)
+        inst = np.ascontiguousarray(inst, np.float64).reshape(-1, 12)
+        sg = None if sgal is None else np.ascontiguousarray(sgal, np.float64).reshape(-1, 5)
+        out = np.zeros(len(inst))
+        lib.ref_noise_logl_channels(d.shape[0], T, fmin, d.shape[1] // 2, _p(d[0]), _p(d[-1]), len(inst), _p(inst),
+                                    _p(sg) if sg is not None else None, _p(out))
         return out
 
     def spline_noise_logl(self, T, fmin, d, transfer, nknots, knot_f, knot_C):

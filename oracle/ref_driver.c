@@ -629,6 +629,65 @@ void ref_noise_logl(double T, double fmin, int NFFT, const double *X, const doub
     free(data);
 }
 
+/* ref_noise_logl for one channel (d0 = X) or two (d0, d1 = A, E): the
+ * reference's instrument (+ foreground) covariance with Nchannel 1 or 2,
+ * invert_noise_covariance_matrix and noise_log_likelihood. */
+void ref_noise_logl_channels(int nch, double T, double fmin, int NFFT, const double *d0, const double *d1, int n,
+                             const double *inst, const double *sgal, double *logl)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->NFFT = NFFT;
+    data->N = 2 * NFFT;
+    data->Nchannel = nch;
+    data->Nlayer = 1;
+    data->T = T;
+    data->fmin = fmin;
+    strcpy(data->basis, "fourier");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, nch);
+    if (nch == 1) {
+        memcpy(data->tdi->X, d0, sizeof(double) * data->N);
+    } else {
+        memcpy(data->tdi->A, d0, sizeof(double) * data->N);
+        memcpy(data->tdi->E, d1, sizeof(double) * data->N);
+    }
+    struct InstrumentModel inst_model;
+    memset(&inst_model, 0, sizeof(inst_model));
+    alloc_instrument_model(&inst_model, NFFT, 1, nch);
+    for (int k = 0; k < NFFT; k++) inst_model.psd->f[k] = data->fmin + (double)k / data->T;
+    struct ForegroundModel gal;
+    memset(&gal, 0, sizeof(gal));
+    alloc_foreground_model(&gal, NFFT, 1, nch);
+    for (int k = 0; k < NFFT; k++) gal.psd->f[k] = data->fmin + (double)k / data->T;
+    struct Noise *psd = malloc(sizeof(struct Noise));
+    alloc_noise(psd, NFFT, 1, nch);
+    for (int p = 0; p < n; p++) {
+        for (int l = 0; l < 6; l++) {
+            inst_model.sacc[l] = inst[12 * p + l];
+            inst_model.soms[l] = inst[12 * p + 6 + l];
+        }
+        generate_instrument_noise_model(&orbit, &inst_model);
+        copy_Cij(inst_model.psd->C, psd->C, psd->Nchannel, psd->N);
+        if (sgal) {
+            for (int q = 0; q < 5; q++) gal.sgal[q] = sgal[5 * p + q];
+            generate_galactic_foreground_model(&gal);
+            generate_full_covariance_matrix(psd, gal.psd, nch);
+        }
+        invert_noise_covariance_matrix(psd);
+        logl[p] = noise_log_likelihood(data, psd);
+    }
+    free_noise(psd);
+    free_noise(inst_model.psd);
+    free(inst_model.sacc);
+    free(inst_model.soms);
+    free_noise(gal.psd);
+    free(gal.sgal);
+    free_tdi(data->tdi);
+    free(data);
+}
+
 /* The noise module's coarse-grained wavelet likelihood for n noise models on
  * layers lmin .. lmin + Nlayer - 1 of an NF x NT grid (pixel dt, layer df):
  * coarse_grain_wavelet_data (noise/src/glass_noise_model.c:1057) of the

@@ -615,10 +615,42 @@ def spline_noise(ref, rng):
     np.savez_compressed(os.path.join(HERE, "spline_noise.npz"), **out)
 
 
+def noise_channels(ref, rng):
+    """The noise module's one- and two-channel instrument (+ foreground)
+    models (generate_instrument_noise_model's case 1 and case 2,
+    generate_galactic_foreground_model's case 1 and 2, noise_log_likelihood):
+    Michelson X and A/E data drawn from the three-channel model's X and A/E
+    covariance, at 0.1 mHz (acceleration noise on), 2 mHz and 12 mHz (above
+    the acceleration cut), six models each around the starting point, with
+    and without the foreground."""
+    from oracle import Port
+
+    port = Port()
+    inst0, sgal0 = wl.default_noise_params(T)
+    out = {}
+    for c, (q, N) in enumerate(((int(1e-4 * T), 512), (int(2e-3 * T), 1000), (int(12e-3 * T), 512))):
+        C6 = port.noise_covariance(T, q / T, N, inst0, sgal0)
+        xx, yy, zz, xy, xz, yz = C6.T
+        var = {1: [xx], 2: [(zz + xx - 2 * xz) / 2, (xx + 4 * yy + zz - 4 * xy + 2 * xz - 4 * yz) / 6]}
+        for nch in (1, 2):
+            d = np.empty((nch, 2 * N))
+            for k in range(nch):
+                sd = np.sqrt(0.5 * var[nch][k])
+                d[k, 0::2] = rng.standard_normal(N) * sd
+                d[k, 1::2] = rng.standard_normal(N) * sd
+            inst = inst0 * np.exp(rng.uniform(-0.3, 0.3, (6, 12)))
+            sgal = sgal0 + rng.uniform(-0.2, 0.2, (6, 5))
+            key = f"c{c}_n{nch}"
+            out[f"{key}_qmin"], out[f"{key}_d"], out[f"{key}_inst"], out[f"{key}_sgal"] = q, d, inst, sgal
+            out[f"{key}_logl"] = ref.noise_logl_channels(T, q / T, d, inst, sgal)
+            out[f"{key}_logl_inst"] = ref.noise_logl_channels(T, q / T, d, inst, None)
+    np.savez_compressed(os.path.join(HERE, "noise_channels.npz"), **out)
+
+
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
              "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210,
              "fisher_wavelet": 20261211, "priors": 20261212, "sgwb": 20261213,
-             "spline_noise": 20261214}
+             "spline_noise": 20261214, "noise_channels": 20261215}
 
 
 def main(names=()):
@@ -646,6 +678,7 @@ def main(names=()):
     priors(ref, np.random.default_rng(OWN_SEEDS["priors"]))
     sgwb(ref, np.random.default_rng(OWN_SEEDS["sgwb"]))
     spline_noise(ref, np.random.default_rng(OWN_SEEDS["spline_noise"]))
+    noise_channels(ref, np.random.default_rng(OWN_SEEDS["noise_channels"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))
