@@ -64,7 +64,7 @@ EXPORTS = (
     "glass_gpu_noise_wavelet_logl_batch_sgwb", "glass_gpu_noise_wavelet_logl_batch_sgwb_host",
     "glass_gpu_checked_build", "glass_gpu_check_status",
     "glass_gpu_spline_noise_setup", "glass_gpu_spline_noise_logl_batch", "glass_gpu_spline_noise_logl_batch_host",
-    "glass_gpu_noise_setup_channels",
+    "glass_gpu_noise_setup_channels", "glass_gpu_rj_propose", "glass_gpu_rj_accept",
 )
 
 _lib = None
@@ -72,6 +72,15 @@ _lib = None
 
 class GlassError(RuntimeError):
     pass
+
+
+class FstatGrid(ctypes.Structure):
+    """glass_gpu_fstat_grid: the F-statistic proposal's density grid (device
+    tensor) for the trans-dimensional step's F-statistic draw."""
+    _fields_ = [("tensor", ctypes.c_void_p), ("n_f", ctypes.c_int), ("n_theta", ctypes.c_int),
+                ("n_phi", ctypes.c_int), ("d_f", ctypes.c_double), ("d_theta", ctypes.c_double),
+                ("d_phi", ctypes.c_double), ("maxp", ctypes.c_double), ("qmin", ctypes.c_int),
+                ("T", ctypes.c_double)]
 
 
 def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
@@ -147,6 +156,11 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_noise_wavelet_logl_batch_host.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D, _D, _D]
     lib.glass_gpu_noise_sgwb_setup.argtypes = [_V, ctypes.c_int, ctypes.c_int, _D]
     lib.glass_gpu_check_status.argtypes = [_V, ctypes.POINTER(ctypes.c_uint)]
+    lib.glass_gpu_rj_propose.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V, ctypes.c_int, _V, _D,
+                                         ctypes.POINTER(FstatGrid)] + [_V] * 9
+    lib.glass_gpu_rj_accept.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 12 + [
+        ctypes.c_int, ctypes.c_int, _V, ctypes.c_int, _V, _V, ctypes.c_double, ctypes.c_double, ctypes.c_int, _V, _V,
+        _V]
     lib.glass_gpu_noise_setup_channels.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D,
                                                    _D, _D]
     lib.glass_gpu_spline_noise_setup.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D,
@@ -600,6 +614,49 @@ class Engine:
         n = int(params.numel() // 8)
         _check(self.lib.glass_gpu_ucb_prior(self._ctx, n, _ptr(params), _ptr(prior), int(per_chain), _ptr(logPV),
                                             _ptr(skyhist), float(dcostheta), float(dphi), int(nphi), _ptr(logP)))
+
+    @staticmethod
+    def fstat_grid(tensor, d_f, d_theta, d_phi, maxp, qmin, T):
+        """The F-statistic draw's grid: tensor a device array [n_f, n_theta, n_phi]."""
+        g = FstatGrid(ctypes.c_void_p(tensor.data_ptr()), int(tensor.shape[0]), int(tensor.shape[1]),
+                      int(tensor.shape[2]), float(d_f), float(d_theta), float(d_phi), float(maxp), int(qmin), float(T))
+        g._keep = tensor
+        return g
+
+    def rj_propose_device(self, Nlive, Neff, src, prior, logPV, rjweight, grid, seed, per_chain=False):
+        """The birth/death proposal of ucb_rjmcmc (glass_gpu_rj_propose) for n
+        chains: device tensors Nlive, Neff (int32 [n]), src [n, maxsrc, 8],
+        seed [n] (advanced); rjweight 9 host floats; grid from fstat_grid (or
+        None).  Returns device tensors (move, slot, kind, params_y, logQxy,
+        logQyx, logPy, status)."""
+        import torch
+
+        n, maxsrc = int(src.shape[0]), int(src.shape[1])
+        dev = src.device
+        move, slot, kind, status = (torch.empty(n, dtype=torch.int32, device=dev) for _ in range(4))
+        y = torch.empty((n, 8), dtype=torch.float64, device=dev)
+        qxy, qyx, lpy = (torch.empty(n, dtype=torch.float64, device=dev) for _ in range(3))
+        w = np.ascontiguousarray(rjweight, np.float64)
+        _check(self.lib.glass_gpu_rj_propose(self._ctx, n, maxsrc, _ptr(Nlive), _ptr(Neff), _ptr(src), _ptr(prior),
+                                             int(per_chain), _ptr(logPV), _pd(w),
+                                             ctypes.byref(grid) if grid is not None else None, _ptr(seed), _ptr(move),
+                                             _ptr(slot), _ptr(kind), _ptr(y), _ptr(qxy), _ptr(qyx), _ptr(lpy),
+                                             _ptr(status)))
+        return move, slot, kind, y, qxy, qyx, lpy, status
+
+    def rj_accept_device(self, Nlive, src, proposal, temperature, dlogl, hh, prior, logPV, seed, logL_x,
+                         dlogl_is_term=False, prior_only=False, per_chain=False, skyhist=None, dcostheta=0.0,
+                         dphi=0.0, nphi=0, accepted=None):
+        """The acceptance half of ucb_rjmcmc (glass_gpu_rj_accept) on the
+        proposal rj_propose_device returned; Nlive, src, seed and logL_x are
+        updated in place."""
+        move, slot, _, y, qxy, qyx, lpy = proposal[:7]
+        n, maxsrc = int(src.shape[0]), int(src.shape[1])
+        _check(self.lib.glass_gpu_rj_accept(self._ctx, n, maxsrc, _ptr(Nlive), _ptr(src), _ptr(move), _ptr(slot),
+                                            _ptr(y), _ptr(qxy), _ptr(qyx), _ptr(lpy), _ptr(temperature), _ptr(dlogl),
+                                            _ptr(hh), int(dlogl_is_term), int(prior_only), _ptr(prior),
+                                            int(per_chain), _ptr(logPV), _ptr(skyhist), float(dcostheta), float(dphi),
+                                            int(nphi), _ptr(seed), _ptr(logL_x), _ptr(accepted)))
 
     def fisher_draw_device(self, params_x, evec, evalue, seed, params_y, logQ=None, status=None):
         """draw_from_fisher for n chains (device tensors: params_x/params_y [n, 8],

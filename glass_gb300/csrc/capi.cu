@@ -1689,6 +1689,114 @@ extern "C" int glass_gpu_ucb_prior(glass_gpu_ctx *ctx, int n, double *params, co
   return GLASS_OK;
 }
 
+// ------------------------------------------- trans-dimensional (RJ) step
+extern "C" int glass_gpu_rj_propose(glass_gpu_ctx *ctx, int n, int maxsrc, const int *Nlive, const int *Neff,
+                                    const double *src, const double *prior, int prior_stride, const double *logPV,
+                                    const double *rjweight, const glass_gpu_fstat_grid *grid, unsigned int *seed,
+                                    int *move, int *slot, int *kind, double *params_y, double *logQxy, double *logQyx,
+                                    double *logPy, int *status) {
+  if (!ctx || n < 0 || maxsrc < 1 || (prior_stride != 0 && prior_stride != 1))
+    return set_err(GLASS_ERR_ARG, "rj_propose: bad argument");
+  if (n == 0) return GLASS_OK;
+  if (!Nlive || !Neff || !src || !prior || !logPV || !rjweight || !seed || !move || !slot || !kind || !params_y ||
+      !logQxy || !logQyx || !logPy)
+    return set_err(GLASS_ERR_ARG, "rj_propose: null argument");
+  RjArgs a{};
+  double wsum = 0.0;
+  for (int k = 0; k < 9; k++) {
+    if (!(rjweight[k] >= 0.0 && rjweight[k] <= 1.0)) return set_err(GLASS_ERR_ARG, "rj_propose: rj weights are 0 .. 1");
+    if (k >= 2 && rjweight[k] > 0.0)
+      return set_err(GLASS_ERR_ARG, "rj_propose: only the prior (0) and F-statistic (1) draws run on the device");
+    a.rjw[k] = rjweight[k];
+    wsum += rjweight[k];
+  }
+  if (!(wsum > 0.0)) return set_err(GLASS_ERR_ARG, "rj_propose: every rj weight is 0");
+  if (rjweight[1] > 0.0) {
+    if (!grid || !grid->tensor || grid->n_f < 1 || grid->n_theta < 1 || grid->n_phi < 1 || !(grid->maxp > 0) ||
+        !(grid->d_f > 0) || !(grid->d_theta > 0) || !(grid->d_phi > 0) || !(grid->T > 0))
+      return set_err(GLASS_ERR_ARG, "rj_propose: the F-statistic draw needs its grid");
+    a.tensor = grid->tensor;
+    a.n_f = grid->n_f;
+    a.n_theta = grid->n_theta;
+    a.n_phi = grid->n_phi;
+    a.qmin = grid->qmin;
+    a.d_f = grid->d_f;
+    a.d_theta = grid->d_theta;
+    a.d_phi = grid->d_phi;
+    a.maxp = grid->maxp;
+    a.T = grid->T;
+  }
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  a.n = n;
+  a.maxsrc = maxsrc;
+  a.Nlive = const_cast<int *>(Nlive);
+  a.Neff = Neff;
+  a.src = const_cast<double *>(src);
+  a.prior = prior;
+  a.logPV = logPV;
+  a.stride = prior_stride;
+  a.seed = seed;
+  a.move = move;
+  a.slot = slot;
+  a.kind = kind;
+  a.status = status;
+  a.params_y = params_y;
+  a.logQxy = logQxy;
+  a.logQyx = logQyx;
+  a.logPy = logPy;
+  GLASS_CUDA(rj_propose_launch(a, ctx->stream), "rj_propose");
+  ctx->last_launches = 1;
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_rj_accept(glass_gpu_ctx *ctx, int n, int maxsrc, int *Nlive, double *src, const int *move,
+                                   const int *slot, double *params_y, const double *logQxy, const double *logQyx,
+                                   const double *logPy, const double *temperature, const double *dlogl,
+                                   const double *hh, int dlogl_is_term, int prior_only, const double *prior,
+                                   int prior_stride, const double *logPV, const double *skyhist, double dcostheta,
+                                   double dphi, int nphi, unsigned int *seed, double *logL_x, int *accepted) {
+  if (!ctx || n < 0 || maxsrc < 1 || (prior_stride != 0 && prior_stride != 1))
+    return set_err(GLASS_ERR_ARG, "rj_accept: bad argument");
+  if (n == 0) return GLASS_OK;
+  if (!Nlive || !src || !move || !slot || !params_y || !logQxy || !logQyx || !logPy || !temperature || !dlogl ||
+      !prior || !logPV || !seed || !logL_x)
+    return set_err(GLASS_ERR_ARG, "rj_accept: null argument");
+  if (dlogl_is_term && !hh) return set_err(GLASS_ERR_ARG, "rj_accept: a death's change from its term needs hh");
+  if (skyhist && !(dcostheta > 0 && dphi > 0 && nphi > 0)) return set_err(GLASS_ERR_ARG, "rj_accept: bad sky grid");
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  RjArgs a{};
+  a.n = n;
+  a.maxsrc = maxsrc;
+  a.Nlive = Nlive;
+  a.src = src;
+  a.move = const_cast<int *>(move);
+  a.slot = const_cast<int *>(slot);
+  a.params_y = params_y;
+  a.logQxy = const_cast<double *>(logQxy);
+  a.logQyx = const_cast<double *>(logQyx);
+  a.logPy = const_cast<double *>(logPy);
+  a.T_chain = temperature;
+  a.dlogl = dlogl;
+  a.hh = hh;
+  a.dlogl_is_term = dlogl_is_term ? 1 : 0;
+  a.prior_only = prior_only ? 1 : 0;
+  a.prior = prior;
+  a.logPV = logPV;
+  a.stride = prior_stride;
+  a.skyhist = skyhist;
+  a.dcostheta = dcostheta;
+  a.dphi = dphi;
+  a.nphi = nphi;
+  a.seed = seed;
+  a.logL_x = logL_x;
+  a.accepted = accepted;
+  GLASS_CUDA(rj_accept_launch(a, ctx->stream), "rj_accept");
+  ctx->last_launches = 1;
+  return GLASS_OK;
+}
+
 // ------------------------------------------------------- drop-in functions
 // Layout of struct Orbit (utils/src/glass_lisa.h:60-109), restated so the
 // drop-in ucb_waveform can read the arm length, transfer frequency and the

@@ -339,104 +339,303 @@ __global__ void __launch_bounds__(32) sym_eigen8_kernel(int n, const double *mat
   }
 }
 
-// draw_from_uniform_prior (utils/src/glass_sampler.c:96-107), one thread per
-// chain: the eight parameters from rand_r_U_0_1 in order, logQ = -sum of the
-// log prior volumes.
+
+// ---------------------------------------------------------------- priors
+// The reference's prior pieces on one parameter set p[8] with bounds pr[16]
+// and log prior volumes lv[8]; each wraps p in place where the reference does,
+// and each sums in the reference's own order.
+constexpr double kTwoPi = 6.283185307179586;
+
+// check_range (ucb/src/glass_ucb_prior.c:400-438): true when p is outside the
+// prior (or NaN); longitude, polarisation and phase are wrapped in place (the
+// wrapping loops stop after 64 turns, the reference's do not).
+__device__ bool prior_check_range(double *p, const double *pr) {
+  for (int k = 0; k < 8; k++)
+    if (p[k] != p[k]) return true;
+  if (p[0] < pr[0] || p[0] > pr[1]) return true;
+  if (p[1] < pr[2] || p[1] > pr[3]) return true;
+  if (p[2] < pr[4] || p[2] >= pr[5]) {
+    p[2] = atan2(sin(p[2]), cos(p[2]));
+    if (p[2] < 0.0) p[2] += kTwoPi;
+  }
+  if (p[3] < pr[6] || p[3] > pr[7]) return true;
+  if (p[4] < pr[8] || p[4] > pr[9]) return true;
+  for (int it = 0; it < 64 && p[5] < pr[10]; it++) p[5] += M_PI;
+  for (int it = 0; it < 64 && p[5] > pr[11]; it++) p[5] -= M_PI;
+  for (int it = 0; it < 64 && p[6] < pr[12]; it++) p[6] += kTwoPi;
+  for (int it = 0; it < 64 && p[6] > pr[13]; it++) p[6] -= kTwoPi;
+  if (p[7] < pr[14] || p[7] > pr[15]) return true;
+  return false;
+}
+
+// evalaute_sky_location_prior (ucb/src/glass_ucb_prior.c:590-639): the galaxy
+// histogram skyhist[i nphi + j] when given, else the uniform sky.
+__device__ double prior_sky(double *p, const double *pr, const double *lv, const double *skyhist, double dcostheta,
+                            double dphi, int nphi) {
+  double logP = 0.0;
+  if (skyhist) {
+    if (p[1] < pr[2] || p[1] > pr[3]) return -INFINITY;
+    if (pr[4] > 0.0 || pr[5] < kTwoPi) {
+      if (p[2] < pr[4] || p[2] > pr[5]) return -INFINITY;
+    } else {
+      for (int it = 0; it < 64 && p[2] < 0; it++) p[2] += kTwoPi;
+      for (int it = 0; it < 64 && p[2] > kTwoPi; it++) p[2] -= kTwoPi;
+    }
+    const int ci = (int)floor((p[1] - pr[2]) / dcostheta);
+    const int cj = (int)floor((p[2] - pr[4]) / dphi);
+    logP += skyhist[ci * nphi + cj];
+  } else {
+    if (p[1] < pr[2] || p[1] > pr[3]) return -INFINITY;
+    logP -= lv[1];
+    if (pr[4] > 0.0 || pr[5] < kTwoPi) {
+      if (p[2] < pr[4] || p[2] > pr[5]) return -INFINITY;
+    } else if (p[2] < pr[4] || p[2] >= pr[5]) {
+      p[2] = atan2(sin(p[2]), cos(p[2]));
+      if (p[2] < 0.0) p[2] += kTwoPi;
+    }
+    logP -= lv[2];
+  }
+  return logP;
+}
+
+// evaluate_uniform_priors (ucb/src/glass_ucb_prior.c:560-588)
+__device__ double prior_uniform(double *p, const double *pr, const double *lv) {
+  if (prior_check_range(p, pr)) return -INFINITY;
+  double logP = 0.0;
+  logP -= log(pr[1] - pr[0]);
+  logP -= lv[3];
+  logP -= lv[4];
+  logP -= lv[5];
+  logP -= lv[6];
+  logP -= lv[7];
+  return logP;
+}
+
+// evaluate_ucb_prior (ucb/src/glass_ucb_prior.c:536-556) on the blind-search
+// path (no catalogue prior)
+__device__ double prior_ucb(double *p, const double *pr, const double *lv, const double *skyhist, double dcostheta,
+                            double dphi, int nphi) {
+  if (prior_check_range(p, pr)) return -INFINITY;
+  double logP = 0.0;
+  logP += prior_sky(p, pr, lv, skyhist, dcostheta, dphi, nphi);
+  logP += prior_uniform(p, pr, lv);
+  return logP;
+}
+
+// draw_from_uniform_prior (utils/src/glass_sampler.c:96-107)
+__device__ double prior_draw(double *p, const double *pr, const double *lv, unsigned int *s) {
+  double logQ = 0.0;
+  for (int k = 0; k < 8; k++) {
+    p[k] = pr[2 * k] + glass_u01(s) * (pr[2 * k + 1] - pr[2 * k]);
+    logQ -= lv[k];
+  }
+  return logQ;
+}
+
+__global__ void ucb_prior_kernel(PriorArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double *pr = a.prior + 16 * (size_t)i * a.stride;
+  const double *lv = a.logPV + 8 * (size_t)i * a.stride;
+  a.out[i] = prior_ucb(a.params + 8 * (size_t)i, pr, lv, a.skyhist, a.dcostheta, a.dphi, a.nphi);
+}
+
+// draw_from_uniform_prior, one thread per chain: the eight parameters from
+// rand_r_U_0_1 in order, logQ = -sum of the log prior volumes.
 __global__ void prior_draw_kernel(PriorArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const double *pr = a.prior + 16 * (size_t)i * a.stride;
   const double *lv = a.logPV + 8 * (size_t)i * a.stride;
   unsigned int s = a.seed[i];
-  double logQ = 0.0;
-  for (int k = 0; k < 8; k++) {
-    a.params[8 * (size_t)i + k] = pr[2 * k] + glass_u01(&s) * (pr[2 * k + 1] - pr[2 * k]);
-    logQ -= lv[k];
-  }
+  a.out[i] = prior_draw(a.params + 8 * (size_t)i, pr, lv, &s);
   a.seed[i] = s;
-  a.out[i] = logQ;
 }
 
-// evaluate_ucb_prior (ucb/src/glass_ucb_prior.c:536-556) on the blind-search
-// path (no catalogue prior): check_range (:400-438, which wraps longitude,
-// polarisation and phase in place), the sky-location prior (:590-639,
-// uniform or the galaxy histogram) and evaluate_uniform_priors (:560-588).
-__global__ void ucb_prior_kernel(PriorArgs a) {
+// ------------------------------------------------- trans-dimensional step
+// The F-statistic proposal's density (evaluate_fstatistic_proposal,
+// ucb/src/glass_ucb_proposal.c:1640-1673): the uniform sky and the uniform
+// priors, plus the log of the grid cell's density.
+__device__ double fstat_density(double *p, const RjArgs &a, const double *pr, const double *lv) {
+  double logP = 0.0;
+  logP += prior_sky(p, pr, lv, nullptr, 1, 1, 1);
+  logP += prior_uniform(p, pr, lv);
+  const int i = (int)floor((p[0] - a.qmin) / (a.d_f * a.T));
+  const int j = (int)floor((p[1] - -1) / a.d_theta);
+  const int k = (int)floor((p[2]) / a.d_phi);
+  if (i < 0 || i >= a.n_f) return -INFINITY;
+  if (j < 0 || j >= a.n_theta) return -INFINITY;
+  if (k < 0 || k >= a.n_phi) return -INFINITY;
+  logP += log(a.tensor[((size_t)i * a.n_theta + j) * a.n_phi + k]);
+  return logP;
+}
+
+// draw_from_fstatistic (ucb/src/glass_ucb_proposal.c:1526-1568): a draw from
+// the prior, then rejection sampling of (f, cos theta, phi) on the grid.  A
+// cell index equal to the grid size (a draw of exactly 1) is taken as the
+// last cell and reported (the reference reads past its grid); the rejection
+// loop stops after kRjMaxTries.
+constexpr int kRjMaxTries = 1 << 20;
+__device__ double fstat_draw(double *p, const RjArgs &a, const double *pr, const double *lv, unsigned int *s,
+                             int *st) {
+  prior_draw(p, pr, lv, s);
+  double q = 0, costheta = 0, phi = 0, pc, alpha;
+  int it = 0;
+  do {
+    const double i = glass_u01(s) * a.n_f;
+    const double j = glass_u01(s) * a.n_theta;
+    const double k = glass_u01(s) * a.n_phi;
+    q = (double)(a.qmin) + i * a.d_f * a.T;
+    costheta = -1. + j * a.d_theta;
+    phi = k * a.d_phi;
+    int ii = (int)i, jj = (int)j, kk = (int)k;
+    if (ii >= a.n_f || jj >= a.n_theta || kk >= a.n_phi) {
+      *st = GLASS_RJ_RNG_EDGE;
+      ii = min(ii, a.n_f - 1);
+      jj = min(jj, a.n_theta - 1);
+      kk = min(kk, a.n_phi - 1);
+    }
+    pc = a.tensor[((size_t)ii * a.n_theta + jj) * a.n_phi + kk];
+    alpha = glass_u01(s) * a.maxp;
+    if (++it >= kRjMaxTries && pc < alpha) {
+      *st = GLASS_RJ_RNG_LIMIT;
+      return -INFINITY;
+    }
+  } while (pc < alpha);
+  p[0] = q;
+  p[1] = costheta;
+  p[2] = phi;
+  return fstat_density(p, a, pr, lv);
+}
+
+// ucb_rjmcmc (ucb/src/glass_ucb_sampler.c:454-483) up to the likelihood, with
+// rj_birth_death (:175-249), one thread per chain, every draw in the
+// reference's order: the proposal by rejection on the rj weights, the
+// birth/death branch draw (always birth/death), birth or death, and the new
+// source from the proposal (birth) or the source to remove and its proposal
+// density (death).
+__global__ void rj_propose_kernel(RjArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const double *pr = a.prior + 16 * (size_t)i * a.stride;
   const double *lv = a.logPV + 8 * (size_t)i * a.stride;
-  double *p = a.params + 8 * (size_t)i;
-  const double twopi = 6.283185307179586;
-  auto lo = [&](int k) { return pr[2 * k]; };
-  auto hi = [&](int k) { return pr[2 * k + 1]; };
-  // check_range
-  bool bad = false;
-  for (int k = 0; k < 8; k++)
-    if (p[k] != p[k]) bad = true;
-  if (!bad && (p[0] < lo(0) || p[0] > hi(0))) bad = true;
-  if (!bad && (p[1] < lo(1) || p[1] > hi(1))) bad = true;
-  if (!bad && (p[2] < lo(2) || p[2] >= hi(2))) {
-    p[2] = atan2(sin(p[2]), cos(p[2]));
-    if (p[2] < 0.0) p[2] += twopi;
-  }
-  if (!bad && (p[3] < lo(3) || p[3] > hi(3))) bad = true;
-  if (!bad && (p[4] < lo(4) || p[4] > hi(4))) bad = true;
-  if (!bad) {
-    for (int it = 0; it < 64 && p[5] < lo(5); it++) p[5] += M_PI;
-    for (int it = 0; it < 64 && p[5] > hi(5); it++) p[5] -= M_PI;
-    for (int it = 0; it < 64 && p[6] < lo(6); it++) p[6] += twopi;
-    for (int it = 0; it < 64 && p[6] > hi(6); it++) p[6] -= twopi;
-    if (p[7] < lo(7) || p[7] > hi(7)) bad = true;
-  }
-  if (bad) {
-    a.out[i] = -INFINITY;
-    return;
-  }
-  double logP = 0.0;
-  // sky location
-  if (a.skyhist) {
-    if (p[1] < lo(1) || p[1] > hi(1)) {
-      a.out[i] = -INFINITY;
-      return;
+  unsigned int s = a.seed[i];
+  int st = GLASS_RJ_OK;
+  int nprop = 0;
+  for (int it = 0;; it++) {
+    nprop = (int)floor(9 * glass_u01(&s));
+    if (nprop > 8) {
+      nprop = 8;  // a draw of exactly 1: the reference reads past its proposals
+      st = GLASS_RJ_RNG_EDGE;
     }
-    if (lo(2) > 0.0 || hi(2) < twopi) {
-      if (p[2] < lo(2) || p[2] > hi(2)) {
-        a.out[i] = -INFINITY;
-        return;
+    if (!(a.rjw[nprop] <= glass_u01(&s))) break;
+    if (it + 1 >= kRjMaxTries) {
+      st = GLASS_RJ_RNG_LIMIT;
+      break;
+    }
+  }
+  (void)glass_u01(&s);  // birth/death or split/merge: always birth/death
+  const int Nx = a.Nlive[i];
+  const double *x = a.src + (size_t)i * a.maxsrc * 8;
+  double *y = a.params_y + 8 * (size_t)i;
+  double lqxy = 0.0, lqyx = 0.0, lpy = 0.0;
+  int move, slot;
+  if (glass_u01(&s) < 0.5) {  // birth
+    move = 1;
+    slot = Nx;
+    if (Nx + 1 < a.Neff[i] && Nx < a.maxsrc && st != GLASS_RJ_RNG_LIMIT) {
+      lqyx = nprop == 0 ? prior_draw(y, pr, lv, &s) : fstat_draw(y, a, pr, lv, &s, &st);
+      lqxy = 0;
+    } else {
+      lpy = -INFINITY;
+    }
+  } else {  // death
+    move = -1;
+    const int kill = (int)(glass_u01(&s) * (double)Nx);
+    slot = kill;
+    if (Nx - 1 > -1 && kill < a.maxsrc && st != GLASS_RJ_RNG_LIMIT) {
+      for (int k = 0; k < 8; k++) y[k] = x[8 * (size_t)kill + k];
+      lqyx = 0;
+      if (nprop == 0) {
+        for (int k = 0; k < 8; k++) lqxy -= lv[k];  // uniform_prior_density
+      } else {
+        double yk[8];  // the density may wrap its copy; the source is kept as it is
+        for (int k = 0; k < 8; k++) yk[k] = y[k];
+        lqxy = fstat_density(yk, a, pr, lv);
       }
     } else {
-      for (int it = 0; it < 64 && p[2] < 0; it++) p[2] += twopi;
-      for (int it = 0; it < 64 && p[2] > twopi; it++) p[2] -= twopi;
+      lpy = -INFINITY;
     }
-    const int ci = (int)floor((p[1] - lo(1)) / a.dcostheta);
-    const int cj = (int)floor((p[2] - lo(2)) / a.dphi);
-    logP += a.skyhist[ci * a.nphi + cj];
-  } else {
-    if (p[1] < lo(1) || p[1] > hi(1)) {
-      a.out[i] = -INFINITY;
-      return;
-    }
-    logP -= lv[1];
-    if (lo(2) > 0.0 || hi(2) < twopi) {
-      if (p[2] < lo(2) || p[2] > hi(2)) {
-        a.out[i] = -INFINITY;
-        return;
-      }
-    } else if (p[2] < lo(2) || p[2] >= hi(2)) {
-      p[2] = atan2(sin(p[2]), cos(p[2]));
-      if (p[2] < 0.0) p[2] += twopi;
-    }
-    logP -= lv[2];
   }
-  // evaluate_uniform_priors (its own range check passes: params are in range now)
-  logP -= log(hi(0) - lo(0));
-  logP -= lv[3];
-  logP -= lv[4];
-  logP -= lv[5];
-  logP -= lv[6];
-  logP -= lv[7];
-  a.out[i] = logP;
+  if (st == GLASS_RJ_RNG_LIMIT) lpy = -INFINITY;
+  a.seed[i] = s;
+  a.move[i] = move;
+  a.slot[i] = slot;
+  a.kind[i] = nprop;
+  a.logQxy[i] = lqxy;
+  a.logQyx[i] = lqyx;
+  a.logPy[i] = lpy;
+  if (a.status) a.status[i] = st;
+}
+
+// ucb_rjmcmc (ucb/src/glass_ucb_sampler.c:485-565) from the likelihood on,
+// one thread per chain: the birth's SNR cut (rj_birth_death :205-210), the
+// priors of the current and proposed source lists, the Hastings ratio, one
+// draw, and on acceptance the proposed list and log-likelihood.
+__global__ void rj_accept_kernel(RjArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double *pr = a.prior + 16 * (size_t)i * a.stride;
+  const double *lv = a.logPV + 8 * (size_t)i * a.stride;
+  const int Nx = a.Nlive[i], move = a.move[i], slot = a.slot[i];
+  double *x = a.src + (size_t)i * a.maxsrc * 8;
+  double *y = a.params_y + 8 * (size_t)i;
+  double lpy = a.logPy[i];
+  double dlogL = a.dlogl[i];
+  if (a.dlogl_is_term && move < 0) dlogL = -dlogL - a.hh[i];  // the removed source's term and (h|h)
+  if (move > 0 && lpy > -INFINITY && !a.prior_only && a.hh && sqrt(a.hh[i]) < 5.0) lpy = -INFINITY;
+  double logPx = 0.0;
+  const int Ny = Nx + move;
+  // a list or slot outside the chain's maxsrc slots is refused, not read
+  const bool inb = Nx >= 0 && Nx <= a.maxsrc && Ny >= 0 && Ny <= a.maxsrc &&
+                   (move > 0 ? (move == 1 && slot == Nx) : (move == -1 && slot >= 0 && slot < Nx));
+  if (!inb) lpy = -INFINITY;
+  if (lpy > -INFINITY) {
+    // The current list is evaluated (and wrapped) in place, as the reference
+    // does; the proposed list's copies of it then give the same values as
+    // the reference's copies taken before the wrapping.
+    for (int n = 0; n < Nx; n++) logPx += prior_ucb(x + 8 * (size_t)n, pr, lv, a.skyhist, a.dcostheta, a.dphi, a.nphi);
+    for (int n = 0; n < Ny; n++) {
+      if (move > 0 && n == Nx) {
+        lpy += prior_ucb(y, pr, lv, a.skyhist, a.dcostheta, a.dphi, a.nphi);
+        continue;
+      }
+      double yn[8];
+      const double *src = x + 8 * (size_t)((move > 0 || n < slot) ? n : n + 1);
+      for (int k = 0; k < 8; k++) yn[k] = src[k];
+      lpy += prior_ucb(yn, pr, lv, a.skyhist, a.dcostheta, a.dphi, a.nphi);
+    }
+  }
+  double logH = 0.0;
+  if (lpy > -INFINITY && !a.prior_only) logH += dlogL / a.T_chain[i];
+  logH += lpy - logPx;
+  logH += a.logQxy[i] - a.logQyx[i];
+  unsigned int s = a.seed[i];
+  const double loga = log(glass_u01(&s));
+  a.seed[i] = s;
+  int acc = 0;
+  if (isfinite(logH) && logH > loga) {
+    acc = 1;
+    if (move > 0) {
+      for (int k = 0; k < 8; k++) x[8 * (size_t)Nx + k] = y[k];
+    } else {
+      for (int n = slot; n < Ny; n++)
+        for (int k = 0; k < 8; k++) x[8 * (size_t)n + k] = x[8 * (size_t)(n + 1) + k];
+    }
+    a.Nlive[i] = Ny;
+    a.logL_x[i] += dlogL;
+  }
+  if (a.accepted) a.accepted[i] = acc;
 }
 
 }  // namespace
@@ -472,6 +671,16 @@ cudaError_t mh_accept_launch(const MhArgs &a, cudaStream_t stream) {
 cudaError_t fisher_draw_launch(const FisherDrawArgs &a, cudaStream_t stream) {
   // eight lanes per chain, sixteen chains per CTA
   fisher_draw_kernel<<<(a.n + 15) / 16, 128, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t rj_propose_launch(const RjArgs &a, cudaStream_t stream) {
+  rj_propose_kernel<<<(a.n + 31) / 32, 32, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t rj_accept_launch(const RjArgs &a, cudaStream_t stream) {
+  rj_accept_kernel<<<(a.n + 31) / 32, 32, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

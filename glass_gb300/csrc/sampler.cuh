@@ -51,7 +51,41 @@ struct PriorArgs {
 };
 
 cudaError_t sym_eigen8_launch(int n, const double *matrix, double *evec, double *evalue, cudaStream_t stream);
+// The trans-dimensional (birth/death) step of ucb_rjmcmc for n chains, in two
+// launches around the likelihood: chain i's live sources src[(i maxsrc + s) 8
+// ..], s < Nlive[i].
+struct RjArgs {
+  int n, maxsrc;
+  int *Nlive;
+  const int *Neff;
+  double *src;
+  const double *prior, *logPV;
+  int stride;
+  double rjw[9];  // the proposals' rj weights (0: prior draw, 1: F-statistic draw, others 0)
+  // the F-statistic proposal's grid (draw_from_fstatistic): density
+  // tensor[(i n_theta + j) n_phi + k], cells d_f x d_theta x d_phi from
+  // (qmin / T, -1, 0), maximum maxp
+  const double *tensor;
+  int n_f, n_theta, n_phi, qmin;
+  double d_f, d_theta, d_phi, maxp, T;
+  unsigned int *seed;
+  // proposal: +1 birth / -1 death, the slot created or removed, the new (or
+  // removed) source, the proposal densities, 0 or -inf (refused), the kind
+  int *move, *slot, *kind, *status;
+  double *params_y, *logQxy, *logQyx, *logPy;
+  // acceptance
+  const double *T_chain, *dlogl, *hh;
+  int dlogl_is_term, prior_only;
+  const double *skyhist;
+  double dcostheta, dphi;
+  int nphi;
+  double *logL_x;
+  int *accepted;
+};
+
 cudaError_t prior_draw_launch(const PriorArgs &a, cudaStream_t stream);
+cudaError_t rj_propose_launch(const RjArgs &a, cudaStream_t stream);
+cudaError_t rj_accept_launch(const RjArgs &a, cudaStream_t stream);
 cudaError_t ucb_prior_launch(const PriorArgs &a, cudaStream_t stream);
 cudaError_t rand_r_fill_launch(int n, int count, unsigned int *seed, int *out, cudaStream_t stream);
 cudaError_t mh_accept_launch(const MhArgs &a, cudaStream_t stream);

@@ -547,6 +547,63 @@ int glass_gpu_ucb_prior(glass_gpu_ctx *ctx, int n, double *params, const double 
                         const double *logPV, const double *skyhist, double dcostheta, double dphi, int nphi,
                         double *logP);
 
+/*
+ * The trans-dimensional (birth/death) step of ucb_rjmcmc
+ * (ucb/src/glass_ucb_sampler.c:454-566, rj_birth_death :175-249) for n
+ * chains on device state, in two launches around the likelihood:
+ *
+ * glass_gpu_rj_propose: per chain, every draw in the reference's order: the
+ * proposal by rejection on the rj weights (rjweight[9], host array: only
+ * 0 = prior draw, draw_from_uniform_prior, and 1 = F-statistic draw,
+ * draw_from_fstatistic with the grid of build_fstatistic_proposal, may be
+ * non-zero: the reference's cocktail without the catalogue and covariance
+ * proposals), the birth/death choice, then for a birth (move = +1) the new
+ * source params_y[8 i ..] and logQyx (refused, logPy = -inf, when Nlive + 1 >=
+ * Neff), for a death (move = -1) the source slot[i] to remove, copied to
+ * params_y, and logQxy (its proposal density; refused when Nlive = 0).
+ * kind[i] = the proposal, status[i] (may be NULL) a GLASS_RJ_* code.  Chain
+ * i's live sources: src[(i maxsrc + s) 8 ..], s < Nlive[i] (maxsrc: the
+ * reference's Nmax).
+ *
+ * The caller then evaluates the likelihood change of each proposal, e.g.
+ * with glass_gpu_dlogl_batch on params_y against the chain's residual
+ * (term_x = 0), which gives a birth's change directly and a death's as
+ * -(term + hh) (dlogl_is_term = 1), and hh = (h|h) for the birth's SNR cut.
+ *
+ * glass_gpu_rj_accept: the birth's SNR cut (sqrt(hh) < 5, skipped with
+ * prior_only or hh NULL), the priors of the current and proposed source
+ * lists (evaluate_ucb_prior as glass_gpu_ucb_prior: sources wrapped in place),
+ * logH = dlogl / temperature + logPy - logPx + logQxy - logQyx, one draw
+ * loga = log U(0,1) (always), and on acceptance the source list (the new
+ * source appended, or the removed one taken out with the rest moved down),
+ * Nlive and logL_x += dlogl.  accepted[i] (may be NULL).  Not restated: the
+ * split/merge and cluster-bomb moves (never chosen by the reference's
+ * branch draws), the maximisation penalty and calibration, the Fisher
+ * matrices the reference refreshes on acceptance.  All arrays DEVICE
+ * arrays; asynchronous.
+ */
+typedef struct {
+  const double *tensor; /* device: density of cell (i, j, k) at (i n_theta + j) n_phi + k */
+  int n_f, n_theta, n_phi;
+  double d_f, d_theta, d_phi; /* cell sizes: Hz, cos theta, phi */
+  double maxp;                /* the largest density */
+  int qmin;                   /* the segment's first bin */
+  double T;
+} glass_gpu_fstat_grid;
+#define GLASS_RJ_OK 0
+#define GLASS_RJ_RNG_EDGE 1  /* a draw of exactly 1 picked one past the end (the reference reads past its arrays) */
+#define GLASS_RJ_RNG_LIMIT 2 /* 2^20 rejections in a row: the proposal is refused */
+int glass_gpu_rj_propose(glass_gpu_ctx *ctx, int n, int maxsrc, const int *Nlive, const int *Neff, const double *src,
+                         const double *prior, int prior_stride, const double *logPV, const double *rjweight,
+                         const glass_gpu_fstat_grid *grid, unsigned int *seed, int *move, int *slot, int *kind,
+                         double *params_y, double *logQxy, double *logQyx, double *logPy, int *status);
+int glass_gpu_rj_accept(glass_gpu_ctx *ctx, int n, int maxsrc, int *Nlive, double *src, const int *move,
+                        const int *slot, double *params_y, const double *logQxy, const double *logQyx,
+                        const double *logPy, const double *temperature, const double *dlogl, const double *hh,
+                        int dlogl_is_term, int prior_only, const double *prior, int prior_stride, const double *logPV,
+                        const double *skyhist, double dcostheta, double dphi, int nphi, unsigned int *seed,
+                        double *logL_x, int *accepted);
+
 /* Number of kernels the last glass_gpu_dlogl_batch launched (for accounting). */
 int glass_gpu_last_launch_count(glass_gpu_ctx *ctx);
 

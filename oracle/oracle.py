@@ -288,6 +288,57 @@ class Port:
                                               _p(r), _p(out), nthreads)
         return out
 
+    def rj_propose(self, Nlive, Neff, src, prior, logPV, rjw, grid, seed):
+        """The birth/death proposal of ucb_rjmcmc per chain (orc_rj_propose):
+        Nlive [n], Neff [n], src [n, maxsrc, 8], prior [8, 2], logPV [8],
+        rjw [9], grid = (tensor [nf, nt, np], df, dt, dp, maxp, qmin, T) or
+        None, seed [n] (advanced in place).  Returns move, slot, kind,
+        params_y, logQxy, logQyx, logPy."""
+        lib = self.lib
+        _U = ctypes.POINTER(ctypes.c_uint)
+        lib.orc_rj_propose.argtypes = [ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D, _D, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_int, ctypes.c_double, _U, _I, _I, _I, _D, _D, _D, _D]
+        n, maxsrc = src.shape[0], src.shape[1]
+        Nl = np.ascontiguousarray(Nlive, np.int32)
+        Ne = np.ascontiguousarray(Neff, np.int32)
+        sr = np.ascontiguousarray(src, np.float64)
+        pr = np.ascontiguousarray(prior, np.float64).reshape(16)
+        lv = np.ascontiguousarray(logPV, np.float64)
+        w = np.ascontiguousarray(rjw, np.float64)
+        if grid is None:
+            ten, df, dt, dp, maxp, qmin, T = np.ones((1, 1, 1)), 1.0, 1.0, 1.0, 1.0, 0, 1.0
+        else:
+            ten, df, dt, dp, maxp, qmin, T = grid
+        ten = np.ascontiguousarray(ten, np.float64)
+        move, slot, kind = (np.zeros(n, np.int32) for _ in range(3))
+        y = np.zeros((n, 8))
+        qxy, qyx, lpy = np.zeros(n), np.zeros(n), np.zeros(n)
+        lib.orc_rj_propose(n, maxsrc, _pi(Nl), _pi(Ne), _p(sr), _p(pr), _p(lv), _p(w), _p(ten), ten.shape[0],
+                           ten.shape[1], ten.shape[2], df, dt, dp, maxp, int(qmin), T, seed.ctypes.data_as(_U),
+                           _pi(move), _pi(slot), _pi(kind), _p(y), _p(qxy), _p(qyx), _p(lpy))
+        return move, slot, kind, y, qxy, qyx, lpy
+
+    def rj_accept(self, Nlive, src, move, slot, params_y, logQxy, logQyx, logPy, T, dlogl, hh, prior, logPV, seed,
+                  logL_x, prior_only=False):
+        """The acceptance half of ucb_rjmcmc (orc_rj_accept); Nlive, src,
+        params_y, seed and logL_x are updated in place.  Returns accepted."""
+        lib = self.lib
+        _U = ctypes.POINTER(ctypes.c_uint)
+        lib.orc_rj_accept.argtypes = [ctypes.c_int, ctypes.c_int, _I, _D, _I, _I, _D, _D, _D, _D, _D, _D, _D,
+                                      ctypes.c_int, _D, _D, _U, _D, _I]
+        n, maxsrc = src.shape[0], src.shape[1]
+        acc = np.zeros(n, np.int32)
+        pr = np.ascontiguousarray(prior, np.float64).reshape(16)
+        lib.orc_rj_accept(n, maxsrc, _pi(Nlive), _p(src), _pi(np.ascontiguousarray(move, np.int32)),
+                          _pi(np.ascontiguousarray(slot, np.int32)), _p(params_y), _p(np.ascontiguousarray(logQxy)),
+                          _p(np.ascontiguousarray(logQyx)), _p(np.ascontiguousarray(logPy)),
+                          _p(np.ascontiguousarray(T, np.float64)), _p(np.ascontiguousarray(dlogl, np.float64)),
+                          _p(np.ascontiguousarray(hh, np.float64)) if hh is not None else None, int(prior_only),
+                          _p(pr), _p(np.ascontiguousarray(logPV, np.float64)), seed.ctypes.data_as(_U), _p(logL_x),
+                          _pi(acc))
+        return acc
+
     def noise_logl_channels(self, T, fmin, d, inst, sgal=None):
         """noise_log_likelihood of the one-channel (d [1, 2 NFFT] = X) or
         two-channel (d [2, 2 NFFT] = A, E) instrument (+ foreground) model for
@@ -837,6 +888,37 @@ class Ref:
                                         _p(md) if md is not None else None, len(inst), _p(inst),
                                         _p(sg) if sg is not None else None, int(sgwb_type), _p(b), len(r), _p(r),
                                         _p(out))
+        return out
+
+    def rj_steps(self, T, NFFT, qmin, dA, dE, invCA, invCE, Neff, Nlive, src, prior, logPV, rjw, grid, temperature,
+                 seed, nsteps, t0=0.0, fmt="sangria"):
+        """The reference's ucb_rjmcmc, nsteps calls per chain (ref_rj_steps).
+        Nlive, src [n, maxsrc, 8] and seed are updated in place.  Returns a
+        dict of the per-call records [nsteps, n, ...] and logL0 [n]."""
+        lib = self.lib
+        _U = ctypes.POINTER(ctypes.c_uint)
+        lib.ref_rj_steps.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                     _D, _D, _D, _D, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, _D, _D, _D,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, _D, _U, ctypes.c_int, _D, _I, _D, _D, _D, _D,
+                                     _I, _U]
+        n, maxsrc = src.shape[0], src.shape[1]
+        ten, df, dt, dp, maxp = grid
+        ten = np.ascontiguousarray(ten, np.float64)
+        K = nsteps
+        out = {"logL0": np.zeros(n), "rec_gen": np.zeros((K, n), np.int32), "rec_params": np.zeros((K, n, 8)),
+               "rec_snr": np.zeros((K, n)), "rec_logLy": np.zeros((K, n)), "logL": np.zeros((K, n)),
+               "Nlive": np.zeros((K, n), np.int32), "seed": np.zeros((K, n), np.uint32)}
+        lib.ref_rj_steps(fmt.encode(), T, t0, NFFT, qmin, _p(np.ascontiguousarray(dA)), _p(np.ascontiguousarray(dE)),
+                         _p(np.ascontiguousarray(invCA)), _p(np.ascontiguousarray(invCE)), n, maxsrc,
+                         np.ascontiguousarray(Neff, np.int32).ctypes.data_as(_I), Nlive.ctypes.data_as(_I), _p(src),
+                         _p(np.ascontiguousarray(prior, np.float64).reshape(16)),
+                         _p(np.ascontiguousarray(logPV, np.float64)), _p(np.ascontiguousarray(rjw, np.float64)),
+                         _p(ten), ten.shape[0], ten.shape[1], ten.shape[2], df, dt, dp, maxp,
+                         _p(np.ascontiguousarray(temperature, np.float64)), seed.ctypes.data_as(_U), K,
+                         _p(out["logL0"]), out["rec_gen"].ctypes.data_as(_I), _p(out["rec_params"]),
+                         _p(out["rec_snr"]), _p(out["rec_logLy"]), _p(out["logL"]), out["Nlive"].ctypes.data_as(_I),
+                         out["seed"].ctypes.data_as(_U))
         return out
 
     def noise_logl_channels(self, T, fmin, d, inst, sgal=None):

@@ -1209,3 +1209,186 @@ double ref_ucb_prior(double *params, const double *prior16, const double *logPV8
     pr.nphi = nphi;
     return evaluate_ucb_prior(&flags, NULL, &m, &pr, params);
 }
+
+/* ------------------------------------------------------------------------
+ * ucb_rjmcmc (ucb/src/glass_ucb_sampler.c:454) for NC chains on one A/E
+ * segment, nsteps successive calls per chain, with the prior (proposal 0)
+ * and F-statistic (proposal 1) draws of the reference's cocktail
+ * (rjweight[9]) and an F-statistic grid given as input.  The model's
+ * likelihood and signal generator are the reference's own
+ * (gaussian_log_likelihood, generate_ucb_model), wrapped to record, per call,
+ * the proposed state's logL (NaN when not evaluated) and, for a birth whose
+ * template was generated, the new source's parameters and SNR.
+ * In/out: Nlive[NC], src[(c maxsrc + s) 8 ..], seed[NC].  Out per step k and
+ * chain c (index k NC + c): rec_gen, rec_params[8], rec_snr, rec_logLy,
+ * and after the call logL, Nlive and seed; logL0[NC] the starting logL.
+ */
+static int g_rec_gen, g_rec_eval;
+static double g_rec_snr, g_rec_logL, g_rec_params[UCB_MODEL_NP];
+
+static double rec_log_likelihood(struct Data *data, struct Model *model)
+{
+    double l = gaussian_log_likelihood(data, model);
+    g_rec_eval = 1;
+    g_rec_logL = l;
+    return l;
+}
+
+static void rec_generate(struct Orbit *orbit, struct Data *data, struct Model *model, int source_id)
+{
+    generate_ucb_model(orbit, data, model, source_id);
+    if (source_id >= 0) {
+        g_rec_gen = 1;
+        g_rec_snr = snr(model->source[source_id], model->noise);
+        for (int p = 0; p < UCB_MODEL_NP; p++) g_rec_params[p] = model->source[source_id]->params[p];
+    }
+}
+
+void ref_rj_steps(const char *format, double T, double t0, int NFFT, int qmin, const double *dA, const double *dE,
+                  const double *invCA, const double *invCE, int NC, int maxsrc, const int *Neff, int *Nlive,
+                  double *src, const double *prior16, const double *logPV8, const double *rjw, const double *tensor,
+                  int nf, int nt, int np, double df, double dt, double dp, double maxp, const double *temperature,
+                  unsigned int *seed, int nsteps, double *logL0, int *rec_gen, double *rec_params, double *rec_snr,
+                  double *rec_logLy, double *logL_after, int *Nlive_after, unsigned int *seed_after)
+{
+    struct Orbit orbit;
+    setup_orbit(&orbit);
+    struct Data *data = calloc(1, sizeof(struct Data));
+    data->NFFT = NFFT;
+    data->N = 2 * NFFT;
+    data->Nchannel = 2;
+    data->Nlayer = 1;
+    data->T = T;
+    data->sqT = sqrt(T);
+    data->t0 = t0;
+    data->qmin = qmin;
+    data->qmax = qmin + NFFT;
+    data->fmin = qmin / T;
+    data->fmax = (qmin + NFFT) / T;
+    strcpy(data->format, format);
+    strcpy(data->basis, "fourier");
+    data->tdi = malloc(sizeof(struct TDI));
+    alloc_tdi(data->tdi, data->N, data->Nchannel);
+    memcpy(data->tdi->A, dA, sizeof(double) * data->N);
+    memcpy(data->tdi->E, dE, sizeof(double) * data->N);
+    data->noise = malloc(sizeof(struct Noise));
+    alloc_noise(data->noise, NFFT, 1, 2);
+    for (int n = 0; n < NFFT; n++) {
+        data->noise->invC[0][0][n] = invCA[n];
+        data->noise->invC[1][1][n] = invCE[n];
+        data->noise->C[0][0][n] = 1.0 / invCA[n];
+        data->noise->C[1][1][n] = 1.0 / invCE[n];
+    }
+
+    struct Flags *flags = calloc(1, sizeof(struct Flags));
+    struct Prior *prior = calloc(1, sizeof(struct Prior));
+    struct Chain *chain = calloc(1, sizeof(struct Chain));
+    chain->NC = NC;
+    chain->r = malloc(sizeof(unsigned int) * NC);
+    chain->temperature = malloc(sizeof(double) * NC);
+    for (int c = 0; c < NC; c++) {
+        chain->r[c] = seed[c];
+        chain->temperature[c] = temperature[c];
+    }
+
+    double ***ten = malloc(sizeof(double **) * nf);
+    for (int i = 0; i < nf; i++) {
+        ten[i] = malloc(sizeof(double *) * nt);
+        for (int j = 0; j < nt; j++) ten[i][j] = (double *)tensor + ((size_t)i * nt + j) * np;
+    }
+    double *mrow[3];
+    double mval[3][2] = {{nf, df}, {nt, dt}, {np, dp}};
+    for (int r = 0; r < 3; r++) mrow[r] = mval[r];
+    struct Proposal **prop = malloc(sizeof(struct Proposal *) * UCB_PROPOSAL_NPROP);
+    for (int k = 0; k < UCB_PROPOSAL_NPROP; k++) {
+        prop[k] = calloc(1, sizeof(struct Proposal));
+        prop[k]->trial = calloc(NC, sizeof(int));
+        prop[k]->accept = calloc(NC, sizeof(int));
+        prop[k]->rjweight = rjw[k];
+        prop[k]->function = &draw_from_uniform_prior;
+        prop[k]->density = &uniform_prior_density;
+    }
+    prop[1]->function = &draw_from_fstatistic;
+    prop[1]->density = &evaluate_fstatistic_proposal;
+    prop[1]->matrix = mrow;
+    prop[1]->tensor = ten;
+    prop[1]->maxp = maxp;
+
+    struct Model **model = malloc(sizeof(struct Model *) * NC), **trial = malloc(sizeof(struct Model *) * NC);
+    for (int c = 0; c < NC; c++) {
+        struct Model *pair[2];
+        for (int w = 0; w < 2; w++) {
+            struct Model *m = calloc(1, sizeof(struct Model));
+            alloc_model(data, m, UCB_MODEL_NP, maxsrc);
+            m->Neff = Neff[c];
+            m->t0 = t0;
+            m->log_likelihood = &rec_log_likelihood;
+            m->generate_signal_model = &rec_generate;
+            for (int k = 0; k < UCB_MODEL_NP; k++) {
+                m->prior[k][0] = prior16[2 * k];
+                m->prior[k][1] = prior16[2 * k + 1];
+                m->logPriorVolume[k] = logPV8[k];
+            }
+            for (int n = 0; n < NFFT; n++) {
+                m->noise->invC[0][0][n] = invCA[n];
+                m->noise->invC[1][1][n] = invCE[n];
+                m->noise->C[0][0][n] = 1.0 / invCA[n];
+                m->noise->C[1][1][n] = 1.0 / invCE[n];
+            }
+            pair[w] = m;
+        }
+        model[c] = pair[0];
+        trial[c] = pair[1];
+        model[c]->Nlive = Nlive[c];
+        for (int s = 0; s < Nlive[c]; s++)
+            for (int p = 0; p < UCB_MODEL_NP; p++)
+                model[c]->source[s]->params[p] = src[((size_t)c * maxsrc + s) * 8 + p];
+        generate_ucb_model(&orbit, data, model[c], -1);
+        model[c]->logL = gaussian_log_likelihood(data, model[c]);
+        logL0[c] = model[c]->logL;
+    }
+
+    for (int k = 0; k < nsteps; k++) {
+        for (int c = 0; c < NC; c++) {
+            size_t o = (size_t)k * NC + c;
+            g_rec_gen = g_rec_eval = 0;
+            g_rec_snr = NAN;
+            g_rec_logL = NAN;
+            ucb_rjmcmc(&orbit, data, model[c], trial[c], chain, flags, prior, prop, c);
+            rec_gen[o] = g_rec_gen;
+            rec_snr[o] = g_rec_gen ? g_rec_snr : NAN;
+            for (int p = 0; p < 8; p++) rec_params[8 * o + p] = g_rec_gen ? g_rec_params[p] : NAN;
+            rec_logLy[o] = g_rec_eval ? g_rec_logL : NAN;
+            logL_after[o] = model[c]->logL;
+            Nlive_after[o] = model[c]->Nlive;
+            seed_after[o] = chain->r[c];
+        }
+    }
+    for (int c = 0; c < NC; c++) {
+        Nlive[c] = model[c]->Nlive;
+        seed[c] = chain->r[c];
+        for (int s = 0; s < maxsrc; s++)
+            for (int p = 0; p < 8; p++)
+                src[((size_t)c * maxsrc + s) * 8 + p] = s < model[c]->Nlive ? model[c]->source[s]->params[p] : 0.0;
+        free_model(model[c]);
+        free_model(trial[c]);
+    }
+    free(model);
+    free(trial);
+    for (int k = 0; k < UCB_PROPOSAL_NPROP; k++) {
+        free(prop[k]->trial);
+        free(prop[k]->accept);
+        free(prop[k]);
+    }
+    free(prop);
+    for (int i = 0; i < nf; i++) free(ten[i]);
+    free(ten);
+    free(chain->r);
+    free(chain->temperature);
+    free(chain);
+    free(prior);
+    free(flags);
+    free_noise(data->noise);
+    free_tdi(data->tdi);
+    free(data);
+}

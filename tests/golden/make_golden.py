@@ -647,10 +647,67 @@ def noise_channels(ref, rng):
     np.savez_compressed(os.path.join(HERE, "noise_channels.npz"), **out)
 
 
+def rj(ref, rng):
+    """ucb_rjmcmc (ucb/src/glass_ucb_sampler.c:454), the birth/death step, run
+    by the reference itself: 48 chains on one 256-bin A/E segment at 3.2 mHz
+    with three injected sources, starting from 0 to 3 sources (injections
+    and prior draws), six successive calls each, the reference's cocktail of
+    the prior draw (rj weight 0.2) and the F-statistic draw (0.8) on a
+    synthetic 64 x 10 x 10 density grid peaked at the injections, and
+    temperatures 1.5^(c mod 12).  Recorded per call: the proposed state's
+    logL when the reference evaluated it, a birth's new source and SNR, and
+    logL, Nlive and the seed after the call; the final source lists."""
+    NFFT, NC, maxsrc, nsteps = 256, 48, 6, 6
+    injs = [wl.draw_source(rng, 3.2e-3 + k * 30 / T, 10 ** rng.uniform(-22.0, -21.3), 1e-17) for k in range(3)]
+
+    def wf(p):
+        al = ref.alignment(T, NFFT, 0, p)
+        h = ref.waveform(p, int(al[0]), T)
+        return int(al[0]), h[3], h[4]
+
+    qmin, dA, dE, iA, iE = wl.make_segment(rng, injs, wf, NFFT=NFFT, T=T, center_f0=3.2e-3 + 30 / T)
+    dA_i = np.empty(2 * NFFT)
+    dA_i[0::2], dA_i[1::2] = dA.real, dA.imag
+    dE_i = np.empty(2 * NFFT)
+    dE_i[0::2], dE_i[1::2] = dE.real, dE.imag
+    prior = np.array([[qmin, qmin + NFFT], [-1.0, 1.0], [0.0, 2 * np.pi], [np.log(1e-23), np.log(2e-21)],
+                      [-1.0, 1.0], [0.0, np.pi], [0.0, 2 * np.pi], [-1.0, 1.0]])
+    logPV = np.log(prior[:, 1] - prior[:, 0])
+    nf, nt, npp = 64, 10, 10
+    df, dt, dp = (NFFT / nf) / T, 2.0 / nt, 2 * np.pi / npp
+    tensor = rng.uniform(0.5, 1.5, (nf, nt, npp))
+    for p in injs:
+        i = int((p[0] - qmin) / (df * T))
+        j = int((p[1] + 1) / dt)
+        k = int((p[2] % (2 * np.pi)) / dp)
+        tensor[min(i, nf - 1), min(j, nt - 1), min(k, npp - 1)] += 200.0
+    maxp = float(tensor.max())
+    Nlive = rng.integers(0, 4, NC).astype(np.int32)
+    Neff = np.full(NC, maxsrc, np.int32)
+    Neff[::7] = Nlive[::7] + 1  # births refused on these chains
+    src = np.zeros((NC, maxsrc, 8))
+    for c in range(NC):
+        for s in range(Nlive[c]):
+            if s < 3 and rng.uniform() < 0.6:
+                src[c, s] = wl.gaussian_jumps(rng, injs[s], wl.jump_scales(injs[s], 30.0), 1)[0]
+            else:
+                src[c, s] = prior[:, 0] + rng.uniform(0, 1, 8) * (prior[:, 1] - prior[:, 0])
+    temperature = 1.5 ** (np.arange(NC) % 12)
+    seed0 = rng.integers(1, 2**31, NC).astype(np.uint32)
+    rjw = np.array([0.2, 0.8, 0, 0, 0, 0, 0, 0, 0])
+    Nl, sr, sd = Nlive.copy(), src.copy(), seed0.copy()
+    out = ref.rj_steps(T, NFFT, qmin, dA_i, dE_i, iA, iE, Neff, Nl, sr, prior, logPV, rjw,
+                       (tensor, df, dt, dp, maxp), temperature, sd, nsteps)
+    np.savez_compressed(os.path.join(HERE, "rj.npz"), NFFT=NFFT, qmin=qmin, dA=dA_i, dE=dE_i, invCA=iA, invCE=iE,
+                        prior=prior, logPV=logPV, tensor=tensor, df=df, dt=dt, dp=dp, maxp=maxp, Nlive0=Nlive,
+                        Neff=Neff, src0=src, temperature=temperature, seed0=seed0, rjw=rjw, Nlive_end=Nl,
+                        src_end=sr, seed_end=sd, **out)
+
+
 OWN_SEEDS = {"fstat": 20261204, "noise": 20261205, "noise_wavelet": 20261206, "noise_eta": 20261207,
              "sampler": 20261208, "fisher_draw": 20261209, "fisher_big": 20261210,
              "fisher_wavelet": 20261211, "priors": 20261212, "sgwb": 20261213,
-             "spline_noise": 20261214, "noise_channels": 20261215}
+             "spline_noise": 20261214, "noise_channels": 20261215, "rj": 20261216}
 
 
 def main(names=()):
@@ -679,6 +736,7 @@ def main(names=()):
     sgwb(ref, np.random.default_rng(OWN_SEEDS["sgwb"]))
     spline_noise(ref, np.random.default_rng(OWN_SEEDS["spline_noise"]))
     noise_channels(ref, np.random.default_rng(OWN_SEEDS["noise_channels"]))
+    rj(ref, np.random.default_rng(OWN_SEEDS["rj"]))
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))
