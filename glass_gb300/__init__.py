@@ -158,7 +158,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_check_status.argtypes = [_V, ctypes.POINTER(ctypes.c_uint)]
     lib.glass_gpu_rj_propose.argtypes = [_V, ctypes.c_int, ctypes.c_int, _V, _V, _V, _V, ctypes.c_int, _V, _D,
                                          ctypes.POINTER(FstatGrid)] + [_V] * 9
-    lib.glass_gpu_rj_accept.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 12 + [
+    lib.glass_gpu_rj_accept.argtypes = [_V, ctypes.c_int, ctypes.c_int] + [_V] * 11 + [
         ctypes.c_int, ctypes.c_int, _V, ctypes.c_int, _V, _V, ctypes.c_double, ctypes.c_double, ctypes.c_int, _V, _V,
         _V]
     lib.glass_gpu_noise_setup_channels.argtypes = [_V, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _D,

@@ -42,6 +42,27 @@ def test_library_exports_every_declared_symbol(lib):
         assert hasattr(lib, name), name
 
 
+def test_bound_argument_counts_match_the_header(lib):
+    """Every glass_gpu_* binding with argtypes has as many as the header's
+    declaration has parameters (ctypes would pass a short list silently
+    shifted or refuse it at call time)."""
+    text = ""
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text += open(os.path.join(ROOT, "include", h)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    checked = 0
+    for m in re.finditer(r"\b(glass_gpu_\w+)\s*\(([^;{]*)\)\s*;", text):
+        name, params = m.group(1), m.group(2).strip()
+        n = 0 if params in ("", "void") else len(params.split(","))
+        at = getattr(lib, name).argtypes
+        if at is None:
+            continue
+        assert len(at) == n, (name, len(at), n)
+        checked += 1
+    assert checked > 50
+
+
 def test_ucb_bandwidth_matches_reference(lib, golden):
     g = golden("bandwidth.npz")
     L, fstar = 2.5e9, wl.FSTAR
