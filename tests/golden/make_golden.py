@@ -698,6 +698,14 @@ def rj(ref, rng):
     Nl, sr, sd = Nlive.copy(), src.copy(), seed0.copy()
     out = ref.rj_steps(T, NFFT, qmin, dA_i, dE_i, iA, iE, Neff, Nl, sr, prior, logPV, rjw,
                        (tensor, df, dt, dp, maxp), temperature, sd, nsteps)
+    # a death's likelihood change: logL of the first eight chains' starting
+    # models with and without their first source
+    full, without = np.full(8, np.nan), np.full(8, np.nan)
+    for c in range(8):
+        if Nlive[c] > 0:
+            full[c] = ref.log_likelihood(T, NFFT, qmin, dA_i, dE_i, iA, iE, src[c, :Nlive[c]])[0]
+            without[c] = ref.log_likelihood(T, NFFT, qmin, dA_i, dE_i, iA, iE, src[c, 1:Nlive[c]])[0]
+    out["death_full"], out["death_without"] = full, without
     np.savez_compressed(os.path.join(HERE, "rj.npz"), NFFT=NFFT, qmin=qmin, dA=dA_i, dE=dE_i, invCA=iA, invCE=iE,
                         prior=prior, logPV=logPV, tensor=tensor, df=df, dt=dt, dp=dp, maxp=maxp, Nlive0=Nlive,
                         Neff=Neff, src0=src, temperature=temperature, seed0=seed0, rjw=rjw, Nlive_end=Nl,

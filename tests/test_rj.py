@@ -126,27 +126,23 @@ def test_gpu_rj_matches_reference(engine, golden):
 def test_gpu_rj_death_change_from_term(engine, golden, port):
     """A death's likelihood change from the engine's term of the removed
     source against the chain's residual and its (h|h):
-    -(term + hh) = logL(without it) - logL(with it), against the reference."""
+    -(term + hh) = logL(without it) - logL(with it), against the reference's
+    logL of the first chains' starting models with and without their first
+    source."""
     import glass_gb300 as gg
-    from oracle import Ref
 
-    ref = Ref()
     g = golden("rj.npz")
     NFFT, qmin = int(g["NFFT"]), int(g["qmin"])
     dA, dE = g["dA"], g["dE"]
+    checked = 0
     for c in range(8):
         n = int(g["Nlive0"][c])
         if n == 0:
             continue
         srcs = g["src0"][c, :n]
-        full = ref.log_likelihood(T, NFFT, qmin, dA, dE, g["invCA"], g["invCE"], srcs)[0]
-        without = ref.log_likelihood(T, NFFT, qmin, dA, dE, g["invCA"], g["invCE"], srcs[1:])[0] if n > 1 else \
-            ref.log_likelihood(T, NFFT, qmin, dA, dE, g["invCA"], g["invCE"], np.zeros((0, 8)))[0]
-        # the chain's residual: data minus every source of the chain
-        rA, rE = dA.copy(), dE.copy()
+        rA, rE = dA.copy(), dE.copy()  # the chain's residual: the data minus its sources
         for p in srcs:
-            al = port.alignment(T, NFFT, qmin, p)
-            N = int(al[0])
+            N = int(port.alignment(T, NFFT, qmin, p)[0])
             h = port.waveform(p, N, T)
             i0 = int(p[0]) - N // 2 - qmin
             for r, hc in ((rA, h[3]), (rE, h[4])):
@@ -155,10 +151,13 @@ def test_gpu_rj_death_change_from_term(engine, golden, port):
                     if 0 <= j < NFFT:
                         r[2 * j] -= hc[2 * m]
                         r[2 * j + 1] -= hc[2 * m + 1]
-        bank = wl.SegmentBank(dA=(rA[0::2] + 1j * rA[1::2])[None], dE=(rE[0::2] + 1j * rE[1::2])[None],
-                              invCA=g["invCA"][None].copy(), invCE=g["invCE"][None].copy(),
-                              qmin=np.array([qmin], np.int32), NFFT=NFFT, T=T)
+        bank = wl.SegmentBank(T=T, NFFT=NFFT, qmin=np.array([qmin], np.int32),
+                              dA=(rA[0::2] + 1j * rA[1::2])[None], dE=(rE[0::2] + 1j * rE[1::2])[None],
+                              invCA=g["invCA"][None].copy(), invCE=g["invCE"][None].copy())
         engine.upload(bank)
         term, _, hh, st = engine.dlogl_host(np.zeros(1, np.int32), srcs[:1], precision=gg.PREC_FP64)
         assert st[0] == 0
-        assert abs(-(term[0] + hh[0]) - (without - full)) <= 1e-8 * max(1.0, abs(full)), c
+        want = g["death_without"][c] - g["death_full"][c]
+        assert abs(-(term[0] + hh[0]) - want) <= 1e-8 * max(1.0, abs(g["death_full"][c])), (c, term, hh, want)
+        checked += 1
+    assert checked >= 3
