@@ -35,12 +35,12 @@ namespace glass {
 constexpr int kHpThreads = 256;
 
 // -------------------------------------------------------- slow part, df
-// Arm q of the two of spacecraft i (12, 13 | 21, 23 | 31, 32) at one sample,
-// as slow_sample_mix computes it, in double-float throughout.  tab: the
+// The two arms of spacecraft i (12, 13 | 21, 23 | 31, 32) at one sample, as
+// slow_sample_mix computes them, in double-float throughout.  tab: the
 // sine/cosine table of df_sincos_tab.
-__device__ __forceinline__ dc slow_arm_hp(const ItemMix &c, const OrbitSampleMix &o, const GeoSampleMix &gm,
-                                          const GeoSampleMix &gl, const SlowArgs &K, const float4 *tab, int i,
-                                          int q) {
+__device__ __forceinline__ void slow_arms_hp(const ItemMix &c, const OrbitSampleMix &o, const GeoSampleMix &gm,
+                                             const GeoSampleMix &gl, const SlowArgs &K, const float4 *tab, int i,
+                                             dc d[2]) {
   const df k0 = {c.k[0], c.kl[0]}, k1 = {c.k[1], c.kl[1]}, k2 = {c.k[2], c.kl[2]};
   // k.(x_j - x_gc) for the three spacecraft (metres)
   df kd[3];
@@ -62,7 +62,8 @@ __device__ __forceinline__ dc slow_arm_hp(const ItemMix &c, const OrbitSampleMix
   const df aev = df_add(df{1.f, 0.f}, df_mul(df{c.aef, c.aefl}, v));
   const df arg2 = df_add(df_add(psi0, df_neg(df_mul(df{c.w0c, c.w0cl}, kd[i]))),
                          df_mul(c.p7pi_d, df_mul(tT, df_add(tT, df{-2.f * u.hi, -2.f * u.lo}))));
-  {
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
     const int a = ua[q];
     df kr = df_mul(df_add(kd[ends[a][1]], df_neg(kd[ends[a][0]])), K.invLd);
     if (neg[q]) kr = df_neg(kr);
@@ -83,22 +84,20 @@ __device__ __forceinline__ dc slow_arm_hp(const ItemMix &c, const OrbitSampleMix
     df_sincos_tab(df_add(arg1, df_neg(arg2)), tab, &s2, &c2);
     const df re = df_add(df_mul(t1r, c2), df_mul(t1i, s2));
     const df im = df_add(df_mul(t1i, c2), df_neg(df_mul(t1r, s2)));
-    return {df_mul(sinc, re), df_mul(sinc, im)};
+    d[q] = {df_mul(sinc, re), df_mul(sinc, im)};
   }
 }
 
-// One CTA of six warps per 32 consecutive samples of one binned proposal,
-// grid-stride over all of them: warp w computes arm w & 1 of spacecraft
-// w >> 1 (the spacecraft's common prefix in both of its warps, then one arm:
-// a shorter dependent chain per sample than two arms in turn); warps 0 and 1
-// then form the A and E arm combinations of ae_combos in double-float.
+// One CTA of three warps per 32 consecutive samples of one binned proposal,
+// grid-stride over all of them: warp i computes the arms of spacecraft i (a
+// third of the dependent chain of a sample each, on separate SM
+// sub-partitions); warps 0 and 1 then form the A and E arm combinations of
+// ae_combos in double-float.
 // sin(k pi / 32), cos(k pi / 32) as hi + lo floats {s.hi, s.lo, c.hi, c.lo},
 // k < 64: built once per device on the host (hp_sincos_table).
 static __device__ float4 g_hp_sincos[64];
 
-constexpr int kSlowHpThreads = 192;
-
-__global__ void __launch_bounds__(kSlowHpThreads) fd_slow_hp_kernel(SlowArgs a) {
+__global__ void __launch_bounds__(96) fd_slow_hp_kernel(SlowArgs a) {
   __shared__ dc s_d[6][32];
   __shared__ float4 s_tab[64];
   if (threadIdx.x < 64) s_tab[threadIdx.x] = g_hp_sincos[threadIdx.x];
@@ -135,7 +134,10 @@ __global__ void __launch_bounds__(kSlowHpThreads) fd_slow_hp_kernel(SlowArgs a) 
     if (!iok) item = 0;
     const long long o0 = ((long long)cb * 32 + (long long)slot * N) * 4 + n;
     const bool wok = lok && iok && chk(o0 >= 0 && o0 + 3LL * N < a.series_len, kChkSeriesWrite);
-    s_d[sc][lane] = slow_arm_hp(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.geolo[b][n], a, s_tab, sc >> 1, sc & 1);
+    dc d2[2];
+    slow_arms_hp(a.itemsmix[item], a.mix[b][n], a.geo[b][n], a.geolo[b][n], a, s_tab, sc, d2);
+    s_d[2 * sc][lane] = d2[0];
+    s_d[2 * sc + 1][lane] = d2[1];
     __syncthreads();
     if (sc < 2 && wok) {
       dc d[6];
@@ -332,10 +334,10 @@ cudaError_t fd_launch_reeval(const SlowArgs &sa, const HpArgs &h, bool perch, in
   static LaunchSetup slow_setup;
   int occ = 0;
   e = launch_setup(slow_setup, [&](int *o) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_slow_hp_kernel, kSlowHpThreads, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(o, fd_slow_hp_kernel, 96, 0);
   }, &occ);
   if (e != cudaSuccess) return e;
-  fd_slow_hp_kernel<<<(occ > 0 ? occ : 1) * num_sms, kSlowHpThreads, 0, stream>>>(sa);
+  fd_slow_hp_kernel<<<(occ > 0 ? occ : 1) * num_sms, 96, 0, stream>>>(sa);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   e = perch ? launch_hp<true>(h, num_sms, stream) : launch_hp<false>(h, num_sms, stream);
   if (nlaunch) *nlaunch += 2;
