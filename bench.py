@@ -91,7 +91,7 @@ def spec_flops_per_eval(N):
 # ncu flushes the caches before the launch, so the spectral kernel's figure is
 # its series scratch (4 x N complex floats per proposal, ~29 MB) read from DRAM;
 # in a live step the slow-part kernel has just written it to L2.
-PROFILED_DRAM_BYTES = {"fd_spec_all_kernel<1, 0>": 31018800 + 768, "fd_slow_kernel<1>": 598528}
+PROFILED_DRAM_BYTES = {"fd_spec_all_kernel<1, 0>": 32264704 + 16128, "fd_slow_kernel<1>": 598528}
 
 
 def make_workload(rank, steps):
