@@ -64,7 +64,7 @@ EXPORTS = (
     "glass_gpu_noise_wavelet_logl_batch_sgwb", "glass_gpu_noise_wavelet_logl_batch_sgwb_host",
     "glass_gpu_checked_build", "glass_gpu_check_status",
     "glass_gpu_spline_noise_setup", "glass_gpu_spline_noise_logl_batch", "glass_gpu_spline_noise_logl_batch_host",
-    "glass_gpu_noise_setup_channels", "glass_gpu_rj_propose", "glass_gpu_rj_accept",
+    "glass_gpu_noise_setup_channels", "glass_gpu_rj_propose", "glass_gpu_rj_accept", "glass_gpu_wavelet_reevaluated",
 )
 
 _lib = None
@@ -104,6 +104,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.glass_gpu_set_mixed_tolerance.argtypes = [_V, ctypes.c_double]
     lib.glass_gpu_set_mixed_tolerance_scale.argtypes = [_V, ctypes.c_int, _D]
     lib.glass_gpu_mixed_reevaluated.argtypes = [_V, _V]
+    lib.glass_gpu_wavelet_reevaluated.argtypes = [_V, _V]
     lib.glass_gpu_set_tuning.argtypes = [_V, ctypes.c_char_p, ctypes.c_int]
     lib.glass_gpu_sym_eigen8.argtypes = [_V, ctypes.c_int, _V, _V, _V]
     lib.glass_gpu_prior_draw.argtypes = [_V, ctypes.c_int, _V, ctypes.c_int, _V, _V, _V, _V]
@@ -732,6 +733,13 @@ class Engine:
         (synchronises the stream)."""
         n = ctypes.c_ulonglong(0)
         _check(self.lib.glass_gpu_mixed_reevaluated(self._ctx, ctypes.byref(n)))
+        return int(n.value)
+
+    def wavelet_reevaluated(self) -> int:
+        """Number of wavelet-domain sources the mixed likelihood evaluated
+        again in FP64 so far (synchronises the stream)."""
+        n = ctypes.c_ulonglong(0)
+        _check(self.lib.glass_gpu_wavelet_reevaluated(self._ctx, ctypes.byref(n)))
         return int(n.value)
 
 

@@ -2260,6 +2260,19 @@ extern "C" int glass_gpu_wavelet_setup(glass_gpu_ctx *ctx, double Tobs, double t
   const size_t wb = wv_work_bytes(kWvChunk, ctx->wv.norb, NT);
   GLASS_CUDA(cudaMalloc(&ctx->wv_work_mem, wb), "cudaMalloc(wavelet work)");
   wv_work_carve(ctx->wvw, ctx->wv_work_mem, kWvChunk, ctx->wv.norb, NT);
+  GLASS_CUDA(cudaMemset(ctx->wvw.total, 0, sizeof(unsigned long long)), "cudaMemset(wavelet re-evaluation count)");
+  return GLASS_OK;
+}
+
+extern "C" int glass_gpu_wavelet_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count) {
+  if (!ctx || !count) return set_err(GLASS_ERR_ARG, "glass_gpu_wavelet_reevaluated: null argument");
+  *count = 0;
+  if (!ctx->wvw.total) return GLASS_OK;
+  int rc = ctx_activate(ctx);
+  if (rc) return rc;
+  GLASS_CUDA(cudaMemcpyAsync(count, ctx->wvw.total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream),
+             "read wavelet re-evaluation count");
+  GLASS_CUDA(cudaStreamSynchronize(ctx->stream), "read wavelet re-evaluation count");
   return GLASS_OK;
 }
 
@@ -2330,7 +2343,7 @@ extern "C" int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int precision, 
     GLASS_CUDA(wv_dlogl_launch(ctx->wv, ctx->wvw, precision, n, term_x ? term_x + off : nullptr,
                                dlogl ? dlogl + off : nullptr,
                                term_y ? term_y + off : nullptr, hh ? hh + off : nullptr,
-                               status ? status + off : nullptr, ctx->stream, &ctx->last_launches),
+                               status ? status + off : nullptr, ctx->stream, &ctx->last_launches, ctx->mixed_tol),
                "wavelet dlogl launch");
   }
   return GLASS_OK;

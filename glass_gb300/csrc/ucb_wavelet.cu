@@ -622,9 +622,14 @@ constexpr int kLayerThreads = 256;
 
 __global__ void __launch_bounds__(kLayerThreads) wv_layers_kernel(WvGridDev g, int n, const WvSrc *srcs,
                                                                   const double *ssb, const double *tdi,
-                                                                  double *coef) {
+                                                                  double *coef, const int *count, const int *list) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  const int s = blockIdx.x / 3, ch = blockIdx.x - 3 * (blockIdx.x / 3);
+  int s = blockIdx.x / 3;
+  const int ch = blockIdx.x - 3 * (blockIdx.x / 3);
+  if (list) {  // the sources of a re-evaluation list, list[0 .. *count - 1]
+    if (s >= *count) return;
+    s = list[s];
+  }
   const WvSrc &S = srcs[s];
   if (S.status || S.c == 0) return;
   const int nl = S.nl, NT = g.NT, Nds = NT * (nl + 1), M = Nds / 2, norb = g.norb;
@@ -770,8 +775,12 @@ constexpr int kDloglThreads = 256;
 __global__ void __launch_bounds__(kDloglThreads) wv_dlogl_kernel(WvGridDev g, int n, const WvSrc *srcs,
                                                                  const double *coef, const double *term_x,
                                                                  double *dlogl, double *term_y, double *hh_out,
-                                                                 int *status) {
-  const int s = blockIdx.x;
+                                                                 int *status, const int *count, const int *list) {
+  int s = blockIdx.x;
+  if (list) {
+    if (s >= *count) return;
+    s = list[s];
+  }
   const WvSrc &S = srcs[s];
   __shared__ double red[2][kDloglThreads / 32];
   if (S.status) {
@@ -975,11 +984,13 @@ __global__ void __launch_bounds__(kLayerThreads) wv_layers_mix_kernel(WvGridDev 
 __global__ void __launch_bounds__(kDloglThreads) wv_dlogl_mix_kernel(WvGridDev g, int n, const WvSrc *srcs,
                                                                      const float *coef, const double *term_x,
                                                                      double *dlogl, double *term_y, double *hh_out,
-                                                                     int *status) {
+                                                                     int *status, double kest, int *count, int *list,
+                                                                     unsigned long long *total) {
   const int s = blockIdx.x;
   const WvSrc &S = srcs[s];
   __shared__ float2 red[2][kDloglThreads / 32];
   __shared__ double redq[kDloglThreads / 32];
+  __shared__ float rede[kDloglThreads / 32];
   if (S.status) {
     if (threadIdx.x == 0) {
       if (dlogl) dlogl[s] = NAN;
@@ -994,6 +1005,7 @@ __global__ void __launch_bounds__(kDloglThreads) wv_dlogl_mix_kernel(WvGridDev g
   const float *rh = g.res_hi, *rl = g.res_lo, *ic = g.invC32;
   df acc = {0.f, 0.f}, hacc = {0.f, 0.f};
   double qacc = 0.0;
+  float eacc = 0.f;  // (r - h)^T C (r - h), for the error estimate
   for (int q = threadIdx.x; q < npix; q += blockDim.x) {
     const int i = q / c, j = S.jlo + (q - i * c);
     const int k = i + j * NT - g.kmin;
@@ -1008,11 +1020,13 @@ __global__ void __launch_bounds__(kDloglThreads) wv_dlogl_mix_kernel(WvGridDev g
     const float e0 = (r0h - a0) + r0l, e1 = (r1h - a1) + r1l, e2 = (r2h - a2) + r2l;
     const float ee = e0 * e0 + e1 * e1 + e2 * e2;
     const float hn = a0 * a0 + a1 * a1 + a2 * a2, rn = r0h * r0h + r1h * r1h + r2h * r2h;
+    const float te = e0 * (e0 * c00 + e1 * c01 + e2 * c02) + e1 * (e0 * c10 + e1 * c11 + e2 * c12) +
+                     e2 * (e0 * c20 + e1 * c21 + e2 * c22);
+    eacc += te;
     float t;
     if (ee * ee <= hn * (hn + 4.f * rn)) {
       // residual form: rounding ~ |e|^2, the data term exact in FP64
-      t = e0 * (e0 * c00 + e1 * c01 + e2 * c02) + e1 * (e0 * c10 + e1 * c11 + e2 * c12) +
-          e2 * (e0 * c20 + e1 * c21 + e2 * c22);
+      t = te;
       qacc += g.qpix[k];
     } else {
       // direct form: rounding ~ |h| (|h| + 2 |r|)
@@ -1030,21 +1044,31 @@ __global__ void __launch_bounds__(kDloglThreads) wv_dlogl_mix_kernel(WvGridDev g
     acc = df_add(acc, ao);
     hacc = df_add(hacc, ho);
     qacc += __shfl_xor_sync(0xffffffffu, qacc, o);
+    eacc += __shfl_xor_sync(0xffffffffu, eacc, o);
   }
   if ((threadIdx.x & 31) == 0) {
     red[0][threadIdx.x >> 5] = make_float2(acc.hi, acc.lo);
     red[1][threadIdx.x >> 5] = make_float2(hacc.hi, hacc.lo);
     redq[threadIdx.x >> 5] = qacc;
+    rede[threadIdx.x >> 5] = eacc;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double sr = 0.0, sh = 0.0, sq = 0.0;
+    double sr = 0.0, sh = 0.0, sq = 0.0, se = 0.0;
     for (int w = 0; w < kDloglThreads / 32; w++) {
       sr += (double)red[0][w].x + (double)red[0][w].y;
       sh += (double)red[1][w].x + (double)red[1][w].y;
       sq += redq[w];
+      se += (double)rede[w];
     }
     const double term = sr - sq;
+    // The template's relative error eps gives |delta logL error| <~
+    // 2 eps sqrt((h|h) (r-h|r-h)) (the error is delta h^T C (h - r)); past
+    // the tolerance, or not finite, the source is listed for FP64.
+    if (kest > 0.0 && c != 0 && (!isfinite(term) || !(kest * sqrt(fmax(sh, 0.0) * fmax(se, 0.0)) <= 1.0))) {
+      list[atomicAdd(count, 1)] = s;
+      atomicAdd(total, 1ull);
+    }
     if (term_y) term_y[s] = term;
     if (hh_out) hh_out[s] = sh;
     if (dlogl) {
@@ -1196,7 +1220,8 @@ size_t wv_work_bytes(int cap, int norb, int NT) {
   auto pad = [](size_t b) { return (b + 255) / 256 * 256; };
   return pad(sizeof(WvSrc) * (size_t)cap) + pad(sizeof(double) * (size_t)cap * 8 * norb) +
          pad(sizeof(double) * (size_t)cap * 7 * norb) + pad(sizeof(double) * (size_t)cap * 24 * norb) +
-         pad(sizeof(double) * (size_t)cap * 3 * kWvMaxLayers * NT);
+         pad(sizeof(double) * (size_t)cap * 3 * kWvMaxLayers * NT) + pad(sizeof(unsigned long long)) +
+         pad(sizeof(int) * ((size_t)cap + 1));
 }
 
 void wv_work_carve(WvWorkDev &w, void *base, int cap, int norb, int NT) {
@@ -1212,6 +1237,11 @@ void wv_work_carve(WvWorkDev &w, void *base, int cap, int norb, int NT) {
   w.tdi = (double *)p;
   p += pad(sizeof(double) * (size_t)cap * 24 * norb);
   w.coef = (double *)p;
+  p += pad(sizeof(double) * (size_t)cap * 3 * kWvMaxLayers * NT);
+  w.total = (unsigned long long *)p;
+  p += pad(sizeof(unsigned long long));
+  w.count = (int *)p;
+  w.list = w.count + 1;
 }
 
 cudaError_t wv_build_grid(const WvGridHost &h, WvGridDev *g, void **mem, cudaStream_t s) {
@@ -1512,7 +1542,7 @@ cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int preci
     const size_t sm = layers_smem(g.NT);
     e = cudaFuncSetAttribute(wv_layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    wv_layers_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, w.coef);
+    wv_layers_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, w.coef, nullptr, nullptr);
   }
   if (nlaunch) *nlaunch += 4;
   return cudaGetLastError();
@@ -1531,14 +1561,35 @@ cudaError_t wv_fisher_launch(const WvGridDev &g, const WvWorkDev &w, int n, cons
 }
 
 cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *term_x,
-                            double *dlogl, double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch) {
+                            double *dlogl, double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch,
+                            double tol) {
   if (n <= 0) return cudaSuccess;
-  if (precision == 1)
+  if (precision == 1) {
+    const double kest = tol > 0.0 ? kWvMixedErrK / tol : 0.0;
+    cudaError_t e;
+    if (kest > 0.0 && (e = cudaMemsetAsync(w.count, 0, sizeof(int), s)) != cudaSuccess) return e;
     wv_dlogl_mix_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, reinterpret_cast<const float *>(w.coef), term_x,
-                                                    dlogl, term_y, hh, status);
-  else
-    wv_dlogl_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, w.coef, term_x, dlogl, term_y, hh, status);
-  if (nlaunch) *nlaunch += 1;
+                                                    dlogl, term_y, hh, status, kest, w.count, w.list, w.total);
+    if (nlaunch) *nlaunch += 1;
+    if (kest > 0.0) {
+      // the listed sources again in FP64: their layers (over the mixed
+      // coefficients, which are no longer read) and their likelihood; the
+      // grids cover every source and the CTAs past the list return at once
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      const size_t sm = layers_smem(g.NT);
+      if ((e = cudaFuncSetAttribute(wv_layers_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) !=
+          cudaSuccess)
+        return e;
+      wv_layers_kernel<<<3 * n, kLayerThreads, sm, s>>>(g, n, w.src, w.ssb, w.tdi, w.coef, w.count, w.list);
+      wv_dlogl_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, w.coef, term_x, dlogl, term_y, hh, status, w.count,
+                                                  w.list);
+      if (nlaunch) *nlaunch += 2;
+    }
+  } else {
+    wv_dlogl_kernel<<<n, kDloglThreads, 0, s>>>(g, n, w.src, w.coef, term_x, dlogl, term_y, hh, status, nullptr,
+                                                nullptr);
+    if (nlaunch) *nlaunch += 1;
+  }
   return cudaGetLastError();
 }
 

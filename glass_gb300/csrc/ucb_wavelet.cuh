@@ -54,6 +54,11 @@ struct WvWorkDev {
   double *resp = nullptr;  // [cap][7][norb] M (3), Mf (3), phase at S/C 1
   double *tdi = nullptr;   // [cap][3][2][4][norb] per-channel amplitude / phase splines
   double *coef = nullptr;  // [cap][3][kWvMaxLayers NT] coefficients, list order first
+  // the mixed likelihood's re-evaluation list: total[0] counts the sources
+  // re-evaluated over the context's life, count[0] those of the current
+  // launch, list[k] their indices
+  unsigned long long *total = nullptr;
+  int *count = nullptr, *list = nullptr;
 };
 
 // Host-side grid description: orbit nodes and positions plus the WDM grid.
@@ -88,8 +93,15 @@ cudaError_t wv_waveform_launch(const WvGridDev &g, const WvWorkDev &w, int preci
                                int *status, cudaStream_t s, int *nlaunch);
 // Sparse likelihood over each source's pixels (after wv_waveform_launch with
 // the same precision).
+// The mixed likelihood's error estimate: |delta logL error| <~ K sqrt((h|h)
+// (r - h|r - h)), K = 2 eps with eps the FP32 template's relative error
+// (rms ~4e-7 over its pixels); with tol > 0 every source whose estimate
+// exceeds tol (or whose mixed result is not finite) is evaluated again in FP64
+// in the same launch sequence.
+constexpr double kWvMixedErrK = 1e-6;
 cudaError_t wv_dlogl_launch(const WvGridDev &g, const WvWorkDev &w, int precision, int n, const double *term_x,
-                            double *dlogl, double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch);
+                            double *dlogl, double *term_y, double *hh, int *status, cudaStream_t s, int *nlaunch,
+                            double tol = 0.0);
 // Fisher matrices of n sources (ucb_fisher_wavelet) in FP64: pp is scratch for
 // 16 n perturbed parameter vectors; needs 16 n <= w.cap; fisher[64 s + 8 i + j].
 cudaError_t wv_fisher_launch(const WvGridDev &g, const WvWorkDev &w, int n, const double *params, double *pp,

@@ -808,9 +808,16 @@ int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, const doubl
  * layer transforms in FP32, the likelihood from FP32 products with
  * double-float sums, per pixel in the form (residual or direct) with the
  * smaller rounding error.  Its error against FP64 is set by the FP32 template
- * (relative ~1e-6): about 1e-6 x |h| x |r - h| summed over the pixels, so it is
- * below 1e-3 where the residual holds noise and the source's own signal, and
- * grows where an unsubtracted loud signal shares the source's pixels.
+ * (relative ~4e-7 rms): at most ~1e-6 sqrt((h|h) (r - h|r - h)), below 1e-3
+ * where the residual holds noise and the source's own signal, and growing
+ * where a loud template meets data that do not contain it.  With the
+ * context's mixed tolerance (glass_gpu_set_mixed_tolerance, default 1e-3;
+ * the per-proposal scale is not applied here) every source whose estimate
+ * 1e-6 sqrt((h|h) (r - h|r - h)) exceeds it, or whose mixed result is not
+ * finite, is evaluated again in FP64 in the same launch sequence (two more
+ * launches), so that |delta logL error| stays below the tolerance; tol <= 0
+ * gives the mixed values alone.  glass_gpu_wavelet_reevaluated counts those
+ * sources over the context's life (synchronises the stream).
  *
  * For each of nitems parameter vectors params[8 i ..] (the reference's UCB
  * params array), the wavelet waveform on its pixel list and
@@ -827,6 +834,7 @@ int glass_gpu_wavelet_dlogl_batch(glass_gpu_ctx *ctx, int precision, int nitems,
                                   const double *term_x, double *dlogl, double *term_y, double *hh, int *status);
 int glass_gpu_wavelet_dlogl_batch_host(glass_gpu_ctx *ctx, int precision, int nitems, const double *params,
                                        const double *term_x, double *dlogl, double *term_y, double *hh, int *status);
+int glass_gpu_wavelet_reevaluated(glass_gpu_ctx *ctx, unsigned long long *count);
 
 /*
  * The waveforms themselves: info[4 i ..] = first layer, layer count, first

@@ -7,9 +7,10 @@ within 1e-10 relative to max(1, |delta logL|).
 
 Mixed precision (FP64 phase, FP32 amplitude, FFTs and products, double-float
 sums) against FP64: waveform values within 1e-5 of the channel's largest
-value; delta logL within 1e-3 absolute where |delta logL| is small (proposals
-near the injection in data of noise plus that source), and within 1e-5 of
-|delta logL| elsewhere; <h|h> within 1e-5 relative.
+value; delta logL within 1e-3 absolute for every source at the default
+tolerance (sources whose error estimate exceeds it are evaluated again in
+FP64), and without the re-evaluation within 1e-3 where |delta logL| is small
+and 1e-5 of |delta logL| elsewhere; <h|h> within 1e-5 relative.
 """
 import numpy as np
 import pytest
@@ -192,7 +193,9 @@ def test_mixed_dlogl_error_budget(engine, golden):
         props = np.concatenate([g[f"c{c}_props"], wide])
         txs = np.full(len(props), tx[0])
         dl64, _, hh64, s64 = engine.wavelet_dlogl_host(props, term_x=txs)
+        engine.set_mixed_tolerance(0.0)  # the mixed values alone
         dl32, _, hh32, s32 = engine.wavelet_dlogl_host(props, term_x=txs, precision=gg.PREC_MIXED)
+        engine.set_mixed_tolerance(1e-3)
         np.testing.assert_array_equal(s32, s64)
         ok = s64 == 0
         assert ok.sum() >= len(g[f"c{c}_props"])
@@ -202,6 +205,44 @@ def test_mixed_dlogl_error_budget(engine, golden):
         assert (err[near] < MIXED_ABS).all(), err[near].max()
         assert (err[~near] < MIXED_REL_FAR * ref[~near]).all()
         np.testing.assert_allclose(hh32[ok], hh64[ok], rtol=MIXED_REL_FAR)
+        # at the default tolerance: every source within 1e-3
+        dlt, _, _, st = engine.wavelet_dlogl_host(props, term_x=txs, precision=gg.PREC_MIXED)
+        np.testing.assert_array_equal(st, s64)
+        assert (np.abs(dlt - dl64)[ok] < MIXED_ABS).all(), np.abs(dlt - dl64)[ok].max()
+
+
+def test_mixed_tolerance_loud_templates(engine, golden):
+    """Loud templates against data that do not contain them (the injection
+    made 30 to 3000 times louder and moved by up to 40 layers' worth of
+    frequency): the mixed values alone miss 1e-3, the default tolerance's
+    FP64 re-evaluation brings every source within it, and the re-evaluated
+    sources are counted."""
+    g = golden("wavelet_likelihood.npz")
+    NF, NT, wdt, Tobs = GRIDS[str(g["grid"])]
+    kmin, kmax = int(g["c0_kmin"]), int(g["c0_kmax"])
+    setup_grid(engine, (NF, NT, wdt, Tobs), 0.0, kmin, kmax)
+    engine.wavelet_set_data(g["c0_d"], wl.wavelet_invC(kmax - kmin, NT, kmin, float(g["c0_scale"])))
+    inj = g["c0_inj"]
+    props = []
+    for fa in (30.0, 300.0, 3000.0):
+        for df in (0.0, 3.0, 10.0, 40.0):
+            p = inj.copy()
+            p[3] += np.log(fa)
+            p[0] += df * 0.5 * NT  # bins of 1/Tobs: half a layer per NT/2
+            props.append(p)
+    props = np.array(props)
+    dl64, _, _, s64 = engine.wavelet_dlogl_host(props)
+    ok = s64 == 0
+    assert ok.sum() >= 8
+    engine.set_mixed_tolerance(0.0)
+    raw, _, _, _ = engine.wavelet_dlogl_host(props, precision=gg.PREC_MIXED)
+    engine.set_mixed_tolerance(1e-3)
+    assert (np.abs(raw - dl64)[ok] > MIXED_ABS).any()
+    n0 = engine.wavelet_reevaluated()
+    dlt, _, _, st = engine.wavelet_dlogl_host(props, precision=gg.PREC_MIXED)
+    np.testing.assert_array_equal(st, s64)
+    assert (np.abs(dlt - dl64)[ok] < MIXED_ABS).all(), np.abs(dlt - dl64)[ok].max()
+    assert engine.wavelet_reevaluated() - n0 >= int((np.abs(raw - dl64)[ok] > MIXED_ABS).sum())
 
 
 def _fisher_oracle(port, p, grid, t0, kmin, kmax, invC, imin, imax):
