@@ -645,7 +645,7 @@ def bench_wavelet(gg, torch, dev, rank, steps, warmup, cpu, peak64):
 
     acc = accuracy(dl32, hh32, st32)
     acc["criterion"] = ("|delta logL error| < 1e-3 vs FP64 on every source: those whose estimate "
-                        "1e-6 sqrt((h|h) (r-h|r-h)) exceeds it are evaluated again in FP64 in the same launches")
+                        "2e-7 sqrt((h|h) (r-h|r-h)) exceeds it are evaluated again in FP64 in the same launches")
     acc_raw = accuracy(dlraw, hhraw, straw)
     acc_raw["error_model"] = ("|err| ~ eps_t SNR |h - r| with eps_t ~ 4e-7 the FP32 template's relative error: "
                               "small where the residual holds the source (r ~ h + noise), ~ eps_t SNR^2 where "

@@ -1062,9 +1062,9 @@ __global__ void __launch_bounds__(kDloglThreads) wv_dlogl_mix_kernel(WvGridDev g
       se += (double)rede[w];
     }
     const double term = sr - sq;
-    // The template's relative error eps gives |delta logL error| <~
-    // 2 eps sqrt((h|h) (r-h|r-h)) (the error is delta h^T C (h - r)); past
-    // the tolerance, or not finite, the source is listed for FP64.
+    // The template's error delta h gives |delta logL error| ~
+    // |delta h^T C (h - r)| <~ kWvMixedErrK sqrt((h|h) (r-h|r-h)); past the
+    // tolerance, or not finite, the source is listed for FP64.
     if (kest > 0.0 && c != 0 && (!isfinite(term) || !(kest * sqrt(fmax(sh, 0.0) * fmax(se, 0.0)) <= 1.0))) {
       list[atomicAdd(count, 1)] = s;
       atomicAdd(total, 1ull);

@@ -808,12 +808,12 @@ int glass_gpu_wavelet_set_data(glass_gpu_ctx *ctx, const double *rX, const doubl
  * layer transforms in FP32, the likelihood from FP32 products with
  * double-float sums, per pixel in the form (residual or direct) with the
  * smaller rounding error.  Its error against FP64 is set by the FP32 template
- * (relative ~4e-7 rms): at most ~1e-6 sqrt((h|h) (r - h|r - h)), below 1e-3
- * where the residual holds noise and the source's own signal, and growing
+ * (relative ~4e-7 rms): measured below 1e-7 sqrt((h|h) (r - h|r - h)), below
+ * 1e-3 where the residual holds noise and the source's own signal, and growing
  * where a loud template meets data that do not contain it.  With the
  * context's mixed tolerance (glass_gpu_set_mixed_tolerance, default 1e-3;
  * the per-proposal scale is not applied here) every source whose estimate
- * 1e-6 sqrt((h|h) (r - h|r - h)) exceeds it, or whose mixed result is not
+ * 2e-7 sqrt((h|h) (r - h|r - h)) exceeds it, or whose mixed result is not
  * finite, is evaluated again in FP64 in the same launch sequence (two more
  * launches), so that |delta logL error| stays below the tolerance; tol <= 0
  * gives the mixed values alone.  glass_gpu_wavelet_reevaluated counts those

@@ -213,8 +213,8 @@ def test_mixed_dlogl_error_budget(engine, golden):
 
 def test_mixed_tolerance_loud_templates(engine, golden):
     """Loud templates against data that do not contain them (the injection
-    made 30 to 3000 times louder and moved by up to 40 layers' worth of
-    frequency): the mixed values alone miss 1e-3, the default tolerance's
+    made 30 to 3000 times louder and moved in frequency by up to two layers):
+    the mixed values alone miss 1e-3, the default tolerance's
     FP64 re-evaluation brings every source within it, and the re-evaluated
     sources are counted."""
     g = golden("wavelet_likelihood.npz")
@@ -225,7 +225,7 @@ def test_mixed_tolerance_loud_templates(engine, golden):
     inj = g["c0_inj"]
     props = []
     for fa in (30.0, 300.0, 3000.0):
-        for df in (0.0, 3.0, 10.0, 40.0):
+        for df in (0.0, 0.5, 1.0, 2.0):
             p = inj.copy()
             p[3] += np.log(fa)
             p[0] += df * 0.5 * NT  # bins of 1/Tobs: half a layer per NT/2
