@@ -1506,6 +1506,260 @@ __global__ void __launch_bounds__(SpecCfg<N>::CTA) fd_spec_kernel(SpecArgs a) {
     spec_unit<N, MIX, GPC, PERCH>(a, a.bin_list, count, base, series, tw, bufs, red);
 }
 
+// ------------------------------------------- mixed spectral unit, size at run time
+// The persistent spectral kernel runs units of six sizes side by side on every
+// SM.  Instantiated per size, each unit is a separate fully unrolled copy of
+// the FFT and the bin epilogue, and together they overflow the SM's
+// instruction caches: a launch of the headline step missed in the per-SM
+// instruction cache on ~40% of its fetches and its warps stalled on
+// instruction fetch more than on any load.  The versions below take log2 N at
+// run time, so every size shares one copy of the epilogue, the reductions and
+// each radix's stage (the radix, which sets the register DFT, stays a
+// template argument: 16 for the first stage of every size and the second of
+// 256..1024, then 2, 4 or 8).  The arithmetic and its order are those of
+// fft4_reg and the mixed branch of spec_unit.
+
+__device__ __forceinline__ void group_sync_rt(int gt) {
+  if (gt <= 32) {
+    __syncwarp();
+  } else {
+    __syncthreads();
+  }
+}
+
+// One Stockham stage of radix R (as reg_stage), sub-transform size P = 2^lp,
+// on a padded series of N = 2^ln points.
+template <int R, typename TW>
+__device__ __forceinline__ void reg_stage_rt(float2 *y, const TW *tw, int t, float2 *v, int ln, int lp, int gt) {
+  constexpr int NB = 16 / R, LR = ilog2c(R);
+  const int M = 1 << (ln - 4), lstride = ln - LR, lts = ln - lp - LR, pm = (1 << lp) - 1;
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int i = t + M * b, k = i & pm;
+#pragma unroll
+    for (int m = 0; m < R; ++m) {
+      float2 val = y[pad16(i + (m << lstride))];
+      if (m > 0) val = twmul(val, tw[pad16((m * k) << lts)]);
+      v[b * R + m] = val;
+    }
+  }
+  group_sync_rt(gt);  // every read of the stage before the in-place writes
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    dft_reg<R>(v + b * R);
+    const int i = t + M * b, k = i & pm;
+#pragma unroll
+    for (int q = 0; q < R; ++q) y[pad16((i - k) * R + k + (q << lp))] = v[b * R + q];
+  }
+  group_sync_rt(gt);
+}
+
+// fft4_reg for N = 2^ln, 32 <= N <= 1024, by the group's GT = N/4 threads.
+template <typename TW>
+__device__ __forceinline__ void fft4_reg_rt(const float2 *src, float2 *sbuf, const TW *tw, int lane, int ln) {
+  const int N = 1 << ln, M = N >> 4, gt = N >> 2;
+  const int s = lane >> (ln - 4), t = lane & (M - 1);
+  const float2 *x = src + (size_t)s * N;
+  float2 *y = sbuf + s * pad16(N);
+  float2 v[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = x[t + m * M];
+  dft_reg<16>(v);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) y[pad16(t * 16 + q)] = v[q];
+  group_sync_rt(gt);
+  if (ln >= 8) {
+    reg_stage_rt<16>(y, tw, t, v, ln, 4, gt);
+    if (ln == 9) {
+      reg_stage_rt<2>(y, tw, t, v, ln, 8, gt);
+    } else if (ln == 10) {
+      reg_stage_rt<4>(y, tw, t, v, ln, 8, gt);
+    }
+  } else if (ln == 7) {
+    reg_stage_rt<8>(y, tw, t, v, ln, 4, gt);
+  } else if (ln == 6) {
+    reg_stage_rt<4>(y, tw, t, v, ln, 4, gt);
+  } else {
+    reg_stage_rt<2>(y, tw, t, v, ln, 4, gt);
+  }
+}
+
+// group_sum_df / group_sum4 for a group of gt threads.
+__device__ __forceinline__ df group_sum_df_rt(df s, float2 *red, int lane, int gt) {
+  for (int off = (gt < 32 ? gt : 32) >> 1; off > 0; off >>= 1) {
+    df o = {__shfl_xor_sync(0xffffffffu, s.hi, off), __shfl_xor_sync(0xffffffffu, s.lo, off)};
+    s = df_add(s, o);
+  }
+  if (gt > 32) {
+    __syncthreads();
+    if ((lane & 31) == 0) red[lane >> 5] = make_float2(s.hi, s.lo);
+    __syncthreads();
+    if (lane == 0) {
+      df t = {0.f, 0.f};
+      for (int w = 0; w < gt / 32; w++) t = df_add(t, df{red[w].x, red[w].y});
+      s = t;
+    }
+  }
+  return s;
+}
+__device__ __forceinline__ float4 group_sum4_rt(float4 v, float *red, int lane, int gt) {
+  for (int off = (gt < 32 ? gt : 32) >> 1; off > 0; off >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+    v.z += __shfl_xor_sync(0xffffffffu, v.z, off);
+    v.w += __shfl_xor_sync(0xffffffffu, v.w, off);
+  }
+  if (gt > 32) {
+    __syncthreads();
+    if ((lane & 31) == 0) {
+      float *o = red + 4 * (lane >> 5);
+      o[0] = v.x;
+      o[1] = v.y;
+      o[2] = v.z;
+      o[3] = v.w;
+    }
+    __syncthreads();
+    if (lane == 0) {
+      v = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int w = 0; w < gt / 32; w++) {
+        v.x += red[4 * w];
+        v.y += red[4 * w + 1];
+        v.z += red[4 * w + 2];
+        v.w += red[4 * w + 3];
+      }
+    }
+  }
+  return v;
+}
+
+// The mixed branch of spec_unit for N = 2^ln (32 <= N <= 1024): 1024/N
+// proposals of the unit, one group of N/4 threads each, in a 256-thread CTA.
+template <bool PERCH>
+__device__ __forceinline__ void spec_unit_mix_rt(const SpecArgs &a, const int *bin_list, int count, int base, int ln,
+                                                 const float2 *series, const float4 *tw, float2 *bufs,
+                                                 double *reds) {
+  const int N = 1 << ln, GT = N >> 2, SN = pad16(N);
+  constexpr int B = 4;  // bins per thread
+  const int g = threadIdx.x >> (ln - 2), lane = threadIdx.x & (GT - 1);
+  float2 *buf = bufs + (size_t)g * 4 * SN;
+  double *red = reds + 96 * g;
+  const int NFFT = a.NFFT;
+  const int slot = base + g;
+  const bool valid = slot < count;
+  const int sl = valid ? slot : count - 1;
+  // checked build: as in spec_unit
+  const bool lok = chk(sl >= 0 && sl < a.cap, kChkBinList);
+  const int item = lok ? bin_list[sl] : 0;
+  const bool iok = chk(item >= 0 && item < a.nitems, kChkItem);
+  int seg = 0, imin = 0;
+  if (iok) {
+    seg = a.itemsmix[item].seg;
+    imin = a.itemsmix[item].imin;
+  }
+  const bool sok = chk(seg >= 0 && seg < a.nseg, kChkBankRead);
+  const bool rok = chk((long long)(sl + 1) * 4 * N <= a.series_len, kChkSeriesRead);
+  const bool inb = lok && iok && sok && rok;
+  if (!inb) seg = 0;
+  const float2 *src = series + (inb ? (size_t)sl * 4 * N : 0);
+  const bool est_on = a.hp_list != nullptr;
+  const bool clipped = imin < 0 || imin + N > NFFT;
+  float rS = 0.f, rE = 0.f, eS = 0.f, eE = 0.f, fh = 0.f;
+  float4 ev = make_float4(0.f, 0.f, 0.f, 0.f);
+  fft4_reg_rt(src, buf, tw, lane, ln);
+#pragma unroll
+  for (int r = 0; r < B; ++r) {
+    const int k = lane + GT * r;
+    const int m = (k + N / 2) & (N - 1);  // fftshift: output bin m holds FFT index m + N/2
+    const int j = imin + m;
+    const int kp = pad16(k);
+    const float2 b0 = buf[0 * SN + kp], b1 = buf[1 * SN + kp], b2 = buf[2 * SN + kp], b3 = buf[3 * SN + kp];
+    const bool inside = j >= 0 && j < NFFT;
+    if (est_on && clipped) {
+      const float pw = fmaf(b0.x, b0.x, fmaf(b0.y, b0.y, fmaf(b1.x, b1.x, fmaf(b1.y, b1.y,
+                       fmaf(b2.x, b2.x, fmaf(b2.y, b2.y, fmaf(b3.x, b3.x, b3.y * b3.y)))))));
+      ev.w += pw;
+      if (inside) ev.z += pw;
+    }
+    if (!inside) continue;
+    const size_t sj = (size_t)seg * NFFT + j;
+    const float4 w = a.w32[sj], wl = a.w32lo[sj];
+    const float4 gA = a.g32[2 * sj], gE = a.g32[2 * sj + 1];
+    const float4 gAl = a.g32lo[2 * sj], gEl = a.g32lo[2 * sj + 1];
+    const float p2 = a.itemsmix[item].amp_p2;
+    const float2 HA = cfma(b0, make_float2(gA.x, gA.y),
+                           cfma(b1, make_float2(gA.z, gA.w),
+                                cfma(b0, make_float2(gAl.x, gAl.y), cmul(b1, make_float2(gAl.z, gAl.w)))));
+    const float2 HE = cfma(b2, make_float2(gE.x, gE.y),
+                           cfma(b3, make_float2(gE.z, gE.w),
+                                cfma(b2, make_float2(gEl.x, gEl.y), cmul(b3, make_float2(gEl.z, gEl.w)))));
+    const float2 hA = cscale(HA, p2), hE = cscale(HE, p2);
+    acc_resid_sq(w.x, wl.x, hA.x, rS, eS);
+    acc_resid_sq(w.y, wl.y, hA.y, rS, eS);
+    acc_resid_sq(w.z, wl.z, hE.x, rE, eE);
+    acc_resid_sq(w.w, wl.w, hE.y, rE, eE);
+    fh += fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y);
+    if (est_on) {
+      const float dAx = w.x - hA.x, dAy = w.y - hA.y, dEx = w.z - hE.x, dEy = w.w - hE.y;
+      ev.x += fmaf(hA.x, dAx, fmaf(hA.y, dAy, fmaf(hE.x, dEx, hE.y * dEy)));
+      ev.y += fmaf(hA.x, dAy, fmaf(-hA.y, dAx, fmaf(hE.x, dEy, -hE.y * dEx)));
+    }
+  }
+  group_sync_rt(GT);
+  df sa, sh, saE;
+  float2 *redf = reinterpret_cast<float2 *>(red);
+  if constexpr (PERCH) {
+    sa = group_sum_df_rt(quick_two_sum(rS, eS), redf, lane, GT);
+    saE = group_sum_df_rt(quick_two_sum(rE, eE), redf + 64, lane, GT);
+  } else {
+    sa = group_sum_df_rt(df_add(quick_two_sum(rS, eS), quick_two_sum(rE, eE)), redf, lane, GT);
+  }
+  sh = group_sum_df_rt(df{fh, 0.f}, redf + 32, lane, GT);
+  if (est_on) ev = group_sum4_rt(ev, reinterpret_cast<float *>(red), lane, GT);
+  if (valid && inb && lane == 0) {
+    double term, hh;
+    // FP64 only for the final sum, once per proposal
+    int jlo = imin < 0 ? 0 : imin;
+    int jhi = imin + N > NFFT ? NFFT : imin + N;
+    const double *Qs = a.Q + (size_t)seg * (NFFT + 1);
+    float rr;  // |r - h|^2 over the support, both channels
+    if constexpr (PERCH) {
+      const double *QAs = a.QA + (size_t)seg * (NFFT + 1);
+      const double qa = QAs[jhi] - QAs[jlo];
+      const double tA = (qa - (double)sa.hi) - (double)sa.lo;
+      const double tE = (((Qs[jhi] - Qs[jlo]) - qa) - (double)saE.hi) - (double)saE.lo;
+      a.term_ch[2 * (size_t)item] = tA;
+      a.term_ch[2 * (size_t)item + 1] = tE;
+      term = tA + tE;
+      rr = sa.hi + saE.hi;
+    } else {
+      term = ((Qs[jhi] - Qs[jlo]) - (double)sa.hi) - (double)sa.lo;
+      rr = sa.hi;
+    }
+    const float hw = sh.hi + sh.lo;
+    hh = 2.0 * (double)hw;
+    if (a.hp_list) {
+      // the error estimate of spec_unit
+      const float hf = clipped && ev.z > 0.f ? hw * (ev.w / ev.z) : hw;
+      const float he = sqrtf(fmaf(ev.x, ev.x, ev.y * ev.y));
+      const float est = fmaf(a.fb_e1, sqrtf(hf * rr * (1.f / (float)N)), a.fb_e2 * he) *
+                        fb_scale_of(a.fb_inv_scale, a.fb_nscale, item);
+      if (!(est <= 1.f)) {  // also a non-finite estimate
+        atomicAdd(a.fb_total, 1ull);
+        atomicAdd(a.fb_count, 1);
+        const int bin = ln - 5;
+        const int k = atomicAdd(&a.hp_count[bin], 1);
+        if (chk(k < a.cap, kChkReevalList)) a.hp_list[(size_t)bin * a.cap + k] = item;
+      }
+    }
+    const double tx = a.term_x ? a.term_x[item] : 0.0;
+    a.dlogl[item] = term - tx;
+    if (a.term_y) a.term_y[item] = term;
+    if (a.hh) a.hh[item] = hh;
+    if (a.status) a.status[item] = isfinite(term) ? 0 : 1;
+  }
+  if (GT > 32) __syncthreads();
+}
+
 // All sizes up to 1024 in one launch: a persistent grid of 256-thread CTAs
 // walks the units (GPC = 1024/N proposals of one size each), largest sizes
 // first so that the long units start early; a CTA reloads the twiddles when
@@ -1572,6 +1826,10 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
     const int count = a.bin_count[b];
     const int *bl = a.bin_list + (size_t)b * a.cap;
     const C *series = reinterpret_cast<const C *>(a.series) + bin_sample_start(a.bin_count, a.NFFT, b) * 4;
+    if constexpr (MIX) {
+      spec_unit_mix_rt<PERCH>(a, bl, count, base, b + 5, series, tw, bufs, reds);
+      continue;
+    }
     switch (b) {
       case 0: spec_unit<32, MIX, 32, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
       case 1: spec_unit<64, MIX, 16, PERCH>(a, bl, count, base, series, tw, bufs, reds); break;
