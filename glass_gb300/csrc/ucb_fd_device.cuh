@@ -1794,18 +1794,24 @@ __global__ void __launch_bounds__(kSpecAllThreads, 4) fd_spec_all_kernel(SpecAll
   TW *tw = reinterpret_cast<TW *>(smem_raw);
   C *bufs = reinterpret_cast<C *>(tw + SN);
   double *reds = reinterpret_cast<double *>(bufs + 4 * SN);
-  int ustart[kSpecAllBins + 1];  // in largest-first order
-  int total = 0;
+  // unit ranges per size, largest first; in shared memory so that they hold
+  // no registers while a unit runs
+  __shared__ int ustart[kSpecAllBins + 1];
+  if (threadIdx.x == 0) {
+    int total = 0;
 #pragma unroll
-  for (int q = 0; q < kSpecAllBins; q++) {
-    const int b = kSpecAllBins - 1 - q;
-    ustart[q] = total;
-    if (b < A.nbins) {
-      const int gpc = 32 >> b;
-      total += (a.bin_count[b] + gpc - 1) / gpc;
+    for (int q = 0; q < kSpecAllBins; q++) {
+      const int b = kSpecAllBins - 1 - q;
+      ustart[q] = total;
+      if (b < A.nbins) {
+        const int gpc = 32 >> b;
+        total += (a.bin_count[b] + gpc - 1) / gpc;
+      }
     }
+    ustart[kSpecAllBins] = total;
   }
-  ustart[kSpecAllBins] = total;
+  __syncthreads();
+  const int total = ustart[kSpecAllBins];
   int cur = -1;
   for (int unit = blockIdx.x; unit < total; unit += gridDim.x) {
     int q = 0;
